@@ -1,0 +1,313 @@
+#!/usr/bin/env python
+"""Benchmark: batched Dirichlet/Neumann Poisson solves at 1e-8 relative
+Schur residual on one GB300 (metric of the batched configuration: 256
+independent problems, grids of 128..512 dual nodes per side, 1-3 bodies each).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Our arm: a step is one ilm_batch_solve of the whole batch (256 solves) with
+the geometry set up and the inputs resident in HBM; the L2 is flushed between
+steps and each step is timed with CUDA events on the solve stream.  `e2e`
+times the public API from host buffers every step: ilm_batch_create (DDF
+windows, tile lists, Schur complements) + host->device copy of the surface
+data from pinned memory + solve + device->host copy of all fields and surface
+strengths.  Reference arm: the reference's CPU algorithm (N_p-column Schur
+build + dense LU), restated in the oracle, on all host cores, on a bounded
+sample of the same batch.
+
+Multi-GPU (torchrun): independent replicas, one batch per rank (weak scaling).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "immersedlayers.jl_gb300"))
+
+METRIC = "Poisson solves/s at 1e-8 rel. residual (batched Dirichlet/Neumann, plain CG)"
+UNIT = "solves/s"
+NPROB = 256
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--nprob", type=int, default=NPROB)
+    ap.add_argument("--tol", type=float, default=1e-8)
+    ap.add_argument("--cpu-sample-cols", type=int, default=32)
+    return ap.parse_args()
+
+
+def dist_init():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl"
+        dist.init_process_group(backend=backend)
+        return rank, world, dist
+    return rank, world, None
+
+
+def config(args, world):
+    return {"workload": f"batched Poisson: {args.nprob} independent problems (even: Dirichlet, odd: Neumann), "
+                        "n~U{128,192,256,384,512}^2 dual nodes, h=4/n, 1-3 circles/ellipses at ds=1.4h, "
+                        "8-mode arc-length Fourier surface data, seeds 3+i",
+            "nprob_per_gpu": args.nprob, "tol": args.tol, "precision": "FP32 grid work, FP64 Schur build + CG",
+            "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{world}"}
+
+
+def clocks_sampler():
+    try:
+        p = subprocess.Popen(["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,"
+                              "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+                              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                              "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "200"],
+                             stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        return p
+    except Exception:
+        return None
+
+
+def clocks_summary(p, dev_index=0):
+    if p is None:
+        return None
+    p.terminate()
+    try:
+        out, _ = p.communicate(timeout=5)
+    except Exception:
+        return None
+    sm, mx, reasons = [], [], set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    for line in out.strip().splitlines():
+        f = [x.strip() for x in line.split(",")]
+        if len(f) < 9 or f[0] != str(dev_index):
+            continue
+        try:
+            sm.append(float(f[1]))
+            mx.append(float(f[2]))
+        except ValueError:
+            continue
+        for n, v in zip(names, f[5:9]):
+            if v.lower() == "active":
+                reasons.add(n)
+    if not sm:
+        return None
+    return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import cpu_reference as R
+    from immersedlayers import workloads as W
+    specs = W.batch_specs(args.nprob)
+    for _ in range(max(0, args.warmup)):
+        pass  # the reference CPU path has no warm-up state worth timing
+    vals = []
+    t_all = time.perf_counter()
+    last = None
+    for _ in range(args.steps):
+        last = R.estimate_batch_time(specs, per_size=2, k_cols=args.cpu_sample_cols)
+        vals.append(args.nprob / last["batch_seconds"])
+    wall = time.perf_counter() - t_all
+    v = statistics.median(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * wall / max(args.steps, 1), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config(args, 1),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": last["cores"], "kind": "port",
+                             "sample": f"two problems per grid size (indices {last['sample']}), {last['k_cols']} "
+                                       "Schur columns timed per problem and scaled by npts/k; LU and grid solves "
+                                       "timed in full; batch time = sum over all problems by size class"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world, dist):
+    import numpy as np
+    import torch
+    import __graft_entry__ as ge
+    ge.build()
+    from immersedlayers import workloads as W
+    from immersedlayers.batch import STAGES, BatchSolver
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.Stream()
+    specs = W.batch_specs(args.nprob) if rank == 0 else \
+        [s for s in _rank_specs(args.nprob, rank)]
+    dt = torch.float32
+    t0 = time.perf_counter()
+    bs = BatchSolver(specs, dtype=dt)
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    fp, fm = bs.surface_data()
+    f_out = torch.empty(bs.total_cells, dtype=dt, device="cuda")
+    s_out = torch.empty(bs.total_points, dtype=dt, device="cuda")
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            bs.solve(fp, fm, f_out, s_out, tol=args.tol, stream=stream)
+    stream.synchronize()
+    its, rr = bs.info()
+    assert (rr <= args.tol).all(), f"not converged: max rel residual {rr.max()}"
+    # timed region
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clk = clocks_sampler()
+    times = []
+    with torch.cuda.stream(stream):
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            bs.solve(fp, fm, f_out, s_out, tol=args.tol, stream=stream)
+            e1.record(stream)
+            times.append((e0, e1))
+    stream.synchronize()
+    torch.cuda.synchronize()
+    ms = [a.elapsed_time(b) for a, b in times]
+    total_ms = sum(ms)
+    if dist:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+        dist.barrier()
+    clocks = clocks_summary(clk, dev)
+    value = world * args.nprob * args.steps / (total_ms / 1000.0)
+
+    # stage profile of one solve (separate, not part of the timed region)
+    bs.set_profiling(True)
+    flush.fill_(1.0)
+    with torch.cuda.stream(stream):
+        bs.solve(fp, fm, f_out, s_out, tol=args.tol, stream=stream)
+    stream.synchronize()
+    stage_ms, launches = bs.stage_times()
+    bs.set_profiling(False)
+    st = bs.stats()
+    its, rr = bs.info()
+
+    # roofline of the dominant stage
+    hbm, peak_kind = peaks()
+    names = STAGES[:len(stage_ms)]
+    dom = int(np.argmax(stage_ms))
+    alg = _algorithmic_bytes(names[dom], st, its)
+    achieved = alg / (stage_ms[dom] / 1000.0) / 1e9
+    roofline = {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "peak_kind": peak_kind, "traffic": None,
+                "algorithmic_bytes": alg, "launch_ms": stage_ms[dom]}
+
+    # end to end through the public API from host buffers
+    e2e = _e2e(args, specs, stream, dt)
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+                "config": config(args, world), "roofline": roofline, "e2e": e2e, "gpu_launches": launches * args.steps,
+                "clocks": clocks, "setup_s": setup_s,
+                "stages_ms": dict(zip(names, [round(x, 4) for x in stage_ms])),
+                "cg_iterations": {"mean": float(np.mean(its)), "max": int(its.max())},
+                "max_rel_residual": float(rr.max())}
+        if world == 1:
+            line["cpu_baseline"] = _cpu_baseline(args, specs)
+        print(json.dumps(line), flush=True)
+
+
+def _rank_specs(nprob, rank):
+    from immersedlayers import workloads as W
+    from immersedlayers.batch import BatchProblemSpec
+    out = []
+    for i in range(nprob):
+        n, h, bl, kind, f = W.batch_problem(i + nprob * rank)
+        out.append(BatchProblemSpec(n, h, bl, kind, f))
+    return out
+
+
+def _algorithmic_bytes(stage, st, its):
+    """Algorithmic HBM bytes of one launch of a stage (FP32 grid data)."""
+    P, C, S2, FFT = st["points"], st["cells"], st["sum_npts2"], st["sum_fft"]
+    if "FFT" in stage:
+        # read the n1 x n2 field, write it back, read the half spectrum (P1/2+1)(P2/2+1)
+        return 4 * C + 4 * C + 4 * FFT / 4
+    if "CG" in stage:
+        # every iteration streams the FP64 Schur matrix once
+        return 8 * S2 * float(its.mean())
+    if "scatter" in stage:
+        return 4 * C + 16 * P
+    return 8 * C
+
+
+def _e2e(args, specs, stream, dt):
+    import torch
+    from immersedlayers.batch import BatchSolver
+    import numpy as np
+    fp_h = torch.tensor(np.concatenate([s.fplus for s in specs]), dtype=dt).pin_memory()
+    fm_h = torch.tensor(np.concatenate([s.fminus for s in specs]), dtype=dt).pin_memory()
+    steps = max(1, min(args.steps, 3))
+    times = []
+    h2d = d2h = 0
+    for _ in range(steps + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        bs = BatchSolver(specs, dtype=dt)
+        with torch.cuda.stream(stream):
+            fp = fp_h.to("cuda", non_blocking=True)
+            fm = fm_h.to("cuda", non_blocking=True)
+            f, s = bs.solve(fp, fm, tol=args.tol, stream=stream)
+            f_h = torch.empty(f.numel(), dtype=dt).pin_memory()
+            s_h = torch.empty(s.numel(), dtype=dt).pin_memory()
+            f_h.copy_(f, non_blocking=True)
+            s_h.copy_(s, non_blocking=True)
+        stream.synchronize()
+        times.append(time.perf_counter() - t0)
+        h2d = fp.numel() * fp.element_size() * 2
+        d2h = (f.numel() + s.numel()) * f.element_size()
+        del bs
+    t = statistics.median(times[1:])
+    return {"value": len(specs) / t, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+            "includes": "batch set-up from host points (DDF windows, tile lists, FP64 Schur build) + H2D + solve "
+                        "+ D2H of all fields", "ms_per_step": 1000 * t}
+
+
+def _cpu_baseline(args, specs):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import cpu_reference as R
+    est = R.estimate_batch_time(specs, per_size=2, k_cols=args.cpu_sample_cols)
+    return {"value": len(specs) / est["batch_seconds"], "unit": UNIT, "cores": est["cores"], "kind": "port",
+            "sample": f"two problems per grid size (indices {est['sample']}), {est['k_cols']} Schur columns per "
+                      f"problem scaled by npts/k, solve timed in full; sample wall {est['sample_wall']:.1f}s"}
+
+
+def main():
+    args = parse()
+    rank, world, dist = dist_init()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, dist)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

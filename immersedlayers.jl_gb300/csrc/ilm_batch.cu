@@ -1,0 +1,722 @@
+// Batched Poisson solves: hundreds of independent Dirichlet / Neumann problems
+// of different grid sizes and geometries advanced together in a fixed
+// sequence of launches (one launch per stage for the whole batch).
+//
+// Per problem this is the reference's block-LU solve (Dirichlet:
+// test/literate/problems.jl:259-298; Neumann: test/literate/neumann.jl:101-127)
+// with its dense LU `S \ s` replaced by device CG on the LGF-assembled Schur
+// complement.  All per-problem descriptors ("tasks") are built on the host
+// once, at batch creation, and live in device memory, so a solve issues no
+// host<->device traffic and can be captured in a CUDA graph.
+#include <string.h>
+
+#include <math.h>
+
+#include <algorithm>
+#include <memory>
+#include <new>
+
+#include "ilm_internal.cuh"
+
+namespace ilm {
+
+struct BScatterTask {
+  int n1, n2, ntx, tile0;
+  const int* tptr;
+  const int* tpts;
+  const int* bx;
+  const int* by;
+  const void* wx;
+  const void* wy;
+  const void* wsc;
+  const void* nx;
+  const void* ny;
+  const void* in;
+  int coef;
+  void* out;
+};
+
+struct BStencilTask {
+  int NX, NY, blk0;
+  const void* in;
+  void* out;
+  double scale;
+};
+
+struct BGatherTask {
+  int npts, pt0, nterms, pad;
+  const int* bx[2];
+  const int* by[2];
+  const void* wx[2];
+  const void* wy[2];
+  const void* nx;
+  const void* ny;
+  const void* arr[2];
+  int n1[2], n2[2], xs[2], ys[2], coef[2];
+  void* out;
+  double scale;
+};
+
+constexpr int SB_X = 32, SB_Y = 8;
+
+template <typename Task>
+__device__ __forceinline__ int find_task(const Task* t, int n, int u, int Task::*field) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (t[mid].*field <= u) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+template <typename T>
+__device__ __forceinline__ T bcoef(int code, const T* nx, const T* ny, int k) {
+  switch (code) {
+    case CF_ONE: return (T)1;
+    case CF_NX: return nx[k];
+    case CF_NY: return ny[k];
+    case CF_MNX: return -nx[k];
+    case CF_MNY: return -ny[k];
+    case CF_MONE: return (T)-1;
+  }
+  return (T)0;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(SB_X* SB_Y) k_bscatter(const BScatterTask* __restrict__ tasks, int ntasks) {
+  const int ti = find_task(tasks, ntasks, (int)blockIdx.x, &BScatterTask::tile0);
+  const BScatterTask& S = tasks[ti];
+  const int t = blockIdx.x - S.tile0;
+  const int tx = t % S.ntx, ty = t / S.ntx;
+  const int i = tx * SB_X + threadIdx.x;
+  const int j = ty * SB_Y + threadIdx.y;
+  const int p0 = S.tptr[t], p1 = S.tptr[t + 1];
+  const T* __restrict__ wx = static_cast<const T*>(S.wx);
+  const T* __restrict__ wy = static_cast<const T*>(S.wy);
+  const T* __restrict__ wsc = static_cast<const T*>(S.wsc);
+  const T* __restrict__ in = static_cast<const T*>(S.in);
+  const T* nx = static_cast<const T*>(S.nx);
+  const T* ny = static_cast<const T*>(S.ny);
+  T acc = (T)0;
+  for (int p = p0; p < p1; ++p) {
+    const int k = S.tpts[p];
+    const int di = i - S.bx[k];
+    const int dj = j - S.by[k];
+    if ((unsigned)di < (unsigned)NTAP && (unsigned)dj < (unsigned)NTAP)
+      acc += wsc[k] * (bcoef<T>(S.coef, nx, ny, k) * in[k]) * wx[k * NTAP + di] * wy[k * NTAP + dj];
+  }
+  if (i < S.n1 && j < S.n2) static_cast<T*>(S.out)[(size_t)j * S.n1 + i] = acc;
+}
+
+// Edges{Primal} -> Nodes{Primal} divergence
+template <typename T>
+__global__ void k_bdiv(const BStencilTask* __restrict__ tasks, int ntasks) {
+  const int ti = find_task(tasks, ntasks, (int)blockIdx.x, &BStencilTask::blk0);
+  const BStencilTask& S = tasks[ti];
+  const int NX = S.NX, NY = S.NY;
+  const int nbx = (NX - 1 + SB_X - 1) / SB_X;
+  const int b = blockIdx.x - S.blk0;
+  const int i = (b % nbx) * SB_X + threadIdx.x, j = (b / nbx) * SB_Y + threadIdx.y;
+  if (i >= NX - 1 || j >= NY - 1) return;
+  const T* u = static_cast<const T*>(S.in);
+  const T* v = u + (size_t)NX * (NY - 1);
+  const T du = u[(size_t)j * NX + i + 1] - u[(size_t)j * NX + i];
+  const T dv = v[(size_t)(j + 1) * (NX - 1) + i] - v[(size_t)j * (NX - 1) + i];
+  static_cast<T*>(S.out)[(size_t)j * (NX - 1) + i] = (du + dv) * (T)S.scale;
+}
+
+// Nodes{Primal} -> Edges{Primal} gradient (block tiles over the NX x NY box)
+template <typename T>
+__global__ void k_bgrad(const BStencilTask* __restrict__ tasks, int ntasks) {
+  const int ti = find_task(tasks, ntasks, (int)blockIdx.x, &BStencilTask::blk0);
+  const BStencilTask& S = tasks[ti];
+  const int NX = S.NX, NY = S.NY;
+  const int nbx = (NX + SB_X - 1) / SB_X;
+  const int b = blockIdx.x - S.blk0;
+  const int i = (b % nbx) * SB_X + threadIdx.x, j = (b / nbx) * SB_Y + threadIdx.y;
+  const T* w = static_cast<const T*>(S.in);
+  T* u = static_cast<T*>(S.out);
+  T* v = u + (size_t)NX * (NY - 1);
+  const T sc = (T)S.scale;
+  if (i < NX && j < NY - 1) {
+    T r = (T)0;
+    if (i >= 1 && i <= NX - 2) r = (w[(size_t)j * (NX - 1) + i] - w[(size_t)j * (NX - 1) + i - 1]) * sc;
+    u[(size_t)j * NX + i] = r;
+  }
+  if (i < NX - 1 && j < NY) {
+    T r = (T)0;
+    if (j >= 1 && j <= NY - 2) r = (w[(size_t)j * (NX - 1) + i] - w[(size_t)(j - 1) * (NX - 1) + i]) * sc;
+    v[(size_t)j * (NX - 1) + i] = r;
+  }
+}
+
+template <typename T>
+__global__ void k_bgather(const BGatherTask* __restrict__ tasks, int ntasks, int Ptot) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= Ptot) return;
+  const int ti = find_task(tasks, ntasks, g, &BGatherTask::pt0);
+  const BGatherTask& G = tasks[ti];
+  const int k = g - G.pt0;
+  if (k >= G.npts) return;
+  T total = (T)0;
+  for (int q = 0; q < G.nterms; ++q) {
+    const int xs = G.xs[q], ys = G.ys[q];
+    const int b0 = G.bx[xs][k], e0 = G.by[ys][k];
+    const T* wx = static_cast<const T*>(G.wx[xs]) + k * NTAP;
+    const T* wy = static_cast<const T*>(G.wy[ys]) + k * NTAP;
+    const T* a = static_cast<const T*>(G.arr[q]);
+    const int n1 = G.n1[q], n2 = G.n2[q];
+    T acc = (T)0;
+#pragma unroll
+    for (int jj = 0; jj < NTAP; ++jj) {
+      const int j = e0 + jj;
+      if ((unsigned)j >= (unsigned)n2) continue;
+      T racc = (T)0;
+#pragma unroll
+      for (int ii = 0; ii < NTAP; ++ii) {
+        const int i = b0 + ii;
+        if ((unsigned)i >= (unsigned)n1) continue;
+        racc += wx[ii] * a[(size_t)j * n1 + i];
+      }
+      acc += wy[jj] * racc;
+    }
+    total += bcoef<T>(G.coef[q], static_cast<const T*>(G.nx), static_cast<const T*>(G.ny), k) * acc;
+  }
+  static_cast<T*>(G.out)[k] = total * (T)G.scale;
+}
+
+// rhs64 = (double)g - (double)avg
+template <typename T>
+__global__ void k_rhs64(int n, const T* __restrict__ g, const T* __restrict__ avg, double* __restrict__ out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    out[i] = (double)g[i] - (double)avg[i];
+}
+
+template <typename T>
+__global__ void k_jump_avg(int n, const T* __restrict__ p, const T* __restrict__ m, T* __restrict__ jump,
+                           T* __restrict__ avg) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    jump[i] = p[i] - m[i];
+    avg[i] = (T)0.5 * (p[i] + m[i]);
+  }
+}
+
+}  // namespace ilm
+
+using namespace ilm;
+
+struct ilm_batch_s {
+  int nprob = 0, dtype = ILM_F64, ddf = ILM_DDF_YANG3, Ptot = 0, maxN = 0, max_grid = 0;
+  std::vector<ilm_batch_problem_t> probs;
+  std::vector<size_t> foff, poff, soff;   // nprob + 1 offsets (fields, points, Schur)
+  size_t ftot = 0, etot = 0, stot = 0;
+  // packed point data
+  DevBuf bx[2], by[2], wx[2], wy[2], wx64[2], wy64[2];
+  DevBuf nx, ny, wsc, nx64, ny64, ds64, pt2prob;
+  DevBuf tptr[4], tpts[4];
+  // work
+  DevBuf fstar, corr, edges, convwork, S, F;
+  DevBuf jump, avg, g, s, rhs64, x64;
+  DevBuf cgp, iters, relres;
+  // tasks
+  DevBuf scatA, divA, gradA, gathA, scatB, divB, convA, convB, schurP;
+  int n_scatA = 0, n_divA = 0, n_gradA = 0, n_gathA = 0, n_scatB = 0, n_divB = 0;
+  int blk_scatA = 0, blk_divA = 0, blk_gradA = 0, blk_scatB = 0, blk_divB = 0;
+  int n_conv = 0;
+  ConvLaunch convL;
+  int schur_tiles = 0;
+  double cg_tol = -1.0;
+  int cg_maxiter = -1;
+  // optional stage timing (CUDA events on the solve stream)
+  int profiling = 0;
+  cudaEvent_t ev[32] = {};
+  int nev = 0, launches = 0;
+  ~ilm_batch_s() {
+    for (auto& e : ev)
+      if (e) cudaEventDestroy(e);
+  }
+};
+
+namespace {
+
+size_t es(int dtype) { return dtype == ILM_F64 ? 8 : 4; }
+
+template <typename V>
+int up(DevBuf& b, const std::vector<V>& v) {
+  ILM_TRY(b.alloc(std::max<size_t>(v.size(), 1) * sizeof(V)));
+  if (!v.empty()) ILM_CHECK_CUDA(cudaMemcpy(b.p, v.data(), v.size() * sizeof(V), cudaMemcpyHostToDevice));
+  return ILM_OK;
+}
+
+int up_typed(DevBuf& b, const std::vector<double>& v, int dtype) {
+  if (dtype == ILM_F64) return up(b, v);
+  std::vector<float> f(v.begin(), v.end());
+  return up(b, f);
+}
+
+#define BDISPATCH(dtype, ...)  \
+  do {                         \
+    if ((dtype) == ILM_F64) {  \
+      using T = double;        \
+      __VA_ARGS__;             \
+    } else {                   \
+      using T = float;         \
+      __VA_ARGS__;             \
+    }                          \
+  } while (0)
+
+}  // namespace
+
+extern "C" {
+
+int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* x, const double* y,
+                     const double* nrmx, const double* nrmy, const double* ds, int ddf, int dtype, ilm_batch_t* out) {
+  ILM_REQUIRE(out && probs && nprob > 0, "batch: bad arguments");
+  ILM_REQUIRE(dtype == ILM_F64 || dtype == ILM_F32, "batch: bad dtype %d", dtype);
+  ILM_REQUIRE(ddf >= ILM_DDF_YANG3 && ddf <= ILM_DDF_M3, "batch: bad ddf %d", ddf);
+  auto* B = new (std::nothrow) ilm_batch_s();
+  if (!B) return ILM_ERR_NO_MEMORY;
+  std::unique_ptr<ilm_batch_s> guard(B);
+  B->nprob = nprob;
+  B->dtype = dtype;
+  B->ddf = ddf;
+  B->probs.assign(probs, probs + nprob);
+  B->foff.assign(nprob + 1, 0);
+  B->poff.assign(nprob + 1, 0);
+  B->soff.assign(nprob + 1, 0);
+  std::vector<size_t> eoff(nprob + 1, 0);
+  for (int p = 0; p < nprob; ++p) {
+    const ilm_batch_problem_t& P = probs[p];
+    ILM_REQUIRE(P.nx >= 8 && P.ny >= 8 && P.nx <= 8192 && P.ny <= 8192 && P.h > 0, "batch: bad grid of problem %d", p);
+    ILM_REQUIRE(P.npts >= 1, "batch: problem %d has no points", p);
+    ILM_REQUIRE(P.kind == 0 || P.kind == 1, "batch: bad kind of problem %d", p);
+    B->foff[p + 1] = B->foff[p] + (size_t)(P.nx - 1) * (P.ny - 1);
+    eoff[p + 1] = eoff[p] + (size_t)P.nx * (P.ny - 1) + (size_t)(P.nx - 1) * P.ny;
+    B->poff[p + 1] = B->poff[p] + P.npts;
+    B->soff[p + 1] = B->soff[p] + (size_t)P.npts * P.npts;
+    B->maxN = std::max(B->maxN, P.npts);
+    B->max_grid = std::max(B->max_grid, std::max(P.nx, P.ny));
+  }
+  const int Ptot = (int)B->poff[nprob];
+  B->Ptot = Ptot;
+  B->ftot = B->foff[nprob];
+  B->etot = eoff[nprob];
+  B->stot = B->soff[nprob];
+  for (int k = 0; k < Ptot; ++k)
+    ILM_REQUIRE(isfinite(x[k]) && isfinite(y[k]) && isfinite(nrmx[k]) && isfinite(nrmy[k]) && isfinite(ds[k]),
+                "batch: non-finite point data at %d", k);
+
+  // ---- host set-up: DDF windows and tile lists, packed -------------------
+  std::vector<int> hbx[2], hby[2], hp2p(Ptot);
+  std::vector<double> hwx[2], hwy[2], hwsc(Ptot);
+  std::vector<int> htp[4], hts[4];
+  std::vector<size_t> tpo[4], tso[4];  // per problem offsets into packed tile arrays
+  for (int c = 0; c < 4; ++c) {
+    tpo[c].assign(nprob, 0);
+    tso[c].assign(nprob, 0);
+  }
+  std::vector<HostWindows> Wall(nprob);
+  for (int p = 0; p < nprob; ++p) {
+    const ilm_batch_problem_t& P = probs[p];
+    ilm_grid_s g{P.nx, P.ny, P.h, P.i0x, P.i0y};
+    const size_t o = B->poff[p];
+    host_windows(g, ddf, P.npts, x + o, y + o, &Wall[p]);
+    HostWindows& W = Wall[p];
+    for (int d = 0; d < 2; ++d) {
+      hbx[d].insert(hbx[d].end(), W.bx[d].begin(), W.bx[d].end());
+      hby[d].insert(hby[d].end(), W.by[d].begin(), W.by[d].end());
+      hwx[d].insert(hwx[d].end(), W.wx[d].begin(), W.wx[d].end());
+      hwy[d].insert(hwy[d].end(), W.wy[d].begin(), W.wy[d].end());
+    }
+    for (int k = 0; k < P.npts; ++k) {
+      hp2p[o + k] = p;
+      hwsc[o + k] = ds[o + k] / (P.h * P.h);
+    }
+    for (int c = 0; c < 4; ++c) {
+      tpo[c][p] = htp[c].size();
+      tso[c][p] = hts[c].size();
+      htp[c].insert(htp[c].end(), W.tptr[c].begin(), W.tptr[c].end());
+      hts[c].insert(hts[c].end(), W.tpts[c].begin(), W.tpts[c].end());
+    }
+  }
+  std::vector<double> hnx(nrmx, nrmx + Ptot), hny(nrmy, nrmy + Ptot), hds(ds, ds + Ptot);
+  for (int d = 0; d < 2; ++d) {
+    ILM_TRY(up(B->bx[d], hbx[d]));
+    ILM_TRY(up(B->by[d], hby[d]));
+    ILM_TRY(up_typed(B->wx[d], hwx[d], dtype));
+    ILM_TRY(up_typed(B->wy[d], hwy[d], dtype));
+    ILM_TRY(up_typed(B->wx64[d], hwx[d], ILM_F64));
+    ILM_TRY(up_typed(B->wy64[d], hwy[d], ILM_F64));
+  }
+  ILM_TRY(up_typed(B->nx, hnx, dtype));
+  ILM_TRY(up_typed(B->ny, hny, dtype));
+  ILM_TRY(up_typed(B->wsc, hwsc, dtype));
+  ILM_TRY(up(B->nx64, hnx));
+  ILM_TRY(up(B->ny64, hny));
+  ILM_TRY(up(B->ds64, hds));
+  ILM_TRY(up(B->pt2prob, hp2p));
+  for (int c = 0; c < 4; ++c) {
+    ILM_TRY(up(B->tptr[c], htp[c]));
+    ILM_TRY(up(B->tpts[c], hts[c]));
+  }
+
+  // ---- device work buffers ----------------------------------------------
+  const size_t e = es(dtype);
+  ILM_TRY(B->fstar.alloc(B->ftot * e));
+  ILM_TRY(B->corr.alloc(B->ftot * e));
+  ILM_TRY(B->edges.alloc(B->etot * e));
+  ILM_TRY(B->jump.alloc((size_t)Ptot * e));
+  ILM_TRY(B->avg.alloc((size_t)Ptot * e));
+  ILM_TRY(B->g.alloc((size_t)Ptot * e));
+  ILM_TRY(B->s.alloc((size_t)Ptot * e));
+  ILM_TRY(B->rhs64.alloc((size_t)Ptot * 8));
+  ILM_TRY(B->x64.alloc((size_t)Ptot * 8));
+  ILM_TRY(B->S.alloc(std::max<size_t>(B->stot, 1) * 8));
+  ILM_TRY(B->F.alloc((size_t)Ptot * functional_size()));
+  ILM_TRY(B->iters.alloc((size_t)nprob * sizeof(int)));
+  ILM_TRY(B->relres.alloc((size_t)nprob * sizeof(double)));
+
+  // FFT convolution jobs (fstar and corr in place); one work area per problem
+  std::vector<size_t> woff(nprob + 1, 0);
+  std::vector<int> P1(nprob), P2(nprob);
+  for (int p = 0; p < nprob; ++p) {
+    const int n1 = probs[p].nx - 1, n2 = probs[p].ny - 1;
+    P1[p] = good_fft_size(2 * n1 - 1);
+    P2[p] = good_fft_size(2 * n2 - 1);
+    woff[p + 1] = woff[p] + (size_t)n2 * (P1[p] / 2 + 1) * 2 * e;
+  }
+  ILM_TRY(B->convwork.alloc(woff[nprob]));
+  std::vector<ConvJobDev> jobsA(nprob), jobsB(nprob);
+  for (int p = 0; p < nprob; ++p) {
+    ConvJobDev J;
+    memset(&J, 0, sizeof(J));
+    ILM_TRY(conv_resources(P1[p], P2[p], dtype, &J.spec, &J.tw1, &J.tw2, nullptr));
+    J.work = static_cast<unsigned char*>(B->convwork.p) + woff[p];
+    J.n1 = probs[p].nx - 1;
+    J.n2 = probs[p].ny - 1;
+    J.n2out = J.n2;
+    J.P1 = P1[p];
+    J.P2 = P2[p];
+    J.scale = probs[p].h * probs[p].h;  // L^{-1} = h^2 G* under GridScaling
+    J.in = J.out = static_cast<unsigned char*>(B->fstar.p) + B->foff[p] * e;
+    jobsA[p] = J;
+    J.in = J.out = static_cast<unsigned char*>(B->corr.p) + B->foff[p] * e;
+    jobsB[p] = J;
+  }
+  ILM_TRY(conv_jobs_finalize(jobsA, dtype, &B->convL));
+  ILM_TRY(conv_jobs_finalize(jobsB, dtype, &B->convL));
+  B->n_conv = nprob;
+  ILM_TRY(up(B->convA, jobsA));
+  ILM_TRY(up(B->convB, jobsB));
+
+  // ---- tasks ---------------------------------------------------------------
+  auto ptr_at = [&](const DevBuf& b, size_t off) { return (void*)(static_cast<unsigned char*>(b.p) + off * e); };
+  auto scat = [&](int p, int pc, const DevBuf& in, int coef, void* outp, int& tiles) {
+    BScatterTask T;
+    memset(&T, 0, sizeof(T));
+    ilm_grid_s g{probs[p].nx, probs[p].ny, probs[p].h, probs[p].i0x, probs[p].i0y};
+    const Shape2 sh = g.shape(pc);
+    const int dx = pc_dx(pc), dy = pc_dy(pc);
+    const size_t o = B->poff[p];
+    T.n1 = sh.n1;
+    T.n2 = sh.n2;
+    T.ntx = Wall[p].ntx[pc];
+    T.tile0 = tiles;
+    tiles += Wall[p].ntx[pc] * Wall[p].nty[pc];
+    T.tptr = B->tptr[pc].as<int>() + tpo[pc][p];
+    T.tpts = B->tpts[pc].as<int>() + tso[pc][p];
+    T.bx = B->bx[dx].as<int>() + o;
+    T.by = B->by[dy].as<int>() + o;
+    T.wx = static_cast<unsigned char*>(B->wx[dx].p) + o * NTAP * e;
+    T.wy = static_cast<unsigned char*>(B->wy[dy].p) + o * NTAP * e;
+    T.wsc = ptr_at(B->wsc, o);
+    T.nx = ptr_at(B->nx, o);
+    T.ny = ptr_at(B->ny, o);
+    T.in = ptr_at(in, o);
+    T.coef = coef;
+    T.out = outp;
+    return T;
+  };
+  auto edge_u = [&](int p) { return ptr_at(B->edges, eoff[p]); };
+  auto edge_v = [&](int p) { return ptr_at(B->edges, eoff[p] + (size_t)probs[p].nx * (probs[p].ny - 1)); };
+  auto field = [&](const DevBuf& b, int p) { return ptr_at(b, B->foff[p]); };
+  auto stencil = [&](int p, const void* in, void* outp, int& blks, bool grad) {
+    BStencilTask T;
+    T.NX = probs[p].nx;
+    T.NY = probs[p].ny;
+    T.blk0 = blks;
+    const int w = grad ? T.NX : T.NX - 1, h = grad ? T.NY : T.NY - 1;
+    blks += ((w + SB_X - 1) / SB_X) * ((h + SB_Y - 1) / SB_Y);
+    T.in = in;
+    T.out = outp;
+    T.scale = grad ? 1.0 : 1.0 / probs[p].h;
+    return T;
+  };
+  auto gath = [&](int p, int& pts) {
+    BGatherTask G;
+    memset(&G, 0, sizeof(G));
+    const size_t o = B->poff[p];
+    G.npts = probs[p].npts;
+    G.pt0 = pts;
+    pts += G.npts;
+    for (int d = 0; d < 2; ++d) {
+      G.bx[d] = B->bx[d].as<int>() + o;
+      G.by[d] = B->by[d].as<int>() + o;
+      G.wx[d] = static_cast<unsigned char*>(B->wx[d].p) + o * NTAP * e;
+      G.wy[d] = static_cast<unsigned char*>(B->wy[d].p) + o * NTAP * e;
+    }
+    G.nx = ptr_at(B->nx, o);
+    G.ny = ptr_at(B->ny, o);
+    G.out = ptr_at(B->g, o);
+    return G;
+  };
+  std::vector<BScatterTask> sA, sB;
+  std::vector<BStencilTask> dA, gA, dB;
+  std::vector<BGatherTask> hA;
+  int tA = 0, tB = 0, bdA = 0, bgA = 0, bdB = 0, ptsA = 0;
+  for (int p = 0; p < nprob; ++p) {
+    const int nx_ = probs[p].nx, ny_ = probs[p].ny;
+    if (probs[p].kind == 0) {  // Dirichlet: f* = L^-1 D_s [f]; correction R s
+      sA.push_back(scat(p, PC_U, B->jump, CF_NX, edge_u(p), tA));
+      sA.push_back(scat(p, PC_V, B->jump, CF_NY, edge_v(p), tA));
+      dA.push_back(stencil(p, edge_u(p), field(B->fstar, p), bdA, false));
+      BGatherTask G = gath(p, ptsA);
+      G.nterms = 1;
+      G.arr[0] = field(B->fstar, p);
+      G.n1[0] = nx_ - 1;
+      G.n2[0] = ny_ - 1;
+      G.xs[0] = 0;
+      G.ys[0] = 0;
+      G.coef[0] = CF_ONE;
+      G.scale = 1.0;
+      hA.push_back(G);
+      sB.push_back(scat(p, PC_P, B->s, CF_ONE, field(B->corr, p), tB));
+    } else {  // Neumann: f* = L^-1 R [vn]; rhs from G_s f*; correction D_s [phi]
+      sA.push_back(scat(p, PC_P, B->jump, CF_ONE, field(B->fstar, p), tA));
+      gA.push_back(stencil(p, field(B->fstar, p), edge_u(p), bgA, true));
+      BGatherTask G = gath(p, ptsA);
+      G.nterms = 2;
+      G.arr[0] = edge_u(p);
+      G.n1[0] = nx_;
+      G.n2[0] = ny_ - 1;
+      G.xs[0] = 1;
+      G.ys[0] = 0;
+      G.coef[0] = CF_NX;
+      G.arr[1] = edge_v(p);
+      G.n1[1] = nx_ - 1;
+      G.n2[1] = ny_;
+      G.xs[1] = 0;
+      G.ys[1] = 1;
+      G.coef[1] = CF_NY;
+      G.scale = 1.0 / probs[p].h;
+      hA.push_back(G);
+      sB.push_back(scat(p, PC_U, B->s, CF_NX, edge_u(p), tB));
+      sB.push_back(scat(p, PC_V, B->s, CF_NY, edge_v(p), tB));
+      dB.push_back(stencil(p, edge_u(p), field(B->corr, p), bdB, false));
+    }
+  }
+  B->n_scatA = (int)sA.size();
+  B->blk_scatA = tA;
+  B->n_scatB = (int)sB.size();
+  B->blk_scatB = tB;
+  B->n_divA = (int)dA.size();
+  B->blk_divA = bdA;
+  B->n_gradA = (int)gA.size();
+  B->blk_gradA = bgA;
+  B->n_divB = (int)dB.size();
+  B->blk_divB = bdB;
+  B->n_gathA = (int)hA.size();
+  ILM_TRY(up(B->scatA, sA));
+  ILM_TRY(up(B->scatB, sB));
+  ILM_TRY(up(B->divA, dA));
+  ILM_TRY(up(B->gradA, gA));
+  ILM_TRY(up(B->divB, dB));
+  ILM_TRY(up(B->gathA, hA));
+
+  // ---- Schur complements (FP64, LGF point-point sums) -----------------------
+  std::vector<SchurProbDev> sp(nprob);
+  int tiles = 0;
+  for (int p = 0; p < nprob; ++p) {
+    sp[p].kind = probs[p].kind == 0 ? ILM_SCHUR_RTLINVR : ILM_SCHUR_CLINVCT;
+    sp[p].n = probs[p].npts;
+    sp[p].poff = (int)B->poff[p];
+    sp[p].tile0 = tiles;
+    const int nt = (probs[p].npts + 15) / 16;
+    tiles += nt * nt;
+    sp[p].soff = B->soff[p];
+    sp[p].invh = 1.0 / probs[p].h;
+  }
+  B->schur_tiles = tiles;
+  ILM_TRY(up(B->schurP, sp));
+  BatchWin BW;
+  for (int d = 0; d < 2; ++d) {
+    BW.bx[d] = B->bx[d].as<int>();
+    BW.by[d] = B->by[d].as<int>();
+    BW.wx64[d] = B->wx64[d].as<double>();
+    BW.wy64[d] = B->wy64[d].as<double>();
+  }
+  BW.nx64 = B->nx64.as<double>();
+  BW.ny64 = B->ny64.as<double>();
+  ILM_TRY(schur_build_batched(nprob, B->schurP.as<SchurProbDev>(), tiles, Ptot, B->pt2prob.as<int>(), BW,
+                              B->ds64.as<double>(), static_cast<Functional*>(B->F.p), B->S.as<double>(), B->max_grid,
+                              nullptr));
+  ILM_CHECK_CUDA(cudaDeviceSynchronize());
+  *out = guard.release();
+  return ILM_OK;
+}
+
+int ilm_batch_destroy(ilm_batch_t b) {
+  delete b;
+  return ILM_OK;
+}
+
+int ilm_batch_layout(ilm_batch_t b, size_t* field_offsets, size_t* point_offsets) {
+  ILM_REQUIRE(b, "null batch");
+  for (int p = 0; p <= b->nprob; ++p) {
+    if (field_offsets) field_offsets[p] = b->foff[p];
+    if (point_offsets) point_offsets[p] = b->poff[p];
+  }
+  return ILM_OK;
+}
+
+int ilm_batch_solve(ilm_batch_t b, const void* fplus, const void* fminus, void* f_out, void* s_out, double tol,
+                    int maxiter, ilm_stream_t stream) {
+  ILM_REQUIRE(b && fplus && fminus && f_out && s_out, "batch_solve: null argument");
+  ILM_REQUIRE(tol > 0 && maxiter > 0, "batch_solve: bad tolerance / iteration limit");
+  cudaStream_t st = as_stream(stream);
+  const int dt = b->dtype;
+  const int Ptot = b->Ptot;
+  if (tol != b->cg_tol || maxiter != b->cg_maxiter) {
+    std::vector<CGParams> cg(b->nprob);
+    for (int p = 0; p < b->nprob; ++p) {
+      const size_t o = b->poff[p];
+      cg[p].A64 = b->S.as<double>() + b->soff[p];
+      cg[p].A32 = nullptr;
+      cg[p].b = b->rhs64.as<double>() + o;
+      cg[p].x = b->x64.as<double>() + o;
+      cg[p].w = b->ds64.as<double>() + o;
+      cg[p].n = b->probs[p].npts;
+      cg[p].maxiter = maxiter;
+      cg[p].tol = tol;
+      cg[p].iters = b->iters.as<int>() + p;
+      cg[p].relres = b->relres.as<double>() + p;
+    }
+    ILM_TRY(up(b->cgp, cg));
+    b->cg_tol = tol;
+    b->cg_maxiter = maxiter;
+  }
+  const int pb = std::min(1024, (Ptot + 255) / 256);
+  b->nev = 0;
+  b->launches = 0;
+#define MARK()                                                     \
+  do {                                                             \
+    if (b->profiling && b->nev < 32) {                             \
+      if (!b->ev[b->nev]) ILM_CHECK_CUDA(cudaEventCreate(&b->ev[b->nev])); \
+      ILM_CHECK_CUDA(cudaEventRecord(b->ev[b->nev], st));          \
+      b->nev++;                                                    \
+    }                                                              \
+  } while (0)
+  MARK();
+  BDISPATCH(dt, {
+    k_jump_avg<T><<<pb, 256, 0, st>>>(Ptot, static_cast<const T*>(fplus), static_cast<const T*>(fminus),
+                                      b->jump.as<T>(), b->avg.as<T>());
+    ILM_CHECK_LAUNCH();
+    b->launches++;
+    MARK();  // 1: surface data jump/average
+    if (b->n_scatA) k_bscatter<T><<<b->blk_scatA, dim3(SB_X, SB_Y), 0, st>>>(b->scatA.as<BScatterTask>(), b->n_scatA);
+    ILM_CHECK_LAUNCH();
+    b->launches += b->n_scatA ? 1 : 0;
+    MARK();  // 2: DDF scatter (double layer / single layer)
+    if (b->n_divA) k_bdiv<T><<<b->blk_divA, dim3(SB_X, SB_Y), 0, st>>>(b->divA.as<BStencilTask>(), b->n_divA);
+    ILM_CHECK_LAUNCH();
+    b->launches += b->n_divA ? 1 : 0;
+    MARK();  // 3: divergence stencil
+  });
+  ILM_TRY(conv_jobs_launch(b->convA.as<ConvJobDev>(), b->n_conv, b->convL, dt, st));
+  b->launches += 3;
+  MARK();  // 4: LGF FFT convolution (f*)
+  BDISPATCH(dt, {
+    if (b->n_gradA) k_bgrad<T><<<b->blk_gradA, dim3(SB_X, SB_Y), 0, st>>>(b->gradA.as<BStencilTask>(), b->n_gradA);
+    ILM_CHECK_LAUNCH();
+    b->launches += b->n_gradA ? 1 : 0;
+    MARK();  // 5: gradient stencil
+    k_bgather<T><<<(Ptot + 127) / 128, 128, 0, st>>>(b->gathA.as<BGatherTask>(), b->n_gathA, Ptot);
+    ILM_CHECK_LAUNCH();
+    k_rhs64<T><<<pb, 256, 0, st>>>(Ptot, b->g.as<T>(), b->avg.as<T>(), b->rhs64.as<double>());
+    ILM_CHECK_LAUNCH();
+    b->launches += 2;
+    MARK();  // 6: DDF gather + Schur right-hand side
+  });
+  ILM_TRY(launch_cg_batched(b->cgp.as<CGParams>(), b->nprob, b->maxN, st));
+  b->launches += 1;
+  MARK();  // 7: Schur CG
+  ILM_TRY(st_convert(Ptot, ILM_F64, b->x64.p, dt, s_out, st));
+  ILM_CHECK_CUDA(cudaMemcpyAsync(b->s.p, s_out, (size_t)Ptot * es(dt), cudaMemcpyDeviceToDevice, st));
+  b->launches += 1;
+  MARK();  // 8: convert
+  BDISPATCH(dt, {
+    if (b->n_scatB) k_bscatter<T><<<b->blk_scatB, dim3(SB_X, SB_Y), 0, st>>>(b->scatB.as<BScatterTask>(), b->n_scatB);
+    ILM_CHECK_LAUNCH();
+    b->launches += b->n_scatB ? 1 : 0;
+    MARK();  // 9: DDF scatter (correction)
+    if (b->n_divB) k_bdiv<T><<<b->blk_divB, dim3(SB_X, SB_Y), 0, st>>>(b->divB.as<BStencilTask>(), b->n_divB);
+    ILM_CHECK_LAUNCH();
+    b->launches += b->n_divB ? 1 : 0;
+    MARK();  // 10: divergence stencil
+  });
+  ILM_TRY(conv_jobs_launch(b->convB.as<ConvJobDev>(), b->n_conv, b->convL, dt, st));
+  b->launches += 3;
+  MARK();  // 11: LGF FFT convolution (correction)
+  ILM_TRY(st_axpby(b->ftot, dt, 1.0, b->corr.p, 1.0, b->fstar.p, f_out, st));
+  b->launches += 1;
+  MARK();  // 12: f = f* + correction
+#undef MARK
+  return ILM_OK;
+}
+
+int ilm_batch_set_profiling(ilm_batch_t b, int enable) {
+  ILM_REQUIRE(b, "null batch");
+  b->profiling = enable ? 1 : 0;
+  return ILM_OK;
+}
+
+int ilm_batch_stage_times(ilm_batch_t b, float* ms, int* nstages, int* launches) {
+  ILM_REQUIRE(b, "null batch");
+  const int n = b->nev > 0 ? b->nev - 1 : 0;
+  if (nstages) *nstages = n;
+  if (launches) *launches = b->launches;
+  if (ms && n > 0) {
+    ILM_CHECK_CUDA(cudaEventSynchronize(b->ev[b->nev - 1]));
+    for (int i = 0; i < n; ++i) ILM_CHECK_CUDA(cudaEventElapsedTime(&ms[i], b->ev[i], b->ev[i + 1]));
+  }
+  return ILM_OK;
+}
+
+int ilm_batch_stats(ilm_batch_t b, double* stats) {
+  ILM_REQUIRE(b && stats, "null argument");
+  // total points, total Nodes{Primal} cells, sum of npts^2, sum over problems of
+  // the padded FFT extent P1*P2, number of problems
+  double p2 = 0.0, fft = 0.0;
+  for (int p = 0; p < b->nprob; ++p) {
+    const auto& P = b->probs[p];
+    p2 += (double)P.npts * P.npts;
+    fft += (double)good_fft_size(2 * (P.nx - 1) - 1) * good_fft_size(2 * (P.ny - 1) - 1);
+  }
+  stats[0] = b->Ptot;
+  stats[1] = (double)b->ftot;
+  stats[2] = p2;
+  stats[3] = fft;
+  stats[4] = b->nprob;
+  return ILM_OK;
+}
+
+int ilm_batch_info(ilm_batch_t b, int* iterations, double* rel_residual) {
+  ILM_REQUIRE(b, "null batch");
+  if (iterations)
+    ILM_CHECK_CUDA(cudaMemcpy(iterations, b->iters.p, (size_t)b->nprob * sizeof(int), cudaMemcpyDeviceToHost));
+  if (rel_residual)
+    ILM_CHECK_CUDA(cudaMemcpy(rel_residual, b->relres.p, (size_t)b->nprob * sizeof(double), cudaMemcpyDeviceToHost));
+  return ILM_OK;
+}
+
+}  // extern "C"

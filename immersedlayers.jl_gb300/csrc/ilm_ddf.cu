@@ -1,0 +1,321 @@
+// DDF regularization (scatter) and interpolation (gather) between surface
+// points and the staggered grid.
+//
+// Replaces the sparse RegularizationMatrix / InterpolationMatrix products of
+// CartesianGrids used by regularize!/interpolate! (src/surface_operators.jl:
+// 38-46, 80-88) and their normal/cross/dot variants (:98-343).
+//
+// Setup (host, once per cache): for every point and each 1-D offset class
+// (x on primal/dual lines, y on primal/dual lines) the 4-tap window base index
+// and the DDF weights phi((x_i - X_k)/h) are computed in FP64; for each grid
+// position class the points are binned into 32x8 output tiles.
+//
+// Scatter: one thread per output cell, one CTA per tile.  Each thread sums the
+// contributions of the tile's candidate points in index order, so the result
+// is deterministic (no atomics) and every cell of the output is written (the
+// reference's fill!(s,0) + mul! overwrite) in one coalesced pass.
+// Gather: one thread per point, 16 taps per term, fixed order.
+#include <math.h>
+
+#include <algorithm>
+
+#include "ilm_internal.cuh"
+
+namespace ilm {
+
+// ---------------------------------------------------------------------------
+// DDF kernels (host, FP64) -- published formulas
+// ---------------------------------------------------------------------------
+static double ddf_eval(int ddf, double r) {
+  r = fabs(r);
+  const double s3 = 1.7320508075688772935;
+  switch (ddf) {
+    case ILM_DDF_YANG3:  // Yang, Zhang, Li & Yang, JCP 228 (2009), smoothed 3-point
+      if (r <= 1.0)
+        return 17.0 / 48.0 + s3 * M_PI / 108.0 + r / 4.0 - r * r / 4.0 +
+               (1.0 - 2.0 * r) / 16.0 * sqrt(std::max(-12.0 * r * r + 12.0 * r + 1.0, 0.0)) -
+               s3 / 12.0 * asin(s3 / 2.0 * (2.0 * r - 1.0));
+      if (r < 2.0)
+        return 55.0 / 48.0 - s3 * M_PI / 108.0 - 13.0 * r / 12.0 + r * r / 4.0 +
+               (2.0 * r - 3.0) / 48.0 * sqrt(std::max(-12.0 * r * r + 36.0 * r - 23.0, 0.0)) +
+               s3 / 36.0 * asin(s3 / 2.0 * (2.0 * r - 3.0));
+      return 0.0;
+    case ILM_DDF_ROMA:  // Roma, Peskin & Berger, JCP 153 (1999)
+      if (r <= 0.5) return (1.0 + sqrt(1.0 - 3.0 * r * r)) / 3.0;
+      if (r < 1.5) return (5.0 - 3.0 * r - sqrt(std::max(1.0 - 3.0 * (1.0 - r) * (1.0 - r), 0.0))) / 6.0;
+      return 0.0;
+    case ILM_DDF_M4PRIME:  // Monaghan M4'
+      if (r <= 1.0) return 1.0 - 2.5 * r * r + 1.5 * r * r * r;
+      if (r < 2.0) return 0.5 * (2.0 - r) * (2.0 - r) * (1.0 - r);
+      return 0.0;
+    case ILM_DDF_WITCHHAT:
+      return r < 1.0 ? 1.0 - r : 0.0;
+    case ILM_DDF_M3:
+      if (r <= 0.5) return 0.75 - r * r;
+      if (r < 1.5) return 0.5 * (1.5 - r) * (1.5 - r);
+      return 0.0;
+  }
+  return 0.0;
+}
+
+// window of 4 taps covering the support: base = floor(r) - 1 (r = fractional
+// index of the point on that line), weights phi(base + t - r)
+static void ddf_window(int ddf, double r, int* base, double* w) {
+  const int b = (int)floor(r) - 1;
+  *base = b;
+  for (int t = 0; t < NTAP; ++t) w[t] = ddf_eval(ddf, (double)(b + t) - r);
+}
+
+template <typename T>
+static int upload(DevBuf& b, const T* h, size_t n) {
+  ILM_TRY(b.alloc(std::max<size_t>(n, 1) * sizeof(T)));
+  if (n) ILM_CHECK_CUDA(cudaMemcpy(b.p, h, n * sizeof(T), cudaMemcpyHostToDevice));
+  return ILM_OK;
+}
+
+static int upload_typed(DevBuf& b, const std::vector<double>& h, int dtype) {
+  if (dtype == ILM_F64) return upload(b, h.data(), h.size());
+  std::vector<float> f(h.begin(), h.end());
+  return upload(b, f.data(), f.size());
+}
+
+void host_windows(const ilm_grid_s& g, int ddf, int N, const double* x, const double* y, HostWindows* W) {
+  const double h = g.h;
+  for (int dual = 0; dual < 2; ++dual) {
+    W->bx[dual].resize(N);
+    W->by[dual].resize(N);
+    W->wx[dual].resize((size_t)N * NTAP);
+    W->wy[dual].resize((size_t)N * NTAP);
+  }
+  // fractional 0-based index of a point on primal / dual lines:
+  // primal i at x = (i + 1 - i0) h ; dual i at x = (i + 1/2 - i0) h
+  for (int k = 0; k < N; ++k) {
+    for (int dual = 0; dual < 2; ++dual) {
+      const double off = dual ? 0.5 : 1.0;
+      const double rx = x[k] / h + g.i0x - off;
+      const double ry = y[k] / h + g.i0y - off;
+      ddf_window(ddf, rx, &W->bx[dual][k], &W->wx[dual][(size_t)k * NTAP]);
+      ddf_window(ddf, ry, &W->by[dual][k], &W->wy[dual][(size_t)k * NTAP]);
+    }
+  }
+  // tile candidate lists per position class, each sorted by point index
+  for (int pc = 0; pc < 4; ++pc) {
+    const Shape2 sh = g.shape(pc);
+    const int dx = pc_dx(pc), dy = pc_dy(pc);
+    W->ntx[pc] = (sh.n1 + TILE_X - 1) / TILE_X;
+    W->nty[pc] = (sh.n2 + TILE_Y - 1) / TILE_Y;
+    const size_t nt = (size_t)W->ntx[pc] * W->nty[pc];
+    std::vector<int>& cnt = W->tptr[pc];
+    cnt.assign(nt + 1, 0);
+    auto tiles_of = [&](int k, int* tx0, int* tx1, int* ty0, int* ty1) {
+      int b0 = W->bx[dx][k], b1 = b0 + NTAP - 1;
+      int e0 = W->by[dy][k], e1 = e0 + NTAP - 1;
+      b0 = std::max(b0, 0);
+      e0 = std::max(e0, 0);
+      b1 = std::min(b1, sh.n1 - 1);
+      e1 = std::min(e1, sh.n2 - 1);
+      if (b0 > b1 || e0 > e1) return false;
+      *tx0 = b0 / TILE_X;
+      *tx1 = b1 / TILE_X;
+      *ty0 = e0 / TILE_Y;
+      *ty1 = e1 / TILE_Y;
+      return true;
+    };
+    for (int k = 0; k < N; ++k) {
+      int a0, a1, b0, b1;
+      if (!tiles_of(k, &a0, &a1, &b0, &b1)) continue;
+      for (int ty = b0; ty <= b1; ++ty)
+        for (int tx = a0; tx <= a1; ++tx) cnt[(size_t)ty * W->ntx[pc] + tx + 1]++;
+    }
+    for (size_t t = 0; t < nt; ++t) cnt[t + 1] += cnt[t];
+    std::vector<int>& pts = W->tpts[pc];
+    pts.assign(std::max(cnt[nt], 1), 0);
+    std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+    for (int k = 0; k < N; ++k) {
+      int a0, a1, b0, b1;
+      if (!tiles_of(k, &a0, &a1, &b0, &b1)) continue;
+      for (int ty = b0; ty <= b1; ++ty)
+        for (int tx = a0; tx <= a1; ++tx) pts[fill[(size_t)ty * W->ntx[pc] + tx]++] = k;
+    }
+  }
+}
+
+int cache_build_windows(ilm_cache_s* c) {
+  const int N = c->npts;
+  HostWindows W;
+  host_windows(c->grid, c->ddf, N, c->hx.data(), c->hy.data(), &W);
+  for (int dual = 0; dual < 2; ++dual) {
+    c->hbx[dual] = W.bx[dual];
+    c->hby[dual] = W.by[dual];
+    ILM_TRY(upload(c->bx[dual], W.bx[dual].data(), N));
+    ILM_TRY(upload(c->by[dual], W.by[dual].data(), N));
+    ILM_TRY(upload_typed(c->wx[dual], W.wx[dual], c->dtype));
+    ILM_TRY(upload_typed(c->wy[dual], W.wy[dual], c->dtype));
+    ILM_TRY(upload_typed(c->wx64[dual], W.wx[dual], ILM_F64));
+    ILM_TRY(upload_typed(c->wy64[dual], W.wy[dual], ILM_F64));
+  }
+  for (int pc = 0; pc < 4; ++pc) {
+    TileList& tl = c->tiles[pc];
+    tl.ntx = W.ntx[pc];
+    tl.nty = W.nty[pc];
+    ILM_TRY(upload(tl.ptr, W.tptr[pc].data(), W.tptr[pc].size()));
+    ILM_TRY(upload(tl.pts, W.tpts[pc].data(), W.tpts[pc].size()));
+  }
+  return ILM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// device kernels
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ T coef_val(int code, const T* __restrict__ nx, const T* __restrict__ ny, int k) {
+  switch (code) {
+    case CF_ONE: return (T)1;
+    case CF_NX: return nx[k];
+    case CF_NY: return ny[k];
+    case CF_MNX: return -nx[k];
+    case CF_MNY: return -ny[k];
+    case CF_MONE: return (T)-1;
+  }
+  return (T)0;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(TILE_X* TILE_Y)
+k_scatter(int n1, int n2, int ntx, const int* __restrict__ tptr, const int* __restrict__ tpts,
+          const int* __restrict__ bx, const int* __restrict__ by, const T* __restrict__ wx,
+          const T* __restrict__ wy, const T* __restrict__ wsc, const T* __restrict__ nx,
+          const T* __restrict__ ny, const T* __restrict__ in1, int c1, const T* __restrict__ in2, int c2,
+          T* __restrict__ out) {
+  const int tx = blockIdx.x % ntx, ty = blockIdx.x / ntx;
+  const int i = tx * TILE_X + threadIdx.x;
+  const int j = ty * TILE_Y + threadIdx.y;
+  const int t = blockIdx.x;
+  const int p0 = tptr[t], p1 = tptr[t + 1];
+  T acc = (T)0;
+  for (int p = p0; p < p1; ++p) {
+    const int k = tpts[p];
+    const int di = i - bx[k];
+    const int dj = j - by[k];
+    if ((unsigned)di < (unsigned)NTAP && (unsigned)dj < (unsigned)NTAP) {
+      T g = coef_val<T>(c1, nx, ny, k) * in1[k];
+      if (in2) g += coef_val<T>(c2, nx, ny, k) * in2[k];
+      acc += wsc[k] * g * wx[k * NTAP + di] * wy[k * NTAP + dj];
+    }
+  }
+  if (i < n1 && j < n2) out[(size_t)j * n1 + i] = acc;
+}
+
+struct GTermDev {
+  const void* arr;
+  int n1, n2;
+  int xsel, ysel;  // 0 primal 1 dual
+  int coef;
+};
+
+template <typename T>
+__global__ void k_gather(int N, const GTermDev* __restrict__ terms_unused, GTermDev t0, GTermDev t1, GTermDev t2,
+                         GTermDev t3, int nterms, const int* __restrict__ bx0, const int* __restrict__ bx1,
+                         const int* __restrict__ by0, const int* __restrict__ by1, const T* __restrict__ wx0,
+                         const T* __restrict__ wx1, const T* __restrict__ wy0, const T* __restrict__ wy1,
+                         const T* __restrict__ nx, const T* __restrict__ ny, T* __restrict__ out, int accumulate,
+                         T scale) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= N) return;
+  T total = (T)0;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    if (q >= nterms) break;
+    const GTermDev tt = q == 0 ? t0 : (q == 1 ? t1 : (q == 2 ? t2 : t3));
+    const int* bx = tt.xsel ? bx1 : bx0;
+    const int* by = tt.ysel ? by1 : by0;
+    const T* wx = tt.xsel ? wx1 : wx0;
+    const T* wy = tt.ysel ? wy1 : wy0;
+    const T* __restrict__ a = static_cast<const T*>(tt.arr);
+    const int b0 = bx[k], e0 = by[k];
+    T acc = (T)0;
+#pragma unroll
+    for (int jj = 0; jj < NTAP; ++jj) {
+      const int j = e0 + jj;
+      if ((unsigned)j >= (unsigned)tt.n2) continue;
+      T racc = (T)0;
+#pragma unroll
+      for (int ii = 0; ii < NTAP; ++ii) {
+        const int i = b0 + ii;
+        if ((unsigned)i >= (unsigned)tt.n1) continue;
+        racc += wx[k * NTAP + ii] * a[(size_t)j * tt.n1 + i];
+      }
+      acc += wy[k * NTAP + jj] * racc;
+    }
+    total += coef_val<T>(tt.coef, nx, ny, k) * acc;
+  }
+  total *= scale;
+  if (accumulate) out[k] += total;
+  else out[k] = total;
+}
+
+int launch_scatter(ilm_cache_s* c, int pc, const void* in1, int coef1, const void* in2, int coef2, void* out,
+                   cudaStream_t st) {
+  const Shape2 sh = c->grid.shape(pc);
+  const TileList& tl = c->tiles[pc];
+  const int dx = pc_dx(pc), dy = pc_dy(pc);
+  dim3 blk(TILE_X, TILE_Y);
+  const int nb = tl.ntx * tl.nty;
+  if (c->dtype == ILM_F64) {
+    k_scatter<double><<<nb, blk, 0, st>>>(sh.n1, sh.n2, tl.ntx, tl.ptr.as<int>(), tl.pts.as<int>(), c->bx[dx].as<int>(),
+                                          c->by[dy].as<int>(), c->wx[dx].as<double>(), c->wy[dy].as<double>(),
+                                          c->wscale.as<double>(), c->nx.as<double>(), c->ny.as<double>(),
+                                          static_cast<const double*>(in1), coef1, static_cast<const double*>(in2),
+                                          coef2, static_cast<double*>(out));
+  } else {
+    k_scatter<float><<<nb, blk, 0, st>>>(sh.n1, sh.n2, tl.ntx, tl.ptr.as<int>(), tl.pts.as<int>(), c->bx[dx].as<int>(),
+                                         c->by[dy].as<int>(), c->wx[dx].as<float>(), c->wy[dy].as<float>(),
+                                         c->wscale.as<float>(), c->nx.as<float>(), c->ny.as<float>(),
+                                         static_cast<const float*>(in1), coef1, static_cast<const float*>(in2), coef2,
+                                         static_cast<float*>(out));
+  }
+  ILM_CHECK_LAUNCH();
+  return ILM_OK;
+}
+
+int launch_gather(ilm_cache_s* c, const GatherTerm* terms, int nterms, void* out, bool accumulate, double scale,
+                  cudaStream_t st) {
+  if (nterms < 1 || nterms > 4) {
+    set_error("gather: 1..4 terms");
+    return ILM_ERR_INVALID_ARG;
+  }
+  GTermDev td[4];
+  for (int q = 0; q < 4; ++q) {
+    td[q] = GTermDev{nullptr, 0, 0, 0, 0, CF_ZERO};
+    if (q < nterms) {
+      const Shape2 sh = c->grid.shape(terms[q].pc);
+      td[q].arr = terms[q].arr;
+      td[q].n1 = sh.n1;
+      td[q].n2 = sh.n2;
+      td[q].xsel = pc_dx(terms[q].pc);
+      td[q].ysel = pc_dy(terms[q].pc);
+      td[q].coef = terms[q].coef;
+    }
+  }
+  const int N = c->npts;
+  if (N == 0) return ILM_OK;
+  const int bs = 128;
+  const int nb = (N + bs - 1) / bs;
+  if (c->dtype == ILM_F64) {
+    k_gather<double><<<nb, bs, 0, st>>>(N, nullptr, td[0], td[1], td[2], td[3], nterms, c->bx[0].as<int>(),
+                                        c->bx[1].as<int>(), c->by[0].as<int>(), c->by[1].as<int>(),
+                                        c->wx[0].as<double>(), c->wx[1].as<double>(), c->wy[0].as<double>(),
+                                        c->wy[1].as<double>(), c->nx.as<double>(), c->ny.as<double>(),
+                                        static_cast<double*>(out), accumulate ? 1 : 0, scale);
+  } else {
+    k_gather<float><<<nb, bs, 0, st>>>(N, nullptr, td[0], td[1], td[2], td[3], nterms, c->bx[0].as<int>(),
+                                       c->bx[1].as<int>(), c->by[0].as<int>(), c->by[1].as<int>(),
+                                       c->wx[0].as<float>(), c->wx[1].as<float>(), c->wy[0].as<float>(),
+                                       c->wy[1].as<float>(), c->nx.as<float>(), c->ny.as<float>(),
+                                       static_cast<float*>(out), accumulate ? 1 : 0, (float)scale);
+  }
+  ILM_CHECK_LAUNCH();
+  return ILM_OK;
+}
+
+}  // namespace ilm

@@ -1,0 +1,647 @@
+// Unbounded-domain inverse Laplacian: linear convolution with the lattice
+// Green's function (LGF) of the 5-point Laplacian by zero-padded real FFTs.
+//
+// Replaces CartesianGrids' plan_laplacian(...; with_inverse=true) / `L \ w`
+// (called from src/grid_operators.jl:177-179, built at src/cache.jl:321-324).
+//
+// Pipeline for an n1 x n2 field (x fastest) and padded sizes P1 >= 2 n1 - 1,
+// P2 >= 2 n2 - 1 (P = 2^a 3^b):
+//   1. k_rfft_rows  : each of the n2 rows -> real FFT of length P1 (complex
+//                     FFT of P1/2 + split), zero padding pruned on input.
+//   2. k_cols       : each of the P1/2+1 spectral columns -> length-P2 complex
+//                     FFT, multiply by the real LGF spectrum, inverse FFT; only
+//                     the n2 input rows are read and the n2 output rows written.
+//   3. k_irfft_rows : each of the n2 rows -> inverse real FFT, first n1 values.
+// The FFTs are Stockham auto-sort radix-4/3/2 transforms held in shared memory.
+// The LGF table and its spectrum are built on the device in FP64 with the same
+// kernels and cached per size.
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <memory>
+
+#include "ilm_internal.cuh"
+
+namespace ilm {
+
+template <typename T> struct CT;
+template <> struct CT<float> { using t = float2; };
+template <> struct CT<double> { using t = double2; };
+
+template <typename C> __device__ __forceinline__ C cadd(C a, C b) { C r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
+template <typename C> __device__ __forceinline__ C csub(C a, C b) { C r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
+template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
+  C r; r.x = a.x * b.x - a.y * b.y; r.y = a.x * b.y + a.y * b.x; return r;
+}
+// s * i * a  (s = +1 or -1)
+template <typename C> __device__ __forceinline__ C cmuli(C a, int s) {
+  C r; r.x = -s * a.y; r.y = s * a.x; return r;
+}
+
+// Stockham auto-sort FFT of `ncol` columns of length L, column c at A[c*cs ..].
+// tw: table of length twlen (multiple of L) with tw[m] = exp(-2 pi i m / twlen).
+// SIGN = -1 forward, +1 inverse (unnormalised).  Returns the buffer holding
+// the result (A or B).  Must be called by all threads of the block.
+template <typename T, int SIGN>
+__device__ typename CT<T>::t* stockham(typename CT<T>::t* A, typename CT<T>::t* B, int L, int ncol, int cs,
+                                      const typename CT<T>::t* __restrict__ tw, int twlen) {
+  using C = typename CT<T>::t;
+  int Ns = 1;
+  int rem = L;
+  const T s3 = (T)0.86602540378443864676;
+  while (rem > 1) {
+    const int r = (rem % 4 == 0) ? 4 : ((rem % 3 == 0) ? 3 : 2);
+    const int stride = L / r;
+    const int tstep0 = twlen / (Ns * r);
+    for (int idx = threadIdx.x; idx < ncol * stride; idx += blockDim.x) {
+      const int c = idx / stride;
+      const int j = idx - c * stride;
+      const C* a_in = A + (size_t)c * cs;
+      C* b_out = B + (size_t)c * cs;
+      const int k = j % Ns;
+      const int tstep = tstep0 * k;
+      C a0 = a_in[j];
+      C a1 = a_in[j + stride];
+      C a2, a3;
+      if (r > 2) a2 = a_in[j + 2 * stride];
+      if (r > 3) a3 = a_in[j + 3 * stride];
+      if (k != 0) {
+        C w = tw[tstep];
+        if (SIGN > 0) w.y = -w.y;
+        a1 = cmul(a1, w);
+        if (r > 2) {
+          C w2 = tw[2 * tstep];
+          if (SIGN > 0) w2.y = -w2.y;
+          a2 = cmul(a2, w2);
+        }
+        if (r > 3) {
+          C w3 = tw[3 * tstep];
+          if (SIGN > 0) w3.y = -w3.y;
+          a3 = cmul(a3, w3);
+        }
+      }
+      const int base = (j / Ns) * Ns * r + k;
+      if (r == 2) {
+        b_out[base] = cadd(a0, a1);
+        b_out[base + Ns] = csub(a0, a1);
+      } else if (r == 4) {
+        C s02 = cadd(a0, a2), d02 = csub(a0, a2);
+        C s13 = cadd(a1, a3), d13 = csub(a1, a3);
+        C id = cmuli(d13, SIGN);
+        b_out[base] = cadd(s02, s13);
+        b_out[base + Ns] = cadd(d02, id);
+        b_out[base + 2 * Ns] = csub(s02, s13);
+        b_out[base + 3 * Ns] = csub(d02, id);
+      } else {  // r == 3
+        C s12 = cadd(a1, a2), d12 = csub(a1, a2);
+        C m;
+        m.x = a0.x - (T)0.5 * s12.x;
+        m.y = a0.y - (T)0.5 * s12.y;
+        C id = cmuli(d12, SIGN);
+        id.x *= s3;
+        id.y *= s3;
+        b_out[base] = cadd(a0, s12);
+        b_out[base + Ns] = cadd(m, id);
+        b_out[base + 2 * Ns] = csub(m, id);
+      }
+    }
+    __syncthreads();
+    C* t = A;
+    A = B;
+    B = t;
+    Ns *= r;
+    rem /= r;
+  }
+  return A;
+}
+
+
+
+__device__ __forceinline__ int find_job(const ConvJobDev* jobs, int njobs, int u, bool rows) {
+  int lo = 0, hi = njobs - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    int off = rows ? jobs[mid].row_off : jobs[mid].col_off;
+    if (off <= u) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// 1. real row FFTs: in (n1 valid of each row, row-major n2 rows) -> work
+template <typename T>
+__global__ void k_rfft_rows(const ConvJobDev* __restrict__ jobs, int njobs) {
+  using C = typename CT<T>::t;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int jb = find_job(jobs, njobs, blockIdx.x, true);
+  const ConvJobDev J = jobs[jb];
+  const int row = blockIdx.x - J.row_off;
+  const int H = J.P1 >> 1;
+  C* A = reinterpret_cast<C*>(smem_raw);
+  C* B = A + H;
+  const T* __restrict__ x = static_cast<const T*>(J.in) + (size_t)row * J.n1;
+  for (int m = threadIdx.x; m < H; m += blockDim.x) {
+    const int i0 = 2 * m;
+    C z;
+    z.x = i0 < J.n1 ? x[i0] : (T)0;
+    z.y = i0 + 1 < J.n1 ? x[i0 + 1] : (T)0;
+    A[m] = z;
+  }
+  __syncthreads();
+  const C* tw = static_cast<const C*>(J.tw1);
+  C* Z = stockham<T, -1>(A, B, H, 1, H, tw, J.P1);
+  C* W = static_cast<C*>(J.work) + (size_t)row * (H + 1);
+  for (int k = threadIdx.x; k <= H; k += blockDim.x) {
+    C zk = Z[k == H ? 0 : k];
+    C zc = Z[k == 0 ? 0 : H - k];
+    zc.y = -zc.y;
+    C e = tw[k];
+    C s = cadd(zk, zc), d = csub(zk, zc);
+    C ed = cmul(e, d);
+    C X;
+    X.x = (T)0.5 * (s.x + ed.y);
+    X.y = (T)0.5 * (s.y - ed.x);
+    W[k] = X;
+  }
+}
+
+// 2. column pass.  mode 0: FFT, multiply by spectrum, inverse FFT (rows
+// [0, n2out) written back).  mode 1: forward FFT only, real part scaled into
+// the spectrum array (spectrum build; J.out is the spectrum).
+template <typename T>
+__global__ void k_cols(const ConvJobDev* __restrict__ jobs, int njobs, int CW, int mode) {
+  using C = typename CT<T>::t;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int jb = find_job(jobs, njobs, blockIdx.x, false);
+  const ConvJobDev J = jobs[jb];
+  const int H = J.P1 >> 1;
+  const int ncols = H + 1;
+  const int c0 = (blockIdx.x - J.col_off) * CW;
+  const int nc = min(CW, ncols - c0);
+  const int P2 = J.P2;
+  const int cs = P2 + 1;  // padded column stride (bank conflicts)
+  C* A = reinterpret_cast<C*>(smem_raw);
+  C* B = A + (size_t)CW * cs;
+  C* W = static_cast<C*>(J.work);
+  for (int idx = threadIdx.x; idx < nc * P2; idx += blockDim.x) {
+    const int row = idx / nc;
+    const int c = idx - row * nc;
+    C v;
+    if (row < J.n2) v = W[(size_t)row * ncols + c0 + c];
+    else { v.x = (T)0; v.y = (T)0; }
+    A[(size_t)c * cs + row] = v;
+  }
+  __syncthreads();
+  const C* tw = static_cast<const C*>(J.tw2);
+  C* F = stockham<T, -1>(A, B, P2, nc, cs, tw, P2);
+  C* G = (F == A) ? B : A;
+  const int hp2 = P2 / 2 + 1;
+  if (mode == 1) {
+    T* spec = static_cast<T*>(J.out);
+    for (int idx = threadIdx.x; idx < nc * hp2; idx += blockDim.x) {
+      const int c = idx / hp2;
+      const int ky = idx - c * hp2;
+      spec[(size_t)(c0 + c) * hp2 + ky] = (T)(F[(size_t)c * cs + ky].x * J.scale);
+    }
+    return;
+  }
+  const T* __restrict__ spec = static_cast<const T*>(J.spec);
+  for (int idx = threadIdx.x; idx < nc * P2; idx += blockDim.x) {
+    const int c = idx / P2;
+    const int ky = idx - c * P2;
+    const int kk = ky <= P2 - ky ? ky : P2 - ky;
+    const T sv = spec[(size_t)(c0 + c) * hp2 + kk];
+    C v = F[(size_t)c * cs + ky];
+    v.x *= sv;
+    v.y *= sv;
+    F[(size_t)c * cs + ky] = v;
+  }
+  __syncthreads();
+  C* R = stockham<T, 1>(F, G, P2, nc, cs, tw, P2);
+  for (int idx = threadIdx.x; idx < nc * J.n2out; idx += blockDim.x) {
+    const int row = idx / nc;
+    const int c = idx - row * nc;
+    W[(size_t)row * ncols + c0 + c] = R[(size_t)c * cs + row];
+  }
+}
+
+// 3. inverse real row FFTs: work -> out (first n1 values of each row) * scale
+template <typename T>
+__global__ void k_irfft_rows(const ConvJobDev* __restrict__ jobs, int njobs) {
+  using C = typename CT<T>::t;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int jb = find_job(jobs, njobs, blockIdx.x, true);
+  const ConvJobDev J = jobs[jb];
+  const int row = blockIdx.x - J.row_off;
+  const int H = J.P1 >> 1;
+  C* X = reinterpret_cast<C*>(smem_raw);
+  C* A = X + (H + 1);
+  C* B = A + H;
+  const C* W = static_cast<const C*>(J.work) + (size_t)row * (H + 1);
+  for (int k = threadIdx.x; k <= H; k += blockDim.x) X[k] = W[k];
+  __syncthreads();
+  const C* tw = static_cast<const C*>(J.tw1);
+  for (int k = threadIdx.x; k < H; k += blockDim.x) {
+    C xk = X[k];
+    C xc = X[H - k];
+    xc.y = -xc.y;
+    C e = tw[k];
+    e.y = -e.y;  // exp(+2 pi i k / P1)
+    C s = cadd(xk, xc), d = csub(xk, xc);
+    C ed = cmul(e, d);
+    C z;  // 0.5 * (s + i * ed)
+    z.x = (T)0.5 * (s.x - ed.y);
+    z.y = (T)0.5 * (s.y + ed.x);
+    A[k] = z;
+  }
+  __syncthreads();
+  C* Z = stockham<T, 1>(A, B, H, 1, H, tw, J.P1);
+  T* __restrict__ out = static_cast<T*>(J.out) + (size_t)row * J.n1;
+  const T sc = (T)J.scale;
+  for (int m = threadIdx.x; m < H; m += blockDim.x) {
+    const int i0 = 2 * m;
+    C z = Z[m];
+    if (i0 < J.n1) out[i0] = z.x * sc;
+    if (i0 + 1 < J.n1) out[i0 + 1] = z.y * sc;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// LGF table: G(m,n) = (1/2pi) int_0^pi (1 - cos(p a) e^{-q s}) / sinh s da,
+// cosh s = 2 - cos a, p = min(m,n), q = max(m,n); G(0,0) = 0, L G = delta.
+// ---------------------------------------------------------------------------
+__global__ void k_lgf_table(int M, const double* __restrict__ a, const double* __restrict__ s,
+                            const double* __restrict__ wt, int nq, double* __restrict__ out) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = blockIdx.y;
+  if (m > M || n > m) return;
+  const double p = (double)n, q = (double)m;
+  double acc = 0.0;
+  for (int j = 0; j < nq; ++j) {
+    const double qs = q * s[j];
+    const double e = exp(-qs);
+    const double sp = sin(0.5 * p * a[j]);
+    acc += (-expm1(-qs) + 2.0 * e * sp * sp) * wt[j];
+  }
+  acc *= 0.15915494309189533577;  // 1/(2 pi)
+  out[(size_t)m * (M + 1) + n] = acc;
+  out[(size_t)n * (M + 1) + m] = acc;
+}
+
+// circulant embedding K[j][i] = G(min(i,P1-i), min(j,P2-j))
+__global__ void k_circulant(const double* __restrict__ G, int ld, int P1, int P2, double* __restrict__ K) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  if (i >= P1) return;
+  const int ii = min(i, P1 - i), jj = min(j, P2 - j);
+  K[(size_t)j * P1 + i] = G[(size_t)ii * ld + jj];
+}
+
+__global__ void k_d2f(const double* __restrict__ in, float* __restrict__ out, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = (float)in[i];
+}
+
+// ---------------------------------------------------------------------------
+// host side: sizes, twiddles, library caches
+// ---------------------------------------------------------------------------
+int good_fft_size(int n) {
+  long best = -1;
+  for (long p3 = 1; p3 < 4L * n + 4; p3 *= 3) {
+    long p2 = 4;
+    while (p2 * p3 < n) p2 *= 2;
+    long cand = p2 * p3;
+    if (best < 0 || cand < best) best = cand;
+  }
+  return (int)best;
+}
+
+namespace {
+
+std::mutex g_mu;
+struct OwnedDev {
+  void* p = nullptr;
+  ~OwnedDev() {}
+};
+std::map<std::pair<int, int>, void*> g_twiddles;             // (L, dtype) -> device table
+std::map<std::tuple<int, int, int>, void*> g_spectra;        // (P1, P2, dtype) -> spectrum
+int g_lgf_M = -1;
+double* g_lgf = nullptr;
+
+void gauss_legendre(int n, std::vector<double>& x, std::vector<double>& w) {
+  x.resize(n);
+  w.resize(n);
+  for (int i = 0; i < n; ++i) {
+    double z = cos(M_PI * (i + 0.75) / (n + 0.5));
+    for (int it = 0; it < 100; ++it) {
+      double p0 = 1.0, p1 = 0.0;
+      for (int k = 1; k <= n; ++k) {
+        double p2 = p1;
+        p1 = p0;
+        p0 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p2) / k;
+      }
+      double dp = n * (z * p0 - p1) / (z * z - 1.0);
+      double dz = p0 / dp;
+      z -= dz;
+      if (fabs(dz) < 1e-16) {
+        p0 = 1.0; p1 = 0.0;
+        for (int k = 1; k <= n; ++k) {
+          double p2 = p1;
+          p1 = p0;
+          p0 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p2) / k;
+        }
+        dp = n * (z * p0 - p1) / (z * z - 1.0);
+        x[i] = z;
+        w[i] = 2.0 / ((1.0 - z * z) * dp * dp);
+        break;
+      }
+    }
+  }
+}
+
+int twiddle_table(int L, int dtype, const void** out) {
+  auto key = std::make_pair(L, dtype);
+  auto it = g_twiddles.find(key);
+  if (it != g_twiddles.end()) {
+    *out = it->second;
+    return ILM_OK;
+  }
+  size_t esz = dtype == ILM_F64 ? 16 : 8;
+  std::vector<unsigned char> h((size_t)L * esz);
+  for (int m = 0; m < L; ++m) {
+    // exact values at the quarter points
+    double c, s;
+    long long mm = m;
+    if ((4LL * mm) % L == 0) {
+      int q = (int)((4LL * mm) / L);
+      const double cq[4] = {1.0, 0.0, -1.0, 0.0};
+      const double sq[4] = {0.0, -1.0, 0.0, 1.0};
+      c = cq[q];
+      s = sq[q];
+    } else {
+      double ang = -2.0 * M_PI * (double)m / (double)L;
+      c = cos(ang);
+      s = sin(ang);
+    }
+    if (dtype == ILM_F64) {
+      double v[2] = {c, s};
+      memcpy(&h[(size_t)m * esz], v, esz);
+    } else {
+      float v[2] = {(float)c, (float)s};
+      memcpy(&h[(size_t)m * esz], v, esz);
+    }
+  }
+  void* d = nullptr;
+  if (cudaMalloc(&d, h.size()) != cudaSuccess) {
+    set_error("cudaMalloc twiddles failed");
+    return ILM_ERR_NO_MEMORY;
+  }
+  ILM_CHECK_CUDA(cudaMemcpy(d, h.data(), h.size(), cudaMemcpyHostToDevice));
+  g_twiddles[key] = d;
+  *out = d;
+  return ILM_OK;
+}
+
+template <typename T>
+size_t rows_smem(int P1) { return (size_t)(3 * (P1 / 2) + 2) * sizeof(typename CT<T>::t); }
+
+template <typename T>
+int cols_cw(int P2) {
+  const size_t budget = 200 * 1024;
+  size_t per = (size_t)2 * (P2 + 1) * sizeof(typename CT<T>::t);
+  int cw = (int)(budget / per);
+  if (cw > 16) cw = 16;
+  if (cw < 1) cw = 1;
+  return cw;
+}
+
+template <typename T>
+int launch_prepared(const ConvJobDev* jd, int nj, const ConvLaunch& L, int mode, cudaStream_t st) {
+  size_t sm_rows = rows_smem<T>(L.maxP1);
+  size_t sm_cols = (size_t)2 * L.CW * (L.maxP2 + 1) * sizeof(typename CT<T>::t);
+  ILM_CHECK_CUDA(cudaFuncSetAttribute(k_rfft_rows<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_rows));
+  ILM_CHECK_CUDA(cudaFuncSetAttribute(k_cols<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_cols));
+  ILM_CHECK_CUDA(cudaFuncSetAttribute(k_irfft_rows<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_rows));
+  k_rfft_rows<T><<<L.rows, 256, sm_rows, st>>>(jd, nj);
+  ILM_CHECK_LAUNCH();
+  k_cols<T><<<L.cols, 256, sm_cols, st>>>(jd, nj, L.CW, mode);
+  ILM_CHECK_LAUNCH();
+  if (mode == 0) {
+    k_irfft_rows<T><<<L.rows, 256, sm_rows, st>>>(jd, nj);
+    ILM_CHECK_LAUNCH();
+  }
+  return ILM_OK;
+}
+
+template <typename T>
+int launch_conv_jobs(const std::vector<ConvJobDev>& jobs_in, int mode, cudaStream_t st, void* jobs_dev_buf) {
+  std::vector<ConvJobDev> jobs = jobs_in;
+  ConvLaunch L;
+  ILM_TRY(conv_jobs_finalize(jobs, sizeof(T) == 8 ? ILM_F64 : ILM_F32, &L));
+  ILM_CHECK_CUDA(cudaMemcpyAsync(jobs_dev_buf, jobs.data(), jobs.size() * sizeof(ConvJobDev),
+                                 cudaMemcpyHostToDevice, st));
+  return launch_prepared<T>(static_cast<const ConvJobDev*>(jobs_dev_buf), (int)jobs.size(), L, mode, st);
+}
+
+}  // namespace
+
+int lgf_table_device(int M, const double** tab, int* ld, cudaStream_t st) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (g_lgf && g_lgf_M >= M) {
+    *tab = g_lgf;
+    *ld = g_lgf_M + 1;
+    return ILM_OK;
+  }
+  // grow geometrically to limit rebuilds
+  int MM = std::max(M, g_lgf_M > 0 ? std::min(2 * g_lgf_M, 1 << 14) : M);
+  if (MM < M) MM = M;
+  std::vector<double> xg, wg;
+  gauss_legendre(24, xg, wg);
+  const int levels = 40;
+  std::vector<double> ha, hs, hw;
+  std::vector<double> edges;
+  edges.push_back(0.0);
+  for (int k = levels; k >= 0; --k) edges.push_back(M_PI * ldexp(1.0, -k));
+  for (size_t e = 0; e + 1 < edges.size(); ++e) {
+    double lo = edges[e], hi = edges[e + 1];
+    for (int i = 0; i < 24; ++i) {
+      double al = 0.5 * (hi - lo) * xg[i] + 0.5 * (hi + lo);
+      double w = 0.5 * (hi - lo) * wg[i];
+      double sh2 = sin(0.5 * al);
+      double u = 2.0 * sh2 * sh2;
+      double sh = sqrt(u * (u + 2.0));
+      double s = log1p(u + sh);
+      ha.push_back(al);
+      hs.push_back(s);
+      hw.push_back(w / sh);
+    }
+  }
+  const int nq = (int)ha.size();
+  DevBuf da, ds, dw;
+  ILM_TRY(da.alloc(nq * sizeof(double)));
+  ILM_TRY(ds.alloc(nq * sizeof(double)));
+  ILM_TRY(dw.alloc(nq * sizeof(double)));
+  ILM_CHECK_CUDA(cudaMemcpy(da.p, ha.data(), nq * sizeof(double), cudaMemcpyHostToDevice));
+  ILM_CHECK_CUDA(cudaMemcpy(ds.p, hs.data(), nq * sizeof(double), cudaMemcpyHostToDevice));
+  ILM_CHECK_CUDA(cudaMemcpy(dw.p, hw.data(), nq * sizeof(double), cudaMemcpyHostToDevice));
+  double* d = nullptr;
+  size_t bytes = (size_t)(MM + 1) * (MM + 1) * sizeof(double);
+  if (cudaMalloc(&d, bytes) != cudaSuccess) {
+    set_error("cudaMalloc LGF table (%zu bytes) failed", bytes);
+    return ILM_ERR_NO_MEMORY;
+  }
+  dim3 grid((MM + 1 + 127) / 128, MM + 1);
+  k_lgf_table<<<grid, 128, 0, st>>>(MM, da.as<double>(), ds.as<double>(), dw.as<double>(), nq, d);
+  ILM_CHECK_LAUNCH();
+  ILM_CHECK_CUDA(cudaStreamSynchronize(st));
+  if (g_lgf) cudaFree(g_lgf);
+  g_lgf = d;
+  g_lgf_M = MM;
+  *tab = g_lgf;
+  *ld = MM + 1;
+  return ILM_OK;
+}
+
+static int spectrum_device(int P1, int P2, int dtype, const void** out, cudaStream_t st) {
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto it = g_spectra.find(std::make_tuple(P1, P2, dtype));
+    if (it != g_spectra.end()) {
+      *out = it->second;
+      return ILM_OK;
+    }
+  }
+  const double* G = nullptr;
+  int ld = 0;
+  ILM_TRY(lgf_table_device(std::max(P1, P2) / 2, &G, &ld, st));
+  const void *tw1 = nullptr, *tw2 = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    ILM_TRY(twiddle_table(P1, ILM_F64, &tw1));
+    ILM_TRY(twiddle_table(P2, ILM_F64, &tw2));
+  }
+  DevBuf K, W, S64, jobsb;
+  ILM_TRY(K.alloc((size_t)P1 * P2 * sizeof(double)));
+  ILM_TRY(W.alloc((size_t)P2 * (P1 / 2 + 1) * 2 * sizeof(double)));
+  const size_t nspec = (size_t)(P1 / 2 + 1) * (P2 / 2 + 1);
+  ILM_TRY(S64.alloc(nspec * sizeof(double)));
+  ILM_TRY(jobsb.alloc(sizeof(ConvJobDev)));
+  k_circulant<<<dim3((P1 + 255) / 256, P2), 256, 0, st>>>(G, ld, P1, P2, K.as<double>());
+  ILM_CHECK_LAUNCH();
+  ConvJobDev J;
+  memset(&J, 0, sizeof(J));
+  J.in = K.p;
+  J.out = S64.p;
+  J.work = W.p;
+  J.tw1 = tw1;
+  J.tw2 = tw2;
+  J.n1 = P1;
+  J.n2 = P2;
+  J.n2out = P2;
+  J.P1 = P1;
+  J.P2 = P2;
+  // unnormalised r2c -> column FFT pair -> c2r gives a factor (P1/2) * P2
+  J.scale = 1.0 / ((double)(P1 / 2) * (double)P2);
+  std::vector<ConvJobDev> jobs{J};
+  ILM_TRY(launch_conv_jobs<double>(jobs, 1, st, jobsb.p));
+  void* d = nullptr;
+  if (dtype == ILM_F64) {
+    if (cudaMalloc(&d, nspec * sizeof(double)) != cudaSuccess) return ILM_ERR_NO_MEMORY;
+    ILM_CHECK_CUDA(cudaMemcpyAsync(d, S64.p, nspec * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  } else {
+    if (cudaMalloc(&d, nspec * sizeof(float)) != cudaSuccess) return ILM_ERR_NO_MEMORY;
+    k_d2f<<<256, 256, 0, st>>>(S64.as<double>(), static_cast<float*>(d), nspec);
+    ILM_CHECK_LAUNCH();
+  }
+  ILM_CHECK_CUDA(cudaStreamSynchronize(st));
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_spectra[std::make_tuple(P1, P2, dtype)] = d;
+  *out = d;
+  return ILM_OK;
+}
+
+int conv_plan_init(ConvPlan* plan, int n1, int n2, int dtype, cudaStream_t st) {
+  plan->n1 = n1;
+  plan->n2 = n2;
+  plan->dtype = dtype;
+  plan->P1 = good_fft_size(2 * n1 - 1);
+  plan->P2 = good_fft_size(2 * n2 - 1);
+  if (plan->P1 > 8192 || plan->P2 > 8192) {
+    set_error("grid too large for the FFT convolution (P=%d x %d)", plan->P1, plan->P2);
+    return ILM_ERR_SIZE_LIMIT;
+  }
+  ILM_TRY(spectrum_device(plan->P1, plan->P2, dtype, &plan->spec, st));
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    ILM_TRY(twiddle_table(plan->P1, dtype, &plan->tw1));
+    ILM_TRY(twiddle_table(plan->P2, dtype, &plan->tw2));
+  }
+  size_t csz = dtype == ILM_F64 ? 16 : 8;
+  ILM_TRY(plan->work.alloc((size_t)n2 * (plan->P1 / 2 + 1) * csz + 256));
+  return ILM_OK;
+}
+
+int conv_apply(ConvPlan* plan, const void* in, void* out, double inv_factor, cudaStream_t st) {
+  ConvJobDev J;
+  memset(&J, 0, sizeof(J));
+  J.in = in;
+  J.out = out;
+  J.work = plan->work.p;
+  J.spec = plan->spec;
+  J.tw1 = plan->tw1;
+  J.tw2 = plan->tw2;
+  J.n1 = plan->n1;
+  J.n2 = plan->n2;
+  J.n2out = plan->n2;
+  J.P1 = plan->P1;
+  J.P2 = plan->P2;
+  J.scale = inv_factor;
+  std::vector<ConvJobDev> jobs{J};
+  // job descriptor lives in the tail of the work buffer
+  size_t csz = plan->dtype == ILM_F64 ? 16 : 8;
+  size_t off = (size_t)plan->n2 * (plan->P1 / 2 + 1) * csz;
+  void* jb = static_cast<unsigned char*>(plan->work.p) + ((off + 15) / 16) * 16;
+  if (((off + 15) / 16) * 16 + sizeof(ConvJobDev) > plan->work.bytes) {
+    set_error("conv work buffer too small");
+    return ILM_ERR_INVALID_ARG;
+  }
+  if (plan->dtype == ILM_F64) return launch_conv_jobs<double>(jobs, 0, st, jb);
+  return launch_conv_jobs<float>(jobs, 0, st, jb);
+}
+
+int conv_jobs_finalize(std::vector<ConvJobDev>& jobs, int dtype, ConvLaunch* L) {
+  int rows = 0, cols = 0, maxP1 = 0, maxP2 = 0;
+  for (auto& J : jobs) {
+    maxP1 = std::max(maxP1, J.P1);
+    maxP2 = std::max(maxP2, J.P2);
+  }
+  const int CW = dtype == ILM_F64 ? cols_cw<double>(maxP2) : cols_cw<float>(maxP2);
+  for (auto& J : jobs) {
+    J.row_off = rows;
+    rows += J.n2;
+    J.col_off = cols;
+    cols += (J.P1 / 2 + 1 + CW - 1) / CW;
+  }
+  L->rows = rows;
+  L->cols = cols;
+  L->CW = CW;
+  L->maxP1 = maxP1;
+  L->maxP2 = maxP2;
+  return ILM_OK;
+}
+
+int conv_jobs_launch(const ConvJobDev* jobs_dev, int njobs, const ConvLaunch& L, int dtype, cudaStream_t st) {
+  if (njobs == 0) return ILM_OK;
+  if (dtype == ILM_F64) return launch_prepared<double>(jobs_dev, njobs, L, 0, st);
+  return launch_prepared<float>(jobs_dev, njobs, L, 0, st);
+}
+
+int conv_resources(int P1, int P2, int dtype, const void** spec, const void** tw1, const void** tw2, cudaStream_t st) {
+  ILM_TRY(spectrum_device(P1, P2, dtype, spec, st));
+  std::lock_guard<std::mutex> lk(g_mu);
+  ILM_TRY(twiddle_table(P1, dtype, tw1));
+  ILM_TRY(twiddle_table(P2, dtype, tw2));
+  return ILM_OK;
+}
+
+}  // namespace ilm

@@ -1,0 +1,306 @@
+// Internal declarations shared by the libilm translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "ilm.h"
+
+namespace ilm {
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+void set_error(const char* fmt, ...);
+
+#define ILM_CHECK_CUDA(expr)                                                     \
+  do {                                                                           \
+    cudaError_t _e = (expr);                                                     \
+    if (_e != cudaSuccess) {                                                     \
+      ::ilm::set_error("%s:%d %s: %s", __FILE__, __LINE__, #expr,                \
+                       cudaGetErrorString(_e));                                  \
+      return ILM_ERR_CUDA;                                                       \
+    }                                                                            \
+  } while (0)
+
+#define ILM_CHECK_LAUNCH() ILM_CHECK_CUDA(cudaGetLastError())
+
+#define ILM_TRY(expr)                 \
+  do {                                \
+    int _s = (expr);                  \
+    if (_s != ILM_OK) return _s;      \
+  } while (0)
+
+#define ILM_REQUIRE(cond, ...)                     \
+  do {                                             \
+    if (!(cond)) {                                 \
+      ::ilm::set_error(__VA_ARGS__);               \
+      return ILM_ERR_INVALID_ARG;                  \
+    }                                              \
+  } while (0)
+
+inline cudaStream_t as_stream(ilm_stream_t s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// ---------------------------------------------------------------------------
+// device buffer (RAII)
+// ---------------------------------------------------------------------------
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  int alloc(size_t nbytes) {
+    if (nbytes <= bytes && p) return ILM_OK;
+    release();
+    if (nbytes == 0) return ILM_OK;
+    cudaError_t e = cudaMalloc(&p, nbytes);
+    if (e != cudaSuccess) {
+      set_error("cudaMalloc(%zu) failed: %s", nbytes, cudaGetErrorString(e));
+      p = nullptr;
+      return ILM_ERR_NO_MEMORY;
+    }
+    bytes = nbytes;
+    return ILM_OK;
+  }
+  template <typename T> T* as() const { return static_cast<T*>(p); }
+};
+
+// ---------------------------------------------------------------------------
+// grid and staggering
+// ---------------------------------------------------------------------------
+// Position classes (dual_x, dual_y): a dual direction is offset by h/2 and
+// carries the ghost layer.
+enum PosClass { PC_P = 0, PC_D = 1, PC_U = 2, PC_V = 3 };  // (0,0) (1,1) (1,0) (0,1)
+
+inline int pc_dx(int pc) { return (pc == PC_D || pc == PC_U) ? 1 : 0; }
+inline int pc_dy(int pc) { return (pc == PC_D || pc == PC_V) ? 1 : 0; }
+
+struct Shape2 {
+  int n1, n2;
+  size_t numel() const { return (size_t)n1 * (size_t)n2; }
+};
+
+}  // namespace ilm
+
+struct ilm_grid_s {
+  int nx, ny;
+  double h;
+  int i0x, i0y;
+  ilm::Shape2 shape(int pc) const {
+    return {ilm::pc_dx(pc) ? nx : nx - 1, ilm::pc_dy(pc) ? ny : ny - 1};
+  }
+};
+
+namespace ilm {
+
+// number of components and their classes for a grid data kind
+int gridkind_components(int kind, int* pcs);  // returns ncomp, fills pcs[]
+size_t gridkind_numel(const ilm_grid_s* g, int kind);
+
+// ---------------------------------------------------------------------------
+// DDF point windows: 4 taps per direction and per 1-D offset class
+// ---------------------------------------------------------------------------
+constexpr int NTAP = 4;
+constexpr int TILE_X = 32;
+constexpr int TILE_Y = 8;
+
+// coefficient codes for fused point-wise products
+enum Coef { CF_ZERO = 0, CF_ONE = 1, CF_NX = 2, CF_NY = 3, CF_MNX = 4, CF_MNY = 5, CF_MONE = 6 };
+
+template <typename T>
+struct PointWin {
+  // [npts] base indices and [npts*4] weights for x-primal, x-dual, y-primal, y-dual
+  const int* bx[2];
+  const int* by[2];
+  const T* wx[2];
+  const T* wy[2];
+};
+
+// tile candidate list for one position class
+struct TileList {
+  DevBuf ptr;   // int [ntiles+1]
+  DevBuf pts;   // int [nnz]
+  int ntx = 0, nty = 0;
+};
+
+// ---------------------------------------------------------------------------
+// FFT convolution (inverse Laplacian)
+// ---------------------------------------------------------------------------
+struct ConvPlan {
+  int n1 = 0, n2 = 0, P1 = 0, P2 = 0, dtype = ILM_F64;
+  const void* spec = nullptr;   // (P1/2+1) x (P2/2+1) real, scaled, device (shared)
+  const void* tw1 = nullptr;    // twiddles length P1 (device, shared)
+  const void* tw2 = nullptr;    // twiddles length P2
+  DevBuf work;                  // n2 x (P1/2+1) complex
+};
+
+struct ConvJobDev {
+  const void* in;
+  void* out;
+  void* work;
+  const void* spec;
+  const void* tw1;   // length P1
+  const void* tw2;   // length P2
+  int n1, n2;        // valid input columns / rows
+  int n2out;         // rows produced by the column pass
+  int P1, P2;
+  double scale;
+  int row_off, col_off;
+};
+struct ConvLaunch {
+  int rows = 0, cols = 0, CW = 1, maxP1 = 0, maxP2 = 0;
+};
+// fill row/col offsets of a job table and the launch geometry
+int conv_jobs_finalize(std::vector<ConvJobDev>& jobs, int dtype, ConvLaunch* L);
+// launch a prepared (device-resident) job table; no host<->device traffic
+int conv_jobs_launch(const ConvJobDev* jobs_dev, int njobs, const ConvLaunch& L, int dtype, cudaStream_t st);
+// shared spectrum and twiddle tables for padded sizes P1 x P2
+int conv_resources(int P1, int P2, int dtype, const void** spec, const void** tw1, const void** tw2, cudaStream_t st);
+
+int good_fft_size(int n);
+// G(m,n) table for 0<=m,n<=M (row-major (M+1)x(M+1), FP64, device; library-owned)
+int lgf_table_device(int M, const double** tab, int* ld, cudaStream_t st);
+int conv_plan_init(ConvPlan* plan, int n1, int n2, int dtype, cudaStream_t st);
+// out = (1/factor) * G * in (linear convolution), in/out n1 x n2 (x fastest)
+int conv_apply(ConvPlan* plan, const void* in, void* out, double inv_factor, cudaStream_t st);
+
+// ---------------------------------------------------------------------------
+// kernels launchers (defined in the .cu files)
+// ---------------------------------------------------------------------------
+struct GatherTerm {
+  int pc;             // position class of the grid array
+  const void* arr;    // grid array (cache dtype)
+  int coef;           // Coef code
+};
+
+}  // namespace ilm
+
+struct ilm_cache_s {
+  ilm_grid_s grid;
+  int kind, npts, ddf, scaling, dtype;
+  double h;
+  // host copies (double)
+  std::vector<double> hx, hy, hnx, hny, hds;
+  // device point data (cache dtype) and FP64 copies used by the Schur build
+  ilm::DevBuf nx, ny, wscale;          // wscale = ds/h^2 (GridScaling) or 1
+  ilm::DevBuf ds64, nx64, ny64;        // FP64
+  ilm::DevBuf bx[2], by[2];            // int
+  ilm::DevBuf wx[2], wy[2];            // cache dtype
+  ilm::DevBuf wx64[2], wy64[2];        // FP64
+  std::vector<int> hbx[2], hby[2];
+  ilm::TileList tiles[4];
+  // inverse Laplacian plans per position class
+  ilm::ConvPlan conv[4];
+  bool conv_ready[4] = {false, false, false, false};
+  // scratch grid buffers (cache dtype)
+  ilm::DevBuf g_scr[6];
+  // scratch point buffers (FP64 and cache dtype)
+  ilm::DevBuf p_scr[8];
+  // cached Schur complements for the problem solves (FP64 and FP32 copies)
+  ilm::DevBuf S_dir64, S_dir32, S_neu64, S_neu32;
+  bool S_dir_ready = false, S_neu_ready = false;
+  ilm::DevBuf red;                     // reduction scratch (double)
+
+  template <typename T> ilm::PointWin<T> win() const {
+    ilm::PointWin<T> w;
+    for (int a = 0; a < 2; ++a) {
+      w.bx[a] = bx[a].as<int>();
+      w.by[a] = by[a].as<int>();
+      w.wx[a] = wx[a].as<T>();
+      w.wy[a] = wy[a].as<T>();
+    }
+    return w;
+  }
+};
+
+namespace ilm {
+
+// DDF / transfer launchers (ilm_ddf.cu)
+struct HostWindows {
+  std::vector<int> bx[2], by[2];         // [primal|dual] base index per point
+  std::vector<double> wx[2], wy[2];      // [primal|dual] 4 weights per point
+  std::vector<int> tptr[4], tpts[4];     // per position class: tile CSR
+  int ntx[4], nty[4];
+};
+void host_windows(const ilm_grid_s& g, int ddf, int N, const double* x, const double* y, HostWindows* W);
+int cache_build_windows(ilm_cache_s* c);
+// out_pc(cell) = sum_k w_k (a_k in1_k + b_k in2_k) phi phi ; in2 may be null
+int launch_scatter(ilm_cache_s* c, int pc, const void* in1, int coef1, const void* in2, int coef2,
+                   void* out, cudaStream_t st);
+// out_k (+)= sum_t coef_t * E_{pc_t} arr_t
+int launch_gather(ilm_cache_s* c, const GatherTerm* terms, int nterms, void* out, bool accumulate,
+                  double scale, cudaStream_t st);
+
+// stencils (ilm_stencil.cu); scale multiplies the result
+int st_div_edges(const ilm_grid_s* g, int dtype, const void* q, void* w, double scale, cudaStream_t st);
+int st_grad_nodes(const ilm_grid_s* g, int dtype, const void* w, void* q, double scale, cudaStream_t st);
+int st_curl_dual_to_edges(const ilm_grid_s* g, int dtype, const void* s, void* q, double scale, cudaStream_t st);
+int st_curl_edges_to_dual(const ilm_grid_s* g, int dtype, const void* q, void* w, double scale, cudaStream_t st);
+int st_grad_edges(const ilm_grid_s* g, int dtype, const void* q, void* t, double scale, cudaStream_t st);
+int st_div_edgegrad(const ilm_grid_s* g, int dtype, const void* t, void* q, double scale, cudaStream_t st);
+int st_laplacian(int n1, int n2, int dtype, const void* in, void* out, double scale, cudaStream_t st);
+int st_axpby(size_t n, int dtype, double a, const void* x, double b, const void* y, void* out, cudaStream_t st);
+int st_fill(size_t n, int dtype, double v, void* out, cudaStream_t st);
+int st_affine(size_t n, int dtype, double a, const void* x, double b, void* out, cudaStream_t st);
+int st_convert(size_t n, int dtype_in, const void* in, int dtype_out, void* out, cudaStream_t st);
+int st_primal_to_dual(const ilm_grid_s* g, int dtype, const void* p, void* out, cudaStream_t st);
+int st_primal_to_edges(const ilm_grid_s* g, int dtype, const void* p, void* out, cudaStream_t st);
+int st_mul(size_t n, int dtype, const void* a, void* inout, cudaStream_t st);
+int st_weighted_dot(int n1, int n2, int dx, int dy, int dtype, const void* a, const void* b,
+                    double* dres, cudaStream_t st);
+int st_point_dot(int n, int dtype, const void* a, const void* b, const double* w, double* dres,
+                 cudaStream_t st);
+
+// Schur (ilm_schur.cu)
+int schur_build(ilm_cache_s* c, int which, double scale, double* A, cudaStream_t st);
+struct CGParams {
+  const double* A64;   // n x n column-major
+  const float* A32;    // n x n column-major
+  const double* b;     // rhs
+  double* x;           // solution
+  const double* w;     // inner-product weights (ds)
+  int n;
+  int maxiter;
+  double tol;
+  int* iters;          // device out
+  double* relres;      // device out
+};
+int launch_cg_batched(const CGParams* probs_dev, int nprob, int max_n, cudaStream_t st);
+
+// batched Schur builds (one launch over all problems of a batch)
+struct SchurProbDev {
+  int kind;      // ILM_SCHUR_RTLINVR (Dirichlet) or ILM_SCHUR_CLINVCT (Neumann)
+  int n;         // points of this problem
+  int poff;      // first point in the packed point arrays
+  int tile0;     // first 16x16 pair tile of this problem
+  size_t soff;   // offset of this problem's n x n matrix
+  double invh;   // derivative scale 1/h
+};
+struct BatchWin {
+  const int* bx[2];
+  const int* by[2];
+  const double* wx64[2];
+  const double* wy64[2];
+  const double* nx64;
+  const double* ny64;
+};
+struct Functional;
+size_t functional_size();
+int schur_build_batched(int nprob, const SchurProbDev* probs_dev, int total_tiles, int Ptot, const int* pt2prob,
+                        const BatchWin& W, const double* w, Functional* F, double* Aall, int max_grid,
+                        cudaStream_t st);
+
+}  // namespace ilm

@@ -1,0 +1,441 @@
+// Staggered-grid stencils: divergence, gradient, curl (both directions),
+// 5-point Laplacian, grid interpolation for masks, and small vector kernels.
+//
+// Replaces CartesianGrids' divergence!/grad!/curl!/laplacian! as called by
+// src/grid_operators.jl:25-134 (with the 1/h GridScaling of :8-9 fused) and
+// grid_interpolate! used by the masks (src/surface_operators.jl:880-923).
+// All kernels are one thread per output cell, x fastest (coalesced), and write
+// every output cell (boundary / ghost cells receive 0), so callers never need a
+// separate fill.
+#include "ilm_internal.cuh"
+
+namespace ilm {
+
+namespace {
+
+constexpr int BX = 32, BY = 8;
+
+inline dim3 grid2(int n1, int n2) { return dim3((n1 + BX - 1) / BX, (n2 + BY - 1) / BY); }
+
+// Edges{Primal} (u: NX x (NY-1), v: (NX-1) x NY) -> Nodes{Primal} (NX-1)x(NY-1)
+template <typename T>
+__global__ void k_div_edges(int NX, int NY, const T* __restrict__ u, const T* __restrict__ v, T* __restrict__ w, T sc) {
+  const int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+  if (i >= NX - 1 || j >= NY - 1) return;
+  const T du = u[(size_t)j * NX + i + 1] - u[(size_t)j * NX + i];
+  const T dv = v[(size_t)(j + 1) * (NX - 1) + i] - v[(size_t)j * (NX - 1) + i];
+  w[(size_t)j * (NX - 1) + i] = (du + dv) * sc;
+}
+
+// Nodes{Primal} -> Edges{Primal}; faces adjacent to the ghost layer are 0
+template <typename T>
+__global__ void k_grad_u(int NX, int NY, const T* __restrict__ w, T* __restrict__ u, T sc) {
+  const int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+  if (i >= NX || j >= NY - 1) return;
+  T r = (T)0;
+  if (i >= 1 && i <= NX - 2) r = (w[(size_t)j * (NX - 1) + i] - w[(size_t)j * (NX - 1) + i - 1]) * sc;
+  u[(size_t)j * NX + i] = r;
+}
+template <typename T>
+__global__ void k_grad_v(int NX, int NY, const T* __restrict__ w, T* __restrict__ v, T sc) {
+  const int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+  if (i >= NX - 1 || j >= NY) return;
+  T r = (T)0;
+  if (j >= 1 && j <= NY - 2) r = (w[(size_t)j * (NX - 1) + i] - w[(size_t)(j - 1) * (NX - 1) + i]) * sc;
+  v[(size_t)j * (NX - 1) + i] = r;
+}
+
+// Nodes{Dual} (NX x NY) -> Edges{Primal}: u = s[j+1]-s[j], v = s[i]-s[i+1]
+template <typename T>
+__global__ void k_curl_s_u(int NX, int NY, const T* __restrict__ s, T* __restrict__ u, T sc) {
+  const int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+  if (i >= NX || j >= NY - 1) return;
+  u[(size_t)j * NX + i] = (s[(size_t)(j + 1) * NX + i] - s[(size_t)j * NX + i]) * sc;
+}
+template <typename T>
+__global__ void k_curl_s_v(int NX, int NY, const T* __restrict__ s, T* __restrict__ v, T sc) {
+  const int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+  if (i >= NX - 1 || j >= NY) return;
+  v[(size_t)j * (NX - 1) + i] = (s[(size_t)j * NX + i] - s[(size_t)j * NX + i + 1]) * sc;
+}
+
+// Edges{Primal} -> Nodes{Dual}: w = v[i]-v[i-1] - (u[j]-u[j-1]) on interior dual nodes
+template <typename T>
+__global__ void k_curl_q(int NX, int NY, const T* __restrict__ u, const T* __restrict__ v, T* __restrict__ w, T sc) {
+  const int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+  if (i >= NX || j >= NY) return;
+  T r = (T)0;
+  if (i >= 1 && i <= NX - 2 && j >= 1 && j <= NY - 2) {
+    r = (v[(size_t)j * (NX - 1) + i] - v[(size_t)j * (NX - 1) + i - 1]) -
+        (u[(size_t)j * NX + i] - u[(size_t)(j - 1) * NX + i]);
+    r *= sc;
+  }
+  w[(size_t)j * NX + i] = r;
+}
+
+// Edges{Primal} -> EdgeGradient{Primal}
+template <typename T>
+__global__ void k_grad_edges(int NX, int NY, const T* __restrict__ u, const T* __restrict__ v, T* __restrict__ dudx,
+                             T* __restrict__ dudy, T* __restrict__ dvdx, T* __restrict__ dvdy, T sc) {
+  const int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+  if (i >= NX || j >= NY) return;
+  if (i < NX - 1 && j < NY - 1) {
+    dudx[(size_t)j * (NX - 1) + i] = (u[(size_t)j * NX + i + 1] - u[(size_t)j * NX + i]) * sc;
+    dvdy[(size_t)j * (NX - 1) + i] = (v[(size_t)(j + 1) * (NX - 1) + i] - v[(size_t)j * (NX - 1) + i]) * sc;
+  }
+  T a = (T)0, b = (T)0;
+  if (i >= 1 && i <= NX - 2 && j >= 1 && j <= NY - 2) {
+    a = (u[(size_t)j * NX + i] - u[(size_t)(j - 1) * NX + i]) * sc;
+    b = (v[(size_t)j * (NX - 1) + i] - v[(size_t)j * (NX - 1) + i - 1]) * sc;
+  }
+  dudy[(size_t)j * NX + i] = a;
+  dvdx[(size_t)j * NX + i] = b;
+}
+
+// EdgeGradient{Primal} -> Edges{Primal}
+template <typename T>
+__global__ void k_div_edgegrad(int NX, int NY, const T* __restrict__ dudx, const T* __restrict__ dudy,
+                               const T* __restrict__ dvdx, const T* __restrict__ dvdy, T* __restrict__ u,
+                               T* __restrict__ v, T sc) {
+  const int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+  if (i >= NX || j >= NY) return;
+  if (j < NY - 1) {
+    T r = (T)0;
+    if (i >= 1 && i <= NX - 2)
+      r = ((dudx[(size_t)j * (NX - 1) + i] - dudx[(size_t)j * (NX - 1) + i - 1]) +
+           (dudy[(size_t)(j + 1) * NX + i] - dudy[(size_t)j * NX + i])) * sc;
+    u[(size_t)j * NX + i] = r;
+  }
+  if (i < NX - 1) {
+    T r = (T)0;
+    if (j >= 1 && j <= NY - 2)
+      r = ((dvdx[(size_t)j * NX + i + 1] - dvdx[(size_t)j * NX + i]) +
+           (dvdy[(size_t)j * (NX - 1) + i] - dvdy[(size_t)(j - 1) * (NX - 1) + i])) * sc;
+    v[(size_t)j * (NX - 1) + i] = r;
+  }
+}
+
+template <typename T>
+__global__ void k_laplacian(int n1, int n2, const T* __restrict__ a, T* __restrict__ o, T sc) {
+  const int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+  if (i >= n1 || j >= n2) return;
+  T r = (T)0;
+  if (i >= 1 && i <= n1 - 2 && j >= 1 && j <= n2 - 2) {
+    const size_t c = (size_t)j * n1 + i;
+    r = (a[c + 1] + a[c - 1] + a[c + n1] + a[c - n1] - (T)4 * a[c]) * sc;
+  }
+  o[(size_t)j * n1 + i] = r;
+}
+
+// Nodes{Primal} -> Nodes{Dual} (4-point average on interior dual nodes)
+template <typename T>
+__global__ void k_p2d(int NX, int NY, const T* __restrict__ p, T* __restrict__ o) {
+  const int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+  if (i >= NX || j >= NY) return;
+  T r = (T)0;
+  if (i >= 1 && i <= NX - 2 && j >= 1 && j <= NY - 2) {
+    const int m = NX - 1;
+    r = (T)0.25 * (p[(size_t)(j - 1) * m + i - 1] + p[(size_t)(j - 1) * m + i] + p[(size_t)j * m + i - 1] +
+                   p[(size_t)j * m + i]);
+  }
+  o[(size_t)j * NX + i] = r;
+}
+
+// Nodes{Primal} -> Edges{Primal} (2-point averages)
+template <typename T>
+__global__ void k_p2e(int NX, int NY, const T* __restrict__ p, T* __restrict__ u, T* __restrict__ v) {
+  const int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+  if (i >= NX || j >= NY) return;
+  const int m = NX - 1;
+  if (j < NY - 1) {
+    T r = (T)0;
+    if (i >= 1 && i <= NX - 2) r = (T)0.5 * (p[(size_t)j * m + i - 1] + p[(size_t)j * m + i]);
+    u[(size_t)j * NX + i] = r;
+  }
+  if (i < NX - 1) {
+    T r = (T)0;
+    if (j >= 1 && j <= NY - 2) r = (T)0.5 * (p[(size_t)(j - 1) * m + i] + p[(size_t)j * m + i]);
+    v[(size_t)j * m + i] = r;
+  }
+}
+
+template <typename T>
+__global__ void k_axpby(size_t n, T a, const T* __restrict__ x, T b, const T* __restrict__ y, T* __restrict__ o) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    T r = a * x[i];
+    if (y) r += b * y[i];
+    o[i] = r;
+  }
+}
+
+template <typename T>
+__global__ void k_affine(size_t n, T a, const T* __restrict__ x, T b, T* __restrict__ o) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    o[i] = a * x[i] + b;
+}
+
+template <typename T>
+__global__ void k_fill(size_t n, T v, T* __restrict__ o) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) o[i] = v;
+}
+
+template <typename T>
+__global__ void k_mul(size_t n, const T* __restrict__ a, T* __restrict__ o) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) o[i] *= a[i];
+}
+
+template <typename A, typename B>
+__global__ void k_convert(size_t n, const A* __restrict__ in, B* __restrict__ out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = (B)in[i];
+}
+
+// weighted grid dot: dual direction interior only, primal trapezoid.  One
+// block per row, fixed-order tree reduction -> per-row partials, then a
+// single block sums the rows in order (deterministic).
+template <typename T>
+__global__ void k_wdot_rows(int n1, int n2, int dx, int dy, const T* __restrict__ a, const T* __restrict__ b,
+                            double* __restrict__ part) {
+  __shared__ double sh[256];
+  const int j = blockIdx.x;
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n1; i += blockDim.x) {
+    double wx = 1.0;
+    if (i == 0 || i == n1 - 1) wx = dx ? 0.0 : 0.5;
+    s += wx * (double)a[(size_t)j * n1 + i] * (double)b[(size_t)j * n1 + i];
+  }
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    double wy = 1.0;
+    if (j == 0 || j == n2 - 1) wy = dy ? 0.0 : 0.5;
+    part[j] = wy * sh[0];
+  }
+}
+
+__global__ void k_sum_ordered(int n, const double* __restrict__ part, double* __restrict__ out, double scale) {
+  __shared__ double sh[256];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += part[i];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[0] = sh[0] * scale;
+}
+
+template <typename T>
+__global__ void k_pdot(int n, const T* __restrict__ a, const T* __restrict__ b, const double* __restrict__ w,
+                       double* __restrict__ out) {
+  __shared__ double sh[256];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += (w ? w[i] : 1.0) * (double)a[i] * (double)b[i];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[0] = sh[0];
+}
+
+inline int nblocks(size_t n) {
+  size_t b = (n + 255) / 256;
+  if (b > 152 * 32) b = 152 * 32;
+  if (b < 1) b = 1;
+  return (int)b;
+}
+
+}  // namespace
+
+#define DISPATCH(dtype, ...)                      \
+  do {                                            \
+    if ((dtype) == ILM_F64) {                     \
+      using T = double;                           \
+      __VA_ARGS__;                                \
+    } else {                                      \
+      using T = float;                            \
+      __VA_ARGS__;                                \
+    }                                             \
+  } while (0)
+
+int st_div_edges(const ilm_grid_s* g, int dtype, const void* q, void* w, double scale, cudaStream_t st) {
+  const int NX = g->nx, NY = g->ny;
+  DISPATCH(dtype, {
+    const T* u = static_cast<const T*>(q);
+    const T* v = u + (size_t)NX * (NY - 1);
+    k_div_edges<T><<<grid2(NX - 1, NY - 1), dim3(BX, BY), 0, st>>>(NX, NY, u, v, static_cast<T*>(w), (T)scale);
+  });
+  ILM_CHECK_LAUNCH();
+  return ILM_OK;
+}
+
+int st_grad_nodes(const ilm_grid_s* g, int dtype, const void* w, void* q, double scale, cudaStream_t st) {
+  const int NX = g->nx, NY = g->ny;
+  DISPATCH(dtype, {
+    T* u = static_cast<T*>(q);
+    T* v = u + (size_t)NX * (NY - 1);
+    k_grad_u<T><<<grid2(NX, NY - 1), dim3(BX, BY), 0, st>>>(NX, NY, static_cast<const T*>(w), u, (T)scale);
+    k_grad_v<T><<<grid2(NX - 1, NY), dim3(BX, BY), 0, st>>>(NX, NY, static_cast<const T*>(w), v, (T)scale);
+  });
+  ILM_CHECK_LAUNCH();
+  return ILM_OK;
+}
+
+int st_curl_dual_to_edges(const ilm_grid_s* g, int dtype, const void* s, void* q, double scale, cudaStream_t st) {
+  const int NX = g->nx, NY = g->ny;
+  DISPATCH(dtype, {
+    T* u = static_cast<T*>(q);
+    T* v = u + (size_t)NX * (NY - 1);
+    k_curl_s_u<T><<<grid2(NX, NY - 1), dim3(BX, BY), 0, st>>>(NX, NY, static_cast<const T*>(s), u, (T)scale);
+    k_curl_s_v<T><<<grid2(NX - 1, NY), dim3(BX, BY), 0, st>>>(NX, NY, static_cast<const T*>(s), v, (T)scale);
+  });
+  ILM_CHECK_LAUNCH();
+  return ILM_OK;
+}
+
+int st_curl_edges_to_dual(const ilm_grid_s* g, int dtype, const void* q, void* w, double scale, cudaStream_t st) {
+  const int NX = g->nx, NY = g->ny;
+  DISPATCH(dtype, {
+    const T* u = static_cast<const T*>(q);
+    const T* v = u + (size_t)NX * (NY - 1);
+    k_curl_q<T><<<grid2(NX, NY), dim3(BX, BY), 0, st>>>(NX, NY, u, v, static_cast<T*>(w), (T)scale);
+  });
+  ILM_CHECK_LAUNCH();
+  return ILM_OK;
+}
+
+int st_grad_edges(const ilm_grid_s* g, int dtype, const void* q, void* t, double scale, cudaStream_t st) {
+  const int NX = g->nx, NY = g->ny;
+  const size_t np = (size_t)(NX - 1) * (NY - 1), nd = (size_t)NX * NY;
+  DISPATCH(dtype, {
+    const T* u = static_cast<const T*>(q);
+    const T* v = u + (size_t)NX * (NY - 1);
+    T* dudx = static_cast<T*>(t);
+    T* dudy = dudx + np;
+    T* dvdx = dudy + nd;
+    T* dvdy = dvdx + nd;
+    k_grad_edges<T><<<grid2(NX, NY), dim3(BX, BY), 0, st>>>(NX, NY, u, v, dudx, dudy, dvdx, dvdy, (T)scale);
+  });
+  ILM_CHECK_LAUNCH();
+  return ILM_OK;
+}
+
+int st_div_edgegrad(const ilm_grid_s* g, int dtype, const void* t, void* q, double scale, cudaStream_t st) {
+  const int NX = g->nx, NY = g->ny;
+  const size_t np = (size_t)(NX - 1) * (NY - 1), nd = (size_t)NX * NY;
+  DISPATCH(dtype, {
+    const T* dudx = static_cast<const T*>(t);
+    const T* dudy = dudx + np;
+    const T* dvdx = dudy + nd;
+    const T* dvdy = dvdx + nd;
+    T* u = static_cast<T*>(q);
+    T* v = u + (size_t)NX * (NY - 1);
+    k_div_edgegrad<T><<<grid2(NX, NY), dim3(BX, BY), 0, st>>>(NX, NY, dudx, dudy, dvdx, dvdy, u, v, (T)scale);
+  });
+  ILM_CHECK_LAUNCH();
+  return ILM_OK;
+}
+
+int st_laplacian(int n1, int n2, int dtype, const void* in, void* out, double scale, cudaStream_t st) {
+  DISPATCH(dtype, {
+    k_laplacian<T><<<grid2(n1, n2), dim3(BX, BY), 0, st>>>(n1, n2, static_cast<const T*>(in), static_cast<T*>(out),
+                                                           (T)scale);
+  });
+  ILM_CHECK_LAUNCH();
+  return ILM_OK;
+}
+
+int st_primal_to_dual(const ilm_grid_s* g, int dtype, const void* p, void* out, cudaStream_t st) {
+  DISPATCH(dtype, {
+    k_p2d<T><<<grid2(g->nx, g->ny), dim3(BX, BY), 0, st>>>(g->nx, g->ny, static_cast<const T*>(p),
+                                                           static_cast<T*>(out));
+  });
+  ILM_CHECK_LAUNCH();
+  return ILM_OK;
+}
+
+int st_primal_to_edges(const ilm_grid_s* g, int dtype, const void* p, void* out, cudaStream_t st) {
+  DISPATCH(dtype, {
+    T* u = static_cast<T*>(out);
+    T* v = u + (size_t)g->nx * (g->ny - 1);
+    k_p2e<T><<<grid2(g->nx, g->ny), dim3(BX, BY), 0, st>>>(g->nx, g->ny, static_cast<const T*>(p), u, v);
+  });
+  ILM_CHECK_LAUNCH();
+  return ILM_OK;
+}
+
+int st_axpby(size_t n, int dtype, double a, const void* x, double b, const void* y, void* out, cudaStream_t st) {
+  if (n == 0) return ILM_OK;
+  DISPATCH(dtype, {
+    k_axpby<T><<<nblocks(n), 256, 0, st>>>(n, (T)a, static_cast<const T*>(x), (T)b, static_cast<const T*>(y),
+                                           static_cast<T*>(out));
+  });
+  ILM_CHECK_LAUNCH();
+  return ILM_OK;
+}
+
+int st_fill(size_t n, int dtype, double v, void* out, cudaStream_t st) {
+  if (n == 0) return ILM_OK;
+  DISPATCH(dtype, { k_fill<T><<<nblocks(n), 256, 0, st>>>(n, (T)v, static_cast<T*>(out)); });
+  ILM_CHECK_LAUNCH();
+  return ILM_OK;
+}
+
+int st_affine(size_t n, int dtype, double a, const void* x, double b, void* out, cudaStream_t st) {
+  if (n == 0) return ILM_OK;
+  DISPATCH(dtype, {
+    k_affine<T><<<nblocks(n), 256, 0, st>>>(n, (T)a, static_cast<const T*>(x), (T)b, static_cast<T*>(out));
+  });
+  ILM_CHECK_LAUNCH();
+  return ILM_OK;
+}
+
+int st_mul(size_t n, int dtype, const void* a, void* inout, cudaStream_t st) {
+  if (n == 0) return ILM_OK;
+  DISPATCH(dtype, { k_mul<T><<<nblocks(n), 256, 0, st>>>(n, static_cast<const T*>(a), static_cast<T*>(inout)); });
+  ILM_CHECK_LAUNCH();
+  return ILM_OK;
+}
+
+int st_convert(size_t n, int dtype_in, const void* in, int dtype_out, void* out, cudaStream_t st) {
+  if (n == 0) return ILM_OK;
+  if (dtype_in == ILM_F64 && dtype_out == ILM_F32)
+    k_convert<double, float><<<nblocks(n), 256, 0, st>>>(n, static_cast<const double*>(in), static_cast<float*>(out));
+  else if (dtype_in == ILM_F32 && dtype_out == ILM_F64)
+    k_convert<float, double><<<nblocks(n), 256, 0, st>>>(n, static_cast<const float*>(in), static_cast<double*>(out));
+  else if (dtype_in == ILM_F64)
+    k_convert<double, double><<<nblocks(n), 256, 0, st>>>(n, static_cast<const double*>(in), static_cast<double*>(out));
+  else
+    k_convert<float, float><<<nblocks(n), 256, 0, st>>>(n, static_cast<const float*>(in), static_cast<float*>(out));
+  ILM_CHECK_LAUNCH();
+  return ILM_OK;
+}
+
+int st_weighted_dot(int n1, int n2, int dx, int dy, int dtype, const void* a, const void* b, double* dres,
+                    cudaStream_t st) {
+  // dres: device buffer of at least n2 + 1 doubles; result in dres[n2]
+  DISPATCH(dtype, {
+    k_wdot_rows<T><<<n2, 256, 0, st>>>(n1, n2, dx, dy, static_cast<const T*>(a), static_cast<const T*>(b), dres);
+  });
+  ILM_CHECK_LAUNCH();
+  k_sum_ordered<<<1, 256, 0, st>>>(n2, dres, dres + n2, 1.0);
+  ILM_CHECK_LAUNCH();
+  return ILM_OK;
+}
+
+int st_point_dot(int n, int dtype, const void* a, const void* b, const double* w, double* dres, cudaStream_t st) {
+  DISPATCH(dtype, {
+    k_pdot<T><<<1, 256, 0, st>>>(n, static_cast<const T*>(a), static_cast<const T*>(b), w, dres);
+  });
+  ILM_CHECK_LAUNCH();
+  return ILM_OK;
+}
+
+}  // namespace ilm

@@ -1,0 +1,129 @@
+"""Batched Dirichlet / Neumann Poisson solves (many independent problems, each
+with its own grid and bodies) through libilm's ilm_batch_* entry points."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _lib as L
+from .bodies import as_bodylist
+from .core import _DT, _ptr, _stream_ptr
+
+DIRICHLET, NEUMANN = 0, 1
+
+
+class BatchProblemSpec:
+    """One problem of a batch: grid (n dual nodes per side, spacing h, origin
+    at the centre), bodies, kind, and its plus/minus surface data."""
+
+    def __init__(self, n, h, bodies, kind, fplus, fminus=None, ny=None):
+        self.nx = int(n)
+        self.ny = int(n if ny is None else ny)
+        self.h = float(h)
+        self.i0 = (self.nx // 2, self.ny // 2)
+        self.bl = as_bodylist(bodies)
+        self.kind = kind
+        self.fplus = np.asarray(fplus, dtype=np.float64)
+        self.fminus = np.zeros_like(self.fplus) if fminus is None else np.asarray(fminus, dtype=np.float64)
+
+    @property
+    def npts(self):
+        return len(self.bl)
+
+
+class BatchSolver:
+    """Set up (DDF windows, tile lists, FP64 Schur complements) and solve a
+    batch of problems on the device."""
+
+    def __init__(self, specs, ddftype="Yang3", dtype=torch.float32):
+        self.specs = list(specs)
+        self.dtype = dtype
+        n = len(self.specs)
+        arr = (L.BatchProblem * n)()
+        for i, s in enumerate(self.specs):
+            arr[i] = L.BatchProblem(s.nx, s.ny, s.h, s.i0[0], s.i0[1], s.npts, s.kind)
+        cat = lambda a: np.ascontiguousarray(np.concatenate([getattr(s.bl, a) for s in self.specs]), np.float64)
+        self._pts = [cat(a) for a in ("x", "y", "nx", "ny", "ds")]
+        ptrs = [a.ctypes.data_as(C.POINTER(C.c_double)) for a in self._pts]
+        h = C.c_void_p()
+        L.call("ilm_batch_create", n, arr, *ptrs, L.DDF[ddftype], _DT[dtype], C.byref(h))
+        self._h = h
+        fo = (C.c_size_t * (n + 1))()
+        po = (C.c_size_t * (n + 1))()
+        L.call("ilm_batch_layout", h, fo, po)
+        self.field_offsets = np.array(fo[:], dtype=np.int64)
+        self.point_offsets = np.array(po[:], dtype=np.int64)
+        self.nprob = n
+
+    def __del__(self):
+        try:
+            if getattr(self, "_h", None):
+                L.load().ilm_batch_destroy(self._h)
+        except Exception:
+            pass
+
+    @property
+    def total_points(self):
+        return int(self.point_offsets[-1])
+
+    @property
+    def total_cells(self):
+        return int(self.field_offsets[-1])
+
+    def surface_data(self, device="cuda"):
+        fp = np.concatenate([s.fplus for s in self.specs])
+        fm = np.concatenate([s.fminus for s in self.specs])
+        return (torch.tensor(fp, dtype=self.dtype, device=device), torch.tensor(fm, dtype=self.dtype, device=device))
+
+    def solve(self, fplus, fminus, f_out=None, s_out=None, tol=1e-8, maxiter=5000, stream=None):
+        if f_out is None:
+            f_out = torch.empty(self.total_cells, dtype=self.dtype, device="cuda")
+        if s_out is None:
+            s_out = torch.empty(self.total_points, dtype=self.dtype, device="cuda")
+        L.call("ilm_batch_solve", self._h, _ptr(fplus), _ptr(fminus), _ptr(f_out), _ptr(s_out), float(tol),
+               int(maxiter), _stream_ptr(stream))
+        return f_out, s_out
+
+    def info(self):
+        it = (C.c_int * self.nprob)()
+        rr = (C.c_double * self.nprob)()
+        L.call("ilm_batch_info", self._h, it, rr)
+        return np.array(it[:]), np.array(rr[:])
+
+    def field(self, f_out, i):
+        s = self.specs[i]
+        a, b = self.field_offsets[i], self.field_offsets[i + 1]
+        return f_out[a:b].view(s.ny - 1, s.nx - 1)
+
+    def surface(self, s_out, i):
+        return s_out[self.point_offsets[i]:self.point_offsets[i + 1]]
+
+
+STAGES = ["jump/avg", "scatter (layer)", "divergence", "LGF FFT conv (f*)", "gradient", "gather + rhs",
+          "Schur CG (FP64)", "convert", "scatter (correction)", "divergence (corr.)", "LGF FFT conv (corr.)",
+          "f = f* + corr"]
+
+
+def _profiling(self, enable=True):
+    L.call("ilm_batch_set_profiling", self._h, 1 if enable else 0)
+
+
+def _stage_times(self):
+    ms = (C.c_float * 32)()
+    n = C.c_int()
+    nl = C.c_int()
+    L.call("ilm_batch_stage_times", self._h, ms, C.byref(n), C.byref(nl))
+    return list(ms[:n.value]), nl.value
+
+
+def _stats(self):
+    st = (C.c_double * 5)()
+    L.call("ilm_batch_stats", self._h, st)
+    return dict(points=int(st[0]), cells=int(st[1]), sum_npts2=st[2], sum_fft=st[3], nprob=int(st[4]))
+
+
+BatchSolver.set_profiling = _profiling
+BatchSolver.stage_times = _stage_times
+BatchSolver.stats = _stats

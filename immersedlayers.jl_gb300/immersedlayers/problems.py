@@ -1,0 +1,139 @@
+"""Problem / system framework: the `@ilmproblem`, `construct_system`,
+`prob_cache` and `solve` layer of ImmersedLayers.jl (src/problem.jl:58-139,
+src/system.jl:18-82), with the Dirichlet and Neumann Poisson problems of the
+reference's literate tests (test/literate/problems.jl:43-298,
+test/literate/neumann.jl:70-142) solved on the device by libilm.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _lib as L
+from .core import (GridScaling, NodesPrimal, PointData, ScalarData, SurfaceScalarCache, SurfaceVectorCache,
+                   _ptr, _stream_ptr, zeros_grid, zeros_surface)
+
+
+@dataclass
+class ILMProblem:
+    """Problem specification (the constructor `@ilmproblem` generates)."""
+    g: object
+    bodies: object
+    scaling: str = GridScaling
+    ddftype: str = "Yang3"
+    dtype: torch.dtype = torch.float64
+    bc: dict = field(default_factory=dict)
+    phys_params: dict = field(default_factory=dict)
+    forcing: object = None
+    timestep_func: object = None
+    motions: object = None
+    datatype = "scalar"
+
+
+class DirichletPoissonProblem(ILMProblem):
+    datatype = "scalar"
+
+
+class NeumannPoissonProblem(ILMProblem):
+    datatype = "scalar"
+
+
+@dataclass
+class ILMSystem:
+    """`ILMSystem`: base cache + problem extra cache (src/ImmersedLayers.jl:100-110)."""
+    base_cache: object
+    extra_cache: object
+    bc: dict
+    phys_params: dict
+    forcing: object
+    motions: object
+    timestep_func: object
+    last_info: dict = field(default_factory=dict)
+
+
+def prob_cache(prob, base_cache):
+    """Extension point (src/problem.jl:129-139); the built-in problems need no
+    extra cache: their Schur complements live inside the libilm cache."""
+    return None
+
+
+def construct_system(prob: ILMProblem) -> ILMSystem:
+    mk = SurfaceScalarCache if prob.datatype == "scalar" else SurfaceVectorCache
+    base = mk(prob.bodies, prob.g, ddftype=prob.ddftype, scaling=prob.scaling, dtype=prob.dtype)
+    return ILMSystem(base, prob_cache(prob, base), prob.bc, prob.phys_params, prob.forcing, prob.motions,
+                     prob.timestep_func)
+
+
+def _as_point(v, like: PointData):
+    if isinstance(v, PointData):
+        return v.data
+    t = torch.as_tensor(np.asarray(v) if not torch.is_tensor(v) else v, dtype=like.data.dtype)
+    return t.to(like.data.device).reshape(-1)
+
+
+def prescribed_surface_jump_(dfb: PointData, sys: ILMSystem):
+    """dfb = bc["exterior"] - bc["interior"] (src/bc.jl:14-34)."""
+    if sys.base_cache.N == 0:
+        dfb.data.zero_()
+        return dfb
+    ext = _as_point(sys.bc["exterior"](sys.base_cache, sys.phys_params), dfb)
+    itr = _as_point(sys.bc["interior"](sys.base_cache, sys.phys_params), dfb)
+    dfb.data.copy_(ext - itr)
+    return dfb
+
+
+def prescribed_surface_average_(fb: PointData, sys: ILMSystem):
+    """fb = (bc["exterior"] + bc["interior"]) / 2 (src/bc.jl:36-56)."""
+    if sys.base_cache.N == 0:
+        fb.data.zero_()
+        return fb
+    ext = _as_point(sys.bc["exterior"](sys.base_cache, sys.phys_params), fb)
+    itr = _as_point(sys.bc["interior"](sys.base_cache, sys.phys_params), fb)
+    fb.data.copy_(0.5 * (ext + itr))
+    return fb
+
+
+def _sides(sys):
+    c = sys.base_cache
+    plus = zeros_surface(c)
+    minus = zeros_surface(c)
+    if c.N:
+        plus.data.copy_(_as_point(sys.bc["exterior"](c, sys.phys_params), plus))
+        minus.data.copy_(_as_point(sys.bc["interior"](c, sys.phys_params), minus))
+    return plus, minus
+
+
+def solve_dirichlet(cache, fplus: PointData, fminus: PointData, tol=1e-8, maxiter=5000, stream=None):
+    """Device Dirichlet solve; returns (f::Nodes{Primal}, s::ScalarData, info)."""
+    f = zeros_grid(cache)
+    s = zeros_surface(cache)
+    info = L.SolveInfo()
+    L.call("ilm_solve_dirichlet", cache._h, _ptr(fplus.data), _ptr(fminus.data), _ptr(f.data), _ptr(s.data),
+           float(tol), int(maxiter), C.byref(info), _stream_ptr(stream))
+    return f, s, dict(iterations=info.iterations, converged=bool(info.converged), rel_residual=info.rel_residual)
+
+
+def solve_neumann(cache, vplus: PointData, vminus: PointData, tol=1e-8, maxiter=5000, stream=None):
+    """Device Neumann solve; returns (f::Nodes{Primal}, df::ScalarData, info)."""
+    f = zeros_grid(cache)
+    df = zeros_surface(cache)
+    info = L.SolveInfo()
+    L.call("ilm_solve_neumann", cache._h, _ptr(vplus.data), _ptr(vminus.data), _ptr(f.data), _ptr(df.data),
+           float(tol), int(maxiter), C.byref(info), _stream_ptr(stream))
+    return f, df, dict(iterations=info.iterations, converged=bool(info.converged), rel_residual=info.rel_residual)
+
+
+def solve(prob: ILMProblem, sys: ILMSystem, tol=1e-8, maxiter=5000):
+    """`solve(prob, sys)` for the built-in problems (bc from `prob.bc`)."""
+    plus, minus = _sides(sys)
+    if isinstance(prob, DirichletPoissonProblem):
+        f, s, info = solve_dirichlet(sys.base_cache, plus, minus, tol, maxiter)
+    elif isinstance(prob, NeumannPoissonProblem):
+        f, s, info = solve_neumann(sys.base_cache, plus, minus, tol, maxiter)
+    else:
+        raise NotImplementedError(type(prob).__name__)
+    sys.last_info = info
+    return f, s

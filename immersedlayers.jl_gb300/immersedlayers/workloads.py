@@ -1,0 +1,91 @@
+"""Seeded synthetic workloads with the shapes and value distributions of the
+benchmark configurations (no external data set exists for this path).
+
+* plain Dirichlet: [-2,2]^2, h = 0.02, circle r = 0.5 with 157 points,
+  f_b = cos(theta) + 0.1 N(0,1) (numpy default_rng(1));
+* batched: 256 problems, n ~ U{128,192,256,384,512} dual nodes per side,
+  h = 4/n, 1-3 bodies (circles r ~ U(0.2,0.6); ellipses a ~ U(0.2,0.6),
+  a/b ~ U(1,4), angle ~ U(0,pi)) at ds = 1.4 h, non-overlapping; surface data
+  sum_{k=1..8} (a_k cos + b_k sin)(2 pi k s / l) with a_k, b_k ~ N(0, 1/k^2);
+  even problems Dirichlet, odd problems Neumann; rng seed 3 + i.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import bodies as B
+
+BATCH_SIZES = (128, 192, 256, 384, 512)
+
+
+def fourier_surface_data(bl, rng, nmodes=8):
+    """Per body: sum of nmodes arc-length Fourier modes, N(0, 1/k^2) coefficients."""
+    out = []
+    for b in bl.bodies:
+        s = b.arcs
+        ell = float(b.ds.sum())
+        f = np.zeros(len(b))
+        for k in range(1, nmodes + 1):
+            a, c = rng.normal(0.0, 1.0 / k, size=2)
+            f += a * np.cos(2 * math.pi * k * s / ell) + c * np.sin(2 * math.pi * k * s / ell)
+        out.append(f)
+    return np.concatenate(out)
+
+
+def random_bodies(rng, h, nbody, lim=1.25, margin_cells=6):
+    """1-3 non-overlapping circles/ellipses inside [-lim, lim]^2."""
+    placed = []
+    bl = B.BodyList()
+    tries = 0
+    while len(placed) < nbody and tries < 2000:
+        tries += 1
+        if rng.random() < 0.5:
+            r = rng.uniform(0.2, 0.6)
+            a = b = r
+            ang = 0.0
+        else:
+            a = rng.uniform(0.2, 0.6)
+            b = a / rng.uniform(1.0, 4.0)
+            ang = rng.uniform(0.0, math.pi)
+        R = max(a, b)
+        c = rng.uniform(-lim + R, lim - R, size=2)
+        if any(np.hypot(*(c - q)) < R + Rq + margin_cells * h for q, Rq in placed):
+            continue
+        placed.append((c, R))
+        if a == b:
+            bl.append(B.circle(a, ds=1.4 * h, center=tuple(c)))
+        else:
+            bl.append(B.ellipse(a, b, ds=1.4 * h, center=tuple(c), angle=ang))
+    return bl
+
+
+def batch_problem(i, sizes=BATCH_SIZES):
+    """Problem i of the batched configuration: (n, h, bodylist, kind, fplus)."""
+    rng = np.random.default_rng(3 + i)
+    n = int(sizes[rng.integers(len(sizes))])
+    h = 4.0 / n
+    nbody = int(rng.integers(1, 4))
+    bl = random_bodies(rng, h, nbody)
+    f = fourier_surface_data(bl, rng)
+    kind = 0 if i % 2 == 0 else 1
+    return n, h, bl, kind, f
+
+
+def batch_specs(nprob=256, sizes=BATCH_SIZES):
+    from .batch import BatchProblemSpec
+    specs = []
+    for i in range(nprob):
+        n, h, bl, kind, f = batch_problem(i, sizes)
+        specs.append(BatchProblemSpec(n, h, bl, kind, f))
+    return specs
+
+
+def dirichlet_plain():
+    """Plain Dirichlet configuration: grid limits, h, body, surface data."""
+    h = 0.02
+    b = B.circle(0.5, n=157)
+    th = np.arctan2(b.y, b.x)
+    fb = np.cos(th) + 0.1 * np.random.default_rng(1).standard_normal(len(b))
+    return (-2.0, 2.0), (-2.0, 2.0), h, b, fb

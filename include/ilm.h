@@ -1,0 +1,251 @@
+/*
+ * ilm.h -- C ABI of the GB300 (sm_103a) immersed-layer library (libilm.so).
+ *
+ * Drop-in boundary for the hot path of ImmersedLayers.jl v0.5.6.  The reference
+ * has no FFI of its own: its operators are Julia generic functions of the form
+ * `op!(out, in, cache)` that mutate `out` (src/surface_operators.jl,
+ * src/grid_operators.jl).  Each entry point below replaces one such method; the
+ * citation beside it names the reference method it stands in for.  A Julia
+ * `ccall` shim (and the Python ctypes mirror shipped with this library) binds
+ * these symbols one-to-one.
+ *
+ * Conventions
+ *  - Every function returns an int status (ilm_status_t); ILM_OK == 0.  The
+ *    message of the last failure on the calling thread is ilm_last_error().
+ *  - Grid and surface arrays passed to operators are DEVICE pointers of the
+ *    cache's dtype (ILM_F64 -> double, ILM_F32 -> float).  Setup functions take
+ *    HOST arrays of double.
+ *  - Memory layout follows the reference (column-major, first index x):
+ *      Nodes{Primal}      (NX-1) x (NY-1), x fastest
+ *      Nodes{Dual}        NX x NY
+ *      Edges{Primal}      u block NX x (NY-1), then v block (NX-1) x NY
+ *      Edges{Dual}        u block (NX-1) x NY, then v block NX x (NY-1)
+ *      EdgeGradient{Primal} dudx (NX-1)x(NY-1), dudy NXxNY, dvdx NXxNY,
+ *                         dvdy (NX-1)x(NY-1), concatenated
+ *      ScalarData N, VectorData [u;v] 2N, TensorData [dudx;dudy;dvdx;dvdy] 4N
+ *  - `stream` is a cudaStream_t (NULL = legacy default stream).  Calls on one
+ *    cache must be serialised by the caller (the cache owns scratch buffers,
+ *    like the reference's non-reentrant BasicILMCache).
+ */
+#ifndef ILM_H
+#define ILM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define ILM_API __attribute__((visibility("default")))
+#else
+#define ILM_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  ILM_OK = 0,
+  ILM_ERR_INVALID_ARG = 1,
+  ILM_ERR_CUDA = 2,
+  ILM_ERR_NO_MEMORY = 3,
+  ILM_ERR_NOT_CONVERGED = 4,
+  ILM_ERR_TIMEOUT = 5,
+  ILM_ERR_UNSUPPORTED = 6,
+  ILM_ERR_SIZE_LIMIT = 7
+} ilm_status_t;
+
+typedef enum { ILM_F64 = 0, ILM_F32 = 1 } ilm_dtype_t;
+
+/* Discrete delta functions (CartesianGrids Yang3 / Roma / M4prime / Witchhat / M3). */
+typedef enum {
+  ILM_DDF_YANG3 = 0, ILM_DDF_ROMA = 1, ILM_DDF_M4PRIME = 2, ILM_DDF_WITCHHAT = 3, ILM_DDF_M3 = 4
+} ilm_ddf_t;
+
+/* src/ImmersedLayers.jl:81-83 (GridScaling default for problems) */
+typedef enum { ILM_GRID_SCALING = 0, ILM_INDEX_SCALING = 1 } ilm_scaling_t;
+
+/* SurfaceScalarCache / SurfaceVectorCache (src/cache.jl:164-202) */
+typedef enum { ILM_CACHE_SCALAR = 0, ILM_CACHE_VECTOR = 1 } ilm_cache_kind_t;
+
+/* CartesianGrids grid data types */
+typedef enum {
+  ILM_NODES_PRIMAL = 0, ILM_NODES_DUAL = 1, ILM_EDGES_PRIMAL = 2, ILM_EDGES_DUAL = 3,
+  ILM_EDGEGRAD_PRIMAL = 4
+} ilm_gridkind_t;
+
+/* Surface point data types */
+typedef enum { ILM_SCALAR_DATA = 0, ILM_VECTOR_DATA = 1, ILM_TENSOR_DATA = 2 } ilm_pointkind_t;
+
+/* Dense Schur-complement builders (src/matrix_operators.jl) */
+typedef enum {
+  ILM_SCHUR_RTLINVR = 0,   /* create_RTLinvR        :9-30    -R^T L^-1 R        */
+  ILM_SCHUR_CLINVCT = 1,   /* create_CLinvCT        :40-61   -C_s L^-1 C_s^T    */
+  ILM_SCHUR_GLINVD = 2,    /* create_GLinvD         :135-155 -G_s L^-1 D_s      */
+  ILM_SCHUR_NRTRN = 3      /* create_nRTRn          :225-244  n.R_f^T R_f n o   */
+} ilm_schur_kind_t;
+
+typedef struct ilm_grid_s* ilm_grid_t;
+typedef struct ilm_cache_s* ilm_cache_t;
+typedef void* ilm_stream_t; /* cudaStream_t */
+
+/* Result of an iterative Schur solve. */
+typedef struct {
+  int iterations;          /* Krylov iterations taken                          */
+  int converged;           /* 1 if rel. residual <= tol                        */
+  double rel_residual;     /* ||b - S s||_2 / ||b||_2, evaluated in FP64       */
+} ilm_solve_info_t;
+
+/* ---- library ----------------------------------------------------------- */
+ILM_API int ilm_version(void);
+ILM_API const char* ilm_status_string(int status);
+ILM_API const char* ilm_last_error(void);
+
+/* ---- grid: PhysicalGrid (CartesianGrids; printed in examples/caches.ipynb) */
+/* nx, ny: number of dual nodes (ghosts included); i0x, i0y: 1-based index of
+ * the origin (primal node i sits at x = (i - i0x) h).                       */
+ILM_API int ilm_grid_create(int nx, int ny, double h, int i0x, int i0y, ilm_grid_t* out);
+ILM_API int ilm_grid_destroy(ilm_grid_t g);
+/* Number of elements of one grid data kind (all components). */
+ILM_API int ilm_grid_numel(ilm_grid_t g, int kind, size_t* numel);
+
+/* ---- cache: SurfaceScalarCache/SurfaceVectorCache (src/cache.jl:209-261) */
+/* x, y: point coordinates; nrmx, nrmy: outward normals; ds: panel areas
+ * (src/tools.jl:16-38).  All host arrays of length npts.                    */
+ILM_API int ilm_cache_create(ilm_grid_t g, int kind, int npts,
+                     const double* x, const double* y,
+                     const double* nrmx, const double* nrmy, const double* ds,
+                     int ddf, int scaling, int dtype, ilm_cache_t* out);
+ILM_API int ilm_cache_destroy(ilm_cache_t c);
+ILM_API int ilm_cache_npts(ilm_cache_t c, int* npts);
+
+/* ---- point <-> grid transfers (src/surface_operators.jl:13-88) --------- */
+/* regularize!(s::Nodes{Primal|Dual}, f::ScalarData) (:13,:25) and
+ * regularize!(v::Edges{Primal}, vb::VectorData) (:36); output overwritten.  */
+ILM_API int ilm_regularize(ilm_cache_t c, int out_kind, const void* f, void* out, ilm_stream_t stream);
+/* interpolate!(f, s::Nodes{Primal|Dual}) (:56,:67), interpolate!(vb, v::Edges{Primal}) (:78) */
+ILM_API int ilm_interpolate(ilm_cache_t c, int in_kind, const void* grid_in, void* f_out, ilm_stream_t stream);
+
+/* regularize_normal!(q::Edges{Primal}, f::ScalarData) (:98-103) and
+ * regularize_normal!(qt::EdgeGradient{Primal}, v::VectorData) (:113-123)    */
+ILM_API int ilm_regularize_normal(ilm_cache_t c, const void* f, void* out, ilm_stream_t stream);
+/* regularize_normal_symm!(qt::EdgeGradient{Primal}, v::VectorData) (:125-133) */
+ILM_API int ilm_regularize_normal_symm(ilm_cache_t c, const void* v, void* out, ilm_stream_t stream);
+/* regularize_normal_cross!(q::Edges{Primal}, f::ScalarData) (:150-165) and
+ * regularize_normal_cross!(w::Nodes{Dual}, vs::VectorData) (:167-178)       */
+ILM_API int ilm_regularize_normal_cross(ilm_cache_t c, int out_kind, const void* in, void* out, ilm_stream_t stream);
+/* regularize_normal_dot!(f::Nodes{Primal}, vs::VectorData) (:188-203) and
+ * regularize_normal_dot!(v::Edges{Primal}, taus::TensorData) (:205-215)     */
+ILM_API int ilm_regularize_normal_dot(ilm_cache_t c, int out_kind, const void* in, void* out, ilm_stream_t stream);
+/* normal_interpolate!(vn, q::Edges{Primal}) (:228-240),
+ * normal_interpolate!(tau::VectorData, A::EdgeGradient{Primal}) (:242-250)  */
+ILM_API int ilm_normal_interpolate(ilm_cache_t c, const void* grid_in, void* out, ilm_stream_t stream);
+/* normal_interpolate_symm!(tau, A::EdgeGradient{Primal}) (:252-283)        */
+ILM_API int ilm_normal_interpolate_symm(ilm_cache_t c, const void* grid_in, void* out, ilm_stream_t stream);
+/* normal_cross_interpolate!(wn, v::Edges{Primal}) (:277-295),
+ * normal_cross_interpolate!(vs::VectorData, s::Nodes{Dual}) (:298-307)      */
+ILM_API int ilm_normal_cross_interpolate(ilm_cache_t c, int in_kind, const void* grid_in, void* out, ilm_stream_t stream);
+/* normal_dot_interpolate!(vs, f::Nodes{Primal}) (:316-330),
+ * normal_dot_interpolate!(taus::TensorData, v::Edges{Primal}) (:332-343)   */
+ILM_API int ilm_normal_dot_interpolate(ilm_cache_t c, int in_kind, const void* grid_in, void* out, ilm_stream_t stream);
+
+/* ---- composite layer operators (src/surface_operators.jl:357-725) ------- */
+/* direction: 0 = surface -> grid (e.g. surface_divergence!(theta, f)),
+ *            1 = grid -> surface (e.g. surface_grad!(vn, phi)).             */
+ILM_API int ilm_surface_divergence(ilm_cache_t c, const void* in, void* out, ilm_stream_t stream);      /* :530-591 */
+ILM_API int ilm_surface_divergence_symm(ilm_cache_t c, const void* in, void* out, ilm_stream_t stream); /* :574-591 */
+ILM_API int ilm_surface_grad(ilm_cache_t c, const void* in, void* out, ilm_stream_t stream);            /* :604-664 */
+ILM_API int ilm_surface_grad_symm(ilm_cache_t c, const void* in, void* out, ilm_stream_t stream);       /* :650-664 */
+ILM_API int ilm_surface_curl(ilm_cache_t c, int direction, int point_kind, const void* in, void* out, ilm_stream_t stream); /* :357-452 */
+ILM_API int ilm_surface_curl_cross(ilm_cache_t c, int direction, const void* in, void* out, ilm_stream_t stream);          /* :467-515 */
+ILM_API int ilm_surface_divergence_cross(ilm_cache_t c, const void* in, void* out, ilm_stream_t stream);/* :679-690 */
+ILM_API int ilm_surface_grad_cross(ilm_cache_t c, const void* in, void* out, ilm_stream_t stream);      /* :704-725 */
+
+/* ---- grid operators (src/grid_operators.jl:17-179) ---------------------- */
+/* divergence!(p::Nodes{Primal}, v::Edges{Primal}) (:25-31) and
+ * divergence!(v::Edges{Primal}, A::EdgeGradient{Primal}); scaled by 1/h
+ * under GridScaling.  in_kind names the input type.                        */
+ILM_API int ilm_divergence(ilm_cache_t c, int in_kind, const void* in, void* out, ilm_stream_t stream);
+/* grad!(v::Edges{Primal}, p::Nodes{Primal}) (:45-52), grad!(A::EdgeGradient{Primal}, v::Edges{Primal}) (:61-67) */
+ILM_API int ilm_grad(ilm_cache_t c, int in_kind, const void* in, void* out, ilm_stream_t stream);
+/* curl!(v::Edges{Primal}, s::Nodes{Dual}) (:79-85), curl!(w::Nodes{Dual}, v::Edges{Primal}) (:97-103) */
+ILM_API int ilm_curl(ilm_cache_t c, int in_kind, const void* in, void* out, ilm_stream_t stream);
+/* laplacian!(w, s) (:123-134): 5-point Laplacian, interior points, x 1/h^2 */
+ILM_API int ilm_laplacian(ilm_cache_t c, int kind, const void* in, void* out, ilm_stream_t stream);
+/* inverse_laplacian!(sol, rhs) (:153-179): unbounded-domain L^-1 via the
+ * lattice Green's function (FFT convolution).  in may equal out.           */
+ILM_API int ilm_inverse_laplacian(ilm_cache_t c, int kind, const void* in, void* out, ilm_stream_t stream);
+/* mask(cache) / complementary_mask(cache) (:737-760, :856-871) evaluated on
+ * grid data of `kind` (the basic type, or Nodes{Dual} / Edges{Primal} via the
+ * grid interpolation of mask! (:880-923)); scalar caches.                    */
+ILM_API int ilm_mask(ilm_cache_t c, int kind, int complementary, void* out, ilm_stream_t stream);
+
+/* ---- inner products (src/tools.jl:101-236, src/cache.jl:815-909) -------- */
+/* dot(u1, u2, cache) for grid data of kind `kind` (cell-volume weighted). */
+ILM_API int ilm_dot_grid(ilm_cache_t c, int kind, const void* a, const void* b, double* result, ilm_stream_t stream);
+/* dot(u1, u2, cache) for point data with `ncomp` components (ds weighted). */
+ILM_API int ilm_dot_surface(ilm_cache_t c, int ncomp, const void* a, const void* b, double* result, ilm_stream_t stream);
+
+/* ---- Schur complements (src/matrix_operators.jl:9-244) ------------------ */
+/* Dense N x N (column-major, FP64, device) Schur complement, built on the
+ * GPU directly from lattice-Green's-function point-point sums instead of the
+ * reference's N operator applications.  A_dev must hold N*N doubles.        */
+ILM_API int ilm_schur_build(ilm_cache_t c, int which, double scale, double* A_dev, ilm_stream_t stream);
+
+/* ---- problem solves (test/literate/problems.jl:259-298, neumann.jl:101-142) */
+/* Dirichlet Poisson: inputs fplus/fminus (ScalarData, device, cache dtype);
+ * outputs f (Nodes{Primal}) and s (ScalarData).  The Schur system is solved
+ * by CG on the device to rel. residual `tol` (FP64).                        */
+ILM_API int ilm_solve_dirichlet(ilm_cache_t c, const void* fplus, const void* fminus,
+                        void* f_out, void* s_out, double tol, int maxiter,
+                        ilm_solve_info_t* info, ilm_stream_t stream);
+/* Neumann Poisson: outputs f (Nodes{Primal}) and df = [phi] (ScalarData). */
+ILM_API int ilm_solve_neumann(ilm_cache_t c, const void* vplus, const void* vminus,
+                      void* f_out, void* df_out, double tol, int maxiter,
+                      ilm_solve_info_t* info, ilm_stream_t stream);
+
+/* ---- batched problem solves (configs of many independent problems) ------ */
+/* Many independent Dirichlet/Neumann Poisson problems (each its own grid and
+ * bodies) set up and solved together: every stage of the block-LU solve of
+ * test/literate/problems.jl:259-298 / neumann.jl:101-127 is one launch for the
+ * whole batch, and the dense LU per problem is replaced by device CG on the
+ * LGF-assembled Schur complement.  GridScaling.                             */
+typedef struct ilm_batch_s* ilm_batch_t;
+typedef struct {
+  int nx, ny;      /* dual nodes of this problem's grid                    */
+  double h;        /* cell size                                            */
+  int i0x, i0y;    /* 1-based origin index                                 */
+  int npts;        /* surface points of this problem                       */
+  int kind;        /* 0 = Dirichlet, 1 = Neumann                           */
+} ilm_batch_problem_t;
+/* x, y, nrmx, nrmy, ds: host arrays of all problems' points, concatenated in
+ * problem order.  dtype: precision of the grid-side work (the Schur CG is
+ * always FP64).  Builds DDF windows, tile lists and the Schur complements.  */
+ILM_API int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* x, const double* y,
+                             const double* nrmx, const double* nrmy, const double* ds, int ddf, int dtype,
+                             ilm_batch_t* out);
+ILM_API int ilm_batch_destroy(ilm_batch_t b);
+/* Offsets (nprob+1 each, in elements) of each problem's Nodes{Primal} field
+ * in the packed field array and of its points in the packed point arrays.  */
+ILM_API int ilm_batch_layout(ilm_batch_t b, size_t* field_offsets, size_t* point_offsets);
+/* fplus/fminus: packed surface data (device, batch dtype).  f_out: packed
+ * Nodes{Primal} fields; s_out: packed surface strengths.  Issues no
+ * host<->device copies (capturable in a CUDA graph once tol/maxiter are set). */
+ILM_API int ilm_batch_solve(ilm_batch_t b, const void* fplus, const void* fminus, void* f_out, void* s_out,
+                            double tol, int maxiter, ilm_stream_t stream);
+/* Stage timing: when enabled, ilm_batch_solve records a CUDA event on its
+ * stream at each stage boundary; ilm_batch_stage_times returns the elapsed
+ * ms per stage (up to 31), the number of stages and the number of kernel
+ * launches the last solve issued.  ilm_batch_stats returns 5 doubles: total
+ * points, total Nodes{Primal} cells, sum of npts^2, sum of padded FFT sizes
+ * P1*P2, number of problems.                                                */
+ILM_API int ilm_batch_set_profiling(ilm_batch_t b, int enable);
+ILM_API int ilm_batch_stage_times(ilm_batch_t b, float* ms, int* nstages, int* launches);
+ILM_API int ilm_batch_stats(ilm_batch_t b, double* stats);
+/* Per-problem CG iterations and FP64 relative residuals of the last solve. */
+ILM_API int ilm_batch_info(ilm_batch_t b, int* iterations, double* rel_residual);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ILM_H */

@@ -1,0 +1,798 @@
+"""CPU FP64 oracle for the immersed-layer hot path -- TEST INFRASTRUCTURE ONLY.
+
+This module restates, in NumPy/SciPy FP64, the algorithms that ImmersedLayers.jl
+(v0.5.6) runs on its hot path, so that the CUDA product path can be checked
+against it.  It is imported only by ``tests/``, by ``__graft_entry__.smoke()``
+and by the ``cpu_baseline`` / ``--impl reference`` legs of ``bench.py``; the
+product path never routes through it.
+
+The reference's arithmetic lives in three un-vendored Julia packages
+(CartesianGrids.jl 0.1.29/0.2, RigidBodyTools.jl 0.5.6, ConstrainedSystems.jl
+0.3.8, pinned in Project.toml:20-30).  Their published algorithms are restated
+here from first principles:
+
+* staggered-grid conventions (array extents, node positions, ghost layers) are
+  inferred from the printed cache/grid objects in examples/caches.ipynb
+  (PhysicalGrid((-2,2),(-2,2),0.01) -> size (406,406), I0=(203,203),
+  Nodes{Primal} 405x405 with x from -2.02 to 2.02, Nodes{Dual} 406x406);
+* discrete delta functions from their papers (Yang et al. 2009 smoothed
+  3-point "Yang3"; Roma, Peskin & Berger 1999; Monaghan M4'; hat; M3);
+* the lattice Green's function of the 5-point Laplacian from its integral
+  representation (normalised G(0,0)=0, so G(1,0)=1/4, G(1,1)=1/pi);
+* the composite layer operators, Schur-complement builders and block-LU solves
+  follow src/surface_operators.jl, src/matrix_operators.jl,
+  test/literate/problems.jl and test/literate/neumann.jl line by line.
+
+Parity is pinned against the reference's own known-answer tests
+(test/tools.jl:107-120, test/surface_ops.jl:63-77,127-146,180-256) and the
+notebook outputs; absolute grid offsets, the LGF constant and the IF-HERK
+tableau are "parity unpinned" (the reference's Julia path cannot run here).
+
+Grid data are numpy arrays of shape (n1, n2) indexed [i, j] with i along x
+(the reference's column-major, first-index-x layout).  Vector grid data are
+tuples of component arrays.  Point data are flat arrays like the reference's
+ScalarData (N), VectorData ([u; v], 2N) and TensorData
+([dudx; dudy; dvdx; dvdy], 4N).
+"""
+from __future__ import annotations
+
+import math
+import os
+from dataclasses import dataclass
+
+import numpy as np
+import scipy.fft as sfft
+import scipy.sparse as sp
+
+EULER_GAMMA = 0.57721566490153286060651209
+
+# ---------------------------------------------------------------------------
+# Discrete delta functions (1-D kernels in index units, sum_j phi(r-j) = 1)
+# ---------------------------------------------------------------------------
+
+
+def ddf_yang3(r):
+    """Smoothed 3-point kernel of Yang, Zhang, Li & Yang (JCP 228, 2009),
+    the reference default (src/ImmersedLayers.jl:83, DEFAULT_DDF = Yang3)."""
+    r = np.abs(np.asarray(r, dtype=np.float64))
+    out = np.zeros_like(r)
+    s3 = math.sqrt(3.0)
+    m1 = r <= 1.0
+    r1 = r[m1]
+    out[m1] = (17.0 / 48.0 + s3 * math.pi / 108.0 + r1 / 4.0 - r1 * r1 / 4.0
+               + (1.0 - 2.0 * r1) / 16.0 * np.sqrt(np.maximum(-12.0 * r1 * r1 + 12.0 * r1 + 1.0, 0.0))
+               - s3 / 12.0 * np.arcsin(s3 / 2.0 * (2.0 * r1 - 1.0)))
+    m2 = (r > 1.0) & (r < 2.0)
+    r2 = r[m2]
+    out[m2] = (55.0 / 48.0 - s3 * math.pi / 108.0 - 13.0 * r2 / 12.0 + r2 * r2 / 4.0
+               + (2.0 * r2 - 3.0) / 48.0 * np.sqrt(np.maximum(-12.0 * r2 * r2 + 36.0 * r2 - 23.0, 0.0))
+               + s3 / 36.0 * np.arcsin(s3 / 2.0 * (2.0 * r2 - 3.0)))
+    return out
+
+
+def ddf_roma(r):
+    """3-point kernel of Roma, Peskin & Berger (JCP 153, 1999)."""
+    r = np.abs(np.asarray(r, dtype=np.float64))
+    out = np.zeros_like(r)
+    m1 = r <= 0.5
+    out[m1] = (1.0 + np.sqrt(1.0 - 3.0 * r[m1] ** 2)) / 3.0
+    m2 = (r > 0.5) & (r < 1.5)
+    out[m2] = (5.0 - 3.0 * r[m2] - np.sqrt(np.maximum(1.0 - 3.0 * (1.0 - r[m2]) ** 2, 0.0))) / 6.0
+    return out
+
+
+def ddf_m4prime(r):
+    """Monaghan's M4' kernel (cubic, interpolating, 4-point support)."""
+    r = np.abs(np.asarray(r, dtype=np.float64))
+    out = np.zeros_like(r)
+    m1 = r <= 1.0
+    out[m1] = 1.0 - 2.5 * r[m1] ** 2 + 1.5 * r[m1] ** 3
+    m2 = (r > 1.0) & (r < 2.0)
+    out[m2] = 0.5 * (2.0 - r[m2]) ** 2 * (1.0 - r[m2])
+    return out
+
+
+def ddf_witchhat(r):
+    """Linear hat kernel (2-point support)."""
+    r = np.abs(np.asarray(r, dtype=np.float64))
+    return np.where(r < 1.0, 1.0 - r, 0.0)
+
+
+def ddf_m3(r):
+    """Quadratic B-spline M3 kernel (3-point support)."""
+    r = np.abs(np.asarray(r, dtype=np.float64))
+    out = np.zeros_like(r)
+    m1 = r <= 0.5
+    out[m1] = 0.75 - r[m1] ** 2
+    m2 = (r > 0.5) & (r < 1.5)
+    out[m2] = 0.5 * (1.5 - r[m2]) ** 2
+    return out
+
+
+# name -> (kernel, half-support radius in cells)
+DDFS = {
+    "Yang3": (ddf_yang3, 2.0),
+    "Roma": (ddf_roma, 1.5),
+    "M4prime": (ddf_m4prime, 2.0),
+    "Witchhat": (ddf_witchhat, 1.0),
+    "M3": (ddf_m3, 1.5),
+}
+
+# ---------------------------------------------------------------------------
+# Grid
+# ---------------------------------------------------------------------------
+
+# Position classes: (dual_x, dual_y); 1 = half-cell offset ("dual" direction)
+NODES_PRIMAL = (0, 0)
+NODES_DUAL = (1, 1)
+EDGES_PRIMAL_U = (1, 0)   # Edges{Primal}.u  (also Edges{Dual}.v)
+EDGES_PRIMAL_V = (0, 1)   # Edges{Primal}.v  (also Edges{Dual}.u)
+
+
+@dataclass
+class Grid:
+    """PhysicalGrid restatement: NX x NY dual nodes (ghosts included), origin
+    index I0 (1-based, as printed by the reference), spacing h.
+
+    Node positions (1-based index i): primal x = (i - I0) h, i = 1..NX-1;
+    dual x = (i - I0 - 1/2) h, i = 1..NX.
+    """
+    nx: int
+    ny: int
+    h: float
+    i0x: int
+    i0y: int
+
+    @classmethod
+    def physical(cls, xlim, ylim, h):
+        """Grid covering xlim x ylim with two cells of padding on each side
+        (the (406,406)/(203,203) sizing printed in examples/caches.ipynb)."""
+        def one(lim):
+            nl = int(math.ceil(-lim[0] / h - 1e-12))
+            nr = int(math.ceil(lim[1] / h - 1e-12))
+            n = nl + nr + 2 * 2 + 2
+            i0 = nl + 2 + 1
+            return n, i0
+        nx, i0x = one(xlim)
+        ny, i0y = one(ylim)
+        return cls(nx, ny, float(h), i0x, i0y)
+
+    @classmethod
+    def centered(cls, n, h, ny=None):
+        """n x ny dual-node grid with the origin at its centre (used for the
+        grids given by cell count)."""
+        ny = n if ny is None else ny
+        return cls(n, ny, float(h), n // 2, ny // 2)
+
+    def shape(self, cls_):
+        dx, dy = cls_
+        return (self.nx if dx else self.nx - 1, self.ny if dy else self.ny - 1)
+
+    def coords(self, cls_):
+        dx, dy = cls_
+        n1, n2 = self.shape(cls_)
+        x = (np.arange(1, n1 + 1) - self.i0x - 0.5 * dx) * self.h
+        y = (np.arange(1, n2 + 1) - self.i0y - 0.5 * dy) * self.h
+        return x, y
+
+    def limits(self):
+        return ((1 - self.i0x) * self.h, (self.nx - 1 - self.i0x) * self.h), \
+               ((1 - self.i0y) * self.h, (self.ny - 1 - self.i0y) * self.h)
+
+
+def zeros(g: Grid, kind):
+    """kind: 'nodes_primal' | 'nodes_dual' | 'edges_primal' | 'edgegrad_primal'."""
+    if kind == "nodes_primal":
+        return np.zeros(g.shape(NODES_PRIMAL))
+    if kind == "nodes_dual":
+        return np.zeros(g.shape(NODES_DUAL))
+    if kind == "edges_primal":
+        return (np.zeros(g.shape(EDGES_PRIMAL_U)), np.zeros(g.shape(EDGES_PRIMAL_V)))
+    if kind == "edgegrad_primal":
+        return (np.zeros(g.shape(NODES_PRIMAL)), np.zeros(g.shape(NODES_DUAL)),
+                np.zeros(g.shape(NODES_DUAL)), np.zeros(g.shape(NODES_PRIMAL)))
+    raise ValueError(kind)
+
+
+# ---------------------------------------------------------------------------
+# Weighted inner products (src/tools.jl:101-236 on top of CartesianGrids' dot)
+# ---------------------------------------------------------------------------
+
+def _axis_weights(n, dual):
+    """Dual direction: ghosts at both ends excluded; primal: trapezoid."""
+    w = np.ones(n)
+    if dual:
+        w[0] = 0.0
+        w[-1] = 0.0
+    else:
+        w[0] = 0.5
+        w[-1] = 0.5
+    return w
+
+
+def grid_dot_array(a, b, cls_, h):
+    wx = _axis_weights(a.shape[0], cls_[0])
+    wy = _axis_weights(a.shape[1], cls_[1])
+    return float(np.einsum("ij,ij,i,j->", a, b, wx, wy)) * h * h
+
+
+# ---------------------------------------------------------------------------
+# Lattice Green's function of the 5-point Laplacian
+# ---------------------------------------------------------------------------
+
+def _lgf_nodes(levels=40, npts=24):
+    """Composite Gauss-Legendre nodes on [0, pi], dyadically graded towards 0."""
+    xg, wg = np.polynomial.legendre.leggauss(npts)
+    edges = [math.pi * 2.0 ** (-k) for k in range(levels, -1, -1)]
+    edges = [0.0] + edges
+    a_list, w_list = [], []
+    for a, b in zip(edges[:-1], edges[1:]):
+        a_list.append(0.5 * (b - a) * xg + 0.5 * (b + a))
+        w_list.append(0.5 * (b - a) * wg)
+    return np.concatenate(a_list), np.concatenate(w_list)
+
+
+def lgf_values(m, n):
+    """G(m, n) = (1/2pi) int_0^pi (1 - cos(p a) e^{-q s(a)}) / sinh s(a) da,
+    cosh s = 2 - cos a, p = min(|m|,|n|), q = max(|m|,|n|).  This is the
+    lattice Green's function of the 5-point Laplacian (L G = delta) with
+    G(0,0) = 0.  Vectorised over m, n."""
+    m = np.abs(np.asarray(m, dtype=np.int64))
+    n = np.abs(np.asarray(n, dtype=np.int64))
+    p = np.minimum(m, n).astype(np.float64).ravel()
+    q = np.maximum(m, n).astype(np.float64).ravel()
+    a, w = _lgf_nodes()
+    u = 2.0 * np.sin(0.5 * a) ** 2             # cosh s - 1
+    sh = np.sqrt(u * (u + 2.0))                # sinh s
+    s = np.log1p(u + sh)                       # s
+    wt = w / sh
+    out = np.empty(p.shape)
+    chunk = 4096
+    for c0 in range(0, p.size, chunk):
+        pc = p[c0:c0 + chunk, None]
+        qc = q[c0:c0 + chunk, None]
+        e = np.exp(-qc * s[None, :])
+        num = -np.expm1(-qc * s[None, :]) + 2.0 * e * np.sin(0.5 * pc * a[None, :]) ** 2
+        out[c0:c0 + chunk] = (num * wt[None, :]).sum(axis=1)
+    return (out / (2.0 * math.pi)).reshape(m.shape)
+
+
+_LGF_TABLE_CACHE = {}
+
+
+def lgf_table(M):
+    """G(m, n) for 0 <= m, n <= M as an (M+1, M+1) array (symmetric)."""
+    if M in _LGF_TABLE_CACHE:
+        return _LGF_TABLE_CACHE[M]
+    for MM, tab in _LGF_TABLE_CACHE.items():
+        if MM >= M:
+            return tab[:M + 1, :M + 1]
+    ii, jj = np.triu_indices(M + 1)
+    vals = lgf_values(ii, jj)
+    tab = np.zeros((M + 1, M + 1))
+    tab[ii, jj] = vals
+    tab[jj, ii] = vals
+    _LGF_TABLE_CACHE[M] = tab
+    return tab
+
+
+def good_fft_size(n):
+    """Smallest 2^a 3^b >= n with a >= 2."""
+    best = None
+    p3 = 1
+    while p3 < 4 * n:
+        p2 = 4
+        while p2 * p3 < n:
+            p2 *= 2
+        cand = p2 * p3
+        if best is None or cand < best:
+            best = cand
+        p3 *= 3
+    return best
+
+
+class InverseLaplacian:
+    """Unbounded-domain inverse of factor*L (5-point) on an n1 x n2 array:
+    linear convolution with G/factor via a zero-padded circulant embedding
+    (grid_operators.jl:153-179, plan_laplacian(...; with_inverse=true))."""
+
+    def __init__(self, n1, n2, factor):
+        self.n1, self.n2, self.factor = n1, n2, factor
+        self.P1 = good_fft_size(2 * n1 - 1)
+        self.P2 = good_fft_size(2 * n2 - 1)
+        M = max(self.P1, self.P2) // 2
+        tab = lgf_table(M)
+        i1 = np.arange(self.P1)
+        i1 = np.minimum(i1, self.P1 - i1)
+        i2 = np.arange(self.P2)
+        i2 = np.minimum(i2, self.P2 - i2)
+        kern = tab[i1[:, None], i2[None, :]]
+        self.spec = sfft.rfft2(kern).real  # real and even
+
+    def __call__(self, w):
+        W = sfft.rfft2(w, s=(self.P1, self.P2), workers=os.cpu_count())
+        out = sfft.irfft2(W * self.spec, s=(self.P1, self.P2), workers=os.cpu_count())
+        return out[:self.n1, :self.n2] / self.factor
+
+
+# ---------------------------------------------------------------------------
+# Staggered stencils (CartesianGrids divergence!/grad!/curl!/laplacian!)
+# ---------------------------------------------------------------------------
+
+def divergence_edges(q):
+    """Edges{Primal} -> Nodes{Primal}: w = u[i+1]-u[i] + v[j+1]-v[j] (all nodes)."""
+    u, v = q
+    return (u[1:, :] - u[:-1, :]) + (v[:, 1:] - v[:, :-1])
+
+
+def grad_nodes(w, g: Grid):
+    """Nodes{Primal} -> Edges{Primal}; boundary (ghost-adjacent) faces zero."""
+    u = np.zeros(g.shape(EDGES_PRIMAL_U))
+    v = np.zeros(g.shape(EDGES_PRIMAL_V))
+    u[1:-1, :] = w[1:, :] - w[:-1, :]
+    v[:, 1:-1] = w[:, 1:] - w[:, :-1]
+    return (u, v)
+
+
+def curl_nodes_dual(s, g: Grid):
+    """Nodes{Dual} -> Edges{Primal}: u = s[j+1]-s[j], v = s[i]-s[i+1]."""
+    u = s[:, 1:] - s[:, :-1]
+    v = s[:-1, :] - s[1:, :]
+    return (u, v)
+
+
+def curl_edges(q, g: Grid):
+    """Edges{Primal} -> Nodes{Dual} (interior dual nodes; ghosts zero)."""
+    u, v = q
+    w = np.zeros(g.shape(NODES_DUAL))
+    w[1:-1, 1:-1] = (v[1:, 1:-1] - v[:-1, 1:-1]) - (u[1:-1, 1:] - u[1:-1, :-1])
+    return w
+
+
+def grad_edges(q, g: Grid):
+    """Edges{Primal} -> EdgeGradient{Primal} (dudx, dudy, dvdx, dvdy)."""
+    u, v = q
+    dudx = u[1:, :] - u[:-1, :]
+    dvdy = v[:, 1:] - v[:, :-1]
+    dudy = np.zeros(g.shape(NODES_DUAL))
+    dvdx = np.zeros(g.shape(NODES_DUAL))
+    dudy[1:-1, 1:-1] = u[1:-1, 1:] - u[1:-1, :-1]
+    dvdx[1:-1, 1:-1] = v[1:, 1:-1] - v[:-1, 1:-1]
+    return (dudx, dudy, dvdx, dvdy)
+
+
+def divergence_edgegrad(t, g: Grid):
+    """EdgeGradient{Primal} -> Edges{Primal} (negative adjoint of grad_edges)."""
+    dudx, dudy, dvdx, dvdy = t
+    u = np.zeros(g.shape(EDGES_PRIMAL_U))
+    v = np.zeros(g.shape(EDGES_PRIMAL_V))
+    u[1:-1, :] = (dudx[1:, :] - dudx[:-1, :]) + (dudy[1:-1, 1:] - dudy[1:-1, :-1])
+    v[:, 1:-1] = (dvdx[1:, 1:-1] - dvdx[:-1, 1:-1]) + (dvdy[:, 1:] - dvdy[:, :-1])
+    return (u, v)
+
+
+def laplacian_nodes(w, factor=1.0):
+    """5-point Laplacian on the interior of a node array, times factor."""
+    out = np.zeros_like(w)
+    out[1:-1, 1:-1] = (w[2:, 1:-1] + w[:-2, 1:-1] + w[1:-1, 2:] + w[1:-1, :-2]
+                       - 4.0 * w[1:-1, 1:-1])
+    return out * factor
+
+
+def grid_interpolate_primal_to_dual(p, g: Grid):
+    out = np.zeros(g.shape(NODES_DUAL))
+    out[1:-1, 1:-1] = 0.25 * (p[:-1, :-1] + p[1:, :-1] + p[:-1, 1:] + p[1:, 1:])
+    return out
+
+
+def grid_interpolate_primal_to_edges(p, g: Grid):
+    u = np.zeros(g.shape(EDGES_PRIMAL_U))
+    v = np.zeros(g.shape(EDGES_PRIMAL_V))
+    u[1:-1, :] = 0.5 * (p[:-1, :] + p[1:, :])
+    v[:, 1:-1] = 0.5 * (p[:, :-1] + p[:, 1:])
+    return (u, v)
+
+
+# ---------------------------------------------------------------------------
+# Cache (src/cache.jl:164-261, 305-324)
+# ---------------------------------------------------------------------------
+
+GRID_SCALING = "GridScaling"
+INDEX_SCALING = "IndexScaling"
+
+
+class SurfaceCache:
+    """BasicILMCache restatement for scalar ('scalar') or vector ('vector')
+    grid data.  Holds the DDF interpolation matrices Phi_c (cells x points)
+    for the four position classes and the inverse Laplacian."""
+
+    def __init__(self, X, Y, nrmx, nrmy, ds, g: Grid, kind="scalar",
+                 ddftype="Yang3", scaling=GRID_SCALING):
+        self.X = np.asarray(X, dtype=np.float64)
+        self.Y = np.asarray(Y, dtype=np.float64)
+        self.nx = np.asarray(nrmx, dtype=np.float64)
+        self.ny = np.asarray(nrmy, dtype=np.float64)
+        self.ds = np.asarray(ds, dtype=np.float64)
+        self.N = self.X.size
+        self.g = g
+        self.kind = kind
+        self.ddftype = ddftype
+        self.scaling = scaling
+        self.h = g.h
+        self._phi = {}
+        self._linv = {}
+
+    # -- DDF matrices -------------------------------------------------------
+    def phi(self, cls_):
+        if cls_ in self._phi:
+            return self._phi[cls_]
+        kern, rad = DDFS[self.ddftype]
+        xg, yg = self.g.coords(cls_)
+        n1, n2 = len(xg), len(yg)
+        h = self.h
+        rows, cols, vals = [], [], []
+        span = int(math.ceil(rad)) + 1
+        for k in range(self.N):
+            ix = int(math.floor((self.X[k] - xg[0]) / h))
+            iy = int(math.floor((self.Y[k] - yg[0]) / h))
+            ii = np.arange(ix - span, ix + span + 1)
+            jj = np.arange(iy - span, iy + span + 1)
+            ii = ii[(ii >= 0) & (ii < n1)]
+            jj = jj[(jj >= 0) & (jj < n2)]
+            wx = kern((xg[ii] - self.X[k]) / h)
+            wy = kern((yg[jj] - self.Y[k]) / h)
+            W = np.outer(wx, wy)
+            nz = W != 0.0
+            I, J = np.meshgrid(ii, jj, indexing="ij")
+            rows.append((I + n1 * J)[nz])
+            cols.append(np.full(int(nz.sum()), k))
+            vals.append(W[nz])
+        rows = np.concatenate(rows) if rows else np.zeros(0, int)
+        cols = np.concatenate(cols) if cols else np.zeros(0, int)
+        vals = np.concatenate(vals) if vals else np.zeros(0)
+        M = sp.csr_matrix((vals, (rows, cols)), shape=(n1 * n2, self.N))
+        self._phi[cls_] = M
+        return M
+
+    def _wscale(self):
+        if self.scaling == GRID_SCALING:
+            return self.ds / (self.h * self.h)
+        return np.ones(self.N)
+
+    def reg_cls(self, f, cls_):
+        """R_c f onto position class cls_ (fill 0 + mul!)."""
+        n1, n2 = self.g.shape(cls_)
+        return (self.phi(cls_) @ (self._wscale() * f)).reshape((n1, n2), order="F")
+
+    def interp_cls(self, s, cls_):
+        """E_c s from position class cls_."""
+        return self.phi(cls_).T @ np.asarray(s).ravel(order="F")
+
+    # -- derivative scaling (grid_operators.jl:8-9) -------------------------
+    def dscale(self):
+        return 1.0 / self.h if self.scaling == GRID_SCALING else 1.0
+
+    def lfactor(self):
+        return 1.0 / self.h ** 2 if self.scaling == GRID_SCALING else 1.0
+
+    def inverse_laplacian(self, w):
+        """inverse_laplacian! on Nodes (array) or Edges (tuple), per component."""
+        if isinstance(w, tuple):
+            return tuple(self.inverse_laplacian(c) for c in w)
+        key = w.shape
+        if key not in self._linv:
+            self._linv[key] = InverseLaplacian(w.shape[0], w.shape[1], self.lfactor())
+        return self._linv[key](w)
+
+    def laplacian(self, w):
+        if isinstance(w, tuple):
+            return tuple(self.laplacian(c) for c in w)
+        return laplacian_nodes(w, self.lfactor())
+
+
+# ---- basic transfers (surface_operators.jl:13-88) --------------------------
+
+def regularize_scalar(c: SurfaceCache, f, target="nodes_primal"):
+    cls_ = NODES_PRIMAL if target == "nodes_primal" else NODES_DUAL
+    return c.reg_cls(f, cls_)
+
+
+def interpolate_scalar(c: SurfaceCache, s, source="nodes_primal"):
+    cls_ = NODES_PRIMAL if source == "nodes_primal" else NODES_DUAL
+    return c.interp_cls(s, cls_)
+
+
+def regularize_vector(c: SurfaceCache, vb):
+    """VectorData -> Edges{Primal}."""
+    N = c.N
+    return (c.reg_cls(vb[:N], EDGES_PRIMAL_U), c.reg_cls(vb[N:], EDGES_PRIMAL_V))
+
+
+def interpolate_vector(c: SurfaceCache, q):
+    return np.concatenate([c.interp_cls(q[0], EDGES_PRIMAL_U), c.interp_cls(q[1], EDGES_PRIMAL_V)])
+
+
+def regularize_tensor(c: SurfaceCache, t):
+    """TensorData -> EdgeGradient{Primal}."""
+    N = c.N
+    return (c.reg_cls(t[:N], NODES_PRIMAL), c.reg_cls(t[N:2 * N], NODES_DUAL),
+            c.reg_cls(t[2 * N:3 * N], NODES_DUAL), c.reg_cls(t[3 * N:], NODES_PRIMAL))
+
+
+def interpolate_tensor(c: SurfaceCache, q):
+    return np.concatenate([c.interp_cls(q[0], NODES_PRIMAL), c.interp_cls(q[1], NODES_DUAL),
+                           c.interp_cls(q[2], NODES_DUAL), c.interp_cls(q[3], NODES_PRIMAL)])
+
+
+# ---- normal products (surface_operators.jl:98-343) ---------------------------
+
+def regularize_normal(c: SurfaceCache, f):
+    """Scalar f -> Edges{Primal}: R_f (n o f)."""
+    return regularize_vector(c, np.concatenate([c.nx * f, c.ny * f]))
+
+
+def normal_interpolate(c: SurfaceCache, q):
+    """Edges{Primal} -> scalar: n . R_f^T q."""
+    v = interpolate_vector(c, q)
+    return c.nx * v[:c.N] + c.ny * v[c.N:]
+
+
+def regularize_normal_cross(c: SurfaceCache, f):
+    """Scalar f -> Edges{Primal}: R_f (n x f e_z) = R_f (n_y f, -n_x f)."""
+    return regularize_vector(c, np.concatenate([c.ny * f, -c.nx * f]))
+
+
+def normal_cross_interpolate(c: SurfaceCache, q):
+    """Edges{Primal} -> scalar: e_z . (n x R_f^T q) = n_x v_y - n_y v_x."""
+    v = interpolate_vector(c, q)
+    return c.nx * v[c.N:] - c.ny * v[:c.N]
+
+
+def regularize_normal_dot(c: SurfaceCache, vs):
+    """VectorData -> Nodes{Primal}: R_c (n . v)."""
+    return c.reg_cls(c.nx * vs[:c.N] + c.ny * vs[c.N:], NODES_PRIMAL)
+
+
+def normal_dot_interpolate(c: SurfaceCache, p):
+    """Nodes{Primal} -> VectorData: n (R_c^T p)."""
+    s = c.interp_cls(p, NODES_PRIMAL)
+    return np.concatenate([c.nx * s, c.ny * s])
+
+
+def _tensor_nv(c, v):
+    """pointwise_tensorproduct!(n, v): (n_x v_x, n_x v_y, n_y v_x, n_y v_y)."""
+    N = c.N
+    vx, vy = v[:N], v[N:]
+    return np.concatenate([c.nx * vx, c.nx * vy, c.ny * vx, c.ny * vy])
+
+
+def _tensor_dot_n(c, t):
+    """pointwise_dot!(n, tau) -> (n_x t11 + n_y t21, n_x t12 + n_y t22)."""
+    N = c.N
+    t11, t12, t21, t22 = t[:N], t[N:2 * N], t[2 * N:3 * N], t[3 * N:]
+    return np.concatenate([c.nx * t11 + c.ny * t21, c.nx * t12 + c.ny * t22])
+
+
+def regularize_normal_tensor(c: SurfaceCache, v):
+    """VectorData -> EdgeGradient: R_t (n o v)."""
+    return regularize_tensor(c, _tensor_nv(c, v))
+
+
+def regularize_normal_symm(c: SurfaceCache, v):
+    """R_t (n o v + v o n - (n.v) I)   (surface_operators.jl:125-133)."""
+    N = c.N
+    t = _tensor_nv(c, v)
+    tt = np.concatenate([t[:N], t[2 * N:3 * N], t[N:2 * N], t[3 * N:]])
+    t = t + tt
+    nv = c.nx * v[:N] + c.ny * v[N:]
+    t[:N] -= nv
+    t[3 * N:] -= nv
+    return regularize_tensor(c, t)
+
+
+def normal_interpolate_tensor(c: SurfaceCache, A):
+    """EdgeGradient -> VectorData: n . R_t^T A."""
+    return _tensor_dot_n(c, interpolate_tensor(c, A))
+
+
+def normal_interpolate_symm(c: SurfaceCache, A):
+    """n . R_t^T (A + A^T - tr(A) I)   (surface_operators.jl:274-283)."""
+    dudx, dudy, dvdx, dvdy = A
+    tr = dudx + dvdy
+    B = (dudx + dudx - tr, dudy + dvdx, dvdx + dudy, dvdy + dvdy - tr)
+    return _tensor_dot_n(c, interpolate_tensor(c, B))
+
+
+# ---- composite layer operators (surface_operators.jl:357-725) ---------------
+
+def surface_divergence(c: SurfaceCache, f):
+    """theta = D R_f (n o f) / h  (scalar cache)."""
+    return divergence_edges(regularize_normal(c, f)) * c.dscale()
+
+
+def surface_grad(c: SurfaceCache, w):
+    """vn = n . R_f^T G w / h."""
+    return normal_interpolate(c, grad_nodes(w, c.g)) * c.dscale()
+
+
+def surface_curl_T(c: SurfaceCache, f):
+    """w = C^T R_f (n o f) / h: scalar f -> Nodes{Dual} (scalar cache)."""
+    return curl_edges(regularize_normal(c, f), c.g) * c.dscale()
+
+
+def surface_curl(c: SurfaceCache, s):
+    """vn = n . R_f^T C s / h: Nodes{Dual} -> scalar (scalar cache)."""
+    return normal_interpolate(c, curl_nodes_dual(s, c.g)) * c.dscale()
+
+
+def surface_curl_cross_T(c: SurfaceCache, f):
+    """w = C^T R_f (n x f e_z) / h."""
+    return curl_edges(regularize_normal_cross(c, f), c.g) * c.dscale()
+
+
+def surface_curl_cross(c: SurfaceCache, s):
+    """gamma = e_z . (n x R_f^T C s) / h."""
+    return normal_cross_interpolate(c, curl_nodes_dual(s, c.g)) * c.dscale()
+
+
+def surface_divergence_cross(c: SurfaceCache, f):
+    """theta = D R_f (n x f e_z) / h."""
+    return divergence_edges(regularize_normal_cross(c, f)) * c.dscale()
+
+
+def surface_grad_cross(c: SurfaceCache, w):
+    """gamma = e_z . (n x R_f^T G w) / h."""
+    return normal_cross_interpolate(c, grad_nodes(w, c.g)) * c.dscale()
+
+
+# vector-cache composite operators
+def surface_curl_T_vector(c: SurfaceCache, v):
+    """w = C^T R_f v / h: VectorData -> Nodes{Dual}."""
+    return curl_edges(regularize_vector(c, v), c.g) * c.dscale()
+
+
+def surface_curl_vector(c: SurfaceCache, s):
+    """v = R_f^T C s / h: Nodes{Dual} -> VectorData."""
+    return interpolate_vector(c, curl_nodes_dual(s, c.g)) * c.dscale()
+
+
+def surface_curl_T_vector_scalar(c: SurfaceCache, f):
+    """Vector cache, scalar input: C^T R_f (n o f) / h with R_f = cache.R."""
+    return surface_curl_T_vector(c, np.concatenate([c.nx * f, c.ny * f]))
+
+
+def surface_curl_vector_scalar(c: SurfaceCache, s):
+    """Vector cache, scalar output: n . R_f^T C s / h."""
+    v = surface_curl_vector(c, s)
+    return c.nx * v[:c.N] + c.ny * v[c.N:]
+
+
+def surface_divergence_vector(c: SurfaceCache, dv):
+    """Edges{Primal} = D R_t (n o dv) / h."""
+    return tuple(x * c.dscale() for x in divergence_edgegrad(regularize_normal_tensor(c, dv), c.g))
+
+
+def surface_divergence_symm(c: SurfaceCache, dv):
+    return tuple(x * c.dscale() for x in divergence_edgegrad(regularize_normal_symm(c, dv), c.g))
+
+
+def surface_grad_vector(c: SurfaceCache, q):
+    return normal_interpolate_tensor(c, grad_edges(q, c.g)) * c.dscale()
+
+
+def surface_grad_symm(c: SurfaceCache, q):
+    return normal_interpolate_symm(c, grad_edges(q, c.g)) * c.dscale()
+
+
+# ---- masks (surface_operators.jl:737-923) ----------------------------------
+
+def mask(c: SurfaceCache):
+    """H = -L^{-1} D_s 1 on Nodes{Primal} (scalar cache)."""
+    return -c.inverse_laplacian(surface_divergence(c, np.ones(c.N)))
+
+
+# ---- Schur-complement builders (matrix_operators.jl:9-244) ------------------
+
+def create_RTLinvR(c: SurfaceCache, scale=1.0):
+    A = np.empty((c.N, c.N))
+    e = np.zeros(c.N)
+    for col in range(c.N):
+        e[:] = 0.0
+        e[col] = 1.0
+        w = c.inverse_laplacian(regularize_scalar(c, e))
+        A[:, col] = -scale * interpolate_scalar(c, w)
+    return A
+
+
+def create_CLinvCT(c: SurfaceCache, scale=1.0):
+    A = np.empty((c.N, c.N))
+    e = np.zeros(c.N)
+    for col in range(c.N):
+        e[:] = 0.0
+        e[col] = 1.0
+        w = c.inverse_laplacian(surface_curl_T(c, e))
+        A[:, col] = -scale * surface_curl(c, w)
+    return A
+
+
+def create_GLinvD(c: SurfaceCache, scale=1.0):
+    A = np.empty((c.N, c.N))
+    e = np.zeros(c.N)
+    for col in range(c.N):
+        e[:] = 0.0
+        e[col] = 1.0
+        w = c.inverse_laplacian(surface_divergence(c, e))
+        A[:, col] = -scale * surface_grad(c, w)
+    return A
+
+
+def create_nRTRn(c: SurfaceCache, scale=1.0):
+    A = np.empty((c.N, c.N))
+    e = np.zeros(c.N)
+    for col in range(c.N):
+        e[:] = 0.0
+        e[col] = 1.0
+        A[:, col] = scale * normal_interpolate(c, regularize_normal(c, e))
+    return A
+
+
+def create_GLinvD_vector(c: SurfaceCache, scale=1.0):
+    n = 2 * c.N
+    A = np.empty((n, n))
+    e = np.zeros(n)
+    for col in range(n):
+        e[:] = 0.0
+        e[col] = 1.0
+        w = c.inverse_laplacian(surface_divergence_vector(c, e))
+        A[:, col] = -scale * surface_grad_vector(c, w)
+    return A
+
+
+# ---------------------------------------------------------------------------
+# Matrix-free Schur operators (what the GPU CG applies)
+# ---------------------------------------------------------------------------
+
+def schur_dirichlet_apply(c: SurfaceCache, s):
+    """S s = E L^{-1} R s  (= -create_RTLinvR(c) @ s)."""
+    return interpolate_scalar(c, c.inverse_laplacian(regularize_scalar(c, s)))
+
+
+def schur_neumann_apply(c: SurfaceCache, s):
+    """S s = -C_s L^{-1} C_s^T s  (= create_CLinvCT(c) @ s)."""
+    return -surface_curl(c, c.inverse_laplacian(surface_curl_T(c, s)))
+
+
+# ---------------------------------------------------------------------------
+# Problem solves (test/literate/problems.jl:259-298, neumann.jl:101-142)
+# ---------------------------------------------------------------------------
+
+def solve_dirichlet(c: SurfaceCache, fplus, fminus, S=None):
+    """Block-LU Dirichlet Poisson solve with dense Schur complement, as the
+    reference's DirichletPoissonProblem `solve` (without the C^6 filter).
+    Returns (f on Nodes{Primal}, s jump strength)."""
+    if S is None:
+        S = create_RTLinvR(c)
+    jump = fplus - fminus
+    avg = 0.5 * (fplus + fminus)
+    fstar = c.inverse_laplacian(surface_divergence(c, jump))
+    s = avg - interpolate_scalar(c, fstar)
+    s = -np.linalg.solve(S, s)
+    f = c.inverse_laplacian(regularize_scalar(c, s)) + fstar
+    return f, s
+
+
+def solve_neumann(c: SurfaceCache, vplus, vminus, S=None):
+    """Neumann Poisson solve (neumann.jl:101-142): returns (f, df, s, ds)."""
+    if S is None:
+        S = create_CLinvCT(c)
+    dvn = vplus - vminus
+    vn = 0.5 * (vplus + vminus)
+    fstar = c.inverse_laplacian(regularize_scalar(c, dvn))
+    df = vn - surface_grad(c, fstar)
+    df = -np.linalg.solve(S, df)
+    f = c.inverse_laplacian(surface_divergence(c, df)) + fstar
+    sstar = surface_curl_T(c, df)
+    ds = np.linalg.solve(S, surface_grad_cross(c, fstar))
+    s = -(surface_curl_cross_T(c, ds) - sstar)
+    s = c.inverse_laplacian(s)
+    return f, df, s, ds

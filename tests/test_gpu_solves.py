@@ -1,0 +1,61 @@
+"""Dirichlet and Neumann Poisson solves on the device against the oracle's
+dense-LU solves (test/literate/problems.jl:259-298, neumann.jl:101-142)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+import ilm_oracle as O
+from geometry import dirichlet_config1, oracle_cache
+
+
+def rel(a, b):
+    return np.abs(np.asarray(a) - np.asarray(b)).max() / np.abs(np.asarray(b)).max()
+
+
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+def test_dirichlet_config1(cuda, dtype):
+    import torch
+    import immersedlayers as il
+    dt = torch.float64 if dtype == "f64" else torch.float32
+    og, b, fb = dirichlet_config1()
+    g = il.PhysicalGrid((-2.0, 2.0), (-2.0, 2.0), og.h)
+    c = il.SurfaceScalarCache(b, g, dtype=dt)
+    fp = il.ScalarData(torch.tensor(fb, dtype=dt, device="cuda"))
+    fm = il.ScalarData.zeros(len(b), dt)
+    f, s, info = il.solve_dirichlet(c, fp, fm, tol=1e-10)
+    assert info["converged"] and info["rel_residual"] <= 1e-10
+    oc = oracle_cache(og, b)
+    S = O.create_RTLinvR(oc)
+    f_ref, s_ref = O.solve_dirichlet(oc, fb, np.zeros_like(fb), S)
+    # s inherits the conditioning of S (cond ~ 4e4 here); f is smooth
+    if dt == torch.float64:
+        assert rel(f.numpy_components(), f_ref) < 1e-7
+        assert rel(s.numpy(), s_ref) < 1e-5
+    else:
+        assert rel(f.numpy_components(), f_ref) < 1e-4
+        assert rel(s.numpy(), s_ref) < 5e-2
+    # residual of the device s in the oracle's FP64 operator
+    rhs = O.interpolate_scalar(oc, oc.inverse_laplacian(O.surface_divergence(oc, fb))) - 0.5 * fb
+    r = np.linalg.norm(S @ s.numpy() - rhs) / np.linalg.norm(rhs)
+    assert r < (1e-9 if dt == torch.float64 else 1e-5)
+
+
+def test_neumann_circle(cuda):
+    import torch
+    import immersedlayers as il
+    from immersedlayers import bodies as B
+    h = 0.04
+    og = O.Grid.physical((-2.0, 2.0), (-2.0, 2.0), h)
+    b = B.circle(1.0, ds=1.4 * h)
+    g = il.PhysicalGrid((-2.0, 2.0), (-2.0, 2.0), h)
+    c = il.SurfaceScalarCache(b, g)
+    vplus = b.nx.copy()   # neumann.jl:157-168: v_n+ = n_x, v_n- = 0
+    vp = il.ScalarData(torch.tensor(vplus, device="cuda"))
+    vm = il.ScalarData.zeros(len(b))
+    f, df, info = il.solve_neumann(c, vp, vm, tol=1e-10, maxiter=20000)
+    assert info["converged"], info
+    oc = oracle_cache(og, b)
+    f_ref, df_ref, _, _ = O.solve_neumann(oc, vplus, np.zeros_like(vplus))
+    # the field is insensitive to the (near-)null space of S; compare it
+    assert rel(f.numpy_components(), f_ref) < 1e-6

@@ -1,0 +1,145 @@
+"""The CPU oracle against the reference's own known-answer tests
+(test/tools.jl, test/surface_ops.jl) and published LGF values."""
+import math
+
+import numpy as np
+import pytest
+
+import ilm_oracle as O
+from geometry import angles, oracle_cache, surface_ops_case, tools_case
+
+
+def test_ddf_partition_of_unity():
+    r = np.linspace(-0.5, 0.5, 41)
+    for name, (k, _) in O.DDFS.items():
+        s = sum(k(r - j) for j in range(-4, 5))
+        assert np.abs(s - 1.0).max() < 1e-14, name
+
+
+def test_lgf_known_values():
+    # exact values of the square-lattice Green's function (G(0,0) = 0)
+    m = np.array([1, 1, 2, 2, 2, 3, 5, 20])
+    n = np.array([0, 1, 0, 1, 2, 0, 5, 20])
+    G = O.lgf_values(m, n)
+    exact = [0.25, 1 / math.pi, 1 - 2 / math.pi, -0.25 + 2 / math.pi, 4 / (3 * math.pi), 17 / 4 - 12 / math.pi,
+             sum(1 / (2 * k - 1) for k in range(1, 6)) / math.pi, sum(1 / (2 * k - 1) for k in range(1, 21)) / math.pi]
+    assert np.abs(G - np.array(exact)).max() < 1e-14
+
+
+def test_lgf_far_field():
+    for m, n in [(300, 0), (200, 150)]:
+        r = math.hypot(m, n)
+        th = math.atan2(n, m)
+        asym = (math.log(r) + O.EULER_GAMMA + 1.5 * math.log(2)) / (2 * math.pi) - math.cos(4 * th) / (24 * math.pi * r * r)
+        assert abs(O.lgf_values(np.array([m]), np.array([n]))[0] - asym) < 1e-10
+
+
+def test_lgf_inverts_laplacian():
+    rng = np.random.default_rng(0)
+    w = np.zeros((40, 36))
+    w[12:28, 10:26] = rng.standard_normal((16, 16))
+    il = O.InverseLaplacian(40, 36, 1.0)
+    u = il(w)
+    lap = O.laplacian_nodes(u)
+    assert np.abs(lap[1:-1, 1:-1] - w[1:-1, 1:-1]).max() < 1e-11
+
+
+def test_grid_sizing_matches_reference_print():
+    # examples/caches.ipynb: PhysicalGrid((-2,2),(-2,2),0.01) -> (406,406), (203,203), xlim +-2.02
+    g = O.Grid.physical((-2.0, 2.0), (-2.0, 2.0), 0.01)
+    assert (g.nx, g.ny, g.i0x, g.i0y) == (406, 406, 203, 203)
+    x, _ = g.coords(O.NODES_PRIMAL)
+    assert g.shape(O.NODES_PRIMAL) == (405, 405)
+    assert abs(x[0] + 2.02) < 1e-12 and abs(x[-1] - 2.02) < 1e-12
+
+
+def test_tools_inner_products_and_adjointness():
+    g, b = tools_case()
+    c = oracle_cache(g, b)
+    h = g.h
+    os_ = np.ones(len(b))
+    oc = np.ones(g.shape(O.NODES_DUAL))
+    # test/tools.jl:36-48
+    lim = g.limits()
+    assert math.sqrt(O.grid_dot_array(oc, oc, O.NODES_DUAL, h)) == pytest.approx(
+        math.sqrt((lim[0][1] - lim[0][0]) * (lim[1][1] - lim[1][0])), abs=1e-12)
+    assert abs(np.dot(os_, os_ * b.ds) - 2 * math.pi) < 1e-3
+    assert abs(np.sum((b.nx ** 2 + b.ny ** 2) * b.ds) - 2 * math.pi) < 1e-3
+    # test/tools.jl:107,112
+    assert abs(O.grid_dot_array(oc, c.reg_cls(os_, O.NODES_DUAL), O.NODES_DUAL, h) - np.dot(os_, os_ * b.ds)) < 1e-14
+    rng = np.random.default_rng(0)
+    u = rng.standard_normal(g.shape(O.NODES_DUAL))
+    phi = rng.standard_normal(len(b))
+    lhs = O.grid_dot_array(u, c.reg_cls(phi, O.NODES_DUAL), O.NODES_DUAL, h)
+    rhs = np.dot(c.interp_cls(u, O.NODES_DUAL), phi * b.ds)
+    assert abs(lhs - rhs) < 1e-13
+    # test/tools.jl:119-120 (Edges{Dual}.u lives on the (primal x, dual y) class)
+    rf = c.reg_cls(os_, O.EDGES_PRIMAL_V)
+    val = O.grid_dot_array(np.ones_like(rf), rf, O.EDGES_PRIMAL_V, h)
+    assert abs(val - b.ds.sum()) < 1e-12
+    assert abs(val - 2 * math.pi) < 1e-3
+
+
+def test_circle_circumference_matches_notebook():
+    # examples/caches.ipynb: dot(os,os,cache) = 6.283288300933757 for Circle(1.0, 0.014)
+    from immersedlayers import bodies as B
+    b = B.circle(1.0, ds=0.014)
+    assert len(b) == 448
+    assert abs(b.ds.sum() - 6.283288300933757) < 1e-9
+
+
+def test_surface_ops_known_answers():
+    g, b = surface_ops_case()
+    c = oracle_cache(g, b)
+    h = g.h
+    N = len(b)
+    f = np.sin(angles(N) - math.pi / 4)
+    f2 = O.normal_interpolate(c, O.regularize_normal(c, f))
+    assert f2.max() == pytest.approx(11, abs=1.0)          # test/surface_ops.jl:66
+    assert f2.min() == pytest.approx(-11, abs=1.0)         # :67
+    A = O.create_CLinvCT(c, scale=h)
+    assert np.abs(np.linalg.eigvals(A)).max() == pytest.approx(0.2, abs=0.1)    # :71
+    A = O.create_GLinvD(c, scale=h)
+    assert np.abs(np.linalg.eigvals(A)).max() == pytest.approx(0.45, abs=0.1)   # :74
+    A = O.create_nRTRn(c)
+    assert np.linalg.svd(A, compute_uv=False).max() == pytest.approx(11, abs=1.0)  # :77
+
+
+def test_vector_surface_ops_known_answers():
+    g, b = surface_ops_case()
+    c = oracle_cache(g, b, kind="vector")
+    N = len(b)
+    f = np.sin(angles(N) - math.pi / 4)
+    vs = np.zeros(2 * N)
+    vs[:N] = f
+    vs = O.normal_interpolate_tensor(c, O.regularize_normal_tensor(c, vs))   # :131-132
+    vs[:N] = f
+    vs = O.normal_interpolate_symm(c, O.regularize_normal_symm(c, vs))      # :135-137
+    assert vs[:N].min() == pytest.approx(-22.5, abs=1.0)
+    assert vs[:N].max() == pytest.approx(22.5, abs=1.0)
+    A = O.create_GLinvD_vector(c, scale=g.h)
+    assert np.abs(np.linalg.eigvals(A)).max() == pytest.approx(0.45, abs=0.1)   # :146
+
+
+def test_masks_area():
+    g, b = surface_ops_case()
+    c = oracle_cache(g, b)
+    m = O.mask(c)
+    assert abs(O.grid_dot_array(np.ones_like(m), m, O.NODES_PRIMAL, g.h) - math.pi) < 2e-3   # :186
+    md = O.grid_interpolate_primal_to_dual(m, g)
+    assert abs(O.grid_dot_array(np.ones_like(md), md, O.NODES_DUAL, g.h) - math.pi) < 1e-3  # :198
+
+
+def test_dirichlet_exterior_analytic():
+    # f+ = x on a circle of radius R: exterior solution x R^2 / r^2
+    from immersedlayers import bodies as B
+    h = 0.02
+    g = O.Grid.physical((-2.0, 2.0), (-2.0, 2.0), h)
+    b = B.circle(0.5, ds=1.4 * h)
+    c = oracle_cache(g, b)
+    f, s = O.solve_dirichlet(c, b.x.copy(), np.zeros(len(b)))
+    x, y = g.coords(O.NODES_PRIMAL)
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    r = np.hypot(X, Y)
+    m = (r > 0.7) & (r < 1.5)
+    assert np.abs(f[m] - X[m] * 0.25 / r[m] ** 2).max() < 5e-3
