@@ -83,6 +83,7 @@ SIGNATURES = {
     "ilm_mask": [_VP, _I, _I, _VP, _VP],
     "ilm_dot_grid": [_VP, _I, _VP, _VP, _DP, _VP],
     "ilm_dot_surface": [_VP, _I, _VP, _VP, _DP, _VP],
+    "ilm_dot_grid_noalloc": [_I, _I, _D, _I, _I, _I, _VP, _VP, _DP, _VP],
     "ilm_schur_build": [_VP, _I, _D, _VP, _VP],
     "ilm_solve_dirichlet": [_VP, _VP, _VP, _VP, _VP, _D, _I, C.POINTER(SolveInfo), _VP],
     "ilm_solve_neumann": [_VP, _VP, _VP, _VP, _VP, _D, _I, C.POINTER(SolveInfo), _VP],

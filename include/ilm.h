@@ -185,6 +185,21 @@ ILM_API int ilm_dot_grid(ilm_cache_t c, int kind, const void* a, const void* b, 
 /* dot(u1, u2, cache) for point data with `ncomp` components (ds weighted). */
 ILM_API int ilm_dot_surface(ilm_cache_t c, int ncomp, const void* a, const void* b, double* result, ilm_stream_t stream);
 
+/* Allocation-free weighted grid inner product.  No counterpart in the
+ * reference: it exists for callers that cannot allocate device memory when
+ * they need an inner product (host code running during a CUDA-graph stream
+ * capture, services whose memory pool owns the device, latency-critical loops
+ * that must not call cudaFree).  Same result as ilm_dot_grid on grid data of
+ * `kind` for an nx x ny grid with cell size h and `scaling`, without a cache;
+ * it calls no allocating routine.  Its scratch is a fixed 128 KiB device array
+ * held by every GPU that loads the library: grids are limited to 16384 dual
+ * nodes per side (larger ones fail with ILM_ERR_SIZE_LIMIT).  The first call on
+ * a device looks up that array's address; make it before any stream capture.
+ * Calls share the array: calls that may overlap on the GPU race and must be
+ * serialised by the caller.  Synchronises `stream` to return the result.     */
+ILM_API int ilm_dot_grid_noalloc(int nx, int ny, double h, int scaling, int kind, int dtype, const void* a,
+                                 const void* b, double* result, ilm_stream_t stream);
+
 /* ---- Schur complements (src/matrix_operators.jl:9-244) ------------------ */
 /* Dense N x N (column-major, FP64, device) Schur complement, built on the
  * GPU directly from lattice-Green's-function point-point sums instead of the
