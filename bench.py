@@ -28,7 +28,7 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "immersedlayers.jl_gb300"))
 
-METRIC = "Poisson solves/s at 1e-8 rel. residual (batched Dirichlet/Neumann, plain CG)"
+METRIC = "Poisson solves/s at 1e-8 rel. residual, 1 GB300 (batched Dirichlet/Neumann)"
 UNIT = "solves/s"
 NPROB = 256
 
@@ -41,6 +41,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--nprob", type=int, default=NPROB)
     ap.add_argument("--tol", type=float, default=1e-8)
+    ap.add_argument("--precond", default="bjacobi", choices=["none", "bjacobi"])
+    ap.add_argument("--block", type=int, default=64)
     ap.add_argument("--cpu-sample-cols", type=int, default=32)
     return ap.parse_args()
 
@@ -61,7 +63,9 @@ def config(args, world):
                         "n~U{128,192,256,384,512}^2 dual nodes, h=4/n, 1-3 circles/ellipses at ds=1.4h, "
                         "8-mode arc-length Fourier surface data, seeds 3+i",
             "nprob_per_gpu": args.nprob, "tol": args.tol, "precision": "FP32 grid work, FP64 Schur build + CG",
-            "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{world}"}
+            "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{world}",
+            "solver": {"none": "plain CG", "bjacobi": f"block-Jacobi flexible CG (blocks of ~{args.block} points)"}[
+                args.precond]}
 
 
 def clocks_sampler():
@@ -141,6 +145,23 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def _timed(bs, fp, fm, f_out, s_out, args, stream, flush, steps):
+    """Time `steps` batch solves with CUDA events on the solve stream (L2 flushed before each)."""
+    import torch
+    times = []
+    with torch.cuda.stream(stream):
+        for _ in range(steps):
+            flush.fill_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            bs.solve(fp, fm, f_out, s_out, tol=args.tol, stream=stream)
+            e1.record(stream)
+            times.append((e0, e1))
+    stream.synchronize()
+    return sum(a.elapsed_time(b) for a, b in times)
+
+
 def run_ours(args, rank, world, dist):
     import numpy as np
     import torch
@@ -162,31 +183,29 @@ def run_ours(args, rank, world, dist):
     f_out = torch.empty(bs.total_cells, dtype=dt, device="cuda")
     s_out = torch.empty(bs.total_points, dtype=dt, device="cuda")
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
-    with torch.cuda.stream(stream):
-        for _ in range(args.warmup):
-            bs.solve(fp, fm, f_out, s_out, tol=args.tol, stream=stream)
-    stream.synchronize()
-    its, rr = bs.info()
-    assert (rr <= args.tol).all(), f"not converged: max rel residual {rr.max()}"
-    # timed region
+
+    # secondary leg: plain CG (no preconditioner), same batch, same timing rules
+    solvers = {}
+    for mode in ["none", args.precond] if args.precond != "none" else ["none"]:
+        bs.set_precond(mode, args.block)
+        with torch.cuda.stream(stream):
+            for _ in range(args.warmup):
+                bs.solve(fp, fm, f_out, s_out, tol=args.tol, stream=stream)
+        stream.synchronize()
+        its, rr = bs.info()
+        assert (rr <= args.tol).all(), f"{mode}: not converged, max rel residual {rr.max()}"
+        if mode != args.precond:
+            ms = _timed(bs, fp, fm, f_out, s_out, args, stream, flush, max(1, args.steps))
+            solvers["plain_cg"] = {"solves_per_s": args.nprob * max(1, args.steps) / (ms / 1000.0),
+                                   "cg_iterations_mean": float(np.mean(its)), "cg_iterations_max": int(its.max())}
+
+    # timed region (the default solver)
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
     clk = clocks_sampler()
-    times = []
-    with torch.cuda.stream(stream):
-        for _ in range(args.steps):
-            flush.fill_(1.0)
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            bs.solve(fp, fm, f_out, s_out, tol=args.tol, stream=stream)
-            e1.record(stream)
-            times.append((e0, e1))
-    stream.synchronize()
+    total_ms = _timed(bs, fp, fm, f_out, s_out, args, stream, flush, args.steps)
     torch.cuda.synchronize()
-    ms = [a.elapsed_time(b) for a, b in times]
-    total_ms = sum(ms)
     if dist:
         t = torch.tensor([total_ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -194,6 +213,11 @@ def run_ours(args, rank, world, dist):
         dist.barrier()
     clocks = clocks_summary(clk, dev)
     value = world * args.nprob * args.steps / (total_ms / 1000.0)
+    its, rr = bs.info()
+    solvers[{"bjacobi": "block_jacobi_pcg", "none": "plain_cg"}[args.precond]] = {
+        "solves_per_s": args.nprob * args.steps / (total_ms / 1000.0), "cg_iterations_mean": float(np.mean(its)),
+        "cg_iterations_max": int(its.max())}
+    solvers.setdefault("learned_pcg", None)
 
     # stage profile of one solve (separate, not part of the timed region)
     bs.set_profiling(True)
@@ -204,7 +228,6 @@ def run_ours(args, rank, world, dist):
     stage_ms, launches = bs.stage_times()
     bs.set_profiling(False)
     st = bs.stats()
-    its, rr = bs.info()
 
     # roofline of the dominant stage
     hbm, peak_kind = peaks()
@@ -218,19 +241,51 @@ def run_ours(args, rank, world, dist):
 
     # end to end through the public API from host buffers
     e2e = _e2e(args, specs, stream, dt)
+    stencil = _stencil_gbs(stream, flush, hbm)
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
                 "config": config(args, world), "roofline": roofline, "e2e": e2e, "gpu_launches": launches * args.steps,
-                "clocks": clocks, "setup_s": setup_s,
+                "clocks": clocks, "setup_s": setup_s, "solvers": solvers, "stencil_gbs": stencil,
                 "stages_ms": dict(zip(names, [round(x, 4) for x in stage_ms])),
                 "cg_iterations": {"mean": float(np.mean(its)), "max": int(its.max())},
                 "max_rel_residual": float(rr.max())}
         if world == 1:
             line["cpu_baseline"] = _cpu_baseline(args, specs)
         print(json.dumps(line), flush=True)
+
+
+def _stencil_gbs(stream, flush, hbm):
+    """Achieved HBM GB/s of the staggered divergence (Edges -> Nodes, 12 B per
+    cell FP32) and gradient (Nodes -> Edges) stencils on a 2048^2 grid."""
+    import torch
+    import immersedlayers as il
+    g = il.PhysicalGrid(h=0.002, nx=2048)
+    c = il.SurfaceScalarCache(None, g, dtype=torch.float32)
+    q = il.EdgesPrimal.zeros(g, torch.float32)
+    q.data.normal_()
+    w = il.NodesPrimal.zeros(g, torch.float32)
+    out = {}
+    for name, fn, a, b in [("divergence", il.divergence_, w, q), ("grad", il.grad_, q, w)]:
+        for _ in range(3):
+            fn(a, b, c, stream=stream)
+        ms = []
+        with torch.cuda.stream(stream):
+            for _ in range(10):
+                flush.fill_(1.0)
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                fn(a, b, c, stream=stream)
+                e1.record(stream)
+                ms.append((e0, e1))
+        stream.synchronize()
+        t = statistics.median(x.elapsed_time(y) for x, y in ms) / 1000.0
+        nbytes = (a.data.numel() + b.data.numel()) * 4
+        out[name] = {"gbs": nbytes / t / 1e9, "frac": nbytes / t / 1e9 / hbm, "bytes": nbytes, "ms": 1000 * t}
+    return out
 
 
 def _rank_specs(nprob, rank):

@@ -215,9 +215,10 @@ struct ilm_batch_s {
   DevBuf nx, ny, wsc, nx64, ny64, ds64, pt2prob;
   DevBuf tptr[4], tpts[4];
   // work
-  DevBuf fstar, corr, edges, convwork, S, F;
+  DevBuf fstar, corr, edges, convwork, Shi, Slo, F;
   DevBuf jump, avg, g, s, rhs64, x64;
-  DevBuf cgp, iters, relres;
+  DevBuf cgp, iters, relres, order, counter;
+  int nclusters = 1;
   // tasks
   DevBuf scatA, divA, gradA, gathA, scatB, divB, convA, convB, schurP;
   int n_scatA = 0, n_divA = 0, n_gradA = 0, n_gathA = 0, n_scatB = 0, n_divB = 0;
@@ -228,6 +229,11 @@ struct ilm_batch_s {
   double cg_tol = -1.0;
   int cg_maxiter = -1;
   // optional stage timing (CUDA events on the solve stream)
+  // preconditioner of the Schur CG: 0 none, 1 block-Jacobi
+  int precond = 0, bj_block = 0;
+  bool params_dirty = false;
+  DevBuf bj_blk, bj_start, bj_size, bj_off, bj_inv, bj_inv_lo, bj_tasks;
+  std::vector<int> bj_first;  // first block of each problem
   int profiling = 0;
   cudaEvent_t ev[32] = {};
   int nev = 0, launches = 0;
@@ -371,10 +377,23 @@ int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* 
   ILM_TRY(B->s.alloc((size_t)Ptot * e));
   ILM_TRY(B->rhs64.alloc((size_t)Ptot * 8));
   ILM_TRY(B->x64.alloc((size_t)Ptot * 8));
-  ILM_TRY(B->S.alloc(std::max<size_t>(B->stot, 1) * 8));
+  ILM_TRY(B->Shi.alloc(std::max<size_t>(B->stot, 1) * 4));
+  ILM_TRY(B->Slo.alloc(std::max<size_t>(B->stot, 1) * 4));
   ILM_TRY(B->F.alloc((size_t)Ptot * functional_size()));
   ILM_TRY(B->iters.alloc((size_t)nprob * sizeof(int)));
   ILM_TRY(B->relres.alloc((size_t)nprob * sizeof(double)));
+  {
+    // CG work queue: largest problems first (cost ~ npts^2 * sqrt(npts))
+    std::vector<int> ord(nprob);
+    for (int p = 0; p < nprob; ++p) ord[p] = p;
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int c) {
+      const double ca = pow((double)probs[a].npts, 2.5), cc = pow((double)probs[c].npts, 2.5);
+      return ca > cc;
+    });
+    ILM_TRY(up(B->order, ord));
+    ILM_TRY(B->counter.alloc(sizeof(int)));
+    B->nclusters = cg_cluster_count(nprob, B->maxN);
+  }
 
   // FFT convolution jobs (fstar and corr in place); one work area per problem
   std::vector<size_t> woff(nprob + 1, 0);
@@ -558,7 +577,7 @@ int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* 
   BW.nx64 = B->nx64.as<double>();
   BW.ny64 = B->ny64.as<double>();
   ILM_TRY(schur_build_batched(nprob, B->schurP.as<SchurProbDev>(), tiles, Ptot, B->pt2prob.as<int>(), BW,
-                              B->ds64.as<double>(), static_cast<Functional*>(B->F.p), B->S.as<double>(), B->max_grid,
+                              B->ds64.as<double>(), static_cast<Functional*>(B->F.p), B->Shi.as<float>(), B->Slo.as<float>(), B->max_grid,
                               nullptr));
   ILM_CHECK_CUDA(cudaDeviceSynchronize());
   *out = guard.release();
@@ -586,20 +605,20 @@ int ilm_batch_solve(ilm_batch_t b, const void* fplus, const void* fminus, void* 
   cudaStream_t st = as_stream(stream);
   const int dt = b->dtype;
   const int Ptot = b->Ptot;
-  if (tol != b->cg_tol || maxiter != b->cg_maxiter) {
-    std::vector<CGParams> cg(b->nprob);
+  if (tol != b->cg_tol || maxiter != b->cg_maxiter || b->params_dirty) {
+    b->params_dirty = false;
+    std::vector<unsigned char> cg((size_t)b->nprob * cgff_params_size());
+    const bool pre = b->precond == 1;
     for (int p = 0; p < b->nprob; ++p) {
       const size_t o = b->poff[p];
-      cg[p].A64 = b->S.as<double>() + b->soff[p];
-      cg[p].A32 = nullptr;
-      cg[p].b = b->rhs64.as<double>() + o;
-      cg[p].x = b->x64.as<double>() + o;
-      cg[p].w = b->ds64.as<double>() + o;
-      cg[p].n = b->probs[p].npts;
-      cg[p].maxiter = maxiter;
-      cg[p].tol = tol;
-      cg[p].iters = b->iters.as<int>() + p;
-      cg[p].relres = b->relres.as<double>() + p;
+      cgff_params_fill(cg.data() + (size_t)p * cgff_params_size(), b->Shi.as<float>() + b->soff[p],
+                       b->Slo.as<float>() + b->soff[p], b->rhs64.as<double>() + o, b->x64.as<double>() + o,
+                       b->ds64.as<double>() + o, b->probs[p].npts, maxiter, tol, b->iters.as<int>() + p,
+                       b->relres.as<double>() + p, pre ? b->bj_blk.as<int>() + o : nullptr,
+                       pre ? b->bj_start.as<int>() + b->bj_first[p] : nullptr,
+                       pre ? b->bj_size.as<int>() + b->bj_first[p] : nullptr,
+                       pre ? b->bj_off.as<int>() + b->bj_first[p] : nullptr, pre ? b->bj_inv.as<float>() : nullptr,
+                       pre ? b->bj_inv_lo.as<float>() : nullptr);
     }
     ILM_TRY(up(b->cgp, cg));
     b->cg_tol = tol;
@@ -647,7 +666,7 @@ int ilm_batch_solve(ilm_batch_t b, const void* fplus, const void* fminus, void* 
     b->launches += 2;
     MARK();  // 6: DDF gather + Schur right-hand side
   });
-  ILM_TRY(launch_cg_batched(b->cgp.as<CGParams>(), b->nprob, b->maxN, st));
+  ILM_TRY(launch_cg_cluster(b->cgp.p, b->order.as<int>(), b->nprob, b->counter.as<int>(), b->maxN, b->nclusters, st));
   b->launches += 1;
   MARK();  // 7: Schur CG
   ILM_TRY(st_convert(Ptot, ILM_F64, b->x64.p, dt, s_out, st));
@@ -671,6 +690,63 @@ int ilm_batch_solve(ilm_batch_t b, const void* fplus, const void* fminus, void* 
   b->launches += 1;
   MARK();  // 12: f = f* + correction
 #undef MARK
+  return ILM_OK;
+}
+
+int ilm_batch_set_precond(ilm_batch_t b, int mode, int block_size) {
+  ILM_REQUIRE(b, "null batch");
+  ILM_REQUIRE(mode == 0 || mode == 1, "batch: unknown preconditioner %d", mode);
+  if (mode == 1) {
+    ILM_REQUIRE(block_size >= 4 && block_size <= 72, "batch: block size %d outside [4, 72]", block_size);
+    if (b->bj_block != block_size) {
+      // blocks of ~block_size consecutive points (at most 1.5 x block_size)
+      std::vector<int> blk(b->Ptot), bst, bsz, boff;
+      std::vector<BJBlockTask> tasks;
+      b->bj_first.assign(b->nprob + 1, 0);
+      size_t total = 0;
+      int max_sz = 1;
+      for (int p = 0; p < b->nprob; ++p) {
+        const int n = b->probs[p].npts;
+        const int nb = std::max(1, (int)lround((double)n / block_size));
+        b->bj_first[p] = (int)bst.size();
+        for (int k = 0; k < nb; ++k) {
+          const int s = (int)((long long)n * k / nb), e = (int)((long long)n * (k + 1) / nb);
+          for (int j = s; j < e; ++j) blk[b->poff[p] + j] = k;
+          bst.push_back(s);
+          bsz.push_back(e - s);
+          boff.push_back((int)total);
+          max_sz = std::max(max_sz, e - s);
+          BJBlockTask T;
+          T.Shi = b->Shi.as<float>() + b->soff[p];
+          T.Slo = b->Slo.as<float>() + b->soff[p];
+          T.n = n;
+          T.s = s;
+          T.sz = e - s;
+          T.out_hi = T.out_lo = nullptr;  // set after allocation
+          tasks.push_back(T);
+          total += (size_t)(e - s) * (e - s);
+        }
+      }
+      b->bj_first[b->nprob] = (int)bst.size();
+      ILM_REQUIRE(max_sz <= 144, "batch: preconditioner block of %d points", max_sz);
+      ILM_TRY(b->bj_inv.alloc(std::max<size_t>(total, 1) * sizeof(float)));
+      ILM_TRY(b->bj_inv_lo.alloc(std::max<size_t>(total, 1) * sizeof(float)));
+      for (size_t t = 0; t < tasks.size(); ++t) {
+        tasks[t].out_hi = b->bj_inv.as<float>() + boff[t];
+        tasks[t].out_lo = b->bj_inv_lo.as<float>() + boff[t];
+      }
+      ILM_TRY(up(b->bj_blk, blk));
+      ILM_TRY(up(b->bj_start, bst));
+      ILM_TRY(up(b->bj_size, bsz));
+      ILM_TRY(up(b->bj_off, boff));
+      ILM_TRY(up(b->bj_tasks, tasks));
+      ILM_TRY(launch_block_inverse(b->bj_tasks.as<BJBlockTask>(), (int)tasks.size(), max_sz, nullptr));
+      ILM_CHECK_CUDA(cudaDeviceSynchronize());
+      b->bj_block = block_size;
+    }
+  }
+  b->precond = mode;
+  b->params_dirty = true;
   return ILM_OK;
 }
 

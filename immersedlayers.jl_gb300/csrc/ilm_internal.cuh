@@ -300,7 +300,25 @@ struct BatchWin {
 struct Functional;
 size_t functional_size();
 int schur_build_batched(int nprob, const SchurProbDev* probs_dev, int total_tiles, int Ptot, const int* pt2prob,
-                        const BatchWin& W, const double* w, Functional* F, double* Aall, int max_grid,
+                        const BatchWin& W, const double* w, Functional* F, float* Shi, float* Slo, int max_grid,
                         cudaStream_t st);
+
+// cluster CG with float-float matvecs (ilm_cg.cu); S stored row-major as hi/lo FP32
+size_t cgff_params_size();
+void cgff_params_fill(void* dst, const float* Shi, const float* Slo, const double* b, double* x, const double* w,
+                      int n, int maxiter, double tol, int* iters, double* relres, const int* blk,
+                      const int* bstart, const int* bsize, const int* boff, const float* binv_hi,
+                      const float* binv_lo);
+struct BJBlockTask {
+  const float* Shi;  // problem's S as float-float pairs (n x n row-major)
+  const float* Slo;
+  int n, s, sz;      // block = points [s, s + sz)
+  float* out_hi;     // sz x sz inverse, row-major, float-float
+  float* out_lo;
+};
+int launch_block_inverse(const BJBlockTask* tasks_dev, int ntasks, int max_sz, cudaStream_t st);
+int launch_cg_cluster(const void* params_dev, const int* order, int nprob, int* counter, int max_n, int nclusters,
+                      cudaStream_t st);
+int cg_cluster_count(int nprob, int max_n);
 
 }  // namespace ilm

@@ -427,7 +427,7 @@ __global__ void __launch_bounds__(256) k_schur_pairs_batched(int nprob, const Sc
                                                              const Functional* __restrict__ F,
                                                              const double* __restrict__ w,
                                                              const double* __restrict__ G, int ld, int M,
-                                                             double* __restrict__ Aall) {
+                                                             float* __restrict__ Shi, float* __restrict__ Slo) {
   int lo = 0, hi = nprob - 1;
   const int u = blockIdx.x;
   while (lo < hi) {
@@ -480,11 +480,15 @@ __global__ void __launch_bounds__(256) k_schur_pairs_batched(int nprob, const Sc
       total += Fk.coef[p] * Fl.coef[q] * acc;
     }
   }
-  Aall[P.soff + (size_t)l * N + k] = -w[P.poff + l] * total;
+  // row-major float-float pair: S[k][l] = hi + lo
+  const double v = -w[P.poff + l] * total;
+  const float vh = (float)v;
+  Shi[P.soff + (size_t)k * N + l] = vh;
+  Slo[P.soff + (size_t)k * N + l] = (float)(v - (double)vh);
 }
 
 int schur_build_batched(int nprob, const SchurProbDev* probs_dev, int total_tiles, int Ptot, const int* pt2prob,
-                        const BatchWin& W, const double* w, Functional* F, double* Aall, int max_grid,
+                        const BatchWin& W, const double* w, Functional* F, float* Shi, float* Slo, int max_grid,
                         cudaStream_t st) {
   if (Ptot == 0) return ILM_OK;
   const double* G = nullptr;
@@ -494,7 +498,7 @@ int schur_build_batched(int nprob, const SchurProbDev* probs_dev, int total_tile
                                                             W.by[1], W.wx64[0], W.wx64[1], W.wy64[0], W.wy64[1],
                                                             W.nx64, W.ny64, F);
   ILM_CHECK_LAUNCH();
-  k_schur_pairs_batched<<<total_tiles, dim3(16, 16), 0, st>>>(nprob, probs_dev, F, w, G, ld, ld - 1, Aall);
+  k_schur_pairs_batched<<<total_tiles, dim3(16, 16), 0, st>>>(nprob, probs_dev, F, w, G, ld, ld - 1, Shi, Slo);
   ILM_CHECK_LAUNCH();
   return ILM_OK;
 }

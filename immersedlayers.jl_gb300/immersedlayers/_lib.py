@@ -92,6 +92,7 @@ SIGNATURES = {
     "ilm_batch_layout": [_VP, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)],
     "ilm_batch_solve": [_VP, _VP, _VP, _VP, _VP, _D, _I, _VP],
     "ilm_batch_info": [_VP, C.POINTER(_I), _DP],
+    "ilm_batch_set_precond": [_VP, _I, _I],
     "ilm_batch_set_profiling": [_VP, _I],
     "ilm_batch_stage_times": [_VP, C.POINTER(C.c_float), C.POINTER(_I), C.POINTER(_I)],
     "ilm_batch_stats": [_VP, _DP],

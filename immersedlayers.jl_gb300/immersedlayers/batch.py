@@ -124,6 +124,13 @@ def _stats(self):
     return dict(points=int(st[0]), cells=int(st[1]), sum_npts2=st[2], sum_fft=st[3], nprob=int(st[4]))
 
 
+def _set_precond(self, mode="none", block_size=64):
+    """Schur-CG preconditioner for the following solves: "none" (plain CG)
+    or "bjacobi" (block-Jacobi over ~block_size consecutive points)."""
+    L.call("ilm_batch_set_precond", self._h, {"none": 0, "bjacobi": 1}[mode], int(block_size))
+
+
+BatchSolver.set_precond = _set_precond
 BatchSolver.set_profiling = _profiling
 BatchSolver.stage_times = _stage_times
 BatchSolver.stats = _stats

@@ -247,6 +247,11 @@ ILM_API int ilm_batch_layout(ilm_batch_t b, size_t* field_offsets, size_t* point
  * host<->device copies (capturable in a CUDA graph once tol/maxiter are set). */
 ILM_API int ilm_batch_solve(ilm_batch_t b, const void* fplus, const void* fminus, void* f_out, void* s_out,
                             double tol, int maxiter, ilm_stream_t stream);
+/* Preconditioner of the Schur CG for the following solves: mode 0 = none
+ * (plain CG), 1 = block-Jacobi (inverses of the diagonal blocks of ~block_size
+ * consecutive surface points, FP32, applied inside flexible CG).  The block
+ * inverses are built on the device by this call.                           */
+ILM_API int ilm_batch_set_precond(ilm_batch_t b, int mode, int block_size);
 /* Stage timing: when enabled, ilm_batch_solve records a CUDA event on its
  * stream at each stage boundary; ilm_batch_stage_times returns the elapsed
  * ms per stage (up to 31), the number of stages and the number of kernel
