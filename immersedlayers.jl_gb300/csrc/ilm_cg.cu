@@ -167,7 +167,47 @@ struct CGFFParams {
   const int* boff;     // offset of each block's inverse (row-major bsize^2)
   const float* binv_hi;  // block inverses as float-float pairs
   const float* binv_lo;
+  // optional sparse matrix (CSR over rows; Shi/Slo hold the nnz values)
+  const int* rowptr;
+  const int* colidx;
+  // optional initial guess (warm start)
+  const double* x0;
 };
+
+// y[i - r0] = (S v)_i for a CSR matrix (float-float values), one warp per row
+__device__ void ff_spmv_rows(const CGFFParams& pr, int r0, int r1, const float* __restrict__ vhi,
+                             const float* __restrict__ vlo, double* __restrict__ y) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int i = r0 + warp; i < r1; i += CGC_WARPS) {
+    const int e0 = pr.rowptr[i], e1 = pr.rowptr[i + 1];
+    FF a0{0.f, 0.f}, a1{0.f, 0.f};
+    int e = e0 + lane;
+    for (; e + 32 < e1; e += 64) {
+      const int c0 = __ldg(pr.colidx + e), c1 = __ldg(pr.colidx + e + 32);
+      ff_fma(a0, __ldg(pr.Shi + e), __ldg(pr.Slo + e), vhi[c0], vlo[c0]);
+      ff_fma(a1, __ldg(pr.Shi + e + 32), __ldg(pr.Slo + e + 32), vhi[c1], vlo[c1]);
+    }
+    if (e < e1) {
+      const int c0 = __ldg(pr.colidx + e);
+      ff_fma(a0, __ldg(pr.Shi + e), __ldg(pr.Slo + e), vhi[c0], vlo[c0]);
+    }
+    FF acc = ff_add(a0, a1);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      FF other;
+      other.hi = __shfl_down_sync(0xffffffffu, acc.hi, o);
+      other.lo = __shfl_down_sync(0xffffffffu, acc.lo, o);
+      acc = ff_add(acc, other);
+    }
+    if (lane == 0) y[i - r0] = (double)acc.hi + (double)acc.lo;
+  }
+}
+
+__device__ __forceinline__ void matvec_rows(const CGFFParams& pr, int n, int r0, int r1, const float* vhi,
+                                            const float* vlo, double* y) {
+  if (pr.rowptr) ff_spmv_rows(pr, r0, r1, vhi, vlo, y);
+  else ff_gemv_rows(pr.Shi, pr.Slo, n, r0, r1, vhi, vlo, y);
+}
 
 // z[i - r0] = (M r)_i for rows i in [r0, r1): float-float block-Jacobi (the
 // diagonal blocks of the Dirichlet Schur complement are indefinite with
@@ -226,33 +266,50 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(CGC_THREADS
     const int r0 = min(n, rank * rows), r1 = min(n, r0 + rows);
     const int nr = r1 - r0;
     for (int i = threadIdx.x; i < nr; i += blockDim.x) {
-      xs[i] = 0.0;
+      xs[i] = pr.x0 ? pr.x0[r0 + i] : 0.0;
       bs[i] = pr.b[r0 + i];
-      rs[i] = bs[i];
       ws[i] = pr.w ? pr.w[r0 + i] : 1.0;
     }
+    if (pr.x0) {  // warm start: r = b - S x0
+      for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        const double v = pr.x0[j];
+        const float h = (float)v;
+        vhi[j] = h;
+        vlo[j] = (float)(v - (double)h);
+      }
+      __syncthreads();
+      matvec_rows(pr, n, r0, r1, vhi, vlo, qs);
+      __syncthreads();
+      for (int i = threadIdx.x; i < nr; i += blockDim.x) rs[i] = bs[i] - qs[i];
+    } else {
+      for (int i = threadIdx.x; i < nr; i += blockDim.x) rs[i] = bs[i];
+    }
+    __syncthreads();
+    const bool pre = pr.blk != nullptr;
+    double bb = 0.0, rz = 0.0;
+    for (int i = threadIdx.x; i < nr; i += blockDim.x) {
+      bb += bs[i] * bs[i];
+      rz += ws[i] * rs[i] * rs[i];
+    }
+    block_sum2(bb, rz, red);
+    cluster_sum2(cl, pub, work + 2, slot, bb, rz);
+    slot = slot == 7 ? 1 : slot + 1;
+    // p = r (gathered from every CTA's final slice)
     for (int j = threadIdx.x; j < n; j += blockDim.x) {
-      const double v = pr.b[j];
+      const int c = j / rows;
+      const double v = cl.map_shared_rank(rs, c)[j - c * rows];
       pf[j] = v;
       const float h = (float)v;
       vhi[j] = h;
       vlo[j] = (float)(v - (double)h);
     }
     __syncthreads();
-    const bool pre = pr.blk != nullptr;
     if (pre) {
       apply_bjacobi(pr, r0, r1, vhi, vlo, zs);
       __syncthreads();
+      cl.sync();
     }
-    double bb = 0.0, rz = 0.0;
-    for (int i = threadIdx.x; i < nr; i += blockDim.x) {
-      bb += rs[i] * rs[i];
-      rz += ws[i] * rs[i] * rs[i];
-    }
-    block_sum2(bb, rz, red);
-    cluster_sum2(cl, pub, work + 2, slot, bb, rz);
-    slot = slot == 7 ? 1 : slot + 1;
-    if (pre) {  // p = z = M b, gathered from every CTA's (final) z slice
+    if (pre) {  // p = z = M r, gathered from every CTA's (final) z slice
       for (int j = threadIdx.x; j < n; j += blockDim.x) {
         const int c = j / rows;
         pf[j] = cl.map_shared_rank(zs, c)[j - c * rows];
@@ -272,7 +329,7 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(CGC_THREADS
         vlo[j] = (float)(v - (double)h);
       }
       __syncthreads();
-      ff_gemv_rows(pr.Shi, pr.Slo, n, r0, r1, vhi, vlo, qs);
+      matvec_rows(pr, n, r0, r1, vhi, vlo, qs);
       __syncthreads();
       double pq = 0.0, pr_ = 0.0;
       for (int i = threadIdx.x; i < nr; i += blockDim.x) {
@@ -306,7 +363,7 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(CGC_THREADS
           vlo[j] = (float)(v - (double)h);
         }
         __syncthreads();
-        ff_gemv_rows(pr.Shi, pr.Slo, n, r0, r1, vhi, vlo, qs);
+        matvec_rows(pr, n, r0, r1, vhi, vlo, qs);
         __syncthreads();
         double tr = 0.0, tz = 0.0;
         for (int i = threadIdx.x; i < nr; i += blockDim.x) {
@@ -408,6 +465,14 @@ void cgff_params_fill(void* dst, const float* Shi, const float* Slo, const doubl
                       const int* bstart, const int* bsize, const int* boff, const float* binv_hi,
                       const float* binv_lo) {
   CGFFParams p{Shi, Slo, b, x, w, n, maxiter, tol, iters, relres, blk, bstart, bsize, boff, binv_hi, binv_lo};
+  *static_cast<CGFFParams*>(dst) = p;
+}
+
+void cgff_params_fill_csr(void* dst, const float* vhi, const float* vlo, const int* rowptr, const int* colidx,
+                          const double* b, double* x, const double* x0, const double* w, int n, int maxiter,
+                          double tol, int* iters, double* relres) {
+  CGFFParams p{vhi, vlo, b, x, w, n, maxiter, tol, iters, relres,
+               nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, rowptr, colidx, x0};
   *static_cast<CGFFParams*>(dst) = p;
 }
 

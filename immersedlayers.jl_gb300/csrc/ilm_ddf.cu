@@ -147,6 +147,8 @@ int cache_build_windows(ilm_cache_s* c) {
   for (int dual = 0; dual < 2; ++dual) {
     c->hbx[dual] = W.bx[dual];
     c->hby[dual] = W.by[dual];
+    c->hwx[dual] = W.wx[dual];
+    c->hwy[dual] = W.wy[dual];
     ILM_TRY(upload(c->bx[dual], W.bx[dual].data(), N));
     ILM_TRY(upload(c->by[dual], W.by[dual].data(), N));
     ILM_TRY(upload_typed(c->wx[dual], W.wx[dual], c->dtype));

@@ -201,6 +201,7 @@ struct ilm_cache_s {
   ilm::DevBuf wx[2], wy[2];            // cache dtype
   ilm::DevBuf wx64[2], wy64[2];        // FP64
   std::vector<int> hbx[2], hby[2];
+  std::vector<double> hwx[2], hwy[2];  // host copies of the window weights
   ilm::TileList tiles[4];
   // inverse Laplacian plans per position class
   ilm::ConvPlan conv[4];
@@ -309,6 +310,9 @@ void cgff_params_fill(void* dst, const float* Shi, const float* Slo, const doubl
                       int n, int maxiter, double tol, int* iters, double* relres, const int* blk,
                       const int* bstart, const int* bsize, const int* boff, const float* binv_hi,
                       const float* binv_lo);
+void cgff_params_fill_csr(void* dst, const float* vhi, const float* vlo, const int* rowptr, const int* colidx,
+                          const double* b, double* x, const double* x0, const double* w, int n, int maxiter,
+                          double tol, int* iters, double* relres);
 struct BJBlockTask {
   const float* Shi;  // problem's S as float-float pairs (n x n row-major)
   const float* Slo;

@@ -22,5 +22,7 @@ from .core import (Dual, EdgeGradient, EdgeGradientPrimal, Edges, EdgesDual, Edg
 from .problems import (DirichletPoissonProblem, ILMProblem, ILMSystem, NeumannPoissonProblem, construct_system,
                        prescribed_surface_average_, prescribed_surface_jump_, solve, solve_dirichlet,
                        solve_neumann)
+from .timemarching import (ConstrainedSolution, DirichletHeatConductionProblem, HeatIntegrator, constraint, init,
+                           init_sol, state, step_, temperature, timestep, timestep_fourier)
 
 __all__ = [n for n in dir() if not n.startswith("_")]

@@ -96,6 +96,10 @@ SIGNATURES = {
     "ilm_batch_set_profiling": [_VP, _I],
     "ilm_batch_stage_times": [_VP, C.POINTER(C.c_float), C.POINTER(_I), C.POINTER(_I)],
     "ilm_batch_stats": [_VP, _DP],
+    "ilm_heat_create": [_VP, _D, _D, _DP, _DP, _D, _I, C.POINTER(_VP)],
+    "ilm_heat_destroy": [_VP],
+    "ilm_heat_advance": [_VP, _VP, _VP, _I, _VP],
+    "ilm_heat_info": [_VP, C.POINTER(_I), _DP, C.POINTER(C.c_size_t)],
 }
 _RESTYPES = {"ilm_status_string": C.c_char_p, "ilm_last_error": C.c_char_p}
 

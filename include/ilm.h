@@ -249,8 +249,9 @@ ILM_API int ilm_batch_solve(ilm_batch_t b, const void* fplus, const void* fminus
                             double tol, int maxiter, ilm_stream_t stream);
 /* Preconditioner of the Schur CG for the following solves: mode 0 = none
  * (plain CG), 1 = block-Jacobi (inverses of the diagonal blocks of ~block_size
- * consecutive surface points, FP32, applied inside flexible CG).  The block
- * inverses are built on the device by this call.                           */
+ * consecutive surface points, inverted in FP64 and applied in float-float
+ * arithmetic inside flexible CG).  The block inverses are built on the
+ * device by this call.                                                      */
 ILM_API int ilm_batch_set_precond(ilm_batch_t b, int mode, int block_size);
 /* Stage timing: when enabled, ilm_batch_solve records a CUDA event on its
  * stream at each stage boundary; ilm_batch_stage_times returns the elapsed
@@ -263,6 +264,29 @@ ILM_API int ilm_batch_stage_times(ilm_batch_t b, float* ms, int* nstages, int* l
 ILM_API int ilm_batch_stats(ilm_batch_t b, double* stats);
 /* Per-problem CG iterations and FP64 relative residuals of the last solve. */
 ILM_API int ilm_batch_info(ilm_batch_t b, int* iterations, double* rel_residual);
+
+/* ---- heat conduction with Dirichlet surfaces (time marching) -------------
+ * dT/dt = kappa L T + R sigma - kappa D_s[T_b+ - T_b-],  E T = (T_b+ + T_b-)/2
+ * on Nodes{Primal}, advanced by IF-HERK (Liska-Colonius scheme A) with the
+ * exact lattice integrating factor.  Replaces the DirichletHeatConduction
+ * problem of test/literate/heatconduction.jl:87-189 driven by
+ * ConstrainedSystems' LiskaIFHERK (src/timemarching.jl:4,254-277).
+ * The cache must be a scalar GridScaling cache; bodies must stay at least
+ * the heat-kernel radius plus two cells away from the grid edge.  The stage
+ * Schur complements E exp(tau kappa L) R are assembled once here as sparse
+ * matrices; each step warm-starts the stage CG solves from the last step.  */
+typedef struct ilm_heat_s* ilm_heat_t;
+ILM_API int ilm_heat_create(ilm_cache_t c, double kappa, double dt, const double* tb_plus, const double* tb_minus,
+                            double tol, int maxiter, ilm_heat_t* out);
+ILM_API int ilm_heat_destroy(ilm_heat_t h);
+/* T: device Nodes{Primal} field (cache dtype), advanced in place by nsteps
+ * steps of dt.  sigma_out (optional, device, cache dtype, npts): the last
+ * stage's constraint force.  Returns after the work is queued on `stream`
+ * and the iteration counts of the last step were read back.               */
+ILM_API int ilm_heat_advance(ilm_heat_t h, void* T, void* sigma_out, int nsteps, ilm_stream_t stream);
+/* CG iterations and relative residuals of the three stage solves of the last
+ * step, and the nonzeros of the sparse S(tau) for tau = dt/3, 2dt/3, dt, 0. */
+ILM_API int ilm_heat_info(ilm_heat_t h, int* last_iters, double* last_relres, size_t* nnz);
 
 #ifdef __cplusplus
 }

@@ -796,3 +796,80 @@ def solve_neumann(c: SurfaceCache, vplus, vminus, S=None):
     s = -(surface_curl_cross_T(c, ds) - sstar)
     s = c.inverse_laplacian(s)
     return f, df, s, ds
+
+
+# ---------------------------------------------------------------------------
+# Heat conduction with a Dirichlet surface: IF-HERK time marching
+# (test/literate/heatconduction.jl:66-189, src/timemarching.jl:254-277)
+# ---------------------------------------------------------------------------
+# Liska & Colonius (2016) IF-HERK, scheme "A": c = (0, 1/3, 1),
+# a21 = 1/3, a31 = -1, a32 = 2, b = (0, 3/4, 1/4).
+IFHERK_A = dict(c=(0.0, 1.0 / 3.0, 1.0), a21=1.0 / 3.0, a31=-1.0, a32=2.0, b=(0.0, 0.75, 0.25))
+
+
+def heat_kernel_1d(a, tol=1e-17, rmax=32):
+    """1-D factor of the lattice heat kernel exp(a L5): e^{-2a} I_m(2a)."""
+    from scipy.special import ive
+    if a == 0.0:
+        return np.array([1.0])
+    m = np.arange(0, rmax + 1)
+    k = ive(m, 2.0 * a)            # e^{-2a} I_m(2a)
+    R = int(np.nonzero(k > tol)[0].max()) if np.any(k > tol) else 0
+    k = k[:R + 1]
+    return np.concatenate([k[:0:-1], k])
+
+
+def apply_if(w, a):
+    """exp(a L5) w on an unbounded lattice (zero outside the array)."""
+    from scipy.ndimage import convolve1d
+    k = heat_kernel_1d(a)
+    if k.size == 1:
+        return w.copy()
+    t = convolve1d(w, k, axis=0, mode="constant")
+    return convolve1d(t, k, axis=1, mode="constant")
+
+
+def heat_schur(c: SurfaceCache, a):
+    """S_a = E exp(a L) R (dense, by columns): the stage Schur complement."""
+    N = c.N
+    S = np.empty((N, N))
+    e = np.zeros(N)
+    for col in range(N):
+        e[:] = 0.0
+        e[col] = 1.0
+        S[:, col] = interpolate_scalar(c, apply_if(regularize_scalar(c, e), a))
+    return S
+
+
+def heat_march(c: SurfaceCache, T0, tb_plus, tb_minus, kappa, dt, nsteps, scheme=IFHERK_A):
+    """Advance dT/dt = kappa L T + R sigma - kappa D_s[T] with E T = avg(T_b)
+    by IF-HERK (the DirichletHeatConduction problem of the reference).
+    Returns (T, sigma of the last stage)."""
+    h = c.h
+    cc, a21, a31, a32, b = scheme["c"], scheme["a21"], scheme["a31"], scheme["a32"], scheme["b"]
+    af = kappa * dt / h ** 2     # IF argument of a full step (grid units)
+    jump = tb_plus - tb_minus
+    avg = 0.5 * (tb_plus + tb_minus)
+    r1 = -kappa * surface_divergence(c, jump)
+    Sm = {t: heat_schur(c, af * t) for t in (cc[1], cc[2] - cc[1], 0.0)}
+    T = T0.copy()
+    sig = np.zeros(c.N)
+
+    def F(s):
+        return r1 + regularize_scalar(c, s)
+
+    for _ in range(nsteps):
+        # stage 2
+        yh = apply_if(T + dt * a21 * r1, af * cc[1])
+        s1 = np.linalg.lstsq(Sm[cc[1]], (avg - interpolate_scalar(c, yh)) / (dt * a21), rcond=None)[0]
+        # stage 3
+        U = apply_if(T + dt * a31 * F(s1), af * cc[1])
+        yh = apply_if(U + dt * a32 * r1, af * (cc[2] - cc[1]))
+        s2 = np.linalg.lstsq(Sm[cc[2] - cc[1]], (avg - interpolate_scalar(c, yh)) / (dt * a32), rcond=None)[0]
+        # final update
+        V = apply_if(T + dt * b[0] * F(s1), af * cc[1])
+        yh = apply_if(V + dt * b[1] * F(s2), af * (cc[2] - cc[1])) + dt * b[2] * r1
+        s3 = np.linalg.lstsq(Sm[0.0], (avg - interpolate_scalar(c, yh)) / (dt * b[2]), rcond=None)[0]
+        T = yh + dt * b[2] * regularize_scalar(c, s3)
+        sig = s3
+    return T, sig

@@ -35,6 +35,14 @@ def dirichlet_config1():
     return g, b, fb
 
 
+def heat_case(h=0.02, r=0.4):
+    """Small heat-conduction set-up: [-1.28,1.28]^2 with spacing h, a circle
+    of radius r at ds = 1.4 h (the reference example at a smaller size)."""
+    g = O.Grid.physical((-1.28, 1.28), (-1.28, 1.28), h)
+    b = B.circle(r, ds=1.4 * h)
+    return g, b
+
+
 def oracle_cache(g, b, kind="scalar", ddf="Yang3"):
     return O.SurfaceCache(b.x, b.y, b.nx, b.ny, b.ds, g, kind=kind, ddftype=ddf)
 

@@ -1,0 +1,92 @@
+"""Heat conduction with a Dirichlet surface marched on the device (IF-HERK,
+test/literate/heatconduction.jl:87-189) against the oracle's dense IF-HERK
+march on the same inputs."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+import ilm_oracle as O
+from geometry import heat_case, oracle_cache
+
+
+def rel(a, b):
+    return np.abs(np.asarray(a) - np.asarray(b)).max() / np.abs(np.asarray(b)).max()
+
+
+def _setup(dtype, fourier):
+    import torch
+    import immersedlayers as il
+    og, b = heat_case()
+    g = il.PhysicalGrid((-1.28, 1.28), (-1.28, 1.28), og.h)
+    prob = il.DirichletHeatConductionProblem(
+        g, b, dtype=dtype, phys_params={"diffusivity": 1.0, "Fourier": fourier},
+        bc={"exterior": lambda t, x, c, p, m: il.zeros_surface(c), "interior": lambda t, x, c, p, m: il.ones_surface(c)},
+        timestep_func=il.timestep_fourier)
+    sys = il.construct_system(prob)
+    x, y = og.coords(O.NODES_PRIMAL)
+    T0 = np.exp(-(x[:, None] ** 2 + y[None, :] ** 2) / 0.2 ** 2)
+    u0 = il.init_sol(sys)
+    u0.state.set_numpy(T0)
+    return il, og, b, sys, u0, T0
+
+
+@pytest.mark.parametrize("dtype_name,fourier", [("f64", 0.5), ("f64", 1.0), ("f32", 0.5)])
+def test_heat_march_matches_oracle(cuda, dtype_name, fourier):
+    import torch
+    dtype = torch.float64 if dtype_name == "f64" else torch.float32
+    il, og, b, sys, u0, T0 = _setup(dtype, fourier)
+    integ = il.init(u0, (0.0, 1.0), sys, tol=1e-12, maxiter=500)
+    nsteps = 8
+    integ.step_(nsteps * integ.dt)
+    torch.cuda.synchronize()
+    assert abs(integ.t - nsteps * integ.dt) < 1e-15
+    oc = oracle_cache(og, b)
+    h = og.h
+    T_ref, sig_ref = O.heat_march(oc, T0, np.zeros(oc.N), np.ones(oc.N), 1.0, fourier * h * h, nsteps)
+    T = il.temperature(integ).numpy_components()
+    sig = integ.u.constraint.numpy()
+    info = integ.info()
+    assert max(info["rel_residual"]) <= 1e-12, info
+    if dtype == torch.float64:
+        assert rel(T, T_ref) < 1e-10
+        assert rel(sig, -sig_ref) < 1e-8   # the reference's constraint force is -R sigma
+        # the surface constraint E T = (T+ + T-)/2 holds after every step
+        assert np.abs(O.interpolate_scalar(oc, T) - 0.5).max() < 1e-10
+    else:
+        assert rel(T, T_ref) < 2e-5
+        assert rel(sig, -sig_ref) < 2e-3
+
+
+def test_heat_warm_start_and_restart(cuda):
+    """Two advances of 4 steps equal one advance of 8 (the warm-start state
+    carries over between calls; the iteration counts drop once warm)."""
+    import torch
+    il, og, b, sys, u0, T0 = _setup(torch.float64, 0.5)
+    a = il.init(u0, (0.0, 1.0), sys, tol=1e-12)
+    a.advance(4)
+    it_first = a.info()["iterations"]
+    a.advance(4)
+    it_warm = a.info()["iterations"]
+    b8 = il.init(u0, (0.0, 1.0), sys, tol=1e-12)
+    b8.advance(8)
+    torch.cuda.synchronize()
+    assert rel(a.u.state.numpy_components(), b8.u.state.numpy_components()) < 1e-12
+    assert sum(it_warm) <= sum(it_first)
+    nnz = a.info()["nnz"]
+    assert all(n > 0 for n in nnz) and nnz[3] < nnz[2]
+
+
+def test_heat_rejects_index_scaling_and_large_steps(cuda):
+    import torch
+    import immersedlayers as il
+    og, b = heat_case()
+    g = il.PhysicalGrid((-1.28, 1.28), (-1.28, 1.28), og.h)
+    for scaling, fo in ((il.IndexScaling, 0.5), (il.GridScaling, 10.0)):
+        prob = il.DirichletHeatConductionProblem(
+            g, b, scaling=scaling, phys_params={"diffusivity": 1.0, "Fourier": fo},
+            bc={"exterior": lambda c, p: np.zeros(len(c)), "interior": lambda c, p: np.ones(len(c))},
+            timestep_func=il.timestep_fourier)
+        sys = il.construct_system(prob)
+        with pytest.raises((ValueError, il._lib.ILMError)):
+            il.init(il.init_sol(sys), (0.0, 1.0), sys)
