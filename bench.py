@@ -44,6 +44,7 @@ def parse():
     ap.add_argument("--precond", default="bjacobi", choices=["none", "bjacobi"])
     ap.add_argument("--block", type=int, default=64)
     ap.add_argument("--cpu-sample-cols", type=int, default=32)
+    ap.add_argument("--heat-steps", type=int, default=1000, help="heat-conduction leg (0: skip)")
     return ap.parse_args()
 
 
@@ -242,6 +243,7 @@ def run_ours(args, rank, world, dist):
     # end to end through the public API from host buffers
     e2e = _e2e(args, specs, stream, dt)
     stencil = _stencil_gbs(stream, flush, hbm)
+    heat = _heat_scale(args, stream) if (rank == 0 and args.heat_steps > 0) else None
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -249,6 +251,7 @@ def run_ours(args, rank, world, dist):
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
                 "config": config(args, world), "roofline": roofline, "e2e": e2e, "gpu_launches": launches * args.steps,
                 "clocks": clocks, "setup_s": setup_s, "solvers": solvers, "stencil_gbs": stencil,
+                "heat": heat,
                 "stages_ms": dict(zip(names, [round(x, 4) for x in stage_ms])),
                 "cg_iterations": {"mean": float(np.mean(its)), "max": int(its.max())},
                 "max_rel_residual": float(rr.max())}
@@ -285,6 +288,60 @@ def _stencil_gbs(stream, flush, hbm):
         t = statistics.median(x.elapsed_time(y) for x, y in ms) / 1000.0
         nbytes = (a.data.numel() + b.data.numel()) * 4
         out[name] = {"gbs": nbytes / t / 1e9, "frac": nbytes / t / 1e9 / hbm, "bytes": nbytes, "ms": 1000 * t}
+    return out
+
+
+def _heat_scale(args, stream):
+    """Heat conduction at scale: 1024^2 grid, 3 bodies, kappa = 1,
+    dt = 0.5 h^2, IF-HERK steps on the device through the public API
+    (init / advance); FP64 and FP32 caches, FP32 error against FP64.
+    Two point sets on the same bodies: 4096 points (ds ~ 0.25 h, stage Schur
+    condition ~1e15: CG on the range with a per-stage iteration cap) and
+    ds = 1.4 h (well posed, CG to 1e-10)."""
+    import numpy as np
+    import torch
+    import immersedlayers as il
+    from immersedlayers import workloads as W
+    ones = lambda c, p: np.ones(len(c))  # noqa: E731
+    out = {"workload": "1024^2 dual nodes, h=0.005, circle r=0.3 + ellipse 0.4x0.1 + hexagon side 0.25, "
+                       "kappa=1, dt=0.5h^2, T_b=1 both sides, T0=exp(-r^2/(2*0.2^2))", "steps": args.heat_steps}
+    for variant, kw, tol, maxiter in (("npts4096", {}, 1e-10, 20), ("ds1.4h", {"ds_factor": 1.4}, 1e-10, 1000)):
+        d = W.operators_at_scale(**kw)
+        g = il.PhysicalGrid(h=d["h"], nx=d["n"])
+        x, y = g.coordinates(0, 0)
+        T0 = d["T0"](x, y)
+        res = {"npts": len(d["bodies"]), "tol": tol, "maxiter_per_stage": maxiter}
+        fields = {}
+        for name, dt in (("f64", torch.float64), ("f32", torch.float32)):
+            prob = il.DirichletHeatConductionProblem(g, d["bodies"], dtype=dt,
+                                                     phys_params={"diffusivity": d["kappa"]},
+                                                     bc={"exterior": ones, "interior": ones})
+            sys_ = il.construct_system(prob)
+            u0 = il.init_sol(sys_)
+            u0.state.set_numpy(T0)
+            t0 = time.perf_counter()
+            integ = il.init(u0, (0.0, 1.0), sys_, dt=d["dt"], tol=tol, maxiter=maxiter, stream=stream)
+            torch.cuda.synchronize()
+            setup = time.perf_counter() - t0
+            integ.advance(3)
+            integ.u.state.data.copy_(u0.state.data)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            integ.advance(args.heat_steps)
+            e1.record(stream)
+            stream.synchronize()
+            ms = e0.elapsed_time(e1)
+            info = integ.info()
+            fields[name] = integ.u.state.data.double()
+            res[name] = {"ms_per_step": ms / args.heat_steps, "steps_per_s": 1000.0 * args.heat_steps / ms,
+                         "setup_s": setup, "cg_iterations_last_step": info["iterations"],
+                         "rel_residual_last_step": info["rel_residual"], "schur_nnz": info["nnz"]}
+            del integ, sys_
+        ref = fields["f64"]
+        res["f32_rel_err_vs_f64"] = float((fields["f32"] - ref).abs().max() / ref.abs().max())
+        out[variant] = res
     return out
 
 

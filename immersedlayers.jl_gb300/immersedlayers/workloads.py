@@ -89,3 +89,53 @@ def dirichlet_plain():
     th = np.arctan2(b.y, b.x)
     fb = np.cos(th) + 0.1 * np.random.default_rng(1).standard_normal(len(b))
     return (-2.0, 2.0), (-2.0, 2.0), h, b, fb
+
+
+def _split_counts(perims, total, multiple_last=6):
+    """Points per body in proportion to perimeter, summing to `total`, the
+    last body's count a multiple of `multiple_last` (a hexagon's six sides)."""
+    P = float(sum(perims))
+    n_last = int(round(total * perims[-1] / P / multiple_last)) * multiple_last
+    rest = total - n_last
+    Q = float(sum(perims[:-1]))
+    counts = [int(round(rest * p / Q)) for p in perims[:-1]]
+    counts[-1] += rest - sum(counts)
+    return counts + [n_last]
+
+
+def operators_at_scale(npts=4096, seed=2, ds_factor=None):
+    """Operators-at-scale / heat configuration: 1024 x 1024 dual nodes with
+    h = 0.005 centred on the origin; a circle r = 0.3, an ellipse 0.4 x 0.1
+    rotated by U(0, pi) and a regular hexagon of side 0.25 at non-overlapping
+    centres (rejection sampling, margin >= 4h, numpy default_rng(seed)),
+    `npts` points split by perimeter (ds ~ 0.25 h at 4096 points).  Heat
+    data: kappa = 1, dt = 0.5 h^2, 1000 steps, T0 = exp(-r^2 / (2 0.2^2)),
+    surface temperature 1 on both sides of every surface.  With `ds_factor`
+    the same bodies get points ds_factor * h apart instead of `npts` in total.
+    Returns dict(n, h, bodies, kappa, dt, nsteps, T0(x, y))."""
+    n, h = 1024, 0.005
+    rng = np.random.default_rng(seed)
+    ang = float(rng.uniform(0.0, math.pi))
+    a_e, b_e = 0.4, 0.1
+    he = ((a_e - b_e) / (a_e + b_e)) ** 2
+    per = [2 * math.pi * 0.3, math.pi * (a_e + b_e) * (1 + 3 * he / (10 + math.sqrt(4 - 3 * he))), 6 * 0.25]
+    radii = [0.3, 0.4, 0.25]
+    centres = []
+    lim = 1.6
+    while len(centres) < 3:
+        c = rng.uniform(-lim + radii[len(centres)], lim - radii[len(centres)], size=2)
+        if all(np.hypot(*(c - q)) >= radii[len(centres)] + rq + 4 * h for q, rq in zip(centres, radii)):
+            centres.append(c)
+    if ds_factor is not None:
+        npts = 6 * int(round(sum(per) / (ds_factor * h) / 6))
+    counts = _split_counts(per, npts)
+    bl = B.BodyList()
+    bl.append(B.circle(0.3, n=counts[0], center=tuple(centres[0])))
+    bl.append(B.ellipse(a_e, b_e, n=counts[1], center=tuple(centres[1]), angle=ang))
+    bl.append(B.hexagon(0.25, ds=per[2] / counts[2], center=tuple(centres[2])))
+    assert len(bl) == npts, len(bl)
+
+    def T0(x, y):
+        return np.exp(-(x[:, None] ** 2 + y[None, :] ** 2) / (2 * 0.2 ** 2))
+
+    return dict(n=n, h=h, bodies=bl, kappa=1.0, dt=0.5 * h * h, nsteps=1000, T0=T0)

@@ -35,11 +35,11 @@ def dirichlet_config1():
     return g, b, fb
 
 
-def heat_case(h=0.02, r=0.4):
+def heat_case(h=0.02, r=0.4, ds_factor=1.4):
     """Small heat-conduction set-up: [-1.28,1.28]^2 with spacing h, a circle
     of radius r at ds = 1.4 h (the reference example at a smaller size)."""
     g = O.Grid.physical((-1.28, 1.28), (-1.28, 1.28), h)
-    b = B.circle(r, ds=1.4 * h)
+    b = B.circle(r, ds=ds_factor * h)
     return g, b
 
 
