@@ -234,6 +234,13 @@ struct ilm_batch_s {
   bool params_dirty = false;
   DevBuf bj_blk, bj_start, bj_size, bj_off, bj_inv, bj_inv_lo, bj_tasks;
   std::vector<int> bj_first;  // first block of each problem
+  // learned banded preconditioner (mode 2): coefficients per packed point,
+  // body segments as local indices
+  int band_k = -1;
+  DevBuf band, lseg_start, lseg_len;
+  // host copies of the points (features of the learned preconditioner)
+  std::vector<double> hx, hy, hnx, hny, hds;
+  DevBuf dpoff;  // point offsets on the device (Schur products)
   int profiling = 0;
   cudaEvent_t ev[32] = {};
   int nev = 0, launches = 0;
@@ -270,6 +277,54 @@ int up_typed(DevBuf& b, const std::vector<double>& v, int dtype) {
       __VA_ARGS__;             \
     }                          \
   } while (0)
+
+// CG parameter records for the current preconditioner, tolerance and limit
+int ensure_cg_params(ilm_batch_s* b, double tol, int maxiter) {
+  if (tol == b->cg_tol && maxiter == b->cg_maxiter && !b->params_dirty) return ILM_OK;
+  b->params_dirty = false;
+  std::vector<unsigned char> cg((size_t)b->nprob * cgff_params_size());
+  const bool pre = b->precond == 1;
+  const int P = 2 * b->band_k + 1;
+  for (int p = 0; p < b->nprob; ++p) {
+    const size_t o = b->poff[p];
+    void* dst = cg.data() + (size_t)p * cgff_params_size();
+    cgff_params_fill(dst, b->Shi.as<float>() + b->soff[p], b->Slo.as<float>() + b->soff[p],
+                     b->rhs64.as<double>() + o, b->x64.as<double>() + o, b->ds64.as<double>() + o, b->probs[p].npts,
+                     maxiter, tol, b->iters.as<int>() + p, b->relres.as<double>() + p,
+                     pre ? b->bj_blk.as<int>() + o : nullptr, pre ? b->bj_start.as<int>() + b->bj_first[p] : nullptr,
+                     pre ? b->bj_size.as<int>() + b->bj_first[p] : nullptr,
+                     pre ? b->bj_off.as<int>() + b->bj_first[p] : nullptr, pre ? b->bj_inv.as<float>() : nullptr,
+                     pre ? b->bj_inv_lo.as<float>() : nullptr);
+    if (b->precond == 2)
+      cgff_params_set_band(dst, b->band.as<float>() + o * P, b->band_k, b->lseg_start.as<int>() + o,
+                           b->lseg_len.as<int>() + o);
+  }
+  ILM_TRY(up(b->cgp, cg));
+  b->cg_tol = tol;
+  b->cg_maxiter = maxiter;
+  return ILM_OK;
+}
+
+// y = S x for every problem (float-float S, FP64 accumulation), one warp per row
+__global__ void k_batch_schur_apply(int Ptot, const int* __restrict__ pt2prob, const size_t* __restrict__ poff,
+                                    const float* __restrict__ Shi, const float* __restrict__ Slo,
+                                    const size_t* __restrict__ soff, const double* __restrict__ x,
+                                    double* __restrict__ y) {
+  const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (row >= Ptot) return;
+  const int p = pt2prob[row];
+  const size_t o = poff[p];
+  const int n = (int)(poff[p + 1] - o);
+  const int i = row - (int)o;
+  const float* sh = Shi + soff[p] + (size_t)i * n;
+  const float* sl = Slo + soff[p] + (size_t)i * n;
+  double acc = 0.0;
+  for (int j = lane; j < n; j += 32) acc += ((double)sh[j] + (double)sl[j]) * x[o + j];
+#pragma unroll
+  for (int s = 16; s > 0; s >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, s);
+  if (lane == 0) y[row] = acc;
+}
 
 }  // namespace
 
@@ -311,6 +366,11 @@ int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* 
   for (int k = 0; k < Ptot; ++k)
     ILM_REQUIRE(isfinite(x[k]) && isfinite(y[k]) && isfinite(nrmx[k]) && isfinite(nrmy[k]) && isfinite(ds[k]),
                 "batch: non-finite point data at %d", k);
+  B->hx.assign(x, x + Ptot);
+  B->hy.assign(y, y + Ptot);
+  B->hnx.assign(nrmx, nrmx + Ptot);
+  B->hny.assign(nrmy, nrmy + Ptot);
+  B->hds.assign(ds, ds + Ptot);
 
   // ---- host set-up: DDF windows and tile lists, packed -------------------
   std::vector<int> hbx[2], hby[2], hp2p(Ptot);
@@ -605,25 +665,7 @@ int ilm_batch_solve(ilm_batch_t b, const void* fplus, const void* fminus, void* 
   cudaStream_t st = as_stream(stream);
   const int dt = b->dtype;
   const int Ptot = b->Ptot;
-  if (tol != b->cg_tol || maxiter != b->cg_maxiter || b->params_dirty) {
-    b->params_dirty = false;
-    std::vector<unsigned char> cg((size_t)b->nprob * cgff_params_size());
-    const bool pre = b->precond == 1;
-    for (int p = 0; p < b->nprob; ++p) {
-      const size_t o = b->poff[p];
-      cgff_params_fill(cg.data() + (size_t)p * cgff_params_size(), b->Shi.as<float>() + b->soff[p],
-                       b->Slo.as<float>() + b->soff[p], b->rhs64.as<double>() + o, b->x64.as<double>() + o,
-                       b->ds64.as<double>() + o, b->probs[p].npts, maxiter, tol, b->iters.as<int>() + p,
-                       b->relres.as<double>() + p, pre ? b->bj_blk.as<int>() + o : nullptr,
-                       pre ? b->bj_start.as<int>() + b->bj_first[p] : nullptr,
-                       pre ? b->bj_size.as<int>() + b->bj_first[p] : nullptr,
-                       pre ? b->bj_off.as<int>() + b->bj_first[p] : nullptr, pre ? b->bj_inv.as<float>() : nullptr,
-                       pre ? b->bj_inv_lo.as<float>() : nullptr);
-    }
-    ILM_TRY(up(b->cgp, cg));
-    b->cg_tol = tol;
-    b->cg_maxiter = maxiter;
-  }
+  ILM_TRY(ensure_cg_params(b, tol, maxiter));
   const int pb = std::min(1024, (Ptot + 255) / 256);
   b->nev = 0;
   b->launches = 0;
@@ -695,7 +737,8 @@ int ilm_batch_solve(ilm_batch_t b, const void* fplus, const void* fminus, void* 
 
 int ilm_batch_set_precond(ilm_batch_t b, int mode, int block_size) {
   ILM_REQUIRE(b, "null batch");
-  ILM_REQUIRE(mode == 0 || mode == 1, "batch: unknown preconditioner %d", mode);
+  ILM_REQUIRE(mode == 0 || mode == 1 || mode == 2, "batch: unknown preconditioner %d", mode);
+  ILM_REQUIRE(mode != 2 || b->band_k >= 0, "batch: no learned preconditioner set (ilm_batch_set_learned)");
   if (mode == 1) {
     ILM_REQUIRE(block_size >= 4 && block_size <= 72, "batch: block size %d outside [4, 72]", block_size);
     if (b->bj_block != block_size) {
@@ -792,6 +835,86 @@ int ilm_batch_info(ilm_batch_t b, int* iterations, double* rel_residual) {
     ILM_CHECK_CUDA(cudaMemcpy(iterations, b->iters.p, (size_t)b->nprob * sizeof(int), cudaMemcpyDeviceToHost));
   if (rel_residual)
     ILM_CHECK_CUDA(cudaMemcpy(rel_residual, b->relres.p, (size_t)b->nprob * sizeof(double), cudaMemcpyDeviceToHost));
+  return ILM_OK;
+}
+
+int ilm_batch_set_learned(ilm_batch_t b, ilm_net_t net, const int* body_start) {
+  ILM_REQUIRE(b && net && body_start, "batch_set_learned: null argument");
+  ILM_REQUIRE(net_nfeat(net) == 8, "batch_set_learned: the network must read the 8 point features");
+  const int K = net_band(net), P = 2 * K + 1;
+  const int Ptot = b->Ptot;
+  std::vector<int> ls(Ptot), ll(Ptot), as(Ptot);
+  for (int p = 0; p < b->nprob; ++p) {
+    const int o = (int)b->poff[p], n = b->probs[p].npts;
+    for (int k = 0; k < n; ++k) {
+      const int s = body_start[o + k];
+      ILM_REQUIRE(s >= 0 && s <= k && (k == 0 ? s == 0 : (s == body_start[o + k - 1] || s == k)),
+                  "batch_set_learned: body starts of problem %d are not contiguous at point %d", p, k);
+      ls[o + k] = s;
+    }
+    for (int k = 0; k < n;) {  // body lengths
+      int e = k + 1;
+      while (e < n && ls[o + e] == ls[o + k]) ++e;
+      ILM_REQUIRE(e - k >= std::max(3, P), "batch_set_learned: body of %d points in problem %d (need >= %d)", e - k,
+                  p, std::max(3, P));
+      for (int q = k; q < e; ++q) {
+        ll[o + q] = e - k;
+        as[o + q] = o + k;
+      }
+      k = e;
+    }
+  }
+  std::vector<float> feat((size_t)Ptot * 8);
+  for (int p = 0; p < b->nprob; ++p) {
+    const int o = (int)b->poff[p], n = b->probs[p].npts;
+    std::vector<int> s0(n), l0(n);
+    for (int k = 0; k < n; ++k) {
+      s0[k] = ls[o + k];
+      l0[k] = ll[o + k];
+    }
+    ILM_TRY(ilm_point_features(n, b->hx.data() + o, b->hy.data() + o, b->hnx.data() + o, b->hny.data() + o,
+                               b->hds.data() + o, s0.data(), l0.data(), b->probs[p].h, feat.data() + (size_t)o * 8));
+  }
+  DevBuf dfeat, das, dll;
+  ILM_TRY(up(dfeat, feat));
+  ILM_TRY(up(das, as));
+  ILM_TRY(up(dll, ll));
+  ILM_TRY(up(b->lseg_start, ls));
+  ILM_TRY(up(b->lseg_len, ll));
+  ILM_TRY(b->band.alloc((size_t)Ptot * P * sizeof(float)));
+  ILM_TRY(net_forward_packed(net, Ptot, dfeat.as<float>(), das.as<int>(), dll.as<int>(), b->band.as<float>(), nullptr));
+  ILM_CHECK_CUDA(cudaDeviceSynchronize());
+  b->band_k = K;
+  b->precond = 2;
+  b->params_dirty = true;
+  return ILM_OK;
+}
+
+int ilm_batch_schur_apply(ilm_batch_t b, const double* x, double* y, ilm_stream_t stream) {
+  ILM_REQUIRE(b && x && y, "batch_schur_apply: null argument");
+  if (!b->dpoff.p) {
+    ILM_TRY(up(b->dpoff, b->poff));
+  }
+  DevBuf dsoff;
+  ILM_TRY(up(dsoff, b->soff));
+  cudaStream_t st = as_stream(stream);
+  k_batch_schur_apply<<<(b->Ptot * 32 + 255) / 256, 256, 0, st>>>(b->Ptot, b->pt2prob.as<int>(),
+                                                                  b->dpoff.as<size_t>(), b->Shi.as<float>(),
+                                                                  b->Slo.as<float>(), dsoff.as<size_t>(), x, y);
+  ILM_CHECK_LAUNCH();
+  ILM_CHECK_CUDA(cudaStreamSynchronize(st));
+  return ILM_OK;
+}
+
+int ilm_batch_schur_solve(ilm_batch_t b, const double* rhs, double* x, double tol, int maxiter,
+                          ilm_stream_t stream) {
+  ILM_REQUIRE(b && rhs && x, "batch_schur_solve: null argument");
+  ILM_REQUIRE(tol > 0 && maxiter > 0, "batch_schur_solve: bad tolerance / iteration limit");
+  cudaStream_t st = as_stream(stream);
+  ILM_TRY(ensure_cg_params(b, tol, maxiter));
+  ILM_CHECK_CUDA(cudaMemcpyAsync(b->rhs64.p, rhs, (size_t)b->Ptot * 8, cudaMemcpyDeviceToDevice, st));
+  ILM_TRY(launch_cg_cluster(b->cgp.p, b->order.as<int>(), b->nprob, b->counter.as<int>(), b->maxN, b->nclusters, st));
+  ILM_CHECK_CUDA(cudaMemcpyAsync(x, b->x64.p, (size_t)b->Ptot * 8, cudaMemcpyDeviceToDevice, st));
   return ILM_OK;
 }
 

@@ -172,6 +172,13 @@ struct CGFFParams {
   const int* colidx;
   // optional initial guess (warm start)
   const double* x0;
+  // optional learned banded preconditioner M r = W^-1 C^T C r: C has
+  // 2 band_k + 1 coefficients per row (row-major), circular within each
+  // body; seg_start / seg_len give each point's body (local indices)
+  const float* band;
+  int band_k;
+  const int* seg_start;
+  const int* seg_len;
 };
 
 // y[i - r0] = (S v)_i for a CSR matrix (float-float values), one warp per row
@@ -233,6 +240,55 @@ __device__ void apply_bjacobi(const CGFFParams& pr, int r0, int r1, const float*
   }
 }
 
+__device__ __forceinline__ int seg_nb(int j, int s, int L, int t) {
+  if (L < 1) return j;
+  int q = (j - s + t) % L;
+  q += q < 0 ? L : 0;
+  return s + q;
+}
+
+// z[i - r0] = (W^-1 C^T C r)_i for rows i in [r0, r1), in float-float
+// arithmetic (an FP32 application changes M from one iteration to the next
+// by rounding and stalls flexible CG near 1e-7 on these indefinite Schur
+// complements).  Each row needs u_j = (C r)_j at its 2K+1 band neighbours
+// j; they are formed on the fly (same body, circular), two threads per row.
+__device__ void apply_band(const CGFFParams& pr, int r0, int r1, const float* __restrict__ rhi,
+                           const float* __restrict__ rlo, const double* __restrict__ ws, double* __restrict__ z) {
+  const int K = pr.band_k, P = 2 * K + 1;
+  const int half = threadIdx.x & 1;
+  const int nrow = r1 - r0;
+  for (int base = 0; base < nrow; base += blockDim.x / 2) {
+    const int row = base + (threadIdx.x >> 1);
+    FF zacc{0.f, 0.f};
+    if (row < nrow) {
+      const int i = r0 + row;
+      const int s = __ldg(pr.seg_start + i), L = __ldg(pr.seg_len + i);
+      // thread `half` takes t = -K + half, -K + half + 2, ...
+      for (int t = -K + half; t <= K; t += 2) {
+        const int j = seg_nb(i, s, L, -t);
+        const float* __restrict__ cj = pr.band + (size_t)j * P;
+        FF u{0.f, 0.f};
+        for (int t2 = -K; t2 <= K; ++t2) {
+          const int q = seg_nb(j, s, L, t2);
+          ff_fma(u, __ldg(cj + t2 + K), 0.f, rhi[q], rlo[q]);
+        }
+        ff_fma(zacc, __ldg(cj + t + K), 0.f, u.hi, u.lo);
+      }
+    }
+    FF other;
+    other.hi = __shfl_xor_sync(0xffffffffu, zacc.hi, 1);
+    other.lo = __shfl_xor_sync(0xffffffffu, zacc.lo, 1);
+    zacc = ff_add(zacc, other);
+    if (row < nrow && half == 0) z[row] = ((double)zacc.hi + (double)zacc.lo) / ws[row];
+  }
+}
+
+__device__ __forceinline__ void apply_precond(const CGFFParams& pr, int r0, int r1, const float* rhi,
+                                              const float* rlo, const double* ws, double* z) {
+  if (pr.band) apply_band(pr, r0, r1, rhi, rlo, ws, z);
+  else apply_bjacobi(pr, r0, r1, rhi, rlo, z);
+}
+
 // Persistent: each cluster takes problems from a work queue (largest first,
 // `order`) until the queue is empty.  `counter` must be 0 at launch.
 __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(CGC_THREADS, 4)
@@ -285,7 +341,7 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(CGC_THREADS
       for (int i = threadIdx.x; i < nr; i += blockDim.x) rs[i] = bs[i];
     }
     __syncthreads();
-    const bool pre = pr.blk != nullptr;
+    const bool pre = pr.blk != nullptr || pr.band != nullptr;
     double bb = 0.0, rz = 0.0;
     for (int i = threadIdx.x; i < nr; i += blockDim.x) {
       bb += bs[i] * bs[i];
@@ -305,7 +361,7 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(CGC_THREADS
     }
     __syncthreads();
     if (pre) {
-      apply_bjacobi(pr, r0, r1, vhi, vlo, zs);
+      apply_precond(pr, r0, r1, vhi, vlo, ws, zs);
       __syncthreads();
       cl.sync();
     }
@@ -402,7 +458,7 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(CGC_THREADS
           vlo[j] = (float)(v - (double)h);
         }
         __syncthreads();
-        apply_bjacobi(pr, r0, r1, vhi, vlo, zs);
+        apply_precond(pr, r0, r1, vhi, vlo, ws, zs);
         __syncthreads();
         double zq = 0.0, d1 = 0.0;
         for (int i = threadIdx.x; i < nr; i += blockDim.x) zq += ws[i] * zs[i] * qs[i];
@@ -474,6 +530,14 @@ void cgff_params_fill_csr(void* dst, const float* vhi, const float* vlo, const i
   CGFFParams p{vhi, vlo, b, x, w, n, maxiter, tol, iters, relres,
                nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, rowptr, colidx, x0};
   *static_cast<CGFFParams*>(dst) = p;
+}
+
+void cgff_params_set_band(void* dst, const float* band, int band_k, const int* seg_start, const int* seg_len) {
+  CGFFParams* p = static_cast<CGFFParams*>(dst);
+  p->band = band;
+  p->band_k = band_k;
+  p->seg_start = seg_start;
+  p->seg_len = seg_len;
 }
 
 // ---------------------------------------------------------------------------

@@ -310,6 +310,11 @@ void cgff_params_fill(void* dst, const float* Shi, const float* Slo, const doubl
                       int n, int maxiter, double tol, int* iters, double* relres, const int* blk,
                       const int* bstart, const int* bsize, const int* boff, const float* binv_hi,
                       const float* binv_lo);
+int net_forward_packed(ilm_net_t n, int N, const float* feat, const int* sst, const int* sln, float* band,
+                       cudaStream_t st);
+int net_band(ilm_net_t n);
+int net_nfeat(ilm_net_t n);
+void cgff_params_set_band(void* dst, const float* band, int band_k, const int* seg_start, const int* seg_len);
 void cgff_params_fill_csr(void* dst, const float* vhi, const float* vlo, const int* rowptr, const int* colidx,
                           const double* b, double* x, const double* x0, const double* w, int n, int maxiter,
                           double tol, int* iters, double* relres);

@@ -96,6 +96,18 @@ SIGNATURES = {
     "ilm_batch_set_profiling": [_VP, _I],
     "ilm_batch_stage_times": [_VP, C.POINTER(C.c_float), C.POINTER(_I), C.POINTER(_I)],
     "ilm_batch_stats": [_VP, _DP],
+    "ilm_net_create": [_I, _I, _I, _I, C.POINTER(_VP)],
+    "ilm_net_destroy": [_VP],
+    "ilm_net_nparams": [_VP, C.POINTER(C.c_size_t)],
+    "ilm_net_set_params": [_VP, C.POINTER(C.c_float)],
+    "ilm_net_get_params": [_VP, C.POINTER(C.c_float)],
+    "ilm_net_forward": [_VP, _I, _VP, _VP, _VP, _VP, _VP],
+    "ilm_net_loss_grad": [_VP, _I, _I, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _DP, C.POINTER(C.c_float), _VP],
+    "ilm_net_train_step": [_VP, _I, _I, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _D, _VP, _VP],
+    "ilm_point_features": [_I, _DP, _DP, _DP, _DP, _DP, C.POINTER(_I), C.POINTER(_I), _D, C.POINTER(C.c_float)],
+    "ilm_batch_set_learned": [_VP, _VP, C.POINTER(_I)],
+    "ilm_batch_schur_apply": [_VP, _VP, _VP, _VP],
+    "ilm_batch_schur_solve": [_VP, _VP, _VP, _D, _I, _VP],
     "ilm_heat_create": [_VP, _D, _D, _DP, _DP, _D, _I, C.POINTER(_VP)],
     "ilm_heat_destroy": [_VP],
     "ilm_heat_advance": [_VP, _VP, _VP, _I, _VP],

@@ -125,9 +125,49 @@ def _stats(self):
 
 
 def _set_precond(self, mode="none", block_size=64):
-    """Schur-CG preconditioner for the following solves: "none" (plain CG)
-    or "bjacobi" (block-Jacobi over ~block_size consecutive points)."""
-    L.call("ilm_batch_set_precond", self._h, {"none": 0, "bjacobi": 1}[mode], int(block_size))
+    """Schur-CG preconditioner for the following solves: "none" (plain CG),
+    "bjacobi" (block-Jacobi over ~block_size consecutive points) or
+    "learned" (the band set by `set_learned`)."""
+    L.call("ilm_batch_set_precond", self._h, {"none": 0, "bjacobi": 1, "learned": 2}[mode], int(block_size))
+
+
+def _body_starts(self):
+    """Per packed point, the local index of its body's first point."""
+    out = []
+    for s in self.specs:
+        fi = s.bl.firstindices()
+        for b in range(len(fi) - 1):
+            out.append(np.full(fi[b + 1] - fi[b], fi[b], dtype=np.int32))
+    return np.ascontiguousarray(np.concatenate(out), dtype=np.int32)
+
+
+def _set_learned(self, net):
+    """Run the learned preconditioner's network over this batch's points and
+    switch the Schur CG to it."""
+    bs = _body_starts(self)
+    L.call("ilm_batch_set_learned", self._h, net._h, bs.ctypes.data_as(C.POINTER(C.c_int)))
+
+
+def _schur_apply(self, x, y=None, stream=None):
+    """y = S x for every problem (device FP64 packed vectors)."""
+    if y is None:
+        y = torch.empty_like(x)
+    L.call("ilm_batch_schur_apply", self._h, _ptr(x), _ptr(y), _stream_ptr(stream))
+    return y
+
+
+def _schur_solve(self, rhs, x=None, tol=1e-10, maxiter=20000, stream=None):
+    """S x = rhs for every problem with the batch's CG (device FP64)."""
+    if x is None:
+        x = torch.empty_like(rhs)
+    L.call("ilm_batch_schur_solve", self._h, _ptr(rhs), _ptr(x), float(tol), int(maxiter), _stream_ptr(stream))
+    return x
+
+
+BatchSolver.body_starts = _body_starts
+BatchSolver.set_learned = _set_learned
+BatchSolver.schur_apply = _schur_apply
+BatchSolver.schur_solve = _schur_solve
 
 
 BatchSolver.set_precond = _set_precond

@@ -139,3 +139,23 @@ def operators_at_scale(npts=4096, seed=2, ds_factor=None):
         return np.exp(-(x[:, None] ** 2 + y[None, :] ** 2) / (2 * 0.2 ** 2))
 
     return dict(n=n, h=h, bodies=bl, kappa=1.0, dt=0.5 * h * h, nsteps=1000, T0=T0)
+
+
+def learned_problem(i, n=512):
+    """Learned-preconditioner configuration, problem i: n x n dual nodes with
+    h = 4/n, one star-shaped body r(theta) = 0.5 (1 + sum_{k=2..6} a_k
+    cos(k theta + phi_k)), a_k ~ U(0, 0.08), phi_k ~ U(0, 2 pi), with
+    N_p ~ U{256..1024} points equally spaced in arc length (numpy
+    default_rng(i); training seeds 10^6 + j, held-out 2 10^6 + j).
+    Returns (n, h, BodyList)."""
+    rng = np.random.default_rng(int(i))
+    amps = rng.uniform(0.0, 0.08, 5)
+    phases = rng.uniform(0.0, 2 * math.pi, 5)
+    npts = int(rng.integers(256, 1025))
+    bl = B.BodyList()
+    bl.append(B.star(0.5, amps, phases, npts))
+    return n, 4.0 / n, bl
+
+
+LEARNED_TRAIN_SEED = 1_000_000
+LEARNED_TEST_SEED = 2_000_000

@@ -265,6 +265,53 @@ ILM_API int ilm_batch_stats(ilm_batch_t b, double* stats);
 /* Per-problem CG iterations and FP64 relative residuals of the last solve. */
 ILM_API int ilm_batch_info(ilm_batch_t b, int* iterations, double* rel_residual);
 
+/* ---- learned Schur-complement preconditioner ------------------------------
+ * No counterpart in the reference (its Schur solve is the dense LU of
+ * test/literate/problems.jl:291); it accelerates the device CG that replaces
+ * that LU.  A 1-D convolutional network over arc length (circular within each
+ * body, kernel 5, ReLU, `nlayers` layers of `width` channels) maps 8 point
+ * features (ilm_point_features) to a band of 2*band+1 coefficients per point,
+ * C; the preconditioner is M r = W^-1 C^T C r with W = diag(ds), self-adjoint
+ * in the ds-weighted inner product in which W S is symmetric.  FP32 master
+ * weights, BF16 copies read by every pass, FP32 accumulation.
+ * Point arrays below are packed over problems/bodies; seg_start/seg_len give
+ * each point's body as [seg_start, seg_start + seg_len) in packed indices.  */
+typedef struct ilm_net_s* ilm_net_t;
+ILM_API int ilm_net_create(int nfeat, int width, int nlayers, int band, ilm_net_t* out);
+ILM_API int ilm_net_destroy(ilm_net_t n);
+ILM_API int ilm_net_nparams(ilm_net_t n, size_t* count);
+/* host FP32 parameters, per layer W[out][in][5] then bias[out]; set resets Adam */
+ILM_API int ilm_net_set_params(ilm_net_t n, const float* host);
+ILM_API int ilm_net_get_params(ilm_net_t n, float* host);
+/* band_out (device, npts x (2 band + 1)): coefficients of C, identity included */
+ILM_API int ilm_net_forward(ilm_net_t n, int npts, const float* feat, const int* seg_start, const int* seg_len,
+                            float* band_out, ilm_stream_t stream);
+/* Loss mean_p |M b - x|^2 / |x|^2 over pairs p (points pair_off[p] ..
+ * pair_off[p+1], device int array) and its gradient w.r.t. the FP32
+ * parameters; loss_out / grad_out are host pointers (either may be NULL). */
+ILM_API int ilm_net_loss_grad(ilm_net_t n, int npts, int npairs, const int* pair_off, const float* feat,
+                              const int* seg_start, const int* seg_len, const float* w, const float* b,
+                              const float* x, double* loss_out, float* grad_out, ilm_stream_t stream);
+/* One Adam step (lr) on the same loss; loss_dev (device double, optional)
+ * receives the loss before the step.  Issues no host synchronisation.   */
+ILM_API int ilm_net_train_step(ilm_net_t n, int npts, int npairs, const int* pair_off, const float* feat,
+                               const int* seg_start, const int* seg_len, const float* w, const float* b,
+                               const float* x, double lr, double* loss_dev, ilm_stream_t stream);
+/* Host: features of npts points (out: npts x 8 floats) -- ds/h,
+ * 10 h curvature, n_x, n_y, sin/cos(2 pi frac(x/h)), sin/cos(2 pi frac(y/h)). */
+ILM_API int ilm_point_features(int npts, const double* x, const double* y, const double* nx, const double* ny,
+                               const double* ds, const int* seg_start, const int* seg_len, double h, float* out);
+/* Batch: run the network over the batch's points (body_start: host, per
+ * packed point, the local index of its body's first point within its
+ * problem) and switch the Schur CG to the learned preconditioner (mode 2 of
+ * ilm_batch_set_precond).                                                  */
+ILM_API int ilm_batch_set_learned(ilm_batch_t b, ilm_net_t net, const int* body_start);
+/* Batch Schur products / solves on device FP64 packed vectors (training data
+ * and checks): y = S x;  S x = rhs by the batch's CG (current preconditioner). */
+ILM_API int ilm_batch_schur_apply(ilm_batch_t b, const double* x, double* y, ilm_stream_t stream);
+ILM_API int ilm_batch_schur_solve(ilm_batch_t b, const double* rhs, double* x, double tol, int maxiter,
+                                  ilm_stream_t stream);
+
 /* ---- heat conduction with Dirichlet surfaces (time marching) -------------
  * dT/dt = kappa L T + R sigma - kappa D_s[T_b+ - T_b-],  E T = (T_b+ + T_b-)/2
  * on Nodes{Primal}, advanced by IF-HERK (Liska-Colonius scheme A) with the

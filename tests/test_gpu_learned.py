@@ -1,0 +1,143 @@
+"""Learned preconditioner on the device against the oracle: network forward,
+loss and gradient, the Adam step, the preconditioned CG's solutions and a
+short training run (its loss must fall)."""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+import learned_oracle as LO
+
+
+def _toy(seed=0, bodies=((23, 17), (31,))):
+    """Random features / data; each pair is one problem with its bodies."""
+    rng = np.random.default_rng(seed)
+    starts, pair_off = [], [0]
+    o = 0
+    for prob in bodies:
+        for n in prob:
+            starts.append(o)
+            o += n
+        pair_off.append(o)
+    N = o
+    st, ln = LO.segments(starts, N)
+    f32 = lambda a: np.asarray(a, dtype=np.float32).astype(np.float64)  # noqa: E731
+    F = f32(rng.standard_normal((N, LO.NFEAT)))
+    w = f32(rng.uniform(0.5, 1.5, N))
+    b = f32(rng.standard_normal(N))
+    x = f32(rng.standard_normal(N))
+    return N, st, ln, F, w, b, x, pair_off
+
+
+def _mb(N, st, ln, F, w, b, x, pair_off):
+    import torch
+    d = "cuda"
+    return {"feat": torch.tensor(F, dtype=torch.float32, device=d).contiguous(),
+            "seg_start": torch.tensor(st, dtype=torch.int32, device=d),
+            "seg_len": torch.tensor(ln, dtype=torch.int32, device=d),
+            "w": torch.tensor(w, dtype=torch.float32, device=d), "b": torch.tensor(b, dtype=torch.float32, device=d),
+            "x": torch.tensor(x, dtype=torch.float32, device=d),
+            "pair_off": torch.tensor(pair_off, dtype=torch.int32, device=d), "npts": N, "npairs": len(pair_off) - 1}
+
+
+def _params(seed):
+    rng = np.random.default_rng(seed + 100)
+    p = LO.init_params(seed)
+    return (p + 0.05 * rng.standard_normal(p.size)).astype(np.float32)
+
+
+def test_forward_matches_oracle(cuda):
+    from immersedlayers.learned import LearnedPreconditioner
+    N, st, ln, F, w, b, x, off = _toy(1)
+    p = _params(1)
+    net = LearnedPreconditioner(params=p)
+    mb = _mb(N, st, ln, F, w, b, x, off)
+    band = net.forward(mb["feat"], mb["seg_start"], mb["seg_len"]).cpu().numpy()
+    ref, _ = LO.forward(p, F, st, ln, weights_bf16=True)
+    assert np.abs(band - ref).max() <= 2e-5 * np.abs(ref).max()
+
+
+def test_loss_and_gradient_match_oracle(cuda):
+    from immersedlayers.learned import LearnedPreconditioner
+    N, st, ln, F, w, b, x, off = _toy(2, bodies=((23, 17), (31,), (40,)))
+    p = _params(2)
+    net = LearnedPreconditioner(params=p)
+    loss, g = net.loss_grad(_mb(N, st, ln, F, w, b, x, off))
+    lref, gref = LO.loss_and_grad(p, F, st, ln, w, b, x, off, weights_bf16=True)
+    assert abs(loss - lref) <= 1e-5 * abs(lref)
+    assert np.linalg.norm(g - gref) <= 1e-4 * np.linalg.norm(gref)
+    assert np.abs(g - gref).max() <= 1e-4 * np.abs(gref).max()
+
+
+def test_adam_step_matches_oracle(cuda):
+    from immersedlayers.learned import LearnedPreconditioner
+    N, st, ln, F, w, b, x, off = _toy(3)
+    p = _params(3)
+    net = LearnedPreconditioner(params=p)
+    mb = _mb(N, st, ln, F, w, b, x, off)
+    _, g = net.loss_grad(mb)
+    net.train_step(mb, 1e-3)
+    p1 = net.get_params()
+    m = np.zeros(p.size)
+    v = np.zeros(p.size)
+    ref = LO.adam_update(p.astype(np.float64), g.astype(np.float64), m, v, 1, 1e-3)
+    assert np.abs(p1 - ref).max() <= 1e-6
+
+
+def _star_batch(nprob=6, n=128, seed=0):
+    from immersedlayers import bodies as B
+    from immersedlayers.batch import BatchProblemSpec, BatchSolver
+    from immersedlayers.workloads import fourier_surface_data
+    import torch
+    specs = []
+    for i in range(nprob):
+        rng = np.random.default_rng(seed + i)
+        amps = rng.uniform(0, 0.08, 5)
+        ph = rng.uniform(0, 2 * math.pi, 5)
+        bl = B.BodyList()
+        bl.append(B.star(0.5, amps, ph, int(rng.integers(70, 121))))   # ds ~ 0.9-1.5 h
+        if i % 2:  # a second body: segments must stay per body
+            bl.append(B.circle(0.25, n=int(rng.integers(36, 52)), center=(1.1, 0.9)))
+        specs.append(BatchProblemSpec(n, 4.0 / n, bl, 0, fourier_surface_data(bl, rng)))
+    return BatchSolver(specs, dtype=torch.float64)
+
+
+def test_learned_pcg_solutions_match_plain(cuda):
+    import torch
+    from immersedlayers.learned import LearnedPreconditioner
+    bs = _star_batch()
+    fp, fm = bs.surface_data()
+    bs.set_precond("none")
+    f0, s0 = bs.solve(fp, fm, tol=1e-10)
+    it0, rr0 = bs.info()
+    net = LearnedPreconditioner(seed=5)
+    bs.set_learned(net)
+    f1, s1 = bs.solve(fp, fm, tol=1e-10)
+    it1, rr1 = bs.info()
+    torch.cuda.synchronize()
+    assert (rr0 <= 1e-10).all() and (rr1 <= 1e-10).all(), (rr0, rr1)
+    assert float((f0 - f1).abs().max() / f0.abs().max()) < 1e-7
+    # and the Schur-only entry points agree with each other: S (S^-1 b) = b
+    b = torch.randn(bs.total_points, dtype=torch.float64, device="cuda")
+    xs = bs.schur_solve(b, tol=1e-11)
+    r = bs.schur_apply(xs) - b
+    assert float(r.norm() / b.norm()) < 1e-9
+
+
+def test_training_reduces_loss(cuda):
+    from immersedlayers import learned as LN
+    from immersedlayers import bodies as B
+
+    def prob(i):
+        rng = np.random.default_rng(i)
+        bl = B.BodyList()
+        bl.append(B.star(0.5, rng.uniform(0, 0.08, 5), rng.uniform(0, 2 * math.pi, 5), int(rng.integers(70, 121))))
+        return 128, 4.0 / 128, bl
+
+    data, stats = LN.generate(prob, list(range(40)), chunk=40, minibatch=8)
+    assert stats["kept"] == 40
+    net = LN.LearnedPreconditioner(seed=0)
+    hist = LN.train(net, data, epochs=12, lr=2e-3, lr_min=2e-4)
+    assert hist[-1] < 0.7 * hist[0], hist
