@@ -45,6 +45,7 @@ def parse():
     ap.add_argument("--block", type=int, default=64)
     ap.add_argument("--cpu-sample-cols", type=int, default=32)
     ap.add_argument("--heat-steps", type=int, default=1000, help="heat-conduction leg (0: skip)")
+    ap.add_argument("--learned-nprob", type=int, default=256, help="learned-preconditioner leg (0: skip)")
     return ap.parse_args()
 
 
@@ -244,6 +245,10 @@ def run_ours(args, rank, world, dist):
     e2e = _e2e(args, specs, stream, dt)
     stencil = _stencil_gbs(stream, flush, hbm)
     heat = _heat_scale(args, stream) if (rank == 0 and args.heat_steps > 0) else None
+    learned = _learned_leg(args) if (rank == 0 and args.learned_nprob > 0) else None
+    if learned and "none" in learned:
+        solvers["learned_pcg"] = {"workload": learned["workload"], **learned["learned"],
+                                  "plain_cg_same_problems": learned["none"]}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -251,7 +256,7 @@ def run_ours(args, rank, world, dist):
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
                 "config": config(args, world), "roofline": roofline, "e2e": e2e, "gpu_launches": launches * args.steps,
                 "clocks": clocks, "setup_s": setup_s, "solvers": solvers, "stencil_gbs": stencil,
-                "heat": heat,
+                "heat": heat, "learned": learned,
                 "stages_ms": dict(zip(names, [round(x, 4) for x in stage_ms])),
                 "cg_iterations": {"mean": float(np.mean(its)), "max": int(its.max())},
                 "max_rel_residual": float(rr.max())}
@@ -343,6 +348,23 @@ def _heat_scale(args, stream):
         res["f32_rel_err_vs_f64"] = float((fields["f32"] - ref).abs().max() / ref.abs().max())
         out[variant] = res
     return out
+
+
+def _learned_leg(args):
+    """Learned preconditioner (trained weights shipped with the package) on
+    held-out star-body problems: 512^2 grids, h = 4/512, N_p ~ U{256..1024},
+    full Dirichlet solves at the bench tolerance; plain CG against the
+    learned preconditioner on the problems plain CG can solve."""
+    from immersedlayers import learned as LN
+    from immersedlayers import workloads as W
+    if not os.path.exists(LN.DEFAULT_WEIGHTS):
+        return {"unavailable": "no trained weights at " + os.path.relpath(LN.DEFAULT_WEIGHTS, ROOT)}
+    net = LN.LearnedPreconditioner.load()
+    ev = LN.evaluate(net, W.learned_problem, [W.LEARNED_TEST_SEED + i for i in range(args.learned_nprob)],
+                     tol=args.tol)
+    ev["workload"] = (f"{args.learned_nprob} held-out star bodies (seeds 2e6+i), 512^2 dual nodes, h=4/512, "
+                      "N_p~U{256..1024}, Dirichlet, arc-length Fourier surface data")
+    return ev
 
 
 def _rank_specs(nprob, rank):

@@ -306,7 +306,8 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(CGC_THREADS
   double* qs = rs + rmax;
   double* ws = qs + rmax;
   double* bs = ws + rmax;
-  double* pf = bs + rmax;                           // full direction (max_n)
+  double* ts = bs + rmax;                           // S x of the residual refresh (q stays S p)
+  double* pf = ts + rmax;                           // full direction (max_n)
   double* zs = pf + max_n;                          // preconditioned residual slice (rmax)
   float* vhi = reinterpret_cast<float*>(zs + max_n); // split vector (max_n each)
   float* vlo = vhi + max_n;
@@ -419,11 +420,11 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(CGC_THREADS
           vlo[j] = (float)(v - (double)h);
         }
         __syncthreads();
-        matvec_rows(pr, n, r0, r1, vhi, vlo, qs);
+        matvec_rows(pr, n, r0, r1, vhi, vlo, ts);
         __syncthreads();
         double tr = 0.0, tz = 0.0;
         for (int i = threadIdx.x; i < nr; i += blockDim.x) {
-          rs[i] = bs[i] - qs[i];
+          rs[i] = bs[i] - ts[i];
           tr += rs[i] * rs[i];
           tz += ws[i] * rs[i] * rs[i];
         }
@@ -485,7 +486,7 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(CGC_THREADS
 
 size_t cg_cluster_smem(int max_n) {
   const int rmax = (max_n + CG_CLUSTER - 1) / CG_CLUSTER;
-  return (16 + 2 * CGC_WARPS + 4 + 5 * (size_t)rmax + 2 * (size_t)max_n) * sizeof(double) +
+  return (16 + 2 * CGC_WARPS + 4 + 6 * (size_t)rmax + 2 * (size_t)max_n) * sizeof(double) +
          2 * (size_t)max_n * sizeof(float) + 64;
 }
 
