@@ -29,6 +29,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "immersedlayers.jl_gb300"))
 
 METRIC = "Poisson solves/s at 1e-8 rel. residual, 1 GB300 (batched Dirichlet/Neumann)"
+# DRAM bytes (read + write) of one launch of the dominant kernel, from one ncu
+# capture of this bench's block-Jacobi CG launch
+# (profiles/k_cg_cluster_block_jacobi_batched_poisson.md)
+NCU_TRAFFIC = {"Schur CG (FP64)": 4.351e9}
 UNIT = "solves/s"
 NPROB = 256
 
@@ -238,7 +242,8 @@ def run_ours(args, rank, world, dist):
     alg = _algorithmic_bytes(names[dom], st, its)
     achieved = alg / (stage_ms[dom] / 1000.0) / 1e9
     roofline = {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": achieved / hbm, "peak_kind": peak_kind, "traffic": None,
+                "frac": achieved / hbm, "peak_kind": peak_kind,
+                "traffic": NCU_TRAFFIC.get(names[dom]) if args.precond == "bjacobi" else None,
                 "algorithmic_bytes": alg, "launch_ms": stage_ms[dom]}
 
     # end to end through the public API from host buffers

@@ -19,9 +19,9 @@ from .core import (Dual, EdgeGradient, EdgeGradientPrimal, Edges, EdgesDual, Edg
                    surface_curl_, surface_curl_cross_, surface_divergence_, surface_divergence_cross_,
                    surface_divergence_symm_, surface_grad_, surface_grad_cross_, surface_grad_symm_, x_grid, y_grid,
                    zeros_grid, zeros_gridcurl, zeros_griddiv, zeros_gridgrad, zeros_surface, zeros_surfacescalar)
-from .problems import (DirichletPoissonProblem, ILMProblem, ILMSystem, NeumannPoissonProblem, construct_system,
-                       prescribed_surface_average_, prescribed_surface_jump_, solve, solve_dirichlet,
-                       solve_neumann)
+from .problems import (DirichletPoissonProblem, ILMProblem, ILMSystem, NeumannPoissonProblem, StokesFlowProblem,
+                       construct_system, prescribed_surface_average_, prescribed_surface_jump_, solve,
+                       solve_dirichlet, solve_neumann, solve_stokes)
 from .timemarching import (ConstrainedSolution, DirichletHeatConductionProblem, HeatIntegrator, constraint, init,
                            init_sol, state, step_, temperature, timestep, timestep_fourier)
 

@@ -41,6 +41,11 @@ class NeumannPoissonProblem(ILMProblem):
     datatype = "scalar"
 
 
+class StokesFlowProblem(ILMProblem):
+    """`@ilmproblem StokesFlow vector` (test/literate/stokes.jl:52)."""
+    datatype = "vector"
+
+
 @dataclass
 class ILMSystem:
     """`ILMSystem`: base cache + problem extra cache (src/ImmersedLayers.jl:100-110)."""
@@ -126,6 +131,20 @@ def solve_neumann(cache, vplus: PointData, vminus: PointData, tol=1e-8, maxiter=
     return f, df, dict(iterations=info.iterations, converged=bool(info.converged), rel_residual=info.rel_residual)
 
 
+def solve_stokes(cache, vplus: PointData, vminus: PointData, tol=1e-8, maxiter=5000, stream=None):
+    """Device Stokes solve (vector cache); returns (v::Edges{Primal},
+    s::Nodes{Dual}, sigma::VectorData, info)."""
+    from .core import zeros_gridcurl
+    v = zeros_grid(cache)
+    s = zeros_gridcurl(cache)
+    sigma = zeros_surface(cache)
+    info = L.SolveInfo()
+    L.call("ilm_solve_stokes", cache._h, _ptr(vplus.data), _ptr(vminus.data), _ptr(v.data), _ptr(s.data),
+           _ptr(sigma.data), float(tol), int(maxiter), C.byref(info), _stream_ptr(stream))
+    return v, s, sigma, dict(iterations=info.iterations, converged=bool(info.converged),
+                             rel_residual=info.rel_residual)
+
+
 def solve(prob: ILMProblem, sys: ILMSystem, tol=1e-8, maxiter=5000):
     """`solve(prob, sys)` for the built-in problems (bc from `prob.bc`)."""
     plus, minus = _sides(sys)
@@ -133,6 +152,10 @@ def solve(prob: ILMProblem, sys: ILMSystem, tol=1e-8, maxiter=5000):
         f, s, info = solve_dirichlet(sys.base_cache, plus, minus, tol, maxiter)
     elif isinstance(prob, NeumannPoissonProblem):
         f, s, info = solve_neumann(sys.base_cache, plus, minus, tol, maxiter)
+    elif isinstance(prob, StokesFlowProblem):
+        v, s, sigma, info = solve_stokes(sys.base_cache, plus, minus, tol, maxiter)
+        sys.last_info = info
+        return v, s, sigma
     else:
         raise NotImplementedError(type(prob).__name__)
     sys.last_info = info

@@ -217,6 +217,18 @@ ILM_API int ilm_solve_dirichlet(ilm_cache_t c, const void* fplus, const void* fm
 ILM_API int ilm_solve_neumann(ilm_cache_t c, const void* vplus, const void* vminus,
                       void* f_out, void* df_out, double tol, int maxiter,
                       ilm_solve_info_t* info, ilm_stream_t stream);
+/* Stokes flow with no-slip surfaces (vector GridScaling cache): the
+ * StokesFlowProblem solve of test/literate/stokes.jl:101-166.  vplus/vminus:
+ * VectorData (2N) surface velocities outside/inside; v_out: Edges{Primal}
+ * velocity, s_out: Nodes{Dual} streamfunction, sigma_out: VectorData
+ * traction (filtered twice, :165).  The Schur systems -C_s L^-2 C_s^T
+ * (create_CL2invCT, src/matrix_operators.jl:102) and -C_s L^-1 C_s^T on
+ * scalars (create_CLinvCT_scalar, :71) are solved matrix-free by CG in place
+ * of the reference's dense LU; info reports both solves (iterations summed,
+ * worst relative residual).                                               */
+ILM_API int ilm_solve_stokes(ilm_cache_t c, const void* vplus, const void* vminus, void* v_out, void* s_out,
+                             void* sigma_out, double tol, int maxiter, ilm_solve_info_t* info,
+                             ilm_stream_t stream);
 
 /* ---- batched problem solves (configs of many independent problems) ------ */
 /* Many independent Dirichlet/Neumann Poisson problems (each its own grid and

@@ -873,3 +873,88 @@ def heat_march(c: SurfaceCache, T0, tb_plus, tb_minus, kappa, dt, nsteps, scheme
         T = yh + dt * b[2] * regularize_scalar(c, s3)
         sig = s3
     return T, sig
+
+
+# ---------------------------------------------------------------------------
+# Stokes flow (test/literate/stokes.jl:52-166; src/matrix_operators.jl:64-128,
+# 247-262) on a vector cache
+# ---------------------------------------------------------------------------
+EDGES_PRIMAL_V = (0, 1)
+
+
+def create_CL2invCT_vector(c: SurfaceCache, scale=1.0):
+    """-C_s L^-2 C_s^T on VectorData (src/matrix_operators.jl:102-128)."""
+    n = 2 * c.N
+    A = np.empty((n, n))
+    e = np.zeros(n)
+    for col in range(n):
+        e[:] = 0.0
+        e[col] = 1.0
+        w = c.inverse_laplacian(c.inverse_laplacian(surface_curl_T_vector(c, e)))
+        A[:, col] = -scale * surface_curl_vector(c, w)
+    return A
+
+
+def create_CLinvCT_scalar_vector(c: SurfaceCache, scale=1.0):
+    """-C_s L^-1 C_s^T on ScalarData of a vector cache (src/matrix_operators.jl:71-93)."""
+    A = np.empty((c.N, c.N))
+    e = np.zeros(c.N)
+    for col in range(c.N):
+        e[:] = 0.0
+        e[col] = 1.0
+        w = c.inverse_laplacian(surface_curl_T_vector_scalar(c, e))
+        A[:, col] = -scale * surface_curl_vector_scalar(c, w)
+    return A
+
+
+def surface_filter_vector(c: SurfaceCache):
+    """Surface filter E~ R on VectorData (src/matrix_operators.jl:247-262).
+    The filtered interpolation E~ of CartesianGrids' Regularize(filter=true)
+    is un-vendored; restated from Goza, Liska, Morley & Colonius (2016), the
+    method it implements: E~ = W^-1 E with W = diag(E R 1), i.e. the rows of
+    E R normalised so that constant surface data are reproduced.  Returns the
+    2N x 2N block-diagonal matrix (u and v components on their own edges)."""
+    n = c.N
+    F = np.zeros((2 * n, 2 * n))
+    for k, cls_ in enumerate((EDGES_PRIMAL_U, EDGES_PRIMAL_V)):
+        P = c.phi(cls_)
+        ER = (P.T @ (P @ sp.diags(c._wscale()))).toarray()
+        F[k * n:(k + 1) * n, k * n:(k + 1) * n] = ER / ER.sum(axis=1, keepdims=True)
+    return F
+
+
+def solve_stokes(c: SurfaceCache, vplus, vminus, S=None, Ss=None, filt=None):
+    """Stokes flow with no-slip surfaces by the reference's block-LU
+    (test/literate/stokes.jl:101-166).  vplus / vminus: VectorData (2N) of
+    the exterior / interior surface velocities.  Returns (v: Edges{Primal}
+    tuple, s: Nodes{Dual} streamfunction, sigma: VectorData traction)."""
+    if S is None:
+        S = create_CL2invCT_vector(c)
+    if Ss is None:
+        Ss = create_CLinvCT_scalar_vector(c)
+    if filt is None:
+        filt = surface_filter_vector(c)
+    n = c.N
+    dv = vplus - vminus
+    vb = 0.5 * (vplus + vminus)
+    # psi*
+    sstar = -curl_edges(surface_divergence_symm(c, dv), c.g) * c.dscale()
+    sstar = c.inverse_laplacian(c.inverse_laplacian(sstar))
+    # normal-velocity jump: potential part
+    dvn = c.nx * dv[:n] + c.ny * dv[n:]
+    phi = c.inverse_laplacian(regularize_scalar(c, dvn))
+    vphi = tuple(x * c.dscale() for x in grad_nodes(phi, c.g))
+    vprime = vb - interpolate_vector(c, vphi)
+    # surface velocity of psi*
+    v = tuple(x * c.dscale() for x in curl_nodes_dual(sstar, c.g))
+    vprime = vprime - interpolate_vector(c, v)
+    sigma = np.linalg.solve(S, vprime)
+    # correction streamfunction
+    s = -surface_curl_T_vector(c, sigma)
+    s = c.inverse_laplacian(c.inverse_laplacian(s)) + sstar
+    v = tuple(a * c.dscale() + b for a, b in zip(curl_nodes_dual(s, c.g), vphi))
+    # streamfunction equivalent of the scalar potential
+    dsc = np.linalg.solve(Ss, surface_grad_cross(c, phi))
+    s = s + c.inverse_laplacian(-surface_curl_cross_T(c, dsc))
+    sigma = filt @ (filt @ sigma)
+    return v, s, sigma

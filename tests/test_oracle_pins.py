@@ -143,3 +143,25 @@ def test_dirichlet_exterior_analytic():
     r = np.hypot(X, Y)
     m = (r > 0.7) & (r < 1.5)
     assert np.abs(f[m] - X[m] * 0.25 / r[m] ** 2).max() < 5e-3
+
+
+def test_oracle_stokes_no_slip_and_symmetry():
+    """Stokes oracle (test/literate/stokes.jl:101-166): W S symmetric and
+    negative definite, the velocity satisfies no-slip exactly, and the
+    translating rectangle's traction has no net lift."""
+    from immersedlayers import bodies as B
+    h = 0.04
+    g = O.Grid.physical((-2.0, 2.0), (-2.0, 2.0), h)
+    b = B.rectangle(0.5, 0.25, ds=1.4 * h)
+    c = O.SurfaceCache(b.x, b.y, b.nx, b.ny, b.ds, g, kind="vector")
+    S = O.create_CL2invCT_vector(c)
+    W = np.diag(np.concatenate([c.ds, c.ds]))
+    WS = W @ S
+    assert np.abs(WS - WS.T).max() < 1e-12 * np.abs(WS).max()
+    assert np.linalg.eigvalsh(0.5 * (WS + WS.T)).max() < 0
+    vp = np.concatenate([np.ones(c.N), np.zeros(c.N)])
+    v, s, sig = O.solve_stokes(c, vp, np.zeros(2 * c.N), S=S)
+    assert np.abs(O.interpolate_vector(c, v) - 0.5 * vp).max() < 1e-12
+    assert abs(sig[c.N:] @ c.ds) < 1e-10 * abs(sig[:c.N] @ c.ds)
+    F = O.surface_filter_vector(c)
+    assert np.allclose(F @ np.ones(2 * c.N), 1.0)
