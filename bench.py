@@ -45,11 +45,12 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--nprob", type=int, default=NPROB)
     ap.add_argument("--tol", type=float, default=1e-8)
-    ap.add_argument("--precond", default="bjacobi", choices=["none", "bjacobi"])
+    ap.add_argument("--precond", default="bjacobi", choices=["none", "bjacobi", "learned"])
     ap.add_argument("--block", type=int, default=64)
     ap.add_argument("--cpu-sample-cols", type=int, default=32)
     ap.add_argument("--heat-steps", type=int, default=1000, help="heat-conduction leg (0: skip)")
     ap.add_argument("--learned-nprob", type=int, default=256, help="learned-preconditioner leg (0: skip)")
+    ap.add_argument("--stokes", type=int, default=1, help="Stokes leg (0: skip)")
     return ap.parse_args()
 
 
@@ -70,7 +71,8 @@ def config(args, world):
                         "8-mode arc-length Fourier surface data, seeds 3+i",
             "nprob_per_gpu": args.nprob, "tol": args.tol, "precision": "FP32 grid work, FP64 Schur build + CG",
             "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{world}",
-            "solver": {"none": "plain CG", "bjacobi": f"block-Jacobi flexible CG (blocks of ~{args.block} points)"}[
+            "solver": {"none": "plain CG", "bjacobi": f"block-Jacobi flexible CG (blocks of ~{args.block} points)",
+                   "learned": "learned banded preconditioner (flexible CG), one network per problem kind"}[
                 args.precond]}
 
 
@@ -190,9 +192,15 @@ def run_ours(args, rank, world, dist):
     s_out = torch.empty(bs.total_points, dtype=dt, device="cuda")
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
 
-    # secondary leg: plain CG (no preconditioner), same batch, same timing rules
+    # secondary legs: the other solvers on the same batch, same timing rules
     solvers = {}
-    for mode in ["none", args.precond] if args.precond != "none" else ["none"]:
+    leg_names = {"none": "plain_cg", "bjacobi": "block_jacobi_pcg", "learned": "learned_pcg"}
+    have_learned = _prepare_learned(bs)
+    if args.precond == "learned" and not have_learned:
+        raise SystemExit("--precond learned: no trained weights for the batched configuration")
+    legs = ["none", "bjacobi"] + (["learned"] if have_learned else [])
+    legs = [m for m in legs if m != args.precond] + [args.precond]
+    for mode in legs:
         bs.set_precond(mode, args.block)
         with torch.cuda.stream(stream):
             for _ in range(args.warmup):
@@ -202,8 +210,8 @@ def run_ours(args, rank, world, dist):
         assert (rr <= args.tol).all(), f"{mode}: not converged, max rel residual {rr.max()}"
         if mode != args.precond:
             ms = _timed(bs, fp, fm, f_out, s_out, args, stream, flush, max(1, args.steps))
-            solvers["plain_cg"] = {"solves_per_s": args.nprob * max(1, args.steps) / (ms / 1000.0),
-                                   "cg_iterations_mean": float(np.mean(its)), "cg_iterations_max": int(its.max())}
+            solvers[leg_names[mode]] = {"solves_per_s": args.nprob * max(1, args.steps) / (ms / 1000.0),
+                                    "cg_iterations_mean": float(np.mean(its)), "cg_iterations_max": int(its.max())}
 
     # timed region (the default solver)
     if dist:
@@ -220,10 +228,9 @@ def run_ours(args, rank, world, dist):
     clocks = clocks_summary(clk, dev)
     value = world * args.nprob * args.steps / (total_ms / 1000.0)
     its, rr = bs.info()
-    solvers[{"bjacobi": "block_jacobi_pcg", "none": "plain_cg"}[args.precond]] = {
+    solvers[leg_names[args.precond]] = {
         "solves_per_s": args.nprob * args.steps / (total_ms / 1000.0), "cg_iterations_mean": float(np.mean(its)),
         "cg_iterations_max": int(its.max())}
-    solvers.setdefault("learned_pcg", None)
 
     # stage profile of one solve (separate, not part of the timed region)
     bs.set_profiling(True)
@@ -251,9 +258,10 @@ def run_ours(args, rank, world, dist):
     stencil = _stencil_gbs(stream, flush, hbm)
     heat = _heat_scale(args, stream) if (rank == 0 and args.heat_steps > 0) else None
     learned = _learned_leg(args) if (rank == 0 and args.learned_nprob > 0) else None
+    stokes = _stokes_leg(args) if (rank == 0 and args.stokes) else None
     if learned and "none" in learned:
-        solvers["learned_pcg"] = {"workload": learned["workload"], **learned["learned"],
-                                  "plain_cg_same_problems": learned["none"]}
+        solvers["learned_pcg_star"] = {"workload": learned["workload"], **learned["learned"],
+                                       "plain_cg_same_problems": learned["none"]}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -261,7 +269,7 @@ def run_ours(args, rank, world, dist):
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
                 "config": config(args, world), "roofline": roofline, "e2e": e2e, "gpu_launches": launches * args.steps,
                 "clocks": clocks, "setup_s": setup_s, "solvers": solvers, "stencil_gbs": stencil,
-                "heat": heat, "learned": learned,
+                "heat": heat, "learned": learned, "stokes": stokes,
                 "stages_ms": dict(zip(names, [round(x, 4) for x in stage_ms])),
                 "cg_iterations": {"mean": float(np.mean(its)), "max": int(its.max())},
                 "max_rel_residual": float(rr.max())}
@@ -353,6 +361,61 @@ def _heat_scale(args, stream):
         res["f32_rel_err_vs_f64"] = float((fields["f32"] - ref).abs().max() / ref.abs().max())
         out[variant] = res
     return out
+
+
+def _stokes_leg(args):
+    """Stokes flow (vector cache, FP64): the reference example's rectangle
+    (PhysicalGrid((-2,2),(-2,2),0.01), Rectangle(0.5,0.25,1.4h), translating
+    at unit speed) solved to the bench tolerance; and the 2048^2, 8192-point
+    configuration (ds ~ 0.35 h: S numerically singular, 1e-8 unattainable)
+    timed per CG iteration over a capped solve."""
+    import numpy as np
+    import torch
+    import immersedlayers as il
+    from immersedlayers import bodies as B
+    from immersedlayers import workloads as W
+
+    def run(g, bl, vp_h, tol, maxiter):
+        c = il.SurfaceVectorCache(bl, g, dtype=torch.float64)
+        N = len(bl)
+        vp = il.VectorData(torch.tensor(vp_h, dtype=torch.float64, device="cuda"))
+        vm = il.VectorData.zeros(N, torch.float64)
+        il.solve_stokes(c, vp, vm, tol=tol, maxiter=3)   # plans and scratch
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _, _, _, info = il.solve_stokes(c, vp, vm, tol=tol, maxiter=maxiter)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        return {"npts": N, "grid": [g.nx, g.ny], "seconds": dt, "cg_iterations": info["iterations"],
+                "ms_per_cg_iteration": 1000 * dt / max(1, info["iterations"]), "converged": info["converged"],
+                "rel_residual": info["rel_residual"]}
+
+    out = {}
+    g = il.PhysicalGrid((-2.0, 2.0), (-2.0, 2.0), 0.01)
+    bl = B.BodyList()
+    bl.append(B.rectangle(0.5, 0.25, ds=1.4 * 0.01))
+    N = len(bl)
+    out["reference_example"] = run(g, bl, np.concatenate([np.ones(N), np.zeros(N)]), args.tol, 20000)
+    d = W.stokes_scale(nrhs=1)
+    g = il.PhysicalGrid(h=d["h"], nx=d["n"])
+    out["npts8192_2048sq"] = run(g, d["bodies"], d["vplus"][0], args.tol, 50)
+    out["workload"] = ("reference example: 406^2, rectangle 0.5x0.25, ds=1.4h, unit translation; "
+                       "2048^2 h=0.002, 2 circles + 2 plates, 8192 points, rigid-body velocities (seed 5), "
+                       "CG capped at 50 iterations")
+    return out
+
+
+def _prepare_learned(bs):
+    """Load the learned preconditioners trained on the batched configuration
+    (one network per problem kind) and set them on the batch."""
+    from immersedlayers import learned as LN
+    from immersedlayers.batch import DIRICHLET, NEUMANN
+    if not all(os.path.exists(LN.BATCHED_WEIGHTS[k]) for k in (DIRICHLET, NEUMANN)):
+        return False
+    bs._nets = [LN.LearnedPreconditioner.load(LN.BATCHED_WEIGHTS[k]) for k in (DIRICHLET, NEUMANN)]
+    bs.set_learned(bs._nets[0], kinds=(DIRICHLET,))
+    bs.set_learned(bs._nets[1], kinds=(NEUMANN,))
+    return True
 
 
 def _learned_leg(args):

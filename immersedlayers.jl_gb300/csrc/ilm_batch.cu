@@ -238,6 +238,7 @@ struct ilm_batch_s {
   // body segments as local indices
   int band_k = -1;
   DevBuf band, lseg_start, lseg_len;
+  std::vector<char> has_band;  // problems whose kind a network was set for
   // host copies of the points (features of the learned preconditioner)
   std::vector<double> hx, hy, hnx, hny, hds;
   DevBuf dpoff;  // point offsets on the device (Schur products)
@@ -295,7 +296,7 @@ int ensure_cg_params(ilm_batch_s* b, double tol, int maxiter) {
                      pre ? b->bj_size.as<int>() + b->bj_first[p] : nullptr,
                      pre ? b->bj_off.as<int>() + b->bj_first[p] : nullptr, pre ? b->bj_inv.as<float>() : nullptr,
                      pre ? b->bj_inv_lo.as<float>() : nullptr);
-    if (b->precond == 2)
+    if (b->precond == 2 && b->has_band[p])
       cgff_params_set_band(dst, b->band.as<float>() + o * P, b->band_k, b->lseg_start.as<int>() + o,
                            b->lseg_len.as<int>() + o);
   }
@@ -838,10 +839,13 @@ int ilm_batch_info(ilm_batch_t b, int* iterations, double* rel_residual) {
   return ILM_OK;
 }
 
-int ilm_batch_set_learned(ilm_batch_t b, ilm_net_t net, const int* body_start) {
+int ilm_batch_set_learned(ilm_batch_t b, ilm_net_t net, int kind_mask, const int* body_start) {
   ILM_REQUIRE(b && net && body_start, "batch_set_learned: null argument");
+  ILM_REQUIRE(kind_mask >= 1 && kind_mask <= 3, "batch_set_learned: kind mask %d (1 Dirichlet, 2 Neumann, 3 both)",
+              kind_mask);
   ILM_REQUIRE(net_nfeat(net) == 8, "batch_set_learned: the network must read the 8 point features");
   const int K = net_band(net), P = 2 * K + 1;
+  ILM_REQUIRE(b->band_k < 0 || b->band_k == K, "batch_set_learned: all networks of a batch must share the band width");
   const int Ptot = b->Ptot;
   std::vector<int> ls(Ptot), ll(Ptot), as(Ptot);
   for (int p = 0; p < b->nprob; ++p) {
@@ -881,8 +885,20 @@ int ilm_batch_set_learned(ilm_batch_t b, ilm_net_t net, const int* body_start) {
   ILM_TRY(up(dll, ll));
   ILM_TRY(up(b->lseg_start, ls));
   ILM_TRY(up(b->lseg_len, ll));
-  ILM_TRY(b->band.alloc((size_t)Ptot * P * sizeof(float)));
-  ILM_TRY(net_forward_packed(net, Ptot, dfeat.as<float>(), das.as<int>(), dll.as<int>(), b->band.as<float>(), nullptr));
+  if (b->band_k < 0) {
+    ILM_TRY(b->band.alloc((size_t)Ptot * P * sizeof(float)));
+    b->has_band.assign(b->nprob, 0);
+  }
+  DevBuf tmp;
+  ILM_TRY(tmp.alloc((size_t)Ptot * P * sizeof(float)));
+  ILM_TRY(net_forward_packed(net, Ptot, dfeat.as<float>(), das.as<int>(), dll.as<int>(), tmp.as<float>(), nullptr));
+  for (int p = 0; p < b->nprob; ++p) {  // this network's band for the problems of the selected kinds
+    if (!(kind_mask & (1 << b->probs[p].kind))) continue;
+    const size_t o = b->poff[p];
+    ILM_CHECK_CUDA(cudaMemcpy(b->band.as<float>() + o * P, tmp.as<float>() + o * P,
+                              (size_t)b->probs[p].npts * P * sizeof(float), cudaMemcpyDeviceToDevice));
+    b->has_band[p] = 1;
+  }
   ILM_CHECK_CUDA(cudaDeviceSynchronize());
   b->band_k = K;
   b->precond = 2;

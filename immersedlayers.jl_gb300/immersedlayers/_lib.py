@@ -106,7 +106,7 @@ SIGNATURES = {
     "ilm_net_loss_grad": [_VP, _I, _I, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _DP, C.POINTER(C.c_float), _VP],
     "ilm_net_train_step": [_VP, _I, _I, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _D, _VP, _VP],
     "ilm_point_features": [_I, _DP, _DP, _DP, _DP, _DP, C.POINTER(_I), C.POINTER(_I), _D, C.POINTER(C.c_float)],
-    "ilm_batch_set_learned": [_VP, _VP, C.POINTER(_I)],
+    "ilm_batch_set_learned": [_VP, _VP, _I, C.POINTER(_I)],
     "ilm_batch_schur_apply": [_VP, _VP, _VP, _VP],
     "ilm_batch_schur_solve": [_VP, _VP, _VP, _D, _I, _VP],
     "ilm_heat_create": [_VP, _D, _D, _DP, _DP, _D, _I, C.POINTER(_VP)],

@@ -141,11 +141,14 @@ def _body_starts(self):
     return np.ascontiguousarray(np.concatenate(out), dtype=np.int32)
 
 
-def _set_learned(self, net):
-    """Run the learned preconditioner's network over this batch's points and
-    switch the Schur CG to it."""
+def _set_learned(self, net, kinds=(DIRICHLET, NEUMANN)):
+    """Run the learned preconditioner's network over this batch's points, use
+    it for the problems of the given kinds and switch the Schur CG to the
+    learned preconditioner (problems of other kinds run plain CG unless
+    another network is set for them)."""
     bs = _body_starts(self)
-    L.call("ilm_batch_set_learned", self._h, net._h, bs.ctypes.data_as(C.POINTER(C.c_int)))
+    mask = sum(1 << k for k in kinds)
+    L.call("ilm_batch_set_learned", self._h, net._h, mask, bs.ctypes.data_as(C.POINTER(C.c_int)))
 
 
 def _schur_apply(self, x, y=None, stream=None):

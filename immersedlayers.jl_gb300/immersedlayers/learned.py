@@ -30,7 +30,10 @@ from . import _lib as L
 from .core import _ptr, _stream_ptr
 
 NFEAT, WIDTH, NLAYERS, KSIZE, BAND = 8, 64, 4, 5, 4
-DEFAULT_WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "learned_star.npz")
+DATA_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data")
+DEFAULT_WEIGHTS = os.path.join(DATA_DIR, "learned_star.npz")
+BATCHED_WEIGHTS = {0: os.path.join(DATA_DIR, "learned_batched_dirichlet.npz"),
+                   1: os.path.join(DATA_DIR, "learned_batched_neumann.npz")}
 
 
 def layer_dims(width=WIDTH, nlayers=NLAYERS, band=BAND, nfeat=NFEAT):
@@ -175,17 +178,25 @@ def _pack_minibatch(items, device="cuda"):
             "npts": off[-1], "npairs": len(items)}
 
 
-def schur_rhs(bl, rng, noise=True):
+def schur_rhs(bl, rng, noise=True, kind=0):
     """Schur right-hand side for training: the batched configuration's
-    arc-length Fourier modes plus (optionally) white noise of random level."""
+    arc-length Fourier modes plus (optionally) white noise of random level.
+    Neumann data (kind 1) get zero ds-weighted mean per body, the
+    compatibility condition of the Neumann problem."""
     from .workloads import fourier_surface_data
     f = fourier_surface_data(bl, rng)
     if noise:
         f = f + rng.uniform(0.0, 1.0) * np.sqrt(np.mean(f * f)) * rng.standard_normal(f.size)
+    if kind == 1:
+        fi = bl.firstindices()
+        ds = np.asarray(bl.ds)
+        for b in range(len(fi) - 1):
+            s = slice(fi[b], fi[b + 1])
+            f[s] -= (f[s] * ds[s]).sum() / ds[s].sum()
     return f
 
 
-def generate(problem_fn, indices, chunk=256, tol=1e-10, maxiter=5000, minibatch=64, noise=True, log=None):
+def generate(problem_fn, indices, chunk=256, tol=1e-10, maxiter=5000, minibatch=64, noise=True, log=None, kind=0):
     """Triples for problems `problem_fn(i)` -> (n, h, BodyList), solved by
     the plain device CG on S x = b.  Problems the plain CG cannot bring to
     `tol` within `maxiter` (points much closer than h: S numerically
@@ -197,13 +208,13 @@ def generate(problem_fn, indices, chunk=256, tol=1e-10, maxiter=5000, minibatch=
     for c0 in range(0, len(indices), chunk):
         idx = indices[c0:c0 + chunk]
         probs = [problem_fn(i) for i in idx]
-        specs = [BatchProblemSpec(n, h, bl, 0, np.zeros(len(bl))) for (n, h, bl) in probs]
+        specs = [BatchProblemSpec(n, h, bl, kind, np.zeros(len(bl))) for (n, h, bl) in probs]
         bs = BatchSolver(specs, dtype=torch.float32)
         bs.set_precond("none")
         rhs = []
         for i, (n, h, bl) in zip(idx, probs):
             rng = np.random.default_rng(int(i) + 7)
-            rhs.append(schur_rhs(bl, rng, noise))
+            rhs.append(schur_rhs(bl, rng, noise, kind))
         b = torch.tensor(np.concatenate(rhs), dtype=torch.float64, device="cuda")
         x = bs.schur_solve(b, tol=tol, maxiter=maxiter)
         its, rr = bs.info()
@@ -330,20 +341,31 @@ def main(argv=None):
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--minibatch", type=int, default=64)
     ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--out", default=DEFAULT_WEIGHTS)
+    ap.add_argument("--out", default=None)
     ap.add_argument("--report", default=None)
+    ap.add_argument("--config", default="star", choices=["star", "batched"])
+    ap.add_argument("--kind", default="dirichlet", choices=["dirichlet", "neumann"])
     a = ap.parse_args(argv)
     log = lambda m: print(m, flush=True)  # noqa: E731
     t0 = time.perf_counter()
-    data, gstats = generate(learned_problem, [LEARNED_TRAIN_SEED + i for i in range(a.train)],
-                            minibatch=a.minibatch, log=log)
+    kind = 0 if a.kind == "dirichlet" else 1
+    if a.config == "star":
+        problem_fn, train_idx = learned_problem, [LEARNED_TRAIN_SEED + i for i in range(a.train)]
+        out = a.out or DEFAULT_WEIGHTS
+    else:
+        from .workloads import batch_problem
+        problem_fn = lambda i: batch_problem(i)[:3]  # noqa: E731
+        train_idx = [10000 + i for i in range(a.train)]   # disjoint from the benchmark batch (0..255)
+        out = a.out or BATCHED_WEIGHTS[kind]
+    data, gstats = generate(problem_fn, train_idx, minibatch=a.minibatch, log=log, kind=kind)
     log(f"training set: {gstats}")
     net = LearnedPreconditioner(seed=a.seed)
     t1 = time.perf_counter()
     hist = train(net, data, epochs=a.epochs, lr=a.lr, seed=a.seed, log=log)
     train_s = time.perf_counter() - t1
-    net.save(a.out, loss_history=np.asarray(hist), train_pairs=gstats["kept"], epochs=a.epochs)
-    ev = evaluate(net, learned_problem, [LEARNED_TEST_SEED + i for i in range(a.test)])
+    net.save(out, loss_history=np.asarray(hist), train_pairs=gstats["kept"], epochs=a.epochs)
+    ev = evaluate(net, learned_problem, [LEARNED_TEST_SEED + i for i in range(a.test)]) if a.config == "star" \
+        else None
     rep = {"generate": gstats, "train_seconds": train_s, "loss_first": hist[0], "loss_last": hist[-1],
            "held_out": ev, "total_seconds": time.perf_counter() - t0}
     log(json.dumps(rep))

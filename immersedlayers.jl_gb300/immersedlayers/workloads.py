@@ -159,3 +159,46 @@ def learned_problem(i, n=512):
 
 LEARNED_TRAIN_SEED = 1_000_000
 LEARNED_TEST_SEED = 2_000_000
+
+
+def stokes_scale(npts=8192, seed=5, nrhs=16, ds_factor=None, n=2048):
+    """Stokes configuration: n x n dual nodes with h = 0.002 (n = 2048)
+    centred on the origin; 2 circles r ~ U(0.1, 0.3) and 2 plates (rectangles
+    of half-lengths 0.25 x h) at non-overlapping seeded centres (margin 4h),
+    `npts` points split by perimeter (ds ~ 0.35 h at 8192), or points
+    ds_factor * h apart; `nrhs` rigid-body surface velocity sets with
+    translation and rotation rates ~ N(0, 1) per body (numpy
+    default_rng(seed)).  Returns dict(n, h, bodies, vplus (nrhs x 2N))."""
+    h = 0.002
+    rng = np.random.default_rng(seed)
+    radii = [float(rng.uniform(0.1, 0.3)), float(rng.uniform(0.1, 0.3))]
+    reach = radii + [0.25, 0.25]
+    centres = []
+    lim = 1.5
+    while len(centres) < 4:
+        R = reach[len(centres)]
+        c = rng.uniform(-lim + R, lim - R, size=2)
+        if all(np.hypot(*(c - q)) >= R + rq + 4 * h for q, rq in zip(centres, reach)):
+            centres.append(c)
+    angles = rng.uniform(0.0, math.pi, 2)
+    per = [2 * math.pi * radii[0], 2 * math.pi * radii[1], 4 * (0.25 + h), 4 * (0.25 + h)]
+    if ds_factor is not None:
+        npts = int(round(sum(per) / (ds_factor * h)))
+    P = sum(per)
+    counts = [max(16, int(round(npts * p / P))) for p in per]
+    bl = B.BodyList()
+    bl.append(B.circle(radii[0], n=counts[0], center=tuple(centres[0])))
+    bl.append(B.circle(radii[1], n=counts[1], center=tuple(centres[1])))
+    for k in (2, 3):
+        bl.append(B.rectangle(0.25, h, ds=per[k] / counts[k], center=tuple(centres[k]), angle=float(angles[k - 2])))
+    N = len(bl)
+    fi = bl.firstindices()
+    V = np.zeros((nrhs, 2 * N))
+    for r in range(nrhs):
+        for b in range(4):
+            s = slice(fi[b], fi[b + 1])
+            ux, uy, om = rng.standard_normal(3)
+            cx, cy = centres[b]
+            V[r, s] = ux - om * (bl.y[s] - cy)
+            V[r, N + fi[b]:N + fi[b + 1]] = uy + om * (bl.x[s] - cx)
+    return dict(n=n, h=h, bodies=bl, vplus=V)

@@ -315,9 +315,11 @@ ILM_API int ilm_point_features(int npts, const double* x, const double* y, const
                                const double* ds, const int* seg_start, const int* seg_len, double h, float* out);
 /* Batch: run the network over the batch's points (body_start: host, per
  * packed point, the local index of its body's first point within its
- * problem) and switch the Schur CG to the learned preconditioner (mode 2 of
- * ilm_batch_set_precond).                                                  */
-ILM_API int ilm_batch_set_learned(ilm_batch_t b, ilm_net_t net, const int* body_start);
+ * problem) and use its band for the problems whose kind is in kind_mask
+ * (bit 0 Dirichlet, bit 1 Neumann); call once per network.  Switches the
+ * Schur CG to the learned preconditioner (mode 2 of ilm_batch_set_precond);
+ * problems of a kind no network was set for run plain CG.                  */
+ILM_API int ilm_batch_set_learned(ilm_batch_t b, ilm_net_t net, int kind_mask, const int* body_start);
 /* Batch Schur products / solves on device FP64 packed vectors (training data
  * and checks): y = S x;  S x = rhs by the batch's CG (current preconditioner). */
 ILM_API int ilm_batch_schur_apply(ilm_batch_t b, const double* x, double* y, ilm_stream_t stream);
