@@ -239,6 +239,10 @@ struct ilm_batch_s {
   int band_k = -1;
   DevBuf band, lseg_start, lseg_len;
   std::vector<char> has_band;  // problems whose kind a network was set for
+  // deflation of the Dirichlet net-charge mode (set up before the first solve)
+  bool defl_ready = false;
+  std::vector<double> defl_gamma, defl_uz;
+  DevBuf defl_z;
   // host copies of the points (features of the learned preconditioner)
   std::vector<double> hx, hy, hnx, hny, hds;
   DevBuf dpoff;  // point offsets on the device (Schur products)
@@ -279,16 +283,22 @@ int up_typed(DevBuf& b, const std::vector<double>& v, int dtype) {
     }                          \
   } while (0)
 
+int ensure_deflation(ilm_batch_s* b);
+
 // CG parameter records for the current preconditioner, tolerance and limit
 int ensure_cg_params(ilm_batch_s* b, double tol, int maxiter) {
   if (tol == b->cg_tol && maxiter == b->cg_maxiter && !b->params_dirty) return ILM_OK;
+  ILM_TRY(ensure_deflation(b));
   b->params_dirty = false;
   std::vector<unsigned char> cg((size_t)b->nprob * cgff_params_size());
-  const bool pre = b->precond == 1;
   const int P = 2 * b->band_k + 1;
+  const bool bj_ready = b->bj_block > 0;
   for (int p = 0; p < b->nprob; ++p) {
     const size_t o = b->poff[p];
     void* dst = cg.data() + (size_t)p * cgff_params_size();
+    // block-Jacobi when selected, and for the problems the learned
+    // preconditioner has no network for (when block-Jacobi is set up)
+    const bool pre = b->precond == 1 || (b->precond == 2 && !b->has_band[p] && bj_ready);
     cgff_params_fill(dst, b->Shi.as<float>() + b->soff[p], b->Slo.as<float>() + b->soff[p],
                      b->rhs64.as<double>() + o, b->x64.as<double>() + o, b->ds64.as<double>() + o, b->probs[p].npts,
                      maxiter, tol, b->iters.as<int>() + p, b->relres.as<double>() + p,
@@ -296,6 +306,7 @@ int ensure_cg_params(ilm_batch_s* b, double tol, int maxiter) {
                      pre ? b->bj_size.as<int>() + b->bj_first[p] : nullptr,
                      pre ? b->bj_off.as<int>() + b->bj_first[p] : nullptr, pre ? b->bj_inv.as<float>() : nullptr,
                      pre ? b->bj_inv_lo.as<float>() : nullptr);
+    cgff_params_set_deflation(dst, b->defl_gamma[p], b->defl_z.as<double>() + o, b->defl_uz[p]);
     if (b->precond == 2 && b->has_band[p])
       cgff_params_set_band(dst, b->band.as<float>() + o * P, b->band_k, b->lseg_start.as<int>() + o,
                            b->lseg_len.as<int>() + o);
@@ -325,6 +336,82 @@ __global__ void k_batch_schur_apply(int Ptot, const int* __restrict__ pt2prob, c
 #pragma unroll
   for (int s = 16; s > 0; s >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, s);
   if (lane == 0) y[row] = acc;
+}
+
+// The Dirichlet Schur complement S = -E L^-1 R has one negative eigenvalue:
+// the net-charge mode (the lattice Green's function is normalised with
+// G(0,0) = 0, the logarithmic energy is positive only for neutral charge).
+// CG then runs on S' = S + gamma 1 1^T W, positive definite because S is
+// positive on the W-orthogonal complement of the constants, with
+// gamma = 2 |rho| / 1^T W 1 where rho is the Rayleigh quotient of the
+// constants; z = S'^-1 1 (solved once here) gives S^-1 by Sherman-Morrison.
+int ensure_deflation(ilm_batch_s* b) {
+  if (b->defl_ready) return ILM_OK;
+  const int Ptot = b->Ptot, np = b->nprob;
+  b->defl_gamma.assign(np, 0.0);
+  b->defl_uz.assign(np, 0.0);
+  ILM_TRY(b->defl_z.alloc((size_t)std::max(Ptot, 1) * sizeof(double)));
+  ILM_CHECK_CUDA(cudaMemset(b->defl_z.p, 0, (size_t)std::max(Ptot, 1) * sizeof(double)));
+  bool any = false;
+  for (int p = 0; p < np; ++p) any |= b->probs[p].kind == 0;
+  if (!any) {
+    b->defl_ready = true;
+    return ILM_OK;
+  }
+  std::vector<double> ones(Ptot, 1.0), rhs(Ptot, 0.0), y(Ptot);
+  for (int p = 0; p < np; ++p)
+    if (b->probs[p].kind == 0)
+      for (size_t k = b->poff[p]; k < b->poff[p + 1]; ++k) rhs[k] = 1.0;
+  DevBuf d1, dy, drhs, dsoff, its, rr, prm;
+  ILM_TRY(up(d1, ones));
+  ILM_TRY(up(drhs, rhs));
+  ILM_TRY(dy.alloc((size_t)Ptot * sizeof(double)));
+  if (!b->dpoff.p) ILM_TRY(up(b->dpoff, b->poff));
+  ILM_TRY(up(dsoff, b->soff));
+  k_batch_schur_apply<<<(Ptot * 32 + 255) / 256, 256>>>(Ptot, b->pt2prob.as<int>(), b->dpoff.as<size_t>(),
+                                                        b->Shi.as<float>(), b->Slo.as<float>(), dsoff.as<size_t>(),
+                                                        d1.as<double>(), dy.as<double>());
+  ILM_CHECK_LAUNCH();
+  ILM_CHECK_CUDA(cudaMemcpy(y.data(), dy.p, (size_t)Ptot * sizeof(double), cudaMemcpyDeviceToHost));
+  for (int p = 0; p < np; ++p) {
+    if (b->probs[p].kind != 0) continue;
+    double su = 0.0, sy = 0.0;
+    for (size_t k = b->poff[p]; k < b->poff[p + 1]; ++k) {
+      su += b->hds[k];
+      sy += b->hds[k] * y[k];
+    }
+    const double rho = sy / su;
+    if (rho < 0.0) b->defl_gamma[p] = 2.0 * fabs(rho) / su;
+  }
+  // z = S'^-1 1 (plain CG, tight tolerance)
+  ILM_TRY(its.alloc((size_t)np * sizeof(int)));
+  ILM_TRY(rr.alloc((size_t)np * sizeof(double)));
+  std::vector<unsigned char> cg((size_t)np * cgff_params_size());
+  for (int p = 0; p < np; ++p) {
+    const size_t o = b->poff[p];
+    void* dst = cg.data() + (size_t)p * cgff_params_size();
+    const bool pre = b->bj_block > 0;  // block-Jacobi (if set up) shortens this solve ~4x
+    cgff_params_fill(dst, b->Shi.as<float>() + b->soff[p], b->Slo.as<float>() + b->soff[p], drhs.as<double>() + o,
+                     b->defl_z.as<double>() + o, b->ds64.as<double>() + o, b->probs[p].npts, 20000, 1e-12,
+                     its.as<int>() + p, rr.as<double>() + p, pre ? b->bj_blk.as<int>() + o : nullptr,
+                     pre ? b->bj_start.as<int>() + b->bj_first[p] : nullptr,
+                     pre ? b->bj_size.as<int>() + b->bj_first[p] : nullptr,
+                     pre ? b->bj_off.as<int>() + b->bj_first[p] : nullptr, pre ? b->bj_inv.as<float>() : nullptr,
+                     pre ? b->bj_inv_lo.as<float>() : nullptr);
+    cgff_params_set_deflation(dst, b->defl_gamma[p], nullptr, 0.0);
+  }
+  ILM_TRY(up(prm, cg));
+  ILM_TRY(launch_cg_cluster(prm.p, b->order.as<int>(), np, b->counter.as<int>(), b->maxN, b->nclusters, nullptr));
+  std::vector<double> z(Ptot);
+  ILM_CHECK_CUDA(cudaMemcpy(z.data(), b->defl_z.p, (size_t)Ptot * sizeof(double), cudaMemcpyDeviceToHost));
+  for (int p = 0; p < np; ++p) {
+    if (b->defl_gamma[p] == 0.0) continue;
+    double uz = 0.0;
+    for (size_t k = b->poff[p]; k < b->poff[p + 1]; ++k) uz += b->hds[k] * z[k];
+    b->defl_uz[p] = uz;
+  }
+  b->defl_ready = true;
+  return ILM_OK;
 }
 
 }  // namespace

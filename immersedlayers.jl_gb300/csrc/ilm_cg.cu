@@ -179,6 +179,14 @@ struct CGFFParams {
   int band_k;
   const int* seg_start;
   const int* seg_len;
+  // optional rank-one deflation of the negative (net-charge) mode of the
+  // Dirichlet Schur complement: CG runs on S' = S + gamma 1 1^T W (SPD) and
+  // x = y + gamma t z, t = 1^T W y / (1 - gamma 1^T W z), z = S'^-1 1
+  // (Sherman-Morrison); gamma = 0: off.  zdef == nullptr: no correction
+  // (the solve for z itself).
+  double gamma;
+  const double* zdef;
+  double uz;
 };
 
 // y[i - r0] = (S v)_i for a CSR matrix (float-float values), one warp per row
@@ -238,6 +246,22 @@ __device__ void apply_bjacobi(const CGFFParams& pr, int r0, int r1, const float*
     }
     if (lane == 0) z[i - r0] = (double)acc.hi + (double)acc.lo;
   }
+}
+
+// sum_j w_j v_j over the whole problem from the split vector in shared
+// memory; every CTA computes the same value (fixed order)
+__device__ double full_wdot(const CGFFParams& pr, int n, const float* vhi, const float* vlo, double* red) {
+  double a = 0.0, unused = 0.0;
+  for (int j = threadIdx.x; j < n; j += blockDim.x) a += __ldg(pr.w + j) * ((double)vhi[j] + (double)vlo[j]);
+  block_sum2(a, unused, red);
+  return a;
+}
+
+__device__ double full_wdot_d(const CGFFParams& pr, int n, const double* v, double* red) {
+  double a = 0.0, unused = 0.0;
+  for (int j = threadIdx.x; j < n; j += blockDim.x) a += __ldg(pr.w + j) * v[j];
+  block_sum2(a, unused, red);
+  return a;
 }
 
 __device__ __forceinline__ int seg_nb(int j, int s, int L, int t) {
@@ -307,7 +331,8 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(CGC_THREADS
   double* ws = qs + rmax;
   double* bs = ws + rmax;
   double* ts = bs + rmax;                           // S x of the residual refresh (q stays S p)
-  double* pf = ts + rmax;                           // full direction (max_n)
+  double* xb = ts + rmax;                           // best iterate so far (true residual)
+  double* pf = xb + rmax;                           // full direction (max_n)
   double* zs = pf + max_n;                          // preconditioned residual slice (rmax)
   float* vhi = reinterpret_cast<float*>(zs + max_n); // split vector (max_n each)
   float* vlo = vhi + max_n;
@@ -317,7 +342,7 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(CGC_THREADS
     cl.sync();
     const int q = (int)cl.map_shared_rank(work, 0)[0];
     if (q >= nprob) break;
-    const CGFFParams pr = P[order[q]];
+    const CGFFParams& pr = P[order[q]];  // fields read through L1 as needed (a copy spills)
     const int n = pr.n;
     const int rows = (n + CG_CLUSTER - 1) / CG_CLUSTER;
     const int r0 = min(n, rank * rows), r1 = min(n, r0 + rows);
@@ -336,8 +361,9 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(CGC_THREADS
       }
       __syncthreads();
       matvec_rows(pr, n, r0, r1, vhi, vlo, qs);
+      const double c0 = pr.gamma != 0.0 ? pr.gamma * full_wdot(pr, n, vhi, vlo, red) : 0.0;
       __syncthreads();
-      for (int i = threadIdx.x; i < nr; i += blockDim.x) rs[i] = bs[i] - qs[i];
+      for (int i = threadIdx.x; i < nr; i += blockDim.x) rs[i] = bs[i] - qs[i] - c0;
     } else {
       for (int i = threadIdx.x; i < nr; i += blockDim.x) rs[i] = bs[i];
     }
@@ -378,6 +404,13 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(CGC_THREADS
     int it = 0;
     double relres = bnorm > 0 ? 1.0 : 0.0;
     bool done = bnorm == 0.0;
+    // stagnation guard: past the attainable accuracy (float-float products on
+    // a Schur complement of condition ~1e6 floor near 1e-10) CG drifts and
+    // eventually diverges; stop after 8 refreshes without a better true
+    // residual and return the best iterate
+    double best = 1e300;
+    int stall = 0;
+    for (int i = threadIdx.x; i < nr; i += blockDim.x) xb[i] = xs[i];
     while (!done && it < pr.maxiter) {
       for (int j = threadIdx.x; j < n; j += blockDim.x) {
         const double v = pf[j];
@@ -387,6 +420,10 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(CGC_THREADS
       }
       __syncthreads();
       matvec_rows(pr, n, r0, r1, vhi, vlo, qs);
+      if (pr.gamma != 0.0) {  // q = S' p
+        const double cp = pr.gamma * full_wdot_d(pr, n, pf, red);
+        for (int i = threadIdx.x; i < nr; i += blockDim.x) qs[i] += cp;
+      }
       __syncthreads();
       double pq = 0.0, pr_ = 0.0;
       for (int i = threadIdx.x; i < nr; i += blockDim.x) {
@@ -421,10 +458,11 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(CGC_THREADS
         }
         __syncthreads();
         matvec_rows(pr, n, r0, r1, vhi, vlo, ts);
+        const double cx = pr.gamma != 0.0 ? pr.gamma * full_wdot(pr, n, vhi, vlo, red) : 0.0;
         __syncthreads();
         double tr = 0.0, tz = 0.0;
         for (int i = threadIdx.x; i < nr; i += blockDim.x) {
-          rs[i] = bs[i] - ts[i];
+          rs[i] = bs[i] - ts[i] - cx;
           tr += rs[i] * rs[i];
           tz += ws[i] * rs[i] * rs[i];
         }
@@ -435,6 +473,13 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(CGC_THREADS
         rzn = tz;
         if (sqrt(tr) <= thr) {
           done = true;
+          break;
+        }
+        if (relres < best) {
+          best = relres;
+          stall = 0;
+          for (int i = threadIdx.x; i < nr; i += blockDim.x) xb[i] = xs[i];
+        } else if (++stall >= 8) {
           break;
         }
       }
@@ -474,6 +519,44 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(CGC_THREADS
         __syncthreads();
       }
     }
+    if (best < relres) {  // stopped past the best iterate: return that one
+      for (int i = threadIdx.x; i < nr; i += blockDim.x) xs[i] = xb[i];
+      relres = best;
+      __syncthreads();
+    }
+    if (pr.zdef != nullptr && pr.gamma != 0.0) {
+      // Sherman-Morrison back to S: x = y + gamma t z, t = 1^T W y / (1 - gamma 1^T W z)
+      double wy = 0.0, unused = 0.0;
+      for (int i = threadIdx.x; i < nr; i += blockDim.x) wy += ws[i] * xs[i];
+      block_sum2(wy, unused, red);
+      cluster_sum2(cl, pub, work + 2, slot, wy, unused);
+      slot = slot == 7 ? 1 : slot + 1;
+      const double t = wy / (1.0 - pr.gamma * pr.uz);
+      for (int i = threadIdx.x; i < nr; i += blockDim.x) xs[i] += pr.gamma * t * pr.zdef[r0 + i];
+      __syncthreads();
+      cl.sync();
+      // reported residual: the true one of S x = b (the deflated operator's
+      // residual equals it up to the accuracy of z)
+      for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        const int c = j / rows;
+        const double v = cl.map_shared_rank(xs, c)[j - c * rows];
+        const float h = (float)v;
+        vhi[j] = h;
+        vlo[j] = (float)(v - (double)h);
+      }
+      __syncthreads();
+      matvec_rows(pr, n, r0, r1, vhi, vlo, ts);
+      __syncthreads();
+      double tr = 0.0;
+      for (int i = threadIdx.x; i < nr; i += blockDim.x) {
+        const double d = bs[i] - ts[i];
+        tr += d * d;
+      }
+      block_sum2(tr, unused, red);
+      cluster_sum2(cl, pub, work + 2, slot, tr, unused);
+      slot = slot == 7 ? 1 : slot + 1;
+      relres = bnorm > 0 ? sqrt(tr) / bnorm : 0.0;
+    }
     for (int i = threadIdx.x; i < nr; i += blockDim.x) pr.x[r0 + i] = xs[i];
     if (rank == 0 && threadIdx.x == 0) {
       if (pr.iters) *pr.iters = it;
@@ -486,7 +569,7 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(CGC_THREADS
 
 size_t cg_cluster_smem(int max_n) {
   const int rmax = (max_n + CG_CLUSTER - 1) / CG_CLUSTER;
-  return (16 + 2 * CGC_WARPS + 4 + 6 * (size_t)rmax + 2 * (size_t)max_n) * sizeof(double) +
+  return (16 + 2 * CGC_WARPS + 4 + 7 * (size_t)rmax + 2 * (size_t)max_n) * sizeof(double) +
          2 * (size_t)max_n * sizeof(float) + 64;
 }
 
@@ -531,6 +614,13 @@ void cgff_params_fill_csr(void* dst, const float* vhi, const float* vlo, const i
   CGFFParams p{vhi, vlo, b, x, w, n, maxiter, tol, iters, relres,
                nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, rowptr, colidx, x0};
   *static_cast<CGFFParams*>(dst) = p;
+}
+
+void cgff_params_set_deflation(void* dst, double gamma, const double* zdef, double uz) {
+  CGFFParams* p = static_cast<CGFFParams*>(dst);
+  p->gamma = gamma;
+  p->zdef = zdef;
+  p->uz = uz;
 }
 
 void cgff_params_set_band(void* dst, const float* band, int band_k, const int* seg_start, const int* seg_len) {

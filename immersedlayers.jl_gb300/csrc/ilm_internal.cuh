@@ -314,6 +314,7 @@ int net_forward_packed(ilm_net_t n, int N, const float* feat, const int* sst, co
                        cudaStream_t st);
 int net_band(ilm_net_t n);
 int net_nfeat(ilm_net_t n);
+void cgff_params_set_deflation(void* dst, double gamma, const double* zdef, double uz);
 void cgff_params_set_band(void* dst, const float* band, int band_k, const int* seg_start, const int* seg_len);
 void cgff_params_fill_csr(void* dst, const float* vhi, const float* vlo, const int* rowptr, const int* colidx,
                           const double* b, double* x, const double* x0, const double* w, int n, int maxiter,

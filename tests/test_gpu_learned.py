@@ -119,14 +119,21 @@ def test_learned_pcg_solutions_match_plain(cuda):
     torch.cuda.synchronize()
     assert (rr0 <= 1e-10).all() and (rr1 <= 1e-10).all(), (rr0, rr1)
     assert float((f0 - f1).abs().max() / f0.abs().max()) < 1e-7
-    # and the Schur-only entry points agree with each other: S (S^-1 b) = b
+    # and the Schur-only entry points agree with each other: S (S^-1 b) = b.
+    # White-noise data on the two-body problems (condition ~1e6) reach ~1e-10
+    # at best in float-float products; the stagnation guard stops there.
     bs.set_precond("none")
     b = torch.randn(bs.total_points, dtype=torch.float64, device="cuda")
-    xs = bs.schur_solve(b, tol=1e-11)
+    xs = bs.schur_solve(b, tol=1e-9)
     its, rr = bs.info()
-    assert (rr <= 1e-11).all(), rr
+    assert (rr <= 1e-9).all(), rr
     r = bs.schur_apply(xs) - b
-    assert float(r.norm() / b.norm()) < 1e-10
+    assert float(r.norm() / b.norm()) < 1e-9
+    # past the attainable accuracy the guard returns the best iterate
+    xs = bs.schur_solve(b, tol=1e-14, maxiter=20000)
+    its, rr = bs.info()
+    assert np.isfinite(rr).all() and (rr < 1e-8).all(), rr
+    assert (its < 20000).all(), its
 
 
 def test_training_reduces_loss(cuda):
