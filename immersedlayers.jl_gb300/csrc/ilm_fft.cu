@@ -5,14 +5,16 @@
 // (called from src/grid_operators.jl:177-179, built at src/cache.jl:321-324).
 //
 // Pipeline for an n1 x n2 field (x fastest) and padded sizes P1 >= 2 n1 - 1,
-// P2 >= 2 n2 - 1 (P = 2^a 3^b):
+// P2 >= 2 n2 - 1 (P = 2^a or 3 * 2^a):
 //   1. k_rfft_rows  : each of the n2 rows -> real FFT of length P1 (complex
 //                     FFT of P1/2 + split), zero padding pruned on input.
 //   2. k_cols       : each of the P1/2+1 spectral columns -> length-P2 complex
 //                     FFT, multiply by the real LGF spectrum, inverse FFT; only
 //                     the n2 input rows are read and the n2 output rows written.
 //   3. k_irfft_rows : each of the n2 rows -> inverse real FFT, first n1 values.
-// The FFTs are Stockham auto-sort radix-4/3/2 transforms held in shared memory.
+// FP32 transforms of length 64..1024 run as register four-step FFTs (two
+// in-register DFT passes, one shared-memory exchange); other lengths and FP64
+// use Stockham auto-sort radix-4/3/2 transforms held in shared memory.
 // The LGF table and its spectrum are built on the device in FP64 with the same
 // kernels and cached per size.
 #include <math.h>
@@ -305,15 +307,14 @@ __global__ void k_d2f(const double* __restrict__ in, float* __restrict__ out, si
 // ---------------------------------------------------------------------------
 // host side: sizes, twiddles, library caches
 // ---------------------------------------------------------------------------
+// smallest 2^a or 3 * 2^a (>= 4) not below n: every such size from 64 to 1024
+// has a register four-step factorisation (N1, N2 in {8, 12, 16, 24, 32})
 int good_fft_size(int n) {
-  long best = -1;
-  for (long p3 = 1; p3 < 4L * n + 4; p3 *= 3) {
-    long p2 = 4;
-    while (p2 * p3 < n) p2 *= 2;
-    long cand = p2 * p3;
-    if (best < 0 || cand < best) best = cand;
-  }
-  return (int)best;
+  long p2 = 4;
+  while (p2 < n) p2 *= 2;
+  long p3 = 12;
+  while (p3 < n) p3 *= 2;
+  return (int)std::min(p2, p3);
 }
 
 namespace {
@@ -402,6 +403,373 @@ int twiddle_table(int L, int dtype, const void** out) {
   return ILM_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Register four-step FFTs (FP32 path).  A length L = N1 * N2 transform with
+// N1, N2 in {8, 12, 16, 24, 32} (every 2^a and 3 * 2^a from 64 to 1024) is
+// done as N2 DFTs of length N1 held in registers, a twiddle by w_L^{k1 n2},
+// and N1 DFTs of length N2 held in registers, with one shared-memory exchange
+// between them.  The data of one transform sit in shared memory as an
+// N1 x (N2 + 1) matrix (row padding keeps both passes free of bank
+// conflicts); element n = n1 N2 + n2 is at n1 (N2 + 1) + n2, in natural order
+// before and after the transform.
+// ---------------------------------------------------------------------------
+__constant__ float2 c_tw32[32];  // exp(-2 pi i j / 32)
+__constant__ float2 c_tw24[24];  // exp(-2 pi i j / 24)
+
+constexpr int FAST_THREADS = 256;
+constexpr int FAST_CW = 8;  // spectral columns per CTA
+
+__host__ __device__ constexpr int bitrev_c(int i, int bits) {
+  int r = 0;
+  for (int b = 0; b < bits; ++b) r |= ((i >> b) & 1) << (bits - 1 - b);
+  return r;
+}
+__host__ __device__ constexpr int ilog2_c(int n) { return n <= 1 ? 0 : 1 + ilog2_c(n / 2); }
+
+// w_N^j (forward sign) for N dividing 32 or 24; conjugated for SIGN > 0
+template <int N, int SIGN>
+__device__ __forceinline__ float2 twr(int j) {
+  float2 w;
+  if (32 % N == 0) w = c_tw32[j * (32 / N)];
+  else w = c_tw24[j * (24 / N)];
+  if (SIGN > 0) w.y = -w.y;
+  return w;
+}
+
+// in-register radix-2 DIT DFT, N a power of two
+template <int N, int SIGN>
+__device__ __forceinline__ void dft_pow2(float2 (&a)[N]) {
+  constexpr int B = ilog2_c(N);
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    const int j = bitrev_c(i, B);
+    if (j > i) {
+      const float2 t = a[i];
+      a[i] = a[j];
+      a[j] = t;
+    }
+  }
+#pragma unroll
+  for (int half = 1; half < N; half *= 2) {
+#pragma unroll
+    for (int k = 0; k < N; k += 2 * half) {
+#pragma unroll
+      for (int j = 0; j < half; ++j) {
+        float2 t = a[k + j + half];
+        if (j != 0) t = cmul(twr<N, SIGN>(j * (N / (2 * half))), t);
+        a[k + j + half] = csub(a[k + j], t);
+        a[k + j] = cadd(a[k + j], t);
+      }
+    }
+  }
+}
+
+// N = 3 M: three interleaved DFTs of length M and a radix-3 combination
+template <int M, int SIGN>
+__device__ __forceinline__ void dft_3m(float2 (&a)[3 * M]) {
+  constexpr int N = 3 * M;
+  float2 b0[M], b1[M], b2[M];
+#pragma unroll
+  for (int m = 0; m < M; ++m) {
+    b0[m] = a[3 * m];
+    b1[m] = a[3 * m + 1];
+    b2[m] = a[3 * m + 2];
+  }
+  dft_pow2<M, SIGN>(b0);
+  dft_pow2<M, SIGN>(b1);
+  dft_pow2<M, SIGN>(b2);
+  const float s3 = 0.86602540378443864676f * (float)SIGN;
+#pragma unroll
+  for (int k = 0; k < M; ++k) {
+    float2 t1 = b1[k], t2 = b2[k];
+    if (k != 0) {
+      t1 = cmul(twr<N, SIGN>(k), t1);
+      t2 = cmul(twr<N, SIGN>(2 * k), t2);
+    }
+    const float2 s = cadd(t1, t2), d = csub(t1, t2);
+    float2 m;
+    m.x = b0[k].x - 0.5f * s.x;
+    m.y = b0[k].y - 0.5f * s.y;
+    float2 id;  // i * SIGN * sqrt(3)/2 * d
+    id.x = -s3 * d.y;
+    id.y = s3 * d.x;
+    a[k] = cadd(b0[k], s);
+    a[k + M] = cadd(m, id);
+    a[k + 2 * M] = csub(m, id);
+  }
+}
+
+template <int N, int SIGN>
+__device__ __forceinline__ void dft_reg(float2 (&a)[N]) {
+  if constexpr (N == 12) dft_3m<4, SIGN>(a);
+  else if constexpr (N == 24) dft_3m<8, SIGN>(a);
+  else dft_pow2<N, SIGN>(a);
+}
+
+// One transform of length N1 N2 on the padded matrix x, by the G threads
+// g = 0..G-1 of a group (act: this group has a transform).  twL[j * tws] =
+// exp(-2 pi i j / (N1 N2)).  Called by every thread of the CTA.
+template <int N1, int N2, int SIGN>
+__device__ __forceinline__ void fft4step(float2* x, int g, bool act, const float2* __restrict__ twL, int tws) {
+  constexpr int ST = N2 + 1;
+  if (act && g < N2) {
+    float2 a[N1];
+#pragma unroll
+    for (int n1 = 0; n1 < N1; ++n1) a[n1] = x[n1 * ST + g];
+    dft_reg<N1, SIGN>(a);
+#pragma unroll
+    for (int k1 = 1; k1 < N1; ++k1) {
+      float2 w = twL[(size_t)(k1 * g) * tws];
+      if (SIGN > 0) w.y = -w.y;
+      a[k1] = cmul(w, a[k1]);
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < N1; ++k1) x[k1 * ST + g] = a[k1];
+  }
+  __syncthreads();
+  float2 b[N2];
+  if (act && g < N1) {
+#pragma unroll
+    for (int n2 = 0; n2 < N2; ++n2) b[n2] = x[g * ST + n2];
+    dft_reg<N2, SIGN>(b);
+  }
+  __syncthreads();
+  if (act && g < N1) {
+#pragma unroll
+    for (int k2 = 0; k2 < N2; ++k2) {
+      const int k = g + N1 * k2;
+      x[(k / N2) * ST + (k % N2)] = b[k2];
+    }
+  }
+  __syncthreads();
+}
+
+template <int N1, int N2>
+__device__ __forceinline__ int padpos(int k) {
+  return (k / N2) * (N2 + 1) + (k % N2);
+}
+
+// rows: real FFT of length 2H (H = N1 N2) per row, rb rows per CTA
+template <int N1, int N2>
+__device__ void rfft_rows_body(const ConvJobDev& J, int r0, float2* sm) {
+  constexpr int H = N1 * N2, G = N1 > N2 ? N1 : N2, CS = N1 * (N2 + 1);
+  constexpr int RB = FAST_THREADS / G;
+  const int nr = min(RB, J.n2 - r0);
+  const float* __restrict__ in = static_cast<const float*>(J.in);
+  for (int idx = threadIdx.x; idx < RB * H; idx += FAST_THREADS) {
+    const int r = idx / H, m = idx - r * H;
+    float2 z = make_float2(0.f, 0.f);
+    if (r < nr) {
+      const float* x = in + (size_t)(r0 + r) * J.n1;
+      const int i0 = 2 * m;
+      if (i0 < J.n1) z.x = x[i0];
+      if (i0 + 1 < J.n1) z.y = x[i0 + 1];
+    }
+    sm[r * CS + padpos<N1, N2>(m)] = z;
+  }
+  __syncthreads();
+  const int r = threadIdx.x / G, g = threadIdx.x - r * G;
+  const float2* tw = static_cast<const float2*>(J.tw1);
+  fft4step<N1, N2, -1>(sm + (r < RB ? r : 0) * CS, g, r < nr, tw, 2);
+  float2* W = static_cast<float2*>(J.work);
+  for (int idx = threadIdx.x; idx < nr * (H + 1); idx += FAST_THREADS) {
+    const int rr = idx / (H + 1), k = idx - rr * (H + 1);
+    const float2* Z = sm + rr * CS;
+    const float2 zk = Z[padpos<N1, N2>(k == H ? 0 : k)];
+    float2 zc = Z[padpos<N1, N2>(k == 0 ? 0 : H - k)];
+    zc.y = -zc.y;
+    const float2 e = tw[k];
+    const float2 s = cadd(zk, zc), d = csub(zk, zc);
+    const float2 ed = cmul(e, d);
+    float2 X;
+    X.x = 0.5f * (s.x + ed.y);
+    X.y = 0.5f * (s.y - ed.x);
+    W[(size_t)(r0 + rr) * (H + 1) + k] = X;
+  }
+}
+
+template <int N1, int N2>
+__device__ void irfft_rows_body(const ConvJobDev& J, int r0, float2* sm) {
+  constexpr int H = N1 * N2, G = N1 > N2 ? N1 : N2, CS = N1 * (N2 + 1);
+  constexpr int RB = FAST_THREADS / G;
+  const int nr = min(RB, J.n2 - r0);
+  const float2* tw = static_cast<const float2*>(J.tw1);
+  const float2* W = static_cast<const float2*>(J.work);
+  for (int idx = threadIdx.x; idx < RB * H; idx += FAST_THREADS) {
+    const int r = idx / H, k = idx - r * H;
+    float2 z = make_float2(0.f, 0.f);
+    if (r < nr) {
+      const float2* X = W + (size_t)(r0 + r) * (H + 1);
+      const float2 xk = X[k];
+      float2 xc = X[H - k];
+      xc.y = -xc.y;
+      float2 e = tw[k];
+      e.y = -e.y;
+      const float2 s = cadd(xk, xc), d = csub(xk, xc);
+      const float2 ed = cmul(e, d);
+      z.x = 0.5f * (s.x - ed.y);
+      z.y = 0.5f * (s.y + ed.x);
+    }
+    sm[r * CS + padpos<N1, N2>(k)] = z;
+  }
+  __syncthreads();
+  const int r = threadIdx.x / G, g = threadIdx.x - r * G;
+  fft4step<N1, N2, 1>(sm + (r < RB ? r : 0) * CS, g, r < nr, tw, 2);
+  float* __restrict__ out = static_cast<float*>(J.out);
+  const float sc = (float)J.scale;
+  for (int idx = threadIdx.x; idx < nr * H; idx += FAST_THREADS) {
+    const int rr = idx / H, m = idx - rr * H;
+    const float2 z = sm[rr * CS + padpos<N1, N2>(m)];
+    float* o = out + (size_t)(r0 + rr) * J.n1;
+    const int i0 = 2 * m;
+    if (i0 < J.n1) o[i0] = z.x * sc;
+    if (i0 + 1 < J.n1) o[i0 + 1] = z.y * sc;
+  }
+}
+
+// columns: FFT of length P2 = N1 N2, spectrum multiply, inverse FFT
+template <int N1, int N2>
+__device__ void cols_body(const ConvJobDev& J, int c0, float2* sm) {
+  constexpr int L = N1 * N2, G = N1 > N2 ? N1 : N2, CS = N1 * (N2 + 1);
+  const int ncols = (J.P1 >> 1) + 1;
+  const int nc = min(FAST_CW, ncols - c0);
+  float2* W = static_cast<float2*>(J.work);
+  for (int idx = threadIdx.x; idx < FAST_CW * L; idx += FAST_THREADS) {
+    const int c = idx % FAST_CW, row = idx / FAST_CW;
+    float2 v = make_float2(0.f, 0.f);
+    if (c < nc && row < J.n2) v = W[(size_t)row * ncols + c0 + c];
+    sm[c * CS + padpos<N1, N2>(row)] = v;
+  }
+  __syncthreads();
+  const int c = threadIdx.x / G, g = threadIdx.x - c * G;
+  const bool act = c < nc;
+  float2* x = sm + (c < FAST_CW ? c : 0) * CS;
+  const float2* tw = static_cast<const float2*>(J.tw2);
+  fft4step<N1, N2, -1>(x, g, act, tw, 1);
+  const float* __restrict__ spec = static_cast<const float*>(J.spec);
+  const int hp2 = L / 2 + 1;
+  for (int idx = threadIdx.x; idx < nc * L; idx += FAST_THREADS) {
+    const int cc = idx / L, ky = idx - cc * L;
+    const int kk = ky <= L - ky ? ky : L - ky;
+    const float sv = spec[(size_t)(c0 + cc) * hp2 + kk];
+    float2* p = sm + cc * CS + padpos<N1, N2>(ky);
+    float2 v = *p;
+    v.x *= sv;
+    v.y *= sv;
+    *p = v;
+  }
+  __syncthreads();
+  fft4step<N1, N2, 1>(x, g, act, tw, 1);
+  for (int idx = threadIdx.x; idx < FAST_CW * J.n2out; idx += FAST_THREADS) {
+    const int cc = idx % FAST_CW, row = idx / FAST_CW;
+    if (cc < nc) W[(size_t)row * ncols + c0 + cc] = sm[cc * CS + padpos<N1, N2>(row)];
+  }
+}
+
+// dispatch on the transform length (block-uniform)
+#define ILM_FAST_SWITCH(L, CALL)                 \
+  switch (L) {                                   \
+    case 64: CALL(8, 8); break;                  \
+    case 96: CALL(8, 12); break;                 \
+    case 128: CALL(8, 16); break;                \
+    case 192: CALL(8, 24); break;                \
+    case 256: CALL(16, 16); break;               \
+    case 384: CALL(16, 24); break;               \
+    case 512: CALL(16, 32); break;               \
+    case 768: CALL(24, 32); break;               \
+    case 1024: CALL(32, 32); break;              \
+    default: break;                              \
+  }
+
+__device__ __forceinline__ int find_job_fast(const ConvJobDev* jobs, int njobs, int u, int which) {
+  int lo = 0, hi = njobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    const int off = which == 0 ? jobs[mid].frow_off : jobs[mid].col_off;
+    if (off <= u) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void __launch_bounds__(FAST_THREADS) k_rfft_rows_fast(const ConvJobDev* __restrict__ jobs, int njobs) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* sm = reinterpret_cast<float2*>(smem_raw);
+  const int jb = find_job_fast(jobs, njobs, blockIdx.x, 0);
+  const ConvJobDev J = jobs[jb];
+  const int r0 = (blockIdx.x - J.frow_off) * J.frb;
+#define ILM_CALL_RF(a, b) rfft_rows_body<a, b>(J, r0, sm)
+  ILM_FAST_SWITCH(J.P1 >> 1, ILM_CALL_RF)
+#undef ILM_CALL_RF
+}
+
+__global__ void __launch_bounds__(FAST_THREADS) k_irfft_rows_fast(const ConvJobDev* __restrict__ jobs, int njobs) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* sm = reinterpret_cast<float2*>(smem_raw);
+  const int jb = find_job_fast(jobs, njobs, blockIdx.x, 0);
+  const ConvJobDev J = jobs[jb];
+  const int r0 = (blockIdx.x - J.frow_off) * J.frb;
+#define ILM_CALL_IRF(a, b) irfft_rows_body<a, b>(J, r0, sm)
+  ILM_FAST_SWITCH(J.P1 >> 1, ILM_CALL_IRF)
+#undef ILM_CALL_IRF
+}
+
+__global__ void __launch_bounds__(FAST_THREADS) k_cols_fast(const ConvJobDev* __restrict__ jobs, int njobs) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* sm = reinterpret_cast<float2*>(smem_raw);
+  const int jb = find_job_fast(jobs, njobs, blockIdx.x, 1);
+  const ConvJobDev J = jobs[jb];
+  const int c0 = (blockIdx.x - J.col_off) * FAST_CW;
+#define ILM_CALL_C(a, b) cols_body<a, b>(J, c0, sm)
+  ILM_FAST_SWITCH(J.P2, ILM_CALL_C)
+#undef ILM_CALL_C
+}
+
+// host: factor of a fast length (0 if none), threads per transform, smem
+bool fast_len(int L, int* n1, int* n2) {
+  static const int tab[][3] = {{64, 8, 8},    {96, 8, 12},   {128, 8, 16},  {192, 8, 24},   {256, 16, 16},
+                               {384, 16, 24}, {512, 16, 32}, {768, 24, 32}, {1024, 32, 32}};
+  for (const auto& t : tab)
+    if (t[0] == L) {
+      *n1 = t[1];
+      *n2 = t[2];
+      return true;
+    }
+  return false;
+}
+
+size_t fast_transform_floats2(int L) {  // padded matrix size of one transform (float2)
+  int a, b;
+  if (!fast_len(L, &a, &b)) return 0;
+  return (size_t)a * (b + 1);
+}
+
+int fast_group(int L) {
+  int a, b;
+  fast_len(L, &a, &b);
+  return a > b ? a : b;
+}
+
+int ensure_fast_tables() {
+  static bool done = false;
+  static std::mutex mu;
+  std::lock_guard<std::mutex> lk(mu);
+  if (done) return ILM_OK;
+  float2 t32[32], t24[24];
+  for (int j = 0; j < 32; ++j) {
+    const double a = -2.0 * M_PI * j / 32.0;
+    t32[j] = make_float2((float)cos(a), (float)sin(a));
+  }
+  for (int j = 0; j < 24; ++j) {
+    const double a = -2.0 * M_PI * j / 24.0;
+    t24[j] = make_float2((float)cos(a), (float)sin(a));
+  }
+  ILM_CHECK_CUDA(cudaMemcpyToSymbol(c_tw32, t32, sizeof(t32)));
+  ILM_CHECK_CUDA(cudaMemcpyToSymbol(c_tw24, t24, sizeof(t24)));
+  done = true;
+  return ILM_OK;
+}
+
 template <typename T>
 size_t rows_smem(int P1) { return (size_t)(3 * (P1 / 2) + 2) * sizeof(typename CT<T>::t); }
 
@@ -417,6 +785,18 @@ int cols_cw(int P2) {
 
 template <typename T>
 int launch_prepared(const ConvJobDev* jd, int nj, const ConvLaunch& L, int mode, cudaStream_t st) {
+  if (L.fast && mode == 0 && sizeof(T) == 4) {
+    ILM_CHECK_CUDA(cudaFuncSetAttribute(k_rfft_rows_fast, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.fsm_rows));
+    ILM_CHECK_CUDA(cudaFuncSetAttribute(k_cols_fast, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.fsm_cols));
+    ILM_CHECK_CUDA(cudaFuncSetAttribute(k_irfft_rows_fast, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.fsm_rows));
+    k_rfft_rows_fast<<<L.frows, FAST_THREADS, L.fsm_rows, st>>>(jd, nj);
+    ILM_CHECK_LAUNCH();
+    k_cols_fast<<<L.cols, FAST_THREADS, L.fsm_cols, st>>>(jd, nj);
+    ILM_CHECK_LAUNCH();
+    k_irfft_rows_fast<<<L.frows, FAST_THREADS, L.fsm_rows, st>>>(jd, nj);
+    ILM_CHECK_LAUNCH();
+    return ILM_OK;
+  }
   size_t sm_rows = rows_smem<T>(L.maxP1);
   size_t sm_cols = (size_t)2 * L.CW * (L.maxP2 + 1) * sizeof(typename CT<T>::t);
   ILM_CHECK_CUDA(cudaFuncSetAttribute(k_rfft_rows<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_rows));
@@ -611,10 +991,40 @@ int conv_apply(ConvPlan* plan, const void* in, void* out, double inv_factor, cud
 
 int conv_jobs_finalize(std::vector<ConvJobDev>& jobs, int dtype, ConvLaunch* L) {
   int rows = 0, cols = 0, maxP1 = 0, maxP2 = 0;
+  bool fast = dtype == ILM_F32 && !jobs.empty();
   for (auto& J : jobs) {
     maxP1 = std::max(maxP1, J.P1);
     maxP2 = std::max(maxP2, J.P2);
+    int a, b;
+    fast = fast && fast_len(J.P1 / 2, &a, &b) && fast_len(J.P2, &a, &b);
   }
+  if (fast) {  // register four-step FFTs: rows in groups, 8 spectral columns per CTA
+    ILM_TRY(ensure_fast_tables());
+    size_t smr = 0, smc = 0;
+    int frows = 0;
+    for (auto& J : jobs) {
+      const int H = J.P1 / 2;
+      J.frb = FAST_THREADS / fast_group(H);
+      J.frow_off = frows;
+      frows += (J.n2 + J.frb - 1) / J.frb;
+      J.row_off = 0;
+      J.col_off = cols;
+      cols += (H + 1 + FAST_CW - 1) / FAST_CW;
+      smr = std::max(smr, (size_t)J.frb * fast_transform_floats2(H) * sizeof(float2));
+      smc = std::max(smc, (size_t)FAST_CW * fast_transform_floats2(J.P2) * sizeof(float2));
+    }
+    L->fast = 1;
+    L->frows = frows;
+    L->rows = 0;
+    L->cols = cols;
+    L->CW = FAST_CW;
+    L->maxP1 = maxP1;
+    L->maxP2 = maxP2;
+    L->fsm_rows = smr;
+    L->fsm_cols = smc;
+    return ILM_OK;
+  }
+  L->fast = 0;
   const int CW = dtype == ILM_F64 ? cols_cw<double>(maxP2) : cols_cw<float>(maxP2);
   for (auto& J : jobs) {
     J.row_off = rows;

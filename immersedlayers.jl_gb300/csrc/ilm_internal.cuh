@@ -159,9 +159,12 @@ struct ConvJobDev {
   int P1, P2;
   double scale;
   int row_off, col_off;
+  int frow_off, frb;   // register-FFT path: first row CTA of this job, rows per CTA
 };
 struct ConvLaunch {
   int rows = 0, cols = 0, CW = 1, maxP1 = 0, maxP2 = 0;
+  int fast = 0, frows = 0;             // register four-step FFT path (FP32)
+  size_t fsm_rows = 0, fsm_cols = 0;   // its dynamic shared memory per CTA
 };
 // fill row/col offsets of a job table and the launch geometry
 int conv_jobs_finalize(std::vector<ConvJobDev>& jobs, int dtype, ConvLaunch* L);

@@ -248,3 +248,24 @@ def test_determinism(setup):
     il.surface_divergence_(b, f, S["sc"])
     il.inverse_laplacian_(b, S["sc"])
     assert torch.equal(a.data, b.data)
+
+
+@pytest.mark.parametrize("n1,n2", [(32, 32), (48, 200), (64, 96), (127, 64), (192, 130), (256, 384), (383, 48),
+                                   (512, 256), (40, 1100)])
+def test_inverse_laplacian_fft_sizes(cuda, n1, n2):
+    """FP32 LGF convolution at every padded length of the register four-step
+    path (64 ... 1024, powers of two and 3 x powers of two) and at lengths
+    that take the Stockham path (rows of 32 / columns of 2048)."""
+    import torch
+    import immersedlayers as il
+    h = 0.01
+    g = il.PhysicalGrid(h=h, nx=n1 + 1, ny=n2 + 1)
+    og = O.Grid(n1 + 1, n2 + 1, h, (n1 + 1) // 2, (n2 + 1) // 2)
+    c = il.SurfaceScalarCache(None, g, dtype=torch.float32)
+    rng = np.random.default_rng(n1 * 7 + n2)
+    w = rng.standard_normal((n1, n2))
+    src = il.NodesPrimal.zeros(g, torch.float32).set_numpy(w)
+    out = il.NodesPrimal.zeros(g, torch.float32)
+    il.inverse_laplacian_(out, src, c)
+    ref = O.InverseLaplacian(n1, n2, 1.0 / h ** 2)(src.numpy_components())
+    assert rel(out.numpy_components(), ref) < 2e-5
