@@ -451,15 +451,16 @@ def _rank_specs(nprob, rank):
 
 def _algorithmic_bytes(stage, st, its):
     """Algorithmic HBM bytes of one launch of a stage (FP32 grid data)."""
-    P, C, S2, FFT = st["points"], st["cells"], st["sum_npts2"], st["sum_fft"]
+    P, C, S2, FFT, BOX = st["points"], st["cells"], st["sum_npts2"], st["sum_fft"], st["box_cells"]
     if "FFT" in stage:
-        # read the n1 x n2 field, write it back, read the half spectrum (P1/2+1)(P2/2+1)
-        return 4 * C + 4 * C + 4 * FFT / 4
+        # read the source box, write the n1 x n2 field, read the half spectrum
+        # (P1/2+1)(P2/2+1); the correction pass also reads f*
+        return 4 * BOX + 4 * C + 4 * FFT / 4 + (4 * C if "f*" in stage and "corr" in stage else 0)
     if "CG" in stage:
         # every iteration streams the FP64 Schur matrix once
         return 8 * S2 * float(its.mean())
     if "scatter" in stage:
-        return 4 * C + 16 * P
+        return 4 * BOX + 16 * P
     return 8 * C
 
 

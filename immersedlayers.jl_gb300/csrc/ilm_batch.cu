@@ -8,6 +8,8 @@
 // complement.  All per-problem descriptors ("tasks") are built on the host
 // once, at batch creation, and live in device memory, so a solve issues no
 // host<->device traffic and can be captured in a CUDA graph.
+#include <array>
+#include <climits>
 #include <string.h>
 
 #include <math.h>
@@ -20,8 +22,12 @@
 
 namespace ilm {
 
+// One DDF scatter of a problem: the tiles of the box [tx0, tx0 + ntxb) x
+// [ty0, ...) of its tile grid (ntx tiles per row); cells of other tiles are
+// not written
 struct BScatterTask {
   int n1, n2, ntx, tile0;
+  int tx0, ty0, ntxb, pad_;
   const int* tptr;
   const int* tpts;
   const int* bx;
@@ -36,8 +42,10 @@ struct BScatterTask {
   void* out;
 };
 
+// a stencil over the box [i0, i0 + bw) x [j0, j0 + bh) of its output array
 struct BStencilTask {
   int NX, NY, blk0;
+  int i0, j0, bw, bh;
   const void* in;
   void* out;
   double scale;
@@ -53,6 +61,11 @@ struct BGatherTask {
   const void* ny;
   const void* arr[2];
   int n1[2], n2[2], xs[2], ys[2], coef[2];
+  // 0: arr is the sampled field (n1 x n2); 1: the field is the x-difference
+  // of the cell array arr ((n1 - 1) x n2, u faces, zero on the ghost
+  // columns); 2: the y-difference (n1 x (n2 - 1), v faces, zero on the ghost
+  // rows) -- the Nodes -> Edges gradient fused into the gather
+  int gmode[2];
   void* out;
   double scale;
 };
@@ -82,15 +95,23 @@ __device__ __forceinline__ T bcoef(int code, const T* nx, const T* ny, int k) {
   return (T)0;
 }
 
+// Deterministic scatter: one thread per output cell of a 32 x 8 tile; the
+// tile's candidate points (index order) are staged in shared memory 256 at
+// a time, one point per thread, then every thread sums them in that order.
 template <typename T>
 __global__ void __launch_bounds__(SB_X* SB_Y) k_bscatter(const BScatterTask* __restrict__ tasks, int ntasks) {
+  constexpr int NB = SB_X * SB_Y;
+  __shared__ int s_bx[NB], s_by[NB];
+  __shared__ T s_amp[NB], s_wx[NB * NTAP], s_wy[NB * NTAP];
   const int ti = find_task(tasks, ntasks, (int)blockIdx.x, &BScatterTask::tile0);
   const BScatterTask& S = tasks[ti];
   const int t = blockIdx.x - S.tile0;
-  const int tx = t % S.ntx, ty = t / S.ntx;
+  const int tx = S.tx0 + t % S.ntxb, ty = S.ty0 + t / S.ntxb;
+  const int tile = ty * S.ntx + tx;
   const int i = tx * SB_X + threadIdx.x;
   const int j = ty * SB_Y + threadIdx.y;
-  const int p0 = S.tptr[t], p1 = S.tptr[t + 1];
+  const int tid = threadIdx.y * SB_X + threadIdx.x;
+  const int p0 = S.tptr[tile], p1 = S.tptr[tile + 1];
   const T* __restrict__ wx = static_cast<const T*>(S.wx);
   const T* __restrict__ wy = static_cast<const T*>(S.wy);
   const T* __restrict__ wsc = static_cast<const T*>(S.wsc);
@@ -98,12 +119,27 @@ __global__ void __launch_bounds__(SB_X* SB_Y) k_bscatter(const BScatterTask* __r
   const T* nx = static_cast<const T*>(S.nx);
   const T* ny = static_cast<const T*>(S.ny);
   T acc = (T)0;
-  for (int p = p0; p < p1; ++p) {
-    const int k = S.tpts[p];
-    const int di = i - S.bx[k];
-    const int dj = j - S.by[k];
-    if ((unsigned)di < (unsigned)NTAP && (unsigned)dj < (unsigned)NTAP)
-      acc += wsc[k] * (bcoef<T>(S.coef, nx, ny, k) * in[k]) * wx[k * NTAP + di] * wy[k * NTAP + dj];
+  for (int c0 = p0; c0 < p1; c0 += NB) {
+    const int nc = min(NB, p1 - c0);
+    if (tid < nc) {
+      const int k = S.tpts[c0 + tid];
+      s_bx[tid] = S.bx[k];
+      s_by[tid] = S.by[k];
+      s_amp[tid] = wsc[k] * (bcoef<T>(S.coef, nx, ny, k) * in[k]);
+#pragma unroll
+      for (int q = 0; q < NTAP; ++q) {
+        s_wx[tid * NTAP + q] = wx[k * NTAP + q];
+        s_wy[tid * NTAP + q] = wy[k * NTAP + q];
+      }
+    }
+    __syncthreads();
+    for (int q = 0; q < nc; ++q) {
+      const int di = i - s_bx[q];
+      const int dj = j - s_by[q];
+      if ((unsigned)di < (unsigned)NTAP && (unsigned)dj < (unsigned)NTAP)
+        acc += s_amp[q] * s_wx[q * NTAP + di] * s_wy[q * NTAP + dj];
+    }
+    __syncthreads();
   }
   if (i < S.n1 && j < S.n2) static_cast<T*>(S.out)[(size_t)j * S.n1 + i] = acc;
 }
@@ -114,40 +150,15 @@ __global__ void k_bdiv(const BStencilTask* __restrict__ tasks, int ntasks) {
   const int ti = find_task(tasks, ntasks, (int)blockIdx.x, &BStencilTask::blk0);
   const BStencilTask& S = tasks[ti];
   const int NX = S.NX, NY = S.NY;
-  const int nbx = (NX - 1 + SB_X - 1) / SB_X;
+  const int nbx = (S.bw + SB_X - 1) / SB_X;
   const int b = blockIdx.x - S.blk0;
-  const int i = (b % nbx) * SB_X + threadIdx.x, j = (b / nbx) * SB_Y + threadIdx.y;
-  if (i >= NX - 1 || j >= NY - 1) return;
+  const int i = S.i0 + (b % nbx) * SB_X + threadIdx.x, j = S.j0 + (b / nbx) * SB_Y + threadIdx.y;
+  if (i >= S.i0 + S.bw || j >= S.j0 + S.bh) return;
   const T* u = static_cast<const T*>(S.in);
   const T* v = u + (size_t)NX * (NY - 1);
   const T du = u[(size_t)j * NX + i + 1] - u[(size_t)j * NX + i];
   const T dv = v[(size_t)(j + 1) * (NX - 1) + i] - v[(size_t)j * (NX - 1) + i];
   static_cast<T*>(S.out)[(size_t)j * (NX - 1) + i] = (du + dv) * (T)S.scale;
-}
-
-// Nodes{Primal} -> Edges{Primal} gradient (block tiles over the NX x NY box)
-template <typename T>
-__global__ void k_bgrad(const BStencilTask* __restrict__ tasks, int ntasks) {
-  const int ti = find_task(tasks, ntasks, (int)blockIdx.x, &BStencilTask::blk0);
-  const BStencilTask& S = tasks[ti];
-  const int NX = S.NX, NY = S.NY;
-  const int nbx = (NX + SB_X - 1) / SB_X;
-  const int b = blockIdx.x - S.blk0;
-  const int i = (b % nbx) * SB_X + threadIdx.x, j = (b / nbx) * SB_Y + threadIdx.y;
-  const T* w = static_cast<const T*>(S.in);
-  T* u = static_cast<T*>(S.out);
-  T* v = u + (size_t)NX * (NY - 1);
-  const T sc = (T)S.scale;
-  if (i < NX && j < NY - 1) {
-    T r = (T)0;
-    if (i >= 1 && i <= NX - 2) r = (w[(size_t)j * (NX - 1) + i] - w[(size_t)j * (NX - 1) + i - 1]) * sc;
-    u[(size_t)j * NX + i] = r;
-  }
-  if (i < NX - 1 && j < NY) {
-    T r = (T)0;
-    if (j >= 1 && j <= NY - 2) r = (w[(size_t)j * (NX - 1) + i] - w[(size_t)(j - 1) * (NX - 1) + i]) * sc;
-    v[(size_t)j * (NX - 1) + i] = r;
-  }
 }
 
 template <typename T>
@@ -165,7 +176,7 @@ __global__ void k_bgather(const BGatherTask* __restrict__ tasks, int ntasks, int
     const T* wx = static_cast<const T*>(G.wx[xs]) + k * NTAP;
     const T* wy = static_cast<const T*>(G.wy[ys]) + k * NTAP;
     const T* a = static_cast<const T*>(G.arr[q]);
-    const int n1 = G.n1[q], n2 = G.n2[q];
+    const int n1 = G.n1[q], n2 = G.n2[q], gm = G.gmode[q];
     T acc = (T)0;
 #pragma unroll
     for (int jj = 0; jj < NTAP; ++jj) {
@@ -176,7 +187,15 @@ __global__ void k_bgather(const BGatherTask* __restrict__ tasks, int ntasks, int
       for (int ii = 0; ii < NTAP; ++ii) {
         const int i = b0 + ii;
         if ((unsigned)i >= (unsigned)n1) continue;
-        racc += wx[ii] * a[(size_t)j * n1 + i];
+        T v;
+        if (gm == 0) {
+          v = a[(size_t)j * n1 + i];
+        } else if (gm == 1) {
+          v = (i >= 1 && i <= n1 - 2) ? a[(size_t)j * (n1 - 1) + i] - a[(size_t)j * (n1 - 1) + i - 1] : (T)0;
+        } else {
+          v = (j >= 1 && j <= n2 - 2) ? a[(size_t)j * n1 + i] - a[(size_t)(j - 1) * n1 + i] : (T)0;
+        }
+        racc += wx[ii] * v;
       }
       acc += wy[jj] * racc;
     }
@@ -220,10 +239,11 @@ struct ilm_batch_s {
   DevBuf cgp, iters, relres, order, counter;
   int nclusters = 1;
   // tasks
-  DevBuf scatA, divA, gradA, gathA, scatB, divB, convA, convB, schurP;
-  int n_scatA = 0, n_divA = 0, n_gradA = 0, n_gathA = 0, n_scatB = 0, n_divB = 0;
-  int blk_scatA = 0, blk_divA = 0, blk_gradA = 0, blk_scatB = 0, blk_divB = 0;
+  DevBuf scatA, divA, gathA, scatB, divB, convA, convB, schurP;
+  int n_scatA = 0, n_divA = 0, n_gathA = 0, n_scatB = 0, n_divB = 0;
+  int blk_scatA = 0, blk_divA = 0, blk_scatB = 0, blk_divB = 0;
   int n_conv = 0;
+  size_t box_cells = 0;  // cells of all source boxes
   ConvLaunch convL;
   int schur_tiles = 0;
   double cg_tol = -1.0;
@@ -553,10 +573,38 @@ int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* 
     woff[p + 1] = woff[p] + (size_t)n2 * (P1[p] / 2 + 1) * 2 * e;
   }
   ILM_TRY(B->convwork.alloc(woff[nprob]));
+  // Source box of each problem: every cell of the two convolution inputs that
+  // can be non-zero (DDF windows of all points, both staggerings, widened by
+  // the divergence stencil) lies in [ca, cb) x [ra, rb).  The scatters and
+  // divergences write only this box and the FFT row pass reads only it.
+  std::vector<std::array<int, 4>> box(nprob);
+  for (int p = 0; p < nprob; ++p) {
+    const HostWindows& W = Wall[p];
+    int xmin = INT_MAX, xmax = INT_MIN, ymin = INT_MAX, ymax = INT_MIN;
+    for (int k = 0; k < probs[p].npts; ++k)
+      for (int d = 0; d < 2; ++d) {
+        xmin = std::min(xmin, W.bx[d][k]);
+        xmax = std::max(xmax, W.bx[d][k] + NTAP - 1);
+        ymin = std::min(ymin, W.by[d][k]);
+        ymax = std::max(ymax, W.by[d][k] + NTAP - 1);
+      }
+    const int n1 = probs[p].nx - 1, n2 = probs[p].ny - 1;
+    int ca = std::max(0, xmin - 3), cb = std::min(n1, xmax + 4);
+    int ra = std::max(0, ymin - 3), rb = std::min(n2, ymax + 4);
+    if (ca >= cb) ca = 0, cb = 1;  // every window off the grid: nothing is scattered
+    if (ra >= rb) ra = 0, rb = 1;
+    box[p] = {ca, cb, ra, rb};
+    B->box_cells += (size_t)(cb - ca) * (rb - ra);
+  }
   std::vector<ConvJobDev> jobsA(nprob), jobsB(nprob);
   for (int p = 0; p < nprob; ++p) {
     ConvJobDev J;
     memset(&J, 0, sizeof(J));
+    J.has_box = 1;
+    J.ca = box[p][0];
+    J.cb = box[p][1];
+    J.ra = box[p][2];
+    J.rb = box[p][3];
     ILM_TRY(conv_resources(P1[p], P2[p], dtype, &J.spec, &J.tw1, &J.tw2, nullptr));
     J.work = static_cast<unsigned char*>(B->convwork.p) + woff[p];
     J.n1 = probs[p].nx - 1;
@@ -567,7 +615,12 @@ int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* 
     J.scale = probs[p].h * probs[p].h;  // L^{-1} = h^2 G* under GridScaling
     J.in = J.out = static_cast<unsigned char*>(B->fstar.p) + B->foff[p] * e;
     jobsA[p] = J;
-    J.in = J.out = static_cast<unsigned char*>(B->corr.p) + B->foff[p] * e;
+    // correction: f = f* + L^-1 q_B, written straight into the caller's
+    // field (out_base at launch)
+    J.in = static_cast<unsigned char*>(B->corr.p) + B->foff[p] * e;
+    J.out = nullptr;
+    J.out_off = B->foff[p] * e;
+    J.add = static_cast<unsigned char*>(B->fstar.p) + B->foff[p] * e;
     jobsB[p] = J;
   }
   ILM_TRY(conv_jobs_finalize(jobsA, dtype, &B->convL));
@@ -588,8 +641,17 @@ int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* 
     T.n1 = sh.n1;
     T.n2 = sh.n2;
     T.ntx = Wall[p].ntx[pc];
+    // cells written: the source box (faces: one more column / row, which the
+    // divergence of the box reads)
+    const int ext = pc == PC_P ? 0 : 1;
+    const int xa = std::min(box[p][0], sh.n1 - 1), xb = std::min(box[p][1] + ext, sh.n1);
+    const int ya = std::min(box[p][2], sh.n2 - 1), yb = std::min(box[p][3] + ext, sh.n2);
+    T.tx0 = xa / SB_X;
+    T.ty0 = ya / SB_Y;
+    T.ntxb = (xb - 1) / SB_X - T.tx0 + 1;
+    const int ntyb = (yb - 1) / SB_Y - T.ty0 + 1;
     T.tile0 = tiles;
-    tiles += Wall[p].ntx[pc] * Wall[p].nty[pc];
+    tiles += T.ntxb * ntyb;
     T.tptr = B->tptr[pc].as<int>() + tpo[pc][p];
     T.tpts = B->tpts[pc].as<int>() + tso[pc][p];
     T.bx = B->bx[dx].as<int>() + o;
@@ -607,16 +669,20 @@ int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* 
   auto edge_u = [&](int p) { return ptr_at(B->edges, eoff[p]); };
   auto edge_v = [&](int p) { return ptr_at(B->edges, eoff[p] + (size_t)probs[p].nx * (probs[p].ny - 1)); };
   auto field = [&](const DevBuf& b, int p) { return ptr_at(b, B->foff[p]); };
-  auto stencil = [&](int p, const void* in, void* outp, int& blks, bool grad) {
+  // divergence Edges -> Nodes{Primal} over the source box
+  auto stencil = [&](int p, const void* in, void* outp, int& blks) {
     BStencilTask T;
     T.NX = probs[p].nx;
     T.NY = probs[p].ny;
     T.blk0 = blks;
-    const int w = grad ? T.NX : T.NX - 1, h = grad ? T.NY : T.NY - 1;
-    blks += ((w + SB_X - 1) / SB_X) * ((h + SB_Y - 1) / SB_Y);
+    T.i0 = box[p][0];
+    T.bw = box[p][1] - box[p][0];
+    T.j0 = box[p][2];
+    T.bh = box[p][3] - box[p][2];
+    blks += ((T.bw + SB_X - 1) / SB_X) * ((T.bh + SB_Y - 1) / SB_Y);
     T.in = in;
     T.out = outp;
-    T.scale = grad ? 1.0 : 1.0 / probs[p].h;
+    T.scale = 1.0 / probs[p].h;
     return T;
   };
   auto gath = [&](int p, int& pts) {
@@ -638,15 +704,15 @@ int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* 
     return G;
   };
   std::vector<BScatterTask> sA, sB;
-  std::vector<BStencilTask> dA, gA, dB;
+  std::vector<BStencilTask> dA, dB;
   std::vector<BGatherTask> hA;
-  int tA = 0, tB = 0, bdA = 0, bgA = 0, bdB = 0, ptsA = 0;
+  int tA = 0, tB = 0, bdA = 0, bdB = 0, ptsA = 0;
   for (int p = 0; p < nprob; ++p) {
     const int nx_ = probs[p].nx, ny_ = probs[p].ny;
     if (probs[p].kind == 0) {  // Dirichlet: f* = L^-1 D_s [f]; correction R s
       sA.push_back(scat(p, PC_U, B->jump, CF_NX, edge_u(p), tA));
       sA.push_back(scat(p, PC_V, B->jump, CF_NY, edge_v(p), tA));
-      dA.push_back(stencil(p, edge_u(p), field(B->fstar, p), bdA, false));
+      dA.push_back(stencil(p, edge_u(p), field(B->fstar, p), bdA));
       BGatherTask G = gath(p, ptsA);
       G.nterms = 1;
       G.arr[0] = field(B->fstar, p);
@@ -658,18 +724,19 @@ int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* 
       G.scale = 1.0;
       hA.push_back(G);
       sB.push_back(scat(p, PC_P, B->s, CF_ONE, field(B->corr, p), tB));
-    } else {  // Neumann: f* = L^-1 R [vn]; rhs from G_s f*; correction D_s [phi]
+    } else {  // Neumann: f* = L^-1 R [vn]; rhs from G_s f* (gradient fused into the gather); correction D_s [phi]
       sA.push_back(scat(p, PC_P, B->jump, CF_ONE, field(B->fstar, p), tA));
-      gA.push_back(stencil(p, field(B->fstar, p), edge_u(p), bgA, true));
       BGatherTask G = gath(p, ptsA);
       G.nterms = 2;
-      G.arr[0] = edge_u(p);
+      G.arr[0] = field(B->fstar, p);
+      G.gmode[0] = 1;
       G.n1[0] = nx_;
       G.n2[0] = ny_ - 1;
       G.xs[0] = 1;
       G.ys[0] = 0;
       G.coef[0] = CF_NX;
-      G.arr[1] = edge_v(p);
+      G.arr[1] = field(B->fstar, p);
+      G.gmode[1] = 2;
       G.n1[1] = nx_ - 1;
       G.n2[1] = ny_;
       G.xs[1] = 0;
@@ -679,7 +746,7 @@ int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* 
       hA.push_back(G);
       sB.push_back(scat(p, PC_U, B->s, CF_NX, edge_u(p), tB));
       sB.push_back(scat(p, PC_V, B->s, CF_NY, edge_v(p), tB));
-      dB.push_back(stencil(p, edge_u(p), field(B->corr, p), bdB, false));
+      dB.push_back(stencil(p, edge_u(p), field(B->corr, p), bdB));
     }
   }
   B->n_scatA = (int)sA.size();
@@ -688,15 +755,12 @@ int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* 
   B->blk_scatB = tB;
   B->n_divA = (int)dA.size();
   B->blk_divA = bdA;
-  B->n_gradA = (int)gA.size();
-  B->blk_gradA = bgA;
   B->n_divB = (int)dB.size();
   B->blk_divB = bdB;
   B->n_gathA = (int)hA.size();
   ILM_TRY(up(B->scatA, sA));
   ILM_TRY(up(B->scatB, sB));
   ILM_TRY(up(B->divA, dA));
-  ILM_TRY(up(B->gradA, gA));
   ILM_TRY(up(B->divB, dB));
   ILM_TRY(up(B->gathA, hA));
 
@@ -785,40 +849,34 @@ int ilm_batch_solve(ilm_batch_t b, const void* fplus, const void* fminus, void* 
   b->launches += 3;
   MARK();  // 4: LGF FFT convolution (f*)
   BDISPATCH(dt, {
-    if (b->n_gradA) k_bgrad<T><<<b->blk_gradA, dim3(SB_X, SB_Y), 0, st>>>(b->gradA.as<BStencilTask>(), b->n_gradA);
-    ILM_CHECK_LAUNCH();
-    b->launches += b->n_gradA ? 1 : 0;
-    MARK();  // 5: gradient stencil
     k_bgather<T><<<(Ptot + 127) / 128, 128, 0, st>>>(b->gathA.as<BGatherTask>(), b->n_gathA, Ptot);
     ILM_CHECK_LAUNCH();
     k_rhs64<T><<<pb, 256, 0, st>>>(Ptot, b->g.as<T>(), b->avg.as<T>(), b->rhs64.as<double>());
     ILM_CHECK_LAUNCH();
     b->launches += 2;
-    MARK();  // 6: DDF gather + Schur right-hand side
+    MARK();  // 5: DDF gather (Neumann: with the gradient) + Schur right-hand side
   });
   ILM_TRY(launch_cg_cluster(b->cgp.p, b->order.as<int>(), b->nprob, b->counter.as<int>(), b->maxN, b->nclusters, st));
   b->launches += 1;
-  MARK();  // 7: Schur CG
+  MARK();  // 6: Schur CG
   ILM_TRY(st_convert(Ptot, ILM_F64, b->x64.p, dt, s_out, st));
   ILM_CHECK_CUDA(cudaMemcpyAsync(b->s.p, s_out, (size_t)Ptot * es(dt), cudaMemcpyDeviceToDevice, st));
   b->launches += 1;
-  MARK();  // 8: convert
+  MARK();  // 7: convert
   BDISPATCH(dt, {
     if (b->n_scatB) k_bscatter<T><<<b->blk_scatB, dim3(SB_X, SB_Y), 0, st>>>(b->scatB.as<BScatterTask>(), b->n_scatB);
     ILM_CHECK_LAUNCH();
     b->launches += b->n_scatB ? 1 : 0;
-    MARK();  // 9: DDF scatter (correction)
+    MARK();  // 8: DDF scatter (correction)
     if (b->n_divB) k_bdiv<T><<<b->blk_divB, dim3(SB_X, SB_Y), 0, st>>>(b->divB.as<BStencilTask>(), b->n_divB);
     ILM_CHECK_LAUNCH();
     b->launches += b->n_divB ? 1 : 0;
-    MARK();  // 10: divergence stencil
+    MARK();  // 9: divergence stencil
   });
-  ILM_TRY(conv_jobs_launch(b->convB.as<ConvJobDev>(), b->n_conv, b->convL, dt, st));
+  // f = f* + L^-1 (correction source), written into f_out by the inverse row pass
+  ILM_TRY(conv_jobs_launch(b->convB.as<ConvJobDev>(), b->n_conv, b->convL, dt, st, f_out));
   b->launches += 3;
-  MARK();  // 11: LGF FFT convolution (correction)
-  ILM_TRY(st_axpby(b->ftot, dt, 1.0, b->corr.p, 1.0, b->fstar.p, f_out, st));
-  b->launches += 1;
-  MARK();  // 12: f = f* + correction
+  MARK();  // 10: LGF FFT convolution (correction) + f*
 #undef MARK
   return ILM_OK;
 }
@@ -914,6 +972,7 @@ int ilm_batch_stats(ilm_batch_t b, double* stats) {
   stats[2] = p2;
   stats[3] = fft;
   stats[4] = b->nprob;
+  stats[5] = (double)b->box_cells;
   return ILM_OK;
 }
 

@@ -142,11 +142,14 @@ __global__ void k_rfft_rows(const ConvJobDev* __restrict__ jobs, int njobs) {
   C* A = reinterpret_cast<C*>(smem_raw);
   C* B = A + H;
   const T* __restrict__ x = static_cast<const T*>(J.in) + (size_t)row * J.n1;
+  // input box: rows outside [ra, rb) and columns outside [ca, cb) are zero
+  const bool rin = !J.has_box || (row >= J.ra && row < J.rb);
+  const int clo = J.has_box ? J.ca : 0, chi = J.has_box ? J.cb : J.n1;
   for (int m = threadIdx.x; m < H; m += blockDim.x) {
     const int i0 = 2 * m;
     C z;
-    z.x = i0 < J.n1 ? x[i0] : (T)0;
-    z.y = i0 + 1 < J.n1 ? x[i0 + 1] : (T)0;
+    z.x = rin && i0 >= clo && i0 < chi ? x[i0] : (T)0;
+    z.y = rin && i0 + 1 >= clo && i0 + 1 < chi ? x[i0 + 1] : (T)0;
     A[m] = z;
   }
   __syncthreads();
@@ -229,7 +232,7 @@ __global__ void k_cols(const ConvJobDev* __restrict__ jobs, int njobs, int CW, i
 
 // 3. inverse real row FFTs: work -> out (first n1 values of each row) * scale
 template <typename T>
-__global__ void k_irfft_rows(const ConvJobDev* __restrict__ jobs, int njobs) {
+__global__ void k_irfft_rows(const ConvJobDev* __restrict__ jobs, int njobs, void* out_base) {
   using C = typename CT<T>::t;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int jb = find_job(jobs, njobs, blockIdx.x, true);
@@ -258,13 +261,16 @@ __global__ void k_irfft_rows(const ConvJobDev* __restrict__ jobs, int njobs) {
   }
   __syncthreads();
   C* Z = stockham<T, 1>(A, B, H, 1, H, tw, J.P1);
-  T* __restrict__ out = static_cast<T*>(J.out) + (size_t)row * J.n1;
+  T* obase = out_base ? reinterpret_cast<T*>(static_cast<unsigned char*>(out_base) + J.out_off)
+                      : static_cast<T*>(J.out);
+  T* __restrict__ out = obase + (size_t)row * J.n1;
+  const T* __restrict__ add = J.add ? static_cast<const T*>(J.add) + (size_t)row * J.n1 : nullptr;
   const T sc = (T)J.scale;
   for (int m = threadIdx.x; m < H; m += blockDim.x) {
     const int i0 = 2 * m;
     C z = Z[m];
-    if (i0 < J.n1) out[i0] = z.x * sc;
-    if (i0 + 1 < J.n1) out[i0 + 1] = z.y * sc;
+    if (i0 < J.n1) out[i0] = add ? add[i0] + z.x * sc : z.x * sc;
+    if (i0 + 1 < J.n1) out[i0 + 1] = add ? add[i0 + 1] + z.y * sc : z.y * sc;
   }
 }
 
@@ -549,24 +555,45 @@ __device__ __forceinline__ int padpos(int k) {
   return (k / N2) * (N2 + 1) + (k % N2);
 }
 
-// rows: real FFT of length 2H (H = N1 N2) per row, rb rows per CTA
+// Asynchronous global -> shared copies (cp.async, sm_80+): every load of a
+// stage is issued before the first one is waited for, so a CTA has its whole
+// tile in flight instead of one dependent load per loop trip.  valid = false
+// copies nothing and zero-fills the destination (src must still be a valid
+// address).
+__device__ __forceinline__ void cpa4(void* dst, const void* src, bool valid) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(s), "l"(src), "r"(valid ? 4 : 0) : "memory");
+}
+__device__ __forceinline__ void cpa8(void* dst, const void* src, bool valid) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(s), "l"(src), "r"(valid ? 8 : 0) : "memory");
+}
+__device__ __forceinline__ void cpa_wait_all() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
+
+// rows: real FFT of length 2H (H = N1 N2) per row, RB rows per CTA starting
+// at row r0 (rows up to the job's box end rb); input columns outside the box
+// [ca, cb) are zero
 template <int N1, int N2>
-__device__ void rfft_rows_body(const ConvJobDev& J, int r0, float2* sm) {
+__device__ void rfft_rows_body(const ConvJobDev& J, int r0, int rend, float2* sm) {
   constexpr int H = N1 * N2, G = N1 > N2 ? N1 : N2, CS = N1 * (N2 + 1);
   constexpr int RB = FAST_THREADS / G;
-  const int nr = min(RB, J.n2 - r0);
+  const int nr = min(RB, rend - r0);
   const float* __restrict__ in = static_cast<const float*>(J.in);
+  const int clo = J.has_box ? J.ca : 0, chi = J.has_box ? J.cb : J.n1;
   for (int idx = threadIdx.x; idx < RB * H; idx += FAST_THREADS) {
     const int r = idx / H, m = idx - r * H;
-    float2 z = make_float2(0.f, 0.f);
-    if (r < nr) {
-      const float* x = in + (size_t)(r0 + r) * J.n1;
-      const int i0 = 2 * m;
-      if (i0 < J.n1) z.x = x[i0];
-      if (i0 + 1 < J.n1) z.y = x[i0 + 1];
-    }
-    sm[r * CS + padpos<N1, N2>(m)] = z;
+    float2* d = sm + r * CS + padpos<N1, N2>(m);
+    const float* x = in + (size_t)(r0 + (r < nr ? r : 0)) * J.n1;
+    const int i0 = 2 * m;
+    const bool v0 = r < nr && i0 >= clo && i0 < chi;
+    const bool v1 = r < nr && i0 + 1 >= clo && i0 + 1 < chi;
+    cpa4(&d->x, v0 ? x + i0 : in, v0);
+    cpa4(&d->y, v1 ? x + i0 + 1 : in, v1);
   }
+  cpa_wait_all();
   __syncthreads();
   const int r = threadIdx.x / G, g = threadIdx.x - r * G;
   const float2* tw = static_cast<const float2*>(J.tw1);
@@ -588,18 +615,24 @@ __device__ void rfft_rows_body(const ConvJobDev& J, int r0, float2* sm) {
   }
 }
 
+// inverse rows: the rows' H + 1 spectral values are staged in `raw`
+// (RB x (H + 1)), split into the half-length complex transform, inverse FFT,
+// first n1 values (+ the `add` field) written
 template <int N1, int N2>
-__device__ void irfft_rows_body(const ConvJobDev& J, int r0, float2* sm) {
+__device__ void irfft_rows_body(const ConvJobDev& J, int r0, float2* sm, float2* raw, void* out_base) {
   constexpr int H = N1 * N2, G = N1 > N2 ? N1 : N2, CS = N1 * (N2 + 1);
   constexpr int RB = FAST_THREADS / G;
   const int nr = min(RB, J.n2 - r0);
   const float2* tw = static_cast<const float2*>(J.tw1);
-  const float2* W = static_cast<const float2*>(J.work);
+  const float2* W = static_cast<const float2*>(J.work) + (size_t)r0 * (H + 1);
+  for (int idx = threadIdx.x; idx < nr * (H + 1); idx += FAST_THREADS) cpa8(raw + idx, W + idx, true);
+  cpa_wait_all();
+  __syncthreads();
   for (int idx = threadIdx.x; idx < RB * H; idx += FAST_THREADS) {
     const int r = idx / H, k = idx - r * H;
     float2 z = make_float2(0.f, 0.f);
     if (r < nr) {
-      const float2* X = W + (size_t)(r0 + r) * (H + 1);
+      const float2* X = raw + r * (H + 1);
       const float2 xk = X[k];
       float2 xc = X[H - k];
       xc.y = -xc.y;
@@ -613,33 +646,56 @@ __device__ void irfft_rows_body(const ConvJobDev& J, int r0, float2* sm) {
     sm[r * CS + padpos<N1, N2>(k)] = z;
   }
   __syncthreads();
+  // the added field's rows go into `raw` (free now; RB (H + 1) float2 >= RB n1
+  // floats) while the transforms run
+  const float* __restrict__ add = static_cast<const float*>(J.add);
+  float* addr = reinterpret_cast<float*>(raw);
+  const int n1 = J.n1;
+  if (add) {
+    const float* a0 = add + (size_t)r0 * n1;
+    for (int idx = threadIdx.x; idx < nr * n1; idx += FAST_THREADS) cpa4(addr + idx, a0 + idx, true);
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+  }
   const int r = threadIdx.x / G, g = threadIdx.x - r * G;
   fft4step<N1, N2, 1>(sm + (r < RB ? r : 0) * CS, g, r < nr, tw, 2);
-  float* __restrict__ out = static_cast<float*>(J.out);
+  if (add) {
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    __syncthreads();
+  }
+  float* obase = out_base ? reinterpret_cast<float*>(static_cast<unsigned char*>(out_base) + J.out_off)
+                          : static_cast<float*>(J.out);
   const float sc = (float)J.scale;
   for (int idx = threadIdx.x; idx < nr * H; idx += FAST_THREADS) {
     const int rr = idx / H, m = idx - rr * H;
     const float2 z = sm[rr * CS + padpos<N1, N2>(m)];
-    float* o = out + (size_t)(r0 + rr) * J.n1;
+    float* o = obase + (size_t)(r0 + rr) * n1;
     const int i0 = 2 * m;
-    if (i0 < J.n1) o[i0] = z.x * sc;
-    if (i0 + 1 < J.n1) o[i0 + 1] = z.y * sc;
+    if (add) {
+      const float* a = addr + rr * n1;
+      if (i0 < n1) o[i0] = a[i0] + z.x * sc;
+      if (i0 + 1 < n1) o[i0 + 1] = a[i0 + 1] + z.y * sc;
+    } else {
+      if (i0 < n1) o[i0] = z.x * sc;
+      if (i0 + 1 < n1) o[i0 + 1] = z.y * sc;
+    }
   }
 }
 
-// columns: FFT of length P2 = N1 N2, spectrum multiply, inverse FFT
+// columns: FFT of length P2 = N1 N2, spectrum multiply, inverse FFT; only
+// the rows [ra, rb) of the row-pass output are read (the rest are zero)
 template <int N1, int N2>
 __device__ void cols_body(const ConvJobDev& J, int c0, float2* sm) {
   constexpr int L = N1 * N2, G = N1 > N2 ? N1 : N2, CS = N1 * (N2 + 1);
   const int ncols = (J.P1 >> 1) + 1;
   const int nc = min(FAST_CW, ncols - c0);
+  const int ra = J.has_box ? J.ra : 0, rb = J.has_box ? J.rb : J.n2;
   float2* W = static_cast<float2*>(J.work);
   for (int idx = threadIdx.x; idx < FAST_CW * L; idx += FAST_THREADS) {
     const int c = idx % FAST_CW, row = idx / FAST_CW;
-    float2 v = make_float2(0.f, 0.f);
-    if (c < nc && row < J.n2) v = W[(size_t)row * ncols + c0 + c];
-    sm[c * CS + padpos<N1, N2>(row)] = v;
+    const bool v = c < nc && row >= ra && row < rb;
+    cpa8(sm + c * CS + padpos<N1, N2>(row), v ? W + (size_t)row * ncols + c0 + c : W, v);
   }
+  cpa_wait_all();
   __syncthreads();
   const int c = threadIdx.x / G, g = threadIdx.x - c * G;
   const bool act = c < nc;
@@ -681,11 +737,12 @@ __device__ void cols_body(const ConvJobDev& J, int c0, float2* sm) {
     default: break;                              \
   }
 
+// which: 0 forward rows (frow_off), 1 columns (col_off), 2 inverse rows (irow_off)
 __device__ __forceinline__ int find_job_fast(const ConvJobDev* jobs, int njobs, int u, int which) {
   int lo = 0, hi = njobs - 1;
   while (lo < hi) {
     const int mid = (lo + hi + 1) >> 1;
-    const int off = which == 0 ? jobs[mid].frow_off : jobs[mid].col_off;
+    const int off = which == 0 ? jobs[mid].frow_off : which == 1 ? jobs[mid].col_off : jobs[mid].irow_off;
     if (off <= u) lo = mid;
     else hi = mid - 1;
   }
@@ -697,19 +754,24 @@ __global__ void __launch_bounds__(FAST_THREADS) k_rfft_rows_fast(const ConvJobDe
   float2* sm = reinterpret_cast<float2*>(smem_raw);
   const int jb = find_job_fast(jobs, njobs, blockIdx.x, 0);
   const ConvJobDev J = jobs[jb];
-  const int r0 = (blockIdx.x - J.frow_off) * J.frb;
-#define ILM_CALL_RF(a, b) rfft_rows_body<a, b>(J, r0, sm)
+  const int ra = J.has_box ? J.ra : 0, rb = J.has_box ? J.rb : J.n2;
+  const int r0 = ra + (blockIdx.x - J.frow_off) * J.frb;
+#define ILM_CALL_RF(a, b) rfft_rows_body<a, b>(J, r0, rb, sm)
   ILM_FAST_SWITCH(J.P1 >> 1, ILM_CALL_RF)
 #undef ILM_CALL_RF
 }
 
-__global__ void __launch_bounds__(FAST_THREADS) k_irfft_rows_fast(const ConvJobDev* __restrict__ jobs, int njobs) {
+__global__ void __launch_bounds__(FAST_THREADS)
+    k_irfft_rows_fast(const ConvJobDev* __restrict__ jobs, int njobs, void* out_base) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* sm = reinterpret_cast<float2*>(smem_raw);
-  const int jb = find_job_fast(jobs, njobs, blockIdx.x, 0);
+  const int jb = find_job_fast(jobs, njobs, blockIdx.x, 2);
   const ConvJobDev J = jobs[jb];
-  const int r0 = (blockIdx.x - J.frow_off) * J.frb;
-#define ILM_CALL_IRF(a, b) irfft_rows_body<a, b>(J, r0, sm)
+  const int r0 = (blockIdx.x - J.irow_off) * J.frb;
+  // layout: the transforms' padded matrices (frb x N1 (N2 + 1)), then the
+  // staging rows (frb x (H + 1)); both sizes are multiples of 8 bytes
+#define ILM_CALL_IRF(a, b) \
+  irfft_rows_body<a, b>(J, r0, sm, sm + (size_t)J.frb * (a) * ((b) + 1), out_base)
   ILM_FAST_SWITCH(J.P1 >> 1, ILM_CALL_IRF)
 #undef ILM_CALL_IRF
 }
@@ -784,16 +846,18 @@ int cols_cw(int P2) {
 }
 
 template <typename T>
-int launch_prepared(const ConvJobDev* jd, int nj, const ConvLaunch& L, int mode, cudaStream_t st) {
+int launch_prepared(const ConvJobDev* jd, int nj, const ConvLaunch& L, int mode, cudaStream_t st,
+                    void* out_base = nullptr) {
   if (L.fast && mode == 0 && sizeof(T) == 4) {
     ILM_CHECK_CUDA(cudaFuncSetAttribute(k_rfft_rows_fast, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.fsm_rows));
     ILM_CHECK_CUDA(cudaFuncSetAttribute(k_cols_fast, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.fsm_cols));
-    ILM_CHECK_CUDA(cudaFuncSetAttribute(k_irfft_rows_fast, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.fsm_rows));
-    k_rfft_rows_fast<<<L.frows, FAST_THREADS, L.fsm_rows, st>>>(jd, nj);
+    ILM_CHECK_CUDA(cudaFuncSetAttribute(k_irfft_rows_fast, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)L.fsm_irows));
+    if (L.frows > 0) k_rfft_rows_fast<<<L.frows, FAST_THREADS, L.fsm_rows, st>>>(jd, nj);
     ILM_CHECK_LAUNCH();
     k_cols_fast<<<L.cols, FAST_THREADS, L.fsm_cols, st>>>(jd, nj);
     ILM_CHECK_LAUNCH();
-    k_irfft_rows_fast<<<L.frows, FAST_THREADS, L.fsm_rows, st>>>(jd, nj);
+    k_irfft_rows_fast<<<L.firows, FAST_THREADS, L.fsm_irows, st>>>(jd, nj, out_base);
     ILM_CHECK_LAUNCH();
     return ILM_OK;
   }
@@ -807,7 +871,7 @@ int launch_prepared(const ConvJobDev* jd, int nj, const ConvLaunch& L, int mode,
   k_cols<T><<<L.cols, 256, sm_cols, st>>>(jd, nj, L.CW, mode);
   ILM_CHECK_LAUNCH();
   if (mode == 0) {
-    k_irfft_rows<T><<<L.rows, 256, sm_rows, st>>>(jd, nj);
+    k_irfft_rows<T><<<L.rows, 256, sm_rows, st>>>(jd, nj, out_base);
     ILM_CHECK_LAUNCH();
   }
   return ILM_OK;
@@ -993,6 +1057,11 @@ int conv_jobs_finalize(std::vector<ConvJobDev>& jobs, int dtype, ConvLaunch* L) 
   int rows = 0, cols = 0, maxP1 = 0, maxP2 = 0;
   bool fast = dtype == ILM_F32 && !jobs.empty();
   for (auto& J : jobs) {
+    if (J.has_box && !(J.ra >= 0 && J.ra < J.rb && J.rb <= J.n2 && J.ca >= 0 && J.ca < J.cb && J.cb <= J.n1)) {
+      set_error("convolution input box [%d,%d) x [%d,%d) outside the %d x %d field", J.ca, J.cb, J.ra, J.rb, J.n1,
+                J.n2);
+      return ILM_ERR_INVALID_ARG;
+    }
     maxP1 = std::max(maxP1, J.P1);
     maxP2 = std::max(maxP2, J.P2);
     int a, b;
@@ -1000,21 +1069,28 @@ int conv_jobs_finalize(std::vector<ConvJobDev>& jobs, int dtype, ConvLaunch* L) 
   }
   if (fast) {  // register four-step FFTs: rows in groups, 8 spectral columns per CTA
     ILM_TRY(ensure_fast_tables());
-    size_t smr = 0, smc = 0;
-    int frows = 0;
+    size_t smr = 0, smc = 0, smi = 0;
+    int frows = 0, firows = 0;
     for (auto& J : jobs) {
       const int H = J.P1 / 2;
       J.frb = FAST_THREADS / fast_group(H);
       J.frow_off = frows;
-      frows += (J.n2 + J.frb - 1) / J.frb;
+      const int nbox = J.has_box ? J.rb - J.ra : J.n2;
+      frows += (nbox + J.frb - 1) / J.frb;
+      J.irow_off = firows;
+      firows += (J.n2 + J.frb - 1) / J.frb;
       J.row_off = 0;
       J.col_off = cols;
       cols += (H + 1 + FAST_CW - 1) / FAST_CW;
-      smr = std::max(smr, (size_t)J.frb * fast_transform_floats2(H) * sizeof(float2));
+      const size_t tr = (size_t)J.frb * fast_transform_floats2(H) * sizeof(float2);
+      smr = std::max(smr, tr);
+      smi = std::max(smi, tr + (size_t)J.frb * (H + 1) * sizeof(float2));
       smc = std::max(smc, (size_t)FAST_CW * fast_transform_floats2(J.P2) * sizeof(float2));
     }
     L->fast = 1;
     L->frows = frows;
+    L->firows = firows;
+    L->fsm_irows = smi;
     L->rows = 0;
     L->cols = cols;
     L->CW = FAST_CW;
@@ -1040,10 +1116,11 @@ int conv_jobs_finalize(std::vector<ConvJobDev>& jobs, int dtype, ConvLaunch* L) 
   return ILM_OK;
 }
 
-int conv_jobs_launch(const ConvJobDev* jobs_dev, int njobs, const ConvLaunch& L, int dtype, cudaStream_t st) {
+int conv_jobs_launch(const ConvJobDev* jobs_dev, int njobs, const ConvLaunch& L, int dtype, cudaStream_t st,
+                     void* out_base) {
   if (njobs == 0) return ILM_OK;
-  if (dtype == ILM_F64) return launch_prepared<double>(jobs_dev, njobs, L, 0, st);
-  return launch_prepared<float>(jobs_dev, njobs, L, 0, st);
+  if (dtype == ILM_F64) return launch_prepared<double>(jobs_dev, njobs, L, 0, st, out_base);
+  return launch_prepared<float>(jobs_dev, njobs, L, 0, st, out_base);
 }
 
 int conv_resources(int P1, int P2, int dtype, const void** spec, const void** tw1, const void** tw2, cudaStream_t st) {

@@ -160,16 +160,28 @@ struct ConvJobDev {
   double scale;
   int row_off, col_off;
   int frow_off, frb;   // register-FFT path: first row CTA of this job, rows per CTA
+  // Input box: only rows [ra, rb) and columns [ca, cb) of `in` are read (the
+  // rest of the input is taken as zero and may hold anything).  has_box = 0:
+  // the whole n1 x n2 input.
+  int has_box, ra, rb, ca, cb;
+  int irow_off;        // register-FFT path: first inverse-row CTA of this job
+  // optional field (n1 x n2) added to the result: out = add + scale * conv
+  const void* add;
+  // out_base != nullptr at launch: out = out_base + out_off bytes (lets a
+  // prepared job table write into a caller's buffer)
+  size_t out_off;
 };
 struct ConvLaunch {
   int rows = 0, cols = 0, CW = 1, maxP1 = 0, maxP2 = 0;
-  int fast = 0, frows = 0;             // register four-step FFT path (FP32)
-  size_t fsm_rows = 0, fsm_cols = 0;   // its dynamic shared memory per CTA
+  int fast = 0, frows = 0, firows = 0;  // register four-step FFT path (FP32): forward / inverse row CTAs
+  size_t fsm_rows = 0, fsm_cols = 0, fsm_irows = 0;  // its dynamic shared memory per CTA
 };
 // fill row/col offsets of a job table and the launch geometry
 int conv_jobs_finalize(std::vector<ConvJobDev>& jobs, int dtype, ConvLaunch* L);
-// launch a prepared (device-resident) job table; no host<->device traffic
-int conv_jobs_launch(const ConvJobDev* jobs_dev, int njobs, const ConvLaunch& L, int dtype, cudaStream_t st);
+// launch a prepared (device-resident) job table; no host<->device traffic.
+// out_base: see ConvJobDev::out_off (nullptr: each job's `out`)
+int conv_jobs_launch(const ConvJobDev* jobs_dev, int njobs, const ConvLaunch& L, int dtype, cudaStream_t st,
+                     void* out_base = nullptr);
 // shared spectrum and twiddle tables for padded sizes P1 x P2
 int conv_resources(int P1, int P2, int dtype, const void** spec, const void** tw1, const void** tw2, cudaStream_t st);
 

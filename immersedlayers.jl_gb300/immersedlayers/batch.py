@@ -101,9 +101,8 @@ class BatchSolver:
         return s_out[self.point_offsets[i]:self.point_offsets[i + 1]]
 
 
-STAGES = ["jump/avg", "scatter (layer)", "divergence", "LGF FFT conv (f*)", "gradient", "gather + rhs",
-          "Schur CG (FP64)", "convert", "scatter (correction)", "divergence (corr.)", "LGF FFT conv (corr.)",
-          "f = f* + corr"]
+STAGES = ["jump/avg", "scatter (layer)", "divergence", "LGF FFT conv (f*)", "gather + rhs", "Schur CG (FP64)",
+          "convert", "scatter (correction)", "divergence (corr.)", "LGF FFT conv (corr.) + f*"]
 
 
 def _profiling(self, enable=True):
@@ -119,9 +118,10 @@ def _stage_times(self):
 
 
 def _stats(self):
-    st = (C.c_double * 5)()
+    st = (C.c_double * 6)()
     L.call("ilm_batch_stats", self._h, st)
-    return dict(points=int(st[0]), cells=int(st[1]), sum_npts2=st[2], sum_fft=st[3], nprob=int(st[4]))
+    return dict(points=int(st[0]), cells=int(st[1]), sum_npts2=st[2], sum_fft=st[3], nprob=int(st[4]),
+                box_cells=int(st[5]))
 
 
 def _set_precond(self, mode="none", block_size=64):

@@ -268,9 +268,11 @@ ILM_API int ilm_batch_set_precond(ilm_batch_t b, int mode, int block_size);
 /* Stage timing: when enabled, ilm_batch_solve records a CUDA event on its
  * stream at each stage boundary; ilm_batch_stage_times returns the elapsed
  * ms per stage (up to 31), the number of stages and the number of kernel
- * launches the last solve issued.  ilm_batch_stats returns 5 doubles: total
+ * launches the last solve issued.  ilm_batch_stats returns 6 doubles: total
  * points, total Nodes{Primal} cells, sum of npts^2, sum of padded FFT sizes
- * P1*P2, number of problems.                                                */
+ * P1*P2, number of problems, total cells of the problems' source boxes (the
+ * part of each grid the surface operators can reach, the only cells the
+ * scatters write and the FFT row pass reads).                               */
 ILM_API int ilm_batch_set_profiling(ilm_batch_t b, int enable);
 ILM_API int ilm_batch_stage_times(ilm_batch_t b, float* ms, int* nstages, int* launches);
 ILM_API int ilm_batch_stats(ilm_batch_t b, double* stats);
