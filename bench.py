@@ -200,8 +200,14 @@ def run_ours(args, rank, world, dist):
         raise SystemExit("--precond learned: no trained weights for the batched configuration")
     legs = ["none", "bjacobi"] + (["learned"] if have_learned else [])
     legs = [m for m in legs if m != args.precond] + [args.precond]
+    tuned = {}
     for mode in legs:
         bs.set_precond(mode, args.block)
+        # the batch autotuner picks the Schur CG kernel for this solver (its
+        # solves double as warm-up)
+        with torch.cuda.stream(stream):
+            ch, ms = bs.autotune(fp, fm, f_out, s_out, tol=args.tol, reps=1, stream=stream)
+        tuned[leg_names[mode]] = {"cg_variant": ch, "ms_per_variant": {str(k): round(v, 4) for k, v in ms.items()}}
         with torch.cuda.stream(stream):
             for _ in range(args.warmup):
                 bs.solve(fp, fm, f_out, s_out, tol=args.tol, stream=stream)
@@ -270,7 +276,7 @@ def run_ours(args, rank, world, dist):
                 "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
                 "config": config(args, world), "roofline": roofline, "e2e": e2e, "gpu_launches": launches * args.steps,
-                "clocks": clocks, "setup_s": setup_s, "solvers": solvers, "stencil_gbs": stencil,
+                "clocks": clocks, "setup_s": setup_s, "solvers": solvers, "autotune": tuned, "stencil_gbs": stencil,
                 "heat": heat, "learned": learned, "stokes": stokes,
                 "stages_ms": dict(zip(names, [round(x, 4) for x in stage_ms])),
                 "cg_iterations": {"mean": float(np.mean(its)), "max": int(its.max())},
@@ -281,33 +287,55 @@ def run_ours(args, rank, world, dist):
 
 
 def _stencil_gbs(stream, flush, hbm):
-    """Achieved HBM GB/s of the staggered divergence (Edges -> Nodes, 12 B per
-    cell FP32) and gradient (Nodes -> Edges) stencils on a 2048^2 grid."""
+    """Achieved HBM GB/s (algorithmic bytes / CUDA-event time, L2 flushed
+    before every launch) of the staggered divergence (Edges -> Nodes, 12 B
+    per cell FP32), the gradient (Nodes -> Edges, 12 B per cell) on 2048^2
+    and 4096^2 grids, and of the DDF regularization of the 8192 points of the
+    Stokes configuration onto Nodes{Primal} of its 2048^2 grid (every cell
+    written: 4 B per cell + 16 B per point)."""
     import torch
     import immersedlayers as il
-    g = il.PhysicalGrid(h=0.002, nx=2048)
-    c = il.SurfaceScalarCache(None, g, dtype=torch.float32)
-    q = il.EdgesPrimal.zeros(g, torch.float32)
-    q.data.normal_()
-    w = il.NodesPrimal.zeros(g, torch.float32)
-    out = {}
-    for name, fn, a, b in [("divergence", il.divergence_, w, q), ("grad", il.grad_, q, w)]:
+    from immersedlayers import workloads as W
+
+    def timed(fn):
         for _ in range(3):
-            fn(a, b, c, stream=stream)
-        ms = []
+            fn()
+        ev = []
         with torch.cuda.stream(stream):
             for _ in range(10):
                 flush.fill_(1.0)
                 e0 = torch.cuda.Event(enable_timing=True)
                 e1 = torch.cuda.Event(enable_timing=True)
                 e0.record(stream)
-                fn(a, b, c, stream=stream)
+                fn()
                 e1.record(stream)
-                ms.append((e0, e1))
+                ev.append((e0, e1))
         stream.synchronize()
-        t = statistics.median(x.elapsed_time(y) for x, y in ms) / 1000.0
-        nbytes = (a.data.numel() + b.data.numel()) * 4
-        out[name] = {"gbs": nbytes / t / 1e9, "frac": nbytes / t / 1e9 / hbm, "bytes": nbytes, "ms": 1000 * t}
+        return statistics.median(x.elapsed_time(y) for x, y in ev) / 1000.0
+
+    out = {}
+    for n in (2048, 4096):
+        g = il.PhysicalGrid(h=4.0 / n, nx=n)
+        c = il.SurfaceScalarCache(None, g, dtype=torch.float32)
+        q = il.EdgesPrimal.zeros(g, torch.float32)
+        q.data.normal_()
+        w = il.NodesPrimal.zeros(g, torch.float32)
+        for name, fn, a, b in [("divergence", il.divergence_, w, q), ("grad", il.grad_, q, w)]:
+            t = timed(lambda: fn(a, b, c, stream=stream))
+            nbytes = (a.data.numel() + b.data.numel()) * 4
+            out[f"{name}_{n}"] = {"gbs": nbytes / t / 1e9, "frac": nbytes / t / 1e9 / hbm, "bytes": nbytes,
+                                  "ms": 1000 * t}
+        del c, q, w
+    d = W.stokes_scale(nrhs=1)
+    g = il.PhysicalGrid(h=d["h"], nx=d["n"])
+    c = il.SurfaceScalarCache(d["bodies"], g, dtype=torch.float32)
+    N = len(d["bodies"])
+    f = il.ScalarData(torch.randn(N, device="cuda"))
+    w = il.NodesPrimal.zeros(g, torch.float32)
+    t = timed(lambda: il.regularize_(w, f, c, stream=stream))
+    nbytes = w.data.numel() * 4 + 16 * N
+    out["regularize_2048_8192pts"] = {"gbs": nbytes / t / 1e9, "frac": nbytes / t / 1e9 / hbm, "bytes": nbytes,
+                                      "ms": 1000 * t}
     return out
 
 

@@ -238,6 +238,7 @@ struct ilm_batch_s {
   DevBuf jump, avg, g, s, rhs64, x64;
   DevBuf cgp, iters, relres, order, counter;
   int nclusters = 1;
+  int cg_variant = 0;  // Schur CG kernel (0 auto, 1 row-distributed, 2 replicated vectors)
   // tasks
   DevBuf scatA, divA, gathA, scatB, divB, convA, convB, schurP;
   int n_scatA = 0, n_divA = 0, n_gathA = 0, n_scatB = 0, n_divB = 0;
@@ -267,11 +268,20 @@ struct ilm_batch_s {
   std::vector<double> hx, hy, hnx, hny, hds;
   DevBuf dpoff;  // point offsets on the device (Schur products)
   int profiling = 0;
+  DevBuf cgtime;  // per problem: CG start / end (global timer ns), SM (profiling)
   cudaEvent_t ev[32] = {};
   int nev = 0, launches = 0;
+  // captured solve (ilm_batch_solve_graph): the launch sequence of one
+  // solve for one set of buffers, tolerance and CG parameter generation
+  cudaGraphExec_t gexec = nullptr;
+  const void* gkey[4] = {};
+  double gtol = -1.0;
+  int gmaxiter = -1, ggen = -1;
+  int param_gen = 0;  // bumped whenever the device CG parameters or the CG launch change
   ~ilm_batch_s() {
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
+    if (gexec) cudaGraphExecDestroy(gexec);
   }
 };
 
@@ -327,6 +337,7 @@ int ensure_cg_params(ilm_batch_s* b, double tol, int maxiter) {
                      pre ? b->bj_off.as<int>() + b->bj_first[p] : nullptr, pre ? b->bj_inv.as<float>() : nullptr,
                      pre ? b->bj_inv_lo.as<float>() : nullptr);
     cgff_params_set_deflation(dst, b->defl_gamma[p], b->defl_z.as<double>() + o, b->defl_uz[p]);
+    cgff_params_set_timing(dst, b->profiling ? b->cgtime.as<unsigned long long>() + 3 * (size_t)p : nullptr);
     if (b->precond == 2 && b->has_band[p])
       cgff_params_set_band(dst, b->band.as<float>() + o * P, b->band_k, b->lseg_start.as<int>() + o,
                            b->lseg_len.as<int>() + o);
@@ -334,6 +345,7 @@ int ensure_cg_params(ilm_batch_s* b, double tol, int maxiter) {
   ILM_TRY(up(b->cgp, cg));
   b->cg_tol = tol;
   b->cg_maxiter = maxiter;
+  b->param_gen++;
   return ILM_OK;
 }
 
@@ -349,8 +361,8 @@ __global__ void k_batch_schur_apply(int Ptot, const int* __restrict__ pt2prob, c
   const size_t o = poff[p];
   const int n = (int)(poff[p + 1] - o);
   const int i = row - (int)o;
-  const float* sh = Shi + soff[p] + (size_t)i * n;
-  const float* sl = Slo + soff[p] + (size_t)i * n;
+  const float* sh = Shi + soff[p] + (size_t)i * schur_ld(n);
+  const float* sl = Slo + soff[p] + (size_t)i * schur_ld(n);
   double acc = 0.0;
   for (int j = lane; j < n; j += 32) acc += ((double)sh[j] + (double)sl[j]) * x[o + j];
 #pragma unroll
@@ -421,7 +433,8 @@ int ensure_deflation(ilm_batch_s* b) {
     cgff_params_set_deflation(dst, b->defl_gamma[p], nullptr, 0.0);
   }
   ILM_TRY(up(prm, cg));
-  ILM_TRY(launch_cg_cluster(prm.p, b->order.as<int>(), np, b->counter.as<int>(), b->maxN, b->nclusters, nullptr));
+  ILM_TRY(launch_cg_cluster(prm.p, b->order.as<int>(), np, b->counter.as<int>(), b->maxN, b->nclusters, nullptr,
+                            b->cg_variant));
   std::vector<double> z(Ptot);
   ILM_CHECK_CUDA(cudaMemcpy(z.data(), b->defl_z.p, (size_t)Ptot * sizeof(double), cudaMemcpyDeviceToHost));
   for (int p = 0; p < np; ++p) {
@@ -462,7 +475,7 @@ int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* 
     B->foff[p + 1] = B->foff[p] + (size_t)(P.nx - 1) * (P.ny - 1);
     eoff[p + 1] = eoff[p] + (size_t)P.nx * (P.ny - 1) + (size_t)(P.nx - 1) * P.ny;
     B->poff[p + 1] = B->poff[p] + P.npts;
-    B->soff[p + 1] = B->soff[p] + (size_t)P.npts * P.npts;
+    B->soff[p + 1] = B->soff[p] + (size_t)P.npts * schur_ld(P.npts);
     B->maxN = std::max(B->maxN, P.npts);
     B->max_grid = std::max(B->max_grid, std::max(P.nx, P.ny));
   }
@@ -547,6 +560,9 @@ int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* 
   ILM_TRY(B->x64.alloc((size_t)Ptot * 8));
   ILM_TRY(B->Shi.alloc(std::max<size_t>(B->stot, 1) * 4));
   ILM_TRY(B->Slo.alloc(std::max<size_t>(B->stot, 1) * 4));
+  // the row padding of every matrix stays zero
+  ILM_CHECK_CUDA(cudaMemset(B->Shi.p, 0, std::max<size_t>(B->stot, 1) * 4));
+  ILM_CHECK_CUDA(cudaMemset(B->Slo.p, 0, std::max<size_t>(B->stot, 1) * 4));
   ILM_TRY(B->F.alloc((size_t)Ptot * functional_size()));
   ILM_TRY(B->iters.alloc((size_t)nprob * sizeof(int)));
   ILM_TRY(B->relres.alloc((size_t)nprob * sizeof(double)));
@@ -856,7 +872,8 @@ int ilm_batch_solve(ilm_batch_t b, const void* fplus, const void* fminus, void* 
     b->launches += 2;
     MARK();  // 5: DDF gather (Neumann: with the gradient) + Schur right-hand side
   });
-  ILM_TRY(launch_cg_cluster(b->cgp.p, b->order.as<int>(), b->nprob, b->counter.as<int>(), b->maxN, b->nclusters, st));
+  ILM_TRY(launch_cg_cluster(b->cgp.p, b->order.as<int>(), b->nprob, b->counter.as<int>(), b->maxN, b->nclusters, st,
+                            b->cg_variant));
   b->launches += 1;
   MARK();  // 6: Schur CG
   ILM_TRY(st_convert(Ptot, ILM_F64, b->x64.p, dt, s_out, st));
@@ -941,7 +958,139 @@ int ilm_batch_set_precond(ilm_batch_t b, int mode, int block_size) {
 
 int ilm_batch_set_profiling(ilm_batch_t b, int enable) {
   ILM_REQUIRE(b, "null batch");
-  b->profiling = enable ? 1 : 0;
+  const int e = enable ? 1 : 0;
+  if (e && !b->cgtime.p) {
+    ILM_TRY(b->cgtime.alloc((size_t)b->nprob * 3 * sizeof(unsigned long long)));
+    ILM_CHECK_CUDA(cudaMemset(b->cgtime.p, 0, (size_t)b->nprob * 3 * sizeof(unsigned long long)));
+  }
+  if (e != b->profiling) b->params_dirty = true;
+  b->profiling = e;
+  return ILM_OK;
+}
+
+int ilm_batch_set_cg_variant(ilm_batch_t b, int variant) {
+  ILM_REQUIRE(b, "null batch");
+  ILM_REQUIRE(variant >= 0 && variant <= 3, "batch: unknown CG variant %d", variant);
+  b->cg_variant = variant;
+  b->nclusters = cg_cluster_count(b->nprob, b->maxN, variant);
+  b->param_gen++;
+  return ILM_OK;
+}
+
+// The whole solve as one CUDA graph launch: the first call for a set of
+// buffers / tolerance / CG configuration captures ilm_batch_solve on the
+// stream (every per-problem descriptor already lives in device memory, so
+// the sequence is fixed) and later calls replay it.  The CG parameter table
+// is rebuilt before the capture, outside it.
+int ilm_batch_solve_graph(ilm_batch_t b, const void* fplus, const void* fminus, void* f_out, void* s_out,
+                          double tol, int maxiter, ilm_stream_t stream) {
+  ILM_REQUIRE(b && fplus && fminus && f_out && s_out, "batch_solve_graph: null argument");
+  ILM_REQUIRE(tol > 0 && maxiter > 0, "batch_solve_graph: bad tolerance / iteration limit");
+  cudaStream_t st = as_stream(stream);
+  ILM_REQUIRE(st != nullptr, "batch_solve_graph: needs a created stream (the legacy default stream cannot be captured)");
+  ILM_TRY(ensure_cg_params(b, tol, maxiter));
+  const void* key[4] = {fplus, fminus, f_out, s_out};
+  bool reuse = b->gexec && b->gtol == tol && b->gmaxiter == maxiter && b->ggen == b->param_gen;
+  for (int i = 0; i < 4 && reuse; ++i) reuse = key[i] == b->gkey[i];
+  if (!reuse) {
+    if (b->gexec) {
+      cudaGraphExecDestroy(b->gexec);
+      b->gexec = nullptr;
+    }
+    const int prof = b->profiling;
+    b->profiling = 0;
+    ILM_CHECK_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+    const int rc = ilm_batch_solve(b, fplus, fminus, f_out, s_out, tol, maxiter, stream);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(st, &g);
+    b->profiling = prof;
+    if (rc != ILM_OK || e != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      if (rc != ILM_OK) return rc;
+      set_error("batch_solve_graph: stream capture failed: %s", cudaGetErrorString(e));
+      return ILM_ERR_CUDA;
+    }
+    const cudaError_t ei = cudaGraphInstantiate(&b->gexec, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) {
+      b->gexec = nullptr;
+      set_error("batch_solve_graph: graph instantiation failed: %s", cudaGetErrorString(ei));
+      return ILM_ERR_CUDA;
+    }
+    for (int i = 0; i < 4; ++i) b->gkey[i] = key[i];
+    b->gtol = tol;
+    b->gmaxiter = maxiter;
+    b->ggen = b->param_gen;
+  }
+  ILM_CHECK_CUDA(cudaGraphLaunch(b->gexec, st));
+  return ILM_OK;
+}
+
+int ilm_batch_get_cg_variant(ilm_batch_t b, int* variant, int* nclusters) {
+  ILM_REQUIRE(b && variant && nclusters, "null argument");
+  *variant = b->cg_variant;
+  *nclusters = b->nclusters;
+  return ILM_OK;
+}
+
+// Autotuner: every candidate Schur CG kernel solves the given data once
+// untimed (plans, deflation set-up) and `reps` times timed with CUDA events
+// on the stream; the fastest is kept.  Candidates whose shared-memory layout
+// does not fit are skipped.
+int ilm_batch_autotune(ilm_batch_t b, const void* fplus, const void* fminus, void* f_out, void* s_out, double tol,
+                       int maxiter, int reps, ilm_stream_t stream, int* chosen, float* ms_per_variant) {
+  ILM_REQUIRE(b && reps >= 1, "batch_autotune: bad arguments");
+  cudaStream_t st = as_stream(stream);
+  cudaEvent_t e0, e1;
+  ILM_CHECK_CUDA(cudaEventCreate(&e0));
+  ILM_CHECK_CUDA(cudaEventCreate(&e1));
+  const int old_prof = b->profiling;
+  b->profiling = 0;
+  int best = 0;
+  float best_ms = 0.f;
+  int rc = ILM_OK;
+  for (int v = 1; v <= 3 && rc == ILM_OK; ++v) {
+    if (ms_per_variant) ms_per_variant[v - 1] = -1.f;
+    if (v == 2 && cg_rep_smem(b->maxN) > 200 * 1024) continue;
+    if ((rc = ilm_batch_set_cg_variant(b, v)) != ILM_OK) break;
+    if ((rc = ilm_batch_solve(b, fplus, fminus, f_out, s_out, tol, maxiter, stream)) != ILM_OK) break;
+    if (cudaEventRecord(e0, st) != cudaSuccess) { rc = ILM_ERR_CUDA; break; }
+    for (int k = 0; k < reps && rc == ILM_OK; ++k) rc = ilm_batch_solve(b, fplus, fminus, f_out, s_out, tol, maxiter, stream);
+    if (rc != ILM_OK) break;
+    float ms = 0.f;
+    if (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+        cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+      rc = ILM_ERR_CUDA;
+      break;
+    }
+    ms /= (float)reps;
+    if (ms_per_variant) ms_per_variant[v - 1] = ms;
+    if (best == 0 || ms < best_ms) {
+      best = v;
+      best_ms = ms;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  b->profiling = old_prof;
+  if (rc != ILM_OK) return rc;
+  ILM_TRY(ilm_batch_set_cg_variant(b, best));
+  if (chosen) *chosen = best;
+  return ILM_OK;
+}
+
+int ilm_batch_cg_times(ilm_batch_t b, double* start_us, double* end_us, int* sm) {
+  ILM_REQUIRE(b && start_us && end_us && sm, "null argument");
+  ILM_REQUIRE(b->cgtime.p, "batch: profiling was never enabled");
+  std::vector<unsigned long long> t((size_t)b->nprob * 3);
+  ILM_CHECK_CUDA(cudaMemcpy(t.data(), b->cgtime.p, t.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+  unsigned long long t0 = ~0ull;
+  for (int p = 0; p < b->nprob; ++p) t0 = std::min(t0, t[3 * p]);
+  for (int p = 0; p < b->nprob; ++p) {
+    start_us[p] = 1e-3 * (double)(t[3 * p] - t0);
+    end_us[p] = 1e-3 * (double)(t[3 * p + 1] - t0);
+    sm[p] = (int)t[3 * p + 2];
+  }
   return ILM_OK;
 }
 
@@ -992,6 +1141,7 @@ int ilm_batch_set_learned(ilm_batch_t b, ilm_net_t net, int kind_mask, const int
   ILM_REQUIRE(net_nfeat(net) == 8, "batch_set_learned: the network must read the 8 point features");
   const int K = net_band(net), P = 2 * K + 1;
   ILM_REQUIRE(b->band_k < 0 || b->band_k == K, "batch_set_learned: all networks of a batch must share the band width");
+  ILM_REQUIRE(K >= 0 && K <= 8, "batch_set_learned: band half-width %d (at most 8)", K);
   const int Ptot = b->Ptot;
   std::vector<int> ls(Ptot), ll(Ptot), as(Ptot);
   for (int p = 0; p < b->nprob; ++p) {
@@ -1075,7 +1225,8 @@ int ilm_batch_schur_solve(ilm_batch_t b, const double* rhs, double* x, double to
   cudaStream_t st = as_stream(stream);
   ILM_TRY(ensure_cg_params(b, tol, maxiter));
   ILM_CHECK_CUDA(cudaMemcpyAsync(b->rhs64.p, rhs, (size_t)b->Ptot * 8, cudaMemcpyDeviceToDevice, st));
-  ILM_TRY(launch_cg_cluster(b->cgp.p, b->order.as<int>(), b->nprob, b->counter.as<int>(), b->maxN, b->nclusters, st));
+  ILM_TRY(launch_cg_cluster(b->cgp.p, b->order.as<int>(), b->nprob, b->counter.as<int>(), b->maxN, b->nclusters, st,
+                            b->cg_variant));
   ILM_CHECK_CUDA(cudaMemcpyAsync(x, b->x64.p, (size_t)b->Ptot * 8, cudaMemcpyDeviceToDevice, st));
   return ILM_OK;
 }

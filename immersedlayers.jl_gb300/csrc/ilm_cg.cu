@@ -50,6 +50,18 @@ __device__ __forceinline__ void ff_fma(FF& acc, float s_hi, float s_lo, float p_
   acc.lo += e + t;
 }
 
+// a / b to ~2^-46 relative: an FP32 reciprocal and one FP64 correction.
+// GB300 issues FP64 at a small fraction of its FP32 rate and the divide is a
+// long FP64 sequence; every thread of a CTA evaluates the CG scalars, so the
+// full-precision divide cost more than the rest of an iteration.
+__device__ __forceinline__ double fdiv(double a, double b) {
+  const double ab = fabs(b);
+  if (!(ab > 1e-30 && ab < 1e30)) return a / b;
+  const double r = (double)(1.0f / (float)b);
+  const double q = a * r;
+  return fma(fma(-q, b, a), r, q);
+}
+
 __device__ __forceinline__ FF ff_add(FF a, FF b) {
   float s, e;
   two_sum(a.hi, b.hi, s, e);
@@ -59,93 +71,36 @@ __device__ __forceinline__ FF ff_add(FF a, FF b) {
   return r;
 }
 
-// y[i - r0] = sum_j S[i][j] v[j] for rows i in [r0, r1); one warp per row,
-// lanes stride the columns (coalesced row-major reads) with four independent
-// accumulators so that eight loads per lane are in flight.
-__device__ void ff_gemv_rows(const float* __restrict__ Shi, const float* __restrict__ Slo, int n, int r0, int r1,
-                             const float* __restrict__ vhi, const float* __restrict__ vlo, double* __restrict__ y) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int i = r0 + warp; i < r1; i += CGC_WARPS) {
-    const float* __restrict__ rh = Shi + (size_t)i * n;
-    const float* __restrict__ rl = Slo + (size_t)i * n;
-    FF a0{0.f, 0.f}, a1{0.f, 0.f}, a2{0.f, 0.f}, a3{0.f, 0.f};
-    int j = lane;
-    for (; j + 96 < n; j += 128) {
-      const float h0 = __ldg(rh + j), h1 = __ldg(rh + j + 32), h2 = __ldg(rh + j + 64), h3 = __ldg(rh + j + 96);
-      const float l0 = __ldg(rl + j), l1 = __ldg(rl + j + 32), l2 = __ldg(rl + j + 64), l3 = __ldg(rl + j + 96);
-      ff_fma(a0, h0, l0, vhi[j], vlo[j]);
-      ff_fma(a1, h1, l1, vhi[j + 32], vlo[j + 32]);
-      ff_fma(a2, h2, l2, vhi[j + 64], vlo[j + 64]);
-      ff_fma(a3, h3, l3, vhi[j + 96], vlo[j + 96]);
+// Block-wide sums of two doubles in fixed order; result valid in all
+// threads.  `red` holds 2 * blockDim + 2 doubles.  The per-thread partials go
+// through shared memory and only warp 0 adds them: GB300 issues FP64 at a
+// small fraction of its FP32 rate, and an add tree in every warp followed by
+// every thread summing the warp totals cost more FP64 issue slots than the
+// whole CG iteration's vector arithmetic.
+__device__ void block_sum2(double& a, double& b, double* red) {
+  const int nt = blockDim.x, t = threadIdx.x;
+  red[t] = a;
+  red[nt + t] = b;
+  __syncthreads();
+  if (t < 32) {
+    double sa = 0.0, sb = 0.0;
+    for (int i = t; i < nt; i += 32) {
+      sa += red[i];
+      sb += red[nt + i];
     }
-    for (; j < n; j += 32) ff_fma(a0, __ldg(rh + j), __ldg(rl + j), vhi[j], vlo[j]);
-    FF acc = ff_add(ff_add(a0, a1), ff_add(a2, a3));
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-      FF other;
-      other.hi = __shfl_down_sync(0xffffffffu, acc.hi, o);
-      other.lo = __shfl_down_sync(0xffffffffu, acc.lo, o);
-      acc = ff_add(acc, other);
-    }
-    if (lane == 0) y[i - r0] = (double)acc.hi + (double)acc.lo;
-  }
-}
-
-// block-wide sums of two doubles in fixed order; result valid in all threads
-__device__ void block_sum2(double& a, double& b, double* red) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    a += __shfl_down_sync(0xffffffffu, a, o);
-    b += __shfl_down_sync(0xffffffffu, b, o);
-  }
-  __syncthreads();
-  if (lane == 0) {
-    red[wid] = a;
-    red[CGC_WARPS + wid] = b;
-  }
-  __syncthreads();
-  double sa = 0.0, sb = 0.0;
-  for (int w = 0; w < CGC_WARPS; ++w) {
-    sa += red[w];
-    sb += red[CGC_WARPS + w];
-  }
-  a = sa;
-  b = sb;
-  __syncthreads();
-}
-
-// publish two partials of this CTA in slot `slot`, cluster barrier, and sum
-// every CTA's partials in rank order (identical result in all CTAs)
-// Only warp 0 touches remote shared memory (lane c reads CTA c's partials);
-// the fixed shuffle tree makes the sum bit-identical in every CTA.
-__device__ void cluster_sum2(cg::cluster_group& cl, double* pub, double* bcast, int slot, double& a, double& b) {
-  if (threadIdx.x == 0) {
-    pub[2 * slot] = a;
-    pub[2 * slot + 1] = b;
-  }
-  cl.sync();
-  if (threadIdx.x < 32) {
-    const int lane = threadIdx.x;
-    double sa = 0.0, sb = 0.0;
-    if (lane < CG_CLUSTER) {
-      const double* rp = cl.map_shared_rank(pub, lane);
-      sa = rp[2 * slot];
-      sb = rp[2 * slot + 1];
-    }
-#pragma unroll
-    for (int o = CG_CLUSTER / 2; o > 0; o >>= 1) {
       sa += __shfl_down_sync(0xffffffffu, sa, o);
       sb += __shfl_down_sync(0xffffffffu, sb, o);
     }
-    if (lane == 0) {
-      bcast[0] = sa;
-      bcast[1] = sb;
+    if (t == 0) {
+      red[2 * nt] = sa;
+      red[2 * nt + 1] = sb;
     }
   }
   __syncthreads();
-  a = bcast[0];
-  b = bcast[1];
+  a = red[2 * nt];
+  b = red[2 * nt + 1];
   __syncthreads();
 }
 
@@ -187,7 +142,21 @@ struct CGFFParams {
   double gamma;
   const double* zdef;
   double uz;
+  // optional: global-timer stamps (ns) when the problem is taken and done,
+  // and the SM of the cluster's first CTA (profiling)
+  unsigned long long* tspan;
 };
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ unsigned sm_id() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%smid;" : "=r"(r));
+  return r;
+}
 
 // y[i - r0] = (S v)_i for a CSR matrix (float-float values), one warp per row
 __device__ void ff_spmv_rows(const CGFFParams& pr, int r0, int r1, const float* __restrict__ vhi,
@@ -218,12 +187,6 @@ __device__ void ff_spmv_rows(const CGFFParams& pr, int r0, int r1, const float* 
   }
 }
 
-__device__ __forceinline__ void matvec_rows(const CGFFParams& pr, int n, int r0, int r1, const float* vhi,
-                                            const float* vlo, double* y) {
-  if (pr.rowptr) ff_spmv_rows(pr, r0, r1, vhi, vlo, y);
-  else ff_gemv_rows(pr.Shi, pr.Slo, n, r0, r1, vhi, vlo, y);
-}
-
 // z[i - r0] = (M r)_i for rows i in [r0, r1): float-float block-Jacobi (the
 // diagonal blocks of the Dirichlet Schur complement are indefinite with
 // condition numbers up to ~1e6, so an FP32 application loses most of the gain)
@@ -248,22 +211,6 @@ __device__ void apply_bjacobi(const CGFFParams& pr, int r0, int r1, const float*
   }
 }
 
-// sum_j w_j v_j over the whole problem from the split vector in shared
-// memory; every CTA computes the same value (fixed order)
-__device__ double full_wdot(const CGFFParams& pr, int n, const float* vhi, const float* vlo, double* red) {
-  double a = 0.0, unused = 0.0;
-  for (int j = threadIdx.x; j < n; j += blockDim.x) a += __ldg(pr.w + j) * ((double)vhi[j] + (double)vlo[j]);
-  block_sum2(a, unused, red);
-  return a;
-}
-
-__device__ double full_wdot_d(const CGFFParams& pr, int n, const double* v, double* red) {
-  double a = 0.0, unused = 0.0;
-  for (int j = threadIdx.x; j < n; j += blockDim.x) a += __ldg(pr.w + j) * v[j];
-  block_sum2(a, unused, red);
-  return a;
-}
-
 __device__ __forceinline__ int seg_nb(int j, int s, int L, int t) {
   if (L < 1) return j;
   int q = (j - s + t) % L;
@@ -271,330 +218,1054 @@ __device__ __forceinline__ int seg_nb(int j, int s, int L, int t) {
   return s + q;
 }
 
-// z[i - r0] = (W^-1 C^T C r)_i for rows i in [r0, r1), in float-float
-// arithmetic (an FP32 application changes M from one iteration to the next
-// by rounding and stalls flexible CG near 1e-7 on these indefinite Schur
-// complements).  Each row needs u_j = (C r)_j at its 2K+1 band neighbours
-// j; they are formed on the fly (same body, circular), two threads per row.
-__device__ void apply_band(const CGFFParams& pr, int r0, int r1, const float* __restrict__ rhi,
-                           const float* __restrict__ rlo, const double* __restrict__ ws, double* __restrict__ z) {
-  const int K = pr.band_k, P = 2 * K + 1;
-  const int half = threadIdx.x & 1;
-  const int nrow = r1 - r0;
-  for (int base = 0; base < nrow; base += blockDim.x / 2) {
-    const int row = base + (threadIdx.x >> 1);
-    FF zacc{0.f, 0.f};
-    if (row < nrow) {
-      const int i = r0 + row;
-      const int s = __ldg(pr.seg_start + i), L = __ldg(pr.seg_len + i);
-      // thread `half` takes t = -K + half, -K + half + 2, ...
-      for (int t = -K + half; t <= K; t += 2) {
-        const int j = seg_nb(i, s, L, -t);
-        const float* __restrict__ cj = pr.band + (size_t)j * P;
-        FF u{0.f, 0.f};
-        for (int t2 = -K; t2 <= K; ++t2) {
-          const int q = seg_nb(j, s, L, t2);
-          ff_fma(u, __ldg(cj + t2 + K), 0.f, rhi[q], rlo[q]);
-        }
-        ff_fma(zacc, __ldg(cj + t + K), 0.f, u.hi, u.lo);
-      }
+// ---------------------------------------------------------------------------
+// Replicated-vector cluster CG (systems of up to a few thousand unknowns).
+//
+// Every CTA of the cluster keeps the whole of x, r, p, z and W in shared
+// memory and runs the vector updates, the dot products and the
+// preconditioner redundantly: the same data and the same fixed reduction
+// order keep the CTAs' copies bit-identical, so they take the same branches.
+// Only the matrix-vector product is split by rows: each CTA writes its rows
+// into its own full-length exchange buffer, one cluster barrier publishes
+// them, and every CTA copies the other CTAs' rows out of their buffers
+// through distributed shared memory.  That is one cluster barrier per
+// iteration (two when the true residual is refreshed), where the
+// row-distributed kernel above needs three barriers and two vector gathers.
+// The two exchange buffers alternate, so a CTA never overwrites rows another
+// CTA may still be reading: between two uses of one buffer lies the barrier
+// of an exchange through the other.
+// ---------------------------------------------------------------------------
+constexpr int CGR_THREADS = 256;
+constexpr int CGR_WARPS = CGR_THREADS / 32;
+
+__device__ __forceinline__ void ff_fma4(FF& acc, float4 h, float4 l, float4 ph, float4 pl) {
+  ff_fma(acc, h.x, l.x, ph.x, pl.x);
+  ff_fma(acc, h.y, l.y, ph.y, pl.y);
+  ff_fma(acc, h.z, l.z, ph.z, pl.z);
+  ff_fma(acc, h.w, l.w, ph.w, pl.w);
+}
+
+// y[i] = (S v)_i for rows i in [r0, r1) of a dense float-float matrix whose
+// rows start on 16-byte boundaries (stride schur_ld(n), zero padding; v
+// zero-padded to the same length): one warp per two rows, 16-byte loads of
+// four consecutive columns.
+__device__ void ff_gemv_rows_v4(const float* __restrict__ Shi, const float* __restrict__ Slo, int n, int r0, int r1,
+                                const float* __restrict__ vhi, const float* __restrict__ vlo, double* __restrict__ y) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int ld = schur_ld(n), nq = ld >> 2;
+  const float4* vh4 = reinterpret_cast<const float4*>(vhi);
+  const float4* vl4 = reinterpret_cast<const float4*>(vlo);
+  for (int i = r0 + 2 * warp; i < r1; i += 2 * CGR_WARPS) {
+    const bool two = i + 1 < r1;
+    const float4* h0 = reinterpret_cast<const float4*>(Shi + (size_t)i * ld);
+    const float4* l0 = reinterpret_cast<const float4*>(Slo + (size_t)i * ld);
+    const float4* h1 = reinterpret_cast<const float4*>(Shi + (size_t)(two ? i + 1 : i) * ld);
+    const float4* l1 = reinterpret_cast<const float4*>(Slo + (size_t)(two ? i + 1 : i) * ld);
+    FF a{0.f, 0.f}, b{0.f, 0.f};
+    for (int j = lane; j < nq; j += 32) {
+      const float4 x0 = __ldg(h0 + j), y0 = __ldg(l0 + j), x1 = __ldg(h1 + j), y1 = __ldg(l1 + j);
+      const float4 ph = vh4[j], pl = vl4[j];
+      ff_fma4(a, x0, y0, ph, pl);
+      ff_fma4(b, x1, y1, ph, pl);
     }
-    FF other;
-    other.hi = __shfl_xor_sync(0xffffffffu, zacc.hi, 1);
-    other.lo = __shfl_xor_sync(0xffffffffu, zacc.lo, 1);
-    zacc = ff_add(zacc, other);
-    if (row < nrow && half == 0) z[row] = ((double)zacc.hi + (double)zacc.lo) / ws[row];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      FF oa, ob;
+      oa.hi = __shfl_down_sync(0xffffffffu, a.hi, o);
+      oa.lo = __shfl_down_sync(0xffffffffu, a.lo, o);
+      ob.hi = __shfl_down_sync(0xffffffffu, b.hi, o);
+      ob.lo = __shfl_down_sync(0xffffffffu, b.lo, o);
+      a = ff_add(a, oa);
+      b = ff_add(b, ob);
+    }
+    if (lane == 0) {
+      y[i] = (double)a.hi + (double)a.lo;
+      if (two) y[i + 1] = (double)b.hi + (double)b.lo;
+    }
   }
 }
 
-__device__ __forceinline__ void apply_precond(const CGFFParams& pr, int r0, int r1, const float* rhi,
-                                              const float* rlo, const double* ws, double* z) {
-  if (pr.band) apply_band(pr, r0, r1, rhi, rlo, ws, z);
-  else apply_bjacobi(pr, r0, r1, rhi, rlo, z);
+// rows [r0, r1) of S v into y (full-length indexing)
+__device__ __forceinline__ void matvec_rows_full(const CGFFParams& pr, int n, int r0, int r1, const float* vhi,
+                                                 const float* vlo, double* y) {
+  if (pr.rowptr) ff_spmv_rows(pr, r0, r1, vhi, vlo, y + r0);
+  else ff_gemv_rows_v4(pr.Shi, pr.Slo, n, r0, r1, vhi, vlo, y);
 }
 
-// Persistent: each cluster takes problems from a work queue (largest first,
-// `order`) until the queue is empty.  `counter` must be 0 at launch.
-__global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(CGC_THREADS, 4)
-    k_cg_cluster(const CGFFParams* __restrict__ P, const int* __restrict__ order, int nprob, int* counter,
-                 int max_n) {
+// neighbour of point j at band offset t within its body [s, s + L) (circular)
+__device__ __forceinline__ int seg_nb_near(int j, int s, int L, int t) {
+  if (L < 1) return j;
+  int q = j + t;
+  if (q < s) q += L;
+  else if (q >= s + L) q -= L;
+  if (q < s || q >= s + L) return seg_nb(j, s, L, t);  // body shorter than the band
+  return q;
+}
+
+// z = W^-1 C^T C r over all n points (float-float): u = C r for every point
+// first (one thread per point), then z from u, so every thread has work and
+// each product is formed once
+__device__ void apply_band_full(const CGFFParams& pr, int n, const float* __restrict__ rhi,
+                                const float* __restrict__ rlo, float* __restrict__ uhi, float* __restrict__ ulo,
+                                const double* __restrict__ w, double* __restrict__ z) {
+  const int K = pr.band_k, P = 2 * K + 1;
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    const int s = __ldg(pr.seg_start + j), L = __ldg(pr.seg_len + j);
+    const float* __restrict__ cj = pr.band + (size_t)j * P;
+    FF u{0.f, 0.f};
+    for (int t2 = -K; t2 <= K; ++t2) {
+      const int q = seg_nb_near(j, s, L, t2);
+      ff_fma(u, __ldg(cj + t2 + K), 0.f, rhi[q], rlo[q]);
+    }
+    uhi[j] = u.hi;
+    ulo[j] = u.lo;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const int s = __ldg(pr.seg_start + i), L = __ldg(pr.seg_len + i);
+    FF acc{0.f, 0.f};
+    for (int t = -K; t <= K; ++t) {
+      const int j = seg_nb_near(i, s, L, -t);
+      ff_fma(acc, __ldg(pr.band + (size_t)j * P + t + K), 0.f, uhi[j], ulo[j]);
+    }
+    z[i] = fdiv((double)acc.hi + (double)acc.lo, w[i]);
+  }
+}
+
+struct CGRShared {
+  double* red;
+  double* work;
+  double *x, *r, *p, *z, *w, *xb[2];
+  float *vhi, *vlo, *uhi, *ulo;
+};
+
+__device__ __forceinline__ void split_full(const double* v, int n, int ld, float* vhi, float* vlo) {
+  for (int j = threadIdx.x; j < ld; j += blockDim.x) {
+    const double a = j < n ? v[j] : 0.0;
+    const float h = (float)a;
+    vhi[j] = h;
+    vlo[j] = (float)(a - (double)h);
+  }
+}
+
+// sum_j w_j a_j b_j and sum_j w2_j c_j d_j over the whole vectors (fixed order)
+__device__ __forceinline__ double wsum(const double* w, const double* a, const double* b, int n, double* red) {
+  double s = 0.0, unused = 0.0;
+  for (int j = threadIdx.x; j < n; j += blockDim.x) s += w[j] * a[j] * b[j];
+  block_sum2(s, unused, red);
+  return s;
+}
+
+// y = S v (full vector in every CTA): rows [r0, r1) here, the rest from the
+// other CTAs' exchange buffers after one cluster barrier.  v must be split
+// into vhi / vlo (zero-padded) and visible to the whole CTA.
+__device__ __forceinline__ double* exchange_matvec(cg::cluster_group& cl, const CGFFParams& pr, const CGRShared& S, int& xsel, int n,
+                                   int rows, int rank, int r0, int r1) {
+  double* buf = S.xb[xsel];
+  xsel ^= 1;
+  matvec_rows_full(pr, n, r0, r1, S.vhi, S.vlo, buf);
+  cl.sync();
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    const int c = j / rows;
+    if (c != rank) buf[j] = cl.map_shared_rank(buf, c)[j];
+  }
+  __syncthreads();
+  return buf;
+}
+
+__device__ __forceinline__ void apply_precond_full(const CGFFParams& pr, int n, const CGRShared& S, double* z) {
+  if (pr.band) apply_band_full(pr, n, S.vhi, S.vlo, S.uhi, S.ulo, S.w, z);
+  else apply_bjacobi(pr, 0, n, S.vhi, S.vlo, z);
+}
+
+__global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(CGR_THREADS, 3)
+    k_cg_rep(const CGFFParams* __restrict__ P, const int* __restrict__ order, int nprob, int* counter, int max_n) {
   cg::cluster_group cl = cg::this_cluster();
   const int rank = (int)cl.block_rank();
-  const int rmax = (max_n + CG_CLUSTER - 1) / CG_CLUSTER;
+  const int ldm = schur_ld(max_n);
   extern __shared__ __align__(16) unsigned char smraw[];
-  double* pub = reinterpret_cast<double*>(smraw);   // 16 doubles: published partials (8 slots x 2)
-  double* red = pub + 16;                           // 2 * warps
-  double* work = red + 2 * CGC_WARPS;               // [0] queue index taken by rank 0, [2..3] broadcast
-  double* xs = work + 4;                            // slices (rmax each)
-  double* rs = xs + rmax;
-  double* qs = rs + rmax;
-  double* ws = qs + rmax;
-  double* bs = ws + rmax;
-  double* ts = bs + rmax;                           // S x of the residual refresh (q stays S p)
-  double* xb = ts + rmax;                           // best iterate so far (true residual)
-  double* pf = xb + rmax;                           // full direction (max_n)
-  double* zs = pf + max_n;                          // preconditioned residual slice (rmax)
-  float* vhi = reinterpret_cast<float*>(zs + max_n); // split vector (max_n each)
-  float* vlo = vhi + max_n;
-  int slot = 1;
+  CGRShared S;
+  S.red = reinterpret_cast<double*>(smraw);  // 2 * threads + 2
+  S.work = S.red + 2 * CGR_THREADS + 2;       // 4: [0] queue index taken by rank 0
+  S.x = S.work + 4;
+  S.r = S.x + ldm;
+  S.p = S.r + ldm;
+  S.z = S.p + ldm;
+  S.w = S.z + ldm;
+  S.xb[0] = S.w + ldm;
+  S.xb[1] = S.xb[0] + ldm;
+  S.vhi = reinterpret_cast<float*>(S.xb[1] + ldm);
+  S.vlo = S.vhi + ldm;
+  S.uhi = S.vlo + ldm;
+  S.ulo = S.uhi + ldm;
+  double* x = S.x;
+  double* r = S.r;
+  double* p = S.p;
+  double* z = S.z;
+  double* w = S.w;
+  double* red = S.red;
+  int xsel = 0;
   while (true) {
-    if (rank == 0 && threadIdx.x == 0) work[0] = (double)atomicAdd(counter, 1);
+    if (rank == 0 && threadIdx.x == 0) S.work[0] = (double)atomicAdd(counter, 1);
     cl.sync();
-    const int q = (int)cl.map_shared_rank(work, 0)[0];
+    const int q = (int)cl.map_shared_rank(S.work, 0)[0];
     if (q >= nprob) break;
-    const CGFFParams& pr = P[order[q]];  // fields read through L1 as needed (a copy spills)
-    const int n = pr.n;
+    const CGFFParams& pr = P[order[q]];
+    if (pr.tspan && rank == 0 && threadIdx.x == 0) {
+      pr.tspan[0] = global_ns();
+      pr.tspan[2] = sm_id();
+    }
+    const int n = pr.n, ld = schur_ld(n);
     const int rows = (n + CG_CLUSTER - 1) / CG_CLUSTER;
     const int r0 = min(n, rank * rows), r1 = min(n, r0 + rows);
-    const int nr = r1 - r0;
-    for (int i = threadIdx.x; i < nr; i += blockDim.x) {
-      xs[i] = pr.x0 ? pr.x0[r0 + i] : 0.0;
-      bs[i] = pr.b[r0 + i];
-      ws[i] = pr.w ? pr.w[r0 + i] : 1.0;
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+      x[j] = pr.x0 ? pr.x0[j] : 0.0;
+      w[j] = pr.w ? pr.w[j] : 1.0;
     }
-    if (pr.x0) {  // warm start: r = b - S x0
-      for (int j = threadIdx.x; j < n; j += blockDim.x) {
-        const double v = pr.x0[j];
-        const float h = (float)v;
-        vhi[j] = h;
-        vlo[j] = (float)(v - (double)h);
+    __syncthreads();
+    if (pr.x0) {  // warm start: r = b - S' x0
+      split_full(x, n, ld, S.vhi, S.vlo);
+      __syncthreads();
+      const double* t = exchange_matvec(cl, pr, S, xsel, n, rows, rank, r0, r1);
+      double c0 = 0.0;
+      if (pr.gamma != 0.0) {
+        double unused = 0.0;
+        for (int j = threadIdx.x; j < n; j += blockDim.x) c0 += w[j] * x[j];
+        block_sum2(c0, unused, red);
+        c0 *= pr.gamma;
       }
-      __syncthreads();
-      matvec_rows(pr, n, r0, r1, vhi, vlo, qs);
-      const double c0 = pr.gamma != 0.0 ? pr.gamma * full_wdot(pr, n, vhi, vlo, red) : 0.0;
-      __syncthreads();
-      for (int i = threadIdx.x; i < nr; i += blockDim.x) rs[i] = bs[i] - qs[i] - c0;
+      for (int j = threadIdx.x; j < n; j += blockDim.x) r[j] = pr.b[j] - t[j] - c0;
     } else {
-      for (int i = threadIdx.x; i < nr; i += blockDim.x) rs[i] = bs[i];
+      for (int j = threadIdx.x; j < n; j += blockDim.x) r[j] = pr.b[j];
     }
     __syncthreads();
     const bool pre = pr.blk != nullptr || pr.band != nullptr;
     double bb = 0.0, rz = 0.0;
-    for (int i = threadIdx.x; i < nr; i += blockDim.x) {
-      bb += bs[i] * bs[i];
-      rz += ws[i] * rs[i] * rs[i];
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+      const double bj = pr.b[j];
+      bb += bj * bj;
+      rz += w[j] * r[j] * r[j];
     }
     block_sum2(bb, rz, red);
-    cluster_sum2(cl, pub, work + 2, slot, bb, rz);
-    slot = slot == 7 ? 1 : slot + 1;
-    // p = r (gathered from every CTA's final slice)
-    for (int j = threadIdx.x; j < n; j += blockDim.x) {
-      const int c = j / rows;
-      const double v = cl.map_shared_rank(rs, c)[j - c * rows];
-      pf[j] = v;
-      const float h = (float)v;
-      vhi[j] = h;
-      vlo[j] = (float)(v - (double)h);
-    }
-    __syncthreads();
     if (pre) {
-      apply_precond(pr, r0, r1, vhi, vlo, ws, zs);
+      split_full(r, n, ld, S.vhi, S.vlo);
       __syncthreads();
-      cl.sync();
-    }
-    if (pre) {  // p = z = M r, gathered from every CTA's (final) z slice
-      for (int j = threadIdx.x; j < n; j += blockDim.x) {
-        const int c = j / rows;
-        pf[j] = cl.map_shared_rank(zs, c)[j - c * rows];
-      }
+      apply_precond_full(pr, n, S, z);
       __syncthreads();
     }
+    for (int j = threadIdx.x; j < n; j += blockDim.x) p[j] = pre ? z[j] : r[j];
     const double bnorm = sqrt(bb);
     const double thr = pr.tol * bnorm;
+    const double thr2 = thr * thr;
+    double rlast = bb;  // latest squared residual norm (recursive or true)
     int it = 0;
     double relres = bnorm > 0 ? 1.0 : 0.0;
     bool done = bnorm == 0.0;
-    // stagnation guard: past the attainable accuracy (float-float products on
-    // a Schur complement of condition ~1e6 floor near 1e-10) CG drifts and
-    // eventually diverges; stop after 8 refreshes without a better true
-    // residual and return the best iterate
+    // stagnation guard (as in k_cg_cluster): the best true-residual iterate
+    // is kept in pr.x (each CTA its rows)
     double best = 1e300;
     int stall = 0;
-    for (int i = threadIdx.x; i < nr; i += blockDim.x) xb[i] = xs[i];
+    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) pr.x[i] = x[i];
+    __syncthreads();
     while (!done && it < pr.maxiter) {
-      for (int j = threadIdx.x; j < n; j += blockDim.x) {
-        const double v = pf[j];
-        const float h = (float)v;
-        vhi[j] = h;
-        vlo[j] = (float)(v - (double)h);
-      }
+      split_full(p, n, ld, S.vhi, S.vlo);
       __syncthreads();
-      matvec_rows(pr, n, r0, r1, vhi, vlo, qs);
+      double* qv = exchange_matvec(cl, pr, S, xsel, n, rows, rank, r0, r1);
       if (pr.gamma != 0.0) {  // q = S' p
-        const double cp = pr.gamma * full_wdot_d(pr, n, pf, red);
-        for (int i = threadIdx.x; i < nr; i += blockDim.x) qs[i] += cp;
+        double cp = 0.0, unused = 0.0;
+        for (int j = threadIdx.x; j < n; j += blockDim.x) cp += w[j] * p[j];
+        block_sum2(cp, unused, red);
+        cp *= pr.gamma;
+        for (int j = threadIdx.x; j < n; j += blockDim.x) qv[j] += cp;
+        __syncthreads();
       }
-      __syncthreads();
       double pq = 0.0, pr_ = 0.0;
-      for (int i = threadIdx.x; i < nr; i += blockDim.x) {
-        pq += ws[i] * pf[r0 + i] * qs[i];
-        pr_ += ws[i] * pf[r0 + i] * rs[i];
+      for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        pq += w[j] * p[j] * qv[j];
+        pr_ += w[j] * p[j] * r[j];
       }
       block_sum2(pq, pr_, red);
-      cluster_sum2(cl, pub, work + 2, slot, pq, pr_);
-      slot = slot == 7 ? 1 : slot + 1;
       if (pq == 0.0) break;
-      const double alpha = pre ? pr_ / pq : rz / pq;
+      const double alpha = fdiv(pre ? pr_ : rz, pq);
       double rr = 0.0, rzn = 0.0;
-      for (int i = threadIdx.x; i < nr; i += blockDim.x) {
-        xs[i] += alpha * pf[r0 + i];
-        rs[i] -= alpha * qs[i];
-        rr += rs[i] * rs[i];
-        rzn += ws[i] * rs[i] * rs[i];
+      for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        x[j] += alpha * p[j];
+        const double rj = r[j] - alpha * qv[j];
+        r[j] = rj;
+        rr += rj * rj;
+        rzn += w[j] * rj * rj;
       }
       block_sum2(rr, rzn, red);
-      cluster_sum2(cl, pub, work + 2, slot,rr, rzn);
-      slot = slot == 7 ? 1 : slot + 1;
       ++it;
-      relres = bnorm > 0 ? sqrt(rr) / bnorm : 0.0;
-      if (sqrt(rr) <= thr || (it % 50) == 0 || it == pr.maxiter) {
-        // true residual b - S x from every CTA's (final) x slice
-        for (int j = threadIdx.x; j < n; j += blockDim.x) {
-          const int c = j / rows;
-          const double v = cl.map_shared_rank(xs, c)[j - c * rows];
-          const float h = (float)v;
-          vhi[j] = h;
-          vlo[j] = (float)(v - (double)h);
+      rlast = rr;
+      if (rr <= thr2 || (it % 50) == 0 || it == pr.maxiter) {
+        // true residual b - S' x (exchange through the other buffer: q = S p stays)
+        split_full(x, n, ld, S.vhi, S.vlo);
+        __syncthreads();
+        const double* t = exchange_matvec(cl, pr, S, xsel, n, rows, rank, r0, r1);
+        double cx = 0.0;
+        if (pr.gamma != 0.0) {
+          double unused = 0.0;
+          for (int j = threadIdx.x; j < n; j += blockDim.x) cx += w[j] * x[j];
+          block_sum2(cx, unused, red);
+          cx *= pr.gamma;
         }
-        __syncthreads();
-        matvec_rows(pr, n, r0, r1, vhi, vlo, ts);
-        const double cx = pr.gamma != 0.0 ? pr.gamma * full_wdot(pr, n, vhi, vlo, red) : 0.0;
-        __syncthreads();
         double tr = 0.0, tz = 0.0;
-        for (int i = threadIdx.x; i < nr; i += blockDim.x) {
-          rs[i] = bs[i] - ts[i] - cx;
-          tr += rs[i] * rs[i];
-          tz += ws[i] * rs[i] * rs[i];
+        for (int j = threadIdx.x; j < n; j += blockDim.x) {
+          const double rj = pr.b[j] - t[j] - cx;
+          r[j] = rj;
+          tr += rj * rj;
+          tz += w[j] * rj * rj;
         }
         block_sum2(tr, tz, red);
-        cluster_sum2(cl, pub, work + 2, slot,tr, tz);
-        slot = slot == 7 ? 1 : slot + 1;
         relres = bnorm > 0 ? sqrt(tr) / bnorm : 0.0;
+        rlast = tr;
         rzn = tz;
-        if (sqrt(tr) <= thr) {
+        if (tr <= thr2) {
           done = true;
           break;
         }
         if (relres < best) {
           best = relres;
           stall = 0;
-          for (int i = threadIdx.x; i < nr; i += blockDim.x) xb[i] = xs[i];
+          for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) pr.x[i] = x[i];
         } else if (++stall >= 8) {
           break;
         }
       }
       if (!pre) {
-        const double beta = rzn / rz;
+        const double beta = fdiv(rzn, rz);
         rz = rzn;
-        // p = r + beta p over the full vector, r gathered from every CTA's
-        // (final) slice: identical in all CTAs, no extra barrier
-        for (int j = threadIdx.x; j < n; j += blockDim.x) {
-          const int c = j / rows;
-          pf[j] = cl.map_shared_rank(rs, c)[j - c * rows] + beta * pf[j];
-        }
+        for (int j = threadIdx.x; j < n; j += blockDim.x) p[j] = r[j] + beta * p[j];
         __syncthreads();
       } else {
-        // flexible CG: z = M r on this CTA's rows (r gathered from every
-        // CTA's final slice), beta = -(z, q) / (p, q), p = z + beta p
-        for (int j = threadIdx.x; j < n; j += blockDim.x) {
-          const int c = j / rows;
-          const double v = cl.map_shared_rank(rs, c)[j - c * rows];
-          const float h = (float)v;
-          vhi[j] = h;
-          vlo[j] = (float)(v - (double)h);
-        }
+        // flexible CG: z = M r, beta = -(z, q) / (p, q), p = z + beta p
+        split_full(r, n, ld, S.vhi, S.vlo);
         __syncthreads();
-        apply_precond(pr, r0, r1, vhi, vlo, ws, zs);
+        apply_precond_full(pr, n, S, z);
         __syncthreads();
-        double zq = 0.0, d1 = 0.0;
-        for (int i = threadIdx.x; i < nr; i += blockDim.x) zq += ws[i] * zs[i] * qs[i];
-        block_sum2(zq, d1, red);
-        cluster_sum2(cl, pub, work + 2, slot, zq, d1);
-        slot = slot == 7 ? 1 : slot + 1;
-        const double beta = -zq / pq;
-        for (int j = threadIdx.x; j < n; j += blockDim.x) {
-          const int c = j / rows;
-          pf[j] = cl.map_shared_rank(zs, c)[j - c * rows] + beta * pf[j];
-        }
+        const double zq = wsum(w, z, qv, n, red);
+        const double beta = fdiv(-zq, pq);
+        for (int j = threadIdx.x; j < n; j += blockDim.x) p[j] = z[j] + beta * p[j];
         __syncthreads();
       }
     }
+    relres = bnorm > 0 ? sqrt(rlast) / bnorm : 0.0;
     if (best < relres) {  // stopped past the best iterate: return that one
-      for (int i = threadIdx.x; i < nr; i += blockDim.x) xs[i] = xb[i];
       relres = best;
+      cl.sync();  // every CTA's rows of the best iterate are in pr.x
+      for (int j = threadIdx.x; j < n; j += blockDim.x) x[j] = __ldcg(pr.x + j);
       __syncthreads();
     }
     if (pr.zdef != nullptr && pr.gamma != 0.0) {
       // Sherman-Morrison back to S: x = y + gamma t z, t = 1^T W y / (1 - gamma 1^T W z)
       double wy = 0.0, unused = 0.0;
-      for (int i = threadIdx.x; i < nr; i += blockDim.x) wy += ws[i] * xs[i];
+      for (int j = threadIdx.x; j < n; j += blockDim.x) wy += w[j] * x[j];
       block_sum2(wy, unused, red);
-      cluster_sum2(cl, pub, work + 2, slot, wy, unused);
-      slot = slot == 7 ? 1 : slot + 1;
       const double t = wy / (1.0 - pr.gamma * pr.uz);
-      for (int i = threadIdx.x; i < nr; i += blockDim.x) xs[i] += pr.gamma * t * pr.zdef[r0 + i];
+      for (int j = threadIdx.x; j < n; j += blockDim.x) x[j] += pr.gamma * t * pr.zdef[j];
       __syncthreads();
-      cl.sync();
-      // reported residual: the true one of S x = b (the deflated operator's
-      // residual equals it up to the accuracy of z)
-      for (int j = threadIdx.x; j < n; j += blockDim.x) {
-        const int c = j / rows;
-        const double v = cl.map_shared_rank(xs, c)[j - c * rows];
-        const float h = (float)v;
-        vhi[j] = h;
-        vlo[j] = (float)(v - (double)h);
-      }
+      // reported residual: the true one of S x = b
+      split_full(x, n, ld, S.vhi, S.vlo);
       __syncthreads();
-      matvec_rows(pr, n, r0, r1, vhi, vlo, ts);
-      __syncthreads();
+      const double* tv = exchange_matvec(cl, pr, S, xsel, n, rows, rank, r0, r1);
       double tr = 0.0;
-      for (int i = threadIdx.x; i < nr; i += blockDim.x) {
-        const double d = bs[i] - ts[i];
+      for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        const double d = pr.b[j] - tv[j];
         tr += d * d;
       }
       block_sum2(tr, unused, red);
-      cluster_sum2(cl, pub, work + 2, slot, tr, unused);
-      slot = slot == 7 ? 1 : slot + 1;
       relres = bnorm > 0 ? sqrt(tr) / bnorm : 0.0;
+    }
+    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) pr.x[i] = x[i];
+    if (rank == 0 && threadIdx.x == 0) {
+      if (pr.iters) *pr.iters = it;
+      if (pr.relres) *pr.relres = relres;
+      if (pr.tspan) pr.tspan[1] = global_ns();
+    }
+  }
+  cl.sync();  // keep shared memory alive until every CTA is done reading it
+}
+
+// ---------------------------------------------------------------------------
+// Row-distributed cluster CG (any size that fits the slices in shared memory).
+//
+// Each CTA owns rows [r0, r1) of every vector (FP64 slices of x, r, p, q, z,
+// W, b) and of the matrix.  Vectors that the whole cluster needs (p for the
+// product, r for the preconditioner, x for the true residual) are exchanged
+// as float-float splits: every CTA writes the split of its slice into its own
+// full-length buffer, a cluster barrier publishes it, and every CTA copies the
+// other CTAs' parts through distributed shared memory (FP32 loads; no FP64
+// work over the full length).  Reductions sum per-thread partials in warp 0
+// only and publish one value per CTA; the CG scalars are formed once, by
+// thread 0, and broadcast.  GB300's FP64 issue rate is a small fraction of
+// its FP32 rate, so FP64 work is kept to the owned rows.  Two exchange
+// buffers alternate; between two writes of one buffer lies the barrier of
+// an exchange through the other, so no CTA overwrites rows that another CTA
+// may still be copying.
+// ---------------------------------------------------------------------------
+
+// rows [r0, r1) of S v as float-float pairs yh/yl[i - r0] (dense rows with
+// 16-byte alignment, or CSR)
+__device__ void matvec_rows_ff(const CGFFParams& pr, int n, int r0, int r1, const float* __restrict__ vhi,
+                               const float* __restrict__ vlo, float* __restrict__ yh, float* __restrict__ yl) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  if (pr.rowptr) {
+    for (int i = r0 + warp; i < r1; i += nwarps) {
+      const int e0 = pr.rowptr[i], e1 = pr.rowptr[i + 1];
+      FF a{0.f, 0.f};
+      for (int e = e0 + lane; e < e1; e += 32) {
+        const int c = __ldg(pr.colidx + e);
+        ff_fma(a, __ldg(pr.Shi + e), __ldg(pr.Slo + e), vhi[c], vlo[c]);
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        FF oa;
+        oa.hi = __shfl_down_sync(0xffffffffu, a.hi, o);
+        oa.lo = __shfl_down_sync(0xffffffffu, a.lo, o);
+        a = ff_add(a, oa);
+      }
+      if (lane == 0) {
+        yh[i - r0] = a.hi;
+        yl[i - r0] = a.lo;
+      }
+    }
+    return;
+  }
+  const int ld = schur_ld(n), nq = ld >> 2;
+  const float4* vh4 = reinterpret_cast<const float4*>(vhi);
+  const float4* vl4 = reinterpret_cast<const float4*>(vlo);
+  for (int i = r0 + 2 * warp; i < r1; i += 2 * nwarps) {
+    const bool two = i + 1 < r1;
+    const float4* h0 = reinterpret_cast<const float4*>(pr.Shi + (size_t)i * ld);
+    const float4* l0 = reinterpret_cast<const float4*>(pr.Slo + (size_t)i * ld);
+    const float4* h1 = reinterpret_cast<const float4*>(pr.Shi + (size_t)(two ? i + 1 : i) * ld);
+    const float4* l1 = reinterpret_cast<const float4*>(pr.Slo + (size_t)(two ? i + 1 : i) * ld);
+    FF a{0.f, 0.f}, b{0.f, 0.f};
+    int j = lane;
+    for (; j + 32 < nq; j += 64) {  // eight 16-byte loads in flight per lane
+      const float4 x0 = __ldg(h0 + j), y0 = __ldg(l0 + j), x1 = __ldg(h1 + j), y1 = __ldg(l1 + j);
+      const float4 x2 = __ldg(h0 + j + 32), y2 = __ldg(l0 + j + 32), x3 = __ldg(h1 + j + 32),
+                   y3 = __ldg(l1 + j + 32);
+      ff_fma4(a, x0, y0, vh4[j], vl4[j]);
+      ff_fma4(b, x1, y1, vh4[j], vl4[j]);
+      ff_fma4(a, x2, y2, vh4[j + 32], vl4[j + 32]);
+      ff_fma4(b, x3, y3, vh4[j + 32], vl4[j + 32]);
+    }
+    if (j < nq) {
+      const float4 x0 = __ldg(h0 + j), y0 = __ldg(l0 + j), x1 = __ldg(h1 + j), y1 = __ldg(l1 + j);
+      ff_fma4(a, x0, y0, vh4[j], vl4[j]);
+      ff_fma4(b, x1, y1, vh4[j], vl4[j]);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      FF oa, ob;
+      oa.hi = __shfl_down_sync(0xffffffffu, a.hi, o);
+      oa.lo = __shfl_down_sync(0xffffffffu, a.lo, o);
+      ob.hi = __shfl_down_sync(0xffffffffu, b.hi, o);
+      ob.lo = __shfl_down_sync(0xffffffffu, b.lo, o);
+      a = ff_add(a, oa);
+      b = ff_add(b, ob);
+    }
+    if (lane == 0) {
+      yh[i - r0] = a.hi;
+      yl[i - r0] = a.lo;
+      if (two) {
+        yh[i + 1 - r0] = b.hi;
+        yl[i + 1 - r0] = b.lo;
+      }
+    }
+  }
+}
+
+// z[i - r0] = (W^-1 C^T C r)_i for the owned rows (float-float): u = C r is
+// formed once for the points [ua, ua + nu) = [r0 - K, r1 + K) (the band
+// neighbours of the owned rows unless a body wraps around), whose band rows
+// and body segments the CTA staged in shared memory (sb, ss, sl) when it
+// took the problem; the rare wrapped neighbours are read from global memory
+__device__ __forceinline__ FF band_u(const CGFFParams& pr, int j, int ua, int nu, const float* __restrict__ sb,
+                                     const int* __restrict__ ss, const int* __restrict__ sl,
+                                     const float* __restrict__ rhi, const float* __restrict__ rlo) {
+  const int K = pr.band_k, P = 2 * K + 1;
+  FF u{0.f, 0.f};
+  if (j >= ua && j < ua + nu) {
+    const int s = ss[j - ua], L = sl[j - ua];
+    const float* c = sb + (size_t)(j - ua) * P;
+    for (int t2 = -K; t2 <= K; ++t2) {
+      const int q = seg_nb_near(j, s, L, t2);
+      ff_fma(u, c[t2 + K], 0.f, rhi[q], rlo[q]);
+    }
+  } else {
+    const int s = __ldg(pr.seg_start + j), L = __ldg(pr.seg_len + j);
+    for (int t2 = -K; t2 <= K; ++t2) {
+      const int q = seg_nb_near(j, s, L, t2);
+      ff_fma(u, __ldg(pr.band + (size_t)j * P + t2 + K), 0.f, rhi[q], rlo[q]);
+    }
+  }
+  return u;
+}
+
+__device__ void apply_band_rows(const CGFFParams& pr, int n, int r0, int r1, const float* __restrict__ rhi,
+                                const float* __restrict__ rlo, const float* __restrict__ sb,
+                                const int* __restrict__ ss, const int* __restrict__ sl, float* __restrict__ uhi,
+                                float* __restrict__ ulo, const double* __restrict__ ws, double* __restrict__ z) {
+  const int K = pr.band_k, P = 2 * K + 1;
+  const int ua = r0 - K, nu = (r1 - r0) + 2 * K;
+  for (int jj = threadIdx.x; jj < nu; jj += blockDim.x) {
+    const int j = ua + jj;
+    FF u{0.f, 0.f};
+    if (j >= 0 && j < n) u = band_u(pr, j, ua, nu, sb, ss, sl, rhi, rlo);
+    uhi[jj] = u.hi;
+    ulo[jj] = u.lo;
+  }
+  __syncthreads();
+  for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+    const int s = ss[i - ua], L = sl[i - ua];
+    FF acc{0.f, 0.f};
+    for (int t = -K; t <= K; ++t) {
+      const int j = seg_nb_near(i, s, L, -t);
+      FF u;
+      float c;
+      if (j >= ua && j < ua + nu) {
+        u.hi = uhi[j - ua];
+        u.lo = ulo[j - ua];
+        c = sb[(size_t)(j - ua) * P + t + K];
+      } else {  // wrapped around a body shorter than the CTA's row range
+        u = band_u(pr, j, ua, nu, sb, ss, sl, rhi, rlo);
+        c = __ldg(pr.band + (size_t)j * P + t + K);
+      }
+      ff_fma(acc, c, 0.f, u.hi, u.lo);
+    }
+    z[i - r0] = fdiv((double)acc.hi + (double)acc.lo, ws[i - r0]);
+  }
+}
+
+// zh/zl[i - r0] = (M r)_i for the owned rows, block-Jacobi in float-float:
+// one warp per four rows so that four rows' loads are in flight together
+__device__ void apply_bjacobi_rows(const CGFFParams& pr, int r0, int r1, const float* __restrict__ rhi,
+                                   const float* __restrict__ rlo, float* __restrict__ zh, float* __restrict__ zl) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int i0 = r0 + 4 * warp; i0 < r1; i0 += 4 * nw) {
+    FF acc[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      acc[u] = FF{0.f, 0.f};
+      const int i = i0 + u;
+      if (i < r1) {
+        const int b = pr.blk[i];
+        const int s = pr.bstart[b], sz = pr.bsize[b];
+        const float* __restrict__ rh = pr.binv_hi + pr.boff[b] + (size_t)(i - s) * sz;
+        const float* __restrict__ rl = pr.binv_lo + pr.boff[b] + (size_t)(i - s) * sz;
+        for (int t = lane; t < sz; t += 32) ff_fma(acc[u], __ldg(rh + t), __ldg(rl + t), rhi[s + t], rlo[s + t]);
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        FF other;
+        other.hi = __shfl_down_sync(0xffffffffu, acc[u].hi, o);
+        other.lo = __shfl_down_sync(0xffffffffu, acc[u].lo, o);
+        acc[u] = ff_add(acc[u], other);
+      }
+    }
+    if (lane == 0) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (i0 + u < r1) {
+          zh[i0 + u - r0] = acc[u].hi;
+          zl[i0 + u - r0] = acc[u].lo;
+        }
+    }
+  }
+}
+
+// Cluster-wide sums of K <= 4 values, partials held by threads [0, nact).
+// On return the totals are in v[] of thread 0 only; thread 0 derives what
+// the other threads need, stores it in the broadcast area and the caller
+// synchronises the CTA before reading it.  Each FP64 partial is split into a
+// float-float pair (hi exact, lo rounded: ~48 bits) and the sums run in FP32
+// float-float arithmetic: GB300 issues FP64 at a small fraction of the FP32
+// rate and a chain of dependent FP64 adds costs far more latency than the
+// same chain of FP32 two-sums.  `red` holds 4 K blockDim floats (2 K blockDim
+// doubles), `pub` 8 slots of 4 float-float values; the published slot
+// rotates over seven values so that a CTA never overwrites a slot another
+// CTA may still be reading.
+template <int K>
+__device__ void csum_t0(cg::cluster_group& cl, double (&v)[K], int nact, double* red, double* pub, int& slot) {
+  const int t = threadIdx.x, nt = blockDim.x;
+  float* rf = reinterpret_cast<float*>(red);
+  float* pf = reinterpret_cast<float*>(pub);
+  nact = min(nact, nt);  // threads beyond hold zero partials (or none)
+  if (t < nact)
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const float h = (float)v[k];
+      rf[(2 * k) * nt + t] = h;
+      rf[(2 * k + 1) * nt + t] = (float)(v[k] - (double)h);
+    }
+  __syncthreads();
+  if (t < 32) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      FF a{0.f, 0.f};
+      for (int i = t; i < nact; i += 32) a = ff_add(a, FF{rf[(2 * k) * nt + i], rf[(2 * k + 1) * nt + i]});
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        FF b;
+        b.hi = __shfl_down_sync(0xffffffffu, a.hi, o);
+        b.lo = __shfl_down_sync(0xffffffffu, a.lo, o);
+        a = ff_add(a, b);
+      }
+      if (t == 0) {
+        pf[8 * slot + 2 * k] = a.hi;
+        pf[8 * slot + 2 * k + 1] = a.lo;
+      }
+    }
+  }
+  cl.sync();
+  if (t < 32) {
+    float rh[K], rl[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      rh[k] = t < CG_CLUSTER ? cl.map_shared_rank(pf, t)[8 * slot + 2 * k] : 0.f;
+      rl[k] = t < CG_CLUSTER ? cl.map_shared_rank(pf, t)[8 * slot + 2 * k + 1] : 0.f;
+    }
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      FF a{rh[k], rl[k]};
+#pragma unroll
+      for (int o = CG_CLUSTER / 2; o > 0; o >>= 1) {
+        FF b;
+        b.hi = __shfl_down_sync(0xffffffffu, a.hi, o);
+        b.lo = __shfl_down_sync(0xffffffffu, a.lo, o);
+        a = ff_add(a, b);
+      }
+      v[k] = (double)a.hi + (double)a.lo;
+    }
+  }
+  slot = slot == 7 ? 1 : slot + 1;
+}
+
+// split of the owned slice into the exchange buffer's owned part
+__device__ __forceinline__ void publish_slice(const double* s, int r0, int nr, float* eh, float* el) {
+  for (int i = threadIdx.x; i < nr; i += blockDim.x) {
+    const double v = s[i];
+    const float h = (float)v;
+    eh[r0 + i] = h;
+    el[r0 + i] = (float)(v - (double)h);
+  }
+}
+
+// copy the other CTAs' parts of an exchange buffer (after the barrier that
+// published them)
+__device__ __forceinline__ void gather_parts(cg::cluster_group& cl, float* eh, float* el, int n, int rows, int rank) {
+  // four elements per thread and trip, all remote loads issued before the stores
+  const int nt = blockDim.x;
+  for (int j0 = threadIdx.x; j0 < n; j0 += 4 * nt) {
+    float h[4], l[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int j = j0 + u * nt;
+      const int c = j < n ? j / rows : rank;
+      h[u] = c != rank ? cl.map_shared_rank(eh, c)[j] : 0.f;
+      l[u] = c != rank ? cl.map_shared_rank(el, c)[j] : 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int j = j0 + u * nt;
+      if (j < n && j / rows != rank) {
+        eh[j] = h[u];
+        el[j] = l[u];
+      }
+    }
+  }
+  __syncthreads();
+}
+
+template <int NT, int MINB>
+__global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(NT, MINB)
+    k_cg_cluster(const CGFFParams* __restrict__ P, const int* __restrict__ order, int nprob, int* counter,
+                 int max_n) {
+  cg::cluster_group cl = cg::this_cluster();
+  const int rank = (int)cl.block_rank();
+  const int rmax = (max_n + CG_CLUSTER - 1) / CG_CLUSTER;
+  const int ldm = schur_ld(max_n);
+  extern __shared__ __align__(16) unsigned char smraw[];
+  double* red = reinterpret_cast<double*>(smraw);  // 2 * threads partials
+  double* bc = red + 2 * NT;                       // 16: scalars broadcast by thread 0
+  double* pub = bc + 16;                           // 32: published CTA sums (8 slots x 4)
+  double* work = pub + 32;                         // 4: [0] queue index taken by rank 0
+  double* xs = work + 4;                           // owned slices (rmax each)
+  double* rs = xs + rmax;
+  double* ps = rs + rmax;
+  double* qs = ps + rmax;
+  double* zs = qs + rmax;
+  double* ws = zs + rmax;
+  double* bs = ws + rmax;
+  float* eh[2];
+  float* el[2];
+  eh[0] = reinterpret_cast<float*>(bs + rmax + (rmax & 1));  // exchange buffers (ldm each, 16-byte aligned)
+  el[0] = eh[0] + ldm;
+  eh[1] = el[0] + ldm;
+  el[1] = eh[1] + ldm;
+  float* uhi = el[1] + ldm;  // band intermediate (rmax + 2 K, K <= 8)
+  float* ulo = uhi + rmax + 16;
+  float* yh = ulo + rmax + 16;  // product rows (float-float)
+  float* yl = yh + rmax;
+  float* sband = yl + rmax;                                      // staged band rows ((rmax + 16) x 17)
+  int* sseg_s = reinterpret_cast<int*>(sband + (rmax + 16) * 17);  // staged body segments (rmax + 16)
+  int* sseg_l = sseg_s + rmax + 16;
+  int slot = 1, eb = 0;
+  while (true) {
+    if (rank == 0 && threadIdx.x == 0) work[0] = (double)atomicAdd(counter, 1);
+    cl.sync();
+    const int q = (int)cl.map_shared_rank(work, 0)[0];
+    if (q >= nprob) break;
+    const CGFFParams& pr = P[order[q]];  // fields read through L1 as needed
+    if (pr.tspan && rank == 0 && threadIdx.x == 0) {
+      pr.tspan[0] = global_ns();
+      pr.tspan[2] = sm_id();
+    }
+    const int n = pr.n, ld = schur_ld(n);
+    const int rows = (n + CG_CLUSTER - 1) / CG_CLUSTER;
+    const int r0 = min(n, rank * rows), r1 = min(n, r0 + rows);
+    const int nr = r1 - r0;
+    const double gamma = pr.gamma;
+    const bool pre = pr.blk != nullptr || pr.band != nullptr;
+    for (int i = threadIdx.x; i < nr; i += blockDim.x) {
+      xs[i] = pr.x0 ? pr.x0[r0 + i] : 0.0;
+      bs[i] = pr.b[r0 + i];
+      ws[i] = pr.w ? pr.w[r0 + i] : 1.0;
+    }
+    for (int j = n + threadIdx.x; j < ld; j += blockDim.x) {  // padding of the products' vectors
+      eh[0][j] = el[0][j] = eh[1][j] = el[1][j] = 0.f;
+    }
+    if (pr.band) {  // stage the band rows and body segments of [r0 - K, r1 + K)
+      const int K = pr.band_k, P = 2 * K + 1, ua = r0 - K, nu = nr + 2 * K;
+      for (int e = threadIdx.x; e < nu * P; e += blockDim.x) {
+        const int j = ua + e / P;
+        sband[e] = (j >= 0 && j < n) ? __ldg(pr.band + (size_t)j * P + e % P) : 0.f;
+      }
+      for (int jj = threadIdx.x; jj < nu; jj += blockDim.x) {
+        const int j = ua + jj;
+        const bool in = j >= 0 && j < n;
+        sseg_s[jj] = in ? __ldg(pr.seg_start + j) : 0;
+        sseg_l[jj] = in ? __ldg(pr.seg_len + j) : 0;
+      }
+    }
+    __syncthreads();
+    if (pr.x0) {  // warm start: r = b - S' x0
+      double v[1] = {0.0};
+      for (int i = threadIdx.x; i < nr; i += blockDim.x) v[0] += ws[i] * xs[i];
+      publish_slice(xs, r0, nr, eh[eb], el[eb]);
+      csum_t0<1>(cl, v, nr, red, pub, slot);
+      if (threadIdx.x == 0) bc[0] = gamma * v[0];
+      gather_parts(cl, eh[eb], el[eb], n, rows, rank);
+      matvec_rows_ff(pr, n, r0, r1, eh[eb], el[eb], yh, yl);
+      eb ^= 1;
+      __syncthreads();
+      const double c0 = bc[0];
+      for (int i = threadIdx.x; i < nr; i += blockDim.x) rs[i] = bs[i] - ((double)yh[i] + (double)yl[i]) - c0;
+    } else {
+      for (int i = threadIdx.x; i < nr; i += blockDim.x) rs[i] = bs[i];
+    }
+    __syncthreads();
+    double rz, bnorm;
+    {
+      double v[2] = {0.0, 0.0};
+      for (int i = threadIdx.x; i < nr; i += blockDim.x) {
+        v[0] += bs[i] * bs[i];
+        v[1] += ws[i] * rs[i] * rs[i];
+      }
+      if (pre) publish_slice(rs, r0, nr, eh[eb], el[eb]);
+      csum_t0<2>(cl, v, nr, red, pub, slot);
+      if (threadIdx.x == 0) {
+        bc[0] = sqrt(v[0]);
+        bc[1] = v[1];
+      }
+      __syncthreads();
+      bnorm = bc[0];
+      rz = bc[1];
+    }
+    if (pre) {
+      gather_parts(cl, eh[eb], el[eb], n, rows, rank);
+      if (pr.band) {
+        apply_band_rows(pr, n, r0, r1, eh[eb], el[eb], sband, sseg_s, sseg_l, uhi, ulo, ws, zs);
+      } else {
+        apply_bjacobi_rows(pr, r0, r1, eh[eb], el[eb], yh, yl);
+        __syncthreads();
+        for (int i = threadIdx.x; i < nr; i += blockDim.x) zs[i] = (double)yh[i] + (double)yl[i];
+      }
+      eb ^= 1;
+      __syncthreads();
+    }
+    for (int i = threadIdx.x; i < nr; i += blockDim.x) ps[i] = pre ? zs[i] : rs[i];
+    const double thr = pr.tol * bnorm;
+    const double thr2 = thr * thr;
+    double rlast = bnorm * bnorm;
+    int it = 0;
+    double relres = bnorm > 0 ? 1.0 : 0.0;
+    bool done = bnorm == 0.0;
+    // stagnation guard: past the attainable accuracy (float-float products on
+    // a Schur complement of condition ~1e6 floor near 1e-10) CG drifts and
+    // eventually diverges; stop after 8 refreshes without a better true
+    // residual and return the best iterate (kept in pr.x, owned rows)
+    double best = 1e300;
+    int stall = 0;
+    for (int i = threadIdx.x; i < nr; i += blockDim.x) pr.x[r0 + i] = xs[i];
+    __syncthreads();
+    while (!done && it < pr.maxiter) {
+      // q = S' p: exchange p, own rows of the product
+      double cp;
+      {
+        double v[1] = {0.0};
+        for (int i = threadIdx.x; i < nr; i += blockDim.x) v[0] += ws[i] * ps[i];
+        publish_slice(ps, r0, nr, eh[eb], el[eb]);
+        csum_t0<1>(cl, v, nr, red, pub, slot);
+        if (threadIdx.x == 0) bc[2] = gamma * v[0];
+        gather_parts(cl, eh[eb], el[eb], n, rows, rank);
+        matvec_rows_ff(pr, n, r0, r1, eh[eb], el[eb], yh, yl);
+        eb ^= 1;
+        __syncthreads();
+        cp = bc[2];
+      }
+      double alpha, pq;
+      {
+        double v[2] = {0.0, 0.0};
+        for (int i = threadIdx.x; i < nr; i += blockDim.x) {
+          const double qi = (double)yh[i] + (double)yl[i] + cp;
+          qs[i] = qi;
+          v[0] += ws[i] * ps[i] * qi;
+          v[1] += ws[i] * ps[i] * rs[i];
+        }
+        csum_t0<2>(cl, v, nr, red, pub, slot);
+        if (threadIdx.x == 0) {
+          bc[3] = v[0];
+          bc[4] = v[0] != 0.0 ? fdiv(pre ? v[1] : rz, v[0]) : 0.0;
+        }
+        __syncthreads();
+        pq = bc[3];
+        alpha = bc[4];
+      }
+      if (pq == 0.0) break;
+      double rr, rzn;
+      {
+        double v[2] = {0.0, 0.0};
+        for (int i = threadIdx.x; i < nr; i += blockDim.x) {
+          xs[i] += alpha * ps[i];
+          const double ri = rs[i] - alpha * qs[i];
+          rs[i] = ri;
+          v[0] += ri * ri;
+          v[1] += ws[i] * ri * ri;
+        }
+        if (pre) publish_slice(rs, r0, nr, eh[eb], el[eb]);
+        csum_t0<2>(cl, v, nr, red, pub, slot);
+        if (threadIdx.x == 0) {
+          bc[5] = v[0];
+          bc[6] = v[1];
+        }
+        __syncthreads();
+        rr = bc[5];
+        rzn = bc[6];
+      }
+      ++it;
+      rlast = rr;
+      if (rr <= thr2 || (it % 50) == 0 || it == pr.maxiter) {
+        // true residual b - S' x (x exchanged through the current buffer: the
+        // split of r published above is superseded)
+        {
+          double v[1] = {0.0};
+          for (int i = threadIdx.x; i < nr; i += blockDim.x) v[0] += ws[i] * xs[i];
+          publish_slice(xs, r0, nr, eh[eb], el[eb]);
+          csum_t0<1>(cl, v, nr, red, pub, slot);
+          if (threadIdx.x == 0) bc[7] = gamma * v[0];
+          gather_parts(cl, eh[eb], el[eb], n, rows, rank);
+          matvec_rows_ff(pr, n, r0, r1, eh[eb], el[eb], yh, yl);
+          eb ^= 1;
+          __syncthreads();
+        }
+        const double cx = bc[7];
+        double v[2] = {0.0, 0.0};
+        for (int i = threadIdx.x; i < nr; i += blockDim.x) {
+          const double ri = bs[i] - ((double)yh[i] + (double)yl[i]) - cx;
+          rs[i] = ri;
+          v[0] += ri * ri;
+          v[1] += ws[i] * ri * ri;
+        }
+        if (pre) publish_slice(rs, r0, nr, eh[eb], el[eb]);
+        csum_t0<2>(cl, v, nr, red, pub, slot);
+        if (threadIdx.x == 0) {
+          bc[8] = v[0];
+          bc[9] = v[1];
+        }
+        __syncthreads();
+        const double tr = bc[8];
+        rzn = bc[9];
+        rlast = tr;
+        if (tr <= thr2) {
+          done = true;
+          break;
+        }
+        relres = bnorm > 0 ? sqrt(tr) / bnorm : 0.0;
+        if (relres < best) {
+          best = relres;
+          stall = 0;
+          for (int i = threadIdx.x; i < nr; i += blockDim.x) pr.x[r0 + i] = xs[i];
+        } else if (++stall >= 8) {
+          break;
+        }
+      }
+      if (!pre) {
+        const double beta = fdiv(rzn, rz);
+        rz = rzn;
+        for (int i = threadIdx.x; i < nr; i += blockDim.x) ps[i] = rs[i] + beta * ps[i];
+        __syncthreads();
+      } else {
+        // flexible CG: z = M r (r exchanged), beta = -(z, q) / (p, q), p = z + beta p
+        gather_parts(cl, eh[eb], el[eb], n, rows, rank);
+        if (pr.band) {
+          apply_band_rows(pr, n, r0, r1, eh[eb], el[eb], sband, sseg_s, sseg_l, uhi, ulo, ws, zs);
+        } else {
+          apply_bjacobi_rows(pr, r0, r1, eh[eb], el[eb], yh, yl);
+          __syncthreads();
+          for (int i = threadIdx.x; i < nr; i += blockDim.x) zs[i] = (double)yh[i] + (double)yl[i];
+        }
+        eb ^= 1;
+        __syncthreads();
+        double v[1] = {0.0};
+        for (int i = threadIdx.x; i < nr; i += blockDim.x) v[0] += ws[i] * zs[i] * qs[i];
+        csum_t0<1>(cl, v, nr, red, pub, slot);
+        if (threadIdx.x == 0) bc[10] = fdiv(-v[0], pq);
+        __syncthreads();
+        const double beta = bc[10];
+        for (int i = threadIdx.x; i < nr; i += blockDim.x) ps[i] = zs[i] + beta * ps[i];
+        __syncthreads();
+      }
+    }
+    relres = bnorm > 0 ? sqrt(rlast) / bnorm : 0.0;
+    if (best < relres) {  // stopped past the best iterate: return that one
+      relres = best;
+      for (int i = threadIdx.x; i < nr; i += blockDim.x) xs[i] = pr.x[r0 + i];
+      __syncthreads();
+    }
+    if (pr.zdef != nullptr && gamma != 0.0) {
+      // Sherman-Morrison back to S: x = y + gamma t z, t = 1^T W y / (1 - gamma 1^T W z)
+      double v[1] = {0.0};
+      for (int i = threadIdx.x; i < nr; i += blockDim.x) v[0] += ws[i] * xs[i];
+      csum_t0<1>(cl, v, nr, red, pub, slot);
+      if (threadIdx.x == 0) bc[11] = gamma * (v[0] / (1.0 - gamma * pr.uz));
+      __syncthreads();
+      const double gt = bc[11];
+      for (int i = threadIdx.x; i < nr; i += blockDim.x) xs[i] += gt * pr.zdef[r0 + i];
+      __syncthreads();
+      // reported residual: the true one of S x = b
+      double u[1] = {0.0};
+      publish_slice(xs, r0, nr, eh[eb], el[eb]);
+      csum_t0<1>(cl, u, nr, red, pub, slot);  // barrier that publishes x
+      gather_parts(cl, eh[eb], el[eb], n, rows, rank);
+      matvec_rows_ff(pr, n, r0, r1, eh[eb], el[eb], yh, yl);
+      eb ^= 1;
+      __syncthreads();
+      double t[1] = {0.0};
+      for (int i = threadIdx.x; i < nr; i += blockDim.x) {
+        const double d = bs[i] - ((double)yh[i] + (double)yl[i]);
+        t[0] += d * d;
+      }
+      csum_t0<1>(cl, t, nr, red, pub, slot);
+      if (threadIdx.x == 0) bc[12] = t[0];
+      __syncthreads();
+      relres = bnorm > 0 ? sqrt(bc[12]) / bnorm : 0.0;
     }
     for (int i = threadIdx.x; i < nr; i += blockDim.x) pr.x[r0 + i] = xs[i];
     if (rank == 0 && threadIdx.x == 0) {
       if (pr.iters) *pr.iters = it;
       if (pr.relres) *pr.relres = relres;
+      if (pr.tspan) pr.tspan[1] = global_ns();
     }
-    cl.sync();  // every CTA done with this problem's shared data
   }
   cl.sync();  // keep shared memory alive until every CTA is done reading it
 }
 
-size_t cg_cluster_smem(int max_n) {
-  const int rmax = (max_n + CG_CLUSTER - 1) / CG_CLUSTER;
-  return (16 + 2 * CGC_WARPS + 4 + 7 * (size_t)rmax + 2 * (size_t)max_n) * sizeof(double) +
-         2 * (size_t)max_n * sizeof(float) + 64;
+size_t cg_cluster_smem(int max_n, int nt) {
+  const size_t rmax = (size_t)(max_n + CG_CLUSTER - 1) / CG_CLUSTER;
+  const size_t ldm = (size_t)schur_ld(max_n);
+  return (2 * (size_t)nt + 16 + 32 + 4 + 7 * rmax + 1) * sizeof(double) +
+         (4 * ldm + 2 * (rmax + 16) + 2 * rmax + 17 * (rmax + 16)) * sizeof(float) +
+         2 * (rmax + 16) * sizeof(int) + 64;
 }
 
+size_t cg_rep_smem(int max_n) {
+  const size_t ldm = (size_t)schur_ld(max_n);
+  return (2 * CGR_THREADS + 2 + 4 + 7 * ldm) * sizeof(double) + 4 * ldm * sizeof(float);
+}
+
+
+// Kernel variants (the batch autotuner picks among them): 0 (default) and 1 =
+// row-distributed, 256 threads per CTA; 3 = row-distributed, 128 threads
+// per CTA (twice as many clusters resident: more problems in flight when the
+// iterations are latency-bound); 2 = replicated vectors, when they fit in
+// shared memory.
+static bool use_rep(int variant, int max_n) { return variant == 2 && cg_rep_smem(max_n) <= 200 * 1024; }
+static int dist_threads(int variant) { return variant == 3 ? 128 : 256; }
+
 int launch_cg_cluster(const void* params_dev, const int* order, int nprob, int* counter, int max_n, int nclusters,
-                      cudaStream_t st) {
-  const size_t smem = cg_cluster_smem(max_n);
+                      cudaStream_t st, int variant) {
+  const CGFFParams* prm = static_cast<const CGFFParams*>(params_dev);
+  ILM_CHECK_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), st));
+  if (use_rep(variant, max_n)) {  // replicated vectors: one cluster barrier per iteration
+    const size_t rsm = cg_rep_smem(max_n);
+    ILM_CHECK_CUDA(cudaFuncSetAttribute(k_cg_rep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsm));
+    k_cg_rep<<<nclusters * CG_CLUSTER, CGR_THREADS, rsm, st>>>(prm, order, nprob, counter, max_n);
+    ILM_CHECK_LAUNCH();
+    return ILM_OK;
+  }
+  const int nt = dist_threads(variant);
+  const size_t smem = cg_cluster_smem(max_n, nt);
   if (smem > 200 * 1024) {
     set_error("cluster CG: %d unknowns exceed the shared-memory layout", max_n);
     return ILM_ERR_SIZE_LIMIT;
   }
-  ILM_CHECK_CUDA(cudaFuncSetAttribute(k_cg_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  ILM_CHECK_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), st));
-  k_cg_cluster<<<nclusters * CG_CLUSTER, CGC_THREADS, smem, st>>>(static_cast<const CGFFParams*>(params_dev), order,
-                                                                  nprob, counter, max_n);
+  if (nt == 128) {
+    ILM_CHECK_CUDA(cudaFuncSetAttribute(k_cg_cluster<128, 6>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_cg_cluster<128, 6><<<nclusters * CG_CLUSTER, 128, smem, st>>>(prm, order, nprob, counter, max_n);
+  } else {
+    ILM_CHECK_CUDA(cudaFuncSetAttribute(k_cg_cluster<256, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_cg_cluster<256, 3><<<nclusters * CG_CLUSTER, 256, smem, st>>>(prm, order, nprob, counter, max_n);
+  }
   ILM_CHECK_LAUNCH();
   return ILM_OK;
 }
 
-int cg_cluster_count(int nprob, int max_n) {
+int cg_cluster_count(int nprob, int max_n, int variant) {
   int dev = 0, nsm = 148;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  // four 256-thread CTAs per SM: about 4 nsm / 8 resident clusters
-  int nc = std::max(1, 4 * nsm / CG_CLUSTER);
-  (void)max_n;
+  // co-resident clusters of the kernel launch_cg_cluster will pick (the
+  // persistent clusters beyond that would only find the queue empty)
+  const bool rep = use_rep(variant, max_n);
+  const int nt = rep ? CGR_THREADS : dist_threads(variant);
+  const size_t smem = rep ? cg_rep_smem(max_n) : cg_cluster_smem(max_n, nt);
+  int nc = 0;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(CG_CLUSTER * nsm);
+  cfg.blockDim = dim3(nt);
+  cfg.dynamicSmemBytes = smem;
+  cudaError_t e;
+  if (rep) {
+    e = cudaFuncSetAttribute(k_cg_rep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveClusters(&nc, k_cg_rep, &cfg);
+  } else if (nt == 128) {
+    e = cudaFuncSetAttribute(k_cg_cluster<128, 6>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveClusters(&nc, k_cg_cluster<128, 6>, &cfg);
+  } else {
+    e = cudaFuncSetAttribute(k_cg_cluster<256, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveClusters(&nc, k_cg_cluster<256, 3>, &cfg);
+  }
+  if (e != cudaSuccess || nc <= 0) {
+    (void)cudaGetLastError();
+    nc = std::max(1, (nt == 128 ? 6 : 3) * nsm / CG_CLUSTER);
+  }
   return std::min(nc, nprob);
 }
 
@@ -623,6 +1294,10 @@ void cgff_params_set_deflation(void* dst, double gamma, const double* zdef, doub
   p->uz = uz;
 }
 
+void cgff_params_set_timing(void* dst, unsigned long long* tspan) {
+  static_cast<CGFFParams*>(dst)->tspan = tspan;
+}
+
 void cgff_params_set_band(void* dst, const float* band, int band_k, const int* seg_start, const int* seg_len) {
   CGFFParams* p = static_cast<CGFFParams*>(dst);
   p->band = band;
@@ -645,7 +1320,7 @@ __global__ void __launch_bounds__(256) k_block_inverse(const BJBlockTask* __rest
   double* scal = fcol + sz;
   for (int idx = threadIdx.x; idx < sz * ld; idx += blockDim.x) {
     const int i = idx / ld, j = idx - i * ld;
-    const size_t g = (size_t)(T.s + i) * T.n + T.s + j;
+    const size_t g = (size_t)(T.s + i) * schur_ld(T.n) + T.s + j;
     Ad[idx] = j < sz ? (double)T.Shi[g] + (double)T.Slo[g] : (j - sz == i ? 1.0 : 0.0);
   }
   __syncthreads();

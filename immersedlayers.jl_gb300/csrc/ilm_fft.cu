@@ -423,7 +423,6 @@ __constant__ float2 c_tw32[32];  // exp(-2 pi i j / 32)
 __constant__ float2 c_tw24[24];  // exp(-2 pi i j / 24)
 
 constexpr int FAST_THREADS = 256;
-constexpr int FAST_CW = 8;  // spectral columns per CTA
 
 __host__ __device__ constexpr int bitrev_c(int i, int bits) {
   int r = 0;
@@ -616,23 +615,32 @@ __device__ void rfft_rows_body(const ConvJobDev& J, int r0, int rend, float2* sm
 }
 
 // inverse rows: the rows' H + 1 spectral values are staged in `raw`
-// (RB x (H + 1)), split into the half-length complex transform, inverse FFT,
-// first n1 values (+ the `add` field) written
+// (RB x (H + 1)).  The thread of k1 forms the half-length complex spectrum
+// z[k1 + N1 k2] of the real inverse transform straight from the staged
+// values (split of X[k] and X[H - k]) and runs the first inverse stage in
+// registers (length-N2 DFT over k2, twiddle w_H^{-n2 k1}); after one
+// exchange the thread of n2 runs the length-N1 DFTs over k1 and writes
+// z[N2 n1 + n2] = (out[2 m], out[2 m + 1]), m = N2 n1 + n2, first n1 values
+// (+ the `add` field, staged while the transforms run)
 template <int N1, int N2>
 __device__ void irfft_rows_body(const ConvJobDev& J, int r0, float2* sm, float2* raw, void* out_base) {
-  constexpr int H = N1 * N2, G = N1 > N2 ? N1 : N2, CS = N1 * (N2 + 1);
+  constexpr int H = N1 * N2, G = N1 > N2 ? N1 : N2, CS = N1 * (N2 + 1), ST = N2 + 1;
   constexpr int RB = FAST_THREADS / G;
   const int nr = min(RB, J.n2 - r0);
-  const float2* tw = static_cast<const float2*>(J.tw1);
+  const float2* __restrict__ tw = static_cast<const float2*>(J.tw1);  // exp(-2 pi i j / 2H)
   const float2* W = static_cast<const float2*>(J.work) + (size_t)r0 * (H + 1);
   for (int idx = threadIdx.x; idx < nr * (H + 1); idx += FAST_THREADS) cpa8(raw + idx, W + idx, true);
   cpa_wait_all();
   __syncthreads();
-  for (int idx = threadIdx.x; idx < RB * H; idx += FAST_THREADS) {
-    const int r = idx / H, k = idx - r * H;
-    float2 z = make_float2(0.f, 0.f);
-    if (r < nr) {
-      const float2* X = raw + r * (H + 1);
+  const int r = threadIdx.x / G, g = threadIdx.x - r * G;
+  const bool act = r < nr;
+  float2* x = sm + (r < RB ? r : 0) * CS;
+  if (act && g < N1) {
+    float2 b[N2];
+    const float2* X = raw + r * (H + 1);
+#pragma unroll
+    for (int k2 = 0; k2 < N2; ++k2) {
+      const int k = g + N1 * k2;
       const float2 xk = X[k];
       float2 xc = X[H - k];
       xc.y = -xc.y;
@@ -640,14 +648,22 @@ __device__ void irfft_rows_body(const ConvJobDev& J, int r0, float2* sm, float2*
       e.y = -e.y;
       const float2 s = cadd(xk, xc), d = csub(xk, xc);
       const float2 ed = cmul(e, d);
-      z.x = 0.5f * (s.x - ed.y);
-      z.y = 0.5f * (s.y + ed.x);
+      b[k2].x = 0.5f * (s.x - ed.y);
+      b[k2].y = 0.5f * (s.y + ed.x);
     }
-    sm[r * CS + padpos<N1, N2>(k)] = z;
+    dft_reg<N2, 1>(b);
+#pragma unroll
+    for (int n2 = 1; n2 < N2; ++n2) {
+      float2 w = tw[2 * n2 * g];
+      w.y = -w.y;
+      b[n2] = cmul(w, b[n2]);
+    }
+#pragma unroll
+    for (int n2 = 0; n2 < N2; ++n2) x[g * ST + n2] = b[n2];
   }
   __syncthreads();
   // the added field's rows go into `raw` (free now; RB (H + 1) float2 >= RB n1
-  // floats) while the transforms run
+  // floats) while the last stage runs
   const float* __restrict__ add = static_cast<const float*>(J.add);
   float* addr = reinterpret_cast<float*>(raw);
   const int n1 = J.n1;
@@ -656,69 +672,124 @@ __device__ void irfft_rows_body(const ConvJobDev& J, int r0, float2* sm, float2*
     for (int idx = threadIdx.x; idx < nr * n1; idx += FAST_THREADS) cpa4(addr + idx, a0 + idx, true);
     asm volatile("cp.async.commit_group;\n" ::: "memory");
   }
-  const int r = threadIdx.x / G, g = threadIdx.x - r * G;
-  fft4step<N1, N2, 1>(sm + (r < RB ? r : 0) * CS, g, r < nr, tw, 2);
+  float2 a[N1];
+  if (act && g < N2) {
+#pragma unroll
+    for (int k1 = 0; k1 < N1; ++k1) a[k1] = x[k1 * ST + g];
+    dft_reg<N1, 1>(a);
+  }
   if (add) {
     asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     __syncthreads();
   }
-  float* obase = out_base ? reinterpret_cast<float*>(static_cast<unsigned char*>(out_base) + J.out_off)
-                          : static_cast<float*>(J.out);
-  const float sc = (float)J.scale;
-  for (int idx = threadIdx.x; idx < nr * H; idx += FAST_THREADS) {
-    const int rr = idx / H, m = idx - rr * H;
-    const float2 z = sm[rr * CS + padpos<N1, N2>(m)];
-    float* o = obase + (size_t)(r0 + rr) * n1;
-    const int i0 = 2 * m;
-    if (add) {
-      const float* a = addr + rr * n1;
-      if (i0 < n1) o[i0] = a[i0] + z.x * sc;
-      if (i0 + 1 < n1) o[i0 + 1] = a[i0 + 1] + z.y * sc;
-    } else {
-      if (i0 < n1) o[i0] = z.x * sc;
-      if (i0 + 1 < n1) o[i0 + 1] = z.y * sc;
+  if (act && g < N2) {
+    float* obase = out_base ? reinterpret_cast<float*>(static_cast<unsigned char*>(out_base) + J.out_off)
+                            : static_cast<float*>(J.out);
+    float* o = obase + (size_t)(r0 + r) * n1;
+    const float* ar = addr + r * n1;
+    const float sc = (float)J.scale;
+#pragma unroll
+    for (int q = 0; q < N1; ++q) {
+      const int i0 = 2 * (N2 * q + g);
+      if (add) {
+        if (i0 < n1) o[i0] = ar[i0] + a[q].x * sc;
+        if (i0 + 1 < n1) o[i0 + 1] = ar[i0 + 1] + a[q].y * sc;
+      } else {
+        if (i0 < n1) o[i0] = a[q].x * sc;
+        if (i0 + 1 < n1) o[i0 + 1] = a[q].y * sc;
+      }
     }
   }
 }
 
-// columns: FFT of length P2 = N1 N2, spectrum multiply, inverse FFT; only
-// the rows [ra, rb) of the row-pass output are read (the rest are zero)
+// Column pass geometry: CW spectral columns per CTA (8 for transforms whose
+// register DFTs use 24 or 32 threads, 16 for 12 or 16, 32 for 8), thread t
+// works on column t % CW.  Each column's N1 x (N2 + 1) matrix is padded to
+// col_stride() float2 so that the 16 threads of a half-warp (16 columns, or
+// 8 columns x 2 rows) hit 16 distinct 8-byte bank pairs.
+__host__ __device__ constexpr int col_cw(int G) { return G >= 24 ? 8 : G >= 12 ? 16 : 32; }
+__host__ __device__ constexpr int col_stride(int N1, int N2) {
+  return col_cw(N1 > N2 ? N1 : N2) == 8 ? (N1 * (N2 + 1) % 4 == 2 ? N1 * (N2 + 1) : N1 * (N2 + 1) + ((6 - N1 * (N2 + 1) % 4) % 4))
+                                        : (N1 * (N2 + 1)) | 1;
+}
+
+// columns: FFT of length L = N1 N2, spectrum multiply, inverse FFT; only the
+// rows [ra, rb) of the row-pass output are read (the rest are zero).  The
+// forward four-step transform leaves the thread of k1 holding X[k1 + N1 k2]
+// for every k2; the spectrum multiply and the first inverse stage (a
+// length-N2 DFT over k2, then the twiddle w_L^{-n2 k1}) run on those
+// registers, and the last inverse stage (length-N1 DFTs over k1) gives the
+// thread of n2 the outputs x[N2 n1 + n2], which go straight to global
+// memory: three shared-memory exchanges for the transform pair.
 template <int N1, int N2>
 __device__ void cols_body(const ConvJobDev& J, int c0, float2* sm) {
-  constexpr int L = N1 * N2, G = N1 > N2 ? N1 : N2, CS = N1 * (N2 + 1);
+  constexpr int L = N1 * N2, G = N1 > N2 ? N1 : N2, ST = N2 + 1;
+  constexpr int CW = col_cw(G), CS = col_stride(N1, N2);
   const int ncols = (J.P1 >> 1) + 1;
-  const int nc = min(FAST_CW, ncols - c0);
+  const int nc = min(CW, ncols - c0);
   const int ra = J.has_box ? J.ra : 0, rb = J.has_box ? J.rb : J.n2;
   float2* W = static_cast<float2*>(J.work);
-  for (int idx = threadIdx.x; idx < FAST_CW * L; idx += FAST_THREADS) {
-    const int c = idx % FAST_CW, row = idx / FAST_CW;
+  for (int idx = threadIdx.x; idx < CW * L; idx += FAST_THREADS) {
+    const int c = idx % CW, row = idx / CW;
     const bool v = c < nc && row >= ra && row < rb;
     cpa8(sm + c * CS + padpos<N1, N2>(row), v ? W + (size_t)row * ncols + c0 + c : W, v);
   }
   cpa_wait_all();
   __syncthreads();
-  const int c = threadIdx.x / G, g = threadIdx.x - c * G;
-  const bool act = c < nc;
-  float2* x = sm + (c < FAST_CW ? c : 0) * CS;
-  const float2* tw = static_cast<const float2*>(J.tw2);
-  fft4step<N1, N2, -1>(x, g, act, tw, 1);
-  const float* __restrict__ spec = static_cast<const float*>(J.spec);
-  const int hp2 = L / 2 + 1;
-  for (int idx = threadIdx.x; idx < nc * L; idx += FAST_THREADS) {
-    const int cc = idx / L, ky = idx - cc * L;
-    const int kk = ky <= L - ky ? ky : L - ky;
-    const float sv = spec[(size_t)(c0 + cc) * hp2 + kk];
-    float2* p = sm + cc * CS + padpos<N1, N2>(ky);
-    float2 v = *p;
-    v.x *= sv;
-    v.y *= sv;
-    *p = v;
+  const int c = threadIdx.x % CW, g = threadIdx.x / CW;
+  const bool act = c < nc && g < G;
+  float2* x = sm + c * CS;
+  const float2* __restrict__ tw = static_cast<const float2*>(J.tw2);
+  // forward stage 1: length-N1 DFTs over n1 (thread n2 = g), twiddle w_L^{k1 n2}
+  if (act && g < N2) {
+    float2 a[N1];
+#pragma unroll
+    for (int n1 = 0; n1 < N1; ++n1) a[n1] = x[n1 * ST + g];
+    dft_reg<N1, -1>(a);
+#pragma unroll
+    for (int k1 = 1; k1 < N1; ++k1) a[k1] = cmul(tw[k1 * g], a[k1]);
+#pragma unroll
+    for (int k1 = 0; k1 < N1; ++k1) x[k1 * ST + g] = a[k1];
   }
   __syncthreads();
-  fft4step<N1, N2, 1>(x, g, act, tw, 1);
-  for (int idx = threadIdx.x; idx < FAST_CW * J.n2out; idx += FAST_THREADS) {
-    const int cc = idx % FAST_CW, row = idx / FAST_CW;
-    if (cc < nc) W[(size_t)row * ncols + c0 + cc] = sm[cc * CS + padpos<N1, N2>(row)];
+  // forward stage 2 (thread k1 = g): X[k1 + N1 k2]; spectrum; inverse stage A
+  if (act && g < N1) {
+    float2 b[N2];
+#pragma unroll
+    for (int n2 = 0; n2 < N2; ++n2) b[n2] = x[g * ST + n2];
+    dft_reg<N2, -1>(b);
+    const float* __restrict__ spec = static_cast<const float*>(J.spec) + (size_t)(c0 + c) * (L / 2 + 1);
+#pragma unroll
+    for (int k2 = 0; k2 < N2; ++k2) {
+      const int k = g + N1 * k2;
+      const float sv = __ldg(spec + (k <= L - k ? k : L - k));
+      b[k2].x *= sv;
+      b[k2].y *= sv;
+    }
+    dft_reg<N2, 1>(b);
+#pragma unroll
+    for (int n2 = 1; n2 < N2; ++n2) {
+      float2 w = tw[n2 * g];
+      w.y = -w.y;
+      b[n2] = cmul(w, b[n2]);
+    }
+    // the thread reads and writes only its own row g of the matrix
+#pragma unroll
+    for (int n2 = 0; n2 < N2; ++n2) x[g * ST + n2] = b[n2];
+  }
+  __syncthreads();
+  // inverse stage B (thread n2 = g): length-N1 DFTs over k1 -> x[N2 n1 + n2]
+  if (act && g < N2) {
+    float2 a[N1];
+#pragma unroll
+    for (int k1 = 0; k1 < N1; ++k1) a[k1] = x[k1 * ST + g];
+    dft_reg<N1, 1>(a);
+    float2* wc = W + c0 + c;
+#pragma unroll
+    for (int n1 = 0; n1 < N1; ++n1) {
+      const int row = N2 * n1 + g;
+      if (row < J.n2out) wc[(size_t)row * ncols] = a[n1];
+    }
   }
 }
 
@@ -781,7 +852,7 @@ __global__ void __launch_bounds__(FAST_THREADS) k_cols_fast(const ConvJobDev* __
   float2* sm = reinterpret_cast<float2*>(smem_raw);
   const int jb = find_job_fast(jobs, njobs, blockIdx.x, 1);
   const ConvJobDev J = jobs[jb];
-  const int c0 = (blockIdx.x - J.col_off) * FAST_CW;
+  const int c0 = (blockIdx.x - J.col_off) * J.fcw;
 #define ILM_CALL_C(a, b) cols_body<a, b>(J, c0, sm)
   ILM_FAST_SWITCH(J.P2, ILM_CALL_C)
 #undef ILM_CALL_C
@@ -1081,11 +1152,14 @@ int conv_jobs_finalize(std::vector<ConvJobDev>& jobs, int dtype, ConvLaunch* L) 
       firows += (J.n2 + J.frb - 1) / J.frb;
       J.row_off = 0;
       J.col_off = cols;
-      cols += (H + 1 + FAST_CW - 1) / FAST_CW;
+      int n1c, n2c;
+      fast_len(J.P2, &n1c, &n2c);
+      J.fcw = col_cw(std::max(n1c, n2c));
+      cols += (H + 1 + J.fcw - 1) / J.fcw;
       const size_t tr = (size_t)J.frb * fast_transform_floats2(H) * sizeof(float2);
       smr = std::max(smr, tr);
       smi = std::max(smi, tr + (size_t)J.frb * (H + 1) * sizeof(float2));
-      smc = std::max(smc, (size_t)FAST_CW * fast_transform_floats2(J.P2) * sizeof(float2));
+      smc = std::max(smc, (size_t)J.fcw * col_stride(n1c, n2c) * sizeof(float2));
     }
     L->fast = 1;
     L->frows = frows;
@@ -1093,7 +1167,7 @@ int conv_jobs_finalize(std::vector<ConvJobDev>& jobs, int dtype, ConvLaunch* L) 
     L->fsm_irows = smi;
     L->rows = 0;
     L->cols = cols;
-    L->CW = FAST_CW;
+    L->CW = 0;  // per job (ConvJobDev::fcw)
     L->maxP1 = maxP1;
     L->maxP2 = maxP2;
     L->fsm_rows = smr;

@@ -165,6 +165,7 @@ struct ConvJobDev {
   // the whole n1 x n2 input.
   int has_box, ra, rb, ca, cb;
   int irow_off;        // register-FFT path: first inverse-row CTA of this job
+  int fcw;             // register-FFT path: spectral columns per column-pass CTA
   // optional field (n1 x n2) added to the result: out = add + scale * conv
   const void* add;
   // out_base != nullptr at launch: out = out_base + out_off bytes (lets a
@@ -297,6 +298,11 @@ struct CGParams {
 int launch_cg_batched(const CGParams* probs_dev, int nprob, int max_n, cudaStream_t st);
 
 // batched Schur builds (one launch over all problems of a batch)
+// Row stride (floats) of a batched n x n Schur complement: n rounded up to a
+// multiple of 4, so that every row starts on a 16-byte boundary (vector
+// loads in the CG); the padding columns hold zeros.
+__host__ __device__ inline int schur_ld(int n) { return (n + 3) & ~3; }
+
 struct SchurProbDev {
   int kind;      // ILM_SCHUR_RTLINVR (Dirichlet) or ILM_SCHUR_CLINVCT (Neumann)
   int n;         // points of this problem
@@ -330,6 +336,8 @@ int net_forward_packed(ilm_net_t n, int N, const float* feat, const int* sst, co
 int net_band(ilm_net_t n);
 int net_nfeat(ilm_net_t n);
 void cgff_params_set_deflation(void* dst, double gamma, const double* zdef, double uz);
+// per-problem timing of the cluster CG (3 u64 per problem: start ns, end ns, SM), nullptr: off
+void cgff_params_set_timing(void* dst, unsigned long long* tspan);
 void cgff_params_set_band(void* dst, const float* band, int band_k, const int* seg_start, const int* seg_len);
 void cgff_params_fill_csr(void* dst, const float* vhi, const float* vlo, const int* rowptr, const int* colidx,
                           const double* b, double* x, const double* x0, const double* w, int n, int maxiter,
@@ -342,8 +350,10 @@ struct BJBlockTask {
   float* out_lo;
 };
 int launch_block_inverse(const BJBlockTask* tasks_dev, int ntasks, int max_sz, cudaStream_t st);
+// variant: 0 auto, 1 row-distributed vectors, 2 replicated vectors (see ilm_cg.cu)
 int launch_cg_cluster(const void* params_dev, const int* order, int nprob, int* counter, int max_n, int nclusters,
-                      cudaStream_t st);
-int cg_cluster_count(int nprob, int max_n);
+                      cudaStream_t st, int variant = 0);
+int cg_cluster_count(int nprob, int max_n, int variant = 0);
+size_t cg_rep_smem(int max_n);  // shared memory of the replicated-vector CG per CTA
 
 }  // namespace ilm

@@ -483,8 +483,8 @@ __global__ void __launch_bounds__(256) k_schur_pairs_batched(int nprob, const Sc
   // row-major float-float pair: S[k][l] = hi + lo
   const double v = -w[P.poff + l] * total;
   const float vh = (float)v;
-  Shi[P.soff + (size_t)k * N + l] = vh;
-  Slo[P.soff + (size_t)k * N + l] = (float)(v - (double)vh);
+  Shi[P.soff + (size_t)k * schur_ld(N) + l] = vh;
+  Slo[P.soff + (size_t)k * schur_ld(N) + l] = (float)(v - (double)vh);
 }
 
 int schur_build_batched(int nprob, const SchurProbDev* probs_dev, int total_tiles, int Ptot, const int* pt2prob,

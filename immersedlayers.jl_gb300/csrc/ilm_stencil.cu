@@ -17,32 +17,62 @@ constexpr int BX = 32, BY = 8;
 
 inline dim3 grid2(int n1, int n2) { return dim3((n1 + BX - 1) / BX, (n2 + BY - 1) / BY); }
 
-// Edges{Primal} (u: NX x (NY-1), v: (NX-1) x NY) -> Nodes{Primal} (NX-1)x(NY-1)
-template <typename T>
-__global__ void k_div_edges(int NX, int NY, const T* __restrict__ u, const T* __restrict__ v, T* __restrict__ w, T sc) {
-  const int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
-  if (i >= NX - 1 || j >= NY - 1) return;
-  const T du = u[(size_t)j * NX + i + 1] - u[(size_t)j * NX + i];
-  const T dv = v[(size_t)(j + 1) * (NX - 1) + i] - v[(size_t)j * (NX - 1) + i];
-  w[(size_t)j * (NX - 1) + i] = (du + dv) * sc;
+// Edges{Primal} (u: NX x (NY-1), v: (NX-1) x NY) -> Nodes{Primal} (NX-1)x(NY-1),
+// RY rows per thread (rows j, j + BY, ...): every load of a thread is issued
+// before its first subtraction, so a thread keeps 4 RY loads in flight (one
+// row per thread left HBM idle between the loads of consecutive rows).
+template <typename T, int RY>
+__global__ void __launch_bounds__(BX* BY) k_div_edges_r(int NX, int NY, const T* __restrict__ u,
+                                                       const T* __restrict__ v, T* __restrict__ w, T sc) {
+  const int i = blockIdx.x * BX + threadIdx.x;
+  const int jb = blockIdx.y * BY * RY + threadIdx.y;
+  if (i >= NX - 1) return;
+  T u0[RY], u1[RY], v0[RY], v1[RY];
+#pragma unroll
+  for (int r = 0; r < RY; ++r) {
+    const int j = jb + r * BY;
+    if (j < NY - 1) {
+      u0[r] = u[(size_t)j * NX + i];
+      u1[r] = u[(size_t)j * NX + i + 1];
+      v0[r] = v[(size_t)j * (NX - 1) + i];
+      v1[r] = v[(size_t)(j + 1) * (NX - 1) + i];
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < RY; ++r) {
+    const int j = jb + r * BY;
+    if (j < NY - 1) w[(size_t)j * (NX - 1) + i] = ((u1[r] - u0[r]) + (v1[r] - v0[r])) * sc;
+  }
 }
 
-// Nodes{Primal} -> Edges{Primal}; faces adjacent to the ghost layer are 0
-template <typename T>
-__global__ void k_grad_u(int NX, int NY, const T* __restrict__ w, T* __restrict__ u, T sc) {
-  const int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
-  if (i >= NX || j >= NY - 1) return;
-  T r = (T)0;
-  if (i >= 1 && i <= NX - 2) r = (w[(size_t)j * (NX - 1) + i] - w[(size_t)j * (NX - 1) + i - 1]) * sc;
-  u[(size_t)j * NX + i] = r;
-}
-template <typename T>
-__global__ void k_grad_v(int NX, int NY, const T* __restrict__ w, T* __restrict__ v, T sc) {
-  const int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
-  if (i >= NX - 1 || j >= NY) return;
-  T r = (T)0;
-  if (j >= 1 && j <= NY - 2) r = (w[(size_t)j * (NX - 1) + i] - w[(size_t)(j - 1) * (NX - 1) + i]) * sc;
-  v[(size_t)j * (NX - 1) + i] = r;
+// Nodes{Primal} -> Edges{Primal} (both components), RY rows per thread; faces
+// adjacent to the ghost layer are 0
+template <typename T, int RY>
+__global__ void __launch_bounds__(BX* BY) k_grad_nodes_r(int NX, int NY, const T* __restrict__ w, T* __restrict__ u,
+                                                        T* __restrict__ v, T sc) {
+  const int i = blockIdx.x * BX + threadIdx.x;
+  const int jb = blockIdx.y * BY * RY + threadIdx.y;
+  if (i >= NX) return;
+  const int m = NX - 1;
+  T wc[RY], wl[RY], wd[RY];
+#pragma unroll
+  for (int r = 0; r < RY; ++r) {
+    const int j = jb + r * BY;
+    wc[r] = wl[r] = wd[r] = (T)0;
+    if (j < NY - 1 && i < m) wc[r] = w[(size_t)j * m + i];
+    if (j < NY - 1 && i >= 1 && i <= NX - 2) wl[r] = w[(size_t)j * m + i - 1];
+    if (j >= 1 && j <= NY - 2 && i < m) wd[r] = w[(size_t)(j - 1) * m + i];
+  }
+#pragma unroll
+  for (int r = 0; r < RY; ++r) {
+    const int j = jb + r * BY;
+    if (j < NY - 1) u[(size_t)j * NX + i] = (i >= 1 && i <= NX - 2) ? (wc[r] - wl[r]) * sc : (T)0;
+    if (j < NY && i < m) {
+      T rv = (T)0;
+      if (j >= 1 && j <= NY - 2) rv = (wc[r] - wd[r]) * sc;
+      v[(size_t)j * m + i] = rv;
+    }
+  }
 }
 
 // Nodes{Dual} (NX x NY) -> Edges{Primal}: u = s[j+1]-s[j], v = s[i]-s[i+1]
@@ -270,7 +300,9 @@ int st_div_edges(const ilm_grid_s* g, int dtype, const void* q, void* w, double 
   DISPATCH(dtype, {
     const T* u = static_cast<const T*>(q);
     const T* v = u + (size_t)NX * (NY - 1);
-    k_div_edges<T><<<grid2(NX - 1, NY - 1), dim3(BX, BY), 0, st>>>(NX, NY, u, v, static_cast<T*>(w), (T)scale);
+    constexpr int RY = 4;
+    const dim3 grid((NX - 1 + BX - 1) / BX, (NY - 1 + BY * RY - 1) / (BY * RY));
+    k_div_edges_r<T, RY><<<grid, dim3(BX, BY), 0, st>>>(NX, NY, u, v, static_cast<T*>(w), (T)scale);
   });
   ILM_CHECK_LAUNCH();
   return ILM_OK;
@@ -281,8 +313,9 @@ int st_grad_nodes(const ilm_grid_s* g, int dtype, const void* w, void* q, double
   DISPATCH(dtype, {
     T* u = static_cast<T*>(q);
     T* v = u + (size_t)NX * (NY - 1);
-    k_grad_u<T><<<grid2(NX, NY - 1), dim3(BX, BY), 0, st>>>(NX, NY, static_cast<const T*>(w), u, (T)scale);
-    k_grad_v<T><<<grid2(NX - 1, NY), dim3(BX, BY), 0, st>>>(NX, NY, static_cast<const T*>(w), v, (T)scale);
+    constexpr int RY = 4;
+    const dim3 grid((NX + BX - 1) / BX, (NY + BY * RY - 1) / (BY * RY));
+    k_grad_nodes_r<T, RY><<<grid, dim3(BX, BY), 0, st>>>(NX, NY, static_cast<const T*>(w), u, v, (T)scale);
   });
   ILM_CHECK_LAUNCH();
   return ILM_OK;

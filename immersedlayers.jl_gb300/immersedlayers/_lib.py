@@ -92,10 +92,15 @@ SIGNATURES = {
     "ilm_batch_destroy": [_VP],
     "ilm_batch_layout": [_VP, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)],
     "ilm_batch_solve": [_VP, _VP, _VP, _VP, _VP, _D, _I, _VP],
+    "ilm_batch_solve_graph": [_VP, _VP, _VP, _VP, _VP, _D, _I, _VP],
     "ilm_batch_info": [_VP, C.POINTER(_I), _DP],
     "ilm_batch_set_precond": [_VP, _I, _I],
     "ilm_batch_set_profiling": [_VP, _I],
     "ilm_batch_stage_times": [_VP, C.POINTER(C.c_float), C.POINTER(_I), C.POINTER(_I)],
+    "ilm_batch_cg_times": [_VP, _DP, _DP, C.POINTER(_I)],
+    "ilm_batch_set_cg_variant": [_VP, _I],
+    "ilm_batch_get_cg_variant": [_VP, C.POINTER(_I), C.POINTER(_I)],
+    "ilm_batch_autotune": [_VP, _VP, _VP, _VP, _VP, C.c_double, _I, _I, _VP, C.POINTER(_I), C.POINTER(C.c_float)],
     "ilm_batch_stats": [_VP, _DP],
     "ilm_net_create": [_I, _I, _I, _I, C.POINTER(_VP)],
     "ilm_net_destroy": [_VP],

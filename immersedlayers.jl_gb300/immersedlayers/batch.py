@@ -77,13 +77,15 @@ class BatchSolver:
         fm = np.concatenate([s.fminus for s in self.specs])
         return (torch.tensor(fp, dtype=self.dtype, device=device), torch.tensor(fm, dtype=self.dtype, device=device))
 
-    def solve(self, fplus, fminus, f_out=None, s_out=None, tol=1e-8, maxiter=5000, stream=None):
+    def solve(self, fplus, fminus, f_out=None, s_out=None, tol=1e-8, maxiter=5000, stream=None, graph=False):
+        """Solve every problem; graph=True replays a captured CUDA graph of
+        the launch sequence (needs a torch.cuda.Stream, not the default)."""
         if f_out is None:
             f_out = torch.empty(self.total_cells, dtype=self.dtype, device="cuda")
         if s_out is None:
             s_out = torch.empty(self.total_points, dtype=self.dtype, device="cuda")
-        L.call("ilm_batch_solve", self._h, _ptr(fplus), _ptr(fminus), _ptr(f_out), _ptr(s_out), float(tol),
-               int(maxiter), _stream_ptr(stream))
+        L.call("ilm_batch_solve_graph" if graph else "ilm_batch_solve", self._h, _ptr(fplus), _ptr(fminus),
+               _ptr(f_out), _ptr(s_out), float(tol), int(maxiter), _stream_ptr(stream))
         return f_out, s_out
 
     def info(self):
@@ -115,6 +117,41 @@ def _stage_times(self):
     nl = C.c_int()
     L.call("ilm_batch_stage_times", self._h, ms, C.byref(n), C.byref(nl))
     return list(ms[:n.value]), nl.value
+
+
+def _cg_times(self):
+    """Per-problem Schur CG (start us, end us, SM) of the last profiled solve."""
+    n = self.nprob
+    a, b, sm = (C.c_double * n)(), (C.c_double * n)(), (C.c_int * n)()
+    L.call("ilm_batch_cg_times", self._h, a, b, sm)
+    return np.array(a[:]), np.array(b[:]), np.array(sm[:])
+
+
+def _set_cg_variant(self, variant):
+    """Schur CG kernel: 0 default (= 1), 1 row-distributed vectors (256
+    threads per CTA), 2 replicated vectors (one cluster barrier per
+    iteration), 3 row-distributed with 128-thread CTAs."""
+    L.call("ilm_batch_set_cg_variant", self._h, int(variant))
+
+
+def _cg_variant(self):
+    v, nc = C.c_int(), C.c_int()
+    L.call("ilm_batch_get_cg_variant", self._h, C.byref(v), C.byref(nc))
+    return v.value, nc.value
+
+
+def _autotune(self, fplus, fminus, f_out=None, s_out=None, tol=1e-8, maxiter=5000, reps=2, stream=None):
+    """Time every Schur CG kernel on this data and keep the fastest; returns
+    (chosen variant, {variant: ms per solve})."""
+    if f_out is None:
+        f_out = torch.empty(self.total_cells, dtype=self.dtype, device="cuda")
+    if s_out is None:
+        s_out = torch.empty(self.total_points, dtype=self.dtype, device="cuda")
+    ch = C.c_int()
+    ms = (C.c_float * 3)()
+    L.call("ilm_batch_autotune", self._h, _ptr(fplus), _ptr(fminus), _ptr(f_out), _ptr(s_out), float(tol),
+           int(maxiter), int(reps), _stream_ptr(stream), C.byref(ch), ms)
+    return ch.value, {v + 1: float(ms[v]) for v in range(3) if ms[v] >= 0}
 
 
 def _stats(self):
@@ -177,3 +214,7 @@ BatchSolver.set_precond = _set_precond
 BatchSolver.set_profiling = _profiling
 BatchSolver.stage_times = _stage_times
 BatchSolver.stats = _stats
+BatchSolver.cg_times = _cg_times
+BatchSolver.set_cg_variant = _set_cg_variant
+BatchSolver.cg_variant = _cg_variant
+BatchSolver.autotune = _autotune

@@ -259,6 +259,13 @@ ILM_API int ilm_batch_layout(ilm_batch_t b, size_t* field_offsets, size_t* point
  * host<->device copies (capturable in a CUDA graph once tol/maxiter are set). */
 ILM_API int ilm_batch_solve(ilm_batch_t b, const void* fplus, const void* fminus, void* f_out, void* s_out,
                             double tol, int maxiter, ilm_stream_t stream);
+/* The same solve as one CUDA graph launch on `stream` (a created stream,
+ * not the legacy default stream): the first call for a set of buffers,
+ * tolerance, limit and CG configuration captures the launch sequence of
+ * ilm_batch_solve, later calls with the same arguments replay it.  A
+ * GB300-side launch path with no counterpart in the reference.             */
+ILM_API int ilm_batch_solve_graph(ilm_batch_t b, const void* fplus, const void* fminus, void* f_out, void* s_out,
+                                  double tol, int maxiter, ilm_stream_t stream);
 /* Preconditioner of the Schur CG for the following solves: mode 0 = none
  * (plain CG), 1 = block-Jacobi (inverses of the diagonal blocks of ~block_size
  * consecutive surface points, inverted in FP64 and applied in float-float
@@ -276,6 +283,27 @@ ILM_API int ilm_batch_set_precond(ilm_batch_t b, int mode, int block_size);
 ILM_API int ilm_batch_set_profiling(ilm_batch_t b, int enable);
 ILM_API int ilm_batch_stage_times(ilm_batch_t b, float* ms, int* nstages, int* launches);
 ILM_API int ilm_batch_stats(ilm_batch_t b, double* stats);
+/* Per-problem Schur CG timing of the last solve issued with profiling
+ * enabled: start and end (us, relative to the first problem taken) and the
+ * SM of the first CTA of the cluster that solved it.  A profiling helper
+ * with no counterpart in the reference.                                     */
+ILM_API int ilm_batch_cg_times(ilm_batch_t b, double* start_us, double* end_us, int* sm);
+/* Schur CG kernel of the batch: 0 default (= 1), 1 row-distributed
+ * vectors with 256-thread CTAs (three or four cluster barriers per
+ * iteration, FP64 work on the owned rows only), 2 replicated vectors (one
+ * cluster barrier per iteration, every vector operation in every CTA), 3
+ * row-distributed with 128-thread CTAs (twice the resident clusters).
+ * ilm_batch_autotune solves the given data with every variant (one untimed
+ * and `reps` timed solves each, CUDA events on `stream`), keeps the fastest
+ * and returns it in *chosen and the mean ms per solve of variants 1..3 in
+ * ms_per_variant[3] (-1: skipped); the outputs hold the last solve.
+ * Tuning helpers with no counterpart in the reference (the reference
+ * solves one problem at a time with a dense LU).                           */
+ILM_API int ilm_batch_set_cg_variant(ilm_batch_t b, int variant);
+ILM_API int ilm_batch_get_cg_variant(ilm_batch_t b, int* variant, int* nclusters);
+ILM_API int ilm_batch_autotune(ilm_batch_t b, const void* fplus, const void* fminus, void* f_out, void* s_out,
+                               double tol, int maxiter, int reps, ilm_stream_t stream, int* chosen,
+                               float* ms_per_variant);
 /* Per-problem CG iterations and FP64 relative residuals of the last solve. */
 ILM_API int ilm_batch_info(ilm_batch_t b, int* iterations, double* rel_residual);
 

@@ -102,3 +102,57 @@ def test_batch_large_grids_match_single_solves(cuda):
         got = bs.field(f, i).double()
         err = ((got - ref).abs().max() / ref.abs().max()).item()
         assert err < 1e-4, (i, sp.kind, sp.nx, err)
+
+
+@pytest.mark.parametrize("precond", ["none", "bjacobi"])
+def test_batch_cg_variants_agree(cuda, precond):
+    """The row-distributed (256- and 128-thread CTAs) and the
+    replicated-vector Schur CG kernels reach the tolerance and the same
+    solution; the autotuner keeps one of them."""
+    import torch
+    from immersedlayers import workloads as W
+    from immersedlayers.batch import BatchSolver
+    specs = W.batch_specs(8, sizes=(96, 128, 192))
+    bs = BatchSolver(specs, dtype=torch.float64)
+    if precond != "none":
+        bs.set_precond(precond, 32)
+    fp, fm = bs.surface_data()
+    out = {}
+    for v in (1, 2, 3):
+        bs.set_cg_variant(v)
+        f, s = bs.solve(fp, fm, tol=1e-10, maxiter=20000)
+        its, rr = bs.info()
+        assert (rr <= 1e-10).all(), (v, its, rr)
+        out[v] = f.clone()
+    assert rel(out[2].cpu().numpy(), out[1].cpu().numpy()) < 1e-8
+    assert rel(out[3].cpu().numpy(), out[1].cpu().numpy()) < 1e-8
+    chosen, ms = bs.autotune(fp, fm, tol=1e-10, maxiter=20000, reps=1)
+    assert chosen in (1, 2, 3) and chosen in ms and bs.cg_variant()[0] == chosen
+
+
+def test_batch_graph_replay_matches_solve(cuda):
+    """The captured CUDA graph of a batch solve gives bit-identical fields
+    to the launch-by-launch solve, on its first (capture) and later
+    (replay) calls and after a change of preconditioner (re-capture)."""
+    import torch
+    from immersedlayers import workloads as W
+    from immersedlayers.batch import BatchSolver
+    specs = W.batch_specs(6, sizes=(64, 96, 128))
+    bs = BatchSolver(specs, dtype=torch.float32)
+    fp, fm = bs.surface_data()
+    st = torch.cuda.Stream()
+    f0, s0 = bs.solve(fp, fm, tol=1e-8, stream=st)
+    f1 = torch.empty_like(f0)
+    s1 = torch.empty_like(s0)
+    for _ in range(2):
+        f1.zero_()
+        bs.solve(fp, fm, f1, s1, tol=1e-8, stream=st, graph=True)
+        st.synchronize()
+        assert torch.equal(f1, f0) and torch.equal(s1, s0)
+    bs.set_precond("bjacobi", 32)
+    f2, s2 = bs.solve(fp, fm, tol=1e-8, stream=st)
+    bs.solve(fp, fm, f1, s1, tol=1e-8, stream=st, graph=True)
+    st.synchronize()
+    assert torch.equal(f1, f2) and torch.equal(s1, s2)
+    its, rr = bs.info()
+    assert (rr <= 1e-8).all()
