@@ -28,6 +28,8 @@ namespace ilm {
 struct BScatterTask {
   int n1, n2, ntx, tile0;
   int tx0, ty0, ntxb, pad_;
+  int xa, xb, ya, yb, fill0, nne;  // box cells [xa, xb) x [ya, yb), first zero-fill block, occupied tiles
+  const int* ne;                    // the box's tiles that hold candidate points (tile ids of the problem)
   const int* tptr;
   const int* tpts;
   const int* bx;
@@ -95,19 +97,32 @@ __device__ __forceinline__ T bcoef(int code, const T* nx, const T* ny, int k) {
   return (T)0;
 }
 
-// Deterministic scatter: one thread per output cell of a 32 x 8 tile; the
-// tile's candidate points (index order) are staged in shared memory 256 at
-// a time, one point per thread, then every thread sums them in that order.
+// Zero fill of every task's box, one block per box row (the scatter below
+// then visits only the tiles that hold points)
 template <typename T>
-__global__ void __launch_bounds__(SB_X* SB_Y) k_bscatter(const BScatterTask* __restrict__ tasks, int ntasks) {
+__global__ void __launch_bounds__(256)
+    k_bfill(const BScatterTask* __restrict__ tasks, int ntasks, const int* __restrict__ bmap) {
+  const int ti = bmap[blockIdx.x];
+  const BScatterTask& S = tasks[ti];
+  const int j = S.ya + (int)blockIdx.x - S.fill0;
+  T* row = static_cast<T*>(S.out) + (size_t)j * S.n1;
+  for (int i = S.xa + threadIdx.x; i < S.xb; i += blockDim.x) row[i] = (T)0;
+}
+
+// Deterministic scatter: one thread per output cell of an occupied 32 x 8
+// tile; the tile's candidate points (index order) are staged in shared
+// memory 256 at a time, one point per thread, then every thread sums them in
+// that order.
+template <typename T>
+__global__ void __launch_bounds__(SB_X* SB_Y)
+    k_bscatter(const BScatterTask* __restrict__ tasks, int ntasks, const int* __restrict__ bmap) {
   constexpr int NB = SB_X * SB_Y;
   __shared__ int s_bx[NB], s_by[NB];
   __shared__ T s_amp[NB], s_wx[NB * NTAP], s_wy[NB * NTAP];
-  const int ti = find_task(tasks, ntasks, (int)blockIdx.x, &BScatterTask::tile0);
+  const int ti = bmap[blockIdx.x];
   const BScatterTask& S = tasks[ti];
-  const int t = blockIdx.x - S.tile0;
-  const int tx = S.tx0 + t % S.ntxb, ty = S.ty0 + t / S.ntxb;
-  const int tile = ty * S.ntx + tx;
+  const int tile = S.ne[blockIdx.x - S.tile0];
+  const int tx = tile % S.ntx, ty = tile / S.ntx;
   const int i = tx * SB_X + threadIdx.x;
   const int j = ty * SB_Y + threadIdx.y;
   const int tid = threadIdx.y * SB_X + threadIdx.x;
@@ -146,8 +161,8 @@ __global__ void __launch_bounds__(SB_X* SB_Y) k_bscatter(const BScatterTask* __r
 
 // Edges{Primal} -> Nodes{Primal} divergence
 template <typename T>
-__global__ void k_bdiv(const BStencilTask* __restrict__ tasks, int ntasks) {
-  const int ti = find_task(tasks, ntasks, (int)blockIdx.x, &BStencilTask::blk0);
+__global__ void k_bdiv(const BStencilTask* __restrict__ tasks, int ntasks, const int* __restrict__ bmap) {
+  const int ti = bmap[blockIdx.x];
   const BStencilTask& S = tasks[ti];
   const int NX = S.NX, NY = S.NY;
   const int nbx = (S.bw + SB_X - 1) / SB_X;
@@ -242,7 +257,10 @@ struct ilm_batch_s {
   // tasks
   DevBuf scatA, divA, gathA, scatB, divB, convA, convB, schurP;
   int n_scatA = 0, n_divA = 0, n_gathA = 0, n_scatB = 0, n_divB = 0;
-  int blk_scatA = 0, blk_divA = 0, blk_scatB = 0, blk_divB = 0;
+  int blk_scatA = 0, blk_divA = 0, blk_scatB = 0, blk_divB = 0, blk_fillA = 0, blk_fillB = 0;
+  DevBuf scat_ne;  // occupied tiles of the scatter tasks
+  // task of every block of the batched launches (no per-block search)
+  DevBuf mfillA, mscatA, mdivA, mfillB, mscatB, mdivB, mconv[3];
   int n_conv = 0;
   size_t box_cells = 0;  // cells of all source boxes
   ConvLaunch convL;
@@ -641,13 +659,20 @@ int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* 
   }
   ILM_TRY(conv_jobs_finalize(jobsA, dtype, &B->convL));
   ILM_TRY(conv_jobs_finalize(jobsB, dtype, &B->convL));
+  if (B->convL.fast) {  // CTA -> job maps (the two job tables share their geometry)
+    ILM_TRY(up(B->mconv[0], B->convL.mrows));
+    ILM_TRY(up(B->mconv[1], B->convL.mcols));
+    ILM_TRY(up(B->mconv[2], B->convL.mirows));
+    for (int k = 0; k < 3; ++k) B->convL.dmap[k] = B->mconv[k].as<int>();
+  }
   B->n_conv = nprob;
   ILM_TRY(up(B->convA, jobsA));
   ILM_TRY(up(B->convB, jobsB));
 
   // ---- tasks ---------------------------------------------------------------
   auto ptr_at = [&](const DevBuf& b, size_t off) { return (void*)(static_cast<unsigned char*>(b.p) + off * e); };
-  auto scat = [&](int p, int pc, const DevBuf& in, int coef, void* outp, int& tiles) {
+  std::vector<int> nelist;  // occupied tiles of every scatter task, packed
+  auto scat = [&](int p, int pc, const DevBuf& in, int coef, void* outp, int& tiles, int& fills) {
     BScatterTask T;
     memset(&T, 0, sizeof(T));
     ilm_grid_s g{probs[p].nx, probs[p].ny, probs[p].h, probs[p].i0x, probs[p].i0y};
@@ -666,8 +691,23 @@ int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* 
     T.ty0 = ya / SB_Y;
     T.ntxb = (xb - 1) / SB_X - T.tx0 + 1;
     const int ntyb = (yb - 1) / SB_Y - T.ty0 + 1;
+    T.xa = xa;
+    T.xb = xb;
+    T.ya = ya;
+    T.yb = yb;
+    T.fill0 = fills;
+    fills += yb - ya;
+    // occupied tiles of the box (ids into the problem's tile grid), packed
+    const std::vector<int>& tp = Wall[p].tptr[pc];
+    T.pad_ = (int)nelist.size();  // offset into the packed list, resolved after upload
+    for (int ty = T.ty0; ty < T.ty0 + ntyb; ++ty)
+      for (int tx = T.tx0; tx < T.tx0 + T.ntxb; ++tx) {
+        const int t = ty * T.ntx + tx;
+        if (tp[t + 1] > tp[t]) nelist.push_back(t);
+      }
+    T.nne = (int)nelist.size() - T.pad_;
     T.tile0 = tiles;
-    tiles += T.ntxb * ntyb;
+    tiles += T.nne;
     T.tptr = B->tptr[pc].as<int>() + tpo[pc][p];
     T.tpts = B->tpts[pc].as<int>() + tso[pc][p];
     T.bx = B->bx[dx].as<int>() + o;
@@ -723,11 +763,12 @@ int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* 
   std::vector<BStencilTask> dA, dB;
   std::vector<BGatherTask> hA;
   int tA = 0, tB = 0, bdA = 0, bdB = 0, ptsA = 0;
+  int fillA = 0, fillB = 0;
   for (int p = 0; p < nprob; ++p) {
     const int nx_ = probs[p].nx, ny_ = probs[p].ny;
     if (probs[p].kind == 0) {  // Dirichlet: f* = L^-1 D_s [f]; correction R s
-      sA.push_back(scat(p, PC_U, B->jump, CF_NX, edge_u(p), tA));
-      sA.push_back(scat(p, PC_V, B->jump, CF_NY, edge_v(p), tA));
+      sA.push_back(scat(p, PC_U, B->jump, CF_NX, edge_u(p), tA, fillA));
+      sA.push_back(scat(p, PC_V, B->jump, CF_NY, edge_v(p), tA, fillA));
       dA.push_back(stencil(p, edge_u(p), field(B->fstar, p), bdA));
       BGatherTask G = gath(p, ptsA);
       G.nterms = 1;
@@ -739,9 +780,9 @@ int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* 
       G.coef[0] = CF_ONE;
       G.scale = 1.0;
       hA.push_back(G);
-      sB.push_back(scat(p, PC_P, B->s, CF_ONE, field(B->corr, p), tB));
+      sB.push_back(scat(p, PC_P, B->s, CF_ONE, field(B->corr, p), tB, fillB));
     } else {  // Neumann: f* = L^-1 R [vn]; rhs from G_s f* (gradient fused into the gather); correction D_s [phi]
-      sA.push_back(scat(p, PC_P, B->jump, CF_ONE, field(B->fstar, p), tA));
+      sA.push_back(scat(p, PC_P, B->jump, CF_ONE, field(B->fstar, p), tA, fillA));
       BGatherTask G = gath(p, ptsA);
       G.nterms = 2;
       G.arr[0] = field(B->fstar, p);
@@ -760,8 +801,8 @@ int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* 
       G.coef[1] = CF_NY;
       G.scale = 1.0 / probs[p].h;
       hA.push_back(G);
-      sB.push_back(scat(p, PC_U, B->s, CF_NX, edge_u(p), tB));
-      sB.push_back(scat(p, PC_V, B->s, CF_NY, edge_v(p), tB));
+      sB.push_back(scat(p, PC_U, B->s, CF_NX, edge_u(p), tB, fillB));
+      sB.push_back(scat(p, PC_V, B->s, CF_NY, edge_v(p), tB, fillB));
       dB.push_back(stencil(p, edge_u(p), field(B->corr, p), bdB));
     }
   }
@@ -774,6 +815,37 @@ int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* 
   B->n_divB = (int)dB.size();
   B->blk_divB = bdB;
   B->n_gathA = (int)hA.size();
+  ILM_TRY(up(B->scat_ne, nelist));
+  for (auto& T : sA) T.ne = B->scat_ne.as<int>() + T.pad_;
+  for (auto& T : sB) T.ne = B->scat_ne.as<int>() + T.pad_;
+  B->blk_fillA = fillA;
+  B->blk_fillB = fillB;
+  {
+    // block -> task maps
+    auto mk_scat = [&](const std::vector<BScatterTask>& v, int nblk, bool fill) {
+      std::vector<int> m(std::max(nblk, 1), 0);
+      for (size_t t = 0; t < v.size(); ++t) {
+        const int b0 = fill ? v[t].fill0 : v[t].tile0;
+        const int nb = fill ? v[t].yb - v[t].ya : v[t].nne;
+        for (int k = 0; k < nb; ++k) m[b0 + k] = (int)t;
+      }
+      return m;
+    };
+    auto mk_div = [&](const std::vector<BStencilTask>& v, int nblk) {
+      std::vector<int> m(std::max(nblk, 1), 0);
+      for (size_t t = 0; t < v.size(); ++t) {
+        const int nb = ((v[t].bw + SB_X - 1) / SB_X) * ((v[t].bh + SB_Y - 1) / SB_Y);
+        for (int k = 0; k < nb; ++k) m[v[t].blk0 + k] = (int)t;
+      }
+      return m;
+    };
+    ILM_TRY(up(B->mfillA, mk_scat(sA, fillA, true)));
+    ILM_TRY(up(B->mscatA, mk_scat(sA, tA, false)));
+    ILM_TRY(up(B->mfillB, mk_scat(sB, fillB, true)));
+    ILM_TRY(up(B->mscatB, mk_scat(sB, tB, false)));
+    ILM_TRY(up(B->mdivA, mk_div(dA, bdA)));
+    ILM_TRY(up(B->mdivB, mk_div(dB, bdB)));
+  }
   ILM_TRY(up(B->scatA, sA));
   ILM_TRY(up(B->scatB, sB));
   ILM_TRY(up(B->divA, dA));
@@ -852,11 +924,14 @@ int ilm_batch_solve(ilm_batch_t b, const void* fplus, const void* fminus, void* 
     ILM_CHECK_LAUNCH();
     b->launches++;
     MARK();  // 1: surface data jump/average
-    if (b->n_scatA) k_bscatter<T><<<b->blk_scatA, dim3(SB_X, SB_Y), 0, st>>>(b->scatA.as<BScatterTask>(), b->n_scatA);
+    if (b->blk_fillA) k_bfill<T><<<b->blk_fillA, 256, 0, st>>>(b->scatA.as<BScatterTask>(), b->n_scatA, b->mfillA.as<int>());
     ILM_CHECK_LAUNCH();
-    b->launches += b->n_scatA ? 1 : 0;
+    if (b->blk_scatA) k_bscatter<T><<<b->blk_scatA, dim3(SB_X, SB_Y), 0, st>>>(b->scatA.as<BScatterTask>(), b->n_scatA,
+                                                                    b->mscatA.as<int>());
+    ILM_CHECK_LAUNCH();
+    b->launches += (b->blk_fillA ? 1 : 0) + (b->blk_scatA ? 1 : 0);
     MARK();  // 2: DDF scatter (double layer / single layer)
-    if (b->n_divA) k_bdiv<T><<<b->blk_divA, dim3(SB_X, SB_Y), 0, st>>>(b->divA.as<BStencilTask>(), b->n_divA);
+    if (b->n_divA) k_bdiv<T><<<b->blk_divA, dim3(SB_X, SB_Y), 0, st>>>(b->divA.as<BStencilTask>(), b->n_divA, b->mdivA.as<int>());
     ILM_CHECK_LAUNCH();
     b->launches += b->n_divA ? 1 : 0;
     MARK();  // 3: divergence stencil
@@ -881,11 +956,14 @@ int ilm_batch_solve(ilm_batch_t b, const void* fplus, const void* fminus, void* 
   b->launches += 1;
   MARK();  // 7: convert
   BDISPATCH(dt, {
-    if (b->n_scatB) k_bscatter<T><<<b->blk_scatB, dim3(SB_X, SB_Y), 0, st>>>(b->scatB.as<BScatterTask>(), b->n_scatB);
+    if (b->blk_fillB) k_bfill<T><<<b->blk_fillB, 256, 0, st>>>(b->scatB.as<BScatterTask>(), b->n_scatB, b->mfillB.as<int>());
     ILM_CHECK_LAUNCH();
-    b->launches += b->n_scatB ? 1 : 0;
+    if (b->blk_scatB) k_bscatter<T><<<b->blk_scatB, dim3(SB_X, SB_Y), 0, st>>>(b->scatB.as<BScatterTask>(), b->n_scatB,
+                                                                    b->mscatB.as<int>());
+    ILM_CHECK_LAUNCH();
+    b->launches += (b->blk_fillB ? 1 : 0) + (b->blk_scatB ? 1 : 0);
     MARK();  // 8: DDF scatter (correction)
-    if (b->n_divB) k_bdiv<T><<<b->blk_divB, dim3(SB_X, SB_Y), 0, st>>>(b->divB.as<BStencilTask>(), b->n_divB);
+    if (b->n_divB) k_bdiv<T><<<b->blk_divB, dim3(SB_X, SB_Y), 0, st>>>(b->divB.as<BStencilTask>(), b->n_divB, b->mdivB.as<int>());
     ILM_CHECK_LAUNCH();
     b->launches += b->n_divB ? 1 : 0;
     MARK();  // 9: divergence stencil

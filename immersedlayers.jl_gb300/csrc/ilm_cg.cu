@@ -455,7 +455,10 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(CGR_THREADS
     }
     for (int j = threadIdx.x; j < n; j += blockDim.x) p[j] = pre ? z[j] : r[j];
     const double bnorm = sqrt(bb);
-    const double thr = pr.tol * bnorm;
+    // with the net-charge mode deflated, CG converges on S' and the reported
+    // residual is the true one of S after the Sherman-Morrison correction,
+    // which adds the (small) error of z: aim at half the tolerance on S'
+    const double thr = (pr.zdef != nullptr && pr.gamma != 0.0 ? 0.5 : 1.0) * pr.tol * bnorm;
     const double thr2 = thr * thr;
     double rlast = bb;  // latest squared residual norm (recursive or true)
     int it = 0;
@@ -1001,7 +1004,10 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(NT, MINB)
       __syncthreads();
     }
     for (int i = threadIdx.x; i < nr; i += blockDim.x) ps[i] = pre ? zs[i] : rs[i];
-    const double thr = pr.tol * bnorm;
+    // with the net-charge mode deflated, CG converges on S' and the reported
+    // residual is the true one of S after the Sherman-Morrison correction,
+    // which adds the (small) error of z: aim at half the tolerance on S'
+    const double thr = (pr.zdef != nullptr && pr.gamma != 0.0 ? 0.5 : 1.0) * pr.tol * bnorm;
     const double thr2 = thr * thr;
     double rlast = bnorm * bnorm;
     int it = 0;

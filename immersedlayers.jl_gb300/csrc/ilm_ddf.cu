@@ -162,6 +162,12 @@ int cache_build_windows(ilm_cache_s* c) {
     tl.nty = W.nty[pc];
     ILM_TRY(upload(tl.ptr, W.tptr[pc].data(), W.tptr[pc].size()));
     ILM_TRY(upload(tl.pts, W.tpts[pc].data(), W.tpts[pc].size()));
+    std::vector<int> ne;
+    for (int t = 0; t < tl.ntx * tl.nty; ++t)
+      if (W.tptr[pc][t + 1] > W.tptr[pc][t]) ne.push_back(t);
+    tl.nne = (int)ne.size();
+    if (ne.empty()) ne.push_back(0);  // keep a valid (unused) upload
+    ILM_TRY(upload(tl.ne, ne.data(), ne.size()));
   }
   return ILM_OK;
 }
@@ -182,30 +188,59 @@ __device__ __forceinline__ T coef_val(int code, const T* __restrict__ nx, const 
   return (T)0;
 }
 
+// Deterministic scatter over the tiles that hold candidate points (the rest
+// of the output was zero-filled): one thread per cell of a 32 x 8 tile; the
+// tile's candidates (index order) are staged in shared memory 256 at a time,
+// one point per thread, then every thread sums them in that order.
 template <typename T>
 __global__ void __launch_bounds__(TILE_X* TILE_Y)
-k_scatter(int n1, int n2, int ntx, const int* __restrict__ tptr, const int* __restrict__ tpts,
-          const int* __restrict__ bx, const int* __restrict__ by, const T* __restrict__ wx,
-          const T* __restrict__ wy, const T* __restrict__ wsc, const T* __restrict__ nx,
+k_scatter(int n1, int n2, int ntx, const int* __restrict__ ne, const int* __restrict__ tptr,
+          const int* __restrict__ tpts, const int* __restrict__ bx, const int* __restrict__ by,
+          const T* __restrict__ wx, const T* __restrict__ wy, const T* __restrict__ wsc, const T* __restrict__ nx,
           const T* __restrict__ ny, const T* __restrict__ in1, int c1, const T* __restrict__ in2, int c2,
           T* __restrict__ out) {
-  const int tx = blockIdx.x % ntx, ty = blockIdx.x / ntx;
+  constexpr int NB = TILE_X * TILE_Y;
+  __shared__ int s_bx[NB], s_by[NB];
+  __shared__ T s_amp[NB], s_wx[NB * NTAP], s_wy[NB * NTAP];
+  const int t = ne[blockIdx.x];
+  const int tx = t % ntx, ty = t / ntx;
   const int i = tx * TILE_X + threadIdx.x;
   const int j = ty * TILE_Y + threadIdx.y;
-  const int t = blockIdx.x;
+  const int tid = threadIdx.y * TILE_X + threadIdx.x;
   const int p0 = tptr[t], p1 = tptr[t + 1];
   T acc = (T)0;
-  for (int p = p0; p < p1; ++p) {
-    const int k = tpts[p];
-    const int di = i - bx[k];
-    const int dj = j - by[k];
-    if ((unsigned)di < (unsigned)NTAP && (unsigned)dj < (unsigned)NTAP) {
+  for (int c0 = p0; c0 < p1; c0 += NB) {
+    const int nc = min(NB, p1 - c0);
+    if (tid < nc) {
+      const int k = tpts[c0 + tid];
       T g = coef_val<T>(c1, nx, ny, k) * in1[k];
       if (in2) g += coef_val<T>(c2, nx, ny, k) * in2[k];
-      acc += wsc[k] * g * wx[k * NTAP + di] * wy[k * NTAP + dj];
+      s_bx[tid] = bx[k];
+      s_by[tid] = by[k];
+      s_amp[tid] = wsc[k] * g;
+#pragma unroll
+      for (int q = 0; q < NTAP; ++q) {
+        s_wx[tid * NTAP + q] = wx[k * NTAP + q];
+        s_wy[tid * NTAP + q] = wy[k * NTAP + q];
+      }
     }
+    __syncthreads();
+    for (int q = 0; q < nc; ++q) {
+      const int di = i - s_bx[q];
+      const int dj = j - s_by[q];
+      if ((unsigned)di < (unsigned)NTAP && (unsigned)dj < (unsigned)NTAP)
+        acc += s_amp[q] * s_wx[q * NTAP + di] * s_wy[q * NTAP + dj];
+    }
+    __syncthreads();
   }
   if (i < n1 && j < n2) out[(size_t)j * n1 + i] = acc;
+}
+
+__global__ void k_fill_zero(float4* __restrict__ p4, size_t n4, unsigned char* __restrict__ tail, int ntail) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n4; k += stride)
+    p4[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (blockIdx.x == 0 && (int)threadIdx.x < ntail) tail[threadIdx.x] = 0;
 }
 
 struct GTermDev {
@@ -256,21 +291,43 @@ __global__ void k_gather(int N, const GTermDev* __restrict__ terms_unused, GTerm
   else out[k] = total;
 }
 
+int fill_zero(void* out, size_t bytes, cudaStream_t st) {
+  if (bytes == 0) return ILM_OK;
+  // vector stores from the first 16-byte boundary, bytes before / after it by the tail path
+  const uintptr_t a = reinterpret_cast<uintptr_t>(out);
+  if (a % 16 != 0) {
+    ILM_CHECK_CUDA(cudaMemsetAsync(out, 0, bytes, st));
+    return ILM_OK;
+  }
+  const size_t n4 = bytes / 16;
+  const int ntail = (int)(bytes - 16 * n4);
+  int dev = 0, nsm = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const size_t want = (n4 + 255) / 256;
+  const int grid = (int)std::max<size_t>(1, std::min<size_t>(want, (size_t)nsm * 8));
+  k_fill_zero<<<grid, 256, 0, st>>>(static_cast<float4*>(out), n4, static_cast<unsigned char*>(out) + 16 * n4, ntail);
+  ILM_CHECK_LAUNCH();
+  return ILM_OK;
+}
+
 int launch_scatter(ilm_cache_s* c, int pc, const void* in1, int coef1, const void* in2, int coef2, void* out,
                    cudaStream_t st) {
   const Shape2 sh = c->grid.shape(pc);
   const TileList& tl = c->tiles[pc];
   const int dx = pc_dx(pc), dy = pc_dy(pc);
   dim3 blk(TILE_X, TILE_Y);
-  const int nb = tl.ntx * tl.nty;
+  ILM_TRY(fill_zero(out, sh.numel() * (c->dtype == ILM_F64 ? 8 : 4), st));
+  const int nb = tl.nne;
+  if (nb == 0) return ILM_OK;
   if (c->dtype == ILM_F64) {
-    k_scatter<double><<<nb, blk, 0, st>>>(sh.n1, sh.n2, tl.ntx, tl.ptr.as<int>(), tl.pts.as<int>(), c->bx[dx].as<int>(),
+    k_scatter<double><<<nb, blk, 0, st>>>(sh.n1, sh.n2, tl.ntx, tl.ne.as<int>(), tl.ptr.as<int>(), tl.pts.as<int>(), c->bx[dx].as<int>(),
                                           c->by[dy].as<int>(), c->wx[dx].as<double>(), c->wy[dy].as<double>(),
                                           c->wscale.as<double>(), c->nx.as<double>(), c->ny.as<double>(),
                                           static_cast<const double*>(in1), coef1, static_cast<const double*>(in2),
                                           coef2, static_cast<double*>(out));
   } else {
-    k_scatter<float><<<nb, blk, 0, st>>>(sh.n1, sh.n2, tl.ntx, tl.ptr.as<int>(), tl.pts.as<int>(), c->bx[dx].as<int>(),
+    k_scatter<float><<<nb, blk, 0, st>>>(sh.n1, sh.n2, tl.ntx, tl.ne.as<int>(), tl.ptr.as<int>(), tl.pts.as<int>(), c->bx[dx].as<int>(),
                                          c->by[dy].as<int>(), c->wx[dx].as<float>(), c->wy[dy].as<float>(),
                                          c->wscale.as<float>(), c->nx.as<float>(), c->ny.as<float>(),
                                          static_cast<const float*>(in1), coef1, static_cast<const float*>(in2), coef2,

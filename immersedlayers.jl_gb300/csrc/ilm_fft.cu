@@ -820,10 +820,11 @@ __device__ __forceinline__ int find_job_fast(const ConvJobDev* jobs, int njobs, 
   return lo;
 }
 
-__global__ void __launch_bounds__(FAST_THREADS) k_rfft_rows_fast(const ConvJobDev* __restrict__ jobs, int njobs) {
+__global__ void __launch_bounds__(FAST_THREADS)
+    k_rfft_rows_fast(const ConvJobDev* __restrict__ jobs, int njobs, const int* __restrict__ bmap) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* sm = reinterpret_cast<float2*>(smem_raw);
-  const int jb = find_job_fast(jobs, njobs, blockIdx.x, 0);
+  const int jb = bmap ? bmap[blockIdx.x] : find_job_fast(jobs, njobs, blockIdx.x, 0);
   const ConvJobDev J = jobs[jb];
   const int ra = J.has_box ? J.ra : 0, rb = J.has_box ? J.rb : J.n2;
   const int r0 = ra + (blockIdx.x - J.frow_off) * J.frb;
@@ -833,10 +834,10 @@ __global__ void __launch_bounds__(FAST_THREADS) k_rfft_rows_fast(const ConvJobDe
 }
 
 __global__ void __launch_bounds__(FAST_THREADS)
-    k_irfft_rows_fast(const ConvJobDev* __restrict__ jobs, int njobs, void* out_base) {
+    k_irfft_rows_fast(const ConvJobDev* __restrict__ jobs, int njobs, void* out_base, const int* __restrict__ bmap) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* sm = reinterpret_cast<float2*>(smem_raw);
-  const int jb = find_job_fast(jobs, njobs, blockIdx.x, 2);
+  const int jb = bmap ? bmap[blockIdx.x] : find_job_fast(jobs, njobs, blockIdx.x, 2);
   const ConvJobDev J = jobs[jb];
   const int r0 = (blockIdx.x - J.irow_off) * J.frb;
   // layout: the transforms' padded matrices (frb x N1 (N2 + 1)), then the
@@ -847,10 +848,11 @@ __global__ void __launch_bounds__(FAST_THREADS)
 #undef ILM_CALL_IRF
 }
 
-__global__ void __launch_bounds__(FAST_THREADS) k_cols_fast(const ConvJobDev* __restrict__ jobs, int njobs) {
+__global__ void __launch_bounds__(FAST_THREADS)
+    k_cols_fast(const ConvJobDev* __restrict__ jobs, int njobs, const int* __restrict__ bmap) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* sm = reinterpret_cast<float2*>(smem_raw);
-  const int jb = find_job_fast(jobs, njobs, blockIdx.x, 1);
+  const int jb = bmap ? bmap[blockIdx.x] : find_job_fast(jobs, njobs, blockIdx.x, 1);
   const ConvJobDev J = jobs[jb];
   const int c0 = (blockIdx.x - J.col_off) * J.fcw;
 #define ILM_CALL_C(a, b) cols_body<a, b>(J, c0, sm)
@@ -924,11 +926,11 @@ int launch_prepared(const ConvJobDev* jd, int nj, const ConvLaunch& L, int mode,
     ILM_CHECK_CUDA(cudaFuncSetAttribute(k_cols_fast, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.fsm_cols));
     ILM_CHECK_CUDA(cudaFuncSetAttribute(k_irfft_rows_fast, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)L.fsm_irows));
-    if (L.frows > 0) k_rfft_rows_fast<<<L.frows, FAST_THREADS, L.fsm_rows, st>>>(jd, nj);
+    if (L.frows > 0) k_rfft_rows_fast<<<L.frows, FAST_THREADS, L.fsm_rows, st>>>(jd, nj, L.dmap[0]);
     ILM_CHECK_LAUNCH();
-    k_cols_fast<<<L.cols, FAST_THREADS, L.fsm_cols, st>>>(jd, nj);
+    k_cols_fast<<<L.cols, FAST_THREADS, L.fsm_cols, st>>>(jd, nj, L.dmap[1]);
     ILM_CHECK_LAUNCH();
-    k_irfft_rows_fast<<<L.firows, FAST_THREADS, L.fsm_irows, st>>>(jd, nj, out_base);
+    k_irfft_rows_fast<<<L.firows, FAST_THREADS, L.fsm_irows, st>>>(jd, nj, out_base, L.dmap[2]);
     ILM_CHECK_LAUNCH();
     return ILM_OK;
   }
@@ -1142,7 +1144,11 @@ int conv_jobs_finalize(std::vector<ConvJobDev>& jobs, int dtype, ConvLaunch* L) 
     ILM_TRY(ensure_fast_tables());
     size_t smr = 0, smc = 0, smi = 0;
     int frows = 0, firows = 0;
-    for (auto& J : jobs) {
+    L->mrows.clear();
+    L->mcols.clear();
+    L->mirows.clear();
+    for (size_t jn = 0; jn < jobs.size(); ++jn) {
+      ConvJobDev& J = jobs[jn];
       const int H = J.P1 / 2;
       J.frb = FAST_THREADS / fast_group(H);
       J.frow_off = frows;
@@ -1156,6 +1162,9 @@ int conv_jobs_finalize(std::vector<ConvJobDev>& jobs, int dtype, ConvLaunch* L) 
       fast_len(J.P2, &n1c, &n2c);
       J.fcw = col_cw(std::max(n1c, n2c));
       cols += (H + 1 + J.fcw - 1) / J.fcw;
+      L->mrows.resize(frows, (int)jn);
+      L->mcols.resize(cols, (int)jn);
+      L->mirows.resize(firows, (int)jn);
       const size_t tr = (size_t)J.frb * fast_transform_floats2(H) * sizeof(float2);
       smr = std::max(smr, tr);
       smi = std::max(smi, tr + (size_t)J.frb * (H + 1) * sizeof(float2));

@@ -133,8 +133,12 @@ struct PointWin {
 struct TileList {
   DevBuf ptr;   // int [ntiles+1]
   DevBuf pts;   // int [nnz]
-  int ntx = 0, nty = 0;
+  DevBuf ne;    // int [nne]: the tiles with at least one candidate point
+  int ntx = 0, nty = 0, nne = 0;
 };
+// out[0, n) = 0 (16-byte stores where aligned); the scatters fill their
+// output with it and then visit only the tiles that hold points
+int fill_zero(void* out, size_t bytes, cudaStream_t st);
 
 // ---------------------------------------------------------------------------
 // FFT convolution (inverse Laplacian)
@@ -176,6 +180,11 @@ struct ConvLaunch {
   int rows = 0, cols = 0, CW = 1, maxP1 = 0, maxP2 = 0;
   int fast = 0, frows = 0, firows = 0;  // register four-step FFT path (FP32): forward / inverse row CTAs
   size_t fsm_rows = 0, fsm_cols = 0, fsm_irows = 0;  // its dynamic shared memory per CTA
+  // register-FFT path: job of every CTA of the forward-row / column /
+  // inverse-row launches (host copies from conv_jobs_finalize; the owner of
+  // the job table uploads them and sets dmap, nullptr = binary search)
+  std::vector<int> mrows, mcols, mirows;
+  const int* dmap[3] = {nullptr, nullptr, nullptr};
 };
 // fill row/col offsets of a job table and the launch geometry
 int conv_jobs_finalize(std::vector<ConvJobDev>& jobs, int dtype, ConvLaunch* L);
