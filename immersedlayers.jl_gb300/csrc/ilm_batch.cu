@@ -1048,7 +1048,7 @@ int ilm_batch_set_profiling(ilm_batch_t b, int enable) {
 
 int ilm_batch_set_cg_variant(ilm_batch_t b, int variant) {
   ILM_REQUIRE(b, "null batch");
-  ILM_REQUIRE(variant >= 0 && variant <= 3, "batch: unknown CG variant %d", variant);
+  ILM_REQUIRE(variant >= 0 && variant <= 5, "batch: unknown CG variant %d", variant);
   b->cg_variant = variant;
   b->nclusters = cg_cluster_count(b->nprob, b->maxN, variant);
   b->param_gen++;
@@ -1127,7 +1127,7 @@ int ilm_batch_autotune(ilm_batch_t b, const void* fplus, const void* fminus, voi
   int best = 0;
   float best_ms = 0.f;
   int rc = ILM_OK;
-  for (int v = 1; v <= 3 && rc == ILM_OK; ++v) {
+  for (int v = 1; v <= 5 && rc == ILM_OK; ++v) {
     if (ms_per_variant) ms_per_variant[v - 1] = -1.f;
     if (v == 2 && cg_rep_smem(b->maxN) > 200 * 1024) continue;
     if ((rc = ilm_batch_set_cg_variant(b, v)) != ILM_OK) break;

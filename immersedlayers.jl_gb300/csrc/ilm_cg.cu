@@ -681,63 +681,59 @@ __device__ void matvec_rows_ff(const CGFFParams& pr, int n, int r0, int r1, cons
   }
 }
 
-// z[i - r0] = (W^-1 C^T C r)_i for the owned rows (float-float): u = C r is
-// formed once for the points [ua, ua + nu) = [r0 - K, r1 + K) (the band
-// neighbours of the owned rows unless a body wraps around), whose band rows
-// and body segments the CTA staged in shared memory (sb, ss, sl) when it
-// took the problem; the rare wrapped neighbours are read from global memory
-__device__ __forceinline__ FF band_u(const CGFFParams& pr, int j, int ua, int nu, const float* __restrict__ sb,
-                                     const int* __restrict__ ss, const int* __restrict__ sl,
-                                     const float* __restrict__ rhi, const float* __restrict__ rlo) {
-  const int K = pr.band_k, P = 2 * K + 1;
-  FF u{0.f, 0.f};
-  if (j >= ua && j < ua + nu) {
-    const int s = ss[j - ua], L = sl[j - ua];
-    const float* c = sb + (size_t)(j - ua) * P;
-    for (int t2 = -K; t2 <= K; ++t2) {
-      const int q = seg_nb_near(j, s, L, t2);
-      ff_fma(u, c[t2 + K], 0.f, rhi[q], rlo[q]);
-    }
-  } else {
-    const int s = __ldg(pr.seg_start + j), L = __ldg(pr.seg_len + j);
-    for (int t2 = -K; t2 <= K; ++t2) {
-      const int q = seg_nb_near(j, s, L, t2);
-      ff_fma(u, __ldg(pr.band + (size_t)j * P + t2 + K), 0.f, rhi[q], rlo[q]);
-    }
-  }
-  return u;
-}
-
+// z[i - r0] = (W^-1 C^T C r)_i for the owned rows (float-float).  u = C r is
+// formed for every point (one thread per point, coefficient rows read from
+// L2; the same values in every CTA), so the owned rows, including those
+// whose band wraps around their body, read their neighbours' u from shared
+// memory.
 __device__ void apply_band_rows(const CGFFParams& pr, int n, int r0, int r1, const float* __restrict__ rhi,
-                                const float* __restrict__ rlo, const float* __restrict__ sb,
-                                const int* __restrict__ ss, const int* __restrict__ sl, float* __restrict__ uhi,
-                                float* __restrict__ ulo, const double* __restrict__ ws, double* __restrict__ z) {
+                                const float* __restrict__ rlo, float* __restrict__ uhi, float* __restrict__ ulo,
+                                const double* __restrict__ ws, double* __restrict__ z) {
   const int K = pr.band_k, P = 2 * K + 1;
-  const int ua = r0 - K, nu = (r1 - r0) + 2 * K;
-  for (int jj = threadIdx.x; jj < nu; jj += blockDim.x) {
-    const int j = ua + jj;
+  // half-width 4 (the shipped networks): fixed trip counts, so every
+  // coefficient load of a point is issued before the first product
+  constexpr int K4 = 4, P4 = 9;
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    const int s = __ldg(pr.seg_start + j), L = __ldg(pr.seg_len + j);
+    const float* __restrict__ cj = pr.band + (size_t)j * P;
     FF u{0.f, 0.f};
-    if (j >= 0 && j < n) u = band_u(pr, j, ua, nu, sb, ss, sl, rhi, rlo);
-    uhi[jj] = u.hi;
-    ulo[jj] = u.lo;
+    if (K == K4) {
+      float c[P4];
+#pragma unroll
+      for (int t = 0; t < P4; ++t) c[t] = __ldg(cj + t);
+#pragma unroll
+      for (int t2 = -K4; t2 <= K4; ++t2) {
+        const int q = seg_nb_near(j, s, L, t2);
+        ff_fma(u, c[t2 + K4], 0.f, rhi[q], rlo[q]);
+      }
+    } else {
+      for (int t2 = -K; t2 <= K; ++t2) {
+        const int q = seg_nb_near(j, s, L, t2);
+        ff_fma(u, __ldg(cj + t2 + K), 0.f, rhi[q], rlo[q]);
+      }
+    }
+    uhi[j] = u.hi;
+    ulo[j] = u.lo;
   }
   __syncthreads();
   for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
-    const int s = ss[i - ua], L = sl[i - ua];
+    const int s = __ldg(pr.seg_start + i), L = __ldg(pr.seg_len + i);
     FF acc{0.f, 0.f};
-    for (int t = -K; t <= K; ++t) {
-      const int j = seg_nb_near(i, s, L, -t);
-      FF u;
-      float c;
-      if (j >= ua && j < ua + nu) {
-        u.hi = uhi[j - ua];
-        u.lo = ulo[j - ua];
-        c = sb[(size_t)(j - ua) * P + t + K];
-      } else {  // wrapped around a body shorter than the CTA's row range
-        u = band_u(pr, j, ua, nu, sb, ss, sl, rhi, rlo);
-        c = __ldg(pr.band + (size_t)j * P + t + K);
+    if (K == K4) {
+      int jn[P4];
+      float c[P4];
+#pragma unroll
+      for (int t = -K4; t <= K4; ++t) {
+        jn[t + K4] = seg_nb_near(i, s, L, -t);
+        c[t + K4] = __ldg(pr.band + (size_t)jn[t + K4] * P4 + t + K4);
       }
-      ff_fma(acc, c, 0.f, u.hi, u.lo);
+#pragma unroll
+      for (int t = 0; t < P4; ++t) ff_fma(acc, c[t], 0.f, uhi[jn[t]], ulo[jn[t]]);
+    } else {
+      for (int t = -K; t <= K; ++t) {
+        const int j = seg_nb_near(i, s, L, -t);
+        ff_fma(acc, __ldg(pr.band + (size_t)j * P + t + K), 0.f, uhi[j], ulo[j]);
+      }
     }
     z[i - r0] = fdiv((double)acc.hi + (double)acc.lo, ws[i - r0]);
   }
@@ -759,7 +755,13 @@ __device__ void apply_bjacobi_rows(const CGFFParams& pr, int r0, int r1, const f
         const int s = pr.bstart[b], sz = pr.bsize[b];
         const float* __restrict__ rh = pr.binv_hi + pr.boff[b] + (size_t)(i - s) * sz;
         const float* __restrict__ rl = pr.binv_lo + pr.boff[b] + (size_t)(i - s) * sz;
-        for (int t = lane; t < sz; t += 32) ff_fma(acc[u], __ldg(rh + t), __ldg(rl + t), rhi[s + t], rlo[s + t]);
+        int t = lane;
+        for (; t + 32 < sz; t += 64) {  // two columns per lane per trip, loads first
+          const float h0 = __ldg(rh + t), l0 = __ldg(rl + t), h1 = __ldg(rh + t + 32), l1 = __ldg(rl + t + 32);
+          ff_fma(acc[u], h0, l0, rhi[s + t], rlo[s + t]);
+          ff_fma(acc[u], h1, l1, rhi[s + t + 32], rlo[s + t + 32]);
+        }
+        if (t < sz) ff_fma(acc[u], __ldg(rh + t), __ldg(rl + t), rhi[s + t], rlo[s + t]);
       }
     }
 #pragma unroll
@@ -790,7 +792,7 @@ __device__ void apply_bjacobi_rows(const CGFFParams& pr, int r0, int r1, const f
 // float-float pair (hi exact, lo rounded: ~48 bits) and the sums run in FP32
 // float-float arithmetic: GB300 issues FP64 at a small fraction of the FP32
 // rate and a chain of dependent FP64 adds costs far more latency than the
-// same chain of FP32 two-sums.  `red` holds 4 K blockDim floats (2 K blockDim
+// same chain of FP32 two-sums.  `red` holds 2 K blockDim floats (K blockDim
 // doubles), `pub` 8 slots of 4 float-float values; the published slot
 // rotates over seven values so that a CTA never overwrites a slot another
 // CTA may still be reading.
@@ -886,6 +888,28 @@ __device__ __forceinline__ void gather_parts(cg::cluster_group& cl, float* eh, f
   __syncthreads();
 }
 
+// p = v + b p in float-float (b = bh + bl); ~2^-46 relative
+__device__ __forceinline__ FF ff_axpy(float bh, float bl, FF p, FF v) {
+  const float m = bh * p.hi;
+  float me = fmaf(bh, p.hi, -m);
+  me = fmaf(bh, p.lo, fmaf(bl, p.hi, me));
+  float s, e;
+  two_sum(v.hi, m, s, e);
+  e += v.lo + me;
+  const float hi = s + e;
+  return FF{hi, e - (hi - s)};
+}
+
+// The search direction p is kept whole in every CTA as a float-float vector
+// (ph/pl) and updated there (p = z + beta p over all n points in FP32
+// float-float arithmetic), so the product S p needs no exchange: only r
+// (and z with a preconditioner) cross the cluster, each with the barrier of
+// the reduction that needs it anyway.  Plain CG takes two cluster barriers
+// per iteration, flexible CG three.  The owned slice of p is read back as
+// (double)hi + (double)lo, so x, r and the product all use the same p.
+// Sum_j w_j p_j (the deflation term of q = S' p) follows the same recurrence
+// as p from the reduced Sum w z (or Sum w r); it is recomputed from p at
+// every true-residual refresh.
 template <int NT, int MINB>
 __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(NT, MINB)
     k_cg_cluster(const CGFFParams* __restrict__ P, const int* __restrict__ order, int nprob, int* counter,
@@ -895,9 +919,9 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(NT, MINB)
   const int rmax = (max_n + CG_CLUSTER - 1) / CG_CLUSTER;
   const int ldm = schur_ld(max_n);
   extern __shared__ __align__(16) unsigned char smraw[];
-  double* red = reinterpret_cast<double*>(smraw);  // 2 * threads partials
-  double* bc = red + 2 * NT;                       // 16: scalars broadcast by thread 0
-  double* pub = bc + 16;                           // 32: published CTA sums (8 slots x 4)
+  double* red = reinterpret_cast<double*>(smraw);  // 4 * threads (2 K floats per thread, K <= 4)
+  double* bc = red + 4 * NT;                       // 16: scalars broadcast by thread 0
+  double* pub = bc + 16;                           // 32: published CTA sums (8 slots x 4 float-float)
   double* work = pub + 32;                         // 4: [0] queue index taken by rank 0
   double* xs = work + 4;                           // owned slices (rmax each)
   double* rs = xs + rmax;
@@ -906,20 +930,19 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(NT, MINB)
   double* zs = qs + rmax;
   double* ws = zs + rmax;
   double* bs = ws + rmax;
-  float* eh[2];
-  float* el[2];
-  eh[0] = reinterpret_cast<float*>(bs + rmax + (rmax & 1));  // exchange buffers (ldm each, 16-byte aligned)
-  el[0] = eh[0] + ldm;
-  eh[1] = el[0] + ldm;
-  el[1] = eh[1] + ldm;
-  float* uhi = el[1] + ldm;  // band intermediate (rmax + 2 K, K <= 8)
-  float* ulo = uhi + rmax + 16;
-  float* yh = ulo + rmax + 16;  // product rows (float-float)
+  // float arrays, 16-byte aligned: p (whole), exchange buffers for r (A) and
+  // for z / x (B), band intermediate, product rows, staged band and segments
+  float* ph = reinterpret_cast<float*>(bs + rmax + (rmax & 1));
+  float* pl = ph + ldm;
+  float* ah = pl + ldm;
+  float* al = ah + ldm;
+  float* bh = al + ldm;
+  float* bl = bh + ldm;
+  float* uhi = bl + ldm;  // band intermediate u = C r (every point)
+  float* ulo = uhi + ldm;
+  float* yh = ulo + ldm;  // product rows
   float* yl = yh + rmax;
-  float* sband = yl + rmax;                                      // staged band rows ((rmax + 16) x 17)
-  int* sseg_s = reinterpret_cast<int*>(sband + (rmax + 16) * 17);  // staged body segments (rmax + 16)
-  int* sseg_l = sseg_s + rmax + 16;
-  int slot = 1, eb = 0;
+  int slot = 1;
   while (true) {
     if (rank == 0 && threadIdx.x == 0) work[0] = (double)atomicAdd(counter, 1);
     cl.sync();
@@ -941,73 +964,75 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(NT, MINB)
       bs[i] = pr.b[r0 + i];
       ws[i] = pr.w ? pr.w[r0 + i] : 1.0;
     }
-    for (int j = n + threadIdx.x; j < ld; j += blockDim.x) {  // padding of the products' vectors
-      eh[0][j] = el[0][j] = eh[1][j] = el[1][j] = 0.f;
-    }
-    if (pr.band) {  // stage the band rows and body segments of [r0 - K, r1 + K)
-      const int K = pr.band_k, P = 2 * K + 1, ua = r0 - K, nu = nr + 2 * K;
-      for (int e = threadIdx.x; e < nu * P; e += blockDim.x) {
-        const int j = ua + e / P;
-        sband[e] = (j >= 0 && j < n) ? __ldg(pr.band + (size_t)j * P + e % P) : 0.f;
-      }
-      for (int jj = threadIdx.x; jj < nu; jj += blockDim.x) {
-        const int j = ua + jj;
-        const bool in = j >= 0 && j < n;
-        sseg_s[jj] = in ? __ldg(pr.seg_start + j) : 0;
-        sseg_l[jj] = in ? __ldg(pr.seg_len + j) : 0;
-      }
+    for (int j = n + threadIdx.x; j < ld; j += blockDim.x) {  // padding of the product's vectors
+      ph[j] = pl[j] = bh[j] = bl[j] = 0.f;
     }
     __syncthreads();
-    if (pr.x0) {  // warm start: r = b - S' x0
+    if (pr.x0) {  // warm start: r = b - S' x0 (x through buffer B)
       double v[1] = {0.0};
       for (int i = threadIdx.x; i < nr; i += blockDim.x) v[0] += ws[i] * xs[i];
-      publish_slice(xs, r0, nr, eh[eb], el[eb]);
+      publish_slice(xs, r0, nr, bh, bl);
       csum_t0<1>(cl, v, nr, red, pub, slot);
       if (threadIdx.x == 0) bc[0] = gamma * v[0];
-      gather_parts(cl, eh[eb], el[eb], n, rows, rank);
-      matvec_rows_ff(pr, n, r0, r1, eh[eb], el[eb], yh, yl);
-      eb ^= 1;
+      gather_parts(cl, bh, bl, n, rows, rank);
+      matvec_rows_ff(pr, n, r0, r1, bh, bl, yh, yl);
       __syncthreads();
       const double c0 = bc[0];
       for (int i = threadIdx.x; i < nr; i += blockDim.x) rs[i] = bs[i] - ((double)yh[i] + (double)yl[i]) - c0;
+      __syncthreads();
     } else {
       for (int i = threadIdx.x; i < nr; i += blockDim.x) rs[i] = bs[i];
+      __syncthreads();
     }
-    __syncthreads();
-    double rz, bnorm;
+    // |b|^2, (r, r)_W, sum w r; r published with the same barrier
+    double rz, bnorm, wp;
     {
-      double v[2] = {0.0, 0.0};
+      double v[3] = {0.0, 0.0, 0.0};
       for (int i = threadIdx.x; i < nr; i += blockDim.x) {
         v[0] += bs[i] * bs[i];
         v[1] += ws[i] * rs[i] * rs[i];
+        v[2] += ws[i] * rs[i];
       }
-      if (pre) publish_slice(rs, r0, nr, eh[eb], el[eb]);
-      csum_t0<2>(cl, v, nr, red, pub, slot);
+      publish_slice(rs, r0, nr, ah, al);
+      csum_t0<3>(cl, v, nr, red, pub, slot);
       if (threadIdx.x == 0) {
         bc[0] = sqrt(v[0]);
         bc[1] = v[1];
+        bc[2] = v[2];
       }
-      __syncthreads();
+      gather_parts(cl, ah, al, n, rows, rank);
       bnorm = bc[0];
       rz = bc[1];
+      wp = bc[2];
     }
-    if (pre) {
-      gather_parts(cl, eh[eb], el[eb], n, rows, rank);
+    if (pre) {  // p = z = M r, exchanged through buffer B (with sum w z)
       if (pr.band) {
-        apply_band_rows(pr, n, r0, r1, eh[eb], el[eb], sband, sseg_s, sseg_l, uhi, ulo, ws, zs);
+        apply_band_rows(pr, n, r0, r1, ah, al, uhi, ulo, ws, zs);
       } else {
-        apply_bjacobi_rows(pr, r0, r1, eh[eb], el[eb], yh, yl);
+        apply_bjacobi_rows(pr, r0, r1, ah, al, yh, yl);
         __syncthreads();
         for (int i = threadIdx.x; i < nr; i += blockDim.x) zs[i] = (double)yh[i] + (double)yl[i];
       }
-      eb ^= 1;
       __syncthreads();
+      double v[1] = {0.0};
+      for (int i = threadIdx.x; i < nr; i += blockDim.x) v[0] += ws[i] * zs[i];
+      publish_slice(zs, r0, nr, bh, bl);
+      csum_t0<1>(cl, v, nr, red, pub, slot);
+      if (threadIdx.x == 0) bc[2] = v[0];
+      gather_parts(cl, bh, bl, n, rows, rank);
+      wp = bc[2];
+      for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        ph[j] = bh[j];
+        pl[j] = bl[j];
+      }
+    } else {
+      for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        ph[j] = ah[j];
+        pl[j] = al[j];
+      }
     }
-    for (int i = threadIdx.x; i < nr; i += blockDim.x) ps[i] = pre ? zs[i] : rs[i];
-    // with the net-charge mode deflated, CG converges on S' and the reported
-    // residual is the true one of S after the Sherman-Morrison correction,
-    // which adds the (small) error of z: aim at half the tolerance on S'
-    const double thr = (pr.zdef != nullptr && pr.gamma != 0.0 ? 0.5 : 1.0) * pr.tol * bnorm;
+    __syncthreads();
+    const double thr = (pr.zdef != nullptr && gamma != 0.0 ? 0.5 : 1.0) * pr.tol * bnorm;
     const double thr2 = thr * thr;
     double rlast = bnorm * bnorm;
     int it = 0;
@@ -1020,30 +1045,21 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(NT, MINB)
     double best = 1e300;
     int stall = 0;
     for (int i = threadIdx.x; i < nr; i += blockDim.x) pr.x[r0 + i] = xs[i];
-    __syncthreads();
     while (!done && it < pr.maxiter) {
-      // q = S' p: exchange p, own rows of the product
-      double cp;
-      {
-        double v[1] = {0.0};
-        for (int i = threadIdx.x; i < nr; i += blockDim.x) v[0] += ws[i] * ps[i];
-        publish_slice(ps, r0, nr, eh[eb], el[eb]);
-        csum_t0<1>(cl, v, nr, red, pub, slot);
-        if (threadIdx.x == 0) bc[2] = gamma * v[0];
-        gather_parts(cl, eh[eb], el[eb], n, rows, rank);
-        matvec_rows_ff(pr, n, r0, r1, eh[eb], el[eb], yh, yl);
-        eb ^= 1;
-        __syncthreads();
-        cp = bc[2];
-      }
+      // q = S' p on the owned rows (p whole in this CTA)
+      matvec_rows_ff(pr, n, r0, r1, ph, pl, yh, yl);
+      __syncthreads();
       double alpha, pq;
       {
+        const double cp = gamma * wp;
         double v[2] = {0.0, 0.0};
         for (int i = threadIdx.x; i < nr; i += blockDim.x) {
+          const double pi = (double)ph[r0 + i] + (double)pl[r0 + i];
           const double qi = (double)yh[i] + (double)yl[i] + cp;
+          ps[i] = pi;
           qs[i] = qi;
-          v[0] += ws[i] * ps[i] * qi;
-          v[1] += ws[i] * ps[i] * rs[i];
+          v[0] += ws[i] * pi * qi;
+          v[1] += ws[i] * pi * rs[i];
         }
         csum_t0<2>(cl, v, nr, red, pub, slot);
         if (threadIdx.x == 0) {
@@ -1055,59 +1071,67 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(NT, MINB)
         alpha = bc[4];
       }
       if (pq == 0.0) break;
-      double rr, rzn;
+      double rr, rzn, wr;
       {
-        double v[2] = {0.0, 0.0};
+        double v[3] = {0.0, 0.0, 0.0};
         for (int i = threadIdx.x; i < nr; i += blockDim.x) {
           xs[i] += alpha * ps[i];
           const double ri = rs[i] - alpha * qs[i];
           rs[i] = ri;
           v[0] += ri * ri;
           v[1] += ws[i] * ri * ri;
+          v[2] += ws[i] * ri;
         }
-        if (pre) publish_slice(rs, r0, nr, eh[eb], el[eb]);
-        csum_t0<2>(cl, v, nr, red, pub, slot);
+        publish_slice(rs, r0, nr, ah, al);
+        csum_t0<3>(cl, v, nr, red, pub, slot);
         if (threadIdx.x == 0) {
           bc[5] = v[0];
           bc[6] = v[1];
+          bc[7] = v[2];
         }
         __syncthreads();
         rr = bc[5];
         rzn = bc[6];
+        wr = bc[7];
       }
       ++it;
       rlast = rr;
       if (rr <= thr2 || (it % 50) == 0 || it == pr.maxiter) {
-        // true residual b - S' x (x exchanged through the current buffer: the
-        // split of r published above is superseded)
+        // true residual b - S' x (x through buffer B; the r published above
+        // is superseded by the refreshed one), and sum w p recomputed
         {
           double v[1] = {0.0};
           for (int i = threadIdx.x; i < nr; i += blockDim.x) v[0] += ws[i] * xs[i];
-          publish_slice(xs, r0, nr, eh[eb], el[eb]);
+          publish_slice(xs, r0, nr, bh, bl);
           csum_t0<1>(cl, v, nr, red, pub, slot);
-          if (threadIdx.x == 0) bc[7] = gamma * v[0];
-          gather_parts(cl, eh[eb], el[eb], n, rows, rank);
-          matvec_rows_ff(pr, n, r0, r1, eh[eb], el[eb], yh, yl);
-          eb ^= 1;
+          if (threadIdx.x == 0) bc[8] = gamma * v[0];
+          gather_parts(cl, bh, bl, n, rows, rank);
+          matvec_rows_ff(pr, n, r0, r1, bh, bl, yh, yl);
           __syncthreads();
         }
-        const double cx = bc[7];
-        double v[2] = {0.0, 0.0};
+        const double cx = bc[8];
+        double v[4] = {0.0, 0.0, 0.0, 0.0};
         for (int i = threadIdx.x; i < nr; i += blockDim.x) {
           const double ri = bs[i] - ((double)yh[i] + (double)yl[i]) - cx;
           rs[i] = ri;
           v[0] += ri * ri;
           v[1] += ws[i] * ri * ri;
+          v[2] += ws[i] * ri;
+          v[3] += ws[i] * ps[i];
         }
-        if (pre) publish_slice(rs, r0, nr, eh[eb], el[eb]);
-        csum_t0<2>(cl, v, nr, red, pub, slot);
+        publish_slice(rs, r0, nr, ah, al);
+        csum_t0<4>(cl, v, nr, red, pub, slot);
         if (threadIdx.x == 0) {
-          bc[8] = v[0];
-          bc[9] = v[1];
+          bc[9] = v[0];
+          bc[10] = v[1];
+          bc[11] = v[2];
+          bc[12] = v[3];
         }
         __syncthreads();
-        const double tr = bc[8];
-        rzn = bc[9];
+        const double tr = bc[9];
+        rzn = bc[10];
+        wr = bc[11];
+        wp = bc[12];
         rlast = tr;
         if (tr <= thr2) {
           done = true;
@@ -1122,32 +1146,53 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(NT, MINB)
           break;
         }
       }
+      // r of every CTA (buffer A), published with the reduction above
+      gather_parts(cl, ah, al, n, rows, rank);
+      double beta, wv;
       if (!pre) {
-        const double beta = fdiv(rzn, rz);
+        beta = fdiv(rzn, rz);
         rz = rzn;
-        for (int i = threadIdx.x; i < nr; i += blockDim.x) ps[i] = rs[i] + beta * ps[i];
-        __syncthreads();
+        wv = wr;
+        // p = r + beta p
+        const float bh_ = (float)beta, bl_ = (float)(beta - (double)bh_);
+        for (int j = threadIdx.x; j < n; j += blockDim.x) {
+          const FF pn = ff_axpy(bh_, bl_, FF{ph[j], pl[j]}, FF{ah[j], al[j]});
+          ph[j] = pn.hi;
+          pl[j] = pn.lo;
+        }
       } else {
-        // flexible CG: z = M r (r exchanged), beta = -(z, q) / (p, q), p = z + beta p
-        gather_parts(cl, eh[eb], el[eb], n, rows, rank);
+        // flexible CG: z = M r, beta = -(z, q) / (p, q), p = z + beta p
         if (pr.band) {
-          apply_band_rows(pr, n, r0, r1, eh[eb], el[eb], sband, sseg_s, sseg_l, uhi, ulo, ws, zs);
+          apply_band_rows(pr, n, r0, r1, ah, al, uhi, ulo, ws, zs);
         } else {
-          apply_bjacobi_rows(pr, r0, r1, eh[eb], el[eb], yh, yl);
+          apply_bjacobi_rows(pr, r0, r1, ah, al, yh, yl);
           __syncthreads();
           for (int i = threadIdx.x; i < nr; i += blockDim.x) zs[i] = (double)yh[i] + (double)yl[i];
         }
-        eb ^= 1;
         __syncthreads();
-        double v[1] = {0.0};
-        for (int i = threadIdx.x; i < nr; i += blockDim.x) v[0] += ws[i] * zs[i] * qs[i];
-        csum_t0<1>(cl, v, nr, red, pub, slot);
-        if (threadIdx.x == 0) bc[10] = fdiv(-v[0], pq);
-        __syncthreads();
-        const double beta = bc[10];
-        for (int i = threadIdx.x; i < nr; i += blockDim.x) ps[i] = zs[i] + beta * ps[i];
-        __syncthreads();
+        double v[2] = {0.0, 0.0};
+        for (int i = threadIdx.x; i < nr; i += blockDim.x) {
+          v[0] += ws[i] * zs[i] * qs[i];
+          v[1] += ws[i] * zs[i];
+        }
+        publish_slice(zs, r0, nr, bh, bl);
+        csum_t0<2>(cl, v, nr, red, pub, slot);
+        if (threadIdx.x == 0) {
+          bc[13] = fdiv(-v[0], pq);
+          bc[14] = v[1];
+        }
+        gather_parts(cl, bh, bl, n, rows, rank);
+        beta = bc[13];
+        wv = bc[14];
+        const float bh_ = (float)beta, bl_ = (float)(beta - (double)bh_);
+        for (int j = threadIdx.x; j < n; j += blockDim.x) {
+          const FF pn = ff_axpy(bh_, bl_, FF{ph[j], pl[j]}, FF{bh[j], bl[j]});
+          ph[j] = pn.hi;
+          pl[j] = pn.lo;
+        }
       }
+      wp = wv + beta * wp;
+      __syncthreads();
     }
     relres = bnorm > 0 ? sqrt(rlast) / bnorm : 0.0;
     if (best < relres) {  // stopped past the best iterate: return that one
@@ -1160,18 +1205,17 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(NT, MINB)
       double v[1] = {0.0};
       for (int i = threadIdx.x; i < nr; i += blockDim.x) v[0] += ws[i] * xs[i];
       csum_t0<1>(cl, v, nr, red, pub, slot);
-      if (threadIdx.x == 0) bc[11] = gamma * (v[0] / (1.0 - gamma * pr.uz));
+      if (threadIdx.x == 0) bc[15] = gamma * (v[0] / (1.0 - gamma * pr.uz));
       __syncthreads();
-      const double gt = bc[11];
+      const double gt = bc[15];
       for (int i = threadIdx.x; i < nr; i += blockDim.x) xs[i] += gt * pr.zdef[r0 + i];
       __syncthreads();
-      // reported residual: the true one of S x = b
+      // reported residual: the true one of S x = b (x through buffer B)
       double u[1] = {0.0};
-      publish_slice(xs, r0, nr, eh[eb], el[eb]);
+      publish_slice(xs, r0, nr, bh, bl);
       csum_t0<1>(cl, u, nr, red, pub, slot);  // barrier that publishes x
-      gather_parts(cl, eh[eb], el[eb], n, rows, rank);
-      matvec_rows_ff(pr, n, r0, r1, eh[eb], el[eb], yh, yl);
-      eb ^= 1;
+      gather_parts(cl, bh, bl, n, rows, rank);
+      matvec_rows_ff(pr, n, r0, r1, bh, bl, yh, yl);
       __syncthreads();
       double t[1] = {0.0};
       for (int i = threadIdx.x; i < nr; i += blockDim.x) {
@@ -1179,9 +1223,9 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(NT, MINB)
         t[0] += d * d;
       }
       csum_t0<1>(cl, t, nr, red, pub, slot);
-      if (threadIdx.x == 0) bc[12] = t[0];
+      if (threadIdx.x == 0) bc[0] = t[0];
       __syncthreads();
-      relres = bnorm > 0 ? sqrt(bc[12]) / bnorm : 0.0;
+      relres = bnorm > 0 ? sqrt(bc[0]) / bnorm : 0.0;
     }
     for (int i = threadIdx.x; i < nr; i += blockDim.x) pr.x[r0 + i] = xs[i];
     if (rank == 0 && threadIdx.x == 0) {
@@ -1196,9 +1240,8 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(NT, MINB)
 size_t cg_cluster_smem(int max_n, int nt) {
   const size_t rmax = (size_t)(max_n + CG_CLUSTER - 1) / CG_CLUSTER;
   const size_t ldm = (size_t)schur_ld(max_n);
-  return (2 * (size_t)nt + 16 + 32 + 4 + 7 * rmax + 1) * sizeof(double) +
-         (4 * ldm + 2 * (rmax + 16) + 2 * rmax + 17 * (rmax + 16)) * sizeof(float) +
-         2 * (rmax + 16) * sizeof(int) + 64;
+  return (4 * (size_t)nt + 16 + 32 + 4 + 7 * rmax + 1) * sizeof(double) +
+         (8 * ldm + 2 * rmax) * sizeof(float) + 64;
 }
 
 size_t cg_rep_smem(int max_n) {
@@ -1208,12 +1251,29 @@ size_t cg_rep_smem(int max_n) {
 
 
 // Kernel variants (the batch autotuner picks among them): 0 (default) and 1 =
-// row-distributed, 256 threads per CTA; 3 = row-distributed, 128 threads
-// per CTA (twice as many clusters resident: more problems in flight when the
-// iterations are latency-bound); 2 = replicated vectors, when they fit in
-// shared memory.
+// row-distributed, 256 threads per CTA, up to 3 CTAs per SM; 3 = 128
+// threads, up to 6 CTAs per SM (more problems in flight); 4 = 256 threads,
+// at most 2 CTAs per SM (more registers, less sharing of an SM between
+// clusters); 5 = 512 threads, one CTA per SM (each cluster alone on its
+// SMs); 2 = replicated vectors, when they fit in shared memory.
 static bool use_rep(int variant, int max_n) { return variant == 2 && cg_rep_smem(max_n) <= 200 * 1024; }
-static int dist_threads(int variant) { return variant == 3 ? 128 : 256; }
+static int dist_threads(int variant) { return variant == 3 ? 128 : variant == 5 ? 512 : 256; }
+
+template <int NT, int MINB>
+static int launch_dist(const CGFFParams* prm, const int* order, int nprob, int* counter, int max_n, int nclusters,
+                       size_t smem, cudaStream_t st) {
+  ILM_CHECK_CUDA(cudaFuncSetAttribute(k_cg_cluster<NT, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_cg_cluster<NT, MINB><<<nclusters * CG_CLUSTER, NT, smem, st>>>(prm, order, nprob, counter, max_n);
+  ILM_CHECK_LAUNCH();
+  return ILM_OK;
+}
+
+template <int NT, int MINB>
+static cudaError_t clusters_dist(int* nc, cudaLaunchConfig_t* cfg, size_t smem) {
+  cudaError_t e = cudaFuncSetAttribute(k_cg_cluster<NT, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveClusters(nc, k_cg_cluster<NT, MINB>, cfg);
+  return e;
+}
 
 int launch_cg_cluster(const void* params_dev, const int* order, int nprob, int* counter, int max_n, int nclusters,
                       cudaStream_t st, int variant) {
@@ -1232,15 +1292,12 @@ int launch_cg_cluster(const void* params_dev, const int* order, int nprob, int* 
     set_error("cluster CG: %d unknowns exceed the shared-memory layout", max_n);
     return ILM_ERR_SIZE_LIMIT;
   }
-  if (nt == 128) {
-    ILM_CHECK_CUDA(cudaFuncSetAttribute(k_cg_cluster<128, 6>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_cg_cluster<128, 6><<<nclusters * CG_CLUSTER, 128, smem, st>>>(prm, order, nprob, counter, max_n);
-  } else {
-    ILM_CHECK_CUDA(cudaFuncSetAttribute(k_cg_cluster<256, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_cg_cluster<256, 3><<<nclusters * CG_CLUSTER, 256, smem, st>>>(prm, order, nprob, counter, max_n);
+  switch (variant) {
+    case 3: return launch_dist<128, 6>(prm, order, nprob, counter, max_n, nclusters, smem, st);
+    case 4: return launch_dist<256, 2>(prm, order, nprob, counter, max_n, nclusters, smem, st);
+    case 5: return launch_dist<512, 1>(prm, order, nprob, counter, max_n, nclusters, smem, st);
+    default: return launch_dist<256, 3>(prm, order, nprob, counter, max_n, nclusters, smem, st);
   }
-  ILM_CHECK_LAUNCH();
-  return ILM_OK;
 }
 
 int cg_cluster_count(int nprob, int max_n, int variant) {
@@ -1261,16 +1318,19 @@ int cg_cluster_count(int nprob, int max_n, int variant) {
   if (rep) {
     e = cudaFuncSetAttribute(k_cg_rep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveClusters(&nc, k_cg_rep, &cfg);
-  } else if (nt == 128) {
-    e = cudaFuncSetAttribute(k_cg_cluster<128, 6>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveClusters(&nc, k_cg_cluster<128, 6>, &cfg);
+  } else if (variant == 3) {
+    e = clusters_dist<128, 6>(&nc, &cfg, smem);
+  } else if (variant == 4) {
+    e = clusters_dist<256, 2>(&nc, &cfg, smem);
+  } else if (variant == 5) {
+    e = clusters_dist<512, 1>(&nc, &cfg, smem);
   } else {
-    e = cudaFuncSetAttribute(k_cg_cluster<256, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveClusters(&nc, k_cg_cluster<256, 3>, &cfg);
+    e = clusters_dist<256, 3>(&nc, &cfg, smem);
   }
   if (e != cudaSuccess || nc <= 0) {
     (void)cudaGetLastError();
-    nc = std::max(1, (nt == 128 ? 6 : 3) * nsm / CG_CLUSTER);
+    const int per_sm = variant == 3 ? 6 : variant == 4 ? 2 : variant == 5 ? 1 : 3;
+    nc = std::max(1, per_sm * nsm / CG_CLUSTER);
   }
   return std::min(nc, nprob);
 }

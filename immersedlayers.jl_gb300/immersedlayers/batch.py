@@ -129,8 +129,9 @@ def _cg_times(self):
 
 def _set_cg_variant(self, variant):
     """Schur CG kernel: 0 default (= 1), 1 row-distributed vectors (256
-    threads per CTA), 2 replicated vectors (one cluster barrier per
-    iteration), 3 row-distributed with 128-thread CTAs."""
+    threads per CTA, up to 3 per SM), 2 replicated vectors (one cluster
+    barrier per iteration), 3 128-thread CTAs, 4 256-thread CTAs at most 2
+    per SM, 5 512-thread CTAs one per SM."""
     L.call("ilm_batch_set_cg_variant", self._h, int(variant))
 
 
@@ -148,10 +149,10 @@ def _autotune(self, fplus, fminus, f_out=None, s_out=None, tol=1e-8, maxiter=500
     if s_out is None:
         s_out = torch.empty(self.total_points, dtype=self.dtype, device="cuda")
     ch = C.c_int()
-    ms = (C.c_float * 3)()
+    ms = (C.c_float * 5)()
     L.call("ilm_batch_autotune", self._h, _ptr(fplus), _ptr(fminus), _ptr(f_out), _ptr(s_out), float(tol),
            int(maxiter), int(reps), _stream_ptr(stream), C.byref(ch), ms)
-    return ch.value, {v + 1: float(ms[v]) for v in range(3) if ms[v] >= 0}
+    return ch.value, {v + 1: float(ms[v]) for v in range(5) if ms[v] >= 0}
 
 
 def _stats(self):
