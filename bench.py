@@ -435,17 +435,23 @@ def _stokes_leg(args):
     return out
 
 
+_NET = {}
+
+
 def _prepare_learned(bs, block=64):
-    """Load the learned preconditioner trained on the batched configuration's
-    Dirichlet problems and set it on the batch; the Neumann problems keep
-    block-Jacobi (the Neumann network trained to a loss of only 0.6: the
-    near-null constants of the Neumann Schur complement dominate its data)."""
+    """Set the learned preconditioner trained on the batched configuration's
+    Dirichlet problems on the batch (the network is loaded once per process,
+    like a model); the Neumann problems keep block-Jacobi (the Neumann
+    network trained to a loss of only 0.6: the near-null constants of the
+    Neumann Schur complement dominate its data)."""
     from immersedlayers import learned as LN
     from immersedlayers.batch import DIRICHLET
     if not os.path.exists(LN.BATCHED_WEIGHTS[DIRICHLET]):
         return False
     bs.set_precond("bjacobi", block)   # block inverses for the Neumann problems
-    bs._nets = [LN.LearnedPreconditioner.load(LN.BATCHED_WEIGHTS[DIRICHLET])]
+    if "dirichlet" not in _NET:
+        _NET["dirichlet"] = LN.LearnedPreconditioner.load(LN.BATCHED_WEIGHTS[DIRICHLET])
+    bs._nets = [_NET["dirichlet"]]
     bs.set_learned(bs._nets[0], kinds=(DIRICHLET,))
     return True
 

@@ -219,6 +219,13 @@ __global__ void k_bgather(const BGatherTask* __restrict__ tasks, int ntasks, int
   static_cast<T*>(G.out)[k] = total * (T)G.scale;
 }
 
+// dst[k][0..P) = src[k][0..P) for the selected points k
+__global__ void k_select_rows(int N, int P, const unsigned char* __restrict__ sel, const float* __restrict__ src,
+                              float* __restrict__ dst) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < N * P; e += gridDim.x * blockDim.x)
+    if (sel[e / P]) dst[e] = src[e];
+}
+
 // rhs64 = (double)g - (double)avg
 template <typename T>
 __global__ void k_rhs64(int n, const T* __restrict__ g, const T* __restrict__ avg, double* __restrict__ out) {
@@ -440,7 +447,10 @@ int ensure_deflation(ilm_batch_s* b) {
   for (int p = 0; p < np; ++p) {
     const size_t o = b->poff[p];
     void* dst = cg.data() + (size_t)p * cgff_params_size();
-    const bool pre = b->bj_block > 0;  // block-Jacobi (if set up) shortens this solve ~4x
+    // the best preconditioner set up so far: the learned band, else
+    // block-Jacobi (each shortens this tight solve several times)
+    const bool band = b->band_k >= 0 && !b->has_band.empty() && b->has_band[p];
+    const bool pre = !band && b->bj_block > 0;
     cgff_params_fill(dst, b->Shi.as<float>() + b->soff[p], b->Slo.as<float>() + b->soff[p], drhs.as<double>() + o,
                      b->defl_z.as<double>() + o, b->ds64.as<double>() + o, b->probs[p].npts, 20000, 1e-12,
                      its.as<int>() + p, rr.as<double>() + p, pre ? b->bj_blk.as<int>() + o : nullptr,
@@ -449,6 +459,9 @@ int ensure_deflation(ilm_batch_s* b) {
                      pre ? b->bj_off.as<int>() + b->bj_first[p] : nullptr, pre ? b->bj_inv.as<float>() : nullptr,
                      pre ? b->bj_inv_lo.as<float>() : nullptr);
     cgff_params_set_deflation(dst, b->defl_gamma[p], nullptr, 0.0);
+    if (band)
+      cgff_params_set_band(dst, b->band.as<float>() + o * (2 * b->band_k + 1), b->band_k,
+                           b->lseg_start.as<int>() + o, b->lseg_len.as<int>() + o);
   }
   ILM_TRY(up(prm, cg));
   ILM_TRY(launch_cg_cluster(prm.p, b->order.as<int>(), np, b->counter.as<int>(), b->maxN, b->nclusters, nullptr,
@@ -521,11 +534,14 @@ int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* 
     tso[c].assign(nprob, 0);
   }
   std::vector<HostWindows> Wall(nprob);
-  for (int p = 0; p < nprob; ++p) {
+  parallel_for(nprob, [&](int p) {  // DDF windows and tile lists of every problem, in parallel
     const ilm_batch_problem_t& P = probs[p];
     ilm_grid_s g{P.nx, P.ny, P.h, P.i0x, P.i0y};
+    host_windows(g, ddf, P.npts, x + B->poff[p], y + B->poff[p], &Wall[p]);
+  });
+  for (int p = 0; p < nprob; ++p) {
+    const ilm_batch_problem_t& P = probs[p];
     const size_t o = B->poff[p];
-    host_windows(g, ddf, P.npts, x + o, y + o, &Wall[p]);
     HostWindows& W = Wall[p];
     for (int d = 0; d < 2; ++d) {
       hbx[d].insert(hbx[d].end(), W.bx[d].begin(), W.bx[d].end());
@@ -861,7 +877,7 @@ int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* 
     sp[p].poff = (int)B->poff[p];
     sp[p].tile0 = tiles;
     const int nt = (probs[p].npts + 15) / 16;
-    tiles += nt * nt;
+    tiles += nt * (nt + 1) / 2;  // upper triangle (the pair sums are symmetric)
     sp[p].soff = B->soff[p];
     sp[p].invh = 1.0 / probs[p].h;
   }
@@ -1243,16 +1259,18 @@ int ilm_batch_set_learned(ilm_batch_t b, ilm_net_t net, int kind_mask, const int
     }
   }
   std::vector<float> feat((size_t)Ptot * 8);
-  for (int p = 0; p < b->nprob; ++p) {
+  std::vector<int> fst(b->nprob, ILM_OK);
+  parallel_for(b->nprob, [&](int p) {  // point features of every problem, in parallel
     const int o = (int)b->poff[p], n = b->probs[p].npts;
     std::vector<int> s0(n), l0(n);
     for (int k = 0; k < n; ++k) {
       s0[k] = ls[o + k];
       l0[k] = ll[o + k];
     }
-    ILM_TRY(ilm_point_features(n, b->hx.data() + o, b->hy.data() + o, b->hnx.data() + o, b->hny.data() + o,
-                               b->hds.data() + o, s0.data(), l0.data(), b->probs[p].h, feat.data() + (size_t)o * 8));
-  }
+    fst[p] = ilm_point_features(n, b->hx.data() + o, b->hy.data() + o, b->hnx.data() + o, b->hny.data() + o,
+                                b->hds.data() + o, s0.data(), l0.data(), b->probs[p].h, feat.data() + (size_t)o * 8);
+  });
+  for (int p = 0; p < b->nprob; ++p) ILM_TRY(fst[p]);
   DevBuf dfeat, das, dll;
   ILM_TRY(up(dfeat, feat));
   ILM_TRY(up(das, as));
@@ -1263,16 +1281,20 @@ int ilm_batch_set_learned(ilm_batch_t b, ilm_net_t net, int kind_mask, const int
     ILM_TRY(b->band.alloc((size_t)Ptot * P * sizeof(float)));
     b->has_band.assign(b->nprob, 0);
   }
-  DevBuf tmp;
+  DevBuf tmp, dsel;
   ILM_TRY(tmp.alloc((size_t)Ptot * P * sizeof(float)));
   ILM_TRY(net_forward_packed(net, Ptot, dfeat.as<float>(), das.as<int>(), dll.as<int>(), tmp.as<float>(), nullptr));
-  for (int p = 0; p < b->nprob; ++p) {  // this network's band for the problems of the selected kinds
+  // this network's band for the points of the problems of the selected kinds
+  std::vector<unsigned char> sel(Ptot, 0);
+  for (int p = 0; p < b->nprob; ++p) {
     if (!(kind_mask & (1 << b->probs[p].kind))) continue;
-    const size_t o = b->poff[p];
-    ILM_CHECK_CUDA(cudaMemcpy(b->band.as<float>() + o * P, tmp.as<float>() + o * P,
-                              (size_t)b->probs[p].npts * P * sizeof(float), cudaMemcpyDeviceToDevice));
+    for (size_t k = b->poff[p]; k < b->poff[p + 1]; ++k) sel[k] = 1;
     b->has_band[p] = 1;
   }
+  ILM_TRY(up(dsel, sel));
+  k_select_rows<<<std::min(4096, (Ptot * P + 255) / 256), 256>>>(Ptot, P, dsel.as<unsigned char>(), tmp.as<float>(),
+                                                                  b->band.as<float>());
+  ILM_CHECK_LAUNCH();
   ILM_CHECK_CUDA(cudaDeviceSynchronize());
   b->band_k = K;
   b->precond = 2;

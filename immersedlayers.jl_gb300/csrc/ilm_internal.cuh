@@ -5,9 +5,11 @@
 #include <stdint.h>
 #include <stdio.h>
 
+#include <algorithm>
 #include <map>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "ilm.h"
@@ -46,6 +48,25 @@ void set_error(const char* fmt, ...);
   } while (0)
 
 inline cudaStream_t as_stream(ilm_stream_t s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// fn(i) for i in [0, n) on up to min(n, hardware threads, 16) host threads
+// (contiguous chunks; fn must only touch data of its own i)
+template <typename F>
+void parallel_for(int n, F fn) {
+  const int hw = (int)std::thread::hardware_concurrency();
+  const int nt = std::max(1, std::min({n, hw > 0 ? hw : 1, 16}));
+  if (nt <= 1) {
+    for (int i = 0; i < n; ++i) fn(i);
+    return;
+  }
+  std::vector<std::thread> th;
+  th.reserve(nt);
+  for (int t = 0; t < nt; ++t)
+    th.emplace_back([&, t] {
+      for (int i = (int)((long long)n * t / nt); i < (int)((long long)n * (t + 1) / nt); ++i) fn(i);
+    });
+  for (auto& x : th) x.join();
+}
 
 // ---------------------------------------------------------------------------
 // device buffer (RAII)

@@ -437,9 +437,18 @@ __global__ void __launch_bounds__(256) k_schur_pairs_batched(int nprob, const Sc
   const SchurProbDev P = pr[lo];
   const int N = P.n;
   const int nt = (N + 15) / 16;
+  // the tile sum T_kl = sum U_k(a) G(a - b) U_l(b) is symmetric (G depends on
+  // |a - b| only and both sides use the same functionals): one CTA per tile
+  // of the upper triangle (ti <= tj) in row-major order, writing S_kl = -w_l
+  // T_kl and, off the diagonal tiles, S_lk = -w_k T_kl
   const int t = u - P.tile0;
-  const int k = (t / nt) * 16 + threadIdx.y;
-  const int l = (t % nt) * 16 + threadIdx.x;
+  int ti = (int)((2.0 * nt + 1.0 - sqrt((2.0 * nt + 1.0) * (2.0 * nt + 1.0) - 8.0 * t)) * 0.5);
+  auto row0 = [nt](int i) { return i * nt - i * (i - 1) / 2; };  // first triangle tile of tile row i
+  while (ti > 0 && row0(ti) > t) --ti;
+  while (ti + 1 < nt && row0(ti + 1) <= t) ++ti;
+  const int tj = ti + (t - row0(ti));
+  const int k = ti * 16 + threadIdx.y;
+  const int l = tj * 16 + threadIdx.x;
   if (k >= N || l >= N) return;
   const Functional& Fk = F[P.poff + k];
   const Functional& Fl = F[P.poff + l];
@@ -485,6 +494,12 @@ __global__ void __launch_bounds__(256) k_schur_pairs_batched(int nprob, const Sc
   const float vh = (float)v;
   Shi[P.soff + (size_t)k * schur_ld(N) + l] = vh;
   Slo[P.soff + (size_t)k * schur_ld(N) + l] = (float)(v - (double)vh);
+  if (ti != tj) {
+    const double vt = -w[P.poff + k] * total;
+    const float th = (float)vt;
+    Shi[P.soff + (size_t)l * schur_ld(N) + k] = th;
+    Slo[P.soff + (size_t)l * schur_ld(N) + k] = (float)(vt - (double)th);
+  }
 }
 
 int schur_build_batched(int nprob, const SchurProbDev* probs_dev, int total_tiles, int Ptot, const int* pt2prob,
