@@ -51,6 +51,9 @@ def parse():
     ap.add_argument("--heat-steps", type=int, default=1000, help="heat-conduction leg (0: skip)")
     ap.add_argument("--learned-nprob", type=int, default=256, help="learned-preconditioner leg (0: skip)")
     ap.add_argument("--stokes", type=int, default=1, help="Stokes leg (0: skip)")
+    ap.add_argument("--profile-solves", type=int, default=0,
+                    help="profiling driver: set up the batch with the default solver, run this many solves on a "
+                         "created stream and exit (no timing, no JSON line)")
     return ap.parse_args()
 
 
@@ -552,10 +555,36 @@ def _cpu_baseline(args, specs):
                       f"problem scaled by npts/k, solve timed in full; sample wall {est['sample_wall']:.1f}s"}
 
 
+def run_profile_solves(args):
+    """Batch and default-solver set-up, then `args.profile_solves` solves (a
+    fixed launch sequence for ncu captures)."""
+    import torch
+    import __graft_entry__ as ge
+    ge.build()
+    from immersedlayers import workloads as W
+    from immersedlayers.batch import BatchSolver
+    bs = BatchSolver(W.batch_specs(args.nprob), dtype=torch.float32)
+    if args.precond == "learned":
+        _prepare_learned(bs, args.block)
+    bs.set_precond(args.precond, args.block)
+    fp, fm = bs.surface_data()
+    f = torch.empty(bs.total_cells, device="cuda")
+    s = torch.empty(bs.total_points, device="cuda")
+    st = torch.cuda.Stream()
+    for _ in range(args.profile_solves):
+        bs.solve(fp, fm, f, s, tol=args.tol, stream=st)
+    st.synchronize()
+    its, rr = bs.info()
+    print(f"solves {args.profile_solves}: CG iterations mean {its.mean():.2f} max {its.max()}, "
+          f"max rel residual {rr.max():.3e}", file=sys.stderr)
+
+
 def main():
     args = parse()
     rank, world, dist = dist_init()
-    if args.impl == "reference":
+    if args.profile_solves > 0:
+        run_profile_solves(args)
+    elif args.impl == "reference":
         run_reference(args, rank, world)
     else:
         run_ours(args, rank, world, dist)

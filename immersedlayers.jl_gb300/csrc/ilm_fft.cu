@@ -419,8 +419,75 @@ int twiddle_table(int L, int dtype, const void** out) {
 // conflicts); element n = n1 N2 + n2 is at n1 (N2 + 1) + n2, in natural order
 // before and after the transform.
 // ---------------------------------------------------------------------------
-__constant__ float2 c_tw32[32];  // exp(-2 pi i j / 32)
-__constant__ float2 c_tw24[24];  // exp(-2 pi i j / 24)
+// exp(-2 pi i k / N) for N = 32 and 24 as literals: in the unrolled register
+// DFTs k is a compile-time constant, so the switch folds to an immediate and
+// the multiplications by the trivial factors (0, +-1, +-1/2) simplify
+__device__ __forceinline__ float2 tw32(int k) {
+  switch (k) {
+    case 0: return make_float2(1.000000000e+00f, 0.000000000e+00f);
+    case 1: return make_float2(9.807852804e-01f, -1.950903220e-01f);
+    case 2: return make_float2(9.238795325e-01f, -3.826834324e-01f);
+    case 3: return make_float2(8.314696123e-01f, -5.555702330e-01f);
+    case 4: return make_float2(7.071067812e-01f, -7.071067812e-01f);
+    case 5: return make_float2(5.555702330e-01f, -8.314696123e-01f);
+    case 6: return make_float2(3.826834324e-01f, -9.238795325e-01f);
+    case 7: return make_float2(1.950903220e-01f, -9.807852804e-01f);
+    case 8: return make_float2(0.000000000e+00f, -1.000000000e+00f);
+    case 9: return make_float2(-1.950903220e-01f, -9.807852804e-01f);
+    case 10: return make_float2(-3.826834324e-01f, -9.238795325e-01f);
+    case 11: return make_float2(-5.555702330e-01f, -8.314696123e-01f);
+    case 12: return make_float2(-7.071067812e-01f, -7.071067812e-01f);
+    case 13: return make_float2(-8.314696123e-01f, -5.555702330e-01f);
+    case 14: return make_float2(-9.238795325e-01f, -3.826834324e-01f);
+    case 15: return make_float2(-9.807852804e-01f, -1.950903220e-01f);
+    case 16: return make_float2(-1.000000000e+00f, 0.000000000e+00f);
+    case 17: return make_float2(-9.807852804e-01f, 1.950903220e-01f);
+    case 18: return make_float2(-9.238795325e-01f, 3.826834324e-01f);
+    case 19: return make_float2(-8.314696123e-01f, 5.555702330e-01f);
+    case 20: return make_float2(-7.071067812e-01f, 7.071067812e-01f);
+    case 21: return make_float2(-5.555702330e-01f, 8.314696123e-01f);
+    case 22: return make_float2(-3.826834324e-01f, 9.238795325e-01f);
+    case 23: return make_float2(-1.950903220e-01f, 9.807852804e-01f);
+    case 24: return make_float2(0.000000000e+00f, 1.000000000e+00f);
+    case 25: return make_float2(1.950903220e-01f, 9.807852804e-01f);
+    case 26: return make_float2(3.826834324e-01f, 9.238795325e-01f);
+    case 27: return make_float2(5.555702330e-01f, 8.314696123e-01f);
+    case 28: return make_float2(7.071067812e-01f, 7.071067812e-01f);
+    case 29: return make_float2(8.314696123e-01f, 5.555702330e-01f);
+    case 30: return make_float2(9.238795325e-01f, 3.826834324e-01f);
+    case 31: return make_float2(9.807852804e-01f, 1.950903220e-01f);
+    default: return make_float2(1.f, 0.f);
+  }
+}
+__device__ __forceinline__ float2 tw24(int k) {
+  switch (k) {
+    case 0: return make_float2(1.000000000e+00f, 0.000000000e+00f);
+    case 1: return make_float2(9.659258263e-01f, -2.588190451e-01f);
+    case 2: return make_float2(8.660254038e-01f, -5.000000000e-01f);
+    case 3: return make_float2(7.071067812e-01f, -7.071067812e-01f);
+    case 4: return make_float2(5.000000000e-01f, -8.660254038e-01f);
+    case 5: return make_float2(2.588190451e-01f, -9.659258263e-01f);
+    case 6: return make_float2(0.000000000e+00f, -1.000000000e+00f);
+    case 7: return make_float2(-2.588190451e-01f, -9.659258263e-01f);
+    case 8: return make_float2(-5.000000000e-01f, -8.660254038e-01f);
+    case 9: return make_float2(-7.071067812e-01f, -7.071067812e-01f);
+    case 10: return make_float2(-8.660254038e-01f, -5.000000000e-01f);
+    case 11: return make_float2(-9.659258263e-01f, -2.588190451e-01f);
+    case 12: return make_float2(-1.000000000e+00f, 0.000000000e+00f);
+    case 13: return make_float2(-9.659258263e-01f, 2.588190451e-01f);
+    case 14: return make_float2(-8.660254038e-01f, 5.000000000e-01f);
+    case 15: return make_float2(-7.071067812e-01f, 7.071067812e-01f);
+    case 16: return make_float2(-5.000000000e-01f, 8.660254038e-01f);
+    case 17: return make_float2(-2.588190451e-01f, 9.659258263e-01f);
+    case 18: return make_float2(0.000000000e+00f, 1.000000000e+00f);
+    case 19: return make_float2(2.588190451e-01f, 9.659258263e-01f);
+    case 20: return make_float2(5.000000000e-01f, 8.660254038e-01f);
+    case 21: return make_float2(7.071067812e-01f, 7.071067812e-01f);
+    case 22: return make_float2(8.660254038e-01f, 5.000000000e-01f);
+    case 23: return make_float2(9.659258263e-01f, 2.588190451e-01f);
+    default: return make_float2(1.f, 0.f);
+  }
+}
 
 constexpr int FAST_THREADS = 256;
 
@@ -435,8 +502,8 @@ __host__ __device__ constexpr int ilog2_c(int n) { return n <= 1 ? 0 : 1 + ilog2
 template <int N, int SIGN>
 __device__ __forceinline__ float2 twr(int j) {
   float2 w;
-  if (32 % N == 0) w = c_tw32[j * (32 / N)];
-  else w = c_tw24[j * (24 / N)];
+  if (32 % N == 0) w = tw32(j * (32 / N));
+  else w = tw24(j * (24 / N));
   if (SIGN > 0) w.y = -w.y;
   return w;
 }
@@ -848,7 +915,7 @@ __global__ void __launch_bounds__(FAST_THREADS)
 #undef ILM_CALL_IRF
 }
 
-__global__ void __launch_bounds__(FAST_THREADS)
+__global__ void __launch_bounds__(FAST_THREADS, 2)
     k_cols_fast(const ConvJobDev* __restrict__ jobs, int njobs, const int* __restrict__ bmap) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* sm = reinterpret_cast<float2*>(smem_raw);
@@ -885,25 +952,7 @@ int fast_group(int L) {
   return a > b ? a : b;
 }
 
-int ensure_fast_tables() {
-  static bool done = false;
-  static std::mutex mu;
-  std::lock_guard<std::mutex> lk(mu);
-  if (done) return ILM_OK;
-  float2 t32[32], t24[24];
-  for (int j = 0; j < 32; ++j) {
-    const double a = -2.0 * M_PI * j / 32.0;
-    t32[j] = make_float2((float)cos(a), (float)sin(a));
-  }
-  for (int j = 0; j < 24; ++j) {
-    const double a = -2.0 * M_PI * j / 24.0;
-    t24[j] = make_float2((float)cos(a), (float)sin(a));
-  }
-  ILM_CHECK_CUDA(cudaMemcpyToSymbol(c_tw32, t32, sizeof(t32)));
-  ILM_CHECK_CUDA(cudaMemcpyToSymbol(c_tw24, t24, sizeof(t24)));
-  done = true;
-  return ILM_OK;
-}
+int ensure_fast_tables() { return ILM_OK; }  // the register DFTs' factors are literals (tw32 / tw24)
 
 template <typename T>
 size_t rows_smem(int P1) { return (size_t)(3 * (P1 / 2) + 2) * sizeof(typename CT<T>::t); }
