@@ -280,6 +280,13 @@ int ilm_cache_create(ilm_grid_t g, int kind, int npts, const double* x, const do
   return ILM_OK;
 }
 
+int ilm_cache_update_points(ilm_cache_t c, const double* x, const double* y, const double* nrmx, const double* nrmy,
+                            const double* ds, ilm_stream_t stream) {
+  CHECK_CACHE(c);
+  ILM_REQUIRE(c->npts == 0 || (x && y && nrmx && nrmy && ds), "cache_update_points: null point array");
+  return cache_rebin_points(c, x, y, nrmx, nrmy, ds, as_stream(stream));
+}
+
 int ilm_cache_destroy(ilm_cache_t c) {
   delete c;
   return ILM_OK;

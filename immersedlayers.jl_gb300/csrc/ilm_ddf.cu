@@ -26,23 +26,23 @@ namespace ilm {
 // ---------------------------------------------------------------------------
 // DDF kernels (host, FP64) -- published formulas
 // ---------------------------------------------------------------------------
-static double ddf_eval(int ddf, double r) {
+__host__ __device__ inline double ddf_eval(int ddf, double r) {
   r = fabs(r);
   const double s3 = 1.7320508075688772935;
   switch (ddf) {
     case ILM_DDF_YANG3:  // Yang, Zhang, Li & Yang, JCP 228 (2009), smoothed 3-point
       if (r <= 1.0)
         return 17.0 / 48.0 + s3 * M_PI / 108.0 + r / 4.0 - r * r / 4.0 +
-               (1.0 - 2.0 * r) / 16.0 * sqrt(std::max(-12.0 * r * r + 12.0 * r + 1.0, 0.0)) -
+               (1.0 - 2.0 * r) / 16.0 * sqrt(fmax(-12.0 * r * r + 12.0 * r + 1.0, 0.0)) -
                s3 / 12.0 * asin(s3 / 2.0 * (2.0 * r - 1.0));
       if (r < 2.0)
         return 55.0 / 48.0 - s3 * M_PI / 108.0 - 13.0 * r / 12.0 + r * r / 4.0 +
-               (2.0 * r - 3.0) / 48.0 * sqrt(std::max(-12.0 * r * r + 36.0 * r - 23.0, 0.0)) +
+               (2.0 * r - 3.0) / 48.0 * sqrt(fmax(-12.0 * r * r + 36.0 * r - 23.0, 0.0)) +
                s3 / 36.0 * asin(s3 / 2.0 * (2.0 * r - 3.0));
       return 0.0;
     case ILM_DDF_ROMA:  // Roma, Peskin & Berger, JCP 153 (1999)
       if (r <= 0.5) return (1.0 + sqrt(1.0 - 3.0 * r * r)) / 3.0;
-      if (r < 1.5) return (5.0 - 3.0 * r - sqrt(std::max(1.0 - 3.0 * (1.0 - r) * (1.0 - r), 0.0))) / 6.0;
+      if (r < 1.5) return (5.0 - 3.0 * r - sqrt(fmax(1.0 - 3.0 * (1.0 - r) * (1.0 - r), 0.0))) / 6.0;
       return 0.0;
     case ILM_DDF_M4PRIME:  // Monaghan M4'
       if (r <= 1.0) return 1.0 - 2.5 * r * r + 1.5 * r * r * r;
@@ -60,7 +60,7 @@ static double ddf_eval(int ddf, double r) {
 
 // window of 4 taps covering the support: base = floor(r) - 1 (r = fractional
 // index of the point on that line), weights phi(base + t - r)
-static void ddf_window(int ddf, double r, int* base, double* w) {
+__host__ __device__ inline void ddf_window(int ddf, double r, int* base, double* w) {
   const int b = (int)floor(r) - 1;
   *base = b;
   for (int t = 0; t < NTAP; ++t) w[t] = ddf_eval(ddf, (double)(b + t) - r);
@@ -161,13 +161,19 @@ int cache_build_windows(ilm_cache_s* c) {
     tl.ntx = W.ntx[pc];
     tl.nty = W.nty[pc];
     ILM_TRY(upload(tl.ptr, W.tptr[pc].data(), W.tptr[pc].size()));
-    ILM_TRY(upload(tl.pts, W.tpts[pc].data(), W.tpts[pc].size()));
+    // candidate list with room for a re-binning (a point's window touches at
+    // most 2 x 2 tiles)
+    std::vector<int> pts = W.tpts[pc];
+    pts.resize(std::max<size_t>(pts.size(), (size_t)4 * std::max(N, 1)), 0);
+    ILM_TRY(upload(tl.pts, pts.data(), pts.size()));
     std::vector<int> ne;
     for (int t = 0; t < tl.ntx * tl.nty; ++t)
       if (W.tptr[pc][t + 1] > W.tptr[pc][t]) ne.push_back(t);
     tl.nne = (int)ne.size();
-    if (ne.empty()) ne.push_back(0);  // keep a valid (unused) upload
+    tl.nne_launch = tl.nne;
+    ne.resize(std::max<size_t>((size_t)tl.ntx * tl.nty, 1), 0);  // room for a re-binning
     ILM_TRY(upload(tl.ne, ne.data(), ne.size()));
+    ILM_TRY(upload(tl.ne_cnt, &tl.nne, 1));
   }
   return ILM_OK;
 }
@@ -194,7 +200,7 @@ __device__ __forceinline__ T coef_val(int code, const T* __restrict__ nx, const 
 // one point per thread, then every thread sums them in that order.
 template <typename T>
 __global__ void __launch_bounds__(TILE_X* TILE_Y)
-k_scatter(int n1, int n2, int ntx, const int* __restrict__ ne, const int* __restrict__ tptr,
+k_scatter(int n1, int n2, int ntx, const int* __restrict__ ne, const int* __restrict__ ne_cnt, const int* __restrict__ tptr,
           const int* __restrict__ tpts, const int* __restrict__ bx, const int* __restrict__ by,
           const T* __restrict__ wx, const T* __restrict__ wy, const T* __restrict__ wsc, const T* __restrict__ nx,
           const T* __restrict__ ny, const T* __restrict__ in1, int c1, const T* __restrict__ in2, int c2,
@@ -202,6 +208,7 @@ k_scatter(int n1, int n2, int ntx, const int* __restrict__ ne, const int* __rest
   constexpr int NB = TILE_X * TILE_Y;
   __shared__ int s_bx[NB], s_by[NB];
   __shared__ T s_amp[NB], s_wx[NB * NTAP], s_wy[NB * NTAP];
+  if ((int)blockIdx.x >= *ne_cnt) return;  // launched for an upper bound after a device re-binning
   const int t = ne[blockIdx.x];
   const int tx = t % ntx, ty = t / ntx;
   const int i = tx * TILE_X + threadIdx.x;
@@ -318,16 +325,16 @@ int launch_scatter(ilm_cache_s* c, int pc, const void* in1, int coef1, const voi
   const int dx = pc_dx(pc), dy = pc_dy(pc);
   dim3 blk(TILE_X, TILE_Y);
   ILM_TRY(fill_zero(out, sh.numel() * (c->dtype == ILM_F64 ? 8 : 4), st));
-  const int nb = tl.nne;
+  const int nb = tl.nne_launch;
   if (nb == 0) return ILM_OK;
   if (c->dtype == ILM_F64) {
-    k_scatter<double><<<nb, blk, 0, st>>>(sh.n1, sh.n2, tl.ntx, tl.ne.as<int>(), tl.ptr.as<int>(), tl.pts.as<int>(), c->bx[dx].as<int>(),
+    k_scatter<double><<<nb, blk, 0, st>>>(sh.n1, sh.n2, tl.ntx, tl.ne.as<int>(), tl.ne_cnt.as<int>(), tl.ptr.as<int>(), tl.pts.as<int>(), c->bx[dx].as<int>(),
                                           c->by[dy].as<int>(), c->wx[dx].as<double>(), c->wy[dy].as<double>(),
                                           c->wscale.as<double>(), c->nx.as<double>(), c->ny.as<double>(),
                                           static_cast<const double*>(in1), coef1, static_cast<const double*>(in2),
                                           coef2, static_cast<double*>(out));
   } else {
-    k_scatter<float><<<nb, blk, 0, st>>>(sh.n1, sh.n2, tl.ntx, tl.ne.as<int>(), tl.ptr.as<int>(), tl.pts.as<int>(), c->bx[dx].as<int>(),
+    k_scatter<float><<<nb, blk, 0, st>>>(sh.n1, sh.n2, tl.ntx, tl.ne.as<int>(), tl.ne_cnt.as<int>(), tl.ptr.as<int>(), tl.pts.as<int>(), c->bx[dx].as<int>(),
                                          c->by[dy].as<int>(), c->wx[dx].as<float>(), c->wy[dy].as<float>(),
                                          c->wscale.as<float>(), c->nx.as<float>(), c->ny.as<float>(),
                                          static_cast<const float*>(in1), coef1, static_cast<const float*>(in2), coef2,
@@ -374,6 +381,248 @@ int launch_gather(ilm_cache_s* c, const GatherTerm* terms, int nterms, void* out
                                        static_cast<float*>(out), accumulate ? 1 : 0, (float)scale);
   }
   ILM_CHECK_LAUNCH();
+  return ILM_OK;
+}
+
+}  // namespace ilm
+
+// ---------------------------------------------------------------------------
+// Device re-binning of a cache's points (moving bodies): windows, point
+// arrays and tile candidate lists recomputed on the device from new point
+// data, with the grid, FFT plans and scratch of the cache kept.
+// ---------------------------------------------------------------------------
+namespace ilm {
+
+struct RebinPtrs {
+  const double *x, *y, *nx, *ny, *ds;
+  int* bx[2];
+  int* by[2];
+  double* wx64[2];
+  double* wy64[2];
+  void* wx[2];
+  void* wy[2];
+  void *nxo, *nyo, *wsc;  // cache dtype
+  double *nx64, *ny64, *ds64, *x64, *y64;
+};
+
+template <typename T>
+__global__ void k_rebin_points(int N, RebinPtrs P, double h, int i0x, int i0y, int ddf, int grid_scaling) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= N) return;
+  const double xk = P.x[k], yk = P.y[k];
+  for (int dual = 0; dual < 2; ++dual) {
+    const double off = dual ? 0.5 : 1.0;
+    const double rx = xk / h + i0x - off;
+    const double ry = yk / h + i0y - off;
+    double w[NTAP];
+    int b;
+    ddf_window(ddf, rx, &b, w);
+    P.bx[dual][k] = b;
+    for (int t = 0; t < NTAP; ++t) {
+      P.wx64[dual][(size_t)k * NTAP + t] = w[t];
+      static_cast<T*>(P.wx[dual])[(size_t)k * NTAP + t] = (T)w[t];
+    }
+    ddf_window(ddf, ry, &b, w);
+    P.by[dual][k] = b;
+    for (int t = 0; t < NTAP; ++t) {
+      P.wy64[dual][(size_t)k * NTAP + t] = w[t];
+      static_cast<T*>(P.wy[dual])[(size_t)k * NTAP + t] = (T)w[t];
+    }
+  }
+  static_cast<T*>(P.nxo)[k] = (T)P.nx[k];
+  static_cast<T*>(P.nyo)[k] = (T)P.ny[k];
+  static_cast<T*>(P.wsc)[k] = (T)(grid_scaling ? P.ds[k] / (h * h) : 1.0);
+  P.nx64[k] = P.nx[k];
+  P.ny64[k] = P.ny[k];
+  P.ds64[k] = P.ds[k];
+  P.x64[k] = xk;
+  P.y64[k] = yk;
+}
+
+// tiles of a position class touched by a point's 4 x 4 window (the host rule)
+__device__ __forceinline__ bool window_tiles(int b0, int e0, int n1, int n2, int* tx0, int* tx1, int* ty0,
+                                             int* ty1) {
+  int b1 = b0 + NTAP - 1, e1 = e0 + NTAP - 1;
+  b0 = max(b0, 0);
+  e0 = max(e0, 0);
+  b1 = min(b1, n1 - 1);
+  e1 = min(e1, n2 - 1);
+  if (b0 > b1 || e0 > e1) return false;
+  *tx0 = b0 / TILE_X;
+  *tx1 = b1 / TILE_X;
+  *ty0 = e0 / TILE_Y;
+  *ty1 = e1 / TILE_Y;
+  return true;
+}
+
+__global__ void k_tile_count(int N, const int* __restrict__ bx, const int* __restrict__ by, int n1, int n2, int ntx,
+                             int* __restrict__ cnt) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= N) return;
+  int a0, a1, b0, b1;
+  if (!window_tiles(bx[k], by[k], n1, n2, &a0, &a1, &b0, &b1)) return;
+  for (int ty = b0; ty <= b1; ++ty)
+    for (int tx = a0; tx <= a1; ++tx) atomicAdd(&cnt[ty * ntx + tx], 1);
+}
+
+// one CTA (1024 threads): ptr = exclusive scan of cnt, cursor = ptr, the
+// occupied tiles in tile order and their number
+__global__ void __launch_bounds__(1024) k_tile_scan(int nt, const int* __restrict__ cnt, int* __restrict__ ptr,
+                                                    int* __restrict__ cursor, int* __restrict__ ne,
+                                                    int* __restrict__ ne_cnt) {
+  __shared__ int s_sum[1024], s_occ[1024];
+  const int T = blockDim.x, i = threadIdx.x;
+  const int chunk = (nt + T - 1) / T;
+  const int a = min(nt, i * chunk), b = min(nt, a + chunk);
+  int sum = 0, occ = 0;
+  for (int t = a; t < b; ++t) {
+    sum += cnt[t];
+    occ += cnt[t] > 0;
+  }
+  s_sum[i] = sum;
+  s_occ[i] = occ;
+  __syncthreads();
+  if (i == 0) {  // exclusive scan of the per-thread totals (fixed order)
+    int rs = 0, ro = 0;
+    for (int j = 0; j < T; ++j) {
+      const int vs = s_sum[j], vo = s_occ[j];
+      s_sum[j] = rs;
+      s_occ[j] = ro;
+      rs += vs;
+      ro += vo;
+    }
+    ptr[nt] = rs;
+    *ne_cnt = ro;
+  }
+  __syncthreads();
+  int run = s_sum[i], o = s_occ[i];
+  for (int t = a; t < b; ++t) {
+    ptr[t] = run;
+    cursor[t] = run;
+    run += cnt[t];
+    if (cnt[t] > 0) ne[o++] = t;
+  }
+}
+
+__global__ void k_tile_fill(int N, const int* __restrict__ bx, const int* __restrict__ by, int n1, int n2, int ntx,
+                            int* __restrict__ cursor, int* __restrict__ pts) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= N) return;
+  int a0, a1, b0, b1;
+  if (!window_tiles(bx[k], by[k], n1, n2, &a0, &a1, &b0, &b1)) return;
+  for (int ty = b0; ty <= b1; ++ty)
+    for (int tx = a0; tx <= a1; ++tx) pts[atomicAdd(&cursor[ty * ntx + tx], 1)] = k;
+}
+
+// each tile's candidates in point order (the scatter sums them in list order)
+__global__ void k_tile_sort(int nt, const int* __restrict__ ptr, int* __restrict__ pts) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nt) return;
+  const int a = ptr[t], b = ptr[t + 1];
+  for (int i = a + 1; i < b; ++i) {
+    const int v = pts[i];
+    int j = i - 1;
+    while (j >= a && pts[j] > v) {
+      pts[j + 1] = pts[j];
+      --j;
+    }
+    pts[j + 1] = v;
+  }
+}
+
+int cache_rebin_points(ilm_cache_s* c, const double* x, const double* y, const double* nx, const double* ny,
+                       const double* ds, cudaStream_t st) {
+  const int N = c->npts;
+  if (!c->x64.p) {
+    ILM_TRY(c->x64.alloc((size_t)std::max(N, 1) * sizeof(double)));
+    ILM_TRY(c->y64.alloc((size_t)std::max(N, 1) * sizeof(double)));
+  }
+  int ntmax = 1;
+  for (int pc = 0; pc < 4; ++pc) ntmax = std::max(ntmax, c->tiles[pc].ntx * c->tiles[pc].nty);
+  if (c->rebin_cnt.bytes < (size_t)ntmax * sizeof(int)) {
+    ILM_TRY(c->rebin_cnt.alloc((size_t)ntmax * sizeof(int)));
+    ILM_TRY(c->rebin_cur.alloc((size_t)ntmax * sizeof(int)));
+  }
+  if (N == 0) return ILM_OK;
+  RebinPtrs P;
+  P.x = x;
+  P.y = y;
+  P.nx = nx;
+  P.ny = ny;
+  P.ds = ds;
+  for (int d = 0; d < 2; ++d) {
+    P.bx[d] = c->bx[d].as<int>();
+    P.by[d] = c->by[d].as<int>();
+    P.wx64[d] = c->wx64[d].as<double>();
+    P.wy64[d] = c->wy64[d].as<double>();
+    P.wx[d] = c->wx[d].p;
+    P.wy[d] = c->wy[d].p;
+  }
+  P.nxo = c->nx.p;
+  P.nyo = c->ny.p;
+  P.wsc = c->wscale.p;
+  P.nx64 = c->nx64.as<double>();
+  P.ny64 = c->ny64.as<double>();
+  P.ds64 = c->ds64.as<double>();
+  P.x64 = c->x64.as<double>();
+  P.y64 = c->y64.as<double>();
+  const int pb = (N + 255) / 256;
+  if (c->dtype == ILM_F64)
+    k_rebin_points<double><<<pb, 256, 0, st>>>(N, P, c->h, c->grid.i0x, c->grid.i0y, c->ddf,
+                                                c->scaling == ILM_GRID_SCALING);
+  else
+    k_rebin_points<float><<<pb, 256, 0, st>>>(N, P, c->h, c->grid.i0x, c->grid.i0y, c->ddf,
+                                               c->scaling == ILM_GRID_SCALING);
+  ILM_CHECK_LAUNCH();
+  for (int pc = 0; pc < 4; ++pc) {
+    TileList& tl = c->tiles[pc];
+    const Shape2 sh = c->grid.shape(pc);
+    const int nt = tl.ntx * tl.nty, dx = pc_dx(pc), dy = pc_dy(pc);
+    ILM_CHECK_CUDA(cudaMemsetAsync(c->rebin_cnt.p, 0, (size_t)nt * sizeof(int), st));
+    k_tile_count<<<pb, 256, 0, st>>>(N, c->bx[dx].as<int>(), c->by[dy].as<int>(), sh.n1, sh.n2, tl.ntx,
+                                     c->rebin_cnt.as<int>());
+    ILM_CHECK_LAUNCH();
+    k_tile_scan<<<1, 1024, 0, st>>>(nt, c->rebin_cnt.as<int>(), tl.ptr.as<int>(), c->rebin_cur.as<int>(),
+                                    tl.ne.as<int>(), tl.ne_cnt.as<int>());
+    ILM_CHECK_LAUNCH();
+    k_tile_fill<<<pb, 256, 0, st>>>(N, c->bx[dx].as<int>(), c->by[dy].as<int>(), sh.n1, sh.n2, tl.ntx,
+                                    c->rebin_cur.as<int>(), tl.pts.as<int>());
+    ILM_CHECK_LAUNCH();
+    k_tile_sort<<<(nt + 255) / 256, 256, 0, st>>>(nt, tl.ptr.as<int>(), tl.pts.as<int>());
+    ILM_CHECK_LAUNCH();
+    // the exact count is on the device; launches cover the largest possible
+    tl.nne_launch = std::min(nt, 4 * N);
+  }
+  c->host_stale = true;
+  c->S_dir_ready = false;
+  c->S_neu_ready = false;
+  return ILM_OK;
+}
+
+// host copies (points, windows) brought up to date after device re-binnings
+int cache_sync_host(ilm_cache_s* c) {
+  if (!c->host_stale) return ILM_OK;
+  const size_t N = (size_t)c->npts;
+  ILM_CHECK_CUDA(cudaDeviceSynchronize());
+  c->hx.resize(N);
+  c->hy.resize(N);
+  c->hnx.resize(N);
+  c->hny.resize(N);
+  c->hds.resize(N);
+  ILM_CHECK_CUDA(cudaMemcpy(c->hx.data(), c->x64.p, N * 8, cudaMemcpyDeviceToHost));
+  ILM_CHECK_CUDA(cudaMemcpy(c->hy.data(), c->y64.p, N * 8, cudaMemcpyDeviceToHost));
+  ILM_CHECK_CUDA(cudaMemcpy(c->hnx.data(), c->nx64.p, N * 8, cudaMemcpyDeviceToHost));
+  ILM_CHECK_CUDA(cudaMemcpy(c->hny.data(), c->ny64.p, N * 8, cudaMemcpyDeviceToHost));
+  ILM_CHECK_CUDA(cudaMemcpy(c->hds.data(), c->ds64.p, N * 8, cudaMemcpyDeviceToHost));
+  HostWindows W;
+  host_windows(c->grid, c->ddf, c->npts, c->hx.data(), c->hy.data(), &W);
+  for (int d = 0; d < 2; ++d) {
+    c->hbx[d] = W.bx[d];
+    c->hby[d] = W.by[d];
+    c->hwx[d] = W.wx[d];
+    c->hwy[d] = W.wy[d];
+  }
+  c->host_stale = false;
   return ILM_OK;
 }
 

@@ -315,6 +315,7 @@ extern "C" {
 
 int ilm_heat_create(ilm_cache_t c, double kappa, double dt, const double* tb_plus, const double* tb_minus,
                     double tol, int maxiter, ilm_heat_t* out) {
+  if (c) ILM_TRY(cache_sync_host(c));  // host windows used below
   ILM_REQUIRE(c && out && tb_plus && tb_minus, "heat: null argument");
   ILM_REQUIRE(c->kind == ILM_CACHE_SCALAR, "heat: scalar cache required");
   ILM_REQUIRE(c->scaling == ILM_GRID_SCALING, "heat: GridScaling cache required");

@@ -152,10 +152,12 @@ struct PointWin {
 
 // tile candidate list for one position class
 struct TileList {
-  DevBuf ptr;   // int [ntiles+1]
-  DevBuf pts;   // int [nnz]
-  DevBuf ne;    // int [nne]: the tiles with at least one candidate point
+  DevBuf ptr;     // int [ntiles+1]
+  DevBuf pts;     // int [capacity >= 4 npts]
+  DevBuf ne;      // int [ntiles]: the tiles with at least one candidate point (first ne_cnt)
+  DevBuf ne_cnt;  // int: their number (device copy)
   int ntx = 0, nty = 0, nne = 0;
+  int nne_launch = 0;  // scatter grid: nne, or an upper bound after a device re-binning
 };
 // out[0, n) = 0 (16-byte stores where aligned); the scatters fill their
 // output with it and then visit only the tiles that hold points
@@ -249,6 +251,9 @@ struct ilm_cache_s {
   std::vector<int> hbx[2], hby[2];
   std::vector<double> hwx[2], hwy[2];  // host copies of the window weights
   ilm::TileList tiles[4];
+  ilm::DevBuf x64, y64;                // FP64 point coordinates (device; set by a re-binning)
+  ilm::DevBuf rebin_cnt, rebin_cur;    // re-binning scratch (int per tile)
+  bool host_stale = false;             // host copies behind the device after ilm_cache_update_points
   // inverse Laplacian plans per position class
   ilm::ConvPlan conv[4];
   bool conv_ready[4] = {false, false, false, false};
@@ -284,6 +289,11 @@ struct HostWindows {
 };
 void host_windows(const ilm_grid_s& g, int ddf, int N, const double* x, const double* y, HostWindows* W);
 int cache_build_windows(ilm_cache_s* c);
+// device re-binning of the cache's points (ilm_cache_update_points); the
+// host copies are refreshed lazily by cache_sync_host
+int cache_rebin_points(ilm_cache_s* c, const double* x, const double* y, const double* nx, const double* ny,
+                       const double* ds, cudaStream_t st);
+int cache_sync_host(ilm_cache_s* c);
 // out_pc(cell) = sum_k w_k (a_k in1_k + b_k in2_k) phi phi ; in2 may be null
 int launch_scatter(ilm_cache_s* c, int pc, const void* in1, int coef1, const void* in2, int coef2,
                    void* out, cudaStream_t st);

@@ -21,7 +21,7 @@ from .core import (Dual, EdgeGradient, EdgeGradientPrimal, Edges, EdgesDual, Edg
                    zeros_grid, zeros_gridcurl, zeros_griddiv, zeros_gridgrad, zeros_surface, zeros_surfacescalar)
 from .problems import (DirichletPoissonProblem, ILMProblem, ILMSystem, NeumannPoissonProblem, StokesFlowProblem,
                        construct_system, prescribed_surface_average_, prescribed_surface_jump_, solve,
-                       solve_dirichlet, solve_neumann, solve_stokes)
+                       solve_dirichlet, solve_neumann, solve_stokes, update_system_)
 from .timemarching import (ConstrainedSolution, DirichletHeatConductionProblem, HeatIntegrator, constraint, init,
                            init_sol, state, step_, temperature, timestep, timestep_fourier)
 

@@ -56,6 +56,7 @@ SIGNATURES = {
     "ilm_grid_numel": [_VP, _I, C.POINTER(C.c_size_t)],
     "ilm_cache_create": [_VP, _I, _I, _DP, _DP, _DP, _DP, _DP, _I, _I, _I, C.POINTER(_VP)],
     "ilm_cache_destroy": [_VP],
+    "ilm_cache_update_points": [_VP, _VP, _VP, _VP, _VP, _VP, _VP],
     "ilm_cache_npts": [_VP, C.POINTER(_I)],
     "ilm_regularize": [_VP, _I, _VP, _VP, _VP],
     "ilm_interpolate": [_VP, _I, _VP, _VP, _VP],

@@ -300,6 +300,21 @@ class BasicILMCache:
     def _surf_type(self):
         return ScalarData if self.kind == L.CACHE_SCALAR else VectorData
 
+    def update_points_(self, x, y, nx, ny, ds, stream=None):
+        """Moving bodies: new point positions, normals and areas (device
+        float64 tensors of the same length), re-binned on the device without
+        rebuilding the cache (the cache rebuild of update_system,
+        src/system.jl:26-49)."""
+        t = [torch.as_tensor(a, dtype=torch.float64, device="cuda").contiguous() for a in (x, y, nx, ny, ds)]
+        if any(a.numel() != self.N for a in t):
+            raise ValueError(f"update_points_: {self.N} points expected")
+        L.call("ilm_cache_update_points", self._h, *[_ptr(a) for a in t], _stream_ptr(stream))
+        self._dev_points = t  # keep the inputs alive until the stream has used them
+        self.pts.data.copy_(torch.cat([t[0], t[1]]).to(self.dtype))
+        self.nrm.data.copy_(torch.cat([t[2], t[3]]).to(self.dtype))
+        self.ds.data.copy_(t[4].to(self.dtype))
+        return self
+
 
 def SurfaceScalarCache(bodies, grid, ddftype="Yang3", scaling=GridScaling, dtype=torch.float64):
     return BasicILMCache(bodies, grid, L.CACHE_SCALAR, ddftype, scaling, dtype)

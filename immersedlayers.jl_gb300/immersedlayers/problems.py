@@ -13,6 +13,7 @@ import numpy as np
 import torch
 
 from . import _lib as L
+from .bodies import as_bodylist
 from .core import (GridScaling, NodesPrimal, PointData, ScalarData, SurfaceScalarCache, SurfaceVectorCache,
                    _ptr, _stream_ptr, zeros_grid, zeros_surface)
 
@@ -70,6 +71,17 @@ def construct_system(prob: ILMProblem) -> ILMSystem:
     base = mk(prob.bodies, prob.g, ddftype=prob.ddftype, scaling=prob.scaling, dtype=prob.dtype)
     return ILMSystem(base, prob_cache(prob, base), prob.bc, prob.phys_params, prob.forcing, prob.motions,
                      prob.timestep_func)
+
+
+def update_system_(sys: ILMSystem, bodies, stream=None) -> ILMSystem:
+    """update_system!(sys, u, sysold, t) / update_system(sysold, bodies)
+    (src/system.jl:26-49): the system for a new configuration of its bodies.
+    The reference regenerates the problem and rebuilds every cache; here the
+    base cache re-bins the new points on the device (same point count)."""
+    bl = as_bodylist(bodies)
+    sys.base_cache.update_points_(bl.x, bl.y, bl.nx, bl.ny, bl.ds, stream=stream)
+    sys.base_cache.bl = bl
+    return sys
 
 
 def _as_point(v, like: PointData):

@@ -115,6 +115,16 @@ ILM_API int ilm_cache_create(ilm_grid_t g, int kind, int npts,
                      const double* x, const double* y,
                      const double* nrmx, const double* nrmy, const double* ds,
                      int ddf, int scaling, int dtype, ilm_cache_t* out);
+/* Moving bodies: replace the cache's points by new positions, normals and
+ * areas (same number of points; DEVICE FP64 arrays of npts each) and redo
+ * the DDF windows, the point arrays and the tile candidate lists on the
+ * device, in stream order, keeping the grid, the FFT plans and the scratch.
+ * Replaces the cache rebuild of update_system / update_system!
+ * (src/system.jl:26-49, regenerate_problem src/problem.jl:95-105), which
+ * constructs new regularization matrices for the new body configuration.
+ * Cached Schur complements are invalidated; no host synchronisation.      */
+ILM_API int ilm_cache_update_points(ilm_cache_t c, const double* x, const double* y, const double* nrmx,
+                                    const double* nrmy, const double* ds, ilm_stream_t stream);
 ILM_API int ilm_cache_destroy(ilm_cache_t c);
 ILM_API int ilm_cache_npts(ilm_cache_t c, int* npts);
 
