@@ -51,6 +51,7 @@ def parse():
     ap.add_argument("--heat-steps", type=int, default=1000, help="heat-conduction leg (0: skip)")
     ap.add_argument("--learned-nprob", type=int, default=256, help="learned-preconditioner leg (0: skip)")
     ap.add_argument("--stokes", type=int, default=1, help="Stokes leg (0: skip)")
+    ap.add_argument("--moving", type=int, default=1, help="moving-body re-binning leg (0: skip)")
     ap.add_argument("--profile-solves", type=int, default=0,
                     help="profiling driver: set up the batch with the default solver, run this many solves on a "
                          "created stream and exit (no timing, no JSON line)")
@@ -270,6 +271,7 @@ def run_ours(args, rank, world, dist):
     heat = _heat_scale(args, stream) if (rank == 0 and args.heat_steps > 0) else None
     learned = _learned_leg(args) if (rank == 0 and args.learned_nprob > 0) else None
     stokes = _stokes_leg(args) if (rank == 0 and args.stokes) else None
+    moving = _moving_leg(stream) if (rank == 0 and args.moving) else None
     if learned and "none" in learned:
         solvers["learned_pcg_star"] = {"workload": learned["workload"], **learned["learned"],
                                        "plain_cg_same_problems": learned["none"]}
@@ -280,7 +282,7 @@ def run_ours(args, rank, world, dist):
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
                 "config": config(args, world), "roofline": roofline, "e2e": e2e, "gpu_launches": launches * args.steps,
                 "clocks": clocks, "setup_s": setup_s, "solvers": solvers, "autotune": tuned, "stencil_gbs": stencil,
-                "heat": heat, "learned": learned, "stokes": stokes,
+                "heat": heat, "learned": learned, "stokes": stokes, "moving": moving,
                 "stages_ms": dict(zip(names, [round(x, 4) for x in stage_ms])),
                 "cg_iterations": {"mean": float(np.mean(its)), "max": int(its.max())},
                 "max_rel_residual": float(rr.max())}
@@ -439,6 +441,64 @@ def _stokes_leg(args):
 
 
 _NET = {}
+
+
+def _moving_leg(stream):
+    """Moving bodies on the Stokes configuration's geometry (8192 points,
+    2048^2 grid, FP32 scalar cache): a rigid motion of all bodies per step,
+    re-binned on the device (update_points_) against building a new cache
+    from host points (the reference's update_system rebuild); each step
+    followed by a regularize onto Nodes{Primal}."""
+    import math
+    import numpy as np
+    import torch
+    import immersedlayers as il
+    from immersedlayers import workloads as W
+    d = W.stokes_scale(nrhs=1)
+    g = il.PhysicalGrid(h=d["h"], nx=d["n"])
+    bl = d["bodies"]
+    c = il.SurfaceScalarCache(bl, g, dtype=torch.float32)
+    f = il.ScalarData(torch.randn(len(bl), device="cuda"))
+    w = il.NodesPrimal.zeros(g, torch.float32)
+    x0 = torch.tensor(bl.x, device="cuda", dtype=torch.float64)
+    y0 = torch.tensor(bl.y, device="cuda", dtype=torch.float64)
+    nx0 = torch.tensor(bl.nx, device="cuda", dtype=torch.float64)
+    ny0 = torch.tensor(bl.ny, device="cuda", dtype=torch.float64)
+    ds0 = torch.tensor(bl.ds, device="cuda", dtype=torch.float64)
+    steps = 20
+
+    def moved(k):
+        th = 0.01 * k
+        cs, sn = math.cos(th), math.sin(th)
+        return (cs * x0 - sn * y0 + 1e-3 * k, sn * x0 + cs * y0, cs * nx0 - sn * ny0, sn * nx0 + cs * ny0, ds0)
+
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):  # the moved points are computed on the same stream
+        for k in range(3):
+            c.update_points_(*moved(k), stream=stream)
+            il.regularize_(w, f, c, stream=stream)
+    stream.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        for k in range(steps):
+            c.update_points_(*moved(k), stream=stream)
+            il.regularize_(w, f, c, stream=stream)
+        e1.record(stream)
+    stream.synchronize()
+    dev_ms = e0.elapsed_time(e1) / steps
+    hx = [m.cpu().numpy() for m in moved(1)]
+    from immersedlayers import bodies as B
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(3):
+        c2 = il.SurfaceScalarCache(B.Body(*hx), g, dtype=torch.float32)
+        il.regularize_(w, f, c2)
+    torch.cuda.synchronize()
+    rebuild_ms = 1000 * (time.perf_counter() - t0) / 3
+    return {"workload": "8192 points (2 circles + 2 plates), 2048^2 dual nodes, FP32 scalar cache, rigid motion per step",
+            "update_points_and_regularize_ms": dev_ms, "rebuild_cache_and_regularize_ms": rebuild_ms}
 
 
 def _prepare_learned(bs, block=64):

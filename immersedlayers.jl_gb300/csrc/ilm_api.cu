@@ -313,6 +313,28 @@ int ilm_regularize(ilm_cache_t c, int out_kind, const void* f, void* out, ilm_st
   return ILM_ERR_INVALID_ARG;
 }
 
+int ilm_regularize_add(ilm_cache_t c, int out_kind, const void* f, void* out, ilm_stream_t stream) {
+  CHECK_CACHE(c);
+  cudaStream_t st = as_stream(stream);
+  switch (out_kind) {
+    case ILM_NODES_PRIMAL: return launch_scatter(c, PC_P, f, CF_ONE, nullptr, CF_ZERO, out, st, true);
+    case ILM_NODES_DUAL: return launch_scatter(c, PC_D, f, CF_ONE, nullptr, CF_ZERO, out, st, true);
+    case ILM_EDGES_PRIMAL: {
+      ILM_TRY(launch_scatter(c, PC_U, f, CF_ONE, nullptr, CF_ZERO, out, st, true));
+      void* vout = comp_ptr(&c->grid, ILM_EDGES_PRIMAL, c->dtype, out, 1);
+      return launch_scatter(c, PC_V, ptr_off(f, c->npts, c->dtype), CF_ONE, nullptr, CF_ZERO, vout, st, true);
+    }
+  }
+  set_error("regularize_add: unsupported output kind %d", out_kind);
+  return ILM_ERR_INVALID_ARG;
+}
+
+int ilm_grid_mul_add(size_t n, int dtype, const void* a, const void* b, void* out, ilm_stream_t stream) {
+  ILM_REQUIRE(dtype == ILM_F64 || dtype == ILM_F32, "grid_mul_add: bad dtype %d", dtype);
+  ILM_REQUIRE(n == 0 || (a && b && out), "grid_mul_add: null argument");
+  return st_mul_add(n, dtype, a, b, out, as_stream(stream));
+}
+
 int ilm_interpolate(ilm_cache_t c, int in_kind, const void* s, void* f, ilm_stream_t stream) {
   CHECK_CACHE(c);
   cudaStream_t st = as_stream(stream);

@@ -204,7 +204,7 @@ k_scatter(int n1, int n2, int ntx, const int* __restrict__ ne, const int* __rest
           const int* __restrict__ tpts, const int* __restrict__ bx, const int* __restrict__ by,
           const T* __restrict__ wx, const T* __restrict__ wy, const T* __restrict__ wsc, const T* __restrict__ nx,
           const T* __restrict__ ny, const T* __restrict__ in1, int c1, const T* __restrict__ in2, int c2,
-          T* __restrict__ out) {
+          T* __restrict__ out, int accumulate) {
   constexpr int NB = TILE_X * TILE_Y;
   __shared__ int s_bx[NB], s_by[NB];
   __shared__ T s_amp[NB], s_wx[NB * NTAP], s_wy[NB * NTAP];
@@ -240,7 +240,10 @@ k_scatter(int n1, int n2, int ntx, const int* __restrict__ ne, const int* __rest
     }
     __syncthreads();
   }
-  if (i < n1 && j < n2) out[(size_t)j * n1 + i] = acc;
+  if (i < n1 && j < n2) {
+    T* o = out + (size_t)j * n1 + i;
+    *o = accumulate ? *o + acc : acc;
+  }
 }
 
 __global__ void k_fill_zero(float4* __restrict__ p4, size_t n4, unsigned char* __restrict__ tail, int ntail) {
@@ -319,12 +322,14 @@ int fill_zero(void* out, size_t bytes, cudaStream_t st) {
 }
 
 int launch_scatter(ilm_cache_s* c, int pc, const void* in1, int coef1, const void* in2, int coef2, void* out,
-                   cudaStream_t st) {
+                   cudaStream_t st, bool accumulate) {
   const Shape2 sh = c->grid.shape(pc);
   const TileList& tl = c->tiles[pc];
   const int dx = pc_dx(pc), dy = pc_dy(pc);
   dim3 blk(TILE_X, TILE_Y);
-  ILM_TRY(fill_zero(out, sh.numel() * (c->dtype == ILM_F64 ? 8 : 4), st));
+  // overwrite: zero fill, then the occupied tiles; accumulate: the occupied
+  // tiles only (the others add nothing)
+  if (!accumulate) ILM_TRY(fill_zero(out, sh.numel() * (c->dtype == ILM_F64 ? 8 : 4), st));
   const int nb = tl.nne_launch;
   if (nb == 0) return ILM_OK;
   if (c->dtype == ILM_F64) {
@@ -332,13 +337,13 @@ int launch_scatter(ilm_cache_s* c, int pc, const void* in1, int coef1, const voi
                                           c->by[dy].as<int>(), c->wx[dx].as<double>(), c->wy[dy].as<double>(),
                                           c->wscale.as<double>(), c->nx.as<double>(), c->ny.as<double>(),
                                           static_cast<const double*>(in1), coef1, static_cast<const double*>(in2),
-                                          coef2, static_cast<double*>(out));
+                                          coef2, static_cast<double*>(out), accumulate ? 1 : 0);
   } else {
     k_scatter<float><<<nb, blk, 0, st>>>(sh.n1, sh.n2, tl.ntx, tl.ne.as<int>(), tl.ne_cnt.as<int>(), tl.ptr.as<int>(), tl.pts.as<int>(), c->bx[dx].as<int>(),
                                          c->by[dy].as<int>(), c->wx[dx].as<float>(), c->wy[dy].as<float>(),
                                          c->wscale.as<float>(), c->nx.as<float>(), c->ny.as<float>(),
                                          static_cast<const float*>(in1), coef1, static_cast<const float*>(in2), coef2,
-                                         static_cast<float*>(out));
+                                         static_cast<float*>(out), accumulate ? 1 : 0);
   }
   ILM_CHECK_LAUNCH();
   return ILM_OK;

@@ -296,12 +296,13 @@ int cache_rebin_points(ilm_cache_s* c, const double* x, const double* y, const d
 int cache_sync_host(ilm_cache_s* c);
 // out_pc(cell) = sum_k w_k (a_k in1_k + b_k in2_k) phi phi ; in2 may be null
 int launch_scatter(ilm_cache_s* c, int pc, const void* in1, int coef1, const void* in2, int coef2,
-                   void* out, cudaStream_t st);
+                   void* out, cudaStream_t st, bool accumulate = false);
 // out_k (+)= sum_t coef_t * E_{pc_t} arr_t
 int launch_gather(ilm_cache_s* c, const GatherTerm* terms, int nterms, void* out, bool accumulate,
                   double scale, cudaStream_t st);
 
 // stencils (ilm_stencil.cu); scale multiplies the result
+int st_mul_add(size_t n, int dtype, const void* a, const void* b, void* out, cudaStream_t st);  // out += a b
 int st_div_edges(const ilm_grid_s* g, int dtype, const void* q, void* w, double scale, cudaStream_t st);
 int st_grad_nodes(const ilm_grid_s* g, int dtype, const void* w, void* q, double scale, cudaStream_t st);
 int st_curl_dual_to_edges(const ilm_grid_s* g, int dtype, const void* s, void* q, double scale, cudaStream_t st);

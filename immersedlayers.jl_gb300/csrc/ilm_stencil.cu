@@ -189,6 +189,13 @@ __global__ void k_p2e(int NX, int NY, const T* __restrict__ p, T* __restrict__ u
   }
 }
 
+// out += a * b (elementwise)
+template <typename T>
+__global__ void k_mul_add(size_t n, const T* __restrict__ a, const T* __restrict__ b, T* __restrict__ out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    out[i] += a[i] * b[i];
+}
+
 template <typename T>
 __global__ void k_axpby(size_t n, T a, const T* __restrict__ x, T b, const T* __restrict__ y, T* __restrict__ o) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
@@ -409,6 +416,16 @@ int st_axpby(size_t n, int dtype, double a, const void* x, double b, const void*
   DISPATCH(dtype, {
     k_axpby<T><<<nblocks(n), 256, 0, st>>>(n, (T)a, static_cast<const T*>(x), (T)b, static_cast<const T*>(y),
                                            static_cast<T*>(out));
+  });
+  ILM_CHECK_LAUNCH();
+  return ILM_OK;
+}
+
+int st_mul_add(size_t n, int dtype, const void* a, const void* b, void* out, cudaStream_t st) {
+  if (n == 0) return ILM_OK;
+  DISPATCH(dtype, {
+    k_mul_add<T><<<nblocks(n), 256, 0, st>>>(n, static_cast<const T*>(a), static_cast<const T*>(b),
+                                             static_cast<T*>(out));
   });
   ILM_CHECK_LAUNCH();
   return ILM_OK;

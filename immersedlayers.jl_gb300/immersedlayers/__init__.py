@@ -22,6 +22,8 @@ from .core import (Dual, EdgeGradient, EdgeGradientPrimal, Edges, EdgesDual, Edg
 from .problems import (DirichletPoissonProblem, ILMProblem, ILMSystem, NeumannPoissonProblem, StokesFlowProblem,
                        construct_system, prescribed_surface_average_, prescribed_surface_jump_, solve,
                        solve_dirichlet, solve_neumann, solve_stokes, update_system_)
+from .forcing import (AreaForcingModel, ForcingModelAndRegion, LineForcingModel, PointForcingModel, apply_forcing_,
+                      forcing_regions)
 from .timemarching import (ConstrainedSolution, DirichletHeatConductionProblem, HeatIntegrator, constraint, init,
                            init_sol, state, step_, temperature, timestep, timestep_fourier)
 

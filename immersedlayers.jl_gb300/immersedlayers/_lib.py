@@ -59,6 +59,8 @@ SIGNATURES = {
     "ilm_cache_update_points": [_VP, _VP, _VP, _VP, _VP, _VP, _VP],
     "ilm_cache_npts": [_VP, C.POINTER(_I)],
     "ilm_regularize": [_VP, _I, _VP, _VP, _VP],
+    "ilm_regularize_add": [_VP, _I, _VP, _VP, _VP],
+    "ilm_grid_mul_add": [C.c_size_t, _I, _VP, _VP, _VP, _VP],
     "ilm_interpolate": [_VP, _I, _VP, _VP, _VP],
     "ilm_regularize_normal": [_VP, _VP, _VP, _VP],
     "ilm_regularize_normal_symm": [_VP, _VP, _VP, _VP],

@@ -132,6 +132,13 @@ ILM_API int ilm_cache_npts(ilm_cache_t c, int* npts);
 /* regularize!(s::Nodes{Primal|Dual}, f::ScalarData) (:13,:25) and
  * regularize!(v::Edges{Primal}, vb::VectorData) (:36); output overwritten.  */
 ILM_API int ilm_regularize(ilm_cache_t c, int out_kind, const void* f, void* out, ilm_stream_t stream);
+/* Forcing (src/forcing.jl:451-515): out += R f without clearing `out` --
+ * the accumulation of line and point forcing (_apply_forcing! does
+ * fill!(gdata,0); regularize!(gdata,str,cache); dy .+= gdata); only the
+ * tiles that hold points are visited.  ilm_grid_mul_add: out += a .* b
+ * over n grid values (area forcing, dy .+= str .* mask).                   */
+ILM_API int ilm_regularize_add(ilm_cache_t c, int out_kind, const void* f, void* out, ilm_stream_t stream);
+ILM_API int ilm_grid_mul_add(size_t n, int dtype, const void* a, const void* b, void* out, ilm_stream_t stream);
 /* interpolate!(f, s::Nodes{Primal|Dual}) (:56,:67), interpolate!(vb, v::Edges{Primal}) (:78) */
 ILM_API int ilm_interpolate(ilm_cache_t c, int in_kind, const void* grid_in, void* f_out, ilm_stream_t stream);
 
