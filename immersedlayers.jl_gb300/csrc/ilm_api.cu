@@ -182,6 +182,15 @@ static int inverse_laplacian_kind(ilm_cache_s* c, int kind, const void* in, void
 
 }  // namespace ilm
 
+namespace ilm {
+// x <- x / d (0 where d = 0): the W^-1 of the surface filter
+template <typename T>
+__global__ void k_div_rows(int n, const T* __restrict__ d, const T* x, T* out) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) out[k] = d[k] != (T)0 ? x[k] / d[k] : (T)0;
+}
+}  // namespace ilm
+
 using namespace ilm;
 
 extern "C" {
@@ -356,6 +365,45 @@ int ilm_interpolate(ilm_cache_t c, int in_kind, const void* s, void* f, ilm_stre
   }
   set_error("interpolate: unsupported input kind %d", in_kind);
   return ILM_ERR_INVALID_ARG;
+}
+
+int ilm_surface_filter(ilm_cache_t c, int power, const void* s_in, void* s_out, ilm_stream_t stream) {
+  CHECK_CACHE(c);
+  ILM_REQUIRE(power >= 0, "surface_filter: negative power %d", power);
+  ILM_REQUIRE(c->npts == 0 || (s_in && s_out), "surface_filter: null argument");
+  cudaStream_t st = as_stream(stream);
+  const int gk = c->kind == ILM_CACHE_SCALAR ? ILM_NODES_PRIMAL : ILM_EDGES_PRIMAL;
+  const size_t n = (size_t)c->npts * (c->kind == ILM_CACHE_SCALAR ? 1 : 2);
+  const size_t es = esize(c->dtype);
+  if (n == 0) return ILM_OK;
+  if (power == 0) {
+    if (s_out != s_in) ILM_CHECK_CUDA(cudaMemcpyAsync(s_out, s_in, n * es, cudaMemcpyDeviceToDevice, st));
+    return ILM_OK;
+  }
+  ILM_TRY(c->filt_grid.alloc(gridkind_numel(&c->grid, gk) * es));
+  if (!c->filt_ready) {
+    // W = E R 1
+    ILM_TRY(c->filt_diag.alloc(n * es));
+    ILM_TRY(st_fill(n, c->dtype, 1.0, c->filt_diag.p, st));
+    ILM_TRY(ilm_regularize(c, gk, c->filt_diag.p, c->filt_grid.p, stream));
+    ILM_TRY(ilm_interpolate(c, gk, c->filt_grid.p, c->filt_diag.p, stream));
+    c->filt_ready = true;
+  }
+  const void* src = s_in;
+  for (int k = 0; k < power; ++k) {
+    ILM_TRY(ilm_regularize(c, gk, src, c->filt_grid.p, stream));
+    ILM_TRY(ilm_interpolate(c, gk, c->filt_grid.p, s_out, stream));
+    const int nb = (int)((n + 255) / 256);
+    if (c->dtype == ILM_F64)
+      k_div_rows<double><<<nb, 256, 0, st>>>((int)n, c->filt_diag.as<double>(), static_cast<const double*>(s_out),
+                                            static_cast<double*>(s_out));
+    else
+      k_div_rows<float><<<nb, 256, 0, st>>>((int)n, c->filt_diag.as<float>(), static_cast<const float*>(s_out),
+                                           static_cast<float*>(s_out));
+    ILM_CHECK_LAUNCH();
+    src = s_out;
+  }
+  return ILM_OK;
 }
 
 int ilm_regularize_normal(ilm_cache_t c, const void* f, void* out, ilm_stream_t stream) {
@@ -576,6 +624,68 @@ int ilm_curl(ilm_cache_t c, int in_kind, const void* in, void* out, ilm_stream_t
     return st_curl_edges_to_dual(&c->grid, c->dtype, in, out, dscale(c), as_stream(stream));
   set_error("curl: unsupported input kind %d", in_kind);
   return ILM_ERR_INVALID_ARG;
+}
+
+int ilm_convective_derivative(ilm_cache_t c, int field_kind, const void* v, const void* q, void* out,
+                              ilm_stream_t stream) {
+  CHECK_CACHE(c);
+  ILM_REQUIRE(v && q && out, "convective_derivative: null argument");
+  ILM_REQUIRE(field_kind == ILM_NODES_PRIMAL || field_kind == ILM_NODES_DUAL || field_kind == ILM_EDGES_PRIMAL,
+              "convective_derivative: unsupported field kind %d", field_kind);
+  ILM_REQUIRE(out != v && out != q, "convective_derivative: out must not alias an input");
+  return st_convective(&c->grid, c->dtype, field_kind, v, q, out, dscale(c), as_stream(stream));
+}
+
+int ilm_w_cross_v(ilm_cache_t c, const void* w, const void* v, void* out, ilm_stream_t stream) {
+  CHECK_CACHE(c);
+  ILM_REQUIRE(w && v && out, "w_cross_v: null argument");
+  ILM_REQUIRE(out != v, "w_cross_v: out must not alias v");
+  return st_w_cross_v(&c->grid, c->dtype, w, v, out, as_stream(stream));
+}
+
+int ilm_vecfield_helmholtz(ilm_cache_t c, const void* curlv, const void* divv, const void* dv, const void* vp,
+                           const double* uniform, void* v_out, ilm_stream_t stream) {
+  CHECK_CACHE(c);
+  ILM_REQUIRE(c->kind == ILM_CACHE_VECTOR, "vecfield_helmholtz needs a vector cache");
+  ILM_REQUIRE(curlv && divv && v_out, "vecfield_helmholtz: null argument");
+  ILM_REQUIRE(c->npts == 0 || dv, "vecfield_helmholtz: null surface jump");
+  cudaStream_t st = as_stream(stream);
+  const int dt = c->dtype;
+  const size_t nd = c->grid.shape(PC_D).numel(), np = c->grid.shape(PC_P).numel();
+  const size_t ne = gridkind_numel(&c->grid, ILM_EDGES_PRIMAL), neu = c->grid.shape(PC_U).numel();
+  void *bd, *bp, *ge;
+  ILM_TRY(gscr(c, 2, &bd));
+  ILM_TRY(gscr(c, 5, &bp));
+  ILM_TRY(gscr(c, 0, &ge));
+  void* psi = ptr_off(bd, nd, dt);
+  void* phi = ptr_off(bp, np, dt);
+  // L psi' = curlv + R_n n x [v];  psi = -psi'  (src/helmholtz.jl:85-100,117-120)
+  if (c->npts > 0) {
+    ILM_TRY(ilm_regularize_normal_cross(c, ILM_NODES_DUAL, dv, bd, stream));
+    ILM_TRY(st_axpby(nd, dt, 1.0, curlv, 1.0, bd, bd, st));
+  } else {
+    ILM_CHECK_CUDA(cudaMemcpyAsync(bd, curlv, nd * esize(dt), cudaMemcpyDeviceToDevice, st));
+  }
+  ILM_TRY(inverse_laplacian_kind(c, ILM_NODES_DUAL, bd, psi, st));
+  // L phi = divv + R_c n . [v]  (:196-207,227-231)
+  if (c->npts > 0) {
+    ILM_TRY(ilm_regularize_normal_dot(c, ILM_NODES_PRIMAL, dv, bp, stream));
+    ILM_TRY(st_axpby(np, dt, 1.0, divv, 1.0, bp, bp, st));
+  } else {
+    ILM_CHECK_CUDA(cudaMemcpyAsync(bp, divv, np * esize(dt), cudaMemcpyDeviceToDevice, st));
+  }
+  ILM_TRY(inverse_laplacian_kind(c, ILM_NODES_PRIMAL, bp, phi, st));
+  // v = curl psi + grad phi + v_p  (:327-344)
+  ILM_TRY(st_curl_dual_to_edges(&c->grid, dt, psi, v_out, dscale(c), st));
+  ILM_TRY(st_grad_nodes(&c->grid, dt, phi, ge, dscale(c), st));
+  ILM_TRY(st_axpby(ne, dt, -1.0, v_out, 1.0, ge, v_out, st));
+  if (vp) ILM_TRY(st_axpby(ne, dt, 1.0, vp, 1.0, v_out, v_out, st));
+  if (uniform) {
+    if (uniform[0] != 0.0) ILM_TRY(st_affine(neu, dt, 1.0, v_out, uniform[0], v_out, st));
+    if (uniform[1] != 0.0) ILM_TRY(st_affine(ne - neu, dt, 1.0, ptr_off(v_out, neu, dt), uniform[1],
+                                             ptr_off(v_out, neu, dt), st));
+  }
+  return ILM_OK;
 }
 
 int ilm_laplacian(ilm_cache_t c, int kind, const void* in, void* out, ilm_stream_t stream) {

@@ -601,6 +601,7 @@ int cache_rebin_points(ilm_cache_s* c, const double* x, const double* y, const d
   c->host_stale = true;
   c->S_dir_ready = false;
   c->S_neu_ready = false;
+  c->filt_ready = false;
   return ILM_OK;
 }
 

@@ -264,6 +264,9 @@ struct ilm_cache_s {
   // cached Schur complements for the problem solves (FP64 and FP32 copies)
   ilm::DevBuf S_dir64, S_dir32, S_neu64, S_neu32;
   bool S_dir_ready = false, S_neu_ready = false;
+  // surface filter: W = E R 1 (cache dtype) and a grid buffer of the cache's class
+  ilm::DevBuf filt_diag, filt_grid;
+  bool filt_ready = false;
   ilm::DevBuf red;                     // reduction scratch (double)
 
   template <typename T> ilm::PointWin<T> win() const {
@@ -317,6 +320,10 @@ int st_convert(size_t n, int dtype_in, const void* in, int dtype_out, void* out,
 int st_primal_to_dual(const ilm_grid_s* g, int dtype, const void* p, void* out, cudaStream_t st);
 int st_primal_to_edges(const ilm_grid_s* g, int dtype, const void* p, void* out, cudaStream_t st);
 int st_mul(size_t n, int dtype, const void* a, void* inout, cudaStream_t st);
+// convective derivatives and w x v (ilm_convective.cu); field_kind: the kind of q and out
+int st_convective(const ilm_grid_s* g, int dtype, int field_kind, const void* v, const void* q, void* out,
+                  double scale, cudaStream_t st);
+int st_w_cross_v(const ilm_grid_s* g, int dtype, const void* w, const void* v, void* out, cudaStream_t st);
 int st_weighted_dot(int n1, int n2, int dx, int dy, int dtype, const void* a, const void* b,
                     double* dres, cudaStream_t st);
 int st_point_dot(int n, int dtype, const void* a, const void* b, const double* w, double* dres,

@@ -42,12 +42,6 @@ __global__ void k_ndot(int n, const T* __restrict__ nx, const T* __restrict__ ny
   if (k < n) out[k] = nx[k] * v[k] + ny[k] * v[n + k];
 }
 
-template <typename T>
-__global__ void k_div_safe(int n, const T* __restrict__ d, T* __restrict__ x) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < n) x[k] = d[k] != (T)0 ? x[k] / d[k] : (T)0;
-}
-
 struct Work {
   DevBuf e1, e2, d1, d2, p1, v1, v2, v3, v4, v5, s1, s2, s3, s4, s5, diag;
 };
@@ -219,22 +213,7 @@ int ilm_solve_stokes(ilm_cache_t c, const void* vplus, const void* vminus, void*
   ILM_TRY(ilm_inverse_laplacian(c, ILM_NODES_DUAL, w.d1.p, w.d2.p, stream));
   ILM_TRY(st_axpby(nd, dt, 1.0, w.d2.p, 1.0, s_out, s_out, st));
   // sigma <- F^2 sigma,  F = W^-1 E R,  W = E R 1
-  ILM_TRY(st_fill(n2, dt, 1.0, w.v4.p, st));
-  ILM_TRY(ilm_regularize(c, ILM_EDGES_PRIMAL, w.v4.p, w.e1.p, stream));
-  ILM_TRY(ilm_interpolate(c, ILM_EDGES_PRIMAL, w.e1.p, w.diag.p, stream));
-  for (int pass = 0; pass < 2; ++pass) {
-    ILM_TRY(ilm_regularize(c, ILM_EDGES_PRIMAL, sigma_out, w.e1.p, stream));
-    ILM_TRY(ilm_interpolate(c, ILM_EDGES_PRIMAL, w.e1.p, sigma_out, stream));
-    if (N > 0) {
-      if (dt == ILM_F64)
-        k_div_safe<double><<<(int)((n2 + 255) / 256), 256, 0, st>>>((int)n2, w.diag.as<double>(),
-                                                                     static_cast<double*>(sigma_out));
-      else
-        k_div_safe<float><<<(int)((n2 + 255) / 256), 256, 0, st>>>((int)n2, w.diag.as<float>(),
-                                                                    static_cast<float*>(sigma_out));
-      ILM_CHECK_LAUNCH();
-    }
-  }
+  ILM_TRY(ilm_surface_filter(c, 2, sigma_out, sigma_out, stream));
   ILM_CHECK_CUDA(cudaStreamSynchronize(st));
   if (info) {
     info->iterations = it1 + it2;

@@ -11,7 +11,8 @@ from .bodies import (Body, BodyList, circle, ellipse, from_vertices, hexagon, po
 from .core import (Dual, EdgeGradient, EdgeGradientPrimal, Edges, EdgesDual, EdgesPrimal, GridData, GridScaling,
                    IndexScaling, Nodes, NodesDual, NodesPrimal, PhysicalGrid, PointData, Primal, ScalarData,
                    SurfaceScalarCache, SurfaceVectorCache, TensorData, VectorData, areas, complementary_mask,
-                   complementary_mask_, create_CLinvCT, create_GLinvD, create_nRTRn, create_RTLinvR, curl_,
+                   complementary_mask_, create_CLinvCT, create_GLinvD, create_nRTRn, create_RTLinvR, create_surface_filter,
+                   curl_, SurfaceFilter,
                    divergence_, dot, grad_, integrate, interpolate_, inverse_laplacian_, laplacian_, mask, mask_,
                    norm, normal_cross_interpolate_, normal_dot_interpolate_, normal_interpolate_,
                    normal_interpolate_symm_, normals, ones_grid, ones_surface, points, regularize_,

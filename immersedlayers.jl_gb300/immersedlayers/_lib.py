@@ -62,6 +62,7 @@ SIGNATURES = {
     "ilm_regularize_add": [_VP, _I, _VP, _VP, _VP],
     "ilm_grid_mul_add": [C.c_size_t, _I, _VP, _VP, _VP, _VP],
     "ilm_interpolate": [_VP, _I, _VP, _VP, _VP],
+    "ilm_surface_filter": [_VP, _I, _VP, _VP, _VP],
     "ilm_regularize_normal": [_VP, _VP, _VP, _VP],
     "ilm_regularize_normal_symm": [_VP, _VP, _VP, _VP],
     "ilm_regularize_normal_cross": [_VP, _I, _VP, _VP, _VP],
@@ -82,6 +83,9 @@ SIGNATURES = {
     "ilm_grad": [_VP, _I, _VP, _VP, _VP],
     "ilm_curl": [_VP, _I, _VP, _VP, _VP],
     "ilm_laplacian": [_VP, _I, _VP, _VP, _VP],
+    "ilm_convective_derivative": [_VP, _I, _VP, _VP, _VP, _VP],
+    "ilm_w_cross_v": [_VP, _VP, _VP, _VP, _VP],
+    "ilm_vecfield_helmholtz": [_VP, _VP, _VP, _VP, _VP, _DP, _VP, _VP],
     "ilm_inverse_laplacian": [_VP, _I, _VP, _VP, _VP],
     "ilm_mask": [_VP, _I, _I, _VP, _VP],
     "ilm_dot_grid": [_VP, _I, _VP, _VP, _DP, _VP],

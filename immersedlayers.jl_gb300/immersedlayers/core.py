@@ -627,3 +627,37 @@ def create_GLinvD(cache, scale=1.0):
 
 def create_nRTRn(cache, scale=1.0):
     return _schur(cache, "nRTRn", scale)
+
+
+class SurfaceFilter:
+    """The surface filter C = E~ R of create_surface_filter
+    (src/matrix_operators.jl:254-268) as an operator: ``C @ s`` filters the
+    surface data once, ``(C ** k) @ s`` k times (the C^6 s of
+    test/literate/problems.jl:107,297).  E~ = W^-1 E with W = diag(E R 1)
+    (the filtered interpolation of CartesianGrids' Regularize(filter=true));
+    no matrix is formed, each power is one regularize, one interpolation and
+    one row scaling on the device."""
+
+    def __init__(self, cache, power=1):
+        self.cache = cache
+        self.power = int(power)
+
+    def __pow__(self, k):
+        return SurfaceFilter(self.cache, self.power * int(k))
+
+    def apply_(self, out: PointData, s: PointData, stream=None):
+        c = self.cache
+        _check(c, out, s)
+        if not isinstance(s, c._surf_type()) or type(out) is not type(s):
+            raise TypeError(f"surface filter acts on {c._surf_type().__name__}")
+        L.call("ilm_surface_filter", c._h, self.power, _ptr(s.data), _ptr(out.data), _stream_ptr(stream))
+        return out
+
+    def __matmul__(self, s: PointData):
+        return self.apply_(s.similar(), s)
+
+    __mul__ = __matmul__
+
+
+def create_surface_filter(cache):
+    return SurfaceFilter(cache)

@@ -157,11 +157,17 @@ def solve_stokes(cache, vplus: PointData, vminus: PointData, tol=1e-8, maxiter=5
                              rel_residual=info.rel_residual)
 
 
-def solve(prob: ILMProblem, sys: ILMSystem, tol=1e-8, maxiter=5000):
-    """`solve(prob, sys)` for the built-in problems (bc from `prob.bc`)."""
+def solve(prob: ILMProblem, sys: ILMSystem, tol=1e-8, maxiter=5000, filter_power=0):
+    """`solve(prob, sys)` for the built-in problems (bc from `prob.bc`).
+    filter_power=k returns the Dirichlet surface data filtered k times,
+    C^k s with C = create_surface_filter(base_cache) (the literate
+    DirichletPoissonProblem returns C^6 s, test/literate/problems.jl:297)."""
     plus, minus = _sides(sys)
     if isinstance(prob, DirichletPoissonProblem):
         f, s, info = solve_dirichlet(sys.base_cache, plus, minus, tol, maxiter)
+        if filter_power:
+            from .core import SurfaceFilter
+            SurfaceFilter(sys.base_cache, filter_power).apply_(s, s)
     elif isinstance(prob, NeumannPoissonProblem):
         f, s, info = solve_neumann(sys.base_cache, plus, minus, tol, maxiter)
     elif isinstance(prob, StokesFlowProblem):

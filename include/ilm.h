@@ -139,6 +139,17 @@ ILM_API int ilm_regularize(ilm_cache_t c, int out_kind, const void* f, void* out
  * over n grid values (area forcing, dy .+= str .* mask).                   */
 ILM_API int ilm_regularize_add(ilm_cache_t c, int out_kind, const void* f, void* out, ilm_stream_t stream);
 ILM_API int ilm_grid_mul_add(size_t n, int dtype, const void* a, const void* b, void* out, ilm_stream_t stream);
+/* Surface filter C = E~ R (create_surface_filter, src/matrix_operators.jl:
+ * 254-268) applied `power` times: s_out = C^power s_in (the C^6 s of
+ * test/literate/problems.jl:107,297).  E~ is the filtered interpolation of
+ * CartesianGrids' Regularize(filter = true): E~ = W^-1 E, W = diag(E R 1),
+ * so constant surface data pass unchanged.  Scalar caches filter
+ * ScalarData through Nodes{Primal}, vector caches VectorData through
+ * Edges{Primal}.  W is formed on the first call and kept until the points
+ * move (ilm_cache_update_points).  s_in may equal s_out; power 0 copies.
+ * No N x N matrix is formed: each power is one regularize, one
+ * interpolation and one scaling.                                          */
+ILM_API int ilm_surface_filter(ilm_cache_t c, int power, const void* s_in, void* s_out, ilm_stream_t stream);
 /* interpolate!(f, s::Nodes{Primal|Dual}) (:56,:67), interpolate!(vb, v::Edges{Primal}) (:78) */
 ILM_API int ilm_interpolate(ilm_cache_t c, int in_kind, const void* grid_in, void* f_out, ilm_stream_t stream);
 
@@ -186,6 +197,29 @@ ILM_API int ilm_divergence(ilm_cache_t c, int in_kind, const void* in, void* out
 ILM_API int ilm_grad(ilm_cache_t c, int in_kind, const void* in, void* out, ilm_stream_t stream);
 /* curl!(v::Edges{Primal}, s::Nodes{Dual}) (:79-85), curl!(w::Nodes{Dual}, v::Edges{Primal}) (:97-103) */
 ILM_API int ilm_curl(ilm_cache_t c, int in_kind, const void* in, void* out, ilm_stream_t stream);
+/* convective_derivative!(out, v, q, base_cache, extra_cache)
+ * (src/grid_operators.jl:258-315, steps :318-371): v . grad q with v on
+ * Edges{Primal} and q of field_kind -- Nodes{Primal} (v . grad p),
+ * Nodes{Dual} (v . grad w) or Edges{Primal} (v . grad u; u . grad u is
+ * q = v) -- scaled by 1/h under GridScaling; out has field_kind and must
+ * not alias v or q.  One fused stencil pass; the reference's
+ * ConvectiveDerivativeCache temporaries are not needed.  (The reference's
+ * 5-argument Edges method v . grad u refers to an undefined variable at
+ * :368 and raises; here it computes v . grad u.)                           */
+ILM_API int ilm_convective_derivative(ilm_cache_t c, int field_kind, const void* v, const void* q, void* out,
+                                      ilm_stream_t stream);
+/* w_cross_v!(out::Edges{Primal}, w::Nodes{Dual}, v::Edges{Primal}) (:401-434):
+ * the rotational convective term w x v (no derivative scaling).           */
+ILM_API int ilm_w_cross_v(ilm_cache_t c, const void* w, const void* v, void* out, ilm_stream_t stream);
+/* vecfield_helmholtz!(v, curlv, divv, dv, vp, base_cache, veccache)
+ * (src/helmholtz.jl:327-347; vector caches): v = curl psi + grad phi + vp
+ * with L psi = -(curlv + R_n n x dv) and L phi = divv + R_c n . dv (:85-120,
+ * :196-231).  curlv: Nodes{Dual} masked curl; divv: Nodes{Primal} masked
+ * divergence; dv: VectorData surface jump (may be null without points);
+ * vp: Edges{Primal} or null; uniform: (Vx, Vy) added to every u / v value
+ * (the tuple method, :346-347) or null.                                    */
+ILM_API int ilm_vecfield_helmholtz(ilm_cache_t c, const void* curlv, const void* divv, const void* dv,
+                                   const void* vp, const double* uniform, void* v_out, ilm_stream_t stream);
 /* laplacian!(w, s) (:123-134): 5-point Laplacian, interior points, x 1/h^2 */
 ILM_API int ilm_laplacian(ilm_cache_t c, int kind, const void* in, void* out, ilm_stream_t stream);
 /* inverse_laplacian!(sol, rhs) (:153-179): unbounded-domain L^-1 via the

@@ -907,6 +907,29 @@ def create_CLinvCT_scalar_vector(c: SurfaceCache, scale=1.0):
     return A
 
 
+def _filter_rows(ER):
+    d = ER.sum(axis=1, keepdims=True)
+    return np.where(d != 0.0, ER / np.where(d != 0.0, d, 1.0), 0.0)
+
+
+def surface_filter_scalar(c: SurfaceCache):
+    """Surface filter C = E~ R on ScalarData through Nodes{Primal}
+    (create_surface_filter, src/matrix_operators.jl:254-268): the rows of
+    E R normalised to sum to one (E~ = W^-1 E, W = diag(E R 1), as in
+    surface_filter_vector).  Returns the N x N matrix."""
+    P = c.phi(NODES_PRIMAL)
+    return _filter_rows((P.T @ (P @ sp.diags(c._wscale()))).toarray())
+
+
+def surface_filter(c: SurfaceCache, s, power=1, vector=False):
+    """C^power s (test/literate/problems.jl:107,297 apply C^6)."""
+    F = surface_filter_vector(c) if vector else surface_filter_scalar(c)
+    out = np.asarray(s, dtype=np.float64)
+    for _ in range(power):
+        out = F @ out
+    return out
+
+
 def surface_filter_vector(c: SurfaceCache):
     """Surface filter E~ R on VectorData (src/matrix_operators.jl:247-262).
     The filtered interpolation E~ of CartesianGrids' Regularize(filter=true)
@@ -919,7 +942,7 @@ def surface_filter_vector(c: SurfaceCache):
     for k, cls_ in enumerate((EDGES_PRIMAL_U, EDGES_PRIMAL_V)):
         P = c.phi(cls_)
         ER = (P.T @ (P @ sp.diags(c._wscale()))).toarray()
-        F[k * n:(k + 1) * n, k * n:(k + 1) * n] = ER / ER.sum(axis=1, keepdims=True)
+        F[k * n:(k + 1) * n, k * n:(k + 1) * n] = _filter_rows(ER)
     return F
 
 
@@ -958,3 +981,133 @@ def solve_stokes(c: SurfaceCache, vplus, vminus, S=None, Ss=None, filt=None):
     s = s + c.inverse_laplacian(-surface_curl_cross_T(c, dsc))
     sigma = filt @ (filt @ sigma)
     return v, s, sigma
+
+
+# ---------------------------------------------------------------------------
+# Grid averaging, convective derivatives and w x v (src/grid_operators.jl:186-434)
+# ---------------------------------------------------------------------------
+# CartesianGrids' grid_interpolate! (un-vendored) restated as staggered-grid
+# averaging: along a direction where the target sits on the primal lattice
+# and the source on the dual one, every target value is the mean of its two
+# neighbours; from primal to dual, only the non-ghost dual positions
+# (1..n-2) have two neighbours and the two ghost layers stay zero (the same
+# boundary rule as grad! / curl! onto dual positions above).  Edges{Dual}.u
+# sits where Edges{Primal}.v sits and Edges{Dual}.v where Edges{Primal}.u
+# sits.  The results carry no known-answer test in the reference ("parity
+# unpinned"): the tests check them against this restatement and against
+# exact answers for linear fields.
+
+def _avg_d2p(a, axis):
+    """Dual -> primal along `axis`: (a[k] + a[k+1]) / 2 at every primal k."""
+    a = np.asarray(a)
+    if axis == 0:
+        return 0.5 * (a[:-1, :] + a[1:, :])
+    return 0.5 * (a[:, :-1] + a[:, 1:])
+
+
+def _avg_p2d(a, axis):
+    """Primal -> dual along `axis`: (a[k-1] + a[k]) / 2 at dual k = 1..n-2
+    (n = primal length + 1); the ghost ends are zero."""
+    a = np.asarray(a)
+    if axis == 0:
+        out = np.zeros((a.shape[0] + 1, a.shape[1]))
+        out[1:-1, :] = 0.5 * (a[:-1, :] + a[1:, :])
+    else:
+        out = np.zeros((a.shape[0], a.shape[1] + 1))
+        out[:, 1:-1] = 0.5 * (a[:, :-1] + a[:, 1:])
+    return out
+
+
+def grad_nodes_dual(w):
+    """grad!(Edges{Dual}, Nodes{Dual}): u = w[i+1]-w[i] (at Edges{Primal}.v
+    positions), v = w[j+1]-w[j] (at Edges{Primal}.u positions), every value."""
+    return (w[1:, :] - w[:-1, :], w[:, 1:] - w[:, :-1])
+
+
+def convective_derivative_nodes_primal(u, p, g: Grid, scale=1.0):
+    """u . grad p for p on Nodes{Primal}, u on Edges{Primal}
+    (_unscaled_convective_derivative!, src/grid_operators.jl:318-327):
+    grad p onto the edges, times u, averaged back onto the nodes (the two
+    components summed), times the derivative scale (:8-9)."""
+    gx, gy = grad_nodes(p, g)
+    return (_avg_d2p(u[0] * gx, 0) + _avg_d2p(u[1] * gy, 1)) * scale
+
+
+def convective_derivative_nodes_dual(u, w, g: Grid, scale=1.0):
+    """u . grad w for w on Nodes{Dual}, u on Edges{Primal} (:330-342): u is
+    averaged onto the Edges{Dual} positions (four-point means), times the
+    Edges{Dual} gradient of w, averaged onto the non-ghost dual nodes."""
+    gu, gv = grad_nodes_dual(w)
+    ud_u = _avg_p2d(_avg_d2p(u[0], 0), 1)      # Edges{Dual}.u (primal x, dual y)
+    ud_v = _avg_p2d(_avg_d2p(u[1], 1), 0)      # Edges{Dual}.v (dual x, primal y)
+    tu, tv = ud_u * gu, ud_v * gv
+    out = np.zeros(w.shape)
+    out[1:-1, 1:-1] = (0.5 * (tu[:-1, :] + tu[1:, :]))[:, 1:-1] + (0.5 * (tv[:, :-1] + tv[:, 1:]))[1:-1, :]
+    return out * scale
+
+
+def convective_derivative_edges(v, u, g: Grid, scale=1.0):
+    """v . grad u for Edges{Primal} v and u (:344-371; u . grad u with
+    v = u): v averaged onto the EdgeGradient positions (u-component onto
+    dudx/dudy, v-component onto dvdx/dvdy), transposed (dudy <-> dvdx),
+    times grad u, averaged back onto the edges."""
+    vu, vv = v
+    a_dudx = _avg_d2p(vu, 0)                   # Nodes{Primal}
+    a_dudy = _avg_p2d(vu, 1)                   # Nodes{Dual}
+    a_dvdx = _avg_p2d(vv, 0)                   # Nodes{Dual}
+    a_dvdy = _avg_d2p(vv, 1)                   # Nodes{Primal}
+    dudx, dudy, dvdx, dvdy = grad_edges(u, g)
+    t_dudx, t_dudy = a_dudx * dudx, a_dvdx * dudy     # transposed: dudy slot holds the dvdx average
+    t_dvdx, t_dvdy = a_dudy * dvdx, a_dvdy * dvdy
+    ou = _avg_p2d(t_dudx, 0) + _avg_d2p(t_dudy, 1)
+    ov = _avg_d2p(t_dvdx, 0) + _avg_p2d(t_dvdy, 1)
+    ou[0, :] = 0.0
+    ou[-1, :] = 0.0
+    ov[:, 0] = 0.0
+    ov[:, -1] = 0.0
+    return (ou * scale, ov * scale)
+
+
+def w_cross_v(w, u):
+    """w x v for vorticity w (Nodes{Dual}) and velocity u (Edges{Primal})
+    (_unscaled_w_cross_v!, src/grid_operators.jl:419-434):
+    (w x v).u = mean_y( -mean_x(v) w ),  (w x v).v = mean_x( mean_y(u) w )."""
+    vd = _avg_p2d(u[1], 0)                     # v onto dual nodes
+    ud = _avg_p2d(u[0], 1)                     # u onto dual nodes
+    return (_avg_d2p(-vd * w, 1), _avg_d2p(ud * w, 0))
+
+
+# ---------------------------------------------------------------------------
+# Helmholtz decomposition (src/helmholtz.jl)
+# ---------------------------------------------------------------------------
+
+def regularize_normal_cross_vector(c: SurfaceCache, vs):
+    """regularize_normal_cross!(w::Nodes{Dual}, vs::VectorData)
+    (src/surface_operators.jl:167-178): R_n (n x v) = R_n (n_x v_y - n_y v_x)."""
+    return c.reg_cls(c.nx * vs[c.N:] - c.ny * vs[:c.N], NODES_DUAL)
+
+
+def vectorpotential_from_masked_curlv(c: SurfaceCache, curlv, dv):
+    """L psi = -(curlv + R_n n x [v]) (src/helmholtz.jl:85-100,117-120)."""
+    rhs = curlv + (regularize_normal_cross_vector(c, dv) if c.N else 0.0)
+    return -c.inverse_laplacian(rhs)
+
+
+def scalarpotential_from_masked_divv(c: SurfaceCache, divv, dv):
+    """L phi = divv + R_c n . [v] (src/helmholtz.jl:196-207,227-231)."""
+    rhs = divv + (regularize_normal_dot(c, dv) if c.N else 0.0)
+    return c.inverse_laplacian(rhs)
+
+
+def vecfield_helmholtz(c: SurfaceCache, curlv, divv, dv, vp=None):
+    """v = curl psi + grad phi + v_p (src/helmholtz.jl:327-344); curl and
+    grad carry the derivative scale of the cache; vp: Edges tuple, a
+    uniform (Vx, Vy) pair, or None."""
+    psi = vectorpotential_from_masked_curlv(c, curlv, dv)
+    phi = scalarpotential_from_masked_divv(c, divv, dv)
+    vpsi = tuple(a * c.dscale() for a in curl_nodes_dual(psi, c.g))
+    vphi = tuple(a * c.dscale() for a in grad_nodes(phi, c.g))
+    v = (vpsi[0] + vphi[0], vpsi[1] + vphi[1])
+    if vp is not None:
+        v = (v[0] + vp[0], v[1] + vp[1])
+    return v

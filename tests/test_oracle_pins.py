@@ -165,3 +165,23 @@ def test_oracle_stokes_no_slip_and_symmetry():
     assert abs(sig[c.N:] @ c.ds) < 1e-10 * abs(sig[:c.N] @ c.ds)
     F = O.surface_filter_vector(c)
     assert np.allclose(F @ np.ones(2 * c.N), 1.0)
+
+
+def test_oracle_surface_filter_properties():
+    """The oracle's surface filter (create_surface_filter,
+    src/matrix_operators.jl:254-268): rows sum to one (constants pass), the
+    entries are those of E R up to the row scaling, and C^6 smooths."""
+    g, b = surface_ops_case()
+    c = O.SurfaceCache(b.x, b.y, b.nx, b.ny, b.ds, g)
+    F = O.surface_filter_scalar(c)
+    np.testing.assert_allclose(F.sum(axis=1), 1.0, rtol=0, atol=1e-13)
+    P = c.phi(O.NODES_PRIMAL)
+    ER = np.asarray((P.T @ P).toarray()) * c._wscale()[None, :]
+    np.testing.assert_allclose(F * ER.sum(axis=1, keepdims=True), ER, rtol=1e-12, atol=1e-15)
+    th = np.arctan2(b.y, b.x)
+    s = np.cos(th) + 0.3 * np.sin(40 * th)
+    s6 = O.surface_filter(c, s, power=6)
+    # the low mode survives, the high mode is damped
+    lo, hi = np.cos(th), np.sin(40 * th)
+    assert abs(np.dot(s6, lo) / np.dot(lo, lo) - 1.0) < 0.01
+    assert abs(np.dot(s6, hi) / np.dot(hi, hi)) < 0.3 * 0.05
