@@ -297,7 +297,9 @@ def _stencil_gbs(stream, flush, hbm):
     per cell FP32), the gradient (Nodes -> Edges, 12 B per cell) on 2048^2
     and 4096^2 grids, and of the DDF regularization of the 8192 points of the
     Stokes configuration onto Nodes{Primal} of its 2048^2 grid (every cell
-    written: 4 B per cell + 16 B per point)."""
+    written: 4 B per cell + 16 B per point); the fused convective derivatives
+    (v . grad p: Edges + 2 Nodes; u . grad u: 2 Edges) and w x v (2 Edges +
+    Nodes{Dual}) on 4096^2, FP32."""
     import torch
     import immersedlayers as il
     from immersedlayers import workloads as W
@@ -331,6 +333,26 @@ def _stencil_gbs(stream, flush, hbm):
             out[f"{name}_{n}"] = {"gbs": nbytes / t / 1e9, "frac": nbytes / t / 1e9 / hbm, "bytes": nbytes,
                                   "ms": 1000 * t}
         del c, q, w
+    # fused convective derivatives and w x v (inputs read once, output written once)
+    n = 4096
+    g = il.PhysicalGrid(h=4.0 / n, nx=n)
+    c = il.SurfaceVectorCache(None, g, dtype=torch.float32)
+    v = il.EdgesPrimal.zeros(g, torch.float32)
+    v.data.normal_()
+    p = il.NodesPrimal.zeros(g, torch.float32)
+    p.data.normal_()
+    w = il.NodesDual.zeros(g, torch.float32)
+    w.data.normal_()
+    o_p, o_e = p.similar(), v.similar()
+    for name, fn, nel in [
+            ("convective_nodes_primal", lambda: il.convective_derivative_(o_p, v, p, c, stream=stream),
+             v.data.numel() + 2 * p.data.numel()),
+            ("convective_edges", lambda: il.convective_derivative_(o_e, v, c, stream=stream), 2 * v.data.numel()),
+            ("w_cross_v", lambda: il.w_cross_v_(o_e, w, v, c, stream=stream), 2 * v.data.numel() + w.data.numel())]:
+        t = timed(fn)
+        out[f"{name}_{n}"] = {"gbs": nel * 4 / t / 1e9, "frac": nel * 4 / t / 1e9 / hbm, "bytes": nel * 4,
+                              "ms": 1000 * t}
+    del c, v, p, w, o_p, o_e
     d = W.stokes_scale(nrhs=1)
     g = il.PhysicalGrid(h=d["h"], nx=d["n"])
     c = il.SurfaceScalarCache(d["bodies"], g, dtype=torch.float32)

@@ -12,7 +12,9 @@ from .core import (Dual, EdgeGradient, EdgeGradientPrimal, Edges, EdgesDual, Edg
                    IndexScaling, Nodes, NodesDual, NodesPrimal, PhysicalGrid, PointData, Primal, ScalarData,
                    SurfaceScalarCache, SurfaceVectorCache, TensorData, VectorData, areas, complementary_mask,
                    complementary_mask_, create_CLinvCT, create_GLinvD, create_nRTRn, create_RTLinvR, create_surface_filter,
-                   curl_, SurfaceFilter,
+                   curl_, SurfaceFilter, ConvectiveDerivativeCache, RotConvectiveDerivativeCache,
+                   convective_derivative, convective_derivative_, w_cross_v, w_cross_v_, x_gridcurl,
+                   y_gridcurl, x_griddiv, y_griddiv,
                    divergence_, dot, grad_, integrate, interpolate_, inverse_laplacian_, laplacian_, mask, mask_,
                    norm, normal_cross_interpolate_, normal_dot_interpolate_, normal_interpolate_,
                    normal_interpolate_symm_, normals, ones_grid, ones_surface, points, regularize_,
@@ -23,6 +25,13 @@ from .core import (Dual, EdgeGradient, EdgeGradientPrimal, Edges, EdgesDual, Edg
 from .problems import (DirichletPoissonProblem, ILMProblem, ILMSystem, NeumannPoissonProblem, StokesFlowProblem,
                        construct_system, prescribed_surface_average_, prescribed_surface_jump_, solve,
                        solve_dirichlet, solve_neumann, solve_stokes, update_system_)
+from .helmholtz import (ScalarPotentialCache, VectorFieldCache, VectorPotentialCache, curlv_masked_from_masked_curlv_,
+                        divv_masked_from_masked_divv_, masked_curlv_from_curlv_masked_,
+                        masked_divv_from_divv_masked_, scalarpotential_from_divv_, scalarpotential_from_masked_divv_,
+                        scalarpotential_uniformvecfield_, vecfield_from_scalarpotential_,
+                        vecfield_from_vectorpotential_, vecfield_helmholtz_, vecfield_uniformvecfield_,
+                        vectorpotential_from_curlv_, vectorpotential_from_masked_curlv_,
+                        vectorpotential_uniformvecfield_)
 from .forcing import (AreaForcingModel, ForcingModelAndRegion, LineForcingModel, PointForcingModel, apply_forcing_,
                       forcing_regions)
 from .timemarching import (ConstrainedSolution, DirichletHeatConductionProblem, HeatIntegrator, constraint, init,

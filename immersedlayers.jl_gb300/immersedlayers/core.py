@@ -371,20 +371,38 @@ def zeros_surfacescalar(cache):
     return ScalarData.zeros(cache.N, cache.dtype)
 
 
-def x_grid(cache):
-    g = zeros_grid(cache)
+def _coords(cache, g, axis):
     for i, (dx, dy) in enumerate(_COMPONENTS[g.kind]):
         x, y = cache.g.coordinates(dx, dy)
-        g.component(i).copy_(torch.as_tensor(np.broadcast_to(x[None, :], (len(y), len(x)))))
+        c = x[None, :] if axis == 0 else y[:, None]
+        g.component(i).copy_(torch.as_tensor(np.ascontiguousarray(np.broadcast_to(c, (len(y), len(x))))))
     return g
+
+
+def x_grid(cache):
+    return _coords(cache, zeros_grid(cache), 0)
 
 
 def y_grid(cache):
-    g = zeros_grid(cache)
-    for i, (dx, dy) in enumerate(_COMPONENTS[g.kind]):
-        x, y = cache.g.coordinates(dx, dy)
-        g.component(i).copy_(torch.as_tensor(np.broadcast_to(y[:, None], (len(y), len(x)))))
-    return g
+    return _coords(cache, zeros_grid(cache), 1)
+
+
+def x_gridcurl(cache):
+    """x coordinates of the curl grid data (Nodes{Dual})."""
+    return _coords(cache, zeros_gridcurl(cache), 0)
+
+
+def y_gridcurl(cache):
+    return _coords(cache, zeros_gridcurl(cache), 1)
+
+
+def x_griddiv(cache):
+    """x coordinates of the divergence grid data (Nodes{Primal}, vector caches)."""
+    return _coords(cache, NodesPrimal.zeros(cache.g, cache.dtype), 0)
+
+
+def y_griddiv(cache):
+    return _coords(cache, NodesPrimal.zeros(cache.g, cache.dtype), 1)
 
 
 # ---------------------------------------------------------------------------
@@ -534,6 +552,61 @@ def curl_(out, inp, cache, stream=None):
     _check(cache, out, inp)
     L.call("ilm_curl", cache._h, inp.kind, _ptr(inp.data), _ptr(out.data), _stream_ptr(stream))
     return out
+
+
+class ConvectiveDerivativeCache:
+    """ConvectiveDerivativeCache (src/grid_operators.jl:193-208).  The device
+    forms the convective derivative in one fused stencil pass, so this extra
+    cache holds no temporaries; it keeps the reference's call signatures."""
+
+    def __init__(self, cache_or_data=None):
+        self.base = cache_or_data
+
+
+class RotConvectiveDerivativeCache(ConvectiveDerivativeCache):
+    """RotConvectiveDerivativeCache (src/grid_operators.jl:376-392), for w_cross_v_."""
+
+
+def convective_derivative_(out, v, *args, stream=None):
+    """convective_derivative!(out, v, q, base_cache[, extra_cache]) -- v . grad q
+    for q on Nodes{Primal}, Nodes{Dual} or Edges{Primal} -- and
+    convective_derivative!(out, u, base_cache[, extra_cache]) -- u . grad u
+    (src/grid_operators.jl:258-315); scaled by 1/h under GridScaling."""
+    if isinstance(args[0], BasicILMCache):
+        q, cache = v, args[0]
+    else:
+        q, cache = args[0], args[1]
+    _check(cache, out, v, q)
+    if not isinstance(v, EdgesPrimal):
+        raise TypeError("convective_derivative_: the velocity must be Edges{Primal}")
+    if type(out) is not type(q) or q.kind not in (L.NODES_PRIMAL, L.NODES_DUAL, L.EDGES_PRIMAL):
+        raise TypeError("convective_derivative_: out and q must be Nodes{Primal}, Nodes{Dual} or Edges{Primal} alike")
+    L.call("ilm_convective_derivative", cache._h, q.kind, _ptr(v.data), _ptr(q.data), _ptr(out.data),
+           _stream_ptr(stream))
+    return out
+
+
+def convective_derivative(v, q_or_cache, cache=None):
+    """convective_derivative(v, q, base_cache) / convective_derivative(u, base_cache)."""
+    if cache is None:
+        q, cache = v, q_or_cache
+    else:
+        q = q_or_cache
+    return convective_derivative_(q.similar(), v, q, cache)
+
+
+def w_cross_v_(out, w, v, base_cache, extra_cache=None, stream=None):
+    """w_cross_v!(out::Edges{Primal}, w::Nodes{Dual}, v::Edges{Primal})
+    (src/grid_operators.jl:401-434)."""
+    _check(base_cache, out, w, v)
+    if not (isinstance(out, EdgesPrimal) and isinstance(w, NodesDual) and isinstance(v, EdgesPrimal)):
+        raise TypeError("w_cross_v_: out and v Edges{Primal}, w Nodes{Dual}")
+    L.call("ilm_w_cross_v", base_cache._h, _ptr(w.data), _ptr(v.data), _ptr(out.data), _stream_ptr(stream))
+    return out
+
+
+def w_cross_v(w, v, base_cache):
+    return w_cross_v_(v.similar(), w, v, base_cache)
 
 
 def laplacian_(out, s, cache, stream=None):

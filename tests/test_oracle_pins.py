@@ -185,3 +185,35 @@ def test_oracle_surface_filter_properties():
     lo, hi = np.cos(th), np.sin(40 * th)
     assert abs(np.dot(s6, lo) / np.dot(lo, lo) - 1.0) < 0.01
     assert abs(np.dot(s6, hi) / np.dot(hi, hi)) < 0.3 * 0.05
+
+
+def test_oracle_convective_derivatives_exact_on_linear_fields():
+    """The oracle's convective derivatives (src/grid_operators.jl:318-371) and
+    w x v (:419-434) reproduce the exact answers of uniform and linear
+    fields away from the ghost layers."""
+    g, _ = surface_ops_case()
+    h = g.h
+    xu, yu = g.coords(O.EDGES_PRIMAL_U)
+    xv, yv = g.coords(O.EDGES_PRIMAL_V)
+    xp, yp = g.coords(O.NODES_PRIMAL)
+    xd, yd = g.coords(O.NODES_DUAL)
+    a, b, c, d = 0.7, -1.3, 2.0, 0.5
+    unif = (np.full(g.shape(O.EDGES_PRIMAL_U), a), np.full(g.shape(O.EDGES_PRIMAL_V), b))
+    p = c * xp[:, None] + d * yp[None, :]
+    r = O.convective_derivative_nodes_primal(unif, p, g, 1.0 / h)
+    np.testing.assert_allclose(r[2:-2, 2:-2], a * c + b * d, atol=1e-11)
+    w = c * xd[:, None] + d * yd[None, :]
+    r = O.convective_derivative_nodes_dual(unif, w, g, 1.0 / h)
+    np.testing.assert_allclose(r[2:-2, 2:-2], a * c + b * d, atol=1e-11)
+    assert np.all(r[0, :] == 0) and np.all(r[:, -1] == 0)
+    # u = (x, y): u . grad u = (x, y)
+    u = (np.broadcast_to(xu[:, None], g.shape(O.EDGES_PRIMAL_U)).copy(),
+         np.broadcast_to(yv[None, :], g.shape(O.EDGES_PRIMAL_V)).copy())
+    ru, rv = O.convective_derivative_edges(u, u, g, 1.0 / h)
+    np.testing.assert_allclose(ru[2:-2, 2:-2], np.broadcast_to(xu[:, None], ru.shape)[2:-2, 2:-2], atol=1e-11)
+    np.testing.assert_allclose(rv[2:-2, 2:-2], np.broadcast_to(yv[None, :], rv.shape)[2:-2, 2:-2], atol=1e-11)
+    # uniform w and v: w x v = (-w b, w a)
+    wu = np.full(g.shape(O.NODES_DUAL), 1.5)
+    ou, ov = O.w_cross_v(wu, unif)
+    np.testing.assert_allclose(ou[1:-1, :], -1.5 * b, atol=1e-13)
+    np.testing.assert_allclose(ov[:, 1:-1], 1.5 * a, atol=1e-13)
