@@ -260,7 +260,7 @@ struct ilm_batch_s {
   DevBuf jump, avg, g, s, rhs64, x64;
   DevBuf cgp, iters, relres, order, counter;
   int nclusters = 1;
-  int cg_variant = 0;  // Schur CG kernel (0 auto, 1 row-distributed, 2 replicated vectors)
+  int cg_variant = 0;  // Schur CG kernel (0 default, 1..ILM_CG_VARIANTS, launch_cg_cluster)
   // tasks
   DevBuf scatA, divA, gathA, scatB, divB, convA, convB, schurP;
   int n_scatA = 0, n_divA = 0, n_gathA = 0, n_scatB = 0, n_divB = 0;
@@ -1064,7 +1064,7 @@ int ilm_batch_set_profiling(ilm_batch_t b, int enable) {
 
 int ilm_batch_set_cg_variant(ilm_batch_t b, int variant) {
   ILM_REQUIRE(b, "null batch");
-  ILM_REQUIRE(variant >= 0 && variant <= 5, "batch: unknown CG variant %d", variant);
+  ILM_REQUIRE(variant >= 0 && variant <= ILM_CG_VARIANTS, "batch: unknown CG variant %d", variant);
   b->cg_variant = variant;
   b->nclusters = cg_cluster_count(b->nprob, b->maxN, variant);
   b->param_gen++;
@@ -1143,11 +1143,19 @@ int ilm_batch_autotune(ilm_batch_t b, const void* fplus, const void* fminus, voi
   int best = 0;
   float best_ms = 0.f;
   int rc = ILM_OK;
-  for (int v = 1; v <= 5 && rc == ILM_OK; ++v) {
+  for (int v = 1; v <= ILM_CG_VARIANTS && rc == ILM_OK; ++v) {
     if (ms_per_variant) ms_per_variant[v - 1] = -1.f;
     if (v == 2 && cg_rep_smem(b->maxN) > 200 * 1024) continue;
+    if (v != 2 && cg_variant_smem(b->maxN, v) > 200 * 1024) continue;
     if ((rc = ilm_batch_set_cg_variant(b, v)) != ILM_OK) break;
-    if ((rc = ilm_batch_solve(b, fplus, fminus, f_out, s_out, tol, maxiter, stream)) != ILM_OK) break;
+    if ((rc = ilm_batch_solve(b, fplus, fminus, f_out, s_out, tol, maxiter, stream)) != ILM_OK) {
+      // a variant the device refuses to launch (cluster size, shared memory)
+      // is skipped; the default variant must run
+      if (v == 1 || rc != ILM_ERR_CUDA || cudaStreamSynchronize(st) != cudaSuccess) break;
+      (void)cudaGetLastError();
+      rc = ILM_OK;
+      continue;
+    }
     if (cudaEventRecord(e0, st) != cudaSuccess) { rc = ILM_ERR_CUDA; break; }
     for (int k = 0; k < reps && rc == ILM_OK; ++k) rc = ilm_batch_solve(b, fplus, fminus, f_out, s_out, tol, maxiter, stream);
     if (rc != ILM_OK) break;

@@ -796,7 +796,7 @@ __device__ void apply_bjacobi_rows(const CGFFParams& pr, int r0, int r1, const f
 // doubles), `pub` 8 slots of 4 float-float values; the published slot
 // rotates over seven values so that a CTA never overwrites a slot another
 // CTA may still be reading.
-template <int K>
+template <int K, int CS = CG_CLUSTER>
 __device__ void csum_t0(cg::cluster_group& cl, double (&v)[K], int nact, double* red, double* pub, int& slot) {
   const int t = threadIdx.x, nt = blockDim.x;
   float* rf = reinterpret_cast<float*>(red);
@@ -833,14 +833,14 @@ __device__ void csum_t0(cg::cluster_group& cl, double (&v)[K], int nact, double*
     float rh[K], rl[K];
 #pragma unroll
     for (int k = 0; k < K; ++k) {
-      rh[k] = t < CG_CLUSTER ? cl.map_shared_rank(pf, t)[8 * slot + 2 * k] : 0.f;
-      rl[k] = t < CG_CLUSTER ? cl.map_shared_rank(pf, t)[8 * slot + 2 * k + 1] : 0.f;
+      rh[k] = t < CS ? cl.map_shared_rank(pf, t)[8 * slot + 2 * k] : 0.f;
+      rl[k] = t < CS ? cl.map_shared_rank(pf, t)[8 * slot + 2 * k + 1] : 0.f;
     }
 #pragma unroll
     for (int k = 0; k < K; ++k) {
       FF a{rh[k], rl[k]};
 #pragma unroll
-      for (int o = CG_CLUSTER / 2; o > 0; o >>= 1) {
+      for (int o = CS / 2; o > 0; o >>= 1) {
         FF b;
         b.hi = __shfl_down_sync(0xffffffffu, a.hi, o);
         b.lo = __shfl_down_sync(0xffffffffu, a.lo, o);
@@ -910,13 +910,13 @@ __device__ __forceinline__ FF ff_axpy(float bh, float bl, FF p, FF v) {
 // Sum_j w_j p_j (the deflation term of q = S' p) follows the same recurrence
 // as p from the reduced Sum w z (or Sum w r); it is recomputed from p at
 // every true-residual refresh.
-template <int NT, int MINB>
-__global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(NT, MINB)
+template <int NT, int MINB, int CS = CG_CLUSTER>
+__global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(NT, MINB)
     k_cg_cluster(const CGFFParams* __restrict__ P, const int* __restrict__ order, int nprob, int* counter,
                  int max_n) {
   cg::cluster_group cl = cg::this_cluster();
   const int rank = (int)cl.block_rank();
-  const int rmax = (max_n + CG_CLUSTER - 1) / CG_CLUSTER;
+  const int rmax = (max_n + CS - 1) / CS;
   const int ldm = schur_ld(max_n);
   extern __shared__ __align__(16) unsigned char smraw[];
   double* red = reinterpret_cast<double*>(smraw);  // 4 * threads (2 K floats per thread, K <= 4)
@@ -954,7 +954,7 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(NT, MINB)
       pr.tspan[2] = sm_id();
     }
     const int n = pr.n, ld = schur_ld(n);
-    const int rows = (n + CG_CLUSTER - 1) / CG_CLUSTER;
+    const int rows = (n + CS - 1) / CS;
     const int r0 = min(n, rank * rows), r1 = min(n, r0 + rows);
     const int nr = r1 - r0;
     const double gamma = pr.gamma;
@@ -972,7 +972,7 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(NT, MINB)
       double v[1] = {0.0};
       for (int i = threadIdx.x; i < nr; i += blockDim.x) v[0] += ws[i] * xs[i];
       publish_slice(xs, r0, nr, bh, bl);
-      csum_t0<1>(cl, v, nr, red, pub, slot);
+      csum_t0<1, CS>(cl, v, nr, red, pub, slot);
       if (threadIdx.x == 0) bc[0] = gamma * v[0];
       gather_parts(cl, bh, bl, n, rows, rank);
       matvec_rows_ff(pr, n, r0, r1, bh, bl, yh, yl);
@@ -994,7 +994,7 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(NT, MINB)
         v[2] += ws[i] * rs[i];
       }
       publish_slice(rs, r0, nr, ah, al);
-      csum_t0<3>(cl, v, nr, red, pub, slot);
+      csum_t0<3, CS>(cl, v, nr, red, pub, slot);
       if (threadIdx.x == 0) {
         bc[0] = sqrt(v[0]);
         bc[1] = v[1];
@@ -1017,7 +1017,7 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(NT, MINB)
       double v[1] = {0.0};
       for (int i = threadIdx.x; i < nr; i += blockDim.x) v[0] += ws[i] * zs[i];
       publish_slice(zs, r0, nr, bh, bl);
-      csum_t0<1>(cl, v, nr, red, pub, slot);
+      csum_t0<1, CS>(cl, v, nr, red, pub, slot);
       if (threadIdx.x == 0) bc[2] = v[0];
       gather_parts(cl, bh, bl, n, rows, rank);
       wp = bc[2];
@@ -1061,7 +1061,7 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(NT, MINB)
           v[0] += ws[i] * pi * qi;
           v[1] += ws[i] * pi * rs[i];
         }
-        csum_t0<2>(cl, v, nr, red, pub, slot);
+        csum_t0<2, CS>(cl, v, nr, red, pub, slot);
         if (threadIdx.x == 0) {
           bc[3] = v[0];
           bc[4] = v[0] != 0.0 ? fdiv(pre ? v[1] : rz, v[0]) : 0.0;
@@ -1083,7 +1083,7 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(NT, MINB)
           v[2] += ws[i] * ri;
         }
         publish_slice(rs, r0, nr, ah, al);
-        csum_t0<3>(cl, v, nr, red, pub, slot);
+        csum_t0<3, CS>(cl, v, nr, red, pub, slot);
         if (threadIdx.x == 0) {
           bc[5] = v[0];
           bc[6] = v[1];
@@ -1103,7 +1103,7 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(NT, MINB)
           double v[1] = {0.0};
           for (int i = threadIdx.x; i < nr; i += blockDim.x) v[0] += ws[i] * xs[i];
           publish_slice(xs, r0, nr, bh, bl);
-          csum_t0<1>(cl, v, nr, red, pub, slot);
+          csum_t0<1, CS>(cl, v, nr, red, pub, slot);
           if (threadIdx.x == 0) bc[8] = gamma * v[0];
           gather_parts(cl, bh, bl, n, rows, rank);
           matvec_rows_ff(pr, n, r0, r1, bh, bl, yh, yl);
@@ -1120,7 +1120,7 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(NT, MINB)
           v[3] += ws[i] * ps[i];
         }
         publish_slice(rs, r0, nr, ah, al);
-        csum_t0<4>(cl, v, nr, red, pub, slot);
+        csum_t0<4, CS>(cl, v, nr, red, pub, slot);
         if (threadIdx.x == 0) {
           bc[9] = v[0];
           bc[10] = v[1];
@@ -1176,7 +1176,7 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(NT, MINB)
           v[1] += ws[i] * zs[i];
         }
         publish_slice(zs, r0, nr, bh, bl);
-        csum_t0<2>(cl, v, nr, red, pub, slot);
+        csum_t0<2, CS>(cl, v, nr, red, pub, slot);
         if (threadIdx.x == 0) {
           bc[13] = fdiv(-v[0], pq);
           bc[14] = v[1];
@@ -1204,7 +1204,7 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(NT, MINB)
       // Sherman-Morrison back to S: x = y + gamma t z, t = 1^T W y / (1 - gamma 1^T W z)
       double v[1] = {0.0};
       for (int i = threadIdx.x; i < nr; i += blockDim.x) v[0] += ws[i] * xs[i];
-      csum_t0<1>(cl, v, nr, red, pub, slot);
+      csum_t0<1, CS>(cl, v, nr, red, pub, slot);
       if (threadIdx.x == 0) bc[15] = gamma * (v[0] / (1.0 - gamma * pr.uz));
       __syncthreads();
       const double gt = bc[15];
@@ -1213,7 +1213,7 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(NT, MINB)
       // reported residual: the true one of S x = b (x through buffer B)
       double u[1] = {0.0};
       publish_slice(xs, r0, nr, bh, bl);
-      csum_t0<1>(cl, u, nr, red, pub, slot);  // barrier that publishes x
+      csum_t0<1, CS>(cl, u, nr, red, pub, slot);  // barrier that publishes x
       gather_parts(cl, bh, bl, n, rows, rank);
       matvec_rows_ff(pr, n, r0, r1, bh, bl, yh, yl);
       __syncthreads();
@@ -1222,7 +1222,7 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(NT, MINB)
         const double d = bs[i] - ((double)yh[i] + (double)yl[i]);
         t[0] += d * d;
       }
-      csum_t0<1>(cl, t, nr, red, pub, slot);
+      csum_t0<1, CS>(cl, t, nr, red, pub, slot);
       if (threadIdx.x == 0) bc[0] = t[0];
       __syncthreads();
       relres = bnorm > 0 ? sqrt(bc[0]) / bnorm : 0.0;
@@ -1237,8 +1237,8 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(NT, MINB)
   cl.sync();  // keep shared memory alive until every CTA is done reading it
 }
 
-size_t cg_cluster_smem(int max_n, int nt) {
-  const size_t rmax = (size_t)(max_n + CG_CLUSTER - 1) / CG_CLUSTER;
+size_t cg_cluster_smem(int max_n, int nt, int cs) {
+  const size_t rmax = (size_t)(max_n + cs - 1) / cs;
   const size_t ldm = (size_t)schur_ld(max_n);
   return (4 * (size_t)nt + 16 + 32 + 4 + 7 * rmax + 1) * sizeof(double) +
          (8 * ldm + 2 * rmax) * sizeof(float) + 64;
@@ -1251,27 +1251,40 @@ size_t cg_rep_smem(int max_n) {
 
 
 // Kernel variants (the batch autotuner picks among them): 0 (default) and 1 =
-// row-distributed, 256 threads per CTA, up to 3 CTAs per SM; 3 = 128
-// threads, up to 6 CTAs per SM (more problems in flight); 4 = 256 threads,
-// at most 2 CTAs per SM (more registers, less sharing of an SM between
-// clusters); 5 = 512 threads, one CTA per SM (each cluster alone on its
-// SMs); 2 = replicated vectors, when they fit in shared memory.
+// row-distributed over 8-CTA clusters, 256 threads per CTA, up to 3 CTAs per
+// SM; 3 = 128 threads, up to 6 CTAs per SM (more problems in flight); 4 =
+// 256 threads, at most 2 CTAs per SM (more registers, less sharing of an SM
+// between clusters); 5 = 512 threads, one CTA per SM (each cluster alone on
+// its SMs); 2 = replicated vectors, when they fit in shared memory.  The
+// cluster size stays 8: clusters of 1, 2, 4 and 16 CTAs (the template's CS)
+// were measured 2.7x, 2.0x, 1.2x and 1.5x slower on the batched
+// configuration with the learned preconditioner (fewer CTAs cannot keep
+// enough of a large problem's matrix rows in flight; 16 pays 16-way
+// barriers).
 static bool use_rep(int variant, int max_n) { return variant == 2 && cg_rep_smem(max_n) <= 200 * 1024; }
 static int dist_threads(int variant) { return variant == 3 ? 128 : variant == 5 ? 512 : 256; }
+static int dist_cluster(int) { return CG_CLUSTER; }
 
-template <int NT, int MINB>
+size_t cg_variant_smem(int max_n, int variant) {
+  return use_rep(variant, max_n) ? cg_rep_smem(max_n)
+                                 : cg_cluster_smem(max_n, dist_threads(variant), dist_cluster(variant));
+}
+
+template <int NT, int MINB, int CS>
 static int launch_dist(const CGFFParams* prm, const int* order, int nprob, int* counter, int max_n, int nclusters,
                        size_t smem, cudaStream_t st) {
-  ILM_CHECK_CUDA(cudaFuncSetAttribute(k_cg_cluster<NT, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_cg_cluster<NT, MINB><<<nclusters * CG_CLUSTER, NT, smem, st>>>(prm, order, nprob, counter, max_n);
+  ILM_CHECK_CUDA(
+      cudaFuncSetAttribute(k_cg_cluster<NT, MINB, CS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_cg_cluster<NT, MINB, CS><<<nclusters * CS, NT, smem, st>>>(prm, order, nprob, counter, max_n);
   ILM_CHECK_LAUNCH();
   return ILM_OK;
 }
 
-template <int NT, int MINB>
+template <int NT, int MINB, int CS>
 static cudaError_t clusters_dist(int* nc, cudaLaunchConfig_t* cfg, size_t smem) {
-  cudaError_t e = cudaFuncSetAttribute(k_cg_cluster<NT, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e == cudaSuccess) e = cudaOccupancyMaxActiveClusters(nc, k_cg_cluster<NT, MINB>, cfg);
+  cudaError_t e =
+      cudaFuncSetAttribute(k_cg_cluster<NT, MINB, CS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveClusters(nc, k_cg_cluster<NT, MINB, CS>, cfg);
   return e;
 }
 
@@ -1286,17 +1299,16 @@ int launch_cg_cluster(const void* params_dev, const int* order, int nprob, int* 
     ILM_CHECK_LAUNCH();
     return ILM_OK;
   }
-  const int nt = dist_threads(variant);
-  const size_t smem = cg_cluster_smem(max_n, nt);
+  const size_t smem = cg_variant_smem(max_n, variant);
   if (smem > 200 * 1024) {
-    set_error("cluster CG: %d unknowns exceed the shared-memory layout", max_n);
+    set_error("cluster CG: %d unknowns exceed the shared-memory layout of CG variant %d", max_n, variant);
     return ILM_ERR_SIZE_LIMIT;
   }
   switch (variant) {
-    case 3: return launch_dist<128, 6>(prm, order, nprob, counter, max_n, nclusters, smem, st);
-    case 4: return launch_dist<256, 2>(prm, order, nprob, counter, max_n, nclusters, smem, st);
-    case 5: return launch_dist<512, 1>(prm, order, nprob, counter, max_n, nclusters, smem, st);
-    default: return launch_dist<256, 3>(prm, order, nprob, counter, max_n, nclusters, smem, st);
+    case 3: return launch_dist<128, 6, CG_CLUSTER>(prm, order, nprob, counter, max_n, nclusters, smem, st);
+    case 4: return launch_dist<256, 2, CG_CLUSTER>(prm, order, nprob, counter, max_n, nclusters, smem, st);
+    case 5: return launch_dist<512, 1, CG_CLUSTER>(prm, order, nprob, counter, max_n, nclusters, smem, st);
+    default: return launch_dist<256, 3, CG_CLUSTER>(prm, order, nprob, counter, max_n, nclusters, smem, st);
   }
 }
 
@@ -1308,29 +1320,31 @@ int cg_cluster_count(int nprob, int max_n, int variant) {
   // persistent clusters beyond that would only find the queue empty)
   const bool rep = use_rep(variant, max_n);
   const int nt = rep ? CGR_THREADS : dist_threads(variant);
-  const size_t smem = rep ? cg_rep_smem(max_n) : cg_cluster_smem(max_n, nt);
+  const int cs = rep ? CG_CLUSTER : dist_cluster(variant);
+  const size_t smem = cg_variant_smem(max_n, variant);
   int nc = 0;
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(CG_CLUSTER * nsm);
+  cfg.gridDim = dim3(cs * nsm);
   cfg.blockDim = dim3(nt);
   cfg.dynamicSmemBytes = smem;
   cudaError_t e;
   if (rep) {
     e = cudaFuncSetAttribute(k_cg_rep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveClusters(&nc, k_cg_rep, &cfg);
-  } else if (variant == 3) {
-    e = clusters_dist<128, 6>(&nc, &cfg, smem);
-  } else if (variant == 4) {
-    e = clusters_dist<256, 2>(&nc, &cfg, smem);
-  } else if (variant == 5) {
-    e = clusters_dist<512, 1>(&nc, &cfg, smem);
+  } else if (smem > 200 * 1024) {
+    e = cudaErrorInvalidValue;  // the launch refuses this variant; any count will do
   } else {
-    e = clusters_dist<256, 3>(&nc, &cfg, smem);
+    switch (variant) {
+      case 3: e = clusters_dist<128, 6, CG_CLUSTER>(&nc, &cfg, smem); break;
+      case 4: e = clusters_dist<256, 2, CG_CLUSTER>(&nc, &cfg, smem); break;
+      case 5: e = clusters_dist<512, 1, CG_CLUSTER>(&nc, &cfg, smem); break;
+      default: e = clusters_dist<256, 3, CG_CLUSTER>(&nc, &cfg, smem); break;
+    }
   }
   if (e != cudaSuccess || nc <= 0) {
     (void)cudaGetLastError();
     const int per_sm = variant == 3 ? 6 : variant == 4 ? 2 : variant == 5 ? 1 : 3;
-    nc = std::max(1, per_sm * nsm / CG_CLUSTER);
+    nc = std::max(1, per_sm * nsm / cs);
   }
   return std::min(nc, nprob);
 }

@@ -85,8 +85,9 @@ __global__ void __launch_bounds__(BX* BY) k_vdw_nd(int NX, int NY, const T* __re
 }
 
 // v . grad u for Edges{Primal} v and u (:344-371; u . grad u with v = u).
-// blockIdx.z = 0: the u component (NX x NY-1), 1: the v component
-// (NX-1 x NY).  The EdgeGradient slots after transpose!:
+// Thread (i, j) writes out.u(i, j) (j <= NY-2) and out.v(i, j) (i <= NX-2):
+// both components in one CTA, so the inputs a CTA needs come from DRAM once.
+// The EdgeGradient slots after transpose!:
 //   dudx (primal x, primal y): mean_x(v.u) * (u.u[k+1]-u.u[k])
 //   dudy (dual, dual):         mean_x(v.v) * (u.u[l]-u.u[l-1])   (non-ghost only)
 //   dvdx (dual, dual):         mean_y(v.u) * (u.v[k]-u.v[k-1])   (non-ghost only)
@@ -99,81 +100,81 @@ __global__ void __launch_bounds__(BX* BY) k_vdu_edges(int NX, int NY, const T* _
                                                       T* __restrict__ ov, T sc) {
   const int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
   const int m = NX - 1;
-  if (blockIdx.z == 0) {
-    if (i >= NX || j >= NY - 1) return;
+  if (i >= NX || j >= NY) return;
+  if (j <= NY - 2) {
     const size_t c = (size_t)j * NX + i;
-    if (i < 1 || i > NX - 2) {
-      ou[c] = (T)0;
-      return;
+    T r = (T)0;
+    if (i >= 1 && i <= NX - 2) {
+      // x part: dudx slots at primal x i-1, i (row j)
+      const T u0 = ld(uu, c - 1), u1 = ld(uu, c), u2 = ld(uu, c + 1);
+      const T v0 = ld(vu, c - 1), v1 = ld(vu, c), v2 = ld(vu, c + 1);
+      const T tx = (T)0.5 * (v0 + v1) * (u1 - u0) + (T)0.5 * (v1 + v2) * (u2 - u1);
+      // y part: dudy slots at dual (i, l), l = j, j+1, nonzero for 1 <= l <= NY-2
+      T ty = (T)0;
+      if (j >= 1) {
+        const T a = (T)0.5 * (ld(vv, (size_t)j * m + i - 1) + ld(vv, (size_t)j * m + i));
+        ty += a * (u1 - ld(uu, c - NX));
+      }
+      if (j + 1 <= NY - 2) {
+        const T a = (T)0.5 * (ld(vv, (size_t)(j + 1) * m + i - 1) + ld(vv, (size_t)(j + 1) * m + i));
+        ty += a * (ld(uu, c + NX) - u1);
+      }
+      r = (T)0.5 * (tx + ty) * sc;
     }
-    // x part: dudx slots at primal x i-1, i (row j)
-    const T u0 = ld(uu, c - 1), u1 = ld(uu, c), u2 = ld(uu, c + 1);
-    const T v0 = ld(vu, c - 1), v1 = ld(vu, c), v2 = ld(vu, c + 1);
-    const T tx = (T)0.5 * (v0 + v1) * (u1 - u0) + (T)0.5 * (v1 + v2) * (u2 - u1);
-    // y part: dudy slots at dual (i, l), l = j, j+1, nonzero for 1 <= l <= NY-2
-    T ty = (T)0;
-    if (j >= 1) {
-      const T a = (T)0.5 * (ld(vv, (size_t)j * m + i - 1) + ld(vv, (size_t)j * m + i));
-      ty += a * (u1 - ld(uu, c - NX));
-    }
-    if (j + 1 <= NY - 2) {
-      const T a = (T)0.5 * (ld(vv, (size_t)(j + 1) * m + i - 1) + ld(vv, (size_t)(j + 1) * m + i));
-      ty += a * (ld(uu, c + NX) - u1);
-    }
-    ou[c] = (T)0.5 * (tx + ty) * sc;
-  } else {
-    if (i >= m || j >= NY) return;
+    ou[c] = r;
+  }
+  if (i <= NX - 2) {
     const size_t c = (size_t)j * m + i;
-    if (j < 1 || j > NY - 2) {
-      ov[c] = (T)0;
-      return;
+    T r = (T)0;
+    if (j >= 1 && j <= NY - 2) {
+      // y part: dvdy slots at primal y j-1, j (column i)
+      const T u0 = ld(uv, c - m), u1 = ld(uv, c), u2 = ld(uv, c + m);
+      const T v0 = ld(vv, c - m), v1 = ld(vv, c), v2 = ld(vv, c + m);
+      const T ty = (T)0.5 * (v0 + v1) * (u1 - u0) + (T)0.5 * (v1 + v2) * (u2 - u1);
+      // x part: dvdx slots at dual (k, j), k = i, i+1, nonzero for 1 <= k <= NX-2
+      T tx = (T)0;
+      if (i >= 1) {
+        const T a = (T)0.5 * (ld(vu, (size_t)(j - 1) * NX + i) + ld(vu, (size_t)j * NX + i));
+        tx += a * (u1 - ld(uv, c - 1));
+      }
+      if (i + 1 <= NX - 2) {
+        const T a = (T)0.5 * (ld(vu, (size_t)(j - 1) * NX + i + 1) + ld(vu, (size_t)j * NX + i + 1));
+        tx += a * (ld(uv, c + 1) - u1);
+      }
+      r = (T)0.5 * (tx + ty) * sc;
     }
-    // y part: dvdy slots at primal y j-1, j (column i)
-    const T u0 = ld(uv, c - m), u1 = ld(uv, c), u2 = ld(uv, c + m);
-    const T v0 = ld(vv, c - m), v1 = ld(vv, c), v2 = ld(vv, c + m);
-    const T ty = (T)0.5 * (v0 + v1) * (u1 - u0) + (T)0.5 * (v1 + v2) * (u2 - u1);
-    // x part: dvdx slots at dual (k, j), k = i, i+1, nonzero for 1 <= k <= NX-2
-    T tx = (T)0;
-    if (i >= 1) {
-      const T a = (T)0.5 * (ld(vu, (size_t)(j - 1) * NX + i) + ld(vu, (size_t)j * NX + i));
-      tx += a * (u1 - ld(uv, c - 1));
-    }
-    if (i + 1 <= NX - 2) {
-      const T a = (T)0.5 * (ld(vu, (size_t)(j - 1) * NX + i + 1) + ld(vu, (size_t)j * NX + i + 1));
-      tx += a * (ld(uv, c + 1) - u1);
-    }
-    ov[c] = (T)0.5 * (tx + ty) * sc;
+    ov[c] = r;
   }
 }
 
 // w x v (:419-434): out.u = mean_y(-mean_x(v.v) w), out.v = mean_x(mean_y(v.u) w),
-// the inner means onto the non-ghost dual nodes only.
+// the inner means onto the non-ghost dual nodes only.  Thread (i, j) writes
+// out.u(i, j) (j <= NY-2) and out.v(i, j) (i <= NX-2).
 template <typename T>
 __global__ void __launch_bounds__(BX* BY) k_w_cross_v(int NX, int NY, const T* __restrict__ w,
                                                       const T* __restrict__ vu, const T* __restrict__ vv,
                                                       T* __restrict__ ou, T* __restrict__ ov) {
   const int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
   const int m = NX - 1;
-  if (blockIdx.z == 0) {
-    if (i >= NX || j >= NY - 1) return;
-    const size_t c = (size_t)j * NX + i;
+  if (i >= NX || j >= NY) return;
+  const T w0 = ld(w, (size_t)j * NX + i);
+  if (j <= NY - 2) {
     T r = (T)0;
     if (i >= 1 && i <= NX - 2) {
       const T vd0 = (T)0.5 * (ld(vv, (size_t)j * m + i - 1) + ld(vv, (size_t)j * m + i));
       const T vd1 = (T)0.5 * (ld(vv, (size_t)(j + 1) * m + i - 1) + ld(vv, (size_t)(j + 1) * m + i));
-      r = (T)-0.5 * (vd0 * ld(w, (size_t)j * NX + i) + vd1 * ld(w, (size_t)(j + 1) * NX + i));
+      r = (T)-0.5 * (vd0 * w0 + vd1 * ld(w, (size_t)(j + 1) * NX + i));
     }
-    ou[c] = r;
-  } else {
-    if (i >= m || j >= NY) return;
-    const size_t c = (size_t)j * m + i;
+    ou[(size_t)j * NX + i] = r;
+  }
+  if (i <= NX - 2) {
     T r = (T)0;
     if (j >= 1 && j <= NY - 2) {
       const T ud0 = (T)0.5 * (ld(vu, (size_t)(j - 1) * NX + i) + ld(vu, (size_t)j * NX + i));
       const T ud1 = (T)0.5 * (ld(vu, (size_t)(j - 1) * NX + i + 1) + ld(vu, (size_t)j * NX + i + 1));
-      r = (T)0.5 * (ud0 * ld(w, (size_t)j * NX + i) + ud1 * ld(w, (size_t)j * NX + i + 1));
+      r = (T)0.5 * (ud0 * w0 + ud1 * ld(w, (size_t)j * NX + i + 1));
     }
-    ov[c] = r;
+    ov[(size_t)j * m + i] = r;
   }
 }
 
@@ -209,7 +210,7 @@ int st_convective(const ilm_grid_s* g, int dtype, int field_kind, const void* v,
       case ILM_EDGES_PRIMAL: {
         const T* uu = static_cast<const T*>(q);
         T* ou = static_cast<T*>(out);
-        k_vdu_edges<T><<<grid2(NX, NY, 2), dim3(BX, BY), 0, st>>>(NX, NY, vu, vv, uu, uu + ne_u, ou, ou + ne_u,
+        k_vdu_edges<T><<<grid2(NX, NY), dim3(BX, BY), 0, st>>>(NX, NY, vu, vv, uu, uu + ne_u, ou, ou + ne_u,
                                                                    (T)scale);
         break;
       }
@@ -228,7 +229,7 @@ int st_w_cross_v(const ilm_grid_s* g, int dtype, const void* w, const void* v, v
   CV_DISPATCH(dtype, {
     const T* vu = static_cast<const T*>(v);
     T* ou = static_cast<T*>(out);
-    k_w_cross_v<T><<<grid2(NX, NY, 2), dim3(BX, BY), 0, st>>>(NX, NY, static_cast<const T*>(w), vu, vu + ne_u, ou,
+    k_w_cross_v<T><<<grid2(NX, NY), dim3(BX, BY), 0, st>>>(NX, NY, static_cast<const T*>(w), vu, vu + ne_u, ou,
                                                                ou + ne_u);
   });
   ILM_CHECK_LAUNCH();

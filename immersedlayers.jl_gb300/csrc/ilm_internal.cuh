@@ -402,6 +402,7 @@ int launch_block_inverse(const BJBlockTask* tasks_dev, int ntasks, int max_sz, c
 int launch_cg_cluster(const void* params_dev, const int* order, int nprob, int* counter, int max_n, int nclusters,
                       cudaStream_t st, int variant = 0);
 int cg_cluster_count(int nprob, int max_n, int variant = 0);
+size_t cg_variant_smem(int max_n, int variant);  // dynamic shared memory of a CG variant
 size_t cg_rep_smem(int max_n);  // shared memory of the replicated-vector CG per CTA
 
 }  // namespace ilm

@@ -127,6 +127,9 @@ def _cg_times(self):
     return np.array(a[:]), np.array(b[:]), np.array(sm[:])
 
 
+CG_VARIANTS = 5  # ILM_CG_VARIANTS of include/ilm.h
+
+
 def _set_cg_variant(self, variant):
     """Schur CG kernel: 0 default (= 1), 1 row-distributed vectors (256
     threads per CTA, up to 3 per SM), 2 replicated vectors (one cluster
@@ -149,10 +152,10 @@ def _autotune(self, fplus, fminus, f_out=None, s_out=None, tol=1e-8, maxiter=500
     if s_out is None:
         s_out = torch.empty(self.total_points, dtype=self.dtype, device="cuda")
     ch = C.c_int()
-    ms = (C.c_float * 5)()
+    ms = (C.c_float * CG_VARIANTS)()
     L.call("ilm_batch_autotune", self._h, _ptr(fplus), _ptr(fminus), _ptr(f_out), _ptr(s_out), float(tol),
            int(maxiter), int(reps), _stream_ptr(stream), C.byref(ch), ms)
-    return ch.value, {v + 1: float(ms[v]) for v in range(5) if ms[v] >= 0}
+    return ch.value, {v + 1: float(ms[v]) for v in range(CG_VARIANTS) if ms[v] >= 0}
 
 
 def _stats(self):

@@ -340,17 +340,20 @@ ILM_API int ilm_batch_stats(ilm_batch_t b, double* stats);
  * with no counterpart in the reference.                                     */
 ILM_API int ilm_batch_cg_times(ilm_batch_t b, double* start_us, double* end_us, int* sm);
 /* Schur CG kernel of the batch: 0 default (= 1), 1 row-distributed
- * vectors with 256-thread CTAs (three or four cluster barriers per
- * iteration, FP64 work on the owned rows only), 2 replicated vectors (one
- * cluster barrier per iteration, every vector operation in every CTA), 3
- * row-distributed with 128-thread CTAs (twice the resident clusters), 4
- * 256-thread CTAs at most two per SM, 5 512-thread CTAs one per SM.
- * ilm_batch_autotune solves the given data with every variant (one untimed
- * and `reps` timed solves each, CUDA events on `stream`), keeps the fastest
- * and returns it in *chosen and the mean ms per solve of variants 1..5 in
- * ms_per_variant[5] (-1: skipped); the outputs hold the last solve.
+ * vectors over 8-CTA clusters with 256-thread CTAs (two or three cluster
+ * barriers per iteration, FP64 work on the owned rows only), 2 replicated
+ * vectors (one cluster barrier per iteration, every vector operation in
+ * every CTA), 3 row-distributed with 128-thread CTAs (twice the resident
+ * clusters), 4 256-thread CTAs at most two per SM, 5 512-thread CTAs one
+ * per SM.  ilm_batch_autotune solves the given
+ * data with every variant (one untimed and `reps` timed solves each, CUDA
+ * events on `stream`), keeps the fastest and returns it in *chosen and the
+ * mean ms per solve of variants 1..ILM_CG_VARIANTS in
+ * ms_per_variant[ILM_CG_VARIANTS] (-1: skipped); the outputs hold the last
+ * solve.
  * Tuning helpers with no counterpart in the reference (the reference
  * solves one problem at a time with a dense LU).                           */
+#define ILM_CG_VARIANTS 5
 ILM_API int ilm_batch_set_cg_variant(ilm_batch_t b, int variant);
 ILM_API int ilm_batch_get_cg_variant(ilm_batch_t b, int* variant, int* nclusters);
 ILM_API int ilm_batch_autotune(ilm_batch_t b, const void* fplus, const void* fminus, void* f_out, void* s_out,
