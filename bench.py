@@ -73,7 +73,7 @@ def config(args, world):
     return {"workload": f"batched Poisson: {args.nprob} independent problems (even: Dirichlet, odd: Neumann), "
                         "n~U{128,192,256,384,512}^2 dual nodes, h=4/n, 1-3 circles/ellipses at ds=1.4h, "
                         "8-mode arc-length Fourier surface data, seeds 3+i",
-            "nprob_per_gpu": args.nprob, "tol": args.tol, "precision": "FP32 grid work, FP64 Schur build + CG",
+            "nprob_per_gpu": args.nprob, "tol": args.tol, "precision": "FP32 grid work; Schur build and CG products in float-float (~44-bit), CG vectors FP64",
             "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{world}",
             "solver": {"none": "plain CG", "bjacobi": f"block-Jacobi flexible CG (blocks of ~{args.block} points)",
                    "learned": "learned banded preconditioner for the Dirichlet problems, block-Jacobi for the Neumann ones (flexible CG)"}[
@@ -621,7 +621,7 @@ def _e2e(args, specs, stream, dt):
     t = statistics.median(times[1:])
     k = times.index(t) if t in times[1:] else 1
     return {"value": len(specs) / t, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-            "includes": "batch set-up from host points (DDF windows, tile lists, FP64 Schur build), preconditioner "
+            "includes": "batch set-up from host points (DDF windows, tile lists, float-float Schur build), preconditioner "
                         "set-up, H2D, solve (first solve also sets up the deflation of the Dirichlet net-charge "
                         "mode), D2H of all fields", "ms_per_step": 1000 * t,
             "ms_breakdown": {"batch_create": 1000 * parts[k][0], "precond_setup": 1000 * parts[k][1],

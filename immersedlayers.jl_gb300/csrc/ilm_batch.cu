@@ -868,7 +868,7 @@ int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* 
   ILM_TRY(up(B->divB, dB));
   ILM_TRY(up(B->gathA, hA));
 
-  // ---- Schur complements (FP64, LGF point-point sums) -----------------------
+  // ---- Schur complements (float-float, LGF point-point sums) ----------------
   std::vector<SchurProbDev> sp(nprob);
   int tiles = 0;
   for (int p = 0; p < nprob; ++p) {

@@ -29,27 +29,6 @@ constexpr int CG_CLUSTER = 8;
 constexpr int CGC_THREADS = 256;
 constexpr int CGC_WARPS = CGC_THREADS / 32;
 
-struct FF {
-  float hi, lo;
-};
-
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
-  s = a + b;
-  const float v = s - a;
-  e = (a - (s - v)) + (b - v);
-}
-
-// acc += S * (p_hi + p_lo) with S = s_hi + s_lo
-__device__ __forceinline__ void ff_fma(FF& acc, float s_hi, float s_lo, float p_hi, float p_lo) {
-  const float ph = s_hi * p_hi;
-  const float pe = fmaf(s_hi, p_hi, -ph);                 // exact error of the product
-  const float t = fmaf(s_hi, p_lo, fmaf(s_lo, p_hi, pe));  // low-order terms
-  float s, e;
-  two_sum(acc.hi, ph, s, e);
-  acc.hi = s;
-  acc.lo += e + t;
-}
-
 // a / b to ~2^-46 relative: an FP32 reciprocal and one FP64 correction.
 // GB300 issues FP64 at a small fraction of its FP32 rate and the divide is a
 // long FP64 sequence; every thread of a CTA evaluates the CG scalars, so the
@@ -60,15 +39,6 @@ __device__ __forceinline__ double fdiv(double a, double b) {
   const double r = (double)(1.0f / (float)b);
   const double q = a * r;
   return fma(fma(-q, b, a), r, q);
-}
-
-__device__ __forceinline__ FF ff_add(FF a, FF b) {
-  float s, e;
-  two_sum(a.hi, b.hi, s, e);
-  FF r;
-  r.hi = s;
-  r.lo = e + a.lo + b.lo;
-  return r;
 }
 
 // Block-wide sums of two doubles in fixed order; result valid in all
@@ -1387,77 +1357,121 @@ void cgff_params_set_band(void* dst, const float* band, int band_k, const int* s
 }
 
 // ---------------------------------------------------------------------------
-// block-Jacobi set-up: inverse of each diagonal block of S, FP64 Gauss-Jordan
+// block-Jacobi set-up: inverse of each diagonal block of S by Gauss-Jordan
 // with partial pivoting on S_hi + S_lo (+ a tiny shift * mean|diag| I against
-// exact singularity), stored as float-float pairs; one CTA per block
+// exact singularity), one CTA per block.  The elimination runs in float-float
+// on the FP32 pipes (each update a - f b to ~2^-44 relative): GB300 issues
+// FP64 at a small fraction of its FP32 rate and the FP64 elimination was the
+// largest part of the preconditioner set-up.  The pivot search is a warp
+// argmax (ties to the lower row, deterministic); the pivot reciprocal is one
+// FP64 divide per step.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_block_inverse(const BJBlockTask* __restrict__ tasks, double shift) {
   const BJBlockTask T = tasks[blockIdx.x];
   const int sz = T.sz;
   const int ld = 2 * sz;
-  extern __shared__ __align__(16) double Ad[];  // sz x 2sz, then fcol[sz], scal[2]
-  double* fcol = Ad + (size_t)sz * ld;
-  double* scal = fcol + sz;
-  for (int idx = threadIdx.x; idx < sz * ld; idx += blockDim.x) {
-    const int i = idx / ld, j = idx - i * ld;
-    const size_t g = (size_t)(T.s + i) * schur_ld(T.n) + T.s + j;
-    Ad[idx] = j < sz ? (double)T.Shi[g] + (double)T.Slo[g] : (j - sz == i ? 1.0 : 0.0);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  extern __shared__ __align__(16) float smf[];  // hi and lo of sz x 2sz, pivot column, scalars
+  float* Ah = smf;
+  float* Al = Ah + (size_t)sz * ld;
+  float* fh = Al + (size_t)sz * ld;
+  float* fl = fh + sz;
+  float* sc = fl + sz;  // [0..1] reciprocal of the pivot (hi, lo), [2] pivot row (int bits), [3] shift
+  const int ldS = schur_ld(T.n);
+  for (int i = warp; i < sz; i += nw)
+    for (int j = lane; j < ld; j += 32) {
+      const size_t g = (size_t)(T.s + i) * ldS + T.s + j;
+      Ah[(size_t)i * ld + j] = j < sz ? T.Shi[g] : (j - sz == i ? 1.f : 0.f);
+      Al[(size_t)i * ld + j] = j < sz ? T.Slo[g] : 0.f;
+    }
+  __syncthreads();
+  if (warp == 0) {
+    float m = 0.f;
+    for (int i = lane; i < sz; i += 32) m += fabsf(Ah[(size_t)i * ld + i]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m += __shfl_xor_sync(0xffffffffu, m, o);
+    if (lane == 0) sc[3] = (float)(shift * (double)m / (double)sz);
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    double m = 0.0;
-    for (int i = 0; i < sz; ++i) m += fabs(Ad[(size_t)i * ld + i]);
-    scal[0] = shift * m / (double)sz;
+  for (int i = threadIdx.x; i < sz; i += blockDim.x) {
+    const FF d = ff_add(FF{Ah[(size_t)i * ld + i], Al[(size_t)i * ld + i]}, FF{sc[3], 0.f});
+    const FF r = ff_renorm(d.hi, d.lo);
+    Ah[(size_t)i * ld + i] = r.hi;
+    Al[(size_t)i * ld + i] = r.lo;
   }
-  __syncthreads();
-  for (int i = threadIdx.x; i < sz; i += blockDim.x) Ad[(size_t)i * ld + i] += scal[0];
   __syncthreads();
   for (int k = 0; k < sz; ++k) {
-    if (threadIdx.x == 0) {
-      int p = k;
-      double best = fabs(Ad[(size_t)k * ld + k]);
-      for (int i = k + 1; i < sz; ++i) {
-        const double v = fabs(Ad[(size_t)i * ld + k]);
+    if (warp == 0) {  // argmax |A[i][k]| over i >= k, ties to the lower row
+      float best = -1.f;
+      int bi = k;
+      for (int i = k + lane; i < sz; i += 32) {
+        const float v = fabsf(Ah[(size_t)i * ld + k]);
         if (v > best) {
           best = v;
-          p = i;
+          bi = i;
         }
       }
-      scal[1] = (double)p;
-    }
-    __syncthreads();
-    const int p = (int)scal[1];
-    if (p != k)
-      for (int j = threadIdx.x; j < ld; j += blockDim.x) {
-        const double t = Ad[(size_t)k * ld + j];
-        Ad[(size_t)k * ld + j] = Ad[(size_t)p * ld + j];
-        Ad[(size_t)p * ld + j] = t;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ob > best || (ob == best && oi < bi)) {
+          best = ob;
+          bi = oi;
+        }
       }
+      if (lane == 0) {
+        sc[2] = __int_as_float(bi);
+        const double piv = (double)Ah[(size_t)bi * ld + k] + (double)Al[(size_t)bi * ld + k];
+        const double inv = piv != 0.0 ? 1.0 / piv : 0.0;
+        const float ih = (float)inv;
+        sc[0] = ih;
+        sc[1] = (float)(inv - (double)ih);
+      }
+    }
     __syncthreads();
-    const double piv = Ad[(size_t)k * ld + k];
-    const double inv = piv != 0.0 ? 1.0 / piv : 0.0;
+    const int p = __float_as_int(sc[2]);
+    const FF inv{sc[0], sc[1]};
+    // swap rows k and p and scale the new row k by the reciprocal of the pivot
+    for (int j = threadIdx.x; j < ld; j += blockDim.x) {
+      const FF rk{Ah[(size_t)k * ld + j], Al[(size_t)k * ld + j]};
+      const FF rp{Ah[(size_t)p * ld + j], Al[(size_t)p * ld + j]};
+      if (p != k) {
+        Ah[(size_t)p * ld + j] = rk.hi;
+        Al[(size_t)p * ld + j] = rk.lo;
+      }
+      const FF v = ff_mul(p != k ? rp : rk, inv);
+      Ah[(size_t)k * ld + j] = v.hi;
+      Al[(size_t)k * ld + j] = v.lo;
+    }
     __syncthreads();
-    for (int j = threadIdx.x; j < ld; j += blockDim.x) Ad[(size_t)k * ld + j] *= inv;
-    for (int i = threadIdx.x; i < sz; i += blockDim.x) fcol[i] = Ad[(size_t)i * ld + k];
+    for (int i = threadIdx.x; i < sz; i += blockDim.x) {
+      fh[i] = Ah[(size_t)i * ld + k];
+      fl[i] = Al[(size_t)i * ld + k];
+    }
     __syncthreads();
-    for (int idx = threadIdx.x; idx < sz * ld; idx += blockDim.x) {
-      const int i = idx / ld, j = idx - i * ld;
-      if (i != k) Ad[idx] -= fcol[i] * Ad[(size_t)k * ld + j];
+    for (int i = warp; i < sz; i += nw) {
+      if (i == k) continue;
+      const FF f{fh[i], fl[i]};
+      for (int j = lane; j < ld; j += 32) {
+        const FF a{Ah[(size_t)i * ld + j], Al[(size_t)i * ld + j]};
+        const FF r = ff_sub_mul(a, f, FF{Ah[(size_t)k * ld + j], Al[(size_t)k * ld + j]});
+        Ah[(size_t)i * ld + j] = r.hi;
+        Al[(size_t)i * ld + j] = r.lo;
+      }
     }
     __syncthreads();
   }
-  for (int idx = threadIdx.x; idx < sz * sz; idx += blockDim.x) {
-    const int i = idx / sz, j = idx - i * sz;
-    const double v = Ad[(size_t)i * ld + sz + j];
-    const float h = (float)v;
-    T.out_hi[idx] = h;
-    T.out_lo[idx] = (float)(v - (double)h);
-  }
+  for (int i = warp; i < sz; i += nw)
+    for (int j = lane; j < sz; j += 32) {
+      T.out_hi[(size_t)i * sz + j] = Ah[(size_t)i * ld + sz + j];
+      T.out_lo[(size_t)i * sz + j] = Al[(size_t)i * ld + sz + j];
+    }
 }
 
 int launch_block_inverse(const BJBlockTask* tasks_dev, int ntasks, int max_sz, cudaStream_t st) {
   if (ntasks == 0) return ILM_OK;
-  const size_t smem = ((size_t)max_sz * 2 * max_sz + max_sz + 2) * sizeof(double);
+  const size_t smem = ((size_t)max_sz * 2 * max_sz * 2 + 2 * max_sz + 4) * sizeof(float);
   if (smem > 200 * 1024) {
     set_error("block-Jacobi block of %d points too large", max_sz);
     return ILM_ERR_SIZE_LIMIT;

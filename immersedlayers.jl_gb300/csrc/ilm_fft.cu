@@ -334,6 +334,8 @@ std::map<std::pair<int, int>, void*> g_twiddles;             // (L, dtype) -> de
 std::map<std::tuple<int, int, int>, void*> g_spectra;        // (P1, P2, dtype) -> spectrum
 int g_lgf_M = -1;
 double* g_lgf = nullptr;
+float2* g_lgf_ff = nullptr;        // float-float copy of g_lgf
+const double* g_lgf_ff_src = nullptr;  // the FP64 table it was split from
 
 void gauss_legendre(int n, std::vector<double>& x, std::vector<double>& w) {
   x.resize(n);
@@ -1065,6 +1067,44 @@ int lgf_table_device(int M, const double** tab, int* ld, cudaStream_t st) {
   g_lgf_M = MM;
   *tab = g_lgf;
   *ld = MM + 1;
+  return ILM_OK;
+}
+
+__global__ void k_split_ff(size_t n, const double* __restrict__ a, float2* __restrict__ out) {
+  const size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (k < n) {
+    const double v = a[k];
+    const float h = (float)v;
+    out[k] = make_float2(h, (float)(v - (double)h));
+  }
+}
+
+// The LGF table as float-float pairs (hi, lo), for the float-float Schur
+// build; rebuilt whenever the FP64 table grows.
+int lgf_table_ff_device(int M, const float2** tab, int* ld, cudaStream_t st) {
+  const double* G = nullptr;
+  int ldd = 0;
+  ILM_TRY(lgf_table_device(M, &G, &ldd, st));
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (g_lgf_ff && g_lgf_ff_src == G) {
+    *tab = g_lgf_ff;
+    *ld = ldd;
+    return ILM_OK;
+  }
+  const size_t n = (size_t)ldd * ldd;
+  float2* d = nullptr;
+  if (cudaMalloc(&d, n * sizeof(float2)) != cudaSuccess) {
+    set_error("cudaMalloc float-float LGF table (%zu bytes) failed", n * sizeof(float2));
+    return ILM_ERR_NO_MEMORY;
+  }
+  k_split_ff<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, G, d);
+  ILM_CHECK_LAUNCH();
+  ILM_CHECK_CUDA(cudaStreamSynchronize(st));
+  if (g_lgf_ff) cudaFree(g_lgf_ff);
+  g_lgf_ff = d;
+  g_lgf_ff_src = G;
+  *tab = g_lgf_ff;
+  *ld = ldd;
   return ILM_OK;
 }
 

@@ -221,6 +221,7 @@ int conv_resources(int P1, int P2, int dtype, const void** spec, const void** tw
 int good_fft_size(int n);
 // G(m,n) table for 0<=m,n<=M (row-major (M+1)x(M+1), FP64, device; library-owned)
 int lgf_table_device(int M, const double** tab, int* ld, cudaStream_t st);
+int lgf_table_ff_device(int M, const float2** tab, int* ld, cudaStream_t st);  // (hi, lo) pairs
 int conv_plan_init(ConvPlan* plan, int n1, int n2, int dtype, cudaStream_t st);
 // out = (1/factor) * G * in (linear convolution), in/out n1 x n2 (x fastest)
 int conv_apply(ConvPlan* plan, const void* in, void* out, double inv_factor, cudaStream_t st);
@@ -228,6 +229,60 @@ int conv_apply(ConvPlan* plan, const void* in, void* out, double inv_factor, cud
 // ---------------------------------------------------------------------------
 // kernels launchers (defined in the .cu files)
 // ---------------------------------------------------------------------------
+// float-float arithmetic on the FP32 pipes (value = hi + lo, ~2^-44 relative
+// per operation): GB300 issues FP64 at a small fraction of its FP32 rate
+struct FF {
+  float hi, lo;
+};
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float v = s - a;
+  e = (a - (s - v)) + (b - v);
+}
+
+// acc += S * (p_hi + p_lo) with S = s_hi + s_lo
+__device__ __forceinline__ void ff_fma(FF& acc, float s_hi, float s_lo, float p_hi, float p_lo) {
+  const float ph = s_hi * p_hi;
+  const float pe = fmaf(s_hi, p_hi, -ph);                 // exact error of the product
+  const float t = fmaf(s_hi, p_lo, fmaf(s_lo, p_hi, pe));  // low-order terms
+  float s, e;
+  two_sum(acc.hi, ph, s, e);
+  acc.hi = s;
+  acc.lo += e + t;
+}
+
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+  float s, e;
+  two_sum(a.hi, b.hi, s, e);
+  FF r;
+  r.hi = s;
+  r.lo = e + a.lo + b.lo;
+  return r;
+}
+
+__device__ __forceinline__ FF ff_renorm(float hi, float lo) {
+  const float s = hi + lo;
+  return FF{s, lo - (s - hi)};
+}
+
+__device__ __forceinline__ FF ff_mul(FF a, FF b) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e));
+  return ff_renorm(p, e);
+}
+
+// a - f b
+__device__ __forceinline__ FF ff_sub_mul(FF a, FF f, FF b) {
+  const float p = f.hi * b.hi;
+  float pe = fmaf(f.hi, b.hi, -p);
+  pe = fmaf(f.hi, b.lo, fmaf(f.lo, b.hi, pe));
+  float s, e;
+  two_sum(a.hi, -p, s, e);
+  return ff_renorm(s, e + a.lo - pe);
+}
+
 struct GatherTerm {
   int pc;             // position class of the grid array
   const void* arr;    // grid array (cache dtype)

@@ -423,10 +423,23 @@ __global__ void k_functionals_batched(int Ptot, const int* __restrict__ pt2prob,
   out[g] = F;
 }
 
+__device__ __forceinline__ FF split_ff(double v) {
+  const float h = (float)v;
+  return FF{h, (float)(v - (double)h)};
+}
+
+// Batched Schur entries in float-float on the FP32 pipes (~2^-44 relative
+// per operation; GB300 issues FP64 at a small fraction of its FP32 rate):
+// the same 1-D weight correlations and LGF contractions as k_schur_pairs,
+// with the weights split into (hi, lo) pairs as they are read and the LGF
+// read from its float-float copy (staging each tile's LGF window in shared
+// memory was measured no faster: the kernel is bound by the float-float
+// arithmetic, not by the lookups).
+
 __global__ void __launch_bounds__(256) k_schur_pairs_batched(int nprob, const SchurProbDev* __restrict__ pr,
                                                              const Functional* __restrict__ F,
                                                              const double* __restrict__ w,
-                                                             const double* __restrict__ G, int ld, int M,
+                                                             const float2* __restrict__ G, int ld, int M,
                                                              float* __restrict__ Shi, float* __restrict__ Slo) {
   int lo = 0, hi = nprob - 1;
   const int u = blockIdx.x;
@@ -452,53 +465,68 @@ __global__ void __launch_bounds__(256) k_schur_pairs_batched(int nprob, const Sc
   if (k >= N || l >= N) return;
   const Functional& Fk = F[P.poff + k];
   const Functional& Fl = F[P.poff + l];
-  double total = 0.0;
+  FF total{0.f, 0.f};
   for (int p = 0; p < Fk.nterm; ++p) {
-    for (int q = 0; q < Fl.nterm; ++q) {
-      double cx[2 * FW - 1], cy[2 * FW - 1];
+    FF xk[FW], yk[FW];
 #pragma unroll
-      for (int d = 0; d < 2 * FW - 1; ++d) {
-        cx[d] = 0.0;
-        cy[d] = 0.0;
+    for (int a = 0; a < FW; ++a) {
+      xk[a] = split_ff(Fk.xw[p][a]);
+      yk[a] = split_ff(Fk.yw[p][a]);
+    }
+    for (int q = 0; q < Fl.nterm; ++q) {
+      FF cx[2 * FW - 1], cy[2 * FW - 1];
+#pragma unroll
+      for (int d = 0; d < 2 * FW - 1; ++d) cx[d] = cy[d] = FF{0.f, 0.f};
+#pragma unroll
+      for (int b = 0; b < FW; ++b) {
+        const FF xb = split_ff(Fl.xw[q][b]);
+        const FF yb = split_ff(Fl.yw[q][b]);
+#pragma unroll
+        for (int a = 0; a < FW; ++a) {
+          ff_fma(cx[a - b + FW - 1], xk[a].hi, xk[a].lo, xb.hi, xb.lo);
+          ff_fma(cy[a - b + FW - 1], yk[a].hi, yk[a].lo, yb.hi, yb.lo);
+        }
       }
 #pragma unroll
-      for (int a = 0; a < FW; ++a) {
-#pragma unroll
-        for (int b = 0; b < FW; ++b) {
-          cx[a - b + FW - 1] += Fk.xw[p][a] * Fl.xw[q][b];
-          cy[a - b + FW - 1] += Fk.yw[p][a] * Fl.yw[q][b];
-        }
+      for (int d = 0; d < 2 * FW - 1; ++d) {
+        cx[d] = ff_renorm(cx[d].hi, cx[d].lo);
+        cy[d] = ff_renorm(cy[d].hi, cy[d].lo);
       }
       const int Dx = Fk.xb[p] - Fl.xb[q] - (FW - 1);
       const int Dy = Fk.yb[p] - Fl.yb[q] - (FW - 1);
-      double acc = 0.0;
+      FF acc{0.f, 0.f};
 #pragma unroll
       for (int dy = 0; dy < 2 * FW - 1; ++dy) {
         int my = abs(Dy + dy);
         my = my > M ? M : my;
-        const double* Grow = G + (size_t)my;
-        double racc = 0.0;
+        const float2* Grow = G + (size_t)my;
+        FF racc{0.f, 0.f};
 #pragma unroll
         for (int dx = 0; dx < 2 * FW - 1; ++dx) {
           int mx = abs(Dx + dx);
           mx = mx > M ? M : mx;
-          racc += cx[dx] * __ldg(Grow + (size_t)mx * ld);
+          const float2 g = __ldg(Grow + (size_t)mx * ld);
+          ff_fma(racc, g.x, g.y, cx[dx].hi, cx[dx].lo);
         }
-        acc += cy[dy] * racc;
+        racc = ff_renorm(racc.hi, racc.lo);
+        ff_fma(acc, cy[dy].hi, cy[dy].lo, racc.hi, racc.lo);
       }
-      total += Fk.coef[p] * Fl.coef[q] * acc;
+      acc = ff_renorm(acc.hi, acc.lo);
+      const FF cc = split_ff(Fk.coef[p] * Fl.coef[q]);
+      ff_fma(total, cc.hi, cc.lo, acc.hi, acc.lo);
     }
   }
+  total = ff_renorm(total.hi, total.lo);
   // row-major float-float pair: S[k][l] = hi + lo
-  const double v = -w[P.poff + l] * total;
-  const float vh = (float)v;
-  Shi[P.soff + (size_t)k * schur_ld(N) + l] = vh;
-  Slo[P.soff + (size_t)k * schur_ld(N) + l] = (float)(v - (double)vh);
+  const FF wl = split_ff(-w[P.poff + l]);
+  const FF v = ff_mul(wl, total);
+  Shi[P.soff + (size_t)k * schur_ld(N) + l] = v.hi;
+  Slo[P.soff + (size_t)k * schur_ld(N) + l] = v.lo;
   if (ti != tj) {
-    const double vt = -w[P.poff + k] * total;
-    const float th = (float)vt;
-    Shi[P.soff + (size_t)l * schur_ld(N) + k] = th;
-    Slo[P.soff + (size_t)l * schur_ld(N) + k] = (float)(vt - (double)th);
+    const FF wk = split_ff(-w[P.poff + k]);
+    const FF vt = ff_mul(wk, total);
+    Shi[P.soff + (size_t)l * schur_ld(N) + k] = vt.hi;
+    Slo[P.soff + (size_t)l * schur_ld(N) + k] = vt.lo;
   }
 }
 
@@ -506,9 +534,9 @@ int schur_build_batched(int nprob, const SchurProbDev* probs_dev, int total_tile
                         const BatchWin& W, const double* w, Functional* F, float* Shi, float* Slo, int max_grid,
                         cudaStream_t st) {
   if (Ptot == 0) return ILM_OK;
-  const double* G = nullptr;
+  const float2* G = nullptr;
   int ld = 0;
-  ILM_TRY(lgf_table_device(max_grid + 16, &G, &ld, st));
+  ILM_TRY(lgf_table_ff_device(max_grid + 16, &G, &ld, st));
   k_functionals_batched<<<(Ptot + 127) / 128, 128, 0, st>>>(Ptot, pt2prob, probs_dev, W.bx[0], W.bx[1], W.by[0],
                                                             W.by[1], W.wx64[0], W.wx64[1], W.wy64[0], W.wy64[1],
                                                             W.nx64, W.ny64, F);
