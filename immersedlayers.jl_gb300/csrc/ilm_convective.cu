@@ -24,9 +24,9 @@ namespace ilm {
 
 namespace {
 
-constexpr int BX = 32, BY = 8;
+constexpr int BX = 32, BY = 8, RY = 4;
 
-inline dim3 grid2(int n1, int n2, int nz = 1) { return dim3((n1 + BX - 1) / BX, (n2 + BY - 1) / BY, nz); }
+inline dim3 grid2(int n1, int n2) { return dim3((n1 + BX - 1) / BX, (n2 + BY * RY - 1) / (BY * RY)); }
 
 template <typename T>
 __device__ __forceinline__ T ld(const T* p, size_t k) {
@@ -36,9 +36,8 @@ __device__ __forceinline__ T ld(const T* p, size_t k) {
 // v . grad p, p on Nodes{Primal} (m = NX-1 by NY-1), v on Edges{Primal}
 // (:318-328).  gx at dual x k: p[k]-p[k-1] for 1 <= k <= NX-2, else 0.
 template <typename T>
-__global__ void __launch_bounds__(BX* BY) k_vdp_np(int NX, int NY, const T* __restrict__ vu, const T* __restrict__ vv,
-                                                   const T* __restrict__ p, T* __restrict__ out, T sc) {
-  const int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+__device__ __forceinline__ void vdp_np_at(int i, int j, int NX, int NY, const T* __restrict__ vu,
+    const T* __restrict__ vv, const T* __restrict__ p, T* __restrict__ out, T sc) {
   const int m = NX - 1;
   if (i >= m || j >= NY - 1) return;
   const size_t c = (size_t)j * m + i;
@@ -52,13 +51,23 @@ __global__ void __launch_bounds__(BX* BY) k_vdp_np(int NX, int NY, const T* __re
   out[c] = (T)0.5 * (tx + ty) * sc;
 }
 
+template <typename T>
+__global__ void __launch_bounds__(BX* BY) k_vdp_np(int NX, int NY, const T* __restrict__ vu, const T* __restrict__ vv,
+    const T* __restrict__ p, T* __restrict__ out, T sc) {
+  // RY output rows per thread (j, j + BY, ...), all independent, so their
+  // loads are in flight together
+  const int i = blockIdx.x * BX + threadIdx.x;
+  const int jb = blockIdx.y * BY * RY + threadIdx.y;
+#pragma unroll
+  for (int r = 0; r < RY; ++r) vdp_np_at(i, jb + r * BY, NX, NY, vu, vv, p, out, sc);
+}
+
 // v . grad w, w on Nodes{Dual} (NX x NY), v on Edges{Primal} (:330-342):
 // v averaged onto the Edges{Dual} positions (four-point means), times the
 // Edges{Dual} gradient of w, averaged onto the non-ghost dual nodes.
 template <typename T>
-__global__ void __launch_bounds__(BX* BY) k_vdw_nd(int NX, int NY, const T* __restrict__ vu, const T* __restrict__ vv,
-                                                   const T* __restrict__ w, T* __restrict__ out, T sc) {
-  const int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+__device__ __forceinline__ void vdw_nd_at(int i, int j, int NX, int NY, const T* __restrict__ vu,
+    const T* __restrict__ vv, const T* __restrict__ w, T* __restrict__ out, T sc) {
   if (i >= NX || j >= NY) return;
   const size_t c = (size_t)j * NX + i;
   if (i < 1 || i > NX - 2 || j < 1 || j > NY - 2) {
@@ -84,6 +93,17 @@ __global__ void __launch_bounds__(BX* BY) k_vdw_nd(int NX, int NY, const T* __re
   out[c] = (T)0.5 * (tx + ty) * sc;
 }
 
+template <typename T>
+__global__ void __launch_bounds__(BX* BY) k_vdw_nd(int NX, int NY, const T* __restrict__ vu, const T* __restrict__ vv,
+    const T* __restrict__ w, T* __restrict__ out, T sc) {
+  // RY output rows per thread (j, j + BY, ...), all independent, so their
+  // loads are in flight together
+  const int i = blockIdx.x * BX + threadIdx.x;
+  const int jb = blockIdx.y * BY * RY + threadIdx.y;
+#pragma unroll
+  for (int r = 0; r < RY; ++r) vdw_nd_at(i, jb + r * BY, NX, NY, vu, vv, w, out, sc);
+}
+
 // v . grad u for Edges{Primal} v and u (:344-371; u . grad u with v = u).
 // Thread (i, j) writes out.u(i, j) (j <= NY-2) and out.v(i, j) (i <= NX-2):
 // both components in one CTA, so the inputs a CTA needs come from DRAM once.
@@ -94,11 +114,9 @@ __global__ void __launch_bounds__(BX* BY) k_vdw_nd(int NX, int NY, const T* __re
 //   dvdy (primal, primal):     mean_y(v.v) * (u.v[l+1]-u.v[l])
 // and the result is their average back onto the edges.
 template <typename T>
-__global__ void __launch_bounds__(BX* BY) k_vdu_edges(int NX, int NY, const T* __restrict__ vu,
-                                                      const T* __restrict__ vv, const T* __restrict__ uu,
-                                                      const T* __restrict__ uv, T* __restrict__ ou,
-                                                      T* __restrict__ ov, T sc) {
-  const int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+__device__ __forceinline__ void vdu_edges_at(int i, int j, int NX, int NY, const T* __restrict__ vu,
+    const T* __restrict__ vv, const T* __restrict__ uu, const T* __restrict__ uv, T* __restrict__ ou,
+    T* __restrict__ ov, T sc) {
   const int m = NX - 1;
   if (i >= NX || j >= NY) return;
   if (j <= NY - 2) {
@@ -147,14 +165,24 @@ __global__ void __launch_bounds__(BX* BY) k_vdu_edges(int NX, int NY, const T* _
   }
 }
 
+template <typename T>
+__global__ void __launch_bounds__(BX* BY) k_vdu_edges(int NX, int NY, const T* __restrict__ vu,
+    const T* __restrict__ vv, const T* __restrict__ uu, const T* __restrict__ uv, T* __restrict__ ou,
+    T* __restrict__ ov, T sc) {
+  // RY output rows per thread (j, j + BY, ...), all independent, so their
+  // loads are in flight together
+  const int i = blockIdx.x * BX + threadIdx.x;
+  const int jb = blockIdx.y * BY * RY + threadIdx.y;
+#pragma unroll
+  for (int r = 0; r < RY; ++r) vdu_edges_at(i, jb + r * BY, NX, NY, vu, vv, uu, uv, ou, ov, sc);
+}
+
 // w x v (:419-434): out.u = mean_y(-mean_x(v.v) w), out.v = mean_x(mean_y(v.u) w),
 // the inner means onto the non-ghost dual nodes only.  Thread (i, j) writes
 // out.u(i, j) (j <= NY-2) and out.v(i, j) (i <= NX-2).
 template <typename T>
-__global__ void __launch_bounds__(BX* BY) k_w_cross_v(int NX, int NY, const T* __restrict__ w,
-                                                      const T* __restrict__ vu, const T* __restrict__ vv,
-                                                      T* __restrict__ ou, T* __restrict__ ov) {
-  const int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+__device__ __forceinline__ void w_cross_v_at(int i, int j, int NX, int NY, const T* __restrict__ w,
+    const T* __restrict__ vu, const T* __restrict__ vv, T* __restrict__ ou, T* __restrict__ ov) {
   const int m = NX - 1;
   if (i >= NX || j >= NY) return;
   const T w0 = ld(w, (size_t)j * NX + i);
@@ -176,6 +204,17 @@ __global__ void __launch_bounds__(BX* BY) k_w_cross_v(int NX, int NY, const T* _
     }
     ov[(size_t)j * m + i] = r;
   }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(BX* BY) k_w_cross_v(int NX, int NY, const T* __restrict__ w,
+    const T* __restrict__ vu, const T* __restrict__ vv, T* __restrict__ ou, T* __restrict__ ov) {
+  // RY output rows per thread (j, j + BY, ...), all independent, so their
+  // loads are in flight together
+  const int i = blockIdx.x * BX + threadIdx.x;
+  const int jb = blockIdx.y * BY * RY + threadIdx.y;
+#pragma unroll
+  for (int r = 0; r < RY; ++r) w_cross_v_at(i, jb + r * BY, NX, NY, w, vu, vv, ou, ov);
 }
 
 }  // namespace
