@@ -899,15 +899,24 @@ int ilm_solve_dirichlet(ilm_cache_t c, const void* fplus, const void* fminus, vo
 //   f = f* + L^{-1} D_s [phi].
 int ilm_solve_neumann(ilm_cache_t c, const void* vplus, const void* vminus, void* f_out, void* df_out, double tol,
                       int maxiter, ilm_solve_info_t* info, ilm_stream_t stream) {
+  return ilm_solve_neumann_full(c, vplus, vminus, f_out, df_out, nullptr, nullptr, tol, maxiter, info, stream);
+}
+
+int ilm_solve_neumann_full(ilm_cache_t c, const void* vplus, const void* vminus, void* f_out, void* df_out,
+                           void* s_out, void* ds_out, double tol, int maxiter, ilm_solve_info_t* info,
+                           ilm_stream_t stream) {
   CHECK_CACHE(c);
   ILM_REQUIRE(c->kind == ILM_CACHE_SCALAR, "solve_neumann needs a scalar cache");
   ILM_REQUIRE(vplus && vminus && f_out && df_out, "null argument");
+  ILM_REQUIRE((s_out == nullptr) == (ds_out == nullptr), "solve_neumann: s_out and ds_out go together");
   ILM_REQUIRE(tol > 0.0 && maxiter > 0, "bad tolerance / iteration limit");
   cudaStream_t st = as_stream(stream);
   const int N = c->npts;
   const size_t np = c->grid.shape(PC_P).numel();
+  const size_t nd = c->grid.shape(PC_D).numel();
   if (N == 0) {
     if (info) *info = ilm_solve_info_t{0, 1, 0.0};
+    if (s_out) ILM_TRY(st_fill(nd, c->dtype, 0.0, s_out, st));
     return st_fill(np, c->dtype, 0.0, f_out, st);
   }
   void *jump, *avg, *g, *rhs64, *x64, *fstar, *corr;
@@ -933,7 +942,26 @@ int ilm_solve_neumann(ilm_cache_t c, const void* vplus, const void* vminus, void
   ILM_TRY(ilm_surface_divergence(c, df_out, corr, stream));
   ILM_TRY(inverse_laplacian_kind(c, ILM_NODES_PRIMAL, corr, corr, st));
   ILM_TRY(st_axpby(np, c->dtype, 1.0, corr, 1.0, fstar, f_out, st));
-  return cg;
+  if (!s_out) return cg;
+  // streamfunction (test/literate/neumann.jl:129-138): s* = C_s^T [phi];
+  // S ds = G^x_s f*;  s = L^-1 (s* - C^x_s^T ds)
+  ilm_solve_info_t info2{0, 1, 0.0};
+  ILM_TRY(ilm_surface_grad_cross(c, fstar, g, stream));
+  ILM_TRY(st_convert(N, c->dtype, g, ILM_F64, rhs64, st));
+  const int cg2 = schur_cg(c, c->S_neu64, c->S_neu32, static_cast<double*>(rhs64), static_cast<double*>(x64), tol,
+                           maxiter, &info2, st);
+  if (cg2 != ILM_OK && cg2 != ILM_ERR_NOT_CONVERGED) return cg2;
+  ILM_TRY(st_convert(N, ILM_F64, x64, c->dtype, ds_out, st));
+  ILM_TRY(ilm_surface_curl(c, 0, ILM_SCALAR_DATA, df_out, s_out, stream));   // s*
+  ILM_TRY(ilm_surface_curl_cross(c, 0, ds_out, corr, stream));               // C^x_s^T ds (Nodes{Dual})
+  ILM_TRY(st_axpby(nd, c->dtype, 1.0, s_out, -1.0, corr, corr, st));
+  ILM_TRY(inverse_laplacian_kind(c, ILM_NODES_DUAL, corr, s_out, st));
+  if (info) {
+    info->iterations += info2.iterations;
+    info->converged = info->converged && info2.converged;
+    info->rel_residual = std::max(info->rel_residual, info2.rel_residual);
+  }
+  return cg != ILM_OK ? cg : cg2;
 }
 
 }  // extern "C"

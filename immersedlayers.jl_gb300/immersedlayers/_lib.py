@@ -94,6 +94,7 @@ SIGNATURES = {
     "ilm_schur_build": [_VP, _I, _D, _VP, _VP],
     "ilm_solve_dirichlet": [_VP, _VP, _VP, _VP, _VP, _D, _I, C.POINTER(SolveInfo), _VP],
     "ilm_solve_neumann": [_VP, _VP, _VP, _VP, _VP, _D, _I, C.POINTER(SolveInfo), _VP],
+    "ilm_solve_neumann_full": [_VP, _VP, _VP, _VP, _VP, _VP, _VP, _D, _I, C.POINTER(SolveInfo), _VP],
     "ilm_solve_stokes": [_VP, _VP, _VP, _VP, _VP, _VP, _D, _I, C.POINTER(SolveInfo), _VP],
     "ilm_batch_create": [_I, C.POINTER(BatchProblem), _DP, _DP, _DP, _DP, _DP, _I, _I, C.POINTER(_VP)],
     "ilm_batch_destroy": [_VP],
@@ -129,7 +130,7 @@ SIGNATURES = {
 _RESTYPES = {"ilm_status_string": C.c_char_p, "ilm_last_error": C.c_char_p}
 
 # functions that may legitimately return ILM_ERR_NOT_CONVERGED (reported via info)
-_SOFT = {"ilm_solve_dirichlet", "ilm_solve_neumann", "ilm_solve_stokes"}
+_SOFT = {"ilm_solve_dirichlet", "ilm_solve_neumann", "ilm_solve_neumann_full", "ilm_solve_stokes"}
 
 _lib = None
 _lock = threading.Lock()

@@ -143,6 +143,22 @@ def solve_neumann(cache, vplus: PointData, vminus: PointData, tol=1e-8, maxiter=
     return f, df, dict(iterations=info.iterations, converged=bool(info.converged), rel_residual=info.rel_residual)
 
 
+def solve_neumann_full(cache, vplus: PointData, vminus: PointData, tol=1e-8, maxiter=5000, stream=None):
+    """The literate NeumannPoissonProblem solve (test/literate/neumann.jl:101-142)
+    on the device: returns (f::Nodes{Primal}, df::ScalarData,
+    s::Nodes{Dual} streamfunction, ds::ScalarData, info)."""
+    from .core import zeros_gridcurl
+    f = zeros_grid(cache)
+    df = zeros_surface(cache)
+    s = zeros_gridcurl(cache)
+    ds = zeros_surface(cache)
+    info = L.SolveInfo()
+    L.call("ilm_solve_neumann_full", cache._h, _ptr(vplus.data), _ptr(vminus.data), _ptr(f.data), _ptr(df.data),
+           _ptr(s.data), _ptr(ds.data), float(tol), int(maxiter), C.byref(info), _stream_ptr(stream))
+    return f, df, s, ds, dict(iterations=info.iterations, converged=bool(info.converged),
+                              rel_residual=info.rel_residual)
+
+
 def solve_stokes(cache, vplus: PointData, vminus: PointData, tol=1e-8, maxiter=5000, stream=None):
     """Device Stokes solve (vector cache); returns (v::Edges{Primal},
     s::Nodes{Dual}, sigma::VectorData, info)."""
@@ -158,7 +174,9 @@ def solve_stokes(cache, vplus: PointData, vminus: PointData, tol=1e-8, maxiter=5
 
 
 def solve(prob: ILMProblem, sys: ILMSystem, tol=1e-8, maxiter=5000, filter_power=0):
-    """`solve(prob, sys)` for the built-in problems (bc from `prob.bc`).
+    """`solve(prob, sys)` for the built-in problems (bc from `prob.bc`):
+    Dirichlet (f, s), Neumann (f, df, s, ds) as test/literate/neumann.jl:140,
+    Stokes (v, s, sigma).
     filter_power=k returns the Dirichlet surface data filtered k times,
     C^k s with C = create_surface_filter(base_cache) (the literate
     DirichletPoissonProblem returns C^6 s, test/literate/problems.jl:297)."""
@@ -169,7 +187,9 @@ def solve(prob: ILMProblem, sys: ILMSystem, tol=1e-8, maxiter=5000, filter_power
             from .core import SurfaceFilter
             SurfaceFilter(sys.base_cache, filter_power).apply_(s, s)
     elif isinstance(prob, NeumannPoissonProblem):
-        f, s, info = solve_neumann(sys.base_cache, plus, minus, tol, maxiter)
+        f, df, s, ds, info = solve_neumann_full(sys.base_cache, plus, minus, tol, maxiter)
+        sys.last_info = info
+        return f, df, s, ds
     elif isinstance(prob, StokesFlowProblem):
         v, s, sigma, info = solve_stokes(sys.base_cache, plus, minus, tol, maxiter)
         sys.last_info = info

@@ -268,6 +268,16 @@ ILM_API int ilm_solve_dirichlet(ilm_cache_t c, const void* fplus, const void* fm
 ILM_API int ilm_solve_neumann(ilm_cache_t c, const void* vplus, const void* vminus,
                       void* f_out, void* df_out, double tol, int maxiter,
                       ilm_solve_info_t* info, ilm_stream_t stream);
+/* The whole NeumannPoissonProblem solve of test/literate/neumann.jl:101-142:
+ * the potential f (Nodes{Primal}) and df = [phi], then the streamfunction
+ * s (Nodes{Dual}) and ds = [psi] (ScalarData): s* = C_s^T df, S ds =
+ * G^x_s f* with the same S = -C_s L^-1 C_s^T, s = L^-1 (s* - C^x_s^T ds)
+ * (:129-138).  s_out and ds_out both null: the potential part only (=
+ * ilm_solve_neumann).  info sums the two CG solves' iterations and reports
+ * the worse residual.                                                      */
+ILM_API int ilm_solve_neumann_full(ilm_cache_t c, const void* vplus, const void* vminus, void* f_out, void* df_out,
+                                   void* s_out, void* ds_out, double tol, int maxiter, ilm_solve_info_t* info,
+                                   ilm_stream_t stream);
 /* Stokes flow with no-slip surfaces (vector GridScaling cache): the
  * StokesFlowProblem solve of test/literate/stokes.jl:101-166.  vplus/vminus:
  * VectorData (2N) surface velocities outside/inside; v_out: Edges{Primal}

@@ -59,3 +59,34 @@ def test_neumann_circle(cuda):
     f_ref, df_ref, _, _ = O.solve_neumann(oc, vplus, np.zeros_like(vplus))
     # the field is insensitive to the (near-)null space of S; compare it
     assert rel(f.numpy_components(), f_ref) < 1e-6
+
+
+def test_neumann_streamfunction_circle(cuda):
+    """The whole literate Neumann solve (test/literate/neumann.jl:101-142):
+    potential, [phi], streamfunction and [psi] against the oracle's
+    block-LU solve on the reference example (v_n+ = n_x, v_n- = 0); S is
+    well conditioned here (cond ~1.3e3), so ds and s are determined."""
+    import torch
+    import immersedlayers as il
+    from immersedlayers import bodies as B
+    h = 0.04
+    og = O.Grid.physical((-2.0, 2.0), (-2.0, 2.0), h)
+    b = B.circle(1.0, ds=1.4 * h)
+    g = il.PhysicalGrid((-2.0, 2.0), (-2.0, 2.0), h)
+    c = il.SurfaceScalarCache(b, g)
+    vplus = b.nx.copy()
+    vp = il.ScalarData(torch.tensor(vplus, device="cuda"))
+    vm = il.ScalarData.zeros(len(b))
+    f, df, s, ds, info = il.solve_neumann_full(c, vp, vm, tol=1e-11, maxiter=20000)
+    assert info["converged"], info
+    f_ref, df_ref, s_ref, ds_ref = O.solve_neumann(oracle_cache(og, b), vplus, np.zeros_like(vplus))
+    assert rel(f.numpy_components(), f_ref) < 1e-6
+    assert rel(s.numpy_components(), s_ref) < 1e-6
+    assert rel(ds.numpy(), ds_ref) < 1e-6
+    assert rel(df.numpy(), df_ref) < 1e-5
+    # the problem API returns the same four fields
+    prob = il.NeumannPoissonProblem(g, b, bc={"exterior": lambda c_, pp: c_.nrm.data[:len(b)],
+                                              "interior": lambda c_, pp: 0.0 * c_.nrm.data[:len(b)]})
+    sys_ = il.construct_system(prob)
+    f2, df2, s2, ds2 = il.solve(prob, sys_, tol=1e-11, maxiter=20000)
+    assert rel(s2.numpy_components(), s_ref) < 1e-6
