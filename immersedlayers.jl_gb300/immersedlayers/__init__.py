@@ -14,7 +14,7 @@ from .core import (Dual, EdgeGradient, EdgeGradientPrimal, Edges, EdgesDual, Edg
                    complementary_mask_, create_CLinvCT, create_GLinvD, create_nRTRn, create_RTLinvR, create_surface_filter,
                    curl_, SurfaceFilter, ConvectiveDerivativeCache, RotConvectiveDerivativeCache,
                    convective_derivative, convective_derivative_, w_cross_v, w_cross_v_, x_gridcurl,
-                   y_gridcurl, x_griddiv, y_griddiv,
+                   y_gridcurl, x_griddiv, y_griddiv, x_gridgrad, y_gridgrad,
                    divergence_, dot, grad_, integrate, interpolate_, inverse_laplacian_, laplacian_, mask, mask_,
                    norm, normal_cross_interpolate_, normal_dot_interpolate_, normal_interpolate_,
                    normal_interpolate_symm_, normals, ones_grid, ones_surface, points, regularize_,

@@ -396,6 +396,16 @@ def y_gridcurl(cache):
     return _coords(cache, zeros_gridcurl(cache), 1)
 
 
+def x_gridgrad(cache):
+    """x coordinates of the gradient grid data (Edges{Primal} for scalar
+    caches, EdgeGradient{Primal} for vector caches; src/cache.jl:684-689)."""
+    return _coords(cache, zeros_gridgrad(cache), 0)
+
+
+def y_gridgrad(cache):
+    return _coords(cache, zeros_gridgrad(cache), 1)
+
+
 def x_griddiv(cache):
     """x coordinates of the divergence grid data (Nodes{Primal}, vector caches)."""
     return _coords(cache, NodesPrimal.zeros(cache.g, cache.dtype), 0)
