@@ -189,6 +189,17 @@ __global__ void k_div_rows(int n, const T* __restrict__ d, const T* x, T* out) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k < n) out[k] = d[k] != (T)0 ? x[k] / d[k] : (T)0;
 }
+// Schur builds by columns: e = unit vector, y = the operator chain of e
+template <typename T>
+__global__ void k_unit_col(int n, int col, T* __restrict__ e) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) e[k] = k == col ? (T)1 : (T)0;
+}
+template <typename T>
+__global__ void k_store_col(int n, const T* __restrict__ y, double s, double* __restrict__ A) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) A[k] = s * (double)y[k];
+}
 }  // namespace ilm
 
 using namespace ilm;
@@ -777,11 +788,89 @@ int ilm_dot_surface(ilm_cache_t c, int ncomp, const void* a, const void* b, doub
 }
 
 // ---- Schur complements ----------------------------------------------------
+// The reference's column-by-column build (src/matrix_operators.jl:9-244) on
+// the device: one unit vector per column through the operator chain, for the
+// kinds and caches the point-pair sums do not cover.
+static int schur_build_columns(ilm_cache_s* c, int which, double scale, double* A, cudaStream_t st) {
+  const bool vec = c->kind == ILM_CACHE_VECTOR;
+  const bool scalar_data = !vec || which == ILM_SCHUR_CLINVCT_SCALAR;
+  const int n = c->npts * (scalar_data ? 1 : 2);
+  if (n == 0) return ILM_OK;
+  void *e, *y, *g1, *g2;
+  ILM_TRY(pscr(c, 1, &e));
+  ILM_TRY(pscr(c, 2, &y));
+  ILM_TRY(gscr(c, 2, &g1));
+  ILM_TRY(gscr(c, 5, &g2));
+  void* const s_ = (void*)st;
+  const int gk = vec ? ILM_EDGES_PRIMAL : ILM_NODES_PRIMAL;  // the cache's grid data
+  const int nb = (n + 255) / 256;
+  double sign = -1.0;
+  for (int col = 0; col < n; ++col) {
+    if (c->dtype == ILM_F64) k_unit_col<double><<<nb, 256, 0, st>>>(n, col, static_cast<double*>(e));
+    else k_unit_col<float><<<nb, 256, 0, st>>>(n, col, static_cast<float*>(e));
+    ILM_CHECK_LAUNCH();
+    switch (which) {
+      case ILM_SCHUR_RTLINVR:  // -R^T L^-1 R
+        ILM_TRY(ilm_regularize(c, gk, e, g1, s_));
+        ILM_TRY(inverse_laplacian_kind(c, gk, g1, g2, st));
+        ILM_TRY(ilm_interpolate(c, gk, g2, y, s_));
+        break;
+      case ILM_SCHUR_CLINVCT:  // -C_s L^-1 C_s^T (point data of the cache)
+      case ILM_SCHUR_CLINVCT_SCALAR: {
+        const int pk = scalar_data ? ILM_SCALAR_DATA : ILM_VECTOR_DATA;
+        ILM_TRY(ilm_surface_curl(c, 0, pk, e, g1, s_));
+        ILM_TRY(inverse_laplacian_kind(c, ILM_NODES_DUAL, g1, g2, st));
+        ILM_TRY(ilm_surface_curl(c, 1, pk, g2, y, s_));
+        break;
+      }
+      case ILM_SCHUR_CL2INVCT:  // -C_s L^-2 C_s^T
+        ILM_TRY(ilm_surface_curl(c, 0, ILM_VECTOR_DATA, e, g1, s_));
+        ILM_TRY(inverse_laplacian_kind(c, ILM_NODES_DUAL, g1, g2, st));
+        ILM_TRY(inverse_laplacian_kind(c, ILM_NODES_DUAL, g2, g1, st));
+        ILM_TRY(ilm_surface_curl(c, 1, ILM_VECTOR_DATA, g1, y, s_));
+        break;
+      case ILM_SCHUR_GLINVD:  // -G_s L^-1 D_s
+        ILM_TRY(ilm_surface_divergence(c, e, g1, s_));
+        ILM_TRY(inverse_laplacian_kind(c, gk, g1, g2, st));
+        ILM_TRY(ilm_surface_grad(c, g2, y, s_));
+        break;
+      case ILM_SCHUR_GLINVD_SYMM:
+        ILM_TRY(ilm_surface_divergence_symm(c, e, g1, s_));
+        ILM_TRY(inverse_laplacian_kind(c, gk, g1, g2, st));
+        ILM_TRY(ilm_surface_grad_symm(c, g2, y, s_));
+        break;
+      case ILM_SCHUR_GLINVD_CROSS:  // -G^x_s L^-1 D^x_s (scalar caches)
+        ILM_TRY(ilm_surface_divergence_cross(c, e, g1, s_));
+        ILM_TRY(inverse_laplacian_kind(c, ILM_NODES_PRIMAL, g1, g2, st));
+        ILM_TRY(ilm_surface_grad_cross(c, g2, y, s_));
+        break;
+      case ILM_SCHUR_NRTRN:  // + n.R_f^T R_f n o (no inverse Laplacian)
+        ILM_TRY(ilm_regularize_normal(c, e, g1, s_));
+        ILM_TRY(ilm_normal_interpolate(c, g1, y, s_));
+        sign = 1.0;
+        break;
+    }
+    if (c->dtype == ILM_F64)
+      k_store_col<double><<<nb, 256, 0, st>>>(n, static_cast<const double*>(y), sign * scale, A + (size_t)col * n);
+    else
+      k_store_col<float><<<nb, 256, 0, st>>>(n, static_cast<const float*>(y), sign * scale, A + (size_t)col * n);
+    ILM_CHECK_LAUNCH();
+  }
+  return ILM_OK;
+}
+
 int ilm_schur_build(ilm_cache_t c, int which, double scale, double* A_dev, ilm_stream_t stream) {
   CHECK_CACHE(c);
   ILM_REQUIRE(A_dev || c->npts == 0, "null matrix");
-  ILM_REQUIRE(which >= ILM_SCHUR_RTLINVR && which <= ILM_SCHUR_NRTRN, "bad Schur kind %d", which);
-  return schur_build(c, which, scale, A_dev, as_stream(stream));
+  ILM_REQUIRE(which >= ILM_SCHUR_RTLINVR && which <= ILM_SCHUR_GLINVD_CROSS, "bad Schur kind %d", which);
+  const bool vec = c->kind == ILM_CACHE_VECTOR;
+  ILM_REQUIRE(vec || (which != ILM_SCHUR_CLINVCT_SCALAR && which != ILM_SCHUR_CL2INVCT &&
+                      which != ILM_SCHUR_GLINVD_SYMM),
+              "Schur kind %d needs a vector cache", which);
+  ILM_REQUIRE(!vec || which != ILM_SCHUR_GLINVD_CROSS, "Schur kind %d needs a scalar cache", which);
+  cudaStream_t st = as_stream(stream);
+  if (!vec && which <= ILM_SCHUR_NRTRN) return schur_build(c, which, scale, A_dev, st);
+  return schur_build_columns(c, which, scale, A_dev, st);
 }
 
 }  // extern "C"

@@ -12,6 +12,7 @@ from .core import (Dual, EdgeGradient, EdgeGradientPrimal, Edges, EdgesDual, Edg
                    IndexScaling, Nodes, NodesDual, NodesPrimal, PhysicalGrid, PointData, Primal, ScalarData,
                    SurfaceScalarCache, SurfaceVectorCache, TensorData, VectorData, areas, complementary_mask,
                    complementary_mask_, create_CLinvCT, create_GLinvD, create_nRTRn, create_RTLinvR, create_surface_filter,
+                   create_CLinvCT_scalar, create_CL2invCT, create_GLinvD_symm, create_GLinvD_cross,
                    curl_, SurfaceFilter, ConvectiveDerivativeCache, RotConvectiveDerivativeCache,
                    convective_derivative, convective_derivative_, w_cross_v, w_cross_v_, x_gridcurl,
                    y_gridcurl, x_griddiv, y_griddiv, x_gridgrad, y_gridgrad,

@@ -21,7 +21,8 @@ GRID_SCALING, INDEX_SCALING = 0, 1
 CACHE_SCALAR, CACHE_VECTOR = 0, 1
 NODES_PRIMAL, NODES_DUAL, EDGES_PRIMAL, EDGES_DUAL, EDGEGRAD_PRIMAL = 0, 1, 2, 3, 4
 SCALAR_DATA, VECTOR_DATA, TENSOR_DATA = 0, 1, 2
-SCHUR = {"RTLinvR": 0, "CLinvCT": 1, "GLinvD": 2, "nRTRn": 3}
+SCHUR = {"RTLinvR": 0, "CLinvCT": 1, "GLinvD": 2, "nRTRn": 3, "CLinvCT_scalar": 4, "CL2invCT": 5, "GLinvD_symm": 6,
+         "GLinvD_cross": 7}
 
 
 class ILMError(RuntimeError):

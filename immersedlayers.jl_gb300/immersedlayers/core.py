@@ -690,7 +690,9 @@ def integrate(a, cache):
 # Schur complements (src/matrix_operators.jl)
 # ---------------------------------------------------------------------------
 def _schur(cache, which, scale):
-    A = torch.empty((cache.N, cache.N), dtype=torch.float64, device="cuda")
+    scalar_data = cache.kind == L.CACHE_SCALAR or which == "CLinvCT_scalar"
+    n = cache.N * (1 if scalar_data else 2)
+    A = torch.empty((n, n), dtype=torch.float64, device="cuda")
     L.call("ilm_schur_build", cache._h, L.SCHUR[which], float(scale), _ptr(A), None)
     # device buffer is column-major (A[k + N l]) -> transpose the row-major view
     return A.t()
@@ -710,6 +712,28 @@ def create_GLinvD(cache, scale=1.0):
 
 def create_nRTRn(cache, scale=1.0):
     return _schur(cache, "nRTRn", scale)
+
+
+def create_CLinvCT_scalar(cache, scale=1.0):
+    """-C_s L^-1 C_s^T on the ScalarData of a vector cache (src/matrix_operators.jl:71-93)."""
+    return _schur(cache, "CLinvCT_scalar", scale)
+
+
+def create_CL2invCT(cache, scale=1.0):
+    """-C_s L^-2 C_s^T on VectorData (vector cache, src/matrix_operators.jl:102-125)."""
+    return _schur(cache, "CL2invCT", scale)
+
+
+def create_GLinvD_symm(cache, scale=1.0):
+    """-G_s L^-1 D_s with the symmetric-tensor operators (vector cache, src/matrix_operators.jl:165-185)."""
+    return _schur(cache, "GLinvD_symm", scale)
+
+
+def create_GLinvD_cross(cache, scale=1.0):
+    """-G^x_s L^-1 D^x_s (scalar cache, src/matrix_operators.jl:195-215; the
+    reference's version raises, its surface_divergence_cross! refers to an
+    undefined variable)."""
+    return _schur(cache, "GLinvD_cross", scale)
 
 
 class SurfaceFilter:

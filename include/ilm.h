@@ -81,7 +81,11 @@ typedef enum {
   ILM_SCHUR_RTLINVR = 0,   /* create_RTLinvR        :9-30    -R^T L^-1 R        */
   ILM_SCHUR_CLINVCT = 1,   /* create_CLinvCT        :40-61   -C_s L^-1 C_s^T    */
   ILM_SCHUR_GLINVD = 2,    /* create_GLinvD         :135-155 -G_s L^-1 D_s      */
-  ILM_SCHUR_NRTRN = 3      /* create_nRTRn          :225-244  n.R_f^T R_f n o   */
+  ILM_SCHUR_NRTRN = 3,     /* create_nRTRn          :225-244  n.R_f^T R_f n o   */
+  ILM_SCHUR_CLINVCT_SCALAR = 4, /* create_CLinvCT_scalar :71-93 (vector cache, ScalarData) */
+  ILM_SCHUR_CL2INVCT = 5,  /* create_CL2invCT       :102-125 -C_s L^-2 C_s^T (vector cache) */
+  ILM_SCHUR_GLINVD_SYMM = 6, /* create_GLinvD_symm  :165-185 (vector cache)     */
+  ILM_SCHUR_GLINVD_CROSS = 7 /* create_GLinvD_cross :195-215 (scalar cache)     */
 } ilm_schur_kind_t;
 
 typedef struct ilm_grid_s* ilm_grid_t;
@@ -252,9 +256,15 @@ ILM_API int ilm_dot_grid_noalloc(int nx, int ny, double h, int scaling, int kind
                                  const void* b, double* result, ilm_stream_t stream);
 
 /* ---- Schur complements (src/matrix_operators.jl:9-244) ------------------ */
-/* Dense N x N (column-major, FP64, device) Schur complement, built on the
- * GPU directly from lattice-Green's-function point-point sums instead of the
- * reference's N operator applications.  A_dev must hold N*N doubles.        */
+/* Dense n x n (column-major, FP64, device) Schur complement; n = N for
+ * ScalarData kinds, 2N for the VectorData of vector caches.  Scalar caches,
+ * kinds 0-3: built directly from lattice-Green's-function point-point sums
+ * instead of the reference's N operator applications.  Vector caches and
+ * kinds 4-7: the reference's column-by-column build, on the device (one unit
+ * vector per column through the operator chain).  create_GLinvD_cross
+ * raises in the reference (surface_divergence_cross! refers to an undefined
+ * variable, src/surface_operators.jl:680); kind 7 builds the operator its
+ * documentation states.  A_dev must hold n*n doubles.                      */
 ILM_API int ilm_schur_build(ilm_cache_t c, int which, double scale, double* A_dev, ilm_stream_t stream);
 
 /* ---- problem solves (test/literate/problems.jl:259-298, neumann.jl:101-142) */

@@ -1111,3 +1111,44 @@ def vecfield_helmholtz(c: SurfaceCache, curlv, divv, dv, vp=None):
     if vp is not None:
         v = (v[0] + vp[0], v[1] + vp[1])
     return v
+
+
+# ---------------------------------------------------------------------------
+# Schur complements of vector caches and the remaining kinds, by columns
+# (src/matrix_operators.jl:9-244), as the reference builds them
+# ---------------------------------------------------------------------------
+
+def _columns(n, apply, scale):
+    A = np.empty((n, n))
+    e = np.zeros(n)
+    for col in range(n):
+        e[:] = 0.0
+        e[col] = 1.0
+        A[:, col] = scale * apply(e)
+    return A
+
+
+def create_RTLinvR_vector(c: SurfaceCache, scale=1.0):
+    return _columns(2 * c.N, lambda e: interpolate_vector(c, c.inverse_laplacian(regularize_vector(c, e))), -scale)
+
+
+def create_CLinvCT_vector(c: SurfaceCache, scale=1.0):
+    return _columns(2 * c.N, lambda e: surface_curl_vector(c, c.inverse_laplacian(surface_curl_T_vector(c, e))),
+                    -scale)
+
+
+def create_nRTRn_vector(c: SurfaceCache, scale=1.0):
+    return _columns(2 * c.N, lambda e: normal_interpolate_tensor(c, regularize_normal_tensor(c, e)), scale)
+
+
+def create_GLinvD_symm(c: SurfaceCache, scale=1.0):
+    """create_GLinvD_symm (src/matrix_operators.jl:165-185), vector caches."""
+    return _columns(2 * c.N, lambda e: surface_grad_symm(c, c.inverse_laplacian(surface_divergence_symm(c, e))),
+                    -scale)
+
+
+def create_GLinvD_cross(c: SurfaceCache, scale=1.0):
+    """-G^x_s L^-1 D^x_s (src/matrix_operators.jl:195-215, the operator its
+    documentation states; the reference's own call raises)."""
+    return _columns(c.N, lambda e: surface_grad_cross(c, c.inverse_laplacian(surface_divergence_cross(c, e))),
+                    -scale)

@@ -90,3 +90,33 @@ def test_neumann_streamfunction_circle(cuda):
     sys_ = il.construct_system(prob)
     f2, df2, s2, ds2 = il.solve(prob, sys_, tol=1e-11, maxiter=20000)
     assert rel(s2.numpy_components(), s_ref) < 1e-6
+
+
+def test_schur_builds_vector_cache_and_remaining_kinds(cuda):
+    """Every Schur kind of src/matrix_operators.jl:9-244 on the device against
+    the oracle's column-by-column builds: the vector-cache kinds (VectorData
+    2N x 2N, and the ScalarData CLinvCT_scalar) and GLinvD_cross on a scalar
+    cache."""
+    import torch
+    import immersedlayers as il
+    from immersedlayers import bodies as B
+    h = 0.04
+    og = O.Grid.physical((-1.0, 1.0), (-1.0, 1.0), h)
+    b = B.circle(0.4, ds=1.4 * h)
+    g = il.PhysicalGrid((-1.0, 1.0), (-1.0, 1.0), h)
+    vc = il.SurfaceVectorCache(b, g)
+    ovc = oracle_cache(og, b, "vector")
+    cases = [(il.create_RTLinvR, O.create_RTLinvR_vector), (il.create_CLinvCT, O.create_CLinvCT_vector),
+             (il.create_GLinvD, O.create_GLinvD_vector), (il.create_nRTRn, O.create_nRTRn_vector),
+             (il.create_CLinvCT_scalar, O.create_CLinvCT_scalar_vector), (il.create_CL2invCT, O.create_CL2invCT_vector),
+             (il.create_GLinvD_symm, O.create_GLinvD_symm)]
+    for fn, ref in cases:
+        A = fn(vc, scale=0.5).cpu().numpy()
+        R = ref(ovc, scale=0.5)
+        assert A.shape == R.shape, fn.__name__
+        assert rel(A, R) < 1e-10, (fn.__name__, rel(A, R))
+    sc = il.SurfaceScalarCache(b, g)
+    A = il.create_GLinvD_cross(sc).cpu().numpy()
+    assert rel(A, O.create_GLinvD_cross(oracle_cache(og, b))) < 1e-10
+    with pytest.raises(il._lib.ILMError):
+        il.create_CL2invCT(sc)
