@@ -108,10 +108,10 @@ static int tensor_scatter(ilm_cache_s* c, const void* v, int symm, void* out, cu
   void* o1 = comp_ptr(g, ILM_EDGEGRAD_PRIMAL, c->dtype, out, 1);
   void* o2 = comp_ptr(g, ILM_EDGEGRAD_PRIMAL, c->dtype, out, 2);
   void* o3 = comp_ptr(g, ILM_EDGEGRAD_PRIMAL, c->dtype, out, 3);
-  if (!symm) {
+  if (!symm) {  // dudx = n_x v_x, dudy = n_y v_x, dvdx = n_x v_y, dvdy = n_y v_y
     ILM_TRY(launch_scatter(c, PC_P, vx, CF_NX, nullptr, CF_ZERO, o0, st));
-    ILM_TRY(launch_scatter(c, PC_D, vy, CF_NX, nullptr, CF_ZERO, o1, st));
-    ILM_TRY(launch_scatter(c, PC_D, vx, CF_NY, nullptr, CF_ZERO, o2, st));
+    ILM_TRY(launch_scatter(c, PC_D, vx, CF_NY, nullptr, CF_ZERO, o1, st));
+    ILM_TRY(launch_scatter(c, PC_D, vy, CF_NX, nullptr, CF_ZERO, o2, st));
     ILM_TRY(launch_scatter(c, PC_P, vy, CF_NY, nullptr, CF_ZERO, o3, st));
   } else {
     ILM_TRY(launch_scatter(c, PC_P, vx, CF_NX, vy, CF_MNY, o0, st));
@@ -142,9 +142,9 @@ static int tensor_gather(ilm_cache_s* c, const void* A, int symm, void* out, dou
   const void* dvdy = comp_ptr(g, ILM_EDGEGRAD_PRIMAL, c->dtype, A, 3);
   void* ox = out;
   void* oy = ptr_off(out, c->npts, c->dtype);
-  if (!symm) {
-    GatherTerm tx[2] = {{PC_P, dudx, CF_NX}, {PC_D, dvdx, CF_NY}};
-    GatherTerm ty[2] = {{PC_D, dudy, CF_NX}, {PC_P, dvdy, CF_NY}};
+  if (!symm) {  // (n_x dudx + n_y dudy, n_x dvdx + n_y dvdy)
+    GatherTerm tx[2] = {{PC_P, dudx, CF_NX}, {PC_D, dudy, CF_NY}};
+    GatherTerm ty[2] = {{PC_D, dvdx, CF_NX}, {PC_P, dvdy, CF_NY}};
     ILM_TRY(launch_gather(c, tx, 2, ox, false, scale, st));
     return launch_gather(c, ty, 2, oy, false, scale, st);
   }
@@ -450,7 +450,8 @@ int ilm_regularize_normal_dot(ilm_cache_t c, int out_kind, const void* in, void*
     const void* t12 = ptr_off(in, N, c->dtype);
     const void* t21 = ptr_off(in, 2 * (size_t)N, c->dtype);
     const void* t22 = ptr_off(in, 3 * (size_t)N, c->dtype);
-    return scatter_edges(c, t11, CF_NX, t21, CF_NY, t12, CF_NX, t22, CF_NY, out, st);
+    // u = n_x dudx + n_y dudy, v = n_x dvdx + n_y dvdy
+    return scatter_edges(c, t11, CF_NX, t12, CF_NY, t21, CF_NX, t22, CF_NY, out, st);
   }
   set_error("regularize_normal_dot: unsupported output kind %d", out_kind);
   return ILM_ERR_INVALID_ARG;
@@ -495,7 +496,8 @@ int ilm_normal_dot_interpolate(ilm_cache_t c, int in_kind, const void* q, void* 
   if (in_kind == ILM_EDGES_PRIMAL) {
     const void* u = q;
     const void* v = comp_ptr(&c->grid, ILM_EDGES_PRIMAL, c->dtype, q, 1);
-    GatherTerm t[4] = {{PC_U, u, CF_NX}, {PC_V, v, CF_NX}, {PC_U, u, CF_NY}, {PC_V, v, CF_NY}};
+    // (dudx, dudy, dvdx, dvdy) = (n_x s_x, n_y s_x, n_x s_y, n_y s_y), s = E v
+    GatherTerm t[4] = {{PC_U, u, CF_NX}, {PC_U, u, CF_NY}, {PC_V, v, CF_NX}, {PC_V, v, CF_NY}};
     for (int i = 0; i < 4; ++i) ILM_TRY(launch_gather(c, &t[i], 1, ptr_off(out, (size_t)i * N, c->dtype), false, 1.0, st));
     return ILM_OK;
   }
@@ -717,10 +719,46 @@ int ilm_inverse_laplacian(ilm_cache_t c, int kind, const void* in, void* out, il
   return inverse_laplacian_kind(c, kind, in, out, as_stream(stream));
 }
 
+// Vector caches (src/surface_operators.jl:872-877, :912-923): the mask on
+// Edges{Primal} from the all-ones VectorData, H = -L^{-1} D_s 1, and for the
+// other grid types its u component interpolated (Nodes{Dual}: mean over y;
+// Nodes{Primal}: mean over x; EdgeGradient per component).
+static int mask_vector(ilm_cache_s* c, int kind, int complementary, void* out, cudaStream_t st) {
+  ILM_REQUIRE(kind == ILM_NODES_PRIMAL || kind == ILM_NODES_DUAL || kind == ILM_EDGES_PRIMAL ||
+                  kind == ILM_EDGEGRAD_PRIMAL,
+              "mask: unsupported grid kind %d", kind);
+  const size_t ne = gridkind_numel(&c->grid, ILM_EDGES_PRIMAL);
+  void* m;
+  ILM_TRY(gscr(c, 1, &m));
+  if (c->npts == 0) {
+    ILM_TRY(st_fill(ne, c->dtype, 1.0, m, st));
+  } else {
+    void* ones;
+    ILM_TRY(pscr(c, 0, &ones));
+    ILM_TRY(st_fill(2 * (size_t)c->npts, c->dtype, 1.0, ones, st));
+    ILM_TRY(ilm_surface_divergence(c, ones, m, (void*)st));
+    ILM_TRY(inverse_laplacian_kind(c, ILM_EDGES_PRIMAL, m, m, st));
+    ILM_TRY(st_affine(ne, c->dtype, -1.0, m, 0.0, m, st));
+  }
+  if (complementary) ILM_TRY(st_affine(ne, c->dtype, -1.0, m, 1.0, m, st));
+  switch (kind) {
+    case ILM_EDGES_PRIMAL: return st_convert(ne, c->dtype, m, c->dtype, out, st);
+    case ILM_NODES_DUAL: return st_xedge_to_dual(&c->grid, c->dtype, m, out, st);
+    case ILM_NODES_PRIMAL: return st_xedge_to_primal(&c->grid, c->dtype, m, out, st);
+    default:  // EdgeGradient: dudx, dvdy on Nodes{Primal}, dudy, dvdx on Nodes{Dual}
+      for (int k = 0; k < 4; ++k) {
+        void* o = comp_ptr(&c->grid, ILM_EDGEGRAD_PRIMAL, c->dtype, out, k);
+        if (k == 0 || k == 3) ILM_TRY(st_xedge_to_primal(&c->grid, c->dtype, m, o, st));
+        else ILM_TRY(st_xedge_to_dual(&c->grid, c->dtype, m, o, st));
+      }
+      return ILM_OK;
+  }
+}
+
 int ilm_mask(ilm_cache_t c, int kind, int complementary, void* out, ilm_stream_t stream) {
   CHECK_CACHE(c);
-  ILM_REQUIRE(c->kind == ILM_CACHE_SCALAR, "mask: scalar caches only");
   ILM_REQUIRE(c->scaling == ILM_GRID_SCALING, "mask: GridScaling caches only (src/surface_operators.jl:737)");
+  if (c->kind == ILM_CACHE_VECTOR) return mask_vector(c, kind, complementary, out, as_stream(stream));
   ILM_REQUIRE(kind == ILM_NODES_PRIMAL || kind == ILM_NODES_DUAL || kind == ILM_EDGES_PRIMAL,
               "mask: unsupported grid kind %d", kind);
   cudaStream_t st = as_stream(stream);

@@ -373,6 +373,9 @@ int st_fill(size_t n, int dtype, double v, void* out, cudaStream_t st);
 int st_affine(size_t n, int dtype, double a, const void* x, double b, void* out, cudaStream_t st);
 int st_convert(size_t n, int dtype_in, const void* in, int dtype_out, void* out, cudaStream_t st);
 int st_primal_to_dual(const ilm_grid_s* g, int dtype, const void* p, void* out, cudaStream_t st);
+// Edges{Primal}.u interpolated to Nodes{Dual} / Nodes{Primal} (vector-cache masks)
+int st_xedge_to_dual(const ilm_grid_s* g, int dtype, const void* u, void* out, cudaStream_t st);
+int st_xedge_to_primal(const ilm_grid_s* g, int dtype, const void* u, void* out, cudaStream_t st);
 int st_primal_to_edges(const ilm_grid_s* g, int dtype, const void* p, void* out, cudaStream_t st);
 int st_mul(size_t n, int dtype, const void* a, void* inout, cudaStream_t st);
 // convective derivatives and w x v (ilm_convective.cu); field_kind: the kind of q and out

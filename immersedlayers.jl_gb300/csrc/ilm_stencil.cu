@@ -158,6 +158,22 @@ __global__ void k_laplacian(int n1, int n2, const T* __restrict__ a, T* __restri
 }
 
 // Nodes{Primal} -> Nodes{Dual} (4-point average on interior dual nodes)
+// Edges{Primal}.u (NX x NY-1) -> Nodes{Dual}: mean over y onto the
+// non-ghost dual rows (ghost rows 0), the vector-cache mask interpolation
+template <typename T>
+__global__ void k_xe2d(int NX, int NY, const T* __restrict__ u, T* __restrict__ o) {
+  const int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+  if (i >= NX || j >= NY) return;
+  o[(size_t)j * NX + i] = (j >= 1 && j <= NY - 2) ? (T)0.5 * (u[(size_t)(j - 1) * NX + i] + u[(size_t)j * NX + i]) : (T)0;
+}
+// Edges{Primal}.u -> Nodes{Primal} ((NX-1) x (NY-1)): mean over x
+template <typename T>
+__global__ void k_xe2p(int NX, int NY, const T* __restrict__ u, T* __restrict__ o) {
+  const int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
+  if (i >= NX - 1 || j >= NY - 1) return;
+  o[(size_t)j * (NX - 1) + i] = (T)0.5 * (u[(size_t)j * NX + i] + u[(size_t)j * NX + i + 1]);
+}
+
 template <typename T>
 __global__ void k_p2d(int NX, int NY, const T* __restrict__ p, T* __restrict__ o) {
   const int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
@@ -396,6 +412,24 @@ int st_primal_to_dual(const ilm_grid_s* g, int dtype, const void* p, void* out, 
   DISPATCH(dtype, {
     k_p2d<T><<<grid2(g->nx, g->ny), dim3(BX, BY), 0, st>>>(g->nx, g->ny, static_cast<const T*>(p),
                                                            static_cast<T*>(out));
+  });
+  ILM_CHECK_LAUNCH();
+  return ILM_OK;
+}
+
+int st_xedge_to_dual(const ilm_grid_s* g, int dtype, const void* u, void* out, cudaStream_t st) {
+  DISPATCH(dtype, {
+    k_xe2d<T><<<grid2(g->nx, g->ny), dim3(BX, BY), 0, st>>>(g->nx, g->ny, static_cast<const T*>(u),
+                                                            static_cast<T*>(out));
+  });
+  ILM_CHECK_LAUNCH();
+  return ILM_OK;
+}
+
+int st_xedge_to_primal(const ilm_grid_s* g, int dtype, const void* u, void* out, cudaStream_t st) {
+  DISPATCH(dtype, {
+    k_xe2p<T><<<grid2(g->nx, g->ny), dim3(BX, BY), 0, st>>>(g->nx, g->ny, static_cast<const T*>(u),
+                                                            static_cast<T*>(out));
   });
   ILM_CHECK_LAUNCH();
   return ILM_OK;

@@ -229,9 +229,12 @@ ILM_API int ilm_laplacian(ilm_cache_t c, int kind, const void* in, void* out, il
 /* inverse_laplacian!(sol, rhs) (:153-179): unbounded-domain L^-1 via the
  * lattice Green's function (FFT convolution).  in may equal out.           */
 ILM_API int ilm_inverse_laplacian(ilm_cache_t c, int kind, const void* in, void* out, ilm_stream_t stream);
-/* mask(cache) / complementary_mask(cache) (:737-760, :856-871) evaluated on
- * grid data of `kind` (the basic type, or Nodes{Dual} / Edges{Primal} via the
- * grid interpolation of mask! (:880-923)); scalar caches.                    */
+/* mask(cache) / complementary_mask(cache) (:737-760, :856-877) evaluated on
+ * grid data of `kind`, GridScaling caches.  Scalar caches: H on
+ * Nodes{Primal}, Nodes{Dual} / Edges{Primal} by the grid interpolation of
+ * mask! (:880-905).  Vector caches: H on Edges{Primal} from the all-ones
+ * VectorData, Nodes{Dual} / Nodes{Primal} / EdgeGradient{Primal} from its u
+ * component (:907-923).                                                   */
 ILM_API int ilm_mask(ilm_cache_t c, int kind, int complementary, void* out, ilm_stream_t stream);
 
 /* ---- inner products (src/tools.jl:101-236, src/cache.jl:815-909) -------- */

@@ -560,17 +560,35 @@ def normal_dot_interpolate(c: SurfaceCache, p):
 
 
 def _tensor_nv(c, v):
-    """pointwise_tensorproduct!(n, v): (n_x v_x, n_x v_y, n_y v_x, n_y v_y)."""
+    """pointwise_tensorproduct!(n, v) in TensorData slots (dudx, dudy, dvdx,
+    dvdy) = (n_x v_x, n_y v_x, n_x v_y, n_y v_y): the slot d(c)/d(k) holds n_k
+    times component c, so that the tensor divergence of n o 1 (u: d/dx dudx +
+    d/dy dudy) is the scalar double layer on each edge component -- the
+    vector-cache mask of src/surface_operators.jl:872-877 then integrates to
+    the enclosed area, as test/surface_ops.jl:221-231 requires."""
     N = c.N
     vx, vy = v[:N], v[N:]
-    return np.concatenate([c.nx * vx, c.nx * vy, c.ny * vx, c.ny * vy])
+    return np.concatenate([c.nx * vx, c.ny * vx, c.nx * vy, c.ny * vy])
 
 
 def _tensor_dot_n(c, t):
-    """pointwise_dot!(n, tau) -> (n_x t11 + n_y t21, n_x t12 + n_y t22)."""
+    """pointwise_dot!(n, tau), the adjoint of _tensor_nv:
+    (n_x dudx + n_y dudy, n_x dvdx + n_y dvdy)."""
     N = c.N
     t11, t12, t21, t22 = t[:N], t[N:2 * N], t[2 * N:3 * N], t[3 * N:]
-    return np.concatenate([c.nx * t11 + c.ny * t21, c.nx * t12 + c.ny * t22])
+    return np.concatenate([c.nx * t11 + c.ny * t12, c.nx * t21 + c.ny * t22])
+
+
+def regularize_normal_dot_tensor(c: SurfaceCache, taus):
+    """regularize_normal_dot!(v::Edges{Primal}, taus::TensorData)
+    (src/surface_operators.jl:205-215): R_f (n . tau)."""
+    return regularize_vector(c, _tensor_dot_n(c, taus))
+
+
+def normal_dot_interpolate_tensor(c: SurfaceCache, q):
+    """normal_dot_interpolate!(taus::TensorData, v::Edges{Primal})
+    (src/surface_operators.jl:332-343): n o R_f^T v."""
+    return _tensor_nv(c, interpolate_vector(c, q))
 
 
 def regularize_normal_tensor(c: SurfaceCache, v):
@@ -1152,3 +1170,19 @@ def create_GLinvD_cross(c: SurfaceCache, scale=1.0):
     documentation states; the reference's own call raises)."""
     return _columns(c.N, lambda e: surface_grad_cross(c, c.inverse_laplacian(surface_divergence_cross(c, e))),
                     -scale)
+
+
+def mask_vector(c: SurfaceCache, kind="edges_primal"):
+    """Vector-cache mask (src/surface_operators.jl:872-877, :907-923): H on
+    Edges{Primal} = -L^{-1} D_s 1 with the all-ones VectorData, other grid
+    types from its u component (Nodes{Dual}: mean over y onto the non-ghost
+    rows; Nodes{Primal}: mean over x)."""
+    H = tuple(-x for x in c.inverse_laplacian(surface_divergence_vector(c, np.ones(2 * c.N))))
+    if kind == "edges_primal":
+        return H
+    nd, npr = _avg_p2d(H[0], 1), _avg_d2p(H[0], 0)
+    if kind == "nodes_dual":
+        return nd
+    if kind == "nodes_primal":
+        return npr
+    return (npr, nd, nd, npr)

@@ -13,6 +13,12 @@ def rel(a, b):
     return np.abs(np.asarray(a) - np.asarray(b)).max() / np.abs(np.asarray(b)).max()
 
 
+def relt(a, b):
+    if isinstance(b, tuple):
+        return max(rel(x, y) for x, y in zip(a, b))
+    return rel(a, b)
+
+
 @pytest.mark.parametrize("dtype", ["f64", "f32"])
 def test_dirichlet_config1(cuda, dtype):
     import torch
@@ -120,3 +126,57 @@ def test_schur_builds_vector_cache_and_remaining_kinds(cuda):
     assert rel(A, O.create_GLinvD_cross(oracle_cache(og, b))) < 1e-10
     with pytest.raises(il._lib.ILMError):
         il.create_CL2invCT(sc)
+
+
+def test_vector_cache_masks(cuda):
+    """Masks of a vector cache (src/surface_operators.jl:872-877, :907-923)
+    against the oracle on every grid type, and the enclosed area."""
+    import torch
+    import immersedlayers as il
+    from immersedlayers import bodies as B
+    h = 0.04
+    og = O.Grid.physical((-2.0, 2.0), (-2.0, 2.0), h)
+    b = B.circle(1.0, ds=1.4 * h)
+    g = il.PhysicalGrid((-2.0, 2.0), (-2.0, 2.0), h)
+    vc = il.SurfaceVectorCache(b, g)
+    ovc = oracle_cache(og, b, "vector")
+    for kind, okind in [(il.EdgesPrimal, "edges_primal"), (il.NodesDual, "nodes_dual"),
+                        (il.NodesPrimal, "nodes_primal"), (il.EdgeGradientPrimal, "edgegrad")]:
+        m = il.mask(vc, kind).numpy_components()
+        ref = O.mask_vector(ovc, okind)
+        assert relt(m, ref) < 1e-10, kind.__name__
+        cm = il.complementary_mask(vc, kind).numpy_components()
+        if kind is il.EdgesPrimal:
+            assert relt(cm, tuple(1.0 - x for x in ref)) < 1e-10
+    mu = il.mask(vc).numpy_components()[0]
+    area = mu.sum() * h * h
+    assert abs(area - np.pi) < 1e-2 * np.pi, area
+
+
+def test_tensor_normal_dot_transfers(cuda):
+    """regularize_normal_dot!(v::Edges, taus::TensorData) and
+    normal_dot_interpolate!(taus::TensorData, v::Edges)
+    (src/surface_operators.jl:205-215, :332-343) on a vector cache against
+    the oracle (TensorData slots dudx, dudy, dvdx, dvdy = n_x s_x, n_y s_x,
+    n_x s_y, n_y s_y)."""
+    import torch
+    import immersedlayers as il
+    from immersedlayers import bodies as B
+    h = 0.04
+    og = O.Grid.physical((-2.0, 2.0), (-2.0, 2.0), h)
+    b = B.circle(1.0, ds=1.4 * h)
+    g = il.PhysicalGrid((-2.0, 2.0), (-2.0, 2.0), h)
+    vc = il.SurfaceVectorCache(b, g)
+    ovc = oracle_cache(og, b, "vector")
+    N = len(b)
+    rng = np.random.default_rng(21)
+    t_h = rng.standard_normal(4 * N)
+    tau = il.TensorData(torch.tensor(t_h, device="cuda"))
+    q = il.regularize_normal_dot_(il.EdgesPrimal.zeros(g), tau, vc)
+    assert relt(q.numpy_components(), O.regularize_normal_dot_tensor(ovc, t_h)) < 1e-12
+    e = il.EdgesPrimal.zeros(g)
+    e_h = (rng.standard_normal(e.numpy_components()[0].shape), rng.standard_normal(e.numpy_components()[1].shape))
+    e.set_numpy(e_h)
+    out = il.TensorData.zeros(N)
+    il.normal_dot_interpolate_(out, e, vc)
+    assert rel(out.numpy(), O.normal_dot_interpolate_tensor(ovc, e_h)) < 1e-12

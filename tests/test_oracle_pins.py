@@ -217,3 +217,17 @@ def test_oracle_convective_derivatives_exact_on_linear_fields():
     ou, ov = O.w_cross_v(wu, unif)
     np.testing.assert_allclose(ou[1:-1, :], -1.5 * b, atol=1e-13)
     np.testing.assert_allclose(ov[:, 1:-1], 1.5 * a, atol=1e-13)
+
+
+def test_vector_cache_masks_area():
+    """test/surface_ops.jl:214-231: the masks of a vector cache on
+    Nodes{Primal}, Nodes{Dual}, Edges{Primal} and EdgeGradient{Primal}
+    integrate to pi (1e-3) for the unit circle.  This pins the TensorData
+    layout of the normal products (dudy = n_y v_x): the transposed layout
+    gives pi/2 on the edges."""
+    g, b = surface_ops_case()
+    c = oracle_cache(g, b, "vector")
+    for kind in ("nodes_primal", "nodes_dual", "edges_primal", "edgegrad"):
+        H = O.mask_vector(c, kind)
+        for comp in (H if isinstance(H, tuple) else (H,)):
+            assert abs(comp.sum() * g.h * g.h - math.pi) < 1e-3, kind
