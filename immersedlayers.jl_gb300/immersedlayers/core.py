@@ -647,15 +647,27 @@ def complementary_mask(cache, kind=None):
     return out
 
 
-def mask_(w: GridData, cache):
-    """mask!(w, cache): multiply w by the mask interpolated to w's grid type."""
+def _shape_cache(w: GridData, surface, grid):
+    """The temporary cache of mask!(w, surface, grid) (src/surface_operators.jl:
+    804-806): scalar for Nodes, vector for Edges and EdgeGradient."""
+    vec = isinstance(w, (EdgesPrimal, EdgeGradientPrimal))
+    return (SurfaceVectorCache if vec else SurfaceScalarCache)(surface, grid, dtype=w.data.dtype)
+
+
+def mask_(w: GridData, cache, grid=None):
+    """mask!(w, cache): multiply w by the mask interpolated to w's grid type;
+    mask!(w, surface, grid): the same for the surface(s) of a body."""
+    if grid is not None:
+        cache = _shape_cache(w, cache, grid)
     m = type(w).zeros(cache.g, cache.dtype)
     L.call("ilm_mask", cache._h, w.kind, 0, _ptr(m.data), None)
     w.data.mul_(m.data)
     return w
 
 
-def complementary_mask_(w: GridData, cache):
+def complementary_mask_(w: GridData, cache, grid=None):
+    if grid is not None:
+        cache = _shape_cache(w, cache, grid)
     m = type(w).zeros(cache.g, cache.dtype)
     L.call("ilm_mask", cache._h, w.kind, 1, _ptr(m.data), None)
     w.data.mul_(m.data)

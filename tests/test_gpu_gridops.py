@@ -174,3 +174,26 @@ def test_uniform_potentials(S):
     tol = 1e-10 if S["dt"].itemsize == 8 else 1e-4
     for v in (v1, v2):
         assert np.abs(v[0][1:-1, 1:-1] - 0.8).max() < tol and np.abs(v[1][1:-1, 1:-1] + 0.6).max() < tol
+
+
+def test_helmholtz_known_answer(S):
+    """test/surface_ops.jl:312-341 on the device: the field from
+    vecfield_helmholtz_ has masked curl w and masked divergence d at the
+    interior nodes (1e-8 in FP64; 1e-2 in FP32, where the second differences
+    of the potentials cancel most of their digits)."""
+    import torch
+    il = S["il"]
+    vc = S["vc"]
+    N = len(S["b"])
+    w, wh = _rand(S, il.NodesDual, 31)
+    d, dh = _rand(S, il.NodesPrimal, 32)
+    dv = il.VectorData(torch.tensor(np.random.default_rng(33).standard_normal(2 * N), dtype=S["dt"], device="cuda"))
+    v = il.vecfield_helmholtz_(il.EdgesPrimal.zeros(S["g"], S["dt"]), w, d, dv, (0.0, 0.0), vc, il.VectorFieldCache(vc))
+    vfc = il.VectorFieldCache(vc)
+    w2 = il.curl_(il.zeros_gridcurl(vc), v, vc)
+    mw = il.masked_curlv_from_curlv_masked_(il.zeros_gridcurl(vc), w2, dv, vc, vfc.wcache).numpy_components()
+    d2 = il.divergence_(il.NodesPrimal.zeros(S["g"], S["dt"]), v, vc)
+    md = il.masked_divv_from_divv_masked_(il.NodesPrimal.zeros(S["g"], S["dt"]), d2, dv, vc, vfc.dcache).numpy_components()
+    tol = 1e-8 if S["dt"] == torch.float64 else 1e-2
+    assert np.abs(mw[1:-1, 1:-1] - wh[1:-1, 1:-1]).max() < tol
+    assert np.abs(md[1:-1, 1:-1] - dh[1:-1, 1:-1]).max() < tol

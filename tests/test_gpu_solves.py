@@ -180,3 +180,20 @@ def test_tensor_normal_dot_transfers(cuda):
     out = il.TensorData.zeros(N)
     il.normal_dot_interpolate_(out, e, vc)
     assert rel(out.numpy(), O.normal_dot_interpolate_tensor(ovc, e_h)) < 1e-12
+
+
+def test_shape_masks_area(cuda):
+    """mask!(w, surface, grid) (test/surface_ops.jl:235-252): Rectangle(0.5,
+    0.25) on Nodes{Primal}, Nodes{Dual}, Edges{Primal} and EdgeGradient,
+    each component integrating to 0.5 within 1e-3."""
+    import immersedlayers as il
+    from immersedlayers import bodies as B
+    h = 0.04
+    g = il.PhysicalGrid((-2.0, 2.0), (-2.0, 2.0), h)
+    r = B.rectangle(0.5, 0.25, ds=1.4 * h)
+    for kind in (il.NodesPrimal, il.NodesDual, il.EdgesPrimal, il.EdgeGradientPrimal):
+        w = kind.zeros(g).fill_(1.0)
+        il.mask_(w, r, g)
+        comps = w.numpy_components()
+        for comp in (comps if isinstance(comps, tuple) else (comps,)):
+            assert abs(comp.sum() * h * h - 0.5) < 1e-3, kind.__name__

@@ -231,3 +231,37 @@ def test_vector_cache_masks_area():
         H = O.mask_vector(c, kind)
         for comp in (H if isinstance(H, tuple) else (H,)):
             assert abs(comp.sum() * g.h * g.h - math.pi) < 1e-3, kind
+
+
+def test_shape_masks_area():
+    """test/surface_ops.jl:235-252: masks of Rectangle(0.5, 0.25) (half
+    lengths) built from a scalar cache (Nodes) or a vector cache (Edges,
+    EdgeGradient) integrate to 0.5 within 1e-3."""
+    from immersedlayers import bodies as B
+    g, _ = surface_ops_case()
+    r = B.rectangle(0.5, 0.25, ds=1.4 * g.h)
+    m = O.mask(oracle_cache(g, r))
+    assert abs(m.sum() * g.h ** 2 - 0.5) < 1e-3
+    assert abs(O.grid_interpolate_primal_to_dual(m, g).sum() * g.h ** 2 - 0.5) < 1e-3
+    vc = oracle_cache(g, r, "vector")
+    for kind in ("edges_primal", "edgegrad"):
+        for comp in O.mask_vector(vc, kind):
+            assert abs(comp.sum() * g.h ** 2 - 0.5) < 1e-3, kind
+
+
+def test_helmholtz_known_answer():
+    """test/surface_ops.jl:312-341: for random masked curl w, masked
+    divergence d and surface jump dv, the field v = vecfield_helmholtz(w, d,
+    dv) has masked curl w and masked divergence d at the interior nodes
+    (1e-8)."""
+    g, b = surface_ops_case()
+    c = oracle_cache(g, b, "vector")
+    rng = np.random.default_rng(0)
+    w = rng.standard_normal(g.shape(O.NODES_DUAL))
+    d = rng.standard_normal(g.shape(O.NODES_PRIMAL))
+    dv = rng.standard_normal(2 * c.N)
+    v = O.vecfield_helmholtz(c, w, d, dv, (0.0, 0.0))
+    mw = O.curl_edges(v, g) * c.dscale() - O.regularize_normal_cross_vector(c, dv)
+    md = O.divergence_edges(v) * c.dscale() - O.regularize_normal_dot(c, dv)
+    assert np.abs(mw[1:-1, 1:-1] - w[1:-1, 1:-1]).max() < 1e-8
+    assert np.abs(md[1:-1, 1:-1] - d[1:-1, 1:-1]).max() < 1e-8
