@@ -52,6 +52,9 @@ def parse():
     ap.add_argument("--learned-nprob", type=int, default=256, help="learned-preconditioner leg (0: skip)")
     ap.add_argument("--stokes", type=int, default=1, help="Stokes leg (0: skip)")
     ap.add_argument("--moving", type=int, default=1, help="moving-body re-binning leg (0: skip)")
+    ap.add_argument("--profile-stencils", type=int, default=0,
+                    help="run the 4096^2 FP32 grid stencils (divergence, gradient, fused convective derivatives, "
+                         "w x v) this many times after one warm-up pass, nothing else (for ncu captures)")
     ap.add_argument("--profile-solves", type=int, default=0,
                     help="profiling driver: set up the batch with the default solver, run this many solves on a "
                          "created stream and exit (no timing, no JSON line)")
@@ -637,6 +640,35 @@ def _cpu_baseline(args, specs):
                       f"problem scaled by npts/k, solve timed in full; sample wall {est['sample_wall']:.1f}s"}
 
 
+def run_profile_stencils(args):
+    """The grid-stencil leg's kernels on 4096^2 FP32 fields, one warm-up pass
+    and `args.profile_stencils` timed-order passes: divergence, gradient,
+    v . grad p, u . grad u, w x v (a fixed launch sequence for ncu)."""
+    import torch
+    import __graft_entry__ as ge
+    ge.build()
+    import immersedlayers as il
+    n = 4096
+    g = il.PhysicalGrid(h=4.0 / n, nx=n)
+    c = il.SurfaceVectorCache(None, g, dtype=torch.float32)
+    v = il.EdgesPrimal.zeros(g, torch.float32)
+    v.data.normal_()
+    p = il.NodesPrimal.zeros(g, torch.float32)
+    p.data.normal_()
+    w = il.NodesDual.zeros(g, torch.float32)
+    w.data.normal_()
+    o_p, o_e = p.similar(), v.similar()
+    sc = il.SurfaceScalarCache(None, g, dtype=torch.float32)
+    for _ in range(1 + args.profile_stencils):
+        il.divergence_(o_p, v, sc)
+        il.grad_(o_e, p, sc)
+        il.convective_derivative_(o_p, v, p, c)
+        il.convective_derivative_(o_e, v, c)
+        il.w_cross_v_(o_e, w, v, c)
+    torch.cuda.synchronize()
+    print(f"stencil passes {1 + args.profile_stencils} on {n}^2", file=sys.stderr)
+
+
 def run_profile_solves(args):
     """Batch and default-solver set-up, then `args.profile_solves` solves (a
     fixed launch sequence for ncu captures)."""
@@ -666,6 +698,8 @@ def main():
     rank, world, dist = dist_init()
     if args.profile_solves > 0:
         run_profile_solves(args)
+    elif args.profile_stencils > 0:
+        run_profile_stencils(args)
     elif args.impl == "reference":
         run_reference(args, rank, world)
     else:

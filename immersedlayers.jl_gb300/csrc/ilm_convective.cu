@@ -17,7 +17,9 @@
 // dual positions 1..n-2 (the ghost layers stay zero), the same boundary rule
 // as grad!/curl! onto dual positions.  Layout: x fastest; Edges{Primal} =
 // [u (NX x NY-1); v (NX-1 x NY)]; Nodes{Primal} (NX-1)x(NY-1); Nodes{Dual}
-// NX x NY.
+// NX x NY.  Indices are 32-bit (grids below 2^31 values; checked at launch):
+// the kernels issue more instructions than they move bytes, and 64-bit index
+// arithmetic was a large part of them.
 #include "ilm_internal.cuh"
 
 namespace ilm {
@@ -29,7 +31,7 @@ constexpr int BX = 32, BY = 8, RY = 4;
 inline dim3 grid2(int n1, int n2) { return dim3((n1 + BX - 1) / BX, (n2 + BY * RY - 1) / (BY * RY)); }
 
 template <typename T>
-__device__ __forceinline__ T ld(const T* p, size_t k) {
+__device__ __forceinline__ T ld(const T* p, int k) {
   return __ldg(p + k);
 }
 
@@ -40,14 +42,14 @@ __device__ __forceinline__ void vdp_np_at(int i, int j, int NX, int NY, const T*
     const T* __restrict__ vv, const T* __restrict__ p, T* __restrict__ out, T sc) {
   const int m = NX - 1;
   if (i >= m || j >= NY - 1) return;
-  const size_t c = (size_t)j * m + i;
+  const int c = j * m + i;
   const T pc = ld(p, c);
   const T gxl = (i >= 1) ? pc - ld(p, c - 1) : (T)0;            // dual x = i
   const T gxr = (i + 1 <= NX - 2) ? ld(p, c + 1) - pc : (T)0;  // dual x = i+1
   const T gyd = (j >= 1) ? pc - ld(p, c - m) : (T)0;           // dual y = j
   const T gyu = (j + 1 <= NY - 2) ? ld(p, c + m) - pc : (T)0;  // dual y = j+1
-  const T tx = ld(vu, (size_t)j * NX + i) * gxl + ld(vu, (size_t)j * NX + i + 1) * gxr;
-  const T ty = ld(vv, (size_t)j * m + i) * gyd + ld(vv, (size_t)(j + 1) * m + i) * gyu;
+  const T tx = ld(vu, j * NX + i) * gxl + ld(vu, j * NX + i + 1) * gxr;
+  const T ty = ld(vv, j * m + i) * gyd + ld(vv, (j + 1) * m + i) * gyu;
   out[c] = (T)0.5 * (tx + ty) * sc;
 }
 
@@ -69,7 +71,7 @@ template <typename T>
 __device__ __forceinline__ void vdw_nd_at(int i, int j, int NX, int NY, const T* __restrict__ vu,
     const T* __restrict__ vv, const T* __restrict__ w, T* __restrict__ out, T sc) {
   if (i >= NX || j >= NY) return;
-  const size_t c = (size_t)j * NX + i;
+  const int c = j * NX + i;
   if (i < 1 || i > NX - 2 || j < 1 || j > NY - 2) {
     out[c] = (T)0;
     return;
@@ -78,14 +80,14 @@ __device__ __forceinline__ void vdw_nd_at(int i, int j, int NX, int NY, const T*
   const T wc = ld(w, c);
   // Edges{Dual}.u at (primal x k, dual y j), k = i-1, i: mean of vu over
   // dual x k, k+1 and primal y j-1, j
-  const size_t r0 = (size_t)(j - 1) * NX, r1 = (size_t)j * NX;
+  const int r0 = (j - 1) * NX, r1 = j * NX;
   const T a0 = ld(vu, r0 + i - 1), a1 = ld(vu, r0 + i), a2 = ld(vu, r0 + i + 1);
   const T b0 = ld(vu, r1 + i - 1), b1 = ld(vu, r1 + i), b2 = ld(vu, r1 + i + 1);
   const T udl = (T)0.25 * (a0 + a1 + b0 + b1), udr = (T)0.25 * (a1 + a2 + b1 + b2);
   const T tx = udl * (wc - ld(w, c - 1)) + udr * (ld(w, c + 1) - wc);
   // Edges{Dual}.v at (dual x i, primal y l), l = j-1, j: mean of vv over
   // primal x i-1, i and dual y l, l+1
-  const size_t s0 = (size_t)(j - 1) * m, s1 = (size_t)j * m, s2 = (size_t)(j + 1) * m;
+  const int s0 = (j - 1) * m, s1 = j * m, s2 = (j + 1) * m;
   const T e0 = ld(vv, s0 + i - 1) + ld(vv, s0 + i), e1 = ld(vv, s1 + i - 1) + ld(vv, s1 + i);
   const T e2 = ld(vv, s2 + i - 1) + ld(vv, s2 + i);
   const T vdd = (T)0.25 * (e0 + e1), vdu = (T)0.25 * (e1 + e2);
@@ -120,7 +122,7 @@ __device__ __forceinline__ void vdu_edges_at(int i, int j, int NX, int NY, const
   const int m = NX - 1;
   if (i >= NX || j >= NY) return;
   if (j <= NY - 2) {
-    const size_t c = (size_t)j * NX + i;
+    const int c = j * NX + i;
     T r = (T)0;
     if (i >= 1 && i <= NX - 2) {
       // x part: dudx slots at primal x i-1, i (row j)
@@ -130,11 +132,11 @@ __device__ __forceinline__ void vdu_edges_at(int i, int j, int NX, int NY, const
       // y part: dudy slots at dual (i, l), l = j, j+1, nonzero for 1 <= l <= NY-2
       T ty = (T)0;
       if (j >= 1) {
-        const T a = (T)0.5 * (ld(vv, (size_t)j * m + i - 1) + ld(vv, (size_t)j * m + i));
+        const T a = (T)0.5 * (ld(vv, j * m + i - 1) + ld(vv, j * m + i));
         ty += a * (u1 - ld(uu, c - NX));
       }
       if (j + 1 <= NY - 2) {
-        const T a = (T)0.5 * (ld(vv, (size_t)(j + 1) * m + i - 1) + ld(vv, (size_t)(j + 1) * m + i));
+        const T a = (T)0.5 * (ld(vv, (j + 1) * m + i - 1) + ld(vv, (j + 1) * m + i));
         ty += a * (ld(uu, c + NX) - u1);
       }
       r = (T)0.5 * (tx + ty) * sc;
@@ -142,7 +144,7 @@ __device__ __forceinline__ void vdu_edges_at(int i, int j, int NX, int NY, const
     ou[c] = r;
   }
   if (i <= NX - 2) {
-    const size_t c = (size_t)j * m + i;
+    const int c = j * m + i;
     T r = (T)0;
     if (j >= 1 && j <= NY - 2) {
       // y part: dvdy slots at primal y j-1, j (column i)
@@ -152,11 +154,11 @@ __device__ __forceinline__ void vdu_edges_at(int i, int j, int NX, int NY, const
       // x part: dvdx slots at dual (k, j), k = i, i+1, nonzero for 1 <= k <= NX-2
       T tx = (T)0;
       if (i >= 1) {
-        const T a = (T)0.5 * (ld(vu, (size_t)(j - 1) * NX + i) + ld(vu, (size_t)j * NX + i));
+        const T a = (T)0.5 * (ld(vu, (j - 1) * NX + i) + ld(vu, j * NX + i));
         tx += a * (u1 - ld(uv, c - 1));
       }
       if (i + 1 <= NX - 2) {
-        const T a = (T)0.5 * (ld(vu, (size_t)(j - 1) * NX + i + 1) + ld(vu, (size_t)j * NX + i + 1));
+        const T a = (T)0.5 * (ld(vu, (j - 1) * NX + i + 1) + ld(vu, j * NX + i + 1));
         tx += a * (ld(uv, c + 1) - u1);
       }
       r = (T)0.5 * (tx + ty) * sc;
@@ -185,24 +187,24 @@ __device__ __forceinline__ void w_cross_v_at(int i, int j, int NX, int NY, const
     const T* __restrict__ vu, const T* __restrict__ vv, T* __restrict__ ou, T* __restrict__ ov) {
   const int m = NX - 1;
   if (i >= NX || j >= NY) return;
-  const T w0 = ld(w, (size_t)j * NX + i);
+  const T w0 = ld(w, j * NX + i);
   if (j <= NY - 2) {
     T r = (T)0;
     if (i >= 1 && i <= NX - 2) {
-      const T vd0 = (T)0.5 * (ld(vv, (size_t)j * m + i - 1) + ld(vv, (size_t)j * m + i));
-      const T vd1 = (T)0.5 * (ld(vv, (size_t)(j + 1) * m + i - 1) + ld(vv, (size_t)(j + 1) * m + i));
-      r = (T)-0.5 * (vd0 * w0 + vd1 * ld(w, (size_t)(j + 1) * NX + i));
+      const T vd0 = (T)0.5 * (ld(vv, j * m + i - 1) + ld(vv, j * m + i));
+      const T vd1 = (T)0.5 * (ld(vv, (j + 1) * m + i - 1) + ld(vv, (j + 1) * m + i));
+      r = (T)-0.5 * (vd0 * w0 + vd1 * ld(w, (j + 1) * NX + i));
     }
-    ou[(size_t)j * NX + i] = r;
+    ou[j * NX + i] = r;
   }
   if (i <= NX - 2) {
     T r = (T)0;
     if (j >= 1 && j <= NY - 2) {
-      const T ud0 = (T)0.5 * (ld(vu, (size_t)(j - 1) * NX + i) + ld(vu, (size_t)j * NX + i));
-      const T ud1 = (T)0.5 * (ld(vu, (size_t)(j - 1) * NX + i + 1) + ld(vu, (size_t)j * NX + i + 1));
-      r = (T)0.5 * (ud0 * w0 + ud1 * ld(w, (size_t)j * NX + i + 1));
+      const T ud0 = (T)0.5 * (ld(vu, (j - 1) * NX + i) + ld(vu, j * NX + i));
+      const T ud1 = (T)0.5 * (ld(vu, (j - 1) * NX + i + 1) + ld(vu, j * NX + i + 1));
+      r = (T)0.5 * (ud0 * w0 + ud1 * ld(w, j * NX + i + 1));
     }
-    ov[(size_t)j * m + i] = r;
+    ov[j * m + i] = r;
   }
 }
 
@@ -233,6 +235,7 @@ __global__ void __launch_bounds__(BX* BY) k_w_cross_v(int NX, int NY, const T* _
 int st_convective(const ilm_grid_s* g, int dtype, int field_kind, const void* v, const void* q, void* out,
                   double scale, cudaStream_t st) {
   const int NX = g->nx, NY = g->ny;
+  ILM_REQUIRE((long long)NX * NY < (1LL << 31), "convective_derivative: grid of %d x %d exceeds 32-bit indexing", NX, NY);
   const size_t ne_u = (size_t)NX * (NY - 1);
   CV_DISPATCH(dtype, {
     const T* vu = static_cast<const T*>(v);
@@ -264,6 +267,7 @@ int st_convective(const ilm_grid_s* g, int dtype, int field_kind, const void* v,
 
 int st_w_cross_v(const ilm_grid_s* g, int dtype, const void* w, const void* v, void* out, cudaStream_t st) {
   const int NX = g->nx, NY = g->ny;
+  ILM_REQUIRE((long long)NX * NY < (1LL << 31), "w_cross_v: grid of %d x %d exceeds 32-bit indexing", NX, NY);
   const size_t ne_u = (size_t)NX * (NY - 1);
   CV_DISPATCH(dtype, {
     const T* vu = static_cast<const T*>(v);
