@@ -62,14 +62,32 @@ def parse():
 
 
 def dist_init():
+    """torchrun environment -> (rank, world, torch.distributed or None); NCCL
+    with GPUs, gloo without (the multi-rank host logic is tested on CPU)."""
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if world > 1:
+        import torch
         import torch.distributed as dist
-        backend = "nccl"
-        dist.init_process_group(backend=backend)
+        dist.init_process_group(backend="nccl" if torch.cuda.is_available() else "gloo")
         return rank, world, dist
     return rank, world, None
+
+
+def max_over_ranks(dist, x, device="cuda"):
+    """The slowest rank's value of x (timings are max over ranks)."""
+    if not dist:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_value(world, nprob, steps, total_ms):
+    """Whole-job solves/s: every rank solves its own batch of nprob problems
+    per step (weak scaling), over the slowest rank's time."""
+    return world * nprob * steps / (total_ms / 1000.0)
 
 
 def config(args, world):
@@ -236,12 +254,10 @@ def run_ours(args, rank, world, dist):
     total_ms = _timed(bs, fp, fm, f_out, s_out, args, stream, flush, args.steps)
     torch.cuda.synchronize()
     if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+        total_ms = max_over_ranks(dist, total_ms)
         dist.barrier()
     clocks = clocks_summary(clk, dev)
-    value = world * args.nprob * args.steps / (total_ms / 1000.0)
+    value = aggregate_value(world, args.nprob, args.steps, total_ms)
     its, rr = bs.info()
     solvers[leg_names[args.precond]] = {
         "solves_per_s": args.nprob * args.steps / (total_ms / 1000.0), "cg_iterations_mean": float(np.mean(its)),
