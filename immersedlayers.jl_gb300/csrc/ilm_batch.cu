@@ -99,14 +99,16 @@ __device__ __forceinline__ T bcoef(int code, const T* nx, const T* ny, int k) {
 
 // Zero fill of every task's box, one block per box row (the scatter below
 // then visits only the tiles that hold points)
+// one warp per box row (box rows are tens to a few hundred cells wide)
 template <typename T>
 __global__ void __launch_bounds__(256)
-    k_bfill(const BScatterTask* __restrict__ tasks, int ntasks, const int* __restrict__ bmap) {
-  const int ti = bmap[blockIdx.x];
-  const BScatterTask& S = tasks[ti];
-  const int j = S.ya + (int)blockIdx.x - S.fill0;
+    k_bfill(const BScatterTask* __restrict__ tasks, int nrows, const int* __restrict__ bmap) {
+  const int r = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (r >= nrows) return;
+  const BScatterTask& S = tasks[bmap[r]];
+  const int j = S.ya + r - S.fill0;
   T* row = static_cast<T*>(S.out) + (size_t)j * S.n1;
-  for (int i = S.xa + threadIdx.x; i < S.xb; i += blockDim.x) row[i] = (T)0;
+  for (int i = S.xa + (threadIdx.x & 31); i < S.xb; i += 32) row[i] = (T)0;
 }
 
 // Deterministic scatter: one thread per output cell of an occupied 32 x 8
@@ -940,7 +942,8 @@ int ilm_batch_solve(ilm_batch_t b, const void* fplus, const void* fminus, void* 
     ILM_CHECK_LAUNCH();
     b->launches++;
     MARK();  // 1: surface data jump/average
-    if (b->blk_fillA) k_bfill<T><<<b->blk_fillA, 256, 0, st>>>(b->scatA.as<BScatterTask>(), b->n_scatA, b->mfillA.as<int>());
+    if (b->blk_fillA)
+      k_bfill<T><<<(b->blk_fillA + 7) / 8, 256, 0, st>>>(b->scatA.as<BScatterTask>(), b->blk_fillA, b->mfillA.as<int>());
     ILM_CHECK_LAUNCH();
     if (b->blk_scatA) k_bscatter<T><<<b->blk_scatA, dim3(SB_X, SB_Y), 0, st>>>(b->scatA.as<BScatterTask>(), b->n_scatA,
                                                                     b->mscatA.as<int>());
@@ -972,7 +975,8 @@ int ilm_batch_solve(ilm_batch_t b, const void* fplus, const void* fminus, void* 
   b->launches += 1;
   MARK();  // 7: convert
   BDISPATCH(dt, {
-    if (b->blk_fillB) k_bfill<T><<<b->blk_fillB, 256, 0, st>>>(b->scatB.as<BScatterTask>(), b->n_scatB, b->mfillB.as<int>());
+    if (b->blk_fillB)
+      k_bfill<T><<<(b->blk_fillB + 7) / 8, 256, 0, st>>>(b->scatB.as<BScatterTask>(), b->blk_fillB, b->mfillB.as<int>());
     ILM_CHECK_LAUNCH();
     if (b->blk_scatB) k_bscatter<T><<<b->blk_scatB, dim3(SB_X, SB_Y), 0, st>>>(b->scatB.as<BScatterTask>(), b->n_scatB,
                                                                     b->mscatB.as<int>());
