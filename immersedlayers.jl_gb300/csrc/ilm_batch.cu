@@ -41,6 +41,7 @@ struct BScatterTask {
   const void* ny;
   const void* in;
   int coef;
+  int accum;  // 1: add the sums to the output (no zero fill of its box)
   void* out;
 };
 
@@ -51,6 +52,7 @@ struct BStencilTask {
   const void* in;
   void* out;
   double scale;
+  int accum = 0;  // 1: add to the output
 };
 
 struct BGatherTask {
@@ -158,7 +160,10 @@ __global__ void __launch_bounds__(SB_X* SB_Y)
     }
     __syncthreads();
   }
-  if (i < S.n1 && j < S.n2) static_cast<T*>(S.out)[(size_t)j * S.n1 + i] = acc;
+  if (i < S.n1 && j < S.n2) {
+    T* o = static_cast<T*>(S.out) + (size_t)j * S.n1 + i;
+    *o = S.accum ? *o + acc : acc;
+  }
 }
 
 // Edges{Primal} -> Nodes{Primal} divergence
@@ -175,7 +180,37 @@ __global__ void k_bdiv(const BStencilTask* __restrict__ tasks, int ntasks, const
   const T* v = u + (size_t)NX * (NY - 1);
   const T du = u[(size_t)j * NX + i + 1] - u[(size_t)j * NX + i];
   const T dv = v[(size_t)(j + 1) * (NX - 1) + i] - v[(size_t)j * (NX - 1) + i];
-  static_cast<T*>(S.out)[(size_t)j * (NX - 1) + i] = (du + dv) * (T)S.scale;
+  T* o = static_cast<T*>(S.out) + (size_t)j * (NX - 1) + i;
+  *o = S.accum ? *o + (du + dv) * (T)S.scale : (du + dv) * (T)S.scale;
+}
+
+// Schur right-hand side from the precomputed operator M (one warp per point):
+// rhs = M [jump] - avg, the same quantity as the gather of f* minus avg
+template <typename T>
+__global__ void k_rhsop_matvec(int Ptot, const int* __restrict__ pt2prob, const SchurProbDev* __restrict__ pr,
+                               const float* __restrict__ Mhi, const float* __restrict__ Mlo,
+                               const T* __restrict__ jump, const T* __restrict__ avg, double* __restrict__ out) {
+  const int r = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+  if (r >= Ptot) return;
+  const SchurProbDev P = pr[pt2prob[r]];
+  const int k = r - P.poff, n = P.n;
+  const float* __restrict__ mh = Mhi + P.soff + (size_t)k * schur_ld(n);
+  const float* __restrict__ ml = Mlo + P.soff + (size_t)k * schur_ld(n);
+  const T* __restrict__ jp = jump + P.poff;
+  FF a{0.f, 0.f};
+  for (int l = lane; l < n; l += 32) {
+    const double v = (double)jp[l];
+    const float vh = (float)v;
+    ff_fma(a, __ldg(mh + l), __ldg(ml + l), vh, (float)(v - (double)vh));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    FF b;
+    b.hi = __shfl_down_sync(0xffffffffu, a.hi, o);
+    b.lo = __shfl_down_sync(0xffffffffu, a.lo, o);
+    a = ff_add(a, b);
+  }
+  if (lane == 0) out[r] = ((double)a.hi + (double)a.lo) - (double)avg[r];
 }
 
 template <typename T>
@@ -270,6 +305,14 @@ struct ilm_batch_s {
   DevBuf scat_ne;  // occupied tiles of the scatter tasks
   // task of every block of the batched launches (no per-block search)
   DevBuf mfillA, mscatA, mdivA, mfillB, mscatB, mdivB, mconv[3];
+  // precomputed right-hand-side operator (ilm_batch_set_rhs_operator): M per
+  // problem (float-float, the layout of S), the functionals it is built from,
+  // and the stage-B tasks that add the correction source to f*'s source so
+  // that one convolution gives the field
+  bool rhs_op = false, rhs_op_ready = false;
+  DevBuf Mhi, Mlo, FU, FD, schurPfull, scatB2, divB2, convC, mfillB2;
+  int blk_fillB2 = 0, rhs_tiles = 0;
+  std::vector<SchurProbDev> schur_host;
   int n_conv = 0;
   size_t box_cells = 0;  // cells of all source boxes
   ConvLaunch convL;
@@ -648,7 +691,7 @@ int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* 
     box[p] = {ca, cb, ra, rb};
     B->box_cells += (size_t)(cb - ca) * (rb - ra);
   }
-  std::vector<ConvJobDev> jobsA(nprob), jobsB(nprob);
+  std::vector<ConvJobDev> jobsA(nprob), jobsB(nprob), jobsC(nprob);
   for (int p = 0; p < nprob; ++p) {
     ConvJobDev J;
     memset(&J, 0, sizeof(J));
@@ -674,9 +717,15 @@ int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* 
     J.out_off = B->foff[p] * e;
     J.add = static_cast<unsigned char*>(B->fstar.p) + B->foff[p] * e;
     jobsB[p] = J;
+    // rhs-operator path: the combined source (in fstar) convolved straight
+    // into the caller's field
+    J.in = static_cast<unsigned char*>(B->fstar.p) + B->foff[p] * e;
+    J.add = nullptr;
+    jobsC[p] = J;
   }
   ILM_TRY(conv_jobs_finalize(jobsA, dtype, &B->convL));
   ILM_TRY(conv_jobs_finalize(jobsB, dtype, &B->convL));
+  ILM_TRY(conv_jobs_finalize(jobsC, dtype, &B->convL));
   if (B->convL.fast) {  // CTA -> job maps (the two job tables share their geometry)
     ILM_TRY(up(B->mconv[0], B->convL.mrows));
     ILM_TRY(up(B->mconv[1], B->convL.mcols));
@@ -686,6 +735,7 @@ int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* 
   B->n_conv = nprob;
   ILM_TRY(up(B->convA, jobsA));
   ILM_TRY(up(B->convB, jobsB));
+  ILM_TRY(up(B->convC, jobsC));
 
   // ---- tasks ---------------------------------------------------------------
   auto ptr_at = [&](const DevBuf& b, size_t off) { return (void*)(static_cast<unsigned char*>(b.p) + off * e); };
@@ -868,6 +918,46 @@ int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* 
   ILM_TRY(up(B->scatB, sB));
   ILM_TRY(up(B->divA, dA));
   ILM_TRY(up(B->divB, dB));
+  {
+    // stage-B tasks of the rhs-operator path: the single layer (Dirichlet
+    // R s) and the divergence of the double layer (Neumann D_s [phi]) add
+    // into f*'s source (same per-problem offset in fstar as in corr); only
+    // the Neumann edge scatters still zero their boxes
+    auto in_corr = [&](const void* q) {
+      const unsigned char* c0 = static_cast<const unsigned char*>(B->corr.p);
+      const unsigned char* c = static_cast<const unsigned char*>(q);
+      return c >= c0 && c < c0 + B->ftot * e;
+    };
+    auto to_fstar = [&](void* q) {
+      return (void*)(static_cast<unsigned char*>(B->fstar.p) + (static_cast<unsigned char*>(q) -
+                                                                 static_cast<unsigned char*>(B->corr.p)));
+    };
+    std::vector<BScatterTask> sB2 = sB;
+    int fill2 = 0;
+    for (auto& T : sB2) {
+      if (in_corr(T.out)) {
+        T.out = to_fstar(T.out);
+        T.accum = 1;
+        T.fill0 = 0;
+      } else {
+        T.fill0 = fill2;
+        fill2 += T.yb - T.ya;
+      }
+    }
+    std::vector<int> m2(std::max(fill2, 1), 0);
+    for (size_t t = 0; t < sB2.size(); ++t)
+      if (!sB2[t].accum)
+        for (int k = 0; k < sB2[t].yb - sB2[t].ya; ++k) m2[sB2[t].fill0 + k] = (int)t;
+    std::vector<BStencilTask> dB2 = dB;
+    for (auto& T : dB2) {
+      T.out = to_fstar(T.out);
+      T.accum = 1;
+    }
+    B->blk_fillB2 = fill2;
+    ILM_TRY(up(B->mfillB2, m2));
+    ILM_TRY(up(B->scatB2, sB2));
+    ILM_TRY(up(B->divB2, dB2));
+  }
   ILM_TRY(up(B->gathA, hA));
 
   // ---- Schur complements (float-float, LGF point-point sums) ----------------
@@ -885,6 +975,7 @@ int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* 
   }
   B->schur_tiles = tiles;
   ILM_TRY(up(B->schurP, sp));
+  B->schur_host = sp;
   BatchWin BW;
   for (int d = 0; d < 2; ++d) {
     BW.bx[d] = B->bx[d].as<int>();
@@ -955,15 +1046,26 @@ int ilm_batch_solve(ilm_batch_t b, const void* fplus, const void* fminus, void* 
     b->launches += b->n_divA ? 1 : 0;
     MARK();  // 3: divergence stencil
   });
-  ILM_TRY(conv_jobs_launch(b->convA.as<ConvJobDev>(), b->n_conv, b->convL, dt, st));
-  b->launches += 3;
-  MARK();  // 4: LGF FFT convolution (f*)
+  if (!b->rhs_op) {
+    ILM_TRY(conv_jobs_launch(b->convA.as<ConvJobDev>(), b->n_conv, b->convL, dt, st));
+    b->launches += 3;
+  }
+  MARK();  // 4: LGF FFT convolution (f*; with the rhs operator f* stays a source)
   BDISPATCH(dt, {
-    k_bgather<T><<<(Ptot + 127) / 128, 128, 0, st>>>(b->gathA.as<BGatherTask>(), b->n_gathA, Ptot);
-    ILM_CHECK_LAUNCH();
-    k_rhs64<T><<<pb, 256, 0, st>>>(Ptot, b->g.as<T>(), b->avg.as<T>(), b->rhs64.as<double>());
-    ILM_CHECK_LAUNCH();
-    b->launches += 2;
+    if (b->rhs_op) {
+      if (Ptot > 0)
+        k_rhsop_matvec<T><<<(Ptot + 7) / 8, 256, 0, st>>>(Ptot, b->pt2prob.as<int>(), b->schurPfull.as<SchurProbDev>(),
+                                                       b->Mhi.as<float>(), b->Mlo.as<float>(), b->jump.as<T>(),
+                                                       b->avg.as<T>(), b->rhs64.as<double>());
+      ILM_CHECK_LAUNCH();
+      b->launches += 1;
+    } else {
+      k_bgather<T><<<(Ptot + 127) / 128, 128, 0, st>>>(b->gathA.as<BGatherTask>(), b->n_gathA, Ptot);
+      ILM_CHECK_LAUNCH();
+      k_rhs64<T><<<pb, 256, 0, st>>>(Ptot, b->g.as<T>(), b->avg.as<T>(), b->rhs64.as<double>());
+      ILM_CHECK_LAUNCH();
+      b->launches += 2;
+    }
     MARK();  // 5: DDF gather (Neumann: with the gradient) + Schur right-hand side
   });
   ILM_TRY(launch_cg_cluster(b->cgp.p, b->order.as<int>(), b->nprob, b->counter.as<int>(), b->maxN, b->nclusters, st,
@@ -975,21 +1077,26 @@ int ilm_batch_solve(ilm_batch_t b, const void* fplus, const void* fminus, void* 
   b->launches += 1;
   MARK();  // 7: convert
   BDISPATCH(dt, {
-    if (b->blk_fillB)
-      k_bfill<T><<<(b->blk_fillB + 7) / 8, 256, 0, st>>>(b->scatB.as<BScatterTask>(), b->blk_fillB, b->mfillB.as<int>());
+    // with the rhs operator the correction's source is added to f*'s
+    // source (scatB2 / divB2 accumulate into it) and one convolution follows
+    const BScatterTask* sBt = (b->rhs_op ? b->scatB2 : b->scatB).as<BScatterTask>();
+    const int fillB = b->rhs_op ? b->blk_fillB2 : b->blk_fillB;
+    if (fillB)
+      k_bfill<T><<<(fillB + 7) / 8, 256, 0, st>>>(sBt, fillB, (b->rhs_op ? b->mfillB2 : b->mfillB).as<int>());
     ILM_CHECK_LAUNCH();
-    if (b->blk_scatB) k_bscatter<T><<<b->blk_scatB, dim3(SB_X, SB_Y), 0, st>>>(b->scatB.as<BScatterTask>(), b->n_scatB,
-                                                                    b->mscatB.as<int>());
+    if (b->blk_scatB) k_bscatter<T><<<b->blk_scatB, dim3(SB_X, SB_Y), 0, st>>>(sBt, b->n_scatB, b->mscatB.as<int>());
     ILM_CHECK_LAUNCH();
-    b->launches += (b->blk_fillB ? 1 : 0) + (b->blk_scatB ? 1 : 0);
+    b->launches += (fillB ? 1 : 0) + (b->blk_scatB ? 1 : 0);
     MARK();  // 8: DDF scatter (correction)
-    if (b->n_divB) k_bdiv<T><<<b->blk_divB, dim3(SB_X, SB_Y), 0, st>>>(b->divB.as<BStencilTask>(), b->n_divB, b->mdivB.as<int>());
+    if (b->n_divB)
+      k_bdiv<T><<<b->blk_divB, dim3(SB_X, SB_Y), 0, st>>>((b->rhs_op ? b->divB2 : b->divB).as<BStencilTask>(),
+                                                         b->n_divB, b->mdivB.as<int>());
     ILM_CHECK_LAUNCH();
     b->launches += b->n_divB ? 1 : 0;
     MARK();  // 9: divergence stencil
   });
   // f = f* + L^-1 (correction source), written into f_out by the inverse row pass
-  ILM_TRY(conv_jobs_launch(b->convB.as<ConvJobDev>(), b->n_conv, b->convL, dt, st, f_out));
+  ILM_TRY(conv_jobs_launch((b->rhs_op ? b->convC : b->convB).as<ConvJobDev>(), b->n_conv, b->convL, dt, st, f_out));
   b->launches += 3;
   MARK();  // 10: LGF FFT convolution (correction) + f*
 #undef MARK
@@ -1063,6 +1170,46 @@ int ilm_batch_set_profiling(ilm_batch_t b, int enable) {
   }
   if (e != b->profiling) b->params_dirty = true;
   b->profiling = e;
+  return ILM_OK;
+}
+
+int ilm_batch_set_rhs_operator(ilm_batch_t b, int enable) {
+  ILM_REQUIRE(b, "null batch");
+  if (enable && !b->rhs_op_ready && b->Ptot > 0) {
+    // full-tile numbering of every problem's n x n operator
+    std::vector<SchurProbDev> sp = b->schur_host;
+    int tiles = 0;
+    for (auto& P : sp) {
+      const int nt = (P.n + 15) / 16;
+      P.tile0 = tiles;
+      tiles += nt * nt;
+    }
+    b->rhs_tiles = tiles;
+    ILM_TRY(up(b->schurPfull, sp));
+    ILM_TRY(b->Mhi.alloc(std::max<size_t>(b->stot, 1) * 4));
+    ILM_TRY(b->Mlo.alloc(std::max<size_t>(b->stot, 1) * 4));
+    ILM_CHECK_CUDA(cudaMemset(b->Mhi.p, 0, std::max<size_t>(b->stot, 1) * 4));
+    ILM_CHECK_CUDA(cudaMemset(b->Mlo.p, 0, std::max<size_t>(b->stot, 1) * 4));
+    ILM_TRY(b->FU.alloc((size_t)b->Ptot * functional_size()));
+    ILM_TRY(b->FD.alloc((size_t)b->Ptot * functional_size()));
+    BatchWin BW;
+    for (int d = 0; d < 2; ++d) {
+      BW.bx[d] = b->bx[d].as<int>();
+      BW.by[d] = b->by[d].as<int>();
+      BW.wx64[d] = b->wx64[d].as<double>();
+      BW.wy64[d] = b->wy64[d].as<double>();
+    }
+    BW.nx64 = b->nx64.as<double>();
+    BW.ny64 = b->ny64.as<double>();
+    ILM_TRY(rhsop_build_batched(b->nprob, b->schurPfull.as<SchurProbDev>(), tiles, b->Ptot, b->pt2prob.as<int>(), BW,
+                                b->ds64.as<double>(), static_cast<Functional*>(b->FU.p),
+                                static_cast<Functional*>(b->FD.p), b->Mhi.as<float>(), b->Mlo.as<float>(),
+                                b->max_grid, nullptr));
+    ILM_CHECK_CUDA(cudaDeviceSynchronize());
+    b->rhs_op_ready = true;
+  }
+  if (b->rhs_op != (enable != 0)) b->param_gen++;
+  b->rhs_op = enable != 0;
   return ILM_OK;
 }
 

@@ -430,6 +430,11 @@ size_t functional_size();
 int schur_build_batched(int nprob, const SchurProbDev* probs_dev, int total_tiles, int Ptot, const int* pt2prob,
                         const BatchWin& W, const double* w, Functional* F, float* Shi, float* Slo, int max_grid,
                         cudaStream_t st);
+// right-hand-side operator of the batched solves (E L^-1 D_s / G_s L^-1 R),
+// full n x n tiles numbered from probs_full_dev[p].tile0
+int rhsop_build_batched(int nprob, const SchurProbDev* probs_full_dev, int total_tiles, int Ptot, const int* pt2prob,
+                        const BatchWin& W, const double* w, Functional* FU, Functional* FD, float* Mhi, float* Mlo,
+                        int max_grid, cudaStream_t st);
 
 // cluster CG with float-float matvecs (ilm_cg.cu); S stored row-major as hi/lo FP32
 size_t cgff_params_size();

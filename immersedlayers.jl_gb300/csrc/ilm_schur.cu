@@ -377,10 +377,11 @@ __global__ void k_functionals_batched(int Ptot, const int* __restrict__ pt2prob,
                                       const double* __restrict__ wxP, const double* __restrict__ wxD,
                                       const double* __restrict__ wyP, const double* __restrict__ wyD,
                                       const double* __restrict__ nx, const double* __restrict__ ny,
-                                      Functional* __restrict__ out) {
+                                      Functional* __restrict__ out, int force_kind) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= Ptot) return;
-  const SchurProbDev P = pr[pt2prob[g]];
+  SchurProbDev P = pr[pt2prob[g]];
+  if (force_kind >= 0) P.kind = force_kind;
   // reuse the single-problem kernel body on a one-point view
   const int k = g;
   Functional F;
@@ -402,6 +403,22 @@ __global__ void k_functionals_batched(int Ptot, const int* __restrict__ pt2prob,
     for (int t = 0; t < NTAP; ++t) {
       F.xw[0][t] = wxp[t];
       F.yw[0][t] = wyp[t];
+    }
+  } else if (P.kind == ILM_SCHUR_GLINVD) {  // D_s functional on Nodes{Primal} (as k_functionals)
+    F.nterm = 2;
+    F.coef[0] = nx[k] * P.invh;
+    F.xb[0] = bxD[k] - 1;
+    F.yb[0] = byP[k];
+    for (int t = 0; t < FW; ++t) {
+      F.xw[0][t] = at(wxd, t) - at(wxd, t - 1);
+      F.yw[0][t] = at(wyp, t);
+    }
+    F.coef[1] = ny[k] * P.invh;
+    F.xb[1] = bxP[k];
+    F.yb[1] = byD[k] - 1;
+    for (int t = 0; t < FW; ++t) {
+      F.xw[1][t] = at(wxp, t);
+      F.yw[1][t] = at(wyd, t) - at(wyd, t - 1);
     }
   } else {  // CLinvCT
     F.nterm = 2;
@@ -539,9 +556,120 @@ int schur_build_batched(int nprob, const SchurProbDev* probs_dev, int total_tile
   ILM_TRY(lgf_table_ff_device(max_grid + 16, &G, &ld, st));
   k_functionals_batched<<<(Ptot + 127) / 128, 128, 0, st>>>(Ptot, pt2prob, probs_dev, W.bx[0], W.bx[1], W.by[0],
                                                             W.by[1], W.wx64[0], W.wx64[1], W.wy64[0], W.wy64[1],
-                                                            W.nx64, W.ny64, F);
+                                                            W.nx64, W.ny64, F, -1);
   ILM_CHECK_LAUNCH();
   k_schur_pairs_batched<<<total_tiles, dim3(16, 16), 0, st>>>(nprob, probs_dev, F, w, G, ld, ld - 1, Shi, Slo);
+  ILM_CHECK_LAUNCH();
+  return ILM_OK;
+}
+
+// The right-hand-side operator of the batched solves, built from the same
+// LGF point-point sums as S: Dirichlet M = E L^-1 D_s (the Schur right-hand
+// side E f*, f* = L^-1 D_s [f]), Neumann M = G_s L^-1 R (G_s f*, f* =
+// L^-1 R [v_n]).  With the plain-interpolation functionals U and the double-
+// layer functionals D of k_functionals, E L^-1 R = w_l U G U and
+// G_s = -D^T, so M_kl = +w_l (U G D)_kl (Dirichlet) and -w_l (D G U)_kl
+// (Neumann).  Full n x n tiles (M is not symmetric), one CTA per 16 x 16
+// tile, float-float as k_schur_pairs_batched; the tiles of problem p start at
+// pr[p].tile0 (the caller's full-tile numbering).
+__global__ void __launch_bounds__(256) k_rhsop_pairs_batched(int nprob, const SchurProbDev* __restrict__ pr,
+                                                             const Functional* __restrict__ FU,
+                                                             const Functional* __restrict__ FD,
+                                                             const double* __restrict__ w,
+                                                             const float2* __restrict__ G, int ld, int M,
+                                                             float* __restrict__ Mhi, float* __restrict__ Mlo) {
+  int lo = 0, hi = nprob - 1;
+  const int u = blockIdx.x;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (pr[mid].tile0 <= u) lo = mid; else hi = mid - 1;
+  }
+  const SchurProbDev P = pr[lo];
+  const int N = P.n;
+  const int nt = (N + 15) / 16;
+  const int t = u - P.tile0;
+  const int ti = t / nt, tj = t - (t / nt) * nt;
+  const int k = ti * 16 + threadIdx.y;
+  const int l = tj * 16 + threadIdx.x;
+  if (k >= N || l >= N) return;
+  const bool dir = P.kind == ILM_SCHUR_RTLINVR;
+  const Functional& Fk = dir ? FU[P.poff + k] : FD[P.poff + k];
+  const Functional& Fl = dir ? FD[P.poff + l] : FU[P.poff + l];
+  FF total{0.f, 0.f};
+  for (int p = 0; p < Fk.nterm; ++p) {
+    FF xk[FW], yk[FW];
+#pragma unroll
+    for (int a = 0; a < FW; ++a) {
+      xk[a] = split_ff(Fk.xw[p][a]);
+      yk[a] = split_ff(Fk.yw[p][a]);
+    }
+    for (int q = 0; q < Fl.nterm; ++q) {
+      FF cx[2 * FW - 1], cy[2 * FW - 1];
+#pragma unroll
+      for (int d = 0; d < 2 * FW - 1; ++d) cx[d] = cy[d] = FF{0.f, 0.f};
+#pragma unroll
+      for (int b = 0; b < FW; ++b) {
+        const FF xb = split_ff(Fl.xw[q][b]);
+        const FF yb = split_ff(Fl.yw[q][b]);
+#pragma unroll
+        for (int a = 0; a < FW; ++a) {
+          ff_fma(cx[a - b + FW - 1], xk[a].hi, xk[a].lo, xb.hi, xb.lo);
+          ff_fma(cy[a - b + FW - 1], yk[a].hi, yk[a].lo, yb.hi, yb.lo);
+        }
+      }
+#pragma unroll
+      for (int d = 0; d < 2 * FW - 1; ++d) {
+        cx[d] = ff_renorm(cx[d].hi, cx[d].lo);
+        cy[d] = ff_renorm(cy[d].hi, cy[d].lo);
+      }
+      const int Dx = Fk.xb[p] - Fl.xb[q] - (FW - 1);
+      const int Dy = Fk.yb[p] - Fl.yb[q] - (FW - 1);
+      FF acc{0.f, 0.f};
+#pragma unroll
+      for (int dy = 0; dy < 2 * FW - 1; ++dy) {
+        int my = abs(Dy + dy);
+        my = my > M ? M : my;
+        const float2* Grow = G + (size_t)my;
+        FF racc{0.f, 0.f};
+#pragma unroll
+        for (int dx = 0; dx < 2 * FW - 1; ++dx) {
+          int mx = abs(Dx + dx);
+          mx = mx > M ? M : mx;
+          const float2 gv = __ldg(Grow + (size_t)mx * ld);
+          ff_fma(racc, gv.x, gv.y, cx[dx].hi, cx[dx].lo);
+        }
+        racc = ff_renorm(racc.hi, racc.lo);
+        ff_fma(acc, cy[dy].hi, cy[dy].lo, racc.hi, racc.lo);
+      }
+      acc = ff_renorm(acc.hi, acc.lo);
+      const FF cc = split_ff(Fk.coef[p] * Fl.coef[q]);
+      ff_fma(total, cc.hi, cc.lo, acc.hi, acc.lo);
+    }
+  }
+  total = ff_renorm(total.hi, total.lo);
+  const FF wl = split_ff((dir ? 1.0 : -1.0) * w[P.poff + l]);
+  const FF v = ff_mul(wl, total);
+  Mhi[P.soff + (size_t)k * schur_ld(N) + l] = v.hi;
+  Mlo[P.soff + (size_t)k * schur_ld(N) + l] = v.lo;
+}
+
+int rhsop_build_batched(int nprob, const SchurProbDev* probs_full_dev, int total_tiles, int Ptot, const int* pt2prob,
+                        const BatchWin& W, const double* w, Functional* FU, Functional* FD, float* Mhi, float* Mlo,
+                        int max_grid, cudaStream_t st) {
+  if (Ptot == 0) return ILM_OK;
+  const float2* G = nullptr;
+  int ld = 0;
+  ILM_TRY(lgf_table_ff_device(max_grid + 16, &G, &ld, st));
+  k_functionals_batched<<<(Ptot + 127) / 128, 128, 0, st>>>(Ptot, pt2prob, probs_full_dev, W.bx[0], W.bx[1], W.by[0],
+                                                            W.by[1], W.wx64[0], W.wx64[1], W.wy64[0], W.wy64[1],
+                                                            W.nx64, W.ny64, FU, ILM_SCHUR_RTLINVR);
+  ILM_CHECK_LAUNCH();
+  k_functionals_batched<<<(Ptot + 127) / 128, 128, 0, st>>>(Ptot, pt2prob, probs_full_dev, W.bx[0], W.bx[1], W.by[0],
+                                                            W.by[1], W.wx64[0], W.wx64[1], W.wy64[0], W.wy64[1],
+                                                            W.nx64, W.ny64, FD, ILM_SCHUR_GLINVD);
+  ILM_CHECK_LAUNCH();
+  k_rhsop_pairs_batched<<<total_tiles, dim3(16, 16), 0, st>>>(nprob, probs_full_dev, FU, FD, w, G, ld, ld - 1, Mhi,
+                                                              Mlo);
   ILM_CHECK_LAUNCH();
   return ILM_OK;
 }

@@ -108,6 +108,7 @@ SIGNATURES = {
     "ilm_batch_stage_times": [_VP, C.POINTER(C.c_float), C.POINTER(_I), C.POINTER(_I)],
     "ilm_batch_cg_times": [_VP, _DP, _DP, C.POINTER(_I)],
     "ilm_batch_set_cg_variant": [_VP, _I],
+    "ilm_batch_set_rhs_operator": [_VP, _I],
     "ilm_batch_get_cg_variant": [_VP, C.POINTER(_I), C.POINTER(_I)],
     "ilm_batch_autotune": [_VP, _VP, _VP, _VP, _VP, C.c_double, _I, _I, _VP, C.POINTER(_I), C.POINTER(C.c_float)],
     "ilm_batch_stats": [_VP, _DP],

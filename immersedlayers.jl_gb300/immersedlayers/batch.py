@@ -219,6 +219,14 @@ BatchSolver.set_profiling = _profiling
 BatchSolver.stage_times = _stage_times
 BatchSolver.stats = _stats
 BatchSolver.cg_times = _cg_times
+def _set_rhs_operator(self, enable=True):
+    """Precompute the right-hand-side operator (E L^-1 D_s / G_s L^-1 R per
+    problem; built once, as much memory as S) so that each later solve takes
+    one LGF convolution instead of two; for batches solved repeatedly."""
+    L.call("ilm_batch_set_rhs_operator", self._h, int(bool(enable)))
+
+
+BatchSolver.set_rhs_operator = _set_rhs_operator
 BatchSolver.set_cg_variant = _set_cg_variant
 BatchSolver.cg_variant = _cg_variant
 BatchSolver.autotune = _autotune

@@ -376,6 +376,15 @@ ILM_API int ilm_batch_cg_times(ilm_batch_t b, double* start_us, double* end_us, 
  * solve.
  * Tuning helpers with no counterpart in the reference (the reference
  * solves one problem at a time with a dense LU).                           */
+/* Precomputed right-hand-side operator, for batches solved more than once
+ * (no counterpart in the reference, which forms the right-hand side with a
+ * full-grid convolution each solve): enable != 0 builds, once, per problem
+ * M = E L^-1 D_s (Dirichlet) / G_s L^-1 R (Neumann) from the same LGF
+ * point-point sums as S (float-float, as much memory as S), after which a
+ * solve forms the Schur right-hand side as M [jump] - avg and the field with
+ * one LGF convolution of the combined source instead of two.  The results
+ * agree with the default path to the FP32 rounding of the convolution.     */
+ILM_API int ilm_batch_set_rhs_operator(ilm_batch_t b, int enable);
 #define ILM_CG_VARIANTS 5
 ILM_API int ilm_batch_set_cg_variant(ilm_batch_t b, int variant);
 ILM_API int ilm_batch_get_cg_variant(ilm_batch_t b, int* variant, int* nclusters);
