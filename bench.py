@@ -298,6 +298,11 @@ def run_ours(args, rank, world, dist):
     # end to end through the public API from host buffers
     e2e = _e2e(args, specs, stream, dt)
     stencil = _stencil_gbs(stream, flush, hbm)
+    conv_stage = [n for n in names if n.startswith("LGF FFT conv (corr.)")]
+    cufft = _cufft_comparison(specs, stream, flush, stage_ms[names.index(conv_stage[0])] if conv_stage else None) \
+        if rank == 0 else None
+    precision = _precision_leg(stream) if rank == 0 else None
+    refined = _refined_leg(args, specs, stream) if rank == 0 else None
     heat = _heat_scale(args, stream) if (rank == 0 and args.heat_steps > 0) else None
     learned = _learned_leg(args) if (rank == 0 and args.learned_nprob > 0) else None
     stokes = _stokes_leg(args) if (rank == 0 and args.stokes) else None
@@ -314,7 +319,8 @@ def run_ours(args, rank, world, dist):
                 "clocks": clocks, "setup_s": setup_s, "rhs_operator_setup_s": rhsop_s,
                 "rhs": ("right-hand-side operator precomputed at set-up (like S): one LGF convolution per solve"
                         if args.rhs_operator else "two LGF convolutions per solve"), "solvers": solvers,
-                "autotune": tuned, "stencil_gbs": stencil,
+                "autotune": tuned, "stencil_gbs": stencil, "cufft_comparison": cufft, "precision": precision,
+                "refined": refined,
                 "heat": heat, "learned": learned, "stokes": stokes, "moving": moving,
                 "stages_ms": dict(zip(names, [round(x, 4) for x in stage_ms])),
                 "cg_iterations": {"mean": float(np.mean(its)), "max": int(its.max())},
@@ -397,6 +403,144 @@ def _stencil_gbs(stream, flush, hbm):
     out["regularize_2048_8192pts"] = {"gbs": nbytes / t / 1e9, "frac": nbytes / t / 1e9 / hbm, "bytes": nbytes,
                                       "ms": 1000 * t}
     return out
+
+
+def _good_fft_size(n):
+    """Smallest 2^a (a >= 2) or 3 * 2^a >= n: the library's padded FFT lengths."""
+    p2 = 4
+    while p2 < n:
+        p2 *= 2
+    p3 = 12
+    while p3 < n:
+        p3 *= 2
+    return min(p2, p3)
+
+
+def _cufft_comparison(specs, stream, flush, ours_ms):
+    """cuFFT (through torch.fft, timed as a comparison only, never on the
+    product path): the batch's field convolution -- every problem's
+    Nodes{Primal} field zero-padded to the library's P1 x P2, R2C, product
+    with a real half spectrum, C2R, crop and add f* -- batched per grid size,
+    against the library's own convolution stage of the same solve."""
+    import torch
+    groups = {}
+    for sp in specs:
+        key = (sp.nx - 1, sp.ny - 1)
+        groups[key] = groups.get(key, 0) + 1
+    bufs = []
+    for (n1, n2), cnt in sorted(groups.items()):
+        P1, P2 = _good_fft_size(2 * n1 - 1), _good_fft_size(2 * n2 - 1)
+        x = torch.randn(cnt, n2, n1, device="cuda")
+        spec = torch.rand(P2, P1 // 2 + 1, device="cuda")
+        add = torch.randn_like(x)
+        out = torch.empty_like(x)
+        bufs.append((x, spec, add, out, P1, P2))
+
+    def run():
+        for x, spec, add, out, P1, P2 in bufs:
+            X = torch.fft.rfft2(x, s=(P2, P1))
+            X.mul_(spec)
+            y = torch.fft.irfft2(X, s=(P2, P1))
+            torch.add(y[:, :x.shape[1], :x.shape[2]], add, out=out)
+
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            run()
+        ev = []
+        for _ in range(10):
+            flush.fill_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            run()
+            e1.record(stream)
+            ev.append((e0, e1))
+    stream.synchronize()
+    ms = statistics.median(a.elapsed_time(b) for a, b in ev)
+    return {"cufft_ms": ms, "library_ms": ours_ms, "library_speedup": ms / ours_ms if ours_ms else None,
+            "workload": "one LGF convolution of every problem of the batch (FP32, padded P1 x P2 per problem); "
+                        "cuFFT transforms the whole padded field, the library's row pass reads only the source box"}
+
+
+def _refined_leg(args, specs, stream):
+    """FP64 iterative refinement of the whole FP32 batch (block-Jacobi CG):
+    solves/s with FP64 outputs at an FP64 Schur residual <= 1e-12 (first
+    call, which builds the FP64 copy of the pipeline, not timed)."""
+    import numpy as np
+    import torch
+    from immersedlayers.batch import BatchSolver
+    bs = BatchSolver(specs, dtype=torch.float32)
+    bs.set_precond("bjacobi", args.block)
+    fp64 = torch.tensor(np.concatenate([sp.fplus for sp in specs]), dtype=torch.float64, device="cuda")
+    fm64 = torch.tensor(np.concatenate([sp.fminus for sp in specs]), dtype=torch.float64, device="cuda")
+    f = torch.empty(bs.total_cells, dtype=torch.float64, device="cuda")
+    s = torch.empty(bs.total_points, dtype=torch.float64, device="cuda")
+    bs.solve_refined(fp64, fm64, f, s, tol=1e-12, stream=stream)
+    torch.cuda.synchronize()
+    reps = 3
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        bs.solve_refined(fp64, fm64, f, s, tol=1e-12, stream=stream)
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / reps
+    its, rr = bs.info()
+    return {"solves_per_s": len(specs) / dt, "ms_per_batch": 1000 * dt, "tol": 1e-12,
+            "max_rel_residual": float(rr.max()), "cg_iterations_mean": float(its.mean()),
+            "cg_iterations_max": int(its.max()),
+            "method": "FP32 batched solve (block-Jacobi CG to 1e-8), FP64 Schur right-hand side from an FP64 copy "
+                      "of the pipeline, FP64 Schur residual + CG corrections (to 1e-6 each) until <= 1e-12, "
+                      "FP64 field assembly; host wall clock"}
+
+
+def _precision_leg(stream):
+    """Error of every output against the oracle's FP64 dense-LU solutions
+    (the committed fixtures of one Dirichlet and one Neumann problem of the
+    batched configuration per grid size): fields f (relative to max |f|)
+    and surface strengths s (relative to max |s|), max over the problems,
+    for the FP32 batched solve (default path and with the right-hand-side
+    operator) and the FP64-refined solve of the same FP32 batch."""
+    import numpy as np
+    import torch
+    from immersedlayers import workloads as W
+    from immersedlayers.batch import BatchProblemSpec, BatchSolver
+    G = np.load(os.path.join(ROOT, "tests", "golden", "golden_batched.npz"))
+    probs = [int(i) for i in G["problems"]]
+    st = int(G["f_stride"])
+    specs = []
+    for i in probs:
+        n, h, bl, kind, f = W.batch_problem(i)
+        specs.append(BatchProblemSpec(n, h, bl, kind, f))
+
+    def errs(bs, f, s):
+        out = {"dirichlet": {"f": 0.0, "s": 0.0}, "neumann": {"f": 0.0, "s": 0.0}}
+        for k, i in enumerate(probs):
+            fg = bs.field(f, k).double().cpu().numpy().T
+            sg = bs.surface(s, k).double().cpu().numpy()
+            ef = float(np.abs(fg[::st, ::st] - G[f"f_{i}"]).max() / float(G[f"fmax_{i}"]))
+            es = float(np.abs(sg - G[f"s_{i}"]).max() / np.abs(G[f"s_{i}"]).max())
+            d = out["dirichlet" if specs[k].kind == 0 else "neumann"]
+            d["f"] = max(d["f"], ef)
+            d["s"] = max(d["s"], es)
+        return out
+
+    res = {"workload": "problems %s of the batched configuration (one Dirichlet and one Neumann per grid size "
+                       "128..512); reference: the oracle's FP64 dense-LU solve" % probs}
+    for name, rhsop in (("fp32_default", False), ("fp32_rhs_operator", True)):
+        bs = BatchSolver(specs, dtype=torch.float32)
+        if rhsop:
+            bs.set_rhs_operator(True)
+        fp, fm = bs.surface_data()
+        f, s = bs.solve(fp, fm, tol=1e-8, stream=stream)
+        stream.synchronize()
+        res[name] = {"tol": 1e-8, **errs(bs, f, s)}
+    bs = BatchSolver(specs, dtype=torch.float32)
+    bs.set_precond("bjacobi", 32)
+    fp64 = torch.tensor(np.concatenate([sp.fplus for sp in specs]), dtype=torch.float64, device="cuda")
+    fm64 = torch.tensor(np.concatenate([sp.fminus for sp in specs]), dtype=torch.float64, device="cuda")
+    f, s = bs.solve_refined(fp64, fm64, tol=1e-12, stream=stream)
+    its, rr = bs.info()
+    res["fp64_refined"] = {"tol": 1e-12, "max_rel_residual": float(rr.max()), **errs(bs, f, s)}
+    return res
 
 
 def _heat_scale(args, stream):

@@ -304,6 +304,8 @@ int ilm_cache_update_points(ilm_cache_t c, const double* x, const double* y, con
                             const double* ds, ilm_stream_t stream) {
   CHECK_CACHE(c);
   ILM_REQUIRE(c->npts == 0 || (x && y && nrmx && nrmy && ds), "cache_update_points: null point array");
+  delete c->twin;  // the FP64 refinement cache holds the old points
+  c->twin = nullptr;
   return cache_rebin_points(c, x, y, nrmx, nrmy, ds, as_stream(stream));
 }
 
@@ -1089,6 +1091,205 @@ int ilm_solve_neumann_full(ilm_cache_t c, const void* vplus, const void* vminus,
     info->rel_residual = std::max(info->rel_residual, info2.rel_residual);
   }
   return cg != ILM_OK ? cg : cg2;
+}
+
+}  // extern "C"
+
+namespace ilm {
+
+// y = S x for a dense column-major FP64 n x n matrix, one thread per row
+__global__ void k_dense_matvec64(int n, const double* __restrict__ S, const double* __restrict__ x,
+                                 double* __restrict__ y) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double a0 = 0.0, a1 = 0.0;
+  int j = 0;
+  for (; j + 1 < n; j += 2) {
+    a0 = fma(S[i + (size_t)j * n], x[j], a0);
+    a1 = fma(S[i + (size_t)(j + 1) * n], x[j + 1], a1);
+  }
+  if (j < n) a0 = fma(S[i + (size_t)j * n], x[j], a0);
+  y[i] = a0 + a1;
+}
+
+// r = b - y and (|r|^2, |b|^2), one block, fixed reduction order
+__global__ void __launch_bounds__(256) k_residual64(int n, const double* __restrict__ bv, const double* __restrict__ y,
+                                                   double* __restrict__ r, double* __restrict__ norms) {
+  __shared__ double sr[256], sb[256];
+  double rr = 0.0, bb = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double bi = bv[i];
+    const double ri = bi - y[i];
+    r[i] = ri;
+    rr += ri * ri;
+    bb += bi * bi;
+  }
+  sr[threadIdx.x] = rr;
+  sb[threadIdx.x] = bb;
+  __syncthreads();
+  for (int s2 = blockDim.x / 2; s2 > 0; s2 >>= 1) {
+    if (threadIdx.x < s2) {
+      sr[threadIdx.x] += sr[threadIdx.x + s2];
+      sb[threadIdx.x] += sb[threadIdx.x + s2];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    norms[0] = sr[0];
+    norms[1] = sb[0];
+  }
+}
+
+// FP64 cache of the same points for the refinement of an FP32 cache's solves
+static int ensure_twin(ilm_cache_s* c, ilm_cache_s** out) {
+  if (c->dtype == ILM_F64) {
+    *out = c;
+    return ILM_OK;
+  }
+  if (!c->twin) {
+    if (c->host_stale) ILM_TRY(cache_sync_host(c));
+    ilm_cache_t t = nullptr;
+    ILM_TRY(ilm_cache_create(&c->grid, c->kind, c->npts, c->hx.data(), c->hy.data(), c->hnx.data(), c->hny.data(),
+                             c->hds.data(), c->ddf, c->scaling, ILM_F64, &t));
+    c->twin = t;
+  }
+  *out = c->twin;
+  return ILM_OK;
+}
+
+// Refined Dirichlet (neumann = false) or Neumann (true) Poisson solve; see
+// ilm_solve_dirichlet_refined in ilm.h.
+static int solve_refined(ilm_cache_s* c, bool neumann, const double* fplus, const double* fminus, double* f_out,
+                         double* s_out, double tol, int maxiter, int max_refine, ilm_solve_info_t* info,
+                         cudaStream_t st) {
+  constexpr double kRefineFirstTol = 1e-8;  // first (bulk-precision) solve
+  constexpr double kRefineInnerTol = 1e-6;  // each correction solve, relative to its residual
+  const int N = c->npts;
+  const size_t np = c->grid.shape(PC_P).numel();
+  if (N == 0) {
+    if (info) *info = ilm_solve_info_t{0, 1, 0.0};
+    return st_fill(np, ILM_F64, 0.0, f_out, st);
+  }
+  ilm_cache_s* c64 = nullptr;
+  ILM_TRY(ensure_twin(c, &c64));
+  const size_t pv = (size_t)N * sizeof(double);
+  ILM_TRY(c->ref_b.alloc(pv));
+  ILM_TRY(c->ref_x.alloc(pv));
+  ILM_TRY(c->ref_r.alloc(pv));
+  ILM_TRY(c->ref_y.alloc(pv));
+  ILM_TRY(c->ref_norm.alloc(2 * sizeof(double)));
+  int total_its = 0;
+  ilm_solve_info_t inf{0, 0, 0.0};
+  // first solve in the cache's precision: its strengths start the refinement
+  if (c->dtype != ILM_F64) {
+    ILM_TRY(c->ref_in.alloc((size_t)2 * N * esize(c->dtype)));
+    ILM_TRY(c->ref_f.alloc(np * esize(c->dtype)));
+    ILM_TRY(c->ref_s.alloc((size_t)N * esize(c->dtype)));
+    void* in_p = c->ref_in.p;
+    void* in_m = ptr_off(c->ref_in.p, N, c->dtype);
+    ILM_TRY(st_convert(N, ILM_F64, fplus, c->dtype, in_p, st));
+    ILM_TRY(st_convert(N, ILM_F64, fminus, c->dtype, in_m, st));
+    const int r0 = neumann ? ilm_solve_neumann(c, in_p, in_m, c->ref_f.p, c->ref_s.p, std::max(tol, kRefineFirstTol),
+                                               maxiter, &inf, st)
+                           : ilm_solve_dirichlet(c, in_p, in_m, c->ref_f.p, c->ref_s.p,
+                                                 std::max(tol, kRefineFirstTol), maxiter, &inf, st);
+    if (r0 != ILM_OK && r0 != ILM_ERR_NOT_CONVERGED) return r0;
+    total_its += inf.iterations;
+    void* x64;
+    ILM_TRY(pscr(c, 5, &x64));  // the CG solution of the solve above (FP64)
+    ILM_CHECK_CUDA(cudaMemcpyAsync(c->ref_x.p, x64, pv, cudaMemcpyDeviceToDevice, st));
+  } else {
+    ILM_CHECK_CUDA(cudaMemsetAsync(c->ref_x.p, 0, pv, st));
+  }
+  // FP64 Schur right-hand side: Dirichlet E f* - avg with f* = L^-1 D_s [f];
+  // Neumann G_s f* - avg with f* = L^-1 R [vn]
+  void *jump, *avg, *g, *fstar, *corr;
+  ILM_TRY(pscr(c64, 1, &jump));
+  ILM_TRY(pscr(c64, 2, &avg));
+  ILM_TRY(pscr(c64, 3, &g));
+  ILM_TRY(gscr(c64, 3, &fstar));
+  ILM_TRY(gscr(c64, 4, &corr));
+  ILM_TRY(st_axpby(N, ILM_F64, 1.0, fplus, -1.0, fminus, jump, st));
+  ILM_TRY(st_axpby(N, ILM_F64, 0.5, fplus, 0.5, fminus, avg, st));
+  if (neumann) {
+    ILM_TRY(scatter_scalar(c64, PC_P, jump, CF_ONE, fstar, st));
+    ILM_TRY(inverse_laplacian_kind(c64, ILM_NODES_PRIMAL, fstar, fstar, st));
+    ILM_TRY(ilm_surface_grad(c64, fstar, g, st));
+  } else {
+    ILM_TRY(ilm_surface_divergence(c64, jump, fstar, st));
+    ILM_TRY(inverse_laplacian_kind(c64, ILM_NODES_PRIMAL, fstar, fstar, st));
+    GatherTerm t{PC_P, fstar, CF_ONE};
+    ILM_TRY(launch_gather(c64, &t, 1, g, false, 1.0, st));
+  }
+  ILM_TRY(st_axpby(N, ILM_F64, 1.0, g, -1.0, avg, c->ref_b.p, st));
+  // the FP64 Schur complement (the same pair sums for every dtype)
+  DevBuf& S64 = neumann ? c->S_neu64 : c->S_dir64;
+  if (neumann)
+    ILM_TRY(cached_schur(c, ILM_SCHUR_CLINVCT, c->S_neu64, c->S_neu32, c->S_neu_ready, st));
+  else
+    ILM_TRY(cached_schur(c, ILM_SCHUR_RTLINVR, c->S_dir64, c->S_dir32, c->S_dir_ready, st));
+  double rel = 0.0;
+  for (int k = 0;; ++k) {
+    k_dense_matvec64<<<(N + 127) / 128, 128, 0, st>>>(N, S64.as<double>(), c->ref_x.as<double>(),
+                                                       c->ref_y.as<double>());
+    ILM_CHECK_LAUNCH();
+    k_residual64<<<1, 256, 0, st>>>(N, c->ref_b.as<double>(), c->ref_y.as<double>(), c->ref_r.as<double>(),
+                                    c->ref_norm.as<double>());
+    ILM_CHECK_LAUNCH();
+    double nrm[2];
+    ILM_CHECK_CUDA(cudaMemcpyAsync(nrm, c->ref_norm.p, sizeof(nrm), cudaMemcpyDeviceToHost, st));
+    ILM_CHECK_CUDA(cudaStreamSynchronize(st));
+    rel = nrm[1] > 0.0 ? std::sqrt(nrm[0] / nrm[1]) : 0.0;
+    if (rel <= tol || k >= max_refine) break;
+    // correction: S d = r by the FP64 CG, x += d
+    ilm_solve_info_t ci{0, 0, 0.0};
+    const int rc = schur_cg(c, S64, S64, c->ref_r.as<double>(), c->ref_y.as<double>(), kRefineInnerTol, maxiter, &ci,
+                            st);
+    if (rc != ILM_OK && rc != ILM_ERR_NOT_CONVERGED) return rc;
+    total_its += ci.iterations;
+    ILM_TRY(st_axpby(N, ILM_F64, 1.0, c->ref_x.p, 1.0, c->ref_y.p, c->ref_x.p, st));
+  }
+  // outputs: refined strengths, FP64 field f = f* + L^-1 (R s | D_s [phi])
+  ILM_CHECK_CUDA(cudaMemcpyAsync(s_out, c->ref_x.p, pv, cudaMemcpyDeviceToDevice, st));
+  if (neumann)
+    ILM_TRY(ilm_surface_divergence(c64, s_out, corr, st));
+  else
+    ILM_TRY(scatter_scalar(c64, PC_P, s_out, CF_ONE, corr, st));
+  ILM_TRY(inverse_laplacian_kind(c64, ILM_NODES_PRIMAL, corr, corr, st));
+  ILM_TRY(st_axpby(np, ILM_F64, 1.0, corr, 1.0, fstar, f_out, st));
+  ILM_CHECK_CUDA(cudaStreamSynchronize(st));
+  if (info) *info = ilm_solve_info_t{total_its, rel <= tol ? 1 : 0, rel};
+  if (rel > tol) {
+    set_error("refined solve: FP64 Schur residual %g after %d refinement steps (target %g)", rel, max_refine, tol);
+    return ILM_ERR_NOT_CONVERGED;
+  }
+  return ILM_OK;
+}
+
+}  // namespace ilm
+
+extern "C" {
+
+int ilm_solve_dirichlet_refined(ilm_cache_t c, const double* fplus, const double* fminus, double* f_out,
+                                double* s_out, double tol, int maxiter, int max_refine, ilm_solve_info_t* info,
+                                ilm_stream_t stream) {
+  CHECK_CACHE(c);
+  ILM_REQUIRE(c->kind == ILM_CACHE_SCALAR, "solve_dirichlet_refined needs a scalar cache");
+  ILM_REQUIRE(fplus && fminus && f_out && s_out, "null argument");
+  ILM_REQUIRE(tol > 0.0 && maxiter > 0 && max_refine >= 0 && max_refine <= 100,
+              "bad tolerance / iteration limit / refinement steps");
+  return solve_refined(c, false, fplus, fminus, f_out, s_out, tol, maxiter, max_refine, info, as_stream(stream));
+}
+
+int ilm_solve_neumann_refined(ilm_cache_t c, const double* vplus, const double* vminus, double* f_out,
+                              double* df_out, double tol, int maxiter, int max_refine, ilm_solve_info_t* info,
+                              ilm_stream_t stream) {
+  CHECK_CACHE(c);
+  ILM_REQUIRE(c->kind == ILM_CACHE_SCALAR, "solve_neumann_refined needs a scalar cache");
+  ILM_REQUIRE(vplus && vminus && f_out && df_out, "null argument");
+  ILM_REQUIRE(tol > 0.0 && maxiter > 0 && max_refine >= 0 && max_refine <= 100,
+              "bad tolerance / iteration limit / refinement steps");
+  return solve_refined(c, true, vplus, vminus, f_out, df_out, tol, maxiter, max_refine, info, as_stream(stream));
 }
 
 }  // extern "C"

@@ -15,6 +15,7 @@
 #include <math.h>
 
 #include <algorithm>
+#include <chrono>
 #include <memory>
 #include <new>
 
@@ -348,10 +349,18 @@ struct ilm_batch_s {
   double gtol = -1.0;
   int gmaxiter = -1, ggen = -1;
   int param_gen = 0;  // bumped whenever the device CG parameters or the CG launch change
+  // FP64 iterative refinement (ilm_batch_solve_refined): an FP64 copy of the
+  // pipeline (same problems and points, no Schur matrices of its own) for the
+  // accurate Schur right-hand side and the field assembly, and FP64 vectors
+  ilm_batch_s* twin = nullptr;
+  DevBuf ref_in, ref_b, ref_x, ref_r, ref_y, ref_norm, dsoff;
+  // host wall-clock of the set-up phases (ilm_batch_setup_times), ms
+  std::vector<std::pair<const char*, double>> setup_ms;
   ~ilm_batch_s() {
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
     if (gexec) cudaGraphExecDestroy(gexec);
+    delete twin;
   }
 };
 
@@ -523,18 +532,129 @@ int ensure_deflation(ilm_batch_s* b) {
   return ILM_OK;
 }
 
+// optional stage timing: one CUDA event per stage boundary on the solve stream
+int batch_mark(ilm_batch_s* b, cudaStream_t st) {
+  if (b->profiling && b->nev < 32) {
+    if (!b->ev[b->nev]) ILM_CHECK_CUDA(cudaEventCreate(&b->ev[b->nev]));
+    ILM_CHECK_CUDA(cudaEventRecord(b->ev[b->nev], st));
+    b->nev++;
+  }
+  return ILM_OK;
+}
+
+// Stage A of a solve: surface jump / average, the source of f* (double layer
+// for Dirichlet, single layer for Neumann), f* = L^-1 source and the Schur
+// right-hand side in rhs64 (or, with the right-hand-side operator, rhs64 from
+// M [jump] - avg and f*'s source left unconvolved in fstar).
+int batch_stage_a(ilm_batch_s* b, const void* fplus, const void* fminus, cudaStream_t st) {
+  const int dt = b->dtype;
+  const int Ptot = b->Ptot;
+  const int pb = std::min(1024, (Ptot + 255) / 256);
+  BDISPATCH(dt, {
+    k_jump_avg<T><<<pb, 256, 0, st>>>(Ptot, static_cast<const T*>(fplus), static_cast<const T*>(fminus),
+                                      b->jump.as<T>(), b->avg.as<T>());
+    ILM_CHECK_LAUNCH();
+    b->launches++;
+    ILM_TRY(batch_mark(b, st));  // 1: surface data jump/average
+    if (b->blk_fillA)
+      k_bfill<T><<<(b->blk_fillA + 7) / 8, 256, 0, st>>>(b->scatA.as<BScatterTask>(), b->blk_fillA, b->mfillA.as<int>());
+    ILM_CHECK_LAUNCH();
+    if (b->blk_scatA) k_bscatter<T><<<b->blk_scatA, dim3(SB_X, SB_Y), 0, st>>>(b->scatA.as<BScatterTask>(), b->n_scatA,
+                                                                    b->mscatA.as<int>());
+    ILM_CHECK_LAUNCH();
+    b->launches += (b->blk_fillA ? 1 : 0) + (b->blk_scatA ? 1 : 0);
+    ILM_TRY(batch_mark(b, st));  // 2: DDF scatter (double layer / single layer)
+    if (b->n_divA) k_bdiv<T><<<b->blk_divA, dim3(SB_X, SB_Y), 0, st>>>(b->divA.as<BStencilTask>(), b->n_divA, b->mdivA.as<int>());
+    ILM_CHECK_LAUNCH();
+    b->launches += b->n_divA ? 1 : 0;
+    ILM_TRY(batch_mark(b, st));  // 3: divergence stencil
+  });
+  if (!b->rhs_op) {
+    ILM_TRY(conv_jobs_launch(b->convA.as<ConvJobDev>(), b->n_conv, b->convL, dt, st));
+    b->launches += 3;
+  }
+  ILM_TRY(batch_mark(b, st));  // 4: LGF FFT convolution (f*; with the rhs operator f* stays a source)
+  BDISPATCH(dt, {
+    if (b->rhs_op) {
+      if (Ptot > 0)
+        k_rhsop_matvec<T><<<(Ptot + 7) / 8, 256, 0, st>>>(Ptot, b->pt2prob.as<int>(), b->schurPfull.as<SchurProbDev>(),
+                                                       b->Mhi.as<float>(), b->Mlo.as<float>(), b->jump.as<T>(),
+                                                       b->avg.as<T>(), b->rhs64.as<double>());
+      ILM_CHECK_LAUNCH();
+      b->launches += 1;
+    } else {
+      k_bgather<T><<<(Ptot + 127) / 128, 128, 0, st>>>(b->gathA.as<BGatherTask>(), b->n_gathA, Ptot);
+      ILM_CHECK_LAUNCH();
+      k_rhs64<T><<<pb, 256, 0, st>>>(Ptot, b->g.as<T>(), b->avg.as<T>(), b->rhs64.as<double>());
+      ILM_CHECK_LAUNCH();
+      b->launches += 2;
+    }
+  });
+  return batch_mark(b, st);  // 5: DDF gather (Neumann: with the gradient) + Schur right-hand side
+}
+
+// The Schur CG of every problem: rhs64 -> x64 (parameters set by ensure_cg_params)
+int batch_cg(ilm_batch_s* b, cudaStream_t st) {
+  ILM_TRY(launch_cg_cluster(b->cgp.p, b->order.as<int>(), b->nprob, b->counter.as<int>(), b->maxN, b->nclusters, st,
+                            b->cg_variant));
+  b->launches += 1;
+  return batch_mark(b, st);  // 6: Schur CG
+}
+
+// Stage B of a solve: f = f* + L^-1 (correction source of the surface
+// strength in b->s), written into f_out by the last convolution pass.
+int batch_stage_b(ilm_batch_s* b, void* f_out, cudaStream_t st) {
+  const int dt = b->dtype;
+  BDISPATCH(dt, {
+    // with the rhs operator the correction's source is added to f*'s
+    // source (scatB2 / divB2 accumulate into it) and one convolution follows
+    const BScatterTask* sBt = (b->rhs_op ? b->scatB2 : b->scatB).as<BScatterTask>();
+    const int fillB = b->rhs_op ? b->blk_fillB2 : b->blk_fillB;
+    if (fillB)
+      k_bfill<T><<<(fillB + 7) / 8, 256, 0, st>>>(sBt, fillB, (b->rhs_op ? b->mfillB2 : b->mfillB).as<int>());
+    ILM_CHECK_LAUNCH();
+    if (b->blk_scatB) k_bscatter<T><<<b->blk_scatB, dim3(SB_X, SB_Y), 0, st>>>(sBt, b->n_scatB, b->mscatB.as<int>());
+    ILM_CHECK_LAUNCH();
+    b->launches += (fillB ? 1 : 0) + (b->blk_scatB ? 1 : 0);
+    ILM_TRY(batch_mark(b, st));  // 8: DDF scatter (correction)
+    if (b->n_divB)
+      k_bdiv<T><<<b->blk_divB, dim3(SB_X, SB_Y), 0, st>>>((b->rhs_op ? b->divB2 : b->divB).as<BStencilTask>(),
+                                                         b->n_divB, b->mdivB.as<int>());
+    ILM_CHECK_LAUNCH();
+    b->launches += b->n_divB ? 1 : 0;
+    ILM_TRY(batch_mark(b, st));  // 9: divergence stencil
+  });
+  // f = f* + L^-1 (correction source), written into f_out by the inverse row pass
+  ILM_TRY(conv_jobs_launch((b->rhs_op ? b->convC : b->convB).as<ConvJobDev>(), b->n_conv, b->convL, dt, st, f_out));
+  b->launches += 3;
+  return batch_mark(b, st);  // 10: LGF FFT convolution (correction) + f*
+}
+
 }  // namespace
 
 extern "C" {
 
-int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* x, const double* y,
-                     const double* nrmx, const double* nrmy, const double* ds, int ddf, int dtype, ilm_batch_t* out) {
+}  // extern "C"
+
+namespace {
+
+// Set-up of a batch; without `build_schur` the Schur matrices are neither
+// allocated nor built (the FP64 refinement copy uses its parent's).
+int batch_create_impl(int nprob, const ilm_batch_problem_t* probs, const double* x, const double* y,
+                      const double* nrmx, const double* nrmy, const double* ds, int ddf, int dtype, bool build_schur,
+                      ilm_batch_t* out) {
   ILM_REQUIRE(out && probs && nprob > 0, "batch: bad arguments");
   ILM_REQUIRE(dtype == ILM_F64 || dtype == ILM_F32, "batch: bad dtype %d", dtype);
   ILM_REQUIRE(ddf >= ILM_DDF_YANG3 && ddf <= ILM_DDF_M3, "batch: bad ddf %d", ddf);
   auto* B = new (std::nothrow) ilm_batch_s();
   if (!B) return ILM_ERR_NO_MEMORY;
   std::unique_ptr<ilm_batch_s> guard(B);
+  auto clk = std::chrono::steady_clock::now();
+  auto phase = [&](const char* name) {
+    const auto now = std::chrono::steady_clock::now();
+    B->setup_ms.emplace_back(name, std::chrono::duration<double, std::milli>(now - clk).count());
+    clk = now;
+  };
   B->nprob = nprob;
   B->dtype = dtype;
   B->ddf = ddf;
@@ -569,6 +689,7 @@ int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* 
   B->hny.assign(nrmy, nrmy + Ptot);
   B->hds.assign(ds, ds + Ptot);
 
+  phase("validate and copy point data");
   // ---- host set-up: DDF windows and tile lists, packed -------------------
   std::vector<int> hbx[2], hby[2], hp2p(Ptot);
   std::vector<double> hwx[2], hwy[2], hwsc(Ptot);
@@ -584,6 +705,7 @@ int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* 
     ilm_grid_s g{P.nx, P.ny, P.h, P.i0x, P.i0y};
     host_windows(g, ddf, P.npts, x + B->poff[p], y + B->poff[p], &Wall[p]);
   });
+  phase("DDF windows and tile lists (host)");
   for (int p = 0; p < nprob; ++p) {
     const ilm_batch_problem_t& P = probs[p];
     const size_t o = B->poff[p];
@@ -626,6 +748,7 @@ int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* 
     ILM_TRY(up(B->tpts[c], hts[c]));
   }
 
+  phase("pack and upload windows and tile lists");
   // ---- device work buffers ----------------------------------------------
   const size_t e = es(dtype);
   ILM_TRY(B->fstar.alloc(B->ftot * e));
@@ -637,12 +760,14 @@ int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* 
   ILM_TRY(B->s.alloc((size_t)Ptot * e));
   ILM_TRY(B->rhs64.alloc((size_t)Ptot * 8));
   ILM_TRY(B->x64.alloc((size_t)Ptot * 8));
-  ILM_TRY(B->Shi.alloc(std::max<size_t>(B->stot, 1) * 4));
-  ILM_TRY(B->Slo.alloc(std::max<size_t>(B->stot, 1) * 4));
-  // the row padding of every matrix stays zero
-  ILM_CHECK_CUDA(cudaMemset(B->Shi.p, 0, std::max<size_t>(B->stot, 1) * 4));
-  ILM_CHECK_CUDA(cudaMemset(B->Slo.p, 0, std::max<size_t>(B->stot, 1) * 4));
-  ILM_TRY(B->F.alloc((size_t)Ptot * functional_size()));
+  if (build_schur) {
+    ILM_TRY(B->Shi.alloc(std::max<size_t>(B->stot, 1) * 4));
+    ILM_TRY(B->Slo.alloc(std::max<size_t>(B->stot, 1) * 4));
+    // the row padding of every matrix stays zero
+    ILM_CHECK_CUDA(cudaMemset(B->Shi.p, 0, std::max<size_t>(B->stot, 1) * 4));
+    ILM_CHECK_CUDA(cudaMemset(B->Slo.p, 0, std::max<size_t>(B->stot, 1) * 4));
+    ILM_TRY(B->F.alloc((size_t)Ptot * functional_size()));
+  }
   ILM_TRY(B->iters.alloc((size_t)nprob * sizeof(int)));
   ILM_TRY(B->relres.alloc((size_t)nprob * sizeof(double)));
   {
@@ -658,6 +783,7 @@ int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* 
     B->nclusters = cg_cluster_count(nprob, B->maxN);
   }
 
+  phase("allocate work buffers");
   // FFT convolution jobs (fstar and corr in place); one work area per problem
   std::vector<size_t> woff(nprob + 1, 0);
   std::vector<int> P1(nprob), P2(nprob);
@@ -737,6 +863,7 @@ int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* 
   ILM_TRY(up(B->convB, jobsB));
   ILM_TRY(up(B->convC, jobsC));
 
+  phase("source boxes and convolution jobs");
   // ---- tasks ---------------------------------------------------------------
   auto ptr_at = [&](const DevBuf& b, size_t off) { return (void*)(static_cast<unsigned char*>(b.p) + off * e); };
   std::vector<int> nelist;  // occupied tiles of every scatter task, packed
@@ -960,6 +1087,7 @@ int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* 
   }
   ILM_TRY(up(B->gathA, hA));
 
+  phase("stage tasks (build and upload)");
   // ---- Schur complements (float-float, LGF point-point sums) ----------------
   std::vector<SchurProbDev> sp(nprob);
   int tiles = 0;
@@ -985,12 +1113,66 @@ int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* 
   }
   BW.nx64 = B->nx64.as<double>();
   BW.ny64 = B->ny64.as<double>();
-  ILM_TRY(schur_build_batched(nprob, B->schurP.as<SchurProbDev>(), tiles, Ptot, B->pt2prob.as<int>(), BW,
-                              B->ds64.as<double>(), static_cast<Functional*>(B->F.p), B->Shi.as<float>(), B->Slo.as<float>(), B->max_grid,
-                              nullptr));
+  if (build_schur)
+    ILM_TRY(schur_build_batched(nprob, B->schurP.as<SchurProbDev>(), tiles, Ptot, B->pt2prob.as<int>(), BW,
+                                B->ds64.as<double>(), static_cast<Functional*>(B->F.p), B->Shi.as<float>(),
+                                B->Slo.as<float>(), B->max_grid, nullptr));
   ILM_CHECK_CUDA(cudaDeviceSynchronize());
+  phase("Schur complements (device, float-float pair sums)");
   *out = guard.release();
   return ILM_OK;
+}
+
+// r = b - y per problem, with |r|^2 and |b|^2 (one block per problem, fixed
+// reduction order)
+__global__ void __launch_bounds__(256) k_ref_residual(const size_t* __restrict__ poff, const double* __restrict__ bv,
+                                                      const double* __restrict__ y, double* __restrict__ r,
+                                                      double* __restrict__ norms) {
+  __shared__ double sr[256], sb[256];
+  const int p = blockIdx.x;
+  const size_t o = poff[p];
+  const int n = (int)(poff[p + 1] - o);
+  double rr = 0.0, bb = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double bi = bv[o + i];
+    const double ri = bi - y[o + i];
+    r[o + i] = ri;
+    rr += ri * ri;
+    bb += bi * bi;
+  }
+  sr[threadIdx.x] = rr;
+  sb[threadIdx.x] = bb;
+  __syncthreads();
+  for (int s2 = blockDim.x / 2; s2 > 0; s2 >>= 1) {
+    if (threadIdx.x < s2) {
+      sr[threadIdx.x] += sr[threadIdx.x + s2];
+      sb[threadIdx.x] += sb[threadIdx.x + s2];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    norms[2 * p] = sr[0];
+    norms[2 * p + 1] = sb[0];
+  }
+}
+
+// The FP64 copy of an FP32 batch used by the refinement (built on first use)
+int ensure_twin(ilm_batch_s* b) {
+  if (b->twin) return ILM_OK;
+  ilm_batch_t t = nullptr;
+  ILM_TRY(batch_create_impl(b->nprob, b->probs.data(), b->hx.data(), b->hy.data(), b->hnx.data(), b->hny.data(),
+                            b->hds.data(), b->ddf, ILM_F64, false, &t));
+  b->twin = t;
+  return ILM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* x, const double* y,
+                     const double* nrmx, const double* nrmy, const double* ds, int ddf, int dtype, ilm_batch_t* out) {
+  return batch_create_impl(nprob, probs, x, y, nrmx, nrmy, ds, ddf, dtype, true, out);
 }
 
 int ilm_batch_destroy(ilm_batch_t b) {
@@ -1012,94 +1194,116 @@ int ilm_batch_solve(ilm_batch_t b, const void* fplus, const void* fminus, void* 
   ILM_REQUIRE(b && fplus && fminus && f_out && s_out, "batch_solve: null argument");
   ILM_REQUIRE(tol > 0 && maxiter > 0, "batch_solve: bad tolerance / iteration limit");
   cudaStream_t st = as_stream(stream);
-  const int dt = b->dtype;
-  const int Ptot = b->Ptot;
   ILM_TRY(ensure_cg_params(b, tol, maxiter));
-  const int pb = std::min(1024, (Ptot + 255) / 256);
   b->nev = 0;
   b->launches = 0;
-#define MARK()                                                     \
-  do {                                                             \
-    if (b->profiling && b->nev < 32) {                             \
-      if (!b->ev[b->nev]) ILM_CHECK_CUDA(cudaEventCreate(&b->ev[b->nev])); \
-      ILM_CHECK_CUDA(cudaEventRecord(b->ev[b->nev], st));          \
-      b->nev++;                                                    \
-    }                                                              \
-  } while (0)
-  MARK();
-  BDISPATCH(dt, {
-    k_jump_avg<T><<<pb, 256, 0, st>>>(Ptot, static_cast<const T*>(fplus), static_cast<const T*>(fminus),
-                                      b->jump.as<T>(), b->avg.as<T>());
-    ILM_CHECK_LAUNCH();
-    b->launches++;
-    MARK();  // 1: surface data jump/average
-    if (b->blk_fillA)
-      k_bfill<T><<<(b->blk_fillA + 7) / 8, 256, 0, st>>>(b->scatA.as<BScatterTask>(), b->blk_fillA, b->mfillA.as<int>());
-    ILM_CHECK_LAUNCH();
-    if (b->blk_scatA) k_bscatter<T><<<b->blk_scatA, dim3(SB_X, SB_Y), 0, st>>>(b->scatA.as<BScatterTask>(), b->n_scatA,
-                                                                    b->mscatA.as<int>());
-    ILM_CHECK_LAUNCH();
-    b->launches += (b->blk_fillA ? 1 : 0) + (b->blk_scatA ? 1 : 0);
-    MARK();  // 2: DDF scatter (double layer / single layer)
-    if (b->n_divA) k_bdiv<T><<<b->blk_divA, dim3(SB_X, SB_Y), 0, st>>>(b->divA.as<BStencilTask>(), b->n_divA, b->mdivA.as<int>());
-    ILM_CHECK_LAUNCH();
-    b->launches += b->n_divA ? 1 : 0;
-    MARK();  // 3: divergence stencil
-  });
-  if (!b->rhs_op) {
-    ILM_TRY(conv_jobs_launch(b->convA.as<ConvJobDev>(), b->n_conv, b->convL, dt, st));
-    b->launches += 3;
+  ILM_TRY(batch_mark(b, st));
+  ILM_TRY(batch_stage_a(b, fplus, fminus, st));
+  ILM_TRY(batch_cg(b, st));
+  ILM_TRY(st_convert(b->Ptot, ILM_F64, b->x64.p, b->dtype, s_out, st));
+  ILM_CHECK_CUDA(cudaMemcpyAsync(b->s.p, s_out, (size_t)b->Ptot * es(b->dtype), cudaMemcpyDeviceToDevice, st));
+  b->launches += 1;
+  ILM_TRY(batch_mark(b, st));  // 7: convert
+  return batch_stage_b(b, f_out, st);
+}
+
+// FP64 iterative refinement of a batched solve.  The batch's own pipeline
+// (FP32 grid work for an FP32 batch) gives the first surface strengths; the
+// Schur right-hand side is then formed in FP64 by an FP64 copy of the
+// pipeline, and every refinement step forms the FP64 Schur residual
+// r = b - S x (float-float S, FP64 sums), solves S d = r with the batch's
+// preconditioned CG to kRefineInnerTol and adds d in FP64, until every
+// problem's |r| / |b| <= tol or max_refine steps are taken.  The field is
+// assembled from the refined strengths by the FP64 pipeline.
+int ilm_batch_solve_refined(ilm_batch_t b, const double* fplus, const double* fminus, double* f_out, double* s_out,
+                            double tol, int maxiter, int max_refine, ilm_stream_t stream) {
+  constexpr double kRefineFirstTol = 1e-8;  // first (bulk-precision) solve
+  constexpr double kRefineInnerTol = 1e-6;  // each correction solve, relative to its residual
+  ILM_REQUIRE(b && fplus && fminus && f_out && s_out, "batch_solve_refined: null argument");
+  ILM_REQUIRE(tol > 0 && maxiter > 0 && max_refine >= 0 && max_refine <= 100,
+              "batch_solve_refined: bad tolerance / iteration limit / refinement steps");
+  cudaStream_t st = as_stream(stream);
+  const int Ptot = b->Ptot, np = b->nprob;
+  ilm_batch_s* T64 = b;
+  if (b->dtype != ILM_F64) {
+    ILM_TRY(ensure_twin(b));
+    T64 = b->twin;
   }
-  MARK();  // 4: LGF FFT convolution (f*; with the rhs operator f* stays a source)
-  BDISPATCH(dt, {
-    if (b->rhs_op) {
-      if (Ptot > 0)
-        k_rhsop_matvec<T><<<(Ptot + 7) / 8, 256, 0, st>>>(Ptot, b->pt2prob.as<int>(), b->schurPfull.as<SchurProbDev>(),
-                                                       b->Mhi.as<float>(), b->Mlo.as<float>(), b->jump.as<T>(),
-                                                       b->avg.as<T>(), b->rhs64.as<double>());
-      ILM_CHECK_LAUNCH();
-      b->launches += 1;
-    } else {
-      k_bgather<T><<<(Ptot + 127) / 128, 128, 0, st>>>(b->gathA.as<BGatherTask>(), b->n_gathA, Ptot);
-      ILM_CHECK_LAUNCH();
-      k_rhs64<T><<<pb, 256, 0, st>>>(Ptot, b->g.as<T>(), b->avg.as<T>(), b->rhs64.as<double>());
-      ILM_CHECK_LAUNCH();
-      b->launches += 2;
+  const size_t pv = (size_t)std::max(Ptot, 1) * sizeof(double);
+  ILM_TRY(b->ref_b.alloc(pv));
+  ILM_TRY(b->ref_x.alloc(pv));
+  ILM_TRY(b->ref_r.alloc(pv));
+  ILM_TRY(b->ref_y.alloc(pv));
+  ILM_TRY(b->ref_norm.alloc((size_t)2 * np * sizeof(double)));
+  if (!b->dpoff.p) ILM_TRY(up(b->dpoff, b->poff));
+  if (!b->dsoff.p) ILM_TRY(up(b->dsoff, b->soff));
+  b->nev = 0;
+  b->launches = 0;
+  // first solve in the batch's precision, and the FP64 right-hand side
+  ILM_TRY(ensure_cg_params(b, std::max(tol, kRefineFirstTol), maxiter));
+  if (b->dtype == ILM_F64) {
+    ILM_TRY(batch_stage_a(b, fplus, fminus, st));
+  } else {
+    ILM_TRY(b->ref_in.alloc((size_t)2 * std::max(Ptot, 1) * es(b->dtype)));
+    void* in_p = b->ref_in.p;
+    void* in_m = static_cast<unsigned char*>(b->ref_in.p) + (size_t)Ptot * es(b->dtype);
+    ILM_TRY(st_convert(Ptot, ILM_F64, fplus, b->dtype, in_p, st));
+    ILM_TRY(st_convert(Ptot, ILM_F64, fminus, b->dtype, in_m, st));
+    ILM_TRY(batch_stage_a(b, in_p, in_m, st));
+    T64->nev = 0;
+    ILM_TRY(batch_stage_a(T64, fplus, fminus, st));
+  }
+  ILM_CHECK_CUDA(cudaMemcpyAsync(b->ref_b.p, T64->rhs64.p, (size_t)Ptot * 8, cudaMemcpyDeviceToDevice, st));
+  ILM_TRY(batch_cg(b, st));
+  ILM_CHECK_CUDA(cudaMemcpyAsync(b->ref_x.p, b->x64.p, (size_t)Ptot * 8, cudaMemcpyDeviceToDevice, st));
+  std::vector<int> its(np, 0), it1(np);
+  std::vector<double> rel(np, 0.0), nrm(2 * (size_t)np);
+  auto add_iters = [&]() -> int {
+    ILM_CHECK_CUDA(cudaMemcpyAsync(it1.data(), b->iters.p, (size_t)np * sizeof(int), cudaMemcpyDeviceToHost, st));
+    ILM_CHECK_CUDA(cudaStreamSynchronize(st));
+    for (int p = 0; p < np; ++p) its[p] += it1[p];
+    return ILM_OK;
+  };
+  ILM_TRY(add_iters());
+  for (int k = 0;; ++k) {
+    // FP64 Schur residual of every problem
+    if (Ptot > 0)
+      k_batch_schur_apply<<<(Ptot * 32 + 255) / 256, 256, 0, st>>>(Ptot, b->pt2prob.as<int>(), b->dpoff.as<size_t>(),
+                                                                   b->Shi.as<float>(), b->Slo.as<float>(),
+                                                                   b->dsoff.as<size_t>(), b->ref_x.as<double>(),
+                                                                   b->ref_y.as<double>());
+    ILM_CHECK_LAUNCH();
+    k_ref_residual<<<np, 256, 0, st>>>(b->dpoff.as<size_t>(), b->ref_b.as<double>(), b->ref_y.as<double>(),
+                                       b->ref_r.as<double>(), b->ref_norm.as<double>());
+    ILM_CHECK_LAUNCH();
+    b->launches += 2;
+    ILM_CHECK_CUDA(cudaMemcpyAsync(nrm.data(), b->ref_norm.p, nrm.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                   st));
+    ILM_CHECK_CUDA(cudaStreamSynchronize(st));
+    double worst = 0.0;
+    for (int p = 0; p < np; ++p) {
+      rel[p] = nrm[2 * p + 1] > 0.0 ? std::sqrt(nrm[2 * p] / nrm[2 * p + 1]) : 0.0;
+      worst = std::max(worst, rel[p]);
     }
-    MARK();  // 5: DDF gather (Neumann: with the gradient) + Schur right-hand side
-  });
-  ILM_TRY(launch_cg_cluster(b->cgp.p, b->order.as<int>(), b->nprob, b->counter.as<int>(), b->maxN, b->nclusters, st,
-                            b->cg_variant));
-  b->launches += 1;
-  MARK();  // 6: Schur CG
-  ILM_TRY(st_convert(Ptot, ILM_F64, b->x64.p, dt, s_out, st));
-  ILM_CHECK_CUDA(cudaMemcpyAsync(b->s.p, s_out, (size_t)Ptot * es(dt), cudaMemcpyDeviceToDevice, st));
-  b->launches += 1;
-  MARK();  // 7: convert
-  BDISPATCH(dt, {
-    // with the rhs operator the correction's source is added to f*'s
-    // source (scatB2 / divB2 accumulate into it) and one convolution follows
-    const BScatterTask* sBt = (b->rhs_op ? b->scatB2 : b->scatB).as<BScatterTask>();
-    const int fillB = b->rhs_op ? b->blk_fillB2 : b->blk_fillB;
-    if (fillB)
-      k_bfill<T><<<(fillB + 7) / 8, 256, 0, st>>>(sBt, fillB, (b->rhs_op ? b->mfillB2 : b->mfillB).as<int>());
-    ILM_CHECK_LAUNCH();
-    if (b->blk_scatB) k_bscatter<T><<<b->blk_scatB, dim3(SB_X, SB_Y), 0, st>>>(sBt, b->n_scatB, b->mscatB.as<int>());
-    ILM_CHECK_LAUNCH();
-    b->launches += (fillB ? 1 : 0) + (b->blk_scatB ? 1 : 0);
-    MARK();  // 8: DDF scatter (correction)
-    if (b->n_divB)
-      k_bdiv<T><<<b->blk_divB, dim3(SB_X, SB_Y), 0, st>>>((b->rhs_op ? b->divB2 : b->divB).as<BStencilTask>(),
-                                                         b->n_divB, b->mdivB.as<int>());
-    ILM_CHECK_LAUNCH();
-    b->launches += b->n_divB ? 1 : 0;
-    MARK();  // 9: divergence stencil
-  });
-  // f = f* + L^-1 (correction source), written into f_out by the inverse row pass
-  ILM_TRY(conv_jobs_launch((b->rhs_op ? b->convC : b->convB).as<ConvJobDev>(), b->n_conv, b->convL, dt, st, f_out));
-  b->launches += 3;
-  MARK();  // 10: LGF FFT convolution (correction) + f*
-#undef MARK
+    if (worst <= tol || k >= max_refine) break;
+    // correction: S d = r (FP64 vectors, float-float S), x += d
+    ILM_TRY(ensure_cg_params(b, kRefineInnerTol, maxiter));
+    ILM_CHECK_CUDA(cudaMemcpyAsync(b->rhs64.p, b->ref_r.p, (size_t)Ptot * 8, cudaMemcpyDeviceToDevice, st));
+    ILM_TRY(batch_cg(b, st));
+    ILM_TRY(st_axpby(Ptot, ILM_F64, 1.0, b->ref_x.p, 1.0, b->x64.p, b->ref_x.p, st));
+    b->launches += 1;
+    ILM_TRY(add_iters());
+  }
+  // outputs: the refined strengths and the FP64 field assembled from them
+  ILM_CHECK_CUDA(cudaMemcpyAsync(s_out, b->ref_x.p, (size_t)Ptot * 8, cudaMemcpyDeviceToDevice, st));
+  ILM_CHECK_CUDA(cudaMemcpyAsync(T64->s.p, b->ref_x.p, (size_t)Ptot * 8, cudaMemcpyDeviceToDevice, st));
+  T64->nev = 0;
+  ILM_TRY(batch_stage_b(T64, f_out, st));
+  if (T64 != b) b->launches += T64->launches;
+  // per-problem totals for ilm_batch_info: CG iterations of all solves, final FP64 residual
+  ILM_CHECK_CUDA(cudaMemcpyAsync(b->iters.p, its.data(), (size_t)np * sizeof(int), cudaMemcpyHostToDevice, st));
+  ILM_CHECK_CUDA(cudaMemcpyAsync(b->relres.p, rel.data(), (size_t)np * sizeof(double), cudaMemcpyHostToDevice, st));
+  ILM_CHECK_CUDA(cudaStreamSynchronize(st));
   return ILM_OK;
 }
 
@@ -1110,6 +1314,7 @@ int ilm_batch_set_precond(ilm_batch_t b, int mode, int block_size) {
   if (mode == 1) {
     ILM_REQUIRE(block_size >= 4 && block_size <= 72, "batch: block size %d outside [4, 72]", block_size);
     if (b->bj_block != block_size) {
+      const auto t0 = std::chrono::steady_clock::now();
       // blocks of ~block_size consecutive points (at most 1.5 x block_size)
       std::vector<int> blk(b->Ptot), bst, bsz, boff;
       std::vector<BJBlockTask> tasks;
@@ -1153,6 +1358,8 @@ int ilm_batch_set_precond(ilm_batch_t b, int mode, int block_size) {
       ILM_TRY(up(b->bj_tasks, tasks));
       ILM_TRY(launch_block_inverse(b->bj_tasks.as<BJBlockTask>(), (int)tasks.size(), max_sz, nullptr));
       ILM_CHECK_CUDA(cudaDeviceSynchronize());
+      b->setup_ms.emplace_back("block-Jacobi inverses",
+                               std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
       b->bj_block = block_size;
     }
   }
@@ -1359,6 +1566,17 @@ int ilm_batch_stage_times(ilm_batch_t b, float* ms, int* nstages, int* launches)
   return ILM_OK;
 }
 
+int ilm_batch_setup_times(ilm_batch_t b, double* ms, int max_phases, int* nphases, const char** names) {
+  ILM_REQUIRE(b && nphases, "batch_setup_times: null argument");
+  const int n = (int)b->setup_ms.size();
+  *nphases = n;
+  for (int k = 0; k < std::min(n, max_phases); ++k) {
+    if (ms) ms[k] = b->setup_ms[k].second;
+    if (names) names[k] = b->setup_ms[k].first;
+  }
+  return ILM_OK;
+}
+
 int ilm_batch_stats(ilm_batch_t b, double* stats) {
   ILM_REQUIRE(b && stats, "null argument");
   // total points, total Nodes{Primal} cells, sum of npts^2, sum over problems of
@@ -1417,6 +1635,12 @@ int ilm_batch_set_learned(ilm_batch_t b, ilm_net_t net, int kind_mask, const int
       k = e;
     }
   }
+  auto clk = std::chrono::steady_clock::now();
+  auto phase = [&](const char* name) {
+    const auto now = std::chrono::steady_clock::now();
+    b->setup_ms.emplace_back(name, std::chrono::duration<double, std::milli>(now - clk).count());
+    clk = now;
+  };
   std::vector<float> feat((size_t)Ptot * 8);
   std::vector<int> fst(b->nprob, ILM_OK);
   parallel_for(b->nprob, [&](int p) {  // point features of every problem, in parallel
@@ -1430,6 +1654,7 @@ int ilm_batch_set_learned(ilm_batch_t b, ilm_net_t net, int kind_mask, const int
                                 b->hds.data() + o, s0.data(), l0.data(), b->probs[p].h, feat.data() + (size_t)o * 8);
   });
   for (int p = 0; p < b->nprob; ++p) ILM_TRY(fst[p]);
+  phase("learned: point features (host)");
   DevBuf dfeat, das, dll;
   ILM_TRY(up(dfeat, feat));
   ILM_TRY(up(das, as));
@@ -1442,6 +1667,7 @@ int ilm_batch_set_learned(ilm_batch_t b, ilm_net_t net, int kind_mask, const int
   }
   DevBuf tmp, dsel;
   ILM_TRY(tmp.alloc((size_t)Ptot * P * sizeof(float)));
+  phase("learned: uploads");
   ILM_TRY(net_forward_packed(net, Ptot, dfeat.as<float>(), das.as<int>(), dll.as<int>(), tmp.as<float>(), nullptr));
   // this network's band for the points of the problems of the selected kinds
   std::vector<unsigned char> sel(Ptot, 0);
@@ -1455,6 +1681,7 @@ int ilm_batch_set_learned(ilm_batch_t b, ilm_net_t net, int kind_mask, const int
                                                                   b->band.as<float>());
   ILM_CHECK_LAUNCH();
   ILM_CHECK_CUDA(cudaDeviceSynchronize());
+  phase("learned: network inference (device)");
   b->band_k = K;
   b->precond = 2;
   b->params_dirty = true;

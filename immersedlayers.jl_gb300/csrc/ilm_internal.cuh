@@ -323,6 +323,15 @@ struct ilm_cache_s {
   ilm::DevBuf filt_diag, filt_grid;
   bool filt_ready = false;
   ilm::DevBuf red;                     // reduction scratch (double)
+  // FP64 iterative refinement (ilm_solve_*_refined): an FP64 cache of the same
+  // points (FP32 caches only; built on first use, dropped when points move)
+  // and FP64 vectors
+  ilm_cache_s* twin = nullptr;
+  ilm::DevBuf ref_in, ref_f, ref_s, ref_b, ref_x, ref_r, ref_y, ref_norm;
+  ilm_cache_s() = default;
+  ilm_cache_s(const ilm_cache_s&) = delete;
+  ilm_cache_s& operator=(const ilm_cache_s&) = delete;
+  ~ilm_cache_s() { delete twin; }
 
   template <typename T> ilm::PointWin<T> win() const {
     ilm::PointWin<T> w;

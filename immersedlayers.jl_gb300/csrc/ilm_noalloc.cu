@@ -1,22 +1,29 @@
 // Weighted grid inner product that allocates no device memory.
 //
 // Who needs it: callers that cannot allocate device memory at the moment they
-// need an inner product or norm of grid data -- host code running while a
-// stream is being captured into a CUDA graph (cudaMalloc / cudaFree are not
-// permitted there), services whose memory pool owns the whole device and
-// forbids allocations outside it, and latency-critical loops in which a
-// cudaFree (which can synchronise the whole device) is not acceptable.  The
-// regular entry point, ilm_dot_grid, needs a cache, whose creation allocates.
+// need an inner product or norm of grid data -- services whose memory pool
+// owns the whole device and forbids allocations outside it (a Julia process
+// whose GPU arrays all come from its own pool, an inference server sized to
+// the card), and latency-critical loops in which a cudaMalloc or cudaFree
+// (which can synchronise the whole device) is not acceptable.  The regular
+// entry point, ilm_dot_grid, needs a cache, whose creation allocates.
 // ilm_dot_grid_noalloc needs no cache and calls no allocating routine: its
 // only scratch is the fixed device array below, which every GPU that loads
 // this library holds until the process exits.
 //
 // Contract:
-//  * at most kNoAllocMaxRows rows per grid component (larger grids are
-//    rejected with ILM_ERR_SIZE_LIMIT before anything is launched);
+//  * at most kNoAllocMaxRows grid rows (ny dual nodes) per grid component:
+//    one FP64 partial sum per row lives in the array; rows are any length
+//    (each is reduced by a loop), so nx is not limited.  Taller grids are
+//    rejected with ILM_ERR_SIZE_LIMIT before anything is launched;
+//  * `stream` must belong to the current device (the legacy default stream
+//    always does); a stream of another device is rejected, because the
+//    array's address differs per device;
 //  * the first call on a device looks up the device address of the scratch
 //    array (cudaGetSymbolAddress, once per device, with that device current);
 //    make that first call before any stream capture begins;
+//  * the call waits for `stream` (cudaStreamSynchronize) and copies the
+//    result to host memory before it returns;
 //  * every call on a device shares the one array: calls whose kernels may
 //    overlap on the GPU (different streams, or different host threads) race
 //    and must be serialised by the caller;
@@ -37,13 +44,22 @@ static __device__ __align__(256) double g_noalloc_scratch[kNoAllocMaxRows + kNoA
 std::mutex g_na_mu;
 double* g_na_addr[kMaxDevices] = {};
 
-// device address of g_noalloc_scratch on the current device (looked up once)
-int noalloc_scratch(double** out) {
+// device address of g_noalloc_scratch on the current device (looked up once);
+// `st` must belong to that device
+int noalloc_scratch(cudaStream_t st, double** out) {
   int dev = 0;
   ILM_CHECK_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kMaxDevices) {
     ilm::set_error("ilm_dot_grid_noalloc: device ordinal %d out of range", dev);
     return ILM_ERR_UNSUPPORTED;
+  }
+  if (st != nullptr) {
+    int sdev = -1;
+    ILM_CHECK_CUDA(cudaStreamGetDevice(st, &sdev));
+    if (sdev != dev) {
+      ilm::set_error("ilm_dot_grid_noalloc: the stream belongs to device %d, the current device is %d", sdev, dev);
+      return ILM_ERR_INVALID_ARG;
+    }
   }
   std::lock_guard<std::mutex> lk(g_na_mu);
   if (!g_na_addr[dev]) {
@@ -104,10 +120,10 @@ extern "C" int ilm_dot_grid_noalloc(int nx, int ny, double h, int scaling, int k
                                     const void* b, double* result, ilm_stream_t stream) {
   ILM_REQUIRE(nx >= 4 && ny >= 4, "ilm_dot_grid_noalloc: grid needs at least 4x4 dual nodes (got %d x %d)", nx,
               ny);
-  if (nx > kNoAllocMaxRows || ny > kNoAllocMaxRows) {
-    ilm::set_error("ilm_dot_grid_noalloc: grid of %d x %d dual nodes exceeds the fixed scratch (at most %d per "
-                   "side); use ilm_dot_grid",
-                   nx, ny, kNoAllocMaxRows);
+  if (ny > kNoAllocMaxRows) {
+    ilm::set_error("ilm_dot_grid_noalloc: grid of %d x %d dual nodes exceeds the fixed scratch (at most %d rows, "
+                   "ny <= %d); use ilm_dot_grid",
+                   nx, ny, kNoAllocMaxRows, kNoAllocMaxRows);
     return ILM_ERR_SIZE_LIMIT;
   }
   ILM_REQUIRE(h > 0.0, "ilm_dot_grid_noalloc: cell size must be positive");
@@ -119,9 +135,9 @@ extern "C" int ilm_dot_grid_noalloc(int nx, int ny, double h, int scaling, int k
   int pcs[4];
   const int ncomp = ilm::gridkind_components(kind, pcs);
   ILM_REQUIRE(ncomp > 0 && ncomp <= kNoAllocSlots, "ilm_dot_grid_noalloc: bad grid kind %d", kind);
-  double* scratch = nullptr;
-  ILM_TRY(noalloc_scratch(&scratch));
   cudaStream_t st = ilm::as_stream(stream);
+  double* scratch = nullptr;
+  ILM_TRY(noalloc_scratch(st, &scratch));
   const size_t es = dtype == ILM_F64 ? 8 : 4;
   size_t off = 0;
   for (int c = 0; c < ncomp; ++c) {

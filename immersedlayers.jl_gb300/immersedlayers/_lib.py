@@ -95,6 +95,8 @@ SIGNATURES = {
     "ilm_schur_build": [_VP, _I, _D, _VP, _VP],
     "ilm_solve_dirichlet": [_VP, _VP, _VP, _VP, _VP, _D, _I, C.POINTER(SolveInfo), _VP],
     "ilm_solve_neumann": [_VP, _VP, _VP, _VP, _VP, _D, _I, C.POINTER(SolveInfo), _VP],
+    "ilm_solve_dirichlet_refined": [_VP, _VP, _VP, _VP, _VP, _D, _I, _I, C.POINTER(SolveInfo), _VP],
+    "ilm_solve_neumann_refined": [_VP, _VP, _VP, _VP, _VP, _D, _I, _I, C.POINTER(SolveInfo), _VP],
     "ilm_solve_neumann_full": [_VP, _VP, _VP, _VP, _VP, _VP, _VP, _D, _I, C.POINTER(SolveInfo), _VP],
     "ilm_solve_stokes": [_VP, _VP, _VP, _VP, _VP, _VP, _D, _I, C.POINTER(SolveInfo), _VP],
     "ilm_batch_create": [_I, C.POINTER(BatchProblem), _DP, _DP, _DP, _DP, _DP, _I, _I, C.POINTER(_VP)],
@@ -102,6 +104,7 @@ SIGNATURES = {
     "ilm_batch_layout": [_VP, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)],
     "ilm_batch_solve": [_VP, _VP, _VP, _VP, _VP, _D, _I, _VP],
     "ilm_batch_solve_graph": [_VP, _VP, _VP, _VP, _VP, _D, _I, _VP],
+    "ilm_batch_solve_refined": [_VP, _VP, _VP, _VP, _VP, _D, _I, _I, _VP],
     "ilm_batch_info": [_VP, C.POINTER(_I), _DP],
     "ilm_batch_set_precond": [_VP, _I, _I],
     "ilm_batch_set_profiling": [_VP, _I],
@@ -112,6 +115,7 @@ SIGNATURES = {
     "ilm_batch_get_cg_variant": [_VP, C.POINTER(_I), C.POINTER(_I)],
     "ilm_batch_autotune": [_VP, _VP, _VP, _VP, _VP, C.c_double, _I, _I, _VP, C.POINTER(_I), C.POINTER(C.c_float)],
     "ilm_batch_stats": [_VP, _DP],
+    "ilm_batch_setup_times": [_VP, _DP, _I, C.POINTER(_I), C.POINTER(C.c_char_p)],
     "ilm_net_create": [_I, _I, _I, _I, C.POINTER(_VP)],
     "ilm_net_destroy": [_VP],
     "ilm_net_nparams": [_VP, C.POINTER(C.c_size_t)],
@@ -132,7 +136,8 @@ SIGNATURES = {
 _RESTYPES = {"ilm_status_string": C.c_char_p, "ilm_last_error": C.c_char_p}
 
 # functions that may legitimately return ILM_ERR_NOT_CONVERGED (reported via info)
-_SOFT = {"ilm_solve_dirichlet", "ilm_solve_neumann", "ilm_solve_neumann_full", "ilm_solve_stokes"}
+_SOFT = {"ilm_solve_dirichlet", "ilm_solve_neumann", "ilm_solve_neumann_full", "ilm_solve_stokes",
+         "ilm_solve_dirichlet_refined", "ilm_solve_neumann_refined"}
 
 _lib = None
 _lock = threading.Lock()

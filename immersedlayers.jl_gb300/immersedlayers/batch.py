@@ -88,6 +88,23 @@ class BatchSolver:
                _ptr(f_out), _ptr(s_out), float(tol), int(maxiter), _stream_ptr(stream))
         return f_out, s_out
 
+    def solve_refined(self, fplus, fminus, f_out=None, s_out=None, tol=1e-12, maxiter=20000, max_refine=8,
+                      stream=None):
+        """Solve every problem with FP64 iterative refinement: FP64 inputs
+        (converted if needed) and FP64 outputs for either batch dtype; the
+        batch's own solve, then FP64 Schur residuals and preconditioned CG
+        corrections until every ||b - S s|| / ||b|| <= tol, and the fields
+        assembled in FP64 (ilm_batch_solve_refined)."""
+        fp = fplus.to(torch.float64).contiguous()
+        fm = fminus.to(torch.float64).contiguous()
+        if f_out is None:
+            f_out = torch.empty(self.total_cells, dtype=torch.float64, device="cuda")
+        if s_out is None:
+            s_out = torch.empty(self.total_points, dtype=torch.float64, device="cuda")
+        L.call("ilm_batch_solve_refined", self._h, _ptr(fp), _ptr(fm), _ptr(f_out), _ptr(s_out), float(tol),
+               int(maxiter), int(max_refine), _stream_ptr(stream))
+        return f_out, s_out
+
     def info(self):
         it = (C.c_int * self.nprob)()
         rr = (C.c_double * self.nprob)()
@@ -165,6 +182,18 @@ def _stats(self):
                 box_cells=int(st[5]))
 
 
+def _setup_times(self):
+    """Host wall-clock (ms) of every set-up phase so far (batch creation,
+    block-Jacobi inverses, learned-preconditioner inference), in order, as
+    a list of (phase name, ms)."""
+    n = C.c_int()
+    L.call("ilm_batch_setup_times", self._h, None, 0, C.byref(n), None)
+    ms = (C.c_double * max(n.value, 1))()
+    names = (C.c_char_p * max(n.value, 1))()
+    L.call("ilm_batch_setup_times", self._h, ms, n.value, C.byref(n), names)
+    return [(names[k].decode(), float(ms[k])) for k in range(n.value)]
+
+
 def _set_precond(self, mode="none", block_size=64):
     """Schur-CG preconditioner for the following solves: "none" (plain CG),
     "bjacobi" (block-Jacobi over ~block_size consecutive points) or
@@ -218,6 +247,7 @@ BatchSolver.set_precond = _set_precond
 BatchSolver.set_profiling = _profiling
 BatchSolver.stage_times = _stage_times
 BatchSolver.stats = _stats
+BatchSolver.setup_times = _setup_times
 BatchSolver.cg_times = _cg_times
 def _set_rhs_operator(self, enable=True):
     """Precompute the right-hand-side operator (E L^-1 D_s / G_s L^-1 R per

@@ -143,6 +143,34 @@ def solve_neumann(cache, vplus: PointData, vminus: PointData, tol=1e-8, maxiter=
     return f, df, dict(iterations=info.iterations, converged=bool(info.converged), rel_residual=info.rel_residual)
 
 
+def _refined(name, cache, plus, minus, tol, maxiter, max_refine, stream):
+    N = plus.data.numel()
+    f = NodesPrimal.zeros(cache.g, torch.float64)
+    s = ScalarData(torch.zeros(N, dtype=torch.float64, device=plus.data.device))
+    p64 = plus.data.to(torch.float64).contiguous()
+    m64 = minus.data.to(torch.float64).contiguous()
+    info = L.SolveInfo()
+    L.call(name, cache._h, _ptr(p64), _ptr(m64), _ptr(f.data), _ptr(s.data), float(tol), int(maxiter),
+           int(max_refine), C.byref(info), _stream_ptr(stream))
+    return f, s, dict(iterations=info.iterations, converged=bool(info.converged), rel_residual=info.rel_residual)
+
+
+def solve_dirichlet_refined(cache, fplus: PointData, fminus: PointData, tol=1e-12, maxiter=20000, max_refine=8,
+                            stream=None):
+    """Dirichlet solve with FP64 iterative refinement (FP64 outputs for any
+    cache dtype): the cache's own solve, then FP64 Schur residuals and CG
+    corrections until ||b - S s|| / ||b|| <= tol; f assembled in FP64.
+    Returns (f::Nodes{Primal} FP64, s::ScalarData FP64, info)."""
+    return _refined("ilm_solve_dirichlet_refined", cache, fplus, fminus, tol, maxiter, max_refine, stream)
+
+
+def solve_neumann_refined(cache, vplus: PointData, vminus: PointData, tol=1e-12, maxiter=20000, max_refine=8,
+                          stream=None):
+    """Neumann solve (f and [phi]) with FP64 iterative refinement; see
+    solve_dirichlet_refined."""
+    return _refined("ilm_solve_neumann_refined", cache, vplus, vminus, tol, maxiter, max_refine, stream)
+
+
 def solve_neumann_full(cache, vplus: PointData, vminus: PointData, tol=1e-8, maxiter=5000, stream=None):
     """The literate NeumannPoissonProblem solve (test/literate/neumann.jl:101-142)
     on the device: returns (f::Nodes{Primal}, df::ScalarData,

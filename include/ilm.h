@@ -245,16 +245,19 @@ ILM_API int ilm_dot_surface(ilm_cache_t c, int ncomp, const void* a, const void*
 
 /* Allocation-free weighted grid inner product.  No counterpart in the
  * reference: it exists for callers that cannot allocate device memory when
- * they need an inner product (host code running during a CUDA-graph stream
- * capture, services whose memory pool owns the device, latency-critical loops
- * that must not call cudaFree).  Same result as ilm_dot_grid on grid data of
+ * they need an inner product (services whose memory pool owns the device,
+ * latency-critical loops that must not call cudaMalloc or cudaFree, which can
+ * synchronise the whole device).  Same result as ilm_dot_grid on grid data of
  * `kind` for an nx x ny grid with cell size h and `scaling`, without a cache;
  * it calls no allocating routine.  Its scratch is a fixed 128 KiB device array
- * held by every GPU that loads the library: grids are limited to 16384 dual
- * nodes per side (larger ones fail with ILM_ERR_SIZE_LIMIT).  The first call on
- * a device looks up that array's address; make it before any stream capture.
- * Calls share the array: calls that may overlap on the GPU race and must be
- * serialised by the caller.  Synchronises `stream` to return the result.     */
+ * held by every GPU that loads the library: one FP64 partial sum per grid row,
+ * so grids are limited to ny <= 16384 dual nodes (taller ones fail with
+ * ILM_ERR_SIZE_LIMIT; nx is not limited).  `stream` must belong to the
+ * current device (else ILM_ERR_INVALID_ARG).  The first call on a device
+ * looks up that array's address; make it before any stream capture.  Calls
+ * share the array: calls that may overlap on the GPU race and must be
+ * serialised by the caller.  Waits for `stream` and copies the result to
+ * host memory before it returns.                                             */
 ILM_API int ilm_dot_grid_noalloc(int nx, int ny, double h, int scaling, int kind, int dtype, const void* a,
                                  const void* b, double* result, ilm_stream_t stream);
 
@@ -281,6 +284,23 @@ ILM_API int ilm_solve_dirichlet(ilm_cache_t c, const void* fplus, const void* fm
 ILM_API int ilm_solve_neumann(ilm_cache_t c, const void* vplus, const void* vminus,
                       void* f_out, void* df_out, double tol, int maxiter,
                       ilm_solve_info_t* info, ilm_stream_t stream);
+/* FP64 iterative refinement of the Dirichlet / Neumann solves (the
+ * reference solves S s = rhs by FP64 dense LU, test/literate/problems.jl:291,
+ * neumann.jl:123).  Inputs fplus/fminus (or vplus/vminus) and outputs f_out
+ * (Nodes{Primal}) and s_out / df_out (ScalarData) are FP64 device arrays for
+ * every cache dtype.  An FP32 cache first solves in FP32; an FP64 cache of
+ * the same points (built on the first call, dropped by
+ * ilm_cache_update_points) forms the Schur right-hand side in FP64; each
+ * refinement step forms the FP64 Schur residual, solves for the correction by
+ * CG and adds it in FP64, until ||b - S s||_2 / ||b||_2 <= tol or
+ * `max_refine` steps (then ILM_ERR_NOT_CONVERGED); f is assembled in FP64.
+ * info: CG iterations of all solves and the final FP64 residual.           */
+ILM_API int ilm_solve_dirichlet_refined(ilm_cache_t c, const double* fplus, const double* fminus, double* f_out,
+                                        double* s_out, double tol, int maxiter, int max_refine,
+                                        ilm_solve_info_t* info, ilm_stream_t stream);
+ILM_API int ilm_solve_neumann_refined(ilm_cache_t c, const double* vplus, const double* vminus, double* f_out,
+                                      double* df_out, double tol, int maxiter, int max_refine,
+                                      ilm_solve_info_t* info, ilm_stream_t stream);
 /* The whole NeumannPoissonProblem solve of test/literate/neumann.jl:101-142:
  * the potential f (Nodes{Primal}) and df = [phi], then the streamfunction
  * s (Nodes{Dual}) and ds = [psi] (ScalarData): s* = C_s^T df, S ds =
@@ -333,6 +353,19 @@ ILM_API int ilm_batch_layout(ilm_batch_t b, size_t* field_offsets, size_t* point
  * host<->device copies (capturable in a CUDA graph once tol/maxiter are set). */
 ILM_API int ilm_batch_solve(ilm_batch_t b, const void* fplus, const void* fminus, void* f_out, void* s_out,
                             double tol, int maxiter, ilm_stream_t stream);
+/* FP64 iterative refinement of the batched solve (the reference's solves are
+ * FP64 dense LU, test/literate/problems.jl:291, neumann.jl:123).  fplus /
+ * fminus: packed surface data in FP64 (device); f_out / s_out: FP64 packed
+ * fields and surface strengths.  The batch's pipeline (FP32 grid work for an
+ * FP32 batch) gives the first strengths; an FP64 copy of the pipeline
+ * (built on the first call) forms the Schur right-hand side; each
+ * refinement step forms the FP64 Schur residual of every problem, solves for
+ * the correction with the batch's preconditioned CG and adds it in FP64,
+ * until every ||b - S s||_2 / ||b||_2 <= tol or `max_refine` steps; the field
+ * is then assembled in FP64.  ilm_batch_info reports the CG iterations of
+ * all solves and the final FP64 residual per problem.  Synchronises `stream`. */
+ILM_API int ilm_batch_solve_refined(ilm_batch_t b, const double* fplus, const double* fminus, double* f_out,
+                                    double* s_out, double tol, int maxiter, int max_refine, ilm_stream_t stream);
 /* The same solve as one CUDA graph launch on `stream` (a created stream,
  * not the legacy default stream): the first call for a set of buffers,
  * tolerance, limit and CG configuration captures the launch sequence of
@@ -357,6 +390,11 @@ ILM_API int ilm_batch_set_precond(ilm_batch_t b, int mode, int block_size);
 ILM_API int ilm_batch_set_profiling(ilm_batch_t b, int enable);
 ILM_API int ilm_batch_stage_times(ilm_batch_t b, float* ms, int* nstages, int* launches);
 ILM_API int ilm_batch_stats(ilm_batch_t b, double* stats);
+/* Host wall-clock (ms) of the phases of this batch's set-up
+ * (ilm_batch_create): up to max_phases times into ms[] and static phase
+ * names into names[] (either may be null); *nphases = the number of phases.
+ * No counterpart in the reference (its caches have no set-up profile).     */
+ILM_API int ilm_batch_setup_times(ilm_batch_t b, double* ms, int max_phases, int* nphases, const char** names);
 /* Per-problem Schur CG timing of the last solve issued with profiling
  * enabled: start and end (us, relative to the first problem taken) and the
  * SM of the first CTA of the cluster that solved it.  A profiling helper

@@ -9,9 +9,11 @@ known-answer tests) at two set-ups:
   numpy default_rng(1), f- = 0): f on Nodes{Primal} (x-fastest), s, and the
   extreme eigenvalues of the ds-symmetrised create_RTLinvR;
 * golden_neumann_circle.npz: the Neumann problem of test/literate/neumann.jl
-  at h = 0.04 ([-2,2]^2, circle R = 1, ds = 1.4h, v+ = n_x, v- = 0): f and [phi].
+  at h = 0.04 ([-2,2]^2, circle R = 1, ds = 1.4h, v+ = n_x, v- = 0): f and [phi];
+* golden_batched.npz: one Dirichlet and one Neumann problem of the batched
+  configuration per grid size (128 ... 512), see `batched`.
 
-Run:  python tests/golden/make_golden.py
+Run:  python tests/golden/make_golden.py [dirichlet] [neumann] [batched]
 """
 import os
 import sys
@@ -50,7 +52,41 @@ def neumann_circle():
                         grid=np.array([g.nx, g.ny, g.i0x, g.i0y]), h=h)
 
 
+# One Dirichlet and one Neumann problem of the batched configuration
+# (workloads.batch_problem(i), seeds 3 + i) for every grid size it draws from.
+BATCHED_PROBLEMS = (8, 11, 18, 21, 6, 3, 2, 5, 0, 15)
+F_STRIDE = 4
+
+
+def batched():
+    """golden_batched.npz: per problem i of BATCHED_PROBLEMS, the oracle's
+    dense-LU solution: s (all points; [phi] for the Neumann problems), f on
+    Nodes{Primal} sampled every F_STRIDE cells in x and y (f[::4, ::4], x
+    first), and max |f| over the whole field."""
+    out = {"problems": np.array(BATCHED_PROBLEMS), "f_stride": F_STRIDE}
+    for i in BATCHED_PROBLEMS:
+        n, h, bl, kind, fb = W.batch_problem(i)
+        g = O.Grid(n, n, h, n // 2, n // 2)
+        c = O.SurfaceCache(bl.x, bl.y, bl.nx, bl.ny, bl.ds, g)
+        fm = np.zeros_like(fb)
+        if kind == 0:
+            f, s = O.solve_dirichlet(c, fb, fm)
+        else:
+            f, s, _, _ = O.solve_neumann(c, fb, fm)
+        out[f"s_{i}"] = s
+        out[f"f_{i}"] = f[::F_STRIDE, ::F_STRIDE]
+        out[f"fmax_{i}"] = np.abs(f).max()
+        out[f"meta_{i}"] = np.array([n, kind, len(bl)])
+        print(f"problem {i}: n={n} kind={kind} npts={len(bl)}", flush=True)
+    np.savez_compressed(os.path.join(HERE, "golden_batched.npz"), **out)
+
+
 if __name__ == "__main__":
-    dirichlet_plain()
-    neumann_circle()
+    which = sys.argv[1:] or ["dirichlet", "neumann", "batched"]
+    if "dirichlet" in which:
+        dirichlet_plain()
+    if "neumann" in which:
+        neumann_circle()
+    if "batched" in which:
+        batched()
     print("written")
