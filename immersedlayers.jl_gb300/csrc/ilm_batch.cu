@@ -1395,8 +1395,16 @@ int ilm_batch_set_rhs_operator(ilm_batch_t b, int enable) {
     ILM_TRY(up(b->schurPfull, sp));
     ILM_TRY(b->Mhi.alloc(std::max<size_t>(b->stot, 1) * 4));
     ILM_TRY(b->Mlo.alloc(std::max<size_t>(b->stot, 1) * 4));
-    ILM_CHECK_CUDA(cudaMemset(b->Mhi.p, 0, std::max<size_t>(b->stot, 1) * 4));
-    ILM_CHECK_CUDA(cudaMemset(b->Mlo.p, 0, std::max<size_t>(b->stot, 1) * 4));
+    // set-up work on a stream of its own (not the legacy stream, which
+    // would wait for and block every other stream of the device)
+    cudaStream_t st = nullptr;
+    ILM_CHECK_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    struct StreamGuard {
+      cudaStream_t s;
+      ~StreamGuard() { cudaStreamDestroy(s); }
+    } sg{st};
+    ILM_CHECK_CUDA(cudaMemsetAsync(b->Mhi.p, 0, std::max<size_t>(b->stot, 1) * 4, st));
+    ILM_CHECK_CUDA(cudaMemsetAsync(b->Mlo.p, 0, std::max<size_t>(b->stot, 1) * 4, st));
     ILM_TRY(b->FU.alloc((size_t)b->Ptot * functional_size()));
     ILM_TRY(b->FD.alloc((size_t)b->Ptot * functional_size()));
     BatchWin BW;
@@ -1411,8 +1419,8 @@ int ilm_batch_set_rhs_operator(ilm_batch_t b, int enable) {
     ILM_TRY(rhsop_build_batched(b->nprob, b->schurPfull.as<SchurProbDev>(), tiles, b->Ptot, b->pt2prob.as<int>(), BW,
                                 b->ds64.as<double>(), static_cast<Functional*>(b->FU.p),
                                 static_cast<Functional*>(b->FD.p), b->Mhi.as<float>(), b->Mlo.as<float>(),
-                                b->max_grid, nullptr));
-    ILM_CHECK_CUDA(cudaDeviceSynchronize());
+                                b->max_grid, st));
+    ILM_CHECK_CUDA(cudaStreamSynchronize(st));
     b->rhs_op_ready = true;
   }
   if (b->rhs_op != (enable != 0)) b->param_gen++;

@@ -421,7 +421,9 @@ ILM_API int ilm_batch_cg_times(ilm_batch_t b, double* start_us, double* end_us, 
  * point-point sums as S (float-float, as much memory as S), after which a
  * solve forms the Schur right-hand side as M [jump] - avg and the field with
  * one LGF convolution of the combined source instead of two.  The results
- * agree with the default path to the FP32 rounding of the convolution.     */
+ * agree with the default path to the FP32 rounding of the convolution.  A
+ * set-up call: the build runs on a stream of its own (no legacy-stream or
+ * device-wide synchronisation) and the call returns when it is done.       */
 ILM_API int ilm_batch_set_rhs_operator(ilm_batch_t b, int enable);
 #define ILM_CG_VARIANTS 5
 ILM_API int ilm_batch_set_cg_variant(ilm_batch_t b, int variant);

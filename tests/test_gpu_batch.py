@@ -34,7 +34,9 @@ def test_batch_matches_oracle(cuda, dtype):
         else:
             fr, sr, _, _ = O.solve_neumann(oc, sp.fplus, sp.fminus)
         fg = bs.field(f, i).double().cpu().numpy().T
-        tol_f = 1e-7 if dt == torch.float64 else 1e-4
+        # FP64: CG residual 1e-10; FP32: grid work in FP32 (the Neumann
+        # right-hand side differentiates the FP32 potential f*)
+        tol_f = 1e-9 if dt == torch.float64 else (1e-5 if sp.kind == 0 else 2e-5)
         assert rel(fg, fr) < tol_f, (i, sp.kind, rel(fg, fr))
 
 
@@ -101,7 +103,7 @@ def test_batch_large_grids_match_single_solves(cuda):
         ref = fr.data.view(sp.ny - 1, sp.nx - 1).double()
         got = bs.field(f, i).double()
         err = ((got - ref).abs().max() / ref.abs().max()).item()
-        assert err < 1e-4, (i, sp.kind, sp.nx, err)
+        assert err < (1e-5 if sp.kind == 0 else 2e-5), (i, sp.kind, sp.nx, err)
 
 
 @pytest.mark.parametrize("precond", ["none", "bjacobi"])
@@ -193,3 +195,19 @@ def test_batch_rhs_operator_matches_default_path(cuda, dtype):
     bs.set_rhs_operator(False)
     f3, s3 = bs.solve(fp, fm, tol=1e-10, maxiter=20000)
     assert torch.equal(f3, f0) and torch.equal(s3, s0)
+    # repeated solves with the operator on and new surface data: the second
+    # solve's fields match the default path on that data (a leftover
+    # accumulation in f*'s source from the previous solve would show here)
+    g = torch.Generator(device="cuda").manual_seed(3)
+    fp2 = torch.randn(fp.shape, generator=g, device="cuda", dtype=dt)
+    fm2 = 0.5 * torch.randn(fm.shape, generator=g, device="cuda", dtype=dt)
+    f4, s4 = bs.solve(fp2, fm2, tol=1e-10, maxiter=20000)
+    f4, s4 = f4.clone(), s4.clone()
+    bs.set_rhs_operator(True)
+    bs.solve(fp, fm, tol=1e-10, maxiter=20000)   # leaves the previous data's source behind
+    f5, s5 = bs.solve(fp2, fm2, tol=1e-10, maxiter=20000)
+    its, rr = bs.info()
+    assert (rr <= 1e-10).all(), (its, rr)
+    for i in range(len(specs)):
+        a, b = bs.field(f5, i).double(), bs.field(f4, i).double()
+        assert ((a - b).abs().max() / b.abs().max()).item() < tol, (i, specs[i].kind)

@@ -34,13 +34,15 @@ def test_dirichlet_config1(cuda, dtype):
     oc = oracle_cache(og, b)
     S = O.create_RTLinvR(oc)
     f_ref, s_ref = O.solve_dirichlet(oc, fb, np.zeros_like(fb), S)
-    # s inherits the conditioning of S (cond ~ 4e4 here); f is smooth
+    # s inherits the conditioning of S (cond ~ 4e4 here): at a 1e-10
+    # residual it is determined to ~1e-9 (FP64); FP32 grid work leaves f and
+    # s within 1e-5 (measured 4.9e-6 and 1.0e-6)
     if dt == torch.float64:
-        assert rel(f.numpy_components(), f_ref) < 1e-7
-        assert rel(s.numpy(), s_ref) < 1e-5
+        assert rel(f.numpy_components(), f_ref) < 1e-9
+        assert rel(s.numpy(), s_ref) < 1e-8
     else:
-        assert rel(f.numpy_components(), f_ref) < 1e-4
-        assert rel(s.numpy(), s_ref) < 5e-2
+        assert rel(f.numpy_components(), f_ref) < 1e-5
+        assert rel(s.numpy(), s_ref) < 1e-5
     # residual of the device s in the oracle's FP64 operator
     rhs = O.interpolate_scalar(oc, oc.inverse_laplacian(O.surface_divergence(oc, fb))) - 0.5 * fb
     r = np.linalg.norm(S @ s.numpy() - rhs) / np.linalg.norm(rhs)
