@@ -331,77 +331,106 @@ def run_ours(args, rank, world, dist):
 
 
 def _stencil_gbs(stream, flush, hbm):
-    """Achieved HBM GB/s (algorithmic bytes / CUDA-event time, L2 flushed
-    before every launch) of the staggered divergence (Edges -> Nodes, 12 B
-    per cell FP32), the gradient (Nodes -> Edges, 12 B per cell) on 2048^2
-    and 4096^2 grids, and of the DDF regularization of the 8192 points of the
-    Stokes configuration onto Nodes{Primal} of its 2048^2 grid (every cell
-    written: 4 B per cell + 16 B per point); the fused convective derivatives
-    (v . grad p: Edges + 2 Nodes; u . grad u: 2 Edges) and w x v (2 Edges +
-    Nodes{Dual}) on 4096^2, FP32."""
+    """Achieved HBM GB/s (algorithmic bytes / time) of the staggered
+    divergence (Edges -> Nodes, 12 B per cell FP32) and gradient (Nodes ->
+    Edges, 12 B per cell) on 2048^2 and 4096^2 grids, of the fused
+    convective derivatives (v . grad p: Edges + 2 Nodes; u . grad u: 2 Edges)
+    and w x v (2 Edges + Nodes{Dual}) on 4096^2, and of the DDF
+    regularization of the 8192 points of the Stokes configuration onto
+    Nodes{Primal} of its 2048^2 grid (every cell written: 4 B per cell + 16 B
+    per point), FP32.  Two timings per kernel, both with CUDA events on the
+    launching stream:
+      * `gbs`: back-to-back launches cycling over rotating input/output sets
+        whose total is > 3x the L2 (every launch reads cold data), the time
+        per launch = event span / launches;
+      * `single_launch_gbs`: one launch between two events after an L2 flush
+        (includes the launch and event overhead, which dominates at 2048^2)."""
     import torch
     import immersedlayers as il
     from immersedlayers import workloads as W
+    L2_BYTES = 129 * 2 ** 20
 
-    def timed(fn):
-        for _ in range(3):
+    def nsets(bytes_per_set):
+        return max(2, -(-3 * L2_BYTES // bytes_per_set))
+
+    def timed(fns, nbytes):
+        for fn in fns:
             fn()
         ev = []
         with torch.cuda.stream(stream):
-            for _ in range(10):
+            for k in range(10):
                 flush.fill_(1.0)
                 e0 = torch.cuda.Event(enable_timing=True)
                 e1 = torch.cuda.Event(enable_timing=True)
                 e0.record(stream)
-                fn()
+                fns[k % len(fns)]()
                 e1.record(stream)
                 ev.append((e0, e1))
+            stream.synchronize()
+            single = statistics.median(x.elapsed_time(y) for x, y in ev) / 1000.0
+            reps = 4 * len(fns)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for k in range(reps):
+                fns[k % len(fns)]()
+            e1.record(stream)
         stream.synchronize()
-        return statistics.median(x.elapsed_time(y) for x, y in ev) / 1000.0
+        t = e0.elapsed_time(e1) / 1000.0 / reps
+        return {"gbs": nbytes / t / 1e9, "frac": nbytes / t / 1e9 / hbm, "ms": 1000 * t, "bytes": nbytes,
+                "sets": len(fns), "single_launch_gbs": nbytes / single / 1e9,
+                "single_launch_frac": nbytes / single / 1e9 / hbm, "single_launch_ms": 1000 * single}
 
     out = {}
     for n in (2048, 4096):
         g = il.PhysicalGrid(h=4.0 / n, nx=n)
         c = il.SurfaceScalarCache(None, g, dtype=torch.float32)
-        q = il.EdgesPrimal.zeros(g, torch.float32)
-        q.data.normal_()
-        w = il.NodesPrimal.zeros(g, torch.float32)
-        for name, fn, a, b in [("divergence", il.divergence_, w, q), ("grad", il.grad_, q, w)]:
-            t = timed(lambda: fn(a, b, c, stream=stream))
-            nbytes = (a.data.numel() + b.data.numel()) * 4
-            out[f"{name}_{n}"] = {"gbs": nbytes / t / 1e9, "frac": nbytes / t / 1e9 / hbm, "bytes": nbytes,
-                                  "ms": 1000 * t}
-        del c, q, w
+        per = (il.EdgesPrimal.zeros(g, torch.float32).data.numel() +
+               il.NodesPrimal.zeros(g, torch.float32).data.numel()) * 4
+        sets = []
+        for _ in range(nsets(per)):
+            q = il.EdgesPrimal.zeros(g, torch.float32)
+            q.data.normal_()
+            w = il.NodesPrimal.zeros(g, torch.float32)
+            w.data.normal_()
+            sets.append((q, w))
+        out[f"divergence_{n}"] = timed([lambda q=q, w=w: il.divergence_(w, q, c, stream=stream) for q, w in sets], per)
+        out[f"grad_{n}"] = timed([lambda q=q, w=w: il.grad_(q, w, c, stream=stream) for q, w in sets], per)
+        del c, sets
     # fused convective derivatives and w x v (inputs read once, output written once)
     n = 4096
     g = il.PhysicalGrid(h=4.0 / n, nx=n)
     c = il.SurfaceVectorCache(None, g, dtype=torch.float32)
-    v = il.EdgesPrimal.zeros(g, torch.float32)
-    v.data.normal_()
-    p = il.NodesPrimal.zeros(g, torch.float32)
-    p.data.normal_()
-    w = il.NodesDual.zeros(g, torch.float32)
-    w.data.normal_()
-    o_p, o_e = p.similar(), v.similar()
-    for name, fn, nel in [
-            ("convective_nodes_primal", lambda: il.convective_derivative_(o_p, v, p, c, stream=stream),
-             v.data.numel() + 2 * p.data.numel()),
-            ("convective_edges", lambda: il.convective_derivative_(o_e, v, c, stream=stream), 2 * v.data.numel()),
-            ("w_cross_v", lambda: il.w_cross_v_(o_e, w, v, c, stream=stream), 2 * v.data.numel() + w.data.numel())]:
-        t = timed(fn)
-        out[f"{name}_{n}"] = {"gbs": nel * 4 / t / 1e9, "frac": nel * 4 / t / 1e9 / hbm, "bytes": nel * 4,
-                              "ms": 1000 * t}
-    del c, v, p, w, o_p, o_e
+    ne = il.EdgesPrimal.zeros(g, torch.float32).data.numel()
+    npn = il.NodesPrimal.zeros(g, torch.float32).data.numel()
+    nd = il.NodesDual.zeros(g, torch.float32).data.numel()
+    sets = []
+    for _ in range(nsets(4 * (2 * ne + 2 * npn + nd))):
+        v = il.EdgesPrimal.zeros(g, torch.float32)
+        v.data.normal_()
+        p = il.NodesPrimal.zeros(g, torch.float32)
+        p.data.normal_()
+        w = il.NodesDual.zeros(g, torch.float32)
+        w.data.normal_()
+        sets.append((v, p, w, p.similar(), v.similar()))
+    for name, mk, nel in [
+            ("convective_nodes_primal", lambda v, p, w, o_p, o_e: lambda: il.convective_derivative_(
+                o_p, v, p, c, stream=stream), ne + 2 * npn),
+            ("convective_edges", lambda v, p, w, o_p, o_e: lambda: il.convective_derivative_(
+                o_e, v, c, stream=stream), 2 * ne),
+            ("w_cross_v", lambda v, p, w, o_p, o_e: lambda: il.w_cross_v_(o_e, w, v, c, stream=stream),
+             2 * ne + nd)]:
+        out[f"{name}_{n}"] = timed([mk(*st) for st in sets], nel * 4)
+    del c, sets
     d = W.stokes_scale(nrhs=1)
     g = il.PhysicalGrid(h=d["h"], nx=d["n"])
     c = il.SurfaceScalarCache(d["bodies"], g, dtype=torch.float32)
     N = len(d["bodies"])
     f = il.ScalarData(torch.randn(N, device="cuda"))
-    w = il.NodesPrimal.zeros(g, torch.float32)
-    t = timed(lambda: il.regularize_(w, f, c, stream=stream))
-    nbytes = w.data.numel() * 4 + 16 * N
-    out["regularize_2048_8192pts"] = {"gbs": nbytes / t / 1e9, "frac": nbytes / t / 1e9 / hbm, "bytes": nbytes,
-                                      "ms": 1000 * t}
+    nbytes = il.NodesPrimal.zeros(g, torch.float32).data.numel() * 4 + 16 * N
+    outs = [il.NodesPrimal.zeros(g, torch.float32) for _ in range(nsets(nbytes))]
+    out["regularize_2048_8192pts"] = timed([lambda w=w: il.regularize_(w, f, c, stream=stream) for w in outs],
+                                           nbytes)
     return out
 
 
@@ -770,6 +799,7 @@ def _e2e(args, specs, stream, dt):
     times = []
     h2d = d2h = 0
     parts = []
+    phases = []
     for _ in range(steps + 1):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -794,6 +824,7 @@ def _e2e(args, specs, stream, dt):
         parts.append((t1 - t0, t2 - t1, time.perf_counter() - t2))
         h2d = fp.numel() * fp.element_size() * 2
         d2h = (f.numel() + s.numel()) * f.element_size()
+        phases.append(bs.setup_times())
         del bs
     t = statistics.median(times[1:])
     k = times.index(t) if t in times[1:] else 1
@@ -802,7 +833,8 @@ def _e2e(args, specs, stream, dt):
                         "set-up, H2D, solve (first solve also sets up the deflation of the Dirichlet net-charge "
                         "mode), D2H of all fields", "ms_per_step": 1000 * t,
             "ms_breakdown": {"batch_create": 1000 * parts[k][0], "precond_setup": 1000 * parts[k][1],
-                             "copies_and_solve": 1000 * parts[k][2]}}
+                             "copies_and_solve": 1000 * parts[k][2]},
+            "setup_phases_ms": {name: round(ms, 3) for name, ms in phases[k]}}
 
 
 def _cpu_baseline(args, specs):

@@ -246,6 +246,75 @@ k_scatter(int n1, int n2, int ntx, const int* __restrict__ ne, const int* __rest
   }
 }
 
+// Overwriting scatter in one launch over the whole output, two kinds of
+// block: blocks [0, nocc) take one occupied tile each (from the list `ne`,
+// the first *ne_cnt entries; the sums of its candidate points staged in
+// shared memory in index order, the same fixed order as k_scatter), the
+// blocks after them write zeros into the empty tiles, SCAT_TPB consecutive
+// tiles (row-major tile ids) each, skipping the occupied ones.  Every tile
+// is written by exactly one block; the long occupied-tile blocks start
+// first and the zero fill's bandwidth overlaps their load latency.
+constexpr int SCAT_TPB = 8;
+template <typename T>
+__global__ void __launch_bounds__(TILE_X* TILE_Y)
+k_scatter_all(int n1, int n2, int ntx, int ntiles, int nocc, const int* __restrict__ ne,
+              const int* __restrict__ ne_cnt, const int* __restrict__ tptr, const int* __restrict__ tpts,
+              const int* __restrict__ bx, const int* __restrict__ by, const T* __restrict__ wx,
+              const T* __restrict__ wy, const T* __restrict__ wsc, const T* __restrict__ nx,
+              const T* __restrict__ ny, const T* __restrict__ in1, int c1, const T* __restrict__ in2, int c2,
+              T* __restrict__ out) {
+  constexpr int NB = TILE_X * TILE_Y;
+  __shared__ int s_ptr[SCAT_TPB + 1];
+  __shared__ int s_bx[NB], s_by[NB];
+  __shared__ T s_amp[NB], s_wx[NB * NTAP], s_wy[NB * NTAP];
+  const int tid = threadIdx.y * TILE_X + threadIdx.x;
+  if ((int)blockIdx.x >= nocc) {  // zero writer
+    const int t0 = ((int)blockIdx.x - nocc) * SCAT_TPB;
+    if (tid <= SCAT_TPB) s_ptr[tid] = tptr[min(t0 + tid, ntiles)];
+    __syncthreads();
+    for (int q = 0; q < SCAT_TPB; ++q) {
+      const int t = t0 + q;
+      if (t >= ntiles) break;
+      if (s_ptr[q + 1] > s_ptr[q]) continue;  // occupied: an occupied-tile block writes it
+      const int i = (t % ntx) * TILE_X + threadIdx.x;
+      const int j = (t / ntx) * TILE_Y + threadIdx.y;
+      if (i < n1 && j < n2) out[(size_t)j * n1 + i] = (T)0;
+    }
+    return;
+  }
+  if ((int)blockIdx.x >= *ne_cnt) return;  // launched for an upper bound after a device re-binning
+  const int t = ne[blockIdx.x];
+  const int i = (t % ntx) * TILE_X + threadIdx.x;
+  const int j = (t / ntx) * TILE_Y + threadIdx.y;
+  const int p0 = tptr[t], p1 = tptr[t + 1];
+  T acc = (T)0;
+  for (int c0 = p0; c0 < p1; c0 += NB) {
+    const int nc = min(NB, p1 - c0);
+    if (tid < nc) {
+      const int k = tpts[c0 + tid];
+      T g = coef_val<T>(c1, nx, ny, k) * in1[k];
+      if (in2) g += coef_val<T>(c2, nx, ny, k) * in2[k];
+      s_bx[tid] = bx[k];
+      s_by[tid] = by[k];
+      s_amp[tid] = wsc[k] * g;
+#pragma unroll
+      for (int e = 0; e < NTAP; ++e) {
+        s_wx[tid * NTAP + e] = wx[k * NTAP + e];
+        s_wy[tid * NTAP + e] = wy[k * NTAP + e];
+      }
+    }
+    __syncthreads();
+    for (int e = 0; e < nc; ++e) {
+      const int di = i - s_bx[e];
+      const int dj = j - s_by[e];
+      if ((unsigned)di < (unsigned)NTAP && (unsigned)dj < (unsigned)NTAP)
+        acc += s_amp[e] * s_wx[e * NTAP + di] * s_wy[e * NTAP + dj];
+    }
+    __syncthreads();
+  }
+  if (i < n1 && j < n2) out[(size_t)j * n1 + i] = acc;
+}
+
 __global__ void k_fill_zero(float4* __restrict__ p4, size_t n4, unsigned char* __restrict__ tail, int ntail) {
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n4; k += stride)
@@ -327,9 +396,30 @@ int launch_scatter(ilm_cache_s* c, int pc, const void* in1, int coef1, const voi
   const TileList& tl = c->tiles[pc];
   const int dx = pc_dx(pc), dy = pc_dy(pc);
   dim3 blk(TILE_X, TILE_Y);
-  // overwrite: zero fill, then the occupied tiles; accumulate: the occupied
-  // tiles only (the others add nothing)
-  if (!accumulate) ILM_TRY(fill_zero(out, sh.numel() * (c->dtype == ILM_F64 ? 8 : 4), st));
+  if (!accumulate) {
+    // overwrite: one launch over every tile (zeros where no point reaches)
+    const int ntiles = tl.ntx * tl.nty;
+    if (ntiles == 0) return ILM_OK;
+    const int nocc = tl.nne_launch;
+    const int nb = nocc + (ntiles + SCAT_TPB - 1) / SCAT_TPB;
+    if (c->dtype == ILM_F64)
+      k_scatter_all<double><<<nb, blk, 0, st>>>(sh.n1, sh.n2, tl.ntx, ntiles, nocc, tl.ne.as<int>(),
+                                                tl.ne_cnt.as<int>(), tl.ptr.as<int>(), tl.pts.as<int>(),
+                                                c->bx[dx].as<int>(), c->by[dy].as<int>(), c->wx[dx].as<double>(),
+                                                c->wy[dy].as<double>(), c->wscale.as<double>(), c->nx.as<double>(),
+                                                c->ny.as<double>(), static_cast<const double*>(in1), coef1,
+                                                static_cast<const double*>(in2), coef2, static_cast<double*>(out));
+    else
+      k_scatter_all<float><<<nb, blk, 0, st>>>(sh.n1, sh.n2, tl.ntx, ntiles, nocc, tl.ne.as<int>(),
+                                               tl.ne_cnt.as<int>(), tl.ptr.as<int>(), tl.pts.as<int>(),
+                                               c->bx[dx].as<int>(), c->by[dy].as<int>(), c->wx[dx].as<float>(),
+                                               c->wy[dy].as<float>(), c->wscale.as<float>(), c->nx.as<float>(),
+                                               c->ny.as<float>(), static_cast<const float*>(in1), coef1,
+                                               static_cast<const float*>(in2), coef2, static_cast<float*>(out));
+    ILM_CHECK_LAUNCH();
+    return ILM_OK;
+  }
+  // accumulate: the occupied tiles only (the others add nothing)
   const int nb = tl.nne_launch;
   if (nb == 0) return ILM_OK;
   if (c->dtype == ILM_F64) {
@@ -337,13 +427,13 @@ int launch_scatter(ilm_cache_s* c, int pc, const void* in1, int coef1, const voi
                                           c->by[dy].as<int>(), c->wx[dx].as<double>(), c->wy[dy].as<double>(),
                                           c->wscale.as<double>(), c->nx.as<double>(), c->ny.as<double>(),
                                           static_cast<const double*>(in1), coef1, static_cast<const double*>(in2),
-                                          coef2, static_cast<double*>(out), accumulate ? 1 : 0);
+                                          coef2, static_cast<double*>(out), 1);
   } else {
     k_scatter<float><<<nb, blk, 0, st>>>(sh.n1, sh.n2, tl.ntx, tl.ne.as<int>(), tl.ne_cnt.as<int>(), tl.ptr.as<int>(), tl.pts.as<int>(), c->bx[dx].as<int>(),
                                          c->by[dy].as<int>(), c->wx[dx].as<float>(), c->wy[dy].as<float>(),
                                          c->wscale.as<float>(), c->nx.as<float>(), c->ny.as<float>(),
                                          static_cast<const float*>(in1), coef1, static_cast<const float*>(in2), coef2,
-                                         static_cast<float*>(out), accumulate ? 1 : 0);
+                                         static_cast<float*>(out), 1);
   }
   ILM_CHECK_LAUNCH();
   return ILM_OK;
