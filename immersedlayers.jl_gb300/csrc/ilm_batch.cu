@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <chrono>
 #include <memory>
+#include <mutex>
 #include <new>
 
 #include "ilm_internal.cuh"
@@ -325,11 +326,15 @@ struct ilm_batch_s {
   int precond = 0, bj_block = 0;
   bool params_dirty = false;
   DevBuf bj_blk, bj_start, bj_size, bj_off, bj_inv, bj_inv_lo, bj_tasks;
+  std::vector<BJBlockTask> bj_tasks_host;  // every block's inversion task
+  std::vector<char> bj_have;               // problems whose block inverses are formed
+  int bj_max_sz = 1;
   std::vector<int> bj_first;  // first block of each problem
   // learned banded preconditioner (mode 2): coefficients per packed point,
   // body segments as local indices
   int band_k = -1;
   DevBuf band, lseg_start, lseg_len;
+  DevBuf arena_learned;  // body segments of the learned preconditioner
   std::vector<char> has_band;  // problems whose kind a network was set for
   // deflation of the Dirichlet net-charge mode (set up before the first solve)
   bool defl_ready = false;
@@ -356,6 +361,10 @@ struct ilm_batch_s {
   DevBuf ref_in, ref_b, ref_x, ref_r, ref_y, ref_norm, dsoff;
   // host wall-clock of the set-up phases (ilm_batch_setup_times), ms
   std::vector<std::pair<const char*, double>> setup_ms;
+  // the set-up's device memory: geometry, work buffers and task tables are
+  // views into two arenas (one allocation and one host->device copy each)
+  DevBuf arena_geom, arena_tasks;
+  DevBuf px, py, ph;  // point coordinates (FP64) and per-problem h on the device
   ~ilm_batch_s() {
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
@@ -394,9 +403,33 @@ int up_typed(DevBuf& b, const std::vector<double>& v, int dtype) {
 
 int ensure_deflation(ilm_batch_s* b);
 
+// Block-Jacobi inverses (Gauss-Jordan, float-float) of the problems whose
+// preconditioner uses them: every problem under block-Jacobi, the problems
+// without a network under the learned preconditioner
+int ensure_block_inverses(ilm_batch_s* b) {
+  if (b->bj_block <= 0 || b->precond == 0) return ILM_OK;
+  std::vector<BJBlockTask> todo;
+  for (int p = 0; p < b->nprob; ++p) {
+    const bool need = b->precond == 1 || (b->precond == 2 && (b->has_band.empty() || !b->has_band[p]));
+    if (!need || b->bj_have[p]) continue;
+    for (int t = b->bj_first[p]; t < b->bj_first[p + 1]; ++t) todo.push_back(b->bj_tasks_host[t]);
+    b->bj_have[p] = 1;
+  }
+  if (todo.empty()) return ILM_OK;
+  const auto t0 = std::chrono::steady_clock::now();
+  DevBuf d;
+  ILM_TRY(up(d, todo));
+  ILM_TRY(launch_block_inverse(d.as<BJBlockTask>(), (int)todo.size(), b->bj_max_sz, nullptr));
+  ILM_CHECK_CUDA(cudaDeviceSynchronize());
+  b->setup_ms.emplace_back("block-Jacobi inverses",
+                           std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
+  return ILM_OK;
+}
+
 // CG parameter records for the current preconditioner, tolerance and limit
 int ensure_cg_params(ilm_batch_s* b, double tol, int maxiter) {
   if (tol == b->cg_tol && maxiter == b->cg_maxiter && !b->params_dirty) return ILM_OK;
+  ILM_TRY(ensure_block_inverses(b));
   ILM_TRY(ensure_deflation(b));
   b->params_dirty = false;
   std::vector<unsigned char> cg((size_t)b->nprob * cgff_params_size());
@@ -504,7 +537,7 @@ int ensure_deflation(ilm_batch_s* b) {
     // the best preconditioner set up so far: the learned band, else
     // block-Jacobi (each shortens this tight solve several times)
     const bool band = b->band_k >= 0 && !b->has_band.empty() && b->has_band[p];
-    const bool pre = !band && b->bj_block > 0;
+    const bool pre = !band && b->bj_block > 0 && !b->bj_have.empty() && b->bj_have[p];
     cgff_params_fill(dst, b->Shi.as<float>() + b->soff[p], b->Slo.as<float>() + b->soff[p], drhs.as<double>() + o,
                      b->defl_z.as<double>() + o, b->ds64.as<double>() + o, b->probs[p].npts, 20000, 1e-12,
                      its.as<int>() + p, rr.as<double>() + p, pre ? b->bj_blk.as<int>() + o : nullptr,
@@ -638,6 +671,86 @@ extern "C" {
 
 namespace {
 
+// learned-preconditioner features of the selected points (compacted order:
+// point i of the selection is point c2o[i] of the batch; its body is
+// [sst[i], sst[i] + sln[i]) in the selection)
+__global__ void k_batch_features(int Nsel, const int* __restrict__ c2o, const int* __restrict__ sst,
+                                 const int* __restrict__ sln, const double* __restrict__ x,
+                                 const double* __restrict__ y, const double* __restrict__ nx,
+                                 const double* __restrict__ ny, const double* __restrict__ ds,
+                                 const int* __restrict__ pt2prob, const double* __restrict__ hprob,
+                                 float* __restrict__ feat) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= Nsel) return;
+  const int s = sst[i], L = sln[i];
+  const int k = c2o[i], kp = c2o[s + (i - s + 1) % L], km = c2o[s + (i - s + L - 1) % L];
+  point_feature(x[k], y[k], nx[k], ny[k], ds[k], nx[kp], ny[kp], ds[kp], nx[km], ny[km], ds[km], hprob[pt2prob[k]],
+                feat + (size_t)i * 8);
+}
+
+// band[c2o[i]] = rows[i] (P coefficients per point)
+__global__ void k_scatter_rows(int Nsel, int P, const int* __restrict__ c2o, const float* __restrict__ rows,
+                               float* __restrict__ band) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < Nsel * P; e += gridDim.x * blockDim.x)
+    band[(size_t)c2o[e / P] * P + e % P] = rows[e];
+}
+
+// Many small device arrays carved out of one allocation; the ones with host
+// data are filled by one host->device copy through pinned staging memory
+// (kept by the library and grown on demand; one batch set-up at a time
+// uses it).
+std::mutex g_stage_mu;
+void* g_stage = nullptr;
+size_t g_stage_bytes = 0;
+
+struct ArenaBuilder {
+  struct Item {
+    DevBuf* dst;
+    size_t off, bytes;
+    const void* src;
+  };
+  std::vector<Item> items;
+  size_t total = 0, copy_end = 0;
+  void add(DevBuf* dst, size_t bytes, const void* src = nullptr) {
+    const size_t off = (total + 255) & ~(size_t)255;
+    items.push_back({dst, off, bytes, src});
+    total = off + std::max<size_t>(bytes, 1);
+    if (src && bytes) copy_end = off + bytes;
+  }
+  template <typename V>
+  void add(DevBuf* dst, const std::vector<V>& v) {
+    add(dst, v.size() * sizeof(V), v.data());
+  }
+  int commit(DevBuf& arena, cudaStream_t st) {
+    ILM_TRY(commit_layout(arena));
+    return commit_upload(arena, st);
+  }
+  // allocate the arena and point every buffer at its part
+  int commit_layout(DevBuf& arena) {
+    ILM_TRY(arena.alloc(std::max<size_t>(total, 256)));
+    for (const Item& it : items) it.dst->view(static_cast<unsigned char*>(arena.p) + it.off, it.bytes);
+    return ILM_OK;
+  }
+  // one copy of every buffer's host data (read now, so the host arrays may
+  // have been edited after commit_layout)
+  int commit_upload(DevBuf& arena, cudaStream_t st) {
+    if (!copy_end) return ILM_OK;
+    std::lock_guard<std::mutex> lk(g_stage_mu);
+    if (g_stage_bytes < copy_end) {
+      if (g_stage) cudaFreeHost(g_stage);
+      g_stage = nullptr;
+      g_stage_bytes = 0;
+      ILM_CHECK_CUDA(cudaMallocHost(&g_stage, copy_end));
+      g_stage_bytes = copy_end;
+    }
+    for (const Item& it : items)
+      if (it.src && it.bytes) memcpy(static_cast<unsigned char*>(g_stage) + it.off, it.src, it.bytes);
+    ILM_CHECK_CUDA(cudaMemcpyAsync(arena.p, g_stage, copy_end, cudaMemcpyHostToDevice, st));
+    ILM_CHECK_CUDA(cudaStreamSynchronize(st));
+    return ILM_OK;
+  }
+};
+
 // Set-up of a batch; without `build_schur` the Schur matrices are neither
 // allocated nor built (the FP64 refinement copy uses its parent's).
 int batch_create_impl(int nprob, const ilm_batch_problem_t* probs, const double* x, const double* y,
@@ -690,100 +803,213 @@ int batch_create_impl(int nprob, const ilm_batch_problem_t* probs, const double*
   B->hds.assign(ds, ds + Ptot);
 
   phase("validate and copy point data");
-  // ---- host set-up: DDF windows and tile lists, packed -------------------
-  std::vector<int> hbx[2], hby[2], hp2p(Ptot);
-  std::vector<double> hwx[2], hwy[2], hwsc(Ptot);
-  std::vector<int> htp[4], hts[4];
-  std::vector<size_t> tpo[4], tso[4];  // per problem offsets into packed tile arrays
+  // ---- geometry and work buffers: one arena; DDF windows and tile lists on
+  // the device -----------------------------------------------------------
+  const size_t e = es(dtype);
+  std::vector<int> hp2p(Ptot), hpoff(nprob + 1), hgrid(4 * (size_t)nprob);
+  std::vector<double> hh(nprob);
+  std::vector<int> tpo[4], tso[4];   // per problem offsets into the packed tile arrays
+  std::vector<int> ntx[4];            // tiles per row, per problem and class
+  int tp_tot[4] = {0, 0, 0, 0}, ts_tot[4] = {0, 0, 0, 0};
   for (int c = 0; c < 4; ++c) {
     tpo[c].assign(nprob, 0);
     tso[c].assign(nprob, 0);
+    ntx[c].assign(nprob, 0);
   }
-  std::vector<HostWindows> Wall(nprob);
-  parallel_for(nprob, [&](int p) {  // DDF windows and tile lists of every problem, in parallel
-    const ilm_batch_problem_t& P = probs[p];
-    ilm_grid_s g{P.nx, P.ny, P.h, P.i0x, P.i0y};
-    host_windows(g, ddf, P.npts, x + B->poff[p], y + B->poff[p], &Wall[p]);
-  });
-  phase("DDF windows and tile lists (host)");
   for (int p = 0; p < nprob; ++p) {
     const ilm_batch_problem_t& P = probs[p];
-    const size_t o = B->poff[p];
-    HostWindows& W = Wall[p];
-    for (int d = 0; d < 2; ++d) {
-      hbx[d].insert(hbx[d].end(), W.bx[d].begin(), W.bx[d].end());
-      hby[d].insert(hby[d].end(), W.by[d].begin(), W.by[d].end());
-      hwx[d].insert(hwx[d].end(), W.wx[d].begin(), W.wx[d].end());
-      hwy[d].insert(hwy[d].end(), W.wy[d].begin(), W.wy[d].end());
-    }
-    for (int k = 0; k < P.npts; ++k) {
-      hp2p[o + k] = p;
-      hwsc[o + k] = ds[o + k] / (P.h * P.h);
-    }
+    hpoff[p] = (int)B->poff[p];
+    for (int k = 0; k < P.npts; ++k) hp2p[B->poff[p] + k] = p;
+    hgrid[4 * p] = P.nx;
+    hgrid[4 * p + 1] = P.ny;
+    hgrid[4 * p + 2] = P.i0x;
+    hgrid[4 * p + 3] = P.i0y;
+    hh[p] = P.h;
+    const ilm_grid_s g{P.nx, P.ny, P.h, P.i0x, P.i0y};
     for (int c = 0; c < 4; ++c) {
-      tpo[c][p] = htp[c].size();
-      tso[c][p] = hts[c].size();
-      htp[c].insert(htp[c].end(), W.tptr[c].begin(), W.tptr[c].end());
-      hts[c].insert(hts[c].end(), W.tpts[c].begin(), W.tpts[c].end());
+      const Shape2 sh = g.shape(c);
+      ntx[c][p] = (sh.n1 + TILE_X - 1) / TILE_X;
+      const int nt = ntx[c][p] * ((sh.n2 + TILE_Y - 1) / TILE_Y);
+      tpo[c][p] = tp_tot[c];
+      tp_tot[c] += nt + 1;
+      tso[c][p] = ts_tot[c];
+      ts_tot[c] += 4 * P.npts;   // a 4 x 4 window touches at most 2 x 2 tiles
     }
   }
-  std::vector<double> hnx(nrmx, nrmx + Ptot), hny(nrmy, nrmy + Ptot), hds(ds, ds + Ptot);
+  hpoff[nprob] = Ptot;
+  // Schur complement descriptors (float-float LGF point-point sums)
+  std::vector<SchurProbDev> sp(nprob);
+  {
+    int tiles = 0;
+    for (int p = 0; p < nprob; ++p) {
+      sp[p].kind = probs[p].kind == 0 ? ILM_SCHUR_RTLINVR : ILM_SCHUR_CLINVCT;
+      sp[p].n = probs[p].npts;
+      sp[p].poff = (int)B->poff[p];
+      sp[p].tile0 = tiles;
+      const int nt = (probs[p].npts + 15) / 16;
+      tiles += nt * (nt + 1) / 2;  // upper triangle (the pair sums are symmetric)
+      sp[p].soff = B->soff[p];
+      sp[p].invh = 1.0 / probs[p].h;
+    }
+    B->schur_tiles = tiles;
+    B->schur_host = sp;
+  }
+  // set-up streams (non-blocking: independent of the legacy stream): the
+  // geometry and task tables on sg, the Schur build on ss, overlapping the
+  // host's task building
+  struct Streams {
+    cudaStream_t g = nullptr, s = nullptr;
+    ~Streams() {
+      if (g) cudaStreamDestroy(g);
+      if (s) cudaStreamDestroy(s);
+    }
+  } SS;
+  ILM_CHECK_CUDA(cudaStreamCreateWithFlags(&SS.g, cudaStreamNonBlocking));
+  ILM_CHECK_CUDA(cudaStreamCreateWithFlags(&SS.s, cudaStreamNonBlocking));
+  cudaStream_t sg = SS.g, ss = SS.s;
+  DevBuf d_in[5], d_poff, d_grid, d_tpo[4], d_tso[4], d_cnt;
+  {
+    ArenaBuilder A;
+    const double* src[5] = {x, y, nrmx, nrmy, ds};
+    DevBuf* dst[5] = {&B->px, &B->py, &d_in[2], &d_in[3], &d_in[4]};
+    for (int q = 0; q < 5; ++q) A.add(dst[q], (size_t)Ptot * 8, src[q]);
+    A.add(&B->pt2prob, hp2p);
+    A.add(&d_poff, hpoff);
+    A.add(&d_grid, hgrid);
+    A.add(&B->ph, hh);
+    A.add(&B->schurP, sp);
+    for (int c = 0; c < 4; ++c) {
+      A.add(&d_tpo[c], tpo[c]);
+      A.add(&d_tso[c], tso[c]);
+    }
+    for (int d = 0; d < 2; ++d) {
+      A.add(&B->bx[d], (size_t)Ptot * 4);
+      A.add(&B->by[d], (size_t)Ptot * 4);
+      A.add(&B->wx[d], (size_t)Ptot * NTAP * e);
+      A.add(&B->wy[d], (size_t)Ptot * NTAP * e);
+      A.add(&B->wx64[d], (size_t)Ptot * NTAP * 8);
+      A.add(&B->wy64[d], (size_t)Ptot * NTAP * 8);
+    }
+    A.add(&B->nx, (size_t)Ptot * e);
+    A.add(&B->ny, (size_t)Ptot * e);
+    A.add(&B->wsc, (size_t)Ptot * e);
+    A.add(&B->nx64, (size_t)Ptot * 8);
+    A.add(&B->ny64, (size_t)Ptot * 8);
+    A.add(&B->ds64, (size_t)Ptot * 8);
+    int cnt_tot = 0;
+    for (int c = 0; c < 4; ++c) {
+      A.add(&B->tptr[c], (size_t)tp_tot[c] * 4);
+      A.add(&B->tpts[c], (size_t)std::max(ts_tot[c], 1) * 4);
+      cnt_tot += tp_tot[c];
+    }
+    A.add(&d_cnt, (size_t)cnt_tot * 4);
+    // work buffers
+    A.add(&B->fstar, B->ftot * e);
+    A.add(&B->corr, B->ftot * e);
+    A.add(&B->edges, B->etot * e);
+    A.add(&B->jump, (size_t)Ptot * e);
+    A.add(&B->avg, (size_t)Ptot * e);
+    A.add(&B->g, (size_t)Ptot * e);
+    A.add(&B->s, (size_t)Ptot * e);
+    A.add(&B->rhs64, (size_t)Ptot * 8);
+    A.add(&B->x64, (size_t)Ptot * 8);
+    if (build_schur) {
+      A.add(&B->Shi, std::max<size_t>(B->stot, 1) * 4);
+      A.add(&B->Slo, std::max<size_t>(B->stot, 1) * 4);
+      A.add(&B->F, (size_t)Ptot * functional_size());
+    }
+    A.add(&B->iters, (size_t)nprob * sizeof(int));
+    A.add(&B->relres, (size_t)nprob * sizeof(double));
+    A.add(&B->counter, sizeof(int));
+    ILM_TRY(A.commit(B->arena_geom, sg));
+    phase("upload points, allocate buffers (one arena)");
+    BatchGeomDev G;
+    memset(&G, 0, sizeof(G));
+    G.x = B->px.as<double>();
+    G.y = B->py.as<double>();
+    G.nx = d_in[2].as<double>();
+    G.ny = d_in[3].as<double>();
+    G.ds = d_in[4].as<double>();
+    G.pt2prob = B->pt2prob.as<int>();
+    G.poff = d_poff.as<int>();
+    G.grid = d_grid.as<int>();
+    G.h = B->ph.as<double>();
+    for (int d = 0; d < 2; ++d) {
+      G.bx[d] = B->bx[d].as<int>();
+      G.by[d] = B->by[d].as<int>();
+      G.wx64[d] = B->wx64[d].as<double>();
+      G.wy64[d] = B->wy64[d].as<double>();
+      G.wx[d] = B->wx[d].p;
+      G.wy[d] = B->wy[d].p;
+    }
+    G.nxo = B->nx.p;
+    G.nyo = B->ny.p;
+    G.wsc = B->wsc.p;
+    G.nx64 = B->nx64.as<double>();
+    G.ny64 = B->ny64.as<double>();
+    G.ds64 = B->ds64.as<double>();
+    int co = 0;
+    for (int c = 0; c < 4; ++c) {
+      G.tptr[c] = B->tptr[c].as<int>();
+      G.tpts[c] = B->tpts[c].as<int>();
+      G.tp_off[c] = d_tpo[c].as<int>();
+      G.ts_off[c] = d_tso[c].as<int>();
+      G.cnt_off[c] = co;
+      co += tp_tot[c];
+    }
+    G.cnt = d_cnt.as<int>();
+    G.cnt_total = co;
+    ILM_TRY(batch_windows_and_tiles(nprob, Ptot, G, ddf, dtype, 1, sg));
+    if (build_schur) {
+      cudaEvent_t geo_done = nullptr;
+      ILM_CHECK_CUDA(cudaEventCreateWithFlags(&geo_done, cudaEventDisableTiming));
+      const cudaError_t e1 = cudaEventRecord(geo_done, sg);
+      const cudaError_t e2 = e1 == cudaSuccess ? cudaStreamWaitEvent(ss, geo_done, 0) : e1;
+      cudaEventDestroy(geo_done);
+      ILM_CHECK_CUDA(e2);
+      // the row padding of every matrix stays zero
+      ILM_CHECK_CUDA(cudaMemsetAsync(B->Shi.p, 0, std::max<size_t>(B->stot, 1) * 4, ss));
+      ILM_CHECK_CUDA(cudaMemsetAsync(B->Slo.p, 0, std::max<size_t>(B->stot, 1) * 4, ss));
+      BatchWin BW;
+      for (int d = 0; d < 2; ++d) {
+        BW.bx[d] = B->bx[d].as<int>();
+        BW.by[d] = B->by[d].as<int>();
+        BW.wx64[d] = B->wx64[d].as<double>();
+        BW.wy64[d] = B->wy64[d].as<double>();
+      }
+      BW.nx64 = B->nx64.as<double>();
+      BW.ny64 = B->ny64.as<double>();
+      ILM_TRY(schur_build_batched(nprob, B->schurP.as<SchurProbDev>(), B->schur_tiles, Ptot, B->pt2prob.as<int>(),
+                                  BW, B->ds64.as<double>(), static_cast<Functional*>(B->F.p), B->Shi.as<float>(),
+                                  B->Slo.as<float>(), B->max_grid, ss));
+    }
+  }
+  // the windows' base indices and the tile pointers, for the boxes and task
+  // tables built on the host
+  std::vector<int> hbx[2], hby[2], htp[4];
   for (int d = 0; d < 2; ++d) {
-    ILM_TRY(up(B->bx[d], hbx[d]));
-    ILM_TRY(up(B->by[d], hby[d]));
-    ILM_TRY(up_typed(B->wx[d], hwx[d], dtype));
-    ILM_TRY(up_typed(B->wy[d], hwy[d], dtype));
-    ILM_TRY(up_typed(B->wx64[d], hwx[d], ILM_F64));
-    ILM_TRY(up_typed(B->wy64[d], hwy[d], ILM_F64));
+    hbx[d].resize(Ptot);
+    hby[d].resize(Ptot);
+    ILM_CHECK_CUDA(cudaMemcpyAsync(hbx[d].data(), B->bx[d].p, (size_t)Ptot * 4, cudaMemcpyDeviceToHost, sg));
+    ILM_CHECK_CUDA(cudaMemcpyAsync(hby[d].data(), B->by[d].p, (size_t)Ptot * 4, cudaMemcpyDeviceToHost, sg));
   }
-  ILM_TRY(up_typed(B->nx, hnx, dtype));
-  ILM_TRY(up_typed(B->ny, hny, dtype));
-  ILM_TRY(up_typed(B->wsc, hwsc, dtype));
-  ILM_TRY(up(B->nx64, hnx));
-  ILM_TRY(up(B->ny64, hny));
-  ILM_TRY(up(B->ds64, hds));
-  ILM_TRY(up(B->pt2prob, hp2p));
   for (int c = 0; c < 4; ++c) {
-    ILM_TRY(up(B->tptr[c], htp[c]));
-    ILM_TRY(up(B->tpts[c], hts[c]));
+    htp[c].resize(tp_tot[c]);
+    ILM_CHECK_CUDA(cudaMemcpyAsync(htp[c].data(), B->tptr[c].p, (size_t)tp_tot[c] * 4, cudaMemcpyDeviceToHost, sg));
   }
-
-  phase("pack and upload windows and tile lists");
-  // ---- device work buffers ----------------------------------------------
-  const size_t e = es(dtype);
-  ILM_TRY(B->fstar.alloc(B->ftot * e));
-  ILM_TRY(B->corr.alloc(B->ftot * e));
-  ILM_TRY(B->edges.alloc(B->etot * e));
-  ILM_TRY(B->jump.alloc((size_t)Ptot * e));
-  ILM_TRY(B->avg.alloc((size_t)Ptot * e));
-  ILM_TRY(B->g.alloc((size_t)Ptot * e));
-  ILM_TRY(B->s.alloc((size_t)Ptot * e));
-  ILM_TRY(B->rhs64.alloc((size_t)Ptot * 8));
-  ILM_TRY(B->x64.alloc((size_t)Ptot * 8));
-  if (build_schur) {
-    ILM_TRY(B->Shi.alloc(std::max<size_t>(B->stot, 1) * 4));
-    ILM_TRY(B->Slo.alloc(std::max<size_t>(B->stot, 1) * 4));
-    // the row padding of every matrix stays zero
-    ILM_CHECK_CUDA(cudaMemset(B->Shi.p, 0, std::max<size_t>(B->stot, 1) * 4));
-    ILM_CHECK_CUDA(cudaMemset(B->Slo.p, 0, std::max<size_t>(B->stot, 1) * 4));
-    ILM_TRY(B->F.alloc((size_t)Ptot * functional_size()));
-  }
-  ILM_TRY(B->iters.alloc((size_t)nprob * sizeof(int)));
-  ILM_TRY(B->relres.alloc((size_t)nprob * sizeof(double)));
+  ILM_CHECK_CUDA(cudaStreamSynchronize(sg));
+  phase("DDF windows and tile lists (device) + read-back");
+  std::vector<int> ord(nprob);
   {
     // CG work queue: largest problems first (cost ~ npts^2 * sqrt(npts))
-    std::vector<int> ord(nprob);
     for (int p = 0; p < nprob; ++p) ord[p] = p;
     std::stable_sort(ord.begin(), ord.end(), [&](int a, int c) {
       const double ca = pow((double)probs[a].npts, 2.5), cc = pow((double)probs[c].npts, 2.5);
       return ca > cc;
     });
-    ILM_TRY(up(B->order, ord));
-    ILM_TRY(B->counter.alloc(sizeof(int)));
     B->nclusters = cg_cluster_count(nprob, B->maxN);
   }
 
-  phase("allocate work buffers");
   // FFT convolution jobs (fstar and corr in place); one work area per problem
   std::vector<size_t> woff(nprob + 1, 0);
   std::vector<int> P1(nprob), P2(nprob);
@@ -800,14 +1026,14 @@ int batch_create_impl(int nprob, const ilm_batch_problem_t* probs, const double*
   // divergences write only this box and the FFT row pass reads only it.
   std::vector<std::array<int, 4>> box(nprob);
   for (int p = 0; p < nprob; ++p) {
-    const HostWindows& W = Wall[p];
+    const size_t o = B->poff[p];
     int xmin = INT_MAX, xmax = INT_MIN, ymin = INT_MAX, ymax = INT_MIN;
     for (int k = 0; k < probs[p].npts; ++k)
       for (int d = 0; d < 2; ++d) {
-        xmin = std::min(xmin, W.bx[d][k]);
-        xmax = std::max(xmax, W.bx[d][k] + NTAP - 1);
-        ymin = std::min(ymin, W.by[d][k]);
-        ymax = std::max(ymax, W.by[d][k] + NTAP - 1);
+        xmin = std::min(xmin, hbx[d][o + k]);
+        xmax = std::max(xmax, hbx[d][o + k] + NTAP - 1);
+        ymin = std::min(ymin, hby[d][o + k]);
+        ymax = std::max(ymax, hby[d][o + k] + NTAP - 1);
       }
     const int n1 = probs[p].nx - 1, n2 = probs[p].ny - 1;
     int ca = std::max(0, xmin - 3), cb = std::min(n1, xmax + 4);
@@ -852,16 +1078,19 @@ int batch_create_impl(int nprob, const ilm_batch_problem_t* probs, const double*
   ILM_TRY(conv_jobs_finalize(jobsA, dtype, &B->convL));
   ILM_TRY(conv_jobs_finalize(jobsB, dtype, &B->convL));
   ILM_TRY(conv_jobs_finalize(jobsC, dtype, &B->convL));
+  // every task table goes to the device in one arena (laid out below, the
+  // device addresses resolved, then one copy)
+  ArenaBuilder TA;
   if (B->convL.fast) {  // CTA -> job maps (the two job tables share their geometry)
-    ILM_TRY(up(B->mconv[0], B->convL.mrows));
-    ILM_TRY(up(B->mconv[1], B->convL.mcols));
-    ILM_TRY(up(B->mconv[2], B->convL.mirows));
-    for (int k = 0; k < 3; ++k) B->convL.dmap[k] = B->mconv[k].as<int>();
+    TA.add(&B->mconv[0], B->convL.mrows);
+    TA.add(&B->mconv[1], B->convL.mcols);
+    TA.add(&B->mconv[2], B->convL.mirows);
   }
   B->n_conv = nprob;
-  ILM_TRY(up(B->convA, jobsA));
-  ILM_TRY(up(B->convB, jobsB));
-  ILM_TRY(up(B->convC, jobsC));
+  TA.add(&B->convA, jobsA);
+  TA.add(&B->convB, jobsB);
+  TA.add(&B->convC, jobsC);
+  TA.add(&B->order, ord);
 
   phase("source boxes and convolution jobs");
   // ---- tasks ---------------------------------------------------------------
@@ -876,7 +1105,7 @@ int batch_create_impl(int nprob, const ilm_batch_problem_t* probs, const double*
     const size_t o = B->poff[p];
     T.n1 = sh.n1;
     T.n2 = sh.n2;
-    T.ntx = Wall[p].ntx[pc];
+    T.ntx = ntx[pc][p];
     // cells written: the source box (faces: one more column / row, which the
     // divergence of the box reads)
     const int ext = pc == PC_P ? 0 : 1;
@@ -893,7 +1122,7 @@ int batch_create_impl(int nprob, const ilm_batch_problem_t* probs, const double*
     T.fill0 = fills;
     fills += yb - ya;
     // occupied tiles of the box (ids into the problem's tile grid), packed
-    const std::vector<int>& tp = Wall[p].tptr[pc];
+    const int* tp = htp[pc].data() + tpo[pc][p];
     T.pad_ = (int)nelist.size();  // offset into the packed list, resolved after upload
     for (int ty = T.ty0; ty < T.ty0 + ntyb; ++ty)
       for (int tx = T.tx0; tx < T.tx0 + T.ntxb; ++tx) {
@@ -1010,11 +1239,12 @@ int batch_create_impl(int nprob, const ilm_batch_problem_t* probs, const double*
   B->n_divB = (int)dB.size();
   B->blk_divB = bdB;
   B->n_gathA = (int)hA.size();
-  ILM_TRY(up(B->scat_ne, nelist));
-  for (auto& T : sA) T.ne = B->scat_ne.as<int>() + T.pad_;
-  for (auto& T : sB) T.ne = B->scat_ne.as<int>() + T.pad_;
+  TA.add(&B->scat_ne, nelist);
   B->blk_fillA = fillA;
   B->blk_fillB = fillB;
+  std::vector<int> maps[7];
+  std::vector<BScatterTask> sB2;
+  std::vector<BStencilTask> dB2;
   {
     // block -> task maps
     auto mk_scat = [&](const std::vector<BScatterTask>& v, int nblk, bool fill) {
@@ -1034,17 +1264,19 @@ int batch_create_impl(int nprob, const ilm_batch_problem_t* probs, const double*
       }
       return m;
     };
-    ILM_TRY(up(B->mfillA, mk_scat(sA, fillA, true)));
-    ILM_TRY(up(B->mscatA, mk_scat(sA, tA, false)));
-    ILM_TRY(up(B->mfillB, mk_scat(sB, fillB, true)));
-    ILM_TRY(up(B->mscatB, mk_scat(sB, tB, false)));
-    ILM_TRY(up(B->mdivA, mk_div(dA, bdA)));
-    ILM_TRY(up(B->mdivB, mk_div(dB, bdB)));
+    maps[0] = mk_scat(sA, fillA, true);
+    maps[1] = mk_scat(sA, tA, false);
+    maps[2] = mk_scat(sB, fillB, true);
+    maps[3] = mk_scat(sB, tB, false);
+    maps[4] = mk_div(dA, bdA);
+    maps[5] = mk_div(dB, bdB);
+    DevBuf* dst[6] = {&B->mfillA, &B->mscatA, &B->mfillB, &B->mscatB, &B->mdivA, &B->mdivB};
+    for (int k = 0; k < 6; ++k) TA.add(dst[k], maps[k]);
   }
-  ILM_TRY(up(B->scatA, sA));
-  ILM_TRY(up(B->scatB, sB));
-  ILM_TRY(up(B->divA, dA));
-  ILM_TRY(up(B->divB, dB));
+  TA.add(&B->scatA, sA);
+  TA.add(&B->scatB, sB);
+  TA.add(&B->divA, dA);
+  TA.add(&B->divB, dB);
   {
     // stage-B tasks of the rhs-operator path: the single layer (Dirichlet
     // R s) and the divergence of the double layer (Neumann D_s [phi]) add
@@ -1059,7 +1291,7 @@ int batch_create_impl(int nprob, const ilm_batch_problem_t* probs, const double*
       return (void*)(static_cast<unsigned char*>(B->fstar.p) + (static_cast<unsigned char*>(q) -
                                                                  static_cast<unsigned char*>(B->corr.p)));
     };
-    std::vector<BScatterTask> sB2 = sB;
+    sB2 = sB;
     int fill2 = 0;
     for (auto& T : sB2) {
       if (in_corr(T.out)) {
@@ -1071,54 +1303,34 @@ int batch_create_impl(int nprob, const ilm_batch_problem_t* probs, const double*
         fill2 += T.yb - T.ya;
       }
     }
-    std::vector<int> m2(std::max(fill2, 1), 0);
+    std::vector<int>& m2 = maps[6];
+    m2.assign(std::max(fill2, 1), 0);
     for (size_t t = 0; t < sB2.size(); ++t)
       if (!sB2[t].accum)
         for (int k = 0; k < sB2[t].yb - sB2[t].ya; ++k) m2[sB2[t].fill0 + k] = (int)t;
-    std::vector<BStencilTask> dB2 = dB;
+    dB2 = dB;
     for (auto& T : dB2) {
       T.out = to_fstar(T.out);
       T.accum = 1;
     }
     B->blk_fillB2 = fill2;
-    ILM_TRY(up(B->mfillB2, m2));
-    ILM_TRY(up(B->scatB2, sB2));
-    ILM_TRY(up(B->divB2, dB2));
+    TA.add(&B->mfillB2, m2);
+    TA.add(&B->scatB2, sB2);
+    TA.add(&B->divB2, dB2);
   }
-  ILM_TRY(up(B->gathA, hA));
+  TA.add(&B->gathA, hA);
+  // lay out the arena, resolve the device addresses the tables hold, copy
+  ILM_TRY(TA.commit_layout(B->arena_tasks));
+  for (auto* v : {&sA, &sB, &sB2})
+    for (auto& T : *v) T.ne = B->scat_ne.as<int>() + T.pad_;
+  if (B->convL.fast)
+    for (int k = 0; k < 3; ++k) B->convL.dmap[k] = B->mconv[k].as<int>();
+  ILM_TRY(TA.commit_upload(B->arena_tasks, sg));
 
   phase("stage tasks (build and upload)");
-  // ---- Schur complements (float-float, LGF point-point sums) ----------------
-  std::vector<SchurProbDev> sp(nprob);
-  int tiles = 0;
-  for (int p = 0; p < nprob; ++p) {
-    sp[p].kind = probs[p].kind == 0 ? ILM_SCHUR_RTLINVR : ILM_SCHUR_CLINVCT;
-    sp[p].n = probs[p].npts;
-    sp[p].poff = (int)B->poff[p];
-    sp[p].tile0 = tiles;
-    const int nt = (probs[p].npts + 15) / 16;
-    tiles += nt * (nt + 1) / 2;  // upper triangle (the pair sums are symmetric)
-    sp[p].soff = B->soff[p];
-    sp[p].invh = 1.0 / probs[p].h;
-  }
-  B->schur_tiles = tiles;
-  ILM_TRY(up(B->schurP, sp));
-  B->schur_host = sp;
-  BatchWin BW;
-  for (int d = 0; d < 2; ++d) {
-    BW.bx[d] = B->bx[d].as<int>();
-    BW.by[d] = B->by[d].as<int>();
-    BW.wx64[d] = B->wx64[d].as<double>();
-    BW.wy64[d] = B->wy64[d].as<double>();
-  }
-  BW.nx64 = B->nx64.as<double>();
-  BW.ny64 = B->ny64.as<double>();
-  if (build_schur)
-    ILM_TRY(schur_build_batched(nprob, B->schurP.as<SchurProbDev>(), tiles, Ptot, B->pt2prob.as<int>(), BW,
-                                B->ds64.as<double>(), static_cast<Functional*>(B->F.p), B->Shi.as<float>(),
-                                B->Slo.as<float>(), B->max_grid, nullptr));
-  ILM_CHECK_CUDA(cudaDeviceSynchronize());
-  phase("Schur complements (device, float-float pair sums)");
+  ILM_CHECK_CUDA(cudaStreamSynchronize(ss));
+  ILM_CHECK_CUDA(cudaStreamSynchronize(sg));
+  phase("Schur complements (device, overlapping the host's task tables)");
   *out = guard.release();
   return ILM_OK;
 }
@@ -1314,10 +1526,11 @@ int ilm_batch_set_precond(ilm_batch_t b, int mode, int block_size) {
   if (mode == 1) {
     ILM_REQUIRE(block_size >= 4 && block_size <= 72, "batch: block size %d outside [4, 72]", block_size);
     if (b->bj_block != block_size) {
-      const auto t0 = std::chrono::steady_clock::now();
-      // blocks of ~block_size consecutive points (at most 1.5 x block_size)
+      // blocks of ~block_size consecutive points (at most 1.5 x block_size);
+      // their inverses are formed by the next solve, for the problems whose
+      // preconditioner uses them (ensure_block_inverses)
       std::vector<int> blk(b->Ptot), bst, bsz, boff;
-      std::vector<BJBlockTask> tasks;
+      b->bj_tasks_host.clear();
       b->bj_first.assign(b->nprob + 1, 0);
       size_t total = 0;
       int max_sz = 1;
@@ -1339,7 +1552,7 @@ int ilm_batch_set_precond(ilm_batch_t b, int mode, int block_size) {
           T.s = s;
           T.sz = e - s;
           T.out_hi = T.out_lo = nullptr;  // set after allocation
-          tasks.push_back(T);
+          b->bj_tasks_host.push_back(T);
           total += (size_t)(e - s) * (e - s);
         }
       }
@@ -1347,19 +1560,16 @@ int ilm_batch_set_precond(ilm_batch_t b, int mode, int block_size) {
       ILM_REQUIRE(max_sz <= 144, "batch: preconditioner block of %d points", max_sz);
       ILM_TRY(b->bj_inv.alloc(std::max<size_t>(total, 1) * sizeof(float)));
       ILM_TRY(b->bj_inv_lo.alloc(std::max<size_t>(total, 1) * sizeof(float)));
-      for (size_t t = 0; t < tasks.size(); ++t) {
-        tasks[t].out_hi = b->bj_inv.as<float>() + boff[t];
-        tasks[t].out_lo = b->bj_inv_lo.as<float>() + boff[t];
+      for (size_t t = 0; t < b->bj_tasks_host.size(); ++t) {
+        b->bj_tasks_host[t].out_hi = b->bj_inv.as<float>() + boff[t];
+        b->bj_tasks_host[t].out_lo = b->bj_inv_lo.as<float>() + boff[t];
       }
       ILM_TRY(up(b->bj_blk, blk));
       ILM_TRY(up(b->bj_start, bst));
       ILM_TRY(up(b->bj_size, bsz));
       ILM_TRY(up(b->bj_off, boff));
-      ILM_TRY(up(b->bj_tasks, tasks));
-      ILM_TRY(launch_block_inverse(b->bj_tasks.as<BJBlockTask>(), (int)tasks.size(), max_sz, nullptr));
-      ILM_CHECK_CUDA(cudaDeviceSynchronize());
-      b->setup_ms.emplace_back("block-Jacobi inverses",
-                               std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
+      b->bj_max_sz = max_sz;
+      b->bj_have.assign(b->nprob, 0);
       b->bj_block = block_size;
     }
   }
@@ -1649,47 +1859,52 @@ int ilm_batch_set_learned(ilm_batch_t b, ilm_net_t net, int kind_mask, const int
     b->setup_ms.emplace_back(name, std::chrono::duration<double, std::milli>(now - clk).count());
     clk = now;
   };
-  std::vector<float> feat((size_t)Ptot * 8);
-  std::vector<int> fst(b->nprob, ILM_OK);
-  parallel_for(b->nprob, [&](int p) {  // point features of every problem, in parallel
-    const int o = (int)b->poff[p], n = b->probs[p].npts;
-    std::vector<int> s0(n), l0(n);
-    for (int k = 0; k < n; ++k) {
-      s0[k] = ls[o + k];
-      l0[k] = ll[o + k];
-    }
-    fst[p] = ilm_point_features(n, b->hx.data() + o, b->hy.data() + o, b->hnx.data() + o, b->hny.data() + o,
-                                b->hds.data() + o, s0.data(), l0.data(), b->probs[p].h, feat.data() + (size_t)o * 8);
-  });
-  for (int p = 0; p < b->nprob; ++p) ILM_TRY(fst[p]);
-  phase("learned: point features (host)");
-  DevBuf dfeat, das, dll;
-  ILM_TRY(up(dfeat, feat));
-  ILM_TRY(up(das, as));
-  ILM_TRY(up(dll, ll));
-  ILM_TRY(up(b->lseg_start, ls));
-  ILM_TRY(up(b->lseg_len, ll));
-  if (b->band_k < 0) {
-    ILM_TRY(b->band.alloc((size_t)Ptot * P * sizeof(float)));
-    b->has_band.assign(b->nprob, 0);
-  }
-  DevBuf tmp, dsel;
-  ILM_TRY(tmp.alloc((size_t)Ptot * P * sizeof(float)));
-  phase("learned: uploads");
-  ILM_TRY(net_forward_packed(net, Ptot, dfeat.as<float>(), das.as<int>(), dll.as<int>(), tmp.as<float>(), nullptr));
-  // this network's band for the points of the problems of the selected kinds
-  std::vector<unsigned char> sel(Ptot, 0);
+  // the points of the problems of the selected kinds, compacted, with their
+  // body segments in compacted indices
+  std::vector<int> c2o, sst_c, sln_c;
+  c2o.reserve(Ptot);
+  if (b->band_k < 0) b->has_band.assign(b->nprob, 0);
   for (int p = 0; p < b->nprob; ++p) {
     if (!(kind_mask & (1 << b->probs[p].kind))) continue;
-    for (size_t k = b->poff[p]; k < b->poff[p + 1]; ++k) sel[k] = 1;
     b->has_band[p] = 1;
+    const int o = (int)b->poff[p], base = (int)c2o.size();
+    for (int k = 0; k < b->probs[p].npts; ++k) {
+      c2o.push_back(o + k);
+      sst_c.push_back(base + (as[o + k] - o));
+      sln_c.push_back(ll[o + k]);
+    }
   }
-  ILM_TRY(up(dsel, sel));
-  k_select_rows<<<std::min(4096, (Ptot * P + 255) / 256), 256>>>(Ptot, P, dsel.as<unsigned char>(), tmp.as<float>(),
-                                                                  b->band.as<float>());
-  ILM_CHECK_LAUNCH();
+  const int Nsel = (int)c2o.size();
+  DevBuf tmp_arena, d_c2o, d_sst, d_sln, dfeat, tmp;
+  {
+    ArenaBuilder A;  // this call's temporaries
+    A.add(&d_c2o, c2o);
+    A.add(&d_sst, sst_c);
+    A.add(&d_sln, sln_c);
+    A.add(&dfeat, (size_t)std::max(Nsel, 1) * 8 * sizeof(float));
+    A.add(&tmp, (size_t)std::max(Nsel, 1) * P * sizeof(float));
+    ILM_TRY(A.commit(tmp_arena, nullptr));
+    ArenaBuilder S;  // the body segments the CG reads (the same for every call)
+    S.add(&b->lseg_start, ls);
+    S.add(&b->lseg_len, ll);
+    ILM_TRY(S.commit(b->arena_learned, nullptr));
+    if (b->band_k < 0) ILM_TRY(b->band.alloc((size_t)std::max(Ptot, 1) * P * sizeof(float)));
+  }
+  phase("learned: segments (host) and upload");
+  if (Nsel > 0) {
+    k_batch_features<<<(Nsel + 255) / 256, 256>>>(Nsel, d_c2o.as<int>(), d_sst.as<int>(), d_sln.as<int>(),
+                                                  b->px.as<double>(), b->py.as<double>(), b->nx64.as<double>(),
+                                                  b->ny64.as<double>(), b->ds64.as<double>(), b->pt2prob.as<int>(),
+                                                  b->ph.as<double>(), dfeat.as<float>());
+    ILM_CHECK_LAUNCH();
+    ILM_TRY(net_forward_packed(net, Nsel, dfeat.as<float>(), d_sst.as<int>(), d_sln.as<int>(), tmp.as<float>(),
+                               nullptr));
+    k_scatter_rows<<<std::min(4096, (Nsel * P + 255) / 256), 256>>>(Nsel, P, d_c2o.as<int>(), tmp.as<float>(),
+                                                                     b->band.as<float>());
+    ILM_CHECK_LAUNCH();
+  }
   ILM_CHECK_CUDA(cudaDeviceSynchronize());
-  phase("learned: network inference (device)");
+  phase("learned: features and network inference (device, selected problems)");
   b->band_k = K;
   b->precond = 2;
   b->params_dirty = true;

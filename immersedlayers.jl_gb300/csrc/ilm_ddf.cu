@@ -625,6 +625,163 @@ __global__ void k_tile_sort(int nt, const int* __restrict__ ptr, int* __restrict
   }
 }
 
+// ---------------------------------------------------------------------------
+// Batched windows and tile lists (ilm_batch_create): every point of every
+// problem at once, the same rules as host_windows / k_rebin_points
+// ---------------------------------------------------------------------------
+struct BGrid {
+  int nx, ny, i0x, i0y;
+};
+
+__device__ __forceinline__ BGrid bgrid(const BatchGeomDev& G, int p) {
+  return BGrid{G.grid[4 * p], G.grid[4 * p + 1], G.grid[4 * p + 2], G.grid[4 * p + 3]};
+}
+
+__device__ __forceinline__ void bshape(const BGrid& g, int pc, int* n1, int* n2) {
+  const int dx = (pc == PC_D || pc == PC_U) ? 1 : 0, dy = (pc == PC_D || pc == PC_V) ? 1 : 0;
+  *n1 = dx ? g.nx : g.nx - 1;
+  *n2 = dy ? g.ny : g.ny - 1;
+}
+
+template <typename T>
+__global__ void k_bwindows(int Ptot, BatchGeomDev G, int ddf, int grid_scaling) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= Ptot) return;
+  const int p = G.pt2prob[k];
+  const BGrid g = bgrid(G, p);
+  const double h = G.h[p];
+  const double xk = G.x[k], yk = G.y[k];
+  for (int dual = 0; dual < 2; ++dual) {
+    const double off = dual ? 0.5 : 1.0;
+    const double rx = xk / h + g.i0x - off;
+    const double ry = yk / h + g.i0y - off;
+    double w[NTAP];
+    int b;
+    ddf_window(ddf, rx, &b, w);
+    G.bx[dual][k] = b;
+    for (int t = 0; t < NTAP; ++t) {
+      G.wx64[dual][(size_t)k * NTAP + t] = w[t];
+      static_cast<T*>(G.wx[dual])[(size_t)k * NTAP + t] = (T)w[t];
+    }
+    ddf_window(ddf, ry, &b, w);
+    G.by[dual][k] = b;
+    for (int t = 0; t < NTAP; ++t) {
+      G.wy64[dual][(size_t)k * NTAP + t] = w[t];
+      static_cast<T*>(G.wy[dual])[(size_t)k * NTAP + t] = (T)w[t];
+    }
+  }
+  static_cast<T*>(G.nxo)[k] = (T)G.nx[k];
+  static_cast<T*>(G.nyo)[k] = (T)G.ny[k];
+  static_cast<T*>(G.wsc)[k] = (T)(grid_scaling ? G.ds[k] / (h * h) : 1.0);
+  G.nx64[k] = G.nx[k];
+  G.ny64[k] = G.ny[k];
+  G.ds64[k] = G.ds[k];
+}
+
+// one thread per (point, position class): count or place the point in the
+// tiles its window touches
+template <bool FILL>
+__global__ void k_btile_place(int Ptot, BatchGeomDev G) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= 4 * Ptot) return;
+  const int k = idx >> 2, pc = idx & 3;
+  const int p = G.pt2prob[k];
+  const BGrid g = bgrid(G, p);
+  int n1, n2;
+  bshape(g, pc, &n1, &n2);
+  const int ntx = (n1 + TILE_X - 1) / TILE_X;
+  const int dx = (pc == PC_D || pc == PC_U) ? 1 : 0, dy = (pc == PC_D || pc == PC_V) ? 1 : 0;
+  int a0, a1, b0, b1;
+  if (!window_tiles(G.bx[dx][k], G.by[dy][k], n1, n2, &a0, &a1, &b0, &b1)) return;
+  int* cnt = G.cnt + G.cnt_off[pc] + G.tp_off[pc][p];
+  for (int ty = b0; ty <= b1; ++ty)
+    for (int tx = a0; tx <= a1; ++tx) {
+      const int pos = atomicAdd(&cnt[ty * ntx + tx], 1);
+      if (FILL) G.tpts[pc][G.ts_off[pc][p] + pos] = k - G.poff[p];
+    }
+}
+
+// one block per (problem, class): exclusive scan of the tile counts into
+// tptr (nt + 1 entries, local to the problem's tpts region); the counters
+// become the fill cursors
+__global__ void __launch_bounds__(1024) k_btile_scan(BatchGeomDev G) {
+  __shared__ int s_sum[1024];
+  const int p = blockIdx.x, pc = blockIdx.y;
+  const BGrid g = bgrid(G, p);
+  int n1, n2;
+  bshape(g, pc, &n1, &n2);
+  const int nt = ((n1 + TILE_X - 1) / TILE_X) * ((n2 + TILE_Y - 1) / TILE_Y);
+  int* cnt = G.cnt + G.cnt_off[pc] + G.tp_off[pc][p];
+  int* ptr = G.tptr[pc] + G.tp_off[pc][p];
+  const int T = blockDim.x, i = threadIdx.x;
+  const int chunk = (nt + T - 1) / T;
+  const int a = min(nt, i * chunk), b = min(nt, a + chunk);
+  int sum = 0;
+  for (int t = a; t < b; ++t) sum += cnt[t];
+  s_sum[i] = sum;
+  __syncthreads();
+  for (int off = 1; off < T; off <<= 1) {  // inclusive Hillis-Steele scan of the chunk sums
+    const int v = i >= off ? s_sum[i - off] : 0;
+    __syncthreads();
+    s_sum[i] += v;
+    __syncthreads();
+  }
+  int run = s_sum[i] - sum;
+  for (int t = a; t < b; ++t) {
+    const int c = cnt[t];
+    ptr[t] = run;
+    cnt[t] = run;
+    run += c;
+  }
+  if (i == T - 1) ptr[nt] = s_sum[T - 1];
+}
+
+// per tile: its candidate list in increasing point order (insertion sort,
+// lists are short), so the scatters' sums have a fixed order
+__global__ void k_btile_sort(BatchGeomDev G) {
+  const int p = blockIdx.x, pc = blockIdx.y;
+  const BGrid g = bgrid(G, p);
+  int n1, n2;
+  bshape(g, pc, &n1, &n2);
+  const int nt = ((n1 + TILE_X - 1) / TILE_X) * ((n2 + TILE_Y - 1) / TILE_Y);
+  const int* ptr = G.tptr[pc] + G.tp_off[pc][p];
+  int* pts = G.tpts[pc] + G.ts_off[pc][p];
+  for (int t = threadIdx.x; t < nt; t += blockDim.x) {
+    const int a = ptr[t], b = ptr[t + 1];
+    for (int u = a + 1; u < b; ++u) {
+      const int v = pts[u];
+      int w = u - 1;
+      while (w >= a && pts[w] > v) {
+        pts[w + 1] = pts[w];
+        --w;
+      }
+      pts[w + 1] = v;
+    }
+  }
+}
+
+int batch_windows_and_tiles(int nprob, int Ptot, const BatchGeomDev& G, int ddf, int dtype, int grid_scaling,
+                            cudaStream_t st) {
+  if (Ptot == 0 || nprob == 0) return ILM_OK;
+  const int pb = (Ptot + 255) / 256;
+  if (dtype == ILM_F64)
+    k_bwindows<double><<<pb, 256, 0, st>>>(Ptot, G, ddf, grid_scaling);
+  else
+    k_bwindows<float><<<pb, 256, 0, st>>>(Ptot, G, ddf, grid_scaling);
+  ILM_CHECK_LAUNCH();
+  ILM_CHECK_CUDA(cudaMemsetAsync(G.cnt, 0, (size_t)G.cnt_total * sizeof(int), st));
+  const int qb = (4 * Ptot + 255) / 256;
+  k_btile_place<false><<<qb, 256, 0, st>>>(Ptot, G);
+  ILM_CHECK_LAUNCH();
+  k_btile_scan<<<dim3(nprob, 4), 1024, 0, st>>>(G);
+  ILM_CHECK_LAUNCH();
+  k_btile_place<true><<<qb, 256, 0, st>>>(Ptot, G);
+  ILM_CHECK_LAUNCH();
+  k_btile_sort<<<dim3(nprob, 4), 256, 0, st>>>(G);
+  ILM_CHECK_LAUNCH();
+  return ILM_OK;
+}
+
 int cache_rebin_points(ilm_cache_s* c, const double* x, const double* y, const double* nx, const double* ny,
                        const double* ds, cudaStream_t st) {
   const int N = c->npts;

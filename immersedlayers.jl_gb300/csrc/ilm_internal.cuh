@@ -74,14 +74,23 @@ void parallel_for(int n, F fn) {
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
+  bool own = true;  // false: a view into memory another DevBuf owns (an arena)
   DevBuf() = default;
   DevBuf(const DevBuf&) = delete;
   DevBuf& operator=(const DevBuf&) = delete;
   ~DevBuf() { release(); }
   void release() {
-    if (p) cudaFree(p);
+    if (p && own) cudaFree(p);
     p = nullptr;
     bytes = 0;
+    own = true;
+  }
+  // point at [ptr, ptr + nbytes) of an arena (not freed by this buffer)
+  void view(void* ptr, size_t nbytes) {
+    release();
+    p = ptr;
+    bytes = nbytes;
+    own = false;
   }
   int alloc(size_t nbytes) {
     if (nbytes <= bytes && p) return ILM_OK;
@@ -356,6 +365,64 @@ struct HostWindows {
 };
 void host_windows(const ilm_grid_s& g, int ddf, int N, const double* x, const double* y, HostWindows* W);
 int cache_build_windows(ilm_cache_s* c);
+// Geometry features of one surface point for the learned preconditioner: ds/h,
+// 10 h x (turning angle over the local arc length), the normal, and sin/cos
+// of the sub-cell position in x and y.  (p, m: the next and previous points
+// of the point's body, circularly.)  Shared by the host entry point
+// ilm_point_features and the batch's device set-up.
+__host__ __device__ inline void point_feature(double xi, double yi, double nxi, double nyi, double dsi, double nxp,
+                                              double nyp, double dsp, double nxm, double nym, double dsm, double h,
+                                              float* f) {
+  const double pi = 3.14159265358979323846, two_pi = 6.283185307179586476925286766559;
+  double dth = atan2(nyp, nxp) - atan2(nym, nxm);
+  dth = fmod(dth + 3.0 * pi, two_pi);
+  if (dth < 0) dth += two_pi;
+  dth -= pi;
+  const double arc = 0.5 * dsm + dsi + 0.5 * dsp;
+  const double fx = xi / h - floor(xi / h), fy = yi / h - floor(yi / h);
+  f[0] = (float)(dsi / h);
+  f[1] = (float)(10.0 * h * dth / arc);
+  f[2] = (float)nxi;
+  f[3] = (float)nyi;
+  f[4] = (float)sin(two_pi * fx);
+  f[5] = (float)cos(two_pi * fx);
+  f[6] = (float)sin(two_pi * fy);
+  f[7] = (float)cos(two_pi * fy);
+}
+
+// Batched DDF windows and tile candidate lists on the device (batch set-up).
+// Per point k of problem p = pt2prob[k] (grid nx, ny, i0 of grid[4p..], h[p]):
+// 4-tap windows on primal and dual lines (FP64 and `dtype` copies), the
+// normals / weights in `dtype` and FP64.  Per problem and position class
+// pc, a CSR list of the problem's points (local index, increasing) per
+// TILE_X x TILE_Y tile: tptr[pc] holds nt + 1 entries per problem at
+// tp_off[pc][p], tpts[pc] holds room for 4 npts entries per problem at
+// ts_off[pc][p] (a 4 x 4 window touches at most 2 x 2 tiles).
+struct BatchGeomDev {
+  const double *x, *y, *nx, *ny, *ds;  // inputs, all points
+  const int* pt2prob;
+  const int* poff;                     // nprob + 1 point offsets
+  const int* grid;                     // per problem: nx, ny, i0x, i0y
+  const double* h;                     // per problem
+  int* bx[2];
+  int* by[2];
+  double* wx64[2];
+  double* wy64[2];
+  void* wx[2];
+  void* wy[2];
+  void *nxo, *nyo, *wsc;               // dtype
+  double *nx64, *ny64, *ds64;
+  int* tptr[4];
+  int* tpts[4];
+  const int* tp_off[4];                // per problem
+  const int* ts_off[4];
+  int* cnt;                            // scratch: one int per entry of every tptr (4 classes), zeroed here
+  int cnt_total;
+  int cnt_off[4];                      // offset of class pc's counters in cnt (= tptr layout)
+};
+int batch_windows_and_tiles(int nprob, int Ptot, const BatchGeomDev& G, int ddf, int dtype, int grid_scaling,
+                            cudaStream_t st);
+
 // device re-binning of the cache's points (ilm_cache_update_points); the
 // host copies are refreshed lazily by cache_sync_host
 int cache_rebin_points(ilm_cache_s* c, const double* x, const double* y, const double* nx, const double* ny,

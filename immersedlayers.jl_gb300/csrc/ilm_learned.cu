@@ -521,26 +521,12 @@ int ilm_point_features(int npts, const double* x, const double* y, const double*
   ILM_REQUIRE(npts >= 0 && (npts == 0 || (x && y && nx && ny && ds && seg_start && seg_len && out)),
               "features: null argument");
   ILM_REQUIRE(h > 0, "features: bad spacing");
-  const double two_pi = 6.283185307179586476925286766559;
   for (int i = 0; i < npts; ++i) {
     const int s = seg_start[i], L = seg_len[i];
     ILM_REQUIRE(L >= 3 && s >= 0 && i >= s && i < s + L && s + L <= npts, "features: bad body segment at %d", i);
     const int ip = s + (i - s + 1) % L, im = s + (i - s + L - 1) % L;
-    double dth = atan2(ny[ip], nx[ip]) - atan2(ny[im], nx[im]);
-    dth = fmod(dth + 3.0 * 3.14159265358979323846, two_pi);
-    if (dth < 0) dth += two_pi;
-    dth -= 3.14159265358979323846;
-    const double arc = 0.5 * ds[im] + ds[i] + 0.5 * ds[ip];
-    const double fx = x[i] / h - floor(x[i] / h), fy = y[i] / h - floor(y[i] / h);
-    float* f = out + (size_t)i * 8;
-    f[0] = (float)(ds[i] / h);
-    f[1] = (float)(10.0 * h * dth / arc);
-    f[2] = (float)nx[i];
-    f[3] = (float)ny[i];
-    f[4] = (float)sin(two_pi * fx);
-    f[5] = (float)cos(two_pi * fx);
-    f[6] = (float)sin(two_pi * fy);
-    f[7] = (float)cos(two_pi * fy);
+    point_feature(x[i], y[i], nx[i], ny[i], ds[i], nx[ip], ny[ip], ds[ip], nx[im], ny[im], ds[im], h,
+                  out + (size_t)i * 8);
   }
   return ILM_OK;
 }
