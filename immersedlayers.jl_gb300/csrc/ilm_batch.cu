@@ -1904,6 +1904,7 @@ int ilm_batch_set_learned(ilm_batch_t b, ilm_net_t net, int kind_mask, const int
     ILM_CHECK_LAUNCH();
   }
   ILM_CHECK_CUDA(cudaDeviceSynchronize());
+  ILM_TRY(net_check_tc(net));
   phase("learned: features and network inference (device, selected problems)");
   b->band_k = K;
   b->precond = 2;

@@ -1,6 +1,7 @@
 // Internal declarations shared by the libilm translation units.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stdio.h>
@@ -365,6 +366,17 @@ struct HostWindows {
 };
 void host_windows(const ilm_grid_s& g, int ddf, int N, const double* x, const double* y, HostWindows* W);
 int cache_build_windows(ilm_cache_s* c);
+// Forward 1-D convolution layer of the learned preconditioner on the tcgen05
+// tensor cores (ilm_tcconv.cu): out = relu?(bias + W * in) with W BF16
+// (Cout x Cin x 5), activations FP32 (split into a BF16 hi / lo pair), FP32
+// accumulation in tensor memory.  *err is set to 1 by a CTA whose MMA
+// completion wait ran out (the layer's output is then incomplete).
+bool conv_tc_supported(int Cin, int Cout);
+int launch_conv_tc(int N, int Cin, int Cout, bool relu, const __nv_bfloat16* W, const float* bias, const float* in,
+                   const int* sst, const int* sln, float* out, int* err, cudaStream_t st);
+// after a completed forward: ILM_ERR_TIMEOUT if a tensor-core layer's wait ran out
+int net_check_tc(ilm_net_t n);
+
 // Geometry features of one surface point for the learned preconditioner: ds/h,
 // 10 h x (turning angle over the local arc length), the normal, and sin/cos
 // of the sub-cell position in x and y.  (p, m: the next and previous points

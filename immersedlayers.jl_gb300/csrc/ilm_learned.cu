@@ -285,6 +285,10 @@ struct ilm_net_s {
   size_t cap = 0, pair_cap = 0;
   DevBuf acts, g0, g1, c, u, e, y, gu, gc, sums, loss, part, partb;
   int step = 0;
+  // forward layers on the tcgen05 tensor cores (default) or FP32 FMA; the
+  // tensor-core kernels' timeout flag (one int on the device)
+  bool tensor_cores = true;
+  DevBuf tc_err;
   int P() const { return 2 * band + 1; }
 };
 
@@ -344,11 +348,19 @@ int launch_conv(int N, int Cin, int Cout, int mode, bool relu, const __nv_bfloat
 // forward through all layers; c = band coefficients (N x P)
 int net_forward(ilm_net_s* n, int N, const float* feat, const int* sst, const int* sln, float* c, cudaStream_t st) {
   const float* in = feat;
+  if (n->tensor_cores && !n->tc_err.p) {
+    ILM_TRY(n->tc_err.alloc(sizeof(int)));
+    ILM_CHECK_CUDA(cudaMemsetAsync(n->tc_err.p, 0, sizeof(int), st));
+  }
   for (int l = 0; l < n->nlayers; ++l) {
     float* out = act_ptr(n, l);
-    ILM_TRY(launch_conv(N, n->cin[l], n->cout[l], 0, l < n->nlayers - 1,
-                        n->thb.as<__nv_bfloat16>() + n->woff[l], n->theta.as<float>() + n->boff[l], in, sst, sln,
-                        out, st));
+    const bool relu = l < n->nlayers - 1;
+    const __nv_bfloat16* W = n->thb.as<__nv_bfloat16>() + n->woff[l];
+    const float* bias = n->theta.as<float>() + n->boff[l];
+    if (n->tensor_cores && conv_tc_supported(n->cin[l], n->cout[l]))
+      ILM_TRY(launch_conv_tc(N, n->cin[l], n->cout[l], relu, W, bias, in, sst, sln, out, n->tc_err.as<int>(), st));
+    else
+      ILM_TRY(launch_conv(N, n->cin[l], n->cout[l], 0, relu, W, bias, in, sst, sln, out, st));
     in = out;
   }
   const int tot = N * n->P();
@@ -481,7 +493,17 @@ int ilm_net_forward(ilm_net_t n, int npts, const float* feat, const int* seg_sta
   ILM_TRY(check_net_inputs(n, npts, feat, seg_start, seg_len));
   ILM_REQUIRE(band_out, "net: null output");
   ILM_TRY(net_reserve(n, npts, 1));
-  return net_forward(n, npts, feat, seg_start, seg_len, band_out, as_stream(stream));
+  cudaStream_t st = as_stream(stream);
+  ILM_TRY(net_forward(n, npts, feat, seg_start, seg_len, band_out, st));
+  if (!n->tensor_cores) return ILM_OK;
+  ILM_CHECK_CUDA(cudaStreamSynchronize(st));
+  return net_check_tc(n);
+}
+
+int ilm_net_set_tensor_cores(ilm_net_t n, int enable) {
+  ILM_REQUIRE(n, "net: null handle");
+  n->tensor_cores = enable != 0;
+  return ILM_OK;
 }
 
 int ilm_net_loss_grad(ilm_net_t n, int npts, int npairs, const int* pair_off, const float* feat,
@@ -495,7 +517,7 @@ int ilm_net_loss_grad(ilm_net_t n, int npts, int npairs, const int* pair_off, co
   if (grad_out)
     ILM_CHECK_CUDA(cudaMemcpyAsync(grad_out, n->grad.p, n->nparam * sizeof(float), cudaMemcpyDeviceToHost, st));
   ILM_CHECK_CUDA(cudaStreamSynchronize(st));
-  return ILM_OK;
+  return net_check_tc(n);
 }
 
 int ilm_net_train_step(ilm_net_t n, int npts, int npairs, const int* pair_off, const float* feat,
@@ -535,6 +557,18 @@ int ilm_point_features(int npts, const double* x, const double* y, const double*
 
 // used by the batch solver: network forward over packed points
 namespace ilm {
+// after a forward has completed: a tensor-core wait that ran out is an error
+int net_check_tc(ilm_net_t n) {
+  if (!n->tensor_cores || !n->tc_err.p) return ILM_OK;
+  int e = 0;
+  ILM_CHECK_CUDA(cudaMemcpy(&e, n->tc_err.p, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e) {
+    ILM_CHECK_CUDA(cudaMemset(n->tc_err.p, 0, sizeof(int)));
+    set_error("learned network: a tensor-core convolution did not complete in time");
+    return ILM_ERR_TIMEOUT;
+  }
+  return ILM_OK;
+}
 int net_forward_packed(ilm_net_t n, int N, const float* feat, const int* sst, const int* sln, float* band,
                        cudaStream_t st) {
   ILM_TRY(net_reserve(n, N, 1));

@@ -118,6 +118,7 @@ SIGNATURES = {
     "ilm_batch_setup_times": [_VP, _DP, _I, C.POINTER(_I), C.POINTER(C.c_char_p)],
     "ilm_net_create": [_I, _I, _I, _I, C.POINTER(_VP)],
     "ilm_net_destroy": [_VP],
+    "ilm_net_set_tensor_cores": [_VP, _I],
     "ilm_net_nparams": [_VP, C.POINTER(C.c_size_t)],
     "ilm_net_set_params": [_VP, C.POINTER(C.c_float)],
     "ilm_net_get_params": [_VP, C.POINTER(C.c_float)],

@@ -105,6 +105,11 @@ class LearnedPreconditioner:
             raise ValueError(f"expected {self.nparams} parameters, got {p.size}")
         L.call("ilm_net_set_params", self._h, p.ctypes.data_as(C.POINTER(C.c_float)))
 
+    def set_tensor_cores(self, enable=True):
+        """Forward convolutions on the tcgen05 tensor cores (default) or by
+        FP32 FMA (ilm_net_set_tensor_cores)."""
+        L.call("ilm_net_set_tensor_cores", self._h, 1 if enable else 0)
+
     def get_params(self):
         p = np.empty(self.nparams, dtype=np.float32)
         L.call("ilm_net_get_params", self._h, p.ctypes.data_as(C.POINTER(C.c_float)))

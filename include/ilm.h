@@ -448,6 +448,12 @@ ILM_API int ilm_batch_info(ilm_batch_t b, int* iterations, double* rel_residual)
 typedef struct ilm_net_s* ilm_net_t;
 ILM_API int ilm_net_create(int nfeat, int width, int nlayers, int band, ilm_net_t* out);
 ILM_API int ilm_net_destroy(ilm_net_t n);
+/* Forward convolutions on the tcgen05 tensor cores (enable != 0, the
+ * default: BF16 weights, FP32 activations as a BF16 hi / lo pair, FP32
+ * accumulation in tensor memory) or by FP32 FMA (0).  GB300-specific: no
+ * counterpart in the reference.  With the tensor cores ilm_net_forward waits
+ * for its stream and returns ILM_ERR_TIMEOUT if a layer did not complete.  */
+ILM_API int ilm_net_set_tensor_cores(ilm_net_t n, int enable);
 ILM_API int ilm_net_nparams(ilm_net_t n, size_t* count);
 /* host FP32 parameters, per layer W[out][in][5] then bias[out]; set resets Adam */
 ILM_API int ilm_net_set_params(ilm_net_t n, const float* host);

@@ -296,6 +296,7 @@ ilm_batch_info(b, iterations, rel_residual) =
 ilm_net_create(nfeat, width, nlayers, band, out) =
     ccall((:ilm_net_create, libilm), Cint, (Cint, Cint, Cint, Cint, Ref{Ptr{Cvoid}}), nfeat, width, nlayers, band, out)
 ilm_net_destroy(n) = ccall((:ilm_net_destroy, libilm), Cint, (Ptr{Cvoid},), n)
+ilm_net_set_tensor_cores(n, enable) = ccall((:ilm_net_set_tensor_cores, libilm), Cint, (Ptr{Cvoid}, Cint), n, enable)
 ilm_net_nparams(n, count) = ccall((:ilm_net_nparams, libilm), Cint, (Ptr{Cvoid}, Ref{Csize_t}), n, count)
 ilm_net_set_params(n, host) = ccall((:ilm_net_set_params, libilm), Cint, (Ptr{Cvoid}, Ptr{Cfloat}), n, host)
 ilm_net_get_params(n, host) = ccall((:ilm_net_get_params, libilm), Cint, (Ptr{Cvoid}, Ptr{Cfloat}), n, host)

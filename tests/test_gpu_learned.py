@@ -218,3 +218,23 @@ def test_shipped_star_weights_gain_on_held_out_problems(cuda):
     assert ev["iteration_ratio"] >= 3.0, ev
     assert ev["speedup_solves"] >= 2.0, ev
     assert ev["converged_fraction_learned"] >= ev["converged_fraction_none"], ev
+
+
+@pytest.mark.parametrize("npts_bodies", [((23, 17), (31,)), ((400, 333), (511,), (128, 129, 130))])
+def test_tensor_core_forward_matches_fp32_forward(cuda, npts_bodies):
+    """The tcgen05 forward (BF16 weights, FP32 activations as a BF16 hi / lo
+    pair, FP32 accumulation in tensor memory) against the FP32-FMA forward
+    of the same network, on point counts below and well above one 128-point
+    tile, and against the oracle."""
+    from immersedlayers.learned import LearnedPreconditioner
+    N, st, ln, F, w, b, x, off = _toy(7, bodies=npts_bodies)
+    p = _params(7)
+    net = LearnedPreconditioner(params=p)
+    mb = _mb(N, st, ln, F, w, b, x, off)
+    net.set_tensor_cores(False)
+    ref = net.forward(mb["feat"], mb["seg_start"], mb["seg_len"]).cpu().numpy()
+    net.set_tensor_cores(True)
+    got = net.forward(mb["feat"], mb["seg_start"], mb["seg_len"]).cpu().numpy()
+    assert np.abs(got - ref).max() <= 5e-5 * np.abs(ref).max(), np.abs(got - ref).max() / np.abs(ref).max()
+    oref, _ = LO.forward(p, F, st, ln, weights_bf16=True)
+    assert np.abs(got - oref).max() <= 5e-5 * np.abs(oref).max()
