@@ -99,6 +99,9 @@ def config(args, world):
                         "8-mode arc-length Fourier surface data, seeds 3+i",
             "nprob_per_gpu": args.nprob, "tol": args.tol, "precision": "FP32 grid work; Schur build and CG products in float-float (~44-bit), CG vectors FP64",
             "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{world}",
+            "value": "geometry resident: the batch's set-up (DDF windows, tile lists, Schur complements, "
+                     "preconditioners, right-hand-side operator) done before the timed solves; the metric with "
+                     "per-problem set-up, host copies included, is `e2e`",
             "solver": {"none": "plain CG", "bjacobi": f"block-Jacobi flexible CG (blocks of ~{args.block} points)",
                    "learned": "learned banded preconditioner for the Dirichlet problems, block-Jacobi for the Neumann ones (flexible CG)"}[
                 args.precond]}
@@ -305,6 +308,7 @@ def run_ours(args, rank, world, dist):
     refined = _refined_leg(args, specs, stream) if rank == 0 else None
     heat = _heat_scale(args, stream) if (rank == 0 and args.heat_steps > 0) else None
     learned = _learned_leg(args) if (rank == 0 and args.learned_nprob > 0) else None
+    network = _network_leg(stream) if (rank == 0 and args.learned_nprob > 0) else None
     stokes = _stokes_leg(args) if (rank == 0 and args.stokes) else None
     moving = _moving_leg(stream) if (rank == 0 and args.moving) else None
     if learned and "none" in learned:
@@ -321,7 +325,7 @@ def run_ours(args, rank, world, dist):
                         if args.rhs_operator else "two LGF convolutions per solve"), "solvers": solvers,
                 "autotune": tuned, "stencil_gbs": stencil, "cufft_comparison": cufft, "precision": precision,
                 "refined": refined,
-                "heat": heat, "learned": learned, "stokes": stokes, "moving": moving,
+                "heat": heat, "learned": learned, "network": network, "stokes": stokes, "moving": moving,
                 "stages_ms": dict(zip(names, [round(x, 4) for x in stage_ms])),
                 "cg_iterations": {"mean": float(np.mean(its)), "max": int(its.max())},
                 "max_rel_residual": float(rr.max())}
@@ -762,6 +766,57 @@ def _learned_leg(args):
     ev["workload"] = (f"{args.learned_nprob} held-out star bodies (seeds 2e6+i), 512^2 dual nodes, h=4/512, "
                       "N_p~U{256..1024}, Dirichlet, arc-length Fourier surface data")
     return ev
+
+
+def _network_leg(stream):
+    """The learned network's own throughput, tensor cores (tcgen05 forward)
+    against FP32 FMA: inference over 40,960 points in bodies of 320 (CUDA
+    events, algorithmic FLOPs 2 x 5 x sum(Cin Cout) per point), and training
+    (forward, backward, Adam) on 64 (b, x) pairs from the plain solver on
+    problems 20000.. of the batched configuration's generator (wall clock
+    over 3 epochs after one warm-up epoch)."""
+    import torch
+    from immersedlayers import learned as LN
+    from immersedlayers import workloads as W
+    net = LN.LearnedPreconditioner(seed=0)
+    N, L = 40960, 320
+    feat = torch.randn(N, 8, device="cuda")
+    idx = torch.arange(N, device="cuda", dtype=torch.int32)
+    sst = (idx // L) * L
+    sln = torch.full((N,), L, dtype=torch.int32, device="cuda")
+    dims = LN.layer_dims()
+    flop = 2.0 * 5 * sum(ci * co for ci, co in dims) * N
+    out = {"inference_points": N, "inference_flop": flop}
+    for tc in (True, False):
+        net.set_tensor_cores(tc)
+        for _ in range(3):
+            net.forward(feat, sst, sln, stream=stream)
+        stream.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            for _ in range(10):
+                net.forward(feat, sst, sln, stream=stream)
+            e1.record(stream)
+        stream.synchronize()
+        ms = e0.elapsed_time(e1) / 10
+        out["tensor_cores" if tc else "fp32_fma"] = {"inference_ms": ms, "inference_tflops": flop / ms / 1e9}
+    data, gst = LN.generate(lambda i: W.batch_problem(i)[:3], [20000 + i for i in range(64)], chunk=64,
+                            minibatch=16)
+    npts = sum(mb["npts"] for mb in data.minibatches)
+    for tc in (True, False):
+        net.set_tensor_cores(tc)
+        LN.train(net, data, epochs=1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        LN.train(net, data, epochs=3)
+        torch.cuda.synchronize()
+        dt = (time.perf_counter() - t0) / 3
+        d = out["tensor_cores" if tc else "fp32_fma"]
+        d.update({"train_steps_per_s": len(data) / dt, "train_pairs_per_s": data.npairs / dt,
+                  "train_points_per_s": npts / dt})
+    out["training_set"] = {"pairs": data.npairs, "points": npts, "minibatches": len(data)}
+    return out
 
 
 def _rank_specs(nprob, rank):
