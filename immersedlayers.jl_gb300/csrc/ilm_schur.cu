@@ -26,8 +26,6 @@
 
 #include <algorithm>
 
-#include <climits>
-
 #include "ilm_internal.cuh"
 
 namespace ilm {
@@ -455,19 +453,11 @@ __device__ __forceinline__ FF split_ff(double v) {
 // memory was measured no faster: the kernel is bound by the float-float
 // arithmetic, not by the lookups).
 
-// The LGF values a tile of the batched build reads, staged in shared memory
-// when the window of offsets its 16 x 16 pairs span is at most this many
-// entries (float-float pairs); larger windows read the table in global memory.
-constexpr int SCHUR_GWIN = 3072;
-
 __global__ void __launch_bounds__(256) k_schur_pairs_batched(int nprob, const SchurProbDev* __restrict__ pr,
                                                              const Functional* __restrict__ F,
                                                              const double* __restrict__ w,
                                                              const float2* __restrict__ G, int ld, int M,
                                                              float* __restrict__ Shi, float* __restrict__ Slo) {
-  __shared__ Functional sF[32];  // the tile's 16 row and 16 column functionals
-  __shared__ float2 sG[SCHUR_GWIN];
-  __shared__ int s_win[5];       // x0, y0, wx, wy, staged
   int lo = 0, hi = nprob - 1;
   const int u = blockIdx.x;
   while (lo < hi) {
@@ -487,57 +477,11 @@ __global__ void __launch_bounds__(256) k_schur_pairs_batched(int nprob, const Sc
   while (ti > 0 && row0(ti) > t) --ti;
   while (ti + 1 < nt && row0(ti + 1) <= t) ++ti;
   const int tj = ti + (t - row0(ti));
-  const int tid = threadIdx.y * 16 + threadIdx.x;
-  // stage the functionals: rows ti*16.., columns tj*16..
-  for (int e = tid; e < 32 * (int)(sizeof(Functional) / 4); e += 256) {
-    const int f = e / (int)(sizeof(Functional) / 4), wd = e % (int)(sizeof(Functional) / 4);
-    const int idx = f < 16 ? ti * 16 + f : tj * 16 + (f - 16);
-    if (idx < N)
-      reinterpret_cast<int*>(&sF[f])[wd] = reinterpret_cast<const int*>(&F[P.poff + idx])[wd];
-  }
-  __syncthreads();
-  if (tid == 0) {
-    int kx0 = INT_MAX, kx1 = INT_MIN, ky0 = INT_MAX, ky1 = INT_MIN;
-    int lx0 = INT_MAX, lx1 = INT_MIN, ly0 = INT_MAX, ly1 = INT_MIN;
-    for (int f = 0; f < 32; ++f) {
-      const int idx = f < 16 ? ti * 16 + f : tj * 16 + (f - 16);
-      if (idx >= N) continue;
-      for (int p = 0; p < sF[f].nterm; ++p) {
-        const int xb = sF[f].xb[p], yb = sF[f].yb[p];
-        if (f < 16) {
-          kx0 = min(kx0, xb); kx1 = max(kx1, xb); ky0 = min(ky0, yb); ky1 = max(ky1, yb);
-        } else {
-          lx0 = min(lx0, xb); lx1 = max(lx1, xb); ly0 = min(ly0, yb); ly1 = max(ly1, yb);
-        }
-      }
-    }
-    const int x0 = kx0 - lx1 - (FW - 1), x1 = kx1 - lx0 + (FW - 1);
-    const int y0 = ky0 - ly1 - (FW - 1), y1 = ky1 - ly0 + (FW - 1);
-    const long long wx = (long long)x1 - x0 + 1, wy = (long long)y1 - y0 + 1;
-    s_win[0] = x0;
-    s_win[1] = y0;
-    s_win[2] = (int)wx;
-    s_win[3] = (int)wy;
-    s_win[4] = (wx > 0 && wy > 0 && wx * wy <= SCHUR_GWIN) ? 1 : 0;
-  }
-  __syncthreads();
-  const bool staged = s_win[4] != 0;
-  const int gx0 = s_win[0], gy0 = s_win[1], gwx = s_win[2];
-  if (staged) {
-    const int n = s_win[2] * s_win[3];
-    for (int e = tid; e < n; e += 256) {
-      int mx = abs(gx0 + e % gwx), my = abs(gy0 + e / gwx);
-      mx = mx > M ? M : mx;
-      my = my > M ? M : my;
-      sG[e] = __ldg(G + (size_t)mx * ld + my);
-    }
-  }
-  __syncthreads();
   const int k = ti * 16 + threadIdx.y;
   const int l = tj * 16 + threadIdx.x;
   if (k >= N || l >= N) return;
-  const Functional& Fk = sF[threadIdx.y];
-  const Functional& Fl = sF[16 + threadIdx.x];
+  const Functional& Fk = F[P.poff + k];
+  const Functional& Fl = F[P.poff + l];
   FF total{0.f, 0.f};
   for (int p = 0; p < Fk.nterm; ++p) {
     FF xk[FW], yk[FW];
@@ -570,25 +514,16 @@ __global__ void __launch_bounds__(256) k_schur_pairs_batched(int nprob, const Sc
       FF acc{0.f, 0.f};
 #pragma unroll
       for (int dy = 0; dy < 2 * FW - 1; ++dy) {
+        int my = abs(Dy + dy);
+        my = my > M ? M : my;
+        const float2* Grow = G + (size_t)my;
         FF racc{0.f, 0.f};
-        if (staged) {
-          const float2* srow = sG + (size_t)(Dy + dy - gy0) * gwx + (Dx - gx0);
 #pragma unroll
-          for (int dx = 0; dx < 2 * FW - 1; ++dx) {
-            const float2 g = srow[dx];
-            ff_fma(racc, g.x, g.y, cx[dx].hi, cx[dx].lo);
-          }
-        } else {
-          int my = abs(Dy + dy);
-          my = my > M ? M : my;
-          const float2* Grow = G + (size_t)my;
-#pragma unroll
-          for (int dx = 0; dx < 2 * FW - 1; ++dx) {
-            int mx = abs(Dx + dx);
-            mx = mx > M ? M : mx;
-            const float2 g = __ldg(Grow + (size_t)mx * ld);
-            ff_fma(racc, g.x, g.y, cx[dx].hi, cx[dx].lo);
-          }
+        for (int dx = 0; dx < 2 * FW - 1; ++dx) {
+          int mx = abs(Dx + dx);
+          mx = mx > M ? M : mx;
+          const float2 g = __ldg(Grow + (size_t)mx * ld);
+          ff_fma(racc, g.x, g.y, cx[dx].hi, cx[dx].lo);
         }
         racc = ff_renorm(racc.hi, racc.lo);
         ff_fma(acc, cy[dy].hi, cy[dy].lo, racc.hi, racc.lo);
