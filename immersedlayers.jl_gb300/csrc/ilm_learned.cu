@@ -357,7 +357,8 @@ int net_forward(ilm_net_s* n, int N, const float* feat, const int* sst, const in
     const bool relu = l < n->nlayers - 1;
     const __nv_bfloat16* W = n->thb.as<__nv_bfloat16>() + n->woff[l];
     const float* bias = n->theta.as<float>() + n->boff[l];
-    if (n->tensor_cores && conv_tc_supported(n->cin[l], n->cout[l]))
+    // the tensor-core kernel gathers 16-byte rows of the input
+    if (n->tensor_cores && conv_tc_supported(n->cin[l], n->cout[l]) && (reinterpret_cast<uintptr_t>(in) & 15) == 0)
       ILM_TRY(launch_conv_tc(N, n->cin[l], n->cout[l], relu, W, bias, in, sst, sln, out, n->tc_err.as<int>(), st));
     else
       ILM_TRY(launch_conv(N, n->cin[l], n->cout[l], 0, relu, W, bias, in, sst, sln, out, st));

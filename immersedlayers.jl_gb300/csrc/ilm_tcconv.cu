@@ -79,17 +79,22 @@ __device__ __forceinline__ void tmem_ld<32>(uint32_t taddr, uint32_t (&v)[32]) {
       : "r"(taddr));
 }
 
-// NP: padded output channels (16 or 64); TMEM columns allocated: max(NP, 32)
-template <int NP, bool RELU>
+// NP: padded output channels (16 or 64); CIN: input channels (a multiple of
+// 4); TMEM columns allocated: max(NP, 32)
+template <int NP, bool RELU, int CIN>
 __global__ void __launch_bounds__(TC_THREADS, 1)
-k_conv_tc(int N, int Cin, int Cout, int kp, const __nv_bfloat16* __restrict__ W, const float* __restrict__ bias,
+k_conv_tc(int N, int Cout, const __nv_bfloat16* __restrict__ W, const float* __restrict__ bias,
           const float* __restrict__ in, const int* __restrict__ sst, const int* __restrict__ sln,
           float* __restrict__ out, int* __restrict__ err) {
   constexpr uint32_t TCOLS = NP < 32 ? 32 : NP;
+  constexpr int K = TC_NK * CIN;
+  constexpr int kp = ((K + 15) / 16) * 16;
+  constexpr int Cin = CIN;
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(8) unsigned long long mbar;
   __shared__ uint32_t tmem_base;
   __shared__ int s_timeout;
+  __shared__ int s_nb[TC_M * TC_NK];  // neighbour index of every (row, tap)
   unsigned char* a_hi = smem;                               // TC_M x kp BF16
   unsigned char* a_lo = a_hi + (size_t)TC_M * kp * 2;       // TC_M x kp BF16
   unsigned char* bm = a_lo + (size_t)TC_M * kp * 2;         // NP x kp BF16
@@ -107,8 +112,12 @@ k_conv_tc(int N, int Cin, int Cout, int kp, const __nv_bfloat16* __restrict__ W,
     asm volatile("fence.mbarrier_init.release.cluster;");
     s_timeout = 0;
   }
+  // neighbours along arc length of every row and tap (rows past N: -1)
+  for (int e = tid; e < TC_M * TC_NK; e += TC_THREADS) {
+    const int r = e / TC_NK, t = e % TC_NK, i = p0 + r;
+    s_nb[e] = i < N ? tc_nbr(i, sst[i], sln[i], t - 2) : -1;
+  }
   // B: weights, B[o][t Cin + c] = W[o][c][t]; zero padding rows / columns
-  const int K = TC_NK * Cin;
   for (int e = tid; e < NP * kp; e += TC_THREADS) {
     const int o = e / kp, k = e % kp;
     __nv_bfloat16 v = __float2bfloat16(0.f);
@@ -118,20 +127,34 @@ k_conv_tc(int N, int Cin, int Cout, int kp, const __nv_bfloat16* __restrict__ W,
     }
     *reinterpret_cast<__nv_bfloat16*>(bm + tc_off(o, k, kp)) = v;
   }
-  // A: gathered activations as a hi / lo BF16 pair
-  for (int e = tid; e < TC_M * kp; e += TC_THREADS) {
-    const int r = e / kp, k = e % kp;
-    const int i = p0 + r;
-    float v = 0.f;
-    if (i < N && k < K) {
-      const int t = k / Cin, c = k % Cin;
-      v = in[(size_t)tc_nbr(i, sst[i], sln[i], t - 2) * Cin + c];
+  // zero K padding of A (columns K .. kp)
+  if (kp > K)
+    for (int e = tid; e < TC_M * (kp - K); e += TC_THREADS) {
+      const int r = e / (kp - K), k = K + e % (kp - K);
+      const uint32_t off = tc_off(r, k, kp);
+      *reinterpret_cast<__nv_bfloat16*>(a_hi + off) = __float2bfloat16(0.f);
+      *reinterpret_cast<__nv_bfloat16*>(a_lo + off) = __float2bfloat16(0.f);
     }
-    const __nv_bfloat16 hi = __float2bfloat16(v);
-    const __nv_bfloat16 lo = __float2bfloat16(v - __bfloat162float(hi));
-    const uint32_t off = tc_off(r, k, kp);
-    *reinterpret_cast<__nv_bfloat16*>(a_hi + off) = hi;
-    *reinterpret_cast<__nv_bfloat16*>(a_lo + off) = lo;
+  __syncthreads();
+  // A: gathered activations as a hi / lo BF16 pair, four channels per item
+  // (one 16-byte load, two 8-byte shared stores: 4 consecutive k stay in one
+  // 16-byte core-matrix row because t Cin + 4 c4 is a multiple of 4)
+  constexpr int C4 = CIN / 4;
+  for (int e = tid; e < TC_M * TC_NK * C4; e += TC_THREADS) {
+    const int r = e / (TC_NK * C4), t = (e / C4) % TC_NK, c4 = e % C4;
+    const int j = s_nb[r * TC_NK + t];
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (j >= 0) v = __ldg(reinterpret_cast<const float4*>(in + (size_t)j * Cin) + c4);
+    const float vv[4] = {v.x, v.y, v.z, v.w};
+    __nv_bfloat16 hi[4], lo[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      hi[q] = __float2bfloat16(vv[q]);
+      lo[q] = __float2bfloat16(vv[q] - __bfloat162float(hi[q]));
+    }
+    const uint32_t off = tc_off(r, t * Cin + 4 * c4, kp);
+    *reinterpret_cast<uint2*>(a_hi + off) = *reinterpret_cast<const uint2*>(hi);
+    *reinterpret_cast<uint2*>(a_lo + off) = *reinterpret_cast<const uint2*>(lo);
   }
   // generic-proxy shared stores -> visible to the tensor cores (async proxy)
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -209,23 +232,21 @@ k_conv_tc(int N, int Cin, int Cout, int kp, const __nv_bfloat16* __restrict__ W,
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TCOLS));
 }
 
-template <int NP, bool RELU>
-int launch_tc(int N, int Cin, int Cout, int kp, const __nv_bfloat16* W, const float* bias, const float* in,
-              const int* sst, const int* sln, float* out, int* err, cudaStream_t st) {
+template <int NP, bool RELU, int CIN>
+int launch_tc(int N, int Cout, const __nv_bfloat16* W, const float* bias, const float* in, const int* sst,
+              const int* sln, float* out, int* err, cudaStream_t st) {
+  constexpr int kp = ((TC_NK * CIN + 15) / 16) * 16;
   const size_t smem = (size_t)(2 * TC_M + NP) * kp * 2;
-  auto kern = k_conv_tc<NP, RELU>;
+  auto kern = k_conv_tc<NP, RELU, CIN>;
   ILM_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  kern<<<(N + TC_M - 1) / TC_M, TC_THREADS, smem, st>>>(N, Cin, Cout, kp, W, bias, in, sst, sln, out, err);
+  kern<<<(N + TC_M - 1) / TC_M, TC_THREADS, smem, st>>>(N, Cout, W, bias, in, sst, sln, out, err);
   ILM_CHECK_LAUNCH();
   return ILM_OK;
 }
 
 }  // namespace
 
-bool conv_tc_supported(int Cin, int Cout) {
-  const int kp = ((TC_NK * Cin + 15) / 16) * 16;
-  return Cin >= 1 && Cin <= 64 && Cout >= 1 && Cout <= 64 && (size_t)(2 * TC_M + 64) * kp * 2 <= 200 * 1024;
-}
+bool conv_tc_supported(int Cin, int Cout) { return (Cin == 8 || Cin == 64) && Cout >= 1 && Cout <= 64; }
 
 int launch_conv_tc(int N, int Cin, int Cout, bool relu, const __nv_bfloat16* W, const float* bias, const float* in,
                    const int* sst, const int* sln, float* out, int* err, cudaStream_t st) {
@@ -234,12 +255,22 @@ int launch_conv_tc(int N, int Cin, int Cout, bool relu, const __nv_bfloat16* W, 
     set_error("tensor-core convolution: unsupported channels %d -> %d", Cin, Cout);
     return ILM_ERR_UNSUPPORTED;
   }
-  const int kp = ((TC_NK * Cin + 15) / 16) * 16;
-  if (Cout <= 16)
-    return relu ? launch_tc<16, true>(N, Cin, Cout, kp, W, bias, in, sst, sln, out, err, st)
-                : launch_tc<16, false>(N, Cin, Cout, kp, W, bias, in, sst, sln, out, err, st);
-  return relu ? launch_tc<64, true>(N, Cin, Cout, kp, W, bias, in, sst, sln, out, err, st)
-              : launch_tc<64, false>(N, Cin, Cout, kp, W, bias, in, sst, sln, out, err, st);
+#define TC_CASE(NPV, RV, CV) return launch_tc<NPV, RV, CV>(N, Cout, W, bias, in, sst, sln, out, err, st)
+  if (Cout <= 16) {
+    if (Cin == 8) {
+      if (relu) TC_CASE(16, true, 8);
+      TC_CASE(16, false, 8);
+    }
+    if (relu) TC_CASE(16, true, 64);
+    TC_CASE(16, false, 64);
+  }
+  if (Cin == 8) {
+    if (relu) TC_CASE(64, true, 8);
+    TC_CASE(64, false, 8);
+  }
+  if (relu) TC_CASE(64, true, 64);
+  TC_CASE(64, false, 64);
+#undef TC_CASE
 }
 
 }  // namespace ilm
