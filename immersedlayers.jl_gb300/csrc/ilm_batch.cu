@@ -357,6 +357,13 @@ struct ilm_batch_s {
   // FP64 iterative refinement (ilm_batch_solve_refined): an FP64 copy of the
   // pipeline (same problems and points, no Schur matrices of its own) for the
   // accurate Schur right-hand side and the field assembly, and FP64 vectors
+  // CG variant 6 (size split): problems above kSplitN points on the 8-CTA
+  // clusters, the others one CTA each on a second stream, joined by events
+  bool split_ready = false;
+  int n_large = 0, n_small = 0, max_small = 0, nctas_small = 0;
+  DevBuf order_large, order_small, counter2;
+  cudaStream_t s2 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   ilm_batch_s* twin = nullptr;
   DevBuf ref_in, ref_b, ref_x, ref_r, ref_y, ref_norm, dsoff;
   // host wall-clock of the set-up phases (ilm_batch_setup_times), ms
@@ -369,6 +376,9 @@ struct ilm_batch_s {
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
     if (gexec) cudaGraphExecDestroy(gexec);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
+    if (s2) cudaStreamDestroy(s2);
     delete twin;
   }
 };
@@ -626,8 +636,56 @@ int batch_stage_a(ilm_batch_s* b, const void* fplus, const void* fminus, cudaStr
   return batch_mark(b, st);  // 5: DDF gather (Neumann: with the gradient) + Schur right-hand side
 }
 
+// CG variant 6: the two queues (largest first each), the second stream and
+// its events (built on first use)
+constexpr int kSplitN = 192;
+int ensure_split(ilm_batch_s* b) {
+  if (b->split_ready) return ILM_OK;
+  std::vector<int> ord(b->nprob), large, small;
+  for (int p = 0; p < b->nprob; ++p) ord[p] = p;
+  std::stable_sort(ord.begin(), ord.end(), [&](int a, int c) { return b->probs[a].npts > b->probs[c].npts; });
+  int max_small = 0;
+  for (int p : ord) {
+    if (b->probs[p].npts > kSplitN) {
+      large.push_back(p);
+    } else {
+      small.push_back(p);
+      max_small = std::max(max_small, b->probs[p].npts);
+    }
+  }
+  ILM_TRY(up(b->order_large, large));
+  ILM_TRY(up(b->order_small, small));
+  ILM_TRY(b->counter2.alloc(sizeof(int)));
+  if (!b->s2) ILM_CHECK_CUDA(cudaStreamCreateWithFlags(&b->s2, cudaStreamNonBlocking));
+  if (!b->ev_fork) ILM_CHECK_CUDA(cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming));
+  if (!b->ev_join) ILM_CHECK_CUDA(cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming));
+  b->n_large = (int)large.size();
+  b->n_small = (int)small.size();
+  b->max_small = max_small;
+  // the CTA slots the large problems' clusters leave free (at least 8)
+  const int slots = small.empty() ? 0 : cg_single_slots(max_small);
+  b->nctas_small = std::max(8, std::min(b->n_small, slots - 8 * cg_cluster_count(b->nprob, b->maxN, 1)));
+  b->split_ready = true;
+  return ILM_OK;
+}
+
 // The Schur CG of every problem: rhs64 -> x64 (parameters set by ensure_cg_params)
 int batch_cg(ilm_batch_s* b, cudaStream_t st) {
+  if (b->cg_variant == 6) {
+    ILM_TRY(ensure_split(b));
+    if (b->n_small > 0 && b->n_large > 0) {
+      ILM_CHECK_CUDA(cudaEventRecord(b->ev_fork, st));
+      ILM_CHECK_CUDA(cudaStreamWaitEvent(b->s2, b->ev_fork, 0));
+      ILM_TRY(launch_cg_cluster(b->cgp.p, b->order_large.as<int>(), b->n_large, b->counter.as<int>(), b->maxN,
+                                b->nclusters, st, 1));
+      ILM_TRY(launch_cg_single(b->cgp.p, b->order_small.as<int>(), b->n_small, b->counter2.as<int>(), b->max_small,
+                               b->nctas_small, b->s2));
+      ILM_CHECK_CUDA(cudaEventRecord(b->ev_join, b->s2));
+      ILM_CHECK_CUDA(cudaStreamWaitEvent(st, b->ev_join, 0));
+      b->launches += 2;
+      return batch_mark(b, st);  // 6: Schur CG
+    }
+  }
   ILM_TRY(launch_cg_cluster(b->cgp.p, b->order.as<int>(), b->nprob, b->counter.as<int>(), b->maxN, b->nclusters, st,
                             b->cg_variant));
   b->launches += 1;

@@ -1282,6 +1282,37 @@ int launch_cg_cluster(const void* params_dev, const int* order, int nprob, int* 
   }
 }
 
+// One CTA per problem (no cluster): the small problems of a size-split CG
+// launch (batch CG variant 6), run beside the 8-CTA clusters of the large
+// ones in the CTA slots those leave free.
+int launch_cg_single(const void* params_dev, const int* order, int nprob, int* counter, int max_n, int nctas,
+                     cudaStream_t st) {
+  const CGFFParams* prm = static_cast<const CGFFParams*>(params_dev);
+  ILM_CHECK_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), st));
+  const size_t smem = cg_cluster_smem(max_n, 256, 1);
+  if (smem > 200 * 1024) {
+    set_error("single-CTA CG: %d unknowns exceed its shared-memory layout", max_n);
+    return ILM_ERR_SIZE_LIMIT;
+  }
+  return launch_dist<256, 3, 1>(prm, order, nprob, counter, max_n, nctas, smem, st);
+}
+
+// co-resident CTAs of the single-CTA CG kernel on the whole device
+int cg_single_slots(int max_n) {
+  int dev = 0, nsm = 148, nb = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const size_t smem = cg_cluster_smem(max_n, 256, 1);
+  if (smem > 200 * 1024) return 0;
+  if (cudaFuncSetAttribute(k_cg_cluster<256, 3, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+          cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_cg_cluster<256, 3, 1>, 256, smem) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return 0;
+  }
+  return nb * nsm;
+}
+
 int cg_cluster_count(int nprob, int max_n, int variant) {
   int dev = 0, nsm = 148;
   cudaGetDevice(&dev);

@@ -550,6 +550,10 @@ struct BJBlockTask {
 };
 int launch_block_inverse(const BJBlockTask* tasks_dev, int ntasks, int max_sz, cudaStream_t st);
 // variant: 0 auto, 1 row-distributed vectors, 2 replicated vectors (see ilm_cg.cu)
+// single-CTA CG over the problems order[0 .. nprob) (CG variant 6's small problems)
+int launch_cg_single(const void* params_dev, const int* order, int nprob, int* counter, int max_n, int nctas,
+                     cudaStream_t st);
+int cg_single_slots(int max_n);
 int launch_cg_cluster(const void* params_dev, const int* order, int nprob, int* counter, int max_n, int nclusters,
                       cudaStream_t st, int variant = 0);
 int cg_cluster_count(int nprob, int max_n, int variant = 0);

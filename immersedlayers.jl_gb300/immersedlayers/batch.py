@@ -144,14 +144,15 @@ def _cg_times(self):
     return np.array(a[:]), np.array(b[:]), np.array(sm[:])
 
 
-CG_VARIANTS = 5  # ILM_CG_VARIANTS of include/ilm.h
+CG_VARIANTS = 6  # ILM_CG_VARIANTS of include/ilm.h
 
 
 def _set_cg_variant(self, variant):
     """Schur CG kernel: 0 default (= 1), 1 row-distributed vectors (256
     threads per CTA, up to 3 per SM), 2 replicated vectors (one cluster
     barrier per iteration), 3 128-thread CTAs, 4 256-thread CTAs at most 2
-    per SM, 5 512-thread CTAs one per SM."""
+    per SM, 5 512-thread CTAs one per SM, 6 size split (problems above 192
+    points on variant 1's clusters, the others one CTA each beside them)."""
     L.call("ilm_batch_set_cg_variant", self._h, int(variant))
 
 

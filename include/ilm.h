@@ -406,7 +406,10 @@ ILM_API int ilm_batch_cg_times(ilm_batch_t b, double* start_us, double* end_us, 
  * vectors (one cluster barrier per iteration, every vector operation in
  * every CTA), 3 row-distributed with 128-thread CTAs (twice the resident
  * clusters), 4 256-thread CTAs at most two per SM, 5 512-thread CTAs one
- * per SM.  ilm_batch_autotune solves the given
+ * per SM, 6 size split: problems above 192 points on variant 1's clusters,
+ * the smaller ones one CTA each (no cluster barriers) on a second stream in
+ * the CTA slots the clusters leave free, joined by events (the Schur-only
+ * entry points run every problem on variant 1).  ilm_batch_autotune solves the given
  * data with every variant (one untimed and `reps` timed solves each, CUDA
  * events on `stream`), keeps the fastest and returns it in *chosen and the
  * mean ms per solve of variants 1..ILM_CG_VARIANTS in
@@ -425,7 +428,7 @@ ILM_API int ilm_batch_cg_times(ilm_batch_t b, double* start_us, double* end_us, 
  * set-up call: the build runs on a stream of its own (no legacy-stream or
  * device-wide synchronisation) and the call returns when it is done.       */
 ILM_API int ilm_batch_set_rhs_operator(ilm_batch_t b, int enable);
-#define ILM_CG_VARIANTS 5
+#define ILM_CG_VARIANTS 6
 ILM_API int ilm_batch_set_cg_variant(ilm_batch_t b, int variant);
 ILM_API int ilm_batch_get_cg_variant(ilm_batch_t b, int* variant, int* nclusters);
 ILM_API int ilm_batch_autotune(ilm_batch_t b, const void* fplus, const void* fminus, void* f_out, void* s_out,

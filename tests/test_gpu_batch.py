@@ -108,9 +108,10 @@ def test_batch_large_grids_match_single_solves(cuda):
 
 @pytest.mark.parametrize("precond", ["none", "bjacobi"])
 def test_batch_cg_variants_agree(cuda, precond):
-    """The row-distributed (256-, 128- and 512-thread CTAs) and the
-    replicated-vector Schur CG kernels reach the tolerance and the same
-    solution; the autotuner keeps one of them."""
+    """The row-distributed (256-, 128- and 512-thread CTAs), the
+    replicated-vector and the size-split (small problems one CTA each)
+    Schur CG kernels reach the tolerance and the same solution; the
+    autotuner keeps one of them."""
     import torch
     from immersedlayers import workloads as W
     from immersedlayers.batch import BatchSolver
@@ -120,18 +121,18 @@ def test_batch_cg_variants_agree(cuda, precond):
         bs.set_precond(precond, 32)
     fp, fm = bs.surface_data()
     out = {}
-    for v in range(1, 6):
+    for v in range(1, 7):
         bs.set_cg_variant(v)
         f, s = bs.solve(fp, fm, tol=1e-10, maxiter=20000)
         its, rr = bs.info()
         assert (rr <= 1e-10).all(), (v, its, rr)
         out[v] = f.clone()
     assert rel(out[2].cpu().numpy(), out[1].cpu().numpy()) < 1e-8
-    for v in range(3, 6):
+    for v in range(3, 7):
         assert rel(out[v].cpu().numpy(), out[1].cpu().numpy()) < 1e-8, v
     chosen, ms = bs.autotune(fp, fm, tol=1e-10, maxiter=20000, reps=1)
-    assert chosen in range(1, 6) and chosen in ms and bs.cg_variant()[0] == chosen
-    assert len(ms) == 5
+    assert chosen in range(1, 7) and chosen in ms and bs.cg_variant()[0] == chosen
+    assert len(ms) == 6
 
 
 def test_batch_graph_replay_matches_solve(cuda):
