@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--learned-nprob", type=int, default=256, help="learned-preconditioner leg (0: skip)")
     ap.add_argument("--stokes", type=int, default=1, help="Stokes leg (0: skip)")
     ap.add_argument("--moving", type=int, default=1, help="moving-body re-binning leg (0: skip)")
+    ap.add_argument("--graph", type=int, default=1,
+                    help="timed solves replay the batch's captured CUDA graph (1) or launch stage by stage (0)")
     ap.add_argument("--rhs-operator", type=int, default=1,
                     help="precompute the right-hand-side operator for the timed (repeated) solves; e2e, which "
                          "builds a new batch every step, never does (1: on, 0: off)")
@@ -99,6 +101,7 @@ def config(args, world):
                         "8-mode arc-length Fourier surface data, seeds 3+i",
             "nprob_per_gpu": args.nprob, "tol": args.tol, "precision": "FP32 grid work; Schur build and CG products in float-float (~44-bit), CG vectors FP64",
             "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{world}",
+            "launch": "captured CUDA graph replayed per solve" if args.graph else "stage by stage",
             "value": "geometry resident: the batch's set-up (DDF windows, tile lists, Schur complements, "
                      "preconditioners, right-hand-side operator) done before the timed solves; the metric with "
                      "per-problem set-up, host copies included, is `e2e`",
@@ -194,7 +197,7 @@ def _timed(bs, fp, fm, f_out, s_out, args, stream, flush, steps):
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            bs.solve(fp, fm, f_out, s_out, tol=args.tol, stream=stream)
+            bs.solve(fp, fm, f_out, s_out, tol=args.tol, stream=stream, graph=bool(args.graph))
             e1.record(stream)
             times.append((e0, e1))
     stream.synchronize()
@@ -248,8 +251,8 @@ def run_ours(args, rank, world, dist):
             ch, ms = bs.autotune(fp, fm, f_out, s_out, tol=args.tol, reps=1, stream=stream)
         tuned[leg_names[mode]] = {"cg_variant": ch, "ms_per_variant": {str(k): round(v, 4) for k, v in ms.items()}}
         with torch.cuda.stream(stream):
-            for _ in range(args.warmup):
-                bs.solve(fp, fm, f_out, s_out, tol=args.tol, stream=stream)
+            for _ in range(args.warmup):   # the first graph solve captures the graph
+                bs.solve(fp, fm, f_out, s_out, tol=args.tol, stream=stream, graph=bool(args.graph))
         stream.synchronize()
         its, rr = bs.info()
         if mode == args.precond:

@@ -1701,6 +1701,7 @@ int ilm_batch_set_cg_variant(ilm_batch_t b, int variant) {
   ILM_REQUIRE(variant >= 0 && variant <= ILM_CG_VARIANTS, "batch: unknown CG variant %d", variant);
   b->cg_variant = variant;
   b->nclusters = cg_cluster_count(b->nprob, b->maxN, variant);
+  if (variant == 6) ILM_TRY(ensure_split(b));  // queues and stream built here, outside any stream capture
   b->param_gen++;
   return ILM_OK;
 }
