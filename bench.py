@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--heat-steps", type=int, default=1000, help="heat-conduction leg (0: skip)")
     ap.add_argument("--learned-nprob", type=int, default=256, help="learned-preconditioner leg (0: skip)")
     ap.add_argument("--stokes", type=int, default=1, help="Stokes leg (0: skip)")
+    ap.add_argument("--stokes-rhs", type=int, default=16, help="Stokes right-hand sides at ds = 1.4 h (0: skip)")
+    ap.add_argument("--stokes-maxiter", type=int, default=600, help="CG cap per Stokes right-hand side")
     ap.add_argument("--moving", type=int, default=1, help="moving-body re-binning leg (0: skip)")
     ap.add_argument("--graph", type=int, default=1,
                     help="timed solves replay the batch's captured CUDA graph (1) or launch stage by stage (0)")
@@ -345,7 +347,8 @@ def _stencil_gbs(stream, flush, hbm):
     and w x v (2 Edges + Nodes{Dual}) on 4096^2, and of the DDF
     regularization of the 8192 points of the Stokes configuration onto
     Nodes{Primal} of its 2048^2 grid (every cell written: 4 B per cell + 16 B
-    per point), FP32.  Two timings per kernel, both with CUDA events on the
+    per point; points 0.35 h apart) and of the same bodies at ds = 1.4 h on a
+    4096^2 grid, FP32.  Two timings per kernel, both with CUDA events on the
     launching stream:
       * `gbs`: back-to-back launches cycling over rotating input/output sets
         whose total is > 3x the L2 (every launch reads cold data), the time
@@ -438,6 +441,17 @@ def _stencil_gbs(stream, flush, hbm):
     outs = [il.NodesPrimal.zeros(g, torch.float32) for _ in range(nsets(nbytes))]
     out["regularize_2048_8192pts"] = timed([lambda w=w: il.regularize_(w, f, c, stream=stream) for w in outs],
                                            nbytes)
+    del c, outs
+    # the same bodies at ds = 1.4 h (the reference's test spacing) on 4096^2
+    d = W.stokes_scale(n=4096, ds_factor=1.4, nrhs=1)
+    g = il.PhysicalGrid(h=d["h"], nx=d["n"])
+    c = il.SurfaceScalarCache(d["bodies"], g, dtype=torch.float32)
+    N = len(d["bodies"])
+    f = il.ScalarData(torch.randn(N, device="cuda"))
+    nbytes = il.NodesPrimal.zeros(g, torch.float32).data.numel() * 4 + 16 * N
+    outs = [il.NodesPrimal.zeros(g, torch.float32) for _ in range(nsets(nbytes))]
+    out[f"regularize_4096_{N}pts_ds1.4h"] = timed([lambda w=w: il.regularize_(w, f, c, stream=stream) for w in outs],
+                                                  nbytes)
     return out
 
 
@@ -672,7 +686,57 @@ def _stokes_leg(args):
     out["workload"] = ("reference example: 406^2, rectangle 0.5x0.25, ds=1.4h, unit translation; "
                        "2048^2 h=0.002, 2 circles + 2 plates, 8192 points, rigid-body velocities (seed 5), "
                        "CG capped at 50 iterations")
+    if args.stokes_rhs > 0:
+        out["rhs16_ds1.4h"] = _stokes_rhs(args)
     return out
+
+
+def _stokes_rhs(args):
+    """The Stokes configuration's velocity right-hand sides (rigid-body
+    translations and rotations ~ N(0, 1) per body, seed 5) on its 2048^2 grid
+    and bodies, at the well-posed point spacing ds = 1.4 h (the as-written
+    8192 points are 0.35 h apart, where S is numerically singular): every
+    right-hand side solved by the FP64 cache to the bench tolerance, and by
+    the FP32 cache; per right-hand side the FP32 velocity (Edges{Primal}) and
+    traction (sigma) errors against the FP64 solution, relative to their max
+    magnitude.  CG capped at `--stokes-maxiter` iterations per solve."""
+    import torch
+    import immersedlayers as il
+    from immersedlayers import workloads as W
+    d = W.stokes_scale(nrhs=args.stokes_rhs, ds_factor=1.4)
+    g = il.PhysicalGrid(h=d["h"], nx=d["n"])
+    bl = d["bodies"]
+    N = len(bl)
+    caches = {dt: il.SurfaceVectorCache(bl, g, dtype=dt) for dt in (torch.float64, torch.float32)}
+    res = {"npts": N, "unknowns": 2 * N, "grid": [g.nx, g.ny], "rhs": args.stokes_rhs, "tol": args.tol,
+           "maxiter": args.stokes_maxiter, "per_rhs": []}
+    t = {torch.float64: 0.0, torch.float32: 0.0}
+    for r in range(args.stokes_rhs):
+        sol = {}
+        for dt, c in caches.items():
+            vp = il.VectorData(torch.tensor(d["vplus"][r], dtype=dt, device="cuda"))
+            vm = il.VectorData.zeros(N, dt)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            v, _, sigma, info = il.solve_stokes(c, vp, vm, tol=args.tol, maxiter=args.stokes_maxiter)
+            torch.cuda.synchronize()
+            t[dt] += time.perf_counter() - t0
+            sol[dt] = (v.data.double(), sigma.data.double(), info)
+        (v64, s64, i64), (v32, s32, i32) = sol[torch.float64], sol[torch.float32]
+        res["per_rhs"].append({
+            "fp64_iterations": i64["iterations"], "fp64_rel_residual": i64["rel_residual"],
+            "fp64_converged": i64["converged"], "fp32_iterations": i32["iterations"],
+            "fp32_rel_residual": i32["rel_residual"], "fp32_converged": i32["converged"],
+            "fp32_velocity_rel_err": float((v32 - v64).abs().max() / v64.abs().max()),
+            "fp32_traction_rel_err": float((s32 - s64).abs().max() / s64.abs().max())})
+    pr = res["per_rhs"]
+    res["fp64_seconds_per_rhs"] = t[torch.float64] / args.stokes_rhs
+    res["fp32_seconds_per_rhs"] = t[torch.float32] / args.stokes_rhs
+    res["fp64_converged"] = sum(p["fp64_converged"] for p in pr)
+    res["fp32_converged"] = sum(p["fp32_converged"] for p in pr)
+    res["max_fp32_velocity_rel_err"] = max(p["fp32_velocity_rel_err"] for p in pr)
+    res["max_fp32_traction_rel_err"] = max(p["fp32_traction_rel_err"] for p in pr)
+    return res
 
 
 _NET = {}
