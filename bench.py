@@ -47,12 +47,14 @@ def parse():
     ap.add_argument("--tol", type=float, default=1e-8)
     ap.add_argument("--precond", default="learned", choices=["none", "bjacobi", "learned"])
     ap.add_argument("--block", type=int, default=64)
+    ap.add_argument("--coarse", type=int, default=1,
+                    help="coarse correction of block-Jacobi on the Neumann problems' per-body constants")
     ap.add_argument("--cpu-sample-cols", type=int, default=32)
     ap.add_argument("--heat-steps", type=int, default=1000, help="heat-conduction leg (0: skip)")
-    ap.add_argument("--learned-nprob", type=int, default=256, help="learned-preconditioner leg (0: skip)")
+    ap.add_argument("--learned-nprob", type=int, default=1000, help="learned-preconditioner leg (0: skip)")
     ap.add_argument("--stokes", type=int, default=1, help="Stokes leg (0: skip)")
     ap.add_argument("--stokes-rhs", type=int, default=16, help="Stokes right-hand sides at ds = 1.4 h (0: skip)")
-    ap.add_argument("--stokes-maxiter", type=int, default=600, help="CG cap per Stokes right-hand side")
+    ap.add_argument("--stokes-maxiter", type=int, default=1500, help="block-CG cap of the Stokes right-hand-side leg")
     ap.add_argument("--moving", type=int, default=1, help="moving-body re-binning leg (0: skip)")
     ap.add_argument("--graph", type=int, default=1,
                     help="timed solves replay the batch's captured CUDA graph (1) or launch stage by stage (0)")
@@ -62,6 +64,9 @@ def parse():
     ap.add_argument("--profile-stencils", type=int, default=0,
                     help="run the 4096^2 FP32 grid stencils (divergence, gradient, fused convective derivatives, "
                          "w x v) this many times after one warm-up pass, nothing else (for ncu captures)")
+    ap.add_argument("--profile-scatter", type=int, default=0,
+                    help="run the DDF regularization of the Stokes bodies (8192 points) onto 2048^2 this many "
+                         "times after one warm-up call, nothing else (for ncu captures)")
     ap.add_argument("--profile-solves", type=int, default=0,
                     help="profiling driver: set up the batch with the default solver, run this many solves on a "
                          "created stream and exit (no timing, no JSON line)")
@@ -109,7 +114,8 @@ def config(args, world):
                      "per-problem set-up, host copies included, is `e2e`",
             "solver": {"none": "plain CG", "bjacobi": f"block-Jacobi flexible CG (blocks of ~{args.block} points)",
                    "learned": "learned banded preconditioner for the Dirichlet problems, block-Jacobi for the Neumann ones (flexible CG)"}[
-                args.precond]}
+                args.precond] + (" with the per-body coarse correction on the Neumann problems"
+                                 if args.coarse and args.precond != "none" else "")}
 
 
 def clocks_sampler():
@@ -239,7 +245,7 @@ def run_ours(args, rank, world, dist):
     # secondary legs: the other solvers on the same batch, same timing rules
     solvers = {}
     leg_names = {"none": "plain_cg", "bjacobi": "block_jacobi_pcg", "learned": "learned_pcg"}
-    have_learned = _prepare_learned(bs, args.block)
+    have_learned = _prepare_learned(bs, args.block, bool(args.coarse))
     if args.precond == "learned" and not have_learned:
         raise SystemExit("--precond learned: no trained weights for the batched configuration")
     legs = ["none", "bjacobi"] + (["learned"] if have_learned else [])
@@ -650,9 +656,11 @@ def _heat_scale(args, stream):
 def _stokes_leg(args):
     """Stokes flow (vector cache, FP64): the reference example's rectangle
     (PhysicalGrid((-2,2),(-2,2),0.01), Rectangle(0.5,0.25,1.4h), translating
-    at unit speed) solved to the bench tolerance; and the 2048^2, 8192-point
-    configuration (ds ~ 0.35 h: S numerically singular, 1e-8 unattainable)
-    timed per CG iteration over a capped solve."""
+    at unit speed) solved to the bench tolerance with the preconditioned CG
+    (and with plain CG for comparison); the 2048^2, 8192-point configuration
+    (ds ~ 0.35 h: S numerically singular, 1e-8 unattainable; above the
+    preconditioner's 4096 points) timed per CG iteration over a capped solve;
+    and the configuration's 16 right-hand sides at ds = 1.4 h."""
     import numpy as np
     import torch
     import immersedlayers as il
@@ -679,7 +687,18 @@ def _stokes_leg(args):
     bl = B.BodyList()
     bl.append(B.rectangle(0.5, 0.25, ds=1.4 * 0.01))
     N = len(bl)
-    out["reference_example"] = run(g, bl, np.concatenate([np.ones(N), np.zeros(N)]), args.tol, 20000)
+    vp_h = np.concatenate([np.ones(N), np.zeros(N)])
+    out["reference_example"] = run(g, bl, vp_h, args.tol, 20000)
+    c = il.SurfaceVectorCache(bl, g, dtype=torch.float64)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    _, _, _, infos = il.solve_stokes_multi(c, torch.tensor(vp_h[None, :], device="cuda"), tol=args.tol,
+                                           maxiter=20000, precond=False)
+    torch.cuda.synchronize()
+    out["reference_example"]["plain_cg"] = {"seconds": time.perf_counter() - t0,
+                                            "cg_iterations": infos[0]["iterations"],
+                                            "converged": infos[0]["converged"]}
+    del c
     d = W.stokes_scale(nrhs=1)
     g = il.PhysicalGrid(h=d["h"], nx=d["n"])
     out["npts8192_2048sq"] = run(g, d["bodies"], d["vplus"][0], args.tol, 50)
@@ -695,11 +714,13 @@ def _stokes_rhs(args):
     """The Stokes configuration's velocity right-hand sides (rigid-body
     translations and rotations ~ N(0, 1) per body, seed 5) on its 2048^2 grid
     and bodies, at the well-posed point spacing ds = 1.4 h (the as-written
-    8192 points are 0.35 h apart, where S is numerically singular): every
-    right-hand side solved by the FP64 cache to the bench tolerance, and by
-    the FP32 cache; per right-hand side the FP32 velocity (Edges{Primal}) and
-    traction (sigma) errors against the FP64 solution, relative to their max
-    magnitude.  CG capped at `--stokes-maxiter` iterations per solve."""
+    8192 points are 0.35 h apart, where S is numerically singular), all
+    solved at once by ilm_solve_stokes_multi (block CG over the right-hand
+    sides, S preconditioned by the inverse point-point Schur complement
+    -E L^-1 E^T per velocity component): FP64 cache to the bench tolerance,
+    FP32 cache to 1e-6; per right-hand side the FP32 velocity (Edges{Primal})
+    and traction (sigma) errors against the FP64 solution, relative to their
+    max magnitude.  Block iterations capped at `--stokes-maxiter`."""
     import torch
     import immersedlayers as il
     from immersedlayers import workloads as W
@@ -707,37 +728,32 @@ def _stokes_rhs(args):
     g = il.PhysicalGrid(h=d["h"], nx=d["n"])
     bl = d["bodies"]
     N = len(bl)
-    caches = {dt: il.SurfaceVectorCache(bl, g, dtype=dt) for dt in (torch.float64, torch.float32)}
-    res = {"npts": N, "unknowns": 2 * N, "grid": [g.nx, g.ny], "rhs": args.stokes_rhs, "tol": args.tol,
-           "maxiter": args.stokes_maxiter, "per_rhs": []}
-    for dt, c in caches.items():   # plans and scratch outside the timing
-        il.solve_stokes(c, il.VectorData.zeros(N, dt), il.VectorData.zeros(N, dt), tol=args.tol, maxiter=3)
-    t = {torch.float64: 0.0, torch.float32: 0.0}
+    res = {"npts": N, "unknowns": 2 * N, "grid": [g.nx, g.ny], "rhs": args.stokes_rhs,
+           "maxiter_block": args.stokes_maxiter, "method": "block CG over the right-hand sides, preconditioned"}
+    sol = {}
+    for dt, tol in ((torch.float64, args.tol), (torch.float32, 1e-6)):
+        c = il.SurfaceVectorCache(bl, g, dtype=dt)
+        V = torch.tensor(d["vplus"], dtype=dt, device="cuda")
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        vs, _, sig, infos = il.solve_stokes_multi(c, V, tol=tol, maxiter=args.stokes_maxiter)
+        torch.cuda.synchronize()
+        sec = time.perf_counter() - t0   # includes the preconditioner set-up (first solve on this cache)
+        key = "fp64" if dt == torch.float64 else "fp32"
+        res[key] = {"tol": tol, "seconds_all_rhs": sec, "block_iterations": infos[0]["iterations"],
+                    "converged": sum(i["converged"] for i in infos),
+                    "max_rel_residual": max(i["rel_residual"] for i in infos)}
+        sol[key] = ([v.data.double() for v in vs], [x.data.double() for x in sig])
+        del c
+    per = []
     for r in range(args.stokes_rhs):
-        sol = {}
-        for dt, c in caches.items():
-            vp = il.VectorData(torch.tensor(d["vplus"][r], dtype=dt, device="cuda"))
-            vm = il.VectorData.zeros(N, dt)
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            v, _, sigma, info = il.solve_stokes(c, vp, vm, tol=args.tol, maxiter=args.stokes_maxiter)
-            torch.cuda.synchronize()
-            t[dt] += time.perf_counter() - t0
-            sol[dt] = (v.data.double(), sigma.data.double(), info)
-        (v64, s64, i64), (v32, s32, i32) = sol[torch.float64], sol[torch.float32]
-        res["per_rhs"].append({
-            "fp64_iterations": i64["iterations"], "fp64_rel_residual": i64["rel_residual"],
-            "fp64_converged": i64["converged"], "fp32_iterations": i32["iterations"],
-            "fp32_rel_residual": i32["rel_residual"], "fp32_converged": i32["converged"],
-            "fp32_velocity_rel_err": float((v32 - v64).abs().max() / v64.abs().max()),
-            "fp32_traction_rel_err": float((s32 - s64).abs().max() / s64.abs().max())})
-    pr = res["per_rhs"]
-    res["fp64_seconds_per_rhs"] = t[torch.float64] / args.stokes_rhs
-    res["fp32_seconds_per_rhs"] = t[torch.float32] / args.stokes_rhs
-    res["fp64_converged"] = sum(p["fp64_converged"] for p in pr)
-    res["fp32_converged"] = sum(p["fp32_converged"] for p in pr)
-    res["max_fp32_velocity_rel_err"] = max(p["fp32_velocity_rel_err"] for p in pr)
-    res["max_fp32_traction_rel_err"] = max(p["fp32_traction_rel_err"] for p in pr)
+        v64, s64 = sol["fp64"][0][r], sol["fp64"][1][r]
+        v32, s32 = sol["fp32"][0][r], sol["fp32"][1][r]
+        per.append({"fp32_velocity_rel_err": float((v32 - v64).abs().max() / v64.abs().max()),
+                    "fp32_traction_rel_err": float((s32 - s64).abs().max() / s64.abs().max())})
+    res["per_rhs"] = per
+    res["max_fp32_velocity_rel_err"] = max(p["fp32_velocity_rel_err"] for p in per)
+    res["max_fp32_traction_rel_err"] = max(p["fp32_traction_rel_err"] for p in per)
     return res
 
 
@@ -802,17 +818,20 @@ def _moving_leg(stream):
             "update_points_and_regularize_ms": dev_ms, "rebuild_cache_and_regularize_ms": rebuild_ms}
 
 
-def _prepare_learned(bs, block=64):
+def _prepare_learned(bs, block=64, coarse=True):
     """Set the learned preconditioner trained on the batched configuration's
     Dirichlet problems on the batch (the network is loaded once per process,
     like a model); the Neumann problems keep block-Jacobi (the Neumann
     network trained to a loss of only 0.6: the near-null constants of the
-    Neumann Schur complement dominate its data)."""
+    Neumann Schur complement dominate its data), with the coarse correction
+    on those constants (one per body) when `coarse`."""
     from immersedlayers import learned as LN
     from immersedlayers.batch import DIRICHLET
     if not os.path.exists(LN.BATCHED_WEIGHTS[DIRICHLET]):
         return False
     bs.set_precond("bjacobi", block)   # block inverses for the Neumann problems
+    if coarse:
+        bs.set_coarse(True)            # and their per-body coarse correction
     if "dirichlet" not in _NET:
         _NET["dirichlet"] = LN.LearnedPreconditioner.load(LN.BATCHED_WEIGHTS[DIRICHLET])
     bs._nets = [_NET["dirichlet"]]
@@ -824,14 +843,15 @@ def _learned_leg(args):
     """Learned preconditioner (trained weights shipped with the package) on
     held-out star-body problems: 512^2 grids, h = 4/512, N_p ~ U{256..1024},
     full Dirichlet solves at the bench tolerance; plain CG against the
-    learned preconditioner on the problems plain CG can solve."""
+    learned preconditioner on the problems plain CG can solve, and the
+    learned solve's field error against the FP64 refined solution."""
     from immersedlayers import learned as LN
     from immersedlayers import workloads as W
     if not os.path.exists(LN.DEFAULT_WEIGHTS):
         return {"unavailable": "no trained weights at " + os.path.relpath(LN.DEFAULT_WEIGHTS, ROOT)}
     net = LN.LearnedPreconditioner.load()
     ev = LN.evaluate(net, W.learned_problem, [W.LEARNED_TEST_SEED + i for i in range(args.learned_nprob)],
-                     tol=args.tol)
+                     tol=args.tol, fp64_errors=True)
     ev["workload"] = (f"{args.learned_nprob} held-out star bodies (seeds 2e6+i), 512^2 dual nodes, h=4/512, "
                       "N_p~U{256..1024}, Dirichlet, arc-length Fourier surface data")
     return ev
@@ -924,6 +944,7 @@ def _e2e(args, specs, stream, dt):
     h2d = d2h = 0
     parts = []
     phases = []
+    f_h = s_h = None   # pinned result buffers, allocated by the untimed first step and reused
     for _ in range(steps + 1):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -931,7 +952,7 @@ def _e2e(args, specs, stream, dt):
         torch.cuda.synchronize()
         t1 = time.perf_counter()
         if args.precond == "learned":
-            _prepare_learned(bs, args.block)
+            _prepare_learned(bs, args.block, bool(args.coarse))
         bs.set_precond(args.precond, args.block)
         torch.cuda.synchronize()
         t2 = time.perf_counter()
@@ -939,8 +960,9 @@ def _e2e(args, specs, stream, dt):
             fp = fp_h.to("cuda", non_blocking=True)
             fm = fm_h.to("cuda", non_blocking=True)
             f, s = bs.solve(fp, fm, tol=args.tol, stream=stream)
-            f_h = torch.empty(f.numel(), dtype=dt).pin_memory()
-            s_h = torch.empty(s.numel(), dtype=dt).pin_memory()
+            if f_h is None:
+                f_h = torch.empty(f.numel(), dtype=dt).pin_memory()
+                s_h = torch.empty(s.numel(), dtype=dt).pin_memory()
             f_h.copy_(f, non_blocking=True)
             s_h.copy_(s, non_blocking=True)
         stream.synchronize()
@@ -999,6 +1021,26 @@ def run_profile_stencils(args):
     print(f"stencil passes {1 + args.profile_stencils} on {n}^2", file=sys.stderr)
 
 
+def run_profile_scatter(args):
+    """FP32 regularization of random surface data on the Stokes bodies (8192
+    points) onto 2048^2 Nodes{Primal}: one warm-up call and
+    `args.profile_scatter` more (a fixed launch sequence for ncu)."""
+    import torch
+    import __graft_entry__ as ge
+    ge.build()
+    import immersedlayers as il
+    from immersedlayers import workloads as W
+    d = W.stokes_scale(nrhs=1)
+    g = il.PhysicalGrid(h=d["h"], nx=d["n"])
+    c = il.SurfaceScalarCache(d["bodies"], g, dtype=torch.float32)
+    f = il.ScalarData(torch.randn(len(d["bodies"]), device="cuda"))
+    w = il.NodesPrimal.zeros(g, torch.float32)
+    for _ in range(1 + args.profile_scatter):
+        il.regularize_(w, f, c)
+    torch.cuda.synchronize()
+    print(f"regularize calls {1 + args.profile_scatter} on {g.nx}^2, {len(d['bodies'])} points", file=sys.stderr)
+
+
 def run_profile_solves(args):
     """Batch and default-solver set-up, then `args.profile_solves` solves (a
     fixed launch sequence for ncu captures)."""
@@ -1009,7 +1051,7 @@ def run_profile_solves(args):
     from immersedlayers.batch import BatchSolver
     bs = BatchSolver(W.batch_specs(args.nprob), dtype=torch.float32)
     if args.precond == "learned":
-        _prepare_learned(bs, args.block)
+        _prepare_learned(bs, args.block, bool(args.coarse))
     bs.set_precond(args.precond, args.block)
     fp, fm = bs.surface_data()
     f = torch.empty(bs.total_cells, device="cuda")
@@ -1030,6 +1072,8 @@ def main():
         run_profile_solves(args)
     elif args.profile_stencils > 0:
         run_profile_stencils(args)
+    elif args.profile_scatter > 0:
+        run_profile_scatter(args)
     elif args.impl == "reference":
         run_reference(args, rank, world)
     else:

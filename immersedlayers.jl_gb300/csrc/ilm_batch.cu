@@ -117,20 +117,19 @@ __global__ void __launch_bounds__(256)
 
 // Deterministic scatter: one thread per output cell of an occupied 32 x 8
 // tile; the tile's candidate points (index order) are staged in shared
-// memory 256 at a time, one point per thread, then every thread sums them in
-// that order.
+// memory 256 at a time, one point per thread, and every cell sums the points
+// of its window buckets (tile_sum_bucketed) in a fixed order.
 template <typename T>
 __global__ void __launch_bounds__(SB_X* SB_Y)
     k_bscatter(const BScatterTask* __restrict__ tasks, int ntasks, const int* __restrict__ bmap) {
-  constexpr int NB = SB_X * SB_Y;
-  __shared__ int s_bx[NB], s_by[NB];
-  __shared__ T s_amp[NB], s_wx[NB * NTAP], s_wy[NB * NTAP];
+  static_assert(SB_X == TILE_X && SB_Y == TILE_Y, "batched scatter tiles are the cache tiles");
+  __shared__ ScatterSmem<T> sm;
   const int ti = bmap[blockIdx.x];
   const BScatterTask& S = tasks[ti];
   const int tile = S.ne[blockIdx.x - S.tile0];
-  const int tx = tile % S.ntx, ty = tile / S.ntx;
-  const int i = tx * SB_X + threadIdx.x;
-  const int j = ty * SB_Y + threadIdx.y;
+  const int x0 = (tile % S.ntx) * SB_X, y0 = (tile / S.ntx) * SB_Y;
+  const int i = x0 + threadIdx.x;
+  const int j = y0 + threadIdx.y;
   const int tid = threadIdx.y * SB_X + threadIdx.x;
   const int p0 = S.tptr[tile], p1 = S.tptr[tile + 1];
   const T* __restrict__ wx = static_cast<const T*>(S.wx);
@@ -140,26 +139,20 @@ __global__ void __launch_bounds__(SB_X* SB_Y)
   const T* nx = static_cast<const T*>(S.nx);
   const T* ny = static_cast<const T*>(S.ny);
   T acc = (T)0;
-  for (int c0 = p0; c0 < p1; c0 += NB) {
-    const int nc = min(NB, p1 - c0);
+  for (int c0 = p0; c0 < p1; c0 += SCAT_NB) {
+    const int nc = min(SCAT_NB, p1 - c0);
     if (tid < nc) {
       const int k = S.tpts[c0 + tid];
-      s_bx[tid] = S.bx[k];
-      s_by[tid] = S.by[k];
-      s_amp[tid] = wsc[k] * (bcoef<T>(S.coef, nx, ny, k) * in[k]);
+      sm.bx[tid] = S.bx[k];
+      sm.by[tid] = S.by[k];
+      sm.amp[tid] = wsc[k] * (bcoef<T>(S.coef, nx, ny, k) * in[k]);
 #pragma unroll
       for (int q = 0; q < NTAP; ++q) {
-        s_wx[tid * NTAP + q] = wx[k * NTAP + q];
-        s_wy[tid * NTAP + q] = wy[k * NTAP + q];
+        sm.wx[tid * NTAP + q] = wx[k * NTAP + q];
+        sm.wy[tid * NTAP + q] = wy[k * NTAP + q];
       }
     }
-    __syncthreads();
-    for (int q = 0; q < nc; ++q) {
-      const int di = i - s_bx[q];
-      const int dj = j - s_by[q];
-      if ((unsigned)di < (unsigned)NTAP && (unsigned)dj < (unsigned)NTAP)
-        acc += s_amp[q] * s_wx[q * NTAP + di] * s_wy[q * NTAP + dj];
-    }
+    acc += tile_sum_bucketed<T>(sm, nc, x0, i, j);
     __syncthreads();
   }
   if (i < S.n1 && j < S.n2) {
@@ -336,6 +329,11 @@ struct ilm_batch_s {
   DevBuf band, lseg_start, lseg_len;
   DevBuf arena_learned;  // body segments of the learned preconditioner
   std::vector<char> has_band;  // problems whose kind a network was set for
+  // coarse correction of block-Jacobi on the bodies' constants
+  // (ilm_batch_set_coarse): per problem the bodies (0: off), their
+  // CG_COARSE_MAX + 1 local starts and E^-1 (CG_COARSE_MAX^2, row-major)
+  std::vector<int> coarse_nb, coarse_start;
+  std::vector<double> coarse_Einv;
   // deflation of the Dirichlet net-charge mode (set up before the first solve)
   bool defl_ready = false;
   std::vector<double> defl_gamma, defl_uz;
@@ -413,6 +411,83 @@ int up_typed(DevBuf& b, const std::vector<double>& v, int dtype) {
 
 int ensure_deflation(ilm_batch_s* b);
 
+struct CoarseTask {
+  const float* Shi;  // n x n row-major float-float (leading dimension schur_ld(n))
+  const float* Slo;
+  const double* w;   // ds of the problem's points
+  int n, nb;
+  int cst[CG_COARSE_MAX + 1];
+};
+
+// E = Z^T W S Z (nb x nb, row-major in E[16 t ...]) of task t: one CTA per
+// task, a warp per row, FP64 sums of the float-float entries; per-warp
+// partials in shared memory summed in warp order (deterministic)
+__global__ void __launch_bounds__(256) k_coarse_E(const CoarseTask* __restrict__ tasks, double* __restrict__ E) {
+  constexpr int NB2 = CG_COARSE_MAX * CG_COARSE_MAX;
+  __shared__ double part[8][NB2];
+  const CoarseTask T = tasks[blockIdx.x];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, ld = schur_ld(T.n);
+  for (int k = lane; k < NB2; k += 32) part[warp][k] = 0.0;
+  __syncwarp();
+  auto body = [&](int i) {
+    int b = 0;
+    for (int k = 1; k < T.nb; ++k) b += i >= T.cst[k] ? 1 : 0;
+    return b;
+  };
+  for (int i = warp; i < T.n; i += 8) {
+    double acc[CG_COARSE_MAX] = {0.0, 0.0, 0.0, 0.0};
+    const float* h = T.Shi + (size_t)i * ld;
+    const float* l = T.Slo + (size_t)i * ld;
+    for (int j = lane; j < T.n; j += 32) {
+      const double v = (double)h[j] + (double)l[j];
+      const int bj = body(j);
+#pragma unroll
+      for (int b = 0; b < CG_COARSE_MAX; ++b) acc[b] += b == bj ? v : 0.0;
+    }
+#pragma unroll
+    for (int b = 0; b < CG_COARSE_MAX; ++b)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc[b] += __shfl_down_sync(0xffffffffu, acc[b], o);
+    if (lane == 0) {
+      const int a = body(i);
+      for (int b = 0; b < T.nb; ++b) part[warp][a * CG_COARSE_MAX + b] += T.w[i] * acc[b];
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < NB2) {
+    double t = 0.0;
+    for (int w = 0; w < 8; ++w) t += part[w][threadIdx.x];
+    E[(size_t)blockIdx.x * NB2 + threadIdx.x] = t;
+  }
+}
+
+// inverse of a k x k matrix (row-major, leading dimension CG_COARSE_MAX) by
+// Gauss-Jordan with partial pivoting; false if singular
+bool small_inverse(int k, const double* A, double* Ainv) {
+  constexpr int M = CG_COARSE_MAX;
+  double a[M][2 * M];
+  for (int i = 0; i < k; ++i)
+    for (int j = 0; j < 2 * k; ++j) a[i][j] = j < k ? A[i * M + j] : (j - k == i ? 1.0 : 0.0);
+  for (int c = 0; c < k; ++c) {
+    int piv = c;
+    for (int r = c + 1; r < k; ++r)
+      if (fabs(a[r][c]) > fabs(a[piv][c])) piv = r;
+    if (!(fabs(a[piv][c]) > 0.0)) return false;
+    for (int j = 0; j < 2 * k; ++j) std::swap(a[c][j], a[piv][j]);
+    const double ip = 1.0 / a[c][c];
+    for (int j = 0; j < 2 * k; ++j) a[c][j] *= ip;
+    for (int r = 0; r < k; ++r) {
+      if (r == c) continue;
+      const double f = a[r][c];
+      for (int j = 0; j < 2 * k; ++j) a[r][j] -= f * a[c][j];
+    }
+  }
+  for (int i = 0; i < M * M; ++i) Ainv[i] = 0.0;
+  for (int i = 0; i < k; ++i)
+    for (int j = 0; j < k; ++j) Ainv[i * M + j] = a[i][k + j];
+  return true;
+}
+
 // Block-Jacobi inverses (Gauss-Jordan, float-float) of the problems whose
 // preconditioner uses them: every problem under block-Jacobi, the problems
 // without a network under the learned preconditioner
@@ -463,6 +538,9 @@ int ensure_cg_params(ilm_batch_s* b, double tol, int maxiter) {
     if (b->precond == 2 && b->has_band[p])
       cgff_params_set_band(dst, b->band.as<float>() + o * P, b->band_k, b->lseg_start.as<int>() + o,
                            b->lseg_len.as<int>() + o);
+    if (pre && !b->coarse_nb.empty() && b->coarse_nb[p] > 0)
+      cgff_params_set_coarse(dst, b->coarse_nb[p], &b->coarse_start[(size_t)p * (CG_COARSE_MAX + 1)],
+                             &b->coarse_Einv[(size_t)p * CG_COARSE_MAX * CG_COARSE_MAX]);
   }
   ILM_TRY(up(b->cgp, cg));
   b->cg_tol = tol;
@@ -1879,6 +1957,63 @@ int ilm_batch_info(ilm_batch_t b, int* iterations, double* rel_residual) {
     ILM_CHECK_CUDA(cudaMemcpy(iterations, b->iters.p, (size_t)b->nprob * sizeof(int), cudaMemcpyDeviceToHost));
   if (rel_residual)
     ILM_CHECK_CUDA(cudaMemcpy(rel_residual, b->relres.p, (size_t)b->nprob * sizeof(double), cudaMemcpyDeviceToHost));
+  return ILM_OK;
+}
+
+int ilm_batch_set_coarse(ilm_batch_t b, int kind_mask, const int* body_start) {
+  ILM_REQUIRE(b, "null batch");
+  ILM_REQUIRE(kind_mask >= 0 && kind_mask <= 2 && kind_mask != 1,
+              "batch_set_coarse: kind mask %d (0 off, 2 Neumann)", kind_mask);
+  constexpr int M = CG_COARSE_MAX, M1 = CG_COARSE_MAX + 1;
+  b->coarse_nb.assign(b->nprob, 0);
+  b->coarse_start.assign((size_t)b->nprob * M1, 0);
+  b->coarse_Einv.assign((size_t)b->nprob * M * M, 0.0);
+  b->params_dirty = true;
+  if (kind_mask == 0) return ILM_OK;
+  ILM_REQUIRE(body_start, "batch_set_coarse: null body starts");
+  const auto t0 = std::chrono::steady_clock::now();
+  std::vector<CoarseTask> tasks;
+  std::vector<int> tprob;
+  for (int p = 0; p < b->nprob; ++p) {
+    const int o = (int)b->poff[p], n = b->probs[p].npts;
+    std::vector<int> st;
+    for (int k = 0; k < n; ++k) {
+      const int s = body_start[o + k];
+      ILM_REQUIRE(s >= 0 && s <= k && (k == 0 ? s == 0 : (s == body_start[o + k - 1] || s == k)),
+                  "batch_set_coarse: body starts of problem %d are not contiguous at point %d", p, k);
+      if (s == k) st.push_back(k);
+    }
+    if (!((kind_mask >> b->probs[p].kind) & 1) || st.empty() || (int)st.size() > M) continue;
+    CoarseTask T;
+    T.Shi = b->Shi.as<float>() + b->soff[p];
+    T.Slo = b->Slo.as<float>() + b->soff[p];
+    T.w = b->ds64.as<double>() + o;
+    T.n = n;
+    T.nb = (int)st.size();
+    for (int q = 0; q < M1; ++q) T.cst[q] = q < T.nb ? st[q] : n;
+    tasks.push_back(T);
+    tprob.push_back(p);
+  }
+  if (tasks.empty()) return ILM_OK;
+  DevBuf dt, dE;
+  ILM_TRY(up(dt, tasks));
+  ILM_TRY(dE.alloc(tasks.size() * M * M * sizeof(double)));
+  k_coarse_E<<<(unsigned)tasks.size(), 256>>>(dt.as<CoarseTask>(), dE.as<double>());
+  ILM_CHECK_LAUNCH();
+  std::vector<double> E(tasks.size() * M * M);
+  ILM_CHECK_CUDA(cudaMemcpy(E.data(), dE.p, E.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  for (size_t t = 0; t < tasks.size(); ++t) {
+    const int p = tprob[t];
+    const CoarseTask& T = tasks[t];
+    double Es[M * M];
+    for (int i = 0; i < M; ++i)  // symmetric part (W S is symmetric up to rounding)
+      for (int j = 0; j < M; ++j) Es[i * M + j] = 0.5 * (E[t * M * M + i * M + j] + E[t * M * M + j * M + i]);
+    if (!small_inverse(T.nb, Es, &b->coarse_Einv[(size_t)p * M * M])) continue;
+    b->coarse_nb[p] = T.nb;
+    for (int q = 0; q < M1; ++q) b->coarse_start[(size_t)p * M1 + q] = T.cst[q];
+  }
+  b->setup_ms.emplace_back("coarse correction (bodies' constants)",
+                           std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
   return ILM_OK;
 }
 

@@ -26,6 +26,8 @@ namespace cg = cooperative_groups;
 namespace ilm {
 
 constexpr int CG_CLUSTER = 8;
+constexpr int CG_RED_K = 8;       // values per cluster reduction (csum_t0)
+constexpr int CG_BC = 24;         // broadcast scalars: [0, 16) CG, [16, 20) coarse coefficients
 constexpr int CGC_THREADS = 256;
 constexpr int CGC_WARPS = CGC_THREADS / 32;
 
@@ -115,6 +117,13 @@ struct CGFFParams {
   // optional: global-timer stamps (ns) when the problem is taken and done,
   // and the SM of the cluster's first CTA (profiling)
   unsigned long long* tspan;
+  // optional coarse correction of the block-Jacobi preconditioner on the
+  // bodies' constant vectors: z = M_bj r + Z E^-1 Z^T W r, Z the indicator
+  // vectors of the cnb bodies (points [cstart[b], cstart[b+1])), E = Z^T W S Z
+  // (cnb = 0: off)
+  int cnb;
+  int cstart[CG_COARSE_MAX + 1];
+  double cEinv[CG_COARSE_MAX * CG_COARSE_MAX];  // row-major
 };
 
 __device__ __forceinline__ unsigned long long global_ns() {
@@ -765,9 +774,11 @@ __device__ void apply_bjacobi_rows(const CGFFParams& pr, int r0, int r1, const f
 // same chain of FP32 two-sums.  `red` holds 2 K blockDim floats (K blockDim
 // doubles), `pub` 8 slots of 4 float-float values; the published slot
 // rotates over seven values so that a CTA never overwrites a slot another
-// CTA may still be reading.
+// CTA may still be reading.  K <= CG_RED_K.
 template <int K, int CS = CG_CLUSTER>
 __device__ void csum_t0(cg::cluster_group& cl, double (&v)[K], int nact, double* red, double* pub, int& slot) {
+  static_assert(K <= CG_RED_K, "too many values in one cluster reduction");
+  constexpr int PS = 2 * CG_RED_K;  // floats per published slot
   const int t = threadIdx.x, nt = blockDim.x;
   float* rf = reinterpret_cast<float*>(red);
   float* pf = reinterpret_cast<float*>(pub);
@@ -793,8 +804,8 @@ __device__ void csum_t0(cg::cluster_group& cl, double (&v)[K], int nact, double*
         a = ff_add(a, b);
       }
       if (t == 0) {
-        pf[8 * slot + 2 * k] = a.hi;
-        pf[8 * slot + 2 * k + 1] = a.lo;
+        pf[PS * slot + 2 * k] = a.hi;
+        pf[PS * slot + 2 * k + 1] = a.lo;
       }
     }
   }
@@ -803,8 +814,8 @@ __device__ void csum_t0(cg::cluster_group& cl, double (&v)[K], int nact, double*
     float rh[K], rl[K];
 #pragma unroll
     for (int k = 0; k < K; ++k) {
-      rh[k] = t < CS ? cl.map_shared_rank(pf, t)[8 * slot + 2 * k] : 0.f;
-      rl[k] = t < CS ? cl.map_shared_rank(pf, t)[8 * slot + 2 * k + 1] : 0.f;
+      rh[k] = t < CS ? cl.map_shared_rank(pf, t)[PS * slot + 2 * k] : 0.f;
+      rl[k] = t < CS ? cl.map_shared_rank(pf, t)[PS * slot + 2 * k + 1] : 0.f;
     }
 #pragma unroll
     for (int k = 0; k < K; ++k) {
@@ -820,6 +831,55 @@ __device__ void csum_t0(cg::cluster_group& cl, double (&v)[K], int nact, double*
     }
   }
   slot = slot == 7 ? 1 : slot + 1;
+}
+
+// body of local point i under the coarse correction (cnb >= 1)
+__device__ __forceinline__ int coarse_body(const CGFFParams& pr, int i) {
+  int b = 0;
+#pragma unroll
+  for (int k = 1; k < CG_COARSE_MAX; ++k) b += (k < pr.cnb && i >= pr.cstart[k]) ? 1 : 0;
+  return b;
+}
+
+// csum_t0 of v[0, K0) and, with the coarse correction, of the per-body sums
+// sum_{i in body b} w_i r_i of the owned rows; thread 0 then forms the
+// coarse coefficients c = E^-1 Z^T W r into bc[16 + b] (read after the
+// caller's next CTA barrier).
+template <int K0, int CS>
+__device__ void csum_coarse(cg::cluster_group& cl, const CGFFParams& pr, double (&v)[K0], const double* ws,
+                            const double* rs, int r0, int nr, double* red, double* pub, int& slot, double* bc) {
+  if (pr.cnb <= 0) {
+    csum_t0<K0, CS>(cl, v, nr, red, pub, slot);
+    return;
+  }
+  double u[K0 + CG_COARSE_MAX];
+#pragma unroll
+  for (int k = 0; k < K0; ++k) u[k] = v[k];
+#pragma unroll
+  for (int b = 0; b < CG_COARSE_MAX; ++b) u[K0 + b] = 0.0;
+  for (int i = threadIdx.x; i < nr; i += blockDim.x) {
+    const int bi = coarse_body(pr, r0 + i);
+    const double wr = ws[i] * rs[i];
+#pragma unroll
+    for (int b = 0; b < CG_COARSE_MAX; ++b) u[K0 + b] += b == bi ? wr : 0.0;
+  }
+  csum_t0<K0 + CG_COARSE_MAX, CS>(cl, u, nr, red, pub, slot);
+#pragma unroll
+  for (int k = 0; k < K0; ++k) v[k] = u[k];
+  if (threadIdx.x == 0)  // entries of E^-1 beyond the bodies are zero
+#pragma unroll
+    for (int a = 0; a < CG_COARSE_MAX; ++a) {
+      double c = 0.0;
+#pragma unroll
+      for (int b = 0; b < CG_COARSE_MAX; ++b) c += pr.cEinv[a * CG_COARSE_MAX + b] * u[K0 + b];
+      bc[16 + a] = c;
+    }
+}
+
+// z_i += c[body(i)] on the owned rows (coarse coefficients in bc[16..])
+__device__ __forceinline__ void add_coarse(const CGFFParams& pr, int r0, int nr, double* zs, const double* bc) {
+  if (pr.cnb <= 0) return;
+  for (int i = threadIdx.x; i < nr; i += blockDim.x) zs[i] += bc[16 + coarse_body(pr, r0 + i)];
 }
 
 // split of the owned slice into the exchange buffer's owned part
@@ -889,10 +949,10 @@ __global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(NT, MINB)
   const int rmax = (max_n + CS - 1) / CS;
   const int ldm = schur_ld(max_n);
   extern __shared__ __align__(16) unsigned char smraw[];
-  double* red = reinterpret_cast<double*>(smraw);  // 4 * threads (2 K floats per thread, K <= 4)
-  double* bc = red + 4 * NT;                       // 16: scalars broadcast by thread 0
-  double* pub = bc + 16;                           // 32: published CTA sums (8 slots x 4 float-float)
-  double* work = pub + 32;                         // 4: [0] queue index taken by rank 0
+  double* red = reinterpret_cast<double*>(smraw);  // CG_RED_K * threads (2 K floats per thread)
+  double* bc = red + CG_RED_K * NT;                // CG_BC: scalars broadcast by thread 0
+  double* pub = bc + CG_BC;                        // 8 slots x CG_RED_K float-float: published CTA sums
+  double* work = pub + 8 * CG_RED_K;               // 4: [0] queue index taken by rank 0
   double* xs = work + 4;                           // owned slices (rmax each)
   double* rs = xs + rmax;
   double* ps = rs + rmax;
@@ -964,7 +1024,7 @@ __global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(NT, MINB)
         v[2] += ws[i] * rs[i];
       }
       publish_slice(rs, r0, nr, ah, al);
-      csum_t0<3, CS>(cl, v, nr, red, pub, slot);
+      csum_coarse<3, CS>(cl, pr, v, ws, rs, r0, nr, red, pub, slot, bc);
       if (threadIdx.x == 0) {
         bc[0] = sqrt(v[0]);
         bc[1] = v[1];
@@ -982,6 +1042,7 @@ __global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(NT, MINB)
         apply_bjacobi_rows(pr, r0, r1, ah, al, yh, yl);
         __syncthreads();
         for (int i = threadIdx.x; i < nr; i += blockDim.x) zs[i] = (double)yh[i] + (double)yl[i];
+        add_coarse(pr, r0, nr, zs, bc);
       }
       __syncthreads();
       double v[1] = {0.0};
@@ -1053,7 +1114,7 @@ __global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(NT, MINB)
           v[2] += ws[i] * ri;
         }
         publish_slice(rs, r0, nr, ah, al);
-        csum_t0<3, CS>(cl, v, nr, red, pub, slot);
+        csum_coarse<3, CS>(cl, pr, v, ws, rs, r0, nr, red, pub, slot, bc);
         if (threadIdx.x == 0) {
           bc[5] = v[0];
           bc[6] = v[1];
@@ -1090,7 +1151,7 @@ __global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(NT, MINB)
           v[3] += ws[i] * ps[i];
         }
         publish_slice(rs, r0, nr, ah, al);
-        csum_t0<4, CS>(cl, v, nr, red, pub, slot);
+        csum_coarse<4, CS>(cl, pr, v, ws, rs, r0, nr, red, pub, slot, bc);
         if (threadIdx.x == 0) {
           bc[9] = v[0];
           bc[10] = v[1];
@@ -1138,6 +1199,7 @@ __global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(NT, MINB)
           apply_bjacobi_rows(pr, r0, r1, ah, al, yh, yl);
           __syncthreads();
           for (int i = threadIdx.x; i < nr; i += blockDim.x) zs[i] = (double)yh[i] + (double)yl[i];
+          add_coarse(pr, r0, nr, zs, bc);
         }
         __syncthreads();
         double v[2] = {0.0, 0.0};
@@ -1210,7 +1272,7 @@ __global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(NT, MINB)
 size_t cg_cluster_smem(int max_n, int nt, int cs) {
   const size_t rmax = (size_t)(max_n + cs - 1) / cs;
   const size_t ldm = (size_t)schur_ld(max_n);
-  return (4 * (size_t)nt + 16 + 32 + 4 + 7 * rmax + 1) * sizeof(double) +
+  return (CG_RED_K * (size_t)nt + CG_BC + 8 * CG_RED_K + 4 + 7 * rmax + 1) * sizeof(double) +
          (8 * ldm + 2 * rmax) * sizeof(float) + 64;
 }
 
@@ -1377,6 +1439,13 @@ void cgff_params_set_deflation(void* dst, double gamma, const double* zdef, doub
 
 void cgff_params_set_timing(void* dst, unsigned long long* tspan) {
   static_cast<CGFFParams*>(dst)->tspan = tspan;
+}
+
+void cgff_params_set_coarse(void* dst, int nb, const int* starts, const double* Einv) {
+  CGFFParams* p = static_cast<CGFFParams*>(dst);
+  p->cnb = nb;
+  for (int b = 0; b <= CG_COARSE_MAX; ++b) p->cstart[b] = b <= nb ? starts[b] : 0;
+  for (int k = 0; k < CG_COARSE_MAX * CG_COARSE_MAX; ++k) p->cEinv[k] = k < nb * CG_COARSE_MAX ? Einv[k] : 0.0;
 }
 
 void cgff_params_set_band(void* dst, const float* band, int band_k, const int* seg_start, const int* seg_len) {

@@ -197,7 +197,44 @@ __device__ __forceinline__ T coef_val(int code, const T* __restrict__ nx, const 
 // Deterministic scatter over the tiles that hold candidate points (the rest
 // of the output was zero-filled): one thread per cell of a 32 x 8 tile; the
 // tile's candidates (index order) are staged in shared memory 256 at a time,
-// one point per thread, then every thread sums them in that order.
+// one point per thread, and every cell sums the points of its window buckets
+// (tile_sum_bucketed) in a fixed order.
+template <typename T>
+__device__ __forceinline__ void stage_point(ScatterSmem<T>& sm, int slot, int k, const int* __restrict__ bx,
+                                            const int* __restrict__ by, const T* __restrict__ wx,
+                                            const T* __restrict__ wy, const T* __restrict__ wsc,
+                                            const T* __restrict__ nx, const T* __restrict__ ny,
+                                            const T* __restrict__ in1, int c1, const T* __restrict__ in2, int c2) {
+  T g = coef_val<T>(c1, nx, ny, k) * in1[k];
+  if (in2) g += coef_val<T>(c2, nx, ny, k) * in2[k];
+  sm.bx[slot] = bx[k];
+  sm.by[slot] = by[k];
+  sm.amp[slot] = wsc[k] * g;
+#pragma unroll
+  for (int q = 0; q < NTAP; ++q) {
+    sm.wx[slot * NTAP + q] = wx[k * NTAP + q];
+    sm.wy[slot * NTAP + q] = wy[k * NTAP + q];
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ T occupied_tile_sum(ScatterSmem<T>& sm, int p0, int p1, int x0, int i, int j,
+                                               const int* __restrict__ tpts, const int* __restrict__ bx,
+                                               const int* __restrict__ by, const T* __restrict__ wx,
+                                               const T* __restrict__ wy, const T* __restrict__ wsc,
+                                               const T* __restrict__ nx, const T* __restrict__ ny,
+                                               const T* __restrict__ in1, int c1, const T* __restrict__ in2, int c2) {
+  const int tid = threadIdx.y * TILE_X + threadIdx.x;
+  T acc = (T)0;
+  for (int c0 = p0; c0 < p1; c0 += SCAT_NB) {
+    const int nc = min(SCAT_NB, p1 - c0);
+    if (tid < nc) stage_point<T>(sm, tid, tpts[c0 + tid], bx, by, wx, wy, wsc, nx, ny, in1, c1, in2, c2);
+    acc += tile_sum_bucketed<T>(sm, nc, x0, i, j);
+    __syncthreads();
+  }
+  return acc;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(TILE_X* TILE_Y)
 k_scatter(int n1, int n2, int ntx, const int* __restrict__ ne, const int* __restrict__ ne_cnt, const int* __restrict__ tptr,
@@ -205,41 +242,13 @@ k_scatter(int n1, int n2, int ntx, const int* __restrict__ ne, const int* __rest
           const T* __restrict__ wx, const T* __restrict__ wy, const T* __restrict__ wsc, const T* __restrict__ nx,
           const T* __restrict__ ny, const T* __restrict__ in1, int c1, const T* __restrict__ in2, int c2,
           T* __restrict__ out, int accumulate) {
-  constexpr int NB = TILE_X * TILE_Y;
-  __shared__ int s_bx[NB], s_by[NB];
-  __shared__ T s_amp[NB], s_wx[NB * NTAP], s_wy[NB * NTAP];
+  __shared__ ScatterSmem<T> sm;
   if ((int)blockIdx.x >= *ne_cnt) return;  // launched for an upper bound after a device re-binning
   const int t = ne[blockIdx.x];
-  const int tx = t % ntx, ty = t / ntx;
-  const int i = tx * TILE_X + threadIdx.x;
-  const int j = ty * TILE_Y + threadIdx.y;
-  const int tid = threadIdx.y * TILE_X + threadIdx.x;
-  const int p0 = tptr[t], p1 = tptr[t + 1];
-  T acc = (T)0;
-  for (int c0 = p0; c0 < p1; c0 += NB) {
-    const int nc = min(NB, p1 - c0);
-    if (tid < nc) {
-      const int k = tpts[c0 + tid];
-      T g = coef_val<T>(c1, nx, ny, k) * in1[k];
-      if (in2) g += coef_val<T>(c2, nx, ny, k) * in2[k];
-      s_bx[tid] = bx[k];
-      s_by[tid] = by[k];
-      s_amp[tid] = wsc[k] * g;
-#pragma unroll
-      for (int q = 0; q < NTAP; ++q) {
-        s_wx[tid * NTAP + q] = wx[k * NTAP + q];
-        s_wy[tid * NTAP + q] = wy[k * NTAP + q];
-      }
-    }
-    __syncthreads();
-    for (int q = 0; q < nc; ++q) {
-      const int di = i - s_bx[q];
-      const int dj = j - s_by[q];
-      if ((unsigned)di < (unsigned)NTAP && (unsigned)dj < (unsigned)NTAP)
-        acc += s_amp[q] * s_wx[q * NTAP + di] * s_wy[q * NTAP + dj];
-    }
-    __syncthreads();
-  }
+  const int x0 = (t % ntx) * TILE_X, y0 = (t / ntx) * TILE_Y;
+  const int i = x0 + threadIdx.x, j = y0 + threadIdx.y;
+  const T acc = occupied_tile_sum<T>(sm, tptr[t], tptr[t + 1], x0, i, j, tpts, bx, by, wx, wy, wsc, nx, ny, in1, c1,
+                                     in2, c2);
   if (i < n1 && j < n2) {
     T* o = out + (size_t)j * n1 + i;
     *o = accumulate ? *o + acc : acc;
@@ -248,13 +257,12 @@ k_scatter(int n1, int n2, int ntx, const int* __restrict__ ne, const int* __rest
 
 // Overwriting scatter in one launch over the whole output, two kinds of
 // block: blocks [0, nocc) take one occupied tile each (from the list `ne`,
-// the first *ne_cnt entries; the sums of its candidate points staged in
-// shared memory in index order, the same fixed order as k_scatter), the
-// blocks after them write zeros into the empty tiles, SCAT_TPB consecutive
-// tiles (row-major tile ids) each, skipping the occupied ones.  Every tile
-// is written by exactly one block; the long occupied-tile blocks start
-// first and the zero fill's bandwidth overlaps their load latency.
-constexpr int SCAT_TPB = 8;
+// the first *ne_cnt entries; summed as in k_scatter), the blocks after them
+// write zeros into the empty tiles, SCAT_TPB consecutive tiles (row-major
+// tile ids) each, skipping the occupied ones.  Every tile is written by
+// exactly one block; the long occupied-tile blocks start first and the zero
+// fill's bandwidth overlaps their load latency.
+constexpr int SCAT_TPB = 32;
 template <typename T>
 __global__ void __launch_bounds__(TILE_X* TILE_Y)
 k_scatter_all(int n1, int n2, int ntx, int ntiles, int nocc, const int* __restrict__ ne,
@@ -263,55 +271,33 @@ k_scatter_all(int n1, int n2, int ntx, int ntiles, int nocc, const int* __restri
               const T* __restrict__ wy, const T* __restrict__ wsc, const T* __restrict__ nx,
               const T* __restrict__ ny, const T* __restrict__ in1, int c1, const T* __restrict__ in2, int c2,
               T* __restrict__ out) {
-  constexpr int NB = TILE_X * TILE_Y;
   __shared__ int s_ptr[SCAT_TPB + 1];
-  __shared__ int s_bx[NB], s_by[NB];
-  __shared__ T s_amp[NB], s_wx[NB * NTAP], s_wy[NB * NTAP];
+  __shared__ ScatterSmem<T> sm;
   const int tid = threadIdx.y * TILE_X + threadIdx.x;
   if ((int)blockIdx.x >= nocc) {  // zero writer
     const int t0 = ((int)blockIdx.x - nocc) * SCAT_TPB;
     if (tid <= SCAT_TPB) s_ptr[tid] = tptr[min(t0 + tid, ntiles)];
     __syncthreads();
-    for (int q = 0; q < SCAT_TPB; ++q) {
-      const int t = t0 + q;
-      if (t >= ntiles) break;
-      if (s_ptr[q + 1] > s_ptr[q]) continue;  // occupied: an occupied-tile block writes it
-      const int i = (t % ntx) * TILE_X + threadIdx.x;
-      const int j = (t / ntx) * TILE_Y + threadIdx.y;
-      if (i < n1 && j < n2) out[(size_t)j * n1 + i] = (T)0;
+    const int nt = min(SCAT_TPB, ntiles - t0);
+    int tx = t0 % ntx, ty = t0 / ntx;
+    for (int q = 0; q < nt; ++q) {
+      if (s_ptr[q + 1] == s_ptr[q]) {  // empty (an occupied-tile block writes the others)
+        const int i = tx * TILE_X + threadIdx.x, j = ty * TILE_Y + threadIdx.y;
+        if (i < n1 && j < n2) out[(size_t)j * n1 + i] = (T)0;
+      }
+      if (++tx == ntx) {
+        tx = 0;
+        ++ty;
+      }
     }
     return;
   }
   if ((int)blockIdx.x >= *ne_cnt) return;  // launched for an upper bound after a device re-binning
   const int t = ne[blockIdx.x];
-  const int i = (t % ntx) * TILE_X + threadIdx.x;
-  const int j = (t / ntx) * TILE_Y + threadIdx.y;
-  const int p0 = tptr[t], p1 = tptr[t + 1];
-  T acc = (T)0;
-  for (int c0 = p0; c0 < p1; c0 += NB) {
-    const int nc = min(NB, p1 - c0);
-    if (tid < nc) {
-      const int k = tpts[c0 + tid];
-      T g = coef_val<T>(c1, nx, ny, k) * in1[k];
-      if (in2) g += coef_val<T>(c2, nx, ny, k) * in2[k];
-      s_bx[tid] = bx[k];
-      s_by[tid] = by[k];
-      s_amp[tid] = wsc[k] * g;
-#pragma unroll
-      for (int e = 0; e < NTAP; ++e) {
-        s_wx[tid * NTAP + e] = wx[k * NTAP + e];
-        s_wy[tid * NTAP + e] = wy[k * NTAP + e];
-      }
-    }
-    __syncthreads();
-    for (int e = 0; e < nc; ++e) {
-      const int di = i - s_bx[e];
-      const int dj = j - s_by[e];
-      if ((unsigned)di < (unsigned)NTAP && (unsigned)dj < (unsigned)NTAP)
-        acc += s_amp[e] * s_wx[e * NTAP + di] * s_wy[e * NTAP + dj];
-    }
-    __syncthreads();
-  }
+  const int x0 = (t % ntx) * TILE_X, y0 = (t / ntx) * TILE_Y;
+  const int i = x0 + threadIdx.x, j = y0 + threadIdx.y;
+  const T acc = occupied_tile_sum<T>(sm, tptr[t], tptr[t + 1], x0, i, j, tpts, bx, by, wx, wy, wsc, nx, ny, in1, c1,
+                                     in2, c2);
   if (i < n1 && j < n2) out[(size_t)j * n1 + i] = acc;
 }
 
@@ -849,6 +835,7 @@ int cache_rebin_points(ilm_cache_s* c, const double* x, const double* y, const d
   c->S_dir_ready = false;
   c->S_neu_ready = false;
   c->filt_ready = false;
+  c->stokes_pc_ready = false;
   return ILM_OK;
 }
 

@@ -151,6 +151,95 @@ constexpr int TILE_Y = 8;
 // coefficient codes for fused point-wise products
 enum Coef { CF_ZERO = 0, CF_ONE = 1, CF_NX = 2, CF_NY = 3, CF_MNX = 4, CF_MNY = 5, CF_MONE = 6 };
 
+// ---------------------------------------------------------------------------
+// Deterministic tile scatter (regularize!): one 256-thread CTA per occupied
+// TILE_X x TILE_Y tile, one thread per cell.  The tile's candidate points are
+// staged in shared memory up to 256 at a time (the caller fills bx, by, amp
+// = weight x data, wx, wy for staging slots [0, nc)).  A point's window
+// starts at column bx, so it reaches the tile's column li only if bx lies in
+// x0 + li - (NTAP - 1) .. x0 + li: the staged points are bucketed by
+// key = bx - x0 + NTAP - 1 (TILE_X + NTAP - 1 keys) and each cell visits
+// only its NTAP buckets, about NTAP / (TILE_X + NTAP - 1) of the points
+// instead of all of them.  The buckets are ordered by key, then by staging
+// slot (warp match groups and per-warp offsets, no atomics), so every cell
+// sums its points in a fixed order.
+// ---------------------------------------------------------------------------
+constexpr int SCAT_NB = TILE_X * TILE_Y;
+constexpr int SCAT_NKEY = TILE_X + NTAP - 1;
+
+template <typename T>
+struct ScatterSmem {
+  int bx[SCAT_NB], by[SCAT_NB];
+  T amp[SCAT_NB], wx[SCAT_NB * NTAP], wy[SCAT_NB * NTAP];
+  int wcnt[SCAT_NB / 32][SCAT_NKEY];  // per-warp bucket counts, then offsets
+  int start[SCAT_NKEY + 1];
+  unsigned short perm[SCAT_NB];       // sorted position -> staging slot
+};
+
+// sum of the staged points' contributions to cell (i, j) of the tile whose
+// first column is x0; all threads of the CTA call it (it synchronises the
+// CTA; the caller synchronises again before restaging)
+template <typename T>
+__device__ __forceinline__ T tile_sum_bucketed(ScatterSmem<T>& sm, int nc, int x0, int i, int j) {
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int q = tid; q < (SCAT_NB / 32) * SCAT_NKEY; q += SCAT_NB) (&sm.wcnt[0][0])[q] = 0;
+  __syncthreads();  // staged points and zeroed counts visible
+  int key = SCAT_NKEY;  // idle slot
+  if (tid < nc) key = min(max(sm.bx[tid] - x0 + (NTAP - 1), 0), SCAT_NKEY - 1);
+  const unsigned grp = __match_any_sync(0xffffffffu, key);
+  const int rank = __popc(grp & ((1u << lane) - 1u));
+  if (key < SCAT_NKEY && rank == 0) sm.wcnt[warp][key] = __popc(grp);
+  __syncthreads();
+  if (warp == 0) {  // exclusive scan of the bucket totals; per-warp offsets
+    int t0 = 0, t1 = 0;
+    for (int w = 0; w < SCAT_NB / 32; ++w) {
+      t0 += lane < SCAT_NKEY ? sm.wcnt[w][lane] : 0;
+      t1 += lane + 32 < SCAT_NKEY ? sm.wcnt[w][lane + 32] : 0;
+    }
+    int i0 = t0, i1 = t1;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int a = __shfl_up_sync(0xffffffffu, i0, o), b = __shfl_up_sync(0xffffffffu, i1, o);
+      if (lane >= o) {
+        i0 += a;
+        i1 += b;
+      }
+    }
+    const int s0 = __shfl_sync(0xffffffffu, i0, 31);
+    int e0 = i0 - t0, e1 = s0 + i1 - t1;
+    if (lane < SCAT_NKEY) {
+      sm.start[lane] = e0;
+      for (int w = 0; w < SCAT_NB / 32; ++w) {
+        const int c = sm.wcnt[w][lane];
+        sm.wcnt[w][lane] = e0;
+        e0 += c;
+      }
+    }
+    if (lane + 32 < SCAT_NKEY) {
+      sm.start[lane + 32] = e1;
+      for (int w = 0; w < SCAT_NB / 32; ++w) {
+        const int c = sm.wcnt[w][lane + 32];
+        sm.wcnt[w][lane + 32] = e1;
+        e1 += c;
+      }
+    }
+    if (lane == 0) sm.start[SCAT_NKEY] = nc;
+  }
+  __syncthreads();
+  if (key < SCAT_NKEY) sm.perm[sm.wcnt[warp][key] + rank] = (unsigned short)tid;
+  __syncthreads();
+  const int li = min(max(i - x0, 0), TILE_X - 1);
+  T acc = (T)0;
+  for (int q = sm.start[li], qe = sm.start[li + NTAP]; q < qe; ++q) {
+    const int e = sm.perm[q];
+    const int di = i - sm.bx[e];
+    const int dj = j - sm.by[e];
+    if ((unsigned)di < (unsigned)NTAP && (unsigned)dj < (unsigned)NTAP)
+      acc += sm.amp[e] * sm.wx[e * NTAP + di] * sm.wy[e * NTAP + dj];
+  }
+  return acc;
+}
+
 template <typename T>
 struct PointWin {
   // [npts] base indices and [npts*4] weights for x-primal, x-dual, y-primal, y-dual
@@ -332,6 +421,10 @@ struct ilm_cache_s {
   // surface filter: W = E R 1 (cache dtype) and a grid buffer of the cache's class
   ilm::DevBuf filt_diag, filt_grid;
   bool filt_ready = false;
+  // Stokes preconditioner: inverse of the gauge-shifted Nodes{Primal} Schur
+  // complement -E L^-1 E^T (FP64, N x N), built on first use
+  ilm::DevBuf stokes_pc;
+  bool stokes_pc_ready = false;
   ilm::DevBuf red;                     // reduction scratch (double)
   // FP64 iterative refinement (ilm_solve_*_refined): an FP64 cache of the same
   // points (FP32 caches only; built on first use, dropped when points move)
@@ -476,7 +569,8 @@ int st_point_dot(int n, int dtype, const void* a, const void* b, const double* w
                  cudaStream_t st);
 
 // Schur (ilm_schur.cu)
-int schur_build(ilm_cache_s* c, int which, double scale, double* A, cudaStream_t st);
+// any_cache: also on vector caches (their Nodes{Primal} / Nodes{Dual} windows)
+int schur_build(ilm_cache_s* c, int which, double scale, double* A, cudaStream_t st, bool any_cache = false);
 struct CGParams {
   const double* A64;   // n x n column-major
   const float* A32;    // n x n column-major
@@ -538,6 +632,10 @@ void cgff_params_set_deflation(void* dst, double gamma, const double* zdef, doub
 // per-problem timing of the cluster CG (3 u64 per problem: start ns, end ns, SM), nullptr: off
 void cgff_params_set_timing(void* dst, unsigned long long* tspan);
 void cgff_params_set_band(void* dst, const float* band, int band_k, const int* seg_start, const int* seg_len);
+// coarse correction of block-Jacobi on up to CG_COARSE_MAX bodies' constants:
+// starts[0..nb] local body boundaries, Einv nb x CG_COARSE_MAX row-major
+constexpr int CG_COARSE_MAX = 4;
+void cgff_params_set_coarse(void* dst, int nb, const int* starts, const double* Einv);
 void cgff_params_fill_csr(void* dst, const float* vhi, const float* vlo, const int* rowptr, const int* colidx,
                           const double* b, double* x, const double* x0, const double* w, int n, int maxiter,
                           double tol, int* iters, double* relres);

@@ -180,7 +180,7 @@ __global__ void k_nrtrn(int N, const int* __restrict__ bxP, const int* __restric
   A[(size_t)l * N + k] = scale * w[l] * (nx[k] * nx[l] * su + ny[k] * ny[l] * sv);
 }
 
-int schur_build(ilm_cache_s* c, int which, double scale, double* A, cudaStream_t st) {
+int schur_build(ilm_cache_s* c, int which, double scale, double* A, cudaStream_t st, bool any_cache) {
   const int N = c->npts;
   if (N == 0) return ILM_OK;
   const ilm_grid_s& g = c->grid;
@@ -202,7 +202,7 @@ int schur_build(ilm_cache_s* c, int which, double scale, double* A, cudaStream_t
     ILM_CHECK_CUDA(cudaStreamSynchronize(st));
     return ILM_OK;
   }
-  if (c->kind == ILM_CACHE_VECTOR) {
+  if (c->kind == ILM_CACHE_VECTOR && !any_cache) {
     set_error("dense Schur build for vector caches not supported");
     return ILM_ERR_UNSUPPORTED;
   }

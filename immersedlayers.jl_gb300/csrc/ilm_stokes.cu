@@ -1,5 +1,6 @@
 // Stokes flow with no-slip surfaces on a vector cache: the reference's
-// StokesFlowProblem `solve` (test/literate/stokes.jl:101-166) on the device.
+// StokesFlowProblem `solve` (test/literate/stokes.jl:101-166) on the device,
+// for one or several velocity right-hand sides at once.
 //
 //   psi*  = L^-2 (-C D_s^symm [v])            (surface viscous flux, twice inverted)
 //   phi   = L^-1 R (n . [v]);  v_phi = G phi   (normal-velocity jump)
@@ -12,10 +13,26 @@
 // The reference forms S and Ss densely (2N and N columns of operator
 // applications) and LU-solves them.  L^-2 is two grid-truncated LGF
 // convolutions, which is not translation invariant, so S has no point-pair
-// closed form; here both Schur systems are solved matrix-free by CG in the
-// ds-weighted inner product (W S symmetric, S negative definite, Ss positive
-// semi-definite), each iteration one surface curl, one or two LGF FFT
-// convolutions and one surface curl back -- no N x N matrix is formed.
+// closed form.  Both Schur systems are solved matrix-free, in the symmetric
+// form y = W sigma (W = diag(ds)): -S W^-1 and Ss W^-1 are symmetric
+// positive semi-definite.  All right-hand sides are solved together by block
+// CG: each iteration applies the operator to every column of the direction
+// block, A-orthonormalises the block (eigen-decomposition of its s x s Gram
+// matrix; directions that have become dependent are dropped), and forms the
+// step and the next direction block from s x s products.  The right-hand
+// sides share the slowly converging modes (the near-null modes of thin
+// bodies), which the block recurrence resolves for all of them at once.
+//
+// Preconditioner of S: -C_s L^-2 C_s^T and the single layer -E L^-1 E^T are
+// pseudo-differential operators of the same order (the Stokeslet and the
+// log kernel), so the inverse of the Nodes{Primal} Schur complement
+// P = -E L^-1 E^T (LGF point-point sums, as create_RTLinvR), applied to each
+// velocity component, bounds the condition number independently of the
+// point count on smooth bodies.  P is indefinite in its constant mode (the
+// LGF's logarithm changes sign at large distances); adding c 1 1^T with
+// c = 2 |1^T P 1| / N^2 makes it positive definite.  Its inverse is formed
+// once per cache by Gauss-Jordan elimination on the device (positive pivots
+// are checked; c grows if one is not) and applied as a dense product.
 //
 // The filter F = W^-1 E R, W = diag(E R 1): the filtered interpolation of
 // CartesianGrids' Regularize(filter = true) (un-vendored) restated from
@@ -25,6 +42,7 @@
 
 #include <algorithm>
 #include <functional>
+#include <vector>
 
 #include "ilm_internal.cuh"
 
@@ -42,73 +60,387 @@ __global__ void k_ndot(int n, const T* __restrict__ nx, const T* __restrict__ ny
   if (k < n) out[k] = nx[k] * v[k] + ny[k] * v[n + k];
 }
 
-struct Work {
-  DevBuf e1, e2, d1, d2, p1, v1, v2, v3, v4, v5, s1, s2, s3, s4, s5, diag;
+constexpr int STOKES_PC_MAX = 4096;  // largest N with a preconditioner (N x N FP64 inverse)
+
+template <typename T>
+__global__ void k_to_op(int n, int N, const double* __restrict__ y, const double* __restrict__ ds,
+                        T* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (T)(y[i] / ds[i % N]);
+}
+
+template <typename T>
+__global__ void k_from_op(int n, const T* __restrict__ in, double sgn, double* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = sgn * (double)in[i];
+}
+
+// G[i + j sa] = sum_k A[k + i lda] B[k + j ldb]; one CTA per entry
+// (deterministic order)
+__global__ void __launch_bounds__(256) k_gram(int n, const double* __restrict__ A, int lda, int sa,
+                                              const double* __restrict__ B, int ldb, double* __restrict__ G) {
+  __shared__ double red[8];
+  const int i = blockIdx.x % sa, j = blockIdx.x / sa;
+  const double* a = A + (size_t)i * lda;
+  const double* b = B + (size_t)j * ldb;
+  double acc = 0.0;
+  for (int k = threadIdx.x; k < n; k += blockDim.x) acc = fma(a[k], b[k], acc);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    G[blockIdx.x] = t;
+  }
+}
+
+// C (n x t) = alpha A (n x k) B (k x t) + beta C, column-major; one thread
+// per row, eight columns of C per pass.  beta = 0 does not read C.
+__global__ void __launch_bounds__(256) k_gemm_rows(int n, int k, int t, const double* __restrict__ A, int lda,
+                                                   const double* __restrict__ B, int ldb, double alpha, double beta,
+                                                   double* C, int ldc) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int j0 = 0; j0 < t; j0 += 8) {
+    double acc[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) acc[q] = 0.0;
+    const int nj = min(8, t - j0);
+    for (int kk = 0; kk < k; ++kk) {
+      const double a = A[i + (size_t)kk * lda];
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (q < nj) acc[q] = fma(a, __ldg(B + kk + (size_t)(j0 + q) * ldb), acc[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      if (q >= nj) break;
+      double* cp = C + i + (size_t)(j0 + q) * ldc;
+      *cp = beta == 0.0 ? alpha * acc[q] : fma(alpha, acc[q], beta * *cp);
+    }
+  }
+}
+
+// T = sym(Sp diag(1/ds)) + shift (N x N); sums[blockIdx] = partial sums of
+// the unshifted entries for the shift
+__global__ void k_pc_form(int N, const double* __restrict__ Sp, const double* __restrict__ ds, double shift,
+                          double* __restrict__ T) {
+  const size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (idx >= (size_t)N * N) return;
+  const int i = (int)(idx % N), j = (int)(idx / N);
+  T[idx] = 0.5 * (Sp[idx] / ds[j] + Sp[j + (size_t)i * N] / ds[i]) + shift;
+}
+
+__global__ void __launch_bounds__(256) k_pc_sum(int N, const double* __restrict__ Sp, const double* __restrict__ ds,
+                                                double* __restrict__ out) {
+  __shared__ double red[8];
+  const int j = blockIdx.x;  // one CTA per column, deterministic
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) acc += Sp[i + (size_t)j * N];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < 8; ++w) t += red[w];
+    out[j] = t / ds[j];
+  }
+}
+
+// Gauss-Jordan inversion in place without pivoting (T symmetric positive
+// definite): step k turns column k into a column of the inverse.  The pivot
+// column and row of step k (old values) come from colk / rowk; the new
+// column and row k + 1 are written to coln / rown for the next step.  A
+// non-positive pivot records k + 1 in *bad (first one wins) and is replaced
+// by 1 so that the remaining steps stay finite.
+__global__ void k_gj_init(int N, const double* __restrict__ T, double* __restrict__ col, double* __restrict__ row) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < N) {
+    col[i] = T[i];
+    row[i] = T[(size_t)i * N];
+  }
+}
+
+__global__ void k_gj_step(int N, int k, double* __restrict__ T, const double* __restrict__ colk,
+                          const double* __restrict__ rowk, double* __restrict__ coln, double* __restrict__ rown,
+                          int* __restrict__ bad) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= N || j >= N) return;
+  double p = rowk[k];
+  if (!(p > 0.0)) {
+    if (i == 0 && j == 0) atomicCAS(bad, 0, k + 1);
+    p = 1.0;
+  }
+  const double ip = 1.0 / p;
+  double v;
+  if (i == k)
+    v = j == k ? ip : rowk[j] * ip;
+  else if (j == k)
+    v = -colk[i] * ip;
+  else
+    v = T[i + (size_t)j * N] - colk[i] * rowk[j] * ip;
+  T[i + (size_t)j * N] = v;
+  if (j == k + 1) coln[i] = v;
+  if (i == k + 1) rown[j] = v;
+}
+
+int ensure_stokes_pc(ilm_cache_s* c, cudaStream_t st) {
+  if (c->stokes_pc_ready) return ILM_OK;
+  const int N = c->npts;
+  const size_t nn = (size_t)N * N;
+  DevBuf Sp, sums, gj, bad;
+  ILM_TRY(Sp.alloc(nn * sizeof(double)));
+  ILM_TRY(c->stokes_pc.alloc(nn * sizeof(double)));
+  ILM_TRY(sums.alloc((size_t)N * sizeof(double)));
+  ILM_TRY(gj.alloc((size_t)4 * N * sizeof(double)));
+  ILM_TRY(bad.alloc(sizeof(int)));
+  ILM_TRY(schur_build(c, ILM_SCHUR_RTLINVR, 1.0, Sp.as<double>(), st, true));
+  k_pc_sum<<<N, 256, 0, st>>>(N, Sp.as<double>(), c->ds64.as<double>(), sums.as<double>());
+  ILM_CHECK_LAUNCH();
+  std::vector<double> hs(N);
+  ILM_CHECK_CUDA(cudaMemcpyAsync(hs.data(), sums.p, N * sizeof(double), cudaMemcpyDeviceToHost, st));
+  ILM_CHECK_CUDA(cudaStreamSynchronize(st));
+  double tot = 0.0;
+  for (double v : hs) tot += v;
+  double shift = 2.0 * fabs(tot) / ((double)N * N);
+  if (!(shift > 0.0)) shift = 1e-300;
+  double* T = c->stokes_pc.as<double>();
+  double* cb[2] = {gj.as<double>(), gj.as<double>() + N};
+  double* rb[2] = {gj.as<double>() + 2 * N, gj.as<double>() + 3 * N};
+  const dim3 blk(32, 8), grd((N + 31) / 32, (N + 7) / 8);
+  for (int attempt = 0; attempt < 4; ++attempt, shift *= 8.0) {
+    k_pc_form<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(N, Sp.as<double>(), c->ds64.as<double>(), shift, T);
+    ILM_CHECK_LAUNCH();
+    ILM_CHECK_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(int), st));
+    k_gj_init<<<(N + 255) / 256, 256, 0, st>>>(N, T, cb[0], rb[0]);
+    ILM_CHECK_LAUNCH();
+    for (int k = 0; k < N; ++k) {
+      k_gj_step<<<grd, blk, 0, st>>>(N, k, T, cb[k & 1], rb[k & 1], cb[(k + 1) & 1], rb[(k + 1) & 1],
+                                     bad.as<int>());
+      ILM_CHECK_LAUNCH();
+    }
+    int hb = 0;
+    ILM_CHECK_CUDA(cudaMemcpyAsync(&hb, bad.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    ILM_CHECK_CUDA(cudaStreamSynchronize(st));
+    if (hb == 0) {
+      c->stokes_pc_ready = true;
+      return ILM_OK;
+    }
+  }
+  set_error("solve_stokes: preconditioner not positive definite after 4 shifts");
+  return ILM_ERR_NOT_CONVERGED;
+}
+
+// eigen-decomposition of a symmetric s x s matrix (cyclic Jacobi rotations);
+// A (row-major) is destroyed, lam[j] and column j of V (row-major) are the
+// eigenpairs
+void sym_eig(int s, std::vector<double>& A, std::vector<double>& lam, std::vector<double>& V) {
+  V.assign((size_t)s * s, 0.0);
+  for (int i = 0; i < s; ++i) V[i * s + i] = 1.0;
+  for (int sweep = 0; sweep < 60; ++sweep) {
+    double off = 0.0, tot = 0.0;
+    for (int i = 0; i < s; ++i)
+      for (int j = 0; j < s; ++j) {
+        tot += A[i * s + j] * A[i * s + j];
+        if (i != j) off += A[i * s + j] * A[i * s + j];
+      }
+    if (off <= 1e-30 * tot || tot == 0.0) break;
+    for (int p = 0; p < s; ++p)
+      for (int q = p + 1; q < s; ++q) {
+        const double apq = A[p * s + q];
+        if (apq == 0.0) continue;
+        const double theta = (A[q * s + q] - A[p * s + p]) / (2.0 * apq);
+        const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+        const double cs = 1.0 / sqrt(t * t + 1.0), sn = t * cs;
+        for (int k = 0; k < s; ++k) {  // A <- A J  (columns p, q)
+          const double akp = A[k * s + p], akq = A[k * s + q];
+          A[k * s + p] = cs * akp - sn * akq;
+          A[k * s + q] = sn * akp + cs * akq;
+        }
+        for (int k = 0; k < s; ++k) {  // A <- J^T A  (rows p, q)
+          const double apk = A[p * s + k], aqk = A[q * s + k];
+          A[p * s + k] = cs * apk - sn * aqk;
+          A[q * s + k] = sn * apk + cs * aqk;
+        }
+        for (int k = 0; k < s; ++k) {
+          const double vkp = V[k * s + p], vkq = V[k * s + q];
+          V[k * s + p] = cs * vkp - sn * vkq;
+          V[k * s + q] = sn * vkp + cs * vkq;
+        }
+      }
+  }
+  lam.resize(s);
+  for (int i = 0; i < s; ++i) lam[i] = A[i * s + i];
+}
+
+// Q (n x s) = B Y (n x s), the operator applied column by column
+using BlockApply = std::function<int(const double*, double*, int)>;
+// Z (n x s) = M R (n x s)
+using BlockPrec = std::function<int(const double*, double*, int)>;
+
+struct BlockCG {
+  int n = 0, s = 0;
+  DevBuf R, Z, P, Q, Pn, Qn, G1, G2, small;
 };
 
-using Apply = std::function<int(const void*, void*)>;
+int gram(const double* A, int sa, const double* B, int sb, int n, double* dG, std::vector<double>& hG,
+         cudaStream_t st, bool sync = true) {
+  k_gram<<<sa * sb, 256, 0, st>>>(n, A, n, sa, B, n, dG);
+  ILM_CHECK_LAUNCH();
+  hG.resize((size_t)sa * sb);
+  ILM_CHECK_CUDA(cudaMemcpyAsync(hG.data(), dG, (size_t)sa * sb * sizeof(double), cudaMemcpyDeviceToHost, st));
+  if (sync) ILM_CHECK_CUDA(cudaStreamSynchronize(st));
+  return ILM_OK;
+}
 
-// CG on A x = b in the ds-weighted inner product (dots through
-// ilm_dot_surface: FP64, host-synchronised).  x starts at 0.
-int cg_matfree(ilm_cache_t c, int ncomp, const Apply& A, const void* b, void* x, void* r, void* p, void* q,
-               double tol, int maxiter, int* iters, double* relres, cudaStream_t st) {
-  const size_t n = (size_t)ncomp * c->npts;
-  const int dt = c->dtype;
-  ILM_TRY(st_fill(n, dt, 0.0, x, st));
-  ILM_TRY(st_affine(n, dt, 1.0, b, 0.0, r, st));
-  ILM_TRY(st_affine(n, dt, 1.0, b, 0.0, p, st));
-  double bb = 0.0, rz = 0.0;
-  // unweighted norm of b for the residual test: weights are ds, so use the
-  // weighted dot for CG and an unweighted norm through a unit-weight pass
-  auto unweighted = [&](const void* a, double* out) -> int {
-    double tot = 0.0;
-    for (int i = 0; i < ncomp; ++i) {
-      ILM_TRY(st_point_dot(c->npts, dt, elem_ptr(a, (size_t)i * c->npts, dt), elem_ptr(a, (size_t)i * c->npts, dt),
-                           nullptr, c->red.as<double>(), st));
-      double v = 0.0;
-      ILM_CHECK_CUDA(cudaMemcpyAsync(&v, c->red.as<double>(), sizeof(double), cudaMemcpyDeviceToHost, st));
-      ILM_CHECK_CUDA(cudaStreamSynchronize(st));
-      tot += v;
-    }
-    *out = tot;
+int gemm(int n, int k, int t, const double* A, const double* B, double alpha, double beta, double* C,
+         cudaStream_t st) {
+  if (n == 0 || t == 0) return ILM_OK;
+  k_gemm_rows<<<(n + 255) / 256, 256, 0, st>>>(n, k, t, A, n, B, k, alpha, beta, C, n);
+  ILM_CHECK_LAUNCH();
+  return ILM_OK;
+}
+
+// Block CG on B Y = Bb (n x s, FP64 device, column-major); Y = 0 at start.
+// relres[j] = ||Bb_j - B Y_j|| / ||Bb_j|| (recomputed from B Y at the end).
+// `drop`: directions whose A-norm^2 falls below drop x the largest are
+// discarded (the operator's rounding level: an FP32 operator is only
+// symmetric to ~1e-7).  The iterate with the smallest worst-column residual
+// is kept; the recurrence stops when that residual grows a thousandfold
+// (an FP32 operator below its attainable accuracy) and returns the kept one.
+int block_cg(int n, int s, const BlockApply& A, const BlockPrec* M, const double* Bb, double* Y, double tol,
+             int maxiter, double drop, int* iters, double* relres, cudaStream_t st) {
+  const size_t nb = (size_t)n * s * sizeof(double);
+  BlockCG w;
+  DevBuf Ybest;
+  for (DevBuf* b : {&w.R, &w.Z, &w.P, &w.Q, &w.Pn, &w.Qn, &Ybest}) ILM_TRY(b->alloc(std::max<size_t>(nb, 8)));
+  ILM_TRY(w.G1.alloc((size_t)s * s * sizeof(double)));
+  ILM_TRY(w.G2.alloc((size_t)s * s * sizeof(double)));
+  ILM_TRY(w.small.alloc((size_t)s * s * sizeof(double)));
+  double *R = w.R.as<double>(), *Z = w.Z.as<double>(), *P = w.P.as<double>(), *Q = w.Q.as<double>();
+  double *Pn = w.Pn.as<double>(), *Qn = w.Qn.as<double>(), *dsm = w.small.as<double>();
+  ILM_CHECK_CUDA(cudaMemsetAsync(Y, 0, nb, st));
+  ILM_CHECK_CUDA(cudaMemcpyAsync(R, Bb, nb, cudaMemcpyDeviceToDevice, st));
+  std::vector<double> hg, hr, bn(s);
+  ILM_TRY(gram(Bb, s, Bb, s, n, w.G1.as<double>(), hg, st));
+  bool all_zero = true;
+  for (int j = 0; j < s; ++j) {
+    bn[j] = sqrt(std::max(hg[j + (size_t)j * s], 0.0));
+    relres[j] = bn[j] > 0.0 ? 1.0 : 0.0;
+    all_zero = all_zero && bn[j] == 0.0;
+  }
+  *iters = 0;
+  if (all_zero || n == 0) return ILM_OK;
+  auto precond = [&](const double* r, double* z) -> int {
+    if (M) return (*M)(r, z, s);
+    ILM_CHECK_CUDA(cudaMemcpyAsync(z, r, nb, cudaMemcpyDeviceToDevice, st));
     return ILM_OK;
   };
-  ILM_TRY(unweighted(b, &bb));
-  ILM_TRY(ilm_dot_surface(c, ncomp, r, r, &rz, st));
-  const double bn = sqrt(bb);
-  int it = 0;
-  double rel = bn > 0 ? 1.0 : 0.0;
-  if (bn == 0.0) {
-    *iters = 0;
-    *relres = 0.0;
+  auto residual_norms = [&](std::vector<double>& out) -> int {
+    std::vector<double> d;
+    ILM_TRY(gram(R, s, R, s, n, w.G2.as<double>(), d, st));
+    out.resize(s);
+    for (int j = 0; j < s; ++j)
+      out[j] = bn[j] > 0.0 ? sqrt(std::max(d[j + (size_t)j * s], 0.0)) / bn[j] : 0.0;
     return ILM_OK;
-  }
-  while (it < maxiter) {
-    ILM_TRY(A(p, q));
-    double pq = 0.0;
-    ILM_TRY(ilm_dot_surface(c, ncomp, p, q, &pq, st));
-    if (pq == 0.0) break;
-    const double alpha = rz / pq;
-    ILM_TRY(st_axpby(n, dt, alpha, p, 1.0, x, x, st));
-    ILM_TRY(st_axpby(n, dt, -alpha, q, 1.0, r, r, st));
+  };
+  ILM_TRY(precond(R, P));
+  int sp = s;  // columns of the direction block
+  std::vector<double> lam, V, Tm, hab;
+  int it = 0;
+  bool done = false, have_best = false;
+  double best = 1.0;  // worst-column residual of Ybest (Y = 0 at start)
+  auto worst = [&](const std::vector<double>& r) {
+    double m = 0.0;
+    for (double v : r) m = (v > m || v != v) ? v : m;
+    return m;
+  };
+  while (it < maxiter && !done) {
+    ILM_TRY(A(P, Q, sp));
+    // A-orthonormalise the direction block: G = P^T Q = V diag(lam) V^T
+    ILM_TRY(gram(P, sp, Q, sp, n, w.G1.as<double>(), hg, st));
+    std::vector<double> Gs((size_t)sp * sp);
+    for (int i = 0; i < sp; ++i)
+      for (int j = 0; j < sp; ++j) Gs[i * sp + j] = 0.5 * (hg[i + (size_t)j * sp] + hg[j + (size_t)i * sp]);
+    sym_eig(sp, Gs, lam, V);
+    double lmax = 0.0;
+    for (double l : lam) lmax = std::max(lmax, l);
+    std::vector<int> keep;
+    for (int j = 0; j < sp; ++j)
+      if (lam[j] > drop * lmax && lam[j] > 0.0) keep.push_back(j);
+    const int sk = (int)keep.size();
+    if (sk == 0) break;  // no direction left (stagnation)
+    Tm.assign((size_t)sp * sk, 0.0);  // column-major sp x sk
+    for (int q = 0; q < sk; ++q)
+      for (int i = 0; i < sp; ++i) Tm[i + (size_t)q * sp] = V[i * sp + keep[q]] / sqrt(lam[keep[q]]);
+    ILM_CHECK_CUDA(cudaMemcpyAsync(dsm, Tm.data(), Tm.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+    ILM_TRY(gemm(n, sp, sk, P, dsm, 1.0, 0.0, Pn, st));
+    ILM_TRY(gemm(n, sp, sk, Q, dsm, 1.0, 0.0, Qn, st));
+    // alpha = Pn^T R; Y += Pn alpha; R -= Qn alpha
+    ILM_TRY(gram(Pn, sk, R, s, n, w.G1.as<double>(), hab, st));
+    ILM_CHECK_CUDA(cudaMemcpyAsync(dsm, hab.data(), hab.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+    ILM_TRY(gemm(n, sk, s, Pn, dsm, 1.0, 1.0, Y, st));
+    ILM_TRY(gemm(n, sk, s, Qn, dsm, -1.0, 1.0, R, st));
     ++it;
-    double rr = 0.0;
-    ILM_TRY(unweighted(r, &rr));
-    rel = sqrt(rr) / bn;
-    if (rel <= tol || it % 50 == 0) {  // true residual
-      ILM_TRY(A(x, q));
-      ILM_TRY(st_axpby(n, dt, 1.0, b, -1.0, q, r, st));
-      ILM_TRY(unweighted(r, &rr));
-      rel = sqrt(rr) / bn;
-      if (rel <= tol) break;
+    ILM_TRY(residual_norms(hr));
+    const double wr = worst(hr);
+    if (wr < best) {
+      best = wr;
+      have_best = true;
+      ILM_CHECK_CUDA(cudaMemcpyAsync(Ybest.p, Y, nb, cudaMemcpyDeviceToDevice, st));
     }
-    double rzn = 0.0;
-    ILM_TRY(ilm_dot_surface(c, ncomp, r, r, &rzn, st));
-    ILM_TRY(st_axpby(n, dt, 1.0, r, rzn / rz, p, p, st));
-    rz = rzn;
+    const bool diverged = !(wr <= 1e3 * best);
+    bool conv = true;
+    for (int j = 0; j < s; ++j) conv = conv && hr[j] <= tol;
+    if (diverged) {  // back to the best iterate; its true residual
+      if (have_best)
+        ILM_CHECK_CUDA(cudaMemcpyAsync(Y, Ybest.p, nb, cudaMemcpyDeviceToDevice, st));
+      else
+        ILM_CHECK_CUDA(cudaMemsetAsync(Y, 0, nb, st));
+      ILM_TRY(A(Y, Q, s));
+      ILM_TRY(st_axpby((size_t)n * s, ILM_F64, 1.0, Bb, -1.0, Q, R, st));
+      ILM_TRY(residual_norms(hr));
+      for (int j = 0; j < s; ++j) relres[j] = hr[j];
+      break;
+    }
+    if (conv || it == maxiter) {  // true residual
+      ILM_TRY(A(Y, Q, s));
+      ILM_TRY(st_axpby((size_t)n * s, ILM_F64, 1.0, Bb, -1.0, Q, R, st));  // R = Bb - B Y
+      ILM_TRY(residual_norms(hr));
+      conv = true;
+      for (int j = 0; j < s; ++j) conv = conv && hr[j] <= tol;
+      if (conv) done = true;
+      if (!conv && it == maxiter && have_best && worst(hr) > best) {  // the kept iterate, if better
+        std::vector<double> hb;
+        ILM_CHECK_CUDA(cudaMemcpyAsync(Pn, Ybest.p, nb, cudaMemcpyDeviceToDevice, st));
+        ILM_TRY(A(Pn, Q, s));
+        ILM_TRY(st_axpby((size_t)n * s, ILM_F64, 1.0, Bb, -1.0, Q, Qn, st));
+        std::swap(R, Qn);
+        ILM_TRY(residual_norms(hb));
+        std::swap(R, Qn);
+        if (worst(hb) < worst(hr)) {
+          ILM_CHECK_CUDA(cudaMemcpyAsync(Y, Pn, nb, cudaMemcpyDeviceToDevice, st));
+          hr = hb;
+        }
+      }
+    }
+    for (int j = 0; j < s; ++j) relres[j] = hr[j];
+    if (done || it == maxiter) break;
+    // Z = M R; beta = -Qn^T Z; P = Z + Pn beta
+    ILM_TRY(precond(R, Z));
+    ILM_TRY(gram(Qn, sk, Z, s, n, w.G1.as<double>(), hab, st));
+    for (double& v : hab) v = -v;
+    ILM_CHECK_CUDA(cudaMemcpyAsync(dsm, hab.data(), hab.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+    ILM_CHECK_CUDA(cudaMemcpyAsync(P, Z, nb, cudaMemcpyDeviceToDevice, st));
+    ILM_TRY(gemm(n, sk, s, Pn, dsm, 1.0, 1.0, P, st));
+    sp = s;
   }
   *iters = it;
-  *relres = rel;
+  ILM_CHECK_CUDA(cudaStreamSynchronize(st));
   return ILM_OK;
 }
 
@@ -119,108 +451,186 @@ using namespace ilm;
 
 extern "C" {
 
-int ilm_solve_stokes(ilm_cache_t c, const void* vplus, const void* vminus, void* v_out, void* s_out, void* sigma_out,
-                     double tol, int maxiter, ilm_solve_info_t* info, ilm_stream_t stream) {
+int ilm_solve_stokes_multi(ilm_cache_t c, int nrhs, const void* vplus, const void* vminus, void* v_out,
+                           void* s_out, void* sigma_out, double tol, int maxiter, int precond,
+                           ilm_solve_info_t* info, ilm_stream_t stream) {
   ILM_REQUIRE(c, "null cache");
   ILM_REQUIRE(vplus && vminus && v_out && s_out && sigma_out, "solve_stokes: null argument");
   ILM_REQUIRE(c->kind == ILM_CACHE_VECTOR, "solve_stokes: vector cache required");
   ILM_REQUIRE(c->scaling == ILM_GRID_SCALING, "solve_stokes: GridScaling cache required");
   ILM_REQUIRE(tol > 0 && maxiter > 0, "solve_stokes: bad tolerance / iteration limit");
+  ILM_REQUIRE(nrhs >= 1 && nrhs <= ILM_STOKES_MAX_RHS, "solve_stokes: nrhs %d outside 1..%d", nrhs,
+              ILM_STOKES_MAX_RHS);
+  ILM_REQUIRE(precond == 0 || precond == 1, "solve_stokes: precond must be 0 or 1");
   cudaStream_t st = as_stream(stream);
   const int N = c->npts, dt = c->dtype;
   const size_t es = dt == ILM_F64 ? 8 : 4;
   const size_t ne = c->grid.shape(PC_U).numel() + c->grid.shape(PC_V).numel();
   const size_t nd = c->grid.shape(PC_D).numel();
   const size_t np = c->grid.shape(PC_P).numel();
-  Work w;
-  ILM_TRY(w.e1.alloc(ne * es));
-  ILM_TRY(w.e2.alloc(ne * es));
-  ILM_TRY(w.d1.alloc(nd * es));
-  ILM_TRY(w.d2.alloc(nd * es));
-  ILM_TRY(w.p1.alloc(np * es));
-  for (DevBuf* b : {&w.v1, &w.v2, &w.v3, &w.v4, &w.v5, &w.diag}) ILM_TRY(b->alloc((size_t)std::max(2 * N, 1) * es));
-  for (DevBuf* b : {&w.s1, &w.s2, &w.s3, &w.s4, &w.s5}) ILM_TRY(b->alloc((size_t)std::max(N, 1) * es));
   const size_t n2 = 2 * (size_t)N;
-  void* dv = w.v1.p;   // [v]
-  void* vb = w.v2.p;   // avg
-  void* vp = w.v3.p;   // v'
-  // jump and average
-  ILM_TRY(st_axpby(n2, dt, 1.0, vplus, -1.0, vminus, dv, st));
-  ILM_TRY(st_axpby(n2, dt, 0.5, vplus, 0.5, vminus, vb, st));
-  // psi* = L^-2 (-C D_s^symm [v])
-  ILM_TRY(ilm_surface_divergence_symm(c, dv, w.e1.p, stream));
-  ILM_TRY(ilm_curl(c, ILM_EDGES_PRIMAL, w.e1.p, w.d1.p, stream));
-  ILM_TRY(st_affine(nd, dt, -1.0, w.d1.p, 0.0, w.d1.p, st));
-  ILM_TRY(ilm_inverse_laplacian(c, ILM_NODES_DUAL, w.d1.p, w.d2.p, stream));
-  ILM_TRY(ilm_inverse_laplacian(c, ILM_NODES_DUAL, w.d2.p, s_out, stream));  // s_out holds psi*
-  // phi = L^-1 R (n . [v]),  v_phi = G phi  (kept in v_out)
-  if (N > 0) {
+  auto at = [&](const void* base, size_t per, int j) { return elem_ptr(base, per * j, dt); };
+  DevBuf e1, d1, d2, p1, p2, v1, v2, v4, s1, Bb, Y, Bs, Ys, vp_all, ss_all;
+  ILM_TRY(e1.alloc(ne * es));
+  ILM_TRY(d1.alloc(nd * es));
+  ILM_TRY(d2.alloc(nd * es));
+  ILM_TRY(p1.alloc(np * es));
+  ILM_TRY(p2.alloc(np * es));
+  for (DevBuf* b : {&v1, &v2, &v4}) ILM_TRY(b->alloc(std::max<size_t>(n2, 1) * es));
+  ILM_TRY(s1.alloc(std::max<size_t>(N, 1) * es));
+  ILM_TRY(vp_all.alloc(std::max<size_t>(n2 * nrhs, 1) * es));
+  ILM_TRY(ss_all.alloc(std::max<size_t>((size_t)N * nrhs, 1) * es));
+  for (DevBuf* b : {&Bb, &Y}) ILM_TRY(b->alloc(std::max<size_t>(n2 * nrhs, 1) * sizeof(double)));
+  for (DevBuf* b : {&Bs, &Ys}) ILM_TRY(b->alloc(std::max<size_t>((size_t)N * nrhs, 1) * sizeof(double)));
+  const unsigned gb2 = (unsigned)((n2 + 255) / 256), gb1 = (unsigned)((N + 255) / 256);
+  // ---- per right-hand side: psi*, v_phi, v' and the Ss right-hand side ----
+  for (int r = 0; r < nrhs; ++r) {
+    const void* vpl = at(vplus, n2, r);
+    const void* vmi = at(vminus, n2, r);
+    void* vo = at(v_out, ne, r);
+    void* so = at(s_out, nd, r);
+    void* dv = v1.p;  // [v]
+    void* vb = v2.p;  // avg
+    void* vp = at(vp_all.p, n2, r);
+    ILM_TRY(st_axpby(n2, dt, 1.0, vpl, -1.0, vmi, dv, st));
+    ILM_TRY(st_axpby(n2, dt, 0.5, vpl, 0.5, vmi, vb, st));
+    // psi* = L^-2 (-C D_s^symm [v])
+    ILM_TRY(ilm_surface_divergence_symm(c, dv, e1.p, stream));
+    ILM_TRY(ilm_curl(c, ILM_EDGES_PRIMAL, e1.p, d1.p, stream));
+    ILM_TRY(st_affine(nd, dt, -1.0, d1.p, 0.0, d1.p, st));
+    ILM_TRY(ilm_inverse_laplacian(c, ILM_NODES_DUAL, d1.p, d2.p, stream));
+    ILM_TRY(ilm_inverse_laplacian(c, ILM_NODES_DUAL, d2.p, so, stream));  // s_out holds psi*
+    // phi = L^-1 R (n . [v]),  v_phi = G phi  (kept in v_out)
+    if (N > 0) {
+      if (dt == ILM_F64)
+        k_ndot<double><<<gb1, 256, 0, st>>>(N, c->nx.as<double>(), c->ny.as<double>(),
+                                            static_cast<const double*>(dv), s1.as<double>());
+      else
+        k_ndot<float><<<gb1, 256, 0, st>>>(N, c->nx.as<float>(), c->ny.as<float>(), static_cast<const float*>(dv),
+                                           s1.as<float>());
+      ILM_CHECK_LAUNCH();
+    }
+    ILM_TRY(ilm_regularize(c, ILM_NODES_PRIMAL, s1.p, p1.p, stream));
+    ILM_TRY(ilm_inverse_laplacian(c, ILM_NODES_PRIMAL, p1.p, p2.p, stream));
+    void* phi = p2.p;
+    ILM_TRY(ilm_grad(c, ILM_NODES_PRIMAL, phi, vo, stream));
+    // v' = avg - E v_phi - E C psi*
+    ILM_TRY(ilm_interpolate(c, ILM_EDGES_PRIMAL, vo, v4.p, stream));
+    ILM_TRY(st_axpby(n2, dt, 1.0, vb, -1.0, v4.p, vp, st));
+    ILM_TRY(ilm_curl(c, ILM_NODES_DUAL, so, e1.p, stream));
+    ILM_TRY(ilm_interpolate(c, ILM_EDGES_PRIMAL, e1.p, v4.p, stream));
+    ILM_TRY(st_axpby(n2, dt, 1.0, vp, -1.0, v4.p, vp, st));
+    // right-hand side of the streamfunction equivalent: G^x_s phi
+    ILM_TRY(ilm_surface_grad_cross(c, phi, at(ss_all.p, N, r), stream));
+  }
+  // ---- block solve of S sigma = v' in y = W sigma: (-S W^-1) y = -v' ----
+  auto to_op = [&](const double* y, void* out, int n) -> int {
+    if (n == 0) return ILM_OK;
     if (dt == ILM_F64)
-      k_ndot<double><<<(N + 255) / 256, 256, 0, st>>>(N, c->nx.as<double>(), c->ny.as<double>(),
-                                                      static_cast<const double*>(dv), w.s1.as<double>());
+      k_to_op<double><<<(n + 255) / 256, 256, 0, st>>>(n, N, y, c->ds64.as<double>(), static_cast<double*>(out));
     else
-      k_ndot<float><<<(N + 255) / 256, 256, 0, st>>>(N, c->nx.as<float>(), c->ny.as<float>(),
-                                                     static_cast<const float*>(dv), w.s1.as<float>());
+      k_to_op<float><<<(n + 255) / 256, 256, 0, st>>>(n, N, y, c->ds64.as<double>(), static_cast<float*>(out));
     ILM_CHECK_LAUNCH();
-  }
-  ILM_TRY(ilm_regularize(c, ILM_NODES_PRIMAL, w.s1.p, w.p1.p, stream));
-  void* phi = w.p1.p;
-  {
-    DevBuf tmp;
-    ILM_TRY(tmp.alloc(np * es));
-    ILM_TRY(ilm_inverse_laplacian(c, ILM_NODES_PRIMAL, phi, tmp.p, stream));
-    ILM_CHECK_CUDA(cudaMemcpyAsync(phi, tmp.p, np * es, cudaMemcpyDeviceToDevice, st));
-    ILM_CHECK_CUDA(cudaStreamSynchronize(st));
-  }
-  ILM_TRY(ilm_grad(c, ILM_NODES_PRIMAL, phi, v_out, stream));
-  // v' = avg - E v_phi - E C psi*
-  ILM_TRY(ilm_interpolate(c, ILM_EDGES_PRIMAL, v_out, w.v4.p, stream));
-  ILM_TRY(st_axpby(n2, dt, 1.0, vb, -1.0, w.v4.p, vp, st));
-  ILM_TRY(ilm_curl(c, ILM_NODES_DUAL, s_out, w.e1.p, stream));
-  ILM_TRY(ilm_interpolate(c, ILM_EDGES_PRIMAL, w.e1.p, w.v4.p, stream));
-  ILM_TRY(st_axpby(n2, dt, 1.0, vp, -1.0, w.v4.p, vp, st));
-  // S sigma = v'  (matrix-free CG)
-  Apply applyS = [&](const void* x, void* y) -> int {
-    ILM_TRY(ilm_surface_curl(c, 0, ILM_VECTOR_DATA, x, w.d1.p, stream));
-    ILM_TRY(ilm_inverse_laplacian(c, ILM_NODES_DUAL, w.d1.p, w.d2.p, stream));
-    ILM_TRY(ilm_inverse_laplacian(c, ILM_NODES_DUAL, w.d2.p, w.d1.p, stream));
-    ILM_TRY(ilm_surface_curl(c, 1, ILM_VECTOR_DATA, w.d1.p, y, stream));
-    return st_affine(n2, dt, -1.0, y, 0.0, y, st);
+    return ILM_OK;
   };
+  auto from_op = [&](const void* in, double sgn, double* out, int n) -> int {
+    if (n == 0) return ILM_OK;
+    if (dt == ILM_F64)
+      k_from_op<double><<<(n + 255) / 256, 256, 0, st>>>(n, static_cast<const double*>(in), sgn, out);
+    else
+      k_from_op<float><<<(n + 255) / 256, 256, 0, st>>>(n, static_cast<const float*>(in), sgn, out);
+    ILM_CHECK_LAUNCH();
+    return ILM_OK;
+  };
+  for (int r = 0; r < nrhs; ++r) ILM_TRY(from_op(at(vp_all.p, n2, r), -1.0, Bb.as<double>() + n2 * r, (int)n2));
+  BlockApply applyB = [&](const double* Yb, double* Qb, int s) -> int {
+    for (int j = 0; j < s; ++j) {
+      ILM_TRY(to_op(Yb + n2 * j, v4.p, (int)n2));
+      ILM_TRY(ilm_surface_curl(c, 0, ILM_VECTOR_DATA, v4.p, d1.p, stream));
+      ILM_TRY(ilm_inverse_laplacian(c, ILM_NODES_DUAL, d1.p, d2.p, stream));
+      ILM_TRY(ilm_inverse_laplacian(c, ILM_NODES_DUAL, d2.p, d1.p, stream));
+      ILM_TRY(ilm_surface_curl(c, 1, ILM_VECTOR_DATA, d1.p, v4.p, stream));
+      ILM_TRY(from_op(v4.p, 1.0, Qb + n2 * j, (int)n2));
+    }
+    return ILM_OK;
+  };
+  const bool use_pc = precond == 1 && N > 0 && N <= STOKES_PC_MAX;
+  if (use_pc) ILM_TRY(ensure_stokes_pc(c, st));
+  BlockPrec applyM = [&](const double* Rb, double* Zb, int s) -> int {
+    // each velocity component: Z_comp = P^-1 R_comp (leading dimension 2N)
+    const double* Ti = c->stokes_pc.as<double>();
+    for (int comp = 0; comp < 2; ++comp)
+      for (int j0 = 0; j0 < s; j0 += 8) {
+        const int t = std::min(8, s - j0);
+        k_gemm_rows<<<gb1, 256, 0, st>>>(N, N, t, Ti, N, Rb + comp * N + n2 * j0, (int)n2, 1.0, 0.0,
+                                         Zb + comp * N + n2 * j0, (int)n2);
+        ILM_CHECK_LAUNCH();
+      }
+    return ILM_OK;
+  };
+  std::vector<double> rr1(nrhs, 0.0), rr2(nrhs, 0.0);
   int it1 = 0, it2 = 0;
-  double rr1 = 0.0, rr2 = 0.0;
-  ILM_TRY(cg_matfree(c, 2, applyS, vp, sigma_out, w.v4.p, w.v5.p, w.diag.p, tol, maxiter, &it1, &rr1, st));
-  // psi = psi* + L^-2 (-C_s^T sigma)
-  ILM_TRY(ilm_surface_curl(c, 0, ILM_VECTOR_DATA, sigma_out, w.d1.p, stream));
-  ILM_TRY(st_affine(nd, dt, -1.0, w.d1.p, 0.0, w.d1.p, st));
-  ILM_TRY(ilm_inverse_laplacian(c, ILM_NODES_DUAL, w.d1.p, w.d2.p, stream));
-  ILM_TRY(ilm_inverse_laplacian(c, ILM_NODES_DUAL, w.d2.p, w.d1.p, stream));
-  ILM_TRY(st_axpby(nd, dt, 1.0, w.d1.p, 1.0, s_out, s_out, st));
-  // v = C psi + v_phi
-  ILM_TRY(ilm_curl(c, ILM_NODES_DUAL, s_out, w.e1.p, stream));
-  ILM_TRY(st_axpby(ne, dt, 1.0, w.e1.p, 1.0, v_out, v_out, st));
-  // streamfunction equivalent of the scalar potential: Ss d = G^x_s phi
-  ILM_TRY(ilm_surface_grad_cross(c, phi, w.s1.p, stream));
-  Apply applySs = [&](const void* x, void* y) -> int {
-    ILM_TRY(ilm_surface_curl(c, 0, ILM_SCALAR_DATA, x, w.d1.p, stream));
-    ILM_TRY(ilm_inverse_laplacian(c, ILM_NODES_DUAL, w.d1.p, w.d2.p, stream));
-    ILM_TRY(ilm_surface_curl(c, 1, ILM_SCALAR_DATA, w.d2.p, y, stream));
-    return st_affine(N, dt, -1.0, y, 0.0, y, st);
-  };
-  ILM_TRY(cg_matfree(c, 1, applySs, w.s1.p, w.s2.p, w.s3.p, w.s4.p, w.s5.p, tol, maxiter, &it2, &rr2, st));
-  ILM_TRY(ilm_surface_curl_cross(c, 0, w.s2.p, w.d1.p, stream));
-  ILM_TRY(st_affine(nd, dt, -1.0, w.d1.p, 0.0, w.d1.p, st));
-  ILM_TRY(ilm_inverse_laplacian(c, ILM_NODES_DUAL, w.d1.p, w.d2.p, stream));
-  ILM_TRY(st_axpby(nd, dt, 1.0, w.d2.p, 1.0, s_out, s_out, st));
-  // sigma <- F^2 sigma,  F = W^-1 E R,  W = E R 1
-  ILM_TRY(ilm_surface_filter(c, 2, sigma_out, sigma_out, stream));
-  ILM_CHECK_CUDA(cudaStreamSynchronize(st));
-  if (info) {
-    info->iterations = it1 + it2;
-    info->converged = (rr1 <= tol && rr2 <= tol) ? 1 : 0;
-    info->rel_residual = std::max(rr1, rr2);
+  const double drop = dt == ILM_F64 ? 1e-13 : 1e-6;
+  ILM_TRY(block_cg((int)n2, nrhs, applyB, use_pc ? &applyM : nullptr, Bb.as<double>(), Y.as<double>(), tol, maxiter,
+                   drop, &it1, rr1.data(), st));
+  // sigma = W^-1 y
+  for (int r = 0; r < nrhs; ++r) ILM_TRY(to_op(Y.as<double>() + n2 * r, at(sigma_out, n2, r), (int)n2));
+  // ---- fields, and the right-hand sides of the Ss solves ----
+  for (int r = 0; r < nrhs; ++r) {
+    void* vo = at(v_out, ne, r);
+    void* so = at(s_out, nd, r);
+    // psi = psi* + L^-2 (-C_s^T sigma)
+    ILM_TRY(ilm_surface_curl(c, 0, ILM_VECTOR_DATA, at(sigma_out, n2, r), d1.p, stream));
+    ILM_TRY(st_affine(nd, dt, -1.0, d1.p, 0.0, d1.p, st));
+    ILM_TRY(ilm_inverse_laplacian(c, ILM_NODES_DUAL, d1.p, d2.p, stream));
+    ILM_TRY(ilm_inverse_laplacian(c, ILM_NODES_DUAL, d2.p, d1.p, stream));
+    ILM_TRY(st_axpby(nd, dt, 1.0, d1.p, 1.0, so, so, st));
+    // v = C psi + v_phi
+    ILM_TRY(ilm_curl(c, ILM_NODES_DUAL, so, e1.p, stream));
+    ILM_TRY(st_axpby(ne, dt, 1.0, e1.p, 1.0, vo, vo, st));
+    ILM_TRY(from_op(at(ss_all.p, N, r), 1.0, Bs.as<double>() + (size_t)N * r, N));
   }
-  return (rr1 <= tol && rr2 <= tol) ? ILM_OK : ILM_ERR_NOT_CONVERGED;
+  // ---- block solve of Ss d = G^x_s phi in y = W d: (Ss W^-1) y = rhs ----
+  BlockApply applyBs = [&](const double* Yb, double* Qb, int s) -> int {
+    for (int j = 0; j < s; ++j) {
+      ILM_TRY(to_op(Yb + (size_t)N * j, s1.p, N));
+      ILM_TRY(ilm_surface_curl(c, 0, ILM_SCALAR_DATA, s1.p, d1.p, stream));
+      ILM_TRY(ilm_inverse_laplacian(c, ILM_NODES_DUAL, d1.p, d2.p, stream));
+      ILM_TRY(ilm_surface_curl(c, 1, ILM_SCALAR_DATA, d2.p, s1.p, stream));
+      ILM_TRY(from_op(s1.p, -1.0, Qb + (size_t)N * j, N));
+    }
+    return ILM_OK;
+  };
+  ILM_TRY(block_cg(N, nrhs, applyBs, nullptr, Bs.as<double>(), Ys.as<double>(), tol, maxiter, drop, &it2, rr2.data(),
+                   st));
+  for (int r = 0; r < nrhs; ++r) {
+    void* so = at(s_out, nd, r);
+    ILM_TRY(to_op(Ys.as<double>() + (size_t)N * r, s1.p, N));
+    ILM_TRY(ilm_surface_curl_cross(c, 0, s1.p, d1.p, stream));
+    ILM_TRY(st_affine(nd, dt, -1.0, d1.p, 0.0, d1.p, st));
+    ILM_TRY(ilm_inverse_laplacian(c, ILM_NODES_DUAL, d1.p, d2.p, stream));
+    ILM_TRY(st_axpby(nd, dt, 1.0, d2.p, 1.0, so, so, st));
+    // sigma <- F^2 sigma,  F = W^-1 E R,  W = E R 1
+    ILM_TRY(ilm_surface_filter(c, 2, at(sigma_out, n2, r), at(sigma_out, n2, r), stream));
+  }
+  ILM_CHECK_CUDA(cudaStreamSynchronize(st));
+  bool ok = true;
+  for (int r = 0; r < nrhs; ++r) {
+    const bool cr = rr1[r] <= tol && rr2[r] <= tol;
+    ok = ok && cr;
+    if (info) {
+      info[r].iterations = it1 + it2;
+      info[r].converged = cr ? 1 : 0;
+      info[r].rel_residual = std::max(rr1[r], rr2[r]);
+    }
+  }
+  if (!ok) set_error("solve_stokes: rel. residual %g not reached in %d block iterations", tol, maxiter);
+  return ok ? ILM_OK : ILM_ERR_NOT_CONVERGED;
+}
+
+int ilm_solve_stokes(ilm_cache_t c, const void* vplus, const void* vminus, void* v_out, void* s_out, void* sigma_out,
+                     double tol, int maxiter, ilm_solve_info_t* info, ilm_stream_t stream) {
+  return ilm_solve_stokes_multi(c, 1, vplus, vminus, v_out, s_out, sigma_out, tol, maxiter, 1, info, stream);
 }
 
 }  // extern "C"

@@ -26,7 +26,8 @@ from .core import (Dual, EdgeGradient, EdgeGradientPrimal, Edges, EdgesDual, Edg
 from .problems import (DirichletPoissonProblem, ILMProblem, ILMSystem, NeumannPoissonProblem, StokesFlowProblem,
                        construct_system, prescribed_surface_average_, prescribed_surface_jump_, solve,
                        solve_dirichlet, solve_dirichlet_refined, solve_neumann, solve_neumann_full,
-                       solve_neumann_refined, solve_stokes, update_system_)
+                       solve_neumann_refined, solve_stokes, solve_stokes_multi,
+                       update_system_)
 from .helmholtz import (ScalarPotentialCache, VectorFieldCache, VectorPotentialCache, curlv_masked_from_masked_curlv_,
                         divv_masked_from_masked_divv_, masked_curlv_from_curlv_masked_,
                         masked_divv_from_divv_masked_, scalarpotential_from_divv_, scalarpotential_from_masked_divv_,

@@ -18,6 +18,7 @@ ILM_ERR_NOT_CONVERGED = 4
 F64, F32 = 0, 1
 DDF = {"Yang3": 0, "Roma": 1, "M4prime": 2, "Witchhat": 3, "M3": 4}
 GRID_SCALING, INDEX_SCALING = 0, 1
+STOKES_MAX_RHS = 32
 CACHE_SCALAR, CACHE_VECTOR = 0, 1
 NODES_PRIMAL, NODES_DUAL, EDGES_PRIMAL, EDGES_DUAL, EDGEGRAD_PRIMAL = 0, 1, 2, 3, 4
 SCALAR_DATA, VECTOR_DATA, TENSOR_DATA = 0, 1, 2
@@ -99,6 +100,7 @@ SIGNATURES = {
     "ilm_solve_neumann_refined": [_VP, _VP, _VP, _VP, _VP, _D, _I, _I, C.POINTER(SolveInfo), _VP],
     "ilm_solve_neumann_full": [_VP, _VP, _VP, _VP, _VP, _VP, _VP, _D, _I, C.POINTER(SolveInfo), _VP],
     "ilm_solve_stokes": [_VP, _VP, _VP, _VP, _VP, _VP, _D, _I, C.POINTER(SolveInfo), _VP],
+    "ilm_solve_stokes_multi": [_VP, _I, _VP, _VP, _VP, _VP, _VP, _D, _I, _I, C.POINTER(SolveInfo), _VP],
     "ilm_batch_create": [_I, C.POINTER(BatchProblem), _DP, _DP, _DP, _DP, _DP, _I, _I, C.POINTER(_VP)],
     "ilm_batch_destroy": [_VP],
     "ilm_batch_layout": [_VP, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)],
@@ -127,6 +129,7 @@ SIGNATURES = {
     "ilm_net_train_step": [_VP, _I, _I, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _D, _VP, _VP],
     "ilm_point_features": [_I, _DP, _DP, _DP, _DP, _DP, C.POINTER(_I), C.POINTER(_I), _D, C.POINTER(C.c_float)],
     "ilm_batch_set_learned": [_VP, _VP, _I, C.POINTER(_I)],
+    "ilm_batch_set_coarse": [_VP, _I, C.POINTER(C.c_int)],
     "ilm_batch_schur_apply": [_VP, _VP, _VP, _VP],
     "ilm_batch_schur_solve": [_VP, _VP, _VP, _D, _I, _VP],
     "ilm_heat_create": [_VP, _D, _D, _DP, _DP, _D, _I, C.POINTER(_VP)],
@@ -138,6 +141,7 @@ _RESTYPES = {"ilm_status_string": C.c_char_p, "ilm_last_error": C.c_char_p}
 
 # functions that may legitimately return ILM_ERR_NOT_CONVERGED (reported via info)
 _SOFT = {"ilm_solve_dirichlet", "ilm_solve_neumann", "ilm_solve_neumann_full", "ilm_solve_stokes",
+         "ilm_solve_stokes_multi",
          "ilm_solve_dirichlet_refined", "ilm_solve_neumann_refined"}
 
 _lib = None

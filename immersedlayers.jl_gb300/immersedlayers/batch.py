@@ -222,6 +222,19 @@ def _set_learned(self, net, kinds=(DIRICHLET, NEUMANN)):
     L.call("ilm_batch_set_learned", self._h, net._h, mask, bs.ctypes.data_as(C.POINTER(C.c_int)))
 
 
+def _set_coarse(self, enable=True, kinds=(NEUMANN,)):
+    """Coarse correction of block-Jacobi on the bodies' constant vectors for
+    the problems of the given kinds (the Neumann problems, whose Schur
+    complement has one near-null mode per body); enable=False removes it."""
+    if not enable:
+        L.call("ilm_batch_set_coarse", self._h, 0, None)
+        return
+    if tuple(kinds) != (NEUMANN,):
+        raise ValueError("the coarse correction applies to the Neumann problems")
+    bs = _body_starts(self)
+    L.call("ilm_batch_set_coarse", self._h, 1 << NEUMANN, bs.ctypes.data_as(C.POINTER(C.c_int)))
+
+
 def _schur_apply(self, x, y=None, stream=None):
     """y = S x for every problem (device FP64 packed vectors)."""
     if y is None:
@@ -240,6 +253,7 @@ def _schur_solve(self, rhs, x=None, tol=1e-10, maxiter=20000, stream=None):
 
 BatchSolver.body_starts = _body_starts
 BatchSolver.set_learned = _set_learned
+BatchSolver.set_coarse = _set_coarse
 BatchSolver.schur_apply = _schur_apply
 BatchSolver.schur_solve = _schur_solve
 

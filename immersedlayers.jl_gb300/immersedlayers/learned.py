@@ -279,7 +279,7 @@ def _timed_solves(bs, fp, fm, tol, maxiter, reps=3):
     return e0.elapsed_time(e1) / 1000.0 / reps, its, rr, f
 
 
-def evaluate(net, problem_fn, indices, tol=1e-8, maxiter=5000):
+def evaluate(net, problem_fn, indices, tol=1e-8, maxiter=5000, fp64_errors=False):
     """Full Dirichlet Poisson solves of held-out problems (surface data:
     arc-length Fourier modes), plain CG against the learned preconditioner.
 
@@ -287,7 +287,9 @@ def evaluate(net, problem_fn, indices, tol=1e-8, maxiter=5000):
     1e11-1e13): no CG reaches `tol` there.  Reported: the fraction of all
     problems each solver brings to `tol` within `maxiter`, and -- on the
     problems plain CG solves -- iterations, solves/s of the batched solve and
-    the field difference between the two solvers."""
+    the field difference between the two solvers; with `fp64_errors`, the
+    learned solve's field error against the FP64 refined solution on every
+    problem it solves."""
     from .batch import BatchProblemSpec, BatchSolver
     from .workloads import fourier_surface_data
     probs = [problem_fn(i) for i in indices]
@@ -330,7 +332,44 @@ def evaluate(net, problem_fn, indices, tol=1e-8, maxiter=5000):
     out["iteration_ratio"] = out["none"]["cg_iterations_mean"] / out["learned"]["cg_iterations_mean"]
     fa, fb = fields["none"], fields["learned"]
     out["field_rel_diff"] = float((fa - fb).abs().max() / fa.abs().max())
+    del bs
+    if fp64_errors:
+        out["error_vs_fp64"] = _errors_vs_refined(net, [specs[k] for k in range(len(specs)) if ok["learned"][k]], tol,
+                                                  maxiter)
     return out
+
+
+def _errors_vs_refined(net, specs, tol, maxiter):
+    """Field error of the learned-preconditioned FP32 solve against the FP64
+    refined solution (ilm_batch_solve_refined to a Schur residual of 1e-12,
+    the path the tests hold to the oracle's dense LU at 1e-10), per problem
+    relative to its max |f|, on the problems the learned solver brings to
+    `tol`."""
+    from .batch import BatchSolver
+    if not specs:
+        return {"problems": 0}
+    bs = BatchSolver(specs, dtype=torch.float32)
+    fp64 = torch.tensor(np.concatenate([s.fplus for s in specs]), dtype=torch.float64, device="cuda")
+    fm64 = torch.tensor(np.concatenate([s.fminus for s in specs]), dtype=torch.float64, device="cuda")
+    bs.set_precond("bjacobi", 64)
+    fr, _ = bs.solve_refined(fp64, fm64, tol=1e-12, maxiter=20000)
+    torch.cuda.synchronize()
+    _, rr_ref = bs.info()
+    ref_ok = rr_ref <= 1e-12
+    bs.set_learned(net)
+    bs.set_precond("learned")
+    fp, fm = bs.surface_data()
+    f, _ = bs.solve(fp, fm, tol=tol, maxiter=maxiter)
+    torch.cuda.synchronize()
+    errs = []
+    for k in range(len(specs)):
+        if not ref_ok[k]:
+            continue
+        a, b = bs.field(f, k).double(), bs.field(fr, k)
+        errs.append(float((a - b).abs().max() / b.abs().max()))
+    e = np.array(errs) if errs else np.zeros(1)
+    return {"problems": len(specs), "refined_converged": int(ref_ok.sum()), "max_field_rel_err": float(e.max()),
+            "median_field_rel_err": float(np.median(e)), "within_1e-5": int((e <= 1e-5).sum())}
 
 
 def main(argv=None):

@@ -15,7 +15,7 @@ import torch
 from . import _lib as L
 from .bodies import as_bodylist
 from .core import (GridScaling, NodesPrimal, PointData, ScalarData, SurfaceScalarCache, SurfaceVectorCache,
-                   _ptr, _stream_ptr, zeros_grid, zeros_surface)
+                   VectorData, _ptr, _stream_ptr, zeros_grid, zeros_surface)
 
 
 @dataclass
@@ -199,6 +199,41 @@ def solve_stokes(cache, vplus: PointData, vminus: PointData, tol=1e-8, maxiter=5
            _ptr(sigma.data), float(tol), int(maxiter), C.byref(info), _stream_ptr(stream))
     return v, s, sigma, dict(iterations=info.iterations, converged=bool(info.converged),
                              rel_residual=info.rel_residual)
+
+
+def solve_stokes_multi(cache, vplus: torch.Tensor, vminus: torch.Tensor = None, tol=1e-8, maxiter=5000,
+                       precond=True, stream=None):
+    """Stokes solves for several velocity right-hand sides at once
+    (stokes.jl:138,156 with one S for every surface velocity).  vplus /
+    vminus: (nrhs, 2N) tensors of VectorData rows in the cache dtype
+    (vminus None: zeros).  Both Schur systems are solved by block CG over
+    the right-hand sides; `precond` preconditions S with the inverse of the
+    gauge-shifted point-point Schur complement -E L^-1 E^T per velocity
+    component.  Returns (v: nrhs Edges{Primal}, s: nrhs Nodes{Dual},
+    sigma: nrhs VectorData, infos: one dict per right-hand side)."""
+    from .core import zeros_gridcurl
+    if vplus.dim() != 2 or vplus.shape[1] != 2 * len(cache):
+        raise ValueError(f"vplus must be (nrhs, {2 * len(cache)})")
+    nrhs = vplus.shape[0]
+    if not 1 <= nrhs <= L.STOKES_MAX_RHS:
+        raise ValueError(f"nrhs must be in 1..{L.STOKES_MAX_RHS}")
+    vplus = vplus.contiguous()
+    vminus = torch.zeros_like(vplus) if vminus is None else vminus.contiguous()
+    vs = [zeros_grid(cache) for _ in range(nrhs)]
+    ss = [zeros_gridcurl(cache) for _ in range(nrhs)]
+    v_all = torch.empty((nrhs,) + tuple(vs[0].data.shape), dtype=vs[0].data.dtype, device=vs[0].data.device)
+    s_all = torch.empty((nrhs,) + tuple(ss[0].data.shape), dtype=ss[0].data.dtype, device=ss[0].data.device)
+    sig_all = torch.empty_like(vplus)
+    infos = (L.SolveInfo * nrhs)()
+    L.call("ilm_solve_stokes_multi", cache._h, nrhs, _ptr(vplus), _ptr(vminus), _ptr(v_all), _ptr(s_all),
+           _ptr(sig_all), float(tol), int(maxiter), 1 if precond else 0, infos, _stream_ptr(stream))
+    sig = []
+    for r in range(nrhs):
+        vs[r].data.copy_(v_all[r])
+        ss[r].data.copy_(s_all[r])
+        sig.append(VectorData(sig_all[r].clone()))
+    return vs, ss, sig, [dict(iterations=i.iterations, converged=bool(i.converged), rel_residual=i.rel_residual)
+                         for i in infos]
 
 
 def solve(prob: ILMProblem, sys: ILMSystem, tol=1e-8, maxiter=5000, filter_power=0):

@@ -317,12 +317,28 @@ ILM_API int ilm_solve_neumann_full(ilm_cache_t c, const void* vplus, const void*
  * velocity, s_out: Nodes{Dual} streamfunction, sigma_out: VectorData
  * traction (filtered twice, :165).  The Schur systems -C_s L^-2 C_s^T
  * (create_CL2invCT, src/matrix_operators.jl:102) and -C_s L^-1 C_s^T on
- * scalars (create_CLinvCT_scalar, :71) are solved matrix-free by CG in place
- * of the reference's dense LU; info reports both solves (iterations summed,
- * worst relative residual).                                               */
+ * scalars (create_CLinvCT_scalar, :71) are solved matrix-free by
+ * (preconditioned) CG in place of the reference's dense LU; info reports
+ * both solves (iterations summed, worst relative residual).               */
 ILM_API int ilm_solve_stokes(ilm_cache_t c, const void* vplus, const void* vminus, void* v_out, void* s_out,
                              void* sigma_out, double tol, int maxiter, ilm_solve_info_t* info,
                              ilm_stream_t stream);
+/* The same solve for `nrhs` (1..ILM_STOKES_MAX_RHS) velocity right-hand
+ * sides at once (stokes.jl:138,156 solved for several surface velocities
+ * with one S).  vplus/vminus: nrhs x 2N (right-hand side r at offset 2N r);
+ * v_out: nrhs Edges{Primal} fields, s_out: nrhs Nodes{Dual} fields,
+ * sigma_out: nrhs x 2N, each contiguous in the cache dtype.  Both Schur
+ * systems are solved by block CG over all right-hand sides (maxiter block
+ * iterations each, Krylov vectors FP64); precond = 1 preconditions S with
+ * the inverse of the gauge-shifted point-point Schur complement -E L^-1 E^T
+ * on each velocity component (N <= 4096; built once per cache and kept
+ * until the points move), 0 runs plain block CG.  info: nrhs entries
+ * (iterations = block iterations of both solves).  ilm_solve_stokes is this
+ * call with nrhs = 1 and precond = 1.                                      */
+#define ILM_STOKES_MAX_RHS 32
+ILM_API int ilm_solve_stokes_multi(ilm_cache_t c, int nrhs, const void* vplus, const void* vminus, void* v_out,
+                                   void* s_out, void* sigma_out, double tol, int maxiter, int precond,
+                                   ilm_solve_info_t* info, ilm_stream_t stream);
 
 /* ---- batched problem solves (configs of many independent problems) ------ */
 /* Many independent Dirichlet/Neumann Poisson problems (each its own grid and
@@ -379,6 +395,16 @@ ILM_API int ilm_batch_solve_graph(ilm_batch_t b, const void* fplus, const void* 
  * arithmetic inside flexible CG).  The block inverses are built on the
  * device by this call.                                                      */
 ILM_API int ilm_batch_set_precond(ilm_batch_t b, int mode, int block_size);
+/* Coarse correction of the block-Jacobi preconditioner on the bodies'
+ * constant vectors (the near-null space of the Neumann Schur complement
+ * -C_s L^-1 C_s^T, neumann.jl:123, one small eigenvalue per closed body):
+ * z = M_bj r + Z E^-1 Z^T W r, Z the bodies' indicator vectors, E = Z^T W S Z
+ * (formed on the device here, inverted on the host).  kind_mask 2: the
+ * Neumann problems with at most 4 bodies; 0: off.  body_start: as
+ * ilm_batch_set_learned.  Applies wherever block-Jacobi runs (mode 1, and
+ * mode 2 for the problems without a network); no counterpart in the
+ * reference (its Schur systems are LU-solved).                             */
+ILM_API int ilm_batch_set_coarse(ilm_batch_t b, int kind_mask, const int* body_start);
 /* Stage timing: when enabled, ilm_batch_solve records a CUDA event on its
  * stream at each stage boundary; ilm_batch_stage_times returns the elapsed
  * ms per stage (up to 31), the number of stages and the number of kernel

@@ -246,6 +246,11 @@ ilm_solve_stokes(c, vplus, vminus, v_out, s_out, sigma_out, tol, maxiter, info, 
           (Ptr{Cvoid}, CuPtr{Cvoid}, CuPtr{Cvoid}, CuPtr{Cvoid}, CuPtr{Cvoid}, CuPtr{Cvoid}, Cdouble, Cint, Ref{SolveInfo},
            Ptr{Cvoid}),
           c, vplus, vminus, v_out, s_out, sigma_out, tol, maxiter, info, stream)
+ilm_solve_stokes_multi(c, nrhs, vplus, vminus, v_out, s_out, sigma_out, tol, maxiter, precond, info, stream) =
+    ccall((:ilm_solve_stokes_multi, libilm), Cint,
+          (Ptr{Cvoid}, Cint, CuPtr{Cvoid}, CuPtr{Cvoid}, CuPtr{Cvoid}, CuPtr{Cvoid}, CuPtr{Cvoid}, Cdouble, Cint, Cint,
+           Ptr{SolveInfo}, Ptr{Cvoid}),
+          c, nrhs, vplus, vminus, v_out, s_out, sigma_out, tol, maxiter, precond, info, stream)
 
 # batched solves
 ilm_batch_create(nprob, probs, x, y, nrmx, nrmy, ds, ddf, dtype, out) =
@@ -321,6 +326,8 @@ ilm_point_features(npts, x, y, nx, ny, ds, seg_start, seg_len, h, out) =
           npts, x, y, nx, ny, ds, seg_start, seg_len, h, out)
 ilm_batch_set_learned(b, net, kind_mask, body_start) =
     ccall((:ilm_batch_set_learned, libilm), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ptr{Cint}), b, net, kind_mask, body_start)
+ilm_batch_set_coarse(b, kind_mask, body_start) =
+    ccall((:ilm_batch_set_coarse, libilm), Cint, (Ptr{Cvoid}, Cint, Ptr{Cint}), b, kind_mask, body_start)
 ilm_batch_schur_apply(b, x, y, stream) =
     ccall((:ilm_batch_schur_apply, libilm), Cint, (Ptr{Cvoid}, CuPtr{Cdouble}, CuPtr{Cdouble}, Ptr{Cvoid}), b, x, y, stream)
 ilm_batch_schur_solve(b, rhs, x, tol, maxiter, stream) =
