@@ -718,9 +718,11 @@ def _stokes_rhs(args):
     solved at once by ilm_solve_stokes_multi (block CG over the right-hand
     sides, S preconditioned by the inverse point-point Schur complement
     -E L^-1 E^T per velocity component): FP64 cache to the bench tolerance,
-    FP32 cache to 1e-6; per right-hand side the FP32 velocity (Edges{Primal})
-    and traction (sigma) errors against the FP64 solution, relative to their
-    max magnitude.  Block iterations capped at `--stokes-maxiter`."""
+    FP32 cache to 1e-6 (capped at 400 block iterations: the FP32 operator
+    stalls near 1e-2 on these thin plates); per right-hand side the FP32
+    velocity (Edges{Primal}) and traction (sigma) errors against the FP64
+    solution, relative to their max magnitude.  FP64 block iterations capped
+    at `--stokes-maxiter`."""
     import torch
     import immersedlayers as il
     from immersedlayers import workloads as W
@@ -729,18 +731,18 @@ def _stokes_rhs(args):
     bl = d["bodies"]
     N = len(bl)
     res = {"npts": N, "unknowns": 2 * N, "grid": [g.nx, g.ny], "rhs": args.stokes_rhs,
-           "maxiter_block": args.stokes_maxiter, "method": "block CG over the right-hand sides, preconditioned"}
+           "method": "block CG over the right-hand sides, preconditioned"}
     sol = {}
-    for dt, tol in ((torch.float64, args.tol), (torch.float32, 1e-6)):
+    for dt, tol, cap in ((torch.float64, args.tol, args.stokes_maxiter), (torch.float32, 1e-6, 400)):
         c = il.SurfaceVectorCache(bl, g, dtype=dt)
         V = torch.tensor(d["vplus"], dtype=dt, device="cuda")
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        vs, _, sig, infos = il.solve_stokes_multi(c, V, tol=tol, maxiter=args.stokes_maxiter)
+        vs, _, sig, infos = il.solve_stokes_multi(c, V, tol=tol, maxiter=cap)
         torch.cuda.synchronize()
         sec = time.perf_counter() - t0   # includes the preconditioner set-up (first solve on this cache)
         key = "fp64" if dt == torch.float64 else "fp32"
-        res[key] = {"tol": tol, "seconds_all_rhs": sec, "block_iterations": infos[0]["iterations"],
+        res[key] = {"tol": tol, "maxiter_block": cap, "seconds_all_rhs": sec, "block_iterations": infos[0]["iterations"],
                     "converged": sum(i["converged"] for i in infos),
                     "max_rel_residual": max(i["rel_residual"] for i in infos)}
         sol[key] = ([v.data.double() for v in vs], [x.data.double() for x in sig])
@@ -956,18 +958,24 @@ def _e2e(args, specs, stream, dt):
         bs.set_precond(args.precond, args.block)
         torch.cuda.synchronize()
         t2 = time.perf_counter()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
         with torch.cuda.stream(stream):
+            ev[0].record(stream)
             fp = fp_h.to("cuda", non_blocking=True)
             fm = fm_h.to("cuda", non_blocking=True)
+            ev[1].record(stream)
             f, s = bs.solve(fp, fm, tol=args.tol, stream=stream)
+            ev[2].record(stream)
             if f_h is None:
                 f_h = torch.empty(f.numel(), dtype=dt).pin_memory()
                 s_h = torch.empty(s.numel(), dtype=dt).pin_memory()
             f_h.copy_(f, non_blocking=True)
             s_h.copy_(s, non_blocking=True)
+            ev[3].record(stream)
         stream.synchronize()
         times.append(time.perf_counter() - t0)
-        parts.append((t1 - t0, t2 - t1, time.perf_counter() - t2))
+        parts.append((t1 - t0, t2 - t1, time.perf_counter() - t2, ev[0].elapsed_time(ev[1]),
+                      ev[1].elapsed_time(ev[2]), ev[2].elapsed_time(ev[3])))
         h2d = fp.numel() * fp.element_size() * 2
         d2h = (f.numel() + s.numel()) * f.element_size()
         phases.append(bs.setup_times())
@@ -980,6 +988,9 @@ def _e2e(args, specs, stream, dt):
                         "mode), D2H of all fields", "ms_per_step": 1000 * t,
             "ms_breakdown": {"batch_create": 1000 * parts[k][0], "precond_setup": 1000 * parts[k][1],
                              "copies_and_solve": 1000 * parts[k][2]},
+            "copies_and_solve_ms": {"h2d": parts[k][3],
+                                    "first solve (with the block inverses and the deflation set-up)": parts[k][4],
+                                    "d2h": parts[k][5], "d2h_gbs": d2h / (parts[k][5] * 1e6)},
             "setup_phases_ms": {name: round(ms, 3) for name, ms in phases[k]}}
 
 

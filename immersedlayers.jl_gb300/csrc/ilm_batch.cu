@@ -419,45 +419,38 @@ struct CoarseTask {
   int cst[CG_COARSE_MAX + 1];
 };
 
-// E = Z^T W S Z (nb x nb, row-major in E[16 t ...]) of task t: one CTA per
-// task, a warp per row, FP64 sums of the float-float entries; per-warp
-// partials in shared memory summed in warp order (deterministic)
+// Partial E = Z^T W S Z over rows [c n / COARSE_SPLIT, (c + 1) n / COARSE_SPLIT)
+// of task t into E[(t COARSE_SPLIT + c) 16 ...] (row-major nb x nb): a warp
+// per row, each body's column range summed in FP32 (the hi parts; E only
+// preconditions), per-warp partials summed in warp order.  The host adds
+// the COARSE_SPLIT partials in order (deterministic).
+constexpr int COARSE_SPLIT = 8;
 __global__ void __launch_bounds__(256) k_coarse_E(const CoarseTask* __restrict__ tasks, double* __restrict__ E) {
   constexpr int NB2 = CG_COARSE_MAX * CG_COARSE_MAX;
   __shared__ double part[8][NB2];
-  const CoarseTask T = tasks[blockIdx.x];
+  const int t = blockIdx.x / COARSE_SPLIT, c = blockIdx.x % COARSE_SPLIT;
+  const CoarseTask T = tasks[t];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, ld = schur_ld(T.n);
   for (int k = lane; k < NB2; k += 32) part[warp][k] = 0.0;
   __syncwarp();
-  auto body = [&](int i) {
-    int b = 0;
-    for (int k = 1; k < T.nb; ++k) b += i >= T.cst[k] ? 1 : 0;
-    return b;
-  };
-  for (int i = warp; i < T.n; i += 8) {
-    double acc[CG_COARSE_MAX] = {0.0, 0.0, 0.0, 0.0};
+  const int i0 = (int)((long long)T.n * c / COARSE_SPLIT), i1 = (int)((long long)T.n * (c + 1) / COARSE_SPLIT);
+  for (int i = i0 + warp; i < i1; i += 8) {
     const float* h = T.Shi + (size_t)i * ld;
-    const float* l = T.Slo + (size_t)i * ld;
-    for (int j = lane; j < T.n; j += 32) {
-      const double v = (double)h[j] + (double)l[j];
-      const int bj = body(j);
+    int a = 0;
+    for (int k = 1; k < T.nb; ++k) a += i >= T.cst[k] ? 1 : 0;
+    for (int b = 0; b < T.nb; ++b) {
+      float acc = 0.f;
+      for (int j = T.cst[b] + lane; j < T.cst[b + 1]; j += 32) acc += h[j];
 #pragma unroll
-      for (int b = 0; b < CG_COARSE_MAX; ++b) acc[b] += b == bj ? v : 0.0;
-    }
-#pragma unroll
-    for (int b = 0; b < CG_COARSE_MAX; ++b)
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) acc[b] += __shfl_down_sync(0xffffffffu, acc[b], o);
-    if (lane == 0) {
-      const int a = body(i);
-      for (int b = 0; b < T.nb; ++b) part[warp][a * CG_COARSE_MAX + b] += T.w[i] * acc[b];
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+      if (lane == 0) part[warp][a * CG_COARSE_MAX + b] += T.w[i] * (double)acc;
     }
   }
   __syncthreads();
   if (threadIdx.x < NB2) {
-    double t = 0.0;
-    for (int w = 0; w < 8; ++w) t += part[w][threadIdx.x];
-    E[(size_t)blockIdx.x * NB2 + threadIdx.x] = t;
+    double s = 0.0;
+    for (int w = 0; w < 8; ++w) s += part[w][threadIdx.x];
+    E[(size_t)blockIdx.x * NB2 + threadIdx.x] = s;
   }
 }
 
@@ -1997,17 +1990,19 @@ int ilm_batch_set_coarse(ilm_batch_t b, int kind_mask, const int* body_start) {
   if (tasks.empty()) return ILM_OK;
   DevBuf dt, dE;
   ILM_TRY(up(dt, tasks));
-  ILM_TRY(dE.alloc(tasks.size() * M * M * sizeof(double)));
-  k_coarse_E<<<(unsigned)tasks.size(), 256>>>(dt.as<CoarseTask>(), dE.as<double>());
+  ILM_TRY(dE.alloc(tasks.size() * COARSE_SPLIT * M * M * sizeof(double)));
+  k_coarse_E<<<(unsigned)(tasks.size() * COARSE_SPLIT), 256>>>(dt.as<CoarseTask>(), dE.as<double>());
   ILM_CHECK_LAUNCH();
-  std::vector<double> E(tasks.size() * M * M);
+  std::vector<double> E(tasks.size() * COARSE_SPLIT * M * M);
   ILM_CHECK_CUDA(cudaMemcpy(E.data(), dE.p, E.size() * sizeof(double), cudaMemcpyDeviceToHost));
   for (size_t t = 0; t < tasks.size(); ++t) {
     const int p = tprob[t];
     const CoarseTask& T = tasks[t];
-    double Es[M * M];
+    double Ef[M * M] = {0.0}, Es[M * M];
+    for (int c = 0; c < COARSE_SPLIT; ++c)
+      for (int k = 0; k < M * M; ++k) Ef[k] += E[(t * COARSE_SPLIT + c) * M * M + k];
     for (int i = 0; i < M; ++i)  // symmetric part (W S is symmetric up to rounding)
-      for (int j = 0; j < M; ++j) Es[i * M + j] = 0.5 * (E[t * M * M + i * M + j] + E[t * M * M + j * M + i]);
+      for (int j = 0; j < M; ++j) Es[i * M + j] = 0.5 * (Ef[i * M + j] + Ef[j * M + i]);
     if (!small_inverse(T.nb, Es, &b->coarse_Einv[(size_t)p * M * M])) continue;
     b->coarse_nb[p] = T.nb;
     for (int q = 0; q < M1; ++q) b->coarse_start[(size_t)p * M1 + q] = T.cst[q];
