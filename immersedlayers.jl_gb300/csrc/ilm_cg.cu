@@ -1458,31 +1458,36 @@ void cgff_params_set_band(void* dst, const float* band, int band_k, const int* s
 
 // ---------------------------------------------------------------------------
 // block-Jacobi set-up: inverse of each diagonal block of S by Gauss-Jordan
-// with partial pivoting on S_hi + S_lo (+ a tiny shift * mean|diag| I against
-// exact singularity), one CTA per block.  The elimination runs in float-float
-// on the FP32 pipes (each update a - f b to ~2^-44 relative): GB300 issues
-// FP64 at a small fraction of its FP32 rate and the FP64 elimination was the
-// largest part of the preconditioner set-up.  The pivot search is a warp
-// argmax (ties to the lower row, deterministic); the pivot reciprocal is one
-// FP64 divide per step.
+// elimination in place with partial pivoting on S_hi + S_lo (+ a tiny
+// shift * mean|diag| I against exact singularity), one CTA per block.  The
+// elimination runs in float-float on the FP32 pipes (each update a - f b to
+// ~2^-44 relative): GB300 issues FP64 at a small fraction of its FP32 rate.
+// In place (no augmented identity: half the work and the shared memory of
+// [A | I], so several blocks share an SM), rows at an odd stride (column
+// reads free of bank conflicts), the pivot reciprocal an FP32 reciprocal and
+// one float-float Newton step (~2^-44), the row swaps undone as a column
+// permutation when the inverse is written.  The pivot search is a warp
+// argmax (ties to the lower row, deterministic).
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_block_inverse(const BJBlockTask* __restrict__ tasks, double shift) {
   const BJBlockTask T = tasks[blockIdx.x];
   const int sz = T.sz;
-  const int ld = 2 * sz;
+  const int ld = sz | 1;  // odd row stride
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  extern __shared__ __align__(16) float smf[];  // hi and lo of sz x 2sz, pivot column, scalars
+  extern __shared__ __align__(16) float smf[];  // hi and lo of sz x ld, pivot column, scalars, pivots, columns
   float* Ah = smf;
   float* Al = Ah + (size_t)sz * ld;
   float* fh = Al + (size_t)sz * ld;
   float* fl = fh + sz;
   float* sc = fl + sz;  // [0..1] reciprocal of the pivot (hi, lo), [2] pivot row (int bits), [3] shift
+  int* piv = reinterpret_cast<int*>(sc + 4);
+  int* src = piv + sz;
   const int ldS = schur_ld(T.n);
   for (int i = warp; i < sz; i += nw)
-    for (int j = lane; j < ld; j += 32) {
+    for (int j = lane; j < sz; j += 32) {
       const size_t g = (size_t)(T.s + i) * ldS + T.s + j;
-      Ah[(size_t)i * ld + j] = j < sz ? T.Shi[g] : (j - sz == i ? 1.f : 0.f);
-      Al[(size_t)i * ld + j] = j < sz ? T.Slo[g] : 0.f;
+      Ah[(size_t)i * ld + j] = T.Shi[g];
+      Al[(size_t)i * ld + j] = T.Slo[g];
     }
   __syncthreads();
   if (warp == 0) {
@@ -1522,38 +1527,52 @@ __global__ void __launch_bounds__(256) k_block_inverse(const BJBlockTask* __rest
       }
       if (lane == 0) {
         sc[2] = __int_as_float(bi);
-        const double piv = (double)Ah[(size_t)bi * ld + k] + (double)Al[(size_t)bi * ld + k];
-        const double inv = piv != 0.0 ? 1.0 / piv : 0.0;
-        const float ih = (float)inv;
-        sc[0] = ih;
-        sc[1] = (float)(inv - (double)ih);
+        piv[k] = bi;
+        const float dh = Ah[(size_t)bi * ld + k], dl = Al[(size_t)bi * ld + k];
+        if (dh != 0.f) {  // 1/d: r = 1/d_hi, then r (1 + e), e = 1 - d r
+          const float r = 1.0f / dh;
+          const float p = dh * r;
+          float pe = fmaf(dh, r, -p);
+          pe = fmaf(dl, r, pe);
+          const float e = (1.0f - p) - pe;
+          const FF inv = ff_renorm(r, r * e);
+          sc[0] = inv.hi;
+          sc[1] = inv.lo;
+        } else {
+          sc[0] = sc[1] = 0.f;
+        }
       }
     }
     __syncthreads();
     const int p = __float_as_int(sc[2]);
     const FF inv{sc[0], sc[1]};
-    // swap rows k and p and scale the new row k by the reciprocal of the pivot
-    for (int j = threadIdx.x; j < ld; j += blockDim.x) {
+    // swap rows k and p; new row k = (row with A[k][k] set to 1) x 1/pivot
+    for (int j = threadIdx.x; j < sz; j += blockDim.x) {
       const FF rk{Ah[(size_t)k * ld + j], Al[(size_t)k * ld + j]};
       const FF rp{Ah[(size_t)p * ld + j], Al[(size_t)p * ld + j]};
       if (p != k) {
         Ah[(size_t)p * ld + j] = rk.hi;
         Al[(size_t)p * ld + j] = rk.lo;
       }
-      const FF v = ff_mul(p != k ? rp : rk, inv);
+      const FF v = j == k ? inv : ff_mul(p != k ? rp : rk, inv);
       Ah[(size_t)k * ld + j] = v.hi;
       Al[(size_t)k * ld + j] = v.lo;
     }
     __syncthreads();
+    // factors f_i = A[i][k] (i != k); column k of those rows becomes 0 - f_i x row k
     for (int i = threadIdx.x; i < sz; i += blockDim.x) {
-      fh[i] = Ah[(size_t)i * ld + k];
-      fl[i] = Al[(size_t)i * ld + k];
+      fh[i] = i == k ? 0.f : Ah[(size_t)i * ld + k];
+      fl[i] = i == k ? 0.f : Al[(size_t)i * ld + k];
+      if (i != k) {
+        Ah[(size_t)i * ld + k] = 0.f;
+        Al[(size_t)i * ld + k] = 0.f;
+      }
     }
     __syncthreads();
     for (int i = warp; i < sz; i += nw) {
       if (i == k) continue;
       const FF f{fh[i], fl[i]};
-      for (int j = lane; j < ld; j += 32) {
+      for (int j = lane; j < sz; j += 32) {
         const FF a{Ah[(size_t)i * ld + j], Al[(size_t)i * ld + j]};
         const FF r = ff_sub_mul(a, f, FF{Ah[(size_t)k * ld + j], Al[(size_t)k * ld + j]});
         Ah[(size_t)i * ld + j] = r.hi;
@@ -1562,16 +1581,30 @@ __global__ void __launch_bounds__(256) k_block_inverse(const BJBlockTask* __rest
     }
     __syncthreads();
   }
+  // the row swaps of the elimination are column swaps of the inverse, undone
+  // in reverse order: column c of the inverse is column src[c] of A
+  if (threadIdx.x == 0) {
+    for (int c = 0; c < sz; ++c) src[c] = c;
+    for (int k = sz - 1; k >= 0; --k) {
+      const int q = piv[k];
+      if (q != k) {
+        const int t = src[k];
+        src[k] = src[q];
+        src[q] = t;
+      }
+    }
+  }
+  __syncthreads();
   for (int i = warp; i < sz; i += nw)
     for (int j = lane; j < sz; j += 32) {
-      T.out_hi[(size_t)i * sz + j] = Ah[(size_t)i * ld + sz + j];
-      T.out_lo[(size_t)i * sz + j] = Al[(size_t)i * ld + sz + j];
+      T.out_hi[(size_t)i * sz + j] = Ah[(size_t)i * ld + src[j]];
+      T.out_lo[(size_t)i * sz + j] = Al[(size_t)i * ld + src[j]];
     }
 }
 
 int launch_block_inverse(const BJBlockTask* tasks_dev, int ntasks, int max_sz, cudaStream_t st) {
   if (ntasks == 0) return ILM_OK;
-  const size_t smem = ((size_t)max_sz * 2 * max_sz * 2 + 2 * max_sz + 4) * sizeof(float);
+  const size_t smem = ((size_t)max_sz * (max_sz | 1) * 2 + 2 * max_sz + 4 + 2 * max_sz) * sizeof(float);
   if (smem > 200 * 1024) {
     set_error("block-Jacobi block of %d points too large", max_sz);
     return ILM_ERR_SIZE_LIMIT;

@@ -40,6 +40,19 @@ struct Functional {
   int nterm;
 };
 
+// The same functional with every weight split into a float-float (hi, lo)
+// pair once per point, for the batched float-float builds (the split is an
+// FP64 subtraction, which GB300 issues at a small fraction of its FP32 rate;
+// split per point pair it was a large part of the build).  Written over the
+// Functional buffers, so it is no larger.
+struct FunctionalFF {
+  float coef[2][2];
+  int xb[2], yb[2];
+  float xw[2][FW][2], yw[2][FW][2];
+  int nterm;
+};
+static_assert(sizeof(FunctionalFF) <= sizeof(Functional), "FunctionalFF overlays Functional buffers");
+
 // Build the per-point functionals for one Schur kind.  side 0 = left
 // (interpolation side, no ds weight), side 1 = right (regularization side).
 __global__ void k_functionals(int N, int kind, const int* __restrict__ bxP, const int* __restrict__ bxD,
@@ -437,7 +450,23 @@ __global__ void k_functionals_batched(int Ptot, const int* __restrict__ pt2prob,
       F.yw[1][t] = at(wyd, t);
     }
   }
-  out[g] = F;
+  FunctionalFF Q;
+  Q.nterm = F.nterm;
+  for (int p = 0; p < 2; ++p) {
+    Q.xb[p] = F.xb[p];
+    Q.yb[p] = F.yb[p];
+    const float ch = (float)F.coef[p];
+    Q.coef[p][0] = ch;
+    Q.coef[p][1] = (float)(F.coef[p] - (double)ch);
+    for (int t = 0; t < FW; ++t) {
+      const float xh = (float)F.xw[p][t], yh = (float)F.yw[p][t];
+      Q.xw[p][t][0] = xh;
+      Q.xw[p][t][1] = (float)(F.xw[p][t] - (double)xh);
+      Q.yw[p][t][0] = yh;
+      Q.yw[p][t][1] = (float)(F.yw[p][t] - (double)yh);
+    }
+  }
+  reinterpret_cast<FunctionalFF*>(out)[g] = Q;
 }
 
 __device__ __forceinline__ FF split_ff(double v) {
@@ -448,47 +477,21 @@ __device__ __forceinline__ FF split_ff(double v) {
 // Batched Schur entries in float-float on the FP32 pipes (~2^-44 relative
 // per operation; GB300 issues FP64 at a small fraction of its FP32 rate):
 // the same 1-D weight correlations and LGF contractions as k_schur_pairs,
-// with the weights split into (hi, lo) pairs as they are read and the LGF
-// read from its float-float copy (staging each tile's LGF window in shared
-// memory was measured no faster: the kernel is bound by the float-float
-// arithmetic, not by the lookups).
-
-__global__ void __launch_bounds__(256) k_schur_pairs_batched(int nprob, const SchurProbDev* __restrict__ pr,
-                                                             const Functional* __restrict__ F,
-                                                             const double* __restrict__ w,
-                                                             const float2* __restrict__ G, int ld, int M,
-                                                             float* __restrict__ Shi, float* __restrict__ Slo) {
-  int lo = 0, hi = nprob - 1;
-  const int u = blockIdx.x;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (pr[mid].tile0 <= u) lo = mid; else hi = mid - 1;
-  }
-  const SchurProbDev P = pr[lo];
-  const int N = P.n;
-  const int nt = (N + 15) / 16;
-  // the tile sum T_kl = sum U_k(a) G(a - b) U_l(b) is symmetric (G depends on
-  // |a - b| only and both sides use the same functionals): one CTA per tile
-  // of the upper triangle (ti <= tj) in row-major order, writing S_kl = -w_l
-  // T_kl and, off the diagonal tiles, S_lk = -w_k T_kl
-  const int t = u - P.tile0;
-  int ti = (int)((2.0 * nt + 1.0 - sqrt((2.0 * nt + 1.0) * (2.0 * nt + 1.0) - 8.0 * t)) * 0.5);
-  auto row0 = [nt](int i) { return i * nt - i * (i - 1) / 2; };  // first triangle tile of tile row i
-  while (ti > 0 && row0(ti) > t) --ti;
-  while (ti + 1 < nt && row0(ti + 1) <= t) ++ti;
-  const int tj = ti + (t - row0(ti));
-  const int k = ti * 16 + threadIdx.y;
-  const int l = tj * 16 + threadIdx.x;
-  if (k >= N || l >= N) return;
-  const Functional& Fk = F[P.poff + k];
-  const Functional& Fl = F[P.poff + l];
+// with the weights read as float-float pairs (split once per point) and the
+// LGF read from its float-float copy.
+//
+// T_kl = sum_{p,q} c_p c_q sum_{dx,dy} Cx(dx) Cy(dy) G(|Dx + dx|, |Dy + dy|)
+// for the functionals of points k and l (Cx, Cy the 1-D correlations of their
+// weights).
+__device__ __forceinline__ FF pair_sum(const FunctionalFF& Fk, const FunctionalFF& Fl, const float2* __restrict__ G,
+                                       int ld, int M) {
   FF total{0.f, 0.f};
   for (int p = 0; p < Fk.nterm; ++p) {
     FF xk[FW], yk[FW];
 #pragma unroll
     for (int a = 0; a < FW; ++a) {
-      xk[a] = split_ff(Fk.xw[p][a]);
-      yk[a] = split_ff(Fk.yw[p][a]);
+      xk[a] = FF{Fk.xw[p][a][0], Fk.xw[p][a][1]};
+      yk[a] = FF{Fk.yw[p][a][0], Fk.yw[p][a][1]};
     }
     for (int q = 0; q < Fl.nterm; ++q) {
       FF cx[2 * FW - 1], cy[2 * FW - 1];
@@ -496,12 +499,12 @@ __global__ void __launch_bounds__(256) k_schur_pairs_batched(int nprob, const Sc
       for (int d = 0; d < 2 * FW - 1; ++d) cx[d] = cy[d] = FF{0.f, 0.f};
 #pragma unroll
       for (int b = 0; b < FW; ++b) {
-        const FF xb = split_ff(Fl.xw[q][b]);
-        const FF yb = split_ff(Fl.yw[q][b]);
+        const float xbh = Fl.xw[q][b][0], xbl = Fl.xw[q][b][1];
+        const float ybh = Fl.yw[q][b][0], ybl = Fl.yw[q][b][1];
 #pragma unroll
         for (int a = 0; a < FW; ++a) {
-          ff_fma(cx[a - b + FW - 1], xk[a].hi, xk[a].lo, xb.hi, xb.lo);
-          ff_fma(cy[a - b + FW - 1], yk[a].hi, yk[a].lo, yb.hi, yb.lo);
+          ff_fma(cx[a - b + FW - 1], xk[a].hi, xk[a].lo, xbh, xbl);
+          ff_fma(cy[a - b + FW - 1], yk[a].hi, yk[a].lo, ybh, ybl);
         }
       }
 #pragma unroll
@@ -529,11 +532,41 @@ __global__ void __launch_bounds__(256) k_schur_pairs_batched(int nprob, const Sc
         ff_fma(acc, cy[dy].hi, cy[dy].lo, racc.hi, racc.lo);
       }
       acc = ff_renorm(acc.hi, acc.lo);
-      const FF cc = split_ff(Fk.coef[p] * Fl.coef[q]);
+      const FF cc = ff_mul(FF{Fk.coef[p][0], Fk.coef[p][1]}, FF{Fl.coef[q][0], Fl.coef[q][1]});
       ff_fma(total, cc.hi, cc.lo, acc.hi, acc.lo);
     }
   }
-  total = ff_renorm(total.hi, total.lo);
+  return ff_renorm(total.hi, total.lo);
+}
+
+__global__ void __launch_bounds__(256) k_schur_pairs_batched(int nprob, const SchurProbDev* __restrict__ pr,
+                                                             const FunctionalFF* __restrict__ F,
+                                                             const double* __restrict__ w,
+                                                             const float2* __restrict__ G, int ld, int M,
+                                                             float* __restrict__ Shi, float* __restrict__ Slo) {
+  int lo = 0, hi = nprob - 1;
+  const int u = blockIdx.x;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (pr[mid].tile0 <= u) lo = mid; else hi = mid - 1;
+  }
+  const SchurProbDev P = pr[lo];
+  const int N = P.n;
+  const int nt = (N + 15) / 16;
+  // the tile sum T_kl = sum U_k(a) G(a - b) U_l(b) is symmetric (G depends on
+  // |a - b| only and both sides use the same functionals): one CTA per tile
+  // of the upper triangle (ti <= tj) in row-major order, writing S_kl = -w_l
+  // T_kl and, off the diagonal tiles, S_lk = -w_k T_kl
+  const int t = u - P.tile0;
+  int ti = (int)((2.0 * nt + 1.0 - sqrt((2.0 * nt + 1.0) * (2.0 * nt + 1.0) - 8.0 * t)) * 0.5);
+  auto row0 = [nt](int i) { return i * nt - i * (i - 1) / 2; };  // first triangle tile of tile row i
+  while (ti > 0 && row0(ti) > t) --ti;
+  while (ti + 1 < nt && row0(ti + 1) <= t) ++ti;
+  const int tj = ti + (t - row0(ti));
+  const int k = ti * 16 + threadIdx.y;
+  const int l = tj * 16 + threadIdx.x;
+  if (k >= N || l >= N) return;
+  const FF total = pair_sum(F[P.poff + k], F[P.poff + l], G, ld, M);
   // row-major float-float pair: S[k][l] = hi + lo
   const FF wl = split_ff(-w[P.poff + l]);
   const FF v = ff_mul(wl, total);
@@ -558,7 +591,8 @@ int schur_build_batched(int nprob, const SchurProbDev* probs_dev, int total_tile
                                                             W.by[1], W.wx64[0], W.wx64[1], W.wy64[0], W.wy64[1],
                                                             W.nx64, W.ny64, F, -1);
   ILM_CHECK_LAUNCH();
-  k_schur_pairs_batched<<<total_tiles, dim3(16, 16), 0, st>>>(nprob, probs_dev, F, w, G, ld, ld - 1, Shi, Slo);
+  k_schur_pairs_batched<<<total_tiles, dim3(16, 16), 0, st>>>(nprob, probs_dev, reinterpret_cast<const FunctionalFF*>(F),
+                                                              w, G, ld, ld - 1, Shi, Slo);
   ILM_CHECK_LAUNCH();
   return ILM_OK;
 }
@@ -573,8 +607,8 @@ int schur_build_batched(int nprob, const SchurProbDev* probs_dev, int total_tile
 // tile, float-float as k_schur_pairs_batched; the tiles of problem p start at
 // pr[p].tile0 (the caller's full-tile numbering).
 __global__ void __launch_bounds__(256) k_rhsop_pairs_batched(int nprob, const SchurProbDev* __restrict__ pr,
-                                                             const Functional* __restrict__ FU,
-                                                             const Functional* __restrict__ FD,
+                                                             const FunctionalFF* __restrict__ FU,
+                                                             const FunctionalFF* __restrict__ FD,
                                                              const double* __restrict__ w,
                                                              const float2* __restrict__ G, int ld, int M,
                                                              float* __restrict__ Mhi, float* __restrict__ Mlo) {
@@ -593,60 +627,7 @@ __global__ void __launch_bounds__(256) k_rhsop_pairs_batched(int nprob, const Sc
   const int l = tj * 16 + threadIdx.x;
   if (k >= N || l >= N) return;
   const bool dir = P.kind == ILM_SCHUR_RTLINVR;
-  const Functional& Fk = dir ? FU[P.poff + k] : FD[P.poff + k];
-  const Functional& Fl = dir ? FD[P.poff + l] : FU[P.poff + l];
-  FF total{0.f, 0.f};
-  for (int p = 0; p < Fk.nterm; ++p) {
-    FF xk[FW], yk[FW];
-#pragma unroll
-    for (int a = 0; a < FW; ++a) {
-      xk[a] = split_ff(Fk.xw[p][a]);
-      yk[a] = split_ff(Fk.yw[p][a]);
-    }
-    for (int q = 0; q < Fl.nterm; ++q) {
-      FF cx[2 * FW - 1], cy[2 * FW - 1];
-#pragma unroll
-      for (int d = 0; d < 2 * FW - 1; ++d) cx[d] = cy[d] = FF{0.f, 0.f};
-#pragma unroll
-      for (int b = 0; b < FW; ++b) {
-        const FF xb = split_ff(Fl.xw[q][b]);
-        const FF yb = split_ff(Fl.yw[q][b]);
-#pragma unroll
-        for (int a = 0; a < FW; ++a) {
-          ff_fma(cx[a - b + FW - 1], xk[a].hi, xk[a].lo, xb.hi, xb.lo);
-          ff_fma(cy[a - b + FW - 1], yk[a].hi, yk[a].lo, yb.hi, yb.lo);
-        }
-      }
-#pragma unroll
-      for (int d = 0; d < 2 * FW - 1; ++d) {
-        cx[d] = ff_renorm(cx[d].hi, cx[d].lo);
-        cy[d] = ff_renorm(cy[d].hi, cy[d].lo);
-      }
-      const int Dx = Fk.xb[p] - Fl.xb[q] - (FW - 1);
-      const int Dy = Fk.yb[p] - Fl.yb[q] - (FW - 1);
-      FF acc{0.f, 0.f};
-#pragma unroll
-      for (int dy = 0; dy < 2 * FW - 1; ++dy) {
-        int my = abs(Dy + dy);
-        my = my > M ? M : my;
-        const float2* Grow = G + (size_t)my;
-        FF racc{0.f, 0.f};
-#pragma unroll
-        for (int dx = 0; dx < 2 * FW - 1; ++dx) {
-          int mx = abs(Dx + dx);
-          mx = mx > M ? M : mx;
-          const float2 gv = __ldg(Grow + (size_t)mx * ld);
-          ff_fma(racc, gv.x, gv.y, cx[dx].hi, cx[dx].lo);
-        }
-        racc = ff_renorm(racc.hi, racc.lo);
-        ff_fma(acc, cy[dy].hi, cy[dy].lo, racc.hi, racc.lo);
-      }
-      acc = ff_renorm(acc.hi, acc.lo);
-      const FF cc = split_ff(Fk.coef[p] * Fl.coef[q]);
-      ff_fma(total, cc.hi, cc.lo, acc.hi, acc.lo);
-    }
-  }
-  total = ff_renorm(total.hi, total.lo);
+  const FF total = pair_sum(dir ? FU[P.poff + k] : FD[P.poff + k], dir ? FD[P.poff + l] : FU[P.poff + l], G, ld, M);
   const FF wl = split_ff((dir ? 1.0 : -1.0) * w[P.poff + l]);
   const FF v = ff_mul(wl, total);
   Mhi[P.soff + (size_t)k * schur_ld(N) + l] = v.hi;
@@ -668,8 +649,10 @@ int rhsop_build_batched(int nprob, const SchurProbDev* probs_full_dev, int total
                                                             W.by[1], W.wx64[0], W.wx64[1], W.wy64[0], W.wy64[1],
                                                             W.nx64, W.ny64, FD, ILM_SCHUR_GLINVD);
   ILM_CHECK_LAUNCH();
-  k_rhsop_pairs_batched<<<total_tiles, dim3(16, 16), 0, st>>>(nprob, probs_full_dev, FU, FD, w, G, ld, ld - 1, Mhi,
-                                                              Mlo);
+  k_rhsop_pairs_batched<<<total_tiles, dim3(16, 16), 0, st>>>(nprob, probs_full_dev,
+                                                              reinterpret_cast<const FunctionalFF*>(FU),
+                                                              reinterpret_cast<const FunctionalFF*>(FD), w, G, ld,
+                                                              ld - 1, Mhi, Mlo);
   ILM_CHECK_LAUNCH();
   return ILM_OK;
 }
