@@ -609,8 +609,7 @@ int ensure_deflation(ilm_batch_s* b) {
   }
   // z = S'^-1 1 for the problems with a deflation shift (the others never
   // read z: their right-hand side is 0 and their CG returns at once), to
-  // 1e-10: z enters x = y + gamma t z linearly, so its error stays two orders
-  // below the solves' 1e-8, and a refined solve corrects it with the rest
+  // 1e-12: z enters x = y + gamma t z linearly, and solves may ask for 1e-10
   bool need = false;
   for (int p = 0; p < np; ++p) {
     if (b->probs[p].kind == 0 && b->defl_gamma[p] == 0.0)
@@ -633,7 +632,7 @@ int ensure_deflation(ilm_batch_s* b) {
     const bool band = b->band_k >= 0 && !b->has_band.empty() && b->has_band[p];
     const bool pre = !band && b->bj_block > 0 && !b->bj_have.empty() && b->bj_have[p];
     cgff_params_fill(dst, b->Shi.as<float>() + b->soff[p], b->Slo.as<float>() + b->soff[p], drhs.as<double>() + o,
-                     b->defl_z.as<double>() + o, b->ds64.as<double>() + o, b->probs[p].npts, 20000, 1e-10,
+                     b->defl_z.as<double>() + o, b->ds64.as<double>() + o, b->probs[p].npts, 20000, 1e-12,
                      its.as<int>() + p, rr.as<double>() + p, pre ? b->bj_blk.as<int>() + o : nullptr,
                      pre ? b->bj_start.as<int>() + b->bj_first[p] : nullptr,
                      pre ? b->bj_size.as<int>() + b->bj_first[p] : nullptr,

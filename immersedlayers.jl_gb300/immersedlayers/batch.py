@@ -33,22 +33,51 @@ class BatchProblemSpec:
         return len(self.bl)
 
 
+_PROBLEM_DTYPE = np.dtype([("nx", np.int32), ("ny", np.int32), ("h", np.float64), ("i0x", np.int32),
+                           ("i0y", np.int32), ("npts", np.int32), ("kind", np.int32)], align=True)
+
+
+class PackedBatch:
+    """The host arrays of a batch in the C ABI's packed layout
+    (ilm_batch_create): problem records, the points' coordinates, normals and
+    areas concatenated in problem order, and per point the local index of its
+    body's first point (ilm_batch_set_learned / ilm_batch_set_coarse).  An
+    application that keeps its geometry in these arrays passes them to every
+    batch it creates."""
+
+    def __init__(self, specs):
+        specs = list(specs)
+        self.records = np.array([(s.nx, s.ny, s.h, s.i0[0], s.i0[1], s.npts, s.kind) for s in specs],
+                                dtype=_PROBLEM_DTYPE)
+        assert self.records.itemsize == C.sizeof(L.BatchProblem)
+        bodies = [b for s in specs for b in s.bl.bodies]
+        self.points = [np.ascontiguousarray(np.concatenate([getattr(b, a) for b in bodies]), np.float64)
+                       if bodies else np.zeros(0) for a in ("x", "y", "nx", "ny", "ds")]
+        starts = []
+        for s in specs:
+            fi = s.bl.firstindices()
+            starts.append(np.repeat(fi[:-1], np.diff(fi)))
+        self.body_starts = np.ascontiguousarray(np.concatenate(starts) if starts else np.zeros(0), dtype=np.int32)
+
+    @property
+    def nbytes(self):
+        return self.records.nbytes + sum(a.nbytes for a in self.points)
+
+
 class BatchSolver:
     """Set up (DDF windows, tile lists, FP64 Schur complements) and solve a
-    batch of problems on the device."""
+    batch of problems on the device.  `packed`: the specs' PackedBatch, when
+    the caller already holds it (else it is built here)."""
 
-    def __init__(self, specs, ddftype="Yang3", dtype=torch.float32):
+    def __init__(self, specs, ddftype="Yang3", dtype=torch.float32, packed=None):
         self.specs = list(specs)
         self.dtype = dtype
         n = len(self.specs)
-        arr = (L.BatchProblem * n)()
-        for i, s in enumerate(self.specs):
-            arr[i] = L.BatchProblem(s.nx, s.ny, s.h, s.i0[0], s.i0[1], s.npts, s.kind)
-        cat = lambda a: np.ascontiguousarray(np.concatenate([getattr(s.bl, a) for s in self.specs]), np.float64)
-        self._pts = [cat(a) for a in ("x", "y", "nx", "ny", "ds")]
-        ptrs = [a.ctypes.data_as(C.POINTER(C.c_double)) for a in self._pts]
+        self._packed = packed if packed is not None else PackedBatch(self.specs)
+        rec = self._packed.records.ctypes.data_as(C.POINTER(L.BatchProblem))
+        ptrs = [a.ctypes.data_as(C.POINTER(C.c_double)) for a in self._packed.points]
         h = C.c_void_p()
-        L.call("ilm_batch_create", n, arr, *ptrs, L.DDF[ddftype], _DT[dtype], C.byref(h))
+        L.call("ilm_batch_create", n, rec, *ptrs, L.DDF[ddftype], _DT[dtype], C.byref(h))
         self._h = h
         fo = (C.c_size_t * (n + 1))()
         po = (C.c_size_t * (n + 1))()
@@ -204,12 +233,7 @@ def _set_precond(self, mode="none", block_size=64):
 
 def _body_starts(self):
     """Per packed point, the local index of its body's first point."""
-    out = []
-    for s in self.specs:
-        fi = s.bl.firstindices()
-        for b in range(len(fi) - 1):
-            out.append(np.full(fi[b + 1] - fi[b], fi[b], dtype=np.int32))
-    return np.ascontiguousarray(np.concatenate(out), dtype=np.int32)
+    return self._packed.body_starts
 
 
 def _set_learned(self, net, kinds=(DIRICHLET, NEUMANN)):
