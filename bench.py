@@ -32,7 +32,7 @@ METRIC = "Poisson solves/s at 1e-8 rel. residual, 1 GB300 (batched Dirichlet/Neu
 # DRAM bytes (read + write) of one launch of the dominant kernel, from one ncu
 # capture of this bench's CG launch per solver
 # (profiles/k_cg_cluster_*_batched_poisson.md)
-NCU_TRAFFIC = {"learned": {"Schur CG (FP64)": 0.7961e9}}
+NCU_TRAFFIC = {"learned": {"Schur CG (FP64)": 0.7326e9}}
 UNIT = "solves/s"
 NPROB = 256
 
