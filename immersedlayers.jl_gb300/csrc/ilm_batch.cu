@@ -572,6 +572,7 @@ __global__ void k_batch_schur_apply(int Ptot, const int* __restrict__ pt2prob, c
 // constants; z = S'^-1 1 (solved once here) gives S^-1 by Sherman-Morrison.
 int ensure_deflation(ilm_batch_s* b) {
   if (b->defl_ready) return ILM_OK;
+  const auto t0 = std::chrono::steady_clock::now();
   const int Ptot = b->Ptot, np = b->nprob;
   b->defl_gamma.assign(np, 0.0);
   b->defl_uz.assign(np, 0.0);
@@ -655,6 +656,8 @@ int ensure_deflation(ilm_batch_s* b) {
     b->defl_uz[p] = uz;
   }
   b->defl_ready = true;
+  b->setup_ms.emplace_back("deflation vectors (Dirichlet problems with a net-charge shift)",
+                           std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
   return ILM_OK;
 }
 
