@@ -162,7 +162,7 @@ enum Coef { CF_ZERO = 0, CF_ONE = 1, CF_NX = 2, CF_NY = 3, CF_MNX = 4, CF_MNY = 
 // only its NTAP buckets, about NTAP / (TILE_X + NTAP - 1) of the points
 // instead of all of them.  The buckets are ordered by key, then by staging
 // slot (warp match groups and per-warp offsets, no atomics), so every cell
-// sums its points in a fixed order.
+// sums its points in a fixed order.  Small chunks skip the bucketing.
 // ---------------------------------------------------------------------------
 constexpr int SCAT_NB = TILE_X * TILE_Y;
 constexpr int SCAT_NKEY = TILE_X + NTAP - 1;
@@ -176,11 +176,27 @@ struct ScatterSmem {
   unsigned short perm[SCAT_NB];       // sorted position -> staging slot
 };
 
+// chunks of at most this many points are summed directly in staging order:
+// for sparse tiles (points ds >= h apart: ~25 per tile) the bucketing's
+// barriers and scan cost more than the loop they shorten
+constexpr int SCAT_DIRECT_MAX = 64;
+
 // sum of the staged points' contributions to cell (i, j) of the tile whose
 // first column is x0; all threads of the CTA call it (it synchronises the
 // CTA; the caller synchronises again before restaging)
 template <typename T>
 __device__ __forceinline__ T tile_sum_bucketed(ScatterSmem<T>& sm, int nc, int x0, int i, int j) {
+  if (nc <= SCAT_DIRECT_MAX) {  // block-uniform
+    __syncthreads();
+    T acc = (T)0;
+    for (int e = 0; e < nc; ++e) {
+      const int di = i - sm.bx[e];
+      const int dj = j - sm.by[e];
+      if ((unsigned)di < (unsigned)NTAP && (unsigned)dj < (unsigned)NTAP)
+        acc += sm.amp[e] * sm.wx[e * NTAP + di] * sm.wy[e * NTAP + dj];
+    }
+    return acc;
+  }
   const int tid = threadIdx.y * blockDim.x + threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (int q = tid; q < (SCAT_NB / 32) * SCAT_NKEY; q += SCAT_NB) (&sm.wcnt[0][0])[q] = 0;
   __syncthreads();  // staged points and zeroed counts visible
