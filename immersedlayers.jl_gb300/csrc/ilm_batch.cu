@@ -120,7 +120,7 @@ __global__ void __launch_bounds__(256)
 // memory 256 at a time, one point per thread, and every cell sums the points
 // of its window buckets (tile_sum_bucketed) in a fixed order.
 template <typename T>
-__global__ void __launch_bounds__(SB_X* SB_Y)
+__global__ void __launch_bounds__(SB_X* SB_Y, 6)
     k_bscatter(const BScatterTask* __restrict__ tasks, int ntasks, const int* __restrict__ bmap) {
   static_assert(SB_X == TILE_X && SB_Y == TILE_Y, "batched scatter tiles are the cache tiles");
   __shared__ ScatterSmem<T> sm;
@@ -361,6 +361,12 @@ struct ilm_batch_s {
   int n_large = 0, n_small = 0, max_small = 0, nctas_small = 0;
   DevBuf order_large, order_small, counter2;
   cudaStream_t s2 = nullptr;
+  // lazy set-up of the first solve (block-Jacobi inverses, deflation
+  // vectors): its own non-blocking stream, so that it overlaps the solve's
+  // stage A, and its scratch allocated before stage A is issued (cudaMalloc
+  // and cudaFree may synchronise the device)
+  cudaStream_t s_setup = nullptr;
+  DevBuf lz_bjtasks, lz_ones, lz_y, lz_rhs, lz_its, lz_rr, lz_prm, lz_soff;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   ilm_batch_s* twin = nullptr;
   DevBuf ref_in, ref_b, ref_x, ref_r, ref_y, ref_norm, dsoff;
@@ -377,6 +383,7 @@ struct ilm_batch_s {
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_join) cudaEventDestroy(ev_join);
     if (s2) cudaStreamDestroy(s2);
+    if (s_setup) cudaStreamDestroy(s_setup);
     delete twin;
   }
 };
@@ -481,6 +488,11 @@ bool small_inverse(int k, const double* A, double* Ainv) {
   return true;
 }
 
+int ensure_setup_stream(ilm_batch_s* b) {
+  if (!b->s_setup) ILM_CHECK_CUDA(cudaStreamCreateWithFlags(&b->s_setup, cudaStreamNonBlocking));
+  return ILM_OK;
+}
+
 // Block-Jacobi inverses (Gauss-Jordan, float-float) of the problems whose
 // preconditioner uses them: every problem under block-Jacobi, the problems
 // without a network under the learned preconditioner
@@ -495,10 +507,12 @@ int ensure_block_inverses(ilm_batch_s* b) {
   }
   if (todo.empty()) return ILM_OK;
   const auto t0 = std::chrono::steady_clock::now();
-  DevBuf d;
-  ILM_TRY(up(d, todo));
-  ILM_TRY(launch_block_inverse(d.as<BJBlockTask>(), (int)todo.size(), b->bj_max_sz, nullptr));
-  ILM_CHECK_CUDA(cudaDeviceSynchronize());
+  ILM_TRY(ensure_setup_stream(b));
+  ILM_TRY(b->lz_bjtasks.alloc(todo.size() * sizeof(BJBlockTask)));
+  ILM_CHECK_CUDA(cudaMemcpyAsync(b->lz_bjtasks.p, todo.data(), todo.size() * sizeof(BJBlockTask),
+                                 cudaMemcpyHostToDevice, b->s_setup));
+  ILM_TRY(launch_block_inverse(b->lz_bjtasks.as<BJBlockTask>(), (int)todo.size(), b->bj_max_sz, b->s_setup));
+  ILM_CHECK_CUDA(cudaStreamSynchronize(b->s_setup));
   b->setup_ms.emplace_back("block-Jacobi inverses",
                            std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
   return ILM_OK;
@@ -570,17 +584,37 @@ __global__ void k_batch_schur_apply(int Ptot, const int* __restrict__ pt2prob, c
 // positive on the W-orthogonal complement of the constants, with
 // gamma = 2 |rho| / 1^T W 1 where rho is the Rayleigh quotient of the
 // constants; z = S'^-1 1 (solved once here) gives S^-1 by Sherman-Morrison.
+// Scratch of the lazy set-up, allocated before a solve issues its stage A
+int prepare_lazy_setup(ilm_batch_s* b) {
+  const int Ptot = b->Ptot, np = b->nprob;
+  ILM_TRY(ensure_setup_stream(b));
+  ILM_TRY(b->defl_z.alloc((size_t)std::max(Ptot, 1) * sizeof(double)));
+  for (DevBuf* d : {&b->lz_ones, &b->lz_y, &b->lz_rhs}) ILM_TRY(d->alloc((size_t)std::max(Ptot, 1) * sizeof(double)));
+  ILM_TRY(b->lz_its.alloc((size_t)std::max(np, 1) * sizeof(int)));
+  ILM_TRY(b->lz_rr.alloc((size_t)std::max(np, 1) * sizeof(double)));
+  ILM_TRY(b->lz_prm.alloc((size_t)std::max(np, 1) * cgff_params_size()));
+  ILM_TRY(b->lz_soff.alloc(b->soff.size() * sizeof(size_t)));
+  if (!b->dpoff.p) ILM_TRY(up(b->dpoff, b->poff));
+  if (b->bj_block > 0) ILM_TRY(b->lz_bjtasks.alloc(std::max<size_t>(b->bj_tasks_host.size(), 1) * sizeof(BJBlockTask)));
+  return ILM_OK;
+}
+
+// Deflation of the Dirichlet net-charge mode: gamma per problem from S 1, and
+// z = S'^-1 1 with S' = S + gamma 1 1^T W.  Runs on the set-up stream (the
+// host waits for that stream only), so it overlaps the first solve's stage A.
 int ensure_deflation(ilm_batch_s* b) {
   if (b->defl_ready) return ILM_OK;
   const auto t0 = std::chrono::steady_clock::now();
   const int Ptot = b->Ptot, np = b->nprob;
+  ILM_TRY(prepare_lazy_setup(b));
+  cudaStream_t ss = b->s_setup;
   b->defl_gamma.assign(np, 0.0);
   b->defl_uz.assign(np, 0.0);
-  ILM_TRY(b->defl_z.alloc((size_t)std::max(Ptot, 1) * sizeof(double)));
-  ILM_CHECK_CUDA(cudaMemset(b->defl_z.p, 0, (size_t)std::max(Ptot, 1) * sizeof(double)));
+  ILM_CHECK_CUDA(cudaMemsetAsync(b->defl_z.p, 0, (size_t)std::max(Ptot, 1) * sizeof(double), ss));
   bool any = false;
   for (int p = 0; p < np; ++p) any |= b->probs[p].kind == 0;
   if (!any) {
+    ILM_CHECK_CUDA(cudaStreamSynchronize(ss));
     b->defl_ready = true;
     return ILM_OK;
   }
@@ -588,16 +622,16 @@ int ensure_deflation(ilm_batch_s* b) {
   for (int p = 0; p < np; ++p)
     if (b->probs[p].kind == 0)
       for (size_t k = b->poff[p]; k < b->poff[p + 1]; ++k) rhs[k] = 1.0;
-  DevBuf d1, dy, drhs, dsoff, its, rr, prm;
-  ILM_TRY(up(d1, ones));
-  ILM_TRY(dy.alloc((size_t)Ptot * sizeof(double)));
-  if (!b->dpoff.p) ILM_TRY(up(b->dpoff, b->poff));
-  ILM_TRY(up(dsoff, b->soff));
-  k_batch_schur_apply<<<(Ptot * 32 + 255) / 256, 256>>>(Ptot, b->pt2prob.as<int>(), b->dpoff.as<size_t>(),
-                                                        b->Shi.as<float>(), b->Slo.as<float>(), dsoff.as<size_t>(),
-                                                        d1.as<double>(), dy.as<double>());
+  ILM_CHECK_CUDA(cudaMemcpyAsync(b->lz_ones.p, ones.data(), (size_t)Ptot * sizeof(double), cudaMemcpyHostToDevice, ss));
+  ILM_CHECK_CUDA(cudaMemcpyAsync(b->lz_soff.p, b->soff.data(), b->soff.size() * sizeof(size_t),
+                                 cudaMemcpyHostToDevice, ss));
+  k_batch_schur_apply<<<(Ptot * 32 + 255) / 256, 256, 0, ss>>>(Ptot, b->pt2prob.as<int>(), b->dpoff.as<size_t>(),
+                                                               b->Shi.as<float>(), b->Slo.as<float>(),
+                                                               b->lz_soff.as<size_t>(), b->lz_ones.as<double>(),
+                                                               b->lz_y.as<double>());
   ILM_CHECK_LAUNCH();
-  ILM_CHECK_CUDA(cudaMemcpy(y.data(), dy.p, (size_t)Ptot * sizeof(double), cudaMemcpyDeviceToHost));
+  ILM_CHECK_CUDA(cudaMemcpyAsync(y.data(), b->lz_y.p, (size_t)Ptot * sizeof(double), cudaMemcpyDeviceToHost, ss));
+  ILM_CHECK_CUDA(cudaStreamSynchronize(ss));
   for (int p = 0; p < np; ++p) {
     if (b->probs[p].kind != 0) continue;
     double su = 0.0, sy = 0.0;
@@ -621,9 +655,7 @@ int ensure_deflation(ilm_batch_s* b) {
     b->defl_ready = true;
     return ILM_OK;
   }
-  ILM_TRY(up(drhs, rhs));
-  ILM_TRY(its.alloc((size_t)np * sizeof(int)));
-  ILM_TRY(rr.alloc((size_t)np * sizeof(double)));
+  ILM_CHECK_CUDA(cudaMemcpyAsync(b->lz_rhs.p, rhs.data(), (size_t)Ptot * sizeof(double), cudaMemcpyHostToDevice, ss));
   std::vector<unsigned char> cg((size_t)np * cgff_params_size());
   for (int p = 0; p < np; ++p) {
     const size_t o = b->poff[p];
@@ -632,10 +664,10 @@ int ensure_deflation(ilm_batch_s* b) {
     // block-Jacobi (each shortens this tight solve several times)
     const bool band = b->band_k >= 0 && !b->has_band.empty() && b->has_band[p];
     const bool pre = !band && b->bj_block > 0 && !b->bj_have.empty() && b->bj_have[p];
-    cgff_params_fill(dst, b->Shi.as<float>() + b->soff[p], b->Slo.as<float>() + b->soff[p], drhs.as<double>() + o,
-                     b->defl_z.as<double>() + o, b->ds64.as<double>() + o, b->probs[p].npts, 20000, 1e-12,
-                     its.as<int>() + p, rr.as<double>() + p, pre ? b->bj_blk.as<int>() + o : nullptr,
-                     pre ? b->bj_start.as<int>() + b->bj_first[p] : nullptr,
+    cgff_params_fill(dst, b->Shi.as<float>() + b->soff[p], b->Slo.as<float>() + b->soff[p],
+                     b->lz_rhs.as<double>() + o, b->defl_z.as<double>() + o, b->ds64.as<double>() + o,
+                     b->probs[p].npts, 20000, 1e-12, b->lz_its.as<int>() + p, b->lz_rr.as<double>() + p,
+                     pre ? b->bj_blk.as<int>() + o : nullptr, pre ? b->bj_start.as<int>() + b->bj_first[p] : nullptr,
                      pre ? b->bj_size.as<int>() + b->bj_first[p] : nullptr,
                      pre ? b->bj_off.as<int>() + b->bj_first[p] : nullptr, pre ? b->bj_inv.as<float>() : nullptr,
                      pre ? b->bj_inv_lo.as<float>() : nullptr);
@@ -644,11 +676,12 @@ int ensure_deflation(ilm_batch_s* b) {
       cgff_params_set_band(dst, b->band.as<float>() + o * (2 * b->band_k + 1), b->band_k,
                            b->lseg_start.as<int>() + o, b->lseg_len.as<int>() + o);
   }
-  ILM_TRY(up(prm, cg));
-  ILM_TRY(launch_cg_cluster(prm.p, b->order.as<int>(), np, b->counter.as<int>(), b->maxN, b->nclusters, nullptr,
+  ILM_CHECK_CUDA(cudaMemcpyAsync(b->lz_prm.p, cg.data(), cg.size(), cudaMemcpyHostToDevice, ss));
+  ILM_TRY(launch_cg_cluster(b->lz_prm.p, b->order.as<int>(), np, b->counter.as<int>(), b->maxN, b->nclusters, ss,
                             b->cg_variant));
   std::vector<double> z(Ptot);
-  ILM_CHECK_CUDA(cudaMemcpy(z.data(), b->defl_z.p, (size_t)Ptot * sizeof(double), cudaMemcpyDeviceToHost));
+  ILM_CHECK_CUDA(cudaMemcpyAsync(z.data(), b->defl_z.p, (size_t)Ptot * sizeof(double), cudaMemcpyDeviceToHost, ss));
+  ILM_CHECK_CUDA(cudaStreamSynchronize(ss));
   for (int p = 0; p < np; ++p) {
     if (b->defl_gamma[p] == 0.0) continue;
     double uz = 0.0;
@@ -1550,11 +1583,20 @@ int ilm_batch_solve(ilm_batch_t b, const void* fplus, const void* fminus, void* 
   ILM_REQUIRE(b && fplus && fminus && f_out && s_out, "batch_solve: null argument");
   ILM_REQUIRE(tol > 0 && maxiter > 0, "batch_solve: bad tolerance / iteration limit");
   cudaStream_t st = as_stream(stream);
-  ILM_TRY(ensure_cg_params(b, tol, maxiter));
+  // new CG parameters (and, for the first solve, the lazy set-up on the
+  // set-up stream) are prepared after stage A is issued, so the set-up
+  // kernels overlap stage A; the stream is drained first so that no earlier
+  // solve still reads the parameters that get replaced
+  const bool rebuild = !(tol == b->cg_tol && maxiter == b->cg_maxiter && !b->params_dirty);
+  if (rebuild) {
+    ILM_CHECK_CUDA(cudaStreamSynchronize(st));
+    ILM_TRY(prepare_lazy_setup(b));
+  }
   b->nev = 0;
   b->launches = 0;
   ILM_TRY(batch_mark(b, st));
   ILM_TRY(batch_stage_a(b, fplus, fminus, st));
+  ILM_TRY(ensure_cg_params(b, tol, maxiter));
   ILM_TRY(batch_cg(b, st));
   ILM_TRY(st_convert(b->Ptot, ILM_F64, b->x64.p, b->dtype, s_out, st));
   ILM_CHECK_CUDA(cudaMemcpyAsync(b->s.p, s_out, (size_t)b->Ptot * es(b->dtype), cudaMemcpyDeviceToDevice, st));

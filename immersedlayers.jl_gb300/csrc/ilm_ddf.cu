@@ -236,7 +236,7 @@ __device__ __forceinline__ T occupied_tile_sum(ScatterSmem<T>& sm, int p0, int p
 }
 
 template <typename T>
-__global__ void __launch_bounds__(TILE_X* TILE_Y)
+__global__ void __launch_bounds__(TILE_X* TILE_Y, 6)
 k_scatter(int n1, int n2, int ntx, const int* __restrict__ ne, const int* __restrict__ ne_cnt, const int* __restrict__ tptr,
           const int* __restrict__ tpts, const int* __restrict__ bx, const int* __restrict__ by,
           const T* __restrict__ wx, const T* __restrict__ wy, const T* __restrict__ wsc, const T* __restrict__ nx,
@@ -264,7 +264,7 @@ k_scatter(int n1, int n2, int ntx, const int* __restrict__ ne, const int* __rest
 // fill's bandwidth overlaps their load latency.
 constexpr int SCAT_TPB = 32;
 template <typename T>
-__global__ void __launch_bounds__(TILE_X* TILE_Y)
+__global__ void __launch_bounds__(TILE_X* TILE_Y, 6)
 k_scatter_all(int n1, int n2, int ntx, int ntiles, int nocc, const int* __restrict__ ne,
               const int* __restrict__ ne_cnt, const int* __restrict__ tptr, const int* __restrict__ tpts,
               const int* __restrict__ bx, const int* __restrict__ by, const T* __restrict__ wx,
