@@ -717,12 +717,13 @@ def _stokes_rhs(args):
     8192 points are 0.35 h apart, where S is numerically singular), all
     solved at once by ilm_solve_stokes_multi (block CG over the right-hand
     sides, S preconditioned by the inverse point-point Schur complement
-    -E L^-1 E^T per velocity component): FP64 cache to the bench tolerance,
-    FP32 cache to 1e-6 (capped at 400 block iterations: the FP32 operator
-    stalls near 1e-2 on these thin plates); per right-hand side the FP32
-    velocity (Edges{Primal}) and traction (sigma) errors against the FP64
-    solution, relative to their max magnitude.  FP64 block iterations capped
-    at `--stokes-maxiter`."""
+    -E L^-1 E^T per velocity component): FP64 cache to the bench tolerance
+    (block iterations capped at `--stokes-maxiter`); FP32 cache with FP64
+    refinement (ilm_solve_stokes_multi_refined) to the same tolerance; FP32
+    cache alone to 1e-6 (capped at 200 block iterations: the FP32 operator
+    stalls near 1e-2 on these thin plates).  Per right-hand side the velocity
+    (Edges{Primal}) and traction (sigma) errors against the FP64 solution,
+    relative to their max magnitude."""
     import torch
     import immersedlayers as il
     from immersedlayers import workloads as W
@@ -733,29 +734,34 @@ def _stokes_rhs(args):
     res = {"npts": N, "unknowns": 2 * N, "grid": [g.nx, g.ny], "rhs": args.stokes_rhs,
            "method": "block CG over the right-hand sides, preconditioned"}
     sol = {}
-    for dt, tol, cap in ((torch.float64, args.tol, args.stokes_maxiter), (torch.float32, 1e-6, 400)):
+    runs = (("fp64", torch.float64, args.tol, args.stokes_maxiter, False),
+            ("fp32_refined", torch.float32, args.tol, 300, True),
+            ("fp32", torch.float32, 1e-6, 200, False))
+    for key, dt, tol, cap, refined in runs:
         c = il.SurfaceVectorCache(bl, g, dtype=dt)
-        V = torch.tensor(d["vplus"], dtype=dt, device="cuda")
+        V = torch.tensor(d["vplus"], dtype=torch.float64 if refined else dt, device="cuda")
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        vs, _, sig, infos = il.solve_stokes_multi(c, V, tol=tol, maxiter=cap)
+        if refined:
+            vs, _, sig, infos = il.solve_stokes_multi_refined(c, V, tol=tol, maxiter=cap)
+        else:
+            vs, _, sig, infos = il.solve_stokes_multi(c, V, tol=tol, maxiter=cap)
         torch.cuda.synchronize()
         sec = time.perf_counter() - t0   # includes the preconditioner set-up (first solve on this cache)
-        key = "fp64" if dt == torch.float64 else "fp32"
         res[key] = {"tol": tol, "maxiter_block": cap, "seconds_all_rhs": sec, "block_iterations": infos[0]["iterations"],
                     "converged": sum(i["converged"] for i in infos),
                     "max_rel_residual": max(i["rel_residual"] for i in infos)}
         sol[key] = ([v.data.double() for v in vs], [x.data.double() for x in sig])
         del c
-    per = []
-    for r in range(args.stokes_rhs):
-        v64, s64 = sol["fp64"][0][r], sol["fp64"][1][r]
-        v32, s32 = sol["fp32"][0][r], sol["fp32"][1][r]
-        per.append({"fp32_velocity_rel_err": float((v32 - v64).abs().max() / v64.abs().max()),
-                    "fp32_traction_rel_err": float((s32 - s64).abs().max() / s64.abs().max())})
-    res["per_rhs"] = per
-    res["max_fp32_velocity_rel_err"] = max(p["fp32_velocity_rel_err"] for p in per)
-    res["max_fp32_traction_rel_err"] = max(p["fp32_traction_rel_err"] for p in per)
+    for key in ("fp32", "fp32_refined"):
+        per = []
+        for r in range(args.stokes_rhs):
+            v64, s64 = sol["fp64"][0][r], sol["fp64"][1][r]
+            va, sa = sol[key][0][r], sol[key][1][r]
+            per.append((float((va - v64).abs().max() / v64.abs().max()), float((sa - s64).abs().max() / s64.abs().max())))
+        res[key]["max_velocity_rel_err_vs_fp64"] = max(p[0] for p in per)
+        res[key]["max_traction_rel_err_vs_fp64"] = max(p[1] for p in per)
+        res[key]["per_rhs_velocity_traction_rel_err"] = per
     return res
 
 

@@ -1141,7 +1141,7 @@ __global__ void __launch_bounds__(256) k_residual64(int n, const double* __restr
 }
 
 // FP64 cache of the same points for the refinement of an FP32 cache's solves
-static int ensure_twin(ilm_cache_s* c, ilm_cache_s** out) {
+int ensure_twin(ilm_cache_s* c, ilm_cache_s** out) {
   if (c->dtype == ILM_F64) {
     *out = c;
     return ILM_OK;

@@ -587,6 +587,9 @@ int st_point_dot(int n, int dtype, const void* a, const void* b, const double* w
 // Schur (ilm_schur.cu)
 // any_cache: also on vector caches (their Nodes{Primal} / Nodes{Dual} windows)
 int schur_build(ilm_cache_s* c, int which, double scale, double* A, cudaStream_t st, bool any_cache = false);
+// an FP64 cache of the same points as c (c itself when it is FP64), built on
+// first use and dropped when the points move
+int ensure_twin(ilm_cache_s* c, ilm_cache_s** out);
 struct CGParams {
   const double* A64;   // n x n column-major
   const float* A32;    // n x n column-major

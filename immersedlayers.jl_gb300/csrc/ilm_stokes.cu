@@ -311,9 +311,11 @@ int gemm(int n, int k, int t, const double* A, const double* B, double alpha, do
 // discarded (the operator's rounding level: an FP32 operator is only
 // symmetric to ~1e-7).  The iterate with the smallest worst-column residual
 // is kept; the recurrence stops when that residual grows a thousandfold
-// (an FP32 operator below its attainable accuracy) and returns the kept one.
+// (an FP32 operator below its attainable accuracy), or with a stall window
+// when it has not improved by 10% for `stall` iterations, and returns the
+// kept one.
 int block_cg(int n, int s, const BlockApply& A, const BlockPrec* M, const double* Bb, double* Y, double tol,
-             int maxiter, double drop, int* iters, double* relres, cudaStream_t st) {
+             int maxiter, double drop, int* iters, double* relres, cudaStream_t st, int stall = 0) {
   const size_t nb = (size_t)n * s * sizeof(double);
   BlockCG w;
   DevBuf Ybest;
@@ -354,6 +356,7 @@ int block_cg(int n, int s, const BlockApply& A, const BlockPrec* M, const double
   int it = 0;
   bool done = false, have_best = false;
   double best = 1.0;  // worst-column residual of Ybest (Y = 0 at start)
+  int last_gain = 0;
   auto worst = [&](const std::vector<double>& r) {
     double m = 0.0;
     for (double v : r) m = (v > m || v != v) ? v : m;
@@ -388,12 +391,15 @@ int block_cg(int n, int s, const BlockApply& A, const BlockPrec* M, const double
     ++it;
     ILM_TRY(residual_norms(hr));
     const double wr = worst(hr);
+    if (wr < 0.9 * best) last_gain = it;  // a 10% gain restarts the stall window
     if (wr < best) {
       best = wr;
       have_best = true;
       ILM_CHECK_CUDA(cudaMemcpyAsync(Ybest.p, Y, nb, cudaMemcpyDeviceToDevice, st));
     }
-    const bool diverged = !(wr <= 1e3 * best);
+    // diverging, or (with a stall window) no 10% gain for `stall` iterations:
+    // return the best iterate
+    const bool diverged = !(wr <= 1e3 * best) || (stall > 0 && it - last_gain >= stall);
     bool conv = true;
     for (int j = 0; j < s; ++j) conv = conv && hr[j] <= tol;
     if (diverged) {  // back to the best iterate; its true residual
@@ -444,54 +450,58 @@ int block_cg(int n, int s, const BlockApply& A, const BlockPrec* M, const double
   return ILM_OK;
 }
 
-}  // namespace
-}  // namespace ilm
+// Work buffers and operators of the Stokes solves on one cache (any dtype;
+// Krylov vectors in FP64, converted at the operator boundary).
+struct StokesWork {
+  ilm_cache_s* c = nullptr;
+  int N = 0, dt = 0;
+  size_t es = 0, ne = 0, nd = 0, np = 0, n2 = 0;
+  DevBuf e1, d1, d2, p1, p2, v1, v2, v4, s1;
 
-using namespace ilm;
+  int init(ilm_cache_s* cache) {
+    c = cache;
+    N = c->npts;
+    dt = c->dtype;
+    es = dt == ILM_F64 ? 8 : 4;
+    ne = c->grid.shape(PC_U).numel() + c->grid.shape(PC_V).numel();
+    nd = c->grid.shape(PC_D).numel();
+    np = c->grid.shape(PC_P).numel();
+    n2 = 2 * (size_t)N;
+    ILM_TRY(e1.alloc(ne * es));
+    ILM_TRY(d1.alloc(nd * es));
+    ILM_TRY(d2.alloc(nd * es));
+    ILM_TRY(p1.alloc(np * es));
+    ILM_TRY(p2.alloc(np * es));
+    for (DevBuf* b : {&v1, &v2, &v4}) ILM_TRY(b->alloc(std::max<size_t>(n2, 1) * es));
+    return s1.alloc(std::max<size_t>(N, 1) * es);
+  }
+  void* at(const void* base, size_t per, int j) const { return elem_ptr(base, per * j, dt); }
 
-extern "C" {
+  int to_op(const double* y, void* out, int n, cudaStream_t st) const {
+    if (n == 0) return ILM_OK;
+    if (dt == ILM_F64)
+      k_to_op<double><<<(n + 255) / 256, 256, 0, st>>>(n, N, y, c->ds64.as<double>(), static_cast<double*>(out));
+    else
+      k_to_op<float><<<(n + 255) / 256, 256, 0, st>>>(n, N, y, c->ds64.as<double>(), static_cast<float*>(out));
+    ILM_CHECK_LAUNCH();
+    return ILM_OK;
+  }
+  int from_op(const void* in, double sgn, double* out, int n, cudaStream_t st) const {
+    if (n == 0) return ILM_OK;
+    if (dt == ILM_F64)
+      k_from_op<double><<<(n + 255) / 256, 256, 0, st>>>(n, static_cast<const double*>(in), sgn, out);
+    else
+      k_from_op<float><<<(n + 255) / 256, 256, 0, st>>>(n, static_cast<const float*>(in), sgn, out);
+    ILM_CHECK_LAUNCH();
+    return ILM_OK;
+  }
 
-int ilm_solve_stokes_multi(ilm_cache_t c, int nrhs, const void* vplus, const void* vminus, void* v_out,
-                           void* s_out, void* sigma_out, double tol, int maxiter, int precond,
-                           ilm_solve_info_t* info, ilm_stream_t stream) {
-  ILM_REQUIRE(c, "null cache");
-  ILM_REQUIRE(vplus && vminus && v_out && s_out && sigma_out, "solve_stokes: null argument");
-  ILM_REQUIRE(c->kind == ILM_CACHE_VECTOR, "solve_stokes: vector cache required");
-  ILM_REQUIRE(c->scaling == ILM_GRID_SCALING, "solve_stokes: GridScaling cache required");
-  ILM_REQUIRE(tol > 0 && maxiter > 0, "solve_stokes: bad tolerance / iteration limit");
-  ILM_REQUIRE(nrhs >= 1 && nrhs <= ILM_STOKES_MAX_RHS, "solve_stokes: nrhs %d outside 1..%d", nrhs,
-              ILM_STOKES_MAX_RHS);
-  ILM_REQUIRE(precond == 0 || precond == 1, "solve_stokes: precond must be 0 or 1");
-  cudaStream_t st = as_stream(stream);
-  const int N = c->npts, dt = c->dtype;
-  const size_t es = dt == ILM_F64 ? 8 : 4;
-  const size_t ne = c->grid.shape(PC_U).numel() + c->grid.shape(PC_V).numel();
-  const size_t nd = c->grid.shape(PC_D).numel();
-  const size_t np = c->grid.shape(PC_P).numel();
-  const size_t n2 = 2 * (size_t)N;
-  auto at = [&](const void* base, size_t per, int j) { return elem_ptr(base, per * j, dt); };
-  DevBuf e1, d1, d2, p1, p2, v1, v2, v4, s1, Bb, Y, Bs, Ys, vp_all, ss_all;
-  ILM_TRY(e1.alloc(ne * es));
-  ILM_TRY(d1.alloc(nd * es));
-  ILM_TRY(d2.alloc(nd * es));
-  ILM_TRY(p1.alloc(np * es));
-  ILM_TRY(p2.alloc(np * es));
-  for (DevBuf* b : {&v1, &v2, &v4}) ILM_TRY(b->alloc(std::max<size_t>(n2, 1) * es));
-  ILM_TRY(s1.alloc(std::max<size_t>(N, 1) * es));
-  ILM_TRY(vp_all.alloc(std::max<size_t>(n2 * nrhs, 1) * es));
-  ILM_TRY(ss_all.alloc(std::max<size_t>((size_t)N * nrhs, 1) * es));
-  for (DevBuf* b : {&Bb, &Y}) ILM_TRY(b->alloc(std::max<size_t>(n2 * nrhs, 1) * sizeof(double)));
-  for (DevBuf* b : {&Bs, &Ys}) ILM_TRY(b->alloc(std::max<size_t>((size_t)N * nrhs, 1) * sizeof(double)));
-  const unsigned gb2 = (unsigned)((n2 + 255) / 256), gb1 = (unsigned)((N + 255) / 256);
-  // ---- per right-hand side: psi*, v_phi, v' and the Ss right-hand side ----
-  for (int r = 0; r < nrhs; ++r) {
-    const void* vpl = at(vplus, n2, r);
-    const void* vmi = at(vminus, n2, r);
-    void* vo = at(v_out, ne, r);
-    void* so = at(s_out, nd, r);
+  // psi* (into s_out), v_phi (into v_out), v' and the Ss right-hand side
+  // G^x_s phi of one right-hand side (cache dtype)
+  int prepare(const void* vpl, const void* vmi, void* vo, void* so, void* vp, void* ssr, cudaStream_t st) {
+    ilm_stream_t stream = st;
     void* dv = v1.p;  // [v]
     void* vb = v2.p;  // avg
-    void* vp = at(vp_all.p, n2, r);
     ILM_TRY(st_axpby(n2, dt, 1.0, vpl, -1.0, vmi, dv, st));
     ILM_TRY(st_axpby(n2, dt, 0.5, vpl, 0.5, vmi, vb, st));
     // psi* = L^-2 (-C D_s^symm [v])
@@ -499,15 +509,15 @@ int ilm_solve_stokes_multi(ilm_cache_t c, int nrhs, const void* vplus, const voi
     ILM_TRY(ilm_curl(c, ILM_EDGES_PRIMAL, e1.p, d1.p, stream));
     ILM_TRY(st_affine(nd, dt, -1.0, d1.p, 0.0, d1.p, st));
     ILM_TRY(ilm_inverse_laplacian(c, ILM_NODES_DUAL, d1.p, d2.p, stream));
-    ILM_TRY(ilm_inverse_laplacian(c, ILM_NODES_DUAL, d2.p, so, stream));  // s_out holds psi*
+    ILM_TRY(ilm_inverse_laplacian(c, ILM_NODES_DUAL, d2.p, so, stream));
     // phi = L^-1 R (n . [v]),  v_phi = G phi  (kept in v_out)
     if (N > 0) {
       if (dt == ILM_F64)
-        k_ndot<double><<<gb1, 256, 0, st>>>(N, c->nx.as<double>(), c->ny.as<double>(),
-                                            static_cast<const double*>(dv), s1.as<double>());
+        k_ndot<double><<<(N + 255) / 256, 256, 0, st>>>(N, c->nx.as<double>(), c->ny.as<double>(),
+                                                        static_cast<const double*>(dv), s1.as<double>());
       else
-        k_ndot<float><<<gb1, 256, 0, st>>>(N, c->nx.as<float>(), c->ny.as<float>(), static_cast<const float*>(dv),
-                                           s1.as<float>());
+        k_ndot<float><<<(N + 255) / 256, 256, 0, st>>>(N, c->nx.as<float>(), c->ny.as<float>(),
+                                                       static_cast<const float*>(dv), s1.as<float>());
       ILM_CHECK_LAUNCH();
     }
     ILM_TRY(ilm_regularize(c, ILM_NODES_PRIMAL, s1.p, p1.p, stream));
@@ -520,99 +530,128 @@ int ilm_solve_stokes_multi(ilm_cache_t c, int nrhs, const void* vplus, const voi
     ILM_TRY(ilm_curl(c, ILM_NODES_DUAL, so, e1.p, stream));
     ILM_TRY(ilm_interpolate(c, ILM_EDGES_PRIMAL, e1.p, v4.p, stream));
     ILM_TRY(st_axpby(n2, dt, 1.0, vp, -1.0, v4.p, vp, st));
-    // right-hand side of the streamfunction equivalent: G^x_s phi
-    ILM_TRY(ilm_surface_grad_cross(c, phi, at(ss_all.p, N, r), stream));
+    return ilm_surface_grad_cross(c, phi, ssr, stream);
   }
-  // ---- block solve of S sigma = v' in y = W sigma: (-S W^-1) y = -v' ----
-  auto to_op = [&](const double* y, void* out, int n) -> int {
-    if (n == 0) return ILM_OK;
-    if (dt == ILM_F64)
-      k_to_op<double><<<(n + 255) / 256, 256, 0, st>>>(n, N, y, c->ds64.as<double>(), static_cast<double*>(out));
-    else
-      k_to_op<float><<<(n + 255) / 256, 256, 0, st>>>(n, N, y, c->ds64.as<double>(), static_cast<float*>(out));
-    ILM_CHECK_LAUNCH();
-    return ILM_OK;
-  };
-  auto from_op = [&](const void* in, double sgn, double* out, int n) -> int {
-    if (n == 0) return ILM_OK;
-    if (dt == ILM_F64)
-      k_from_op<double><<<(n + 255) / 256, 256, 0, st>>>(n, static_cast<const double*>(in), sgn, out);
-    else
-      k_from_op<float><<<(n + 255) / 256, 256, 0, st>>>(n, static_cast<const float*>(in), sgn, out);
-    ILM_CHECK_LAUNCH();
-    return ILM_OK;
-  };
-  for (int r = 0; r < nrhs; ++r) ILM_TRY(from_op(at(vp_all.p, n2, r), -1.0, Bb.as<double>() + n2 * r, (int)n2));
-  BlockApply applyB = [&](const double* Yb, double* Qb, int s) -> int {
+
+  // Q = (-S W^-1) Y = C_s L^-2 C_s^T W^-1 Y, column by column (n2 x s)
+  int applyB(const double* Yb, double* Qb, int s, cudaStream_t st) {
+    ilm_stream_t stream = st;
     for (int j = 0; j < s; ++j) {
-      ILM_TRY(to_op(Yb + n2 * j, v4.p, (int)n2));
+      ILM_TRY(to_op(Yb + n2 * j, v4.p, (int)n2, st));
       ILM_TRY(ilm_surface_curl(c, 0, ILM_VECTOR_DATA, v4.p, d1.p, stream));
       ILM_TRY(ilm_inverse_laplacian(c, ILM_NODES_DUAL, d1.p, d2.p, stream));
       ILM_TRY(ilm_inverse_laplacian(c, ILM_NODES_DUAL, d2.p, d1.p, stream));
       ILM_TRY(ilm_surface_curl(c, 1, ILM_VECTOR_DATA, d1.p, v4.p, stream));
-      ILM_TRY(from_op(v4.p, 1.0, Qb + n2 * j, (int)n2));
+      ILM_TRY(from_op(v4.p, 1.0, Qb + n2 * j, (int)n2, st));
     }
     return ILM_OK;
-  };
-  const bool use_pc = precond == 1 && N > 0 && N <= STOKES_PC_MAX;
-  if (use_pc) ILM_TRY(ensure_stokes_pc(c, st));
-  BlockPrec applyM = [&](const double* Rb, double* Zb, int s) -> int {
-    // each velocity component: Z_comp = P^-1 R_comp (leading dimension 2N)
+  }
+  // Q = (Ss W^-1) Y, Ss = -C_s L^-1 C_s^T on scalars (N x s)
+  int applyBs(const double* Yb, double* Qb, int s, cudaStream_t st) {
+    ilm_stream_t stream = st;
+    for (int j = 0; j < s; ++j) {
+      ILM_TRY(to_op(Yb + (size_t)N * j, s1.p, N, st));
+      ILM_TRY(ilm_surface_curl(c, 0, ILM_SCALAR_DATA, s1.p, d1.p, stream));
+      ILM_TRY(ilm_inverse_laplacian(c, ILM_NODES_DUAL, d1.p, d2.p, stream));
+      ILM_TRY(ilm_surface_curl(c, 1, ILM_SCALAR_DATA, d2.p, s1.p, stream));
+      ILM_TRY(from_op(s1.p, -1.0, Qb + (size_t)N * j, N, st));
+    }
+    return ILM_OK;
+  }
+  // each velocity component: Z_comp = P^-1 R_comp (leading dimension 2N)
+  int applyM(const double* Rb, double* Zb, int s, cudaStream_t st) const {
     const double* Ti = c->stokes_pc.as<double>();
     for (int comp = 0; comp < 2; ++comp)
       for (int j0 = 0; j0 < s; j0 += 8) {
         const int t = std::min(8, s - j0);
-        k_gemm_rows<<<gb1, 256, 0, st>>>(N, N, t, Ti, N, Rb + comp * N + n2 * j0, (int)n2, 1.0, 0.0,
-                                         Zb + comp * N + n2 * j0, (int)n2);
+        k_gemm_rows<<<(N + 255) / 256, 256, 0, st>>>(N, N, t, Ti, N, Rb + comp * N + n2 * j0, (int)n2, 1.0, 0.0,
+                                                     Zb + comp * N + n2 * j0, (int)n2);
         ILM_CHECK_LAUNCH();
       }
     return ILM_OK;
-  };
-  std::vector<double> rr1(nrhs, 0.0), rr2(nrhs, 0.0);
-  int it1 = 0, it2 = 0;
-  const double drop = dt == ILM_F64 ? 1e-13 : 1e-6;
-  ILM_TRY(block_cg((int)n2, nrhs, applyB, use_pc ? &applyM : nullptr, Bb.as<double>(), Y.as<double>(), tol, maxiter,
-                   drop, &it1, rr1.data(), st));
-  // sigma = W^-1 y
-  for (int r = 0; r < nrhs; ++r) ILM_TRY(to_op(Y.as<double>() + n2 * r, at(sigma_out, n2, r), (int)n2));
-  // ---- fields, and the right-hand sides of the Ss solves ----
-  for (int r = 0; r < nrhs; ++r) {
-    void* vo = at(v_out, ne, r);
-    void* so = at(s_out, nd, r);
-    // psi = psi* + L^-2 (-C_s^T sigma)
-    ILM_TRY(ilm_surface_curl(c, 0, ILM_VECTOR_DATA, at(sigma_out, n2, r), d1.p, stream));
+  }
+
+  // sigma = W^-1 y; psi = psi* + L^-2 (-C_s^T sigma); v = C psi + v_phi
+  int fields(const double* Yr, void* sig, void* vo, void* so, cudaStream_t st) {
+    ilm_stream_t stream = st;
+    ILM_TRY(to_op(Yr, sig, (int)n2, st));
+    ILM_TRY(ilm_surface_curl(c, 0, ILM_VECTOR_DATA, sig, d1.p, stream));
     ILM_TRY(st_affine(nd, dt, -1.0, d1.p, 0.0, d1.p, st));
     ILM_TRY(ilm_inverse_laplacian(c, ILM_NODES_DUAL, d1.p, d2.p, stream));
     ILM_TRY(ilm_inverse_laplacian(c, ILM_NODES_DUAL, d2.p, d1.p, stream));
     ILM_TRY(st_axpby(nd, dt, 1.0, d1.p, 1.0, so, so, st));
-    // v = C psi + v_phi
     ILM_TRY(ilm_curl(c, ILM_NODES_DUAL, so, e1.p, stream));
-    ILM_TRY(st_axpby(ne, dt, 1.0, e1.p, 1.0, vo, vo, st));
-    ILM_TRY(from_op(at(ss_all.p, N, r), 1.0, Bs.as<double>() + (size_t)N * r, N));
+    return st_axpby(ne, dt, 1.0, e1.p, 1.0, vo, vo, st);
   }
-  // ---- block solve of Ss d = G^x_s phi in y = W d: (Ss W^-1) y = rhs ----
-  BlockApply applyBs = [&](const double* Yb, double* Qb, int s) -> int {
-    for (int j = 0; j < s; ++j) {
-      ILM_TRY(to_op(Yb + (size_t)N * j, s1.p, N));
-      ILM_TRY(ilm_surface_curl(c, 0, ILM_SCALAR_DATA, s1.p, d1.p, stream));
-      ILM_TRY(ilm_inverse_laplacian(c, ILM_NODES_DUAL, d1.p, d2.p, stream));
-      ILM_TRY(ilm_surface_curl(c, 1, ILM_SCALAR_DATA, d2.p, s1.p, stream));
-      ILM_TRY(from_op(s1.p, -1.0, Qb + (size_t)N * j, N));
-    }
-    return ILM_OK;
-  };
-  ILM_TRY(block_cg(N, nrhs, applyBs, nullptr, Bs.as<double>(), Ys.as<double>(), tol, maxiter, drop, &it2, rr2.data(),
-                   st));
-  for (int r = 0; r < nrhs; ++r) {
-    void* so = at(s_out, nd, r);
-    ILM_TRY(to_op(Ys.as<double>() + (size_t)N * r, s1.p, N));
+  // psi += L^-1 (-C^x_s^T W^-1 ys); sigma <- F^2 sigma
+  int finish(const double* Ysr, void* sig, void* so, cudaStream_t st) {
+    ilm_stream_t stream = st;
+    ILM_TRY(to_op(Ysr, s1.p, N, st));
     ILM_TRY(ilm_surface_curl_cross(c, 0, s1.p, d1.p, stream));
     ILM_TRY(st_affine(nd, dt, -1.0, d1.p, 0.0, d1.p, st));
     ILM_TRY(ilm_inverse_laplacian(c, ILM_NODES_DUAL, d1.p, d2.p, stream));
     ILM_TRY(st_axpby(nd, dt, 1.0, d2.p, 1.0, so, so, st));
-    // sigma <- F^2 sigma,  F = W^-1 E R,  W = E R 1
-    ILM_TRY(ilm_surface_filter(c, 2, at(sigma_out, n2, r), at(sigma_out, n2, r), stream));
+    return ilm_surface_filter(c, 2, sig, sig, stream);
   }
+};
+
+int stokes_check(ilm_cache_s* c, int nrhs, double tol, int maxiter) {
+  ILM_REQUIRE(c, "null cache");
+  ILM_REQUIRE(c->kind == ILM_CACHE_VECTOR, "solve_stokes: vector cache required");
+  ILM_REQUIRE(c->scaling == ILM_GRID_SCALING, "solve_stokes: GridScaling cache required");
+  ILM_REQUIRE(tol > 0 && maxiter > 0, "solve_stokes: bad tolerance / iteration limit");
+  ILM_REQUIRE(nrhs >= 1 && nrhs <= ILM_STOKES_MAX_RHS, "solve_stokes: nrhs %d outside 1..%d", nrhs,
+              ILM_STOKES_MAX_RHS);
+  return ILM_OK;
+}
+
+}  // namespace
+}  // namespace ilm
+
+using namespace ilm;
+
+extern "C" {
+
+int ilm_solve_stokes_multi(ilm_cache_t c, int nrhs, const void* vplus, const void* vminus, void* v_out,
+                           void* s_out, void* sigma_out, double tol, int maxiter, int precond,
+                           ilm_solve_info_t* info, ilm_stream_t stream) {
+  ILM_TRY(stokes_check(c, nrhs, tol, maxiter));
+  ILM_REQUIRE(vplus && vminus && v_out && s_out && sigma_out, "solve_stokes: null argument");
+  ILM_REQUIRE(precond == 0 || precond == 1, "solve_stokes: precond must be 0 or 1");
+  cudaStream_t st = as_stream(stream);
+  StokesWork w;
+  ILM_TRY(w.init(c));
+  const int N = w.N;
+  const size_t n2 = w.n2, ne = w.ne, nd = w.nd;
+  DevBuf Bb, Y, Bs, Ys, vp_all, ss_all;
+  ILM_TRY(vp_all.alloc(std::max<size_t>(n2 * nrhs, 1) * w.es));
+  ILM_TRY(ss_all.alloc(std::max<size_t>((size_t)N * nrhs, 1) * w.es));
+  for (DevBuf* b : {&Bb, &Y}) ILM_TRY(b->alloc(std::max<size_t>(n2 * nrhs, 1) * sizeof(double)));
+  for (DevBuf* b : {&Bs, &Ys}) ILM_TRY(b->alloc(std::max<size_t>((size_t)N * nrhs, 1) * sizeof(double)));
+  for (int r = 0; r < nrhs; ++r) {
+    ILM_TRY(w.prepare(w.at(vplus, n2, r), w.at(vminus, n2, r), w.at(v_out, ne, r), w.at(s_out, nd, r),
+                      w.at(vp_all.p, n2, r), w.at(ss_all.p, N, r), st));
+    ILM_TRY(w.from_op(w.at(vp_all.p, n2, r), -1.0, Bb.as<double>() + n2 * r, (int)n2, st));
+    ILM_TRY(w.from_op(w.at(ss_all.p, N, r), 1.0, Bs.as<double>() + (size_t)N * r, N, st));
+  }
+  // S sigma = v' in y = W sigma: (-S W^-1) y = -v'
+  BlockApply applyB = [&](const double* Yb, double* Qb, int s) { return w.applyB(Yb, Qb, s, st); };
+  BlockApply applyBs = [&](const double* Yb, double* Qb, int s) { return w.applyBs(Yb, Qb, s, st); };
+  BlockPrec applyM = [&](const double* Rb, double* Zb, int s) { return w.applyM(Rb, Zb, s, st); };
+  const bool use_pc = precond == 1 && N > 0 && N <= STOKES_PC_MAX;
+  if (use_pc) ILM_TRY(ensure_stokes_pc(c, st));
+  std::vector<double> rr1(nrhs, 0.0), rr2(nrhs, 0.0);
+  int it1 = 0, it2 = 0;
+  const double drop = w.dt == ILM_F64 ? 1e-13 : 1e-6;
+  ILM_TRY(block_cg((int)n2, nrhs, applyB, use_pc ? &applyM : nullptr, Bb.as<double>(), Y.as<double>(), tol, maxiter,
+                   drop, &it1, rr1.data(), st));
+  for (int r = 0; r < nrhs; ++r)
+    ILM_TRY(w.fields(Y.as<double>() + n2 * r, w.at(sigma_out, n2, r), w.at(v_out, ne, r), w.at(s_out, nd, r), st));
+  // Ss d = G^x_s phi in y = W d: (Ss W^-1) y = rhs
+  ILM_TRY(block_cg(N, nrhs, applyBs, nullptr, Bs.as<double>(), Ys.as<double>(), tol, maxiter, drop, &it2, rr2.data(),
+                   st));
+  for (int r = 0; r < nrhs; ++r)
+    ILM_TRY(w.finish(Ys.as<double>() + (size_t)N * r, w.at(sigma_out, n2, r), w.at(s_out, nd, r), st));
   ILM_CHECK_CUDA(cudaStreamSynchronize(st));
   bool ok = true;
   for (int r = 0; r < nrhs; ++r) {
@@ -631,6 +670,105 @@ int ilm_solve_stokes_multi(ilm_cache_t c, int nrhs, const void* vplus, const voi
 int ilm_solve_stokes(ilm_cache_t c, const void* vplus, const void* vminus, void* v_out, void* s_out, void* sigma_out,
                      double tol, int maxiter, ilm_solve_info_t* info, ilm_stream_t stream) {
   return ilm_solve_stokes_multi(c, 1, vplus, vminus, v_out, s_out, sigma_out, tol, maxiter, 1, info, stream);
+}
+
+// FP64-refined Stokes solves (see ilm.h).  The pre-step, the FP64 residuals
+// and the field assembly run on the FP64 twin cache; each correction is a
+// block CG with the cache's own operator (FP32 for an FP32 cache) to
+// kStokesInnerTol of its residual, stopped early when it stalls.
+int ilm_solve_stokes_multi_refined(ilm_cache_t c, int nrhs, const double* vplus, const double* vminus,
+                                   double* v_out, double* s_out, double* sigma_out, double tol, int maxiter,
+                                   int max_refine, ilm_solve_info_t* info, ilm_stream_t stream) {
+  constexpr double kStokesInnerTol = 1e-4;
+  constexpr int kStokesStall = 40;  // block iterations without a 10% gain end a correction
+  ILM_TRY(stokes_check(c, nrhs, tol, maxiter));
+  ILM_REQUIRE(vplus && vminus && v_out && s_out && sigma_out, "solve_stokes_refined: null argument");
+  ILM_REQUIRE(max_refine >= 1, "solve_stokes_refined: max_refine must be >= 1");
+  cudaStream_t st = as_stream(stream);
+  ilm_cache_s* c64 = nullptr;
+  ILM_TRY(ensure_twin(c, &c64));
+  StokesWork w64, wb;
+  ILM_TRY(w64.init(c64));
+  const bool sep = c64 != c;
+  if (sep) ILM_TRY(wb.init(c));
+  StokesWork& wk = sep ? wb : w64;  // the corrections' operator
+  const int N = w64.N;
+  const size_t n2 = w64.n2, ne = w64.ne, nd = w64.nd;
+  DevBuf vp_all, ss_all, Bb, Y, R, D, Q, Bs, Ys, Rs, Ds, Qs;
+  ILM_TRY(vp_all.alloc(std::max<size_t>(n2 * nrhs, 1) * 8));
+  ILM_TRY(ss_all.alloc(std::max<size_t>((size_t)N * nrhs, 1) * 8));
+  for (DevBuf* b : {&Bb, &Y, &R, &D, &Q}) ILM_TRY(b->alloc(std::max<size_t>(n2 * nrhs, 1) * sizeof(double)));
+  for (DevBuf* b : {&Bs, &Ys, &Rs, &Ds, &Qs}) ILM_TRY(b->alloc(std::max<size_t>((size_t)N * nrhs, 1) * sizeof(double)));
+  for (int r = 0; r < nrhs; ++r) {
+    ILM_TRY(w64.prepare(vplus + n2 * r, vminus + n2 * r, v_out + ne * r, s_out + nd * r, vp_all.as<double>() + n2 * r,
+                        ss_all.as<double>() + (size_t)N * r, st));
+    ILM_TRY(w64.from_op(vp_all.as<double>() + n2 * r, -1.0, Bb.as<double>() + n2 * r, (int)n2, st));
+    ILM_TRY(w64.from_op(ss_all.as<double>() + (size_t)N * r, 1.0, Bs.as<double>() + (size_t)N * r, N, st));
+  }
+  const bool use_pc = N > 0 && N <= STOKES_PC_MAX;
+  if (use_pc) ILM_TRY(ensure_stokes_pc(c, st));
+  BlockPrec applyM = [&](const double* Rb, double* Zb, int s) { return wk.applyM(Rb, Zb, s, st); };
+  const double drop = wk.dt == ILM_F64 ? 1e-13 : 1e-6;
+  // y += B^-1 (b - B y) with B in the corrections' precision, b - B y in FP64
+  auto refine = [&](size_t n, bool vec, const double* b, double* y, double* res, double* d, double* q,
+                    std::vector<double>& rel, int* iters) -> int {
+    BlockApply A64 = [&](const double* Yb, double* Qb, int s) {
+      return vec ? w64.applyB(Yb, Qb, s, st) : w64.applyBs(Yb, Qb, s, st);
+    };
+    BlockApply Ak = [&](const double* Yb, double* Qb, int s) {
+      return vec ? wk.applyB(Yb, Qb, s, st) : wk.applyBs(Yb, Qb, s, st);
+    };
+    const size_t nb = n * nrhs * sizeof(double);
+    ILM_CHECK_CUDA(cudaMemsetAsync(y, 0, nb, st));
+    ILM_CHECK_CUDA(cudaMemcpyAsync(res, b, nb, cudaMemcpyDeviceToDevice, st));
+    std::vector<double> bn(nrhs), g;
+    DevBuf G;
+    ILM_TRY(G.alloc((size_t)nrhs * nrhs * sizeof(double)));
+    ILM_TRY(gram(b, nrhs, b, nrhs, (int)n, G.as<double>(), g, st));
+    for (int j = 0; j < nrhs; ++j) bn[j] = sqrt(std::max(g[j + (size_t)j * nrhs], 0.0));
+    rel.assign(nrhs, 1.0);
+    *iters = 0;
+    std::vector<double> rin(nrhs);
+    for (int k = 0; k < max_refine; ++k) {
+      int it = 0;
+      ILM_TRY(block_cg((int)n, nrhs, Ak, vec && use_pc ? &applyM : nullptr, res, d, kStokesInnerTol, maxiter, drop,
+                       &it, rin.data(), st, kStokesStall));
+      *iters += it;
+      ILM_TRY(st_axpby(n * nrhs, ILM_F64, 1.0, y, 1.0, d, y, st));
+      ILM_TRY(A64(y, q, nrhs));
+      ILM_TRY(st_axpby(n * nrhs, ILM_F64, 1.0, b, -1.0, q, res, st));
+      ILM_TRY(gram(res, nrhs, res, nrhs, (int)n, G.as<double>(), g, st));
+      bool all = true;
+      for (int j = 0; j < nrhs; ++j) {
+        rel[j] = bn[j] > 0.0 ? sqrt(std::max(g[j + (size_t)j * nrhs], 0.0)) / bn[j] : 0.0;
+        all = all && rel[j] <= tol;
+      }
+      if (all) break;
+    }
+    return ILM_OK;
+  };
+  std::vector<double> rr1, rr2;
+  int it1 = 0, it2 = 0;
+  ILM_TRY(refine(n2, true, Bb.as<double>(), Y.as<double>(), R.as<double>(), D.as<double>(), Q.as<double>(), rr1, &it1));
+  for (int r = 0; r < nrhs; ++r)
+    ILM_TRY(w64.fields(Y.as<double>() + n2 * r, sigma_out + n2 * r, v_out + ne * r, s_out + nd * r, st));
+  ILM_TRY(refine(N, false, Bs.as<double>(), Ys.as<double>(), Rs.as<double>(), Ds.as<double>(), Qs.as<double>(), rr2,
+                 &it2));
+  for (int r = 0; r < nrhs; ++r)
+    ILM_TRY(w64.finish(Ys.as<double>() + (size_t)N * r, sigma_out + n2 * r, s_out + nd * r, st));
+  ILM_CHECK_CUDA(cudaStreamSynchronize(st));
+  bool ok = true;
+  for (int r = 0; r < nrhs; ++r) {
+    const bool cr = rr1[r] <= tol && rr2[r] <= tol;
+    ok = ok && cr;
+    if (info) {
+      info[r].iterations = it1 + it2;
+      info[r].converged = cr ? 1 : 0;
+      info[r].rel_residual = std::max(rr1[r], rr2[r]);
+    }
+  }
+  if (!ok) set_error("solve_stokes_refined: rel. residual %g not reached in %d refinement steps", tol, max_refine);
+  return ok ? ILM_OK : ILM_ERR_NOT_CONVERGED;
 }
 
 }  // extern "C"

@@ -26,7 +26,7 @@ from .core import (Dual, EdgeGradient, EdgeGradientPrimal, Edges, EdgesDual, Edg
 from .problems import (DirichletPoissonProblem, ILMProblem, ILMSystem, NeumannPoissonProblem, StokesFlowProblem,
                        construct_system, prescribed_surface_average_, prescribed_surface_jump_, solve,
                        solve_dirichlet, solve_dirichlet_refined, solve_neumann, solve_neumann_full,
-                       solve_neumann_refined, solve_stokes, solve_stokes_multi,
+                       solve_neumann_refined, solve_stokes, solve_stokes_multi, solve_stokes_multi_refined,
                        update_system_)
 from .helmholtz import (ScalarPotentialCache, VectorFieldCache, VectorPotentialCache, curlv_masked_from_masked_curlv_,
                         divv_masked_from_masked_divv_, masked_curlv_from_curlv_masked_,

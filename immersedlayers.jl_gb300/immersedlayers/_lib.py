@@ -101,6 +101,7 @@ SIGNATURES = {
     "ilm_solve_neumann_full": [_VP, _VP, _VP, _VP, _VP, _VP, _VP, _D, _I, C.POINTER(SolveInfo), _VP],
     "ilm_solve_stokes": [_VP, _VP, _VP, _VP, _VP, _VP, _D, _I, C.POINTER(SolveInfo), _VP],
     "ilm_solve_stokes_multi": [_VP, _I, _VP, _VP, _VP, _VP, _VP, _D, _I, _I, C.POINTER(SolveInfo), _VP],
+    "ilm_solve_stokes_multi_refined": [_VP, _I, _VP, _VP, _VP, _VP, _VP, _D, _I, _I, C.POINTER(SolveInfo), _VP],
     "ilm_batch_create": [_I, C.POINTER(BatchProblem), _DP, _DP, _DP, _DP, _DP, _I, _I, C.POINTER(_VP)],
     "ilm_batch_destroy": [_VP],
     "ilm_batch_layout": [_VP, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)],
@@ -141,7 +142,7 @@ _RESTYPES = {"ilm_status_string": C.c_char_p, "ilm_last_error": C.c_char_p}
 
 # functions that may legitimately return ILM_ERR_NOT_CONVERGED (reported via info)
 _SOFT = {"ilm_solve_dirichlet", "ilm_solve_neumann", "ilm_solve_neumann_full", "ilm_solve_stokes",
-         "ilm_solve_stokes_multi",
+         "ilm_solve_stokes_multi", "ilm_solve_stokes_multi_refined",
          "ilm_solve_dirichlet_refined", "ilm_solve_neumann_refined"}
 
 _lib = None

@@ -236,6 +236,39 @@ def solve_stokes_multi(cache, vplus: torch.Tensor, vminus: torch.Tensor = None, 
                          for i in infos]
 
 
+def solve_stokes_multi_refined(cache, vplus: torch.Tensor, vminus: torch.Tensor = None, tol=1e-10, maxiter=2000,
+                               max_refine=8, stream=None):
+    """Stokes solves for several right-hand sides with FP64 iterative
+    refinement (FP64 outputs for any cache dtype): FP64 pre-step, residuals
+    and fields on an FP64 cache of the same points, corrections by block CG
+    with the cache's own operator.  vplus / vminus: (nrhs, 2N) tensors
+    (converted to FP64).  Returns (v: nrhs Edges{Primal} FP64, s: nrhs
+    Nodes{Dual} FP64, sigma: nrhs VectorData FP64, infos)."""
+    from .core import EdgesPrimal, NodesDual
+    if vplus.dim() != 2 or vplus.shape[1] != 2 * len(cache):
+        raise ValueError(f"vplus must be (nrhs, {2 * len(cache)})")
+    nrhs = vplus.shape[0]
+    if not 1 <= nrhs <= L.STOKES_MAX_RHS:
+        raise ValueError(f"nrhs must be in 1..{L.STOKES_MAX_RHS}")
+    p64 = vplus.to(torch.float64).contiguous()
+    m64 = torch.zeros_like(p64) if vminus is None else vminus.to(torch.float64).contiguous()
+    vs = [EdgesPrimal.zeros(cache.g, torch.float64) for _ in range(nrhs)]
+    ss = [NodesDual.zeros(cache.g, torch.float64) for _ in range(nrhs)]
+    v_all = torch.empty((nrhs,) + tuple(vs[0].data.shape), dtype=torch.float64, device=p64.device)
+    s_all = torch.empty((nrhs,) + tuple(ss[0].data.shape), dtype=torch.float64, device=p64.device)
+    sig_all = torch.empty_like(p64)
+    infos = (L.SolveInfo * nrhs)()
+    L.call("ilm_solve_stokes_multi_refined", cache._h, nrhs, _ptr(p64), _ptr(m64), _ptr(v_all), _ptr(s_all),
+           _ptr(sig_all), float(tol), int(maxiter), int(max_refine), infos, _stream_ptr(stream))
+    sig = []
+    for r in range(nrhs):
+        vs[r].data.copy_(v_all[r])
+        ss[r].data.copy_(s_all[r])
+        sig.append(VectorData(sig_all[r].clone()))
+    return vs, ss, sig, [dict(iterations=i.iterations, converged=bool(i.converged), rel_residual=i.rel_residual)
+                         for i in infos]
+
+
 def solve(prob: ILMProblem, sys: ILMSystem, tol=1e-8, maxiter=5000, filter_power=0):
     """`solve(prob, sys)` for the built-in problems (bc from `prob.bc`):
     Dirichlet (f, s), Neumann (f, df, s, ds) as test/literate/neumann.jl:140,

@@ -339,6 +339,18 @@ ILM_API int ilm_solve_stokes(ilm_cache_t c, const void* vplus, const void* vminu
 ILM_API int ilm_solve_stokes_multi(ilm_cache_t c, int nrhs, const void* vplus, const void* vminus, void* v_out,
                                    void* s_out, void* sigma_out, double tol, int maxiter, int precond,
                                    ilm_solve_info_t* info, ilm_stream_t stream);
+/* FP64-refined Stokes solves for `nrhs` right-hand sides: FP64 inputs and
+ * outputs (layouts as ilm_solve_stokes_multi).  The pre-step (psi*, v_phi,
+ * v'), every Schur residual b - S sigma and the field assembly run in FP64
+ * on an FP64 cache of the same points (built on first use, dropped when the
+ * points move); the corrections S d = r are block CG with the cache's own
+ * operator (FP32 for an FP32 cache; S preconditioned as in
+ * ilm_solve_stokes_multi), each to 1e-4 of its residual or until it stops
+ * improving, for at most max_refine steps per Schur system.  info: FP64
+ * relative residuals; iterations = block iterations of all corrections.    */
+ILM_API int ilm_solve_stokes_multi_refined(ilm_cache_t c, int nrhs, const double* vplus, const double* vminus,
+                                           double* v_out, double* s_out, double* sigma_out, double tol, int maxiter,
+                                           int max_refine, ilm_solve_info_t* info, ilm_stream_t stream);
 
 /* ---- batched problem solves (configs of many independent problems) ------ */
 /* Many independent Dirichlet/Neumann Poisson problems (each its own grid and

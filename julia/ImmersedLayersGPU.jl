@@ -251,6 +251,12 @@ ilm_solve_stokes_multi(c, nrhs, vplus, vminus, v_out, s_out, sigma_out, tol, max
           (Ptr{Cvoid}, Cint, CuPtr{Cvoid}, CuPtr{Cvoid}, CuPtr{Cvoid}, CuPtr{Cvoid}, CuPtr{Cvoid}, Cdouble, Cint, Cint,
            Ptr{SolveInfo}, Ptr{Cvoid}),
           c, nrhs, vplus, vminus, v_out, s_out, sigma_out, tol, maxiter, precond, info, stream)
+ilm_solve_stokes_multi_refined(c, nrhs, vplus, vminus, v_out, s_out, sigma_out, tol, maxiter, max_refine, info,
+                               stream) =
+    ccall((:ilm_solve_stokes_multi_refined, libilm), Cint,
+          (Ptr{Cvoid}, Cint, CuPtr{Cdouble}, CuPtr{Cdouble}, CuPtr{Cdouble}, CuPtr{Cdouble}, CuPtr{Cdouble}, Cdouble,
+           Cint, Cint, Ptr{SolveInfo}, Ptr{Cvoid}),
+          c, nrhs, vplus, vminus, v_out, s_out, sigma_out, tol, maxiter, max_refine, info, stream)
 
 # batched solves
 ilm_batch_create(nprob, probs, x, y, nrmx, nrmy, ds, ddf, dtype, out) =

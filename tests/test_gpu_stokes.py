@@ -176,3 +176,29 @@ def test_stokes_multi_rejects_bad_arguments(cuda):
     sc = il.SurfaceScalarCache(bl, g, dtype=torch.float64)
     with pytest.raises(ILMError, match="vector cache"):
         il.solve_stokes_multi(sc, torch.zeros(1, 2 * N, dtype=torch.float64, device="cuda"))
+
+
+@pytest.mark.parametrize("dtype", ["f32", "f64"])
+def test_stokes_multi_refined_matches_oracle(cuda, dtype):
+    """FP64 refinement of the Stokes solves from an FP32 (or FP64) cache:
+    FP64 outputs, Schur residuals <= 1e-10, and every right-hand side's v, s
+    and sigma against the oracle's dense block-LU solve at the FP64 bars."""
+    import torch
+    import immersedlayers as il
+    og, bl = _case(two_bodies=True)
+    g = il.PhysicalGrid((-2.0, 2.0), (-2.0, 2.0), og.h)
+    c = il.SurfaceVectorCache(bl, g, dtype=torch.float32 if dtype == "f32" else torch.float64)
+    N = len(bl)
+    V = _rigid_rhs(bl, 3, 5)
+    vs, ss, sig, infos = il.solve_stokes_multi_refined(c, torch.tensor(V, device="cuda"), tol=1e-10)
+    assert all(i["converged"] and i["rel_residual"] <= 1e-10 for i in infos), infos
+    assert vs[0].data.dtype == torch.float64 and sig[0].data.dtype == torch.float64
+    oc = oracle_cache(og, bl, kind="vector")
+    S = O.create_CL2invCT_vector(oc)
+    Ss = O.create_CLinvCT_scalar_vector(oc)
+    filt = O.surface_filter_vector(oc)
+    for r in range(V.shape[0]):
+        v_ref, s_ref, sig_ref = O.solve_stokes(oc, V[r], np.zeros(2 * N), S=S, Ss=Ss, filt=filt)
+        assert rel(vs[r].numpy_components(), v_ref) < 1e-7, r
+        assert rel(ss[r].numpy_components(), s_ref) < 1e-7, r
+        assert rel(sig[r].numpy(), sig_ref) < 1e-4, r
