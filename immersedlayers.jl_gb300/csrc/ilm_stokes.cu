@@ -728,7 +728,8 @@ int ilm_solve_stokes_multi_refined(ilm_cache_t c, int nrhs, const double* vplus,
     for (int j = 0; j < nrhs; ++j) bn[j] = sqrt(std::max(g[j + (size_t)j * nrhs], 0.0));
     rel.assign(nrhs, 1.0);
     *iters = 0;
-    std::vector<double> rin(nrhs);
+    std::vector<double> rin(nrhs), relk(nrhs);
+    double worst_prev = 1.0;
     for (int k = 0; k < max_refine; ++k) {
       int it = 0;
       ILM_TRY(block_cg((int)n, nrhs, Ak, vec && use_pc ? &applyM : nullptr, res, d, kStokesInnerTol, maxiter, drop,
@@ -736,13 +737,24 @@ int ilm_solve_stokes_multi_refined(ilm_cache_t c, int nrhs, const double* vplus,
       *iters += it;
       ILM_TRY(st_axpby(n * nrhs, ILM_F64, 1.0, y, 1.0, d, y, st));
       ILM_TRY(A64(y, q, nrhs));
-      ILM_TRY(st_axpby(n * nrhs, ILM_F64, 1.0, b, -1.0, q, res, st));
-      ILM_TRY(gram(res, nrhs, res, nrhs, (int)n, G.as<double>(), g, st));
+      ILM_TRY(st_axpby(n * nrhs, ILM_F64, 1.0, b, -1.0, q, q, st));  // q = b - B y (candidate residual)
+      ILM_TRY(gram(q, nrhs, q, nrhs, (int)n, G.as<double>(), g, st));
       bool all = true;
+      double worst = 0.0;
       for (int j = 0; j < nrhs; ++j) {
-        rel[j] = bn[j] > 0.0 ? sqrt(std::max(g[j + (size_t)j * nrhs], 0.0)) / bn[j] : 0.0;
-        all = all && rel[j] <= tol;
+        relk[j] = bn[j] > 0.0 ? sqrt(std::max(g[j + (size_t)j * nrhs], 0.0)) / bn[j] : 0.0;
+        all = all && relk[j] <= tol;
+        worst = std::max(worst, relk[j]);
       }
+      if (!(worst < worst_prev)) {
+        // the correction did not reduce the FP64 residual (the corrections'
+        // operator cannot resolve the slowest modes): keep the previous y
+        ILM_TRY(st_axpby(n * nrhs, ILM_F64, 1.0, y, -1.0, d, y, st));
+        break;
+      }
+      worst_prev = worst;
+      rel = relk;
+      ILM_CHECK_CUDA(cudaMemcpyAsync(res, q, nb, cudaMemcpyDeviceToDevice, st));
       if (all) break;
     }
     return ILM_OK;

@@ -346,8 +346,11 @@ ILM_API int ilm_solve_stokes_multi(ilm_cache_t c, int nrhs, const void* vplus, c
  * points move); the corrections S d = r are block CG with the cache's own
  * operator (FP32 for an FP32 cache; S preconditioned as in
  * ilm_solve_stokes_multi), each to 1e-4 of its residual or until it stops
- * improving, for at most max_refine steps per Schur system.  info: FP64
- * relative residuals; iterations = block iterations of all corrections.    */
+ * improving, for at most max_refine steps per Schur system, and until a step
+ * no longer reduces the FP64 residual (refinement converges while the
+ * corrections' operator resolves every mode of S: cond(S) x its rounding
+ * < 1).  info: FP64 relative residuals; iterations = block iterations of all
+ * corrections.                                                             */
 ILM_API int ilm_solve_stokes_multi_refined(ilm_cache_t c, int nrhs, const double* vplus, const double* vminus,
                                            double* v_out, double* s_out, double* sigma_out, double tol, int maxiter,
                                            int max_refine, ilm_solve_info_t* info, ilm_stream_t stream);
