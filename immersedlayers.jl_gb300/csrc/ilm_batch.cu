@@ -336,6 +336,7 @@ struct ilm_batch_s {
   std::vector<double> coarse_Einv;
   // deflation of the Dirichlet net-charge mode (set up before the first solve)
   bool defl_ready = false;
+  double defl_tol = 0.0;  // tolerance the deflation vectors were solved to
   std::vector<double> defl_gamma, defl_uz;
   DevBuf defl_z;
   // host copies of the points (features of the learned preconditioner)
@@ -416,7 +417,7 @@ int up_typed(DevBuf& b, const std::vector<double>& v, int dtype) {
     }                          \
   } while (0)
 
-int ensure_deflation(ilm_batch_s* b);
+int ensure_deflation(ilm_batch_s* b, double tol);
 
 struct CoarseTask {
   const float* Shi;  // n x n row-major float-float (leading dimension schur_ld(n))
@@ -522,7 +523,7 @@ int ensure_block_inverses(ilm_batch_s* b) {
 int ensure_cg_params(ilm_batch_s* b, double tol, int maxiter) {
   if (tol == b->cg_tol && maxiter == b->cg_maxiter && !b->params_dirty) return ILM_OK;
   ILM_TRY(ensure_block_inverses(b));
-  ILM_TRY(ensure_deflation(b));
+  ILM_TRY(ensure_deflation(b, tol));
   b->params_dirty = false;
   std::vector<unsigned char> cg((size_t)b->nprob * cgff_params_size());
   const int P = 2 * b->band_k + 1;
@@ -600,14 +601,21 @@ int prepare_lazy_setup(ilm_batch_s* b) {
 }
 
 // Deflation of the Dirichlet net-charge mode: gamma per problem from S 1, and
-// z = S'^-1 1 with S' = S + gamma 1 1^T W.  Runs on the set-up stream (the
-// host waits for that stream only), so it overlaps the first solve's stage A.
-int ensure_deflation(ilm_batch_s* b) {
-  if (b->defl_ready) return ILM_OK;
+// z = S'^-1 1 with S' = S + gamma 1 1^T W, to 1e-2 of the requested solve
+// tolerance (between 1e-12 and 1e-10: z enters x = y + gamma t z
+// linearly); a later, tighter request re-solves z warm-started from the
+// current one.  Runs on the set-up stream (the host waits for that stream
+// only), so it overlaps the first solve's stage A.
+int ensure_deflation(ilm_batch_s* b, double tol) {
+  const double ztol = std::min(1e-10, std::max(1e-12, 1e-2 * tol));
+  if (b->defl_ready && b->defl_tol <= ztol) return ILM_OK;
+  const bool refresh = b->defl_ready;
   const auto t0 = std::chrono::steady_clock::now();
   const int Ptot = b->Ptot, np = b->nprob;
   ILM_TRY(prepare_lazy_setup(b));
   cudaStream_t ss = b->s_setup;
+  std::vector<double> rhs(Ptot, 0.0);
+  if (!refresh) {
   b->defl_gamma.assign(np, 0.0);
   b->defl_uz.assign(np, 0.0);
   ILM_CHECK_CUDA(cudaMemsetAsync(b->defl_z.p, 0, (size_t)std::max(Ptot, 1) * sizeof(double), ss));
@@ -616,12 +624,10 @@ int ensure_deflation(ilm_batch_s* b) {
   if (!any) {
     ILM_CHECK_CUDA(cudaStreamSynchronize(ss));
     b->defl_ready = true;
+    b->defl_tol = 0.0;
     return ILM_OK;
   }
-  std::vector<double> ones(Ptot, 1.0), rhs(Ptot, 0.0), y(Ptot);
-  for (int p = 0; p < np; ++p)
-    if (b->probs[p].kind == 0)
-      for (size_t k = b->poff[p]; k < b->poff[p + 1]; ++k) rhs[k] = 1.0;
+  std::vector<double> ones(Ptot, 1.0), y(Ptot);
   ILM_CHECK_CUDA(cudaMemcpyAsync(b->lz_ones.p, ones.data(), (size_t)Ptot * sizeof(double), cudaMemcpyHostToDevice, ss));
   ILM_CHECK_CUDA(cudaMemcpyAsync(b->lz_soff.p, b->soff.data(), b->soff.size() * sizeof(size_t),
                                  cudaMemcpyHostToDevice, ss));
@@ -642,17 +648,18 @@ int ensure_deflation(ilm_batch_s* b) {
     const double rho = sy / su;
     if (rho < 0.0) b->defl_gamma[p] = 2.0 * fabs(rho) / su;
   }
+  }
   // z = S'^-1 1 for the problems with a deflation shift (the others never
-  // read z: their right-hand side is 0 and their CG returns at once), to
-  // 1e-12: z enters x = y + gamma t z linearly, and solves may ask for 1e-10
+  // read z: their right-hand side is 0 and their CG returns at once)
   bool need = false;
   for (int p = 0; p < np; ++p) {
-    if (b->probs[p].kind == 0 && b->defl_gamma[p] == 0.0)
-      for (size_t k = b->poff[p]; k < b->poff[p + 1]; ++k) rhs[k] = 0.0;
+    if (b->defl_gamma[p] != 0.0)
+      for (size_t k = b->poff[p]; k < b->poff[p + 1]; ++k) rhs[k] = 1.0;
     need |= b->defl_gamma[p] != 0.0;
   }
   if (!need) {
     b->defl_ready = true;
+    b->defl_tol = 0.0;
     return ILM_OK;
   }
   ILM_CHECK_CUDA(cudaMemcpyAsync(b->lz_rhs.p, rhs.data(), (size_t)Ptot * sizeof(double), cudaMemcpyHostToDevice, ss));
@@ -666,12 +673,13 @@ int ensure_deflation(ilm_batch_s* b) {
     const bool pre = !band && b->bj_block > 0 && !b->bj_have.empty() && b->bj_have[p];
     cgff_params_fill(dst, b->Shi.as<float>() + b->soff[p], b->Slo.as<float>() + b->soff[p],
                      b->lz_rhs.as<double>() + o, b->defl_z.as<double>() + o, b->ds64.as<double>() + o,
-                     b->probs[p].npts, 20000, 1e-12, b->lz_its.as<int>() + p, b->lz_rr.as<double>() + p,
+                     b->probs[p].npts, 20000, ztol, b->lz_its.as<int>() + p, b->lz_rr.as<double>() + p,
                      pre ? b->bj_blk.as<int>() + o : nullptr, pre ? b->bj_start.as<int>() + b->bj_first[p] : nullptr,
                      pre ? b->bj_size.as<int>() + b->bj_first[p] : nullptr,
                      pre ? b->bj_off.as<int>() + b->bj_first[p] : nullptr, pre ? b->bj_inv.as<float>() : nullptr,
                      pre ? b->bj_inv_lo.as<float>() : nullptr);
     cgff_params_set_deflation(dst, b->defl_gamma[p], nullptr, 0.0);
+    if (refresh) cgff_params_set_x0(dst, b->defl_z.as<double>() + o);
     if (band)
       cgff_params_set_band(dst, b->band.as<float>() + o * (2 * b->band_k + 1), b->band_k,
                            b->lseg_start.as<int>() + o, b->lseg_len.as<int>() + o);
@@ -689,6 +697,8 @@ int ensure_deflation(ilm_batch_s* b) {
     b->defl_uz[p] = uz;
   }
   b->defl_ready = true;
+  b->defl_tol = ztol;
+  b->params_dirty = true;  // uz changed
   b->setup_ms.emplace_back("deflation vectors (Dirichlet problems with a net-charge shift)",
                            std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
   return ILM_OK;

@@ -1441,6 +1441,8 @@ void cgff_params_set_timing(void* dst, unsigned long long* tspan) {
   static_cast<CGFFParams*>(dst)->tspan = tspan;
 }
 
+void cgff_params_set_x0(void* dst, const double* x0) { static_cast<CGFFParams*>(dst)->x0 = x0; }
+
 void cgff_params_set_coarse(void* dst, int nb, const int* starts, const double* Einv) {
   CGFFParams* p = static_cast<CGFFParams*>(dst);
   p->cnb = nb;

@@ -655,6 +655,8 @@ void cgff_params_set_band(void* dst, const float* band, int band_k, const int* s
 // starts[0..nb] local body boundaries, Einv nb x CG_COARSE_MAX row-major
 constexpr int CG_COARSE_MAX = 4;
 void cgff_params_set_coarse(void* dst, int nb, const int* starts, const double* Einv);
+// warm start from x0 (may be the output array itself: each CTA reads its rows first)
+void cgff_params_set_x0(void* dst, const double* x0);
 void cgff_params_fill_csr(void* dst, const float* vhi, const float* vlo, const int* rowptr, const int* colidx,
                           const double* b, double* x, const double* x0, const double* w, int n, int maxiter,
                           double tol, int* iters, double* relres);
