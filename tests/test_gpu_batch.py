@@ -212,3 +212,25 @@ def test_batch_rhs_operator_matches_default_path(cuda, dtype):
     for i in range(len(specs)):
         a, b = bs.field(f5, i).double(), bs.field(f4, i).double()
         assert ((a - b).abs().max() / b.abs().max()).item() < tol, (i, specs[i].kind)
+
+
+def test_batch_deflation_follows_the_tolerance(cuda):
+    """The Dirichlet deflation vectors are solved to 1e-2 of the requested
+    tolerance; a later, tighter solve re-solves them (warm-started) and
+    reaches its tolerance on every problem."""
+    import torch
+    from immersedlayers import workloads as W
+    from immersedlayers.batch import BatchSolver
+    specs = W.batch_specs(8, sizes=(96, 128, 192))
+    bs = BatchSolver(specs, dtype=torch.float64)
+    bs.set_precond("bjacobi", 32)
+    fp, fm = bs.surface_data()
+    f1, s1 = bs.solve(fp, fm, tol=1e-8, maxiter=20000)
+    it1, rr1 = bs.info()
+    assert (rr1 <= 1e-8).all(), rr1
+    f2, s2 = bs.solve(fp, fm, tol=1e-11, maxiter=20000)
+    it2, rr2 = bs.info()
+    assert (rr2 <= 1e-11).all(), rr2
+    assert torch.allclose(s1, s2, rtol=0, atol=1e-6 * float(s2.abs().max()))
+    names = [n for n, _ in bs.setup_times()]
+    assert names.count("deflation vectors (Dirichlet problems with a net-charge shift)") == 2
