@@ -21,7 +21,6 @@
 //    array's address differs per device;
 //  * the first call on a device looks up the device address of the scratch
 //    array (cudaGetSymbolAddress, once per device, with that device current);
-//    make that first call before any stream capture begins;
 //  * the call waits for `stream` (cudaStreamSynchronize) and copies the
 //    result to host memory before it returns;
 //  * every call on a device shares the one array: calls whose kernels may

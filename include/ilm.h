@@ -254,8 +254,8 @@ ILM_API int ilm_dot_surface(ilm_cache_t c, int ncomp, const void* a, const void*
  * so grids are limited to ny <= 16384 dual nodes (taller ones fail with
  * ILM_ERR_SIZE_LIMIT; nx is not limited).  `stream` must belong to the
  * current device (else ILM_ERR_INVALID_ARG).  The first call on a device
- * looks up that array's address; make it before any stream capture.  Calls
- * share the array: calls that may overlap on the GPU race and must be
+ * looks up that array's address (cudaGetSymbolAddress).  Calls share the
+ * array: calls that may overlap on the GPU race and must be
  * serialised by the caller.  Waits for `stream` and copies the result to
  * host memory before it returns.                                             */
 ILM_API int ilm_dot_grid_noalloc(int nx, int ny, double h, int scaling, int kind, int dtype, const void* a,
