@@ -588,10 +588,7 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(CGR_THREADS
 // ---------------------------------------------------------------------------
 
 // rows [r0, r1) of S v as float-float pairs yh/yl[i - r0] (dense rows with
-// 16-byte alignment, or CSR).  DEEP (kernels with registers to spare): 16
-// 16-byte loads in flight per lane instead of 8, for the matrix stream of
-// the large problems.
-template <bool DEEP = false>
+// 16-byte alignment, or CSR)
 __device__ void matvec_rows_ff(const CGFFParams& pr, int n, int r0, int r1, const float* __restrict__ vhi,
                                const float* __restrict__ vlo, float* __restrict__ yh, float* __restrict__ yl) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
@@ -628,22 +625,6 @@ __device__ void matvec_rows_ff(const CGFFParams& pr, int n, int r0, int r1, cons
     const float4* l1 = reinterpret_cast<const float4*>(pr.Slo + (size_t)(two ? i + 1 : i) * ld);
     FF a{0.f, 0.f}, b{0.f, 0.f};
     int j = lane;
-    if (DEEP)
-      for (; j + 96 < nq; j += 128) {  // sixteen 16-byte loads in flight per lane
-        float4 x[4], y[4], u[4], w[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          x[q] = __ldg(h0 + j + 32 * q);
-          y[q] = __ldg(l0 + j + 32 * q);
-          u[q] = __ldg(h1 + j + 32 * q);
-          w[q] = __ldg(l1 + j + 32 * q);
-        }
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          ff_fma4(a, x[q], y[q], vh4[j + 32 * q], vl4[j + 32 * q]);
-          ff_fma4(b, u[q], w[q], vh4[j + 32 * q], vl4[j + 32 * q]);
-        }
-      }
     for (; j + 32 < nq; j += 64) {  // eight 16-byte loads in flight per lane
       const float4 x0 = __ldg(h0 + j), y0 = __ldg(l0 + j), x1 = __ldg(h1 + j), y1 = __ldg(l1 + j);
       const float4 x2 = __ldg(h0 + j + 32), y2 = __ldg(l0 + j + 32), x3 = __ldg(h1 + j + 32),
@@ -1024,7 +1005,7 @@ __global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(NT, MINB)
       csum_t0<1, CS>(cl, v, nr, red, pub, slot);
       if (threadIdx.x == 0) bc[0] = gamma * v[0];
       gather_parts(cl, bh, bl, n, rows, rank);
-      matvec_rows_ff<(MINB <= 2)>(pr, n, r0, r1, bh, bl, yh, yl);
+      matvec_rows_ff(pr, n, r0, r1, bh, bl, yh, yl);
       __syncthreads();
       const double c0 = bc[0];
       for (int i = threadIdx.x; i < nr; i += blockDim.x) rs[i] = bs[i] - ((double)yh[i] + (double)yl[i]) - c0;
@@ -1097,7 +1078,7 @@ __global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(NT, MINB)
     for (int i = threadIdx.x; i < nr; i += blockDim.x) pr.x[r0 + i] = xs[i];
     while (!done && it < pr.maxiter) {
       // q = S' p on the owned rows (p whole in this CTA)
-      matvec_rows_ff<(MINB <= 2)>(pr, n, r0, r1, ph, pl, yh, yl);
+      matvec_rows_ff(pr, n, r0, r1, ph, pl, yh, yl);
       __syncthreads();
       double alpha, pq;
       {
@@ -1156,7 +1137,7 @@ __global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(NT, MINB)
           csum_t0<1, CS>(cl, v, nr, red, pub, slot);
           if (threadIdx.x == 0) bc[8] = gamma * v[0];
           gather_parts(cl, bh, bl, n, rows, rank);
-          matvec_rows_ff<(MINB <= 2)>(pr, n, r0, r1, bh, bl, yh, yl);
+          matvec_rows_ff(pr, n, r0, r1, bh, bl, yh, yl);
           __syncthreads();
         }
         const double cx = bc[8];
@@ -1266,7 +1247,7 @@ __global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(NT, MINB)
       publish_slice(xs, r0, nr, bh, bl);
       csum_t0<1, CS>(cl, u, nr, red, pub, slot);  // barrier that publishes x
       gather_parts(cl, bh, bl, n, rows, rank);
-      matvec_rows_ff<(MINB <= 2)>(pr, n, r0, r1, bh, bl, yh, yl);
+      matvec_rows_ff(pr, n, r0, r1, bh, bl, yh, yl);
       __syncthreads();
       double t[1] = {0.0};
       for (int i = threadIdx.x; i < nr; i += blockDim.x) {
