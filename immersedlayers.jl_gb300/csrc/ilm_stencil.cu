@@ -7,8 +7,6 @@
 // All kernels are one thread per output cell, x fastest (coalesced), and write
 // every output cell (boundary / ghost cells receive 0), so callers never need a
 // separate fill.
-#include <cmath>
-
 #include "ilm_internal.cuh"
 
 namespace ilm {
@@ -320,57 +318,14 @@ inline int nblocks(size_t n) {
     }                                             \
   } while (0)
 
-// Rows per thread of the row-blocked stencils: the largest of 4, 2, 1 whose
-// grid fills its last wave of resident 256-thread blocks (8 per SM) to at
-// least 90%, else the best filled.  A launch of a few waves is bound by its
-// partial last wave: on 2048^2, 4 rows per thread give 3.4 waves (the last
-// 37% full), 2 rows 6.7 waves.
-int stencil_rows_per_thread(int gx, int rows) {
-  static int slots = 0;
-  if (!slots) {
-    int dev = 0, nsm = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess ||
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0)
-      return 4;
-    slots = nsm * 8;
-  }
-  int best = 4;
-  double beff = -1.0;
-  for (int ry : {4, 2, 1}) {
-    const double blocks = (double)gx * ((rows + BY * ry - 1) / (BY * ry));
-    const double waves = blocks / slots;
-    const double eff = waves / std::ceil(waves);
-    if (eff >= 0.9) return ry;
-    if (eff > beff) {
-      beff = eff;
-      best = ry;
-    }
-  }
-  return best;
-}
-
-template <typename T, int RY>
-void launch_div_edges(int NX, int NY, const T* u, const T* v, T* w, T sc, cudaStream_t st) {
-  const dim3 grid((NX - 1 + BX - 1) / BX, (NY - 1 + BY * RY - 1) / (BY * RY));
-  k_div_edges_r<T, RY><<<grid, dim3(BX, BY), 0, st>>>(NX, NY, u, v, w, sc);
-}
-
-template <typename T, int RY>
-void launch_grad_nodes(int NX, int NY, const T* w, T* u, T* v, T sc, cudaStream_t st) {
-  const dim3 grid((NX + BX - 1) / BX, (NY + BY * RY - 1) / (BY * RY));
-  k_grad_nodes_r<T, RY><<<grid, dim3(BX, BY), 0, st>>>(NX, NY, w, u, v, sc);
-}
-
 int st_div_edges(const ilm_grid_s* g, int dtype, const void* q, void* w, double scale, cudaStream_t st) {
   const int NX = g->nx, NY = g->ny;
-  const int ry = stencil_rows_per_thread((NX - 1 + BX - 1) / BX, NY - 1);
   DISPATCH(dtype, {
     const T* u = static_cast<const T*>(q);
     const T* v = u + (size_t)NX * (NY - 1);
-    T* o = static_cast<T*>(w);
-    if (ry == 4) launch_div_edges<T, 4>(NX, NY, u, v, o, (T)scale, st);
-    else if (ry == 2) launch_div_edges<T, 2>(NX, NY, u, v, o, (T)scale, st);
-    else launch_div_edges<T, 1>(NX, NY, u, v, o, (T)scale, st);
+    constexpr int RY = 4;
+    const dim3 grid((NX - 1 + BX - 1) / BX, (NY - 1 + BY * RY - 1) / (BY * RY));
+    k_div_edges_r<T, RY><<<grid, dim3(BX, BY), 0, st>>>(NX, NY, u, v, static_cast<T*>(w), (T)scale);
   });
   ILM_CHECK_LAUNCH();
   return ILM_OK;
@@ -378,14 +333,12 @@ int st_div_edges(const ilm_grid_s* g, int dtype, const void* q, void* w, double 
 
 int st_grad_nodes(const ilm_grid_s* g, int dtype, const void* w, void* q, double scale, cudaStream_t st) {
   const int NX = g->nx, NY = g->ny;
-  const int ry = stencil_rows_per_thread((NX + BX - 1) / BX, NY);
   DISPATCH(dtype, {
     T* u = static_cast<T*>(q);
     T* v = u + (size_t)NX * (NY - 1);
-    const T* in = static_cast<const T*>(w);
-    if (ry == 4) launch_grad_nodes<T, 4>(NX, NY, in, u, v, (T)scale, st);
-    else if (ry == 2) launch_grad_nodes<T, 2>(NX, NY, in, u, v, (T)scale, st);
-    else launch_grad_nodes<T, 1>(NX, NY, in, u, v, (T)scale, st);
+    constexpr int RY = 4;
+    const dim3 grid((NX + BX - 1) / BX, (NY + BY * RY - 1) / (BY * RY));
+    k_grad_nodes_r<T, RY><<<grid, dim3(BX, BY), 0, st>>>(NX, NY, static_cast<const T*>(w), u, v, (T)scale);
   });
   ILM_CHECK_LAUNCH();
   return ILM_OK;
