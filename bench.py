@@ -553,8 +553,9 @@ def _precision_leg(stream):
     (the committed fixtures of one Dirichlet and one Neumann problem of the
     batched configuration per grid size): fields f (relative to max |f|)
     and surface strengths s (relative to max |s|), max over the problems,
-    for the FP32 batched solve (default path and with the right-hand-side
-    operator) and the FP64-refined solve of the same FP32 batch."""
+    for the FP32 batched solve with the default solver (default path and
+    with the right-hand-side operator) and the FP64-refined solve of the
+    same FP32 batch."""
     import numpy as np
     import torch
     from immersedlayers import workloads as W
@@ -583,6 +584,8 @@ def _precision_leg(stream):
                        "128..512); reference: the oracle's FP64 dense-LU solve" % probs}
     for name, rhsop in (("fp32_default", False), ("fp32_rhs_operator", True)):
         bs = BatchSolver(specs, dtype=torch.float32)
+        if _prepare_learned(bs, 64, True):   # the default solver, as the e2e and value legs
+            bs.set_precond("learned", 64)
         if rhsop:
             bs.set_rhs_operator(True)
         fp, fm = bs.surface_data()
