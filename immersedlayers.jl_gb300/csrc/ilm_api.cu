@@ -248,6 +248,38 @@ int ilm_grid_numel(ilm_grid_t g, int kind, size_t* numel) {
   return ILM_OK;
 }
 
+int ilm_alloc(size_t nbytes, void** out) {
+  ILM_REQUIRE(out, "alloc: null argument");
+  *out = nullptr;
+  if (nbytes == 0) return ILM_OK;
+  const cudaError_t e = cudaMalloc(out, nbytes);
+  if (e != cudaSuccess) {
+    *out = nullptr;
+    set_error("alloc: cudaMalloc(%zu) failed: %s", nbytes, cudaGetErrorString(e));
+    return ILM_ERR_NO_MEMORY;
+  }
+  return ILM_OK;
+}
+
+int ilm_free(void* p) {
+  if (p) ILM_CHECK_CUDA(cudaFree(p));
+  return ILM_OK;
+}
+
+int ilm_copy_h2d(void* dst_dev, const void* src_host, size_t nbytes, ilm_stream_t stream) {
+  ILM_REQUIRE(nbytes == 0 || (dst_dev && src_host), "copy_h2d: null argument");
+  if (nbytes) ILM_CHECK_CUDA(cudaMemcpyAsync(dst_dev, src_host, nbytes, cudaMemcpyHostToDevice, as_stream(stream)));
+  return ILM_OK;
+}
+
+int ilm_copy_d2h(void* dst_host, const void* src_dev, size_t nbytes, ilm_stream_t stream) {
+  ILM_REQUIRE(nbytes == 0 || (dst_host && src_dev), "copy_d2h: null argument");
+  if (!nbytes) return ILM_OK;
+  ILM_CHECK_CUDA(cudaMemcpyAsync(dst_host, src_dev, nbytes, cudaMemcpyDeviceToHost, as_stream(stream)));
+  ILM_CHECK_CUDA(cudaStreamSynchronize(as_stream(stream)));
+  return ILM_OK;
+}
+
 int ilm_cache_create(ilm_grid_t g, int kind, int npts, const double* x, const double* y, const double* nrmx,
                      const double* nrmy, const double* ds, int ddf, int scaling, int dtype, ilm_cache_t* out) {
   ILM_REQUIRE(g && out, "null argument");

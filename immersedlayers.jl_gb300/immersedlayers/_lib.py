@@ -56,6 +56,10 @@ SIGNATURES = {
     "ilm_grid_create": [_I, _I, _D, _I, _I, C.POINTER(_VP)],
     "ilm_grid_destroy": [_VP],
     "ilm_grid_numel": [_VP, _I, C.POINTER(C.c_size_t)],
+    "ilm_alloc": [C.c_size_t, C.POINTER(_VP)],
+    "ilm_free": [_VP],
+    "ilm_copy_h2d": [_VP, _VP, C.c_size_t, _VP],
+    "ilm_copy_d2h": [_VP, _VP, C.c_size_t, _VP],
     "ilm_cache_create": [_VP, _I, _I, _DP, _DP, _DP, _DP, _DP, _I, _I, _I, C.POINTER(_VP)],
     "ilm_cache_destroy": [_VP],
     "ilm_cache_update_points": [_VP, _VP, _VP, _VP, _VP, _VP, _VP],

@@ -112,6 +112,16 @@ ILM_API int ilm_grid_destroy(ilm_grid_t g);
 /* Number of elements of one grid data kind (all components). */
 ILM_API int ilm_grid_numel(ilm_grid_t g, int kind, size_t* numel);
 
+/* ---- device buffers -------------------------------------------------------
+ * For callers without their own device allocator (the Julia shim passes
+ * CuArray pointers instead): nbytes of device memory on the current device,
+ * freed by ilm_free; host <-> device copies in `stream` order (host memory
+ * may be pageable; ilm_copy_d2h returns after the copy has completed).     */
+ILM_API int ilm_alloc(size_t nbytes, void** out);
+ILM_API int ilm_free(void* p);
+ILM_API int ilm_copy_h2d(void* dst_dev, const void* src_host, size_t nbytes, ilm_stream_t stream);
+ILM_API int ilm_copy_d2h(void* dst_host, const void* src_dev, size_t nbytes, ilm_stream_t stream);
+
 /* ---- cache: SurfaceScalarCache/SurfaceVectorCache (src/cache.jl:209-261) */
 /* x, y: point coordinates; nrmx, nrmy: outward normals; ds: panel areas
  * (src/tools.jl:16-38).  All host arrays of length npts.                    */

@@ -100,6 +100,12 @@ ilm_grid_create(nx, ny, h, i0x, i0y, out) =
 ilm_grid_destroy(g) = ccall((:ilm_grid_destroy, libilm), Cint, (Ptr{Cvoid},), g)
 ilm_grid_numel(g, kind, numel) =
     ccall((:ilm_grid_numel, libilm), Cint, (Ptr{Cvoid}, Cint, Ref{Csize_t}), g, kind, numel)
+ilm_alloc(nbytes, out) = ccall((:ilm_alloc, libilm), Cint, (Csize_t, Ref{Ptr{Cvoid}}), nbytes, out)
+ilm_free(p) = ccall((:ilm_free, libilm), Cint, (Ptr{Cvoid},), p)
+ilm_copy_h2d(dst, src, nbytes, stream) =
+    ccall((:ilm_copy_h2d, libilm), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Csize_t, Ptr{Cvoid}), dst, src, nbytes, stream)
+ilm_copy_d2h(dst, src, nbytes, stream) =
+    ccall((:ilm_copy_d2h, libilm), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Csize_t, Ptr{Cvoid}), dst, src, nbytes, stream)
 
 ilm_cache_create(g, kind, npts, x, y, nrmx, nrmy, ds, ddf, scaling, dtype, out) =
     ccall((:ilm_cache_create, libilm), Cint,

@@ -96,6 +96,8 @@ def jl_class(t):
 def compatible(c, j):
     if j == "void*|handle":
         return c in ("void*", "handle")
+    if j == "handle*":  # Ref{Ptr{Cvoid}}: an out-pointer to a handle or to a device pointer
+        return c in ("handle*", "void**")
     return c == j
 
 
