@@ -123,8 +123,7 @@ __global__ void __launch_bounds__(256) k_gemm_rows(int n, int k, int t, const do
   }
 }
 
-// T = sym(Sp diag(1/ds)) + shift (N x N); sums[blockIdx] = partial sums of
-// the unshifted entries for the shift
+// T = sym(Sp diag(1/ds)) + shift (N x N)
 __global__ void k_pc_form(int N, const double* __restrict__ Sp, const double* __restrict__ ds, double shift,
                           double* __restrict__ T) {
   const size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
@@ -133,6 +132,7 @@ __global__ void k_pc_form(int N, const double* __restrict__ Sp, const double* __
   T[idx] = 0.5 * (Sp[idx] / ds[j] + Sp[j + (size_t)i * N] / ds[i]) + shift;
 }
 
+// out[j] = sum_i Sp[i][j] / ds[j] (column sums of Sp diag(1/ds), for the shift)
 __global__ void __launch_bounds__(256) k_pc_sum(int N, const double* __restrict__ Sp, const double* __restrict__ ds,
                                                 double* __restrict__ out) {
   __shared__ double red[8];
