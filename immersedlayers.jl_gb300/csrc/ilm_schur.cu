@@ -47,9 +47,9 @@ struct Functional {
 // Functional buffers, so it is no larger.
 struct FunctionalFF {
   float coef[2][2];
-  int xb[2], yb[2];
+  float w[2];                  // the point's regularization weight ds (hi, lo)
+  short xb[2], yb[2], nterm, pad_;  // grid base indices (|index| < 32768)
   float xw[2][FW][2], yw[2][FW][2];
-  int nterm;
 };
 static_assert(sizeof(FunctionalFF) <= sizeof(Functional), "FunctionalFF overlays Functional buffers");
 
@@ -390,7 +390,7 @@ __global__ void k_functionals_batched(int Ptot, const int* __restrict__ pt2prob,
                                       const double* __restrict__ wxP, const double* __restrict__ wxD,
                                       const double* __restrict__ wyP, const double* __restrict__ wyD,
                                       const double* __restrict__ nx, const double* __restrict__ ny,
-                                      Functional* __restrict__ out, int force_kind) {
+                                      const double* __restrict__ w, Functional* __restrict__ out, int force_kind) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= Ptot) return;
   SchurProbDev P = pr[pt2prob[g]];
@@ -451,10 +451,17 @@ __global__ void k_functionals_batched(int Ptot, const int* __restrict__ pt2prob,
     }
   }
   FunctionalFF Q;
-  Q.nterm = F.nterm;
+  Q.nterm = (short)F.nterm;
+  Q.pad_ = 0;
+  {
+    const double wk = w ? w[g] : 0.0;
+    const float wh = (float)wk;
+    Q.w[0] = wh;
+    Q.w[1] = (float)(wk - (double)wh);
+  }
   for (int p = 0; p < 2; ++p) {
-    Q.xb[p] = F.xb[p];
-    Q.yb[p] = F.yb[p];
+    Q.xb[p] = (short)F.xb[p];
+    Q.yb[p] = (short)F.yb[p];
     const float ch = (float)F.coef[p];
     Q.coef[p][0] = ch;
     Q.coef[p][1] = (float)(F.coef[p] - (double)ch);
@@ -469,10 +476,6 @@ __global__ void k_functionals_batched(int Ptot, const int* __restrict__ pt2prob,
   reinterpret_cast<FunctionalFF*>(out)[g] = Q;
 }
 
-__device__ __forceinline__ FF split_ff(double v) {
-  const float h = (float)v;
-  return FF{h, (float)(v - (double)h)};
-}
 
 // Batched Schur entries in float-float on the FP32 pipes (~2^-44 relative
 // per operation; GB300 issues FP64 at a small fraction of its FP32 rate):
@@ -558,7 +561,9 @@ __global__ void __launch_bounds__(256) k_schur_pairs_batched(int nprob, const Sc
   // of the upper triangle (ti <= tj) in row-major order, writing S_kl = -w_l
   // T_kl and, off the diagonal tiles, S_lk = -w_k T_kl
   const int t = u - P.tile0;
-  int ti = (int)((2.0 * nt + 1.0 - sqrt((2.0 * nt + 1.0) * (2.0 * nt + 1.0) - 8.0 * t)) * 0.5);
+  // tile row of triangle index t (FP32 estimate, corrected exactly below)
+  const float tn = 2.0f * nt + 1.0f;
+  int ti = (int)((tn - sqrtf(fmaxf(tn * tn - 8.0f * t, 0.0f))) * 0.5f);
   auto row0 = [nt](int i) { return i * nt - i * (i - 1) / 2; };  // first triangle tile of tile row i
   while (ti > 0 && row0(ti) > t) --ti;
   while (ti + 1 < nt && row0(ti + 1) <= t) ++ti;
@@ -566,14 +571,16 @@ __global__ void __launch_bounds__(256) k_schur_pairs_batched(int nprob, const Sc
   const int k = ti * 16 + threadIdx.y;
   const int l = tj * 16 + threadIdx.x;
   if (k >= N || l >= N) return;
-  const FF total = pair_sum(F[P.poff + k], F[P.poff + l], G, ld, M);
+  const FunctionalFF& Fk = F[P.poff + k];
+  const FunctionalFF& Fl = F[P.poff + l];
+  const FF total = pair_sum(Fk, Fl, G, ld, M);
   // row-major float-float pair: S[k][l] = hi + lo
-  const FF wl = split_ff(-w[P.poff + l]);
+  const FF wl{-Fl.w[0], -Fl.w[1]};
   const FF v = ff_mul(wl, total);
   Shi[P.soff + (size_t)k * schur_ld(N) + l] = v.hi;
   Slo[P.soff + (size_t)k * schur_ld(N) + l] = v.lo;
   if (ti != tj) {
-    const FF wk = split_ff(-w[P.poff + k]);
+    const FF wk{-Fk.w[0], -Fk.w[1]};
     const FF vt = ff_mul(wk, total);
     Shi[P.soff + (size_t)l * schur_ld(N) + k] = vt.hi;
     Slo[P.soff + (size_t)l * schur_ld(N) + k] = vt.lo;
@@ -589,7 +596,7 @@ int schur_build_batched(int nprob, const SchurProbDev* probs_dev, int total_tile
   ILM_TRY(lgf_table_ff_device(max_grid + 16, &G, &ld, st));
   k_functionals_batched<<<(Ptot + 127) / 128, 128, 0, st>>>(Ptot, pt2prob, probs_dev, W.bx[0], W.bx[1], W.by[0],
                                                             W.by[1], W.wx64[0], W.wx64[1], W.wy64[0], W.wy64[1],
-                                                            W.nx64, W.ny64, F, -1);
+                                                            W.nx64, W.ny64, w, F, -1);
   ILM_CHECK_LAUNCH();
   k_schur_pairs_batched<<<total_tiles, dim3(16, 16), 0, st>>>(nprob, probs_dev, reinterpret_cast<const FunctionalFF*>(F),
                                                               w, G, ld, ld - 1, Shi, Slo);
@@ -627,8 +634,9 @@ __global__ void __launch_bounds__(256) k_rhsop_pairs_batched(int nprob, const Sc
   const int l = tj * 16 + threadIdx.x;
   if (k >= N || l >= N) return;
   const bool dir = P.kind == ILM_SCHUR_RTLINVR;
-  const FF total = pair_sum(dir ? FU[P.poff + k] : FD[P.poff + k], dir ? FD[P.poff + l] : FU[P.poff + l], G, ld, M);
-  const FF wl = split_ff((dir ? 1.0 : -1.0) * w[P.poff + l]);
+  const FunctionalFF& Fl = dir ? FD[P.poff + l] : FU[P.poff + l];
+  const FF total = pair_sum(dir ? FU[P.poff + k] : FD[P.poff + k], Fl, G, ld, M);
+  const FF wl = dir ? FF{Fl.w[0], Fl.w[1]} : FF{-Fl.w[0], -Fl.w[1]};
   const FF v = ff_mul(wl, total);
   Mhi[P.soff + (size_t)k * schur_ld(N) + l] = v.hi;
   Mlo[P.soff + (size_t)k * schur_ld(N) + l] = v.lo;
@@ -643,11 +651,11 @@ int rhsop_build_batched(int nprob, const SchurProbDev* probs_full_dev, int total
   ILM_TRY(lgf_table_ff_device(max_grid + 16, &G, &ld, st));
   k_functionals_batched<<<(Ptot + 127) / 128, 128, 0, st>>>(Ptot, pt2prob, probs_full_dev, W.bx[0], W.bx[1], W.by[0],
                                                             W.by[1], W.wx64[0], W.wx64[1], W.wy64[0], W.wy64[1],
-                                                            W.nx64, W.ny64, FU, ILM_SCHUR_RTLINVR);
+                                                            W.nx64, W.ny64, w, FU, ILM_SCHUR_RTLINVR);
   ILM_CHECK_LAUNCH();
   k_functionals_batched<<<(Ptot + 127) / 128, 128, 0, st>>>(Ptot, pt2prob, probs_full_dev, W.bx[0], W.bx[1], W.by[0],
                                                             W.by[1], W.wx64[0], W.wx64[1], W.wy64[0], W.wy64[1],
-                                                            W.nx64, W.ny64, FD, ILM_SCHUR_GLINVD);
+                                                            W.nx64, W.ny64, w, FD, ILM_SCHUR_GLINVD);
   ILM_CHECK_LAUNCH();
   k_rhsop_pairs_batched<<<total_tiles, dim3(16, 16), 0, st>>>(nprob, probs_full_dev,
                                                               reinterpret_cast<const FunctionalFF*>(FU),
