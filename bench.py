@@ -349,12 +349,12 @@ def _stencil_gbs(stream, flush, hbm):
     """Achieved HBM GB/s (algorithmic bytes / time) of the staggered
     divergence (Edges -> Nodes, 12 B per cell FP32) and gradient (Nodes ->
     Edges, 12 B per cell) on 2048^2 and 4096^2 grids, of the fused
-    convective derivatives (v . grad p: Edges + 2 Nodes; u . grad u: 2 Edges)
-    and w x v (2 Edges + Nodes{Dual}) on 4096^2, and of the DDF
-    regularization of the 8192 points of the Stokes configuration onto
-    Nodes{Primal} of its 2048^2 grid (every cell written: 4 B per cell + 16 B
-    per point; points 0.35 h apart) and of the same bodies at ds = 1.4 h on a
-    4096^2 grid, FP32.  Two timings per kernel, both with CUDA events on the
+    convective derivatives (v . grad p: Edges + 2 Nodes{Primal}; v . grad w:
+    Edges + 2 Nodes{Dual}; u . grad u: 2 Edges) and w x v (2 Edges +
+    Nodes{Dual}) on 4096^2, and of the DDF regularization of the 8192 points
+    of the Stokes configuration onto Nodes{Primal} of its 2048^2 grid (every
+    cell written: 4 B per cell + 16 B per point; points 0.35 h apart) and of
+    the same bodies at ds = 1.4 h on a 4096^2 grid, FP32.  Two timings per kernel, both with CUDA events on the
     launching stream:
       * `gbs`: back-to-back launches cycling over rotating input/output sets
         whose total is > 3x the L2 (every launch reads cold data), the time
@@ -421,20 +421,22 @@ def _stencil_gbs(stream, flush, hbm):
     npn = il.NodesPrimal.zeros(g, torch.float32).data.numel()
     nd = il.NodesDual.zeros(g, torch.float32).data.numel()
     sets = []
-    for _ in range(nsets(4 * (2 * ne + 2 * npn + nd))):
+    for _ in range(nsets(4 * (2 * ne + 2 * npn + 2 * nd))):
         v = il.EdgesPrimal.zeros(g, torch.float32)
         v.data.normal_()
         p = il.NodesPrimal.zeros(g, torch.float32)
         p.data.normal_()
         w = il.NodesDual.zeros(g, torch.float32)
         w.data.normal_()
-        sets.append((v, p, w, p.similar(), v.similar()))
+        sets.append((v, p, w, p.similar(), v.similar(), w.similar()))
     for name, mk, nel in [
-            ("convective_nodes_primal", lambda v, p, w, o_p, o_e: lambda: il.convective_derivative_(
+            ("convective_nodes_primal", lambda v, p, w, o_p, o_e, o_d: lambda: il.convective_derivative_(
                 o_p, v, p, c, stream=stream), ne + 2 * npn),
-            ("convective_edges", lambda v, p, w, o_p, o_e: lambda: il.convective_derivative_(
+            ("convective_nodes_dual", lambda v, p, w, o_p, o_e, o_d: lambda: il.convective_derivative_(
+                o_d, v, w, c, stream=stream), ne + 2 * nd),
+            ("convective_edges", lambda v, p, w, o_p, o_e, o_d: lambda: il.convective_derivative_(
                 o_e, v, c, stream=stream), 2 * ne),
-            ("w_cross_v", lambda v, p, w, o_p, o_e: lambda: il.w_cross_v_(o_e, w, v, c, stream=stream),
+            ("w_cross_v", lambda v, p, w, o_p, o_e, o_d: lambda: il.w_cross_v_(o_e, w, v, c, stream=stream),
              2 * ne + nd)]:
         out[f"{name}_{n}"] = timed([mk(*st) for st in sets], nel * 4)
     del c, sets
@@ -1018,7 +1020,8 @@ def _cpu_baseline(args, specs):
 def run_profile_stencils(args):
     """The grid-stencil leg's kernels on 4096^2 FP32 fields, one warm-up pass
     and `args.profile_stencils` timed-order passes: divergence, gradient,
-    v . grad p, u . grad u, w x v (a fixed launch sequence for ncu)."""
+    v . grad p, v . grad w, u . grad u, w x v (a fixed launch sequence for
+    ncu)."""
     import torch
     import __graft_entry__ as ge
     ge.build()
@@ -1032,12 +1035,13 @@ def run_profile_stencils(args):
     p.data.normal_()
     w = il.NodesDual.zeros(g, torch.float32)
     w.data.normal_()
-    o_p, o_e = p.similar(), v.similar()
+    o_p, o_e, o_d = p.similar(), v.similar(), w.similar()
     sc = il.SurfaceScalarCache(None, g, dtype=torch.float32)
     for _ in range(1 + args.profile_stencils):
         il.divergence_(o_p, v, sc)
         il.grad_(o_e, p, sc)
         il.convective_derivative_(o_p, v, p, c)
+        il.convective_derivative_(o_d, v, w, c)
         il.convective_derivative_(o_e, v, c)
         il.w_cross_v_(o_e, w, v, c)
     torch.cuda.synchronize()

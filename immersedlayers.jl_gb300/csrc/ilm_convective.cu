@@ -37,73 +37,110 @@ __device__ __forceinline__ T ld(const T* p, int k) {
 
 // v . grad p, p on Nodes{Primal} (m = NX-1 by NY-1), v on Edges{Primal}
 // (:318-328).  gx at dual x k: p[k]-p[k-1] for 1 <= k <= NX-2, else 0.
-template <typename T>
-__device__ __forceinline__ void vdp_np_at(int i, int j, int NX, int NY, const T* __restrict__ vu,
-    const T* __restrict__ vv, const T* __restrict__ p, T* __restrict__ out, T sc) {
-  const int m = NX - 1;
-  if (i >= m || j >= NY - 1) return;
-  const int c = j * m + i;
-  const T pc = ld(p, c);
-  const T gxl = (i >= 1) ? pc - ld(p, c - 1) : (T)0;            // dual x = i
-  const T gxr = (i + 1 <= NX - 2) ? ld(p, c + 1) - pc : (T)0;  // dual x = i+1
-  const T gyd = (j >= 1) ? pc - ld(p, c - m) : (T)0;           // dual y = j
-  const T gyu = (j + 1 <= NY - 2) ? ld(p, c + m) - pc : (T)0;  // dual y = j+1
-  const T tx = ld(vu, j * NX + i) * gxl + ld(vu, j * NX + i + 1) * gxr;
-  const T ty = ld(vv, j * m + i) * gyd + ld(vv, (j + 1) * m + i) * gyu;
-  out[c] = (T)0.5 * (tx + ty) * sc;
-}
-
+// RY consecutive output rows per thread (jb .. jb+RY-1): the rows share
+// their vertical neighbours in registers, and every load of the RY rows is
+// issued before the arithmetic.
 template <typename T>
 __global__ void __launch_bounds__(BX* BY) k_vdp_np(int NX, int NY, const T* __restrict__ vu, const T* __restrict__ vv,
     const T* __restrict__ p, T* __restrict__ out, T sc) {
-  // RY output rows per thread (j, j + BY, ...), all independent, so their
-  // loads are in flight together
+  const int m = NX - 1, n = NY - 1;  // p is m x n
   const int i = blockIdx.x * BX + threadIdx.x;
-  const int jb = blockIdx.y * BY * RY + threadIdx.y;
+  const int jb = (blockIdx.y * BY + threadIdx.y) * RY;
+  if (i >= m || jb >= n) return;
+  const bool has_l = i >= 1, has_r = i + 1 <= NX - 2;
+  T pc[RY + 2], pl[RY], pr[RY], u0[RY], u1[RY], vd[RY + 1];
 #pragma unroll
-  for (int r = 0; r < RY; ++r) vdp_np_at(i, jb + r * BY, NX, NY, vu, vv, p, out, sc);
+  for (int k = 0; k < RY + 2; ++k) {  // p column i, rows jb-1 .. jb+RY
+    const int j = jb - 1 + k;
+    pc[k] = (j >= 0 && j < n) ? ld(p, j * m + i) : (T)0;
+  }
+#pragma unroll
+  for (int k = 0; k < RY; ++k) {
+    const int j = jb + k;
+    const bool ok = j < n;
+    pl[k] = (ok && has_l) ? ld(p, j * m + i - 1) : (T)0;
+    pr[k] = (ok && has_r) ? ld(p, j * m + i + 1) : (T)0;
+    u0[k] = ok ? ld(vu, j * NX + i) : (T)0;
+    u1[k] = ok ? ld(vu, j * NX + i + 1) : (T)0;
+  }
+#pragma unroll
+  for (int k = 0; k < RY + 1; ++k) {  // vv column i, rows jb .. jb+RY (vv is m x NY)
+    const int j = jb + k;
+    vd[k] = (j < NY) ? ld(vv, j * m + i) : (T)0;
+  }
+#pragma unroll
+  for (int k = 0; k < RY; ++k) {
+    const int j = jb + k;
+    if (j < n) {
+      const T c = pc[k + 1];
+      const T gxl = has_l ? c - pl[k] : (T)0;
+      const T gxr = has_r ? pr[k] - c : (T)0;
+      const T gyd = (j >= 1) ? c - pc[k] : (T)0;
+      const T gyu = (j + 1 <= NY - 2) ? pc[k + 2] - c : (T)0;
+      const T tx = u0[k] * gxl + u1[k] * gxr;
+      const T ty = vd[k] * gyd + vd[k + 1] * gyu;
+      out[j * m + i] = (T)0.5 * (tx + ty) * sc;
+    }
+  }
 }
 
 // v . grad w, w on Nodes{Dual} (NX x NY), v on Edges{Primal} (:330-342):
 // v averaged onto the Edges{Dual} positions (four-point means), times the
 // Edges{Dual} gradient of w, averaged onto the non-ghost dual nodes.
-template <typename T>
-__device__ __forceinline__ void vdw_nd_at(int i, int j, int NX, int NY, const T* __restrict__ vu,
-    const T* __restrict__ vv, const T* __restrict__ w, T* __restrict__ out, T sc) {
-  if (i >= NX || j >= NY) return;
-  const int c = j * NX + i;
-  if (i < 1 || i > NX - 2 || j < 1 || j > NY - 2) {
-    out[c] = (T)0;
-    return;
-  }
-  const int m = NX - 1;
-  const T wc = ld(w, c);
-  // Edges{Dual}.u at (primal x k, dual y j), k = i-1, i: mean of vu over
-  // dual x k, k+1 and primal y j-1, j
-  const int r0 = (j - 1) * NX, r1 = j * NX;
-  const T a0 = ld(vu, r0 + i - 1), a1 = ld(vu, r0 + i), a2 = ld(vu, r0 + i + 1);
-  const T b0 = ld(vu, r1 + i - 1), b1 = ld(vu, r1 + i), b2 = ld(vu, r1 + i + 1);
-  const T udl = (T)0.25 * (a0 + a1 + b0 + b1), udr = (T)0.25 * (a1 + a2 + b1 + b2);
-  const T tx = udl * (wc - ld(w, c - 1)) + udr * (ld(w, c + 1) - wc);
-  // Edges{Dual}.v at (dual x i, primal y l), l = j-1, j: mean of vv over
-  // primal x i-1, i and dual y l, l+1
-  const int s0 = (j - 1) * m, s1 = j * m, s2 = (j + 1) * m;
-  const T e0 = ld(vv, s0 + i - 1) + ld(vv, s0 + i), e1 = ld(vv, s1 + i - 1) + ld(vv, s1 + i);
-  const T e2 = ld(vv, s2 + i - 1) + ld(vv, s2 + i);
-  const T vdd = (T)0.25 * (e0 + e1), vdu = (T)0.25 * (e1 + e2);
-  const T ty = vdd * (wc - ld(w, c - NX)) + vdu * (ld(w, c + NX) - wc);
-  out[c] = (T)0.5 * (tx + ty) * sc;
-}
-
+// RY consecutive output rows per thread (jb .. jb+RY-1), vertical
+// neighbours shared in registers, every load issued before the arithmetic.
+// Interior cells only (1 <= i <= NX-2, 1 <= j <= NY-2); the ghost layer is 0.
 template <typename T>
 __global__ void __launch_bounds__(BX* BY) k_vdw_nd(int NX, int NY, const T* __restrict__ vu, const T* __restrict__ vv,
     const T* __restrict__ w, T* __restrict__ out, T sc) {
-  // RY output rows per thread (j, j + BY, ...), all independent, so their
-  // loads are in flight together
+  const int m = NX - 1;
   const int i = blockIdx.x * BX + threadIdx.x;
-  const int jb = blockIdx.y * BY * RY + threadIdx.y;
+  const int jb = (blockIdx.y * BY + threadIdx.y) * RY;
+  if (i >= NX || jb >= NY) return;
+  const bool col = i >= 1 && i <= NX - 2;
+  // wc: w column i rows jb-1 .. jb+RY; wl, wr: columns i-1, i+1 rows jb ..
+  // jb+RY-1; a0..a2: vu columns i-1, i, i+1 rows jb-1 .. jb+RY-1 (vu is
+  // NX x NY-1); e0, e1: vv columns i-1, i rows jb-1 .. jb+RY (vv is m x NY)
+  T wc[RY + 2], wl[RY], wr[RY], a0[RY + 1], a1[RY + 1], a2[RY + 1], e0[RY + 2], e1[RY + 2];
 #pragma unroll
-  for (int r = 0; r < RY; ++r) vdw_nd_at(i, jb + r * BY, NX, NY, vu, vv, w, out, sc);
+  for (int k = 0; k < RY + 2; ++k) {
+    const int j = jb - 1 + k;
+    const bool row = col && j >= 0 && j < NY;
+    wc[k] = row ? ld(w, j * NX + i) : (T)0;
+    e0[k] = row ? ld(vv, j * m + i - 1) : (T)0;
+    e1[k] = row ? ld(vv, j * m + i) : (T)0;
+    if (k < RY + 1) {
+      const bool urow = col && j >= 0 && j <= NY - 2;
+      a0[k] = urow ? ld(vu, j * NX + i - 1) : (T)0;
+      a1[k] = urow ? ld(vu, j * NX + i) : (T)0;
+      a2[k] = urow ? ld(vu, j * NX + i + 1) : (T)0;
+    }
+    if (k >= 1 && k <= RY) {
+      wl[k - 1] = row ? ld(w, j * NX + i - 1) : (T)0;
+      wr[k - 1] = row ? ld(w, j * NX + i + 1) : (T)0;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < RY; ++k) {
+    const int j = jb + k;
+    if (j >= NY) break;
+    T r = (T)0;
+    if (col && j >= 1 && j <= NY - 2) {
+      const T c = wc[k + 1];
+      // Edges{Dual}.u at (primal x i-1 / i, dual y j): mean of vu over
+      // dual x and primal y j-1, j
+      const T udl = (T)0.25 * (a0[k] + a1[k] + a0[k + 1] + a1[k + 1]);
+      const T udr = (T)0.25 * (a1[k] + a2[k] + a1[k + 1] + a2[k + 1]);
+      const T tx = udl * (c - wl[k]) + udr * (wr[k] - c);
+      // Edges{Dual}.v at (dual x i, primal y j-1 / j): mean of vv over
+      // primal x i-1, i and dual y
+      const T s0 = e0[k] + e1[k], s1 = e0[k + 1] + e1[k + 1], s2 = e0[k + 2] + e1[k + 2];
+      const T vdd = (T)0.25 * (s0 + s1), vdu = (T)0.25 * (s1 + s2);
+      const T ty = vdd * (c - wc[k]) + vdu * (wc[k + 2] - c);
+      r = (T)0.5 * (tx + ty) * sc;
+    }
+    out[j * NX + i] = r;
+  }
 }
 
 // v . grad u for Edges{Primal} v and u (:344-371; u . grad u with v = u).
@@ -115,108 +152,152 @@ __global__ void __launch_bounds__(BX* BY) k_vdw_nd(int NX, int NY, const T* __re
 //   dvdx (dual, dual):         mean_y(v.u) * (u.v[k]-u.v[k-1])   (non-ghost only)
 //   dvdy (primal, primal):     mean_y(v.v) * (u.v[l+1]-u.v[l])
 // and the result is their average back onto the edges.
-template <typename T>
-__device__ __forceinline__ void vdu_edges_at(int i, int j, int NX, int NY, const T* __restrict__ vu,
-    const T* __restrict__ vv, const T* __restrict__ uu, const T* __restrict__ uv, T* __restrict__ ou,
-    T* __restrict__ ov, T sc) {
-  const int m = NX - 1;
-  if (i >= NX || j >= NY) return;
-  if (j <= NY - 2) {
-    const int c = j * NX + i;
-    T r = (T)0;
-    if (i >= 1 && i <= NX - 2) {
-      // x part: dudx slots at primal x i-1, i (row j)
-      const T u0 = ld(uu, c - 1), u1 = ld(uu, c), u2 = ld(uu, c + 1);
-      const T v0 = ld(vu, c - 1), v1 = ld(vu, c), v2 = ld(vu, c + 1);
-      const T tx = (T)0.5 * (v0 + v1) * (u1 - u0) + (T)0.5 * (v1 + v2) * (u2 - u1);
-      // y part: dudy slots at dual (i, l), l = j, j+1, nonzero for 1 <= l <= NY-2
-      T ty = (T)0;
-      if (j >= 1) {
-        const T a = (T)0.5 * (ld(vv, j * m + i - 1) + ld(vv, j * m + i));
-        ty += a * (u1 - ld(uu, c - NX));
-      }
-      if (j + 1 <= NY - 2) {
-        const T a = (T)0.5 * (ld(vv, (j + 1) * m + i - 1) + ld(vv, (j + 1) * m + i));
-        ty += a * (ld(uu, c + NX) - u1);
-      }
-      r = (T)0.5 * (tx + ty) * sc;
-    }
-    ou[c] = r;
-  }
-  if (i <= NX - 2) {
-    const int c = j * m + i;
-    T r = (T)0;
-    if (j >= 1 && j <= NY - 2) {
-      // y part: dvdy slots at primal y j-1, j (column i)
-      const T u0 = ld(uv, c - m), u1 = ld(uv, c), u2 = ld(uv, c + m);
-      const T v0 = ld(vv, c - m), v1 = ld(vv, c), v2 = ld(vv, c + m);
-      const T ty = (T)0.5 * (v0 + v1) * (u1 - u0) + (T)0.5 * (v1 + v2) * (u2 - u1);
-      // x part: dvdx slots at dual (k, j), k = i, i+1, nonzero for 1 <= k <= NX-2
-      T tx = (T)0;
-      if (i >= 1) {
-        const T a = (T)0.5 * (ld(vu, (j - 1) * NX + i) + ld(vu, j * NX + i));
-        tx += a * (u1 - ld(uv, c - 1));
-      }
-      if (i + 1 <= NX - 2) {
-        const T a = (T)0.5 * (ld(vu, (j - 1) * NX + i + 1) + ld(vu, j * NX + i + 1));
-        tx += a * (ld(uv, c + 1) - u1);
-      }
-      r = (T)0.5 * (tx + ty) * sc;
-    }
-    ov[c] = r;
-  }
-}
-
+// RY consecutive rows per thread (jb .. jb+RY-1), the vertical neighbours
+// shared in registers (53 loads for four rows of both components instead of
+// 96) and every load issued before the arithmetic.
 template <typename T>
 __global__ void __launch_bounds__(BX* BY) k_vdu_edges(int NX, int NY, const T* __restrict__ vu,
     const T* __restrict__ vv, const T* __restrict__ uu, const T* __restrict__ uv, T* __restrict__ ou,
     T* __restrict__ ov, T sc) {
-  // RY output rows per thread (j, j + BY, ...), all independent, so their
-  // loads are in flight together
+  const int m = NX - 1;
   const int i = blockIdx.x * BX + threadIdx.x;
-  const int jb = blockIdx.y * BY * RY + threadIdx.y;
+  const int jb = (blockIdx.y * BY + threadIdx.y) * RY;
+  if (i >= NX || jb >= NY) return;
+  const bool u_in = i >= 1 && i <= NX - 2;  // out.u nonzero in this column
+  const bool v_col = i <= NX - 2;           // out.v has this column
+  const bool v_rt = i + 1 <= NX - 2;        // out.v's dvdx slot at dual x i+1
+  // Columns of the u components (NX x NY-1): uuc = uu column i rows jb-1 ..
+  // jb+RY, uul / uur columns i-1 / i+1 rows jb .. jb+RY-1; vuc / vur = vu
+  // columns i / i+1 rows jb-1 .. jb+RY-1, vul column i-1 rows jb ..
+  // jb+RY-1.  Columns of the v components (NX-1 x NY): vvc / uvc = column i
+  // rows jb-1 .. jb+RY, vvl column i-1 rows jb .. jb+RY, uvl / uvr columns
+  // i-1 / i+1 rows jb .. jb+RY-1.
+  T uuc[RY + 2], uul[RY], uur[RY], vuc[RY + 1], vur[RY + 1], vul[RY];
+  T vvc[RY + 2], uvc[RY + 2], vvl[RY + 1], uvl[RY], uvr[RY];
 #pragma unroll
-  for (int r = 0; r < RY; ++r) vdu_edges_at(i, jb + r * BY, NX, NY, vu, vv, uu, uv, ou, ov, sc);
+  for (int k = 0; k < RY + 2; ++k) {
+    const int j = jb - 1 + k;  // row of index k in the jb-1 based arrays
+    const bool urow = j >= 0 && j <= NY - 2, vrow = j >= 0 && j < NY;
+    uuc[k] = (u_in && urow) ? ld(uu, j * NX + i) : (T)0;
+    vvc[k] = (v_col && vrow) ? ld(vv, j * m + i) : (T)0;
+    uvc[k] = (v_col && vrow) ? ld(uv, j * m + i) : (T)0;
+    if (k < RY + 1) {
+      vuc[k] = (u_in && urow) ? ld(vu, j * NX + i) : (T)0;
+      vur[k] = ((u_in || v_rt) && urow) ? ld(vu, j * NX + i + 1) : (T)0;
+    }
+    if (k >= 1) {  // rows jb .. jb+RY
+      vvl[k - 1] = (u_in && vrow) ? ld(vv, j * m + i - 1) : (T)0;
+      if (k <= RY) {  // rows jb .. jb+RY-1
+        uul[k - 1] = (u_in && urow) ? ld(uu, j * NX + i - 1) : (T)0;
+        uur[k - 1] = (u_in && urow) ? ld(uu, j * NX + i + 1) : (T)0;
+        vul[k - 1] = (u_in && urow) ? ld(vu, j * NX + i - 1) : (T)0;
+        uvl[k - 1] = (u_in && vrow) ? ld(uv, j * m + i - 1) : (T)0;
+        uvr[k - 1] = (v_rt && vrow) ? ld(uv, j * m + i + 1) : (T)0;
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < RY; ++k) {
+    const int j = jb + k;
+    if (j >= NY) break;
+    if (j <= NY - 2) {
+      T r = (T)0;
+      if (u_in) {
+        // x part: dudx slots at primal x i-1, i (row j)
+        const T u0 = uul[k], u1 = uuc[k + 1], u2 = uur[k];
+        const T v0 = vul[k], v1 = vuc[k + 1], v2 = vur[k + 1];
+        const T tx = (T)0.5 * (v0 + v1) * (u1 - u0) + (T)0.5 * (v1 + v2) * (u2 - u1);
+        // y part: dudy slots at dual (i, l), l = j, j+1, nonzero for 1 <= l <= NY-2
+        T ty = (T)0;
+        if (j >= 1) {
+          const T a = (T)0.5 * (vvl[k] + vvc[k + 1]);
+          ty += a * (u1 - uuc[k]);
+        }
+        if (j + 1 <= NY - 2) {
+          const T a = (T)0.5 * (vvl[k + 1] + vvc[k + 2]);
+          ty += a * (uuc[k + 2] - u1);
+        }
+        r = (T)0.5 * (tx + ty) * sc;
+      }
+      ou[j * NX + i] = r;
+    }
+    if (v_col) {
+      T r = (T)0;
+      if (j >= 1 && j <= NY - 2) {
+        // y part: dvdy slots at primal y j-1, j (column i)
+        const T u0 = uvc[k], u1 = uvc[k + 1], u2 = uvc[k + 2];
+        const T v0 = vvc[k], v1 = vvc[k + 1], v2 = vvc[k + 2];
+        const T ty = (T)0.5 * (v0 + v1) * (u1 - u0) + (T)0.5 * (v1 + v2) * (u2 - u1);
+        // x part: dvdx slots at dual (k, j), k = i, i+1, nonzero for 1 <= k <= NX-2
+        T tx = (T)0;
+        if (i >= 1) {
+          const T a = (T)0.5 * (vuc[k] + vuc[k + 1]);
+          tx += a * (u1 - uvl[k]);
+        }
+        if (v_rt) {
+          const T a = (T)0.5 * (vur[k] + vur[k + 1]);
+          tx += a * (uvr[k] - u1);
+        }
+        r = (T)0.5 * (tx + ty) * sc;
+      }
+      ov[j * m + i] = r;
+    }
+  }
 }
 
 // w x v (:419-434): out.u = mean_y(-mean_x(v.v) w), out.v = mean_x(mean_y(v.u) w),
 // the inner means onto the non-ghost dual nodes only.  Thread (i, j) writes
 // out.u(i, j) (j <= NY-2) and out.v(i, j) (i <= NX-2).
-template <typename T>
-__device__ __forceinline__ void w_cross_v_at(int i, int j, int NX, int NY, const T* __restrict__ w,
-    const T* __restrict__ vu, const T* __restrict__ vv, T* __restrict__ ou, T* __restrict__ ov) {
-  const int m = NX - 1;
-  if (i >= NX || j >= NY) return;
-  const T w0 = ld(w, j * NX + i);
-  if (j <= NY - 2) {
-    T r = (T)0;
-    if (i >= 1 && i <= NX - 2) {
-      const T vd0 = (T)0.5 * (ld(vv, j * m + i - 1) + ld(vv, j * m + i));
-      const T vd1 = (T)0.5 * (ld(vv, (j + 1) * m + i - 1) + ld(vv, (j + 1) * m + i));
-      r = (T)-0.5 * (vd0 * w0 + vd1 * ld(w, (j + 1) * NX + i));
-    }
-    ou[j * NX + i] = r;
-  }
-  if (i <= NX - 2) {
-    T r = (T)0;
-    if (j >= 1 && j <= NY - 2) {
-      const T ud0 = (T)0.5 * (ld(vu, (j - 1) * NX + i) + ld(vu, j * NX + i));
-      const T ud1 = (T)0.5 * (ld(vu, (j - 1) * NX + i + 1) + ld(vu, j * NX + i + 1));
-      r = (T)0.5 * (ud0 * w0 + ud1 * ld(w, j * NX + i + 1));
-    }
-    ov[j * m + i] = r;
-  }
-}
-
+// RY consecutive rows per thread (jb .. jb+RY-1), vertical neighbours shared
+// in registers, every load issued before the arithmetic.
 template <typename T>
 __global__ void __launch_bounds__(BX* BY) k_w_cross_v(int NX, int NY, const T* __restrict__ w,
     const T* __restrict__ vu, const T* __restrict__ vv, T* __restrict__ ou, T* __restrict__ ov) {
-  // RY output rows per thread (j, j + BY, ...), all independent, so their
-  // loads are in flight together
+  const int m = NX - 1;
   const int i = blockIdx.x * BX + threadIdx.x;
-  const int jb = blockIdx.y * BY * RY + threadIdx.y;
+  const int jb = (blockIdx.y * BY + threadIdx.y) * RY;
+  if (i >= NX || jb >= NY) return;
+  const bool u_in = i >= 1 && i <= NX - 2;  // out.u nonzero in this column
+  const bool v_col = i <= NX - 2;           // out.v has this column
+  // wc: w column i rows jb .. jb+RY; wr: w column i+1 rows jb .. jb+RY-1;
+  // vl, vr: vv columns i-1, i rows jb .. jb+RY; ua, ub: vu columns i, i+1
+  // rows jb-1 .. jb+RY-1
+  T wc[RY + 1], wr[RY], vl[RY + 1], vr[RY + 1], ua[RY + 1], ub[RY + 1];
 #pragma unroll
-  for (int r = 0; r < RY; ++r) w_cross_v_at(i, jb + r * BY, NX, NY, w, vu, vv, ou, ov);
+  for (int k = 0; k < RY + 1; ++k) {
+    const int j = jb + k;
+    const bool row = j < NY;
+    wc[k] = row ? ld(w, j * NX + i) : (T)0;
+    vl[k] = (row && u_in) ? ld(vv, j * m + i - 1) : (T)0;
+    vr[k] = (row && u_in) ? ld(vv, j * m + i) : (T)0;
+    const int jv = j - 1;
+    const bool vrow = v_col && jv >= 0 && jv <= NY - 2;
+    ua[k] = vrow ? ld(vu, jv * NX + i) : (T)0;
+    ub[k] = vrow ? ld(vu, jv * NX + i + 1) : (T)0;
+    if (k < RY) wr[k] = (row && v_col) ? ld(w, j * NX + i + 1) : (T)0;
+  }
+#pragma unroll
+  for (int k = 0; k < RY; ++k) {
+    const int j = jb + k;
+    if (j <= NY - 2) {
+      T r = (T)0;
+      if (u_in) {
+        const T vd0 = (T)0.5 * (vl[k] + vr[k]);
+        const T vd1 = (T)0.5 * (vl[k + 1] + vr[k + 1]);
+        r = (T)-0.5 * (vd0 * wc[k] + vd1 * wc[k + 1]);
+      }
+      ou[j * NX + i] = r;
+    }
+    if (v_col && j < NY) {
+      T r = (T)0;
+      if (j >= 1 && j <= NY - 2) {
+        const T ud0 = (T)0.5 * (ua[k] + ua[k + 1]);
+        const T ud1 = (T)0.5 * (ub[k] + ub[k + 1]);
+        r = (T)0.5 * (ud0 * wc[k] + ud1 * wr[k]);
+      }
+      ov[j * m + i] = r;
+    }
+  }
 }
 
 }  // namespace

@@ -81,6 +81,33 @@ def test_w_cross_v(S):
     assert rel(il.w_cross_v(w, v, S["vc"]).numpy_components(), O.w_cross_v(wh, vh)) < S["tol"]
 
 
+@pytest.mark.parametrize("nx,ny", [(37, 23), (70, 9), (5, 6), (33, 34)])
+def test_convective_ragged_grids(S, nx, ny):
+    """Rectangular grids whose sizes are not multiples of the kernels' tiles
+    (32 columns by 32 rows, four consecutive rows per thread): every output,
+    ghost layers included, against the oracle."""
+    il, torch = S["il"], S["torch"]
+    h = 0.1
+    g = il.PhysicalGrid(h=h, nx=nx, ny=ny)
+    og = O.Grid(nx, ny, h, g.i0[0], g.i0[1])
+    S2 = dict(S, g=g)
+    sc = il.SurfaceScalarCache(None, g, dtype=S["dt"])
+    vc = il.SurfaceVectorCache(None, g, dtype=S["dt"])
+    v, vh = _rand(S2, il.EdgesPrimal, 11)
+    u, uh = _rand(S2, il.EdgesPrimal, 12)
+    p, ph = _rand(S2, il.NodesPrimal, 13)
+    w, wh = _rand(S2, il.NodesDual, 14)
+    s = 1.0 / h
+    out = il.convective_derivative(v, p, sc)
+    assert rel(out.numpy_components(), O.convective_derivative_nodes_primal(vh, ph, og, s)) < S["tol"]
+    out = il.convective_derivative(v, w, sc)
+    assert rel(out.numpy_components(), O.convective_derivative_nodes_dual(vh, wh, og, s)) < S["tol"]
+    out = il.EdgesPrimal.zeros(g, S["dt"])
+    il.convective_derivative_(out, v, u, vc, il.ConvectiveDerivativeCache(vc))
+    assert rel(out.numpy_components(), O.convective_derivative_edges(vh, uh, og, s)) < S["tol"]
+    assert rel(il.w_cross_v(w, v, vc).numpy_components(), O.w_cross_v(wh, vh)) < S["tol"]
+
+
 def test_convective_derivative_linear_fields_exact(S):
     """Uniform velocity (a, b) and linear p = c x + d y: v . grad p = a c + b d
     away from the ghost layers (GridScaling: differences / h)."""
