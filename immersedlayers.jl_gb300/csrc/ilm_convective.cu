@@ -35,29 +35,39 @@ __device__ __forceinline__ T ld(const T* p, int k) {
   return __ldg(p + k);
 }
 
+// A block is inner when every thread's columns i-1 .. i+2 and rows jb-1 ..
+// jb+RY+1 lie inside the grid with the ghost layers excluded: columns
+// 1 <= i <= NX-3 and rows 1 <= jb, jb+RY <= NY-2 for all of its threads.
+// The kernels below then take a path with every bounds test constant (IN =
+// true); the blocks along the edges take the general one.
+__device__ __forceinline__ bool inner_block(int NX, int NY) {
+  const int i0 = blockIdx.x * BX, j0 = blockIdx.y * BY * RY;
+  return i0 >= 1 && i0 + BX - 1 <= NX - 3 && j0 >= 1 && j0 + BY * RY <= NY - 2;
+}
+
 // v . grad p, p on Nodes{Primal} (m = NX-1 by NY-1), v on Edges{Primal}
 // (:318-328).  gx at dual x k: p[k]-p[k-1] for 1 <= k <= NX-2, else 0.
 // RY consecutive output rows per thread (jb .. jb+RY-1): the rows share
 // their vertical neighbours in registers, and every load of the RY rows is
 // issued before the arithmetic.
-template <typename T>
-__global__ void __launch_bounds__(BX* BY) k_vdp_np(int NX, int NY, const T* __restrict__ vu, const T* __restrict__ vv,
+template <typename T, bool IN>
+__device__ __forceinline__ void vdp_np_rows(int NX, int NY, const T* __restrict__ vu, const T* __restrict__ vv,
     const T* __restrict__ p, T* __restrict__ out, T sc) {
   const int m = NX - 1, n = NY - 1;  // p is m x n
   const int i = blockIdx.x * BX + threadIdx.x;
   const int jb = (blockIdx.y * BY + threadIdx.y) * RY;
-  if (i >= m || jb >= n) return;
-  const bool has_l = i >= 1, has_r = i + 1 <= NX - 2;
+  if (!IN && (i >= m || jb >= n)) return;
+  const bool has_l = IN || i >= 1, has_r = IN || i + 1 <= NX - 2;
   T pc[RY + 2], pl[RY], pr[RY], u0[RY], u1[RY], vd[RY + 1];
 #pragma unroll
   for (int k = 0; k < RY + 2; ++k) {  // p column i, rows jb-1 .. jb+RY
     const int j = jb - 1 + k;
-    pc[k] = (j >= 0 && j < n) ? ld(p, j * m + i) : (T)0;
+    pc[k] = (IN || (j >= 0 && j < n)) ? ld(p, j * m + i) : (T)0;
   }
 #pragma unroll
   for (int k = 0; k < RY; ++k) {
     const int j = jb + k;
-    const bool ok = j < n;
+    const bool ok = IN || j < n;
     pl[k] = (ok && has_l) ? ld(p, j * m + i - 1) : (T)0;
     pr[k] = (ok && has_r) ? ld(p, j * m + i + 1) : (T)0;
     u0[k] = ok ? ld(vu, j * NX + i) : (T)0;
@@ -66,22 +76,31 @@ __global__ void __launch_bounds__(BX* BY) k_vdp_np(int NX, int NY, const T* __re
 #pragma unroll
   for (int k = 0; k < RY + 1; ++k) {  // vv column i, rows jb .. jb+RY (vv is m x NY)
     const int j = jb + k;
-    vd[k] = (j < NY) ? ld(vv, j * m + i) : (T)0;
+    vd[k] = (IN || j < NY) ? ld(vv, j * m + i) : (T)0;
   }
 #pragma unroll
   for (int k = 0; k < RY; ++k) {
     const int j = jb + k;
-    if (j < n) {
+    if (IN || j < n) {
       const T c = pc[k + 1];
       const T gxl = has_l ? c - pl[k] : (T)0;
       const T gxr = has_r ? pr[k] - c : (T)0;
-      const T gyd = (j >= 1) ? c - pc[k] : (T)0;
-      const T gyu = (j + 1 <= NY - 2) ? pc[k + 2] - c : (T)0;
+      const T gyd = (IN || j >= 1) ? c - pc[k] : (T)0;
+      const T gyu = (IN || j + 1 <= NY - 2) ? pc[k + 2] - c : (T)0;
       const T tx = u0[k] * gxl + u1[k] * gxr;
       const T ty = vd[k] * gyd + vd[k + 1] * gyu;
       out[j * m + i] = (T)0.5 * (tx + ty) * sc;
     }
   }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(BX* BY) k_vdp_np(int NX, int NY, const T* __restrict__ vu, const T* __restrict__ vv,
+    const T* __restrict__ p, T* __restrict__ out, T sc) {
+  if (inner_block(NX, NY))
+    vdp_np_rows<T, true>(NX, NY, vu, vv, p, out, sc);
+  else
+    vdp_np_rows<T, false>(NX, NY, vu, vv, p, out, sc);
 }
 
 // v . grad w, w on Nodes{Dual} (NX x NY), v on Edges{Primal} (:330-342):
@@ -90,14 +109,14 @@ __global__ void __launch_bounds__(BX* BY) k_vdp_np(int NX, int NY, const T* __re
 // RY consecutive output rows per thread (jb .. jb+RY-1), vertical
 // neighbours shared in registers, every load issued before the arithmetic.
 // Interior cells only (1 <= i <= NX-2, 1 <= j <= NY-2); the ghost layer is 0.
-template <typename T>
-__global__ void __launch_bounds__(BX* BY) k_vdw_nd(int NX, int NY, const T* __restrict__ vu, const T* __restrict__ vv,
+template <typename T, bool IN>
+__device__ __forceinline__ void vdw_nd_rows(int NX, int NY, const T* __restrict__ vu, const T* __restrict__ vv,
     const T* __restrict__ w, T* __restrict__ out, T sc) {
   const int m = NX - 1;
   const int i = blockIdx.x * BX + threadIdx.x;
   const int jb = (blockIdx.y * BY + threadIdx.y) * RY;
-  if (i >= NX || jb >= NY) return;
-  const bool col = i >= 1 && i <= NX - 2;
+  if (!IN && (i >= NX || jb >= NY)) return;
+  const bool col = IN || (i >= 1 && i <= NX - 2);
   // wc: w column i rows jb-1 .. jb+RY; wl, wr: columns i-1, i+1 rows jb ..
   // jb+RY-1; a0..a2: vu columns i-1, i, i+1 rows jb-1 .. jb+RY-1 (vu is
   // NX x NY-1); e0, e1: vv columns i-1, i rows jb-1 .. jb+RY (vv is m x NY)
@@ -105,12 +124,12 @@ __global__ void __launch_bounds__(BX* BY) k_vdw_nd(int NX, int NY, const T* __re
 #pragma unroll
   for (int k = 0; k < RY + 2; ++k) {
     const int j = jb - 1 + k;
-    const bool row = col && j >= 0 && j < NY;
+    const bool row = IN || (col && j >= 0 && j < NY);
     wc[k] = row ? ld(w, j * NX + i) : (T)0;
     e0[k] = row ? ld(vv, j * m + i - 1) : (T)0;
     e1[k] = row ? ld(vv, j * m + i) : (T)0;
     if (k < RY + 1) {
-      const bool urow = col && j >= 0 && j <= NY - 2;
+      const bool urow = IN || (col && j >= 0 && j <= NY - 2);
       a0[k] = urow ? ld(vu, j * NX + i - 1) : (T)0;
       a1[k] = urow ? ld(vu, j * NX + i) : (T)0;
       a2[k] = urow ? ld(vu, j * NX + i + 1) : (T)0;
@@ -123,9 +142,9 @@ __global__ void __launch_bounds__(BX* BY) k_vdw_nd(int NX, int NY, const T* __re
 #pragma unroll
   for (int k = 0; k < RY; ++k) {
     const int j = jb + k;
-    if (j >= NY) break;
+    if (!IN && j >= NY) break;
     T r = (T)0;
-    if (col && j >= 1 && j <= NY - 2) {
+    if (IN || (col && j >= 1 && j <= NY - 2)) {
       const T c = wc[k + 1];
       // Edges{Dual}.u at (primal x i-1 / i, dual y j): mean of vu over
       // dual x and primal y j-1, j
@@ -143,6 +162,15 @@ __global__ void __launch_bounds__(BX* BY) k_vdw_nd(int NX, int NY, const T* __re
   }
 }
 
+template <typename T>
+__global__ void __launch_bounds__(BX* BY) k_vdw_nd(int NX, int NY, const T* __restrict__ vu, const T* __restrict__ vv,
+    const T* __restrict__ w, T* __restrict__ out, T sc) {
+  if (inner_block(NX, NY))
+    vdw_nd_rows<T, true>(NX, NY, vu, vv, w, out, sc);
+  else
+    vdw_nd_rows<T, false>(NX, NY, vu, vv, w, out, sc);
+}
+
 // v . grad u for Edges{Primal} v and u (:344-371; u . grad u with v = u).
 // Thread (i, j) writes out.u(i, j) (j <= NY-2) and out.v(i, j) (i <= NX-2):
 // both components in one CTA, so the inputs a CTA needs come from DRAM once.
@@ -155,17 +183,17 @@ __global__ void __launch_bounds__(BX* BY) k_vdw_nd(int NX, int NY, const T* __re
 // RY consecutive rows per thread (jb .. jb+RY-1), the vertical neighbours
 // shared in registers (53 loads for four rows of both components instead of
 // 96) and every load issued before the arithmetic.
-template <typename T>
-__global__ void __launch_bounds__(BX* BY) k_vdu_edges(int NX, int NY, const T* __restrict__ vu,
+template <typename T, bool IN>
+__device__ __forceinline__ void vdu_edges_rows(int NX, int NY, const T* __restrict__ vu,
     const T* __restrict__ vv, const T* __restrict__ uu, const T* __restrict__ uv, T* __restrict__ ou,
     T* __restrict__ ov, T sc) {
   const int m = NX - 1;
   const int i = blockIdx.x * BX + threadIdx.x;
   const int jb = (blockIdx.y * BY + threadIdx.y) * RY;
-  if (i >= NX || jb >= NY) return;
-  const bool u_in = i >= 1 && i <= NX - 2;  // out.u nonzero in this column
-  const bool v_col = i <= NX - 2;           // out.v has this column
-  const bool v_rt = i + 1 <= NX - 2;        // out.v's dvdx slot at dual x i+1
+  if (!IN && (i >= NX || jb >= NY)) return;
+  const bool u_in = IN || (i >= 1 && i <= NX - 2);  // out.u nonzero in this column
+  const bool v_col = IN || i <= NX - 2;             // out.v has this column
+  const bool v_rt = IN || i + 1 <= NX - 2;          // out.v's dvdx slot at dual x i+1
   // Columns of the u components (NX x NY-1): uuc = uu column i rows jb-1 ..
   // jb+RY, uul / uur columns i-1 / i+1 rows jb .. jb+RY-1; vuc / vur = vu
   // columns i / i+1 rows jb-1 .. jb+RY-1, vul column i-1 rows jb ..
@@ -177,7 +205,7 @@ __global__ void __launch_bounds__(BX* BY) k_vdu_edges(int NX, int NY, const T* _
 #pragma unroll
   for (int k = 0; k < RY + 2; ++k) {
     const int j = jb - 1 + k;  // row of index k in the jb-1 based arrays
-    const bool urow = j >= 0 && j <= NY - 2, vrow = j >= 0 && j < NY;
+    const bool urow = IN || (j >= 0 && j <= NY - 2), vrow = IN || (j >= 0 && j < NY);
     uuc[k] = (u_in && urow) ? ld(uu, j * NX + i) : (T)0;
     vvc[k] = (v_col && vrow) ? ld(vv, j * m + i) : (T)0;
     uvc[k] = (v_col && vrow) ? ld(uv, j * m + i) : (T)0;
@@ -199,8 +227,8 @@ __global__ void __launch_bounds__(BX* BY) k_vdu_edges(int NX, int NY, const T* _
 #pragma unroll
   for (int k = 0; k < RY; ++k) {
     const int j = jb + k;
-    if (j >= NY) break;
-    if (j <= NY - 2) {
+    if (!IN && j >= NY) break;
+    if (IN || j <= NY - 2) {
       T r = (T)0;
       if (u_in) {
         // x part: dudx slots at primal x i-1, i (row j)
@@ -209,11 +237,11 @@ __global__ void __launch_bounds__(BX* BY) k_vdu_edges(int NX, int NY, const T* _
         const T tx = (T)0.5 * (v0 + v1) * (u1 - u0) + (T)0.5 * (v1 + v2) * (u2 - u1);
         // y part: dudy slots at dual (i, l), l = j, j+1, nonzero for 1 <= l <= NY-2
         T ty = (T)0;
-        if (j >= 1) {
+        if (IN || j >= 1) {
           const T a = (T)0.5 * (vvl[k] + vvc[k + 1]);
           ty += a * (u1 - uuc[k]);
         }
-        if (j + 1 <= NY - 2) {
+        if (IN || j + 1 <= NY - 2) {
           const T a = (T)0.5 * (vvl[k + 1] + vvc[k + 2]);
           ty += a * (uuc[k + 2] - u1);
         }
@@ -223,14 +251,14 @@ __global__ void __launch_bounds__(BX* BY) k_vdu_edges(int NX, int NY, const T* _
     }
     if (v_col) {
       T r = (T)0;
-      if (j >= 1 && j <= NY - 2) {
+      if (IN || (j >= 1 && j <= NY - 2)) {
         // y part: dvdy slots at primal y j-1, j (column i)
         const T u0 = uvc[k], u1 = uvc[k + 1], u2 = uvc[k + 2];
         const T v0 = vvc[k], v1 = vvc[k + 1], v2 = vvc[k + 2];
         const T ty = (T)0.5 * (v0 + v1) * (u1 - u0) + (T)0.5 * (v1 + v2) * (u2 - u1);
         // x part: dvdx slots at dual (k, j), k = i, i+1, nonzero for 1 <= k <= NX-2
         T tx = (T)0;
-        if (i >= 1) {
+        if (IN || i >= 1) {
           const T a = (T)0.5 * (vuc[k] + vuc[k + 1]);
           tx += a * (u1 - uvl[k]);
         }
@@ -245,20 +273,33 @@ __global__ void __launch_bounds__(BX* BY) k_vdu_edges(int NX, int NY, const T* _
   }
 }
 
+// FP32: at most 64 registers, four CTAs per SM (32 bytes of spills; the
+// kernel is issue-limited, and 80 registers left three CTAs per SM: 53% ->
+// 55% of HBM on 4096^2); FP64 keeps its 128 registers
+template <typename T>
+__global__ void __launch_bounds__(BX* BY, sizeof(T) == 4 ? 4 : 2) k_vdu_edges(int NX, int NY, const T* __restrict__ vu,
+    const T* __restrict__ vv, const T* __restrict__ uu, const T* __restrict__ uv, T* __restrict__ ou,
+    T* __restrict__ ov, T sc) {
+  if (inner_block(NX, NY))
+    vdu_edges_rows<T, true>(NX, NY, vu, vv, uu, uv, ou, ov, sc);
+  else
+    vdu_edges_rows<T, false>(NX, NY, vu, vv, uu, uv, ou, ov, sc);
+}
+
 // w x v (:419-434): out.u = mean_y(-mean_x(v.v) w), out.v = mean_x(mean_y(v.u) w),
 // the inner means onto the non-ghost dual nodes only.  Thread (i, j) writes
 // out.u(i, j) (j <= NY-2) and out.v(i, j) (i <= NX-2).
 // RY consecutive rows per thread (jb .. jb+RY-1), vertical neighbours shared
 // in registers, every load issued before the arithmetic.
-template <typename T>
-__global__ void __launch_bounds__(BX* BY) k_w_cross_v(int NX, int NY, const T* __restrict__ w,
+template <typename T, bool IN>
+__device__ __forceinline__ void w_cross_v_rows(int NX, int NY, const T* __restrict__ w,
     const T* __restrict__ vu, const T* __restrict__ vv, T* __restrict__ ou, T* __restrict__ ov) {
   const int m = NX - 1;
   const int i = blockIdx.x * BX + threadIdx.x;
   const int jb = (blockIdx.y * BY + threadIdx.y) * RY;
-  if (i >= NX || jb >= NY) return;
-  const bool u_in = i >= 1 && i <= NX - 2;  // out.u nonzero in this column
-  const bool v_col = i <= NX - 2;           // out.v has this column
+  if (!IN && (i >= NX || jb >= NY)) return;
+  const bool u_in = IN || (i >= 1 && i <= NX - 2);  // out.u nonzero in this column
+  const bool v_col = IN || i <= NX - 2;             // out.v has this column
   // wc: w column i rows jb .. jb+RY; wr: w column i+1 rows jb .. jb+RY-1;
   // vl, vr: vv columns i-1, i rows jb .. jb+RY; ua, ub: vu columns i, i+1
   // rows jb-1 .. jb+RY-1
@@ -266,12 +307,12 @@ __global__ void __launch_bounds__(BX* BY) k_w_cross_v(int NX, int NY, const T* _
 #pragma unroll
   for (int k = 0; k < RY + 1; ++k) {
     const int j = jb + k;
-    const bool row = j < NY;
+    const bool row = IN || j < NY;
     wc[k] = row ? ld(w, j * NX + i) : (T)0;
     vl[k] = (row && u_in) ? ld(vv, j * m + i - 1) : (T)0;
     vr[k] = (row && u_in) ? ld(vv, j * m + i) : (T)0;
     const int jv = j - 1;
-    const bool vrow = v_col && jv >= 0 && jv <= NY - 2;
+    const bool vrow = IN || (v_col && jv >= 0 && jv <= NY - 2);
     ua[k] = vrow ? ld(vu, jv * NX + i) : (T)0;
     ub[k] = vrow ? ld(vu, jv * NX + i + 1) : (T)0;
     if (k < RY) wr[k] = (row && v_col) ? ld(w, j * NX + i + 1) : (T)0;
@@ -279,7 +320,7 @@ __global__ void __launch_bounds__(BX* BY) k_w_cross_v(int NX, int NY, const T* _
 #pragma unroll
   for (int k = 0; k < RY; ++k) {
     const int j = jb + k;
-    if (j <= NY - 2) {
+    if (IN || j <= NY - 2) {
       T r = (T)0;
       if (u_in) {
         const T vd0 = (T)0.5 * (vl[k] + vr[k]);
@@ -288,9 +329,9 @@ __global__ void __launch_bounds__(BX* BY) k_w_cross_v(int NX, int NY, const T* _
       }
       ou[j * NX + i] = r;
     }
-    if (v_col && j < NY) {
+    if (IN || (v_col && j < NY)) {
       T r = (T)0;
-      if (j >= 1 && j <= NY - 2) {
+      if (IN || (j >= 1 && j <= NY - 2)) {
         const T ud0 = (T)0.5 * (ua[k] + ua[k + 1]);
         const T ud1 = (T)0.5 * (ub[k] + ub[k + 1]);
         r = (T)0.5 * (ud0 * wc[k] + ud1 * wr[k]);
@@ -298,6 +339,15 @@ __global__ void __launch_bounds__(BX* BY) k_w_cross_v(int NX, int NY, const T* _
       ov[j * m + i] = r;
     }
   }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(BX* BY) k_w_cross_v(int NX, int NY, const T* __restrict__ w,
+    const T* __restrict__ vu, const T* __restrict__ vv, T* __restrict__ ou, T* __restrict__ ov) {
+  if (inner_block(NX, NY))
+    w_cross_v_rows<T, true>(NX, NY, w, vu, vv, ou, ov);
+  else
+    w_cross_v_rows<T, false>(NX, NY, w, vu, vv, ou, ov);
 }
 
 }  // namespace
