@@ -327,18 +327,20 @@ struct ilm_batch_s {
   // body segments as local indices
   int band_k = -1;
   DevBuf band, lseg_start, lseg_len;
-  DevBuf arena_learned;  // body segments of the learned preconditioner
+  DevBuf arena_learned;      // body segments of the learned preconditioner
+  DevBuf arena_learned_tmp;  // its set-up's scratch (features, band before the scatter), kept for reuse
   std::vector<char> has_band;  // problems whose kind a network was set for
   // coarse correction of block-Jacobi on the bodies' constants
   // (ilm_batch_set_coarse): per problem the bodies (0: off), their
   // CG_COARSE_MAX + 1 local starts and E^-1 (CG_COARSE_MAX^2, row-major)
   std::vector<int> coarse_nb, coarse_start;
   std::vector<double> coarse_Einv;
-  // deflation of the Dirichlet net-charge mode (set up before the first solve)
+  // deflation of the Dirichlet net-charge mode (set up before the first
+  // solve): S 1 for every point, and per problem 1 / (1^T W S 1) when that
+  // is negative (0: no deflation)
   bool defl_ready = false;
-  double defl_tol = 0.0;  // tolerance the deflation vectors were solved to
-  std::vector<double> defl_gamma, defl_uz;
-  DevBuf defl_z;
+  std::vector<double> defl_inv_e;
+  DevBuf defl_sz;
   // host copies of the points (features of the learned preconditioner)
   std::vector<double> hx, hy, hnx, hny, hds;
   DevBuf dpoff;  // point offsets on the device (Schur products)
@@ -367,7 +369,12 @@ struct ilm_batch_s {
   // stage A, and its scratch allocated before stage A is issued (cudaMalloc
   // and cudaFree may synchronise the device)
   cudaStream_t s_setup = nullptr;
-  DevBuf lz_bjtasks, lz_ones, lz_y, lz_rhs, lz_its, lz_rr, lz_prm, lz_soff;
+  DevBuf lz_bjtasks, lz_ones, lz_soff;
+  // block-Jacobi inverses: formed on their own stream beside the first
+  // solve's stage A and deflation set-up; the CG launches that read them
+  // wait for bj_ready (wait_bj)
+  cudaStream_t s_bj = nullptr;
+  cudaEvent_t bj_ready = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   ilm_batch_s* twin = nullptr;
   DevBuf ref_in, ref_b, ref_x, ref_r, ref_y, ref_norm, dsoff;
@@ -377,7 +384,15 @@ struct ilm_batch_s {
   // views into two arenas (one allocation and one host->device copy each)
   DevBuf arena_geom, arena_tasks;
   DevBuf px, py, ph;  // point coordinates (FP64) and per-problem h on the device
+  // set while the Schur build of ilm_batch_create may still be running: it
+  // continues past the call's return, and every launch that reads S waits
+  // for this event (wait_schur)
+  cudaEvent_t schur_ready = nullptr;
   ~ilm_batch_s() {
+    if (schur_ready) {
+      cudaEventSynchronize(schur_ready);
+      cudaEventDestroy(schur_ready);
+    }
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
     if (gexec) cudaGraphExecDestroy(gexec);
@@ -385,6 +400,11 @@ struct ilm_batch_s {
     if (ev_join) cudaEventDestroy(ev_join);
     if (s2) cudaStreamDestroy(s2);
     if (s_setup) cudaStreamDestroy(s_setup);
+    if (bj_ready) {
+      cudaEventSynchronize(bj_ready);
+      cudaEventDestroy(bj_ready);
+    }
+    if (s_bj) cudaStreamDestroy(s_bj);
     delete twin;
   }
 };
@@ -417,7 +437,7 @@ int up_typed(DevBuf& b, const std::vector<double>& v, int dtype) {
     }                          \
   } while (0)
 
-int ensure_deflation(ilm_batch_s* b, double tol);
+int ensure_deflation(ilm_batch_s* b);
 
 struct CoarseTask {
   const float* Shi;  // n x n row-major float-float (leading dimension schur_ld(n))
@@ -489,6 +509,49 @@ bool small_inverse(int k, const double* A, double* Ainv) {
   return true;
 }
 
+// Order work on stream st after the batch's Schur build (ilm_batch_create
+// returns while it runs): a device-side wait on its event, or a host wait
+// when st is being captured (the capture takes no dependency on work outside
+// it).  Once the build is known to be done the event is dropped.
+int wait_schur_host(ilm_batch_s* b) {
+  if (!b->schur_ready) return ILM_OK;
+  ILM_CHECK_CUDA(cudaEventSynchronize(b->schur_ready));
+  cudaEventDestroy(b->schur_ready);
+  b->schur_ready = nullptr;
+  return ILM_OK;
+}
+
+int wait_schur(ilm_batch_s* b, cudaStream_t st) {
+  if (!b->schur_ready) return ILM_OK;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  ILM_CHECK_CUDA(cudaStreamIsCapturing(st, &cs));
+  if (cs != cudaStreamCaptureStatusNone) return wait_schur_host(b);
+  const cudaError_t q = cudaEventQuery(b->schur_ready);
+  if (q == cudaSuccess) {
+    cudaEventDestroy(b->schur_ready);
+    b->schur_ready = nullptr;
+    return ILM_OK;
+  }
+  if (q != cudaErrorNotReady) ILM_CHECK_CUDA(q);
+  if (cudaPeekAtLastError() == cudaErrorNotReady) (void)cudaGetLastError();  // a status, not a launch error
+  ILM_CHECK_CUDA(cudaStreamWaitEvent(st, b->schur_ready, 0));
+  return ILM_OK;
+}
+
+// Order work on stream st after the block-Jacobi inverses issued so far
+// (a host wait when st is being captured)
+int wait_bj(ilm_batch_s* b, cudaStream_t st) {
+  if (!b->bj_ready) return ILM_OK;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  ILM_CHECK_CUDA(cudaStreamIsCapturing(st, &cs));
+  if (cs != cudaStreamCaptureStatusNone) {
+    ILM_CHECK_CUDA(cudaEventSynchronize(b->bj_ready));
+    return ILM_OK;
+  }
+  ILM_CHECK_CUDA(cudaStreamWaitEvent(st, b->bj_ready, 0));
+  return ILM_OK;
+}
+
 int ensure_setup_stream(ilm_batch_s* b) {
   if (!b->s_setup) ILM_CHECK_CUDA(cudaStreamCreateWithFlags(&b->s_setup, cudaStreamNonBlocking));
   return ILM_OK;
@@ -508,13 +571,16 @@ int ensure_block_inverses(ilm_batch_s* b) {
   }
   if (todo.empty()) return ILM_OK;
   const auto t0 = std::chrono::steady_clock::now();
-  ILM_TRY(ensure_setup_stream(b));
+  if (!b->s_bj) ILM_CHECK_CUDA(cudaStreamCreateWithFlags(&b->s_bj, cudaStreamNonBlocking));
+  if (!b->bj_ready) ILM_CHECK_CUDA(cudaEventCreateWithFlags(&b->bj_ready, cudaEventDisableTiming));
+  ILM_TRY(wait_schur(b, b->s_bj));
   ILM_TRY(b->lz_bjtasks.alloc(todo.size() * sizeof(BJBlockTask)));
+  // (from pageable memory: the copy has read todo when the call returns)
   ILM_CHECK_CUDA(cudaMemcpyAsync(b->lz_bjtasks.p, todo.data(), todo.size() * sizeof(BJBlockTask),
-                                 cudaMemcpyHostToDevice, b->s_setup));
-  ILM_TRY(launch_block_inverse(b->lz_bjtasks.as<BJBlockTask>(), (int)todo.size(), b->bj_max_sz, b->s_setup));
-  ILM_CHECK_CUDA(cudaStreamSynchronize(b->s_setup));
-  b->setup_ms.emplace_back("block-Jacobi inverses",
+                                 cudaMemcpyHostToDevice, b->s_bj));
+  ILM_TRY(launch_block_inverse(b->lz_bjtasks.as<BJBlockTask>(), (int)todo.size(), b->bj_max_sz, b->s_bj));
+  ILM_CHECK_CUDA(cudaEventRecord(b->bj_ready, b->s_bj));
+  b->setup_ms.emplace_back("block-Jacobi inverses (issued; formed on their own stream)",
                            std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
   return ILM_OK;
 }
@@ -523,7 +589,7 @@ int ensure_block_inverses(ilm_batch_s* b) {
 int ensure_cg_params(ilm_batch_s* b, double tol, int maxiter) {
   if (tol == b->cg_tol && maxiter == b->cg_maxiter && !b->params_dirty) return ILM_OK;
   ILM_TRY(ensure_block_inverses(b));
-  ILM_TRY(ensure_deflation(b, tol));
+  ILM_TRY(ensure_deflation(b));
   b->params_dirty = false;
   std::vector<unsigned char> cg((size_t)b->nprob * cgff_params_size());
   const int P = 2 * b->band_k + 1;
@@ -541,7 +607,8 @@ int ensure_cg_params(ilm_batch_s* b, double tol, int maxiter) {
                      pre ? b->bj_size.as<int>() + b->bj_first[p] : nullptr,
                      pre ? b->bj_off.as<int>() + b->bj_first[p] : nullptr, pre ? b->bj_inv.as<float>() : nullptr,
                      pre ? b->bj_inv_lo.as<float>() : nullptr);
-    cgff_params_set_deflation(dst, b->defl_gamma[p], b->defl_z.as<double>() + o, b->defl_uz[p]);
+    cgff_params_set_deflation(dst, b->defl_inv_e[p] != 0.0 ? b->defl_sz.as<double>() + o : nullptr,
+                              b->defl_inv_e[p]);
     cgff_params_set_timing(dst, b->profiling ? b->cgtime.as<unsigned long long>() + 3 * (size_t)p : nullptr);
     if (b->precond == 2 && b->has_band[p])
       cgff_params_set_band(dst, b->band.as<float>() + o * P, b->band_k, b->lseg_start.as<int>() + o,
@@ -578,128 +645,61 @@ __global__ void k_batch_schur_apply(int Ptot, const int* __restrict__ pt2prob, c
   if (lane == 0) y[row] = acc;
 }
 
-// The Dirichlet Schur complement S = -E L^-1 R has one negative eigenvalue:
-// the net-charge mode (the lattice Green's function is normalised with
-// G(0,0) = 0, the logarithmic energy is positive only for neutral charge).
-// CG then runs on S' = S + gamma 1 1^T W, positive definite because S is
-// positive on the W-orthogonal complement of the constants, with
-// gamma = 2 |rho| / 1^T W 1 where rho is the Rayleigh quotient of the
-// constants; z = S'^-1 1 (solved once here) gives S^-1 by Sherman-Morrison.
 // Scratch of the lazy set-up, allocated before a solve issues its stage A
+// (cudaMalloc and cudaFree may synchronise the device)
 int prepare_lazy_setup(ilm_batch_s* b) {
-  const int Ptot = b->Ptot, np = b->nprob;
+  const int Ptot = b->Ptot;
   ILM_TRY(ensure_setup_stream(b));
-  ILM_TRY(b->defl_z.alloc((size_t)std::max(Ptot, 1) * sizeof(double)));
-  for (DevBuf* d : {&b->lz_ones, &b->lz_y, &b->lz_rhs}) ILM_TRY(d->alloc((size_t)std::max(Ptot, 1) * sizeof(double)));
-  ILM_TRY(b->lz_its.alloc((size_t)std::max(np, 1) * sizeof(int)));
-  ILM_TRY(b->lz_rr.alloc((size_t)std::max(np, 1) * sizeof(double)));
-  ILM_TRY(b->lz_prm.alloc((size_t)std::max(np, 1) * cgff_params_size()));
+  ILM_TRY(b->defl_sz.alloc((size_t)std::max(Ptot, 1) * sizeof(double)));
+  ILM_TRY(b->lz_ones.alloc((size_t)std::max(Ptot, 1) * sizeof(double)));
   ILM_TRY(b->lz_soff.alloc(b->soff.size() * sizeof(size_t)));
   if (!b->dpoff.p) ILM_TRY(up(b->dpoff, b->poff));
   if (b->bj_block > 0) ILM_TRY(b->lz_bjtasks.alloc(std::max<size_t>(b->bj_tasks_host.size(), 1) * sizeof(BJBlockTask)));
   return ILM_OK;
 }
 
-// Deflation of the Dirichlet net-charge mode: gamma per problem from S 1, and
-// z = S'^-1 1 with S' = S + gamma 1 1^T W, to 1e-2 of the requested solve
-// tolerance (between 1e-12 and 1e-10: z enters x = y + gamma t z
-// linearly); a later, tighter request re-solves z warm-started from the
-// current one.  Runs on the set-up stream (the host waits for that stream
-// only), so it overlaps the first solve's stage A.
-int ensure_deflation(ilm_batch_s* b, double tol) {
-  const double ztol = std::min(1e-10, std::max(1e-12, 1e-2 * tol));
-  if (b->defl_ready && b->defl_tol <= ztol) return ILM_OK;
-  const bool refresh = b->defl_ready;
+// The Dirichlet Schur complement S = -E L^-1 R has one negative eigenvalue:
+// the net-charge mode (the lattice Green's function is normalised with
+// G(0,0) = 0, the logarithmic energy is positive only for neutral charge);
+// plain CG on it can break down.  Where E = 1^T W S 1 < 0 the constants see
+// that mode, and the CG deflates them (deflated CG on Z = 1, CGFFParams::sz):
+// S is positive definite on the S-orthogonal complement of 1 because E takes
+// the one negative eigenvalue (inertia additivity).  The set-up is S 1 and
+// E per problem, once per batch (it does not depend on the tolerance), on
+// the set-up stream, so it overlaps the first solve's stage A.
+int ensure_deflation(ilm_batch_s* b) {
+  if (b->defl_ready) return ILM_OK;
   const auto t0 = std::chrono::steady_clock::now();
   const int Ptot = b->Ptot, np = b->nprob;
-  ILM_TRY(prepare_lazy_setup(b));
-  cudaStream_t ss = b->s_setup;
-  std::vector<double> rhs(Ptot, 0.0);
-  if (!refresh) {
-  b->defl_gamma.assign(np, 0.0);
-  b->defl_uz.assign(np, 0.0);
-  ILM_CHECK_CUDA(cudaMemsetAsync(b->defl_z.p, 0, (size_t)std::max(Ptot, 1) * sizeof(double), ss));
+  b->defl_inv_e.assign(np, 0.0);
   bool any = false;
   for (int p = 0; p < np; ++p) any |= b->probs[p].kind == 0;
   if (!any) {
-    ILM_CHECK_CUDA(cudaStreamSynchronize(ss));
     b->defl_ready = true;
-    b->defl_tol = 0.0;
     return ILM_OK;
   }
-  std::vector<double> ones(Ptot, 1.0), y(Ptot);
+  ILM_TRY(prepare_lazy_setup(b));
+  cudaStream_t ss = b->s_setup;
+  ILM_TRY(wait_schur(b, ss));
+  std::vector<double> ones(Ptot, 1.0), sz(Ptot);
   ILM_CHECK_CUDA(cudaMemcpyAsync(b->lz_ones.p, ones.data(), (size_t)Ptot * sizeof(double), cudaMemcpyHostToDevice, ss));
   ILM_CHECK_CUDA(cudaMemcpyAsync(b->lz_soff.p, b->soff.data(), b->soff.size() * sizeof(size_t),
                                  cudaMemcpyHostToDevice, ss));
   k_batch_schur_apply<<<(Ptot * 32 + 255) / 256, 256, 0, ss>>>(Ptot, b->pt2prob.as<int>(), b->dpoff.as<size_t>(),
                                                                b->Shi.as<float>(), b->Slo.as<float>(),
                                                                b->lz_soff.as<size_t>(), b->lz_ones.as<double>(),
-                                                               b->lz_y.as<double>());
+                                                               b->defl_sz.as<double>());
   ILM_CHECK_LAUNCH();
-  ILM_CHECK_CUDA(cudaMemcpyAsync(y.data(), b->lz_y.p, (size_t)Ptot * sizeof(double), cudaMemcpyDeviceToHost, ss));
+  ILM_CHECK_CUDA(cudaMemcpyAsync(sz.data(), b->defl_sz.p, (size_t)Ptot * sizeof(double), cudaMemcpyDeviceToHost, ss));
   ILM_CHECK_CUDA(cudaStreamSynchronize(ss));
   for (int p = 0; p < np; ++p) {
     if (b->probs[p].kind != 0) continue;
-    double su = 0.0, sy = 0.0;
-    for (size_t k = b->poff[p]; k < b->poff[p + 1]; ++k) {
-      su += b->hds[k];
-      sy += b->hds[k] * y[k];
-    }
-    const double rho = sy / su;
-    if (rho < 0.0) b->defl_gamma[p] = 2.0 * fabs(rho) / su;
-  }
-  }
-  // z = S'^-1 1 for the problems with a deflation shift (the others never
-  // read z: their right-hand side is 0 and their CG returns at once)
-  bool need = false;
-  for (int p = 0; p < np; ++p) {
-    if (b->defl_gamma[p] != 0.0)
-      for (size_t k = b->poff[p]; k < b->poff[p + 1]; ++k) rhs[k] = 1.0;
-    need |= b->defl_gamma[p] != 0.0;
-  }
-  if (!need) {
-    b->defl_ready = true;
-    b->defl_tol = 0.0;
-    return ILM_OK;
-  }
-  ILM_CHECK_CUDA(cudaMemcpyAsync(b->lz_rhs.p, rhs.data(), (size_t)Ptot * sizeof(double), cudaMemcpyHostToDevice, ss));
-  std::vector<unsigned char> cg((size_t)np * cgff_params_size());
-  for (int p = 0; p < np; ++p) {
-    const size_t o = b->poff[p];
-    void* dst = cg.data() + (size_t)p * cgff_params_size();
-    // the best preconditioner set up so far: the learned band, else
-    // block-Jacobi (each shortens this tight solve several times)
-    const bool band = b->band_k >= 0 && !b->has_band.empty() && b->has_band[p];
-    const bool pre = !band && b->bj_block > 0 && !b->bj_have.empty() && b->bj_have[p];
-    cgff_params_fill(dst, b->Shi.as<float>() + b->soff[p], b->Slo.as<float>() + b->soff[p],
-                     b->lz_rhs.as<double>() + o, b->defl_z.as<double>() + o, b->ds64.as<double>() + o,
-                     b->probs[p].npts, 20000, ztol, b->lz_its.as<int>() + p, b->lz_rr.as<double>() + p,
-                     pre ? b->bj_blk.as<int>() + o : nullptr, pre ? b->bj_start.as<int>() + b->bj_first[p] : nullptr,
-                     pre ? b->bj_size.as<int>() + b->bj_first[p] : nullptr,
-                     pre ? b->bj_off.as<int>() + b->bj_first[p] : nullptr, pre ? b->bj_inv.as<float>() : nullptr,
-                     pre ? b->bj_inv_lo.as<float>() : nullptr);
-    cgff_params_set_deflation(dst, b->defl_gamma[p], nullptr, 0.0);
-    if (refresh) cgff_params_set_x0(dst, b->defl_z.as<double>() + o);
-    if (band)
-      cgff_params_set_band(dst, b->band.as<float>() + o * (2 * b->band_k + 1), b->band_k,
-                           b->lseg_start.as<int>() + o, b->lseg_len.as<int>() + o);
-  }
-  ILM_CHECK_CUDA(cudaMemcpyAsync(b->lz_prm.p, cg.data(), cg.size(), cudaMemcpyHostToDevice, ss));
-  ILM_TRY(launch_cg_cluster(b->lz_prm.p, b->order.as<int>(), np, b->counter.as<int>(), b->maxN, b->nclusters, ss,
-                            b->cg_variant));
-  std::vector<double> z(Ptot);
-  ILM_CHECK_CUDA(cudaMemcpyAsync(z.data(), b->defl_z.p, (size_t)Ptot * sizeof(double), cudaMemcpyDeviceToHost, ss));
-  ILM_CHECK_CUDA(cudaStreamSynchronize(ss));
-  for (int p = 0; p < np; ++p) {
-    if (b->defl_gamma[p] == 0.0) continue;
-    double uz = 0.0;
-    for (size_t k = b->poff[p]; k < b->poff[p + 1]; ++k) uz += b->hds[k] * z[k];
-    b->defl_uz[p] = uz;
+    double e = 0.0;
+    for (size_t k = b->poff[p]; k < b->poff[p + 1]; ++k) e += b->hds[k] * sz[k];
+    if (e < 0.0) b->defl_inv_e[p] = 1.0 / e;
   }
   b->defl_ready = true;
-  b->defl_tol = ztol;
-  b->params_dirty = true;  // uz changed
-  b->setup_ms.emplace_back("deflation vectors (Dirichlet problems with a net-charge shift)",
+  b->setup_ms.emplace_back("deflation: S 1 and 1^T W S 1 (Dirichlet problems)",
                            std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
   return ILM_OK;
 }
@@ -800,6 +800,8 @@ int ensure_split(ilm_batch_s* b) {
 
 // The Schur CG of every problem: rhs64 -> x64 (parameters set by ensure_cg_params)
 int batch_cg(ilm_batch_s* b, cudaStream_t st) {
+  ILM_TRY(wait_schur(b, st));
+  ILM_TRY(wait_bj(b, st));
   if (b->cg_variant == 6) {
     ILM_TRY(ensure_split(b));
     if (b->n_small > 0 && b->n_large > 0) {
@@ -1515,9 +1517,13 @@ int batch_create_impl(int nprob, const ilm_batch_problem_t* probs, const double*
   ILM_TRY(TA.commit_upload(B->arena_tasks, sg));
 
   phase("stage tasks (build and upload)");
-  ILM_CHECK_CUDA(cudaStreamSynchronize(ss));
   ILM_CHECK_CUDA(cudaStreamSynchronize(sg));
-  phase("Schur complements (device, overlapping the host's task tables)");
+  if (build_schur) {
+    // the Schur build runs on past the return (its stream is released once
+    // the build ends); the launches that read S wait for this event
+    ILM_CHECK_CUDA(cudaEventCreateWithFlags(&B->schur_ready, cudaEventDisableTiming));
+    ILM_CHECK_CUDA(cudaEventRecord(B->schur_ready, ss));
+  }
   *out = guard.release();
   return ILM_OK;
 }
@@ -1722,6 +1728,8 @@ int ilm_batch_set_precond(ilm_batch_t b, int mode, int block_size) {
   if (mode == 1) {
     ILM_REQUIRE(block_size >= 4 && block_size <= 72, "batch: block size %d outside [4, 72]", block_size);
     if (b->bj_block != block_size) {
+      // inverses still being formed write into the arrays rebuilt here
+      if (b->bj_ready) ILM_CHECK_CUDA(cudaEventSynchronize(b->bj_ready));
       // blocks of ~block_size consecutive points (at most 1.5 x block_size);
       // their inverses are formed by the next solve, for the problems whose
       // preconditioner uses them (ensure_block_inverses)
@@ -1856,6 +1864,8 @@ int ilm_batch_solve_graph(ilm_batch_t b, const void* fplus, const void* fminus, 
   cudaStream_t st = as_stream(stream);
   ILM_REQUIRE(st != nullptr, "batch_solve_graph: needs a created stream (the legacy default stream cannot be captured)");
   ILM_TRY(ensure_cg_params(b, tol, maxiter));
+  ILM_TRY(wait_schur_host(b));
+  if (b->bj_ready) ILM_CHECK_CUDA(cudaEventSynchronize(b->bj_ready));
   const void* key[4] = {fplus, fminus, f_out, s_out};
   bool reuse = b->gexec && b->gtol == tol && b->gmaxiter == maxiter && b->ggen == b->param_gen;
   for (int i = 0; i < 4 && reuse; ++i) reuse = key[i] == b->gkey[i];
@@ -2058,6 +2068,7 @@ int ilm_batch_set_coarse(ilm_batch_t b, int kind_mask, const int* body_start) {
   DevBuf dt, dE;
   ILM_TRY(up(dt, tasks));
   ILM_TRY(dE.alloc(tasks.size() * COARSE_SPLIT * M * M * sizeof(double)));
+  ILM_TRY(wait_schur(b, nullptr));
   k_coarse_E<<<(unsigned)(tasks.size() * COARSE_SPLIT), 256>>>(dt.as<CoarseTask>(), dE.as<double>());
   ILM_CHECK_LAUNCH();
   std::vector<double> E(tasks.size() * COARSE_SPLIT * M * M);
@@ -2131,15 +2142,17 @@ int ilm_batch_set_learned(ilm_batch_t b, ilm_net_t net, int kind_mask, const int
     }
   }
   const int Nsel = (int)c2o.size();
-  DevBuf tmp_arena, d_c2o, d_sst, d_sln, dfeat, tmp;
+  DevBuf d_c2o, d_sst, d_sln, dfeat, tmp;
   {
-    ArenaBuilder A;  // this call's temporaries
+    // this call's temporaries, in an arena the batch keeps (freeing device
+    // memory would wait for the whole device, the Schur build included)
+    ArenaBuilder A;
     A.add(&d_c2o, c2o);
     A.add(&d_sst, sst_c);
     A.add(&d_sln, sln_c);
     A.add(&dfeat, (size_t)std::max(Nsel, 1) * 8 * sizeof(float));
     A.add(&tmp, (size_t)std::max(Nsel, 1) * P * sizeof(float));
-    ILM_TRY(A.commit(tmp_arena, nullptr));
+    ILM_TRY(A.commit(b->arena_learned_tmp, nullptr));
     ArenaBuilder S;  // the body segments the CG reads (the same for every call)
     S.add(&b->lseg_start, ls);
     S.add(&b->lseg_len, ll);
@@ -2159,7 +2172,9 @@ int ilm_batch_set_learned(ilm_batch_t b, ilm_net_t net, int kind_mask, const int
                                                                      b->band.as<float>());
     ILM_CHECK_LAUNCH();
   }
-  ILM_CHECK_CUDA(cudaDeviceSynchronize());
+  // the features, the network and the band scatter ran on the legacy
+  // default stream, which does not wait for the (non-blocking) Schur build
+  ILM_CHECK_CUDA(cudaStreamSynchronize(nullptr));
   ILM_TRY(net_check_tc(net));
   phase("learned: features and network inference (device, selected problems)");
   b->band_k = K;
@@ -2176,6 +2191,7 @@ int ilm_batch_schur_apply(ilm_batch_t b, const double* x, double* y, ilm_stream_
   DevBuf dsoff;
   ILM_TRY(up(dsoff, b->soff));
   cudaStream_t st = as_stream(stream);
+  ILM_TRY(wait_schur(b, st));
   k_batch_schur_apply<<<(b->Ptot * 32 + 255) / 256, 256, 0, st>>>(b->Ptot, b->pt2prob.as<int>(),
                                                                   b->dpoff.as<size_t>(), b->Shi.as<float>(),
                                                                   b->Slo.as<float>(), dsoff.as<size_t>(), x, y);
@@ -2191,6 +2207,8 @@ int ilm_batch_schur_solve(ilm_batch_t b, const double* rhs, double* x, double to
   cudaStream_t st = as_stream(stream);
   ILM_TRY(ensure_cg_params(b, tol, maxiter));
   ILM_CHECK_CUDA(cudaMemcpyAsync(b->rhs64.p, rhs, (size_t)b->Ptot * 8, cudaMemcpyDeviceToDevice, st));
+  ILM_TRY(wait_schur(b, st));
+  ILM_TRY(wait_bj(b, st));
   ILM_TRY(launch_cg_cluster(b->cgp.p, b->order.as<int>(), b->nprob, b->counter.as<int>(), b->maxN, b->nclusters, st,
                             b->cg_variant));
   ILM_CHECK_CUDA(cudaMemcpyAsync(x, b->x64.p, (size_t)b->Ptot * 8, cudaMemcpyDeviceToDevice, st));

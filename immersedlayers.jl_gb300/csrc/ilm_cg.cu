@@ -106,14 +106,17 @@ struct CGFFParams {
   int band_k;
   const int* seg_start;
   const int* seg_len;
-  // optional rank-one deflation of the negative (net-charge) mode of the
-  // Dirichlet Schur complement: CG runs on S' = S + gamma 1 1^T W (SPD) and
-  // x = y + gamma t z, t = 1^T W y / (1 - gamma 1^T W z), z = S'^-1 1
-  // (Sherman-Morrison); gamma = 0: off.  zdef == nullptr: no correction
-  // (the solve for z itself).
-  double gamma;
-  const double* zdef;
-  double uz;
+  // optional deflation of the negative (net-charge) mode of the Dirichlet
+  // Schur complement by deflated CG on Z = 1 (Nicolaides 1987; Saad, Yeung,
+  // Erhel and Guyomarc'h 2000): sz = S 1 (this problem's rows) and
+  // inv_e = 1 / E, E = 1^T W S 1 < 0.  S has one negative eigenvalue and E
+  // takes it, so S is positive definite on the S-orthogonal complement of 1
+  // (inertia additivity of the Schur complement).  x0 is corrected by
+  // (1^T W r0 / E) 1 so that 1^T W r0 = 0, and every search direction is
+  // kept S-orthogonal to 1, p <- p - ((S 1)^T W p / E) 1, which keeps
+  // 1^T W r = 0.  sz == nullptr: off.
+  const double* sz;
+  double inv_e;
   // optional: global-timer stamps (ns) when the problem is taken and done,
   // and the SM of the cluster's first CTA (profiling)
   unsigned long long* tspan;
@@ -357,6 +360,18 @@ __device__ __forceinline__ void apply_precond_full(const CGFFParams& pr, int n, 
   else apply_bjacobi(pr, 0, n, S.vhi, S.vlo, z);
 }
 
+// deflation of a whole search direction (sz = S 1, inv_e = 1 / 1^T W S 1):
+// p -= ((S 1)^T W p / E) 1, each thread its own entries (no-op without sz)
+__device__ __forceinline__ void deflate_full(const double* sz, double inv_e, const double* w, double* p, int n,
+                                             double* red) {
+  if (!sz) return;
+  double m = 0.0, unused = 0.0;
+  for (int j = threadIdx.x; j < n; j += blockDim.x) m += w[j] * __ldg(sz + j) * p[j];
+  block_sum2(m, unused, red);
+  m *= inv_e;
+  for (int j = threadIdx.x; j < n; j += blockDim.x) p[j] -= m;
+}
+
 __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(CGR_THREADS, 3)
     k_cg_rep(const CGFFParams* __restrict__ P, const int* __restrict__ order, int nprob, int* counter, int max_n) {
   cg::cluster_group cl = cg::this_cluster();
@@ -402,22 +417,27 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(CGR_THREADS
       w[j] = pr.w ? pr.w[j] : 1.0;
     }
     __syncthreads();
-    if (pr.x0) {  // warm start: r = b - S' x0
+    if (pr.x0) {  // warm start: r = b - S x0
       split_full(x, n, ld, S.vhi, S.vlo);
       __syncthreads();
       const double* t = exchange_matvec(cl, pr, S, xsel, n, rows, rank, r0, r1);
-      double c0 = 0.0;
-      if (pr.gamma != 0.0) {
-        double unused = 0.0;
-        for (int j = threadIdx.x; j < n; j += blockDim.x) c0 += w[j] * x[j];
-        block_sum2(c0, unused, red);
-        c0 *= pr.gamma;
-      }
-      for (int j = threadIdx.x; j < n; j += blockDim.x) r[j] = pr.b[j] - t[j] - c0;
+      for (int j = threadIdx.x; j < n; j += blockDim.x) r[j] = pr.b[j] - t[j];
     } else {
       for (int j = threadIdx.x; j < n; j += blockDim.x) r[j] = pr.b[j];
     }
     __syncthreads();
+    const double* sz = pr.sz;  // deflation (as k_cg_cluster): S 1, whole vector
+    if (sz) {  // x += c 1, r -= c S 1, c = 1^T W r / E
+      double c = 0.0, unused = 0.0;
+      for (int j = threadIdx.x; j < n; j += blockDim.x) c += w[j] * r[j];
+      block_sum2(c, unused, red);
+      c *= pr.inv_e;
+      for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        x[j] += c;
+        r[j] -= c * __ldg(sz + j);
+      }
+      __syncthreads();
+    }
     const bool pre = pr.blk != nullptr || pr.band != nullptr;
     double bb = 0.0, rz = 0.0;
     for (int j = threadIdx.x; j < n; j += blockDim.x) {
@@ -433,11 +453,9 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(CGR_THREADS
       __syncthreads();
     }
     for (int j = threadIdx.x; j < n; j += blockDim.x) p[j] = pre ? z[j] : r[j];
+    deflate_full(sz, pr.inv_e, w, p, n, red);
     const double bnorm = sqrt(bb);
-    // with the net-charge mode deflated, CG converges on S' and the reported
-    // residual is the true one of S after the Sherman-Morrison correction,
-    // which adds the (small) error of z: aim at half the tolerance on S'
-    const double thr = (pr.zdef != nullptr && pr.gamma != 0.0 ? 0.5 : 1.0) * pr.tol * bnorm;
+    const double thr = pr.tol * bnorm;
     const double thr2 = thr * thr;
     double rlast = bb;  // latest squared residual norm (recursive or true)
     int it = 0;
@@ -453,14 +471,6 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(CGR_THREADS
       split_full(p, n, ld, S.vhi, S.vlo);
       __syncthreads();
       double* qv = exchange_matvec(cl, pr, S, xsel, n, rows, rank, r0, r1);
-      if (pr.gamma != 0.0) {  // q = S' p
-        double cp = 0.0, unused = 0.0;
-        for (int j = threadIdx.x; j < n; j += blockDim.x) cp += w[j] * p[j];
-        block_sum2(cp, unused, red);
-        cp *= pr.gamma;
-        for (int j = threadIdx.x; j < n; j += blockDim.x) qv[j] += cp;
-        __syncthreads();
-      }
       double pq = 0.0, pr_ = 0.0;
       for (int j = threadIdx.x; j < n; j += blockDim.x) {
         pq += w[j] * p[j] * qv[j];
@@ -481,20 +491,13 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(CGR_THREADS
       ++it;
       rlast = rr;
       if (rr <= thr2 || (it % 50) == 0 || it == pr.maxiter) {
-        // true residual b - S' x (exchange through the other buffer: q = S p stays)
+        // true residual b - S x (exchange through the other buffer: q = S p stays)
         split_full(x, n, ld, S.vhi, S.vlo);
         __syncthreads();
         const double* t = exchange_matvec(cl, pr, S, xsel, n, rows, rank, r0, r1);
-        double cx = 0.0;
-        if (pr.gamma != 0.0) {
-          double unused = 0.0;
-          for (int j = threadIdx.x; j < n; j += blockDim.x) cx += w[j] * x[j];
-          block_sum2(cx, unused, red);
-          cx *= pr.gamma;
-        }
         double tr = 0.0, tz = 0.0;
         for (int j = threadIdx.x; j < n; j += blockDim.x) {
-          const double rj = pr.b[j] - t[j] - cx;
+          const double rj = pr.b[j] - t[j];
           r[j] = rj;
           tr += rj * rj;
           tz += w[j] * rj * rj;
@@ -519,6 +522,7 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(CGR_THREADS
         const double beta = fdiv(rzn, rz);
         rz = rzn;
         for (int j = threadIdx.x; j < n; j += blockDim.x) p[j] = r[j] + beta * p[j];
+        deflate_full(sz, pr.inv_e, w, p, n, red);
         __syncthreads();
       } else {
         // flexible CG: z = M r, beta = -(z, q) / (p, q), p = z + beta p
@@ -529,6 +533,7 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(CGR_THREADS
         const double zq = wsum(w, z, qv, n, red);
         const double beta = fdiv(-zq, pq);
         for (int j = threadIdx.x; j < n; j += blockDim.x) p[j] = z[j] + beta * p[j];
+        deflate_full(sz, pr.inv_e, w, p, n, red);
         __syncthreads();
       }
     }
@@ -538,26 +543,6 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(CGR_THREADS
       cl.sync();  // every CTA's rows of the best iterate are in pr.x
       for (int j = threadIdx.x; j < n; j += blockDim.x) x[j] = __ldcg(pr.x + j);
       __syncthreads();
-    }
-    if (pr.zdef != nullptr && pr.gamma != 0.0) {
-      // Sherman-Morrison back to S: x = y + gamma t z, t = 1^T W y / (1 - gamma 1^T W z)
-      double wy = 0.0, unused = 0.0;
-      for (int j = threadIdx.x; j < n; j += blockDim.x) wy += w[j] * x[j];
-      block_sum2(wy, unused, red);
-      const double t = wy / (1.0 - pr.gamma * pr.uz);
-      for (int j = threadIdx.x; j < n; j += blockDim.x) x[j] += pr.gamma * t * pr.zdef[j];
-      __syncthreads();
-      // reported residual: the true one of S x = b
-      split_full(x, n, ld, S.vhi, S.vlo);
-      __syncthreads();
-      const double* tv = exchange_matvec(cl, pr, S, xsel, n, rows, rank, r0, r1);
-      double tr = 0.0;
-      for (int j = threadIdx.x; j < n; j += blockDim.x) {
-        const double d = pr.b[j] - tv[j];
-        tr += d * d;
-      }
-      block_sum2(tr, unused, red);
-      relres = bnorm > 0 ? sqrt(tr) / bnorm : 0.0;
     }
     for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) pr.x[i] = x[i];
     if (rank == 0 && threadIdx.x == 0) {
@@ -930,6 +915,15 @@ __device__ __forceinline__ FF ff_axpy(float bh, float bl, FF p, FF v) {
   return FF{hi, e - (hi - s)};
 }
 
+// a - (mh + ml) in float-float
+__device__ __forceinline__ FF ff_sub_const(FF a, float mh, float ml) {
+  float s, e;
+  two_sum(a.hi, -mh, s, e);
+  e += a.lo - ml;
+  const float hi = s + e;
+  return FF{hi, e - (hi - s)};
+}
+
 // The search direction p is kept whole in every CTA as a float-float vector
 // (ph/pl) and updated there (p = z + beta p over all n points in FP32
 // float-float arithmetic), so the product S p needs no exchange: only r
@@ -937,9 +931,8 @@ __device__ __forceinline__ FF ff_axpy(float bh, float bl, FF p, FF v) {
 // the reduction that needs it anyway.  Plain CG takes two cluster barriers
 // per iteration, flexible CG three.  The owned slice of p is read back as
 // (double)hi + (double)lo, so x, r and the product all use the same p.
-// Sum_j w_j p_j (the deflation term of q = S' p) follows the same recurrence
-// as p from the reduced Sum w z (or Sum w r); it is recomputed from p at
-// every true-residual refresh.
+// With the deflation (pr.sz) the projection of p rides in the reduction of
+// z (or r) that the update needs anyway: no barrier is added.
 template <int NT, int MINB, int CS = CG_CLUSTER>
 __global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(NT, MINB)
     k_cg_cluster(const CGFFParams* __restrict__ P, const int* __restrict__ order, int nprob, int* counter,
@@ -987,7 +980,8 @@ __global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(NT, MINB)
     const int rows = (n + CS - 1) / CS;
     const int r0 = min(n, rank * rows), r1 = min(n, r0 + rows);
     const int nr = r1 - r0;
-    const double gamma = pr.gamma;
+    const double* sz = pr.sz != nullptr ? pr.sz + r0 : nullptr;  // S 1, owned rows (deflation)
+    const double inv_e = pr.inv_e;
     const bool pre = pr.blk != nullptr || pr.band != nullptr;
     for (int i = threadIdx.x; i < nr; i += blockDim.x) {
       xs[i] = pr.x0 ? pr.x0[r0 + i] : 0.0;
@@ -998,44 +992,55 @@ __global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(NT, MINB)
       ph[j] = pl[j] = bh[j] = bl[j] = 0.f;
     }
     __syncthreads();
-    if (pr.x0) {  // warm start: r = b - S' x0 (x through buffer B)
+    if (pr.x0) {  // warm start: r = b - S x0 (x through buffer B)
       double v[1] = {0.0};
-      for (int i = threadIdx.x; i < nr; i += blockDim.x) v[0] += ws[i] * xs[i];
       publish_slice(xs, r0, nr, bh, bl);
-      csum_t0<1, CS>(cl, v, nr, red, pub, slot);
-      if (threadIdx.x == 0) bc[0] = gamma * v[0];
+      csum_t0<1, CS>(cl, v, nr, red, pub, slot);  // the barrier that publishes x
       gather_parts(cl, bh, bl, n, rows, rank);
       matvec_rows_ff(pr, n, r0, r1, bh, bl, yh, yl);
       __syncthreads();
-      const double c0 = bc[0];
-      for (int i = threadIdx.x; i < nr; i += blockDim.x) rs[i] = bs[i] - ((double)yh[i] + (double)yl[i]) - c0;
+      for (int i = threadIdx.x; i < nr; i += blockDim.x) rs[i] = bs[i] - ((double)yh[i] + (double)yl[i]);
       __syncthreads();
     } else {
       for (int i = threadIdx.x; i < nr; i += blockDim.x) rs[i] = bs[i];
       __syncthreads();
     }
-    // |b|^2, (r, r)_W, sum w r; r published with the same barrier
-    double rz, bnorm, wp;
+    if (sz) {  // deflation: x += c 1, r -= c S 1, c = 1^T W r / E (then 1^T W r = 0)
+      double v[1] = {0.0};
+      for (int i = threadIdx.x; i < nr; i += blockDim.x) v[0] += ws[i] * rs[i];
+      csum_t0<1, CS>(cl, v, nr, red, pub, slot);
+      if (threadIdx.x == 0) bc[0] = v[0] * inv_e;
+      __syncthreads();
+      const double c = bc[0];
+      for (int i = threadIdx.x; i < nr; i += blockDim.x) {
+        xs[i] += c;
+        rs[i] -= c * __ldg(sz + i);
+      }
+      __syncthreads();
+    }
+    // |b|^2, (r, r)_W and (S 1)^T W r (the deflation's projection of p = r);
+    // r published with the same barrier
+    double rz, bnorm, mu;
     {
       double v[3] = {0.0, 0.0, 0.0};
       for (int i = threadIdx.x; i < nr; i += blockDim.x) {
         v[0] += bs[i] * bs[i];
         v[1] += ws[i] * rs[i] * rs[i];
-        v[2] += ws[i] * rs[i];
+        if (sz) v[2] += ws[i] * __ldg(sz + i) * rs[i];
       }
       publish_slice(rs, r0, nr, ah, al);
       csum_coarse<3, CS>(cl, pr, v, ws, rs, r0, nr, red, pub, slot, bc);
       if (threadIdx.x == 0) {
         bc[0] = sqrt(v[0]);
         bc[1] = v[1];
-        bc[2] = v[2];
+        bc[2] = v[2] * inv_e;
       }
       gather_parts(cl, ah, al, n, rows, rank);
       bnorm = bc[0];
       rz = bc[1];
-      wp = bc[2];
+      mu = bc[2];
     }
-    if (pre) {  // p = z = M r, exchanged through buffer B (with sum w z)
+    if (pre) {  // p = z = M r (- mu 1), exchanged through buffer B (with (S 1)^T W z)
       if (pr.band) {
         apply_band_rows(pr, n, r0, r1, ah, al, uhi, ulo, ws, zs);
       } else {
@@ -1046,24 +1051,29 @@ __global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(NT, MINB)
       }
       __syncthreads();
       double v[1] = {0.0};
-      for (int i = threadIdx.x; i < nr; i += blockDim.x) v[0] += ws[i] * zs[i];
+      if (sz)
+        for (int i = threadIdx.x; i < nr; i += blockDim.x) v[0] += ws[i] * __ldg(sz + i) * zs[i];
       publish_slice(zs, r0, nr, bh, bl);
       csum_t0<1, CS>(cl, v, nr, red, pub, slot);
-      if (threadIdx.x == 0) bc[2] = v[0];
+      if (threadIdx.x == 0) bc[2] = v[0] * inv_e;
       gather_parts(cl, bh, bl, n, rows, rank);
-      wp = bc[2];
+      mu = bc[2];
+      const float mh = (float)mu, ml = (float)(mu - (double)mh);
       for (int j = threadIdx.x; j < n; j += blockDim.x) {
-        ph[j] = bh[j];
-        pl[j] = bl[j];
+        const FF pj = sz ? ff_sub_const(FF{bh[j], bl[j]}, mh, ml) : FF{bh[j], bl[j]};
+        ph[j] = pj.hi;
+        pl[j] = pj.lo;
       }
     } else {
+      const float mh = (float)mu, ml = (float)(mu - (double)mh);
       for (int j = threadIdx.x; j < n; j += blockDim.x) {
-        ph[j] = ah[j];
-        pl[j] = al[j];
+        const FF pj = sz ? ff_sub_const(FF{ah[j], al[j]}, mh, ml) : FF{ah[j], al[j]};
+        ph[j] = pj.hi;
+        pl[j] = pj.lo;
       }
     }
     __syncthreads();
-    const double thr = (pr.zdef != nullptr && gamma != 0.0 ? 0.5 : 1.0) * pr.tol * bnorm;
+    const double thr = pr.tol * bnorm;
     const double thr2 = thr * thr;
     double rlast = bnorm * bnorm;
     int it = 0;
@@ -1077,16 +1087,15 @@ __global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(NT, MINB)
     int stall = 0;
     for (int i = threadIdx.x; i < nr; i += blockDim.x) pr.x[r0 + i] = xs[i];
     while (!done && it < pr.maxiter) {
-      // q = S' p on the owned rows (p whole in this CTA)
+      // q = S p on the owned rows (p whole in this CTA)
       matvec_rows_ff(pr, n, r0, r1, ph, pl, yh, yl);
       __syncthreads();
       double alpha, pq;
       {
-        const double cp = gamma * wp;
         double v[2] = {0.0, 0.0};
         for (int i = threadIdx.x; i < nr; i += blockDim.x) {
           const double pi = (double)ph[r0 + i] + (double)pl[r0 + i];
-          const double qi = (double)yh[i] + (double)yl[i] + cp;
+          const double qi = (double)yh[i] + (double)yl[i];
           ps[i] = pi;
           qs[i] = qi;
           v[0] += ws[i] * pi * qi;
@@ -1102,7 +1111,7 @@ __global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(NT, MINB)
         alpha = bc[4];
       }
       if (pq == 0.0) break;
-      double rr, rzn, wr;
+      double rr, rzn, mur;  // mur: the deflation's projection of p = r + beta p
       {
         double v[3] = {0.0, 0.0, 0.0};
         for (int i = threadIdx.x; i < nr; i += blockDim.x) {
@@ -1111,58 +1120,52 @@ __global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(NT, MINB)
           rs[i] = ri;
           v[0] += ri * ri;
           v[1] += ws[i] * ri * ri;
-          v[2] += ws[i] * ri;
+          if (sz) v[2] += ws[i] * __ldg(sz + i) * ri;
         }
         publish_slice(rs, r0, nr, ah, al);
         csum_coarse<3, CS>(cl, pr, v, ws, rs, r0, nr, red, pub, slot, bc);
         if (threadIdx.x == 0) {
           bc[5] = v[0];
           bc[6] = v[1];
-          bc[7] = v[2];
+          bc[7] = v[2] * inv_e;
         }
         __syncthreads();
         rr = bc[5];
         rzn = bc[6];
-        wr = bc[7];
+        mur = bc[7];
       }
       ++it;
       rlast = rr;
       if (rr <= thr2 || (it % 50) == 0 || it == pr.maxiter) {
-        // true residual b - S' x (x through buffer B; the r published above
-        // is superseded by the refreshed one), and sum w p recomputed
+        // true residual b - S x (x through buffer B; the r published above
+        // is superseded by the refreshed one)
         {
           double v[1] = {0.0};
-          for (int i = threadIdx.x; i < nr; i += blockDim.x) v[0] += ws[i] * xs[i];
           publish_slice(xs, r0, nr, bh, bl);
-          csum_t0<1, CS>(cl, v, nr, red, pub, slot);
-          if (threadIdx.x == 0) bc[8] = gamma * v[0];
+          csum_t0<1, CS>(cl, v, nr, red, pub, slot);  // the barrier that publishes x
           gather_parts(cl, bh, bl, n, rows, rank);
           matvec_rows_ff(pr, n, r0, r1, bh, bl, yh, yl);
           __syncthreads();
         }
-        const double cx = bc[8];
-        double v[4] = {0.0, 0.0, 0.0, 0.0};
+        double v[3] = {0.0, 0.0, 0.0};
         for (int i = threadIdx.x; i < nr; i += blockDim.x) {
-          const double ri = bs[i] - ((double)yh[i] + (double)yl[i]) - cx;
+          const double ri = bs[i] - ((double)yh[i] + (double)yl[i]);
           rs[i] = ri;
           v[0] += ri * ri;
           v[1] += ws[i] * ri * ri;
-          v[2] += ws[i] * ri;
-          v[3] += ws[i] * ps[i];
+          if (sz) v[2] += ws[i] * __ldg(sz + i) * ri;
         }
         publish_slice(rs, r0, nr, ah, al);
-        csum_coarse<4, CS>(cl, pr, v, ws, rs, r0, nr, red, pub, slot, bc);
+        csum_coarse<3, CS>(cl, pr, v, ws, rs, r0, nr, red, pub, slot, bc);
         if (threadIdx.x == 0) {
           bc[9] = v[0];
           bc[10] = v[1];
-          bc[11] = v[2];
-          bc[12] = v[3];
+          bc[11] = v[2] * inv_e;
         }
         __syncthreads();
         const double tr = bc[9];
         rzn = bc[10];
-        wr = bc[11];
-        wp = bc[12];
+        mur = bc[11];
         rlast = tr;
         if (tr <= thr2) {
           done = true;
@@ -1179,15 +1182,18 @@ __global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(NT, MINB)
       }
       // r of every CTA (buffer A), published with the reduction above
       gather_parts(cl, ah, al, n, rows, rank);
-      double beta, wv;
+      // with the deflation the new p is projected: p -= ((S 1)^T W p / E) 1,
+      // where (S 1)^T W p = (S 1)^T W (r or z) (the old p is S-orthogonal to 1)
+      double beta;
       if (!pre) {
         beta = fdiv(rzn, rz);
         rz = rzn;
-        wv = wr;
-        // p = r + beta p
+        // p = r + beta p (- mur 1)
         const float bh_ = (float)beta, bl_ = (float)(beta - (double)bh_);
+        const float mh = (float)mur, ml = (float)(mur - (double)mh);
         for (int j = threadIdx.x; j < n; j += blockDim.x) {
-          const FF pn = ff_axpy(bh_, bl_, FF{ph[j], pl[j]}, FF{ah[j], al[j]});
+          FF pn = ff_axpy(bh_, bl_, FF{ph[j], pl[j]}, FF{ah[j], al[j]});
+          if (sz) pn = ff_sub_const(pn, mh, ml);
           ph[j] = pn.hi;
           pl[j] = pn.lo;
         }
@@ -1205,25 +1211,26 @@ __global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(NT, MINB)
         double v[2] = {0.0, 0.0};
         for (int i = threadIdx.x; i < nr; i += blockDim.x) {
           v[0] += ws[i] * zs[i] * qs[i];
-          v[1] += ws[i] * zs[i];
+          if (sz) v[1] += ws[i] * __ldg(sz + i) * zs[i];
         }
         publish_slice(zs, r0, nr, bh, bl);
         csum_t0<2, CS>(cl, v, nr, red, pub, slot);
         if (threadIdx.x == 0) {
           bc[13] = fdiv(-v[0], pq);
-          bc[14] = v[1];
+          bc[14] = v[1] * inv_e;
         }
         gather_parts(cl, bh, bl, n, rows, rank);
         beta = bc[13];
-        wv = bc[14];
+        const double muz = bc[14];
         const float bh_ = (float)beta, bl_ = (float)(beta - (double)bh_);
+        const float mh = (float)muz, ml = (float)(muz - (double)mh);
         for (int j = threadIdx.x; j < n; j += blockDim.x) {
-          const FF pn = ff_axpy(bh_, bl_, FF{ph[j], pl[j]}, FF{bh[j], bl[j]});
+          FF pn = ff_axpy(bh_, bl_, FF{ph[j], pl[j]}, FF{bh[j], bl[j]});
+          if (sz) pn = ff_sub_const(pn, mh, ml);
           ph[j] = pn.hi;
           pl[j] = pn.lo;
         }
       }
-      wp = wv + beta * wp;
       __syncthreads();
     }
     relres = bnorm > 0 ? sqrt(rlast) / bnorm : 0.0;
@@ -1231,33 +1238,6 @@ __global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(NT, MINB)
       relres = best;
       for (int i = threadIdx.x; i < nr; i += blockDim.x) xs[i] = pr.x[r0 + i];
       __syncthreads();
-    }
-    if (pr.zdef != nullptr && gamma != 0.0) {
-      // Sherman-Morrison back to S: x = y + gamma t z, t = 1^T W y / (1 - gamma 1^T W z)
-      double v[1] = {0.0};
-      for (int i = threadIdx.x; i < nr; i += blockDim.x) v[0] += ws[i] * xs[i];
-      csum_t0<1, CS>(cl, v, nr, red, pub, slot);
-      if (threadIdx.x == 0) bc[15] = gamma * (v[0] / (1.0 - gamma * pr.uz));
-      __syncthreads();
-      const double gt = bc[15];
-      for (int i = threadIdx.x; i < nr; i += blockDim.x) xs[i] += gt * pr.zdef[r0 + i];
-      __syncthreads();
-      // reported residual: the true one of S x = b (x through buffer B)
-      double u[1] = {0.0};
-      publish_slice(xs, r0, nr, bh, bl);
-      csum_t0<1, CS>(cl, u, nr, red, pub, slot);  // barrier that publishes x
-      gather_parts(cl, bh, bl, n, rows, rank);
-      matvec_rows_ff(pr, n, r0, r1, bh, bl, yh, yl);
-      __syncthreads();
-      double t[1] = {0.0};
-      for (int i = threadIdx.x; i < nr; i += blockDim.x) {
-        const double d = bs[i] - ((double)yh[i] + (double)yl[i]);
-        t[0] += d * d;
-      }
-      csum_t0<1, CS>(cl, t, nr, red, pub, slot);
-      if (threadIdx.x == 0) bc[0] = t[0];
-      __syncthreads();
-      relres = bnorm > 0 ? sqrt(bc[0]) / bnorm : 0.0;
     }
     for (int i = threadIdx.x; i < nr; i += blockDim.x) pr.x[r0 + i] = xs[i];
     if (rank == 0 && threadIdx.x == 0) {
@@ -1430,11 +1410,10 @@ void cgff_params_fill_csr(void* dst, const float* vhi, const float* vlo, const i
   *static_cast<CGFFParams*>(dst) = p;
 }
 
-void cgff_params_set_deflation(void* dst, double gamma, const double* zdef, double uz) {
+void cgff_params_set_deflation(void* dst, const double* sz, double inv_e) {
   CGFFParams* p = static_cast<CGFFParams*>(dst);
-  p->gamma = gamma;
-  p->zdef = zdef;
-  p->uz = uz;
+  p->sz = sz;
+  p->inv_e = inv_e;
 }
 
 void cgff_params_set_timing(void* dst, unsigned long long* tspan) {

@@ -381,7 +381,11 @@ typedef struct {
 } ilm_batch_problem_t;
 /* x, y, nrmx, nrmy, ds: host arrays of all problems' points, concatenated in
  * problem order.  dtype: precision of the grid-side work (the Schur CG is
- * always FP64).  Builds DDF windows, tile lists and the Schur complements.  */
+ * always FP64).  Builds DDF windows, tile lists and the Schur complements.
+ * Returns while the Schur build still runs on the device (its own stream):
+ * every later call that reads the Schur complements orders its device work
+ * after that build, so the caller's host work (the preconditioner set-up)
+ * overlaps it.                                                              */
 ILM_API int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* x, const double* y,
                              const double* nrmx, const double* nrmy, const double* ds, int ddf, int dtype,
                              ilm_batch_t* out);
