@@ -29,10 +29,12 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "immersedlayers.jl_gb300"))
 
 METRIC = "Poisson solves/s at 1e-8 rel. residual, 1 GB300 (batched Dirichlet/Neumann)"
-# DRAM bytes (read + write) of one launch of the dominant kernel, from one ncu
-# capture of this bench's CG launch per solver
-# (profiles/k_cg_cluster_*_batched_poisson.md)
-NCU_TRAFFIC = {"learned": {"Schur CG (FP64)": 0.7326e9}}
+# DRAM bytes (read + write) of the dominant stage of one solve, from one ncu
+# capture of this bench's CG launches per solver (the default solver's CG
+# variant 6: the 8-CTA cluster launch of the large problems and the
+# single-CTA launch of the small ones, 639.1 + 6.5 + 18.9 + 0.0 MB;
+# profiles/k_cg_cluster_learned_batched_poisson.md)
+NCU_TRAFFIC = {"learned": {"Schur CG (FP64)": 0.6645e9}}
 UNIT = "solves/s"
 NPROB = 256
 
@@ -70,6 +72,9 @@ def parse():
     ap.add_argument("--profile-solves", type=int, default=0,
                     help="profiling driver: set up the batch with the default solver, run this many solves on a "
                          "created stream and exit (no timing, no JSON line)")
+    ap.add_argument("--cg-variant", type=int, default=0,
+                    help="--profile-solves: Schur CG kernel variant (0: the library default; the timed bench "
+                         "takes the autotuner's choice, 6 for the default solver)")
     return ap.parse_args()
 
 
@@ -1085,6 +1090,8 @@ def run_profile_solves(args):
     if args.precond == "learned":
         _prepare_learned(bs, args.block, bool(args.coarse))
     bs.set_precond(args.precond, args.block)
+    if args.cg_variant:
+        bs.set_cg_variant(args.cg_variant)
     fp, fm = bs.surface_data()
     f = torch.empty(bs.total_cells, device="cuda")
     s = torch.empty(bs.total_points, device="cuda")
