@@ -261,7 +261,7 @@ def run_ours(args, rank, world, dist):
         # the batch autotuner picks the Schur CG kernel for this solver (its
         # solves double as warm-up)
         with torch.cuda.stream(stream):
-            ch, ms = bs.autotune(fp, fm, f_out, s_out, tol=args.tol, reps=1, stream=stream)
+            ch, ms = bs.autotune(fp, fm, f_out, s_out, tol=args.tol, reps=3, stream=stream)
         tuned[leg_names[mode]] = {"cg_variant": ch, "ms_per_variant": {str(k): round(v, 4) for k, v in ms.items()}}
         with torch.cuda.stream(stream):
             for _ in range(args.warmup):   # the first graph solve captures the graph

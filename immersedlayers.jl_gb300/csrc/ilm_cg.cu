@@ -109,14 +109,16 @@ struct CGFFParams {
   // optional deflation of the negative (net-charge) mode of the Dirichlet
   // Schur complement by deflated CG on Z = 1 (Nicolaides 1987; Saad, Yeung,
   // Erhel and Guyomarc'h 2000): sz = S 1 (this problem's rows) and
-  // inv_e = 1 / E, E = 1^T W S 1 < 0.  S has one negative eigenvalue and E
+  // *inv_e = 1 / E, E = 1^T W S 1 < 0 (device memory, formed after the
+  // Schur build; 0 makes the deflation a no-op).  S has one negative
+  // eigenvalue and E
   // takes it, so S is positive definite on the S-orthogonal complement of 1
   // (inertia additivity of the Schur complement).  x0 is corrected by
   // (1^T W r0 / E) 1 so that 1^T W r0 = 0, and every search direction is
   // kept S-orthogonal to 1, p <- p - ((S 1)^T W p / E) 1, which keeps
   // 1^T W r = 0.  sz == nullptr: off.
   const double* sz;
-  double inv_e;
+  const double* inv_e;
   // optional: global-timer stamps (ns) when the problem is taken and done,
   // and the SM of the cluster's first CTA (profiling)
   unsigned long long* tspan;
@@ -126,7 +128,7 @@ struct CGFFParams {
   // (cnb = 0: off)
   int cnb;
   int cstart[CG_COARSE_MAX + 1];
-  double cEinv[CG_COARSE_MAX * CG_COARSE_MAX];  // row-major
+  const double* cEinv;  // CG_COARSE_MAX^2, row-major (device memory)
 };
 
 __device__ __forceinline__ unsigned long long global_ns() {
@@ -427,11 +429,12 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(CGR_THREADS
     }
     __syncthreads();
     const double* sz = pr.sz;  // deflation (as k_cg_cluster): S 1, whole vector
+    const double inv_e = sz ? __ldg(pr.inv_e) : 0.0;
     if (sz) {  // x += c 1, r -= c S 1, c = 1^T W r / E
       double c = 0.0, unused = 0.0;
       for (int j = threadIdx.x; j < n; j += blockDim.x) c += w[j] * r[j];
       block_sum2(c, unused, red);
-      c *= pr.inv_e;
+      c *= inv_e;
       for (int j = threadIdx.x; j < n; j += blockDim.x) {
         x[j] += c;
         r[j] -= c * __ldg(sz + j);
@@ -453,7 +456,7 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(CGR_THREADS
       __syncthreads();
     }
     for (int j = threadIdx.x; j < n; j += blockDim.x) p[j] = pre ? z[j] : r[j];
-    deflate_full(sz, pr.inv_e, w, p, n, red);
+    deflate_full(sz, inv_e, w, p, n, red);
     const double bnorm = sqrt(bb);
     const double thr = pr.tol * bnorm;
     const double thr2 = thr * thr;
@@ -522,7 +525,7 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(CGR_THREADS
         const double beta = fdiv(rzn, rz);
         rz = rzn;
         for (int j = threadIdx.x; j < n; j += blockDim.x) p[j] = r[j] + beta * p[j];
-        deflate_full(sz, pr.inv_e, w, p, n, red);
+        deflate_full(sz, inv_e, w, p, n, red);
         __syncthreads();
       } else {
         // flexible CG: z = M r, beta = -(z, q) / (p, q), p = z + beta p
@@ -533,7 +536,7 @@ __global__ void __cluster_dims__(CG_CLUSTER, 1, 1) __launch_bounds__(CGR_THREADS
         const double zq = wsum(w, z, qv, n, red);
         const double beta = fdiv(-zq, pq);
         for (int j = threadIdx.x; j < n; j += blockDim.x) p[j] = z[j] + beta * p[j];
-        deflate_full(sz, pr.inv_e, w, p, n, red);
+        deflate_full(sz, inv_e, w, p, n, red);
         __syncthreads();
       }
     }
@@ -981,7 +984,7 @@ __global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(NT, MINB)
     const int r0 = min(n, rank * rows), r1 = min(n, r0 + rows);
     const int nr = r1 - r0;
     const double* sz = pr.sz != nullptr ? pr.sz + r0 : nullptr;  // S 1, owned rows (deflation)
-    const double inv_e = pr.inv_e;
+    const double inv_e = sz ? __ldg(pr.inv_e) : 0.0;
     const bool pre = pr.blk != nullptr || pr.band != nullptr;
     for (int i = threadIdx.x; i < nr; i += blockDim.x) {
       xs[i] = pr.x0 ? pr.x0[r0 + i] : 0.0;
@@ -1410,7 +1413,7 @@ void cgff_params_fill_csr(void* dst, const float* vhi, const float* vlo, const i
   *static_cast<CGFFParams*>(dst) = p;
 }
 
-void cgff_params_set_deflation(void* dst, const double* sz, double inv_e) {
+void cgff_params_set_deflation(void* dst, const double* sz, const double* inv_e) {
   CGFFParams* p = static_cast<CGFFParams*>(dst);
   p->sz = sz;
   p->inv_e = inv_e;
@@ -1426,7 +1429,7 @@ void cgff_params_set_coarse(void* dst, int nb, const int* starts, const double* 
   CGFFParams* p = static_cast<CGFFParams*>(dst);
   p->cnb = nb;
   for (int b = 0; b <= CG_COARSE_MAX; ++b) p->cstart[b] = b <= nb ? starts[b] : 0;
-  for (int k = 0; k < CG_COARSE_MAX * CG_COARSE_MAX; ++k) p->cEinv[k] = k < nb * CG_COARSE_MAX ? Einv[k] : 0.0;
+  p->cEinv = Einv;
 }
 
 void cgff_params_set_band(void* dst, const float* band, int band_k, const int* seg_start, const int* seg_len) {

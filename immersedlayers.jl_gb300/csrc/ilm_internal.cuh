@@ -646,8 +646,9 @@ void cgff_params_fill(void* dst, const float* Shi, const float* Slo, const doubl
 int net_forward_packed(ilm_net_t n, int N, const float* feat, const int* sst, const int* sln, float* band,
                        cudaStream_t st);
 int net_band(ilm_net_t n);
+int* net_tc_flag(ilm_net_t n);
 int net_nfeat(ilm_net_t n);
-void cgff_params_set_deflation(void* dst, const double* sz, double inv_e);
+void cgff_params_set_deflation(void* dst, const double* sz, const double* inv_e);
 // per-problem timing of the cluster CG (3 u64 per problem: start ns, end ns, SM), nullptr: off
 void cgff_params_set_timing(void* dst, unsigned long long* tspan);
 void cgff_params_set_band(void* dst, const float* band, int band_k, const int* seg_start, const int* seg_len);

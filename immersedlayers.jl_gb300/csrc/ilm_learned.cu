@@ -289,10 +289,36 @@ struct ilm_net_s {
   // tensor-core kernels' timeout flag (one int on the device)
   bool tensor_cores = true;
   DevBuf tc_err;
+  // the end of the last stream-ordered use of the work buffers and
+  // parameters above (a batch's learned set-up, a training step): the next
+  // stream-ordered use waits for it on the device (net_after / net_mark),
+  // the host-side parameter copies on the host (net_idle), so two launches
+  // never share the buffers at once
+  cudaEvent_t busy = nullptr;
   int P() const { return 2 * band + 1; }
+  ~ilm_net_s() {
+    if (busy) {
+      cudaEventSynchronize(busy);
+      cudaEventDestroy(busy);
+    }
+  }
 };
 
 namespace {
+
+int net_idle(ilm_net_s* n) {
+  if (n->busy) ILM_CHECK_CUDA(cudaEventSynchronize(n->busy));
+  return ILM_OK;
+}
+int net_after(ilm_net_s* n, cudaStream_t st) {
+  if (n->busy) ILM_CHECK_CUDA(cudaStreamWaitEvent(st, n->busy, 0));
+  return ILM_OK;
+}
+int net_mark(ilm_net_s* n, cudaStream_t st) {
+  if (!n->busy) ILM_CHECK_CUDA(cudaEventCreateWithFlags(&n->busy, cudaEventDisableTiming));
+  ILM_CHECK_CUDA(cudaEventRecord(n->busy, st));
+  return ILM_OK;
+}
 
 int net_reserve(ilm_net_s* n, int N, int npair) {
   if ((size_t)N > n->cap) {
@@ -473,6 +499,7 @@ int ilm_net_nparams(ilm_net_t n, size_t* count) {
 
 int ilm_net_set_params(ilm_net_t n, const float* host) {
   ILM_REQUIRE(n && host, "net: null argument");
+  ILM_TRY(net_idle(n));
   ILM_CHECK_CUDA(cudaMemcpy(n->theta.p, host, n->nparam * sizeof(float), cudaMemcpyHostToDevice));
   k_to_bf16<<<256, 256>>>(n->nparam, n->theta.as<float>(), n->thb.as<__nv_bfloat16>());
   ILM_CHECK_LAUNCH();
@@ -485,6 +512,7 @@ int ilm_net_set_params(ilm_net_t n, const float* host) {
 
 int ilm_net_get_params(ilm_net_t n, float* host) {
   ILM_REQUIRE(n && host, "net: null argument");
+  ILM_TRY(net_idle(n));
   ILM_CHECK_CUDA(cudaMemcpy(host, n->theta.p, n->nparam * sizeof(float), cudaMemcpyDeviceToHost));
   return ILM_OK;
 }
@@ -493,9 +521,11 @@ int ilm_net_forward(ilm_net_t n, int npts, const float* feat, const int* seg_sta
                     float* band_out, ilm_stream_t stream) {
   ILM_TRY(check_net_inputs(n, npts, feat, seg_start, seg_len));
   ILM_REQUIRE(band_out, "net: null output");
-  ILM_TRY(net_reserve(n, npts, 1));
   cudaStream_t st = as_stream(stream);
+  ILM_TRY(net_after(n, st));
+  ILM_TRY(net_reserve(n, npts, 1));
   ILM_TRY(net_forward(n, npts, feat, seg_start, seg_len, band_out, st));
+  ILM_TRY(net_mark(n, st));
   if (!n->tensor_cores) return ILM_OK;
   ILM_CHECK_CUDA(cudaStreamSynchronize(st));
   return net_check_tc(n);
@@ -503,6 +533,7 @@ int ilm_net_forward(ilm_net_t n, int npts, const float* feat, const int* seg_sta
 
 int ilm_net_set_tensor_cores(ilm_net_t n, int enable) {
   ILM_REQUIRE(n, "net: null handle");
+  ILM_TRY(net_idle(n));
   n->tensor_cores = enable != 0;
   return ILM_OK;
 }
@@ -513,7 +544,9 @@ int ilm_net_loss_grad(ilm_net_t n, int npts, int npairs, const int* pair_off, co
   ILM_TRY(check_net_inputs(n, npts, feat, seg_start, seg_len));
   ILM_REQUIRE(npairs > 0 && pair_off && w && b && x, "net: bad training inputs");
   cudaStream_t st = as_stream(stream);
+  ILM_TRY(net_after(n, st));
   ILM_TRY(net_loss_grad(n, npts, npairs, pair_off, feat, seg_start, seg_len, w, b, x, st));
+  ILM_TRY(net_mark(n, st));
   if (loss_out) ILM_CHECK_CUDA(cudaMemcpyAsync(loss_out, n->loss.p, sizeof(double), cudaMemcpyDeviceToHost, st));
   if (grad_out)
     ILM_CHECK_CUDA(cudaMemcpyAsync(grad_out, n->grad.p, n->nparam * sizeof(float), cudaMemcpyDeviceToHost, st));
@@ -527,6 +560,7 @@ int ilm_net_train_step(ilm_net_t n, int npts, int npairs, const int* pair_off, c
   ILM_TRY(check_net_inputs(n, npts, feat, seg_start, seg_len));
   ILM_REQUIRE(npairs > 0 && pair_off && w && b && x && lr > 0, "net: bad training inputs");
   cudaStream_t st = as_stream(stream);
+  ILM_TRY(net_after(n, st));
   ILM_TRY(net_loss_grad(n, npts, npairs, pair_off, feat, seg_start, seg_len, w, b, x, st));
   n->step++;
   const float b1 = 0.9f, b2 = 0.999f;
@@ -536,7 +570,7 @@ int ilm_net_train_step(ilm_net_t n, int npts, int npairs, const int* pair_off, c
       1e-8f, c1, c2, n->thb.as<__nv_bfloat16>());
   ILM_CHECK_LAUNCH();
   if (loss_dev) ILM_CHECK_CUDA(cudaMemcpyAsync(loss_dev, n->loss.p, sizeof(double), cudaMemcpyDeviceToDevice, st));
-  return ILM_OK;
+  return net_mark(n, st);
 }
 
 int ilm_point_features(int npts, const double* x, const double* y, const double* nx, const double* ny,
@@ -559,6 +593,11 @@ int ilm_point_features(int npts, const double* x, const double* y, const double*
 // used by the batch solver: network forward over packed points
 namespace ilm {
 // after a forward has completed: a tensor-core wait that ran out is an error
+// the device flag a tensor-core convolution of the forward sets when it gives
+// up waiting (nullptr when the FP32 path runs); callers that do not
+// synchronise copy it and check it later
+int* net_tc_flag(ilm_net_t n) { return n->tensor_cores && n->tc_err.p ? n->tc_err.as<int>() : nullptr; }
+
 int net_check_tc(ilm_net_t n) {
   if (!n->tensor_cores || !n->tc_err.p) return ILM_OK;
   int e = 0;
@@ -572,8 +611,10 @@ int net_check_tc(ilm_net_t n) {
 }
 int net_forward_packed(ilm_net_t n, int N, const float* feat, const int* sst, const int* sln, float* band,
                        cudaStream_t st) {
+  ILM_TRY(net_after(n, st));
   ILM_TRY(net_reserve(n, N, 1));
-  return net_forward(n, N, feat, sst, sln, band, st);
+  ILM_TRY(net_forward(n, N, feat, sst, sln, band, st));
+  return net_mark(n, st);
 }
 int net_band(ilm_net_t n) { return n->band; }
 int net_nfeat(ilm_net_t n) { return n->nfeat; }

@@ -177,7 +177,8 @@ CG_VARIANTS = 6  # ILM_CG_VARIANTS of include/ilm.h
 
 
 def _set_cg_variant(self, variant):
-    """Schur CG kernel: 0 default (= 1), 1 row-distributed vectors (256
+    """Schur CG kernel: 0 default (= 6, the size split; 1 when no problem is
+    at or below the split), 1 row-distributed vectors (256
     threads per CTA, up to 3 per SM), 2 replicated vectors (one cluster
     barrier per iteration), 3 128-thread CTAs, 4 256-thread CTAs at most 2
     per SM, 5 512-thread CTAs one per SM, 6 size split (problems above 192

@@ -455,7 +455,8 @@ ILM_API int ilm_batch_setup_times(ilm_batch_t b, double* ms, int max_phases, int
  * SM of the first CTA of the cluster that solved it.  A profiling helper
  * with no counterpart in the reference.                                     */
 ILM_API int ilm_batch_cg_times(ilm_batch_t b, double* start_us, double* end_us, int* sm);
-/* Schur CG kernel of the batch: 0 default (= 1), 1 row-distributed
+/* Schur CG kernel of the batch: 0 default (= 6, which is 1 when no problem
+ * is at or below the size split), 1 row-distributed
  * vectors over 8-CTA clusters with 256-thread CTAs (two or three cluster
  * barriers per iteration, FP64 work on the owned rows only), 2 replicated
  * vectors (one cluster barrier per iteration, every vector operation in
@@ -465,11 +466,12 @@ ILM_API int ilm_batch_cg_times(ilm_batch_t b, double* start_us, double* end_us, 
  * the smaller ones one CTA each (no cluster barriers) on a second stream in
  * the CTA slots the clusters leave free, joined by events (the Schur-only
  * entry points run every problem on variant 1).  ilm_batch_autotune solves the given
- * data with every variant (one untimed and `reps` timed solves each, CUDA
- * events on `stream`), keeps the fastest and returns it in *chosen and the
- * mean ms per solve of variants 1..ILM_CG_VARIANTS in
- * ms_per_variant[ILM_CG_VARIANTS] (-1: skipped); the outputs hold the last
- * solve.
+ * data with every variant (one untimed and `reps` timed solves each, each
+ * between CUDA events on `stream`), keeps the fastest and returns it in
+ * *chosen and the least ms per solve of variants 1..ILM_CG_VARIANTS in
+ * ms_per_variant[ILM_CG_VARIANTS] (-1: skipped; the least of the reps, so
+ * that one solve delayed by the host does not decide); the outputs hold the
+ * last solve.
  * Tuning helpers with no counterpart in the reference (the reference
  * solves one problem at a time with a dense LU).                           */
 /* Precomputed right-hand-side operator, for batches solved more than once
