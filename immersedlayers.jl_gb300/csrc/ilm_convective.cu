@@ -97,6 +97,7 @@ __device__ __forceinline__ void vdp_np_rows(int NX, int NY, const T* __restrict_
 template <typename T>
 __global__ void __launch_bounds__(BX* BY) k_vdp_np(int NX, int NY, const T* __restrict__ vu, const T* __restrict__ vv,
     const T* __restrict__ p, T* __restrict__ out, T sc) {
+  pdl_begin();
   if (inner_block(NX, NY))
     vdp_np_rows<T, true>(NX, NY, vu, vv, p, out, sc);
   else
@@ -165,6 +166,7 @@ __device__ __forceinline__ void vdw_nd_rows(int NX, int NY, const T* __restrict_
 template <typename T>
 __global__ void __launch_bounds__(BX* BY) k_vdw_nd(int NX, int NY, const T* __restrict__ vu, const T* __restrict__ vv,
     const T* __restrict__ w, T* __restrict__ out, T sc) {
+  pdl_begin();
   if (inner_block(NX, NY))
     vdw_nd_rows<T, true>(NX, NY, vu, vv, w, out, sc);
   else
@@ -280,6 +282,7 @@ template <typename T>
 __global__ void __launch_bounds__(BX* BY, sizeof(T) == 4 ? 4 : 2) k_vdu_edges(int NX, int NY, const T* __restrict__ vu,
     const T* __restrict__ vv, const T* __restrict__ uu, const T* __restrict__ uv, T* __restrict__ ou,
     T* __restrict__ ov, T sc) {
+  pdl_begin();
   if (inner_block(NX, NY))
     vdu_edges_rows<T, true>(NX, NY, vu, vv, uu, uv, ou, ov, sc);
   else
@@ -344,6 +347,7 @@ __device__ __forceinline__ void w_cross_v_rows(int NX, int NY, const T* __restri
 template <typename T>
 __global__ void __launch_bounds__(BX* BY) k_w_cross_v(int NX, int NY, const T* __restrict__ w,
     const T* __restrict__ vu, const T* __restrict__ vv, T* __restrict__ ou, T* __restrict__ ov) {
+  pdl_begin();
   if (inner_block(NX, NY))
     w_cross_v_rows<T, true>(NX, NY, w, vu, vv, ou, ov);
   else
@@ -373,18 +377,18 @@ int st_convective(const ilm_grid_s* g, int dtype, int field_kind, const void* v,
     const T* vv = vu + ne_u;
     switch (field_kind) {
       case ILM_NODES_PRIMAL:
-        k_vdp_np<T><<<grid2(NX - 1, NY - 1), dim3(BX, BY), 0, st>>>(NX, NY, vu, vv, static_cast<const T*>(q),
-                                                                     static_cast<T*>(out), (T)scale);
+        ILM_CHECK_CUDA(launch_pdl(k_vdp_np<T>, grid2(NX - 1, NY - 1), dim3(BX, BY), st, NX, NY, vu, vv,
+                                  static_cast<const T*>(q), static_cast<T*>(out), (T)scale));
         break;
       case ILM_NODES_DUAL:
-        k_vdw_nd<T><<<grid2(NX, NY), dim3(BX, BY), 0, st>>>(NX, NY, vu, vv, static_cast<const T*>(q),
-                                                             static_cast<T*>(out), (T)scale);
+        ILM_CHECK_CUDA(launch_pdl(k_vdw_nd<T>, grid2(NX, NY), dim3(BX, BY), st, NX, NY, vu, vv,
+                                  static_cast<const T*>(q), static_cast<T*>(out), (T)scale));
         break;
       case ILM_EDGES_PRIMAL: {
         const T* uu = static_cast<const T*>(q);
         T* ou = static_cast<T*>(out);
-        k_vdu_edges<T><<<grid2(NX, NY), dim3(BX, BY), 0, st>>>(NX, NY, vu, vv, uu, uu + ne_u, ou, ou + ne_u,
-                                                                   (T)scale);
+        ILM_CHECK_CUDA(launch_pdl(k_vdu_edges<T>, grid2(NX, NY), dim3(BX, BY), st, NX, NY, vu, vv, uu, uu + ne_u,
+                                  ou, ou + ne_u, (T)scale));
         break;
       }
       default:
@@ -403,10 +407,9 @@ int st_w_cross_v(const ilm_grid_s* g, int dtype, const void* w, const void* v, v
   CV_DISPATCH(dtype, {
     const T* vu = static_cast<const T*>(v);
     T* ou = static_cast<T*>(out);
-    k_w_cross_v<T><<<grid2(NX, NY), dim3(BX, BY), 0, st>>>(NX, NY, static_cast<const T*>(w), vu, vu + ne_u, ou,
-                                                               ou + ne_u);
+    ILM_CHECK_CUDA(launch_pdl(k_w_cross_v<T>, grid2(NX, NY), dim3(BX, BY), st, NX, NY, static_cast<const T*>(w), vu,
+                              vu + ne_u, ou, ou + ne_u));
   });
-  ILM_CHECK_LAUNCH();
   return ILM_OK;
 }
 

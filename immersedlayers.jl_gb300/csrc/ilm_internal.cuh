@@ -346,6 +346,31 @@ int conv_apply(ConvPlan* plan, const void* in, void* out, double inv_factor, cud
 // ---------------------------------------------------------------------------
 // float-float arithmetic on the FP32 pipes (value = hi + lo, ~2^-44 relative
 // per operation): GB300 issues FP64 at a small fraction of its FP32 rate
+// Programmatic dependent launch for chains of stream-ordered grid kernels:
+// launched by launch_pdl, a kernel lets the next launch in its stream begin
+// scheduling as soon as all of its CTAs have started
+// (griddepcontrol.launch_dependents) and waits for the previous grid's
+// completion and memory before its first load (griddepcontrol.wait; a no-op
+// when the launch has no programmatic dependency), so launch latency and
+// the ramp of one grid overlap the tail of the one before.
+__device__ __forceinline__ void pdl_begin() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+template <typename... P, typename... A>
+cudaError_t launch_pdl(void (*kernel)(P...), dim3 grid, dim3 block, cudaStream_t st, A... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<P>(args)...);
+}
+
 struct FF {
   float hi, lo;
 };

@@ -24,6 +24,7 @@ inline dim3 grid2(int n1, int n2) { return dim3((n1 + BX - 1) / BX, (n2 + BY - 1
 template <typename T, int RY>
 __global__ void __launch_bounds__(BX* BY) k_div_edges_r(int NX, int NY, const T* __restrict__ u,
                                                        const T* __restrict__ v, T* __restrict__ w, T sc) {
+  pdl_begin();
   const int i = blockIdx.x * BX + threadIdx.x;
   const int jb = blockIdx.y * BY * RY + threadIdx.y;
   if (i >= NX - 1) return;
@@ -50,6 +51,7 @@ __global__ void __launch_bounds__(BX* BY) k_div_edges_r(int NX, int NY, const T*
 template <typename T, int RY>
 __global__ void __launch_bounds__(BX* BY) k_grad_nodes_r(int NX, int NY, const T* __restrict__ w, T* __restrict__ u,
                                                         T* __restrict__ v, T sc) {
+  pdl_begin();
   const int i = blockIdx.x * BX + threadIdx.x;
   const int jb = blockIdx.y * BY * RY + threadIdx.y;
   if (i >= NX) return;
@@ -325,9 +327,9 @@ int st_div_edges(const ilm_grid_s* g, int dtype, const void* q, void* w, double 
     const T* v = u + (size_t)NX * (NY - 1);
     constexpr int RY = 4;
     const dim3 grid((NX - 1 + BX - 1) / BX, (NY - 1 + BY * RY - 1) / (BY * RY));
-    k_div_edges_r<T, RY><<<grid, dim3(BX, BY), 0, st>>>(NX, NY, u, v, static_cast<T*>(w), (T)scale);
+    ILM_CHECK_CUDA(launch_pdl(k_div_edges_r<T, RY>, grid, dim3(BX, BY), st, NX, NY, u, v, static_cast<T*>(w),
+                              (T)scale));
   });
-  ILM_CHECK_LAUNCH();
   return ILM_OK;
 }
 
@@ -338,9 +340,9 @@ int st_grad_nodes(const ilm_grid_s* g, int dtype, const void* w, void* q, double
     T* v = u + (size_t)NX * (NY - 1);
     constexpr int RY = 4;
     const dim3 grid((NX + BX - 1) / BX, (NY + BY * RY - 1) / (BY * RY));
-    k_grad_nodes_r<T, RY><<<grid, dim3(BX, BY), 0, st>>>(NX, NY, static_cast<const T*>(w), u, v, (T)scale);
+    ILM_CHECK_CUDA(launch_pdl(k_grad_nodes_r<T, RY>, grid, dim3(BX, BY), st, NX, NY, static_cast<const T*>(w), u, v,
+                              (T)scale));
   });
-  ILM_CHECK_LAUNCH();
   return ILM_OK;
 }
 
