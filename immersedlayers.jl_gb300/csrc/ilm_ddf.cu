@@ -273,6 +273,7 @@ k_scatter_all(int n1, int n2, int ntx, int ntiles, int nocc, const int* __restri
               T* __restrict__ out) {
   __shared__ int s_ptr[SCAT_TPB + 1];
   __shared__ ScatterSmem<T> sm;
+  pdl_begin();
   const int tid = threadIdx.y * TILE_X + threadIdx.x;
   if ((int)blockIdx.x >= nocc) {  // zero writer
     const int t0 = ((int)blockIdx.x - nocc) * SCAT_TPB;
@@ -389,20 +390,19 @@ int launch_scatter(ilm_cache_s* c, int pc, const void* in1, int coef1, const voi
     const int nocc = tl.nne_launch;
     const int nb = nocc + (ntiles + SCAT_TPB - 1) / SCAT_TPB;
     if (c->dtype == ILM_F64)
-      k_scatter_all<double><<<nb, blk, 0, st>>>(sh.n1, sh.n2, tl.ntx, ntiles, nocc, tl.ne.as<int>(),
-                                                tl.ne_cnt.as<int>(), tl.ptr.as<int>(), tl.pts.as<int>(),
-                                                c->bx[dx].as<int>(), c->by[dy].as<int>(), c->wx[dx].as<double>(),
-                                                c->wy[dy].as<double>(), c->wscale.as<double>(), c->nx.as<double>(),
-                                                c->ny.as<double>(), static_cast<const double*>(in1), coef1,
-                                                static_cast<const double*>(in2), coef2, static_cast<double*>(out));
+      ILM_CHECK_CUDA(launch_pdl(k_scatter_all<double>, dim3(nb), blk, st, sh.n1, sh.n2, tl.ntx, ntiles, nocc,
+                                tl.ne.as<int>(), tl.ne_cnt.as<int>(), tl.ptr.as<int>(), tl.pts.as<int>(),
+                                c->bx[dx].as<int>(), c->by[dy].as<int>(), c->wx[dx].as<double>(),
+                                c->wy[dy].as<double>(), c->wscale.as<double>(), c->nx.as<double>(),
+                                c->ny.as<double>(), static_cast<const double*>(in1), coef1,
+                                static_cast<const double*>(in2), coef2, static_cast<double*>(out)));
     else
-      k_scatter_all<float><<<nb, blk, 0, st>>>(sh.n1, sh.n2, tl.ntx, ntiles, nocc, tl.ne.as<int>(),
-                                               tl.ne_cnt.as<int>(), tl.ptr.as<int>(), tl.pts.as<int>(),
-                                               c->bx[dx].as<int>(), c->by[dy].as<int>(), c->wx[dx].as<float>(),
-                                               c->wy[dy].as<float>(), c->wscale.as<float>(), c->nx.as<float>(),
-                                               c->ny.as<float>(), static_cast<const float*>(in1), coef1,
-                                               static_cast<const float*>(in2), coef2, static_cast<float*>(out));
-    ILM_CHECK_LAUNCH();
+      ILM_CHECK_CUDA(launch_pdl(k_scatter_all<float>, dim3(nb), blk, st, sh.n1, sh.n2, tl.ntx, ntiles, nocc,
+                                tl.ne.as<int>(), tl.ne_cnt.as<int>(), tl.ptr.as<int>(), tl.pts.as<int>(),
+                                c->bx[dx].as<int>(), c->by[dy].as<int>(), c->wx[dx].as<float>(),
+                                c->wy[dy].as<float>(), c->wscale.as<float>(), c->nx.as<float>(),
+                                c->ny.as<float>(), static_cast<const float*>(in1), coef1,
+                                static_cast<const float*>(in2), coef2, static_cast<float*>(out)));
     return ILM_OK;
   }
   // accumulate: the occupied tiles only (the others add nothing)
