@@ -324,3 +324,44 @@ def test_batch_async_precond_setup_matches_synchronised(cuda):
     assert torch.equal(outs[0][1], outs[1][1])
     assert torch.equal(outs[0][0], outs[1][0])
     assert (outs[0][2] == outs[1][2]).all()
+
+
+def test_batch_shared_network_across_batches(cuda):
+    """One network handle serving two batches whose learned set-ups are issued
+    back to back without waiting (the network's work buffers are ordered by
+    its own event): each batch solves as it does set up alone."""
+    import os
+    import torch
+    from immersedlayers import workloads as W
+    from immersedlayers import learned as LN
+    from immersedlayers.batch import BatchSolver, DIRICHLET
+    if not os.path.exists(LN.BATCHED_WEIGHTS[DIRICHLET]):
+        pytest.skip("no trained weights for the batched configuration")
+    net = LN.LearnedPreconditioner.load(LN.BATCHED_WEIGHTS[DIRICHLET])
+    specs_a = W.batch_specs(48)
+    specs_b = W.batch_specs(48, sizes=(128, 192))
+    st = torch.cuda.Stream()
+
+    def run(bs):
+        fp, fm = bs.surface_data()
+        with torch.cuda.stream(st):
+            f, s = bs.solve(fp, fm, tol=1e-8, stream=st)
+        st.synchronize()
+        its, rr = bs.info()
+        assert (rr <= 1e-8).all(), rr.max()
+        return f.clone(), s.clone()
+
+    alone = []
+    for specs in (specs_a, specs_b):
+        bs = BatchSolver(specs, dtype=torch.float32)
+        bs.set_learned(net, kinds=(DIRICHLET,))
+        torch.cuda.synchronize()
+        alone.append(run(bs))
+        del bs
+    a = BatchSolver(specs_a, dtype=torch.float32)
+    b = BatchSolver(specs_b, dtype=torch.float32)
+    a.set_learned(net, kinds=(DIRICHLET,))
+    b.set_learned(net, kinds=(DIRICHLET,))
+    for bs, ref in zip((a, b), alone):
+        f, s = run(bs)
+        assert torch.equal(s, ref[1]) and torch.equal(f, ref[0])
