@@ -46,35 +46,51 @@ __global__ void __launch_bounds__(BX* BY) k_div_edges_r(int NX, int NY, const T*
   }
 }
 
-// Nodes{Primal} -> Edges{Primal} (both components), RY rows per thread; faces
-// adjacent to the ghost layer are 0
+// Nodes{Primal} -> Edges{Primal} (both components); faces adjacent to the
+// ghost layer are 0.  RY consecutive rows per thread (jb .. jb+RY-1): a
+// row's lower neighbour is the previous row's centre value, kept in a
+// register; every load is issued before the arithmetic; 32-bit indices
+// (checked at launch).  Blocks whose threads all lie inside the grid
+// (1 <= i <= NX-2 and rows 1 .. NY-2, neighbours included) take the path
+// with every bounds test constant (IN): the kernel was issue-bound.
+template <typename T, int RY, bool IN>
+__device__ __forceinline__ void grad_nodes_rows(int NX, int NY, const T* __restrict__ w, T* __restrict__ u,
+                                                T* __restrict__ v, T sc) {
+  const int m = NX - 1;
+  const int i = blockIdx.x * BX + threadIdx.x;
+  const int jb = (blockIdx.y * BY + threadIdx.y) * RY;
+  if (!IN && (i >= NX || jb >= NY)) return;
+  const bool ci = IN || i < m;                     // w (m columns) has column i
+  const bool cu = IN || (i >= 1 && i <= NX - 2);  // u nonzero in this column
+  T wc[RY + 1], wl[RY];  // wc: column i rows jb-1 .. jb+RY-1; wl: column i-1 rows jb .. jb+RY-1
+#pragma unroll
+  for (int k = 0; k < RY + 1; ++k) {
+    const int j = jb - 1 + k;
+    wc[k] = (ci && (IN || (j >= 0 && j < NY - 1))) ? w[j * m + i] : (T)0;
+  }
+#pragma unroll
+  for (int k = 0; k < RY; ++k) {
+    const int j = jb + k;
+    wl[k] = (cu && (IN || j < NY - 1)) ? w[j * m + i - 1] : (T)0;
+  }
+#pragma unroll
+  for (int k = 0; k < RY; ++k) {
+    const int j = jb + k;
+    if (!IN && j >= NY) break;
+    if (IN || j < NY - 1) u[j * NX + i] = cu ? (wc[k + 1] - wl[k]) * sc : (T)0;
+    if (ci) v[j * m + i] = (IN || (j >= 1 && j <= NY - 2)) ? (wc[k + 1] - wc[k]) * sc : (T)0;
+  }
+}
+
 template <typename T, int RY>
 __global__ void __launch_bounds__(BX* BY) k_grad_nodes_r(int NX, int NY, const T* __restrict__ w, T* __restrict__ u,
                                                         T* __restrict__ v, T sc) {
   pdl_begin();
-  const int i = blockIdx.x * BX + threadIdx.x;
-  const int jb = blockIdx.y * BY * RY + threadIdx.y;
-  if (i >= NX) return;
-  const int m = NX - 1;
-  T wc[RY], wl[RY], wd[RY];
-#pragma unroll
-  for (int r = 0; r < RY; ++r) {
-    const int j = jb + r * BY;
-    wc[r] = wl[r] = wd[r] = (T)0;
-    if (j < NY - 1 && i < m) wc[r] = w[(size_t)j * m + i];
-    if (j < NY - 1 && i >= 1 && i <= NX - 2) wl[r] = w[(size_t)j * m + i - 1];
-    if (j >= 1 && j <= NY - 2 && i < m) wd[r] = w[(size_t)(j - 1) * m + i];
-  }
-#pragma unroll
-  for (int r = 0; r < RY; ++r) {
-    const int j = jb + r * BY;
-    if (j < NY - 1) u[(size_t)j * NX + i] = (i >= 1 && i <= NX - 2) ? (wc[r] - wl[r]) * sc : (T)0;
-    if (j < NY && i < m) {
-      T rv = (T)0;
-      if (j >= 1 && j <= NY - 2) rv = (wc[r] - wd[r]) * sc;
-      v[(size_t)j * m + i] = rv;
-    }
-  }
+  const int i0 = blockIdx.x * BX, j0 = blockIdx.y * BY * RY;
+  if (i0 >= 1 && i0 + BX - 1 <= NX - 2 && j0 >= 1 && j0 + BY * RY - 1 <= NY - 2)
+    grad_nodes_rows<T, RY, true>(NX, NY, w, u, v, sc);
+  else
+    grad_nodes_rows<T, RY, false>(NX, NY, w, u, v, sc);
 }
 
 // Nodes{Dual} (NX x NY) -> Edges{Primal}: u = s[j+1]-s[j], v = s[i]-s[i+1]
@@ -335,6 +351,7 @@ int st_div_edges(const ilm_grid_s* g, int dtype, const void* q, void* w, double 
 
 int st_grad_nodes(const ilm_grid_s* g, int dtype, const void* w, void* q, double scale, cudaStream_t st) {
   const int NX = g->nx, NY = g->ny;
+  ILM_REQUIRE((long long)NX * NY < (1LL << 31), "grad: grid of %d x %d exceeds 32-bit indexing", NX, NY);
   DISPATCH(dtype, {
     T* u = static_cast<T*>(q);
     T* v = u + (size_t)NX * (NY - 1);

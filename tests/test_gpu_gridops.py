@@ -84,8 +84,9 @@ def test_w_cross_v(S):
 @pytest.mark.parametrize("nx,ny", [(37, 23), (70, 9), (5, 6), (33, 34)])
 def test_convective_ragged_grids(S, nx, ny):
     """Rectangular grids whose sizes are not multiples of the kernels' tiles
-    (32 columns by 32 rows, four consecutive rows per thread): every output,
-    ghost layers included, against the oracle."""
+    (32 columns by 32 rows, four consecutive rows per thread): every output
+    of the convective kernels, the gradient and the divergence, ghost layers
+    included, against the oracle."""
     il, torch = S["il"], S["torch"]
     h = 0.1
     g = il.PhysicalGrid(h=h, nx=nx, ny=ny)
@@ -106,6 +107,12 @@ def test_convective_ragged_grids(S, nx, ny):
     il.convective_derivative_(out, v, u, vc, il.ConvectiveDerivativeCache(vc))
     assert rel(out.numpy_components(), O.convective_derivative_edges(vh, uh, og, s)) < S["tol"]
     assert rel(il.w_cross_v(w, v, vc).numpy_components(), O.w_cross_v(wh, vh)) < S["tol"]
+    q = il.EdgesPrimal.zeros(g, S["dt"])
+    il.grad_(q, p, sc)
+    assert rel(q.numpy_components(), tuple(x * s for x in O.grad_nodes(ph, og))) < S["tol"]
+    d = il.NodesPrimal.zeros(g, S["dt"])
+    il.divergence_(d, v, sc)
+    assert rel(d.numpy_components(), O.divergence_edges(vh) * s) < S["tol"]
 
 
 def test_convective_derivative_linear_fields_exact(S):
