@@ -21,29 +21,45 @@ inline dim3 grid2(int n1, int n2) { return dim3((n1 + BX - 1) / BX, (n2 + BY - 1
 // RY rows per thread (rows j, j + BY, ...): every load of a thread is issued
 // before its first subtraction, so a thread keeps 4 RY loads in flight (one
 // row per thread left HBM idle between the loads of consecutive rows).
+// RY consecutive rows per thread (jb .. jb+RY-1): the v value above a row is
+// the next row's own, kept in a register; 32-bit indices (checked at
+// launch); blocks wholly inside the grid take the path without bounds tests.
+template <typename T, int RY, bool IN>
+__device__ __forceinline__ void div_edges_rows(int NX, int NY, const T* __restrict__ u, const T* __restrict__ v,
+                                               T* __restrict__ w, T sc) {
+  const int m = NX - 1;
+  const int i = blockIdx.x * BX + threadIdx.x;
+  const int jb = (blockIdx.y * BY + threadIdx.y) * RY;
+  if (!IN && (i >= m || jb >= NY - 1)) return;
+  T u0[RY], u1[RY], vv[RY + 1];
+#pragma unroll
+  for (int k = 0; k < RY; ++k) {
+    const int j = jb + k;
+    const bool row = IN || j < NY - 1;
+    u0[k] = row ? u[j * NX + i] : (T)0;
+    u1[k] = row ? u[j * NX + i + 1] : (T)0;
+  }
+#pragma unroll
+  for (int k = 0; k < RY + 1; ++k) {  // v rows jb .. jb+RY (v is m x NY)
+    const int j = jb + k;
+    vv[k] = (IN || j < NY) ? v[j * m + i] : (T)0;
+  }
+#pragma unroll
+  for (int k = 0; k < RY; ++k) {
+    const int j = jb + k;
+    if (IN || j < NY - 1) w[j * m + i] = ((u1[k] - u0[k]) + (vv[k + 1] - vv[k])) * sc;
+  }
+}
+
 template <typename T, int RY>
 __global__ void __launch_bounds__(BX* BY) k_div_edges_r(int NX, int NY, const T* __restrict__ u,
                                                        const T* __restrict__ v, T* __restrict__ w, T sc) {
   pdl_begin();
-  const int i = blockIdx.x * BX + threadIdx.x;
-  const int jb = blockIdx.y * BY * RY + threadIdx.y;
-  if (i >= NX - 1) return;
-  T u0[RY], u1[RY], v0[RY], v1[RY];
-#pragma unroll
-  for (int r = 0; r < RY; ++r) {
-    const int j = jb + r * BY;
-    if (j < NY - 1) {
-      u0[r] = u[(size_t)j * NX + i];
-      u1[r] = u[(size_t)j * NX + i + 1];
-      v0[r] = v[(size_t)j * (NX - 1) + i];
-      v1[r] = v[(size_t)(j + 1) * (NX - 1) + i];
-    }
-  }
-#pragma unroll
-  for (int r = 0; r < RY; ++r) {
-    const int j = jb + r * BY;
-    if (j < NY - 1) w[(size_t)j * (NX - 1) + i] = ((u1[r] - u0[r]) + (v1[r] - v0[r])) * sc;
-  }
+  const int i0 = blockIdx.x * BX, j0 = blockIdx.y * BY * RY;
+  if (i0 + BX - 1 <= NX - 2 && j0 + BY * RY - 1 <= NY - 2)
+    div_edges_rows<T, RY, true>(NX, NY, u, v, w, sc);
+  else
+    div_edges_rows<T, RY, false>(NX, NY, u, v, w, sc);
 }
 
 // Nodes{Primal} -> Edges{Primal} (both components); faces adjacent to the
@@ -338,6 +354,7 @@ inline int nblocks(size_t n) {
 
 int st_div_edges(const ilm_grid_s* g, int dtype, const void* q, void* w, double scale, cudaStream_t st) {
   const int NX = g->nx, NY = g->ny;
+  ILM_REQUIRE((long long)NX * NY < (1LL << 31), "divergence: grid of %d x %d exceeds 32-bit indexing", NX, NY);
   DISPATCH(dtype, {
     const T* u = static_cast<const T*>(q);
     const T* v = u + (size_t)NX * (NY - 1);
