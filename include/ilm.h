@@ -420,9 +420,12 @@ ILM_API int ilm_batch_solve_graph(ilm_batch_t b, const void* fplus, const void* 
                                   double tol, int maxiter, ilm_stream_t stream);
 /* Preconditioner of the Schur CG for the following solves: mode 0 = none
  * (plain CG), 1 = block-Jacobi (inverses of the diagonal blocks of ~block_size
- * consecutive surface points, inverted in FP64 and applied in float-float
- * arithmetic inside flexible CG).  The block inverses are built on the
- * device by this call.                                                      */
+ * consecutive surface points, eliminated and applied in float-float
+ * arithmetic inside flexible CG), 2 = the learned band set by
+ * ilm_batch_set_learned, block-Jacobi for the problems without a network.
+ * The block inverses are formed on the device on a stream of the batch,
+ * issued by this call in mode 2 and by the first solve in mode 1; the
+ * call does not wait for them, and the solves order their CG after them.   */
 ILM_API int ilm_batch_set_precond(ilm_batch_t b, int mode, int block_size);
 /* Coarse correction of the block-Jacobi preconditioner on the bodies'
  * constant vectors (the near-null space of the Neumann Schur complement
