@@ -431,7 +431,9 @@ ILM_API int ilm_batch_set_precond(ilm_batch_t b, int mode, int block_size);
  * constant vectors (the near-null space of the Neumann Schur complement
  * -C_s L^-1 C_s^T, neumann.jl:123, one small eigenvalue per closed body):
  * z = M_bj r + Z E^-1 Z^T W r, Z the bodies' indicator vectors, E = Z^T W S Z
- * (formed on the device here, inverted on the host).  kind_mask 2: the
+ * (E and E^-1 formed on the device on a stream of the batch after the Schur
+ * build; the call does not wait for them, the solves order their CG after
+ * them; a singular E leaves the correction out).  kind_mask 2: the
  * Neumann problems with at most 4 bodies; 0: off.  body_start: as
  * ilm_batch_set_learned.  Applies wherever block-Jacobi runs (mode 1, and
  * mode 2 for the problems without a network); no counterpart in the
@@ -544,7 +546,11 @@ ILM_API int ilm_point_features(int npts, const double* x, const double* y, const
  * problem) and use its band for the problems whose kind is in kind_mask
  * (bit 0 Dirichlet, bit 1 Neumann); call once per network.  Switches the
  * Schur CG to the learned preconditioner (mode 2 of ilm_batch_set_precond);
- * problems of a kind no network was set for run plain CG.                  */
+ * problems of a kind no network was set for run plain CG.  The features
+ * and the network run on a stream of the batch; the call does not wait for
+ * them (the first solve that reads the band orders its CG after them and
+ * reports a tensor-core timeout of the network).  A network may serve
+ * several batches: its forwards are ordered among themselves.              */
 ILM_API int ilm_batch_set_learned(ilm_batch_t b, ilm_net_t net, int kind_mask, const int* body_start);
 /* Batch Schur products / solves on device FP64 packed vectors (training data
  * and checks): y = S x;  S x = rhs by the batch's CG (current preconditioner). */
