@@ -352,8 +352,9 @@ def run_ours(args, rank, world, dist):
 
 def _stencil_gbs(stream, flush, hbm):
     """Achieved HBM GB/s (algorithmic bytes / time) of the staggered
-    divergence (Edges -> Nodes, 12 B per cell FP32) and gradient (Nodes ->
-    Edges, 12 B per cell) on 2048^2 and 4096^2 grids, of the fused
+    divergence (Edges -> Nodes, 12 B per cell FP32), gradient (Nodes ->
+    Edges, 12 B per cell), curl both ways (12 B per cell) and 5-point
+    Laplacian (8 B per cell) on 2048^2 and 4096^2 grids, of the fused
     convective derivatives (v . grad p: Edges + 2 Nodes{Primal}; v . grad w:
     Edges + 2 Nodes{Dual}; u . grad u: 2 Edges) and w x v (2 Edges +
     Nodes{Dual}) on 4096^2, and of the DDF regularization of the 8192 points
@@ -417,7 +418,26 @@ def _stencil_gbs(stream, flush, hbm):
             sets.append((q, w))
         out[f"divergence_{n}"] = timed([lambda q=q, w=w: il.divergence_(w, q, c, stream=stream) for q, w in sets], per)
         out[f"grad_{n}"] = timed([lambda q=q, w=w: il.grad_(q, w, c, stream=stream) for q, w in sets], per)
-        del c, sets
+        # curl both ways (Nodes{Dual} <-> Edges{Primal}, 12 B per cell) and the
+        # 5-point Laplacian on Nodes{Primal} (8 B per cell)
+        nd = il.NodesDual.zeros(g, torch.float32).data.numel()
+        ne = il.EdgesPrimal.zeros(g, torch.float32).data.numel()
+        npn = il.NodesPrimal.zeros(g, torch.float32).data.numel()
+        csets = []
+        for _ in range(nsets((nd + ne) * 4)):
+            sd = il.NodesDual.zeros(g, torch.float32)
+            sd.data.normal_()
+            csets.append((sd, il.EdgesPrimal.zeros(g, torch.float32)))
+        out[f"curl_nodes_to_edges_{n}"] = timed(
+            [lambda sd=sd, q=q: il.curl_(q, sd, c, stream=stream) for sd, q in csets], (nd + ne) * 4)
+        for _, q in csets:
+            q.data.normal_()
+        out[f"curl_edges_to_nodes_{n}"] = timed(
+            [lambda sd=sd, q=q: il.curl_(sd, q, c, stream=stream) for sd, q in csets], (nd + ne) * 4)
+        lsets = [(w, w.similar()) for _, w in sets]
+        out[f"laplacian_{n}"] = timed(
+            [lambda w=w, o=o: il.laplacian_(o, w, c, stream=stream) for w, o in lsets], 2 * npn * 4)
+        del c, sets, csets, lsets
     # fused convective derivatives and w x v (inputs read once, output written once)
     n = 4096
     g = il.PhysicalGrid(h=4.0 / n, nx=n)

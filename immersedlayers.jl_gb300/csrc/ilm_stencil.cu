@@ -109,32 +109,100 @@ __global__ void __launch_bounds__(BX* BY) k_grad_nodes_r(int NX, int NY, const T
     grad_nodes_rows<T, RY, false>(NX, NY, w, u, v, sc);
 }
 
-// Nodes{Dual} (NX x NY) -> Edges{Primal}: u = s[j+1]-s[j], v = s[i]-s[i+1]
-template <typename T>
-__global__ void k_curl_s_u(int NX, int NY, const T* __restrict__ s, T* __restrict__ u, T sc) {
-  const int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
-  if (i >= NX || j >= NY - 1) return;
-  u[(size_t)j * NX + i] = (s[(size_t)(j + 1) * NX + i] - s[(size_t)j * NX + i]) * sc;
+// The curl and Laplacian kernels below take the layout of the divergence and
+// gradient: RY consecutive rows per thread (jb .. jb+RY-1), vertical
+// neighbours shared in registers, every load before the arithmetic, 32-bit
+// indices (checked at launch), a path without bounds tests for the blocks
+// inside the grid (IN), programmatic dependent launch.
+constexpr int SRY = 4;
+inline dim3 grid_rows(int n1, int n2) { return dim3((n1 + BX - 1) / BX, (n2 + BY * SRY - 1) / (BY * SRY)); }
+// blockIdx inner: columns [lo, n1 - 1 - hi] and rows [lo, n2 - 1 - hi] hold
+// every thread of the block
+__device__ __forceinline__ bool block_within(int n1, int n2, int lo, int hi) {
+  const int i0 = blockIdx.x * BX, j0 = blockIdx.y * BY * SRY;
+  return i0 >= lo && i0 + BX - 1 <= n1 - 1 - hi && j0 >= lo && j0 + BY * SRY - 1 <= n2 - 1 - hi;
+}
+
+// Nodes{Dual} (NX x NY) -> Edges{Primal} in one pass: u = s[j+1]-s[j]
+// (NX x NY-1), v = s[i]-s[i+1] ((NX-1) x NY)
+template <typename T, bool IN>
+__device__ __forceinline__ void curl_s_rows(int NX, int NY, const T* __restrict__ s, T* __restrict__ u,
+                                            T* __restrict__ v, T sc) {
+  const int i = blockIdx.x * BX + threadIdx.x;
+  const int jb = (blockIdx.y * BY + threadIdx.y) * SRY;
+  if (!IN && (i >= NX || jb >= NY)) return;
+  const bool vc = IN || i < NX - 1;  // v has column i
+  T s0[SRY + 1], s1[SRY];  // s column i rows jb .. jb+SRY; column i+1 rows jb .. jb+SRY-1
+#pragma unroll
+  for (int k = 0; k < SRY + 1; ++k) {
+    const int j = jb + k;
+    s0[k] = (IN || j < NY) ? s[j * NX + i] : (T)0;
+  }
+#pragma unroll
+  for (int k = 0; k < SRY; ++k) {
+    const int j = jb + k;
+    s1[k] = (vc && (IN || j < NY)) ? s[j * NX + i + 1] : (T)0;
+  }
+#pragma unroll
+  for (int k = 0; k < SRY; ++k) {
+    const int j = jb + k;
+    if (!IN && j >= NY) break;
+    if (IN || j < NY - 1) u[j * NX + i] = (s0[k + 1] - s0[k]) * sc;
+    if (vc) v[j * (NX - 1) + i] = (s0[k] - s1[k]) * sc;
+  }
 }
 template <typename T>
-__global__ void k_curl_s_v(int NX, int NY, const T* __restrict__ s, T* __restrict__ v, T sc) {
-  const int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
-  if (i >= NX - 1 || j >= NY) return;
-  v[(size_t)j * (NX - 1) + i] = (s[(size_t)j * NX + i] - s[(size_t)j * NX + i + 1]) * sc;
+__global__ void __launch_bounds__(BX* BY) k_curl_s(int NX, int NY, const T* __restrict__ s, T* __restrict__ u,
+                                                   T* __restrict__ v, T sc) {
+  pdl_begin();
+  if (block_within(NX, NY, 0, 1))
+    curl_s_rows<T, true>(NX, NY, s, u, v, sc);
+  else
+    curl_s_rows<T, false>(NX, NY, s, u, v, sc);
 }
 
 // Edges{Primal} -> Nodes{Dual}: w = v[i]-v[i-1] - (u[j]-u[j-1]) on interior dual nodes
-template <typename T>
-__global__ void k_curl_q(int NX, int NY, const T* __restrict__ u, const T* __restrict__ v, T* __restrict__ w, T sc) {
-  const int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
-  if (i >= NX || j >= NY) return;
-  T r = (T)0;
-  if (i >= 1 && i <= NX - 2 && j >= 1 && j <= NY - 2) {
-    r = (v[(size_t)j * (NX - 1) + i] - v[(size_t)j * (NX - 1) + i - 1]) -
-        (u[(size_t)j * NX + i] - u[(size_t)(j - 1) * NX + i]);
-    r *= sc;
+template <typename T, bool IN>
+__device__ __forceinline__ void curl_q_rows(int NX, int NY, const T* __restrict__ u, const T* __restrict__ v,
+                                            T* __restrict__ w, T sc) {
+  const int m = NX - 1;
+  const int i = blockIdx.x * BX + threadIdx.x;
+  const int jb = (blockIdx.y * BY + threadIdx.y) * SRY;
+  if (!IN && (i >= NX || jb >= NY)) return;
+  const bool col = IN || (i >= 1 && i <= NX - 2);
+  T uc[SRY + 1], vl[SRY], vr[SRY];  // u column i rows jb-1 .. jb+SRY-1; v columns i-1, i rows jb ..
+#pragma unroll
+  for (int k = 0; k < SRY + 1; ++k) {
+    const int j = jb - 1 + k;
+    uc[k] = (col && (IN || (j >= 0 && j <= NY - 2))) ? u[j * NX + i] : (T)0;
   }
-  w[(size_t)j * NX + i] = r;
+#pragma unroll
+  for (int k = 0; k < SRY; ++k) {
+    const int j = jb + k;
+    const bool r = col && (IN || j < NY);
+    vl[k] = r ? v[j * m + i - 1] : (T)0;
+    vr[k] = r ? v[j * m + i] : (T)0;
+  }
+#pragma unroll
+  for (int k = 0; k < SRY; ++k) {
+    const int j = jb + k;
+    if (!IN && j >= NY) break;
+    T r = (T)0;
+    if (IN || (col && j >= 1 && j <= NY - 2)) {
+      r = (vr[k] - vl[k]) - (uc[k + 1] - uc[k]);
+      r *= sc;
+    }
+    w[j * NX + i] = r;
+  }
+}
+template <typename T>
+__global__ void __launch_bounds__(BX* BY) k_curl_q(int NX, int NY, const T* __restrict__ u, const T* __restrict__ v,
+                                                   T* __restrict__ w, T sc) {
+  pdl_begin();
+  if (block_within(NX, NY, 1, 1))
+    curl_q_rows<T, true>(NX, NY, u, v, w, sc);
+  else
+    curl_q_rows<T, false>(NX, NY, u, v, w, sc);
 }
 
 // Edges{Primal} -> EdgeGradient{Primal}
@@ -179,16 +247,44 @@ __global__ void k_div_edgegrad(int NX, int NY, const T* __restrict__ dudx, const
   }
 }
 
-template <typename T>
-__global__ void k_laplacian(int n1, int n2, const T* __restrict__ a, T* __restrict__ o, T sc) {
-  const int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
-  if (i >= n1 || j >= n2) return;
-  T r = (T)0;
-  if (i >= 1 && i <= n1 - 2 && j >= 1 && j <= n2 - 2) {
-    const size_t c = (size_t)j * n1 + i;
-    r = (a[c + 1] + a[c - 1] + a[c + n1] + a[c - n1] - (T)4 * a[c]) * sc;
+// 5-point Laplacian on an n1 x n2 node grid (interior nodes; the outer ring
+// is 0), times sc
+template <typename T, bool IN>
+__device__ __forceinline__ void laplacian_rows(int n1, int n2, const T* __restrict__ a, T* __restrict__ o, T sc) {
+  const int i = blockIdx.x * BX + threadIdx.x;
+  const int jb = (blockIdx.y * BY + threadIdx.y) * SRY;
+  if (!IN && (i >= n1 || jb >= n2)) return;
+  const bool col = IN || (i >= 1 && i <= n1 - 2);
+  T ac[SRY + 2], al[SRY], ar[SRY];  // column i rows jb-1 .. jb+SRY; columns i-1, i+1 rows jb .. jb+SRY-1
+#pragma unroll
+  for (int k = 0; k < SRY + 2; ++k) {
+    const int j = jb - 1 + k;
+    ac[k] = (col && (IN || (j >= 0 && j < n2))) ? a[j * n1 + i] : (T)0;
   }
-  o[(size_t)j * n1 + i] = r;
+#pragma unroll
+  for (int k = 0; k < SRY; ++k) {
+    const int j = jb + k;
+    const bool r = col && (IN || j < n2);
+    al[k] = r ? a[j * n1 + i - 1] : (T)0;
+    ar[k] = r ? a[j * n1 + i + 1] : (T)0;
+  }
+#pragma unroll
+  for (int k = 0; k < SRY; ++k) {
+    const int j = jb + k;
+    if (!IN && j >= n2) break;
+    T r = (T)0;
+    if (IN || (col && j >= 1 && j <= n2 - 2)) r = (ar[k] + al[k] + ac[k + 2] + ac[k] - (T)4 * ac[k + 1]) * sc;
+    o[j * n1 + i] = r;
+  }
+}
+template <typename T>
+__global__ void __launch_bounds__(BX* BY) k_laplacian(int n1, int n2, const T* __restrict__ a, T* __restrict__ o,
+                                                      T sc) {
+  pdl_begin();
+  if (block_within(n1, n2, 1, 1))
+    laplacian_rows<T, true>(n1, n2, a, o, sc);
+  else
+    laplacian_rows<T, false>(n1, n2, a, o, sc);
 }
 
 // Nodes{Primal} -> Nodes{Dual} (4-point average on interior dual nodes)
@@ -382,11 +478,12 @@ int st_grad_nodes(const ilm_grid_s* g, int dtype, const void* w, void* q, double
 
 int st_curl_dual_to_edges(const ilm_grid_s* g, int dtype, const void* s, void* q, double scale, cudaStream_t st) {
   const int NX = g->nx, NY = g->ny;
+  ILM_REQUIRE((long long)NX * NY < (1LL << 31), "curl: grid of %d x %d exceeds 32-bit indexing", NX, NY);
   DISPATCH(dtype, {
     T* u = static_cast<T*>(q);
     T* v = u + (size_t)NX * (NY - 1);
-    k_curl_s_u<T><<<grid2(NX, NY - 1), dim3(BX, BY), 0, st>>>(NX, NY, static_cast<const T*>(s), u, (T)scale);
-    k_curl_s_v<T><<<grid2(NX - 1, NY), dim3(BX, BY), 0, st>>>(NX, NY, static_cast<const T*>(s), v, (T)scale);
+    ILM_CHECK_CUDA(launch_pdl(k_curl_s<T>, grid_rows(NX, NY), dim3(BX, BY), st, NX, NY, static_cast<const T*>(s), u,
+                              v, (T)scale));
   });
   ILM_CHECK_LAUNCH();
   return ILM_OK;
@@ -394,10 +491,12 @@ int st_curl_dual_to_edges(const ilm_grid_s* g, int dtype, const void* s, void* q
 
 int st_curl_edges_to_dual(const ilm_grid_s* g, int dtype, const void* q, void* w, double scale, cudaStream_t st) {
   const int NX = g->nx, NY = g->ny;
+  ILM_REQUIRE((long long)NX * NY < (1LL << 31), "curl: grid of %d x %d exceeds 32-bit indexing", NX, NY);
   DISPATCH(dtype, {
     const T* u = static_cast<const T*>(q);
     const T* v = u + (size_t)NX * (NY - 1);
-    k_curl_q<T><<<grid2(NX, NY), dim3(BX, BY), 0, st>>>(NX, NY, u, v, static_cast<T*>(w), (T)scale);
+    ILM_CHECK_CUDA(launch_pdl(k_curl_q<T>, grid_rows(NX, NY), dim3(BX, BY), st, NX, NY, u, v, static_cast<T*>(w),
+                              (T)scale));
   });
   ILM_CHECK_LAUNCH();
   return ILM_OK;
@@ -436,9 +535,10 @@ int st_div_edgegrad(const ilm_grid_s* g, int dtype, const void* t, void* q, doub
 }
 
 int st_laplacian(int n1, int n2, int dtype, const void* in, void* out, double scale, cudaStream_t st) {
+  ILM_REQUIRE((long long)n1 * n2 < (1LL << 31), "laplacian: grid of %d x %d exceeds 32-bit indexing", n1, n2);
   DISPATCH(dtype, {
-    k_laplacian<T><<<grid2(n1, n2), dim3(BX, BY), 0, st>>>(n1, n2, static_cast<const T*>(in), static_cast<T*>(out),
-                                                           (T)scale);
+    ILM_CHECK_CUDA(launch_pdl(k_laplacian<T>, grid_rows(n1, n2), dim3(BX, BY), st, n1, n2, static_cast<const T*>(in),
+                              static_cast<T*>(out), (T)scale));
   });
   ILM_CHECK_LAUNCH();
   return ILM_OK;

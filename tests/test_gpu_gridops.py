@@ -85,8 +85,8 @@ def test_w_cross_v(S):
 def test_convective_ragged_grids(S, nx, ny):
     """Rectangular grids whose sizes are not multiples of the kernels' tiles
     (32 columns by 32 rows, four consecutive rows per thread): every output
-    of the convective kernels, the gradient and the divergence, ghost layers
-    included, against the oracle."""
+    of the convective kernels, the gradient, the divergence, the curl both
+    ways and the Laplacian, ghost layers included, against the oracle."""
     il, torch = S["il"], S["torch"]
     h = 0.1
     g = il.PhysicalGrid(h=h, nx=nx, ny=ny)
@@ -113,6 +113,14 @@ def test_convective_ragged_grids(S, nx, ny):
     d = il.NodesPrimal.zeros(g, S["dt"])
     il.divergence_(d, v, sc)
     assert rel(d.numpy_components(), O.divergence_edges(vh) * s) < S["tol"]
+    il.curl_(q, w, sc)                                   # Nodes{Dual} -> Edges{Primal}
+    assert rel(q.numpy_components(), tuple(x * s for x in O.curl_nodes_dual(wh, og))) < S["tol"]
+    wd = il.NodesDual.zeros(g, S["dt"])
+    il.curl_(wd, v, sc)                                  # Edges{Primal} -> Nodes{Dual}
+    assert rel(wd.numpy_components(), O.curl_edges(vh, og) * s) < S["tol"]
+    lap = il.NodesPrimal.zeros(g, S["dt"])
+    il.laplacian_(lap, p, sc)
+    assert rel(lap.numpy_components(), O.laplacian_nodes(ph, s * s)) < S["tol"]
 
 
 def test_convective_derivative_linear_fields_exact(S):
