@@ -353,8 +353,9 @@ def run_ours(args, rank, world, dist):
 def _stencil_gbs(stream, flush, hbm):
     """Achieved HBM GB/s (algorithmic bytes / time) of the staggered
     divergence (Edges -> Nodes, 12 B per cell FP32), gradient (Nodes ->
-    Edges, 12 B per cell), curl both ways (12 B per cell) and 5-point
-    Laplacian (8 B per cell) on 2048^2 and 4096^2 grids, of the fused
+    Edges, 12 B per cell), curl both ways (12 B per cell), 5-point
+    Laplacian (8 B per cell) and vector gradient / divergence (Edges <->
+    EdgeGradient, 24 B per cell) on 2048^2 and 4096^2 grids, of the fused
     convective derivatives (v . grad p: Edges + 2 Nodes{Primal}; v . grad w:
     Edges + 2 Nodes{Dual}; u . grad u: 2 Edges) and w x v (2 Edges +
     Nodes{Dual}) on 4096^2, and of the DDF regularization of the 8192 points
@@ -437,7 +438,20 @@ def _stencil_gbs(stream, flush, hbm):
         lsets = [(w, w.similar()) for _, w in sets]
         out[f"laplacian_{n}"] = timed(
             [lambda w=w, o=o: il.laplacian_(o, w, c, stream=stream) for w, o in lsets], 2 * npn * 4)
-        del c, sets, csets, lsets
+        del sets, csets, lsets
+        # vector gradient / divergence (Edges{Primal} <-> EdgeGradient{Primal}, 24 B per cell)
+        vcache = il.SurfaceVectorCache(None, g, dtype=torch.float32)
+        nt = il.EdgeGradientPrimal.zeros(g, torch.float32).data.numel()
+        vsets = []
+        for _ in range(nsets((ne + nt) * 4)):
+            q = il.EdgesPrimal.zeros(g, torch.float32)
+            q.data.normal_()
+            vsets.append((q, il.EdgeGradientPrimal.zeros(g, torch.float32)))
+        out[f"vector_grad_{n}"] = timed(
+            [lambda q=q, t=t: il.grad_(t, q, vcache, stream=stream) for q, t in vsets], (ne + nt) * 4)
+        out[f"vector_div_{n}"] = timed(
+            [lambda q=q, t=t: il.divergence_(q, t, vcache, stream=stream) for q, t in vsets], (ne + nt) * 4)
+        del c, vcache, vsets
     # fused convective derivatives and w x v (inputs read once, output written once)
     n = 4096
     g = il.PhysicalGrid(h=4.0 / n, nx=n)

@@ -205,46 +205,118 @@ __global__ void __launch_bounds__(BX* BY) k_curl_q(int NX, int NY, const T* __re
     curl_q_rows<T, false>(NX, NY, u, v, w, sc);
 }
 
-// Edges{Primal} -> EdgeGradient{Primal}
+// Edges{Primal} -> EdgeGradient{Primal}: dudx, dvdy ((NX-1) x (NY-1)),
+// dudy, dvdx (NX x NY, interior dual nodes only)
+template <typename T, bool IN>
+__device__ __forceinline__ void grad_edges_rows(int NX, int NY, const T* __restrict__ u, const T* __restrict__ v,
+                                                T* __restrict__ dudx, T* __restrict__ dudy, T* __restrict__ dvdx,
+                                                T* __restrict__ dvdy, T sc) {
+  const int m = NX - 1;
+  const int i = blockIdx.x * BX + threadIdx.x;
+  const int jb = (blockIdx.y * BY + threadIdx.y) * SRY;
+  if (!IN && (i >= NX || jb >= NY)) return;
+  const bool cp = IN || i < NX - 1;                 // the (NX-1)-column arrays have column i
+  const bool cd = IN || (i >= 1 && i <= NX - 2);    // dudy, dvdx nonzero in this column
+  // uc: u column i rows jb-1 .. jb+SRY-1; ur: u column i+1 rows jb .. jb+SRY-1;
+  // vc: v column i rows jb .. jb+SRY; vl: v column i-1 rows jb .. jb+SRY-1
+  T uc[SRY + 1], ur[SRY], vc[SRY + 1], vl[SRY];
+#pragma unroll
+  for (int k = 0; k < SRY + 1; ++k) {
+    const int j = jb - 1 + k;
+    uc[k] = (IN || (j >= 0 && j <= NY - 2)) ? u[j * NX + i] : (T)0;
+    const int jv = jb + k;
+    vc[k] = (cp && (IN || jv < NY)) ? v[jv * m + i] : (T)0;
+  }
+#pragma unroll
+  for (int k = 0; k < SRY; ++k) {
+    const int j = jb + k;
+    ur[k] = (cp && (IN || j <= NY - 2)) ? u[j * NX + i + 1] : (T)0;
+    vl[k] = (cd && (IN || j < NY)) ? v[j * m + i - 1] : (T)0;
+  }
+#pragma unroll
+  for (int k = 0; k < SRY; ++k) {
+    const int j = jb + k;
+    if (!IN && j >= NY) break;
+    if (cp && (IN || j < NY - 1)) {
+      dudx[j * m + i] = (ur[k] - uc[k + 1]) * sc;
+      dvdy[j * m + i] = (vc[k + 1] - vc[k]) * sc;
+    }
+    T a = (T)0, b = (T)0;
+    if (IN || (cd && j >= 1 && j <= NY - 2)) {
+      a = (uc[k + 1] - uc[k]) * sc;
+      b = (vc[k] - vl[k]) * sc;
+    }
+    dudy[j * NX + i] = a;
+    dvdx[j * NX + i] = b;
+  }
+}
 template <typename T>
-__global__ void k_grad_edges(int NX, int NY, const T* __restrict__ u, const T* __restrict__ v, T* __restrict__ dudx,
-                             T* __restrict__ dudy, T* __restrict__ dvdx, T* __restrict__ dvdy, T sc) {
-  const int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
-  if (i >= NX || j >= NY) return;
-  if (i < NX - 1 && j < NY - 1) {
-    dudx[(size_t)j * (NX - 1) + i] = (u[(size_t)j * NX + i + 1] - u[(size_t)j * NX + i]) * sc;
-    dvdy[(size_t)j * (NX - 1) + i] = (v[(size_t)(j + 1) * (NX - 1) + i] - v[(size_t)j * (NX - 1) + i]) * sc;
-  }
-  T a = (T)0, b = (T)0;
-  if (i >= 1 && i <= NX - 2 && j >= 1 && j <= NY - 2) {
-    a = (u[(size_t)j * NX + i] - u[(size_t)(j - 1) * NX + i]) * sc;
-    b = (v[(size_t)j * (NX - 1) + i] - v[(size_t)j * (NX - 1) + i - 1]) * sc;
-  }
-  dudy[(size_t)j * NX + i] = a;
-  dvdx[(size_t)j * NX + i] = b;
+__global__ void __launch_bounds__(BX* BY) k_grad_edges(int NX, int NY, const T* __restrict__ u, const T* __restrict__ v,
+                                                       T* __restrict__ dudx, T* __restrict__ dudy, T* __restrict__ dvdx,
+                                                       T* __restrict__ dvdy, T sc) {
+  pdl_begin();
+  if (block_within(NX, NY, 1, 1))
+    grad_edges_rows<T, true>(NX, NY, u, v, dudx, dudy, dvdx, dvdy, sc);
+  else
+    grad_edges_rows<T, false>(NX, NY, u, v, dudx, dudy, dvdx, dvdy, sc);
 }
 
-// EdgeGradient{Primal} -> Edges{Primal}
+// EdgeGradient{Primal} -> Edges{Primal}: u (NX x NY-1) from dudx, dudy on the
+// interior columns, v ((NX-1) x NY) from dvdx, dvdy on the interior rows
+template <typename T, bool IN>
+__device__ __forceinline__ void div_edgegrad_rows(int NX, int NY, const T* __restrict__ dudx,
+                                                  const T* __restrict__ dudy, const T* __restrict__ dvdx,
+                                                  const T* __restrict__ dvdy, T* __restrict__ u, T* __restrict__ v,
+                                                  T sc) {
+  const int m = NX - 1;
+  const int i = blockIdx.x * BX + threadIdx.x;
+  const int jb = (blockIdx.y * BY + threadIdx.y) * SRY;
+  if (!IN && (i >= NX || jb >= NY)) return;
+  const bool cu = IN || (i >= 1 && i <= NX - 2);  // u nonzero in this column
+  const bool cv = IN || i < NX - 1;               // v has this column
+  // xl, xr: dudx columns i-1, i rows jb .. jb+SRY-1; yc: dudy column i rows
+  // jb .. jb+SRY; vx0, vx1: dvdx columns i, i+1 rows jb .. jb+SRY-1; vy: dvdy
+  // column i rows jb-1 .. jb+SRY-1
+  T xl[SRY], xr[SRY], yc[SRY + 1], vx0[SRY], vx1[SRY], vy[SRY + 1];
+#pragma unroll
+  for (int k = 0; k < SRY + 1; ++k) {
+    const int j = jb + k;
+    yc[k] = (cu && (IN || j < NY)) ? dudy[j * NX + i] : (T)0;
+    const int jy = jb - 1 + k;
+    vy[k] = (cv && (IN || (jy >= 0 && jy <= NY - 2))) ? dvdy[jy * m + i] : (T)0;
+  }
+#pragma unroll
+  for (int k = 0; k < SRY; ++k) {
+    const int j = jb + k;
+    const bool ur = cu && (IN || j <= NY - 2);
+    xl[k] = ur ? dudx[j * m + i - 1] : (T)0;
+    xr[k] = ur ? dudx[j * m + i] : (T)0;
+    const bool vr = cv && (IN || j < NY);
+    vx0[k] = vr ? dvdx[j * NX + i] : (T)0;
+    vx1[k] = vr ? dvdx[j * NX + i + 1] : (T)0;
+  }
+#pragma unroll
+  for (int k = 0; k < SRY; ++k) {
+    const int j = jb + k;
+    if (!IN && j >= NY) break;
+    if (IN || j < NY - 1) u[j * NX + i] = cu ? ((xr[k] - xl[k]) + (yc[k + 1] - yc[k])) * sc : (T)0;
+    if (cv) {
+      T r = (T)0;
+      if (IN || (j >= 1 && j <= NY - 2)) r = ((vx1[k] - vx0[k]) + (vy[k + 1] - vy[k])) * sc;
+      v[j * m + i] = r;
+    }
+  }
+}
 template <typename T>
-__global__ void k_div_edgegrad(int NX, int NY, const T* __restrict__ dudx, const T* __restrict__ dudy,
-                               const T* __restrict__ dvdx, const T* __restrict__ dvdy, T* __restrict__ u,
-                               T* __restrict__ v, T sc) {
-  const int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y;
-  if (i >= NX || j >= NY) return;
-  if (j < NY - 1) {
-    T r = (T)0;
-    if (i >= 1 && i <= NX - 2)
-      r = ((dudx[(size_t)j * (NX - 1) + i] - dudx[(size_t)j * (NX - 1) + i - 1]) +
-           (dudy[(size_t)(j + 1) * NX + i] - dudy[(size_t)j * NX + i])) * sc;
-    u[(size_t)j * NX + i] = r;
-  }
-  if (i < NX - 1) {
-    T r = (T)0;
-    if (j >= 1 && j <= NY - 2)
-      r = ((dvdx[(size_t)j * NX + i + 1] - dvdx[(size_t)j * NX + i]) +
-           (dvdy[(size_t)j * (NX - 1) + i] - dvdy[(size_t)(j - 1) * (NX - 1) + i])) * sc;
-    v[(size_t)j * (NX - 1) + i] = r;
-  }
+__global__ void __launch_bounds__(BX* BY) k_div_edgegrad(int NX, int NY, const T* __restrict__ dudx,
+                                                         const T* __restrict__ dudy, const T* __restrict__ dvdx,
+                                                         const T* __restrict__ dvdy, T* __restrict__ u,
+                                                         T* __restrict__ v, T sc) {
+  pdl_begin();
+  if (block_within(NX, NY, 1, 1))
+    div_edgegrad_rows<T, true>(NX, NY, dudx, dudy, dvdx, dvdy, u, v, sc);
+  else
+    div_edgegrad_rows<T, false>(NX, NY, dudx, dudy, dvdx, dvdy, u, v, sc);
 }
 
 // 5-point Laplacian on an n1 x n2 node grid (interior nodes; the outer ring
@@ -504,6 +576,7 @@ int st_curl_edges_to_dual(const ilm_grid_s* g, int dtype, const void* q, void* w
 
 int st_grad_edges(const ilm_grid_s* g, int dtype, const void* q, void* t, double scale, cudaStream_t st) {
   const int NX = g->nx, NY = g->ny;
+  ILM_REQUIRE((long long)NX * NY < (1LL << 31), "vector gradient: grid of %d x %d exceeds 32-bit indexing", NX, NY);
   const size_t np = (size_t)(NX - 1) * (NY - 1), nd = (size_t)NX * NY;
   DISPATCH(dtype, {
     const T* u = static_cast<const T*>(q);
@@ -512,7 +585,8 @@ int st_grad_edges(const ilm_grid_s* g, int dtype, const void* q, void* t, double
     T* dudy = dudx + np;
     T* dvdx = dudy + nd;
     T* dvdy = dvdx + nd;
-    k_grad_edges<T><<<grid2(NX, NY), dim3(BX, BY), 0, st>>>(NX, NY, u, v, dudx, dudy, dvdx, dvdy, (T)scale);
+    ILM_CHECK_CUDA(launch_pdl(k_grad_edges<T>, grid_rows(NX, NY), dim3(BX, BY), st, NX, NY, u, v, dudx, dudy, dvdx,
+                              dvdy, (T)scale));
   });
   ILM_CHECK_LAUNCH();
   return ILM_OK;
@@ -520,6 +594,7 @@ int st_grad_edges(const ilm_grid_s* g, int dtype, const void* q, void* t, double
 
 int st_div_edgegrad(const ilm_grid_s* g, int dtype, const void* t, void* q, double scale, cudaStream_t st) {
   const int NX = g->nx, NY = g->ny;
+  ILM_REQUIRE((long long)NX * NY < (1LL << 31), "vector gradient: grid of %d x %d exceeds 32-bit indexing", NX, NY);
   const size_t np = (size_t)(NX - 1) * (NY - 1), nd = (size_t)NX * NY;
   DISPATCH(dtype, {
     const T* dudx = static_cast<const T*>(t);
@@ -528,7 +603,8 @@ int st_div_edgegrad(const ilm_grid_s* g, int dtype, const void* t, void* q, doub
     const T* dvdy = dvdx + nd;
     T* u = static_cast<T*>(q);
     T* v = u + (size_t)NX * (NY - 1);
-    k_div_edgegrad<T><<<grid2(NX, NY), dim3(BX, BY), 0, st>>>(NX, NY, dudx, dudy, dvdx, dvdy, u, v, (T)scale);
+    ILM_CHECK_CUDA(launch_pdl(k_div_edgegrad<T>, grid_rows(NX, NY), dim3(BX, BY), st, NX, NY, dudx, dudy, dvdx,
+                              dvdy, u, v, (T)scale));
   });
   ILM_CHECK_LAUNCH();
   return ILM_OK;

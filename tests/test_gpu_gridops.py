@@ -86,7 +86,8 @@ def test_convective_ragged_grids(S, nx, ny):
     """Rectangular grids whose sizes are not multiples of the kernels' tiles
     (32 columns by 32 rows, four consecutive rows per thread): every output
     of the convective kernels, the gradient, the divergence, the curl both
-    ways and the Laplacian, ghost layers included, against the oracle."""
+    ways, the Laplacian and the vector gradient and divergence, ghost layers
+    included, against the oracle."""
     il, torch = S["il"], S["torch"]
     h = 0.1
     g = il.PhysicalGrid(h=h, nx=nx, ny=ny)
@@ -121,6 +122,13 @@ def test_convective_ragged_grids(S, nx, ny):
     lap = il.NodesPrimal.zeros(g, S["dt"])
     il.laplacian_(lap, p, sc)
     assert rel(lap.numpy_components(), O.laplacian_nodes(ph, s * s)) < S["tol"]
+    t = il.EdgeGradientPrimal.zeros(g, S["dt"])
+    il.grad_(t, v, vc)                                   # Edges{Primal} -> EdgeGradient{Primal}
+    assert rel(t.numpy_components(), tuple(x * s for x in O.grad_edges(vh, og))) < S["tol"]
+    th = t.numpy_components()
+    q2 = il.EdgesPrimal.zeros(g, S["dt"])
+    il.divergence_(q2, t, vc)                            # EdgeGradient{Primal} -> Edges{Primal}
+    assert rel(q2.numpy_components(), tuple(x * s for x in O.divergence_edgegrad(th, og))) < S["tol"]
 
 
 def test_convective_derivative_linear_fields_exact(S):
