@@ -429,12 +429,6 @@ int up(DevBuf& b, const std::vector<V>& v) {
   return ILM_OK;
 }
 
-int up_typed(DevBuf& b, const std::vector<double>& v, int dtype) {
-  if (dtype == ILM_F64) return up(b, v);
-  std::vector<float> f(v.begin(), v.end());
-  return up(b, f);
-}
-
 #define BDISPATCH(dtype, ...)  \
   do {                         \
     if ((dtype) == ILM_F64) {  \
