@@ -1064,8 +1064,8 @@ def _cpu_baseline(args, specs):
 def run_profile_stencils(args):
     """The grid-stencil leg's kernels on 4096^2 FP32 fields, one warm-up pass
     and `args.profile_stencils` timed-order passes: divergence, gradient,
-    v . grad p, v . grad w, u . grad u, w x v (a fixed launch sequence for
-    ncu)."""
+    v . grad p, v . grad w, u . grad u, w x v, curl both ways, Laplacian,
+    vector gradient and divergence (a fixed launch sequence for ncu)."""
     import torch
     import __graft_entry__ as ge
     ge.build()
@@ -1080,6 +1080,7 @@ def run_profile_stencils(args):
     w = il.NodesDual.zeros(g, torch.float32)
     w.data.normal_()
     o_p, o_e, o_d = p.similar(), v.similar(), w.similar()
+    t = il.EdgeGradientPrimal.zeros(g, torch.float32)
     sc = il.SurfaceScalarCache(None, g, dtype=torch.float32)
     for _ in range(1 + args.profile_stencils):
         il.divergence_(o_p, v, sc)
@@ -1088,6 +1089,11 @@ def run_profile_stencils(args):
         il.convective_derivative_(o_d, v, w, c)
         il.convective_derivative_(o_e, v, c)
         il.w_cross_v_(o_e, w, v, c)
+        il.curl_(o_e, w, sc)
+        il.curl_(o_d, v, sc)
+        il.laplacian_(o_p, p, sc)
+        il.grad_(t, v, c)
+        il.divergence_(o_e, t, c)
     torch.cuda.synchronize()
     print(f"stencil passes {1 + args.profile_stencils} on {n}^2", file=sys.stderr)
 
