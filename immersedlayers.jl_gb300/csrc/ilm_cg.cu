@@ -983,8 +983,8 @@ __global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(NT, MINB)
     const int rows = (n + CS - 1) / CS;
     const int r0 = min(n, rank * rows), r1 = min(n, r0 + rows);
     const int nr = r1 - r0;
-    const double* sz = pr.sz != nullptr ? pr.sz + r0 : nullptr;  // S 1, owned rows (deflation)
-    const double inv_e = sz ? __ldg(pr.inv_e) : 0.0;
+    const bool sz = pr.sz != nullptr;  // deflation: S 1 read from pr.sz (owned rows from r0)
+    // 1 / E (deflation) is read by thread 0 where it forms the scalars
     const bool pre = pr.blk != nullptr || pr.band != nullptr;
     for (int i = threadIdx.x; i < nr; i += blockDim.x) {
       xs[i] = pr.x0 ? pr.x0[r0 + i] : 0.0;
@@ -1012,12 +1012,12 @@ __global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(NT, MINB)
       double v[1] = {0.0};
       for (int i = threadIdx.x; i < nr; i += blockDim.x) v[0] += ws[i] * rs[i];
       csum_t0<1, CS>(cl, v, nr, red, pub, slot);
-      if (threadIdx.x == 0) bc[0] = v[0] * inv_e;
+      if (threadIdx.x == 0) bc[0] = v[0] * __ldg(pr.inv_e);
       __syncthreads();
       const double c = bc[0];
       for (int i = threadIdx.x; i < nr; i += blockDim.x) {
         xs[i] += c;
-        rs[i] -= c * __ldg(sz + i);
+        rs[i] -= c * __ldg(pr.sz + r0 + i);
       }
       __syncthreads();
     }
@@ -1029,14 +1029,14 @@ __global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(NT, MINB)
       for (int i = threadIdx.x; i < nr; i += blockDim.x) {
         v[0] += bs[i] * bs[i];
         v[1] += ws[i] * rs[i] * rs[i];
-        if (sz) v[2] += ws[i] * __ldg(sz + i) * rs[i];
+        if (sz) v[2] += ws[i] * __ldg(pr.sz + r0 + i) * rs[i];
       }
       publish_slice(rs, r0, nr, ah, al);
       csum_coarse<3, CS>(cl, pr, v, ws, rs, r0, nr, red, pub, slot, bc);
       if (threadIdx.x == 0) {
         bc[0] = sqrt(v[0]);
         bc[1] = v[1];
-        bc[2] = v[2] * inv_e;
+        bc[2] = sz ? v[2] * __ldg(pr.inv_e) : 0.0;
       }
       gather_parts(cl, ah, al, n, rows, rank);
       bnorm = bc[0];
@@ -1055,10 +1055,10 @@ __global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(NT, MINB)
       __syncthreads();
       double v[1] = {0.0};
       if (sz)
-        for (int i = threadIdx.x; i < nr; i += blockDim.x) v[0] += ws[i] * __ldg(sz + i) * zs[i];
+        for (int i = threadIdx.x; i < nr; i += blockDim.x) v[0] += ws[i] * __ldg(pr.sz + r0 + i) * zs[i];
       publish_slice(zs, r0, nr, bh, bl);
       csum_t0<1, CS>(cl, v, nr, red, pub, slot);
-      if (threadIdx.x == 0) bc[2] = v[0] * inv_e;
+      if (threadIdx.x == 0) bc[2] = sz ? v[0] * __ldg(pr.inv_e) : 0.0;
       gather_parts(cl, bh, bl, n, rows, rank);
       mu = bc[2];
       const float mh = (float)mu, ml = (float)(mu - (double)mh);
@@ -1123,14 +1123,14 @@ __global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(NT, MINB)
           rs[i] = ri;
           v[0] += ri * ri;
           v[1] += ws[i] * ri * ri;
-          if (sz) v[2] += ws[i] * __ldg(sz + i) * ri;
+          if (sz) v[2] += ws[i] * __ldg(pr.sz + r0 + i) * ri;
         }
         publish_slice(rs, r0, nr, ah, al);
         csum_coarse<3, CS>(cl, pr, v, ws, rs, r0, nr, red, pub, slot, bc);
         if (threadIdx.x == 0) {
           bc[5] = v[0];
           bc[6] = v[1];
-          bc[7] = v[2] * inv_e;
+          bc[7] = sz ? v[2] * __ldg(pr.inv_e) : 0.0;
         }
         __syncthreads();
         rr = bc[5];
@@ -1156,14 +1156,14 @@ __global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(NT, MINB)
           rs[i] = ri;
           v[0] += ri * ri;
           v[1] += ws[i] * ri * ri;
-          if (sz) v[2] += ws[i] * __ldg(sz + i) * ri;
+          if (sz) v[2] += ws[i] * __ldg(pr.sz + r0 + i) * ri;
         }
         publish_slice(rs, r0, nr, ah, al);
         csum_coarse<3, CS>(cl, pr, v, ws, rs, r0, nr, red, pub, slot, bc);
         if (threadIdx.x == 0) {
           bc[9] = v[0];
           bc[10] = v[1];
-          bc[11] = v[2] * inv_e;
+          bc[11] = sz ? v[2] * __ldg(pr.inv_e) : 0.0;
         }
         __syncthreads();
         const double tr = bc[9];
@@ -1214,13 +1214,13 @@ __global__ void __cluster_dims__(CS, 1, 1) __launch_bounds__(NT, MINB)
         double v[2] = {0.0, 0.0};
         for (int i = threadIdx.x; i < nr; i += blockDim.x) {
           v[0] += ws[i] * zs[i] * qs[i];
-          if (sz) v[1] += ws[i] * __ldg(sz + i) * zs[i];
+          if (sz) v[1] += ws[i] * __ldg(pr.sz + r0 + i) * zs[i];
         }
         publish_slice(zs, r0, nr, bh, bl);
         csum_t0<2, CS>(cl, v, nr, red, pub, slot);
         if (threadIdx.x == 0) {
           bc[13] = fdiv(-v[0], pq);
-          bc[14] = v[1] * inv_e;
+          bc[14] = sz ? v[1] * __ldg(pr.inv_e) : 0.0;
         }
         gather_parts(cl, bh, bl, n, rows, rank);
         beta = bc[13];
