@@ -395,10 +395,21 @@ struct ilm_batch_s {
   // continues past the call's return, and every launch that reads S waits
   // for this event (wait_schur)
   cudaEvent_t schur_ready = nullptr;
+  // The build runs as two launches when the batch holds both kinds, the
+  // Neumann problems' matrices first: schur_first is recorded between them,
+  // and set-up work that reads only those matrices (their block inverses and
+  // coarse E) waits for it instead of schur_ready (wait_schur_for).
+  // in_first[p]: problem p's S is built by the first launch.
+  cudaEvent_t schur_first = nullptr;
+  std::vector<char> in_first;
   ~ilm_batch_s() {
     if (schur_ready) {
       cudaEventSynchronize(schur_ready);
       cudaEventDestroy(schur_ready);
+    }
+    if (schur_first) {
+      cudaEventSynchronize(schur_first);
+      cudaEventDestroy(schur_first);
     }
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
@@ -564,6 +575,16 @@ int wait_schur(ilm_batch_s* b, cudaStream_t st) {
   return ILM_OK;
 }
 
+int wait_event(cudaEvent_t ev, cudaStream_t st);
+
+// Order work on stream st after the Schur build of the problems probs: the
+// first launch's event when all of them are built by it, else the whole build
+int wait_schur_for(ilm_batch_s* b, cudaStream_t st, const std::vector<int>& probs) {
+  bool first = b->schur_first != nullptr && b->schur_ready != nullptr && !probs.empty();
+  for (int p : probs) first = first && b->in_first[p];
+  return first ? wait_event(b->schur_first, st) : wait_schur(b, st);
+}
+
 // Order work on stream st after the work recorded by event ev (a host wait
 // when st is being captured: the capture takes no dependency on work outside
 // it); ev == nullptr: nothing to wait for
@@ -613,17 +634,19 @@ int ensure_setup_stream(ilm_batch_s* b) {
 int ensure_block_inverses(ilm_batch_s* b) {
   if (b->bj_block <= 0 || b->precond == 0) return ILM_OK;
   std::vector<BJBlockTask> todo;
+  std::vector<int> todo_probs;
   for (int p = 0; p < b->nprob; ++p) {
     const bool need = b->precond == 1 || (b->precond == 2 && (b->has_band.empty() || !b->has_band[p]));
     if (!need || b->bj_have[p]) continue;
     for (int t = b->bj_first[p]; t < b->bj_first[p + 1]; ++t) todo.push_back(b->bj_tasks_host[t]);
     b->bj_have[p] = 1;
+    todo_probs.push_back(p);
   }
   if (todo.empty()) return ILM_OK;
   const auto t0 = std::chrono::steady_clock::now();
   if (!b->s_bj) ILM_CHECK_CUDA(cudaStreamCreateWithFlags(&b->s_bj, cudaStreamNonBlocking));
   if (!b->bj_ready) ILM_CHECK_CUDA(cudaEventCreateWithFlags(&b->bj_ready, cudaEventDisableTiming));
-  ILM_TRY(wait_schur(b, b->s_bj));
+  ILM_TRY(wait_schur_for(b, b->s_bj, todo_probs));
   ILM_TRY(b->lz_bjtasks.alloc(todo.size() * sizeof(BJBlockTask)));
   // (from pageable memory: the copy has read todo when the call returns)
   ILM_CHECK_CUDA(cudaMemcpyAsync(b->lz_bjtasks.p, todo.data(), todo.size() * sizeof(BJBlockTask),
@@ -1101,6 +1124,27 @@ int batch_create_impl(int nprob, const ilm_batch_problem_t* probs, const double*
     B->schur_tiles = tiles;
     B->schur_host = sp;
   }
+  // build order of a batch with both kinds: the Neumann problems' matrices
+  // first (two launches, schur_first recorded between them); each group's
+  // descriptors number its tiles from zero
+  std::vector<SchurProbDev> sp_build;
+  int nfirst = 0, tiles_first = 0, tiles_second = 0;  // (tiles_first + tiles_second = schur_tiles)
+  B->in_first.assign(nprob, 0);
+  for (int p = 0; p < nprob; ++p) nfirst += probs[p].kind != 0;
+  if (nfirst > 0 && nfirst < nprob) {
+    sp_build.reserve(nprob);
+    for (int pass = 0; pass < 2; ++pass)
+      for (int p = 0; p < nprob; ++p) {
+        if ((probs[p].kind != 0) != (pass == 0)) continue;
+        SchurProbDev q = sp[p];
+        int& t = pass == 0 ? tiles_first : tiles_second;
+        const int nt = (q.n + 15) / 16;
+        q.tile0 = t;
+        t += nt * (nt + 1) / 2;
+        sp_build.push_back(q);
+        if (pass == 0) B->in_first[p] = 1;
+      }
+  }
   // set-up streams (non-blocking: independent of the legacy stream): the
   // geometry and task tables on sg, the Schur build on ss, overlapping the
   // host's task building
@@ -1114,7 +1158,7 @@ int batch_create_impl(int nprob, const ilm_batch_problem_t* probs, const double*
   ILM_CHECK_CUDA(cudaStreamCreateWithFlags(&SS.g, cudaStreamNonBlocking));
   ILM_CHECK_CUDA(cudaStreamCreateWithFlags(&SS.s, cudaStreamNonBlocking));
   cudaStream_t sg = SS.g, ss = SS.s;
-  DevBuf d_in[5], d_poff, d_grid, d_tpo[4], d_tso[4], d_cnt;
+  DevBuf d_in[5], d_poff, d_grid, d_tpo[4], d_tso[4], d_cnt, d_spb;
   {
     ArenaBuilder A;
     const double* src[5] = {x, y, nrmx, nrmy, ds};
@@ -1125,6 +1169,7 @@ int batch_create_impl(int nprob, const ilm_batch_problem_t* probs, const double*
     A.add(&d_grid, hgrid);
     A.add(&B->ph, hh);
     A.add(&B->schurP, sp);
+    if (!sp_build.empty()) A.add(&d_spb, sp_build);
     for (int c = 0; c < 4; ++c) {
       A.add(&d_tpo[c], tpo[c]);
       A.add(&d_tso[c], tso[c]);
@@ -1228,9 +1273,12 @@ int batch_create_impl(int nprob, const ilm_batch_problem_t* probs, const double*
       }
       BW.nx64 = B->nx64.as<double>();
       BW.ny64 = B->ny64.as<double>();
+      const bool split = !sp_build.empty();
+      if (split) ILM_CHECK_CUDA(cudaEventCreateWithFlags(&B->schur_first, cudaEventDisableTiming));
+      const SchurProbDev* spb = split ? d_spb.as<SchurProbDev>() : nullptr;
       ILM_TRY(schur_build_batched(nprob, B->schurP.as<SchurProbDev>(), B->schur_tiles, Ptot, B->pt2prob.as<int>(),
                                   BW, B->ds64.as<double>(), static_cast<Functional*>(B->F.p), B->Shi.as<float>(),
-                                  B->Slo.as<float>(), B->max_grid, ss));
+                                  B->Slo.as<float>(), B->max_grid, ss, spb, nfirst, tiles_first, B->schur_first));
       // the deflation data of the Dirichlet problems, after S on its stream
       k_defl_rows<<<(unsigned)(((size_t)Ptot * 32 + 255) / 256), 256, 0, ss>>>(
           Ptot, B->pt2prob.as<int>(), B->schurP.as<SchurProbDev>(), B->Shi.as<float>(), B->Slo.as<float>(),
@@ -2162,7 +2210,7 @@ int ilm_batch_set_coarse(ilm_batch_t b, int kind_mask, const int* body_start) {
                                  cudaMemcpyHostToDevice, ss));
   ILM_CHECK_CUDA(cudaMemcpyAsync(b->coarse_tprob.p, tprob.data(), (size_t)nt * sizeof(int), cudaMemcpyHostToDevice,
                                  ss));
-  ILM_TRY(wait_schur(b, ss));
+  ILM_TRY(wait_schur_for(b, ss, tprob));
   k_coarse_E<<<(unsigned)(nt * COARSE_SPLIT), 256, 0, ss>>>(b->coarse_tasks.as<CoarseTask>(),
                                                             b->coarse_part.as<double>());
   ILM_CHECK_LAUNCH();

@@ -683,9 +683,14 @@ struct BatchWin {
 };
 struct Functional;
 size_t functional_size();
+// probs_dev: the nprob descriptors in problem order.  order != nullptr: the
+// pair tiles in two launches, the descriptors order[0, nfirst) (tiles_first
+// tiles, numbered from zero) then the rest (numbered from zero again), event
+// mid recorded between them
 int schur_build_batched(int nprob, const SchurProbDev* probs_dev, int total_tiles, int Ptot, const int* pt2prob,
                         const BatchWin& W, const double* w, Functional* F, float* Shi, float* Slo, int max_grid,
-                        cudaStream_t st);
+                        cudaStream_t st, const SchurProbDev* order = nullptr, int nfirst = 0, int tiles_first = 0,
+                        cudaEvent_t mid = nullptr);
 // right-hand-side operator of the batched solves (E L^-1 D_s / G_s L^-1 R),
 // full n x n tiles numbered from probs_full_dev[p].tile0
 int rhsop_build_batched(int nprob, const SchurProbDev* probs_full_dev, int total_tiles, int Ptot, const int* pt2prob,

@@ -589,7 +589,8 @@ __global__ void __launch_bounds__(256) k_schur_pairs_batched(int nprob, const Sc
 
 int schur_build_batched(int nprob, const SchurProbDev* probs_dev, int total_tiles, int Ptot, const int* pt2prob,
                         const BatchWin& W, const double* w, Functional* F, float* Shi, float* Slo, int max_grid,
-                        cudaStream_t st) {
+                        cudaStream_t st, const SchurProbDev* order, int nfirst, int tiles_first,
+                        cudaEvent_t mid) {
   if (Ptot == 0) return ILM_OK;
   const float2* G = nullptr;
   int ld = 0;
@@ -598,8 +599,24 @@ int schur_build_batched(int nprob, const SchurProbDev* probs_dev, int total_tile
                                                             W.by[1], W.wx64[0], W.wx64[1], W.wy64[0], W.wy64[1],
                                                             W.nx64, W.ny64, w, F, -1);
   ILM_CHECK_LAUNCH();
-  k_schur_pairs_batched<<<total_tiles, dim3(16, 16), 0, st>>>(nprob, probs_dev, reinterpret_cast<const FunctionalFF*>(F),
-                                                              w, G, ld, ld - 1, Shi, Slo);
+  // the pair tiles: one launch over probs_dev, or two over the build order
+  // (the functionals above index probs_dev by problem, so it stays in
+  // problem order)
+  const FunctionalFF* FF_ = reinterpret_cast<const FunctionalFF*>(F);
+  if (!order) {
+    if (total_tiles > 0)
+      k_schur_pairs_batched<<<total_tiles, dim3(16, 16), 0, st>>>(nprob, probs_dev, FF_, w, G, ld, ld - 1, Shi, Slo);
+    ILM_CHECK_LAUNCH();
+    return ILM_OK;
+  }
+  if (tiles_first > 0)
+    k_schur_pairs_batched<<<tiles_first, dim3(16, 16), 0, st>>>(nfirst, order, FF_, w, G, ld, ld - 1, Shi, Slo);
+  ILM_CHECK_LAUNCH();
+  if (mid) ILM_CHECK_CUDA(cudaEventRecord(mid, st));
+  const int tiles_second = total_tiles - tiles_first;
+  if (tiles_second > 0)
+    k_schur_pairs_batched<<<tiles_second, dim3(16, 16), 0, st>>>(nprob - nfirst, order + nfirst, FF_, w, G, ld,
+                                                                 ld - 1, Shi, Slo);
   ILM_CHECK_LAUNCH();
   return ILM_OK;
 }

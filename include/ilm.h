@@ -385,7 +385,10 @@ typedef struct {
  * Returns while the Schur build still runs on the device (its own stream):
  * every later call that reads the Schur complements orders its device work
  * after that build, so the caller's host work (the preconditioner set-up)
- * overlaps it.                                                              */
+ * overlaps it.  With both kinds in the batch the Neumann problems' matrices
+ * are built first, and the set-up work that reads only those (their block
+ * inverses, the coarse correction) starts before the Dirichlet ones are
+ * done.                                                                     */
 ILM_API int ilm_batch_create(int nprob, const ilm_batch_problem_t* probs, const double* x, const double* y,
                              const double* nrmx, const double* nrmy, const double* ds, int ddf, int dtype,
                              ilm_batch_t* out);
