@@ -968,10 +968,14 @@ __global__ void k_scatter_rows(int Nsel, int P, const int* __restrict__ c2o, con
 // Many small device arrays carved out of one allocation; the ones with host
 // data are filled by one host->device copy through pinned staging memory
 // (kept by the library and grown on demand; one batch set-up at a time
-// uses it).
+// uses it).  g_stage_done marks the end of the last copy out of it: the next
+// set-up waits for it before writing the staging memory again, so a copy's
+// stream need not be synchronised (work after it on that stream is ordered
+// after it anyway).
 std::mutex g_stage_mu;
 void* g_stage = nullptr;
 size_t g_stage_bytes = 0;
+cudaEvent_t g_stage_done = nullptr;
 
 struct ArenaBuilder {
   struct Item {
@@ -1006,6 +1010,8 @@ struct ArenaBuilder {
   int commit_upload(DevBuf& arena, cudaStream_t st) {
     if (!copy_end) return ILM_OK;
     std::lock_guard<std::mutex> lk(g_stage_mu);
+    if (!g_stage_done) ILM_CHECK_CUDA(cudaEventCreateWithFlags(&g_stage_done, cudaEventDisableTiming));
+    ILM_CHECK_CUDA(cudaEventSynchronize(g_stage_done));  // the last copy out of the staging memory
     if (g_stage_bytes < copy_end) {
       if (g_stage) cudaFreeHost(g_stage);
       g_stage = nullptr;
@@ -1016,7 +1022,7 @@ struct ArenaBuilder {
     for (const Item& it : items)
       if (it.src && it.bytes) memcpy(static_cast<unsigned char*>(g_stage) + it.off, it.src, it.bytes);
     ILM_CHECK_CUDA(cudaMemcpyAsync(arena.p, g_stage, copy_end, cudaMemcpyHostToDevice, st));
-    ILM_CHECK_CUDA(cudaStreamSynchronize(st));
+    ILM_CHECK_CUDA(cudaEventRecord(g_stage_done, st));
     return ILM_OK;
   }
 };
@@ -1066,13 +1072,8 @@ int batch_create_impl(int nprob, const ilm_batch_problem_t* probs, const double*
   for (int k = 0; k < Ptot; ++k)
     ILM_REQUIRE(isfinite(x[k]) && isfinite(y[k]) && isfinite(nrmx[k]) && isfinite(nrmy[k]) && isfinite(ds[k]),
                 "batch: non-finite point data at %d", k);
-  B->hx.assign(x, x + Ptot);
-  B->hy.assign(y, y + Ptot);
-  B->hnx.assign(nrmx, nrmx + Ptot);
-  B->hny.assign(nrmy, nrmy + Ptot);
-  B->hds.assign(ds, ds + Ptot);
 
-  phase("validate and copy point data");
+  phase("validate point data");
   // ---- geometry and work buffers: one arena; DDF windows and tile lists on
   // the device -----------------------------------------------------------
   const size_t e = es(dtype);
@@ -1289,8 +1290,16 @@ int batch_create_impl(int nprob, const ilm_batch_problem_t* probs, const double*
       ILM_CHECK_LAUNCH();
     }
   }
+  // the host's copy of the point data (read by the FP64 refinement copy of
+  // the batch), taken while the windows kernels and the Schur build run: the
+  // device copy above read the caller's arrays
+  B->hx.assign(x, x + Ptot);
+  B->hy.assign(y, y + Ptot);
+  B->hnx.assign(nrmx, nrmx + Ptot);
+  B->hny.assign(nrmy, nrmy + Ptot);
+  B->hds.assign(ds, ds + Ptot);
   // the windows' base indices and the tile pointers, for the boxes and task
-  // tables built on the host
+  // tables built on the host (the copies to pageable memory return once done)
   std::vector<int> hbx[2], hby[2], htp[4];
   for (int d = 0; d < 2; ++d) {
     hbx[d].resize(Ptot);
@@ -1303,7 +1312,7 @@ int batch_create_impl(int nprob, const ilm_batch_problem_t* probs, const double*
     ILM_CHECK_CUDA(cudaMemcpyAsync(htp[c].data(), B->tptr[c].p, (size_t)tp_tot[c] * 4, cudaMemcpyDeviceToHost, sg));
   }
   ILM_CHECK_CUDA(cudaStreamSynchronize(sg));
-  phase("DDF windows and tile lists (device) + read-back");
+  phase("DDF windows and tile lists (device) + read-back; host copy of the points");
   std::vector<int> ord(nprob);
   {
     // CG work queue: largest problems first (cost ~ npts^2 * sqrt(npts))
