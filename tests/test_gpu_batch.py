@@ -40,6 +40,38 @@ def test_batch_matches_oracle(cuda, dtype):
         assert rel(fg, fr) < tol_f, (i, sp.kind, rel(fg, fr))
 
 
+def test_batch_split_schur_build_matches_single_kind_batches(cuda):
+    """A batch with both kinds builds its Schur complements in two launches
+    (the Neumann problems' first; their block inverses wait only for that
+    launch).  Each problem of such a batch solves, bit for bit and in the
+    same iterations, as it does in a batch of its kind alone (one launch)."""
+    import torch
+    from immersedlayers import workloads as W
+    from immersedlayers.batch import BatchSolver
+    specs = W.batch_specs(8, sizes=(64, 96))
+    assert {sp.kind for sp in specs} == {0, 1}
+
+    def run(sub):
+        bs = BatchSolver(sub, dtype=torch.float32)
+        bs.set_precond("bjacobi", 32)
+        fp, fm = bs.surface_data()
+        f, s = bs.solve(fp, fm, tol=1e-8, maxiter=20000)
+        torch.cuda.synchronize()
+        its, rr = bs.info()
+        assert (rr <= 1e-8).all(), rr
+        return [(bs.field(f, i).clone(), bs.surface(s, i).clone()) for i in range(len(sub))], its.copy()
+
+    mixed, its_m = run(specs)
+    for kind in (0, 1):
+        idx = [i for i, sp in enumerate(specs) if sp.kind == kind]
+        alone, its_a = run([specs[i] for i in idx])
+        for j, i in enumerate(idx):
+            df = (alone[j][0] - mixed[i][0]).abs().max().item()
+            ds = (alone[j][1] - mixed[i][1]).abs().max().item()
+            assert df == 0 and ds == 0, (kind, i, df, ds)
+            assert its_a[j] == its_m[i], (kind, i, its_a[j], its_m[i])
+
+
 def test_batch_block_jacobi_matches_plain(cuda):
     """Flexible CG with the block-Jacobi preconditioner reaches the same
     FP64 residual and the same solution as plain CG, in fewer iterations."""
